@@ -1,0 +1,188 @@
+"""ctypes access to the C restatement (libsbc_oracle.so) and to the reference
+binary built by build_ref.py.  TEST INFRASTRUCTURE ONLY: imported by tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg, never by the product.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "libsbc_oracle.so"
+REF_EXE = HERE / "_ref" / "seg"
+
+ARRAYS = [
+    "raw_b", "raw_c", "raw_t", "uniq_b", "uniq_c", "uniq_t",
+    "isect_xy", "isect_ab", "isect_ac",
+    "merged_bxy", "merged_cxy", "merged_balpha", "merged_calpha", "merged_bnb", "merged_cnb",
+    "label_b", "label_c", "ring_offsets", "ring_xy",
+]
+REAL_ARRAYS = {"isect_xy", "merged_bxy", "merged_cxy", "ring_xy"}
+STATS = ["edges", "elem_count", "tree_size", "cover_total", "leaf_end_total"]
+
+
+def build_oracle_lib() -> Path:
+    """Compile the C restatement (unfused FP64) into oracle/_build/."""
+    LIB_PATH.parent.mkdir(parents=True, exist_ok=True)
+    src = HERE / "sbc_oracle.c"
+    if not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < src.stat().st_mtime:
+        subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", str(src),
+                        "-o", str(LIB_PATH), "-lm"], check=True)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build_oracle_lib()
+        L = ctypes.CDLL(str(LIB_PATH))
+        L.sbco_clip.restype = ctypes.c_void_p
+        L.sbco_clip.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                ctypes.c_int]
+        L.sbco_status.argtypes = [ctypes.c_void_p]
+        L.sbco_message.restype = ctypes.c_char_p
+        L.sbco_message.argtypes = [ctypes.c_void_p]
+        L.sbco_len.restype = ctypes.c_long
+        L.sbco_len.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.sbco_data.restype = ctypes.c_void_p
+        L.sbco_data.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.sbco_stat.restype = ctypes.c_long
+        L.sbco_stat.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.sbco_free.argtypes = [ctypes.c_void_p]
+        L.sbco_segment_intersection.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_void_p] * 2
+        _lib = L
+    return _lib
+
+
+class OracleError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"oracle status {status}: {msg}")
+        self.status = status
+
+
+def clip(base: np.ndarray, overlays) -> dict:
+    """Run the restatement.  Returns {'stats': {...}, 'overlays': [ {name: array} ]}."""
+    L = lib()
+    b = np.ascontiguousarray(base, dtype=np.float64).reshape(-1, 2)
+    ovs = [np.ascontiguousarray(o, dtype=np.float64).reshape(-1, 2) for o in overlays]
+    cxy = np.ascontiguousarray(np.concatenate(ovs, axis=0))
+    sizes = np.array([o.shape[0] for o in ovs], dtype=np.int32)
+    run = L.sbco_clip(b.ctypes.data, b.shape[0], cxy.ctypes.data, sizes.ctypes.data, len(ovs))
+    try:
+        st = L.sbco_status(run)
+        if st != 0:
+            raise OracleError(st, L.sbco_message(run).decode())
+        out = {"stats": {n: L.sbco_stat(run, i) for i, n in enumerate(STATS)}, "overlays": []}
+        for ov in range(1, len(ovs) + 1):
+            d = {}
+            for w, name in enumerate(ARRAYS):
+                n = L.sbco_len(run, ov, w)
+                ptr = L.sbco_data(run, ov, w)
+                if name in REAL_ARRAYS:
+                    a = np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctypes.c_double)), (max(n, 1),))[:n]
+                else:
+                    a = np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctypes.c_int)), (max(n, 1),))[:n]
+                d[name] = a.copy()
+            out["overlays"].append(d)
+        return out
+    finally:
+        L.sbco_free(run)
+
+
+def rings_of(d: dict):
+    """List of (n,2) arrays from an overlay result dict."""
+    off = d["ring_offsets"]
+    xy = d["ring_xy"].reshape(-1, 2)
+    return [xy[off[i]:off[i + 1]] for i in range(len(off) - 1)]
+
+
+def segment_intersection(p1, p2, q1, q2):
+    L = lib()
+    arrs = [np.ascontiguousarray(v, dtype=np.float64) for v in (p1, p2, q1, q2)]
+    a = ctypes.c_double()
+    b = ctypes.c_double()
+    t = L.sbco_segment_intersection(*[x.ctypes.data for x in arrs], ctypes.byref(a), ctypes.byref(b))
+    return t, a.value, b.value
+
+
+# ---------------------------------------------------------------------------
+# the reference binary
+# ---------------------------------------------------------------------------
+
+def ref_available() -> bool:
+    return REF_EXE.exists()
+
+
+def parse_rings(text: str):
+    """Parse the reference's result text (`x y,` lines, `;` closes a ring)."""
+    rings, cur = [], []
+    for line in text.splitlines():
+        line = line.strip()
+        if not line:
+            continue
+        end = line.endswith(";")
+        body = line.rstrip(",;").strip()
+        if body:
+            x, y = body.split()
+            cur.append((float(x), float(y)))
+        if end:
+            rings.append(np.array(cur, dtype=np.float64).reshape(-1, 2))
+            cur = []
+    return rings
+
+
+def run_reference(base: np.ndarray, overlays, threads: int = 1, precision: int = 17,
+                  dump: bool = False, timeout: float = 600.0) -> dict:
+    """Run oracle/_ref/seg on the polygons (written `x,y` at %.17g).
+
+    Returns {'rings': [list per overlay], 'time_line': [...], 'dumps': {...}}.
+    """
+    import sys
+    sys.path.insert(0, str(HERE.parent / "segment-tree-based-clipping_gb300"))
+    import sbclip_gen as gen  # noqa: E402
+
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        (td / "work").mkdir()
+        (td / "results").mkdir()
+        gen.write_poly(td / "b.txt", base)
+        files = []
+        for i, o in enumerate(overlays):
+            f = td / f"c{i + 1}.txt"
+            gen.write_poly(f, o)
+            files.append(str(f))
+        env = dict(os.environ)
+        env["OMP_NUM_THREADS"] = str(threads)
+        env["SBC_REF_PRECISION"] = str(precision)
+        if dump:
+            env["SBC_REF_DUMP"] = str(td / "dump")
+        p = subprocess.run([str(REF_EXE), str(td / "b.txt"), *files], cwd=td / "work", env=env,
+                           capture_output=True, text=True, timeout=timeout)
+        if p.returncode != 0:
+            raise RuntimeError(f"reference exited {p.returncode}: {p.stderr[-400:]}")
+        lines = p.stdout.strip().splitlines()
+        time_line = [int(x) for x in lines[-1].split() if x.lstrip('-').isdigit()] if lines else []
+        rings = []
+        for i in range(len(overlays)):
+            rp = td / "results" / f"Fig-def-R{i + 1}.txt"
+            rings.append(parse_rings(rp.read_text()) if rp.exists() else [])
+        dumps = {}
+        if dump:
+            for i in range(len(overlays)):
+                d = {}
+                for name in ARRAYS[:-2]:
+                    f = td / f"dump.{i + 1}.{name}.txt"
+                    if f.exists():
+                        dt = np.float64 if name in REAL_ARRAYS else np.int64
+                        txt = f.read_text().split()
+                        d[name] = np.array(txt, dtype=dt) if txt else np.zeros(0, dt)
+                dumps[i + 1] = d
+        return {"rings": rings, "time_line": time_line, "dumps": dumps, "stdout": p.stdout}

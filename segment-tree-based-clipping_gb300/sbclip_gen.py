@@ -1,0 +1,128 @@
+"""Seeded synthetic star-shaped polygons for the segment-tree clipping workloads.
+
+The reference's own datasets (real-world ocean / continent / lake / park rings)
+are not available, so every workload is a seeded synthetic stand-in with the
+shapes and sizes of the benchmark configurations:
+
+* ``star``            vertex i at angle theta_i (n sorted, distinct U[0, 2pi)
+                      draws), radius R*(0.5 + 0.5*u_i), counter-clockwise.
+* ``jagged_star``     the same angles with radius R*(1 + 0.3*g_i), g the sum of
+                      8 octaves of periodic 1-D value noise over theta (amplitude
+                      halving per octave), clamped to >= 0.2R.
+* ``pair_small``      10k x 8k plain stars (base at (0,0), overlay at (0.3,0.2)).
+* ``pair_large``      1M x 1M jagged stars; overlay offset (0.25R, 0.1R) and
+                      rotated 0.3 rad about its centre.
+
+Files use the reference's text format (``src/clip.cpp:181-298``): the vertex
+count on the first line, then one ``x,y`` line per vertex, no closing duplicate.
+Seeds follow ``1000*config + polygon_index`` with NumPy's PCG64.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+TWO_PI = 2.0 * np.pi
+
+# Base lattice frequency (cells around the circle) of the lowest noise octave of
+# the large jagged pair; chosen so that the 1M x 1M pair has 1e5..1e6 unique
+# edge intersections.
+JAGGED_BASE_FREQ = 3000
+
+
+def _angles(rng: np.random.Generator, n: int) -> np.ndarray:
+    """n sorted, pairwise distinct U[0, 2pi) draws."""
+    th = np.sort(rng.uniform(0.0, TWO_PI, n))
+    while True:
+        dup = np.flatnonzero(np.diff(th) <= 0.0)
+        if dup.size == 0:
+            return th
+        th[dup + 1] = rng.uniform(0.0, TWO_PI, dup.size)
+        th.sort()
+
+
+def star(n: int, seed: int, centre=(0.0, 0.0), R: float = 1.0) -> np.ndarray:
+    """Plain star: radius R*(0.5+0.5u). Returns (n, 2) float64, CCW."""
+    rng = np.random.default_rng(seed)
+    th = _angles(rng, n)
+    r = R * (0.5 + 0.5 * rng.uniform(0.0, 1.0, n))
+    xy = np.empty((n, 2), dtype=np.float64)
+    xy[:, 0] = centre[0] + r * np.cos(th)
+    xy[:, 1] = centre[1] + r * np.sin(th)
+    return xy
+
+
+def value_noise(theta: np.ndarray, rng: np.random.Generator, base_freq: int,
+                octaves: int = 8) -> np.ndarray:
+    """Sum of `octaves` periodic 1-D value-noise octaves over theta in [0, 2pi).
+
+    Octave o has base_freq*2^o lattice cells, lattice values U[-1, 1], smoothstep
+    interpolation, amplitude 0.5^o.
+    """
+    g = np.zeros_like(theta)
+    amp = 1.0
+    for o in range(octaves):
+        cells = base_freq << o
+        lattice = rng.uniform(-1.0, 1.0, cells)
+        t = theta / TWO_PI * cells
+        k = np.floor(t).astype(np.int64) % cells
+        f = t - np.floor(t)
+        s = f * f * (3.0 - 2.0 * f)
+        g += amp * (lattice[k] * (1.0 - s) + lattice[(k + 1) % cells] * s)
+        amp *= 0.5
+    return g
+
+
+def jagged_star(n: int, seed: int, centre=(0.0, 0.0), R: float = 1.0,
+                rotation: float = 0.0, base_freq: int = JAGGED_BASE_FREQ) -> np.ndarray:
+    """Jagged star: radius R*(1+0.3g), clamped >= 0.2R, rotated then translated."""
+    rng = np.random.default_rng(seed)
+    th = _angles(rng, n)
+    g = value_noise(th, rng, base_freq)
+    r = np.maximum(R * (1.0 + 0.3 * g), 0.2 * R)
+    a = th + rotation
+    xy = np.empty((n, 2), dtype=np.float64)
+    xy[:, 0] = centre[0] + r * np.cos(a)
+    xy[:, 1] = centre[1] + r * np.sin(a)
+    return xy
+
+
+def pair_small(seed_base: int = 1000):
+    """10,000-vertex base at (0,0) and 8,000-vertex overlay at (0.3,0.2)."""
+    return star(10_000, seed_base + 0), star(8_000, seed_base + 1, centre=(0.3, 0.2))
+
+
+def pair_large(n: int = 1_000_000, seed_base: int = 2000, base_freq: int = JAGGED_BASE_FREQ):
+    """Two n-vertex jagged stars; overlay offset (0.25, 0.1) and rotated 0.3 rad."""
+    b = jagged_star(n, seed_base + 0, base_freq=base_freq)
+    c = jagged_star(n, seed_base + 1, centre=(0.25, 0.1), rotation=0.3, base_freq=base_freq)
+    return b, c
+
+
+def small_pairs(npairs: int, seed: int = 4000, lo: int = 4, hi: int = 64):
+    """Independent small pairs: sizes U[lo, hi], r=0.5+0.5u, overlay centre U[-0.5,0.5]^2."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for p in range(npairs):
+        nb, nc = rng.integers(lo, hi + 1, 2)
+        off = rng.uniform(-0.5, 0.5, 2)
+        s = int(rng.integers(0, 2**62))
+        out.append((star(int(nb), s), star(int(nc), s + 1, centre=(off[0], off[1]))))
+    return out
+
+
+def write_poly(path, xy: np.ndarray, sep: str = ",") -> None:
+    """Reference text format: count line, then `x<sep>y` per vertex at %.17g."""
+    xy = np.asarray(xy, dtype=np.float64)
+    with open(path, "w") as f:
+        f.write(f"{xy.shape[0]}\n")
+        f.write("\n".join(f"{x:.17g}{sep}{y:.17g}" for x, y in xy))
+        f.write("\n")
+
+
+def read_poly(path) -> np.ndarray:
+    """Parse the reference text format (`x,y` or `x y` per line)."""
+    with open(path) as f:
+        n = int(f.readline())
+        data = f.read().replace(",", " ").split()
+    arr = np.array(data[: 2 * n], dtype=np.float64).reshape(n, 2)
+    return arr
