@@ -1,0 +1,311 @@
+#!/usr/bin/env python3
+"""Benchmark: milliseconds per 1M x 1M polygon clip on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload pair_1m_1m|pair_10k_8k]
+
+A step is one full clip of the workload pair (segment tree build, candidate
+stab queries, FP64 intersection, merge, labelling and ring tracing) by the
+CUDA library.  `value` times K steps on device-resident inputs with CUDA
+events on the library's stream; L2 is flushed (a 256 MiB write) between
+steps, outside the timed window.  `e2e` times the public host API
+(sbc_clip_pair): host->device copy of the inputs from pinned staging and the
+device->host copy of the result rings inside every step.
+
+The single pair does not shard across GPUs (the tree and the tracing are
+global), so N > 1 runs N independent replicas, one per rank (torchrun), and
+reports the max over ranks.
+
+`--impl reference` times the reference's own CPU (OpenMP) build
+(oracle/_ref/seg, all host threads) on the same workload; when that build is
+absent, the C restatement of the same algorithm (one thread).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "segment-tree-based-clipping_gb300"
+for _p in (PKG, ROOT / "oracle"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+import sbclip_gen as gen  # noqa: E402
+
+METRIC = "ms per 1M×1M clip"
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+
+
+def workload(name: str):
+    if name == "pair_1m_1m":
+        b, c = gen.pair_large()
+        desc = {"workload": "pair_1m_1m", "base_vertices": len(b), "overlay_vertices": len(c),
+                "generator": "jagged stars, 8 octaves value noise, base_freq=%d" % gen.JAGGED_BASE_FREQ}
+    elif name == "pair_10k_8k":
+        b, c = gen.pair_small()
+        desc = {"workload": "pair_10k_8k", "base_vertices": len(b), "overlay_vertices": len(c),
+                "generator": "plain stars r=0.5+0.5u"}
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return b, c, desc
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d, "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = [l.split(",") for l in open(self.path).read().strip().splitlines() if l.strip()]
+        os.unlink(self.path)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for i, n in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# algorithmic bytes per launch of the kernels that can dominate a step,
+# from the run's statistics (see the roofline table in the design doc)
+def algorithmic_bytes(kernel: str, st: dict, launches: int):
+    E = st["edges"]
+    P = 2 * E
+    if kernel == "k_rad_scatter_u64":
+        return 24.0 * P  # read (key 8 + value 4) and write them once per pass
+    if kernel == "k_rad_hist_u64":
+        return 8.0 * P
+    if kernel == "k_cand_test":
+        return 64.0 * st["candidates_tested"] / max(launches, 1)
+    if kernel == "k_cover":
+        return (16.0 * E + 8.0 * st["cover_entries"]) / max(launches, 1)
+    if kernel == "k_find_leaves":
+        return 16.0 * E + 8.0 * E
+    if kernel in ("k_rad_scatter_u32",):
+        return 16.0 * st["cover_entries"]
+    return None
+
+
+def run_gb300(args, rank: int, world: int):
+    import torch
+    import sbclip
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    b, c, desc = workload(args.workload)
+    nb, nc = len(b), len(c)
+    d_b = torch.from_numpy(np.ascontiguousarray(b)).to(f"cuda:{dev}")
+    d_c = torch.from_numpy(np.ascontiguousarray(c)).to(f"cuda:{dev}")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
+    clip = sbclip.Clipper(dev)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    for _ in range(args.warmup):
+        clip.clip_pair_device(d_b.data_ptr(), nb, d_c.data_ptr(), nc, sp)
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    st_launch = sbclip.kernel_launches()
+    times = []
+    sbclip.profile_begin()
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            clip.clip_pair_device(d_b.data_ptr(), nb, d_c.data_ptr(), nc, sp)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+    prof = sbclip.profile_end()
+    launches = sbclip.kernel_launches() - st_launch
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    ms = float(np.mean(times))
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    stats = clip.stats()
+
+    # ---- end to end through the host API
+    e2e_times = []
+    rings = None
+    for i in range(max(args.steps, 1)):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rings = clip.clip_pair(b, c)
+        torch.cuda.synchronize()
+        e2e_times.append((time.perf_counter() - t0) * 1e3)
+    nverts = sum(len(r) for r in rings)
+    e2e = {"value": float(np.mean(e2e_times)), "unit": "ms",
+           "h2d_bytes_per_step": int(16 * (nb + nc)),
+           "d2h_bytes_per_step": int(4 * (len(rings) + 1) + 16 * nverts)}
+
+    # ---- roofline of the dominant kernel
+    pk, kind = peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][0]) if prof else None
+    roof = None
+    if dom:
+        name, (tot_ms, n_l) = dom
+        per_launch_ms = tot_ms / max(n_l, 1)
+        ab = algorithmic_bytes(name, stats, n_l // max(args.steps, 1))
+        achieved = (ab / (per_launch_ms * 1e-3) / 1e9) if ab else None
+        roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
+                "unit": "GB/s", "frac": (achieved / pk["hbm_gbs"]) if achieved else None,
+                "traffic": None, "peak_source": kind,
+                "share_of_step": tot_ms / max(sum(v[0] for v in prof.values()), 1e-9),
+                "ms_per_launch": per_launch_ms}
+    top = sorted(prof.items(), key=lambda kv: -kv[1][0])[:8]
+
+    out = {
+        "metric": METRIC if args.workload == "pair_1m_1m" else "ms per 10k×8k clip",
+        "value": ms, "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded star polygons)",
+        "config": dict(desc, parallelism="replicas" if world > 1 else "single",
+                       l2="flushed between steps (256 MiB write)"),
+        "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
+        "kernels_top": {k: {"ms_per_step": v[0] / max(args.steps, 1),
+                            "launches_per_step": v[1] // max(args.steps, 1)} for k, v in top},
+        "stats": stats, "clocks": clk.summary(),
+        "counts": {"rings": len(rings), "vertices": nverts, "unique_intersections": stats["unique"],
+                   "candidates_tested_per_s": stats["candidates_tested"] / (ms * 1e-3)},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(b, c, args)
+    clip.close()
+    return out
+
+
+def cpu_baseline(b, c, args, steps: int = 1):
+    """The reference's CPU build (all host threads) on the full workload."""
+    import oracle_py as O
+    threads = os.cpu_count() or 1
+    if O.ref_available():
+        vals = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            res = O.run_reference(b, [c], threads=threads, precision=6, timeout=1800)
+            wall = (time.perf_counter() - t0) * 1e3
+            tl = res["time_line"]
+            vals.append(tl[-1] / 1e3 if tl else wall)
+        return {"value": float(np.mean(vals)), "unit": "ms", "cores": threads, "kind": "reference",
+                "sample": f"{steps} full {args.workload} clip(s), reference TIME-line total "
+                          f"(OMP_NUM_THREADS={threads})"}
+    vals = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        O.clip(b, [c])
+        vals.append((time.perf_counter() - t0) * 1e3)
+    return {"value": float(np.mean(vals)), "unit": "ms", "cores": 1, "kind": "port",
+            "sample": f"{steps} full {args.workload} clip(s) by the C restatement (1 thread)"}
+
+
+def run_reference_arm(args):
+    b, c, desc = workload(args.workload)
+    # each step is one full clip; the CPU arm is capped at 3 steps so the run
+    # stays within a few minutes
+    steps = max(1, min(args.steps, 3))
+    base = cpu_baseline(b, c, args, steps=steps)
+    out = {
+        "impl": "reference",
+        "metric": METRIC if args.workload == "pair_1m_1m" else "ms per 10k×8k clip",
+        "value": base["value"], "unit": "ms", "n_gpus": args.gpus, "steps": steps,
+        "warmup": 0, "ms_per_step": base["value"], "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded star polygons)",
+        "config": dict(desc, parallelism="host cores"),
+        "cpu_baseline": base,
+        "e2e": {"value": base["value"], "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="pair_1m_1m", choices=["pair_1m_1m", "pair_10k_8k"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference_arm(args)), flush=True)
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    out = run_gb300(args, rank, world)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,140 @@
+/*
+ * sbclip.h -- C ABI of the GB300 segment-tree polygon clipping library
+ * (libsbclip.so).  Plain pointers and sizes; no C++ or torch types.
+ *
+ * The reference exposes this path only as the `seg` command line
+ * (src/clip.cpp:2117-2130 `main` -> `multicore_clipping`, src/clip.cpp:1415);
+ * these entry points replace multicore_clipping one to one, and the drop-in
+ * `seg` binary of this package is a thin reader/writer around them.
+ *
+ * Conventions
+ *  - Every function returns an int status: SBC_OK (0) or one of SBC_E*.
+ *    The library never exits the process; sbc_last_error() explains a failure.
+ *  - Polygons are interleaved x,y doubles, one ring each, no repeated closing
+ *    vertex (the reference's input file format, src/clip.cpp:181-298).
+ *  - Results are rings in the reference's output order: `offsets` has
+ *    nrings+1 entries (vertex offsets), `xy` 2*nverts doubles.  Result memory
+ *    belongs to the context and stays valid until its next clipping call.
+ *  - `stream` is a cudaStream_t (NULL: the context's own stream).
+ *  - One context per host thread; contexts hold all state, no globals.
+ */
+#ifndef SBCLIP_H
+#define SBCLIP_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SBC_OK 0
+#define SBC_EINPUT 1     /* malformed input: < 3 vertices, non-finite coordinate, ... */
+#define SBC_EUNDEF 2     /* input on which the reference's behaviour is undefined */
+#define SBC_ENOMEM 3     /* device or host allocation failed */
+#define SBC_ECUDA 4      /* CUDA runtime error */
+#define SBC_EINTERNAL 5
+
+typedef struct sbc_ctx sbc_ctx;
+
+typedef struct sbc_options {
+  int device;       /* CUDA device ordinal */
+  int flags;        /* SBC_FLAG_* */
+} sbc_options;
+
+#define SBC_FLAG_TIMING 1          /* record per-phase CUDA-event times (sbc_stats) */
+#define SBC_FLAG_SERIAL_BACKEND 2  /* run the back end's exact single-thread emulation */
+
+typedef struct sbc_rings {
+  int nrings;
+  long long nverts;
+  const int* offsets;   /* nrings+1 */
+  const double* xy;     /* 2*nverts */
+} sbc_rings;
+
+/* Create / destroy a context (replaces the reference's process-wide state:
+ * SegTree and the Foster globals bPolysList / cPolysList / rPolyList,
+ * foster/polyclip.h:35-37). */
+int sbc_create(const sbc_options* opt, sbc_ctx** out);
+void sbc_destroy(sbc_ctx* ctx);
+const char* sbc_last_error(const sbc_ctx* ctx);
+
+/* Intersection of a base polygon with k overlays in one segment tree, exactly
+ * as multicore_clipping (src/clip.cpp:1415-2115) computes it for
+ * `seg base overlay_1 ... overlay_k`: out[i] receives overlay i+1's rings
+ * (the reference's ../results/Fig-def-R<i+1>.txt).  Host buffers in and out;
+ * host<->device copies happen inside the call. */
+int sbc_clip_one_to_many(sbc_ctx* ctx, const double* b_xy, int nb, const double* c_xy,
+                         const int* c_sizes, int k, sbc_rings* out, void* stream);
+
+/* The single-pair case of sbc_clip_one_to_many (k = 1). */
+int sbc_clip_pair(sbc_ctx* ctx, const double* b_xy, int nb, const double* c_xy, int nc,
+                  sbc_rings* out, void* stream);
+
+/* Device-resident variant: inputs are device pointers; `out` receives device
+ * pointers (offsets and xy in device memory owned by the context). */
+int sbc_clip_pair_device(sbc_ctx* ctx, const double* d_b_xy, int nb, const double* d_c_xy,
+                         int nc, sbc_rings* out, void* stream);
+
+/* Diagnostics of the last call, written into out[0..n): see SBC_STAT_*. */
+#define SBC_STAT_EDGES 0
+#define SBC_STAT_ELEMENTARY_POINTS 1
+#define SBC_STAT_TREE_SIZE 2
+#define SBC_STAT_COVER_ENTRIES 3
+#define SBC_STAT_LEAF_END_ENTRIES 4
+#define SBC_STAT_CANDIDATES_TESTED 5    /* overlay 1: pairs reaching the FP64 test */
+#define SBC_STAT_RAW_HITS 6             /* overlay 1 */
+#define SBC_STAT_UNIQUE 7               /* overlay 1: unique intersecting edge pairs */
+#define SBC_STAT_SLOTS_B 8
+#define SBC_STAT_SLOTS_C 9
+#define SBC_STAT_SERIAL_BACKEND 10      /* 1 if the exact serial back end ran */
+#define SBC_STAT_NUM 11
+int sbc_stats(const sbc_ctx* ctx, long long* out, int n);
+
+/* Per-phase device milliseconds of the last call when SBC_FLAG_TIMING is set:
+ * [setup, elementary, end lists, cover lists, candidates+merge, back end,
+ *  device->host, total]. */
+int sbc_phase_times(const sbc_ctx* ctx, float* out_ms, int n);
+
+/* Intermediate arrays of the last overlay of the last call (for parity
+ * checks), copied to host memory: see SBC_ARR_*.  Returns the element count
+ * in *count (the copy is truncated to cap elements). */
+#define SBC_ARR_UNIQ_B 0       /* int */
+#define SBC_ARR_UNIQ_C 1       /* int */
+#define SBC_ARR_UNIQ_T 2       /* int */
+#define SBC_ARR_ISECT_XY 3     /* double */
+#define SBC_ARR_ISECT_AB 4     /* int */
+#define SBC_ARR_ISECT_AC 5     /* int */
+#define SBC_ARR_MERGED_BXY 6   /* double */
+#define SBC_ARR_MERGED_CXY 7   /* double */
+#define SBC_ARR_MERGED_BALPHA 8
+#define SBC_ARR_MERGED_CALPHA 9
+#define SBC_ARR_MERGED_BNB 10
+#define SBC_ARR_MERGED_CNB 11
+#define SBC_ARR_LABEL_B 12
+#define SBC_ARR_LABEL_C 13
+int sbc_debug_array(sbc_ctx* ctx, int which, void* host_dst, long long cap, long long* count);
+
+/* Edge-pair classification of n pairs (p1,p2,q1,q2 as 8 doubles per pair,
+ * host memory) on the device: the reference's lineSegmentIntersection
+ * (p_seg_tree/oacc_segment_tree.cpp:5426-5517) with alphaToInt
+ * (:7247-7252).  types/alpha/beta/alpha_int/beta_int receive n values each
+ * (any output pointer may be NULL). */
+int sbc_classify_pairs(sbc_ctx* ctx, const double* pairs, int n, int* types, double* alpha,
+                       double* beta, int* alpha_int, int* beta_int);
+
+/* Number of this library's kernel launches in the process so far. */
+unsigned long long sbc_kernel_launches(void);
+
+/* Per-kernel device times (diagnostics; no counterpart in the reference).
+ * Between sbc_profile_begin and sbc_profile_end every launch of this library
+ * is bracketed by CUDA events on its stream.  sbc_profile_end writes up to
+ * `cap` kernels: NUL-separated names into `names` (names_len bytes), total
+ * milliseconds into ms[i], launch counts into counts[i]; *n_out = kernels. */
+int sbc_profile_begin(void);
+int sbc_profile_end(char* names, int names_len, float* ms, int* counts, int cap, int* n_out);
+
+/* Library version string. */
+const char* sbc_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,394 @@
+// sbc_api.cu -- the C ABI (include/sbclip.h): contexts, host<->device
+// staging, the one-to-many driver and diagnostics.
+//
+// Pipeline::run follows multicore_clipping (src/clip.cpp:1415-2115): one
+// segment tree over the base and every overlay, then the per-overlay loop
+// (src/clip.cpp:1702-2062).
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/sbclip.h"
+#include "sbc_pipeline.cuh"
+
+namespace sbc {
+
+int Pipeline::run(const double* d_bxy, int nb_, const double* d_cxy, const int* c_sizes, int k_) {
+  err_.clear();
+  outs_.assign(k_, OverlayOut());
+  nb = nb_;
+  k = k_;
+  if (nb < 3) return fail(kEInput, "base polygon needs at least 3 vertices");
+  if (k < 1 || k > 9) return fail(kEInput, "1 to 9 overlays are supported");
+  for (int i = 0; i < k; ++i)
+    if (c_sizes[i] < 3) return fail(kEInput, "overlay polygon needs at least 3 vertices");
+  cudaEvent_t ev[8];
+  if (timing)
+    for (int i = 0; i < 8; ++i) cudaEventCreate(&ev[i]);
+  auto mark = [&](int i) {
+    if (timing) cudaEventRecord(ev[i], st_);
+  };
+  mark(0);
+  int rc = stage_setup(d_bxy, d_cxy, c_sizes);
+  mark(1);
+  if (!rc) rc = stage_elementary();
+  mark(2);
+  if (!rc) rc = stage_endlists();
+  mark(3);
+  if (!rc) rc = stage_cover();
+  mark(4);
+  for (int t = 1; t <= k && !rc; ++t) rc = stage_overlay(t, outs_[t - 1]);
+  mark(5);
+  if (cudaGetLastError() != cudaSuccess && !rc) rc = fail(kECuda, "CUDA error in the pipeline");
+  if (timing) {
+    cudaEventSynchronize(ev[5]);
+    for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&times.ms[i], ev[i], ev[i + 1]);
+    cudaEventElapsedTime(&times.ms[7], ev[0], ev[5]);
+    for (int i = 0; i < 8; ++i) cudaEventDestroy(ev[i]);
+  }
+  return rc;
+}
+
+}  // namespace sbc
+
+using sbc::Pipeline;
+
+struct sbc_ctx {
+  int device = 0;
+  int flags = 0;
+  cudaStream_t own = nullptr;
+  Pipeline* pl = nullptr;
+  std::string err;
+  // host staging (pinned)
+  double* h_in = nullptr;
+  size_t h_in_cap = 0;
+  std::vector<int*> h_off;
+  std::vector<double*> h_xy;
+  std::vector<size_t> h_off_cap, h_xy_cap;
+  double* d_in = nullptr;
+  size_t d_in_cap = 0;
+  long long stats[SBC_STAT_NUM] = {0};
+  float phase_ms[8] = {0};
+};
+
+namespace {
+
+int set_err(sbc_ctx* c, int code, const std::string& m) {
+  if (c) c->err = m;
+  return code;
+}
+
+int cuda_check(sbc_ctx* c, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return SBC_OK;
+  return set_err(c, SBC_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+bool ensure_pinned(T*& p, size_t& cap, size_t n) {
+  if (cap >= n && p) return true;
+  if (p) cudaFreeHost(p);
+  p = nullptr;
+  cap = 0;
+  size_t want = n + n / 8 + 16;
+  if (cudaMallocHost((void**)&p, want * sizeof(T)) != cudaSuccess) {
+    cudaGetLastError();
+    p = nullptr;
+    return false;
+  }
+  cap = want;
+  return true;
+}
+
+void fill_stats(sbc_ctx* c) {
+  Pipeline& pl = *c->pl;
+  for (auto& s : c->stats) s = 0;
+  c->stats[SBC_STAT_EDGES] = pl.stat_edges;
+  c->stats[SBC_STAT_ELEMENTARY_POINTS] = pl.stat_epc;
+  c->stats[SBC_STAT_TREE_SIZE] = pl.stat_ts;
+  c->stats[SBC_STAT_COVER_ENTRIES] = pl.stat_cover;
+  c->stats[SBC_STAT_LEAF_END_ENTRIES] = pl.stat_leaf;
+  if (!pl.outputs().empty()) {
+    const auto& o = pl.outputs()[0];
+    c->stats[SBC_STAT_CANDIDATES_TESTED] = o.tests;
+    c->stats[SBC_STAT_RAW_HITS] = o.raw_hits;
+    c->stats[SBC_STAT_UNIQUE] = o.unique;
+    c->stats[SBC_STAT_SLOTS_B] = o.slots_b;
+    c->stats[SBC_STAT_SLOTS_C] = o.slots_c;
+    int slow = 0;
+    for (const auto& x : pl.outputs()) slow |= x.slow_path;
+    c->stats[SBC_STAT_SERIAL_BACKEND] = slow;
+  }
+}
+
+int run_device(sbc_ctx* c, const double* d_b, int nb, const double* d_c, const int* sizes, int k,
+               cudaStream_t st) {
+  Pipeline& pl = *c->pl;
+  pl.set_stream(st);
+  pl.timing = (c->flags & SBC_FLAG_TIMING) != 0;
+  pl.force_serial_backend = (c->flags & SBC_FLAG_SERIAL_BACKEND) ? 1 : 0;
+  int rc = pl.run(d_b, nb, d_c, sizes, k);
+  if (rc) return set_err(c, rc, pl.error());
+  fill_stats(c);
+  for (int i = 0; i < 8; ++i) c->phase_ms[i] = pl.times.ms[i];
+  return SBC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sbc_create(const sbc_options* opt, sbc_ctx** out) {
+  if (!out) return SBC_EINPUT;
+  *out = nullptr;
+  sbc_ctx* c = new (std::nothrow) sbc_ctx();
+  if (!c) return SBC_ENOMEM;
+  c->device = opt ? opt->device : 0;
+  c->flags = opt ? opt->flags : 0;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    int rc = cuda_check(c, e, "sbc_create");
+    delete c;
+    return rc;
+  }
+  c->pl = new Pipeline(c->device, c->own);
+  *out = c;
+  return SBC_OK;
+}
+
+void sbc_destroy(sbc_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->own) cudaStreamSynchronize(c->own);
+  delete c->pl;
+  if (c->h_in) cudaFreeHost(c->h_in);
+  for (auto p : c->h_off)
+    if (p) cudaFreeHost(p);
+  for (auto p : c->h_xy)
+    if (p) cudaFreeHost(p);
+  if (c->d_in) cudaFree(c->d_in);
+  if (c->own) cudaStreamDestroy(c->own);
+  delete c;
+}
+
+const char* sbc_last_error(const sbc_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int sbc_clip_one_to_many(sbc_ctx* c, const double* b_xy, int nb, const double* c_xy,
+                         const int* c_sizes, int k, sbc_rings* out, void* stream) {
+  if (!c || !b_xy || !c_xy || !c_sizes || !out) return set_err(c, SBC_EINPUT, "null argument");
+  if (k < 1 || k > 9) return set_err(c, SBC_EINPUT, "1 to 9 overlays are supported");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  long long ncv = 0;
+  for (int i = 0; i < k; ++i) {
+    if (c_sizes[i] < 3) return set_err(c, SBC_EINPUT, "overlay needs at least 3 vertices");
+    ncv += c_sizes[i];
+  }
+  if (nb < 3) return set_err(c, SBC_EINPUT, "base needs at least 3 vertices");
+  size_t nin = 2 * ((size_t)nb + (size_t)ncv);
+  if (!ensure_pinned(c->h_in, c->h_in_cap, nin)) return set_err(c, SBC_ENOMEM, "pinned staging");
+  if (c->d_in_cap < nin) {
+    if (c->d_in) cudaFree(c->d_in);
+    c->d_in = nullptr;
+    c->d_in_cap = 0;
+    if (cudaMalloc(&c->d_in, nin * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      return set_err(c, SBC_ENOMEM, "device input staging");
+    }
+    c->d_in_cap = nin;
+  }
+  memcpy(c->h_in, b_xy, sizeof(double) * 2 * nb);
+  memcpy(c->h_in + 2 * nb, c_xy, sizeof(double) * 2 * ncv);
+  int rc = cuda_check(c, cudaMemcpyAsync(c->d_in, c->h_in, nin * sizeof(double),
+                                         cudaMemcpyHostToDevice, st),
+                      "input copy");
+  if (rc) return rc;
+  rc = run_device(c, c->d_in, nb, c->d_in + 2 * nb, c_sizes, k, st);
+  if (rc) return rc;
+  cudaEvent_t e0, e1;
+  if (c->flags & SBC_FLAG_TIMING) {
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+  }
+  const auto& outs = c->pl->outputs();
+  c->h_off.resize(k, nullptr);
+  c->h_xy.resize(k, nullptr);
+  c->h_off_cap.resize(k, 0);
+  c->h_xy_cap.resize(k, 0);
+  for (int i = 0; i < k; ++i) {
+    const auto& o = outs[i];
+    if (!ensure_pinned(c->h_off[i], c->h_off_cap[i], (size_t)o.nrings + 1) ||
+        !ensure_pinned(c->h_xy[i], c->h_xy_cap[i], 2 * (size_t)o.nverts + 2))
+      return set_err(c, SBC_ENOMEM, "pinned result buffers");
+    c->h_off[i][0] = 0;
+    if (o.nrings > 0)
+      cudaMemcpyAsync(c->h_off[i], o.d_off, sizeof(int) * (o.nrings + 1), cudaMemcpyDeviceToHost,
+                      st);
+    if (o.nverts > 0)
+      cudaMemcpyAsync(c->h_xy[i], o.d_xy, sizeof(double) * 2 * o.nverts, cudaMemcpyDeviceToHost,
+                      st);
+  }
+  rc = cuda_check(c, cudaStreamSynchronize(st), "result copy");
+  if (rc) return rc;
+  if (c->flags & SBC_FLAG_TIMING) {
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&c->phase_ms[6], e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  for (int i = 0; i < k; ++i) {
+    out[i].nrings = outs[i].nrings;
+    out[i].nverts = outs[i].nverts;
+    out[i].offsets = c->h_off[i];
+    out[i].xy = c->h_xy[i];
+  }
+  return SBC_OK;
+}
+
+int sbc_clip_pair(sbc_ctx* c, const double* b_xy, int nb, const double* c_xy, int nc,
+                  sbc_rings* out, void* stream) {
+  int sizes[1] = {nc};
+  return sbc_clip_one_to_many(c, b_xy, nb, c_xy, sizes, 1, out, stream);
+}
+
+int sbc_clip_pair_device(sbc_ctx* c, const double* d_b, int nb, const double* d_c, int nc,
+                         sbc_rings* out, void* stream) {
+  if (!c || !d_b || !d_c || !out) return set_err(c, SBC_EINPUT, "null argument");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  int sizes[1] = {nc};
+  int rc = run_device(c, d_b, nb, d_c, sizes, 1, st);
+  if (rc) return rc;
+  const auto& o = c->pl->outputs()[0];
+  out->nrings = o.nrings;
+  out->nverts = o.nverts;
+  out->offsets = o.d_off;
+  out->xy = o.d_xy;
+  return SBC_OK;
+}
+
+int sbc_stats(const sbc_ctx* c, long long* out, int n) {
+  if (!c || !out) return SBC_EINPUT;
+  for (int i = 0; i < n && i < SBC_STAT_NUM; ++i) out[i] = c->stats[i];
+  return SBC_OK;
+}
+
+int sbc_phase_times(const sbc_ctx* c, float* out, int n) {
+  if (!c || !out) return SBC_EINPUT;
+  for (int i = 0; i < n && i < 8; ++i) out[i] = c->phase_ms[i];
+  return SBC_OK;
+}
+
+int sbc_debug_array(sbc_ctx* c, int which, void* dst, long long cap, long long* count) {
+  if (!c || !count) return set_err(c, SBC_EINPUT, "null argument");
+  Pipeline& p = *c->pl;
+  const void* src = nullptr;
+  long long n = 0;
+  size_t es = sizeof(int);
+  switch (which) {
+    case SBC_ARR_UNIQ_B: src = p.dbg_ub; n = p.dbg_K; break;
+    case SBC_ARR_UNIQ_C: src = p.dbg_uc; n = p.dbg_K; break;
+    case SBC_ARR_UNIQ_T: src = p.dbg_ut; n = p.dbg_K; break;
+    case SBC_ARR_ISECT_XY: src = p.dbg_isxy; n = 2LL * p.dbg_K; es = sizeof(double); break;
+    case SBC_ARR_ISECT_AB: src = p.dbg_aB; n = p.dbg_K; break;
+    case SBC_ARR_ISECT_AC: src = p.dbg_aC; n = p.dbg_K; break;
+    case SBC_ARR_MERGED_BXY: src = p.dbg_ixB; n = 2LL * p.dbg_nB; es = sizeof(double); break;
+    case SBC_ARR_MERGED_CXY: src = p.dbg_ixC; n = 2LL * p.dbg_nQ; es = sizeof(double); break;
+    case SBC_ARR_MERGED_BALPHA: src = p.dbg_alB; n = p.dbg_nB; break;
+    case SBC_ARR_MERGED_CALPHA: src = p.dbg_alC; n = p.dbg_nQ; break;
+    case SBC_ARR_MERGED_BNB: src = p.dbg_nbB; n = p.dbg_nB; break;
+    case SBC_ARR_MERGED_CNB: src = p.dbg_nbC; n = p.dbg_nQ; break;
+    case SBC_ARR_LABEL_B: src = p.dbg_labB; n = p.dbg_nB; break;
+    case SBC_ARR_LABEL_C: src = p.dbg_labC; n = p.dbg_nQ; break;
+    default: return set_err(c, SBC_EINPUT, "unknown array");
+  }
+  *count = n;
+  long long m = n < cap ? n : cap;
+  if (dst && src && m > 0) {
+    cudaStream_t st = c->pl->stream();
+    int rc = cuda_check(c, cudaMemcpyAsync(dst, src, es * m, cudaMemcpyDeviceToHost, st), "debug");
+    if (rc) return rc;
+    return cuda_check(c, cudaStreamSynchronize(st), "debug");
+  }
+  return SBC_OK;
+}
+
+unsigned long long sbc_kernel_launches(void) { return sbc::g_launches; }
+
+int sbc_profile_begin(void) {
+  sbc::profile_begin();
+  return SBC_OK;
+}
+
+int sbc_profile_end(char* names, int names_len, float* ms, int* counts, int cap, int* n_out) {
+  std::vector<std::string> nm;
+  std::vector<float> t;
+  std::vector<int> c;
+  int n = sbc::profile_end(&nm, &t, &c);
+  if (n_out) *n_out = n;
+  int w = 0;
+  for (int i = 0; i < n && i < cap; ++i) {
+    if (ms) ms[i] = t[i];
+    if (counts) counts[i] = c[i];
+    if (names) {
+      int need = (int)nm[i].size() + 1;
+      if (w + need <= names_len) {
+        memcpy(names + w, nm[i].c_str(), need);
+        w += need;
+      }
+    }
+  }
+  return SBC_OK;
+}
+
+const char* sbc_version(void) { return "sbclip-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- classifier
+namespace {
+__global__ void k_classify(const double* __restrict__ pairs, int n, int* __restrict__ types,
+                           double* __restrict__ alpha, double* __restrict__ beta,
+                           int* __restrict__ ai, int* __restrict__ bi) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* p = pairs + 8 * (size_t)i;
+  double a = 0.0, b = 0.0;
+  int t = sbc::seg_isect(p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], &a, &b);
+  types[i] = t;
+  alpha[i] = a;
+  beta[i] = b;
+  ai[i] = t ? sbc::alpha_to_int(a) : 0;
+  bi[i] = t ? sbc::alpha_to_int(b) : 0;
+}
+}  // namespace
+
+extern "C" int sbc_classify_pairs(sbc_ctx* c, const double* pairs, int n, int* types,
+                                  double* alpha, double* beta, int* alpha_int, int* beta_int) {
+  if (!c || (!pairs && n > 0)) return set_err(c, SBC_EINPUT, "null argument");
+  if (n <= 0) return SBC_OK;
+  cudaSetDevice(c->device);
+  cudaStream_t st = c->own;
+  sbc::BufferPool& bp = c->pl->pool();
+  double* dp = (double*)bp.get("cls_pairs", sizeof(double) * 8 * (size_t)n);
+  int* dt = (int*)bp.get("cls_t", sizeof(int) * n);
+  double* da = (double*)bp.get("cls_a", sizeof(double) * n);
+  double* db = (double*)bp.get("cls_b", sizeof(double) * n);
+  int* dai = (int*)bp.get("cls_ai", sizeof(int) * n);
+  int* dbi = (int*)bp.get("cls_bi", sizeof(int) * n);
+  if (bp.failed) return set_err(c, SBC_ENOMEM, "device allocation failed (classifier)");
+  cudaMemcpyAsync(dp, pairs, sizeof(double) * 8 * (size_t)n, cudaMemcpyHostToDevice, st);
+  {
+    ::sbc::KProbe kp_("k_classify", st);
+    k_classify<<<sbc::grid_for(n, 256), 256, 0, st>>>(dp, n, dt, da, db, dai, dbi);
+  }
+  if (types) cudaMemcpyAsync(types, dt, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
+  if (alpha) cudaMemcpyAsync(alpha, da, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
+  if (beta) cudaMemcpyAsync(beta, db, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
+  if (alpha_int) cudaMemcpyAsync(alpha_int, dai, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
+  if (beta_int) cudaMemcpyAsync(beta_int, dbi, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
+  return cuda_check(c, cudaStreamSynchronize(st), "classifier");
+}

@@ -1,0 +1,1339 @@
+// sbc_back.cu -- Greiner-Hormann / Foster back end on the merged ring arrays
+// (reference rows A15-A19):
+//
+//  A15  copyToLinkedList        src/clip.cpp:606-695
+//  A16  labelIntersections2     foster/polyclip.h:337-709
+//  A17  createResult2           foster/polyclip.h:717-759
+//  A18  cleanUpResult2          foster/polyclip.h:767-787
+//
+// The reference walks linked lists one vertex at a time.  Here the linked
+// lists are the slot arrays themselves (list order == slot order), and the
+// common case runs data-parallel:
+//   * entry/exit flags are a prefix parity over crossing vertices, seeded by
+//     a parallel point-in-polygon reduction;
+//   * ring starts come from pointer jumping (the first crossing vertex of a
+//     ring in list order starts it);
+//   * rings are traced segment by segment (one thread per ring, O(segments)),
+//     then every vertex is copied in parallel;
+//   * collinear clean-up is a parallel test, with an exact per-ring pass
+//     only for rings that lose vertices.
+// Inputs the data-parallel path does not cover (intersection chains, bouncing
+// split pairs, polygons made only of intersection vertices, inconsistent
+// entry/exit structure, coordinate collisions in the list bridge) are
+// detected on the device and run through `k_serial_backend`, a single-thread
+// kernel that follows the reference's linked-list algorithm step by step.
+#include <cstdio>
+
+#include "sbc_pipeline.cuh"
+
+namespace sbc {
+
+namespace {
+
+enum { L_NONE = 0, L_CROSSING, L_BOUNCING, L_LEFT_ON, L_RIGHT_ON, L_ON_ON, L_ON_LEFT, L_ON_RIGHT,
+       L_DCROSS, L_DBOUNCE };
+enum { EX_EXIT = 0, EX_ENTRY = 1, EX_NEITHER = 2 };
+
+// scalars the fast path computes (one struct, one read-back)
+struct BkScalars {
+  unsigned anomaly;
+  int crossCount[2];
+  int firstFree[2];     // first slot that is not an intersection vertex
+  int notOnOn[2];       // vertices whose label is not ON_ON
+  int winding[2];       // winding number of the seed point against the other ring
+  int nRings;
+  int pad;
+};
+
+// ---------------------------------------------------------------- list bridge (A15)
+__global__ void k_mark_src(int n, const int* __restrict__ ndPS, unsigned char* __restrict__ src) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  src[k + ndPS[k]] = 1;
+}
+
+// copyToLinkedList matches list vertices by coordinates: an inserted entry
+// equal to the next source vertex would be taken for it (anomaly)
+__global__ void k_bridge_check(int nSrc, int nSlots, const int* __restrict__ ndPS,
+                               const double* __restrict__ ix, const double* __restrict__ poly,
+                               int polyOff, BkScalars* sc) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nSrc) return;
+  int a = k + ndPS[k] + 1;
+  int b = (k + 1 < nSrc) ? (k + 1 + ndPS[k + 1]) : nSlots;
+  int nx = (k + 1 < nSrc) ? k + 1 : 0;
+  double vx = poly[2 * (polyOff + nx)], vy = poly[2 * (polyOff + nx) + 1];
+  for (int i = a; i < b; ++i)
+    if (ix[2 * i] == vx && ix[2 * i + 1] == vy) atomicOr(&sc->anomaly, 1u);
+}
+
+// P: intersection flag, label; Q: flag, label, neighbour (copyToLinkedList)
+__global__ void k_init_P(int nB, const unsigned char* __restrict__ src, const int* __restrict__ alB,
+                         const int* __restrict__ labB, unsigned char* __restrict__ isect,
+                         int* __restrict__ lab) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nB) return;
+  isect[i] = (!src[i] || alB[i] != -100) ? 1 : 0;
+  lab[i] = labB[i];
+}
+
+__global__ void k_init_Q(int nQ, int nB, const unsigned char* __restrict__ src,
+                         const int* __restrict__ nbC, const int* __restrict__ labC,
+                         unsigned char* __restrict__ isect, int* __restrict__ lab,
+                         int* __restrict__ nbQ, int* __restrict__ winP, BkScalars* sc) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nQ) return;
+  bool is = !src[q] || nbC[q] != -100;
+  isect[q] = is ? 1 : 0;
+  lab[q] = labC[q];
+  nbQ[q] = -1;
+  if (is) {
+    int t = nbC[q] - 1;
+    if (t < 0 || t >= nB) {
+      atomicOr(&sc->anomaly, 2u);
+      return;
+    }
+    nbQ[q] = t;
+    atomicMax(&winP[t], q);  // the last C vertex linked to t wins
+  }
+}
+
+// per-side statistics: crossing count, first non-intersection slot, ON_ON
+__global__ void k_side_stats(int n, const unsigned char* __restrict__ isect,
+                             const int* __restrict__ lab, int side, int checkChains,
+                             BkScalars* sc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int cross = 0, notonon = 0;
+  if (i < n) {
+    int l = lab[i];
+    if (isect[i] && l == L_CROSSING) cross = 1;
+    if (l != L_ON_ON) notonon = 1;
+    if (!isect[i]) atomicMin(&sc->firstFree[side], i);
+    if (checkChains && isect[i] && (l == L_LEFT_ON || l == L_RIGHT_ON)) atomicOr(&sc->anomaly, 4u);
+    if (l == L_DCROSS || l == L_DBOUNCE) atomicOr(&sc->anomaly, 4u);
+  }
+  for (int s = 16; s > 0; s >>= 1) {
+    cross += __shfl_xor_sync(0xffffffffu, cross, s);
+    notonon += __shfl_xor_sync(0xffffffffu, notonon, s);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (cross) atomicAdd(&sc->crossCount[side], cross);
+    if (notonon) atomicAdd(&sc->notOnOn[side], notonon);
+  }
+}
+
+// pointInPoly (foster/polygon.h:427-448) as a reduction over the ring's edges;
+// the seed point is slot `seed` of `sp` (or an explicit point)
+__global__ void k_pip(int n, const double* __restrict__ ring, const double* __restrict__ sp,
+                      const int* __restrict__ seedSlot, int side, BkScalars* sc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int s = *seedSlot;
+  double rx = sp[2 * s], ry = sp[2 * s + 1];
+  int w = 0;
+  if (i < n) {
+    int j = (i + 1 == n) ? 0 : i + 1;
+    double x0 = ring[2 * i], y0 = ring[2 * i + 1], x1 = ring[2 * j], y1 = ring[2 * j + 1];
+    if ((y0 < ry) != (y1 < ry)) {
+      int d = 2 * (y1 > y0) - 1;
+      if (x0 >= rx) {
+        if (x1 > rx) w = d;
+        else if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (y1 > y0)) w = d;
+      } else if (x1 > rx) {
+        if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (y1 > y0)) w = d;
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+  if ((threadIdx.x & 31) == 0 && w) atomicAdd(&sc->winding[side], w);
+}
+
+// ---------------------------------------------------------------- entry/exit (A16 step 4)
+__global__ void k_cross_flags(int n, const unsigned char* __restrict__ isect,
+                              const int* __restrict__ lab, int* __restrict__ c) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  c[i] = (i < n && isect[i] && lab[i] == L_CROSSING) ? 1 : 0;
+}
+
+// status before vertex i = ENTRY ^ inside(V) ^ parity(crossings from V to i)
+__global__ void k_enex(int n, const unsigned char* __restrict__ isect, const int* __restrict__ lab,
+                       const int* __restrict__ pre, int side, const BkScalars* __restrict__ sc,
+                       unsigned char* __restrict__ enex, unsigned char* __restrict__ split,
+                       int* __restrict__ list) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int V = sc->firstFree[side];
+  int total = pre[n];
+  int r = (i >= V) ? (pre[i] - pre[V]) : (pre[i] + total - pre[V]);
+  int status0 = (sc->winding[side] & 1) ? EX_EXIT : EX_ENTRY;
+  int status = (r & 1) ? (1 - status0) : status0;
+  int l = lab[i];
+  unsigned char e = EX_NEITHER;
+  if (isect[i] && l == L_CROSSING) {
+    e = (unsigned char)status;
+    list[pre[i]] = i;
+  }
+  enex[i] = e;
+  split[i] = (isect[i] && l == L_BOUNCING && status == EX_EXIT) ? 1 : 0;
+}
+
+// a bouncing vertex whose neighbour is also a split candidate needs the
+// split-pair insertion of step 5 (serial path)
+__global__ void k_split_check(int nB, const unsigned char* __restrict__ splitP,
+                              const unsigned char* __restrict__ splitQ, const int* __restrict__ winP,
+                              BkScalars* sc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nB) return;
+  if (!splitP[i]) return;
+  int q = winP[i];
+  if (q >= 0 && splitQ[q]) atomicOr(&sc->anomaly, 8u);
+}
+
+// ---------------------------------------------------------------- tracing (A17)
+// enex vertices are indexed 0..cP-1 (P, slot order) then cP..cP+cQ-1 (Q)
+struct Trace {
+  int nB, nQ, cP, cQ;
+  const int* listP;   // enex slots of P in slot order
+  const int* listQ;
+  const unsigned char* enexP;
+  const unsigned char* enexQ;
+  const int* winP;    // neighbour of P slot (Q slot) or -1
+  const int* nbQ;     // neighbour of Q slot (P slot) or -1
+  const int* rankP;   // slot -> enex index (valid for enex slots)
+  const int* rankQ;
+};
+
+__device__ __forceinline__ int tr_slot(const Trace& T, int x) {
+  return x < T.cP ? T.listP[x] : T.listQ[x - T.cP];
+}
+
+// target: next EXIT forward from an ENTRY vertex, previous ENTRY backward from
+// an EXIT vertex; with alternating flags this is the adjacent enex vertex
+__device__ __forceinline__ int tr_target(const Trace& T, int x) {
+  if (x < T.cP) {
+    int e = T.enexP[T.listP[x]];
+    return e == EX_ENTRY ? (x + 1 == T.cP ? 0 : x + 1) : (x == 0 ? T.cP - 1 : x - 1);
+  }
+  int y = x - T.cP;
+  int e = T.enexQ[T.listQ[y]];
+  int z = e == EX_ENTRY ? (y + 1 == T.cQ ? 0 : y + 1) : (y == 0 ? T.cQ - 1 : y - 1);
+  return T.cP + z;
+}
+
+// neighbour jump from enex vertex t (-1 if the neighbour is no enex vertex)
+__device__ __forceinline__ int tr_jump(const Trace& T, int t) {
+  if (t < T.cP) {
+    int q = T.winP[T.listP[t]];
+    if (q < 0 || T.enexQ[q] == EX_NEITHER) return -1;
+    return T.cP + T.rankQ[q];
+  }
+  int p = T.nbQ[T.listQ[t - T.cP]];
+  if (p < 0 || T.enexP[p] == EX_NEITHER) return -1;
+  return T.rankP[p];
+}
+
+__global__ void k_rank(int n, const int* __restrict__ list, int* __restrict__ rank) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= n) return;
+  rank[list[x]] = x;
+}
+
+__global__ void k_tr_init(Trace T, int* __restrict__ jmp, int* __restrict__ mval, BkScalars* sc) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = T.cP + T.cQ;
+  if (x >= n) return;
+  int t = tr_target(T, x);
+  // alternation: the target must carry the opposite flag
+  int ex = x < T.cP ? T.enexP[T.listP[x]] : T.enexQ[T.listQ[x - T.cP]];
+  int et = t < T.cP ? T.enexP[T.listP[t]] : T.enexQ[T.listQ[t - T.cP]];
+  if (ex == et) atomicOr(&sc->anomaly, 16u);
+  int s = tr_jump(T, t);
+  if (s < 0) {
+    atomicOr(&sc->anomaly, 32u);
+    s = x;
+  }
+  jmp[x] = s;
+  int a = x < T.cP ? T.listP[x] : 0x7fffffff;
+  int b = t < T.cP ? T.listP[t] : 0x7fffffff;
+  mval[x] = a < b ? a : b;
+}
+
+__global__ void k_tr_jump(int n, const int* __restrict__ jin, const int* __restrict__ min_,
+                          int* __restrict__ jout, int* __restrict__ mout) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= n) return;
+  int j = jin[x];
+  int a = min_[x], b = min_[j];
+  mout[x] = a < b ? a : b;
+  jout[x] = jin[j];
+}
+
+// every enex vertex must agree with its successor and its target on the
+// ring minimum (rings are closed under both)
+__global__ void k_tr_consistent(Trace T, const int* __restrict__ mval, BkScalars* sc) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = T.cP + T.cQ;
+  if (x >= n) return;
+  int t = tr_target(T, x);
+  int s = tr_jump(T, t);
+  if (s < 0 || mval[x] != mval[t] || mval[x] != mval[s]) atomicOr(&sc->anomaly, 64u);
+}
+
+__global__ void k_tr_starts(Trace T, const int* __restrict__ mval, int* __restrict__ isStart) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x > T.cP) return;
+  isStart[x] = (x < T.cP && mval[x] == T.listP[x]) ? 1 : 0;
+}
+
+__global__ void k_tr_startlist(int cP, const int* __restrict__ pre, int* __restrict__ starts) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= cP) return;
+  if (pre[x + 1] != pre[x]) starts[pre[x]] = x;
+}
+
+__device__ __forceinline__ int tr_len(const Trace& T, int x, int t) {
+  int n = x < T.cP ? T.nB : T.nQ;
+  int sx = tr_slot(T, x), st = tr_slot(T, t);
+  bool fwd = (x < T.cP ? T.enexP[sx] : T.enexQ[sx]) == EX_ENTRY;
+  int d = fwd ? st - sx : sx - st;
+  if (d <= 0) d += n;
+  return d;
+}
+
+// createResult2 per ring, segment by segment.  PASS 0 counts, PASS 1 writes
+// segment descriptors (enex index of the segment start, output offset).
+template <int PASS>
+__global__ void k_tr_walk(Trace T, int nRings, const int* __restrict__ starts,
+                          int* __restrict__ rlen, int* __restrict__ rseg,
+                          const int* __restrict__ vOff, const int* __restrict__ sOff,
+                          int* __restrict__ segX, int* __restrict__ segOut, BkScalars* sc) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nRings) return;
+  const int I = starts[r];
+  int cur = I;
+  int len = 0, nseg = 0;
+  int guard = T.cP + T.cQ + 2;
+  int vo = PASS ? vOff[r] : 0, so = PASS ? sOff[r] : 0;
+  while (true) {
+    int t = tr_target(T, cur);
+    if (PASS) {
+      segX[so + nseg] = cur;
+      segOut[so + nseg] = vo + len;
+    }
+    len += tr_len(T, cur, t);
+    ++nseg;
+    if (t == I) break;
+    int s = tr_jump(T, t);
+    if (s == I) break;
+    if (s < 0 || --guard < 0) {
+      atomicOr(&sc->anomaly, 128u);
+      break;
+    }
+    cur = s;
+  }
+  if (!PASS) {
+    rlen[r] = len;
+    rseg[r] = nseg;
+  }
+}
+
+__global__ void k_tr_copy(Trace T, long long nv, int nseg, const int* __restrict__ segX,
+                          const int* __restrict__ segOut, const double* __restrict__ ixB,
+                          const double* __restrict__ ixC, double* __restrict__ out) {
+  long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  int lo = 0, hi = nseg;  // last segment with segOut <= v
+  while (hi - lo > 1) {
+    int m = (lo + hi) >> 1;
+    if (segOut[m] <= v) lo = m;
+    else hi = m;
+  }
+  int x = segX[lo];
+  int step = (int)(v - segOut[lo]) + 1;
+  bool onP = x < T.cP;
+  int n = onP ? T.nB : T.nQ;
+  int sx = tr_slot(T, x);
+  bool fwd = (onP ? T.enexP[sx] : T.enexQ[sx]) == EX_ENTRY;
+  int slot = fwd ? (sx + step) % n : ((sx - step) % n + n) % n;
+  const double* src = onP ? ixB : ixC;
+  out[2 * v] = src[2 * slot];
+  out[2 * v + 1] = src[2 * slot + 1];
+}
+
+// ---------------------------------------------------------------- clean-up (A18)
+__global__ void k_ring_of(int nRings, const int* __restrict__ off, int* __restrict__ ringOf) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nRings) return;
+  for (int v = off[r]; v < off[r + 1]; ++v) ringOf[v] = r;
+}
+
+__global__ void k_collinear(long long nv, const int* __restrict__ off,
+                            const int* __restrict__ ringOf, const double* __restrict__ xy,
+                            int* __restrict__ ringFlag) {
+  long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  int r = ringOf[v];
+  int a = off[r], b = off[r + 1];
+  long long p = v == a ? b - 1 : v - 1;
+  long long q = v + 1 == b ? a : v + 1;
+  if (fabs(area3(xy[2 * p], xy[2 * p + 1], xy[2 * v], xy[2 * v + 1], xy[2 * q], xy[2 * q + 1])) <
+      kEps)
+    ringFlag[r] = 1;
+}
+
+// exact cleanUpResult2 on one ring (thread per flagged ring); the reference
+// follows a deleted vertex's old next pointer, which this loop does
+__global__ void k_cleanup_ring(int nRings, const int* __restrict__ off,
+                               const int* __restrict__ ringFlag, const double* __restrict__ xy,
+                               int* __restrict__ nxt, int* __restrict__ prv,
+                               int* __restrict__ keep) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nRings) return;
+  int a = off[r], b = off[r + 1];
+  for (int v = a; v < b; ++v) keep[v] = 1;
+  if (!ringFlag[r] || b == a) return;
+  for (int v = a; v < b; ++v) {
+    nxt[v] = v + 1 == b ? a : v + 1;
+    prv[v] = v == a ? b - 1 : v - 1;
+  }
+  auto A = [&](int v) {
+    int p = prv[v], q = nxt[v];
+    return fabs(area3(xy[2 * p], xy[2 * p + 1], xy[2 * v], xy[2 * v + 1], xy[2 * q], xy[2 * q + 1]));
+  };
+  int root = a;
+  auto remove = [&](int V) {
+    if (root == V) {
+      root = nxt[V];
+      if (nxt[root] == root) root = -1;
+    }
+    nxt[prv[V]] = nxt[V];
+    prv[nxt[V]] = prv[V];
+    keep[V] = 0;
+  };
+  while (root >= 0 && A(root) < kEps) remove(root);
+  if (root < 0) {
+    for (int v = a; v < b; ++v) keep[v] = 0;
+    return;
+  }
+  int start = root, V = start;
+  do {
+    int nx = nxt[V];
+    if (A(V) < kEps) remove(V);
+    V = nx;
+  } while (V != start);
+  if (root < 0)
+    for (int v = a; v < b; ++v) keep[v] = 0;
+}
+
+__global__ void k_keep_counts(int nRings, const int* __restrict__ off, const int* __restrict__ keep,
+                              int* __restrict__ cnt) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r > nRings) return;
+  if (r == nRings) {
+    cnt[r] = 0;
+    return;
+  }
+  int c = 0;
+  for (int v = off[r]; v < off[r + 1]; ++v) c += keep[v];
+  cnt[r] = c;
+}
+
+// output ring order starts at the ring's root, which stays at its first kept
+// vertex after the root loop; rings that lost every vertex print nothing
+__global__ void k_compact_rings(int nRings, const int* __restrict__ off,
+                                const int* __restrict__ keep, const int* __restrict__ kpre,
+                                const int* __restrict__ rpre, const double* __restrict__ xy,
+                                double* __restrict__ oxy, int* __restrict__ ooff) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nRings) return;
+  int a = off[r], b = off[r + 1];
+  int kept = kpre[r + 1] - kpre[r];
+  if (kept > 0) ooff[rpre[r]] = kpre[r];
+  // the root is the first vertex surviving the root loop; later removals
+  // never touch it, so the output starts at the first kept vertex
+  int w = kpre[r];
+  for (int v = a; v < b; ++v)
+    if (keep[v]) {
+      oxy[2 * w] = xy[2 * v];
+      oxy[2 * w + 1] = xy[2 * v + 1];
+      ++w;
+    }
+}
+
+__global__ void k_ring_nonempty(int nRings, const int* __restrict__ kpre, int* __restrict__ ne) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r > nRings) return;
+  ne[r] = (r < nRings && kpre[r + 1] > kpre[r]) ? 1 : 0;
+}
+
+__global__ void k_set_last(int* __restrict__ ooff, const int* __restrict__ rpre, int nRings,
+                           const int* __restrict__ kpre) {
+  ooff[rpre[nRings]] = kpre[nRings];
+}
+
+// ---------------------------------------------------------------- whole-list rings (A16 step 3.5)
+__global__ void k_copy_list(int n, const double* __restrict__ src, double* __restrict__ dst) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 2 * n) return;
+  dst[i] = src[i];
+}
+
+// ================================================================ serial emulation
+// A literal restatement of copyToLinkedList + labelIntersections2 +
+// createResult2 + cleanUpResult2 over index-linked pools (one thread).
+struct Pool {
+  double *x, *y;
+  int *next, *prev, *nb, *label, *enex;
+  unsigned char *source, *isect;
+  int n, cap;
+};
+
+struct SerialArgs {
+  Pool P, Q, R;
+  int* rroot;
+  int rcap;
+  int* nrings;
+  unsigned char *splitP, *splitQ, *crossP, *crossQ;
+  int bSize, cSize, cStart, nB, nQ;
+  const double *bP, *cP, *ixB, *ixC;
+  const int *alB, *nbC, *labB, *labC;
+  int* status;   // 0 ok, 2 undefined, 3 capacity
+};
+
+__device__ int pnew(Pool& p, double x, double y) {
+  if (p.n >= p.cap) return -1;
+  int v = p.n++;
+  p.x[v] = x;
+  p.y[v] = y;
+  p.next[v] = p.prev[v] = v;
+  p.nb[v] = -1;
+  p.label[v] = L_NONE;
+  p.enex[v] = EX_NEITHER;
+  p.source[v] = 0;
+  p.isect[v] = 0;
+  return v;
+}
+
+__device__ void pinsert_after(Pool& p, int V, int curr) {
+  curr = p.next[curr];
+  p.next[p.prev[curr]] = V;
+  p.prev[V] = p.prev[curr];
+  p.next[V] = curr;
+  p.prev[curr] = V;
+}
+
+__device__ int ppip(const Pool& p, int root, double rx, double ry) {
+  int w = 0, one = root;
+  do {
+    int two = p.next[one];
+    double x0 = p.x[one], y0 = p.y[one], x1 = p.x[two], y1 = p.y[two];
+    if ((y0 < ry) != (y1 < ry)) {
+      if (x0 >= rx) {
+        if (x1 > rx) w = w + 2 * (y1 > y0) - 1;
+        else if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (y1 > y0)) w = w + 2 * (y1 > y0) - 1;
+      } else if (x1 > rx) {
+        if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (y1 > y0)) w = w + 2 * (y1 > y0) - 1;
+      }
+    }
+    one = two;
+  } while (one != root);
+  return (w % 2) != 0;
+}
+
+__device__ int rnew(SerialArgs& a) {
+  if (*a.nrings >= a.rcap) return -1;
+  int r = (*a.nrings)++;
+  a.rroot[r] = -1;
+  return r;
+}
+
+__device__ int radd(SerialArgs& a, int r, double x, double y) {
+  int v = pnew(a.R, x, y);
+  if (v < 0) return -1;
+  int root = a.rroot[r];
+  if (root < 0) {
+    a.rroot[r] = v;
+  } else {
+    a.R.prev[v] = a.R.prev[root];
+    a.R.next[v] = root;
+    a.R.next[a.R.prev[root]] = v;
+    a.R.prev[root] = v;
+  }
+  return 0;
+}
+
+__device__ int rcopy(SerialArgs& a, const Pool& p, int root) {
+  int r = rnew(a);
+  if (r < 0) return -1;
+  int v = root;
+  do {
+    if (radd(a, r, p.x[v], p.y[v])) return -1;
+    v = p.next[v];
+  } while (v != root);
+  return 0;
+}
+
+__device__ void tog(int* s) {
+  if (*s == EX_ENTRY) *s = EX_EXIT;
+  else if (*s == EX_EXIT) *s = EX_ENTRY;
+}
+
+__device__ int ser_build(SerialArgs& a) {
+  Pool& P = a.P;
+  Pool& Q = a.Q;
+  int nB = a.nB, nQ = a.nQ, i = 0;
+  for (int ii = 0; ii <= a.bSize; ++ii) {
+    int sv = ii < a.bSize ? ii : 0;
+    double vx = a.bP[2 * sv], vy = a.bP[2 * sv + 1];
+    while (a.ixB[(2 * i) % (2 * nB)] != vx || a.ixB[(2 * i + 1) % (2 * nB)] != vy) {
+      if (i >= nB) return 2;
+      int v = pnew(P, a.ixB[2 * i], a.ixB[2 * i + 1]);
+      if (v < 0) return 3;
+      P.label[v] = a.labB[i];
+      P.isect[v] = 1;
+      i++;
+    }
+    if (ii < a.bSize) {
+      int v = pnew(P, vx, vy);
+      if (v != i) return 2;
+      P.source[v] = 1;
+      P.label[v] = a.labB[i];
+      if (a.alB[i] != -100) P.isect[v] = 1;
+    }
+    i++;
+  }
+  if (P.n != nB) return 2;
+  for (int v = 0; v < nB; ++v) {
+    P.next[v] = (v + 1) % nB;
+    P.prev[v] = (v + nB - 1) % nB;
+  }
+  i = 0;
+  for (int ii = 0; ii <= a.cSize; ++ii) {
+    int sv = ii < a.cSize ? ii : 0;
+    double vx = a.cP[2 * (a.cStart + sv)], vy = a.cP[2 * (a.cStart + sv) + 1];
+    while (a.ixC[(2 * i) % (2 * nQ)] != vx || a.ixC[(2 * i + 1) % (2 * nQ)] != vy) {
+      if (i >= nQ) return 2;
+      int v = pnew(Q, a.ixC[2 * i], a.ixC[2 * i + 1]);
+      if (v < 0) return 3;
+      Q.label[v] = a.labC[i];
+      Q.isect[v] = 1;
+      int t = a.nbC[i] - 1;
+      if (t < 0 || t >= nB) return 2;
+      Q.nb[v] = t;
+      P.nb[t] = v;
+      i++;
+    }
+    if (ii < a.cSize) {
+      int v = pnew(Q, vx, vy);
+      if (v != i) return 2;
+      Q.source[v] = 1;
+      Q.label[v] = a.labC[i];
+      if (a.nbC[i] != -100) {
+        int t = a.nbC[i] - 1;
+        if (t < 0 || t >= nB) return 2;
+        Q.isect[v] = 1;
+        Q.nb[v] = t;
+        P.nb[t] = v;
+      }
+    }
+    i++;
+  }
+  if (Q.n != nQ) return 2;
+  for (int v = 0; v < nQ; ++v) {
+    Q.next[v] = (v + 1) % nQ;
+    Q.prev[v] = (v + nQ - 1) % nQ;
+  }
+  return 0;
+}
+
+__device__ Pool& side(SerialArgs& a, int s) { return s == 0 ? a.P : a.Q; }
+
+__device__ int ser_non_isect_vertex(SerialArgs& a, int s, int root) {
+  Pool& p = side(a, s);
+  Pool& o = side(a, 1 - s);
+  int V = root;
+  do {
+    if (!p.isect[V]) return V;
+    V = p.next[V];
+  } while (V != root);
+  V = root;
+  do {
+    int nbV = p.nb[V], nbN = p.nb[p.next[V]];
+    if (nbV < 0) return -2;
+    if (nbN != o.prev[nbV] && nbN != o.next[nbV]) {
+      double mx = 0.5 * (p.x[V] + p.x[p.next[V]]);
+      double my = 0.5 * (p.y[V] + p.y[p.next[V]]);
+      mx = dmul(0.5, dadd(p.x[V], p.x[p.next[V]]));
+      my = dmul(0.5, dadd(p.y[V], p.y[p.next[V]]));
+      int T = pnew(p, mx, my);
+      if (T < 0) return -3;
+      pinsert_after(p, T, V);
+      return T;
+    }
+    V = p.next[V];
+  } while (V != root);
+  return -2;
+}
+
+__device__ int ser_label_trace(SerialArgs& a) {
+  Pool& P = a.P;
+  Pool& Q = a.Q;
+  int roots[2] = {0, 0};
+  // (2) chains
+  {
+    int V = roots[0];
+    do {
+      if (P.isect[V] && (P.label[V] == L_LEFT_ON || P.label[V] == L_RIGHT_ON)) {
+        int x = P.label[V] == L_LEFT_ON ? 0 : 1;
+        int X = V, I = V;
+        int guard = P.n + 1;
+        do {
+          P.label[I] = L_NONE;
+          if (P.nb[I] < 0) return 2;
+          Q.label[P.nb[I]] = L_NONE;
+          I = P.next[I];
+          if (--guard < 0) return 2;
+        } while (P.label[I] == L_ON_ON);
+        int y = P.label[I] == L_ON_LEFT ? 0 : 1;
+        int chain = (x != y) ? L_DCROSS : L_DBOUNCE;
+        P.label[X] = chain;
+        P.label[I] = chain;
+        if (P.nb[X] < 0 || P.nb[I] < 0) return 2;
+        Q.label[P.nb[X]] = chain;
+        Q.label[P.nb[I]] = chain;
+      }
+      V = P.next[V];
+    } while (V != roots[0]);
+  }
+  // (3.5)
+  int noIsect[2] = {0, 0}, ident[2] = {0, 0};
+  for (int s = 0; s < 2; ++s) {
+    Pool& p = side(a, s);
+    int root = roots[s], nocross = 1, V = root;
+    do {
+      if (p.isect[V] && (p.label[V] == L_CROSSING || p.label[V] == L_DCROSS)) nocross = 0;
+      V = p.next[V];
+    } while (V != root);
+    if (!nocross) continue;
+    noIsect[s] = 1;
+    int allon = 1;
+    V = root;
+    do {
+      if (p.label[V] != L_ON_ON) allon = 0;
+      V = p.next[V];
+    } while (V != root);
+    if (allon) {
+      ident[s] = 1;
+      continue;
+    }
+    double px = 0, py = 0;
+    int found = 0;
+    V = root;
+    do {
+      if (!p.isect[V]) {
+        px = p.x[V];
+        py = p.y[V];
+        found = 1;
+        break;
+      }
+      V = p.next[V];
+    } while (V != root);
+    if (!found) {
+      Pool& o = side(a, 1 - s);
+      V = root;
+      do {
+        int nbV = p.nb[V], nbN = p.nb[p.next[V]];
+        if (nbV < 0) return 2;
+        if (nbN != o.prev[nbV] && nbN != o.next[nbV]) {
+          px = dmul(0.5, dadd(p.x[V], p.x[p.next[V]]));
+          py = dmul(0.5, dadd(p.y[V], p.y[p.next[V]]));
+          found = 1;
+          break;
+        }
+        V = p.next[V];
+      } while (V != root);
+      if (!found) return 2;
+    }
+    if (ppip(side(a, 1 - s), roots[1 - s], px, py))
+      if (rcopy(a, p, root)) return 3;
+  }
+  if (ident[0] && ident[1]) {
+    int target = P.nb[roots[0]], V = roots[1], found = 0;
+    do {
+      if (V == target) found = 1;
+      V = Q.next[V];
+    } while (V != roots[1]);
+    if (found && rcopy(a, P, roots[0])) return 3;
+  }
+  // (4)
+  for (int s = 0; s < 2; ++s) {
+    if (noIsect[s]) continue;
+    Pool& p = side(a, s);
+    unsigned char* split = s == 0 ? a.splitP : a.splitQ;
+    unsigned char* cross = s == 0 ? a.crossP : a.crossQ;
+    int V = ser_non_isect_vertex(a, s, roots[s]);
+    if (V == -3) return 3;
+    if (V < 0) return 2;
+    int status = EX_ENTRY;
+    if (ppip(side(a, 1 - s), roots[1 - s], p.x[V], p.y[V])) tog(&status);
+    int first = 1, I = V;
+    do {
+      if (p.isect[I]) {
+        if (p.label[I] == L_CROSSING) {
+          p.enex[I] = status;
+          tog(&status);
+        }
+        if (p.label[I] == L_BOUNCING && status == EX_EXIT) split[I] = 1;
+        if (p.label[I] == L_DCROSS) {
+          p.enex[I] = status;
+          if (first) {
+            if (status == EX_EXIT) p.label[I] = L_CROSSING;
+            first = 0;
+          } else {
+            if (status == EX_ENTRY) p.label[I] = L_CROSSING;
+            first = 1;
+            tog(&status);
+          }
+        }
+        if (p.label[I] == L_DBOUNCE) {
+          p.enex[I] = status;
+          if (first) {
+            if (status == EX_EXIT) cross[I] = 1;
+            first = 0;
+          } else {
+            if (status == EX_ENTRY) cross[I] = 1;
+            first = 1;
+          }
+          tog(&status);
+        }
+      }
+      I = p.next[I];
+    } while (I != V);
+  }
+  // (5) split pairs
+  {
+    int nP0 = P.n;
+    for (int IP = 0; IP < nP0; ++IP) {
+      if (!a.splitP[IP]) continue;
+      int IQ = P.nb[IP];
+      if (IQ < 0 || !a.splitQ[IQ]) continue;
+      int VP = pnew(P, P.x[IP], P.y[IP]);
+      int VQ = pnew(Q, Q.x[IQ], Q.y[IQ]);
+      if (VP < 0 || VQ < 0) return 3;
+      double sP = area3(P.x[P.prev[IP]], P.y[P.prev[IP]], P.x[IP], P.y[IP], P.x[P.next[IP]],
+                        P.y[P.next[IP]]);
+      double sQ = area3(Q.x[Q.prev[IQ]], Q.y[Q.prev[IQ]], Q.x[IQ], Q.y[IQ], Q.x[Q.next[IQ]],
+                        Q.y[Q.next[IQ]]);
+      if (dmul(sP, sQ) > 0) {
+        P.nb[IP] = VQ; Q.nb[VQ] = IP; P.isect[IP] = 1; Q.isect[VQ] = 1;
+        Q.nb[IQ] = VP; P.nb[VP] = IQ; Q.isect[IQ] = 1; P.isect[VP] = 1;
+      } else {
+        P.nb[VP] = VQ; Q.nb[VQ] = VP; P.isect[VP] = 1; Q.isect[VQ] = 1;
+      }
+      pinsert_after(P, VP, IP);
+      pinsert_after(Q, VQ, IQ);
+      P.enex[IP] = EX_EXIT; P.enex[VP] = EX_ENTRY;
+      Q.enex[IQ] = EX_EXIT; Q.enex[VQ] = EX_ENTRY;
+      P.label[IP] = P.label[VP] = L_CROSSING;
+      Q.label[IQ] = Q.label[VQ] = L_CROSSING;
+    }
+  }
+  // (6)
+  for (int IP = 0; IP < P.n; ++IP) {
+    if (!a.crossP[IP]) continue;
+    int IQ = P.nb[IP];
+    if (IQ >= 0 && a.crossQ[IQ]) {
+      P.label[IP] = L_CROSSING;
+      Q.label[IQ] = L_CROSSING;
+    }
+  }
+  // createResult2
+  {
+    int root = roots[0], It = root;
+    long long guard = 4LL * (P.n + Q.n) + 16;
+    do {
+      if (P.isect[It] && P.label[It] == L_CROSSING) {
+        int r = rnew(a);
+        if (r < 0) return 3;
+        int sI = 0, I = It, sV = 0, V = I;
+        P.isect[I] = 0;
+        do {
+          int status = side(a, sV).enex[V];
+          tog(&status);
+          Pool* pv;
+          do {
+            pv = &side(a, sV);
+            V = (status == EX_EXIT) ? pv->next[V] : pv->prev[V];
+            pv->isect[V] = 0;
+            if (radd(a, r, pv->x[V], pv->y[V])) return 2;
+            if (--guard < 0) return 2;
+          } while (!(pv->enex[V] == status) && !(sV == sI && V == I));
+          if (!(sV == sI && V == I)) {
+            int nbv = side(a, sV).nb[V];
+            if (nbv < 0) return 2;
+            sV = 1 - sV;
+            V = nbv;
+            side(a, sV).isect[V] = 0;
+          }
+        } while (!(sV == sI && V == I));
+      }
+      It = P.next[It];
+    } while (It != root);
+  }
+  return 0;
+}
+
+__device__ void ser_cleanup(SerialArgs& a) {
+  Pool& p = a.R;
+  for (int r = 0; r < *a.nrings; ++r) {
+    auto A = [&](int v) {
+      return fabs(area3(p.x[p.prev[v]], p.y[p.prev[v]], p.x[v], p.y[v], p.x[p.next[v]],
+                        p.y[p.next[v]]));
+    };
+    auto remove = [&](int V) {
+      if (a.rroot[r] == V) {
+        a.rroot[r] = p.next[V];
+        if (p.next[a.rroot[r]] == a.rroot[r]) a.rroot[r] = -1;
+      }
+      p.next[p.prev[V]] = p.next[V];
+      p.prev[p.next[V]] = p.prev[V];
+    };
+    while (a.rroot[r] >= 0 && A(a.rroot[r]) < kEps) remove(a.rroot[r]);
+    if (a.rroot[r] < 0) continue;
+    int start = a.rroot[r], V = start;
+    do {
+      int nx = p.next[V];
+      if (A(V) < kEps) remove(V);
+      V = nx;
+    } while (V != start);
+  }
+}
+
+__global__ void k_serial_backend(SerialArgs a) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  *a.status = 0;
+  *a.nrings = 0;
+  int st = ser_build(a);
+  if (!st) st = ser_label_trace(a);
+  if (!st) ser_cleanup(a);
+  *a.status = st;
+}
+
+// serial output: ring vertex counts and coordinates in ring order
+__global__ void k_serial_emit(SerialArgs a, int* __restrict__ ooff, double* __restrict__ oxy,
+                              long long cap, int* __restrict__ counts) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  long long w = 0;
+  int nr = 0;
+  ooff[0] = 0;
+  for (int r = 0; r < *a.nrings; ++r) {
+    int root = a.rroot[r];
+    if (root < 0) continue;
+    int v = root;
+    do {
+      if (w < cap) {
+        oxy[2 * w] = a.R.x[v];
+        oxy[2 * w + 1] = a.R.y[v];
+      }
+      ++w;
+      v = a.R.next[v];
+    } while (v != root);
+    ooff[++nr] = (int)w;
+  }
+  counts[0] = nr;
+  counts[1] = (int)w;
+}
+
+}  // namespace
+
+// ============================================================== host driver
+static int serial_backend(Pipeline& pl, const Merged& m, OverlayOut& out, int tag) {
+  cudaStream_t st = pl.stream();
+  BufferPool& bp = pl.pool();
+  int extra = 2 * m.K + 8;
+  int capP = m.nB + extra, capQ = m.nQ + extra, capR = m.nB + m.nQ + 2 * extra + 16;
+  auto mk = [&](const char* nm, int cap, Pool& p) {
+    std::string s(nm);
+    p.x = (double*)bp.get(s + "_x", sizeof(double) * cap);
+    p.y = (double*)bp.get(s + "_y", sizeof(double) * cap);
+    p.next = (int*)bp.get(s + "_next", sizeof(int) * cap);
+    p.prev = (int*)bp.get(s + "_prev", sizeof(int) * cap);
+    p.nb = (int*)bp.get(s + "_nb", sizeof(int) * cap);
+    p.label = (int*)bp.get(s + "_label", sizeof(int) * cap);
+    p.enex = (int*)bp.get(s + "_enex", sizeof(int) * cap);
+    p.source = (unsigned char*)bp.get(s + "_src", cap);
+    p.isect = (unsigned char*)bp.get(s + "_isect", cap);
+    p.n = 0;
+    p.cap = cap;
+  };
+  SerialArgs a;
+  mk("serP", capP, a.P);
+  mk("serQ", capQ, a.Q);
+  mk("serR", capR, a.R);
+  a.rcap = m.nB + 16;
+  a.rroot = (int*)bp.get("ser_roots", sizeof(int) * a.rcap);
+  a.nrings = (int*)bp.get("ser_nrings", 256);
+  a.status = (int*)bp.get("ser_status", 256);
+  a.splitP = (unsigned char*)bp.get("ser_splitP", capP);
+  a.splitQ = (unsigned char*)bp.get("ser_splitQ", capQ);
+  a.crossP = (unsigned char*)bp.get("ser_crossP", capP);
+  a.crossQ = (unsigned char*)bp.get("ser_crossQ", capQ);
+  if (bp.failed) return pl.fail(kENoMem, "device allocation failed (serial back end)");
+  cudaMemsetAsync(a.splitP, 0, capP, st);
+  cudaMemsetAsync(a.splitQ, 0, capQ, st);
+  cudaMemsetAsync(a.crossP, 0, capP, st);
+  cudaMemsetAsync(a.crossQ, 0, capQ, st);
+  a.bSize = m.bSize;
+  a.cSize = m.cSize;
+  a.cStart = m.cStart;
+  a.nB = m.nB;
+  a.nQ = m.nQ;
+  a.bP = m.bP;
+  a.cP = m.cP;
+  a.ixB = m.ixB;
+  a.ixC = m.ixC;
+  a.alB = m.alB;
+  a.nbC = m.nbC;
+  a.labB = m.labB;
+  a.labC = m.labC;
+  {
+    ::sbc::KProbe kp_("k_serial_backend", st);
+    k_serial_backend<<<1, 1, 0, st>>>(a);
+  }
+  int hst = 0;
+  cudaMemcpyAsync(&hst, a.status, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  if (hst == 2) return pl.fail(kEUndef, "reference behaviour undefined in the linked-list back end");
+  if (hst == 3) return pl.fail(kEInternal, "serial back end capacity exceeded");
+  std::string t = std::to_string(tag);
+  long long cap = capR;
+  int* ooff = (int*)bp.get("ring_off_" + t, sizeof(int) * (a.rcap + 1));
+  double* oxy = (double*)bp.get("ring_xy_" + t, sizeof(double) * 2 * cap);
+  int* counts = (int*)bp.get("ser_counts", 256);
+  if (bp.failed) return pl.fail(kENoMem, "device allocation failed (rings)");
+  {
+    ::sbc::KProbe kp_("k_serial_emit", st);
+    k_serial_emit<<<1, 1, 0, st>>>(a, ooff, oxy, cap, counts);
+  }
+  int hc[2];
+  cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  out.nrings = hc[0];
+  out.nverts = hc[1];
+  out.d_off = ooff;
+  out.d_xy = oxy;
+  out.slow_path = 1;
+  return kOk;
+}
+
+int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
+  cudaStream_t st = pl.stream();
+  BufferPool& bp = pl.pool();
+  const int ovTag = (int)(&out - &pl.outputs()[0]);
+  if (pl.force_serial_backend) return serial_backend(pl, m, out, ovTag);
+  const int nB = m.nB, nQ = m.nQ;
+  auto* sc = (BkScalars*)bp.get("bk_scalars", sizeof(BkScalars));
+  auto* srcP = (unsigned char*)bp.get("bk_srcP", nB);
+  auto* srcQ = (unsigned char*)bp.get("bk_srcQ", nQ);
+  auto* isP = (unsigned char*)bp.get("bk_isP", nB);
+  auto* isQ = (unsigned char*)bp.get("bk_isQ", nQ);
+  int* labP = (int*)bp.get("bk_labP", sizeof(int) * nB);
+  int* labQ = (int*)bp.get("bk_labQ", sizeof(int) * nQ);
+  int* nbQ = (int*)bp.get("bk_nbQ", sizeof(int) * nQ);
+  int* winP = (int*)bp.get("bk_winP", sizeof(int) * nB);
+  int* seed = (int*)bp.get("bk_seed", 256);
+  if (bp.failed) return pl.fail(kENoMem, "device allocation failed (back end)");
+  BkScalars init;
+  memset(&init, 0, sizeof init);
+  init.firstFree[0] = init.firstFree[1] = 0x7fffffff;
+  cudaMemcpyAsync(sc, &init, sizeof init, cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(srcP, 0, nB, st);
+  cudaMemsetAsync(srcQ, 0, nQ, st);
+  cudaMemsetAsync(winP, 0xff, sizeof(int) * nB, st);
+  {
+    ::sbc::KProbe kp_("k_mark_src", st);
+    k_mark_src<<<grid_for(m.bSize, 256), 256, 0, st>>>(m.bSize, m.bND, srcP);
+  }
+  {
+    ::sbc::KProbe kp_("k_mark_src", st);
+    k_mark_src<<<grid_for(m.cSize, 256), 256, 0, st>>>(m.cSize, m.cND, srcQ);
+  }
+  {
+    ::sbc::KProbe kp_("k_bridge_check", st);
+    k_bridge_check<<<grid_for(m.bSize, 128), 128, 0, st>>>(m.bSize, nB, m.bND, m.ixB, m.bP, 0, sc);
+  }
+  {
+    ::sbc::KProbe kp_("k_bridge_check", st);
+    k_bridge_check<<<grid_for(m.cSize, 128), 128, 0, st>>>(m.cSize, nQ, m.cND, m.ixC, m.cP, m.cStart,
+                                                         sc);
+  }
+  {
+    ::sbc::KProbe kp_("k_init_P", st);
+    k_init_P<<<grid_for(nB, 256), 256, 0, st>>>(nB, srcP, m.alB, m.labB, isP, labP);
+  }
+  {
+    ::sbc::KProbe kp_("k_init_Q", st);
+    k_init_Q<<<grid_for(nQ, 256), 256, 0, st>>>(nQ, nB, srcQ, m.nbC, m.labC, isQ, labQ, nbQ, winP,
+                                              sc);
+  }
+  {
+    ::sbc::KProbe kp_("k_side_stats", st);
+    k_side_stats<<<grid_for(nB, 256), 256, 0, st>>>(nB, isP, labP, 0, 1, sc);
+  }
+  {
+    ::sbc::KProbe kp_("k_side_stats", st);
+    k_side_stats<<<grid_for(nQ, 256), 256, 0, st>>>(nQ, isQ, labQ, 1, 0, sc);
+  }
+  BkScalars h;
+  cudaMemcpyAsync(&h, sc, sizeof h, cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  if (h.anomaly) return serial_backend(pl, m, out, ovTag);
+  const bool noP = h.crossCount[0] == 0, noQ = h.crossCount[1] == 0;
+  if (noP != noQ) return serial_backend(pl, m, out, ovTag);
+  if (h.firstFree[0] == 0x7fffffff || h.firstFree[1] == 0x7fffffff)
+    return serial_backend(pl, m, out, ovTag);
+  if (noP && (h.notOnOn[0] == 0 || h.notOnOn[1] == 0)) return serial_backend(pl, m, out, ovTag);
+
+  // seeds: the first non-intersection vertex of each side against the other side
+  int seeds[2] = {h.firstFree[0], h.firstFree[1]};
+  cudaMemcpyAsync(seed, seeds, sizeof seeds, cudaMemcpyHostToDevice, st);
+  {
+    ::sbc::KProbe kp_("k_pip", st);
+    k_pip<<<grid_for(nQ, 256), 256, 0, st>>>(nQ, m.ixC, m.ixB, seed, 0, sc);
+  }
+  {
+    ::sbc::KProbe kp_("k_pip", st);
+    k_pip<<<grid_for(nB, 256), 256, 0, st>>>(nB, m.ixB, m.ixC, seed + 1, 1, sc);
+  }
+
+  std::string tg = std::to_string(ovTag);
+  if (noP) {
+    // both polygons without crossings: each one inside the other is a ring
+    cudaMemcpyAsync(&h, sc, sizeof h, cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    bool inP = (h.winding[0] % 2) != 0, inQ = (h.winding[1] % 2) != 0;
+    int nr = (inP ? 1 : 0) + (inQ ? 1 : 0);
+    long long nv = (inP ? nB : 0) + (inQ ? nQ : 0);
+    double* xy = (double*)bp.get("bk_rxy", sizeof(double) * 2 * (nv + 1));
+    int* off = (int*)bp.get("bk_roff", sizeof(int) * 4);
+    if (bp.failed) return pl.fail(kENoMem, "device allocation failed (rings)");
+    int hoff[3] = {0, 0, 0};
+    long long w = 0;
+    int r = 0;
+    if (inP) {
+      {
+        ::sbc::KProbe kp_("k_copy_list", st);
+        k_copy_list<<<grid_for(2 * nB, 256), 256, 0, st>>>(nB, m.ixB, xy);
+      }
+      w += nB;
+      hoff[++r] = (int)w;
+    }
+    if (inQ) {
+      {
+        ::sbc::KProbe kp_("k_copy_list", st);
+        k_copy_list<<<grid_for(2 * nQ, 256), 256, 0, st>>>(nQ, m.ixC, xy + 2 * w);
+      }
+      w += nQ;
+      hoff[++r] = (int)w;
+    }
+    cudaMemcpyAsync(off, hoff, sizeof hoff, cudaMemcpyHostToDevice, st);
+    out.d_off = off;
+    out.d_xy = xy;
+    out.nrings = nr;
+    out.nverts = nv;
+  } else {
+    // ---- entry/exit flags
+    int* preP = (int*)bp.get("bk_preP", sizeof(int) * (nB + 1));
+    int* preQ = (int*)bp.get("bk_preQ", sizeof(int) * (nQ + 1));
+    auto* enexP = (unsigned char*)bp.get("bk_enexP", nB);
+    auto* enexQ = (unsigned char*)bp.get("bk_enexQ", nQ);
+    auto* splitP = (unsigned char*)bp.get("bk_splitP", nB);
+    auto* splitQ = (unsigned char*)bp.get("bk_splitQ", nQ);
+    int* listP = (int*)bp.get("bk_listP", sizeof(int) * (h.crossCount[0] + 1));
+    int* listQ = (int*)bp.get("bk_listQ", sizeof(int) * (h.crossCount[1] + 1));
+    int* rankP = (int*)bp.get("bk_rankP", sizeof(int) * nB);
+    int* rankQ = (int*)bp.get("bk_rankQ", sizeof(int) * nQ);
+    void* sscr = bp.get("bk_scan", scan_scratch_bytes((long long)nB + nQ + 4));
+    if (bp.failed) return pl.fail(kENoMem, "device allocation failed (entry/exit)");
+    {
+      ::sbc::KProbe kp_("k_cross_flags", st);
+      k_cross_flags<<<grid_for(nB + 1, 256), 256, 0, st>>>(nB, isP, labP, preP);
+    }
+    {
+      ::sbc::KProbe kp_("k_cross_flags", st);
+      k_cross_flags<<<grid_for(nQ + 1, 256), 256, 0, st>>>(nQ, isQ, labQ, preQ);
+    }
+    exclusive_scan_i32(preP, nB + 1, sscr, st);
+    exclusive_scan_i32(preQ, nQ + 1, sscr, st);
+    {
+      ::sbc::KProbe kp_("k_enex", st);
+      k_enex<<<grid_for(nB, 256), 256, 0, st>>>(nB, isP, labP, preP, 0, sc, enexP, splitP, listP);
+    }
+    {
+      ::sbc::KProbe kp_("k_enex", st);
+      k_enex<<<grid_for(nQ, 256), 256, 0, st>>>(nQ, isQ, labQ, preQ, 1, sc, enexQ, splitQ, listQ);
+    }
+    {
+      ::sbc::KProbe kp_("k_split_check", st);
+      k_split_check<<<grid_for(nB, 256), 256, 0, st>>>(nB, splitP, splitQ, winP, sc);
+    }
+    const int cPn = h.crossCount[0], cQn = h.crossCount[1];
+    if ((cPn & 1) || (cQn & 1)) return serial_backend(pl, m, out, ovTag);
+    {
+      ::sbc::KProbe kp_("k_rank", st);
+      k_rank<<<grid_for(cPn, 256), 256, 0, st>>>(cPn, listP, rankP);
+    }
+    {
+      ::sbc::KProbe kp_("k_rank", st);
+      k_rank<<<grid_for(cQn, 256), 256, 0, st>>>(cQn, listQ, rankQ);
+    }
+    Trace T{nB, nQ, cPn, cQn, listP, listQ, enexP, enexQ, winP, nbQ, rankP, rankQ};
+    const int nE = cPn + cQn;
+    int* jmpA = (int*)bp.get("bk_jmpA", sizeof(int) * (nE + 1));
+    int* jmpB = (int*)bp.get("bk_jmpB", sizeof(int) * (nE + 1));
+    int* mA = (int*)bp.get("bk_mA", sizeof(int) * (nE + 1));
+    int* mB = (int*)bp.get("bk_mB", sizeof(int) * (nE + 1));
+    int* isStart = (int*)bp.get("bk_isStart", sizeof(int) * (cPn + 1));
+    if (bp.failed) return pl.fail(kENoMem, "device allocation failed (rings)");
+    {
+      ::sbc::KProbe kp_("k_tr_init", st);
+      k_tr_init<<<grid_for(nE, 256), 256, 0, st>>>(T, jmpA, mA, sc);
+    }
+    for (int span = 1; span < nE; span <<= 1) {
+      {
+        ::sbc::KProbe kp_("k_tr_jump", st);
+        k_tr_jump<<<grid_for(nE, 256), 256, 0, st>>>(nE, jmpA, mA, jmpB, mB);
+      }
+      std::swap(jmpA, jmpB);
+      std::swap(mA, mB);
+    }
+    {
+      ::sbc::KProbe kp_("k_tr_consistent", st);
+      k_tr_consistent<<<grid_for(nE, 256), 256, 0, st>>>(T, mA, sc);
+    }
+    cudaMemcpyAsync(&h, sc, sizeof h, cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    if (h.anomaly) return serial_backend(pl, m, out, ovTag);
+
+    // ---- ring starts and segment walks
+    {
+      ::sbc::KProbe kp_("k_tr_starts", st);
+      k_tr_starts<<<grid_for(cPn + 1, 256), 256, 0, st>>>(T, mA, isStart);
+    }
+    exclusive_scan_i32(isStart, cPn + 1, sscr, st);
+    int nRings = 0;
+    cudaMemcpyAsync(&nRings, isStart + cPn, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    int* starts = (int*)bp.get("bk_starts", sizeof(int) * (nRings + 1));
+    int* rlen = (int*)bp.get("bk_rlen", sizeof(int) * (nRings + 2));
+    int* rseg = (int*)bp.get("bk_rseg", sizeof(int) * (nRings + 2));
+    if (bp.failed) return pl.fail(kENoMem, "device allocation failed (rings)");
+    {
+      ::sbc::KProbe kp_("k_tr_startlist", st);
+      k_tr_startlist<<<grid_for(cPn, 256), 256, 0, st>>>(cPn, isStart, starts);
+    }
+    {
+      ::sbc::KProbe kp_("k_tr_walk", st);
+      k_tr_walk<0><<<grid_for(nRings, 128), 128, 0, st>>>(T, nRings, starts, rlen, rseg, nullptr,
+                                                        nullptr, nullptr, nullptr, sc);
+    }
+    cudaMemsetAsync(rlen + nRings, 0, sizeof(int), st);
+    cudaMemsetAsync(rseg + nRings, 0, sizeof(int), st);
+    exclusive_scan_i32(rlen, nRings + 1, sscr, st);
+    exclusive_scan_i32(rseg, nRings + 1, sscr, st);
+    int hv[2];
+    cudaMemcpyAsync(&hv[0], rlen + nRings, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&hv[1], rseg + nRings, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&h, sc, sizeof h, cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    if (h.anomaly) return serial_backend(pl, m, out, ovTag);
+    const long long nv = hv[0];
+    const int nseg = hv[1];
+    int* segX = (int*)bp.get("bk_segX", sizeof(int) * (nseg + 1));
+    int* segOut = (int*)bp.get("bk_segOut", sizeof(int) * (nseg + 1));
+    double* rxy = (double*)bp.get("bk_rxy", sizeof(double) * 2 * (nv + 1));
+    if (bp.failed) return pl.fail(kENoMem, "device allocation failed (ring vertices)");
+    {
+      ::sbc::KProbe kp_("k_tr_walk", st);
+      k_tr_walk<1><<<grid_for(nRings, 128), 128, 0, st>>>(T, nRings, starts, nullptr, nullptr, rlen,
+                                                        rseg, segX, segOut, sc);
+    }
+    if (nv > 0) {
+      {
+        ::sbc::KProbe kp_("k_tr_copy", st);
+        k_tr_copy<<<grid_for(nv, 256), 256, 0, st>>>(T, nv, nseg, segX, segOut, m.ixB, m.ixC, rxy);
+      }
+    }
+    out.d_off = rlen;  // exclusive prefix of ring lengths, nRings+1 entries
+    out.d_xy = rxy;
+    out.nrings = nRings;
+    out.nverts = nv;
+  }
+
+  // ---- clean-up and compaction
+  {
+    const int nR = out.nrings;
+    const long long nv = out.nverts;
+    int* ringOf = (int*)bp.get("cl_ringOf", sizeof(int) * (nv + 1));
+    int* ringFlag = (int*)bp.get("cl_flag", sizeof(int) * (nR + 1));
+    int* nxt = (int*)bp.get("cl_next", sizeof(int) * (nv + 1));
+    int* prv = (int*)bp.get("cl_prev", sizeof(int) * (nv + 1));
+    int* keep = (int*)bp.get("cl_keep", sizeof(int) * (nv + 1));
+    int* kpre = (int*)bp.get("cl_kpre", sizeof(int) * (nR + 2));
+    int* rpre = (int*)bp.get("cl_rpre", sizeof(int) * (nR + 2));
+    int* ooff = (int*)bp.get("ring_off_" + tg, sizeof(int) * (nR + 2));
+    double* oxy = (double*)bp.get("ring_xy_" + tg, sizeof(double) * 2 * (nv + 1));
+    void* sscr = bp.get("cl_scan", scan_scratch_bytes(nR + 2));
+    if (bp.failed) return pl.fail(kENoMem, "device allocation failed (clean-up)");
+    cudaMemsetAsync(ringFlag, 0, sizeof(int) * (nR + 1), st);
+    if (nR > 0) {
+      {
+        ::sbc::KProbe kp_("k_ring_of", st);
+        k_ring_of<<<grid_for(nR, 128), 128, 0, st>>>(nR, out.d_off, ringOf);
+      }
+      if (nv > 0) {
+        {
+          ::sbc::KProbe kp_("k_collinear", st);
+          k_collinear<<<grid_for(nv, 256), 256, 0, st>>>(nv, out.d_off, ringOf, out.d_xy, ringFlag);
+        }
+      }
+      {
+        ::sbc::KProbe kp_("k_cleanup_ring", st);
+        k_cleanup_ring<<<grid_for(nR, 128), 128, 0, st>>>(nR, out.d_off, ringFlag, out.d_xy, nxt, prv,
+                                                        keep);
+      }
+    }
+    {
+      ::sbc::KProbe kp_("k_keep_counts", st);
+      k_keep_counts<<<grid_for(nR + 1, 128), 128, 0, st>>>(nR, out.d_off, keep, kpre);
+    }
+    exclusive_scan_i32(kpre, nR + 1, sscr, st);
+    {
+      ::sbc::KProbe kp_("k_ring_nonempty", st);
+      k_ring_nonempty<<<grid_for(nR + 1, 128), 128, 0, st>>>(nR, kpre, rpre);
+    }
+    exclusive_scan_i32(rpre, nR + 1, sscr, st);
+    if (nR > 0) {
+      {
+        ::sbc::KProbe kp_("k_compact_rings", st);
+        k_compact_rings<<<grid_for(nR, 128), 128, 0, st>>>(nR, out.d_off, keep, kpre, rpre, out.d_xy,
+                                                         oxy, ooff);
+      }
+    }
+    {
+      ::sbc::KProbe kp_("k_set_last", st);
+      k_set_last<<<1, 1, 0, st>>>(ooff, rpre, nR, kpre);
+    }
+    int hh[2];
+    cudaMemcpyAsync(&hh[0], rpre + nR, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&hh[1], kpre + nR, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    out.nrings = hh[0];
+    out.nverts = hh[1];
+    out.d_off = ooff;
+    out.d_xy = oxy;
+  }
+  return kOk;
+}
+
+}  // namespace sbc

@@ -1,0 +1,661 @@
+// sbc_front.cu -- polygon setup, elementary intervals, end lists and cover
+// lists of the flattened segment tree (reference rows A1, A4-A7).
+//
+//  A1  gpc_read_multi_polygon            src/clip.cpp:172-311
+//  A4  constructElementaryIntervals...   p_seg_tree/oacc_segment_tree.cpp:4513-4692
+//  A5  constructTreeIntervalArray...     oacc_segment_tree.cpp:4948-4994 (derived on the fly)
+//  A6  insertToLeafLevelEdgeList...      oacc_segment_tree.cpp:1970-2113, merges :1717-1968
+//  A7  insertEdgeParallel                oacc_segment_tree.cpp:2496-2607
+#include <cstdio>
+
+#include "sbc_pipeline.cuh"
+
+namespace sbc {
+
+// ---------------------------------------------------------------- BufferPool
+BufferPool::~BufferPool() { release_all(); }
+
+void* BufferPool::get(const std::string& name, size_t bytes) {
+  bytes = ((bytes + 255) / 256) * 256;
+  if (bytes == 0) bytes = 256;
+  Buf& b = bufs_[name];
+  if (b.n >= bytes) return b.p;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.n = 0;
+  size_t want = bytes + bytes / 8;  // headroom for slightly larger repeat calls
+  if (cudaMalloc(&b.p, want) != cudaSuccess) {
+    cudaGetLastError();
+    if (cudaMalloc(&b.p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      b.p = nullptr;
+      failed = 1;
+      return nullptr;
+    }
+    want = bytes;
+  }
+  b.n = want;
+  return b.p;
+}
+
+size_t BufferPool::bytes_held() const {
+  size_t t = 0;
+  for (auto& kv : bufs_) t += kv.second.n;
+  return t;
+}
+
+void BufferPool::release_all() {
+  for (auto& kv : bufs_)
+    if (kv.second.p) cudaFree(kv.second.p);
+  bufs_.clear();
+}
+
+unsigned Pipeline::read_flags() {
+  unsigned f = 0;
+  cudaMemcpyAsync(&f, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st_);
+  cudaStreamSynchronize(st_);
+  return f;
+}
+
+void Pipeline::clear_flags() { cudaMemsetAsync(d_flags, 0, sizeof(unsigned), st_); }
+
+// ---------------------------------------------------------------- helpers
+__device__ __forceinline__ int overlay_of(const int* pref, int k, int g) {
+  int i = 0;
+  while (i + 1 < k && pref[i + 1] <= g) ++i;
+  return i;
+}
+
+// interval of tree node v (heap layout, leaves at [L, 2L)): start of its
+// leftmost leaf and end of its rightmost leaf; node 0 was never written by the
+// reference and reads as [0,0] (zero-filled heap).
+__device__ __forceinline__ void node_interval(const double* __restrict__ ea, int logL, int v,
+                                              double* s, double* e) {
+  if (v <= 0) {
+    *s = 0.0;
+    *e = 0.0;
+    return;
+  }
+  int d = 31 - __clz(v);
+  int h = logL - d;
+  int L = 1 << logL;
+  int lo = (v << h) - L;
+  int hi = ((v + 1) << h) - 1 - L;
+  *s = ea[lo];
+  *e = ea[hi + 1];
+}
+
+// ---------------------------------------------------------------- A1 setup
+__global__ void k_setup_base(const double* __restrict__ bxy, int nb, double* __restrict__ bP) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > nb) return;
+  int s = (i == nb) ? 0 : i;
+  bP[2 * i] = bxy[2 * s];
+  bP[2 * i + 1] = bxy[2 * s + 1];
+}
+
+__global__ void k_setup_overlays(const double* __restrict__ cxy, const int* __restrict__ cS,
+                                 const int* __restrict__ cc, int k, int total,
+                                 double* __restrict__ cP) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= total) return;
+  int i = overlay_of(cS, k, g);
+  int v = g - cS[i];
+  int c = cc[i + 1] - cc[i];
+  int src = cc[i] + (v < c ? v : 0);
+  cP[2 * g] = cxy[2 * src];
+  cP[2 * g + 1] = cxy[2 * src + 1];
+}
+
+// Edge::getData (edge.h:190-202); ids are offsets into the interleaved arrays
+__global__ void k_setup_edges(const double* __restrict__ bP, const double* __restrict__ cP,
+                              const int* __restrict__ cS, const int* __restrict__ cc, int nb, int k,
+                              int E, int* __restrict__ eid, double* __restrict__ es,
+                              double* __restrict__ ee, unsigned long long* __restrict__ minmax,
+                              unsigned* __restrict__ flags) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long kmin = ~0ull, kmax = 0ull;
+  if (e < E) {
+    int id;
+    double a, b;
+    if (e < nb) {
+      id = 2 * e;
+      a = bP[id];
+      b = bP[id + 2];
+    } else {
+      int g = e - nb;
+      int i = overlay_of(cc, k, g);
+      id = 2 * (cS[i] + (g - cc[i]));
+      a = cP[id];
+      b = cP[id + 2];
+    }
+    eid[e] = id;
+    if (a < b) {
+      es[e] = a;
+      ee[e] = b;
+    } else {
+      ee[e] = a;
+      es[e] = b;
+    }
+    // every vertex is the first endpoint of exactly one edge: min/max over
+    // vertices equals the reference's min/max over non-closing edges
+    if (!isfinite(a)) atomicOr(flags, (unsigned)kFlagUndef);
+    kmin = kmax = dkey(a);
+  }
+  for (int s = 16; s > 0; s >>= 1) {
+    unsigned long long o1 = __shfl_xor_sync(0xffffffffu, kmin, s);
+    unsigned long long o2 = __shfl_xor_sync(0xffffffffu, kmax, s);
+    kmin = o1 < kmin ? o1 : kmin;
+    kmax = o2 > kmax ? o2 : kmax;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&minmax[0], kmin);
+    atomicMax(&minmax[1], kmax);
+  }
+}
+
+static double key_to_double(unsigned long long k) {
+  unsigned long long u = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+  double d;
+  memcpy(&d, &u, sizeof d);
+  return d;
+}
+
+int Pipeline::stage_setup(const double* d_bxy, const double* d_cxy, const int* c_sizes) {
+  hcS.assign(k + 1, 0);
+  hcc.assign(k + 1, 0);
+  for (int i = 0; i < k; ++i) {
+    hcS[i + 1] = hcS[i] + c_sizes[i] + 1;
+    hcc[i + 1] = hcc[i] + c_sizes[i];
+  }
+  clSize = hcc[k];
+  E = nb + clSize;
+  bP = (double*)pool_.get("bP", sizeof(double) * 2 * (nb + 1));
+  cP = (double*)pool_.get("cP", sizeof(double) * 2 * (clSize + k));
+  cS = (int*)pool_.get("cS", sizeof(int) * (k + 1));
+  cc = (int*)pool_.get("cc", sizeof(int) * (k + 1));
+  e_id = (int*)pool_.get("e_id", sizeof(int) * E);
+  e_s = (double*)pool_.get("e_s", sizeof(double) * E);
+  e_e = (double*)pool_.get("e_e", sizeof(double) * E);
+  unsigned long long* mm = (unsigned long long*)pool_.get("minmax", 16);
+  d_flags = (unsigned*)pool_.get("flags", 256);
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (setup)");
+  cudaMemcpyAsync(cS, hcS.data(), sizeof(int) * (k + 1), cudaMemcpyHostToDevice, st_);
+  cudaMemcpyAsync(cc, hcc.data(), sizeof(int) * (k + 1), cudaMemcpyHostToDevice, st_);
+  unsigned long long init[2] = {~0ull, 0ull};
+  cudaMemcpyAsync(mm, init, 16, cudaMemcpyHostToDevice, st_);
+  clear_flags();
+  {
+    ::sbc::KProbe kp_("k_setup_base", st_);
+    k_setup_base<<<grid_for(nb + 1, 256), 256, 0, st_>>>(d_bxy, nb, bP);
+  }
+  {
+    ::sbc::KProbe kp_("k_setup_overlays", st_);
+    k_setup_overlays<<<grid_for(clSize + k, 256), 256, 0, st_>>>(d_cxy, cS, cc, k, clSize + k, cP);
+  }
+  {
+    ::sbc::KProbe kp_("k_setup_edges", st_);
+    k_setup_edges<<<grid_for(E, 256), 256, 0, st_>>>(bP, cP, cS, cc, nb, k, E, e_id, e_s, e_e, mm,
+                                                   d_flags);
+  }
+  unsigned long long hm[2];
+  cudaMemcpyAsync(hm, mm, 16, cudaMemcpyDeviceToHost, st_);
+  cudaStreamSynchronize(st_);
+  if (read_flags() & kFlagUndef) return fail(kEInput, "non-finite vertex coordinate");
+  minI = key_to_double(hm[0]);
+  maxI = key_to_double(hm[1]);
+  return kOk;
+}
+
+// ---------------------------------------------------------------- A4 elementary intervals
+__global__ void k_ele_keys(const double* __restrict__ es, const double* __restrict__ ee, int E,
+                           unsigned long long* __restrict__ keys, unsigned* __restrict__ vals) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= E) return;
+  keys[2 * j] = dkey(es[j]);
+  keys[2 * j + 1] = dkey(ee[j]);
+  vals[2 * j] = 2 * j;
+  vals[2 * j + 1] = 2 * j + 1;
+}
+
+__device__ __forceinline__ double ele_val(const double* es, const double* ee, unsigned idx) {
+  return (idx & 1u) ? ee[idx >> 1] : es[idx >> 1];
+}
+
+// mark vertical edges reached from the first E sorted endpoints (:4568-4576)
+__global__ void k_vl_mark(const unsigned* __restrict__ sidx, const double* __restrict__ es,
+                          const double* __restrict__ ee, int E, int* __restrict__ vl) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= E) return;
+  int i = sidx[j] >> 1;
+  if (es[i] == ee[i]) vl[i] = 1;
+}
+
+__global__ void k_vl_loc(const int* __restrict__ vl, int E, int* __restrict__ vloc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= E) return;
+  if (vl[i] != vl[i + 1]) vloc[vl[i]] = i;
+}
+
+// keep flags (:4603-4636); flag[] has 2E+1 zeroed entries, val[] 2E
+__global__ void k_ele_flags(const unsigned* __restrict__ sidx, const double* __restrict__ es,
+                            const double* __restrict__ ee, const int* __restrict__ vl,
+                            const int* __restrict__ vloc, int E, int* __restrict__ flag,
+                            double* __restrict__ val) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long n2 = 2LL * E;
+  if (i >= n2 - 1) return;
+  double v0 = ele_val(es, ee, sidx[i]);
+  double v1 = ele_val(es, ee, sidx[i + 1]);
+  int intvi = sidx[i] >> 1;
+  int comid = vl[i / 2];
+  if (v0 != v1) {
+    val[i] = v0;
+    flag[i] = 1;
+  } else if (es[intvi] == ee[intvi]) {
+    bool keep = comid == 0;
+    if (!keep) {
+      int lookup = vloc[comid - 1];
+      keep = es[lookup] != es[intvi] && ee[lookup] != es[intvi];
+    }
+    if (keep) {
+      val[i] = es[intvi];
+      flag[i] = 1;
+    }
+  }
+  if (i == n2 - 2) {
+    // the last slot repeats the second-to-last sorted value (:4630-4635)
+    if (v0 != v1) {
+      val[n2 - 1] = v0;
+      flag[n2 - 1] = 1;
+    }
+  }
+}
+
+__global__ void k_ele_compact(const int* __restrict__ flag, const double* __restrict__ val,
+                              long long n2, double* __restrict__ ea) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n2) return;
+  if (flag[i] != flag[i + 1]) ea[flag[i]] = val[i];
+}
+
+__global__ void k_ele_pad(double* __restrict__ ea, int count, int round) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x + count;
+  if (i >= round) return;
+  ea[i] = ea[count - 1];
+}
+
+static int npow2_host(int n) {
+  int p = 1;
+  while (p < n) p <<= 1;
+  return p;
+}
+
+int Pipeline::stage_elementary() {
+  long long n2 = 2LL * E;
+  auto* keys = (unsigned long long*)pool_.get("ele_keys", sizeof(unsigned long long) * n2);
+  auto* keys2 = (unsigned long long*)pool_.get("ele_keys2", sizeof(unsigned long long) * n2);
+  auto* sidx = (unsigned*)pool_.get("ele_sidx", sizeof(unsigned) * n2);
+  auto* sidx2 = (unsigned*)pool_.get("ele_sidx2", sizeof(unsigned) * n2);
+  void* rscr = pool_.get("radix_scr", radix_scratch_bytes(n2));
+  int* vl = (int*)pool_.get("ele_vl", sizeof(int) * (E + 1));
+  int* vloc = (int*)pool_.get("ele_vloc", sizeof(int) * (E + 1));
+  int* flag = (int*)pool_.get("ele_flag", sizeof(int) * (n2 + 1));
+  double* val = (double*)pool_.get("ele_val", sizeof(double) * n2);
+  void* sscr = pool_.get("scan_scr", scan_scratch_bytes(n2 + 1));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (elementary)");
+  {
+    ::sbc::KProbe kp_("k_ele_keys", st_);
+    k_ele_keys<<<grid_for(E, 256), 256, 0, st_>>>(e_s, e_e, E, keys, sidx);
+  }
+  radix_sort_u64(keys, sidx, keys2, sidx2, n2, rscr, st_);
+  cudaMemsetAsync(vl, 0, sizeof(int) * (E + 1), st_);
+  {
+    ::sbc::KProbe kp_("k_vl_mark", st_);
+    k_vl_mark<<<grid_for(E, 256), 256, 0, st_>>>(sidx, e_s, e_e, E, vl);
+  }
+  exclusive_scan_i32(vl, E + 1, sscr, st_);
+  {
+    ::sbc::KProbe kp_("k_vl_loc", st_);
+    k_vl_loc<<<grid_for(E, 256), 256, 0, st_>>>(vl, E, vloc);
+  }
+  cudaMemsetAsync(flag, 0, sizeof(int) * (n2 + 1), st_);
+  {
+    ::sbc::KProbe kp_("k_ele_flags", st_);
+    k_ele_flags<<<grid_for(n2, 256), 256, 0, st_>>>(sidx, e_s, e_e, vl, vloc, E, flag, val);
+  }
+  exclusive_scan_i32(flag, n2 + 1, sscr, st_);
+  int count = 0;
+  cudaMemcpyAsync(&count, flag + n2, sizeof(int), cudaMemcpyDeviceToHost, st_);
+  cudaStreamSynchronize(st_);
+  if (count < 1) return fail(kEUndef, "no elementary interval (all endpoints equal)");
+  int round = npow2_host(count) + 1;
+  epc = round;
+  numLeaves = round - 1;
+  ts = 2 * numLeaves;
+  logL = 0;
+  while ((1 << logL) < numLeaves) ++logL;
+  ea = (double*)pool_.get("ea", sizeof(double) * (round + 1));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (ea)");
+  {
+    ::sbc::KProbe kp_("k_ele_compact", st_);
+    k_ele_compact<<<grid_for(n2, 256), 256, 0, st_>>>(flag, val, n2, ea);
+  }
+  if (round > count) {
+    {
+      ::sbc::KProbe kp_("k_ele_pad", st_);
+      k_ele_pad<<<grid_for(round - count, 256), 256, 0, st_>>>(ea, count, round);
+    }
+  }
+  stat_edges = E;
+  stat_epc = epc;
+  stat_ts = ts;
+  return kOk;
+}
+
+// ---------------------------------------------------------------- A6 end lists
+// Border sequence S(m) = boaders[sortedIndex[m]] (:1970-2008, :2016-2020):
+// boaders[i-1] = ea[i] for i in [1, epc); the never-written slot epc-1 reads
+// 0.0 and its digit key 0 sorts after the z leading zero keys.
+struct Borders {
+  const double* ea;
+  int epc, z;
+  __device__ __forceinline__ double S(int m) const {
+    if (m < 0 || m >= epc) return __longlong_as_double(0x7ff8000000000000ll);  // past the arrays
+    if (m < z) return ea[m + 1];
+    if (m == z) return 0.0;
+    return ea[m];
+  }
+  // boundary index j = sortedIndex[m]
+  __device__ __forceinline__ int J(int m) const { return m < z ? m : (m == z ? epc - 1 : m - 1); }
+};
+
+// findBoarder, oacc_segment_tree.cpp:420-460
+__device__ __forceinline__ int find_border(const Borders& B, double q) {
+  int l = 0, h = B.epc;
+  while (l < h) {
+    int m = l + (h - l) / 2;
+    double sm = B.S(m);
+    if (sm == q) {
+      if (B.S(m - 1) != q) {
+        h = m;
+        l = h;
+      } else {
+        h = m - 1;
+      }
+    } else if (sm < q) {
+      l = m + 1;
+    } else {
+      h = m - 1;
+    }
+  }
+  if (!(B.S(h) == q)) return -1;
+  return h;
+}
+
+// integer border keys must be non-decreasing and non-negative for the
+// shortcut ordering above (they are, by construction, unless rounding pushes
+// a key to 1e11)
+__global__ void k_border_check(const double* __restrict__ ea, int epc, double scale, double absMin,
+                               int shift, int* __restrict__ zcount, unsigned* __restrict__ flags) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x + 1;  // boundary i in [1, epc)
+  if (i >= epc) return;
+  auto key = [&](int t) -> long long {
+    double v = shift ? dmul(scale, dadd(ea[t], absMin)) : dmul(scale, ea[t]);
+    return (long long)v;
+  };
+  long long ki = key(i);
+  if (ki < 0 || ki >= 100000000000LL) atomicOr(flags, (unsigned)kFlagUndef);
+  if (i + 1 < epc && key(i + 1) < ki) atomicOr(flags, (unsigned)kFlagUndef);
+  if (ki == 0) atomicAdd(zcount, 1);
+}
+
+__global__ void k_find_leaves(const double* __restrict__ es, const double* __restrict__ ee, int E,
+                              Borders B, int logL, int* __restrict__ aft, int* __restrict__ bef,
+                              const int* __restrict__ typeOfEdgeStart, int k, int numLeaves,
+                              int* __restrict__ cnt) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  const int L = 1 << logL;
+  const double* ea = B.ea;
+  int a = -1, b = -1;
+  int en = find_border(B, ee[e]);
+  int st = find_border(B, es[e]);
+  if (en >= 0) {
+    int j = B.J(en);  // right[j]
+    int node = 0;
+    if (j <= B.epc - 2) {
+      int i = j + 1;
+      node = L + i;
+      if (i != 1 && i + 1 < B.epc && ea[i] == ea[i + 1]) node = L + i + 1;
+    }
+    // node 0 ([0,0]) and node 2L (past the tree) are dropped
+    if (node >= L && node < 2 * L && ea[node - L] != ea[node - L + 1]) a = node;
+  }
+  if (st >= 0) {
+    int j = B.J(st);  // left[j]
+    int node = 0;
+    if (j <= B.epc - 2) node = L + j;
+    if (node >= L && node < 2 * L && ea[node - L] != ea[node - L + 1]) b = node;
+  }
+  aft[e] = a;
+  bef[e] = b;
+  int cls = 0;
+  while (cls < k && typeOfEdgeStart[cls + 1] <= e) ++cls;  // 0 base, t overlay t
+  if (a >= 0) atomicAdd(&cnt[(size_t)cls * numLeaves + (a - L)], 1);
+  if (b >= 0) atomicAdd(&cnt[(size_t)cls * numLeaves + (b - L)], 1);
+}
+
+__global__ void k_leaf_scatter(const int* __restrict__ aft, const int* __restrict__ bef, int E,
+                               int logL, const int* __restrict__ typeOfEdgeStart, int k,
+                               int numLeaves, const int* __restrict__ off, int* __restrict__ fill,
+                               int* __restrict__ le_edge, int* __restrict__ le_leaf) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  const int L = 1 << logL;
+  int cls = 0;
+  while (cls < k && typeOfEdgeStart[cls + 1] <= e) ++cls;
+  int a = aft[e], b = bef[e];
+  if (a >= 0) {
+    size_t c = (size_t)cls * numLeaves + (a - L);
+    int p = off[c] + atomicAdd(&fill[c], 1);
+    le_edge[p] = e;
+    le_leaf[p] = a - L;
+  }
+  if (b >= 0) {
+    size_t c = (size_t)cls * numLeaves + (b - L);
+    int p = off[c] + atomicAdd(&fill[c], 1);
+    le_edge[p] = e;
+    le_leaf[p] = b - L;
+  }
+}
+
+static int digit_count_host(double val) {
+  int d = 1;
+  int iv = (int)trunc(val);
+  while (iv / 10 > 0) {
+    iv /= 10;
+    d++;
+  }
+  return d;
+}
+
+int Pipeline::stage_endlists() {
+  double absMin = fabs(minI);
+  double dv = maxI + absMin;
+  if (!(dv < 2147483647.0)) return fail(kEUndef, "coordinate range too large for realToInt");
+  int d = digit_count_host(dv);
+  double scale = pow(10.0, 11 - d);
+  // edge-index start of each polygon class: base 0, overlay t at nb + cc[t-1]
+  std::vector<int> hstart(k + 2);
+  hstart[0] = 0;
+  for (int t = 0; t <= k; ++t) hstart[t + 1] = nb + hcc[t];
+  int* tstart = (int*)pool_.get("type_start", sizeof(int) * (k + 2));
+  int* zc = (int*)pool_.get("zcount", 256);
+  aft = (int*)pool_.get("aft", sizeof(int) * E);
+  bef = (int*)pool_.get("bef", sizeof(int) * E);
+  size_t ncls = (size_t)(k + 1) * numLeaves;
+  int* cnt = (int*)pool_.get("le_cnt", sizeof(int) * (ncls + 1));
+  int* fill = (int*)pool_.get("le_fill", sizeof(int) * (ncls + 1));
+  void* sscr = pool_.get("scan_scr2", scan_scratch_bytes(ncls + 1));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (end lists)");
+  cudaMemcpyAsync(tstart, hstart.data(), sizeof(int) * (k + 2), cudaMemcpyHostToDevice, st_);
+  cudaMemsetAsync(zc, 0, sizeof(int), st_);
+  clear_flags();
+  {
+    ::sbc::KProbe kp_("k_border_check", st_);
+    k_border_check<<<grid_for(epc, 256), 256, 0, st_>>>(ea, epc, scale, absMin, minI < 0 ? 1 : 0, zc,
+                                                     d_flags);
+  }
+  int z = 0;
+  cudaMemcpyAsync(&z, zc, sizeof(int), cudaMemcpyDeviceToHost, st_);
+  if (read_flags() & kFlagUndef) return fail(kEUndef, "border keys not monotone (realToInt)");
+  z_garbage = z;
+  // ea[0] < 0 decides the shift; ea[0] equals minI
+  Borders B{ea, epc, z};
+  cudaMemsetAsync(cnt, 0, sizeof(int) * (ncls + 1), st_);
+  {
+    ::sbc::KProbe kp_("k_find_leaves", st_);
+    k_find_leaves<<<grid_for(E, 256), 256, 0, st_>>>(e_s, e_e, E, B, logL, aft, bef, tstart, k,
+                                                   numLeaves, cnt);
+  }
+  exclusive_scan_i32(cnt, ncls + 1, sscr, st_);
+  int total = 0;
+  cudaMemcpyAsync(&total, cnt + ncls, sizeof(int), cudaMemcpyDeviceToHost, st_);
+  cudaStreamSynchronize(st_);
+  nLeafEnt = total;
+  le_off = cnt;
+  le_edge = (int*)pool_.get("le_edge", sizeof(int) * (total + 1));
+  le_leaf = (int*)pool_.get("le_leaf", sizeof(int) * (total + 1));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (leaf entries)");
+  cudaMemsetAsync(fill, 0, sizeof(int) * (ncls + 1), st_);
+  {
+    ::sbc::KProbe kp_("k_leaf_scatter", st_);
+    k_leaf_scatter<<<grid_for(E, 256), 256, 0, st_>>>(aft, bef, E, logL, tstart, k, numLeaves, cnt,
+                                                    fill, le_edge, le_leaf);
+  }
+  stat_leaf = total;
+  return kOk;
+}
+
+// ---------------------------------------------------------------- A7 cover lists
+// Edge::contains / Edge::intersects (edge.h:160-188) on the node interval
+__device__ __forceinline__ bool contains_node(double s, double x, double ns, double ne) {
+  return s <= ns && x >= ne;
+}
+__device__ __forceinline__ bool intersects_node(double s, double x, double cs, double ce) {
+  return (s <= cs && x >= ce) || (cs <= s && ce >= x) || (s <= cs && x >= cs) ||
+         (ce <= x && ce >= s);
+}
+
+// insertEdgeParallel as an explicit-stack pre-order descent (left child first)
+template <bool EMIT>
+__global__ void k_cover(const double* __restrict__ es, const double* __restrict__ ee, int E,
+                        const double* __restrict__ ea, int logL, int ts, int* __restrict__ count,
+                        const long long* __restrict__ off, unsigned* __restrict__ onode,
+                        unsigned* __restrict__ oedge, unsigned* __restrict__ flags) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  double s = es[e], x = ee[e];
+  int stack[96];
+  int sp = 0;
+  stack[sp++] = 1;
+  int n = 0;
+  long long base = EMIT ? off[e] : 0;
+  while (sp > 0) {
+    int v = stack[--sp];
+    double ns, ne;
+    node_interval(ea, logL, v, &ns, &ne);
+    if (contains_node(s, x, ns, ne)) {
+      if (EMIT) {
+        onode[base + n] = (unsigned)v;
+        oedge[base + n] = (unsigned)e;
+      }
+      ++n;
+      continue;
+    }
+    int c = 2 * v;
+    if (c + 1 < ts) {
+      double cs, ce;
+      node_interval(ea, logL, c + 1, &cs, &ce);
+      if (intersects_node(s, x, cs, ce)) {
+        if (sp < 96) stack[sp++] = c + 1;
+        else atomicOr(flags, (unsigned)kFlagOverflow);
+      }
+    }
+    if (c < ts) {
+      double cs, ce;
+      node_interval(ea, logL, c, &cs, &ce);
+      if (intersects_node(s, x, cs, ce)) {
+        if (sp < 96) stack[sp++] = c;
+        else atomicOr(flags, (unsigned)kFlagOverflow);
+      }
+    }
+  }
+  if (!EMIT) count[e] = n;
+}
+
+__global__ void k_i32_to_i64(const int* __restrict__ a, long long n, long long* __restrict__ b) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = a[i];
+}
+
+__global__ void k_node_ranges(const unsigned* __restrict__ node, long long n,
+                              int* __restrict__ nstart, int* __restrict__ nend) {
+  long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  unsigned v = node[p];
+  if (p == 0 || node[p - 1] != v) nstart[v] = (int)p;
+  if (p == n - 1 || node[p + 1] != v) nend[v] = (int)(p + 1);
+}
+
+int Pipeline::stage_cover() {
+  int* cnt = (int*)pool_.get("cov_cnt", sizeof(int) * (E + 1));
+  long long* off = (long long*)pool_.get("cov_off", sizeof(long long) * (E + 1));
+  void* sscr = pool_.get("scan_scr3", scan_scratch_bytes(E + 1));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (cover)");
+  clear_flags();
+  {
+    ::sbc::KProbe kp_("k_cover", st_);
+    k_cover<false><<<grid_for(E, 128), 128, 0, st_>>>(e_s, e_e, E, ea, logL, ts, cnt, nullptr,
+                                                    nullptr, nullptr, d_flags);
+  }
+  cudaMemsetAsync(cnt + E, 0, sizeof(int), st_);
+  {
+    ::sbc::KProbe kp_("k_i32_to_i64", st_);
+    k_i32_to_i64<<<grid_for(E + 1, 256), 256, 0, st_>>>(cnt, E + 1, off);
+  }
+  exclusive_scan_i64(off, E + 1, sscr, st_);
+  long long total = 0;
+  cudaMemcpyAsync(&total, off + E, sizeof(long long), cudaMemcpyDeviceToHost, st_);
+  cudaStreamSynchronize(st_);
+  if (read_flags() & kFlagOverflow) return fail(kEInternal, "cover descent stack overflow");
+  if (total >= (1LL << 28)) return fail(kEInput, "more than 2^28 cover-list entries");
+  nCover = total;
+  cov_node = (unsigned*)pool_.get("cov_node", sizeof(unsigned) * (total + 1));
+  cov_edge = (unsigned*)pool_.get("cov_edge", sizeof(unsigned) * (total + 1));
+  auto* tn = (unsigned*)pool_.get("cov_node2", sizeof(unsigned) * (total + 1));
+  auto* te = (unsigned*)pool_.get("cov_edge2", sizeof(unsigned) * (total + 1));
+  void* rscr = pool_.get("radix_scr_cov", radix_scratch_bytes(total + 1));
+  node_start = (int*)pool_.get("node_start", sizeof(int) * ts);
+  node_end = (int*)pool_.get("node_end", sizeof(int) * ts);
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (cover entries)");
+  {
+    ::sbc::KProbe kp_("k_cover", st_);
+    k_cover<true><<<grid_for(E, 128), 128, 0, st_>>>(e_s, e_e, E, ea, logL, ts, nullptr, off,
+                                                   cov_node, cov_edge, d_flags);
+  }
+  int bits = 1;
+  while ((1LL << bits) < ts) ++bits;
+  radix_sort_u32(cov_node, cov_edge, tn, te, total, bits, rscr, st_);
+  if (total > 0) {
+    {
+      ::sbc::KProbe kp_("k_node_ranges", st_);
+      k_node_ranges<<<grid_for(total, 256), 256, 0, st_>>>(cov_node, total, node_start, node_end);
+    }
+  }
+  stat_cover = total;
+  return kOk;
+}
+
+}  // namespace sbc

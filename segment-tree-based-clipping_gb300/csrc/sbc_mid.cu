@@ -1,0 +1,814 @@
+// sbc_mid.cu -- per-overlay stages between the tree and the back end
+// (reference rows A8-A14):
+//
+//  A8   saveIntersectionsIdsMulticore      p_seg_tree/oacc_segment_tree.cpp:6108-6244
+//  A9   radixsort + removeDuplicatesAtEdge src/clip.cpp:368-493, :1731-1742
+//  A10  countEdgeIntersections + scans     src/clip.cpp:522-601, :1805-1861
+//  A11  saveIntersectionsParallel          oacc_segment_tree.cpp:7247-7341
+//  A12  sortIntersectionsAtEdgesParallel   oacc_segment_tree.cpp:7436-7473
+//  A13  copyIntersectionsParallel          oacc_segment_tree.cpp:7508-7664
+//  A14  calculateInitLabelParallel         oacc_segment_tree.cpp:7826-7988
+//
+// Emission order.  The reference emits candidates node by node, and inside a
+// node by cover entry, then cover x cover before cover x end, then partner
+// order.  Each hit here carries the key (cover position P, phase, partner id)
+// which orders hits exactly like that; duplicates keep the smallest key, and
+// hits of one base edge stay in key order, which is the reference's
+// first-occurrence order after its stable radix sort by base id.
+#include <cstdio>
+
+#include "sbc_pipeline.cuh"
+
+namespace sbc {
+
+namespace {
+
+__device__ __forceinline__ int lower_bound_u32(const unsigned* a, int lo, int hi, unsigned x) {
+  while (lo < hi) {
+    int m = (lo + hi) >> 1;
+    if (a[m] < x) lo = m + 1;
+    else hi = m;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int class_of(const int* tstart, int k, int e) {
+  int c = 0;
+  while (c < k && tstart[c + 1] <= e) ++c;
+  return c;
+}
+
+__device__ __forceinline__ void leaf_range(int v, int logL, int* lo, int* hi) {
+  int d = 31 - __clz(v);
+  int h = logL - d;
+  int L = 1 << logL;
+  *lo = (v << h) - L;
+  *hi = ((v + 1) << h) - 1 - L;
+}
+
+// ---------------------------------------------------------------- A8 work
+__global__ void k_cand_work(const unsigned* __restrict__ cov_node,
+                            const unsigned* __restrict__ cov_edge, long long nCover,
+                            const int* __restrict__ node_start, const int* __restrict__ node_end,
+                            const int* __restrict__ tstart, int k, int cType, int logL,
+                            int numLeaves, const int* __restrict__ le_off,
+                            long long* __restrict__ work, int* __restrict__ blk_s,
+                            int* __restrict__ wcc) {
+  long long P = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (P >= nCover) return;
+  int v = (int)cov_node[P];
+  int e = (int)cov_edge[P];
+  int t = class_of(tstart, k, e);
+  long long w = 0;
+  int bs = 0, nc = 0;
+  int lo, hi;
+  leaf_range(v, logL, &lo, &hi);
+  if (t == 0) {
+    int a = node_start[v], b = node_end[v];
+    bs = lower_bound_u32(cov_edge, a, b, (unsigned)tstart[cType]);
+    int be = lower_bound_u32(cov_edge, a, b, (unsigned)tstart[cType + 1]);
+    nc = be - bs;
+    size_t c = (size_t)cType * numLeaves;
+    w = nc + (le_off[c + hi + 1] - le_off[c + lo]);
+  } else if (t == cType) {
+    w = le_off[hi + 1] - le_off[lo];
+  }
+  work[P] = w;
+  blk_s[P] = bs;
+  wcc[P] = nc;
+}
+
+// LSMF bounding-box filter, oacc_segment_tree.cpp:5282-5316
+__device__ __forceinline__ bool lsmf(double p1x, double p1y, double p2x, double p2y, double q1x,
+                                     double q1y, double q2x, double q2y) {
+  double minPX = p1x, minPY = p1y, maxPX = p2x, maxPY = p2y;
+  double minQX = q1x, minQY = q1y, maxQX = q2x, maxQY = q2y;
+  if (minPX > p2x) { minPX = p2x; maxPX = p1x; }
+  if (minPY > p2y) { minPY = p2y; maxPY = p1y; }
+  if (minQX > q2x) { minQX = q2x; maxQX = q1x; }
+  if (minQY > q2y) { minQY = q2y; maxQY = q1y; }
+  if (minPX > maxQX || maxPX < minQX) return false;
+  if (minPY > maxQY || maxPY < minQY) return false;
+  return true;
+}
+
+constexpr int kCandThreads = 256;
+constexpr int kCandItems = 8;
+constexpr int kCandChunk = kCandThreads * kCandItems;
+constexpr int kCandSm = 1024;
+
+// load-balanced candidate tests: unit u -> (cover entry P, partner j)
+__global__ void __launch_bounds__(kCandThreads)
+k_cand_test(const long long* __restrict__ wscan, long long nCover, long long W,
+            const unsigned* __restrict__ cov_node, const unsigned* __restrict__ cov_edge,
+            const int* __restrict__ blk_s, const int* __restrict__ wcc,
+            const int* __restrict__ tstart, int k, int cType, int logL, int numLeaves,
+            const int* __restrict__ le_off, const int* __restrict__ le_edge,
+            const int* __restrict__ le_leaf, const int* __restrict__ aft,
+            const int* __restrict__ bef, const int* __restrict__ e_id,
+            const double* __restrict__ bP, const double* __restrict__ cP,
+            unsigned long long* __restrict__ counters, long long cap, int* __restrict__ rb,
+            int* __restrict__ rc, int* __restrict__ rt, unsigned long long* __restrict__ rkey) {
+  __shared__ long long sw[kCandSm + 1];
+  __shared__ long long sP[2];
+  const long long c0 = (long long)blockIdx.x * kCandChunk;
+  const long long c1 = min(c0 + (long long)kCandChunk, W);
+  if (threadIdx.x < 2) {
+    long long target = threadIdx.x == 0 ? c0 : c1 - 1;
+    long long lo = 0, hi = nCover;  // last P with wscan[P] <= target
+    while (hi - lo > 1) {
+      long long m = (lo + hi) >> 1;
+      if (wscan[m] <= target) lo = m;
+      else hi = m;
+    }
+    sP[threadIdx.x] = lo;
+  }
+  __syncthreads();
+  const long long Plo = sP[0], Phi = sP[1];
+  const bool in_smem = (Phi - Plo + 1) <= kCandSm;
+  if (in_smem)
+    for (long long i = threadIdx.x; i <= Phi - Plo + 1; i += blockDim.x) sw[i] = wscan[Plo + i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const int L = 1 << logL;
+  unsigned tested = 0;
+  for (int it = 0; it < kCandItems; ++it) {
+    long long u = c0 + (long long)it * kCandThreads + threadIdx.x;
+    bool hit = false;
+    int bId = 0, cId = 0, ty = 0;
+    unsigned long long key = 0;
+    if (u < c1) {
+      long long P;
+      if (in_smem) {
+        int lo = 0, hi = (int)(Phi - Plo + 1);
+        while (hi - lo > 1) {
+          int m = (lo + hi) >> 1;
+          if (sw[m] <= u) lo = m;
+          else hi = m;
+        }
+        P = Plo + lo;
+      } else {
+        long long lo = Plo, hi = Phi + 1;
+        while (hi - lo > 1) {
+          long long m = (lo + hi) >> 1;
+          if (wscan[m] <= u) lo = m;
+          else hi = m;
+        }
+        P = lo;
+      }
+      long long j = u - (in_smem ? sw[P - Plo] : wscan[P]);
+      int self = (int)cov_edge[P];
+      int v = (int)cov_node[P];
+      int tself = class_of(tstart, k, self);
+      int partner = -1, phase = 0;
+      if (j < wcc[P]) {
+        partner = (int)cov_edge[blk_s[P] + j];
+      } else {
+        phase = 1;
+        int lo, hi;
+        leaf_range(v, logL, &lo, &hi);
+        int cls = tself == 0 ? cType : 0;
+        long long idx = le_off[(size_t)cls * numLeaves + lo] + (j - wcc[P]);
+        int e2 = le_edge[idx];
+        int leaf = le_leaf[idx] + L;
+        int other = (aft[e2] == leaf) ? bef[e2] : aft[e2];
+        // the edge's other leaf entry inside this subtree comes first: a set
+        // holds the edge once
+        bool dup = other >= 0 && other >= lo + L && other <= hi + L && other < leaf;
+        if (!dup) partner = e2;
+      }
+      if (partner >= 0) {
+        int b = tself == 0 ? self : partner;
+        int c = tself == 0 ? partner : self;
+        bId = e_id[b];
+        cId = e_id[c];
+        const double* pb = bP + bId;
+        const double* pc = cP + cId;
+        double p1x = pb[0], p1y = pb[1], p2x = pb[2], p2y = pb[3];
+        double q1x = pc[0], q1y = pc[1], q2x = pc[2], q2y = pc[3];
+        if (lsmf(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y)) {
+          ++tested;
+          double al, be;
+          ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &be);
+          if (ty) {
+            hit = true;
+            key = ((unsigned long long)P << 36) | ((unsigned long long)phase << 35) |
+                  (unsigned long long)(e_id[partner] >> 1);
+          }
+        }
+      }
+    }
+    unsigned m = __ballot_sync(0xffffffffu, hit);
+    if (m) {
+      int leader = __ffs(m) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(&counters[0], (unsigned long long)__popc(m));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (hit) {
+        long long idx = (long long)base + __popc(m & lt);
+        if (idx < cap) {
+          rb[idx] = bId;
+          rc[idx] = cId;
+          rt[idx] = ty;
+          rkey[idx] = key;
+        }
+      }
+    }
+  }
+  for (int s = 16; s > 0; s >>= 1) tested += __shfl_xor_sync(0xffffffffu, tested, s);
+  if (lane == 0 && tested) atomicAdd(&counters[1], (unsigned long long)tested);
+}
+
+// ---------------------------------------------------------------- A9 dedup
+__global__ void k_iota_keys(const int* __restrict__ rb, long long n, unsigned* __restrict__ keys,
+                            unsigned* __restrict__ vals) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  keys[i] = (unsigned)rb[i];
+  vals[i] = (unsigned)i;
+}
+
+__global__ void k_seg_heads(const unsigned* __restrict__ keys, long long n, int* __restrict__ h) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  h[i] = (i < n && (i == 0 || keys[i] != keys[i - 1])) ? 1 : 0;
+}
+
+__global__ void k_seg_starts(const int* __restrict__ hs, long long n, int* __restrict__ start) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  if (i == n) {
+    start[hs[n]] = (int)n;
+    return;
+  }
+  if (hs[i + 1] != hs[i]) start[hs[i]] = (int)i;
+}
+
+// per base edge: order hits by emission key, keep the first hit of each
+// overlay edge (removeDuplicatesAtEdge); ord[] receives raw indices in key
+// order, keep[] the flags
+__global__ void k_dedup(const int* __restrict__ start, int nseg, const unsigned* __restrict__ svals,
+                        const unsigned long long* __restrict__ rkey, const int* __restrict__ rc,
+                        unsigned* __restrict__ ord, int* __restrict__ keep) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  int a = start[s], b = start[s + 1];
+  int m = b - a;
+  // insertion sort of raw indices by key, in place in ord[a..b)
+  for (int i = 0; i < m; ++i) {
+    unsigned r = svals[a + i];
+    unsigned long long kr = rkey[r];
+    int j = i;
+    while (j > 0 && rkey[ord[a + j - 1]] > kr) {
+      ord[a + j] = ord[a + j - 1];
+      --j;
+    }
+    ord[a + j] = r;
+  }
+  for (int i = 0; i < m; ++i) {
+    int ci = rc[ord[a + i]];
+    int k2 = 1;
+    for (int j = 0; j < i; ++j)
+      if (rc[ord[a + j]] == ci) {
+        k2 = 0;
+        break;
+      }
+    keep[a + i] = k2;
+  }
+}
+
+__global__ void k_dedup_write(const unsigned* __restrict__ ord, const int* __restrict__ pos,
+                              long long n, const int* __restrict__ rb, const int* __restrict__ rc,
+                              const int* __restrict__ rt, int* __restrict__ ub, int* __restrict__ uc,
+                              int* __restrict__ ut) {
+  long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  if (pos[p + 1] == pos[p]) return;
+  int j = pos[p];
+  unsigned r = ord[p];
+  ub[j] = rb[r];
+  uc[j] = rc[r];
+  ut[j] = rt[r];
+}
+
+// ---------------------------------------------------------------- A10 counts
+// isNonDegenerateCase, src/clip.cpp:508-517
+__device__ __forceinline__ bool nondeg_b(int t) { return t == 1 || t == 3 || t == 5 || t == 7; }
+__device__ __forceinline__ bool nondeg_c(int t) { return t == 1 || t == 2 || t == 6; }
+
+__global__ void k_counts(const int* __restrict__ ub, const int* __restrict__ uc,
+                         const int* __restrict__ ut, int K, int cStart, int* __restrict__ bAll,
+                         int* __restrict__ bND, int* __restrict__ cAll, int* __restrict__ cND) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= K) return;
+  int t = ut[j];
+  int eb = ub[j] >> 1;
+  int ec = (uc[j] >> 1) - cStart;
+  atomicAdd(&bAll[eb], 1);
+  if (nondeg_b(t)) atomicAdd(&bND[eb], 1);
+  atomicAdd(&cAll[ec], 1);
+  if (nondeg_c(t)) atomicAdd(&cND[ec], 1);
+}
+
+// ---------------------------------------------------------------- A11 records
+__global__ void k_records(const int* __restrict__ ub, const int* __restrict__ uc,
+                          int* __restrict__ ut, int K, const double* __restrict__ bP,
+                          const double* __restrict__ cP, double* __restrict__ isxy,
+                          int* __restrict__ aB, int* __restrict__ aC) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= K) return;
+  const double* b = bP + ub[j];
+  const double* c = cP + uc[j];
+  double al = 0.0, be = 0.0;
+  int ty = seg_isect(b[0], b[1], b[2], b[3], c[0], c[1], c[2], c[3], &al, &be);
+  double x = 0.0, y = 0.0;
+  if (ty == 1) {
+    // (1-alpha)*b1 + alpha*b2, mulScalar/add (:5349-5363)
+    double oma = dsub(1.0, al);
+    x = dadd(dmul(oma, b[0]), dmul(al, b[2]));
+    y = dadd(dmul(oma, b[1]), dmul(al, b[3]));
+  } else if (ty == 3 || ty == 4 || ty == 5 || ty == 7 || ty == 8) {
+    x = c[0];
+    y = c[1];
+  } else if (ty == 2 || ty == 6) {
+    x = b[0];
+    y = b[1];
+  }
+  isxy[2 * j] = x;
+  isxy[2 * j + 1] = y;
+  if (ty) {
+    ut[j] = ty;
+    aB[j] = alpha_to_int(al);
+    aC[j] = alpha_to_int(be);
+  } else {
+    aB[j] = 0;
+    aC[j] = 0;
+  }
+}
+
+// ---------------------------------------------------------------- A12 alpha sort
+// stable sort of positions [s,e) of one edge by alpha mod 1e9 (9 decimal
+// LSD passes), only for edges with more than one non-degenerate intersection
+__global__ void k_alpha_sort(int n, const int* __restrict__ allPS, const int* __restrict__ ndPS,
+                             const int* __restrict__ alpha, const int* __restrict__ order,
+                             int* __restrict__ sorted, unsigned* __restrict__ flags) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  int s = allPS[e], t = allPS[e + 1];
+  for (int i = s; i < t; ++i) sorted[i] = i;
+  if (ndPS[e + 1] - ndPS[e] <= 1) return;
+  for (int i = s; i < t; ++i) {
+    int a = alpha[order ? order[i] : i];
+    if (a < 0) {
+      atomicOr(flags, (unsigned)kFlagUndef);
+      return;
+    }
+  }
+  for (int i = s + 1; i < t; ++i) {
+    int p = sorted[i];
+    int kp = alpha[order ? order[p] : p] % 1000000000;
+    int j = i;
+    while (j > s) {
+      int q = sorted[j - 1];
+      int kq = alpha[order ? order[q] : q] % 1000000000;
+      if (kq <= kp) break;
+      sorted[j] = q;
+      --j;
+    }
+    sorted[j] = p;
+  }
+}
+
+// ---------------------------------------------------------------- A13 merged arrays
+__global__ void k_copy_src(const double* __restrict__ P, int n, int off, const int* __restrict__ ndPS,
+                           double* __restrict__ ix, int* __restrict__ al, int* __restrict__ nbr) {
+  int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= n) return;
+  int p = id + ndPS[id];
+  ix[2 * p] = P[2 * (off + id)];
+  ix[2 * p + 1] = P[2 * (off + id) + 1];
+  al[p] = -100;
+  nbr[p] = -100;
+}
+
+// one edge run of the reference's copy loop (:7556-7656).  entry(pos) maps a
+// position of the alpha-sorted order to a unique-record index.
+template <bool BASE>
+__global__ void k_copy_runs(int n, int K, const int* __restrict__ allPS,
+                            const int* __restrict__ ndPS, const int* __restrict__ sorted,
+                            const int* __restrict__ order, const int* __restrict__ ids, int idShift,
+                            const int* __restrict__ ut, const double* __restrict__ isxy,
+                            const int* __restrict__ avals, double* __restrict__ ix,
+                            int* __restrict__ al, int* __restrict__ NI) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  int s = allPS[e];
+  if (allPS[e + 1] == s) return;
+  auto entry = [&](int pos) { return order ? order[sorted[pos]] : sorted[pos]; };
+  int bid = s;
+  int lid = entry(bid);
+  int t = ut[lid];
+  bool deg = BASE ? (t == 2 || t == 4 || t == 6 || t == 8)
+                  : (t == 3 || t == 4 || t == 5 || t == 7 || t == 8);
+  if (deg) {
+    int slot = e + ndPS[e];
+    al[slot] = avals[lid];
+    NI[lid] = slot;
+    if (bid < K - 1) lid = entry(++bid);
+  }
+  int edge = (ids[lid] >> 1) - idShift;
+  // a run holding only its degenerate entry hands the loop to the next
+  // edge's entries; the reference rewrites those slots when it reaches that
+  // edge, so nothing is written here
+  if (edge != e) return;
+  int ns = ndPS[e], ne = ndPS[e + 1];
+  for (int q = 0; q < ne - ns; ++q) {
+    int slot = ns + e + 1 + q;
+    ix[2 * slot] = isxy[2 * lid];
+    ix[2 * slot + 1] = isxy[2 * lid + 1];
+    al[slot] = avals[lid];
+    NI[lid] = slot;
+    if (bid < K - 1) lid = entry(++bid);
+  }
+}
+
+__global__ void k_winner(const int* __restrict__ tgt, int K, int* __restrict__ win) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K) return;
+  atomicMax(&win[tgt[i]], i);
+}
+
+__global__ void k_nbr_apply(const int* __restrict__ win, int n, const int* __restrict__ otherNI,
+                            int* __restrict__ nbr) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  int w = win[p];
+  if (w >= 0) nbr[p] = otherNI[w] + 1;
+}
+
+// ---------------------------------------------------------------- A14 labels
+__global__ void k_labels(int nB, int nQ, const double* __restrict__ ixB,
+                         const double* __restrict__ ixC, const int* __restrict__ alB,
+                         const int* __restrict__ nbB, int* __restrict__ labB,
+                         int* __restrict__ cWin, unsigned* __restrict__ flags) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nB) return;
+  labB[i] = 0;
+  if (alB[i] == -100) return;
+  double cx = ixB[2 * i], cy = ixB[2 * i + 1];
+  int tm = (i - 1 == -1) ? nB - 1 : i - 1;  // getCircularId
+  double pmx = ixB[2 * tm], pmy = ixB[2 * tm + 1];
+  int pMN = alB[tm] != -100 ? nbB[tm] - 1 : -100;
+  int tp = (i + 1 == nB) ? 0 : i + 1;
+  double ppx = ixB[2 * tp], ppy = ixB[2 * tp + 1];
+  int pPN = alB[tp] != -100 ? nbB[tp] - 1 : -100;
+  int nId = nbB[i] - 1;
+  int qt[2];
+  for (int side = 0; side < 2; ++side) {
+    int q = side == 0 ? nId - 1 : nId + 1;
+    if (q == nQ) q = 0;
+    else if (q == -1) q = nQ - 1;
+    if (q < 0 || q >= nQ) {
+      atomicOr(flags, (unsigned)kFlagUndef);
+      return;
+    }
+    double qx = ixC[2 * q], qy = ixC[2 * q + 1];
+    int r;
+    if (pMN != -100 && pMN == q) r = 2;
+    else if (pPN != -100 && pPN == q) r = 3;
+    else {
+      double s1 = area3(qx, qy, pmx, pmy, cx, cy);
+      double s2 = area3(qx, qy, cx, cy, ppx, ppy);
+      double s3 = area3(pmx, pmy, cx, cy, ppx, ppy);
+      if (s3 > 0) r = (s1 > 0 && s2 > 0) ? 0 : 1;
+      else r = (s1 < 0 && s2 < 0) ? 1 : 0;
+    }
+    qt[side] = r;
+  }
+  int qm = qt[0], qp = qt[1], lab;
+  if ((qm == 0 && qp == 1) || (qm == 1 && qp == 0)) lab = 1;
+  else if ((qm == 0 && qp == 0) || (qm == 1 && qp == 1)) lab = 2;
+  else if ((qp == 3 && qm == 1) || (qm == 3 && qp == 1)) lab = 3;
+  else if ((qp == 3 && qm == 0) || (qm == 3 && qp == 0)) lab = 4;
+  else if ((qp == 3 && qm == 2) || (qm == 3 && qp == 2)) lab = 5;
+  else if ((qm == 2 && qp == 1) || (qp == 2 && qm == 1)) lab = 6;
+  else if ((qm == 2 && qp == 0) || (qp == 2 && qm == 0)) lab = 7;
+  else lab = -102;
+  labB[i] = lab;
+  if (nId < 0 || nId >= nQ) {
+    atomicOr(flags, (unsigned)kFlagUndef);
+    return;
+  }
+  atomicMax(&cWin[nId], i);
+}
+
+__global__ void k_labels_c(int nQ, const int* __restrict__ cWin, const int* __restrict__ labB,
+                           int* __restrict__ labC) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nQ) return;
+  int w = cWin[q];
+  labC[q] = w >= 0 ? labB[w] : 0;
+}
+
+}  // namespace
+
+// ============================================================== stage_overlay
+int Pipeline::stage_overlay(int cType, OverlayOut& out) {
+  cudaStream_t st = st_;
+  const int cListId = cType - 1;
+  const int bSize = nb;
+  const int cStart = hcS[cListId];
+  const int cSize = hcS[cType] - hcS[cListId] - 1;
+  std::vector<int> hstart(k + 2);
+  hstart[0] = 0;
+  for (int t = 0; t <= k; ++t) hstart[t + 1] = nb + hcc[t];
+  int* tstart = (int*)pool_.get("type_start", sizeof(int) * (k + 2));
+  cudaMemcpyAsync(tstart, hstart.data(), sizeof(int) * (k + 2), cudaMemcpyHostToDevice, st);
+
+  // ---- A8 candidate work per cover entry
+  long long* work = (long long*)pool_.get("cand_work", sizeof(long long) * (nCover + 1));
+  int* blk_s = (int*)pool_.get("cand_blk", sizeof(int) * (nCover + 1));
+  int* wcc = (int*)pool_.get("cand_wcc", sizeof(int) * (nCover + 1));
+  void* sscr = pool_.get("scan_scr4", scan_scratch_bytes(nCover + 1));
+  auto* counters = (unsigned long long*)pool_.get("cand_counters", 64);
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (candidates)");
+  if (nCover > 0) {
+    {
+      ::sbc::KProbe kp_("k_cand_work", st);
+      k_cand_work<<<grid_for(nCover, 256), 256, 0, st>>>(cov_node, cov_edge, nCover, node_start,
+                                                       node_end, tstart, k, cType, logL,
+                                                       numLeaves, le_off, work, blk_s, wcc);
+    }
+  }
+  cudaMemsetAsync(work + nCover, 0, sizeof(long long), st);
+  exclusive_scan_i64(work, nCover + 1, sscr, st);
+  long long W = 0;
+  cudaMemcpyAsync(&W, work + nCover, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+
+  long long cap = 4LL * E + (1 << 20);
+  long long nraw = 0, ntested = 0;
+  int *rb = nullptr, *rc = nullptr, *rt = nullptr;
+  unsigned long long* rkey = nullptr;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    rb = (int*)pool_.get("raw_b", sizeof(int) * cap);
+    rc = (int*)pool_.get("raw_c", sizeof(int) * cap);
+    rt = (int*)pool_.get("raw_t", sizeof(int) * cap);
+    rkey = (unsigned long long*)pool_.get("raw_key", sizeof(unsigned long long) * cap);
+    if (pool_.failed) return fail(kENoMem, "device allocation failed (raw candidates)");
+    cudaMemsetAsync(counters, 0, 16, st);
+    if (W > 0) {
+      {
+        ::sbc::KProbe kp_("k_cand_test", st);
+        k_cand_test<<<grid_for(W, kCandChunk), kCandThreads, 0, st>>>(
+          work, nCover, W, cov_node, cov_edge, blk_s, wcc, tstart, k, cType, logL, numLeaves,
+          le_off, le_edge, le_leaf, aft, bef, e_id, bP, cP, counters, cap, rb, rc, rt, rkey);
+      }
+    }
+    unsigned long long hc[2];
+    cudaMemcpyAsync(hc, counters, 16, cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    nraw = (long long)hc[0];
+    ntested = (long long)hc[1];
+    if (nraw <= cap) break;
+    cap = nraw + (1 << 20);
+  }
+  if (nraw >= (1LL << 31)) return fail(kEInput, "too many candidate hits");
+  out.raw_hits = nraw;
+  out.tests = ntested;
+
+  // ---- A9 dedup: stable sort by base id, per-edge key order, first per overlay edge
+  long long R = nraw;
+  auto* sk = (unsigned*)pool_.get("dd_keys", sizeof(unsigned) * (R + 1));
+  auto* sv = (unsigned*)pool_.get("dd_vals", sizeof(unsigned) * (R + 1));
+  auto* sk2 = (unsigned*)pool_.get("dd_keys2", sizeof(unsigned) * (R + 1));
+  auto* sv2 = (unsigned*)pool_.get("dd_vals2", sizeof(unsigned) * (R + 1));
+  int* heads = (int*)pool_.get("dd_heads", sizeof(int) * (R + 2));
+  int* segstart = (int*)pool_.get("dd_segstart", sizeof(int) * (R + 2));
+  auto* ord = (unsigned*)pool_.get("dd_ord", sizeof(unsigned) * (R + 1));
+  int* keep = (int*)pool_.get("dd_keep", sizeof(int) * (R + 2));
+  void* rscr = pool_.get("radix_scr_dd", radix_scratch_bytes(R + 1));
+  void* sscr2 = pool_.get("scan_scr5", scan_scratch_bytes(R + 2));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (dedup)");
+  int K = 0;
+  int nseg = 0;
+  if (R > 0) {
+    {
+      ::sbc::KProbe kp_("k_iota_keys", st);
+      k_iota_keys<<<grid_for(R, 256), 256, 0, st>>>(rb, R, sk, sv);
+    }
+    int bits = 1;
+    while ((1LL << bits) < 2LL * bSize) ++bits;
+    radix_sort_u32(sk, sv, sk2, sv2, R, bits, rscr, st);
+    {
+      ::sbc::KProbe kp_("k_seg_heads", st);
+      k_seg_heads<<<grid_for(R + 1, 256), 256, 0, st>>>(sk, R, heads);
+    }
+    exclusive_scan_i32(heads, R + 1, sscr2, st);
+    cudaMemcpyAsync(&nseg, heads + R, sizeof(int), cudaMemcpyDeviceToHost, st);
+    {
+      ::sbc::KProbe kp_("k_seg_starts", st);
+      k_seg_starts<<<grid_for(R + 1, 256), 256, 0, st>>>(heads, R, segstart);
+    }
+    cudaStreamSynchronize(st);
+    {
+      ::sbc::KProbe kp_("k_dedup", st);
+      k_dedup<<<grid_for(nseg, 128), 128, 0, st>>>(segstart, nseg, sv, rkey, rc, ord, keep);
+    }
+    cudaMemsetAsync(keep + R, 0, sizeof(int), st);
+    exclusive_scan_i32(keep, R + 1, sscr2, st);
+    cudaMemcpyAsync(&K, keep + R, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+  }
+  out.unique = K;
+  int* ub = (int*)pool_.get("u_b", sizeof(int) * (K + 1));
+  int* uc = (int*)pool_.get("u_c", sizeof(int) * (K + 1));
+  int* ut = (int*)pool_.get("u_t", sizeof(int) * (K + 1));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (unique)");
+  if (K > 0) {
+    {
+      ::sbc::KProbe kp_("k_dedup_write", st);
+      k_dedup_write<<<grid_for(R, 256), 256, 0, st>>>(ord, keep, R, rb, rc, rt, ub, uc, ut);
+    }
+  }
+
+  // ---- A10 counts (radixsort of overlay ids by value mod 10^d must be complete)
+  {
+    long long m = 1;
+    long long v = 2LL * clSize;
+    while (v > 0) {
+      v /= 10;
+      m *= 10;
+    }
+    long long maxCid = 2LL * (hcS[k] - 2);
+    if (maxCid >= m) return fail(kEUndef, "overlay ids exceed the reference's radix digit count");
+  }
+  int* bAll = (int*)pool_.get("bAll", sizeof(int) * (bSize + 2));
+  int* bND = (int*)pool_.get("bND", sizeof(int) * (bSize + 2));
+  int* cAll = (int*)pool_.get("cAll", sizeof(int) * (cSize + 2));
+  int* cND = (int*)pool_.get("cND", sizeof(int) * (cSize + 2));
+  auto* csk = (unsigned*)pool_.get("cs_keys", sizeof(unsigned) * (K + 1));
+  auto* csv = (unsigned*)pool_.get("cs_vals", sizeof(unsigned) * (K + 1));
+  auto* csk2 = (unsigned*)pool_.get("cs_keys2", sizeof(unsigned) * (K + 1));
+  auto* csv2 = (unsigned*)pool_.get("cs_vals2", sizeof(unsigned) * (K + 1));
+  void* rscr2 = pool_.get("radix_scr_cs", radix_scratch_bytes(K + 1));
+  void* sscr3 = pool_.get("scan_scr6", scan_scratch_bytes(bSize + cSize + 4));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (counts)");
+  cudaMemsetAsync(bAll, 0, sizeof(int) * (bSize + 1), st);
+  cudaMemsetAsync(bND, 0, sizeof(int) * (bSize + 1), st);
+  cudaMemsetAsync(cAll, 0, sizeof(int) * (cSize + 1), st);
+  cudaMemsetAsync(cND, 0, sizeof(int) * (cSize + 1), st);
+  if (K > 0) {
+    {
+      ::sbc::KProbe kp_("k_counts", st);
+      k_counts<<<grid_for(K, 256), 256, 0, st>>>(ub, uc, ut, K, cStart, bAll, bND, cAll, cND);
+    }
+    {
+      ::sbc::KProbe kp_("k_iota_keys", st);
+      k_iota_keys<<<grid_for(K, 256), 256, 0, st>>>(uc, K, csk, csv);
+    }
+    int bits = 1;
+    while ((1LL << bits) < 2LL * (clSize + k)) ++bits;
+    radix_sort_u32(csk, csv, csk2, csv2, K, bits, rscr2, st);
+  }
+  exclusive_scan_i32(bAll, bSize + 1, sscr3, st);
+  exclusive_scan_i32(bND, bSize + 1, sscr3, st);
+  exclusive_scan_i32(cAll, cSize + 1, sscr3, st);
+  exclusive_scan_i32(cND, cSize + 1, sscr3, st);
+  int hb = 0, hc = 0;
+  cudaMemcpyAsync(&hb, bND + bSize, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(&hc, cND + cSize, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  const int nB = bSize + hb, nQ = cSize + hc;
+  out.slots_b = nB;
+  out.slots_c = nQ;
+  const int* csorted = (const int*)csv;
+
+  // ---- A11 records
+  double* isxy = (double*)pool_.get("isxy", sizeof(double) * 2 * (K + 1));
+  int* aB = (int*)pool_.get("aB", sizeof(int) * (K + 1));
+  int* aC = (int*)pool_.get("aC", sizeof(int) * (K + 1));
+  int* sB = (int*)pool_.get("sB", sizeof(int) * (K + 1));
+  int* sC = (int*)pool_.get("sC", sizeof(int) * (K + 1));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (records)");
+  clear_flags();
+  if (K > 0) {
+    {
+      ::sbc::KProbe kp_("k_records", st);
+      k_records<<<grid_for(K, 256), 256, 0, st>>>(ub, uc, ut, K, bP, cP, isxy, aB, aC);
+    }
+    // ---- A12 per-edge alpha sorts
+    {
+      ::sbc::KProbe kp_("k_alpha_sort", st);
+      k_alpha_sort<<<grid_for(bSize, 128), 128, 0, st>>>(bSize, bAll, bND, aB, nullptr, sB, d_flags);
+    }
+    {
+      ::sbc::KProbe kp_("k_alpha_sort", st);
+      k_alpha_sort<<<grid_for(cSize, 128), 128, 0, st>>>(cSize, cAll, cND, aC, csorted, sC, d_flags);
+    }
+  }
+
+  // ---- A13 merged arrays
+  double* ixB = (double*)pool_.get("ixB", sizeof(double) * 2 * nB);
+  double* ixC = (double*)pool_.get("ixC", sizeof(double) * 2 * nQ);
+  int* alB = (int*)pool_.get("alB", sizeof(int) * nB);
+  int* alC = (int*)pool_.get("alC", sizeof(int) * nQ);
+  int* nbB = (int*)pool_.get("nbB", sizeof(int) * nB);
+  int* nbC = (int*)pool_.get("nbC", sizeof(int) * nQ);
+  int* bNI = (int*)pool_.get("bNI", sizeof(int) * (K + 1));
+  int* cNI = (int*)pool_.get("cNI", sizeof(int) * (K + 1));
+  int* winB = (int*)pool_.get("winB", sizeof(int) * nB);
+  int* winC = (int*)pool_.get("winC", sizeof(int) * nQ);
+  int* labB = (int*)pool_.get("labB", sizeof(int) * nB);
+  int* labC = (int*)pool_.get("labC", sizeof(int) * nQ);
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (merged)");
+  // the reference's arrays come from a zero-filled heap: slots no loop writes read 0
+  cudaMemsetAsync(ixB, 0, sizeof(double) * 2 * nB, st);
+  cudaMemsetAsync(ixC, 0, sizeof(double) * 2 * nQ, st);
+  cudaMemsetAsync(alB, 0, sizeof(int) * nB, st);
+  cudaMemsetAsync(alC, 0, sizeof(int) * nQ, st);
+  cudaMemsetAsync(nbB, 0, sizeof(int) * nB, st);
+  cudaMemsetAsync(nbC, 0, sizeof(int) * nQ, st);
+  {
+    ::sbc::KProbe kp_("k_copy_src", st);
+    k_copy_src<<<grid_for(bSize, 256), 256, 0, st>>>(bP, bSize, 0, bND, ixB, alB, nbB);
+  }
+  {
+    ::sbc::KProbe kp_("k_copy_src", st);
+    k_copy_src<<<grid_for(cSize, 256), 256, 0, st>>>(cP, cSize, cStart, cND, ixC, alC, nbC);
+  }
+  cudaMemsetAsync(bNI, 0, sizeof(int) * (K + 1), st);
+  cudaMemsetAsync(cNI, 0, sizeof(int) * (K + 1), st);
+  if (K > 0) {
+    {
+      ::sbc::KProbe kp_("k_copy_runs", st);
+      k_copy_runs<true><<<grid_for(bSize, 128), 128, 0, st>>>(bSize, K, bAll, bND, sB, nullptr, ub, 0,
+                                                           ut, isxy, aB, ixB, alB, bNI);
+    }
+    {
+      ::sbc::KProbe kp_("k_copy_runs", st);
+      k_copy_runs<false><<<grid_for(cSize, 128), 128, 0, st>>>(cSize, K, cAll, cND, sC, csorted, uc,
+                                                            cStart, ut, isxy, aC, ixC, alC, cNI);
+    }
+    cudaMemsetAsync(winB, 0xff, sizeof(int) * nB, st);
+    cudaMemsetAsync(winC, 0xff, sizeof(int) * nQ, st);
+    {
+      ::sbc::KProbe kp_("k_winner", st);
+      k_winner<<<grid_for(K, 256), 256, 0, st>>>(bNI, K, winB);
+    }
+    {
+      ::sbc::KProbe kp_("k_winner", st);
+      k_winner<<<grid_for(K, 256), 256, 0, st>>>(cNI, K, winC);
+    }
+    {
+      ::sbc::KProbe kp_("k_nbr_apply", st);
+      k_nbr_apply<<<grid_for(nB, 256), 256, 0, st>>>(winB, nB, cNI, nbB);
+    }
+    {
+      ::sbc::KProbe kp_("k_nbr_apply", st);
+      k_nbr_apply<<<grid_for(nQ, 256), 256, 0, st>>>(winC, nQ, bNI, nbC);
+    }
+  }
+
+  // ---- A14 initial labels
+  cudaMemsetAsync(winC, 0xff, sizeof(int) * nQ, st);
+  {
+    ::sbc::KProbe kp_("k_labels", st);
+    k_labels<<<grid_for(nB, 256), 256, 0, st>>>(nB, nQ, ixB, ixC, alB, nbB, labB, winC, d_flags);
+  }
+  {
+    ::sbc::KProbe kp_("k_labels_c", st);
+    k_labels_c<<<grid_for(nQ, 256), 256, 0, st>>>(nQ, winC, labB, labC);
+  }
+  if (read_flags() & kFlagUndef)
+    return fail(kEUndef, "reference behaviour undefined (negative alpha key or bad neighbour)");
+
+  // ---- A15-A19 back end
+  Merged m;
+  m.nB = nB;
+  m.nQ = nQ;
+  m.K = K;
+  m.bSize = bSize;
+  m.cSize = cSize;
+  m.cStart = cStart;
+  m.ixB = ixB;
+  m.ixC = ixC;
+  m.alB = alB;
+  m.nbB = nbB;
+  m.nbC = nbC;
+  m.labB = labB;
+  m.labC = labC;
+  m.bND = bND;
+  m.cND = cND;
+  m.bP = bP;
+  m.cP = cP;
+  // keep the intermediate arrays reachable for diagnostics
+  dbg_ub = ub; dbg_uc = uc; dbg_ut = ut; dbg_K = K;
+  dbg_isxy = isxy; dbg_aB = aB; dbg_aC = aC;
+  dbg_ixB = ixB; dbg_ixC = ixC; dbg_alB = alB; dbg_alC = alC; dbg_nbB = nbB; dbg_nbC = nbC;
+  dbg_labB = labB; dbg_labC = labC; dbg_nB = nB; dbg_nQ = nQ;
+  return run_backend(*this, m, out);
+}
+
+}  // namespace sbc

@@ -1,0 +1,142 @@
+// sbc_pipeline.cuh -- state of one clipping run (base polygon + k overlays)
+// and the stage entry points implemented in sbc_front.cu / sbc_mid.cu /
+// sbc_back.cu.  One Pipeline per sbc_ctx; every buffer is grow-only so
+// repeated calls of the same size allocate nothing.
+#pragma once
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "sbc_internal.cuh"
+
+namespace sbc {
+
+// grow-only device buffers keyed by name
+class BufferPool {
+ public:
+  ~BufferPool();
+  // returns a device pointer of at least `bytes` (256-byte aligned)
+  void* get(const std::string& name, size_t bytes);
+  size_t bytes_held() const;
+  void release_all();
+  int failed = 0;
+
+ private:
+  struct Buf {
+    void* p = nullptr;
+    size_t n = 0;
+  };
+  std::map<std::string, Buf> bufs_;
+};
+
+// per-overlay results kept on the device
+struct OverlayOut {
+  int nrings = 0;
+  long long nverts = 0;
+  int* d_off = nullptr;     // nrings+1 vertex offsets
+  double* d_xy = nullptr;   // 2*nverts
+  // diagnostics
+  long long raw_hits = 0, tests = 0, unique = 0, slots_b = 0, slots_c = 0;
+  int slow_path = 0;
+};
+
+struct Timing {
+  // milliseconds per phase (CUDA events), accumulated over one run
+  float ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+};
+
+class Pipeline {
+ public:
+  Pipeline(int device, cudaStream_t st) : dev_(device), st_(st) {}
+  // polygons already on the device (no closing vertex), sizes on the host
+  int run(const double* d_bxy, int nb, const double* d_cxy, const int* c_sizes, int k);
+  const std::vector<OverlayOut>& outputs() const { return outs_; }
+  const char* error() const { return err_.c_str(); }
+  BufferPool& pool() { return pool_; }
+  cudaStream_t stream() const { return st_; }
+  void set_stream(cudaStream_t s) { st_ = s; }
+  bool timing = false;
+  Timing times;
+  // tree statistics of the last run
+  long long stat_edges = 0, stat_epc = 0, stat_ts = 0, stat_cover = 0, stat_leaf = 0;
+  // force the serial emulation of the back end (test hook)
+  int force_serial_backend = 0;
+
+  // ---- shared state (public for the stage kernels' launchers) ----
+  int nb = 0, k = 0, clSize = 0, E = 0;
+  std::vector<int> hcS, hcc;           // prefix of (c_i + 1) and of c_i
+  double* bP = nullptr;                // (nb+1)*2
+  double* cP = nullptr;                // (clSize+k)*2
+  int* cS = nullptr;                   // device copy of hcS (k+1)
+  int* cc = nullptr;                   // device copy of hcc (k+1)
+  int* e_id = nullptr;
+  double* e_s = nullptr;
+  double* e_e = nullptr;
+  double minI = 0, maxI = 0;
+  // tree
+  double* ea = nullptr;
+  int epc = 0, numLeaves = 0, ts = 0, logL = 0;
+  int z_garbage = 0;                   // position of the zero border entry
+  int* aft = nullptr;                  // leaf node from the edge's end (or -1)
+  int* bef = nullptr;                  // leaf node from the edge's start (or -1)
+  int* le_off = nullptr;               // (k+1)*numLeaves+1 offsets by (class, leaf)
+  int* le_edge = nullptr;              // edge index per leaf entry
+  int* le_leaf = nullptr;              // leaf (relative) per leaf entry
+  long long nLeafEnt = 0;
+  unsigned* cov_node = nullptr;        // cover entries sorted by (node, edge)
+  unsigned* cov_edge = nullptr;
+  long long nCover = 0;
+  int* node_start = nullptr;           // first cover entry of node (valid if node has entries)
+  int* node_end = nullptr;
+  unsigned* d_flags = nullptr;         // device error flags (DevFlag bits)
+  // intermediate arrays of the last overlay processed (device, diagnostics)
+  int *dbg_ub = nullptr, *dbg_uc = nullptr, *dbg_ut = nullptr;
+  int dbg_K = 0;
+  double* dbg_isxy = nullptr;
+  int *dbg_aB = nullptr, *dbg_aC = nullptr;
+  double *dbg_ixB = nullptr, *dbg_ixC = nullptr;
+  int *dbg_alB = nullptr, *dbg_alC = nullptr, *dbg_nbB = nullptr, *dbg_nbC = nullptr;
+  int *dbg_labB = nullptr, *dbg_labC = nullptr;
+  int dbg_nB = 0, dbg_nQ = 0;
+
+  // stage entry points (return Status)
+  int stage_setup(const double* d_bxy, const double* d_cxy, const int* c_sizes);
+  int stage_elementary();
+  int stage_endlists();
+  int stage_cover();
+  int stage_overlay(int cType, OverlayOut& out);
+
+  int fail(int code, const std::string& msg) {
+    if (err_.empty()) err_ = msg;
+    return code;
+  }
+  unsigned read_flags();
+  void clear_flags();
+
+ private:
+  int dev_;
+  cudaStream_t st_;
+  BufferPool pool_;
+  std::vector<OverlayOut> outs_;
+  std::string err_;
+};
+
+// back end entry (sbc_back.cu): from the merged arrays to rings
+struct Merged {
+  int nB = 0, nQ = 0, K = 0, bSize = 0, cSize = 0, cStart = 0;
+  const double* ixB;   // 2*nB
+  const double* ixC;   // 2*nQ
+  const int* alB;      // nB
+  const int* nbB;      // nB
+  const int* nbC;      // nQ
+  const int* labB;     // nB
+  const int* labC;     // nQ
+  const int* bND;      // bSize+1 exclusive prefix of non-degenerate counts
+  const int* cND;      // cSize+1
+  const double* bP;    // base with closing vertex
+  const double* cP;    // overlays with closing vertices
+};
+int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out);
+
+}  // namespace sbc

@@ -1,0 +1,358 @@
+// sbc_prims.cu -- device-wide exclusive scan and stable LSD radix sort.
+//
+// These replace the reference's Thrust calls (p_seg_tree/thrust_func.cu:19-42:
+// stable_sort_by_key on double / int / long keys, exclusive_scan on int /
+// long).  HBM-bound: each radix pass reads and writes every (key, value) once
+// plus a per-tile digit histogram; passes whose digit is constant over all
+// keys are skipped (one OR/AND reduction decides).
+#include "sbc_internal.cuh"
+
+#include <cstdio>
+
+namespace sbc {
+
+unsigned long long g_launches = 0;
+
+// ============================================================== launch probes
+namespace {
+struct ProbeRec {
+  const char* name;
+  cudaEvent_t a, b;
+};
+bool g_prof_on = false;
+std::vector<ProbeRec> g_recs;
+std::vector<cudaEvent_t> g_event_pool;
+size_t g_event_next = 0;
+
+cudaEvent_t next_event() {
+  if (g_event_next == g_event_pool.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    g_event_pool.push_back(e);
+  }
+  return g_event_pool[g_event_next++];
+}
+}  // namespace
+
+KProbe::KProbe(const char* name, cudaStream_t st) : name_(name), st_(st), slot_(-1) {
+  ++g_launches;
+  if (!g_prof_on) return;
+  ProbeRec r{name, next_event(), next_event()};
+  cudaEventRecord(r.a, st);
+  slot_ = (int)g_recs.size();
+  g_recs.push_back(r);
+}
+
+KProbe::~KProbe() {
+  if (slot_ >= 0) cudaEventRecord(g_recs[slot_].b, st_);
+}
+
+void profile_begin() {
+  g_recs.clear();
+  g_event_next = 0;
+  g_prof_on = true;
+}
+
+int profile_end(std::vector<std::string>* names, std::vector<float>* ms, std::vector<int>* counts) {
+  g_prof_on = false;
+  names->clear();
+  ms->clear();
+  counts->clear();
+  for (auto& r : g_recs) {
+    cudaEventSynchronize(r.b);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, r.a, r.b);
+    size_t i = 0;
+    while (i < names->size() && (*names)[i] != r.name) ++i;
+    if (i == names->size()) {
+      names->push_back(r.name);
+      ms->push_back(0.f);
+      counts->push_back(0);
+    }
+    (*ms)[i] += t;
+    (*counts)[i] += 1;
+  }
+  g_recs.clear();
+  g_event_next = 0;
+  return (int)names->size();
+}
+
+// ============================================================== scan
+namespace {
+
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;  // 4096
+
+template <typename T>
+__device__ T block_exclusive_scan(T v, T* smem_warp, T* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) smem_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    T w = lane < nw ? smem_warp[lane] : T(0);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      T y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < nw) smem_warp[lane] = w;
+  }
+  __syncthreads();
+  T warp_off = warp > 0 ? smem_warp[warp - 1] : T(0);
+  if (total) *total = smem_warp[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return warp_off + x - v;
+}
+
+template <typename T>
+__global__ void k_scan_reduce(const T* __restrict__ d, long long n, T* __restrict__ sums) {
+  __shared__ T sw[32];
+  long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
+  T s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i)
+    if (base + i < n) s += d[base + i];
+  T tot;
+  block_exclusive_scan<T>(s, sw, &tot);
+  if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+template <typename T>
+__global__ void k_scan_apply(T* __restrict__ d, long long n, const T* __restrict__ offs) {
+  __shared__ T sw[32];
+  long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
+  T v[kScanItems];
+  T s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    v[i] = (base + i < n) ? d[base + i] : T(0);
+    s += v[i];
+  }
+  T ex = block_exclusive_scan<T>(s, sw, nullptr);
+  T run = ex + (offs ? offs[blockIdx.x] : T(0));
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    if (base + i < n) d[base + i] = run;
+    run += v[i];
+  }
+}
+
+template <typename T>
+void scan_rec(T* d, long long n, T* scratch, cudaStream_t st) {
+  if (n <= 0) return;
+  long long nb = (n + kScanTile - 1) / kScanTile;
+  if (nb == 1) {
+    {
+      ::sbc::KProbe kp_("k_scan_apply", st);
+      k_scan_apply<T><<<1, kScanThreads, 0, st>>>(d, n, nullptr);
+    }
+    return;
+  }
+  T* sums = scratch;
+  {
+    ::sbc::KProbe kp_("k_scan_reduce", st);
+    k_scan_reduce<T><<<(unsigned)nb, kScanThreads, 0, st>>>(d, n, sums);
+  }
+  scan_rec<T>(sums, nb, scratch + ((nb + 63) / 64) * 64, st);
+  {
+    ::sbc::KProbe kp_("k_scan_apply", st);
+    k_scan_apply<T><<<(unsigned)nb, kScanThreads, 0, st>>>(d, n, sums);
+  }
+}
+
+}  // namespace
+
+size_t scan_scratch_bytes(long long n) {
+  size_t tot = 0;
+  while (n > kScanTile) {
+    long long nb = (n + kScanTile - 1) / kScanTile;
+    tot += (size_t)((nb + 63) / 64) * 64 * sizeof(long long);
+    n = nb;
+  }
+  return tot + 256;
+}
+
+void exclusive_scan_i32(int* d, long long n, void* scratch, cudaStream_t st) {
+  scan_rec<int>(d, n, (int*)scratch, st);
+}
+void exclusive_scan_i64(long long* d, long long n, void* scratch, cudaStream_t st) {
+  scan_rec<long long>(d, n, (long long*)scratch, st);
+}
+
+// ============================================================== radix sort
+namespace {
+
+constexpr int kRadThreads = 256;
+constexpr int kRadWarps = kRadThreads / 32;
+constexpr int kRadRounds = 8;                               // 32-key rounds per warp
+constexpr int kRadTile = kRadThreads * kRadRounds;          // 2048 keys per block
+
+template <typename K>
+__global__ void k_bits_reduce(const K* __restrict__ keys, long long n, K* __restrict__ out_or,
+                              K* __restrict__ out_and) {
+  K o = 0, a = ~K(0);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    K k = keys[i];
+    o |= k;
+    a &= k;
+  }
+  for (int s = 16; s > 0; s >>= 1) {
+    o |= __shfl_xor_sync(0xffffffffu, o, s);
+    a &= __shfl_xor_sync(0xffffffffu, a, s);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicOr(out_or, o);
+    atomicAnd(out_and, a);
+  }
+}
+
+template <typename K>
+__device__ __forceinline__ unsigned digit_of(K k, int shift) {
+  return (unsigned)((k >> shift) & 0xffu);
+}
+
+// per-block digit histogram, digit-major layout hist[d * nblocks + b]
+template <typename K>
+__global__ void k_rad_hist(const K* __restrict__ keys, long long n, int shift,
+                           unsigned* __restrict__ hist, unsigned nblocks) {
+  __shared__ unsigned h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  long long base = (long long)blockIdx.x * kRadTile;
+  for (int i = threadIdx.x; i < kRadTile; i += kRadThreads) {
+    long long j = base + i;
+    if (j < n) atomicAdd(&h[digit_of(keys[j], shift)], 1u);
+  }
+  __syncthreads();
+  hist[(size_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+// stable scatter: warp w owns keys [base + w*256, base + (w+1)*256) in order
+template <typename K>
+__global__ void k_rad_scatter(const K* __restrict__ keys, const unsigned* __restrict__ vals,
+                              K* __restrict__ okeys, unsigned* __restrict__ ovals, long long n,
+                              int shift, const unsigned* __restrict__ offs, unsigned nblocks) {
+  __shared__ unsigned wcnt[kRadWarps][256];
+  __shared__ unsigned boff[256];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < kRadWarps * 256; i += kRadThreads) (&wcnt[0][0])[i] = 0;
+  boff[threadIdx.x] = offs[(size_t)threadIdx.x * nblocks + blockIdx.x];
+  __syncthreads();
+  const long long wbase = (long long)blockIdx.x * kRadTile + (long long)warp * (32 * kRadRounds);
+  const unsigned lt = (1u << lane) - 1u;
+  // pass A: per-warp digit counts
+  for (int r = 0; r < kRadRounds; ++r) {
+    long long j = wbase + r * 32 + lane;
+    unsigned d = j < n ? digit_of(keys[j], shift) : 256u;
+    unsigned peers = __match_any_sync(0xffffffffu, d);
+    if (d < 256u && (peers & lt) == 0) wcnt[warp][d] += __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  // exclusive scan over warps per digit
+  {
+    unsigned d = threadIdx.x, run = 0;
+    for (int w = 0; w < kRadWarps; ++w) {
+      unsigned c = wcnt[w][d];
+      wcnt[w][d] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  // pass B: ranks and scatter
+  for (int r = 0; r < kRadRounds; ++r) {
+    long long j = wbase + r * 32 + lane;
+    bool ok = j < n;
+    K k = ok ? keys[j] : K(0);
+    unsigned d = ok ? digit_of(k, shift) : 256u;
+    unsigned peers = __match_any_sync(0xffffffffu, d);
+    unsigned pos = 0;
+    if (ok) pos = boff[d] + wcnt[warp][d] + __popc(peers & lt);
+    __syncwarp();
+    if (ok && (peers & lt) == 0) wcnt[warp][d] += __popc(peers);
+    __syncwarp();
+    if (ok) {
+      okeys[pos] = k;
+      ovals[pos] = vals[j];
+    }
+  }
+}
+
+template <typename K>
+void radix_sort_impl(K* keys, unsigned* vals, K* keys_tmp, unsigned* vals_tmp, long long n,
+                     int key_bits, void* scratch, cudaStream_t st) {
+  if (n <= 1) return;
+  unsigned nblocks = (unsigned)((n + kRadTile - 1) / kRadTile);
+  // scratch: [or, and] then hist (256*nblocks u32) then scan scratch
+  K* d_or = (K*)scratch;
+  K* d_and = d_or + 1;
+  unsigned* hist = (unsigned*)((char*)scratch + 64);
+  void* sscr = (char*)scratch + 64 + (((size_t)256 * nblocks * sizeof(unsigned) + 255) / 256) * 256;
+  K h_or = 0, h_and = ~K(0);
+  cudaMemcpyAsync(d_or, &h_or, sizeof(K), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(d_and, &h_and, sizeof(K), cudaMemcpyHostToDevice, st);
+  unsigned g = (unsigned)((n + 1023) / 1024);
+  if (g > 2048) g = 2048;
+  {
+    ::sbc::KProbe kp_("k_bits_reduce", st);
+    k_bits_reduce<K><<<g, 1024, 0, st>>>(keys, n, d_or, d_and);
+  }
+  K o, a;
+  cudaMemcpyAsync(&o, d_or, sizeof(K), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(&a, d_and, sizeof(K), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  K vary = o ^ a;
+  K* src_k = keys;
+  unsigned* src_v = vals;
+  K* dst_k = keys_tmp;
+  unsigned* dst_v = vals_tmp;
+  for (int shift = 0; shift < key_bits; shift += 8) {
+    if (((vary >> shift) & K(0xff)) == 0) continue;
+    {
+      ::sbc::KProbe kp_(sizeof(K) == 8 ? "k_rad_hist_u64" : "k_rad_hist_u32", st);
+      k_rad_hist<K><<<nblocks, kRadThreads, 0, st>>>(src_k, n, shift, hist, nblocks);
+    }
+    // exclusive scan of the digit-major histogram gives each (digit, block) its base
+    scan_rec<int>((int*)hist, (long long)256 * nblocks, (int*)sscr, st);
+    {
+      ::sbc::KProbe kp_(sizeof(K) == 8 ? "k_rad_scatter_u64" : "k_rad_scatter_u32", st);
+      k_rad_scatter<K><<<nblocks, kRadThreads, 0, st>>>(src_k, src_v, dst_k, dst_v, n, shift, hist,
+                                                     nblocks);
+    }
+    K* tk = src_k; src_k = dst_k; dst_k = tk;
+    unsigned* tv = src_v; src_v = dst_v; dst_v = tv;
+  }
+  if (src_k != keys) {
+    cudaMemcpyAsync(keys, src_k, sizeof(K) * n, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(vals, src_v, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, st);
+  }
+}
+
+}  // namespace
+
+size_t radix_scratch_bytes(long long n) {
+  long long nblocks = (n + kRadTile - 1) / kRadTile;
+  size_t h = (((size_t)256 * nblocks * sizeof(unsigned) + 255) / 256) * 256;
+  return 64 + h + scan_scratch_bytes(256 * nblocks) * 2 + 256;
+}
+
+void radix_sort_u32(unsigned* keys, unsigned* vals, unsigned* keys_tmp, unsigned* vals_tmp,
+                    long long n, int key_bits, void* scratch, cudaStream_t st) {
+  radix_sort_impl<unsigned>(keys, vals, keys_tmp, vals_tmp, n, key_bits, scratch, st);
+}
+
+void radix_sort_u64(unsigned long long* keys, unsigned* vals, unsigned long long* keys_tmp,
+                    unsigned* vals_tmp, long long n, void* scratch, cudaStream_t st) {
+  radix_sort_impl<unsigned long long>(keys, vals, keys_tmp, vals_tmp, n, 64, scratch, st);
+}
+
+}  // namespace sbc

@@ -1,0 +1,207 @@
+"""Python binding of libsbclip.so (the C ABI in include/sbclip.h) via ctypes.
+
+Mirrors the reference's one entry point, ``seg <base> <overlay...>``
+(src/clip.cpp:2117-2130 -> multicore_clipping, src/clip.cpp:1415): a base
+polygon and k overlays in, for each overlay the list of intersection rings
+out, in the reference's output order.  All computation runs in the CUDA
+library; if it cannot be loaded every call raises (there is no CPU path).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "_build" / "libsbclip.so"
+
+SBC_FLAG_TIMING = 1
+SBC_FLAG_SERIAL_BACKEND = 2
+
+STATS = ["edges", "elementary_points", "tree_size", "cover_entries", "leaf_end_entries",
+         "candidates_tested", "raw_hits", "unique", "slots_b", "slots_c", "serial_backend"]
+PHASES = ["setup", "elementary", "end_lists", "cover_lists", "candidates_merge", "back_end",
+          "device_to_host", "total"]
+DEBUG_ARRAYS = {
+    "uniq_b": (0, np.int32), "uniq_c": (1, np.int32), "uniq_t": (2, np.int32),
+    "isect_xy": (3, np.float64), "isect_ab": (4, np.int32), "isect_ac": (5, np.int32),
+    "merged_bxy": (6, np.float64), "merged_cxy": (7, np.float64),
+    "merged_balpha": (8, np.int32), "merged_calpha": (9, np.int32),
+    "merged_bnb": (10, np.int32), "merged_cnb": (11, np.int32),
+    "label_b": (12, np.int32), "label_c": (13, np.int32),
+}
+
+
+class SbcError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"sbclip error {code}: {msg}")
+        self.code = code
+
+
+class _Rings(ctypes.Structure):
+    _fields_ = [("nrings", ctypes.c_int), ("nverts", ctypes.c_longlong),
+                ("offsets", ctypes.c_void_p), ("xy", ctypes.c_void_p)]
+
+
+class _Options(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("flags", ctypes.c_int)]
+
+
+_lib = None
+
+
+def load_library(path: str | os.PathLike | None = None):
+    """Load libsbclip.so (raises OSError when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise OSError(f"libsbclip.so not built at {p}; run segment-tree-based-clipping_gb300/build.py")
+    L = ctypes.CDLL(str(p))
+    vp, i, ll = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong
+    L.sbc_create.argtypes = [ctypes.POINTER(_Options), ctypes.POINTER(vp)]
+    L.sbc_destroy.argtypes = [vp]
+    L.sbc_last_error.argtypes = [vp]
+    L.sbc_last_error.restype = ctypes.c_char_p
+    L.sbc_clip_one_to_many.argtypes = [vp, vp, i, vp, vp, i, ctypes.POINTER(_Rings), vp]
+    L.sbc_clip_pair.argtypes = [vp, vp, i, vp, i, ctypes.POINTER(_Rings), vp]
+    L.sbc_clip_pair_device.argtypes = [vp, vp, i, vp, i, ctypes.POINTER(_Rings), vp]
+    L.sbc_stats.argtypes = [vp, ctypes.POINTER(ll), i]
+    L.sbc_phase_times.argtypes = [vp, ctypes.POINTER(ctypes.c_float), i]
+    L.sbc_debug_array.argtypes = [vp, i, vp, ll, ctypes.POINTER(ll)]
+    L.sbc_classify_pairs.argtypes = [vp, vp, i, vp, vp, vp, vp, vp]
+    L.sbc_kernel_launches.restype = ctypes.c_ulonglong
+    L.sbc_profile_end.argtypes = [vp, i, vp, vp, i, ctypes.POINTER(i)]
+    L.sbc_version.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def kernel_launches() -> int:
+    return int(load_library().sbc_kernel_launches())
+
+
+def profile_begin() -> None:
+    """Start bracketing every library launch with CUDA events."""
+    load_library().sbc_profile_begin()
+
+
+def profile_end() -> dict:
+    """Stop profiling; {kernel name: (total ms, launches)}."""
+    L = load_library()
+    cap = 256
+    names = ctypes.create_string_buffer(cap * 64)
+    ms = (ctypes.c_float * cap)()
+    cnt = (ctypes.c_int * cap)()
+    n = ctypes.c_int()
+    L.sbc_profile_end(names, cap * 64, ms, cnt, cap, ctypes.byref(n))
+    nm = names.raw.split(b"\0")
+    return {nm[i].decode(): (float(ms[i]), int(cnt[i])) for i in range(min(n.value, cap))}
+
+
+def _rings_from(r: _Rings):
+    n = r.nrings
+    if n <= 0:
+        return []
+    off = np.ctypeslib.as_array(ctypes.cast(r.offsets, ctypes.POINTER(ctypes.c_int)), (n + 1,)).copy()
+    nv = int(r.nverts)
+    xy = np.ctypeslib.as_array(ctypes.cast(r.xy, ctypes.POINTER(ctypes.c_double)), (2 * nv,)).copy()
+    xy = xy.reshape(-1, 2)
+    return [xy[off[j]:off[j + 1]] for j in range(n)]
+
+
+class Clipper:
+    """One library context (one CUDA stream, grow-only device buffers)."""
+
+    def __init__(self, device: int = 0, timing: bool = False, serial_backend: bool = False):
+        self._L = load_library()
+        opt = _Options(device, (SBC_FLAG_TIMING if timing else 0) |
+                       (SBC_FLAG_SERIAL_BACKEND if serial_backend else 0))
+        h = ctypes.c_void_p()
+        rc = self._L.sbc_create(ctypes.byref(opt), ctypes.byref(h))
+        if rc != 0:
+            raise SbcError(rc, "sbc_create failed")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.sbc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise SbcError(rc, self._L.sbc_last_error(self._h).decode())
+
+    def clip(self, base, overlays, stream: int | None = None):
+        """Rings of base ∩ overlay_i for every overlay (one segment tree)."""
+        b = np.ascontiguousarray(base, dtype=np.float64).reshape(-1, 2)
+        ovs = [np.ascontiguousarray(o, dtype=np.float64).reshape(-1, 2) for o in overlays]
+        cxy = np.ascontiguousarray(np.concatenate(ovs, axis=0))
+        sizes = np.array([o.shape[0] for o in ovs], dtype=np.int32)
+        outs = (_Rings * len(ovs))()
+        self._check(self._L.sbc_clip_one_to_many(self._h, b.ctypes.data, b.shape[0], cxy.ctypes.data,
+                                                 sizes.ctypes.data, len(ovs), outs, stream))
+        return [_rings_from(outs[i]) for i in range(len(ovs))]
+
+    def clip_pair(self, base, overlay, stream: int | None = None):
+        return self.clip(base, [overlay], stream)[0]
+
+    def clip_pair_device(self, d_base: int, nb: int, d_overlay: int, nc: int,
+                         stream: int | None = None):
+        """Device pointers in; returns (nrings, nverts, d_offsets, d_xy) device pointers."""
+        r = _Rings()
+        self._check(self._L.sbc_clip_pair_device(self._h, d_base, nb, d_overlay, nc,
+                                                 ctypes.byref(r), stream))
+        return r.nrings, int(r.nverts), r.offsets, r.xy
+
+    def stats(self) -> dict:
+        arr = (ctypes.c_longlong * len(STATS))()
+        self._check(self._L.sbc_stats(self._h, arr, len(STATS)))
+        return {n: int(arr[i]) for i, n in enumerate(STATS)}
+
+    def phase_times(self) -> dict:
+        arr = (ctypes.c_float * len(PHASES))()
+        self._check(self._L.sbc_phase_times(self._h, arr, len(PHASES)))
+        return {n: float(arr[i]) for i, n in enumerate(PHASES)}
+
+    def debug_array(self, name: str) -> np.ndarray:
+        which, dt = DEBUG_ARRAYS[name]
+        cnt = ctypes.c_longlong()
+        self._check(self._L.sbc_debug_array(self._h, which, None, 0, ctypes.byref(cnt)))
+        out = np.empty(max(cnt.value, 1), dtype=dt)
+        self._check(self._L.sbc_debug_array(self._h, which, out.ctypes.data, cnt.value,
+                                            ctypes.byref(cnt)))
+        return out[:cnt.value]
+
+    def classify(self, pairs):
+        """Edge-pair classifier on the device; pairs: (n, 8) p1 p2 q1 q2."""
+        p = np.ascontiguousarray(pairs, dtype=np.float64).reshape(-1, 8)
+        n = p.shape[0]
+        t = np.empty(n, np.int32)
+        a = np.empty(n, np.float64)
+        b = np.empty(n, np.float64)
+        ai = np.empty(n, np.int32)
+        bi = np.empty(n, np.int32)
+        self._check(self._L.sbc_classify_pairs(self._h, p.ctypes.data, n, t.ctypes.data, a.ctypes.data,
+                                               b.ctypes.data, ai.ctypes.data, bi.ctypes.data))
+        return t, a, b, ai, bi
+
+
+def format_rings(rings, precision: int = 6) -> str:
+    """The reference's result text (foster/polygon.h:576-585): `x y,` per
+    vertex, `;` after a ring's last vertex, ostream default precision."""
+    fmt = f"%.{precision}g"
+    out = []
+    for r in rings:
+        lines = [f"{fmt % x} {fmt % y}" for x, y in r]
+        out.append(",\n".join(lines) + ";\n")
+    return "".join(out)

@@ -10,8 +10,8 @@ shapes and sizes of the benchmark configurations:
                       8 octaves of periodic 1-D value noise over theta (amplitude
                       halving per octave), clamped to >= 0.2R.
 * ``pair_small``      10k x 8k plain stars (base at (0,0), overlay at (0.3,0.2)).
-* ``pair_large``      1M x 1M jagged stars; overlay offset (0.25R, 0.1R) and
-                      rotated 0.3 rad about its centre.
+* ``pair_large``      1M x 1M jagged stars, R = 1000; overlay offset
+                      (0.25R, 0.1R) and rotated 0.3 rad about its centre.
 
 Files use the reference's text format (``src/clip.cpp:181-298``): the vertex
 count on the first line, then one ``x,y`` line per vertex, no closing duplicate.
@@ -26,7 +26,39 @@ TWO_PI = 2.0 * np.pi
 # Base lattice frequency (cells around the circle) of the lowest noise octave of
 # the large jagged pair; chosen so that the 1M x 1M pair has 1e5..1e6 unique
 # edge intersections.
-JAGGED_BASE_FREQ = 3000
+JAGGED_BASE_FREQ = 6000
+
+
+_HALF_PI_HI = float.fromhex("0x1.921fb544p+0")        # pi/2 to 33 bits (q*HI is exact)
+_HALF_PI_LO = 1.5707963267948966 - _HALF_PI_HI
+_SIN_C = [(-1) ** k / float(np.prod(np.arange(1, 2 * k + 2, dtype=np.float64))) for k in range(9)]
+_COS_C = [(-1) ** k / float(np.prod(np.arange(1, 2 * k + 1, dtype=np.float64))) for k in range(10)]
+
+
+def sincos(theta):
+    """Platform-independent (sin, cos) built from correctly rounded +, -, *.
+
+    Libm / NumPy SIMD sin and cos may differ by an ulp between hosts (x86-64
+    and aarch64), which would change the generated polygons.  Quadrant
+    reduction by pi/2 (two-part constant) and Taylor polynomials on
+    [-pi/4, pi/4] evaluated with separate NumPy multiplies and adds give the
+    same bits everywhere (truncation error below 1e-16).
+    """
+    t = np.asarray(theta, dtype=np.float64)
+    q = np.floor(t * (2.0 / np.pi) + 0.5)
+    r = (t - q * _HALF_PI_HI) - q * _HALF_PI_LO
+    r2 = r * r
+    s = np.full_like(r, _SIN_C[-1])
+    for c in reversed(_SIN_C[:-1]):
+        s = s * r2 + c
+    s = s * r
+    c_ = np.full_like(r, _COS_C[-1])
+    for c in reversed(_COS_C[:-1]):
+        c_ = c_ * r2 + c
+    k = q.astype(np.int64) & 3
+    sin_t = np.select([k == 0, k == 1, k == 2], [s, c_, -s], -c_)
+    cos_t = np.select([k == 0, k == 1, k == 2], [c_, -s, -c_], s)
+    return sin_t, cos_t
 
 
 def _angles(rng: np.random.Generator, n: int) -> np.ndarray:
@@ -45,9 +77,10 @@ def star(n: int, seed: int, centre=(0.0, 0.0), R: float = 1.0) -> np.ndarray:
     rng = np.random.default_rng(seed)
     th = _angles(rng, n)
     r = R * (0.5 + 0.5 * rng.uniform(0.0, 1.0, n))
+    sn, cs = sincos(th)
     xy = np.empty((n, 2), dtype=np.float64)
-    xy[:, 0] = centre[0] + r * np.cos(th)
-    xy[:, 1] = centre[1] + r * np.sin(th)
+    xy[:, 0] = centre[0] + r * cs
+    xy[:, 1] = centre[1] + r * sn
     return xy
 
 
@@ -79,10 +112,10 @@ def jagged_star(n: int, seed: int, centre=(0.0, 0.0), R: float = 1.0,
     th = _angles(rng, n)
     g = value_noise(th, rng, base_freq)
     r = np.maximum(R * (1.0 + 0.3 * g), 0.2 * R)
-    a = th + rotation
+    sn, cs = sincos(th + rotation)
     xy = np.empty((n, 2), dtype=np.float64)
-    xy[:, 0] = centre[0] + r * np.cos(a)
-    xy[:, 1] = centre[1] + r * np.sin(a)
+    xy[:, 0] = centre[0] + r * cs
+    xy[:, 1] = centre[1] + r * sn
     return xy
 
 
@@ -91,10 +124,21 @@ def pair_small(seed_base: int = 1000):
     return star(10_000, seed_base + 0), star(8_000, seed_base + 1, centre=(0.3, 0.2))
 
 
-def pair_large(n: int = 1_000_000, seed_base: int = 2000, base_freq: int = JAGGED_BASE_FREQ):
-    """Two n-vertex jagged stars; overlay offset (0.25, 0.1) and rotated 0.3 rad."""
-    b = jagged_star(n, seed_base + 0, base_freq=base_freq)
-    c = jagged_star(n, seed_base + 1, centre=(0.25, 0.1), rotation=0.3, base_freq=base_freq)
+# Scale of the large jagged pair.  The reference tests signed areas against an
+# absolute EPSILON of 1e-9 (p_seg_tree/util/constants.h:13); at R = 1 the
+# million-vertex rings have tangential edges ~6e-6 long whose cross products
+# (~4e-11) fall below it, so nearly parallel edges are classified as collinear
+# overlaps and the reference's chain handling loops.  R = 1000 keeps every
+# area far above the threshold without changing the shape.
+LARGE_R = 1000.0
+
+
+def pair_large(n: int = 1_000_000, seed_base: int = 2000, base_freq: int = JAGGED_BASE_FREQ,
+               R: float = LARGE_R):
+    """Two n-vertex jagged stars; overlay offset (0.25R, 0.1R) and rotated 0.3 rad."""
+    b = jagged_star(n, seed_base + 0, R=R, base_freq=base_freq)
+    c = jagged_star(n, seed_base + 1, centre=(0.25 * R, 0.1 * R), R=R, rotation=0.3,
+                    base_freq=base_freq)
     return b, c
 
 

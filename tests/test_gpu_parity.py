@@ -1,0 +1,150 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle and the
+reference's golden outputs.  Integer and index results are compared for
+equality and FP64 results bit for bit (no tolerance: the reference's output
+rings must be reproduced exactly)."""
+from __future__ import annotations
+
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle_py as O
+import sbclip_gen as gen
+from conftest import KAT_PAIRS, digest, ring_digest, rings_equal
+
+pytestmark = pytest.mark.gpu
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def test_classifier_known_answers(clipper):
+    pairs = np.array([[*p1, *p2, *q1, *q2] for p1, p2, q1, q2, _ in KAT_PAIRS], float)
+    t, a, b, ai, bi = clipper.classify(pairs)
+    assert list(t) == [w for *_, w in KAT_PAIRS]
+
+
+def test_classifier_matches_oracle_random(clipper):
+    rng = np.random.default_rng(5)
+    n = 20000
+    pairs = rng.uniform(-1, 1, (n, 8))
+    # make a share of the pairs touch or overlap (degenerate types)
+    pairs[: n // 4, 4:6] = pairs[: n // 4, 0:2]
+    pairs[n // 4: n // 2, 6:8] = pairs[n // 4: n // 2, 0:2] * 2 - pairs[n // 4: n // 2, 2:4]
+    t, a, b, _, _ = clipper.classify(pairs)
+    for i in range(0, n, 7):
+        ot, oa, ob = O.segment_intersection(pairs[i, 0:2], pairs[i, 2:4], pairs[i, 4:6], pairs[i, 6:8])
+        assert t[i] == ot
+        if ot:
+            assert a[i] == oa and b[i] == ob
+
+
+def test_small_cases_match_reference(clipper, small_cases):
+    for case in small_cases:
+        got = clipper.clip(case.base, case.overlays)
+        for i in range(len(case.overlays)):
+            assert rings_equal(got[i], case.rings[i]), case.kind
+
+
+def test_small_cases_serial_back_end_matches(small_cases):
+    import sbclip
+    c = sbclip.Clipper(0, serial_backend=True)
+    try:
+        for case in small_cases:
+            got = c.clip(case.base, case.overlays)
+            for i in range(len(case.overlays)):
+                assert rings_equal(got[i], case.rings[i]), case.kind
+    finally:
+        c.close()
+
+
+def test_unique_pairs_match_reference(clipper, small_cases):
+    for case in small_cases:
+        if len(case.overlays) != 1:
+            continue
+        clipper.clip(case.base, case.overlays)
+        ub, uc, ut = case.uniq[0]
+        assert np.array_equal(clipper.debug_array("uniq_b"), ub)
+        assert np.array_equal(clipper.debug_array("uniq_c"), uc)
+        assert np.array_equal(clipper.debug_array("uniq_t"), ut)
+
+
+def _compare_all(clipper, b, c, entry=None):
+    rings = clipper.clip(b, [c])[0]
+    ora = O.clip(b, [c])["overlays"][0]
+    for name in ("uniq_b", "uniq_c", "uniq_t", "isect_ab", "isect_ac", "isect_xy",
+                 "merged_bxy", "merged_cxy", "merged_balpha", "merged_calpha",
+                 "merged_bnb", "merged_cnb", "label_b", "label_c"):
+        g = clipper.debug_array(name)
+        assert np.array_equal(g, ora[name].astype(g.dtype)), name
+    assert rings_equal(rings, O.rings_of(ora))
+    if entry is not None and digest(b, c) == entry["input_sha256"]:
+        assert len(rings) == entry["rings"]
+        assert ring_digest(rings) == entry["rings_sha256"]
+    return rings
+
+
+def test_pair_10k_8k_all_stages(clipper, digests):
+    b, c = gen.pair_small()
+    _compare_all(clipper, b, c, digests["pair_10k_8k"])
+    st = clipper.stats()
+    assert st["unique"] == digests["pair_10k_8k"]["unique"]
+    assert st["serial_backend"] == 0
+
+
+@pytest.mark.slow
+def test_pair_1m_1m_all_stages(clipper, digests):
+    b, c = gen.pair_large()
+    _compare_all(clipper, b, c, digests["pair_1m_1m"])
+    assert clipper.stats()["serial_backend"] == 0
+
+
+def test_swapped_roles_and_jagged_mid_size(clipper):
+    b, c = gen.pair_large(n=50_000)
+    _compare_all(clipper, b, c)
+    _compare_all(clipper, c, b)
+
+
+def test_cli_text_matches_reference(tmp_path, digests):
+    b, c = gen.pair_small()
+    gen.write_poly(tmp_path / "b.txt", b)
+    gen.write_poly(tmp_path / "c.txt", c)
+    (tmp_path / "work").mkdir()
+    (tmp_path / "results").mkdir()
+    exe = ROOT / "segment-tree-based-clipping_gb300" / "_build" / "seg"
+    p = subprocess.run([str(exe), str(tmp_path / "b.txt"), str(tmp_path / "c.txt")],
+                       cwd=tmp_path / "work", capture_output=True, text=True, timeout=120)
+    assert p.returncode == 0, p.stderr
+    text = (tmp_path / "results" / "Fig-def-R1.txt").read_text()
+    import hashlib
+    assert hashlib.sha256(text.encode()).hexdigest() == digests["pair_10k_8k"]["text6_sha256"]
+
+
+def test_errors_are_status_codes(clipper):
+    import sbclip
+    with pytest.raises(sbclip.SbcError) as e:
+        clipper.clip(np.array([[0, 0], [1, 0]], float), [gen.star(5, 1)])
+    assert e.value.code == 1
+    bad = gen.star(10, 1)
+    bad[3, 0] = np.nan
+    with pytest.raises(sbclip.SbcError) as e:
+        clipper.clip(bad, [gen.star(5, 2)])
+    assert e.value.code == 1
+    # the context stays usable after an error
+    b, c = gen.star(40, 3), gen.star(30, 4, centre=(0.2, 0.1))
+    assert rings_equal(clipper.clip(b, [c])[0], O.rings_of(O.clip(b, [c])["overlays"][0]))
+
+
+def test_repeat_calls_are_identical(clipper):
+    b, c = gen.pair_small()
+    r1 = clipper.clip(b, [c])[0]
+    r2 = clipper.clip(b, [c])[0]
+    assert rings_equal(r1, r2)
+
+
+def test_kernels_were_launched(clipper):
+    import sbclip
+    before = sbclip.kernel_launches()
+    clipper.clip(gen.star(100, 1), [gen.star(80, 2, centre=(0.1, 0.1))])
+    assert sbclip.kernel_launches() > before + 20
