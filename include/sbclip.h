@@ -85,7 +85,8 @@ int sbc_clip_pair_device(sbc_ctx* ctx, const double* d_b_xy, int nb, const doubl
 #define SBC_STAT_SLOTS_B 8
 #define SBC_STAT_SLOTS_C 9
 #define SBC_STAT_SERIAL_BACKEND 10      /* 1 if the exact serial back end ran */
-#define SBC_STAT_NUM 11
+#define SBC_STAT_WORK_UNITS 11          /* overlay 1: candidate pairs enumerated (cover x cover + cover x end) */
+#define SBC_STAT_NUM 12
 int sbc_stats(const sbc_ctx* ctx, long long* out, int n);
 
 /* Per-phase device milliseconds of the last call when SBC_FLAG_TIMING is set:

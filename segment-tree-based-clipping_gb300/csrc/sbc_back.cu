@@ -361,17 +361,32 @@ __global__ void k_tr_copy(Trace T, long long nv, int nseg, const int* __restrict
 }
 
 // ---------------------------------------------------------------- clean-up (A18)
-__global__ void k_ring_of(int nRings, const int* __restrict__ off, int* __restrict__ ringOf) {
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nRings) return;
-  for (int v = off[r]; v < off[r + 1]; ++v) ringOf[v] = r;
-}
-
-__global__ void k_collinear(long long nv, const int* __restrict__ off,
-                            const int* __restrict__ ringOf, const double* __restrict__ xy,
-                            int* __restrict__ ringFlag) {
+// ring of vertex v: last ring whose offset is <= v (empty rings are skipped)
+__global__ void k_ring_of(long long nv, int nRings, const int* __restrict__ off,
+                          int* __restrict__ ringOf) {
   long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv) return;
+  int lo = 0, hi = nRings;
+  while (hi - lo > 1) {
+    int m = (lo + hi) >> 1;
+    if (off[m] <= v) lo = m;
+    else hi = m;
+  }
+  ringOf[v] = lo;
+}
+
+// a ring can only lose vertices if one of them is collinear with its
+// original neighbours (removals only ever follow such a vertex)
+__global__ void k_collinear(long long nv, const int* __restrict__ off,
+                            const int* __restrict__ ringOf, const double* __restrict__ xy,
+                            int* __restrict__ ringFlag, int* __restrict__ keep) {
+  long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v > nv) return;
+  if (v == nv) {
+    keep[v] = 0;
+    return;
+  }
+  keep[v] = 1;
   int r = ringOf[v];
   int a = off[r], b = off[r + 1];
   long long p = v == a ? b - 1 : v - 1;
@@ -381,8 +396,9 @@ __global__ void k_collinear(long long nv, const int* __restrict__ off,
     ringFlag[r] = 1;
 }
 
-// exact cleanUpResult2 on one ring (thread per flagged ring); the reference
-// follows a deleted vertex's old next pointer, which this loop does
+// exact cleanUpResult2 on one flagged ring (thread per ring); the reference
+// keeps iterating from a deleted vertex through its old next pointer, which
+// this loop does
 __global__ void k_cleanup_ring(int nRings, const int* __restrict__ off,
                                const int* __restrict__ ringFlag, const double* __restrict__ xy,
                                int* __restrict__ nxt, int* __restrict__ prv,
@@ -390,7 +406,6 @@ __global__ void k_cleanup_ring(int nRings, const int* __restrict__ off,
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nRings) return;
   int a = off[r], b = off[r + 1];
-  for (int v = a; v < b; ++v) keep[v] = 1;
   if (!ringFlag[r] || b == a) return;
   for (int v = a; v < b; ++v) {
     nxt[v] = v + 1 == b ? a : v + 1;
@@ -421,54 +436,37 @@ __global__ void k_cleanup_ring(int nRings, const int* __restrict__ off,
     if (A(V) < kEps) remove(V);
     V = nx;
   } while (V != start);
-  if (root < 0)
-    for (int v = a; v < b; ++v) keep[v] = 0;
 }
 
-__global__ void k_keep_counts(int nRings, const int* __restrict__ off, const int* __restrict__ keep,
-                              int* __restrict__ cnt) {
+// rings that lost every vertex print nothing (foster/polygon.h:577)
+__global__ void k_ring_nonempty(int nRings, const int* __restrict__ off, const int* __restrict__ kpv,
+                                int* __restrict__ ne) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r > nRings) return;
+  ne[r] = (r < nRings && kpv[off[r + 1]] > kpv[off[r]]) ? 1 : 0;
+}
+
+// kept vertices keep their ring order: the reference's root is the first
+// vertex surviving the root loop, and later removals never touch it
+__global__ void k_compact_xy(long long nv, const int* __restrict__ kpv,
+                             const double* __restrict__ xy, double* __restrict__ oxy) {
+  long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv || kpv[v + 1] == kpv[v]) return;  // flag = difference of the prefix
+  long long w = kpv[v];
+  oxy[2 * w] = xy[2 * v];
+  oxy[2 * w + 1] = xy[2 * v + 1];
+}
+
+__global__ void k_compact_off(int nRings, long long nv, const int* __restrict__ off,
+                              const int* __restrict__ kpv, const int* __restrict__ rpre,
+                              int* __restrict__ ooff) {
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r > nRings) return;
   if (r == nRings) {
-    cnt[r] = 0;
+    ooff[rpre[nRings]] = kpv[nv];
     return;
   }
-  int c = 0;
-  for (int v = off[r]; v < off[r + 1]; ++v) c += keep[v];
-  cnt[r] = c;
-}
-
-// output ring order starts at the ring's root, which stays at its first kept
-// vertex after the root loop; rings that lost every vertex print nothing
-__global__ void k_compact_rings(int nRings, const int* __restrict__ off,
-                                const int* __restrict__ keep, const int* __restrict__ kpre,
-                                const int* __restrict__ rpre, const double* __restrict__ xy,
-                                double* __restrict__ oxy, int* __restrict__ ooff) {
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nRings) return;
-  int a = off[r], b = off[r + 1];
-  int kept = kpre[r + 1] - kpre[r];
-  if (kept > 0) ooff[rpre[r]] = kpre[r];
-  // the root is the first vertex surviving the root loop; later removals
-  // never touch it, so the output starts at the first kept vertex
-  int w = kpre[r];
-  for (int v = a; v < b; ++v)
-    if (keep[v]) {
-      oxy[2 * w] = xy[2 * v];
-      oxy[2 * w + 1] = xy[2 * v + 1];
-      ++w;
-    }
-}
-
-__global__ void k_ring_nonempty(int nRings, const int* __restrict__ kpre, int* __restrict__ ne) {
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r > nRings) return;
-  ne[r] = (r < nRings && kpre[r + 1] > kpre[r]) ? 1 : 0;
-}
-
-__global__ void k_set_last(int* __restrict__ ooff, const int* __restrict__ rpre, int nRings,
-                           const int* __restrict__ kpre) {
-  ooff[rpre[nRings]] = kpre[nRings];
+  if (rpre[r + 1] != rpre[r]) ooff[rpre[r]] = kpv[off[r]];
 }
 
 // ---------------------------------------------------------------- whole-list rings (A16 step 3.5)
@@ -1279,54 +1277,44 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
     int* nxt = (int*)bp.get("cl_next", sizeof(int) * (nv + 1));
     int* prv = (int*)bp.get("cl_prev", sizeof(int) * (nv + 1));
     int* keep = (int*)bp.get("cl_keep", sizeof(int) * (nv + 1));
-    int* kpre = (int*)bp.get("cl_kpre", sizeof(int) * (nR + 2));
     int* rpre = (int*)bp.get("cl_rpre", sizeof(int) * (nR + 2));
     int* ooff = (int*)bp.get("ring_off_" + tg, sizeof(int) * (nR + 2));
     double* oxy = (double*)bp.get("ring_xy_" + tg, sizeof(double) * 2 * (nv + 1));
-    void* sscr = bp.get("cl_scan", scan_scratch_bytes(nR + 2));
+    void* sscr = bp.get("cl_scan", scan_scratch_bytes(nv + nR + 4));
     if (bp.failed) return pl.fail(kENoMem, "device allocation failed (clean-up)");
     cudaMemsetAsync(ringFlag, 0, sizeof(int) * (nR + 1), st);
-    if (nR > 0) {
-      {
-        ::sbc::KProbe kp_("k_ring_of", st);
-        k_ring_of<<<grid_for(nR, 128), 128, 0, st>>>(nR, out.d_off, ringOf);
-      }
-      if (nv > 0) {
-        {
-          ::sbc::KProbe kp_("k_collinear", st);
-          k_collinear<<<grid_for(nv, 256), 256, 0, st>>>(nv, out.d_off, ringOf, out.d_xy, ringFlag);
-        }
-      }
-      {
-        ::sbc::KProbe kp_("k_cleanup_ring", st);
-        k_cleanup_ring<<<grid_for(nR, 128), 128, 0, st>>>(nR, out.d_off, ringFlag, out.d_xy, nxt, prv,
-                                                        keep);
-      }
+    if (nv > 0) {
+      ::sbc::KProbe kp_("k_ring_of", st);
+      k_ring_of<<<grid_for(nv, 256), 256, 0, st>>>(nv, nR, out.d_off, ringOf);
     }
     {
-      ::sbc::KProbe kp_("k_keep_counts", st);
-      k_keep_counts<<<grid_for(nR + 1, 128), 128, 0, st>>>(nR, out.d_off, keep, kpre);
+      ::sbc::KProbe kp_("k_collinear", st);
+      k_collinear<<<grid_for(nv + 1, 256), 256, 0, st>>>(nv, out.d_off, ringOf, out.d_xy, ringFlag,
+                                                        keep);
     }
-    exclusive_scan_i32(kpre, nR + 1, sscr, st);
+    if (nR > 0) {
+      ::sbc::KProbe kp_("k_cleanup_ring", st);
+      k_cleanup_ring<<<grid_for(nR, 128), 128, 0, st>>>(nR, out.d_off, ringFlag, out.d_xy, nxt, prv,
+                                                      keep);
+    }
+    int* kpv = keep;  // exclusive prefix of the keep flags (nv+1 entries)
+    exclusive_scan_i32(kpv, nv + 1, sscr, st);
     {
       ::sbc::KProbe kp_("k_ring_nonempty", st);
-      k_ring_nonempty<<<grid_for(nR + 1, 128), 128, 0, st>>>(nR, kpre, rpre);
+      k_ring_nonempty<<<grid_for(nR + 1, 128), 128, 0, st>>>(nR, out.d_off, kpv, rpre);
     }
     exclusive_scan_i32(rpre, nR + 1, sscr, st);
-    if (nR > 0) {
-      {
-        ::sbc::KProbe kp_("k_compact_rings", st);
-        k_compact_rings<<<grid_for(nR, 128), 128, 0, st>>>(nR, out.d_off, keep, kpre, rpre, out.d_xy,
-                                                         oxy, ooff);
-      }
+    if (nv > 0) {
+      ::sbc::KProbe kp_("k_compact_xy", st);
+      k_compact_xy<<<grid_for(nv, 256), 256, 0, st>>>(nv, kpv, out.d_xy, oxy);
     }
     {
-      ::sbc::KProbe kp_("k_set_last", st);
-      k_set_last<<<1, 1, 0, st>>>(ooff, rpre, nR, kpre);
+      ::sbc::KProbe kp_("k_compact_off", st);
+      k_compact_off<<<grid_for(nR + 1, 128), 128, 0, st>>>(nR, nv, out.d_off, kpv, rpre, ooff);
     }
     int hh[2];
     cudaMemcpyAsync(&hh[0], rpre + nR, sizeof(int), cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(&hh[1], kpre + nR, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&hh[1], kpv + nv, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
     out.nrings = hh[0];
     out.nverts = hh[1];

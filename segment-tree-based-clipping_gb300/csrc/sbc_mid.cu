@@ -577,6 +577,7 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
   if (nraw >= (1LL << 31)) return fail(kEInput, "too many candidate hits");
   out.raw_hits = nraw;
   out.tests = ntested;
+  out.work = W;
 
   // ---- A9 dedup: stable sort by base id, per-edge key order, first per overlay edge
   long long R = nraw;

@@ -37,7 +37,7 @@ struct OverlayOut {
   int* d_off = nullptr;     // nrings+1 vertex offsets
   double* d_xy = nullptr;   // 2*nverts
   // diagnostics
-  long long raw_hits = 0, tests = 0, unique = 0, slots_b = 0, slots_c = 0;
+  long long raw_hits = 0, tests = 0, unique = 0, slots_b = 0, slots_c = 0, work = 0;
   int slow_path = 0;
 };
 
