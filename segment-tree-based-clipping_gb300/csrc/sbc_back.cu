@@ -379,11 +379,13 @@ __global__ void k_ring_of(long long nv, int nRings, const int* __restrict__ off,
 // original neighbours (removals only ever follow such a vertex)
 __global__ void k_collinear(long long nv, const int* __restrict__ off,
                             const int* __restrict__ ringOf, const double* __restrict__ xy,
-                            int* __restrict__ ringFlag, int* __restrict__ keep) {
+                            int* __restrict__ ringFlag, int* __restrict__ keep,
+                            int* __restrict__ flagV, int* __restrict__ nxt, int* __restrict__ prv) {
   long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (v > nv) return;
   if (v == nv) {
     keep[v] = 0;
+    flagV[v] = 0;
     return;
   }
   keep[v] = 1;
@@ -391,26 +393,35 @@ __global__ void k_collinear(long long nv, const int* __restrict__ off,
   int a = off[r], b = off[r + 1];
   long long p = v == a ? b - 1 : v - 1;
   long long q = v + 1 == b ? a : v + 1;
-  if (fabs(area3(xy[2 * p], xy[2 * p + 1], xy[2 * v], xy[2 * v + 1], xy[2 * q], xy[2 * q + 1])) <
-      kEps)
-    ringFlag[r] = 1;
+  nxt[v] = (int)q;
+  prv[v] = (int)p;
+  int f = fabs(area3(xy[2 * p], xy[2 * p + 1], xy[2 * v], xy[2 * v + 1], xy[2 * q], xy[2 * q + 1])) <
+          kEps;
+  flagV[v] = f;
+  if (f) ringFlag[r] = 1;
 }
 
-// exact cleanUpResult2 on one flagged ring (thread per ring); the reference
-// keeps iterating from a deleted vertex through its old next pointer, which
-// this loop does
+__global__ void k_flag_list(long long nv, const int* __restrict__ fpre, int* __restrict__ list) {
+  long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  if (fpre[v + 1] != fpre[v]) list[fpre[v]] = (int)v;
+}
+
+// cleanUpResult2 (foster/polyclip.h:767-787) on one flagged ring, thread per
+// ring.  The linked-list steps are the reference's; vertices whose links are
+// still the original ones and that are not collinear with their original
+// neighbours cannot be removed, so the walk jumps over them: it visits the
+// flagged vertices, the successor of every removed vertex and the last
+// vertex (whose next is the root the root loop left).  The reference keeps
+// iterating from a deleted vertex through its old next pointer; so does this.
 __global__ void k_cleanup_ring(int nRings, const int* __restrict__ off,
-                               const int* __restrict__ ringFlag, const double* __restrict__ xy,
-                               int* __restrict__ nxt, int* __restrict__ prv,
-                               int* __restrict__ keep) {
+                               const int* __restrict__ ringFlag, const int* __restrict__ flist,
+                               int nflag, const double* __restrict__ xy, int* __restrict__ nxt,
+                               int* __restrict__ prv, int* __restrict__ keep) {
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nRings) return;
   int a = off[r], b = off[r + 1];
   if (!ringFlag[r] || b == a) return;
-  for (int v = a; v < b; ++v) {
-    nxt[v] = v + 1 == b ? a : v + 1;
-    prv[v] = v == a ? b - 1 : v - 1;
-  }
   auto A = [&](int v) {
     int p = prv[v], q = nxt[v];
     return fabs(area3(xy[2 * p], xy[2 * p + 1], xy[2 * v], xy[2 * v + 1], xy[2 * q], xy[2 * q + 1]));
@@ -426,16 +437,27 @@ __global__ void k_cleanup_ring(int nRings, const int* __restrict__ off,
     keep[V] = 0;
   };
   while (root >= 0 && A(root) < kEps) remove(root);
-  if (root < 0) {
-    for (int v = a; v < b; ++v) keep[v] = 0;
-    return;
+  if (root < 0) return;  // every vertex was removed (each keep flag cleared)
+  const bool prefixRemoved = root != a;
+  int lo = 0, hi = nflag;  // first flagged vertex >= root
+  while (lo < hi) {
+    int m = (lo + hi) >> 1;
+    if (flist[m] < root) lo = m + 1;
+    else hi = m;
   }
-  int start = root, V = start;
-  do {
-    int nx = nxt[V];
-    if (A(V) < kEps) remove(V);
-    V = nx;
-  } while (V != start);
+  int fi = lo;
+  int V = root;
+  while (true) {
+    bool removed = A(V) < kEps;
+    if (removed) remove(V);
+    int cand = 0x7fffffff;
+    if (removed && V + 1 < b) cand = V + 1;
+    while (fi < nflag && flist[fi] <= V) ++fi;
+    if (fi < nflag && flist[fi] < b && flist[fi] < cand) cand = flist[fi];
+    if (prefixRemoved && V < b - 1 && b - 1 < cand) cand = b - 1;
+    if (cand >= b) break;
+    V = cand;
+  }
 }
 
 // rings that lost every vertex print nothing (foster/polygon.h:577)
@@ -1277,6 +1299,8 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
     int* nxt = (int*)bp.get("cl_next", sizeof(int) * (nv + 1));
     int* prv = (int*)bp.get("cl_prev", sizeof(int) * (nv + 1));
     int* keep = (int*)bp.get("cl_keep", sizeof(int) * (nv + 1));
+    int* flagV = (int*)bp.get("cl_flagV", sizeof(int) * (nv + 1));
+    int* flist = (int*)bp.get("cl_flist", sizeof(int) * (nv + 1));
     int* rpre = (int*)bp.get("cl_rpre", sizeof(int) * (nR + 2));
     int* ooff = (int*)bp.get("ring_off_" + tg, sizeof(int) * (nR + 2));
     double* oxy = (double*)bp.get("ring_xy_" + tg, sizeof(double) * 2 * (nv + 1));
@@ -1290,12 +1314,20 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
     {
       ::sbc::KProbe kp_("k_collinear", st);
       k_collinear<<<grid_for(nv + 1, 256), 256, 0, st>>>(nv, out.d_off, ringOf, out.d_xy, ringFlag,
-                                                        keep);
+                                                        keep, flagV, nxt, prv);
     }
-    if (nR > 0) {
+    exclusive_scan_i32(flagV, nv + 1, sscr, st);
+    int nflag = 0;
+    cudaMemcpyAsync(&nflag, flagV + nv, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    if (nflag > 0) {
+      {
+        ::sbc::KProbe kp_("k_flag_list", st);
+        k_flag_list<<<grid_for(nv, 256), 256, 0, st>>>(nv, flagV, flist);
+      }
       ::sbc::KProbe kp_("k_cleanup_ring", st);
-      k_cleanup_ring<<<grid_for(nR, 128), 128, 0, st>>>(nR, out.d_off, ringFlag, out.d_xy, nxt, prv,
-                                                      keep);
+      k_cleanup_ring<<<grid_for(nR, 128), 128, 0, st>>>(nR, out.d_off, ringFlag, flist, nflag,
+                                                      out.d_xy, nxt, prv, keep);
     }
     int* kpv = keep;  // exclusive prefix of the keep flags (nv+1 entries)
     exclusive_scan_i32(kpv, nv + 1, sscr, st);

@@ -92,126 +92,158 @@ __device__ __forceinline__ bool lsmf(double p1x, double p1y, double p2x, double 
   return true;
 }
 
-constexpr int kCandThreads = 256;
-constexpr int kCandItems = 8;
-constexpr int kCandChunk = kCandThreads * kCandItems;
-constexpr int kCandSm = 1024;
+constexpr int kChunk = 256;       // candidate units per chunk (8 rounds of 32 lanes)
+constexpr int kWarpChunks = 8;    // consecutive chunks per warp
+constexpr int kCandBlock = 256;
 
-// load-balanced candidate tests: unit u -> (cover entry P, partner j)
-__global__ void __launch_bounds__(kCandThreads)
-k_cand_test(const long long* __restrict__ wscan, long long nCover, long long W,
-            const unsigned* __restrict__ cov_node, const unsigned* __restrict__ cov_edge,
-            const int* __restrict__ blk_s, const int* __restrict__ wcc,
-            const int* __restrict__ tstart, int k, int cType, int logL, int numLeaves,
-            const int* __restrict__ le_off, const int* __restrict__ le_edge,
-            const int* __restrict__ le_leaf, const int* __restrict__ aft,
-            const int* __restrict__ bef, const int* __restrict__ e_id,
+// conservative float bounds of an edge's y extent (rounded outwards), one
+// record per leaf entry: {edge, leaf, ymin rounded down, ymax rounded up}
+__global__ void k_pack_leaf(long long n, const int* __restrict__ le_edge,
+                            const int* __restrict__ le_leaf, const int* __restrict__ e_id,
+                            const int* __restrict__ tstart, int k, const double* __restrict__ bP,
+                            const double* __restrict__ cP, int4* __restrict__ pack) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int e = le_edge[i];
+  const double* p = (class_of(tstart, k, e) == 0 ? bP : cP) + e_id[e];
+  double y0 = fmin(p[1], p[3]), y1 = fmax(p[1], p[3]);
+  pack[i] = make_int4(e, le_leaf[i], __float_as_int(__double2float_rd(y0)),
+                      __float_as_int(__double2float_ru(y1)));
+}
+
+__global__ void k_edge_ybox(int E, const int* __restrict__ e_id, const int* __restrict__ tstart,
+                            int k, const double* __restrict__ bP, const double* __restrict__ cP,
+                            float2* __restrict__ ybox, int2* __restrict__ ab,
+                            const int* __restrict__ aft, const int* __restrict__ bef) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  const double* p = (class_of(tstart, k, e) == 0 ? bP : cP) + e_id[e];
+  double y0 = fmin(p[1], p[3]), y1 = fmax(p[1], p[3]);
+  ybox[e] = make_float2(__double2float_rd(y0), __double2float_ru(y1));
+  ab[e] = make_int2(aft[e], bef[e]);
+}
+
+__global__ void k_chunks(long long n, const long long* __restrict__ wscan,
+                         long long* __restrict__ chunks) {
+  long long P = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (P > n) return;
+  chunks[P] = P < n ? (wscan[P + 1] - wscan[P] + kChunk - 1) / kChunk : 0;
+}
+
+// Candidate tests.  Every partner in the same cover list or in the end list
+// of the node overlaps the cover edge in x (both span or touch the node's
+// interval), so the reference's LSMF box test reduces to the y test; a
+// conservative float y test (bounds rounded outwards) skips most partners
+// with one 16-byte load, and the exact FP64 LSMF and classification run on
+// the rest.  Each warp walks kWarpChunks consecutive chunks of 256 units.
+__global__ void __launch_bounds__(kCandBlock)
+k_cand_test(const long long* __restrict__ cscan, long long nCover, long long TC,
+            const long long* __restrict__ wscan, const unsigned* __restrict__ cov_node,
+            const unsigned* __restrict__ cov_edge, const int* __restrict__ blk_s,
+            const int* __restrict__ wcc, const int* __restrict__ tstart, int k, int cType,
+            int logL, int numLeaves, const int* __restrict__ le_off,
+            const int4* __restrict__ pack, const float2* __restrict__ ybox,
+            const int2* __restrict__ ab, const int* __restrict__ e_id,
             const double* __restrict__ bP, const double* __restrict__ cP,
             unsigned long long* __restrict__ counters, long long cap, int* __restrict__ rb,
             int* __restrict__ rc, int* __restrict__ rt, unsigned long long* __restrict__ rkey) {
-  __shared__ long long sw[kCandSm + 1];
-  __shared__ long long sP[2];
-  const long long c0 = (long long)blockIdx.x * kCandChunk;
-  const long long c1 = min(c0 + (long long)kCandChunk, W);
-  if (threadIdx.x < 2) {
-    long long target = threadIdx.x == 0 ? c0 : c1 - 1;
-    long long lo = 0, hi = nCover;  // last P with wscan[P] <= target
-    while (hi - lo > 1) {
-      long long m = (lo + hi) >> 1;
-      if (wscan[m] <= target) lo = m;
-      else hi = m;
-    }
-    sP[threadIdx.x] = lo;
-  }
-  __syncthreads();
-  const long long Plo = sP[0], Phi = sP[1];
-  const bool in_smem = (Phi - Plo + 1) <= kCandSm;
-  if (in_smem)
-    for (long long i = threadIdx.x; i <= Phi - Plo + 1; i += blockDim.x) sw[i] = wscan[Plo + i];
-  __syncthreads();
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long c0 = warp * kWarpChunks;
+  if (c0 >= TC) return;  // warp-uniform
+  const long long c1 = min(c0 + (long long)kWarpChunks, TC);
   const int L = 1 << logL;
+  long long P;
+  {
+    long long lo = 0, hi = nCover;  // last P with cscan[P] <= c0
+    while (hi - lo > 1) {
+      long long m = (lo + hi) >> 1;
+      if (cscan[m] <= c0) lo = m;
+      else hi = m;
+    }
+    P = lo;
+  }
   unsigned tested = 0;
-  for (int it = 0; it < kCandItems; ++it) {
-    long long u = c0 + (long long)it * kCandThreads + threadIdx.x;
-    bool hit = false;
-    int bId = 0, cId = 0, ty = 0;
-    unsigned long long key = 0;
-    if (u < c1) {
-      long long P;
-      if (in_smem) {
-        int lo = 0, hi = (int)(Phi - Plo + 1);
-        while (hi - lo > 1) {
-          int m = (lo + hi) >> 1;
-          if (sw[m] <= u) lo = m;
-          else hi = m;
+  for (long long c = c0; c < c1; ++c) {
+    while (cscan[P + 1] <= c) ++P;
+    const long long j0 = (c - cscan[P]) * kChunk;
+    const long long w = wscan[P + 1] - wscan[P];
+    const int self = (int)cov_edge[P];
+    const int v = (int)cov_node[P];
+    const int tself = class_of(tstart, k, self);
+    const int nc = wcc[P], bs = blk_s[P];
+    int lo = 0, hi = 0;
+    {
+      int d = 31 - __clz(v), h = logL - d;
+      lo = (v << h) - L;
+      hi = ((v + 1) << h) - 1 - L;
+    }
+    const long long lbase = le_off[(size_t)(tself == 0 ? cType : 0) * numLeaves + lo];
+    const float2 sb = ybox[self];
+    const int sid = e_id[self];
+    const double* sp = (tself == 0 ? bP : cP) + sid;
+    for (int r = 0; r < kChunk / 32; ++r) {
+      const long long j = j0 + r * 32 + lane;
+      bool hit = false;
+      int bId = 0, cId = 0, ty = 0;
+      unsigned long long key = 0;
+      if (j < w) {
+        int partner = -1, phase = 0;
+        bool pass;
+        if (j < nc) {
+          partner = (int)cov_edge[bs + j];
+          float2 pbx = ybox[partner];
+          pass = !(sb.x > pbx.y || sb.y < pbx.x);
+        } else {
+          phase = 1;
+          int4 q = pack[lbase + (j - nc)];
+          partner = q.x;
+          pass = !(sb.x > __int_as_float(q.w) || sb.y < __int_as_float(q.z));
+          if (pass) {
+            // the edge's other leaf entry in this subtree comes first: an end
+            // list holds each edge once
+            int2 o = ab[partner];
+            int leaf = q.y + L;
+            int other = (o.x == leaf) ? o.y : o.x;
+            if (other >= 0 && other >= lo + L && other <= hi + L && other < leaf) pass = false;
+          }
         }
-        P = Plo + lo;
-      } else {
-        long long lo = Plo, hi = Phi + 1;
-        while (hi - lo > 1) {
-          long long m = (lo + hi) >> 1;
-          if (wscan[m] <= u) lo = m;
-          else hi = m;
-        }
-        P = lo;
-      }
-      long long j = u - (in_smem ? sw[P - Plo] : wscan[P]);
-      int self = (int)cov_edge[P];
-      int v = (int)cov_node[P];
-      int tself = class_of(tstart, k, self);
-      int partner = -1, phase = 0;
-      if (j < wcc[P]) {
-        partner = (int)cov_edge[blk_s[P] + j];
-      } else {
-        phase = 1;
-        int lo, hi;
-        leaf_range(v, logL, &lo, &hi);
-        int cls = tself == 0 ? cType : 0;
-        long long idx = le_off[(size_t)cls * numLeaves + lo] + (j - wcc[P]);
-        int e2 = le_edge[idx];
-        int leaf = le_leaf[idx] + L;
-        int other = (aft[e2] == leaf) ? bef[e2] : aft[e2];
-        // the edge's other leaf entry inside this subtree comes first: a set
-        // holds the edge once
-        bool dup = other >= 0 && other >= lo + L && other <= hi + L && other < leaf;
-        if (!dup) partner = e2;
-      }
-      if (partner >= 0) {
-        int b = tself == 0 ? self : partner;
-        int c = tself == 0 ? partner : self;
-        bId = e_id[b];
-        cId = e_id[c];
-        const double* pb = bP + bId;
-        const double* pc = cP + cId;
-        double p1x = pb[0], p1y = pb[1], p2x = pb[2], p2y = pb[3];
-        double q1x = pc[0], q1y = pc[1], q2x = pc[2], q2y = pc[3];
-        if (lsmf(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y)) {
-          ++tested;
-          double al, be;
-          ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &be);
-          if (ty) {
-            hit = true;
-            key = ((unsigned long long)P << 36) | ((unsigned long long)phase << 35) |
-                  (unsigned long long)(e_id[partner] >> 1);
+        if (pass) {
+          const int pid = e_id[partner];
+          const double* pp = (tself == 0 ? cP : bP) + pid;
+          const double* pbp = tself == 0 ? sp : pp;
+          const double* pcp = tself == 0 ? pp : sp;
+          double p1x = pbp[0], p1y = pbp[1], p2x = pbp[2], p2y = pbp[3];
+          double q1x = pcp[0], q1y = pcp[1], q2x = pcp[2], q2y = pcp[3];
+          if (lsmf(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y)) {
+            ++tested;
+            double al, be;
+            ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &be);
+            if (ty) {
+              hit = true;
+              bId = tself == 0 ? sid : pid;
+              cId = tself == 0 ? pid : sid;
+              key = ((unsigned long long)P << 36) | ((unsigned long long)phase << 35) |
+                    (unsigned long long)(pid >> 1);
+            }
           }
         }
       }
-    }
-    unsigned m = __ballot_sync(0xffffffffu, hit);
-    if (m) {
-      int leader = __ffs(m) - 1;
-      unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(&counters[0], (unsigned long long)__popc(m));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (hit) {
-        long long idx = (long long)base + __popc(m & lt);
-        if (idx < cap) {
-          rb[idx] = bId;
-          rc[idx] = cId;
-          rt[idx] = ty;
-          rkey[idx] = key;
+      unsigned m = __ballot_sync(0xffffffffu, hit);
+      if (m) {
+        int leader = __ffs(m) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(&counters[0], (unsigned long long)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (hit) {
+          long long idx = (long long)base + __popc(m & lt);
+          if (idx < cap) {
+            rb[idx] = bId;
+            rc[idx] = cId;
+            rt[idx] = ty;
+            rkey[idx] = key;
+          }
         }
       }
     }
@@ -547,6 +579,30 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
   cudaMemcpyAsync(&W, work + nCover, sizeof(long long), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
 
+  // packed leaf entries, edge y boxes and chunk prefix for the test kernel
+  int4* pack = (int4*)pool_.get("cand_pack", sizeof(int4) * (nLeafEnt + 1));
+  float2* ybox = (float2*)pool_.get("cand_ybox", sizeof(float2) * (E + 1));
+  int2* abx = (int2*)pool_.get("cand_ab", sizeof(int2) * (E + 1));
+  long long* cscan = (long long*)pool_.get("cand_cscan", sizeof(long long) * (nCover + 1));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (candidate tables)");
+  if (cType == 1) {
+    if (nLeafEnt > 0) {
+      ::sbc::KProbe kp_("k_pack_leaf", st);
+      k_pack_leaf<<<grid_for(nLeafEnt, 256), 256, 0, st>>>(nLeafEnt, le_edge, le_leaf, e_id, tstart, k,
+                                                        bP, cP, pack);
+    }
+    ::sbc::KProbe kp_("k_edge_ybox", st);
+    k_edge_ybox<<<grid_for(E, 256), 256, 0, st>>>(E, e_id, tstart, k, bP, cP, ybox, abx, aft, bef);
+  }
+  {
+    ::sbc::KProbe kp_("k_chunks", st);
+    k_chunks<<<grid_for(nCover + 1, 256), 256, 0, st>>>(nCover, work, cscan);
+  }
+  exclusive_scan_i64(cscan, nCover + 1, sscr, st);
+  long long TC = 0;
+  cudaMemcpyAsync(&TC, cscan + nCover, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+
   long long cap = 4LL * E + (1 << 20);
   long long nraw = 0, ntested = 0;
   int *rb = nullptr, *rc = nullptr, *rt = nullptr;
@@ -558,13 +614,12 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
     rkey = (unsigned long long*)pool_.get("raw_key", sizeof(unsigned long long) * cap);
     if (pool_.failed) return fail(kENoMem, "device allocation failed (raw candidates)");
     cudaMemsetAsync(counters, 0, 16, st);
-    if (W > 0) {
-      {
-        ::sbc::KProbe kp_("k_cand_test", st);
-        k_cand_test<<<grid_for(W, kCandChunk), kCandThreads, 0, st>>>(
-          work, nCover, W, cov_node, cov_edge, blk_s, wcc, tstart, k, cType, logL, numLeaves,
-          le_off, le_edge, le_leaf, aft, bef, e_id, bP, cP, counters, cap, rb, rc, rt, rkey);
-      }
+    if (TC > 0) {
+      long long warps = (TC + kWarpChunks - 1) / kWarpChunks;
+      ::sbc::KProbe kp_("k_cand_test", st);
+      k_cand_test<<<grid_for(warps * 32, kCandBlock), kCandBlock, 0, st>>>(
+          cscan, nCover, TC, work, cov_node, cov_edge, blk_s, wcc, tstart, k, cType, logL,
+          numLeaves, le_off, pack, ybox, abx, e_id, bP, cP, counters, cap, rb, rc, rt, rkey);
     }
     unsigned long long hc[2];
     cudaMemcpyAsync(hc, counters, 16, cudaMemcpyDeviceToHost, st);
