@@ -300,64 +300,83 @@ __device__ __forceinline__ int tr_len(const Trace& T, int x, int t) {
   return d;
 }
 
-// createResult2 per ring, segment by segment.  PASS 0 counts, PASS 1 writes
-// segment descriptors (enex index of the segment start, output offset).
-template <int PASS>
-__global__ void k_tr_walk(Trace T, int nRings, const int* __restrict__ starts,
-                          int* __restrict__ rlen, int* __restrict__ rseg,
-                          const int* __restrict__ vOff, const int* __restrict__ sOff,
-                          int* __restrict__ segX, int* __restrict__ segOut, BkScalars* sc) {
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nRings) return;
-  const int I = starts[r];
-  int cur = I;
-  int len = 0, nseg = 0;
-  int guard = T.cP + T.cQ + 2;
-  int vo = PASS ? vOff[r] : 0, so = PASS ? sOff[r] : 0;
-  while (true) {
-    int t = tr_target(T, cur);
-    if (PASS) {
-      segX[so + nseg] = cur;
-      segOut[so + nseg] = vo + len;
-    }
-    len += tr_len(T, cur, t);
-    ++nseg;
-    if (t == I) break;
-    int s = tr_jump(T, t);
-    if (s == I) break;
-    if (s < 0 || --guard < 0) {
-      atomicOr(&sc->anomaly, 128u);
-      break;
-    }
-    cur = s;
-  }
-  if (!PASS) {
-    rlen[r] = len;
-    rseg[r] = nseg;
+// createResult2 as weighted list ranking.  A ring is the orbit of its start I
+// under succ(x) = neighbour(target(x)); segment x contributes the vertices
+// after x up to target(x).  Breaking each orbit before I and pointer jumping
+// gives every segment the number of ring vertices from it to the ring's end,
+// hence its output position; vertices of the opposite orbit of the same ring
+// never reach the break and are not part of the output.
+__global__ void k_lr_init(Trace T, const int* __restrict__ mval, int* __restrict__ nxt,
+                          long long* __restrict__ S, int* __restrict__ ringI,
+                          int* __restrict__ indeg, BkScalars* sc) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = T.cP + T.cQ;
+  if (x >= n) return;
+  int I = T.rankP[mval[x]];
+  int t = tr_target(T, x);
+  int s = tr_jump(T, t);
+  ringI[x] = I;
+  nxt[x] = (s == I) ? -1 : s;
+  S[x] = tr_len(T, x, t);
+  if (s >= 0) atomicAdd(&indeg[s], 1);
+  // a segment ending at the ring's start vertex itself stops the reference's
+  // walk early: not covered here
+  if (t == I) atomicOr(&sc->anomaly, 256u);
+}
+
+__global__ void k_lr_jump(int n, const int* __restrict__ nin, const long long* __restrict__ Sin,
+                          int* __restrict__ nout, long long* __restrict__ Sout) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= n) return;
+  int j = nin[x];
+  if (j < 0) {
+    nout[x] = -1;
+    Sout[x] = Sin[x];
+  } else {
+    nout[x] = nin[j];
+    Sout[x] = Sin[x] + Sin[j];
   }
 }
 
-__global__ void k_tr_copy(Trace T, long long nv, int nseg, const int* __restrict__ segX,
-                          const int* __restrict__ segOut, const double* __restrict__ ixB,
+// succ must be a permutation and every ring start must reach its orbit's end
+__global__ void k_lr_check(int n, const int* __restrict__ nxt, const int* __restrict__ ringI,
+                           const int* __restrict__ indeg, BkScalars* sc) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= n) return;
+  if (indeg[x] != 1) atomicOr(&sc->anomaly, 512u);
+  if (ringI[x] == x && nxt[x] != -1) atomicOr(&sc->anomaly, 1024u);
+}
+
+__global__ void k_lr_ringlen(int nRings, const int* __restrict__ starts,
+                             const long long* __restrict__ S, int* __restrict__ rlen) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r > nRings) return;
+  rlen[r] = r < nRings ? (int)S[starts[r]] : 0;
+}
+
+__global__ void k_lr_copy(Trace T, const int* __restrict__ nxt, const long long* __restrict__ S,
+                          const int* __restrict__ ringI, const int* __restrict__ startPre,
+                          const int* __restrict__ vOff, const double* __restrict__ ixB,
                           const double* __restrict__ ixC, double* __restrict__ out) {
-  long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= nv) return;
-  int lo = 0, hi = nseg;  // last segment with segOut <= v
-  while (hi - lo > 1) {
-    int m = (lo + hi) >> 1;
-    if (segOut[m] <= v) lo = m;
-    else hi = m;
-  }
-  int x = segX[lo];
-  int step = (int)(v - segOut[lo]) + 1;
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = T.cP + T.cQ;
+  if (x >= n || nxt[x] != -1) return;  // only segments of a start's orbit
+  int I = ringI[x];
+  long long base = vOff[startPre[I]] + S[I] - S[x];
+  int t = tr_target(T, x);
+  int len = tr_len(T, x, t);
   bool onP = x < T.cP;
-  int n = onP ? T.nB : T.nQ;
+  int m = onP ? T.nB : T.nQ;
   int sx = tr_slot(T, x);
   bool fwd = (onP ? T.enexP[sx] : T.enexQ[sx]) == EX_ENTRY;
-  int slot = fwd ? (sx + step) % n : ((sx - step) % n + n) % n;
   const double* src = onP ? ixB : ixC;
-  out[2 * v] = src[2 * slot];
-  out[2 * v + 1] = src[2 * slot + 1];
+  for (int step = 1; step <= len; ++step) {
+    int slot = fwd ? sx + step : sx - step;
+    if (slot >= m) slot -= m;
+    if (slot < 0) slot += m;
+    out[2 * (base + step - 1)] = src[2 * slot];
+    out[2 * (base + step - 1) + 1] = src[2 * slot + 1];
+  }
 }
 
 // ---------------------------------------------------------------- clean-up (A18)
@@ -1246,43 +1265,49 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
     cudaStreamSynchronize(st);
     int* starts = (int*)bp.get("bk_starts", sizeof(int) * (nRings + 1));
     int* rlen = (int*)bp.get("bk_rlen", sizeof(int) * (nRings + 2));
-    int* rseg = (int*)bp.get("bk_rseg", sizeof(int) * (nRings + 2));
+    int* nxA = (int*)bp.get("bk_lrnA", sizeof(int) * (nE + 1));
+    int* nxB = (int*)bp.get("bk_lrnB", sizeof(int) * (nE + 1));
+    long long* SA = (long long*)bp.get("bk_lrSA", sizeof(long long) * (nE + 1));
+    long long* SB = (long long*)bp.get("bk_lrSB", sizeof(long long) * (nE + 1));
+    int* ringI = (int*)bp.get("bk_lrI", sizeof(int) * (nE + 1));
+    int* indeg = (int*)bp.get("bk_lrdeg", sizeof(int) * (nE + 1));
     if (bp.failed) return pl.fail(kENoMem, "device allocation failed (rings)");
     {
       ::sbc::KProbe kp_("k_tr_startlist", st);
       k_tr_startlist<<<grid_for(cPn, 256), 256, 0, st>>>(cPn, isStart, starts);
     }
+    cudaMemsetAsync(indeg, 0, sizeof(int) * (nE + 1), st);
     {
-      ::sbc::KProbe kp_("k_tr_walk", st);
-      k_tr_walk<0><<<grid_for(nRings, 128), 128, 0, st>>>(T, nRings, starts, rlen, rseg, nullptr,
-                                                        nullptr, nullptr, nullptr, sc);
+      ::sbc::KProbe kp_("k_lr_init", st);
+      k_lr_init<<<grid_for(nE, 256), 256, 0, st>>>(T, mA, nxA, SA, ringI, indeg, sc);
     }
-    cudaMemsetAsync(rlen + nRings, 0, sizeof(int), st);
-    cudaMemsetAsync(rseg + nRings, 0, sizeof(int), st);
+    for (int span = 1; span < nE; span <<= 1) {
+      ::sbc::KProbe kp_("k_lr_jump", st);
+      k_lr_jump<<<grid_for(nE, 256), 256, 0, st>>>(nE, nxA, SA, nxB, SB);
+      std::swap(nxA, nxB);
+      std::swap(SA, SB);
+    }
+    {
+      ::sbc::KProbe kp_("k_lr_check", st);
+      k_lr_check<<<grid_for(nE, 256), 256, 0, st>>>(nE, nxA, ringI, indeg, sc);
+    }
+    {
+      ::sbc::KProbe kp_("k_lr_ringlen", st);
+      k_lr_ringlen<<<grid_for(nRings + 1, 256), 256, 0, st>>>(nRings, starts, SA, rlen);
+    }
     exclusive_scan_i32(rlen, nRings + 1, sscr, st);
-    exclusive_scan_i32(rseg, nRings + 1, sscr, st);
-    int hv[2];
-    cudaMemcpyAsync(&hv[0], rlen + nRings, sizeof(int), cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(&hv[1], rseg + nRings, sizeof(int), cudaMemcpyDeviceToHost, st);
+    int hv = 0;
+    cudaMemcpyAsync(&hv, rlen + nRings, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(&h, sc, sizeof h, cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
     if (h.anomaly) return serial_backend(pl, m, out, ovTag);
-    const long long nv = hv[0];
-    const int nseg = hv[1];
-    int* segX = (int*)bp.get("bk_segX", sizeof(int) * (nseg + 1));
-    int* segOut = (int*)bp.get("bk_segOut", sizeof(int) * (nseg + 1));
+    const long long nv = hv;
     double* rxy = (double*)bp.get("bk_rxy", sizeof(double) * 2 * (nv + 1));
     if (bp.failed) return pl.fail(kENoMem, "device allocation failed (ring vertices)");
     {
-      ::sbc::KProbe kp_("k_tr_walk", st);
-      k_tr_walk<1><<<grid_for(nRings, 128), 128, 0, st>>>(T, nRings, starts, nullptr, nullptr, rlen,
-                                                        rseg, segX, segOut, sc);
-    }
-    if (nv > 0) {
-      {
-        ::sbc::KProbe kp_("k_tr_copy", st);
-        k_tr_copy<<<grid_for(nv, 256), 256, 0, st>>>(T, nv, nseg, segX, segOut, m.ixB, m.ixC, rxy);
-      }
+      ::sbc::KProbe kp_("k_lr_copy", st);
+      k_lr_copy<<<grid_for(nE, 128), 128, 0, st>>>(T, nxA, SA, ringI, isStart, rlen, m.ixB, m.ixC,
+                                                    rxy);
     }
     out.d_off = rlen;  // exclusive prefix of ring lengths, nRings+1 entries
     out.d_xy = rxy;

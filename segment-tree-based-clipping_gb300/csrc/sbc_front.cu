@@ -539,57 +539,61 @@ int Pipeline::stage_endlists() {
 }
 
 // ---------------------------------------------------------------- A7 cover lists
-// Edge::contains / Edge::intersects (edge.h:160-188) on the node interval
-__device__ __forceinline__ bool contains_node(double s, double x, double ns, double ne) {
-  return s <= ns && x >= ne;
-}
-__device__ __forceinline__ bool intersects_node(double s, double x, double cs, double ce) {
-  return (s <= cs && x >= ce) || (cs <= s && ce >= x) || (s <= cs && x >= cs) ||
-         (ce <= x && ce >= s);
-}
-
-// insertEdgeParallel as an explicit-stack pre-order descent (left child first)
+// insertEdgeParallel (oacc_segment_tree.cpp:2496-2564) adds an edge to node v
+// when v's interval lies inside the edge's [start, end] and recurses into the
+// children whose interval touches it.  A leaf q = [ea[q], ea[q+1]] lies inside
+// iff ea[q] >= start and ea[q+1] <= end; ea is sorted, so those leaves form
+// one range [l, r], every ancestor of a contained node touches the edge, and
+// the nodes the recursion adds are exactly the canonical decomposition of
+// [l, r] (maximal nodes inside it).  Two binary searches and the bottom-up
+// decomposition give them without the descent.
 template <bool EMIT>
 __global__ void k_cover(const double* __restrict__ es, const double* __restrict__ ee, int E,
-                        const double* __restrict__ ea, int logL, int ts, int* __restrict__ count,
+                        const double* __restrict__ ea, int logL, int* __restrict__ count,
                         const long long* __restrict__ off, unsigned* __restrict__ onode,
-                        unsigned* __restrict__ oedge, unsigned* __restrict__ flags) {
+                        unsigned* __restrict__ oedge) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
+  const int L = 1 << logL;
   double s = es[e], x = ee[e];
-  int stack[96];
-  int sp = 0;
-  stack[sp++] = 1;
+  int lo = 0, hi = L;  // l = first leaf with ea[q] >= s
+  while (lo < hi) {
+    int m = (lo + hi) >> 1;
+    if (ea[m] < s) lo = m + 1;
+    else hi = m;
+  }
+  int l = lo;
+  lo = 0;
+  hi = L;  // r+1 = first leaf with ea[q+1] > x
+  while (lo < hi) {
+    int m = (lo + hi) >> 1;
+    if (ea[m + 1] <= x) lo = m + 1;
+    else hi = m;
+  }
+  int r1 = lo;
   int n = 0;
   long long base = EMIT ? off[e] : 0;
-  while (sp > 0) {
-    int v = stack[--sp];
-    double ns, ne;
-    node_interval(ea, logL, v, &ns, &ne);
-    if (contains_node(s, x, ns, ne)) {
-      if (EMIT) {
-        onode[base + n] = (unsigned)v;
-        oedge[base + n] = (unsigned)e;
+  if (l < r1) {
+    int a = l + L, b = r1 + L;
+    while (a < b) {
+      if (a & 1) {
+        if (EMIT) {
+          onode[base + n] = (unsigned)a;
+          oedge[base + n] = (unsigned)e;
+        }
+        ++n;
+        ++a;
       }
-      ++n;
-      continue;
-    }
-    int c = 2 * v;
-    if (c + 1 < ts) {
-      double cs, ce;
-      node_interval(ea, logL, c + 1, &cs, &ce);
-      if (intersects_node(s, x, cs, ce)) {
-        if (sp < 96) stack[sp++] = c + 1;
-        else atomicOr(flags, (unsigned)kFlagOverflow);
+      if (b & 1) {
+        --b;
+        if (EMIT) {
+          onode[base + n] = (unsigned)b;
+          oedge[base + n] = (unsigned)e;
+        }
+        ++n;
       }
-    }
-    if (c < ts) {
-      double cs, ce;
-      node_interval(ea, logL, c, &cs, &ce);
-      if (intersects_node(s, x, cs, ce)) {
-        if (sp < 96) stack[sp++] = c;
-        else atomicOr(flags, (unsigned)kFlagOverflow);
-      }
+      a >>= 1;
+      b >>= 1;
     }
   }
   if (!EMIT) count[e] = n;
@@ -617,8 +621,8 @@ int Pipeline::stage_cover() {
   clear_flags();
   {
     ::sbc::KProbe kp_("k_cover", st_);
-    k_cover<false><<<grid_for(E, 128), 128, 0, st_>>>(e_s, e_e, E, ea, logL, ts, cnt, nullptr,
-                                                    nullptr, nullptr, d_flags);
+    k_cover<false><<<grid_for(E, 128), 128, 0, st_>>>(e_s, e_e, E, ea, logL, cnt, nullptr, nullptr,
+                                                    nullptr);
   }
   cudaMemsetAsync(cnt + E, 0, sizeof(int), st_);
   {
@@ -629,7 +633,6 @@ int Pipeline::stage_cover() {
   long long total = 0;
   cudaMemcpyAsync(&total, off + E, sizeof(long long), cudaMemcpyDeviceToHost, st_);
   cudaStreamSynchronize(st_);
-  if (read_flags() & kFlagOverflow) return fail(kEInternal, "cover descent stack overflow");
   if (total >= (1LL << 28)) return fail(kEInput, "more than 2^28 cover-list entries");
   nCover = total;
   cov_node = (unsigned*)pool_.get("cov_node", sizeof(unsigned) * (total + 1));
@@ -642,8 +645,8 @@ int Pipeline::stage_cover() {
   if (pool_.failed) return fail(kENoMem, "device allocation failed (cover entries)");
   {
     ::sbc::KProbe kp_("k_cover", st_);
-    k_cover<true><<<grid_for(E, 128), 128, 0, st_>>>(e_s, e_e, E, ea, logL, ts, nullptr, off,
-                                                   cov_node, cov_edge, d_flags);
+    k_cover<true><<<grid_for(E, 128), 128, 0, st_>>>(e_s, e_e, E, ea, logL, nullptr, off, cov_node,
+                                                   cov_edge);
   }
   int bits = 1;
   while ((1LL << bits) < ts) ++bits;

@@ -46,38 +46,7 @@ __device__ __forceinline__ void leaf_range(int v, int logL, int* lo, int* hi) {
   *hi = ((v + 1) << h) - 1 - L;
 }
 
-// ---------------------------------------------------------------- A8 work
-__global__ void k_cand_work(const unsigned* __restrict__ cov_node,
-                            const unsigned* __restrict__ cov_edge, long long nCover,
-                            const int* __restrict__ node_start, const int* __restrict__ node_end,
-                            const int* __restrict__ tstart, int k, int cType, int logL,
-                            int numLeaves, const int* __restrict__ le_off,
-                            long long* __restrict__ work, int* __restrict__ blk_s,
-                            int* __restrict__ wcc) {
-  long long P = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (P >= nCover) return;
-  int v = (int)cov_node[P];
-  int e = (int)cov_edge[P];
-  int t = class_of(tstart, k, e);
-  long long w = 0;
-  int bs = 0, nc = 0;
-  int lo, hi;
-  leaf_range(v, logL, &lo, &hi);
-  if (t == 0) {
-    int a = node_start[v], b = node_end[v];
-    bs = lower_bound_u32(cov_edge, a, b, (unsigned)tstart[cType]);
-    int be = lower_bound_u32(cov_edge, a, b, (unsigned)tstart[cType + 1]);
-    nc = be - bs;
-    size_t c = (size_t)cType * numLeaves;
-    w = nc + (le_off[c + hi + 1] - le_off[c + lo]);
-  } else if (t == cType) {
-    w = le_off[hi + 1] - le_off[lo];
-  }
-  work[P] = w;
-  blk_s[P] = bs;
-  wcc[P] = nc;
-}
-
+// ---------------------------------------------------------------- A8 candidates
 // LSMF bounding-box filter, oacc_segment_tree.cpp:5282-5316
 __device__ __forceinline__ bool lsmf(double p1x, double p1y, double p2x, double p2y, double q1x,
                                      double q1y, double q2x, double q2y) {
@@ -92,8 +61,6 @@ __device__ __forceinline__ bool lsmf(double p1x, double p1y, double p2x, double 
   return true;
 }
 
-constexpr int kChunk = 256;       // candidate units per chunk (8 rounds of 32 lanes)
-constexpr int kWarpChunks = 8;    // consecutive chunks per warp
 constexpr int kCandBlock = 256;
 
 // conservative float bounds of an edge's y extent (rounded outwards), one
@@ -123,128 +90,208 @@ __global__ void k_edge_ybox(int E, const int* __restrict__ e_id, const int* __re
   ab[e] = make_int2(aft[e], bef[e]);
 }
 
-__global__ void k_chunks(long long n, const long long* __restrict__ wscan,
-                         long long* __restrict__ chunks) {
-  long long P = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (P > n) return;
-  chunks[P] = P < n ? (wscan[P + 1] - wscan[P] + kChunk - 1) / kChunk : 0;
+// per node with cover entries: the candidate tiles of its three tile kinds
+//   kind 0: base cover entries x overlay cover entries of the same node
+//   kind 1: base cover entries x overlay end-list entries (class cType leaves)
+//   kind 2: overlay cover entries x base end-list entries (class 0 leaves)
+struct NodeTiles {
+  int s, e;        // cover entries [s, e) of the node
+  int nb;          // base cover entries [s, s+nb)
+  int bsT, ncT;    // overlay cover entries [bsT, bsT+ncT)
+  long long lbT, nT, lb0, n0;  // leaf-entry ranges of class cType and of class 0
+  int lo, hi;      // leaf range of the node
+};
+
+constexpr int kTile = 256;  // partners per tile (8 per lane)
+
+__device__ __forceinline__ NodeTiles node_tiles(int v, const int* node_start, const int* node_end,
+                                                const unsigned* cov_edge, const int* tstart,
+                                                int cType, int logL, int numLeaves,
+                                                const int* le_off) {
+  NodeTiles t;
+  t.s = node_start[v];
+  t.e = node_end[v];
+  t.nb = lower_bound_u32(cov_edge, t.s, t.e, (unsigned)tstart[1]) - t.s;
+  t.bsT = lower_bound_u32(cov_edge, t.s, t.e, (unsigned)tstart[cType]);
+  t.ncT = lower_bound_u32(cov_edge, t.s, t.e, (unsigned)tstart[cType + 1]) - t.bsT;
+  int d = 31 - __clz(v), h = logL - d, L = 1 << logL;
+  t.lo = (v << h) - L;
+  t.hi = ((v + 1) << h) - 1 - L;
+  size_t cT = (size_t)cType * numLeaves;
+  t.lbT = le_off[cT + t.lo];
+  t.nT = le_off[cT + t.hi + 1] - t.lbT;
+  t.lb0 = le_off[t.lo];
+  t.n0 = le_off[t.hi + 1] - t.lb0;
+  return t;
 }
 
-// Candidate tests.  Every partner in the same cover list or in the end list
-// of the node overlaps the cover edge in x (both span or touch the node's
-// interval), so the reference's LSMF box test reduces to the y test; a
-// conservative float y test (bounds rounded outwards) skips most partners
-// with one 16-byte load, and the exact FP64 LSMF and classification run on
-// the rest.  Each warp walks kWarpChunks consecutive chunks of 256 units.
+__device__ __forceinline__ long long tiles_of(long long n) { return (n + kTile - 1) / kTile; }
+
+__global__ void k_node_list(long long nCover, const unsigned* __restrict__ cov_node,
+                            const int* __restrict__ hpre, int* __restrict__ nodes) {
+  long long P = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (P >= nCover) return;
+  if (P == 0 || cov_node[P] != cov_node[P - 1]) nodes[hpre[P]] = (int)cov_node[P];
+}
+
+__global__ void k_node_heads(long long nCover, const unsigned* __restrict__ cov_node,
+                             int* __restrict__ h) {
+  long long P = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (P > nCover) return;
+  h[P] = (P < nCover && (P == 0 || cov_node[P] != cov_node[P - 1])) ? 1 : 0;
+}
+
+__global__ void k_node_items(int nNodes, const int* __restrict__ nodes,
+                             const int* __restrict__ node_start, const int* __restrict__ node_end,
+                             const unsigned* __restrict__ cov_edge, const int* __restrict__ tstart,
+                             int cType, int logL, int numLeaves, const int* __restrict__ le_off,
+                             long long* __restrict__ items, long long* __restrict__ wunits) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > nNodes) return;
+  if (i == nNodes) {
+    items[i] = 0;
+    wunits[i] = 0;
+    return;
+  }
+  NodeTiles t = node_tiles(nodes[i], node_start, node_end, cov_edge, tstart, cType, logL,
+                           numLeaves, le_off);
+  long long n = 0, w = 0;
+  if (t.nb > 0 && t.ncT > 0) n += tiles_of(t.ncT), w += (long long)t.nb * t.ncT;
+  if (t.nb > 0 && t.nT > 0) n += tiles_of(t.nT), w += (long long)t.nb * t.nT;
+  if (t.ncT > 0 && t.n0 > 0) n += tiles_of(t.n0), w += (long long)t.ncT * t.n0;
+  items[i] = n;
+  wunits[i] = w;
+}
+
+// Candidate tests by node tiles (saveIntersectionsIdsMulticore,
+// oacc_segment_tree.cpp:6118-6241, reordered).  A warp holds 256 partners of
+// one node in registers and sweeps the node's cover entries of the other
+// polygon over them, so an end list is read once per node instead of once
+// per cover entry.  Every partner in the same cover list or the end list of
+// the node overlaps the cover edge in x (both span or touch the node's
+// interval), so the LSMF box test reduces to the y test; a conservative float
+// y test (bounds rounded outwards) rejects most pairs from registers and the
+// exact FP64 LSMF and classification run on the rest.  Hits keep the
+// reference's emission key (cover position, phase, partner id).
 __global__ void __launch_bounds__(kCandBlock)
-k_cand_test(const long long* __restrict__ cscan, long long nCover, long long TC,
-            const long long* __restrict__ wscan, const unsigned* __restrict__ cov_node,
-            const unsigned* __restrict__ cov_edge, const int* __restrict__ blk_s,
-            const int* __restrict__ wcc, const int* __restrict__ tstart, int k, int cType,
-            int logL, int numLeaves, const int* __restrict__ le_off,
-            const int4* __restrict__ pack, const float2* __restrict__ ybox,
-            const int2* __restrict__ ab, const int* __restrict__ e_id,
-            const double* __restrict__ bP, const double* __restrict__ cP,
-            unsigned long long* __restrict__ counters, long long cap, int* __restrict__ rb,
-            int* __restrict__ rc, int* __restrict__ rt, unsigned long long* __restrict__ rkey) {
+k_cand_test(int nNodes, const int* __restrict__ nodes, const long long* __restrict__ items,
+            long long nItems, const int* __restrict__ node_start,
+            const int* __restrict__ node_end, const unsigned* __restrict__ cov_edge,
+            const int* __restrict__ tstart, int cType, int logL, int numLeaves,
+            const int* __restrict__ le_off, const int4* __restrict__ pack,
+            const float2* __restrict__ ybox, const int2* __restrict__ ab,
+            const int* __restrict__ e_id, const double* __restrict__ bP,
+            const double* __restrict__ cP, unsigned long long* __restrict__ counters,
+            long long cap, int* __restrict__ rb, int* __restrict__ rc, int* __restrict__ rt,
+            unsigned long long* __restrict__ rkey) {
   const int lane = threadIdx.x & 31;
-  const unsigned lt = (1u << lane) - 1u;
-  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long c0 = warp * kWarpChunks;
-  if (c0 >= TC) return;  // warp-uniform
-  const long long c1 = min(c0 + (long long)kWarpChunks, TC);
-  const int L = 1 << logL;
-  long long P;
+  const long long it = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (it >= nItems) return;  // warp-uniform
+  int ni;
   {
-    long long lo = 0, hi = nCover;  // last P with cscan[P] <= c0
+    int lo = 0, hi = nNodes;  // last node with items[ni] <= it
     while (hi - lo > 1) {
-      long long m = (lo + hi) >> 1;
-      if (cscan[m] <= c0) lo = m;
+      int m = (lo + hi) >> 1;
+      if (items[m] <= it) lo = m;
       else hi = m;
     }
-    P = lo;
+    ni = lo;
   }
-  unsigned tested = 0;
-  for (long long c = c0; c < c1; ++c) {
-    while (cscan[P + 1] <= c) ++P;
-    const long long j0 = (c - cscan[P]) * kChunk;
-    const long long w = wscan[P + 1] - wscan[P];
-    const int self = (int)cov_edge[P];
-    const int v = (int)cov_node[P];
-    const int tself = class_of(tstart, k, self);
-    const int nc = wcc[P], bs = blk_s[P];
-    int lo = 0, hi = 0;
-    {
-      int d = 31 - __clz(v), h = logL - d;
-      lo = (v << h) - L;
-      hi = ((v + 1) << h) - 1 - L;
+  const int v = nodes[ni];
+  const NodeTiles t = node_tiles(v, node_start, node_end, cov_edge, tstart, cType, logL,
+                                 numLeaves, le_off);
+  long long tile = it - items[ni];
+  int kind = 0;
+  long long n0 = (t.nb > 0 && t.ncT > 0) ? tiles_of(t.ncT) : 0;
+  long long n1 = (t.nb > 0 && t.nT > 0) ? tiles_of(t.nT) : 0;
+  if (tile >= n0) {
+    tile -= n0;
+    kind = 1;
+    if (tile >= n1) {
+      tile -= n1;
+      kind = 2;
     }
-    const long long lbase = le_off[(size_t)(tself == 0 ? cType : 0) * numLeaves + lo];
-    const float2 sb = ybox[self];
-    const int sid = e_id[self];
-    const double* sp = (tself == 0 ? bP : cP) + sid;
-    for (int r = 0; r < kChunk / 32; ++r) {
-      const long long j = j0 + r * 32 + lane;
-      bool hit = false;
-      int bId = 0, cId = 0, ty = 0;
-      unsigned long long key = 0;
-      if (j < w) {
-        int partner = -1, phase = 0;
-        bool pass;
-        if (j < nc) {
-          partner = (int)cov_edge[bs + j];
-          float2 pbx = ybox[partner];
-          pass = !(sb.x > pbx.y || sb.y < pbx.x);
-        } else {
-          phase = 1;
-          int4 q = pack[lbase + (j - nc)];
-          partner = q.x;
-          pass = !(sb.x > __int_as_float(q.w) || sb.y < __int_as_float(q.z));
-          if (pass) {
-            // the edge's other leaf entry in this subtree comes first: an end
-            // list holds each edge once
-            int2 o = ab[partner];
-            int leaf = q.y + L;
-            int other = (o.x == leaf) ? o.y : o.x;
-            if (other >= 0 && other >= lo + L && other <= hi + L && other < leaf) pass = false;
-          }
-        }
-        if (pass) {
-          const int pid = e_id[partner];
-          const double* pp = (tself == 0 ? cP : bP) + pid;
-          const double* pbp = tself == 0 ? sp : pp;
-          const double* pcp = tself == 0 ? pp : sp;
-          double p1x = pbp[0], p1y = pbp[1], p2x = pbp[2], p2y = pbp[3];
-          double q1x = pcp[0], q1y = pcp[1], q2x = pcp[2], q2y = pcp[3];
-          if (lsmf(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y)) {
-            ++tested;
-            double al, be;
-            ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &be);
-            if (ty) {
-              hit = true;
-              bId = tself == 0 ? sid : pid;
-              cId = tself == 0 ? pid : sid;
-              key = ((unsigned long long)P << 36) | ((unsigned long long)phase << 35) |
-                    (unsigned long long)(pid >> 1);
-            }
-          }
+  }
+  const int L = 1 << logL;
+  // ---- the tile's partners, 8 per lane
+  const long long pbase = tile * kTile;
+  const long long pcount = kind == 0 ? t.ncT : (kind == 1 ? t.nT : t.n0);
+  int pe[8];
+  float py0[8], py1[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    long long j = pbase + q * 32 + lane;
+    pe[q] = -1;
+    py0[q] = 1.0f;
+    py1[q] = -1.0f;  // empty box: never overlaps
+    if (j < pcount) {
+      if (kind == 0) {
+        int e = (int)cov_edge[t.bsT + j];
+        float2 bx = ybox[e];
+        pe[q] = e;
+        py0[q] = bx.x;
+        py1[q] = bx.y;
+      } else {
+        int4 r = pack[(kind == 1 ? t.lbT : t.lb0) + j];
+        int2 o = ab[r.x];
+        int leaf = r.y + L;
+        int other = (o.x == leaf) ? o.y : o.x;
+        // the edge's other leaf entry in this subtree comes first: an end list
+        // holds each edge once
+        bool dup = other >= 0 && other >= t.lo + L && other <= t.hi + L && other < leaf;
+        if (!dup) {
+          pe[q] = r.x;
+          py0[q] = __int_as_float(r.z);
+          py1[q] = __int_as_float(r.w);
         }
       }
-      unsigned m = __ballot_sync(0xffffffffu, hit);
-      if (m) {
-        int leader = __ffs(m) - 1;
-        unsigned long long base = 0;
-        if (lane == leader) base = atomicAdd(&counters[0], (unsigned long long)__popc(m));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (hit) {
-          long long idx = (long long)base + __popc(m & lt);
-          if (idx < cap) {
-            rb[idx] = bId;
-            rc[idx] = cId;
-            rt[idx] = ty;
-            rkey[idx] = key;
-          }
-        }
+    }
+  }
+  // ---- sweep the node's cover entries of the other polygon
+  const int cs = kind == 2 ? t.bsT : t.s;
+  const int cn = kind == 2 ? t.ncT : t.nb;
+  const bool selfBase = kind != 2;
+  const int phase = kind == 0 ? 0 : 1;
+  const double* selfPoly = selfBase ? bP : cP;
+  const double* partPoly = selfBase ? cP : bP;
+  unsigned tested = 0;
+  for (int ci = 0; ci < cn; ++ci) {
+    const int P = cs + ci;
+    const int self = (int)cov_edge[P];
+    const float2 sb = ybox[self];
+    unsigned m = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (!(sb.x > py1[q] || sb.y < py0[q])) m |= 1u << q;
+    if (!m) continue;
+    const int sid = e_id[self];
+    const double* sp = selfPoly + sid;
+    const double s1x = sp[0], s1y = sp[1], s2x = sp[2], s2y = sp[3];
+    while (m) {
+      int q = __ffs(m) - 1;
+      m &= m - 1;
+      int pid = e_id[pe[q]];
+      const double* pp = partPoly + pid;
+      double p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y;
+      if (selfBase) {
+        p1x = s1x; p1y = s1y; p2x = s2x; p2y = s2y;
+        q1x = pp[0]; q1y = pp[1]; q2x = pp[2]; q2y = pp[3];
+      } else {
+        p1x = pp[0]; p1y = pp[1]; p2x = pp[2]; p2y = pp[3];
+        q1x = s1x; q1y = s1y; q2x = s2x; q2y = s2y;
+      }
+      if (!lsmf(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y)) continue;
+      ++tested;
+      double al, be;
+      int ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &be);
+      if (!ty) continue;
+      unsigned long long idx = atomicAdd(&counters[0], 1ull);
+      if ((long long)idx < cap) {
+        rb[idx] = selfBase ? sid : pid;
+        rc[idx] = selfBase ? pid : sid;
+        rt[idx] = ty;
+        rkey[idx] = ((unsigned long long)P << 36) | ((unsigned long long)phase << 35) |
+                    (unsigned long long)(pid >> 1);
       }
     }
   }
@@ -558,32 +605,16 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
   int* tstart = (int*)pool_.get("type_start", sizeof(int) * (k + 2));
   cudaMemcpyAsync(tstart, hstart.data(), sizeof(int) * (k + 2), cudaMemcpyHostToDevice, st);
 
-  // ---- A8 candidate work per cover entry
-  long long* work = (long long*)pool_.get("cand_work", sizeof(long long) * (nCover + 1));
-  int* blk_s = (int*)pool_.get("cand_blk", sizeof(int) * (nCover + 1));
-  int* wcc = (int*)pool_.get("cand_wcc", sizeof(int) * (nCover + 1));
-  void* sscr = pool_.get("scan_scr4", scan_scratch_bytes(nCover + 1));
+  // ---- A8 candidate tests
+  void* sscr = pool_.get("scan_scr4", scan_scratch_bytes(nCover + 2));
   auto* counters = (unsigned long long*)pool_.get("cand_counters", 64);
   if (pool_.failed) return fail(kENoMem, "device allocation failed (candidates)");
-  if (nCover > 0) {
-    {
-      ::sbc::KProbe kp_("k_cand_work", st);
-      k_cand_work<<<grid_for(nCover, 256), 256, 0, st>>>(cov_node, cov_edge, nCover, node_start,
-                                                       node_end, tstart, k, cType, logL,
-                                                       numLeaves, le_off, work, blk_s, wcc);
-    }
-  }
-  cudaMemsetAsync(work + nCover, 0, sizeof(long long), st);
-  exclusive_scan_i64(work, nCover + 1, sscr, st);
   long long W = 0;
-  cudaMemcpyAsync(&W, work + nCover, sizeof(long long), cudaMemcpyDeviceToHost, st);
-  cudaStreamSynchronize(st);
-
-  // packed leaf entries, edge y boxes and chunk prefix for the test kernel
+  // packed leaf entries, edge y boxes and the node tiles of the test kernel
   int4* pack = (int4*)pool_.get("cand_pack", sizeof(int4) * (nLeafEnt + 1));
   float2* ybox = (float2*)pool_.get("cand_ybox", sizeof(float2) * (E + 1));
   int2* abx = (int2*)pool_.get("cand_ab", sizeof(int2) * (E + 1));
-  long long* cscan = (long long*)pool_.get("cand_cscan", sizeof(long long) * (nCover + 1));
+  int* nheads = (int*)pool_.get("cand_nheads", sizeof(int) * (nCover + 2));
   if (pool_.failed) return fail(kENoMem, "device allocation failed (candidate tables)");
   if (cType == 1) {
     if (nLeafEnt > 0) {
@@ -595,12 +626,32 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
     k_edge_ybox<<<grid_for(E, 256), 256, 0, st>>>(E, e_id, tstart, k, bP, cP, ybox, abx, aft, bef);
   }
   {
-    ::sbc::KProbe kp_("k_chunks", st);
-    k_chunks<<<grid_for(nCover + 1, 256), 256, 0, st>>>(nCover, work, cscan);
+    ::sbc::KProbe kp_("k_node_heads", st);
+    k_node_heads<<<grid_for(nCover + 1, 256), 256, 0, st>>>(nCover, cov_node, nheads);
   }
-  exclusive_scan_i64(cscan, nCover + 1, sscr, st);
-  long long TC = 0;
-  cudaMemcpyAsync(&TC, cscan + nCover, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  exclusive_scan_i32(nheads, nCover + 1, sscr, st);
+  int nNodes = 0;
+  cudaMemcpyAsync(&nNodes, nheads + nCover, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  int* nodes = (int*)pool_.get("cand_nodes", sizeof(int) * (nNodes + 1));
+  long long* items = (long long*)pool_.get("cand_items", sizeof(long long) * (nNodes + 1));
+  long long* wun = (long long*)pool_.get("cand_wunits", sizeof(long long) * (nNodes + 1));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (candidate nodes)");
+  if (nCover > 0) {
+    ::sbc::KProbe kp_("k_node_list", st);
+    k_node_list<<<grid_for(nCover, 256), 256, 0, st>>>(nCover, cov_node, nheads, nodes);
+  }
+  {
+    ::sbc::KProbe kp_("k_node_items", st);
+    k_node_items<<<grid_for(nNodes + 1, 256), 256, 0, st>>>(nNodes, nodes, node_start, node_end,
+                                                          cov_edge, tstart, cType, logL, numLeaves,
+                                                          le_off, items, wun);
+  }
+  exclusive_scan_i64(items, nNodes + 1, sscr, st);
+  exclusive_scan_i64(wun, nNodes + 1, sscr, st);
+  long long nItems = 0;
+  cudaMemcpyAsync(&nItems, items + nNodes, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(&W, wun + nNodes, sizeof(long long), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
 
   long long cap = 4LL * E + (1 << 20);
@@ -614,11 +665,10 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
     rkey = (unsigned long long*)pool_.get("raw_key", sizeof(unsigned long long) * cap);
     if (pool_.failed) return fail(kENoMem, "device allocation failed (raw candidates)");
     cudaMemsetAsync(counters, 0, 16, st);
-    if (TC > 0) {
-      long long warps = (TC + kWarpChunks - 1) / kWarpChunks;
+    if (nItems > 0) {
       ::sbc::KProbe kp_("k_cand_test", st);
-      k_cand_test<<<grid_for(warps * 32, kCandBlock), kCandBlock, 0, st>>>(
-          cscan, nCover, TC, work, cov_node, cov_edge, blk_s, wcc, tstart, k, cType, logL,
+      k_cand_test<<<grid_for(nItems * 32, kCandBlock), kCandBlock, 0, st>>>(
+          nNodes, nodes, items, nItems, node_start, node_end, cov_edge, tstart, cType, logL,
           numLeaves, le_off, pack, ybox, abx, e_id, bP, cP, counters, cap, rb, rc, rt, rkey);
     }
     unsigned long long hc[2];
