@@ -312,6 +312,13 @@ __global__ void k_lr_init(Trace T, const int* __restrict__ mval, int* __restrict
   int x = blockIdx.x * blockDim.x + threadIdx.x;
   int n = T.cP + T.cQ;
   if (x >= n) return;
+  if (mval[x] < 0 || mval[x] >= T.nB) {  // every ring holds a P crossing vertex
+    atomicOr(&sc->anomaly, 2048u);
+    ringI[x] = x;
+    nxt[x] = -1;
+    S[x] = 0;
+    return;
+  }
   int I = T.rankP[mval[x]];
   int t = tr_target(T, x);
   int s = tr_jump(T, t);

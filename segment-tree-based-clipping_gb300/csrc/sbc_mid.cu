@@ -222,8 +222,8 @@ k_cand_test(int nNodes, const int* __restrict__ nodes, const long long* __restri
   for (int q = 0; q < 8; ++q) {
     long long j = pbase + q * 32 + lane;
     pe[q] = -1;
-    py0[q] = 1.0f;
-    py1[q] = -1.0f;  // empty box: never overlaps
+    py0[q] = __int_as_float(0x7f800000);   // +inf
+    py1[q] = __int_as_float(0xff800000);   // -inf: overlaps no finite box
     if (j < pcount) {
       if (kind == 0) {
         int e = (int)cov_edge[t.bsT + j];
@@ -262,7 +262,7 @@ k_cand_test(int nNodes, const int* __restrict__ nodes, const long long* __restri
     unsigned m = 0;
 #pragma unroll
     for (int q = 0; q < 8; ++q)
-      if (!(sb.x > py1[q] || sb.y < py0[q])) m |= 1u << q;
+      if (pe[q] >= 0 && !(sb.x > py1[q] || sb.y < py0[q])) m |= 1u << q;
     if (!m) continue;
     const int sid = e_id[self];
     const double* sp = selfPoly + sid;
