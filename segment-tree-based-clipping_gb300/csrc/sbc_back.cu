@@ -326,9 +326,6 @@ __global__ void k_lr_init(Trace T, const int* __restrict__ mval, int* __restrict
   nxt[x] = (s == I) ? -1 : s;
   S[x] = tr_len(T, x, t);
   if (s >= 0) atomicAdd(&indeg[s], 1);
-  // a segment ending at the ring's start vertex itself stops the reference's
-  // walk early: not covered here
-  if (t == I) atomicOr(&sc->anomaly, 256u);
 }
 
 __global__ void k_lr_jump(int n, const int* __restrict__ nin, const long long* __restrict__ Sin,
@@ -345,13 +342,17 @@ __global__ void k_lr_jump(int n, const int* __restrict__ nin, const long long* _
   }
 }
 
-// succ must be a permutation and every ring start must reach its orbit's end
-__global__ void k_lr_check(int n, const int* __restrict__ nxt, const int* __restrict__ ringI,
+// succ must be a permutation, every ring start must reach its orbit's end,
+// and no segment of a start's orbit may end at the start vertex itself (that
+// stops the reference's walk early; the serial path covers it)
+__global__ void k_lr_check(Trace T, const int* __restrict__ nxt, const int* __restrict__ ringI,
                            const int* __restrict__ indeg, BkScalars* sc) {
   int x = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = T.cP + T.cQ;
   if (x >= n) return;
   if (indeg[x] != 1) atomicOr(&sc->anomaly, 512u);
   if (ringI[x] == x && nxt[x] != -1) atomicOr(&sc->anomaly, 1024u);
+  if (nxt[x] == -1 && tr_target(T, x) == ringI[x]) atomicOr(&sc->anomaly, 256u);
 }
 
 __global__ void k_lr_ringlen(int nRings, const int* __restrict__ starts,
@@ -1296,7 +1297,7 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
     }
     {
       ::sbc::KProbe kp_("k_lr_check", st);
-      k_lr_check<<<grid_for(nE, 256), 256, 0, st>>>(nE, nxA, ringI, indeg, sc);
+      k_lr_check<<<grid_for(nE, 256), 256, 0, st>>>(T, nxA, ringI, indeg, sc);
     }
     {
       ::sbc::KProbe kp_("k_lr_ringlen", st);
