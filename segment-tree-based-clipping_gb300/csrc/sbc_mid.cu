@@ -163,16 +163,17 @@ __global__ void k_node_items(int nNodes, const int* __restrict__ nodes,
   wunits[i] = w;
 }
 
-// Candidate tests by node tiles (saveIntersectionsIdsMulticore,
+// Candidate filter by node tiles (saveIntersectionsIdsMulticore,
 // oacc_segment_tree.cpp:6118-6241, reordered).  A warp holds 256 partners of
 // one node in registers and sweeps the node's cover entries of the other
 // polygon over them, so an end list is read once per node instead of once
 // per cover entry.  Every partner in the same cover list or the end list of
 // the node overlaps the cover edge in x (both span or touch the node's
 // interval), so the LSMF box test reduces to the y test; a conservative float
-// y test (bounds rounded outwards) rejects most pairs from registers and the
-// exact FP64 LSMF and classification run on the rest.  Hits keep the
-// reference's emission key (cover position, phase, partner id).
+// y test (bounds rounded outwards) rejects most pairs from registers.  The
+// rest are compacted warp-wide into a survivor list for k_cand_exact (FP64
+// work in full warps: the FP64 pipe costs the same per warp instruction
+// however few lanes are active).
 __global__ void __launch_bounds__(kCandBlock)
 k_cand_test(int nNodes, const int* __restrict__ nodes, const long long* __restrict__ items,
             long long nItems, const int* __restrict__ node_start,
@@ -180,10 +181,7 @@ k_cand_test(int nNodes, const int* __restrict__ nodes, const long long* __restri
             const int* __restrict__ tstart, int cType, int logL, int numLeaves,
             const int* __restrict__ le_off, const int4* __restrict__ pack,
             const float2* __restrict__ ybox, const int2* __restrict__ ab,
-            const int* __restrict__ e_id, const double* __restrict__ bP,
-            const double* __restrict__ cP, unsigned long long* __restrict__ counters,
-            long long cap, int* __restrict__ rb, int* __restrict__ rc, int* __restrict__ rt,
-            unsigned long long* __restrict__ rkey) {
+            unsigned long long* __restrict__ counters, long long scap, int2* __restrict__ surv) {
   const int lane = threadIdx.x & 31;
   const long long it = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (it >= nItems) return;  // warp-uniform
@@ -247,56 +245,97 @@ k_cand_test(int nNodes, const int* __restrict__ nodes, const long long* __restri
       }
     }
   }
-  // ---- sweep the node's cover entries of the other polygon
+  // ---- sweep the node's cover entries of the other polygon; survivors of the
+  // float y test are appended as (cover position, partner | kind << 30)
   const int cs = kind == 2 ? t.bsT : t.s;
   const int cn = kind == 2 ? t.ncT : t.nb;
-  const bool selfBase = kind != 2;
-  const int phase = kind == 0 ? 0 : 1;
-  const double* selfPoly = selfBase ? bP : cP;
-  const double* partPoly = selfBase ? cP : bP;
-  unsigned tested = 0;
+  const unsigned lt = (1u << lane) - 1u;
   for (int ci = 0; ci < cn; ++ci) {
     const int P = cs + ci;
-    const int self = (int)cov_edge[P];
-    const float2 sb = ybox[self];
+    const float2 sb = ybox[cov_edge[P]];
     unsigned m = 0;
 #pragma unroll
     for (int q = 0; q < 8; ++q)
       if (pe[q] >= 0 && !(sb.x > py1[q] || sb.y < py0[q])) m |= 1u << q;
-    if (!m) continue;
-    const int sid = e_id[self];
-    const double* sp = selfPoly + sid;
-    const double s1x = sp[0], s1y = sp[1], s2x = sp[2], s2y = sp[3];
+    int cnt = __popc(m);
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0) continue;
+    unsigned long long base = 0;
+    if (lane == 31) base = atomicAdd(&counters[2], (unsigned long long)total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    long long w = (long long)base + incl - cnt;
     while (m) {
       int q = __ffs(m) - 1;
       m &= m - 1;
-      int pid = e_id[pe[q]];
-      const double* pp = partPoly + pid;
-      double p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y;
-      if (selfBase) {
-        p1x = s1x; p1y = s1y; p2x = s2x; p2y = s2y;
-        q1x = pp[0]; q1y = pp[1]; q2x = pp[2]; q2y = pp[3];
-      } else {
-        p1x = pp[0]; p1y = pp[1]; p2x = pp[2]; p2y = pp[3];
-        q1x = s1x; q1y = s1y; q2x = s2x; q2y = s2y;
-      }
-      if (!lsmf(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y)) continue;
-      ++tested;
+      if (w < scap) surv[w] = make_int2(P, pe[q] | (kind << 30));
+      ++w;
+    }
+    (void)lt;
+  }
+}
+
+// exact LSMF and classification of the filtered pairs, one per thread
+__global__ void __launch_bounds__(256)
+k_cand_exact(long long n, const int2* __restrict__ surv, const unsigned* __restrict__ cov_edge,
+             const int* __restrict__ e_id, const double* __restrict__ bP,
+             const double* __restrict__ cP, unsigned long long* __restrict__ counters,
+             long long cap, int* __restrict__ rb, int* __restrict__ rc, int* __restrict__ rt,
+             unsigned long long* __restrict__ rkey) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  bool hit = false, tested = false;
+  int bId = 0, cId = 0, ty = 0;
+  unsigned long long key = 0;
+  if (i < n) {
+    int2 sv = surv[i];
+    const int P = sv.x;
+    const int partner = sv.y & 0x3fffffff;
+    const int kind = (unsigned)sv.y >> 30;
+    const bool selfBase = kind != 2;
+    const int sid = e_id[cov_edge[P]];
+    const int pid = e_id[partner];
+    bId = selfBase ? sid : pid;
+    cId = selfBase ? pid : sid;
+    const double* pb = bP + bId;
+    const double* pc = cP + cId;
+    double p1x = pb[0], p1y = pb[1], p2x = pb[2], p2y = pb[3];
+    double q1x = pc[0], q1y = pc[1], q2x = pc[2], q2y = pc[3];
+    if (lsmf(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y)) {
+      tested = true;
       double al, be;
-      int ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &be);
-      if (!ty) continue;
-      unsigned long long idx = atomicAdd(&counters[0], 1ull);
-      if ((long long)idx < cap) {
-        rb[idx] = selfBase ? sid : pid;
-        rc[idx] = selfBase ? pid : sid;
-        rt[idx] = ty;
-        rkey[idx] = ((unsigned long long)P << 36) | ((unsigned long long)phase << 35) |
-                    (unsigned long long)(pid >> 1);
+      ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &be);
+      if (ty) {
+        hit = true;
+        key = ((unsigned long long)P << 36) | ((unsigned long long)(kind == 0 ? 0 : 1) << 35) |
+              (unsigned long long)(pid >> 1);
       }
     }
   }
-  for (int s = 16; s > 0; s >>= 1) tested += __shfl_xor_sync(0xffffffffu, tested, s);
-  if (lane == 0 && tested) atomicAdd(&counters[1], (unsigned long long)tested);
+  unsigned tm = __ballot_sync(0xffffffffu, tested);
+  unsigned m = __ballot_sync(0xffffffffu, hit);
+  if (lane == 0 && tm) atomicAdd(&counters[1], (unsigned long long)__popc(tm));
+  if (m) {
+    int leader = __ffs(m) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(&counters[0], (unsigned long long)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (hit) {
+      long long idx = (long long)base + __popc(m & lt);
+      if (idx < cap) {
+        rb[idx] = bId;
+        rc[idx] = cId;
+        rt[idx] = ty;
+        rkey[idx] = key;
+      }
+    }
+  }
 }
 
 // ---------------------------------------------------------------- A9 dedup
@@ -654,31 +693,51 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
   cudaMemcpyAsync(&W, wun + nNodes, sizeof(long long), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
 
-  long long cap = 4LL * E + (1 << 20);
-  long long nraw = 0, ntested = 0;
-  int *rb = nullptr, *rc = nullptr, *rt = nullptr;
-  unsigned long long* rkey = nullptr;
+  // filter: node tiles -> survivor pairs (grow and retry on overflow)
+  long long scap = sv_cap_ > 0 ? sv_cap_ : 8LL * E + (1 << 20);
+  long long nsurv = 0;
+  int2* surv = nullptr;
+  auto* counters3 = counters;
   for (int attempt = 0; attempt < 2; ++attempt) {
-    rb = (int*)pool_.get("raw_b", sizeof(int) * cap);
-    rc = (int*)pool_.get("raw_c", sizeof(int) * cap);
-    rt = (int*)pool_.get("raw_t", sizeof(int) * cap);
-    rkey = (unsigned long long*)pool_.get("raw_key", sizeof(unsigned long long) * cap);
-    if (pool_.failed) return fail(kENoMem, "device allocation failed (raw candidates)");
-    cudaMemsetAsync(counters, 0, 16, st);
+    surv = (int2*)pool_.get("cand_surv", sizeof(int2) * (scap + 1));
+    if (pool_.failed) return fail(kENoMem, "device allocation failed (candidate survivors)");
+    cudaMemsetAsync(counters3, 0, 24, st);
     if (nItems > 0) {
       ::sbc::KProbe kp_("k_cand_test", st);
       k_cand_test<<<grid_for(nItems * 32, kCandBlock), kCandBlock, 0, st>>>(
           nNodes, nodes, items, nItems, node_start, node_end, cov_edge, tstart, cType, logL,
-          numLeaves, le_off, pack, ybox, abx, e_id, bP, cP, counters, cap, rb, rc, rt, rkey);
+          numLeaves, le_off, pack, ybox, abx, counters3, scap, surv);
     }
-    unsigned long long hc[2];
-    cudaMemcpyAsync(hc, counters, 16, cudaMemcpyDeviceToHost, st);
+    unsigned long long hs = 0;
+    cudaMemcpyAsync(&hs, counters3 + 2, sizeof(hs), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
-    nraw = (long long)hc[0];
-    ntested = (long long)hc[1];
-    if (nraw <= cap) break;
-    cap = nraw + (1 << 20);
+    nsurv = (long long)hs;
+    if (nsurv <= scap) break;
+    scap = nsurv + (1 << 20);
   }
+  sv_cap_ = scap;
+  // exact LSMF + classification of the survivors
+  long long cap = 4LL * E + (1 << 20);
+  if (cap > nsurv + 1) cap = nsurv + 1;
+  int *rb = nullptr, *rc = nullptr, *rt = nullptr;
+  unsigned long long* rkey = nullptr;
+  rb = (int*)pool_.get("raw_b", sizeof(int) * cap);
+  rc = (int*)pool_.get("raw_c", sizeof(int) * cap);
+  rt = (int*)pool_.get("raw_t", sizeof(int) * cap);
+  rkey = (unsigned long long*)pool_.get("raw_key", sizeof(unsigned long long) * cap);
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (raw candidates)");
+  if (nsurv > 0) {
+    ::sbc::KProbe kp_("k_cand_exact", st);
+    k_cand_exact<<<grid_for(nsurv, 256), 256, 0, st>>>(nsurv, surv, cov_edge, e_id, bP, cP,
+                                                       counters3, cap, rb, rc, rt, rkey);
+  }
+  unsigned long long hcnt[2];
+  cudaMemcpyAsync(hcnt, counters3, 16, cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  long long nraw = (long long)hcnt[0];
+  long long ntested = (long long)hcnt[1];
+  if (nraw > cap) return fail(kEInternal, "candidate hit buffer overflow");
+  out.survivors = nsurv;
   if (nraw >= (1LL << 31)) return fail(kEInput, "too many candidate hits");
   out.raw_hits = nraw;
   out.tests = ntested;

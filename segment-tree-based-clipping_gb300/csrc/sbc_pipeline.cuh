@@ -37,7 +37,7 @@ struct OverlayOut {
   int* d_off = nullptr;     // nrings+1 vertex offsets
   double* d_xy = nullptr;   // 2*nverts
   // diagnostics
-  long long raw_hits = 0, tests = 0, unique = 0, slots_b = 0, slots_c = 0, work = 0;
+  long long raw_hits = 0, tests = 0, unique = 0, slots_b = 0, slots_c = 0, work = 0, survivors = 0;
   int slow_path = 0;
 };
 
@@ -62,6 +62,7 @@ class Pipeline {
   long long stat_edges = 0, stat_epc = 0, stat_ts = 0, stat_cover = 0, stat_leaf = 0;
   // force the serial emulation of the back end (test hook)
   int force_serial_backend = 0;
+  long long sv_cap_ = 0;  // survivor buffer size that sufficed last time
 
   // ---- shared state (public for the stage kernels' launchers) ----
   int nb = 0, k = 0, clSize = 0, E = 0;
