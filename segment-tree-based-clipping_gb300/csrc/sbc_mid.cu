@@ -102,7 +102,8 @@ struct NodeTiles {
   int lo, hi;      // leaf range of the node
 };
 
-constexpr int kTile = 256;  // partners per tile (8 per lane)
+constexpr int kTile = 256;   // partners per tile (8 per lane)
+constexpr int kCTile = 1024; // cover entries per tile
 
 __device__ __forceinline__ NodeTiles node_tiles(int v, const int* node_start, const int* node_end,
                                                 const unsigned* cov_edge, const int* tstart,
@@ -126,6 +127,7 @@ __device__ __forceinline__ NodeTiles node_tiles(int v, const int* node_start, co
 }
 
 __device__ __forceinline__ long long tiles_of(long long n) { return (n + kTile - 1) / kTile; }
+__device__ __forceinline__ long long ctiles_of(long long n) { return (n + kCTile - 1) / kCTile; }
 
 __global__ void k_node_list(long long nCover, const unsigned* __restrict__ cov_node,
                             const int* __restrict__ hpre, int* __restrict__ nodes) {
@@ -156,9 +158,9 @@ __global__ void k_node_items(int nNodes, const int* __restrict__ nodes,
   NodeTiles t = node_tiles(nodes[i], node_start, node_end, cov_edge, tstart, cType, logL,
                            numLeaves, le_off);
   long long n = 0, w = 0;
-  if (t.nb > 0 && t.ncT > 0) n += tiles_of(t.ncT), w += (long long)t.nb * t.ncT;
-  if (t.nb > 0 && t.nT > 0) n += tiles_of(t.nT), w += (long long)t.nb * t.nT;
-  if (t.ncT > 0 && t.n0 > 0) n += tiles_of(t.n0), w += (long long)t.ncT * t.n0;
+  if (t.nb > 0 && t.ncT > 0) n += tiles_of(t.ncT) * ctiles_of(t.nb), w += (long long)t.nb * t.ncT;
+  if (t.nb > 0 && t.nT > 0) n += tiles_of(t.nT) * ctiles_of(t.nb), w += (long long)t.nb * t.nT;
+  if (t.ncT > 0 && t.n0 > 0) n += tiles_of(t.n0) * ctiles_of(t.ncT), w += (long long)t.ncT * t.n0;
   items[i] = n;
   wunits[i] = w;
 }
@@ -200,8 +202,8 @@ k_cand_test(int nNodes, const int* __restrict__ nodes, const long long* __restri
                                  numLeaves, le_off);
   long long tile = it - items[ni];
   int kind = 0;
-  long long n0 = (t.nb > 0 && t.ncT > 0) ? tiles_of(t.ncT) : 0;
-  long long n1 = (t.nb > 0 && t.nT > 0) ? tiles_of(t.nT) : 0;
+  long long n0 = (t.nb > 0 && t.ncT > 0) ? tiles_of(t.ncT) * ctiles_of(t.nb) : 0;
+  long long n1 = (t.nb > 0 && t.nT > 0) ? tiles_of(t.nT) * ctiles_of(t.nb) : 0;
   if (tile >= n0) {
     tile -= n0;
     kind = 1;
@@ -210,6 +212,10 @@ k_cand_test(int nNodes, const int* __restrict__ nodes, const long long* __restri
       kind = 2;
     }
   }
+  // 2-D tile: partner tile x cover tile
+  const long long ptiles = tiles_of(kind == 0 ? t.ncT : (kind == 1 ? t.nT : t.n0));
+  const long long ctile = tile / ptiles;
+  tile -= ctile * ptiles;
   const int L = 1 << logL;
   // ---- the tile's partners, 8 per lane
   const long long pbase = tile * kTile;
@@ -247,36 +253,43 @@ k_cand_test(int nNodes, const int* __restrict__ nodes, const long long* __restri
   }
   // ---- sweep the node's cover entries of the other polygon; survivors of the
   // float y test are appended as (cover position, partner | kind << 30)
-  const int cs = kind == 2 ? t.bsT : t.s;
-  const int cn = kind == 2 ? t.ncT : t.nb;
-  const unsigned lt = (1u << lane) - 1u;
-  for (int ci = 0; ci < cn; ++ci) {
-    const int P = cs + ci;
-    const float2 sb = ybox[cov_edge[P]];
-    unsigned m = 0;
+  const int cs0 = kind == 2 ? t.bsT : t.s;
+  const int cnAll = kind == 2 ? t.ncT : t.nb;
+  const int cs = cs0 + (int)ctile * kCTile;
+  const int cn = min(kCTile, cnAll - (int)ctile * kCTile);
+  for (int cb = 0; cb < cn; cb += 32) {
+    // 32 cover boxes per load round, broadcast by shuffles
+    float2 mybox = make_float2(0.f, 0.f);
+    if (cb + lane < cn) mybox = ybox[cov_edge[cs + cb + lane]];
+    const int nthis = min(32, cn - cb);
+    for (int k2 = 0; k2 < nthis; ++k2) {
+      const float sx = __shfl_sync(0xffffffffu, mybox.x, k2);
+      const float sy = __shfl_sync(0xffffffffu, mybox.y, k2);
+      unsigned m = 0;
 #pragma unroll
-    for (int q = 0; q < 8; ++q)
-      if (pe[q] >= 0 && !(sb.x > py1[q] || sb.y < py0[q])) m |= 1u << q;
-    int cnt = __popc(m);
-    int incl = cnt;
+      for (int q = 0; q < 8; ++q)
+        if (pe[q] >= 0 && !(sx > py1[q] || sy < py0[q])) m |= 1u << q;
+      if (!__any_sync(0xffffffffu, m != 0)) continue;
+      const int P = cs + cb + k2;
+      int cnt = __popc(m);
+      int incl = cnt;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      int total = __shfl_sync(0xffffffffu, incl, 31);
+      unsigned long long base = 0;
+      if (lane == 31) base = atomicAdd(&counters[2], (unsigned long long)total);
+      base = __shfl_sync(0xffffffffu, base, 31);
+      long long w = (long long)base + incl - cnt;
+      while (m) {
+        int q = __ffs(m) - 1;
+        m &= m - 1;
+        if (w < scap) surv[w] = make_int2(P, pe[q] | (kind << 30));
+        ++w;
+      }
     }
-    int total = __shfl_sync(0xffffffffu, incl, 31);
-    if (total == 0) continue;
-    unsigned long long base = 0;
-    if (lane == 31) base = atomicAdd(&counters[2], (unsigned long long)total);
-    base = __shfl_sync(0xffffffffu, base, 31);
-    long long w = (long long)base + incl - cnt;
-    while (m) {
-      int q = __ffs(m) - 1;
-      m &= m - 1;
-      if (w < scap) surv[w] = make_int2(P, pe[q] | (kind << 30));
-      ++w;
-    }
-    (void)lt;
   }
 }
 
