@@ -147,7 +147,8 @@ __global__ void k_node_items(int nNodes, const int* __restrict__ nodes,
                              const int* __restrict__ node_start, const int* __restrict__ node_end,
                              const unsigned* __restrict__ cov_edge, const int* __restrict__ tstart,
                              int cType, int logL, int numLeaves, const int* __restrict__ le_off,
-                             long long* __restrict__ items, long long* __restrict__ wunits) {
+                             long long* __restrict__ items, long long* __restrict__ wunits,
+                             int4* __restrict__ desc) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i > nNodes) return;
   if (i == nNodes) {
@@ -157,12 +158,34 @@ __global__ void k_node_items(int nNodes, const int* __restrict__ nodes,
   }
   NodeTiles t = node_tiles(nodes[i], node_start, node_end, cov_edge, tstart, cType, logL,
                            numLeaves, le_off);
+  desc[3 * i + 0] = make_int4(t.s, t.nb, t.bsT, t.ncT);
+  desc[3 * i + 1] = make_int4(t.lo, t.hi, (int)t.lbT, (int)t.nT);
+  desc[3 * i + 2] = make_int4((int)t.lb0, (int)t.n0, 0, 0);
   long long n = 0, w = 0;
   if (t.nb > 0 && t.ncT > 0) n += tiles_of(t.ncT) * ctiles_of(t.nb), w += (long long)t.nb * t.ncT;
   if (t.nb > 0 && t.nT > 0) n += tiles_of(t.nT) * ctiles_of(t.nb), w += (long long)t.nb * t.nT;
   if (t.ncT > 0 && t.n0 > 0) n += tiles_of(t.n0) * ctiles_of(t.ncT), w += (long long)t.ncT * t.n0;
   items[i] = n;
   wunits[i] = w;
+}
+
+// one record per tile: {node index, kind, partner tile, cover tile}
+__global__ void k_expand_items(int nNodes, const long long* __restrict__ items,
+                               const int4* __restrict__ desc, int4* __restrict__ rec) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nNodes) return;
+  int4 d0 = desc[3 * i], d1 = desc[3 * i + 1], d2 = desc[3 * i + 2];
+  int nb = d0.y, ncT = d0.w, nT = d1.w, n0 = d2.y;
+  long long w = items[i];
+  for (int kind = 0; kind < 3; ++kind) {
+    long long np = kind == 0 ? ((nb > 0 && ncT > 0) ? tiles_of(ncT) : 0)
+                             : kind == 1 ? ((nb > 0 && nT > 0) ? tiles_of(nT) : 0)
+                                         : ((ncT > 0 && n0 > 0) ? tiles_of(n0) : 0);
+    if (np == 0) continue;
+    long long nc = ctiles_of(kind == 2 ? ncT : nb);
+    for (long long c = 0; c < nc; ++c)
+      for (long long p = 0; p < np; ++p) rec[w++] = make_int4(i, kind, (int)p, (int)c);
+  }
 }
 
 // Candidate filter by node tiles (saveIntersectionsIdsMulticore,
@@ -177,45 +200,29 @@ __global__ void k_node_items(int nNodes, const int* __restrict__ nodes,
 // work in full warps: the FP64 pipe costs the same per warp instruction
 // however few lanes are active).
 __global__ void __launch_bounds__(kCandBlock)
-k_cand_test(int nNodes, const int* __restrict__ nodes, const long long* __restrict__ items,
-            long long nItems, const int* __restrict__ node_start,
-            const int* __restrict__ node_end, const unsigned* __restrict__ cov_edge,
-            const int* __restrict__ tstart, int cType, int logL, int numLeaves,
-            const int* __restrict__ le_off, const int4* __restrict__ pack,
+k_cand_test(const int4* __restrict__ rec, const int4* __restrict__ desc, long long nItems,
+            const unsigned* __restrict__ cov_edge, int logL, const int4* __restrict__ pack,
             const float2* __restrict__ ybox, const int2* __restrict__ ab,
             unsigned long long* __restrict__ counters, long long scap, int2* __restrict__ surv) {
   const int lane = threadIdx.x & 31;
   const long long it = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (it >= nItems) return;  // warp-uniform
-  int ni;
-  {
-    int lo = 0, hi = nNodes;  // last node with items[ni] <= it
-    while (hi - lo > 1) {
-      int m = (lo + hi) >> 1;
-      if (items[m] <= it) lo = m;
-      else hi = m;
-    }
-    ni = lo;
-  }
-  const int v = nodes[ni];
-  const NodeTiles t = node_tiles(v, node_start, node_end, cov_edge, tstart, cType, logL,
-                                 numLeaves, le_off);
-  long long tile = it - items[ni];
-  int kind = 0;
-  long long n0 = (t.nb > 0 && t.ncT > 0) ? tiles_of(t.ncT) * ctiles_of(t.nb) : 0;
-  long long n1 = (t.nb > 0 && t.nT > 0) ? tiles_of(t.nT) * ctiles_of(t.nb) : 0;
-  if (tile >= n0) {
-    tile -= n0;
-    kind = 1;
-    if (tile >= n1) {
-      tile -= n1;
-      kind = 2;
-    }
-  }
-  // 2-D tile: partner tile x cover tile
-  const long long ptiles = tiles_of(kind == 0 ? t.ncT : (kind == 1 ? t.nT : t.n0));
-  const long long ctile = tile / ptiles;
-  tile -= ctile * ptiles;
+  const int4 rc4 = rec[it];
+  const int4 d0 = desc[3 * rc4.x], d1 = desc[3 * rc4.x + 1], d2 = desc[3 * rc4.x + 2];
+  NodeTiles t;
+  t.s = d0.x;
+  t.nb = d0.y;
+  t.bsT = d0.z;
+  t.ncT = d0.w;
+  t.lo = d1.x;
+  t.hi = d1.y;
+  t.lbT = d1.z;
+  t.nT = d1.w;
+  t.lb0 = d2.x;
+  t.n0 = d2.y;
+  const int kind = rc4.y;
+  long long tile = rc4.z;
+  const long long ctile = rc4.w;
   const int L = 1 << logL;
   // ---- the tile's partners, 8 per lane
   const long long pbase = tile * kTile;
@@ -688,6 +695,7 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
   int* nodes = (int*)pool_.get("cand_nodes", sizeof(int) * (nNodes + 1));
   long long* items = (long long*)pool_.get("cand_items", sizeof(long long) * (nNodes + 1));
   long long* wun = (long long*)pool_.get("cand_wunits", sizeof(long long) * (nNodes + 1));
+  int4* desc = (int4*)pool_.get("cand_desc", sizeof(int4) * 3 * (nNodes + 1));
   if (pool_.failed) return fail(kENoMem, "device allocation failed (candidate nodes)");
   if (nCover > 0) {
     ::sbc::KProbe kp_("k_node_list", st);
@@ -697,7 +705,7 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
     ::sbc::KProbe kp_("k_node_items", st);
     k_node_items<<<grid_for(nNodes + 1, 256), 256, 0, st>>>(nNodes, nodes, node_start, node_end,
                                                           cov_edge, tstart, cType, logL, numLeaves,
-                                                          le_off, items, wun);
+                                                          le_off, items, wun, desc);
   }
   exclusive_scan_i64(items, nNodes + 1, sscr, st);
   exclusive_scan_i64(wun, nNodes + 1, sscr, st);
@@ -705,6 +713,12 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
   cudaMemcpyAsync(&nItems, items + nNodes, sizeof(long long), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(&W, wun + nNodes, sizeof(long long), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
+  int4* rec = (int4*)pool_.get("cand_rec", sizeof(int4) * (nItems + 1));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (candidate tiles)");
+  if (nNodes > 0) {
+    ::sbc::KProbe kp_("k_expand_items", st);
+    k_expand_items<<<grid_for(nNodes, 256), 256, 0, st>>>(nNodes, items, desc, rec);
+  }
 
   // filter: node tiles -> survivor pairs (grow and retry on overflow)
   long long scap = sv_cap_ > 0 ? sv_cap_ : 8LL * E + (1 << 20);
@@ -718,8 +732,7 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
     if (nItems > 0) {
       ::sbc::KProbe kp_("k_cand_test", st);
       k_cand_test<<<grid_for(nItems * 32, kCandBlock), kCandBlock, 0, st>>>(
-          nNodes, nodes, items, nItems, node_start, node_end, cov_edge, tstart, cType, logL,
-          numLeaves, le_off, pack, ybox, abx, counters3, scap, surv);
+          rec, desc, nItems, cov_edge, logL, pack, ybox, abx, counters3, scap, surv);
     }
     unsigned long long hs = 0;
     cudaMemcpyAsync(&hs, counters3 + 2, sizeof(hs), cudaMemcpyDeviceToHost, st);
