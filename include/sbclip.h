@@ -121,6 +121,69 @@ int sbc_debug_array(sbc_ctx* ctx, int which, void* host_dst, long long cap, long
 int sbc_classify_pairs(sbc_ctx* ctx, const double* pairs, int n, int* types, double* alpha,
                        double* beta, int* alpha_int, int* beta_int);
 
+/* Allocation-free ring tracing.  No counterpart in the reference: it exists
+ * for callers that are not allowed to allocate device memory themselves or
+ * through this library -- for example an engine that owns every byte of the
+ * GPU and hands each plug-in fixed input and output buffers, or a process
+ * running against a hard device-memory cap where a cudaMalloc would fail or
+ * spoil the host's accounting.  Every other entry point grows
+ * context-owned device buffers on demand; this one allocates nothing.
+ *
+ * It runs the library's exact linked-list back end (the reference's
+ * copyToLinkedList, labelIntersections2, createResult2 and cleanUpResult2,
+ * applied one step at a time by a single device thread) on the merged
+ * vertex/intersection lists of ONE base/overlay pair.  Those lists are the
+ * arrays sbc_debug_array exports after a clipping call: merged_bxy and
+ * merged_cxy (SBC_ARR_MERGED_BXY / _CXY), merged_balpha (SBC_ARR_MERGED_BALPHA),
+ * merged_cnb (SBC_ARR_MERGED_CNB), label_b and label_c (SBC_ARR_LABEL_B / _C);
+ * n_isect is the number of unique intersecting edge pairs (SBC_ARR_UNIQ_B's
+ * count).  The result equals sbc_clip_pair's rings for that pair.  Array
+ * contents are not validated: pass the lists of one pair unchanged.
+ *
+ * Limits and sharing:
+ *  - The node pools live in one file-scope device array of
+ *    SBC_NOALLOC_SCRATCH_BYTES (24 MiB), which every GPU that loads the
+ *    library holds until the process exits.  A call must satisfy
+ *    n_slots_b + n_slots_c + 4 * n_isect <= SBC_NOALLOC_MAX_UNITS; larger
+ *    calls are rejected with SBC_EINPUT before any device work.
+ *  - The first call on a device looks up that array's device address (once
+ *    per device, with the device current); make that first call before any
+ *    stream capture begins.
+ *  - All calls on a device share the array, and it keeps the last call's
+ *    contents.  Calls whose device work overlaps (different streams, or
+ *    different host threads, without ordering between them) race on it;
+ *    order them, e.g. by issuing them on one stream.
+ *  - Runs on the calling thread's current device; `stream` must belong to
+ *    it (NULL: the legacy default stream).  The call waits for its own work
+ *    on `stream` before it returns.
+ *
+ * Inputs are device pointers.  Outputs: ring_offsets (device, at least
+ * n_slots_b + 17 ints, checked), ring_xy (device, room for xy_cap_verts
+ * vertices = 2*xy_cap_verts doubles), *nrings_out and *nverts_out (host).
+ * If the rings need more than xy_cap_verts vertices the call returns
+ * SBC_EINPUT with *nverts_out set to the number needed.  A message for any
+ * non-zero status is written to err (err_len bytes, may be NULL). */
+#define SBC_NOALLOC_MAX_UNITS 262144
+#define SBC_NOALLOC_SCRATCH_BYTES (24 * 1024 * 1024)
+typedef struct sbc_merged_lists {
+  const double* b_xy;          /* base polygon, nb vertices (2*nb doubles) */
+  int nb;
+  const double* c_xy;          /* overlay polygon, nc vertices */
+  int nc;
+  const double* merged_bxy;    /* 2*n_slots_b doubles */
+  const int* merged_balpha;    /* n_slots_b */
+  const int* label_b;          /* n_slots_b */
+  int n_slots_b;
+  const double* merged_cxy;    /* 2*n_slots_c doubles */
+  const int* merged_cnb;       /* n_slots_c */
+  const int* label_c;          /* n_slots_c */
+  int n_slots_c;
+  int n_isect;
+} sbc_merged_lists;
+int sbc_trace_rings_noalloc(const sbc_merged_lists* in, int* ring_offsets, int offsets_cap,
+                            double* ring_xy, long long xy_cap_verts, int* nrings_out,
+                            long long* nverts_out, void* stream, char* err, int err_len);
+
 /* Number of this library's kernel launches in the process so far. */
 unsigned long long sbc_kernel_launches(void);
 

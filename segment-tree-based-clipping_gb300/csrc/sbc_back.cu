@@ -23,7 +23,9 @@
 // detected on the device and run through `k_serial_backend`, a single-thread
 // kernel that follows the reference's linked-list algorithm step by step.
 #include <cstdio>
+#include <mutex>
 
+#include "../../include/sbclip.h"
 #include "sbc_pipeline.cuh"
 
 namespace sbc {
@@ -1390,3 +1392,202 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
 }
 
 }  // namespace sbc
+
+// ================================================= allocation-free tracing
+// sbc_trace_rings_noalloc (include/sbclip.h) runs k_serial_backend and
+// k_serial_emit, unchanged, with every pool carved out of one file-scope
+// device array instead of context buffers, so the call allocates nothing.
+// It serves callers that may not allocate device memory: plug-in hosts that
+// own the GPU's memory and hand out fixed buffers, and processes under a hard
+// device-memory cap.  The array is shared by every call on a device and keeps
+// the last call's contents; calls whose device work overlaps race on it.
+
+// Device-side scratch: every GPU that loads this library holds it until the
+// process exits.  In host code this name only stands in for the symbol; its
+// device address comes from cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char sbc_noalloc_scratch[SBC_NOALLOC_SCRATCH_BYTES];
+
+namespace sbc {
+namespace {
+
+constexpr size_t na_align(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// bytes of one node pool of `cap` nodes (x, y, next, prev, nb, label, enex,
+// source, isect), each sub-array 256-byte aligned
+constexpr size_t na_pool_bytes(long long cap) {
+  return 2 * na_align(sizeof(double) * cap) + 5 * na_align(sizeof(int) * cap) + 2 * na_align(cap);
+}
+
+// Capacities the context path uses for the same pair (serial_backend above).
+struct NaCaps {
+  long long capP, capQ, capR, rcap;
+};
+constexpr NaCaps na_caps(long long nB, long long nQ, long long K) {
+  return NaCaps{nB + 2 * K + 8, nQ + 2 * K + 8, nB + nQ + 2 * (2 * K + 8) + 16, nB + 16};
+}
+
+// Scratch bytes of one call: three pools, ring roots, one 256-byte block of
+// counters, four byte-flag arrays.  The layout in na_carve follows this sum.
+constexpr size_t na_bytes(long long nB, long long nQ, long long K) {
+  return na_pool_bytes(na_caps(nB, nQ, K).capP) + na_pool_bytes(na_caps(nB, nQ, K).capQ) +
+         na_pool_bytes(na_caps(nB, nQ, K).capR) + na_align(sizeof(int) * na_caps(nB, nQ, K).rcap) +
+         256 + 2 * na_align(na_caps(nB, nQ, K).capP) + 2 * na_align(na_caps(nB, nQ, K).capQ);
+}
+
+// The pools need 2*(nB + nQ + 4K) + const nodes and the ring roots nB + 16
+// entries, so under nB + nQ + 4K <= SBC_NOALLOC_MAX_UNITS the largest need
+// is at nB = SBC_NOALLOC_MAX_UNITS, nQ = K = 0.
+static_assert(na_bytes(SBC_NOALLOC_MAX_UNITS, 0, 0) <= SBC_NOALLOC_SCRATCH_BYTES,
+              "allocation-free scratch array too small for its stated limit");
+
+struct NaBump {
+  unsigned char* p;
+  template <class T>
+  T* take(long long n) {
+    T* r = (T*)p;
+    p += na_align(sizeof(T) * n);
+    return r;
+  }
+};
+
+void na_pool(NaBump& b, long long cap, Pool& pool) {
+  pool.x = b.take<double>(cap);
+  pool.y = b.take<double>(cap);
+  pool.next = b.take<int>(cap);
+  pool.prev = b.take<int>(cap);
+  pool.nb = b.take<int>(cap);
+  pool.label = b.take<int>(cap);
+  pool.enex = b.take<int>(cap);
+  pool.source = b.take<unsigned char>(cap);
+  pool.isect = b.take<unsigned char>(cap);
+  pool.n = 0;
+  pool.cap = (int)cap;
+}
+
+constexpr int kNaMaxDevices = 64;
+std::mutex g_na_mu;
+void* g_na_ptr[kNaMaxDevices] = {};
+
+int na_fail(char* err, int err_len, int code, const char* msg, long long v0 = 0, long long v1 = 0) {
+  if (err && err_len > 0) snprintf(err, (size_t)err_len, msg, v0, v1);
+  return code;
+}
+
+}  // namespace
+}  // namespace sbc
+
+extern "C" int sbc_trace_rings_noalloc(const sbc_merged_lists* in, int* ring_offsets,
+                                       int offsets_cap, double* ring_xy, long long xy_cap_verts,
+                                       int* nrings_out, long long* nverts_out, void* stream,
+                                       char* err, int err_len) {
+  using namespace sbc;
+  if (err && err_len > 0) err[0] = 0;
+  if (!in || !ring_offsets || (!ring_xy && xy_cap_verts > 0) || !nrings_out || !nverts_out)
+    return na_fail(err, err_len, SBC_EINPUT, "null argument");
+  if (!in->b_xy || !in->c_xy || !in->merged_bxy || !in->merged_balpha || !in->label_b ||
+      !in->merged_cxy || !in->merged_cnb || !in->label_c)
+    return na_fail(err, err_len, SBC_EINPUT, "null input array");
+  if (in->nb < 3 || in->nc < 3)
+    return na_fail(err, err_len, SBC_EINPUT, "polygons need at least 3 vertices (base %lld, overlay %lld)",
+                   in->nb, in->nc);
+  if (in->n_slots_b < in->nb || in->n_slots_c < in->nc || in->n_isect < 0 || xy_cap_verts < 0)
+    return na_fail(err, err_len, SBC_EINPUT,
+                   "merged lists shorter than their polygons (slots %lld / %lld)", in->n_slots_b,
+                   in->n_slots_c);
+  const long long units = (long long)in->n_slots_b + in->n_slots_c + 4LL * in->n_isect;
+  if (units > SBC_NOALLOC_MAX_UNITS)
+    return na_fail(err, err_len, SBC_EINPUT,
+                   "n_slots_b + n_slots_c + 4*n_isect = %lld exceeds the allocation-free limit %lld",
+                   units, (long long)SBC_NOALLOC_MAX_UNITS);
+  if ((long long)offsets_cap < (long long)in->n_slots_b + 17)
+    return na_fail(err, err_len, SBC_EINPUT, "ring_offsets holds %lld ints, needs n_slots_b + 17 = %lld",
+                   offsets_cap, (long long)in->n_slots_b + 17);
+  const long long nB = in->n_slots_b, nQ = in->n_slots_c, K = in->n_isect;
+  if (na_bytes(nB, nQ, K) > (size_t)SBC_NOALLOC_SCRATCH_BYTES)
+    return na_fail(err, err_len, SBC_EINPUT, "scratch need %lld bytes exceeds the array (%lld)",
+                   (long long)na_bytes(nB, nQ, K), (long long)SBC_NOALLOC_SCRATCH_BYTES);
+
+  // per-device set-up: the array's device address, looked up once per device
+  int dev = -1;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess)
+    return na_fail(err, err_len, SBC_ECUDA, "cudaGetDevice failed (%lld)", (long long)ce);
+  if (dev < 0 || dev >= kNaMaxDevices)
+    return na_fail(err, err_len, SBC_EINPUT, "device ordinal %lld out of range", dev);
+  unsigned char* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_na_mu);
+    if (!g_na_ptr[dev]) {
+      void* p = nullptr;
+      ce = cudaGetSymbolAddress(&p, sbc_noalloc_scratch);
+      if (ce != cudaSuccess || !p)
+        return na_fail(err, err_len, SBC_ECUDA, "cudaGetSymbolAddress failed (%lld)", (long long)ce);
+      g_na_ptr[dev] = p;
+    }
+    base = (unsigned char*)g_na_ptr[dev];
+  }
+
+  // carve the pools in the order na_bytes counts them
+  const NaCaps cp = na_caps(nB, nQ, K);
+  SerialArgs a;
+  NaBump b{base};
+  na_pool(b, cp.capP, a.P);
+  na_pool(b, cp.capQ, a.Q);
+  na_pool(b, cp.capR, a.R);
+  a.rcap = (int)cp.rcap;
+  a.rroot = b.take<int>(cp.rcap);
+  int* block = b.take<int>(64);    // [0..1] emit counts, [2] status, [4] ring counter
+  unsigned char* flags = b.p;      // splitP, crossP (capP each), splitQ, crossQ (capQ each)
+  a.splitP = b.take<unsigned char>(cp.capP);
+  a.crossP = b.take<unsigned char>(cp.capP);
+  a.splitQ = b.take<unsigned char>(cp.capQ);
+  a.crossQ = b.take<unsigned char>(cp.capQ);
+  const size_t flag_bytes = (size_t)(b.p - flags);
+  a.status = block + 2;
+  a.nrings = block + 4;
+  a.bSize = in->nb;
+  a.cSize = in->nc;
+  a.cStart = 0;
+  a.nB = (int)nB;
+  a.nQ = (int)nQ;
+  a.bP = in->b_xy;
+  a.cP = in->c_xy;
+  a.ixB = in->merged_bxy;
+  a.ixC = in->merged_cxy;
+  a.alB = in->merged_balpha;
+  a.nbC = in->merged_cnb;
+  a.labB = in->label_b;
+  a.labC = in->label_c;
+
+  // the flags and counters must start at zero; the pools are written before
+  // they are read
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaMemsetAsync(block, 0, 256, st);
+  cudaMemsetAsync(flags, 0, flag_bytes, st);
+  ++g_launches;
+  k_serial_backend<<<1, 1, 0, st>>>(a);
+  int hst = 0;
+  cudaMemcpyAsync(&hst, a.status, sizeof(int), cudaMemcpyDeviceToHost, st);
+  ce = cudaStreamSynchronize(st);
+  if (ce == cudaSuccess) ce = cudaGetLastError();
+  if (ce != cudaSuccess)
+    return na_fail(err, err_len, SBC_ECUDA, "CUDA error %lld in the allocation-free back end", (long long)ce);
+  if (hst == 2)
+    return na_fail(err, err_len, SBC_EUNDEF, "reference behaviour undefined in the linked-list back end");
+  if (hst != 0)
+    return na_fail(err, err_len, SBC_EINTERNAL, "linked-list back end capacity exceeded (status %lld)", hst);
+  ++g_launches;
+  k_serial_emit<<<1, 1, 0, st>>>(a, ring_offsets, ring_xy, xy_cap_verts, block);
+  int hc[2] = {0, 0};
+  cudaMemcpyAsync(hc, block, sizeof(hc), cudaMemcpyDeviceToHost, st);
+  ce = cudaStreamSynchronize(st);
+  if (ce == cudaSuccess) ce = cudaGetLastError();
+  if (ce != cudaSuccess)
+    return na_fail(err, err_len, SBC_ECUDA, "CUDA error %lld in the allocation-free ring output", (long long)ce);
+  *nrings_out = hc[0];
+  *nverts_out = hc[1];
+  if (hc[1] > xy_cap_verts)
+    return na_fail(err, err_len, SBC_EINPUT, "ring_xy holds %lld vertices, the rings need %lld",
+                   xy_cap_verts, (long long)hc[1]);
+  return SBC_OK;
+}

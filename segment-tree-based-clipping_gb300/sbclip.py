@@ -50,6 +50,19 @@ class _Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("flags", ctypes.c_int)]
 
 
+class _MergedLists(ctypes.Structure):
+    _fields_ = [("b_xy", ctypes.c_void_p), ("nb", ctypes.c_int),
+                ("c_xy", ctypes.c_void_p), ("nc", ctypes.c_int),
+                ("merged_bxy", ctypes.c_void_p), ("merged_balpha", ctypes.c_void_p),
+                ("label_b", ctypes.c_void_p), ("n_slots_b", ctypes.c_int),
+                ("merged_cxy", ctypes.c_void_p), ("merged_cnb", ctypes.c_void_p),
+                ("label_c", ctypes.c_void_p), ("n_slots_c", ctypes.c_int),
+                ("n_isect", ctypes.c_int)]
+
+
+NOALLOC_MAX_UNITS = 262144
+
+
 _lib = None
 
 
@@ -77,6 +90,9 @@ def load_library(path: str | os.PathLike | None = None):
     L.sbc_kernel_launches.restype = ctypes.c_ulonglong
     L.sbc_profile_end.argtypes = [vp, i, vp, vp, i, ctypes.POINTER(i)]
     L.sbc_version.restype = ctypes.c_char_p
+    L.sbc_trace_rings_noalloc.argtypes = [ctypes.POINTER(_MergedLists), vp, i, vp, ll,
+                                          ctypes.POINTER(i), ctypes.POINTER(ll), vp,
+                                          ctypes.c_char_p, i]
     _lib = L
     return L
 
@@ -195,6 +211,28 @@ class Clipper:
         self._check(self._L.sbc_classify_pairs(self._h, p.ctypes.data, n, t.ctypes.data, a.ctypes.data,
                                                b.ctypes.data, ai.ctypes.data, bi.ctypes.data))
         return t, a, b, ai, bi
+
+
+def trace_rings_noalloc(b_xy: int, nb: int, c_xy: int, nc: int, merged_bxy: int,
+                        merged_balpha: int, label_b: int, n_slots_b: int, merged_cxy: int,
+                        merged_cnb: int, label_c: int, n_slots_c: int, n_isect: int,
+                        ring_offsets: int, offsets_cap: int, ring_xy: int, xy_cap_verts: int,
+                        stream: int | None = None):
+    """Allocation-free ring tracing (sbc_trace_rings_noalloc): every pointer
+    is a device address the caller owns; returns (nrings, nverts).  Raises
+    SbcError on a non-zero status."""
+    L = load_library()
+    m = _MergedLists(b_xy, nb, c_xy, nc, merged_bxy, merged_balpha, label_b, n_slots_b,
+                     merged_cxy, merged_cnb, label_c, n_slots_c, n_isect)
+    nr = ctypes.c_int()
+    nv = ctypes.c_longlong()
+    err = ctypes.create_string_buffer(256)
+    rc = L.sbc_trace_rings_noalloc(ctypes.byref(m), ring_offsets, offsets_cap, ring_xy,
+                                   xy_cap_verts, ctypes.byref(nr), ctypes.byref(nv), stream,
+                                   err, 256)
+    if rc != 0:
+        raise SbcError(rc, err.value.decode())
+    return nr.value, nv.value
 
 
 def format_rings(rings, precision: int = 6) -> str:
