@@ -2,15 +2,17 @@
 """Benchmark: milliseconds per 1M x 1M polygon clip on one GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload pair_1m_1m|pair_10k_8k]
+                    [--workload pair_1m_1m|pair_200k_200k|pair_10k_8k]
 
 A step is one full clip of the workload pair (segment tree build, candidate
 stab queries, FP64 intersection, merge, labelling and ring tracing) by the
 CUDA library.  `value` times K steps on device-resident inputs with CUDA
 events on the library's stream; L2 is flushed (a 256 MiB write) between
-steps, outside the timed window.  `e2e` times the public host API
-(sbc_clip_pair): host->device copy of the inputs from pinned staging and the
-device->host copy of the result rings inside every step.
+steps, outside the timed window.  Per-kernel times (the `roofline` and
+`kernels_top` entries) come from one extra step outside the timed window,
+with every launch bracketed by CUDA events.  `e2e` times the public host API
+(sbc_clip_pair): host->device copy of the inputs and the device->host copy of
+the result rings (offsets + vertices) inside every step.
 
 The single pair does not shard across GPUs (the tree and the tracing are
 global), so N > 1 runs N independent replicas, one per rank (torchrun), and
@@ -43,6 +45,11 @@ for _p in (PKG, ROOT / "oracle"):
 import sbclip_gen as gen  # noqa: E402
 
 METRIC = "ms per 1M×1M clip"
+
+
+def metric_of(workload: str) -> str:
+    return {"pair_1m_1m": METRIC, "pair_200k_200k": "ms per 200k×200k clip",
+            "pair_10k_8k": "ms per 10k×8k clip"}[workload]
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 
 
@@ -50,6 +57,10 @@ def workload(name: str):
     if name == "pair_1m_1m":
         b, c = gen.pair_large()
         desc = {"workload": "pair_1m_1m", "base_vertices": len(b), "overlay_vertices": len(c),
+                "generator": "jagged stars, 8 octaves value noise, base_freq=%d" % gen.JAGGED_BASE_FREQ}
+    elif name == "pair_200k_200k":
+        b, c = gen.pair_large(n=200_000)
+        desc = {"workload": "pair_200k_200k", "base_vertices": len(b), "overlay_vertices": len(c),
                 "generator": "jagged stars, 8 octaves value noise, base_freq=%d" % gen.JAGGED_BASE_FREQ}
     elif name == "pair_10k_8k":
         b, c = gen.pair_small()
@@ -120,22 +131,25 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# algorithmic bytes per launch of the kernels that can dominate a step,
-# from the run's statistics (see the roofline table in the design doc)
+# Algorithmic bytes per launch of the kernels that can dominate a step, from
+# the run's statistics.  The candidate kernels count 64 B per candidate pair
+# tested (the two edges' coordinates); the tree kernels count their inputs
+# and outputs once.
 def algorithmic_bytes(kernel: str, st: dict, launches: int):
     E = st["edges"]
     P = 2 * E
+    per = max(launches, 1)
+    if kernel in ("k_cand_test", "k_cand_exact"):
+        return 64.0 * st["candidates_tested"] / per
     if kernel == "k_rad_scatter_u64":
         return 24.0 * P  # read (key 8 + value 4) and write them once per pass
     if kernel == "k_rad_hist_u64":
         return 8.0 * P
-    if kernel == "k_cand_test":
-        return 64.0 * st["candidates_tested"] / max(launches, 1)
     if kernel == "k_cover":
-        return (16.0 * E + 8.0 * st["cover_entries"]) / max(launches, 1)
+        return (16.0 * E + 8.0 * st["cover_entries"]) / per
     if kernel == "k_find_leaves":
         return 16.0 * E + 8.0 * E
-    if kernel in ("k_rad_scatter_u32",):
+    if kernel == "k_rad_scatter_u32":
         return 16.0 * st["cover_entries"]
     return None
 
@@ -162,7 +176,6 @@ def run_gb300(args, rank: int, world: int):
         dist.barrier()
     st_launch = sbclip.kernel_launches()
     times = []
-    sbclip.profile_begin()
     with ClockSampler(dev) as clk:
         for _ in range(args.steps):
             flush.fill_(1.0)
@@ -174,7 +187,6 @@ def run_gb300(args, rank: int, world: int):
             e1.record(stream)
             torch.cuda.synchronize()
             times.append(e0.elapsed_time(e1))
-    prof = sbclip.profile_end()
     launches = sbclip.kernel_launches() - st_launch
     if world > 1:
         import torch.distributed as dist
@@ -187,20 +199,30 @@ def run_gb300(args, rank: int, world: int):
         ms = float(t.item())
     stats = clip.stats()
 
-    # ---- end to end through the host API
+    # ---- per-kernel device times: one more step, outside the timed region,
+    # with every launch bracketed by CUDA events on the library's stream
+    flush.fill_(1.0)
+    torch.cuda.synchronize()
+    sbclip.profile_begin()
+    clip.clip_pair_device(d_b.data_ptr(), nb, d_c.data_ptr(), nc, sp)
+    torch.cuda.synchronize()
+    prof = sbclip.profile_end()
+
+    # ---- end to end through the host C ABI (sbc_clip_pair): host buffers in,
+    # host->device and device->host copies inside every step
     e2e_times = []
-    rings = None
+    off = xy = None
     for i in range(max(args.steps, 1)):
         flush.fill_(1.0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        rings = clip.clip_pair(b, c)
-        torch.cuda.synchronize()
+        off, xy = clip.clip_pair_flat(b, c)
         e2e_times.append((time.perf_counter() - t0) * 1e3)
-    nverts = sum(len(r) for r in rings)
+    nrings = len(off) - 1
+    nverts = int(xy.shape[0])
     e2e = {"value": float(np.mean(e2e_times)), "unit": "ms",
            "h2d_bytes_per_step": int(16 * (nb + nc)),
-           "d2h_bytes_per_step": int(4 * (len(rings) + 1) + 16 * nverts)}
+           "d2h_bytes_per_step": int(4 * (nrings + 1) + 16 * nverts)}
 
     # ---- roofline of the dominant kernel
     pk, kind = peaks()
@@ -209,27 +231,26 @@ def run_gb300(args, rank: int, world: int):
     if dom:
         name, (tot_ms, n_l) = dom
         per_launch_ms = tot_ms / max(n_l, 1)
-        ab = algorithmic_bytes(name, stats, n_l // max(args.steps, 1))
+        ab = algorithmic_bytes(name, stats, n_l)
         achieved = (ab / (per_launch_ms * 1e-3) / 1e9) if ab else None
         roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
                 "unit": "GB/s", "frac": (achieved / pk["hbm_gbs"]) if achieved else None,
                 "traffic": None, "peak_source": kind,
                 "share_of_step": tot_ms / max(sum(v[0] for v in prof.values()), 1e-9),
                 "ms_per_launch": per_launch_ms}
-    top = sorted(prof.items(), key=lambda kv: -kv[1][0])[:8]
+    top = sorted(prof.items(), key=lambda kv: -kv[1][0])[:10]
 
     out = {
-        "metric": METRIC if args.workload == "pair_1m_1m" else "ms per 10k×8k clip",
+        "metric": metric_of(args.workload),
         "value": ms, "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded star polygons)",
         "config": dict(desc, parallelism="replicas" if world > 1 else "single",
                        l2="flushed between steps (256 MiB write)"),
         "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
-        "kernels_top": {k: {"ms_per_step": v[0] / max(args.steps, 1),
-                            "launches_per_step": v[1] // max(args.steps, 1)} for k, v in top},
+        "kernels_top": {k: {"ms_per_step": v[0], "launches_per_step": v[1]} for k, v in top},
         "stats": stats, "clocks": clk.summary(),
-        "counts": {"rings": len(rings), "vertices": nverts, "unique_intersections": stats["unique"],
+        "counts": {"rings": nrings, "vertices": nverts, "unique_intersections": stats["unique"],
                    "candidates_tested_per_s": stats["candidates_tested"] / (ms * 1e-3)},
     }
     if rank == 0 and not args.no_cpu_baseline:
@@ -270,7 +291,7 @@ def run_reference_arm(args):
     base = cpu_baseline(b, c, args, steps=steps)
     out = {
         "impl": "reference",
-        "metric": METRIC if args.workload == "pair_1m_1m" else "ms per 10k×8k clip",
+        "metric": metric_of(args.workload),
         "value": base["value"], "unit": "ms", "n_gpus": args.gpus, "steps": steps,
         "warmup": 0, "ms_per_step": base["value"], "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded star polygons)",
@@ -287,7 +308,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="pair_1m_1m", choices=["pair_1m_1m", "pair_10k_8k"])
+    ap.add_argument("--workload", default="pair_1m_1m",
+                    choices=["pair_1m_1m", "pair_200k_200k", "pair_10k_8k"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

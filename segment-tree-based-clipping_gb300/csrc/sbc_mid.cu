@@ -90,10 +90,11 @@ __global__ void k_edge_ybox(int E, const int* __restrict__ e_id, const int* __re
   ab[e] = make_int2(aft[e], bef[e]);
 }
 
-// per node with cover entries: the candidate tiles of its three tile kinds
+// per node with cover entries: the candidate products of its three kinds
 //   kind 0: base cover entries x overlay cover entries of the same node
 //   kind 1: base cover entries x overlay end-list entries (class cType leaves)
 //   kind 2: overlay cover entries x base end-list entries (class 0 leaves)
+// In every kind the "covers" are swept and the "partners" held in registers.
 struct NodeTiles {
   int s, e;        // cover entries [s, e) of the node
   int nb;          // base cover entries [s, s+nb)
@@ -102,8 +103,10 @@ struct NodeTiles {
   int lo, hi;      // leaf range of the node
 };
 
-constexpr int kTile = 256;   // partners per tile (8 per lane)
-constexpr int kCTile = 1024; // cover entries per tile
+constexpr int kTile = 256;     // partners per warp tile (8 per lane)
+constexpr int kCTile = 1024;   // cover entries per warp tile
+constexpr int kSmallMax = 64;  // products of at most this many pairs: one thread each
+constexpr int kStage = 512;    // survivors staged per warp in shared memory
 
 __device__ __forceinline__ NodeTiles node_tiles(int v, const int* node_start, const int* node_end,
                                                 const unsigned* cov_edge, const int* tstart,
@@ -126,8 +129,65 @@ __device__ __forceinline__ NodeTiles node_tiles(int v, const int* node_start, co
   return t;
 }
 
+// node descriptor: three int4 per node, written by k_node_items
+__device__ __forceinline__ NodeTiles load_desc(const int4* __restrict__ desc, int i) {
+  const int4 d0 = desc[3 * i], d1 = desc[3 * i + 1], d2 = desc[3 * i + 2];
+  NodeTiles t;
+  t.s = d0.x;
+  t.e = 0;
+  t.nb = d0.y;
+  t.bsT = d0.z;
+  t.ncT = d0.w;
+  t.lo = d1.x;
+  t.hi = d1.y;
+  t.lbT = d1.z;
+  t.nT = d1.w;
+  t.lb0 = d2.x;
+  t.n0 = d2.y;
+  return t;
+}
+
+__device__ __forceinline__ void kind_sizes(const NodeTiles& t, int kind, long long* p,
+                                           long long* cv) {
+  *p = kind == 0 ? t.ncT : (kind == 1 ? t.nT : t.n0);
+  *cv = kind == 2 ? t.ncT : t.nb;
+}
+
+__device__ __forceinline__ int cover_start(const NodeTiles& t, int kind) {
+  return kind == 2 ? t.bsT : t.s;
+}
+
 __device__ __forceinline__ long long tiles_of(long long n) { return (n + kTile - 1) / kTile; }
 __device__ __forceinline__ long long ctiles_of(long long n) { return (n + kCTile - 1) / kCTile; }
+
+// Partner j of `kind` in node t: its edge index and float y box, or -1 (and
+// an empty box) when it is the second leaf entry of an edge whose first entry
+// lies in the same subtree (an end list holds each edge once).
+__device__ __forceinline__ int load_partner(const NodeTiles& t, int kind, long long j, int L,
+                                            const unsigned* __restrict__ cov_edge,
+                                            const int4* __restrict__ pack,
+                                            const float2* __restrict__ ybox,
+                                            const int2* __restrict__ ab, float* y0, float* y1) {
+  if (kind == 0) {
+    int e = (int)cov_edge[t.bsT + j];
+    float2 bx = ybox[e];
+    *y0 = bx.x;
+    *y1 = bx.y;
+    return e;
+  }
+  int4 r = pack[(kind == 1 ? t.lbT : t.lb0) + j];
+  int2 o = ab[r.x];
+  int leaf = r.y + L;
+  int other = (o.x == leaf) ? o.y : o.x;
+  if (other >= 0 && other >= t.lo + L && other <= t.hi + L && other < leaf) {
+    *y0 = __int_as_float(0x7f800000);  // +inf
+    *y1 = __int_as_float(0xff800000);  // -inf: overlaps no finite box
+    return -1;
+  }
+  *y0 = __int_as_float(r.z);
+  *y1 = __int_as_float(r.w);
+  return r.x;
+}
 
 __global__ void k_node_list(long long nCover, const unsigned* __restrict__ cov_node,
                             const int* __restrict__ hpre, int* __restrict__ nodes) {
@@ -143,16 +203,19 @@ __global__ void k_node_heads(long long nCover, const unsigned* __restrict__ cov_
   h[P] = (P < nCover && (P == 0 || cov_node[P] != cov_node[P - 1])) ? 1 : 0;
 }
 
+// per node: its descriptor, its warp tiles (items), its small products
+// (smalls) and its pair count (work units)
 __global__ void k_node_items(int nNodes, const int* __restrict__ nodes,
                              const int* __restrict__ node_start, const int* __restrict__ node_end,
                              const unsigned* __restrict__ cov_edge, const int* __restrict__ tstart,
                              int cType, int logL, int numLeaves, const int* __restrict__ le_off,
-                             long long* __restrict__ items, long long* __restrict__ wunits,
-                             int4* __restrict__ desc) {
+                             long long* __restrict__ items, long long* __restrict__ smalls,
+                             long long* __restrict__ wunits, int4* __restrict__ desc) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i > nNodes) return;
   if (i == nNodes) {
     items[i] = 0;
+    smalls[i] = 0;
     wunits[i] = 0;
     return;
   }
@@ -161,111 +224,114 @@ __global__ void k_node_items(int nNodes, const int* __restrict__ nodes,
   desc[3 * i + 0] = make_int4(t.s, t.nb, t.bsT, t.ncT);
   desc[3 * i + 1] = make_int4(t.lo, t.hi, (int)t.lbT, (int)t.nT);
   desc[3 * i + 2] = make_int4((int)t.lb0, (int)t.n0, 0, 0);
-  long long n = 0, w = 0;
-  if (t.nb > 0 && t.ncT > 0) n += tiles_of(t.ncT) * ctiles_of(t.nb), w += (long long)t.nb * t.ncT;
-  if (t.nb > 0 && t.nT > 0) n += tiles_of(t.nT) * ctiles_of(t.nb), w += (long long)t.nb * t.nT;
-  if (t.ncT > 0 && t.n0 > 0) n += tiles_of(t.n0) * ctiles_of(t.ncT), w += (long long)t.ncT * t.n0;
+  long long n = 0, ns = 0, w = 0;
+  for (int kind = 0; kind < 3; ++kind) {
+    long long p, cv;
+    kind_sizes(t, kind, &p, &cv);
+    if (p <= 0 || cv <= 0) continue;
+    w += p * cv;
+    if (p * cv <= kSmallMax) ++ns;
+    else n += tiles_of(p) * ctiles_of(cv);
+  }
   items[i] = n;
+  smalls[i] = ns;
   wunits[i] = w;
 }
 
-// one record per tile: {node index, kind, partner tile, cover tile}
+// warp tiles {node index, kind, partner tile, cover tile} and small
+// products {node index, kind}, in node order
 __global__ void k_expand_items(int nNodes, const long long* __restrict__ items,
-                               const int4* __restrict__ desc, int4* __restrict__ rec) {
+                               const long long* __restrict__ smalls,
+                               const int4* __restrict__ desc, int4* __restrict__ rec,
+                               int2* __restrict__ srec) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nNodes) return;
-  int4 d0 = desc[3 * i], d1 = desc[3 * i + 1], d2 = desc[3 * i + 2];
-  int nb = d0.y, ncT = d0.w, nT = d1.w, n0 = d2.y;
-  long long w = items[i];
+  const NodeTiles t = load_desc(desc, i);
+  long long w = items[i], sw = smalls[i];
   for (int kind = 0; kind < 3; ++kind) {
-    long long np = kind == 0 ? ((nb > 0 && ncT > 0) ? tiles_of(ncT) : 0)
-                             : kind == 1 ? ((nb > 0 && nT > 0) ? tiles_of(nT) : 0)
-                                         : ((ncT > 0 && n0 > 0) ? tiles_of(n0) : 0);
-    if (np == 0) continue;
-    long long nc = ctiles_of(kind == 2 ? ncT : nb);
+    long long p, cv;
+    kind_sizes(t, kind, &p, &cv);
+    if (p <= 0 || cv <= 0) continue;
+    if (p * cv <= kSmallMax) {
+      srec[sw++] = make_int2(i, kind);
+      continue;
+    }
+    const long long np = tiles_of(p), nc = ctiles_of(cv);
     for (long long c = 0; c < nc; ++c)
-      for (long long p = 0; p < np; ++p) rec[w++] = make_int4(i, kind, (int)p, (int)c);
+      for (long long q = 0; q < np; ++q) rec[w++] = make_int4(i, kind, (int)q, (int)c);
   }
 }
 
-// Candidate filter by node tiles (saveIntersectionsIdsMulticore,
-// oacc_segment_tree.cpp:6118-6241, reordered).  A warp holds 256 partners of
-// one node in registers and sweeps the node's cover entries of the other
-// polygon over them, so an end list is read once per node instead of once
-// per cover entry.  Every partner in the same cover list or the end list of
-// the node overlaps the cover edge in x (both span or touch the node's
-// interval), so the LSMF box test reduces to the y test; a conservative float
-// y test (bounds rounded outwards) rejects most pairs from registers.  The
-// rest are compacted warp-wide into a survivor list for k_cand_exact (FP64
-// work in full warps: the FP64 pipe costs the same per warp instruction
-// however few lanes are active).
-__global__ void __launch_bounds__(kCandBlock)
-k_cand_test(const int4* __restrict__ rec, const int4* __restrict__ desc, long long nItems,
-            const unsigned* __restrict__ cov_edge, int logL, const int4* __restrict__ pack,
-            const float2* __restrict__ ybox, const int2* __restrict__ ab,
-            unsigned long long* __restrict__ counters, long long scap, int2* __restrict__ surv) {
-  const int lane = threadIdx.x & 31;
-  const long long it = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (it >= nItems) return;  // warp-uniform
-  const int4 rc4 = rec[it];
-  const int4 d0 = desc[3 * rc4.x], d1 = desc[3 * rc4.x + 1], d2 = desc[3 * rc4.x + 2];
-  NodeTiles t;
-  t.s = d0.x;
-  t.nb = d0.y;
-  t.bsT = d0.z;
-  t.ncT = d0.w;
-  t.lo = d1.x;
-  t.hi = d1.y;
-  t.lbT = d1.z;
-  t.nT = d1.w;
-  t.lb0 = d2.x;
-  t.n0 = d2.y;
-  const int kind = rc4.y;
-  long long tile = rc4.z;
-  const long long ctile = rc4.w;
-  const int L = 1 << logL;
-  // ---- the tile's partners, 8 per lane
-  const long long pbase = tile * kTile;
-  const long long pcount = kind == 0 ? t.ncT : (kind == 1 ? t.nT : t.n0);
-  int pe[8];
-  float py0[8], py1[8];
-#pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    long long j = pbase + q * 32 + lane;
-    pe[q] = -1;
-    py0[q] = __int_as_float(0x7f800000);   // +inf
-    py1[q] = __int_as_float(0xff800000);   // -inf: overlaps no finite box
-    if (j < pcount) {
-      if (kind == 0) {
-        int e = (int)cov_edge[t.bsT + j];
-        float2 bx = ybox[e];
-        pe[q] = e;
-        py0[q] = bx.x;
-        py1[q] = bx.y;
-      } else {
-        int4 r = pack[(kind == 1 ? t.lbT : t.lb0) + j];
-        int2 o = ab[r.x];
-        int leaf = r.y + L;
-        int other = (o.x == leaf) ? o.y : o.x;
-        // the edge's other leaf entry in this subtree comes first: an end list
-        // holds each edge once
-        bool dup = other >= 0 && other >= t.lo + L && other <= t.hi + L && other < leaf;
-        if (!dup) {
-          pe[q] = r.x;
-          py0[q] = __int_as_float(r.z);
-          py1[q] = __int_as_float(r.w);
-        }
-      }
-    }
+// Survivors of the float filter are staged per warp in shared memory and
+// reserved in the global list with one atomic per flush.
+struct WarpStage {
+  int2* buf;
+  int n;  // warp-uniform fill
+};
+
+__device__ __forceinline__ void stage_flush(WarpStage& s, int lane,
+                                            unsigned long long* __restrict__ counter,
+                                            long long scap, int2* __restrict__ surv) {
+  __syncwarp();
+  if (s.n == 0) return;
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(counter, (unsigned long long)s.n);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  for (int k = lane; k < s.n; k += 32) {
+    long long w = (long long)base + k;
+    if (w < scap) surv[w] = s.buf[k];
   }
-  // ---- sweep the node's cover entries of the other polygon; survivors of the
-  // float y test are appended as (cover position, partner | kind << 30)
-  const int cs0 = kind == 2 ? t.bsT : t.s;
-  const int cnAll = kind == 2 ? t.ncT : t.nb;
-  const int cs = cs0 + (int)ctile * kCTile;
-  const int cn = min(kCTile, cnAll - (int)ctile * kCTile);
+  __syncwarp();
+  s.n = 0;
+}
+
+// at most one survivor per lane
+__device__ __forceinline__ void stage_push1(WarpStage& s, int lane, bool hit, int2 v,
+                                            unsigned long long* __restrict__ counter,
+                                            long long scap, int2* __restrict__ surv) {
+  const unsigned b = __ballot_sync(0xffffffffu, hit);
+  if (b == 0) return;
+  if (hit) s.buf[s.n + __popc(b & ((1u << lane) - 1u))] = v;
+  s.n += __popc(b);
+  if (s.n > kStage - 32) stage_flush(s, lane, counter, scap, surv);
+}
+
+// Candidate filter by node tiles (saveIntersectionsIdsMulticore,
+// oacc_segment_tree.cpp:6118-6241, reordered).  A warp holds up to 256
+// partners of one node in registers and sweeps the node's cover entries of
+// the other polygon over them, so an end list is read once per node instead
+// of once per cover entry.  Every partner in the same cover list or the end
+// list of the node overlaps the cover edge in x (both span or touch the
+// node's interval), so the LSMF box test reduces to the y test; a
+// conservative float y test (bounds rounded outwards) rejects most pairs from
+// registers.  The rest are compacted into a survivor list for k_cand_exact
+// (FP64 work in full warps: the FP64 pipe costs the same per warp
+// instruction however few lanes are active).
+//
+// Tile shapes: more than 32 partners -> Q = 2, 4 or 8 partners per lane, one
+// cover per step for the whole warp; at most 32 partners -> lanes form
+// 32 / P2 groups of P2 = next power of two >= partners, each group testing
+// a different cover per step.
+template <int Q>
+__device__ __forceinline__ void sweep_wide(const NodeTiles& t, int kind, long long pbase, int pt,
+                                           int cs, int cn, int L, int lane,
+                                           const unsigned* __restrict__ cov_edge,
+                                           const int4* __restrict__ pack,
+                                           const float2* __restrict__ ybox,
+                                           const int2* __restrict__ ab, WarpStage& st,
+                                           unsigned long long* __restrict__ counter,
+                                           long long scap, int2* __restrict__ surv) {
+  int pe[Q];
+  float py0[Q], py1[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int jj = q * 32 + lane;
+    pe[q] = -1;
+    py0[q] = __int_as_float(0x7f800000);
+    py1[q] = __int_as_float(0xff800000);
+    if (jj < pt) pe[q] = load_partner(t, kind, pbase + jj, L, cov_edge, pack, ybox, ab, &py0[q], &py1[q]);
+  }
   for (int cb = 0; cb < cn; cb += 32) {
-    // 32 cover boxes per load round, broadcast by shuffles
     float2 mybox = make_float2(0.f, 0.f);
     if (cb + lane < cn) mybox = ybox[cov_edge[cs + cb + lane]];
     const int nthis = min(32, cn - cb);
@@ -274,30 +340,142 @@ k_cand_test(const int4* __restrict__ rec, const int4* __restrict__ desc, long lo
       const float sy = __shfl_sync(0xffffffffu, mybox.y, k2);
       unsigned m = 0;
 #pragma unroll
-      for (int q = 0; q < 8; ++q)
-        if (pe[q] >= 0 && !(sx > py1[q] || sy < py0[q])) m |= 1u << q;
+      for (int q = 0; q < Q; ++q)
+        if (!(sx > py1[q] || sy < py0[q])) m |= 1u << q;
       if (!__any_sync(0xffffffffu, m != 0)) continue;
       const int P = cs + cb + k2;
-      int cnt = __popc(m);
+      const int cnt = __popc(m);
       int incl = cnt;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         int y = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += y;
       }
-      int total = __shfl_sync(0xffffffffu, incl, 31);
-      unsigned long long base = 0;
-      if (lane == 31) base = atomicAdd(&counters[2], (unsigned long long)total);
-      base = __shfl_sync(0xffffffffu, base, 31);
-      long long w = (long long)base + incl - cnt;
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
+      int w = st.n + incl - cnt;
       while (m) {
         int q = __ffs(m) - 1;
         m &= m - 1;
-        if (w < scap) surv[w] = make_int2(P, pe[q] | (kind << 30));
-        ++w;
+        st.buf[w++] = make_int2(P, pe[q] | (kind << 30));
       }
+      st.n += total;
+      if (st.n > kStage - 32 * Q) stage_flush(st, lane, counter, scap, surv);
     }
   }
+}
+
+__device__ __forceinline__ void sweep_grouped(const NodeTiles& t, int kind, long long pbase,
+                                              int pt, int cs, int cn, int L, int lane,
+                                              const unsigned* __restrict__ cov_edge,
+                                              const int4* __restrict__ pack,
+                                              const float2* __restrict__ ybox,
+                                              const int2* __restrict__ ab, WarpStage& st,
+                                              unsigned long long* __restrict__ counter,
+                                              long long scap, int2* __restrict__ surv) {
+  const int lg = pt <= 1 ? 0 : 32 - __clz(pt - 1);  // P2 = 1 << lg >= pt
+  const int G = 32 >> lg;                            // cover groups
+  const int slot = lane & ((1 << lg) - 1);
+  const int g = lane >> lg;
+  float py0 = __int_as_float(0x7f800000), py1 = __int_as_float(0xff800000);
+  int pe = -1;
+  if (slot < pt) pe = load_partner(t, kind, pbase + slot, L, cov_edge, pack, ybox, ab, &py0, &py1);
+  for (int cb = 0; cb < cn; cb += 32) {
+    float2 mybox = make_float2(0.f, 0.f);
+    if (cb + lane < cn) mybox = ybox[cov_edge[cs + cb + lane]];
+    const int nthis = min(32, cn - cb);
+    const int steps = (nthis + G - 1) / G;  // steps * G <= 32 (G divides 32)
+    for (int k2 = 0; k2 < steps; ++k2) {
+      const int ci = k2 * G + g;
+      const float sx = __shfl_sync(0xffffffffu, mybox.x, ci);
+      const float sy = __shfl_sync(0xffffffffu, mybox.y, ci);
+      const bool hit = ci < nthis && pe >= 0 && !(sx > py1 || sy < py0);
+      stage_push1(st, lane, hit, make_int2(cs + cb + ci, pe | (kind << 30)), counter, scap, surv);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kCandBlock)
+k_cand_test(const int4* __restrict__ rec, const int4* __restrict__ desc, long long nItems,
+            const unsigned* __restrict__ cov_edge, int logL, const int4* __restrict__ pack,
+            const float2* __restrict__ ybox, const int2* __restrict__ ab,
+            unsigned long long* __restrict__ counters, long long scap, int2* __restrict__ surv) {
+  __shared__ int2 stage_all[kCandBlock / 32][kStage];
+  const int lane = threadIdx.x & 31;
+  const long long it = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (it >= nItems) return;  // warp-uniform; no block-wide barrier follows
+  WarpStage st{stage_all[threadIdx.x >> 5], 0};
+  const int4 rc4 = rec[it];
+  const NodeTiles t = load_desc(desc, rc4.x);
+  const int kind = rc4.y;
+  const long long tile = rc4.z;
+  const int ctile = rc4.w;
+  const int L = 1 << logL;
+  long long p, cv;
+  kind_sizes(t, kind, &p, &cv);
+  const long long pbase = tile * kTile;
+  const int pt = (int)min((long long)kTile, p - pbase);
+  const int cs = cover_start(t, kind) + ctile * kCTile;
+  const int cn = (int)min((long long)kCTile, cv - (long long)ctile * kCTile);
+  unsigned long long* counter = &counters[2];
+  if (pt > 128)
+    sweep_wide<8>(t, kind, pbase, pt, cs, cn, L, lane, cov_edge, pack, ybox, ab, st, counter, scap, surv);
+  else if (pt > 64)
+    sweep_wide<4>(t, kind, pbase, pt, cs, cn, L, lane, cov_edge, pack, ybox, ab, st, counter, scap, surv);
+  else if (pt > 32)
+    sweep_wide<2>(t, kind, pbase, pt, cs, cn, L, lane, cov_edge, pack, ybox, ab, st, counter, scap, surv);
+  else
+    sweep_grouped(t, kind, pbase, pt, cs, cn, L, lane, cov_edge, pack, ybox, ab, st, counter, scap, surv);
+  stage_flush(st, lane, counter, scap, surv);
+}
+
+// Small products (at most kSmallMax pairs): one thread each, the warp's
+// threads stepping through their own products in lockstep (partner-major).
+__global__ void __launch_bounds__(kCandBlock)
+k_cand_small(const int2* __restrict__ srec, long long nS, const int4* __restrict__ desc,
+             const unsigned* __restrict__ cov_edge, int logL, const int4* __restrict__ pack,
+             const float2* __restrict__ ybox, const int2* __restrict__ ab,
+             unsigned long long* __restrict__ counters, long long scap, int2* __restrict__ surv) {
+  __shared__ int2 stage_all[kCandBlock / 32][kStage];
+  const int lane = threadIdx.x & 31;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i - lane >= nS) return;  // warp-uniform; no block-wide barrier follows
+  WarpStage st{stage_all[threadIdx.x >> 5], 0};
+  const int L = 1 << logL;
+  NodeTiles t{};
+  int kind = 0, prod = 0, cvn = 1, cs = 0;
+  if (i < nS) {
+    const int2 r = srec[i];
+    t = load_desc(desc, r.x);
+    kind = r.y;
+    long long p, cv;
+    kind_sizes(t, kind, &p, &cv);
+    prod = (int)(p * cv);
+    cvn = (int)cv;
+    cs = cover_start(t, kind);
+  }
+  const int maxp = __reduce_max_sync(0xffffffffu, prod);
+  unsigned long long* counter = &counters[2];
+  int pj = 0, ck = 0, pe = -1;
+  float py0 = 0.f, py1 = 0.f;
+  for (int k = 0; k < maxp; ++k) {
+    bool hit = false;
+    int P = 0, e = -1;
+    if (k < prod) {
+      if (ck == 0) pe = load_partner(t, kind, pj, L, cov_edge, pack, ybox, ab, &py0, &py1);
+      P = cs + ck;
+      e = pe;
+      if (pe >= 0) {
+        const float2 bx = ybox[cov_edge[P]];
+        hit = !(bx.x > py1 || bx.y < py0);
+      }
+      if (++ck == cvn) {
+        ck = 0;
+        ++pj;
+      }
+    }
+    stage_push1(st, lane, hit, make_int2(P, e | (kind << 30)), counter, scap, surv);
+  }
+  stage_flush(st, lane, counter, scap, surv);
 }
 
 // exact LSMF and classification of the filtered pairs, one per thread
@@ -695,6 +873,7 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
   int* nodes = (int*)pool_.get("cand_nodes", sizeof(int) * (nNodes + 1));
   long long* items = (long long*)pool_.get("cand_items", sizeof(long long) * (nNodes + 1));
   long long* wun = (long long*)pool_.get("cand_wunits", sizeof(long long) * (nNodes + 1));
+  long long* smalls = (long long*)pool_.get("cand_smalls", sizeof(long long) * (nNodes + 1));
   int4* desc = (int4*)pool_.get("cand_desc", sizeof(int4) * 3 * (nNodes + 1));
   if (pool_.failed) return fail(kENoMem, "device allocation failed (candidate nodes)");
   if (nCover > 0) {
@@ -705,19 +884,22 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
     ::sbc::KProbe kp_("k_node_items", st);
     k_node_items<<<grid_for(nNodes + 1, 256), 256, 0, st>>>(nNodes, nodes, node_start, node_end,
                                                           cov_edge, tstart, cType, logL, numLeaves,
-                                                          le_off, items, wun, desc);
+                                                          le_off, items, smalls, wun, desc);
   }
   exclusive_scan_i64(items, nNodes + 1, sscr, st);
+  exclusive_scan_i64(smalls, nNodes + 1, sscr, st);
   exclusive_scan_i64(wun, nNodes + 1, sscr, st);
-  long long nItems = 0;
+  long long nItems = 0, nSmall = 0;
   cudaMemcpyAsync(&nItems, items + nNodes, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(&nSmall, smalls + nNodes, sizeof(long long), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(&W, wun + nNodes, sizeof(long long), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
   int4* rec = (int4*)pool_.get("cand_rec", sizeof(int4) * (nItems + 1));
+  int2* srec = (int2*)pool_.get("cand_srec", sizeof(int2) * (nSmall + 1));
   if (pool_.failed) return fail(kENoMem, "device allocation failed (candidate tiles)");
   if (nNodes > 0) {
     ::sbc::KProbe kp_("k_expand_items", st);
-    k_expand_items<<<grid_for(nNodes, 256), 256, 0, st>>>(nNodes, items, desc, rec);
+    k_expand_items<<<grid_for(nNodes, 256), 256, 0, st>>>(nNodes, items, smalls, desc, rec, srec);
   }
 
   // filter: node tiles -> survivor pairs (grow and retry on overflow)
@@ -733,6 +915,11 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
       ::sbc::KProbe kp_("k_cand_test", st);
       k_cand_test<<<grid_for(nItems * 32, kCandBlock), kCandBlock, 0, st>>>(
           rec, desc, nItems, cov_edge, logL, pack, ybox, abx, counters3, scap, surv);
+    }
+    if (nSmall > 0) {
+      ::sbc::KProbe kp_("k_cand_small", st);
+      k_cand_small<<<grid_for(nSmall, kCandBlock), kCandBlock, 0, st>>>(
+          srec, nSmall, desc, cov_edge, logL, pack, ybox, abx, counters3, scap, surv);
     }
     unsigned long long hs = 0;
     cudaMemcpyAsync(&hs, counters3 + 2, sizeof(hs), cudaMemcpyDeviceToHost, st);

@@ -172,6 +172,22 @@ class Clipper:
     def clip_pair(self, base, overlay, stream: int | None = None):
         return self.clip(base, [overlay], stream)[0]
 
+    def clip_pair_flat(self, base, overlay, stream: int | None = None):
+        """sbc_clip_pair with the result as two arrays: ring offsets
+        (nrings+1 int32) and vertices (nverts x 2 float64), copied once."""
+        b = np.ascontiguousarray(base, dtype=np.float64).reshape(-1, 2)
+        c = np.ascontiguousarray(overlay, dtype=np.float64).reshape(-1, 2)
+        r = _Rings()
+        self._check(self._L.sbc_clip_pair(self._h, b.ctypes.data, b.shape[0], c.ctypes.data,
+                                          c.shape[0], ctypes.byref(r), stream))
+        if r.nrings <= 0:
+            return np.zeros(1, np.int32), np.zeros((0, 2))
+        off = np.ctypeslib.as_array(ctypes.cast(r.offsets, ctypes.POINTER(ctypes.c_int)),
+                                    (r.nrings + 1,)).copy()
+        xy = np.ctypeslib.as_array(ctypes.cast(r.xy, ctypes.POINTER(ctypes.c_double)),
+                                   (2 * int(r.nverts),)).copy()
+        return off, xy.reshape(-1, 2)
+
     def clip_pair_device(self, d_base: int, nb: int, d_overlay: int, nc: int,
                          stream: int | None = None):
         """Device pointers in; returns (nrings, nverts, d_offsets, d_xy) device pointers."""
