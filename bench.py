@@ -12,7 +12,8 @@ steps, outside the timed window.  Per-kernel times (the `roofline` and
 `kernels_top` entries) come from one extra step outside the timed window,
 with every launch bracketed by CUDA events.  `e2e` times the public host API
 (sbc_clip_pair): host->device copy of the inputs and the device->host copy of
-the result rings (offsets + vertices) inside every step.
+the result rings (offsets + vertices, into the context's host result memory
+that a C caller reads in place) inside every step.
 
 The single pair does not shard across GPUs (the tree and the tracing are
 global), so N > 1 runs N independent replicas, one per rank (torchrun), and
@@ -216,7 +217,7 @@ def run_gb300(args, rank: int, world: int):
         flush.fill_(1.0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        off, xy = clip.clip_pair_flat(b, c)
+        off, xy = clip.clip_pair_flat(b, c, copy=False)
         e2e_times.append((time.perf_counter() - t0) * 1e3)
     nrings = len(off) - 1
     nverts = int(xy.shape[0])

@@ -61,8 +61,6 @@ struct sbc_ctx {
   Pipeline* pl = nullptr;
   std::string err;
   // host staging (pinned)
-  double* h_in = nullptr;
-  size_t h_in_cap = 0;
   std::vector<int*> h_off;
   std::vector<double*> h_xy;
   std::vector<size_t> h_off_cap, h_xy_cap;
@@ -163,7 +161,6 @@ void sbc_destroy(sbc_ctx* c) {
   cudaSetDevice(c->device);
   if (c->own) cudaStreamSynchronize(c->own);
   delete c->pl;
-  if (c->h_in) cudaFreeHost(c->h_in);
   for (auto p : c->h_off)
     if (p) cudaFreeHost(p);
   for (auto p : c->h_xy)
@@ -188,7 +185,6 @@ int sbc_clip_one_to_many(sbc_ctx* c, const double* b_xy, int nb, const double* c
   }
   if (nb < 3) return set_err(c, SBC_EINPUT, "base needs at least 3 vertices");
   size_t nin = 2 * ((size_t)nb + (size_t)ncv);
-  if (!ensure_pinned(c->h_in, c->h_in_cap, nin)) return set_err(c, SBC_ENOMEM, "pinned staging");
   if (c->d_in_cap < nin) {
     if (c->d_in) cudaFree(c->d_in);
     c->d_in = nullptr;
@@ -199,11 +195,16 @@ int sbc_clip_one_to_many(sbc_ctx* c, const double* b_xy, int nb, const double* c
     }
     c->d_in_cap = nin;
   }
-  memcpy(c->h_in, b_xy, sizeof(double) * 2 * nb);
-  memcpy(c->h_in + 2 * nb, c_xy, sizeof(double) * 2 * ncv);
-  int rc = cuda_check(c, cudaMemcpyAsync(c->d_in, c->h_in, nin * sizeof(double),
+  // Copy straight from the caller's buffers: on a Grace host the copy engine
+  // reads pageable memory over NVLink-C2C as fast as pinned memory, so a
+  // host-side copy into pinned staging would only add a CPU memcpy.
+  int rc = cuda_check(c, cudaMemcpyAsync(c->d_in, b_xy, sizeof(double) * 2 * nb,
                                          cudaMemcpyHostToDevice, st),
                       "input copy");
+  if (!rc)
+    rc = cuda_check(c, cudaMemcpyAsync(c->d_in + 2 * nb, c_xy, sizeof(double) * 2 * ncv,
+                                       cudaMemcpyHostToDevice, st),
+                    "input copy");
   if (rc) return rc;
   rc = run_device(c, c->d_in, nb, c->d_in + 2 * nb, c_sizes, k, st);
   if (rc) return rc;

@@ -478,59 +478,168 @@ k_cand_small(const int2* __restrict__ srec, long long nS, const int4* __restrict
   stage_flush(st, lane, counter, scap, surv);
 }
 
-// exact LSMF and classification of the filtered pairs, one per thread
-__global__ void __launch_bounds__(256)
+// Vertex coordinates as float pairs: hi = x rounded to float, lo = (x - hi)
+// rounded to float, so hi + lo is within 2^-48 |x| of the double.  The
+// difference of two nearby vertices, (hiA - hiB) + (loA - loB), is then
+// accurate to about 2^-23 of itself plus 2^-46 of the coordinates.
+__global__ void k_vertex_f4(long long nv, const double* __restrict__ xy, float4* __restrict__ out) {
+  long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const double x = xy[2 * v], y = xy[2 * v + 1];
+  const float hx = __double2float_rn(x), hy = __double2float_rn(y);
+  out[v] = make_float4(hx, hy, __double2float_rn(dsub(x, (double)hx)),
+                       __double2float_rn(dsub(y, (double)hy)));
+}
+
+__device__ __forceinline__ float vdx(const float4& a, const float4& b) {
+  return __fadd_rn(__fsub_rn(a.x, b.x), __fsub_rn(a.z, b.z));
+}
+__device__ __forceinline__ float vdy(const float4& a, const float4& b) {
+  return __fadd_rn(__fsub_rn(a.y, b.y), __fsub_rn(a.w, b.w));
+}
+__device__ __forceinline__ float fcross(float ax, float ay, float bx, float by) {
+  return __fsub_rn(__fmul_rn(ax, by), __fmul_rn(ay, bx));
+}
+
+// True only when lineSegmentIntersection2 (seg_isect) certainly returns 0
+// for P = (p1, p2), Q = (q1, q2), decided in float.
+//
+// With a = q1 - p1, b = q2 - p1, w = p2 - p1 the four areas seg_isect uses
+// are AP1 = a x b, AQ1 = w x a, AQ2 = w x b and AP2 = AP1 + AQ1 - AQ2.
+//  * If AP1 and AP2 have the same strict sign, |AP1| > 2e-9 and
+//    |AP1| > 2e-9 |AP2|, then alpha = AP1 / (AP1 - AP2) is > 1 or
+//    < -EPSILON, and the collinear branch (|AP1| < EPSILON) is excluded:
+//    the type is 0.
+//  * If AQ1 and AQ2 have the same strict sign, |AQ1| > 2e-9 |AQ2| and
+//    |AP1| > 2e-9, then beta is > 1 or < -EPSILON in the general branch and
+//    the collinear branch is excluded again: the type is 0.
+// Segments that do not meet satisfy one of the two unless they are within
+// the float error of touching.  Each float area carries the bound
+// 32 u m^2 + 64 u^2 m M (u = 2^-24, m = largest difference component,
+// M = coordinate magnitude), at least 2.6 times the worst case of the
+// difference and product rounding; the FP64 areas of seg_isect differ from
+// the exact ones by about 1e-15 m^2, far inside it.
+__device__ __forceinline__ bool certainly_disjoint(const float4& p1, const float4& p2,
+                                                   const float4& q1, const float4& q2) {
+  const float ax = vdx(q1, p1), ay = vdy(q1, p1);
+  const float bx = vdx(q2, p1), by = vdy(q2, p1);
+  const float wx = vdx(p2, p1), wy = vdy(p2, p1);
+  const float AP1 = fcross(ax, ay, bx, by);
+  const float AQ1 = fcross(wx, wy, ax, ay);
+  const float AQ2 = fcross(wx, wy, bx, by);
+  const float AP2 = __fsub_rn(__fadd_rn(AP1, AQ1), AQ2);
+  const float m = fmaxf(fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fmaxf(fabsf(bx), fabsf(by))),
+                        fmaxf(fabsf(wx), fabsf(wy)));
+  const float M = __fadd_rn(fmaxf(fabsf(p1.x), fabsf(p1.y)), __fmul_rn(2.f, m));
+  const float u = 5.9604645e-8f;  // 2^-24
+  const float Bx = __fadd_rn(__fmul_rn(__fmul_rn(32.f * u, m), m),
+                             __fadd_rn(__fmul_rn(__fmul_rn(64.f * u * u, m), M), 1e-30f));
+  const float B2 = __fadd_rn(__fmul_rn(3.f, Bx),
+                             __fmul_rn(4.f * u, __fadd_rn(__fadd_rn(fabsf(AP1), fabsf(AQ1)), fabsf(AQ2))));
+  const float L1 = __fsub_rn(fabsf(AP1), Bx);
+  if (!(L1 > 2e-9f)) return false;  // also keeps the collinear branch out
+  const bool sameP = (AP1 > Bx && AP2 > B2) || (AP1 < -Bx && AP2 < -B2);
+  if (sameP && L1 > __fmul_rn(2e-9f, __fadd_rn(fabsf(AP2), B2))) return true;
+  const bool sameQ = (AQ1 > Bx && AQ2 > Bx) || (AQ1 < -Bx && AQ2 < -Bx);
+  const float LQ1 = __fsub_rn(fabsf(AQ1), Bx);
+  return sameQ && LQ1 > __fmul_rn(2e-9f, __fadd_rn(fabsf(AQ2), Bx));
+}
+
+// Exact LSMF and classification of the filtered pairs.  Phase 1 (one
+// survivor per thread, kExPer rounds): FP64 LSMF, then the float pre-test;
+// pairs it cannot rule out are queued in shared memory.  Phase 2: the queue
+// runs seg_isect in full warps, so the FP64 pipe serves only the pairs that
+// need it.
+constexpr int kExBlock = 256;
+constexpr int kExPer = 4;
+constexpr int kExChunk = kExBlock * kExPer;
+
+__global__ void __launch_bounds__(kExBlock)
 k_cand_exact(long long n, const int2* __restrict__ surv, const unsigned* __restrict__ cov_edge,
              const int* __restrict__ e_id, const double* __restrict__ bP,
-             const double* __restrict__ cP, unsigned long long* __restrict__ counters,
+             const double* __restrict__ cP, const float4* __restrict__ vfB,
+             const float4* __restrict__ vfC, unsigned long long* __restrict__ counters,
              long long cap, int* __restrict__ rb, int* __restrict__ rc, int* __restrict__ rt,
              unsigned long long* __restrict__ rkey) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31;
+  __shared__ int4 q[kExChunk];
+  __shared__ int qn;
+  __shared__ unsigned long long ntested;
+  const int tid = threadIdx.x, lane = tid & 31;
   const unsigned lt = (1u << lane) - 1u;
-  bool hit = false, tested = false;
-  int bId = 0, cId = 0, ty = 0;
-  unsigned long long key = 0;
-  if (i < n) {
-    int2 sv = surv[i];
-    const int P = sv.x;
-    const int partner = sv.y & 0x3fffffff;
-    const int kind = (unsigned)sv.y >> 30;
-    const bool selfBase = kind != 2;
-    const int sid = e_id[cov_edge[P]];
-    const int pid = e_id[partner];
-    bId = selfBase ? sid : pid;
-    cId = selfBase ? pid : sid;
-    const double* pb = bP + bId;
-    const double* pc = cP + cId;
-    double p1x = pb[0], p1y = pb[1], p2x = pb[2], p2y = pb[3];
-    double q1x = pc[0], q1y = pc[1], q2x = pc[2], q2y = pc[3];
-    if (lsmf(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y)) {
-      tested = true;
-      double al, be;
-      ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &be);
-      if (ty) {
-        hit = true;
-        key = ((unsigned long long)P << 36) | ((unsigned long long)(kind == 0 ? 0 : 1) << 35) |
-              (unsigned long long)(pid >> 1);
+  const long long base = (long long)blockIdx.x * kExChunk;
+  if (tid == 0) {
+    qn = 0;
+    ntested = 0;
+  }
+  __syncthreads();
+  unsigned my_tested = 0;
+  for (int r = 0; r < kExPer; ++r) {
+    const long long i = base + (long long)r * kExBlock + tid;
+    bool keep = false;
+    int4 e = make_int4(0, 0, 0, 0);
+    if (i < n) {
+      const int2 sv = surv[i];
+      const int P = sv.x;
+      const int partner = sv.y & 0x3fffffff;
+      const int kind = (unsigned)sv.y >> 30;
+      const bool selfBase = kind != 2;
+      const int sid = e_id[cov_edge[P]];
+      const int pid = e_id[partner];
+      const int bId = selfBase ? sid : pid;
+      const int cId = selfBase ? pid : sid;
+      const double* pb = bP + bId;
+      const double* pc = cP + cId;
+      if (lsmf(pb[0], pb[1], pb[2], pb[3], pc[0], pc[1], pc[2], pc[3])) {
+        ++my_tested;
+        if (!certainly_disjoint(vfB[bId >> 1], vfB[(bId >> 1) + 1], vfC[cId >> 1],
+                                vfC[(cId >> 1) + 1])) {
+          keep = true;
+          e = make_int4(bId, cId, P, ((kind == 0 ? 0 : 1) << 30) | (pid >> 1));
+        }
       }
     }
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    if (bal) {
+      int w0 = 0;
+      if (lane == 0) w0 = atomicAdd(&qn, __popc(bal));
+      w0 = __shfl_sync(0xffffffffu, w0, 0);
+      if (keep) q[w0 + __popc(bal & lt)] = e;
+    }
   }
-  unsigned tm = __ballot_sync(0xffffffffu, tested);
-  unsigned m = __ballot_sync(0xffffffffu, hit);
-  if (lane == 0 && tm) atomicAdd(&counters[1], (unsigned long long)__popc(tm));
-  if (m) {
-    int leader = __ffs(m) - 1;
-    unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(&counters[0], (unsigned long long)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (hit) {
-      long long idx = (long long)base + __popc(m & lt);
-      if (idx < cap) {
-        rb[idx] = bId;
-        rc[idx] = cId;
-        rt[idx] = ty;
-        rkey[idx] = key;
+  my_tested = __reduce_add_sync(0xffffffffu, my_tested);
+  if (lane == 0 && my_tested) atomicAdd(&ntested, (unsigned long long)my_tested);
+  __syncthreads();
+  if (tid == 0 && ntested) atomicAdd(&counters[1], ntested);
+  const int nq = qn;
+  const int nq32 = (nq + 31) & ~31;  // warp-uniform loop bound
+  for (int j = tid; j < nq32; j += kExBlock) {
+    bool hit = false;
+    int ty = 0;
+    int4 e = make_int4(0, 0, 0, 0);
+    if (j < nq) {
+      e = q[j];
+      const double* pb = bP + e.x;
+      const double* pc = cP + e.y;
+      double al, be;
+      ty = seg_isect(pb[0], pb[1], pb[2], pb[3], pc[0], pc[1], pc[2], pc[3], &al, &be);
+      hit = ty != 0;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, hit);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      unsigned long long hb = 0;
+      if (lane == leader) hb = atomicAdd(&counters[0], (unsigned long long)__popc(m));
+      hb = __shfl_sync(0xffffffffu, hb, leader);
+      if (hit) {
+        const long long idx = (long long)hb + __popc(m & lt);
+        if (idx < cap) {
+          rb[idx] = e.x;
+          rc[idx] = e.y;
+          rt[idx] = ty;
+          rkey[idx] = ((unsigned long long)e.z << 36) |
+                      ((unsigned long long)((unsigned)e.w >> 30) << 35) |
+                      (unsigned long long)(e.w & 0x3fffffff);
+        }
       }
     }
   }
@@ -862,6 +971,17 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
     ::sbc::KProbe kp_("k_edge_ybox", st);
     k_edge_ybox<<<grid_for(E, 256), 256, 0, st>>>(E, e_id, tstart, k, bP, cP, ybox, abx, aft, bef);
   }
+  float4* vfB = (float4*)pool_.get("cand_vfB", sizeof(float4) * (nb + 1));
+  float4* vfC = (float4*)pool_.get("cand_vfC", sizeof(float4) * ((long long)clSize + k));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (vertex tables)");
+  if (cType == 1) {
+    {
+      ::sbc::KProbe kp_("k_vertex_f4", st);
+      k_vertex_f4<<<grid_for(nb + 1, 256), 256, 0, st>>>(nb + 1, bP, vfB);
+    }
+    ::sbc::KProbe kp_("k_vertex_f4", st);
+    k_vertex_f4<<<grid_for((long long)clSize + k, 256), 256, 0, st>>>((long long)clSize + k, cP, vfC);
+  }
   {
     ::sbc::KProbe kp_("k_node_heads", st);
     k_node_heads<<<grid_for(nCover + 1, 256), 256, 0, st>>>(nCover, cov_node, nheads);
@@ -941,8 +1061,9 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
   if (pool_.failed) return fail(kENoMem, "device allocation failed (raw candidates)");
   if (nsurv > 0) {
     ::sbc::KProbe kp_("k_cand_exact", st);
-    k_cand_exact<<<grid_for(nsurv, 256), 256, 0, st>>>(nsurv, surv, cov_edge, e_id, bP, cP,
-                                                       counters3, cap, rb, rc, rt, rkey);
+    k_cand_exact<<<grid_for(nsurv, kExChunk), kExBlock, 0, st>>>(nsurv, surv, cov_edge, e_id, bP,
+                                                                 cP, vfB, vfC, counters3, cap, rb,
+                                                                 rc, rt, rkey);
   }
   unsigned long long hcnt[2];
   cudaMemcpyAsync(hcnt, counters3, 16, cudaMemcpyDeviceToHost, st);

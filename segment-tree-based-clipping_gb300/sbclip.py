@@ -172,9 +172,11 @@ class Clipper:
     def clip_pair(self, base, overlay, stream: int | None = None):
         return self.clip(base, [overlay], stream)[0]
 
-    def clip_pair_flat(self, base, overlay, stream: int | None = None):
+    def clip_pair_flat(self, base, overlay, stream: int | None = None, copy: bool = True):
         """sbc_clip_pair with the result as two arrays: ring offsets
-        (nrings+1 int32) and vertices (nverts x 2 float64), copied once."""
+        (nrings+1 int32) and vertices (nverts x 2 float64).  With copy=False
+        they are views of the context's result memory, valid until the next
+        call on this Clipper (what a C caller of sbc_clip_pair receives)."""
         b = np.ascontiguousarray(base, dtype=np.float64).reshape(-1, 2)
         c = np.ascontiguousarray(overlay, dtype=np.float64).reshape(-1, 2)
         r = _Rings()
@@ -183,9 +185,11 @@ class Clipper:
         if r.nrings <= 0:
             return np.zeros(1, np.int32), np.zeros((0, 2))
         off = np.ctypeslib.as_array(ctypes.cast(r.offsets, ctypes.POINTER(ctypes.c_int)),
-                                    (r.nrings + 1,)).copy()
+                                    (r.nrings + 1,))
         xy = np.ctypeslib.as_array(ctypes.cast(r.xy, ctypes.POINTER(ctypes.c_double)),
-                                   (2 * int(r.nverts),)).copy()
+                                   (2 * int(r.nverts),))
+        if copy:
+            off, xy = off.copy(), xy.copy()
         return off, xy.reshape(-1, 2)
 
     def clip_pair_device(self, d_base: int, nb: int, d_overlay: int, nc: int,
