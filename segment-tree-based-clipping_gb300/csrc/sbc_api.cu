@@ -37,6 +37,7 @@ int Pipeline::run(const double* d_bxy, int nb_, const double* d_cxy, const int* 
   if (!rc) rc = stage_endlists();
   mark(3);
   if (!rc) rc = stage_cover();
+  if (!rc) rc = stage_grid();
   mark(4);
   for (int t = 1; t <= k && !rc; ++t) rc = stage_overlay(t, outs_[t - 1]);
   mark(5);

@@ -1,0 +1,806 @@
+// sbc_cand.cu -- candidate edge pairs (reference row A8) without the node
+// enumeration.
+//
+// The reference (saveIntersectionsIdsMulticore, p_seg_tree/oacc_segment_tree.cpp:
+// 6108-6244) walks every tree node with a cover list and tests every ordered
+// pair in cover x cover and cover x end list.  A pair (b, c) of a base and an
+// overlay edge is emitted at node v exactly when
+//   kind 0: v is in the cover lists of both (emitted twice, once per order),
+//   kind 1: v is in b's cover list and c has an end-list leaf below v,
+//   kind 2: v is in c's cover list and b has an end-list leaf below v,
+// and the emission is kept when LSMF passes and the classification is not 0.
+// Only box-overlapping pairs can pass LSMF, so this file finds those with a
+// uniform grid over float edge boxes, and derives from each pair's two
+// cover decompositions and end leaves (a) how many times the reference emits
+// it and (b) its first emission in the reference's order: smallest node,
+// then the cover entry b before c, then cover x cover before cover x end,
+// then the partner's id.  That key orders the unique pairs of one base edge
+// exactly as the reference's stable sort + first-occurrence dedup does
+// (src/clip.cpp:441-493).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "sbc_pipeline.cuh"
+
+namespace sbc {
+
+namespace {
+
+constexpr int kLongCells = 1024;  // edges spanning more cells are joined by brute force
+constexpr int kGBlock = 256;
+constexpr int kGSmallMax = 64;    // cell products up to this size: one thread each
+constexpr int kGStage = 512;      // survivors staged per warp in shared memory
+
+__device__ __forceinline__ int class_of_edge(const int* tstart, int k, int e) {
+  int c = 0;
+  while (c < k && tstart[c + 1] <= e) ++c;
+  return c;
+}
+
+__device__ __forceinline__ unsigned fkey(float f) {
+  unsigned u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// LSMF bounding-box filter, oacc_segment_tree.cpp:5282-5316
+__device__ __forceinline__ bool lsmf_exact(double p1x, double p1y, double p2x, double p2y,
+                                           double q1x, double q1y, double q2x, double q2y) {
+  double minPX = p1x, minPY = p1y, maxPX = p2x, maxPY = p2y;
+  double minQX = q1x, minQY = q1y, maxQX = q2x, maxQY = q2y;
+  if (minPX > p2x) { minPX = p2x; maxPX = p1x; }
+  if (minPY > p2y) { minPY = p2y; maxPY = p1y; }
+  if (minQX > q2x) { minQX = q2x; maxQX = q1x; }
+  if (minQY > q2y) { minQY = q2y; maxQY = q1y; }
+  if (minPX > maxQX || maxPX < minQX) return false;
+  if (minPY > maxQY || maxPY < minQY) return false;
+  return true;
+}
+
+// ------------------------------------------------------------------ grid
+struct Grid {
+  float x0, y0, inv;
+  int gx, gy;
+  __device__ __forceinline__ int cx(float x) const {
+    int c = (int)floorf(__fmul_rn(__fsub_rn(x, x0), inv));
+    return min(max(c, 0), gx - 1);
+  }
+  __device__ __forceinline__ int cy(float y) const {
+    int c = (int)floorf(__fmul_rn(__fsub_rn(y, y0), inv));
+    return min(max(c, 0), gy - 1);
+  }
+};
+
+// float edge boxes (bounds rounded outwards), their union and summed extent
+__global__ void k_edge_fbox(int E, const int* __restrict__ e_id, const int* __restrict__ tstart,
+                            int k, const double* __restrict__ bP, const double* __restrict__ cP,
+                            float4* __restrict__ fbox, unsigned* __restrict__ bnd,
+                            double* __restrict__ sum_ext) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned k0 = 0xffffffffu, k1 = 0xffffffffu, k2 = 0u, k3 = 0u;
+  float ext = 0.f;
+  if (e < E) {
+    const double* p = (class_of_edge(tstart, k, e) == 0 ? bP : cP) + e_id[e];
+    const float4 f = make_float4(__double2float_rd(fmin(p[0], p[2])), __double2float_rd(fmin(p[1], p[3])),
+                                 __double2float_ru(fmax(p[0], p[2])), __double2float_ru(fmax(p[1], p[3])));
+    fbox[e] = f;
+    k0 = fkey(f.x);
+    k1 = fkey(f.y);
+    k2 = fkey(f.z);
+    k3 = fkey(f.w);
+    ext = fmaxf(f.z - f.x, f.w - f.y);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    k0 = min(k0, __shfl_xor_sync(0xffffffffu, k0, o));
+    k1 = min(k1, __shfl_xor_sync(0xffffffffu, k1, o));
+    k2 = max(k2, __shfl_xor_sync(0xffffffffu, k2, o));
+    k3 = max(k3, __shfl_xor_sync(0xffffffffu, k3, o));
+    ext += __shfl_xor_sync(0xffffffffu, ext, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&bnd[0], k0);
+    atomicMin(&bnd[1], k1);
+    atomicMax(&bnd[2], k2);
+    atomicMax(&bnd[3], k3);
+    atomicAdd(sum_ext, (double)ext);
+  }
+}
+
+// cells per edge (0 for edges joined by brute force, which go to long_list)
+__global__ void k_grid_count(int E, const float4* __restrict__ fbox, Grid g,
+                             long long* __restrict__ cnt, unsigned char* __restrict__ islong,
+                             int* __restrict__ long_list, unsigned* __restrict__ long_count) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e > E) return;
+  if (e == E) {
+    cnt[e] = 0;
+    return;
+  }
+  const float4 f = fbox[e];
+  const long long n = (long long)(g.cx(f.z) - g.cx(f.x) + 1) * (g.cy(f.w) - g.cy(f.y) + 1);
+  const bool lg = n > kLongCells;
+  islong[e] = lg ? 1 : 0;
+  cnt[e] = lg ? 0 : n;
+  if (lg) long_list[atomicAdd(long_count, 1u)] = e;
+}
+
+__global__ void k_grid_emit(int E, const float4* __restrict__ fbox, Grid g,
+                            const long long* __restrict__ off, const unsigned char* __restrict__ islong,
+                            unsigned* __restrict__ keys, unsigned* __restrict__ vals) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E || islong[e]) return;
+  const float4 f = fbox[e];
+  const int x0 = g.cx(f.x), x1 = g.cx(f.z), y0 = g.cy(f.y), y1 = g.cy(f.w);
+  long long w = off[e];
+  for (int y = y0; y <= y1; ++y)
+    for (int x = x0; x <= x1; ++x) {
+      keys[w] = (unsigned)y * (unsigned)g.gx + (unsigned)x;
+      vals[w] = (unsigned)e;
+      ++w;
+    }
+}
+
+__global__ void k_cell_heads(long long n, const unsigned* __restrict__ keys, int* __restrict__ h) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  h[i] = (i < n && (i == 0 || keys[i] != keys[i - 1])) ? 1 : 0;
+}
+
+__global__ void k_cell_starts(long long n, const int* __restrict__ hpre, int nCells,
+                              int* __restrict__ cstart) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  if (i == n) {
+    cstart[nCells] = (int)n;
+    return;
+  }
+  if (hpre[i + 1] != hpre[i]) cstart[hpre[i]] = (int)i;
+}
+
+__device__ __forceinline__ int lower_bound_v(const unsigned* a, int lo, int hi, unsigned x) {
+  while (lo < hi) {
+    int m = (lo + hi) >> 1;
+    if (a[m] < x) lo = m + 1;
+    else hi = m;
+  }
+  return lo;
+}
+
+// per cell: {first entry, base entries, first cType entry, cType entries};
+// whether it is a small product (one thread) and its warp tiles otherwise
+__global__ void k_cell_items(int nCells, const int* __restrict__ cstart,
+                             const unsigned* __restrict__ vals, const int* __restrict__ tstart,
+                             int cType, int4* __restrict__ cdesc, int* __restrict__ smalls,
+                             int* __restrict__ tiles, long long* __restrict__ work) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c > nCells) return;
+  if (c == nCells) {
+    smalls[c] = 0;
+    tiles[c] = 0;
+    work[c] = 0;
+    return;
+  }
+  const int a = cstart[c], z = cstart[c + 1];
+  const int nB = lower_bound_v(vals, a, z, (unsigned)tstart[1]) - a;
+  const int cs = lower_bound_v(vals, a, z, (unsigned)tstart[cType]);
+  const int nC = lower_bound_v(vals, cs, z, (unsigned)tstart[cType + 1]) - cs;
+  const long long prod = (long long)nB * nC;
+  cdesc[c] = make_int4(a, nB, cs, nC);
+  smalls[c] = (prod > 0 && prod <= kGSmallMax) ? 1 : 0;
+  tiles[c] = prod > kGSmallMax ? (nC + 31) / 32 : 0;
+  work[c] = prod;
+}
+
+__global__ void k_cell_expand(int nCells, const int* __restrict__ smalls,
+                              const int* __restrict__ tiles, int* __restrict__ srec,
+                              int2* __restrict__ wrec) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nCells) return;
+  if (smalls[c + 1] != smalls[c]) srec[smalls[c]] = c;
+  for (int t = 0, w = tiles[c]; w < tiles[c + 1]; ++t, ++w) wrec[w] = make_int2(c, t);
+}
+
+// ---- survivor staging (per warp, shared memory; one atomic per flush)
+struct Stage {
+  int2* buf;
+  int n;
+};
+
+__device__ __forceinline__ void st_flush(Stage& s, int lane, unsigned long long* counter,
+                                         long long cap, int2* out) {
+  __syncwarp();
+  if (s.n == 0) return;
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(counter, (unsigned long long)s.n);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  for (int k = lane; k < s.n; k += 32) {
+    const long long w = (long long)base + k;
+    if (w < cap) out[w] = s.buf[k];
+  }
+  __syncwarp();
+  s.n = 0;
+}
+
+__device__ __forceinline__ void st_push(Stage& s, int lane, bool hit, int2 v,
+                                        unsigned long long* counter, long long cap, int2* out) {
+  const unsigned b = __ballot_sync(0xffffffffu, hit);
+  if (b == 0) return;
+  if (hit) s.buf[s.n + __popc(b & ((1u << lane) - 1u))] = v;
+  s.n += __popc(b);
+  if (s.n > kGStage - 32) st_flush(s, lane, counter, cap, out);
+}
+
+// boxes overlap, and the lower corner of their overlap lies in cell (gxc,
+// gyc): each overlapping pair is reported by exactly one of the cells both
+// boxes touch
+__device__ __forceinline__ bool pair_here(const float4& a, const float4& b, const Grid& g, int gxc,
+                                          int gyc) {
+  if (a.x > b.z || a.z < b.x || a.y > b.w || a.w < b.y) return false;
+  return g.cx(fmaxf(a.x, b.x)) == gxc && g.cy(fmaxf(a.y, b.y)) == gyc;
+}
+
+// small cell products: one thread per cell, the warp's threads in lockstep
+__global__ void __launch_bounds__(kGBlock)
+k_grid_small(const int* __restrict__ srec, int nS, const int4* __restrict__ cdesc,
+             const unsigned* __restrict__ keys, const unsigned* __restrict__ vals,
+             const float4* __restrict__ fbox, Grid g, unsigned long long* __restrict__ counter,
+             long long cap, int2* __restrict__ out) {
+  __shared__ int2 stage[kGBlock / 32][kGStage];
+  const int lane = threadIdx.x & 31;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i - lane >= nS) return;  // warp-uniform; no block-wide barrier follows
+  Stage st{stage[threadIdx.x >> 5], 0};
+  int4 d = make_int4(0, 0, 0, 1);
+  int gxc = 0, gyc = 0, prod = 0;
+  if (i < nS) {
+    d = cdesc[srec[i]];
+    const unsigned key = keys[d.x];
+    gxc = (int)(key % (unsigned)g.gx);
+    gyc = (int)(key / (unsigned)g.gx);
+    prod = d.y * d.w;
+  }
+  const int maxp = __reduce_max_sync(0xffffffffu, prod);
+  int ib = 0, ic = 0, be = 0;
+  float4 bb = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int k2 = 0; k2 < maxp; ++k2) {
+    bool hit = false;
+    int ce = 0;
+    if (k2 < prod) {
+      if (ic == 0) {
+        be = (int)vals[d.x + ib];
+        bb = fbox[be];
+      }
+      ce = (int)vals[d.z + ic];
+      hit = pair_here(bb, fbox[ce], g, gxc, gyc);
+      if (++ic == d.w) {
+        ic = 0;
+        ++ib;
+      }
+    }
+    st_push(st, lane, hit, make_int2(be, ce), counter, cap, out);
+  }
+  st_flush(st, lane, counter, cap, out);
+}
+
+// larger cell products: one warp per 32 overlay entries of a cell, base
+// entries broadcast 32 at a time
+__global__ void __launch_bounds__(kGBlock)
+k_grid_warp(const int2* __restrict__ wrec, int nW, const int4* __restrict__ cdesc,
+            const unsigned* __restrict__ keys, const unsigned* __restrict__ vals,
+            const float4* __restrict__ fbox, Grid g, unsigned long long* __restrict__ counter,
+            long long cap, int2* __restrict__ out) {
+  __shared__ int2 stage[kGBlock / 32][kGStage];
+  const int lane = threadIdx.x & 31;
+  const long long it = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (it >= nW) return;  // warp-uniform; no block-wide barrier follows
+  Stage st{stage[threadIdx.x >> 5], 0};
+  const int2 r = wrec[it];
+  const int4 d = cdesc[r.x];
+  const unsigned key = keys[d.x];
+  const int gxc = (int)(key % (unsigned)g.gx), gyc = (int)(key / (unsigned)g.gx);
+  const int j = r.y * 32 + lane;
+  const bool cvalid = j < d.w;
+  const int ce = cvalid ? (int)vals[d.z + j] : 0;
+  const float4 cb = cvalid ? fbox[ce] : make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int b0 = 0; b0 < d.y; b0 += 32) {
+    const int nthis = min(32, d.y - b0);
+    int mye = 0;
+    float4 myb = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (lane < nthis) {
+      mye = (int)vals[d.x + b0 + lane];
+      myb = fbox[mye];
+    }
+    for (int k2 = 0; k2 < nthis; ++k2) {
+      float4 bb;
+      bb.x = __shfl_sync(0xffffffffu, myb.x, k2);
+      bb.y = __shfl_sync(0xffffffffu, myb.y, k2);
+      bb.z = __shfl_sync(0xffffffffu, myb.z, k2);
+      bb.w = __shfl_sync(0xffffffffu, myb.w, k2);
+      const int be = __shfl_sync(0xffffffffu, mye, k2);
+      const bool hit = cvalid && pair_here(bb, cb, g, gxc, gyc);
+      st_push(st, lane, hit, make_int2(be, ce), counter, cap, out);
+    }
+  }
+  st_flush(st, lane, counter, cap, out);
+}
+
+// edges too long for the grid: one warp per long edge against every edge of
+// the other polygon (long x long pairs once, from the base side)
+__global__ void __launch_bounds__(kGBlock)
+k_grid_long(const int* __restrict__ long_list, const unsigned* __restrict__ long_count,
+            const int* __restrict__ tstart, int cType, const unsigned char* __restrict__ islong,
+            const float4* __restrict__ fbox, unsigned long long* __restrict__ counter, long long cap,
+            int2* __restrict__ out) {
+  __shared__ int2 stage[kGBlock / 32][kGStage];
+  const int lane = threadIdx.x & 31;
+  Stage st{stage[threadIdx.x >> 5], 0};
+  const unsigned nl = *long_count;
+  const long long nw = (long long)gridDim.x * (kGBlock / 32);
+  for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nl; w += nw) {
+    const int e = long_list[w];
+    const bool isBase = e < tstart[1];
+    if (!isBase && (e < tstart[cType] || e >= tstart[cType + 1])) continue;  // other overlay
+    const int o0 = isBase ? tstart[cType] : 0, o1 = isBase ? tstart[cType + 1] : tstart[1];
+    const float4 fe = fbox[e];
+    for (int ob = o0; ob < o1; ob += 32) {
+      const int o = ob + lane;
+      bool hit = false;
+      if (o < o1 && (isBase || !islong[o])) {
+        const float4 fo = fbox[o];
+        hit = !(fe.x > fo.z || fe.z < fo.x || fe.y > fo.w || fe.w < fo.y);
+      }
+      st_push(st, lane, hit, isBase ? make_int2(e, o) : make_int2(o, e), counter, cap, out);
+    }
+  }
+  st_flush(st, lane, counter, cap, out);
+}
+
+// ------------------------------------------------------------------ emission
+// Node v's leaf range is [lo, hi) (leaf indices); canonical for [l, r1) when
+// contained in it and its parent is not.
+__device__ __forceinline__ bool canonical(int v, int logL, int l, int r1) {
+  const int L = 1 << logL;
+  const int d = 31 - __clz(v), h = logL - d;
+  const int lo = (v << h) - L, hi = ((v + 1) << h) - L;
+  if (lo < l || hi > r1) return false;
+  if (v == 1) return true;
+  const int p = v >> 1;
+  const int plo = (p << (h + 1)) - L, phi = ((p + 1) << (h + 1)) - L;
+  return !(plo >= l && phi <= r1);
+}
+
+// leaf node x (or -1) lies below node v
+__device__ __forceinline__ bool below(int x, int v, int logL) {
+  if (x < 0) return false;
+  const int h = logL - (31 - __clz(v));
+  return (x >> h) == v;
+}
+
+// How many times the reference emits base edge b with overlay edge c, and
+// the key of the first emission: node << 33 | (cover entry is c) << 32 |
+// payload, payload = phase << 31 | cId for cover entry b (phase 0 cover x
+// cover, 1 cover x end) and c's edge index for cover entry c.
+__device__ __forceinline__ unsigned emission(int b, int c, int cId, const int2* __restrict__ lr,
+                                             const int* __restrict__ aft,
+                                             const int* __restrict__ bef, int logL,
+                                             unsigned long long* key) {
+  const int L = 1 << logL;
+  const int2 rb = lr[b], rc = lr[c];
+  const int eb0 = aft[b], eb1 = bef[b], ec0 = aft[c], ec1 = bef[c];
+  unsigned n = 0;
+  unsigned long long best = ~0ull;
+  int a = rb.x + L, z = rb.y + L;
+  while (a < z) {
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      int v = -1;
+      if (side == 0 && (a & 1)) v = a++;
+      if (side == 1 && (z & 1)) v = --z;
+      if (v < 0) continue;
+      if (canonical(v, logL, rc.x, rc.y)) {
+        n += 2;
+        best = min(best, ((unsigned long long)v << 33) | (unsigned)cId);
+      }
+      if (below(ec0, v, logL) || below(ec1, v, logL)) {
+        n += 1;
+        best = min(best, ((unsigned long long)v << 33) | (1ull << 31) | (unsigned)cId);
+      }
+    }
+    a >>= 1;
+    z >>= 1;
+  }
+  a = rc.x + L;
+  z = rc.y + L;
+  while (a < z) {
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      int v = -1;
+      if (side == 0 && (a & 1)) v = a++;
+      if (side == 1 && (z & 1)) v = --z;
+      if (v < 0) continue;
+      if (below(eb0, v, logL) || below(eb1, v, logL)) {
+        n += 1;
+        best = min(best, ((unsigned long long)v << 33) | (1ull << 32) | (unsigned)c);
+      }
+    }
+    a >>= 1;
+    z >>= 1;
+  }
+  *key = best;
+  return n;
+}
+
+// ------------------------------------------------------------------ exact stage
+__device__ __forceinline__ float vdx(const float4& a, const float4& b) {
+  return __fadd_rn(__fsub_rn(a.x, b.x), __fsub_rn(a.z, b.z));
+}
+__device__ __forceinline__ float vdy(const float4& a, const float4& b) {
+  return __fadd_rn(__fsub_rn(a.y, b.y), __fsub_rn(a.w, b.w));
+}
+__device__ __forceinline__ float fcross(float ax, float ay, float bx, float by) {
+  return __fsub_rn(__fmul_rn(ax, by), __fmul_rn(ay, bx));
+}
+
+// True only when lineSegmentIntersection2 (seg_isect) certainly returns 0
+// for P = (p1, p2), Q = (q1, q2), decided in float from vertex hi/lo pairs.
+//
+// With a = q1 - p1, b = q2 - p1, w = p2 - p1 the four areas seg_isect uses
+// are AP1 = a x b, AQ1 = w x a, AQ2 = w x b and AP2 = AP1 + AQ1 - AQ2.
+//  * If AP1 and AP2 have the same strict sign, |AP1| > 2e-9 and
+//    |AP1| > 2e-9 |AP2|, then alpha = AP1 / (AP1 - AP2) is > 1 or
+//    < -EPSILON, and the collinear branch (|AP1| < EPSILON) is excluded:
+//    the type is 0.
+//  * If AQ1 and AQ2 have the same strict sign, |AQ1| > 2e-9 |AQ2| and
+//    |AP1| > 2e-9, then beta is > 1 or < -EPSILON in the general branch and
+//    the collinear branch is excluded again: the type is 0.
+// Segments that do not meet satisfy one of the two unless they are within
+// the float error of touching.  Each float area carries the bound
+// 32 u m^2 + 64 u^2 m M (u = 2^-24, m = largest difference component,
+// M = coordinate magnitude), at least 2.6 times the worst case of the
+// difference and product rounding; the FP64 areas of seg_isect differ from
+// the exact ones by about 1e-15 m^2, far inside it.
+__device__ __forceinline__ bool certainly_disjoint(const float4& p1, const float4& p2,
+                                                   const float4& q1, const float4& q2) {
+  const float ax = vdx(q1, p1), ay = vdy(q1, p1);
+  const float bx = vdx(q2, p1), by = vdy(q2, p1);
+  const float wx = vdx(p2, p1), wy = vdy(p2, p1);
+  const float AP1 = fcross(ax, ay, bx, by);
+  const float AQ1 = fcross(wx, wy, ax, ay);
+  const float AQ2 = fcross(wx, wy, bx, by);
+  const float AP2 = __fsub_rn(__fadd_rn(AP1, AQ1), AQ2);
+  const float m = fmaxf(fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fmaxf(fabsf(bx), fabsf(by))),
+                        fmaxf(fabsf(wx), fabsf(wy)));
+  const float M = __fadd_rn(fmaxf(fabsf(p1.x), fabsf(p1.y)), __fmul_rn(2.f, m));
+  const float u = 5.9604645e-8f;  // 2^-24
+  const float Bx = __fadd_rn(__fmul_rn(__fmul_rn(32.f * u, m), m),
+                             __fadd_rn(__fmul_rn(__fmul_rn(64.f * u * u, m), M), 1e-30f));
+  const float B2 = __fadd_rn(__fmul_rn(3.f, Bx),
+                             __fmul_rn(4.f * u, __fadd_rn(__fadd_rn(fabsf(AP1), fabsf(AQ1)), fabsf(AQ2))));
+  const float L1 = __fsub_rn(fabsf(AP1), Bx);
+  if (!(L1 > 2e-9f)) return false;  // also keeps the collinear branch out
+  const bool sameP = (AP1 > Bx && AP2 > B2) || (AP1 < -Bx && AP2 < -B2);
+  if (sameP && L1 > __fmul_rn(2e-9f, __fadd_rn(fabsf(AP2), B2))) return true;
+  const bool sameQ = (AQ1 > Bx && AQ2 > Bx) || (AQ1 < -Bx && AQ2 < -Bx);
+  const float LQ1 = __fsub_rn(fabsf(AQ1), Bx);
+  return sameQ && LQ1 > __fmul_rn(2e-9f, __fadd_rn(fabsf(AQ2), Bx));
+}
+
+// Vertex coordinates as float pairs: hi = x rounded to float, lo = (x - hi)
+// rounded to float, so hi + lo is within 2^-48 |x| of the double.
+__global__ void k_vertex_f4(long long nv, const double* __restrict__ xy, float4* __restrict__ out) {
+  long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const double x = xy[2 * v], y = xy[2 * v + 1];
+  const float hx = __double2float_rn(x), hy = __double2float_rn(y);
+  out[v] = make_float4(hx, hy, __double2float_rn(dsub(x, (double)hx)),
+                       __double2float_rn(dsub(y, (double)hy)));
+}
+
+// Exact stage per candidate pair.  Phase 1 (one pair per thread): FP64 LSMF,
+// the emission count and first key, then the float pre-test; pairs it cannot
+// rule out are queued in shared memory.  Phase 2: the queue runs seg_isect
+// in full warps (divergent FP64 lanes would cost a full warp each).
+// counters: [0] unique hits, [1] emissions reaching the FP64 test,
+// [3] emissions with a non-zero type (the reference's raw hit count).
+constexpr int kExBlock = 256;
+constexpr int kExPer = 4;
+constexpr int kExChunk = kExBlock * kExPer;
+
+__global__ void __launch_bounds__(kExBlock)
+k_pair_exact(long long n, const int2* __restrict__ pairs, const int* __restrict__ e_id,
+             const double* __restrict__ bP, const double* __restrict__ cP,
+             const float4* __restrict__ vfB, const float4* __restrict__ vfC,
+             const int2* __restrict__ lr, const int* __restrict__ aft, const int* __restrict__ bef,
+             int logL, unsigned long long* __restrict__ counters, long long cap,
+             int* __restrict__ rb, int* __restrict__ rc, int* __restrict__ rt,
+             unsigned long long* __restrict__ rkey) {
+  __shared__ int4 q[kExChunk];
+  __shared__ unsigned long long qk[kExChunk];
+  __shared__ int qn;
+  __shared__ unsigned long long ntested;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const long long base = (long long)blockIdx.x * kExChunk;
+  if (tid == 0) {
+    qn = 0;
+    ntested = 0;
+  }
+  __syncthreads();
+  unsigned long long my_tested = 0;
+  for (int r = 0; r < kExPer; ++r) {
+    const long long i = base + (long long)r * kExBlock + tid;
+    bool keep = false;
+    int4 e = make_int4(0, 0, 0, 0);
+    unsigned long long key = 0;
+    if (i < n) {
+      const int2 pr = pairs[i];
+      const int bId = e_id[pr.x], cId = e_id[pr.y];
+      const double* pb = bP + bId;
+      const double* pc = cP + cId;
+      if (lsmf_exact(pb[0], pb[1], pb[2], pb[3], pc[0], pc[1], pc[2], pc[3])) {
+        const unsigned cnt = emission(pr.x, pr.y, cId, lr, aft, bef, logL, &key);
+        if (cnt > 0) {
+          my_tested += cnt;
+          if (!certainly_disjoint(vfB[bId >> 1], vfB[(bId >> 1) + 1], vfC[cId >> 1],
+                                  vfC[(cId >> 1) + 1])) {
+            keep = true;
+            e = make_int4(bId, cId, (int)cnt, 0);
+          }
+        }
+      }
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    if (bal) {
+      int w0 = 0;
+      if (lane == 0) w0 = atomicAdd(&qn, __popc(bal));
+      w0 = __shfl_sync(0xffffffffu, w0, 0);
+      if (keep) {
+        q[w0 + __popc(bal & lt)] = e;
+        qk[w0 + __popc(bal & lt)] = key;
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) my_tested += __shfl_xor_sync(0xffffffffu, my_tested, o);
+  if (lane == 0 && my_tested) atomicAdd(&ntested, my_tested);
+  __syncthreads();
+  if (tid == 0 && ntested) atomicAdd(&counters[1], ntested);
+  const int nq = qn;
+  const int nq32 = (nq + 31) & ~31;  // warp-uniform loop bound
+  unsigned long long my_raw = 0;
+  for (int j = tid; j < nq32; j += kExBlock) {
+    bool hit = false;
+    int ty = 0;
+    int4 e = make_int4(0, 0, 0, 0);
+    if (j < nq) {
+      e = q[j];
+      const double* pb = bP + e.x;
+      const double* pc = cP + e.y;
+      double al, be;
+      ty = seg_isect(pb[0], pb[1], pb[2], pb[3], pc[0], pc[1], pc[2], pc[3], &al, &be);
+      hit = ty != 0;
+      if (hit) my_raw += (unsigned)e.z;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, hit);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      unsigned long long hb = 0;
+      if (lane == leader) hb = atomicAdd(&counters[0], (unsigned long long)__popc(m));
+      hb = __shfl_sync(0xffffffffu, hb, leader);
+      if (hit) {
+        const long long idx = (long long)hb + __popc(m & lt);
+        if (idx < cap) {
+          rb[idx] = e.x;
+          rc[idx] = e.y;
+          rt[idx] = ty;
+          rkey[idx] = qk[j];
+        }
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) my_raw += __shfl_xor_sync(0xffffffffu, my_raw, o);
+  if (lane == 0 && my_raw) atomicAdd(&counters[3], my_raw);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host
+int Pipeline::stage_grid() {
+  cudaStream_t st = st_;
+  std::vector<int> hstart(k + 2);
+  hstart[0] = 0;
+  for (int t = 0; t <= k; ++t) hstart[t + 1] = nb + hcc[t];
+  g_tstart = (int*)pool_.get("grid_tstart", sizeof(int) * (k + 2));
+  fbox = (float4*)pool_.get("grid_fbox", sizeof(float4) * (E + 1));
+  auto* bnd = (unsigned*)pool_.get("grid_bnd", 256);
+  auto* sum_ext = (double*)((char*)bnd + 64);
+  vfB = (float4*)pool_.get("grid_vfB", sizeof(float4) * (nb + 1));
+  vfC = (float4*)pool_.get("grid_vfC", sizeof(float4) * ((long long)clSize + k));
+  long long* cnt = (long long*)pool_.get("grid_cnt", sizeof(long long) * (E + 1));
+  g_islong = (unsigned char*)pool_.get("grid_islong", (size_t)E + 1);
+  g_long = (int*)pool_.get("grid_long", sizeof(int) * (E + 1));
+  g_long_count = (unsigned*)pool_.get("grid_long_count", 256);
+  void* sscr = pool_.get("scan_scr_grid", scan_scratch_bytes(E + 1));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (grid)");
+  cudaMemcpyAsync(g_tstart, hstart.data(), sizeof(int) * (k + 2), cudaMemcpyHostToDevice, st);
+  unsigned init[4] = {0xffffffffu, 0xffffffffu, 0u, 0u};
+  cudaMemcpyAsync(bnd, init, sizeof(init), cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(sum_ext, 0, sizeof(double), st);
+  cudaMemsetAsync(g_long_count, 0, sizeof(unsigned), st);
+  {
+    ::sbc::KProbe kp_("k_edge_fbox", st);
+    k_edge_fbox<<<grid_for(E, 256), 256, 0, st>>>(E, e_id, g_tstart, k, bP, cP, fbox, bnd, sum_ext);
+  }
+  {
+    ::sbc::KProbe kp_("k_vertex_f4", st);
+    k_vertex_f4<<<grid_for(nb + 1, 256), 256, 0, st>>>(nb + 1, bP, vfB);
+  }
+  {
+    ::sbc::KProbe kp_("k_vertex_f4", st);
+    k_vertex_f4<<<grid_for((long long)clSize + k, 256), 256, 0, st>>>((long long)clSize + k, cP, vfC);
+  }
+  unsigned hb[4];
+  double hsum = 0.0;
+  cudaMemcpyAsync(hb, bnd, sizeof(hb), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(&hsum, sum_ext, sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "grid bounds");
+  auto unkey = [](unsigned kk) {
+    unsigned u = (kk & 0x80000000u) ? (kk & 0x7fffffffu) : ~kk;
+    float f;
+    memcpy(&f, &u, sizeof f);
+    return f;
+  };
+  const float x0 = unkey(hb[0]), y0 = unkey(hb[1]), x1 = unkey(hb[2]), y1 = unkey(hb[3]);
+  const double spanx = (double)x1 - x0, spany = (double)y1 - y0;
+  // cell size: 1.5 x the mean edge extent, at most 8192 cells per side and
+  // 2^25 cells in all
+  double s = 1.5 * hsum / (E > 0 ? E : 1);
+  s = std::max(s, std::max(spanx, spany) / 8192.0);
+  s = std::max(s, std::sqrt(spanx * spany / 33554432.0));
+  if (!(s > 0.0)) s = 1.0;
+  grid_.x0 = x0;
+  grid_.y0 = y0;
+  grid_.inv = (float)(1.0 / s);
+  grid_.gx = (int)std::min(8192.0, std::floor(spanx / s) + 1.0);
+  grid_.gy = (int)std::min(8192.0, std::floor(spany / s) + 1.0);
+  const Grid g{grid_.x0, grid_.y0, grid_.inv, grid_.gx, grid_.gy};
+  {
+    ::sbc::KProbe kp_("k_grid_count", st);
+    k_grid_count<<<grid_for(E + 1, 256), 256, 0, st>>>(E, fbox, g, cnt, g_islong, g_long,
+                                                     g_long_count);
+  }
+  exclusive_scan_i64(cnt, E + 1, sscr, st);
+  long long total = 0;
+  cudaMemcpyAsync(&total, cnt + E, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "grid count");
+  if (total >= (1LL << 31)) return fail(kEInput, "grid too large");
+  g_n = total;
+  g_keys = (unsigned*)pool_.get("grid_keys", sizeof(unsigned) * (total + 1));
+  g_vals = (unsigned*)pool_.get("grid_vals", sizeof(unsigned) * (total + 1));
+  auto* k2 = (unsigned*)pool_.get("grid_keys2", sizeof(unsigned) * (total + 1));
+  auto* v2 = (unsigned*)pool_.get("grid_vals2", sizeof(unsigned) * (total + 1));
+  int* heads = (int*)pool_.get("grid_heads", sizeof(int) * (total + 2));
+  void* rscr = pool_.get("radix_scr_grid", radix_scratch_bytes(total + 1));
+  void* sscr2 = pool_.get("scan_scr_grid2", scan_scratch_bytes(total + 2));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (grid entries)");
+  if (total > 0) {
+    {
+      ::sbc::KProbe kp_("k_grid_emit", st);
+      k_grid_emit<<<grid_for(E, 256), 256, 0, st>>>(E, fbox, g, cnt, g_islong, g_keys, g_vals);
+    }
+    int bits = 1;
+    while ((1LL << bits) < (long long)grid_.gx * grid_.gy) ++bits;
+    radix_sort_u32(g_keys, g_vals, k2, v2, total, bits, rscr, st);
+  }
+  {
+    ::sbc::KProbe kp_("k_cell_heads", st);
+    k_cell_heads<<<grid_for(total + 1, 256), 256, 0, st>>>(total, g_keys, heads);
+  }
+  exclusive_scan_i32(heads, total + 1, sscr2, st);
+  int nc = 0;
+  cudaMemcpyAsync(&nc, heads + total, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "grid cells");
+  g_nCells = nc;
+  g_cstart = (int*)pool_.get("grid_cstart", sizeof(int) * ((long long)nc + 1));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (grid cells)");
+  {
+    ::sbc::KProbe kp_("k_cell_starts", st);
+    k_cell_starts<<<grid_for(total + 1, 256), 256, 0, st>>>(total, heads, nc, g_cstart);
+  }
+  return kOk;
+}
+
+int Pipeline::stage_candidates(int cType, int** rb_out, int** rc_out, int** rt_out,
+                               unsigned long long** rkey_out, long long* nhits, OverlayOut& out) {
+  cudaStream_t st = st_;
+  const Grid g{grid_.x0, grid_.y0, grid_.inv, grid_.gx, grid_.gy};
+  const int nCells = g_nCells;
+  auto* cdesc = (int4*)pool_.get("cg_desc", sizeof(int4) * ((long long)nCells + 1));
+  int* smalls = (int*)pool_.get("cg_small", sizeof(int) * ((long long)nCells + 1));
+  int* tiles = (int*)pool_.get("cg_tiles", sizeof(int) * ((long long)nCells + 1));
+  long long* work = (long long*)pool_.get("cg_work", sizeof(long long) * ((long long)nCells + 1));
+  auto* counters = (unsigned long long*)pool_.get("cg_counters", 64);
+  void* sscr = pool_.get("scan_scr_cg", scan_scratch_bytes((long long)nCells + 1));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (grid items)");
+  {
+    ::sbc::KProbe kp_("k_cell_items", st);
+    k_cell_items<<<grid_for((long long)nCells + 1, 256), 256, 0, st>>>(
+        nCells, g_cstart, g_vals, g_tstart, cType, cdesc, smalls, tiles, work);
+  }
+  exclusive_scan_i32(smalls, (long long)nCells + 1, sscr, st);
+  exclusive_scan_i32(tiles, (long long)nCells + 1, sscr, st);
+  exclusive_scan_i64(work, (long long)nCells + 1, sscr, st);
+  int nS = 0, nW = 0;
+  long long W = 0;
+  cudaMemcpyAsync(&nS, smalls + nCells, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(&nW, tiles + nCells, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(&W, work + nCells, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "grid items");
+  int* srec = (int*)pool_.get("cg_srec", sizeof(int) * ((long long)nS + 1));
+  auto* wrec = (int2*)pool_.get("cg_wrec", sizeof(int2) * ((long long)nW + 1));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (grid items)");
+  if (nCells > 0) {
+    ::sbc::KProbe kp_("k_cell_expand", st);
+    k_cell_expand<<<grid_for(nCells, 256), 256, 0, st>>>(nCells, smalls, tiles, srec, wrec);
+  }
+  // box-overlapping pairs (grow and retry on overflow)
+  long long cap = pair_cap_ > 0 ? pair_cap_ : 4LL * E + (1 << 20);
+  long long npairs = 0;
+  int2* pairs = nullptr;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    pairs = (int2*)pool_.get("cg_pairs", sizeof(int2) * (cap + 1));
+    if (pool_.failed) return fail(kENoMem, "device allocation failed (candidate pairs)");
+    cudaMemsetAsync(counters, 0, 64, st);
+    if (nS > 0) {
+      ::sbc::KProbe kp_("k_grid_small", st);
+      k_grid_small<<<grid_for(nS, kGBlock), kGBlock, 0, st>>>(srec, nS, cdesc, g_keys, g_vals, fbox, g,
+                                                            &counters[2], cap, pairs);
+    }
+    if (nW > 0) {
+      ::sbc::KProbe kp_("k_grid_warp", st);
+      k_grid_warp<<<grid_for((long long)nW * 32, kGBlock), kGBlock, 0, st>>>(
+          wrec, nW, cdesc, g_keys, g_vals, fbox, g, &counters[2], cap, pairs);
+    }
+    {
+      ::sbc::KProbe kp_("k_grid_long", st);
+      k_grid_long<<<64, kGBlock, 0, st>>>(g_long, g_long_count, g_tstart, cType, g_islong, fbox,
+                                          &counters[2], cap, pairs);
+    }
+    unsigned long long hp = 0;
+    cudaMemcpyAsync(&hp, counters + 2, sizeof(hp), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "candidate pairs");
+    npairs = (long long)hp;
+    if (npairs <= cap) break;
+    cap = npairs + (1 << 20);
+  }
+  pair_cap_ = cap;
+  // exact stage: one record per unique hit
+  long long hcap = npairs + 1;
+  int* rb = (int*)pool_.get("raw_b", sizeof(int) * hcap);
+  int* rc = (int*)pool_.get("raw_c", sizeof(int) * hcap);
+  int* rt = (int*)pool_.get("raw_t", sizeof(int) * hcap);
+  auto* rkey = (unsigned long long*)pool_.get("raw_key", sizeof(unsigned long long) * hcap);
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (hits)");
+  if (npairs > 0) {
+    ::sbc::KProbe kp_("k_pair_exact", st);
+    k_pair_exact<<<grid_for(npairs, kExChunk), kExBlock, 0, st>>>(
+        npairs, pairs, e_id, bP, cP, vfB, vfC, lr, aft, bef, logL, counters, hcap, rb, rc, rt, rkey);
+  }
+  unsigned long long hc[4];
+  cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "exact stage");
+  if ((long long)hc[0] > hcap) return fail(kEInternal, "hit buffer overflow");
+  if (hc[0] >= (1ULL << 31)) return fail(kEInput, "too many intersections");
+  *rb_out = rb;
+  *rc_out = rc;
+  *rt_out = rt;
+  *rkey_out = rkey;
+  *nhits = (long long)hc[0];
+  out.survivors = npairs;
+  out.tests = (long long)hc[1];
+  out.raw_hits = (long long)hc[3];
+  out.work = W;
+  return kOk;
+}
+
+}  // namespace sbc

@@ -410,12 +410,18 @@ __global__ void k_border_check(const double* __restrict__ ea, int epc, double sc
   if (ki == 0) atomicAdd(zcount, 1);
 }
 
+// The two end-list leaves of each edge (insertToLeafLevelEdgeListMulticore,
+// oacc_segment_tree.cpp:2010-2113): the leaf right of its end's border and
+// the leaf left of its start's border; -1 where the reference drops the
+// entry.  An internal node's end list is the set of edges with a leaf below
+// it (buildInternalEndListsMulticore, :1717-1968), so these two leaves are
+// all the end lists hold.  cnt[0] counts the entries.
 __global__ void k_find_leaves(const double* __restrict__ es, const double* __restrict__ ee, int E,
                               Borders B, int logL, int* __restrict__ aft, int* __restrict__ bef,
-                              const int* __restrict__ typeOfEdgeStart, int k, int numLeaves,
-                              int* __restrict__ cnt) {
+                              unsigned long long* __restrict__ cnt) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= E) return;
+  unsigned n = 0;
+  if (e < E) {
   const int L = 1 << logL;
   const double* ea = B.ea;
   int a = -1, b = -1;
@@ -440,34 +446,10 @@ __global__ void k_find_leaves(const double* __restrict__ es, const double* __res
   }
   aft[e] = a;
   bef[e] = b;
-  int cls = 0;
-  while (cls < k && typeOfEdgeStart[cls + 1] <= e) ++cls;  // 0 base, t overlay t
-  if (a >= 0) atomicAdd(&cnt[(size_t)cls * numLeaves + (a - L)], 1);
-  if (b >= 0) atomicAdd(&cnt[(size_t)cls * numLeaves + (b - L)], 1);
-}
-
-__global__ void k_leaf_scatter(const int* __restrict__ aft, const int* __restrict__ bef, int E,
-                               int logL, const int* __restrict__ typeOfEdgeStart, int k,
-                               int numLeaves, const int* __restrict__ off, int* __restrict__ fill,
-                               int* __restrict__ le_edge, int* __restrict__ le_leaf) {
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= E) return;
-  const int L = 1 << logL;
-  int cls = 0;
-  while (cls < k && typeOfEdgeStart[cls + 1] <= e) ++cls;
-  int a = aft[e], b = bef[e];
-  if (a >= 0) {
-    size_t c = (size_t)cls * numLeaves + (a - L);
-    int p = off[c] + atomicAdd(&fill[c], 1);
-    le_edge[p] = e;
-    le_leaf[p] = a - L;
+  n = (a >= 0) + (b >= 0);
   }
-  if (b >= 0) {
-    size_t c = (size_t)cls * numLeaves + (b - L);
-    int p = off[c] + atomicAdd(&fill[c], 1);
-    le_edge[p] = e;
-    le_leaf[p] = b - L;
-  }
+  n = __reduce_add_sync(0xffffffffu, n);
+  if ((threadIdx.x & 31) == 0 && n) atomicAdd(cnt, (unsigned long long)n);
 }
 
 static int digit_count_host(double val) {
@@ -486,21 +468,13 @@ int Pipeline::stage_endlists() {
   if (!(dv < 2147483647.0)) return fail(kEUndef, "coordinate range too large for realToInt");
   int d = digit_count_host(dv);
   double scale = pow(10.0, 11 - d);
-  // edge-index start of each polygon class: base 0, overlay t at nb + cc[t-1]
-  std::vector<int> hstart(k + 2);
-  hstart[0] = 0;
-  for (int t = 0; t <= k; ++t) hstart[t + 1] = nb + hcc[t];
-  int* tstart = (int*)pool_.get("type_start", sizeof(int) * (k + 2));
   int* zc = (int*)pool_.get("zcount", 256);
   aft = (int*)pool_.get("aft", sizeof(int) * E);
   bef = (int*)pool_.get("bef", sizeof(int) * E);
-  size_t ncls = (size_t)(k + 1) * numLeaves;
-  int* cnt = (int*)pool_.get("le_cnt", sizeof(int) * (ncls + 1));
-  int* fill = (int*)pool_.get("le_fill", sizeof(int) * (ncls + 1));
-  void* sscr = pool_.get("scan_scr2", scan_scratch_bytes(ncls + 1));
+  d_treecnt = (unsigned long long*)pool_.get("tree_counts", 256);
   if (pool_.failed) return fail(kENoMem, "device allocation failed (end lists)");
-  cudaMemcpyAsync(tstart, hstart.data(), sizeof(int) * (k + 2), cudaMemcpyHostToDevice, st_);
   cudaMemsetAsync(zc, 0, sizeof(int), st_);
+  cudaMemsetAsync(d_treecnt, 0, 2 * sizeof(unsigned long long), st_);
   clear_flags();
   {
     ::sbc::KProbe kp_("k_border_check", st_);
@@ -513,28 +487,10 @@ int Pipeline::stage_endlists() {
   z_garbage = z;
   // ea[0] < 0 decides the shift; ea[0] equals minI
   Borders B{ea, epc, z};
-  cudaMemsetAsync(cnt, 0, sizeof(int) * (ncls + 1), st_);
   {
     ::sbc::KProbe kp_("k_find_leaves", st_);
-    k_find_leaves<<<grid_for(E, 256), 256, 0, st_>>>(e_s, e_e, E, B, logL, aft, bef, tstart, k,
-                                                   numLeaves, cnt);
+    k_find_leaves<<<grid_for(E, 256), 256, 0, st_>>>(e_s, e_e, E, B, logL, aft, bef, d_treecnt);
   }
-  exclusive_scan_i32(cnt, ncls + 1, sscr, st_);
-  int total = 0;
-  cudaMemcpyAsync(&total, cnt + ncls, sizeof(int), cudaMemcpyDeviceToHost, st_);
-  cudaStreamSynchronize(st_);
-  nLeafEnt = total;
-  le_off = cnt;
-  le_edge = (int*)pool_.get("le_edge", sizeof(int) * (total + 1));
-  le_leaf = (int*)pool_.get("le_leaf", sizeof(int) * (total + 1));
-  if (pool_.failed) return fail(kENoMem, "device allocation failed (leaf entries)");
-  cudaMemsetAsync(fill, 0, sizeof(int) * (ncls + 1), st_);
-  {
-    ::sbc::KProbe kp_("k_leaf_scatter", st_);
-    k_leaf_scatter<<<grid_for(E, 256), 256, 0, st_>>>(aft, bef, E, logL, tstart, k, numLeaves, cnt,
-                                                    fill, le_edge, le_leaf);
-  }
-  stat_leaf = total;
   return kOk;
 }
 
@@ -543,121 +499,61 @@ int Pipeline::stage_endlists() {
 // when v's interval lies inside the edge's [start, end] and recurses into the
 // children whose interval touches it.  A leaf q = [ea[q], ea[q+1]] lies inside
 // iff ea[q] >= start and ea[q+1] <= end; ea is sorted, so those leaves form
-// one range [l, r], every ancestor of a contained node touches the edge, and
+// one range [l, r1), every ancestor of a contained node touches the edge, and
 // the nodes the recursion adds are exactly the canonical decomposition of
-// [l, r] (maximal nodes inside it).  Two binary searches and the bottom-up
-// decomposition give them without the descent.
-template <bool EMIT>
-__global__ void k_cover(const double* __restrict__ es, const double* __restrict__ ee, int E,
-                        const double* __restrict__ ea, int logL, int* __restrict__ count,
-                        const long long* __restrict__ off, unsigned* __restrict__ onode,
-                        unsigned* __restrict__ oedge) {
+// [l, r1) (maximal nodes inside it).  The range is all the candidate stage
+// needs; the lists themselves are never built.  cnt[1] counts their entries.
+__global__ void k_edge_range(const double* __restrict__ es, const double* __restrict__ ee, int E,
+                             const double* __restrict__ ea, int logL, int2* __restrict__ lr,
+                             unsigned long long* __restrict__ cnt) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= E) return;
-  const int L = 1 << logL;
-  double s = es[e], x = ee[e];
-  int lo = 0, hi = L;  // l = first leaf with ea[q] >= s
-  while (lo < hi) {
-    int m = (lo + hi) >> 1;
-    if (ea[m] < s) lo = m + 1;
-    else hi = m;
-  }
-  int l = lo;
-  lo = 0;
-  hi = L;  // r+1 = first leaf with ea[q+1] > x
-  while (lo < hi) {
-    int m = (lo + hi) >> 1;
-    if (ea[m + 1] <= x) lo = m + 1;
-    else hi = m;
-  }
-  int r1 = lo;
-  int n = 0;
-  long long base = EMIT ? off[e] : 0;
-  if (l < r1) {
-    int a = l + L, b = r1 + L;
-    while (a < b) {
+  unsigned n = 0;
+  if (e < E) {
+    const int L = 1 << logL;
+    double s = es[e], x = ee[e];
+    int lo = 0, hi = L;  // l = first leaf with ea[q] >= s
+    while (lo < hi) {
+      int m = (lo + hi) >> 1;
+      if (ea[m] < s) lo = m + 1;
+      else hi = m;
+    }
+    const int l = lo;
+    lo = 0;
+    hi = L;  // r1 = first leaf with ea[q+1] > x
+    while (lo < hi) {
+      int m = (lo + hi) >> 1;
+      if (ea[m + 1] <= x) lo = m + 1;
+      else hi = m;
+    }
+    const int r1 = lo;
+    lr[e] = make_int2(l, r1 > l ? r1 : l);
+    for (int a = l + L, b = r1 + L; a < b; a >>= 1, b >>= 1) {
       if (a & 1) {
-        if (EMIT) {
-          onode[base + n] = (unsigned)a;
-          oedge[base + n] = (unsigned)e;
-        }
         ++n;
         ++a;
       }
       if (b & 1) {
-        --b;
-        if (EMIT) {
-          onode[base + n] = (unsigned)b;
-          oedge[base + n] = (unsigned)e;
-        }
         ++n;
+        --b;
       }
-      a >>= 1;
-      b >>= 1;
     }
   }
-  if (!EMIT) count[e] = n;
-}
-
-__global__ void k_i32_to_i64(const int* __restrict__ a, long long n, long long* __restrict__ b) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) b[i] = a[i];
-}
-
-__global__ void k_node_ranges(const unsigned* __restrict__ node, long long n,
-                              int* __restrict__ nstart, int* __restrict__ nend) {
-  long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  unsigned v = node[p];
-  if (p == 0 || node[p - 1] != v) nstart[v] = (int)p;
-  if (p == n - 1 || node[p + 1] != v) nend[v] = (int)(p + 1);
+  n = __reduce_add_sync(0xffffffffu, n);
+  if ((threadIdx.x & 31) == 0 && n) atomicAdd(cnt + 1, (unsigned long long)n);
 }
 
 int Pipeline::stage_cover() {
-  int* cnt = (int*)pool_.get("cov_cnt", sizeof(int) * (E + 1));
-  long long* off = (long long*)pool_.get("cov_off", sizeof(long long) * (E + 1));
-  void* sscr = pool_.get("scan_scr3", scan_scratch_bytes(E + 1));
-  if (pool_.failed) return fail(kENoMem, "device allocation failed (cover)");
-  clear_flags();
+  lr = (int2*)pool_.get("edge_leaf_range", sizeof(int2) * (E + 1));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (leaf ranges)");
   {
-    ::sbc::KProbe kp_("k_cover", st_);
-    k_cover<false><<<grid_for(E, 128), 128, 0, st_>>>(e_s, e_e, E, ea, logL, cnt, nullptr, nullptr,
-                                                    nullptr);
+    ::sbc::KProbe kp_("k_edge_range", st_);
+    k_edge_range<<<grid_for(E, 256), 256, 0, st_>>>(e_s, e_e, E, ea, logL, lr, d_treecnt);
   }
-  cudaMemsetAsync(cnt + E, 0, sizeof(int), st_);
-  {
-    ::sbc::KProbe kp_("k_i32_to_i64", st_);
-    k_i32_to_i64<<<grid_for(E + 1, 256), 256, 0, st_>>>(cnt, E + 1, off);
-  }
-  exclusive_scan_i64(off, E + 1, sscr, st_);
-  long long total = 0;
-  cudaMemcpyAsync(&total, off + E, sizeof(long long), cudaMemcpyDeviceToHost, st_);
-  cudaStreamSynchronize(st_);
-  if (total >= (1LL << 28)) return fail(kEInput, "more than 2^28 cover-list entries");
-  nCover = total;
-  cov_node = (unsigned*)pool_.get("cov_node", sizeof(unsigned) * (total + 1));
-  cov_edge = (unsigned*)pool_.get("cov_edge", sizeof(unsigned) * (total + 1));
-  auto* tn = (unsigned*)pool_.get("cov_node2", sizeof(unsigned) * (total + 1));
-  auto* te = (unsigned*)pool_.get("cov_edge2", sizeof(unsigned) * (total + 1));
-  void* rscr = pool_.get("radix_scr_cov", radix_scratch_bytes(total + 1));
-  node_start = (int*)pool_.get("node_start", sizeof(int) * ts);
-  node_end = (int*)pool_.get("node_end", sizeof(int) * ts);
-  if (pool_.failed) return fail(kENoMem, "device allocation failed (cover entries)");
-  {
-    ::sbc::KProbe kp_("k_cover", st_);
-    k_cover<true><<<grid_for(E, 128), 128, 0, st_>>>(e_s, e_e, E, ea, logL, nullptr, off, cov_node,
-                                                   cov_edge);
-  }
-  int bits = 1;
-  while ((1LL << bits) < ts) ++bits;
-  radix_sort_u32(cov_node, cov_edge, tn, te, total, bits, rscr, st_);
-  if (total > 0) {
-    {
-      ::sbc::KProbe kp_("k_node_ranges", st_);
-      k_node_ranges<<<grid_for(total, 256), 256, 0, st_>>>(cov_node, total, node_start, node_end);
-    }
-  }
-  stat_cover = total;
+  unsigned long long hc[2] = {0, 0};
+  cudaMemcpyAsync(hc, d_treecnt, sizeof(hc), cudaMemcpyDeviceToHost, st_);
+  if (cudaStreamSynchronize(st_) != cudaSuccess) return fail(kECuda, "leaf ranges");
+  stat_leaf = (long long)hc[0];
+  stat_cover = (long long)hc[1];
   return kOk;
 }
 

@@ -1,6 +1,6 @@
 // sbc_pipeline.cuh -- state of one clipping run (base polygon + k overlays)
-// and the stage entry points implemented in sbc_front.cu / sbc_mid.cu /
-// sbc_back.cu.  One Pipeline per sbc_ctx; every buffer is grow-only so
+// and the stage entry points implemented in sbc_front.cu / sbc_cand.cu /
+// sbc_mid.cu / sbc_back.cu.  One Pipeline per sbc_ctx; every buffer is grow-only so
 // repeated calls of the same size allocate nothing.
 #pragma once
 
@@ -62,7 +62,6 @@ class Pipeline {
   long long stat_edges = 0, stat_epc = 0, stat_ts = 0, stat_cover = 0, stat_leaf = 0;
   // force the serial emulation of the back end (test hook)
   int force_serial_backend = 0;
-  long long sv_cap_ = 0;  // survivor buffer size that sufficed last time
 
   // ---- shared state (public for the stage kernels' launchers) ----
   int nb = 0, k = 0, clSize = 0, E = 0;
@@ -81,15 +80,26 @@ class Pipeline {
   int z_garbage = 0;                   // position of the zero border entry
   int* aft = nullptr;                  // leaf node from the edge's end (or -1)
   int* bef = nullptr;                  // leaf node from the edge's start (or -1)
-  int* le_off = nullptr;               // (k+1)*numLeaves+1 offsets by (class, leaf)
-  int* le_edge = nullptr;              // edge index per leaf entry
-  int* le_leaf = nullptr;              // leaf (relative) per leaf entry
-  long long nLeafEnt = 0;
-  unsigned* cov_node = nullptr;        // cover entries sorted by (node, edge)
-  unsigned* cov_edge = nullptr;
-  long long nCover = 0;
-  int* node_start = nullptr;           // first cover entry of node (valid if node has entries)
-  int* node_end = nullptr;
+  int2* lr = nullptr;                  // per edge: leaves [l, r1) its interval contains
+  unsigned long long* d_treecnt = nullptr;  // [0] end-list leaf entries, [1] cover entries
+  // uniform grid over float edge boxes (candidate pairs, sbc_cand.cu)
+  struct GridParams {
+    float x0 = 0.f, y0 = 0.f, inv = 1.f;
+    int gx = 1, gy = 1;
+  } grid_;
+  int* g_tstart = nullptr;             // edge-index start of each polygon class (k+2)
+  float4* fbox = nullptr;              // float edge boxes, bounds rounded outwards
+  float4* vfB = nullptr;               // base vertices as float hi/lo pairs
+  float4* vfC = nullptr;               // overlay vertices as float hi/lo pairs
+  unsigned char* g_islong = nullptr;   // edge spans too many cells for the grid
+  int* g_long = nullptr;               // those edges
+  unsigned* g_long_count = nullptr;
+  unsigned* g_keys = nullptr;          // cell of each grid entry, sorted
+  unsigned* g_vals = nullptr;          // edge of each grid entry (edge order within a cell)
+  long long g_n = 0;
+  int* g_cstart = nullptr;             // first entry of each occupied cell (+ end)
+  int g_nCells = 0;
+  long long pair_cap_ = 0;             // candidate-pair buffer size that sufficed last time
   unsigned* d_flags = nullptr;         // device error flags (DevFlag bits)
   // intermediate arrays of the last overlay processed (device, diagnostics)
   int *dbg_ub = nullptr, *dbg_uc = nullptr, *dbg_ut = nullptr;
@@ -106,6 +116,9 @@ class Pipeline {
   int stage_elementary();
   int stage_endlists();
   int stage_cover();
+  int stage_grid();
+  int stage_candidates(int cType, int** rb, int** rc, int** rt, unsigned long long** rkey,
+                       long long* nhits, OverlayOut& out);
   int stage_overlay(int cType, OverlayOut& out);
 
   int fail(int code, const std::string& msg) {
