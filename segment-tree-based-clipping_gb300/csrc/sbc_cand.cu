@@ -98,80 +98,81 @@ __global__ void k_edge_fbox(int E, const int* __restrict__ e_id, const int* __re
     k3 = max(k3, __shfl_xor_sync(0xffffffffu, k3, o));
     ext += __shfl_xor_sync(0xffffffffu, ext, o);
   }
+  // one set of atomics per block (same-address atomics serialise)
+  __shared__ unsigned sk[4][8];
+  __shared__ float se[8];
+  const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
+    sk[0][w] = k0;
+    sk[1][w] = k1;
+    sk[2][w] = k2;
+    sk[3][w] = k3;
+    se[w] = ext;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = blockDim.x >> 5;
+    double es = 0.0;
+    for (int i = 1; i < nw; ++i) {
+      k0 = min(k0, sk[0][i]);
+      k1 = min(k1, sk[1][i]);
+      k2 = max(k2, sk[2][i]);
+      k3 = max(k3, sk[3][i]);
+    }
+    for (int i = 0; i < nw; ++i) es += se[i];
     atomicMin(&bnd[0], k0);
     atomicMin(&bnd[1], k1);
     atomicMax(&bnd[2], k2);
     atomicMax(&bnd[3], k3);
-    atomicAdd(sum_ext, (double)ext);
+    atomicAdd(sum_ext, es);
   }
 }
 
-// cells per edge (0 for edges joined by brute force, which go to long_list)
+// Grid entries are grouped by bucket = cell * (k + 1) + polygon class (a
+// counting sort: the order inside a bucket does not matter, each pair is a
+// set element and its emission key fixes its final order).  Edges spanning
+// more than kLongCells cells go to long_list instead.
 __global__ void k_grid_count(int E, const float4* __restrict__ fbox, Grid g,
-                             long long* __restrict__ cnt, unsigned char* __restrict__ islong,
-                             int* __restrict__ long_list, unsigned* __restrict__ long_count) {
+                             const int* __restrict__ tstart, int k, int* __restrict__ bcnt,
+                             unsigned char* __restrict__ islong, int* __restrict__ long_list,
+                             unsigned* __restrict__ long_count) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e > E) return;
-  if (e == E) {
-    cnt[e] = 0;
-    return;
-  }
+  if (e >= E) return;
   const float4 f = fbox[e];
-  const long long n = (long long)(g.cx(f.z) - g.cx(f.x) + 1) * (g.cy(f.w) - g.cy(f.y) + 1);
+  const int x0 = g.cx(f.x), x1 = g.cx(f.z), y0 = g.cy(f.y), y1 = g.cy(f.w);
+  const long long n = (long long)(x1 - x0 + 1) * (y1 - y0 + 1);
   const bool lg = n > kLongCells;
   islong[e] = lg ? 1 : 0;
-  cnt[e] = lg ? 0 : n;
-  if (lg) long_list[atomicAdd(long_count, 1u)] = e;
+  if (lg) {
+    long_list[atomicAdd(long_count, 1u)] = e;
+    return;
+  }
+  const int cls = class_of_edge(tstart, k, e);
+  for (int y = y0; y <= y1; ++y)
+    for (int x = x0; x <= x1; ++x) atomicAdd(&bcnt[((long long)y * g.gx + x) * (k + 1) + cls], 1);
 }
 
-__global__ void k_grid_emit(int E, const float4* __restrict__ fbox, Grid g,
-                            const long long* __restrict__ off, const unsigned char* __restrict__ islong,
-                            unsigned* __restrict__ keys, unsigned* __restrict__ vals) {
+__global__ void k_grid_scatter(int E, const float4* __restrict__ fbox, Grid g,
+                               const int* __restrict__ tstart, int k, const int* __restrict__ bstart,
+                               int* __restrict__ fill, const unsigned char* __restrict__ islong,
+                               unsigned* __restrict__ vals) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E || islong[e]) return;
   const float4 f = fbox[e];
   const int x0 = g.cx(f.x), x1 = g.cx(f.z), y0 = g.cy(f.y), y1 = g.cy(f.w);
-  long long w = off[e];
+  const int cls = class_of_edge(tstart, k, e);
   for (int y = y0; y <= y1; ++y)
     for (int x = x0; x <= x1; ++x) {
-      keys[w] = (unsigned)y * (unsigned)g.gx + (unsigned)x;
-      vals[w] = (unsigned)e;
-      ++w;
+      const long long bkt = ((long long)y * g.gx + x) * (k + 1) + cls;
+      vals[bstart[bkt] + atomicAdd(&fill[bkt], 1)] = (unsigned)e;
     }
 }
 
-__global__ void k_cell_heads(long long n, const unsigned* __restrict__ keys, int* __restrict__ h) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i > n) return;
-  h[i] = (i < n && (i == 0 || keys[i] != keys[i - 1])) ? 1 : 0;
-}
-
-__global__ void k_cell_starts(long long n, const int* __restrict__ hpre, int nCells,
-                              int* __restrict__ cstart) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i > n) return;
-  if (i == n) {
-    cstart[nCells] = (int)n;
-    return;
-  }
-  if (hpre[i + 1] != hpre[i]) cstart[hpre[i]] = (int)i;
-}
-
-__device__ __forceinline__ int lower_bound_v(const unsigned* a, int lo, int hi, unsigned x) {
-  while (lo < hi) {
-    int m = (lo + hi) >> 1;
-    if (a[m] < x) lo = m + 1;
-    else hi = m;
-  }
-  return lo;
-}
-
-// per cell: {first entry, base entries, first cType entry, cType entries};
-// whether it is a small product (one thread) and its warp tiles otherwise
-__global__ void k_cell_items(int nCells, const int* __restrict__ cstart,
-                             const unsigned* __restrict__ vals, const int* __restrict__ tstart,
-                             int cType, int4* __restrict__ cdesc, int* __restrict__ smalls,
+// per cell: {first base entry, base entries, first cType entry, cType
+// entries}; whether it is a small product (one thread) and its warp tiles
+// otherwise
+__global__ void k_cell_items(int nCells, const int* __restrict__ bstart, int k, int cType,
+                             int4* __restrict__ cdesc, int* __restrict__ smalls,
                              int* __restrict__ tiles, long long* __restrict__ work) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c > nCells) return;
@@ -181,10 +182,9 @@ __global__ void k_cell_items(int nCells, const int* __restrict__ cstart,
     work[c] = 0;
     return;
   }
-  const int a = cstart[c], z = cstart[c + 1];
-  const int nB = lower_bound_v(vals, a, z, (unsigned)tstart[1]) - a;
-  const int cs = lower_bound_v(vals, a, z, (unsigned)tstart[cType]);
-  const int nC = lower_bound_v(vals, cs, z, (unsigned)tstart[cType + 1]) - cs;
+  const long long b0 = (long long)c * (k + 1);
+  const int a = bstart[b0], nB = bstart[b0 + 1] - a;
+  const int cs = bstart[b0 + cType], nC = bstart[b0 + cType + 1] - cs;
   const long long prod = (long long)nB * nC;
   cdesc[c] = make_int4(a, nB, cs, nC);
   smalls[c] = (prod > 0 && prod <= kGSmallMax) ? 1 : 0;
@@ -243,7 +243,7 @@ __device__ __forceinline__ bool pair_here(const float4& a, const float4& b, cons
 // small cell products: one thread per cell, the warp's threads in lockstep
 __global__ void __launch_bounds__(kGBlock)
 k_grid_small(const int* __restrict__ srec, int nS, const int4* __restrict__ cdesc,
-             const unsigned* __restrict__ keys, const unsigned* __restrict__ vals,
+             const unsigned* __restrict__ vals,
              const float4* __restrict__ fbox, Grid g, unsigned long long* __restrict__ counter,
              long long cap, int2* __restrict__ out) {
   __shared__ int2 stage[kGBlock / 32][kGStage];
@@ -254,10 +254,10 @@ k_grid_small(const int* __restrict__ srec, int nS, const int4* __restrict__ cdes
   int4 d = make_int4(0, 0, 0, 1);
   int gxc = 0, gyc = 0, prod = 0;
   if (i < nS) {
-    d = cdesc[srec[i]];
-    const unsigned key = keys[d.x];
-    gxc = (int)(key % (unsigned)g.gx);
-    gyc = (int)(key / (unsigned)g.gx);
+    const int cell = srec[i];
+    d = cdesc[cell];
+    gxc = cell % g.gx;
+    gyc = cell / g.gx;
     prod = d.y * d.w;
   }
   const int maxp = __reduce_max_sync(0xffffffffu, prod);
@@ -287,7 +287,7 @@ k_grid_small(const int* __restrict__ srec, int nS, const int4* __restrict__ cdes
 // entries broadcast 32 at a time
 __global__ void __launch_bounds__(kGBlock)
 k_grid_warp(const int2* __restrict__ wrec, int nW, const int4* __restrict__ cdesc,
-            const unsigned* __restrict__ keys, const unsigned* __restrict__ vals,
+            const unsigned* __restrict__ vals,
             const float4* __restrict__ fbox, Grid g, unsigned long long* __restrict__ counter,
             long long cap, int2* __restrict__ out) {
   __shared__ int2 stage[kGBlock / 32][kGStage];
@@ -297,8 +297,7 @@ k_grid_warp(const int2* __restrict__ wrec, int nW, const int4* __restrict__ cdes
   Stage st{stage[threadIdx.x >> 5], 0};
   const int2 r = wrec[it];
   const int4 d = cdesc[r.x];
-  const unsigned key = keys[d.x];
-  const int gxc = (int)(key % (unsigned)g.gx), gyc = (int)(key / (unsigned)g.gx);
+  const int gxc = r.x % g.gx, gyc = r.x / g.gx;
   const int j = r.y * 32 + lane;
   const bool cvalid = j < d.w;
   const int ce = cvalid ? (int)vals[d.z + j] : 0;
@@ -616,11 +615,9 @@ int Pipeline::stage_grid() {
   auto* sum_ext = (double*)((char*)bnd + 64);
   vfB = (float4*)pool_.get("grid_vfB", sizeof(float4) * (nb + 1));
   vfC = (float4*)pool_.get("grid_vfC", sizeof(float4) * ((long long)clSize + k));
-  long long* cnt = (long long*)pool_.get("grid_cnt", sizeof(long long) * (E + 1));
   g_islong = (unsigned char*)pool_.get("grid_islong", (size_t)E + 1);
   g_long = (int*)pool_.get("grid_long", sizeof(int) * (E + 1));
   g_long_count = (unsigned*)pool_.get("grid_long_count", 256);
-  void* sscr = pool_.get("scan_scr_grid", scan_scratch_bytes(E + 1));
   if (pool_.failed) return fail(kENoMem, "device allocation failed (grid)");
   cudaMemcpyAsync(g_tstart, hstart.data(), sizeof(int) * (k + 2), cudaMemcpyHostToDevice, st);
   unsigned init[4] = {0xffffffffu, 0xffffffffu, 0u, 0u};
@@ -652,11 +649,12 @@ int Pipeline::stage_grid() {
   };
   const float x0 = unkey(hb[0]), y0 = unkey(hb[1]), x1 = unkey(hb[2]), y1 = unkey(hb[3]);
   const double spanx = (double)x1 - x0, spany = (double)y1 - y0;
-  // cell size: 1.5 x the mean edge extent, at most 8192 cells per side and
-  // 2^25 cells in all
+  // cell size: 1.5 x the mean edge extent, with at most max(2^21, 4E)
+  // (cell, class) buckets in all
+  const double maxBuckets = std::max(2097152.0, 4.0 * E);
   double s = 1.5 * hsum / (E > 0 ? E : 1);
   s = std::max(s, std::max(spanx, spany) / 8192.0);
-  s = std::max(s, std::sqrt(spanx * spany / 33554432.0));
+  s = std::max(s, std::sqrt(spanx * spany * (k + 1) / maxBuckets));
   if (!(s > 0.0)) s = 1.0;
   grid_.x0 = x0;
   grid_.y0 = y0;
@@ -664,48 +662,31 @@ int Pipeline::stage_grid() {
   grid_.gx = (int)std::min(8192.0, std::floor(spanx / s) + 1.0);
   grid_.gy = (int)std::min(8192.0, std::floor(spany / s) + 1.0);
   const Grid g{grid_.x0, grid_.y0, grid_.inv, grid_.gx, grid_.gy};
+  g_nCells = grid_.gx * grid_.gy;
+  const long long nBk = (long long)g_nCells * (k + 1);
+  g_bstart = (int*)pool_.get("grid_bstart", sizeof(int) * (nBk + 1));
+  int* fill = (int*)pool_.get("grid_fill", sizeof(int) * (nBk + 1));
+  void* sscr2 = pool_.get("scan_scr_grid2", scan_scratch_bytes(nBk + 1));
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (grid buckets)");
+  cudaMemsetAsync(g_bstart, 0, sizeof(int) * (nBk + 1), st);
+  cudaMemsetAsync(fill, 0, sizeof(int) * (nBk + 1), st);
   {
     ::sbc::KProbe kp_("k_grid_count", st);
-    k_grid_count<<<grid_for(E + 1, 256), 256, 0, st>>>(E, fbox, g, cnt, g_islong, g_long,
-                                                     g_long_count);
+    k_grid_count<<<grid_for(E, 256), 256, 0, st>>>(E, fbox, g, g_tstart, k, g_bstart, g_islong,
+                                                 g_long, g_long_count);
   }
-  exclusive_scan_i64(cnt, E + 1, sscr, st);
-  long long total = 0;
-  cudaMemcpyAsync(&total, cnt + E, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  exclusive_scan_i32(g_bstart, nBk + 1, sscr2, st);
+  int total = 0;
+  cudaMemcpyAsync(&total, g_bstart + nBk, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "grid count");
-  if (total >= (1LL << 31)) return fail(kEInput, "grid too large");
+  if (total < 0) return fail(kEInput, "grid too large");
   g_n = total;
-  g_keys = (unsigned*)pool_.get("grid_keys", sizeof(unsigned) * (total + 1));
-  g_vals = (unsigned*)pool_.get("grid_vals", sizeof(unsigned) * (total + 1));
-  auto* k2 = (unsigned*)pool_.get("grid_keys2", sizeof(unsigned) * (total + 1));
-  auto* v2 = (unsigned*)pool_.get("grid_vals2", sizeof(unsigned) * (total + 1));
-  int* heads = (int*)pool_.get("grid_heads", sizeof(int) * (total + 2));
-  void* rscr = pool_.get("radix_scr_grid", radix_scratch_bytes(total + 1));
-  void* sscr2 = pool_.get("scan_scr_grid2", scan_scratch_bytes(total + 2));
+  g_vals = (unsigned*)pool_.get("grid_vals", sizeof(unsigned) * ((long long)total + 1));
   if (pool_.failed) return fail(kENoMem, "device allocation failed (grid entries)");
   if (total > 0) {
-    {
-      ::sbc::KProbe kp_("k_grid_emit", st);
-      k_grid_emit<<<grid_for(E, 256), 256, 0, st>>>(E, fbox, g, cnt, g_islong, g_keys, g_vals);
-    }
-    int bits = 1;
-    while ((1LL << bits) < (long long)grid_.gx * grid_.gy) ++bits;
-    radix_sort_u32(g_keys, g_vals, k2, v2, total, bits, rscr, st);
-  }
-  {
-    ::sbc::KProbe kp_("k_cell_heads", st);
-    k_cell_heads<<<grid_for(total + 1, 256), 256, 0, st>>>(total, g_keys, heads);
-  }
-  exclusive_scan_i32(heads, total + 1, sscr2, st);
-  int nc = 0;
-  cudaMemcpyAsync(&nc, heads + total, sizeof(int), cudaMemcpyDeviceToHost, st);
-  if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "grid cells");
-  g_nCells = nc;
-  g_cstart = (int*)pool_.get("grid_cstart", sizeof(int) * ((long long)nc + 1));
-  if (pool_.failed) return fail(kENoMem, "device allocation failed (grid cells)");
-  {
-    ::sbc::KProbe kp_("k_cell_starts", st);
-    k_cell_starts<<<grid_for(total + 1, 256), 256, 0, st>>>(total, heads, nc, g_cstart);
+    ::sbc::KProbe kp_("k_grid_scatter", st);
+    k_grid_scatter<<<grid_for(E, 256), 256, 0, st>>>(E, fbox, g, g_tstart, k, g_bstart, fill,
+                                                   g_islong, g_vals);
   }
   return kOk;
 }
@@ -724,8 +705,8 @@ int Pipeline::stage_candidates(int cType, int** rb_out, int** rc_out, int** rt_o
   if (pool_.failed) return fail(kENoMem, "device allocation failed (grid items)");
   {
     ::sbc::KProbe kp_("k_cell_items", st);
-    k_cell_items<<<grid_for((long long)nCells + 1, 256), 256, 0, st>>>(
-        nCells, g_cstart, g_vals, g_tstart, cType, cdesc, smalls, tiles, work);
+    k_cell_items<<<grid_for((long long)nCells + 1, 256), 256, 0, st>>>(nCells, g_bstart, k, cType,
+                                                                       cdesc, smalls, tiles, work);
   }
   exclusive_scan_i32(smalls, (long long)nCells + 1, sscr, st);
   exclusive_scan_i32(tiles, (long long)nCells + 1, sscr, st);
@@ -753,13 +734,13 @@ int Pipeline::stage_candidates(int cType, int** rb_out, int** rc_out, int** rt_o
     cudaMemsetAsync(counters, 0, 64, st);
     if (nS > 0) {
       ::sbc::KProbe kp_("k_grid_small", st);
-      k_grid_small<<<grid_for(nS, kGBlock), kGBlock, 0, st>>>(srec, nS, cdesc, g_keys, g_vals, fbox, g,
+      k_grid_small<<<grid_for(nS, kGBlock), kGBlock, 0, st>>>(srec, nS, cdesc, g_vals, fbox, g,
                                                             &counters[2], cap, pairs);
     }
     if (nW > 0) {
       ::sbc::KProbe kp_("k_grid_warp", st);
       k_grid_warp<<<grid_for((long long)nW * 32, kGBlock), kGBlock, 0, st>>>(
-          wrec, nW, cdesc, g_keys, g_vals, fbox, g, &counters[2], cap, pairs);
+          wrec, nW, cdesc, g_vals, fbox, g, &counters[2], cap, pairs);
     }
     {
       ::sbc::KProbe kp_("k_grid_long", st);

@@ -32,25 +32,22 @@ __global__ void k_iota_keys(const int* __restrict__ rb, long long n, unsigned* _
   vals[i] = (unsigned)i;
 }
 
-__global__ void k_seg_heads(const unsigned* __restrict__ keys, long long n, int* __restrict__ h) {
+// hits grouped by base edge (bId = 2 x vertex index): counts, then positions
+__global__ void k_bucket_count(const int* __restrict__ rb, long long n, int* __restrict__ cnt) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i > n) return;
-  h[i] = (i < n && (i == 0 || keys[i] != keys[i - 1])) ? 1 : 0;
+  if (i >= n) return;
+  atomicAdd(&cnt[rb[i] >> 1], 1);
 }
 
-__global__ void k_seg_starts(const int* __restrict__ hs, long long n, int* __restrict__ start) {
+__global__ void k_bucket_scatter(const int* __restrict__ rb, long long n,
+                                 const int* __restrict__ start, int* __restrict__ fill,
+                                 unsigned* __restrict__ out) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i > n) return;
-  if (i == n) {
-    start[hs[n]] = (int)n;
-    return;
-  }
-  if (hs[i + 1] != hs[i]) start[hs[i]] = (int)i;
+  if (i >= n) return;
+  const int b = rb[i] >> 1;
+  out[start[b] + atomicAdd(&fill[b], 1)] = (unsigned)i;
 }
 
-// per base edge: order hits by emission key, keep the first hit of each
-// overlay edge (removeDuplicatesAtEdge); ord[] receives raw indices in key
-// order, keep[] the flags
 // Segments (hits of one base edge, or records of one edge) longer than
 // kSegShort go to a warp-per-segment ranking kernel; shorter ones are sorted
 // by one thread.
@@ -439,40 +436,30 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
     if (rc0) return rc0;
   }
 
-  // ---- A9 dedup: stable sort by base id, per-edge key order, first per overlay edge
+  // ---- A9 dedup: hits grouped by base edge (counting sort), put in key order
+  // per edge, first occurrence per overlay edge kept
   long long R = nraw;
-  auto* sk = (unsigned*)pool_.get("dd_keys", sizeof(unsigned) * (R + 1));
   auto* sv = (unsigned*)pool_.get("dd_vals", sizeof(unsigned) * (R + 1));
-  auto* sk2 = (unsigned*)pool_.get("dd_keys2", sizeof(unsigned) * (R + 1));
-  auto* sv2 = (unsigned*)pool_.get("dd_vals2", sizeof(unsigned) * (R + 1));
-  int* heads = (int*)pool_.get("dd_heads", sizeof(int) * (R + 2));
-  int* segstart = (int*)pool_.get("dd_segstart", sizeof(int) * (R + 2));
+  int* segstart = (int*)pool_.get("dd_segstart", sizeof(int) * ((long long)bSize + 2));
+  int* bfill = (int*)pool_.get("dd_bfill", sizeof(int) * ((long long)bSize + 2));
   auto* ord = (unsigned*)pool_.get("dd_ord", sizeof(unsigned) * (R + 1));
   int* keep = (int*)pool_.get("dd_keep", sizeof(int) * (R + 2));
-  void* rscr = pool_.get("radix_scr_dd", radix_scratch_bytes(R + 1));
-  void* sscr2 = pool_.get("scan_scr5", scan_scratch_bytes(R + 2));
+  void* sscr2 = pool_.get("scan_scr5", scan_scratch_bytes(R + 2 > bSize + 2 ? R + 2 : bSize + 2));
   if (pool_.failed) return fail(kENoMem, "device allocation failed (dedup)");
   int K = 0;
-  int nseg = 0;
+  const int nseg = bSize;
   if (R > 0) {
+    cudaMemsetAsync(segstart, 0, sizeof(int) * ((long long)bSize + 1), st);
+    cudaMemsetAsync(bfill, 0, sizeof(int) * ((long long)bSize + 1), st);
     {
-      ::sbc::KProbe kp_("k_iota_keys", st);
-      k_iota_keys<<<grid_for(R, 256), 256, 0, st>>>(rb, R, sk, sv);
+      ::sbc::KProbe kp_("k_bucket_count", st);
+      k_bucket_count<<<grid_for(R, 256), 256, 0, st>>>(rb, R, segstart);
     }
-    int bits = 1;
-    while ((1LL << bits) < 2LL * bSize) ++bits;
-    radix_sort_u32(sk, sv, sk2, sv2, R, bits, rscr, st);
+    exclusive_scan_i32(segstart, (long long)bSize + 1, sscr2, st);
     {
-      ::sbc::KProbe kp_("k_seg_heads", st);
-      k_seg_heads<<<grid_for(R + 1, 256), 256, 0, st>>>(sk, R, heads);
+      ::sbc::KProbe kp_("k_bucket_scatter", st);
+      k_bucket_scatter<<<grid_for(R, 256), 256, 0, st>>>(rb, R, segstart, bfill, sv);
     }
-    exclusive_scan_i32(heads, R + 1, sscr2, st);
-    cudaMemcpyAsync(&nseg, heads + R, sizeof(int), cudaMemcpyDeviceToHost, st);
-    {
-      ::sbc::KProbe kp_("k_seg_starts", st);
-      k_seg_starts<<<grid_for(R + 1, 256), 256, 0, st>>>(heads, R, segstart);
-    }
-    cudaStreamSynchronize(st);
     int* long_list = (int*)pool_.get("seg_long_list", sizeof(int) * ((long long)nseg + 1));
     auto* long_count = (unsigned*)pool_.get("seg_long_count", 256);
     if (pool_.failed) return fail(kENoMem, "device allocation failed (dedup lists)");

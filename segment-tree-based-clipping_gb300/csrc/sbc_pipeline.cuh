@@ -94,11 +94,10 @@ class Pipeline {
   unsigned char* g_islong = nullptr;   // edge spans too many cells for the grid
   int* g_long = nullptr;               // those edges
   unsigned* g_long_count = nullptr;
-  unsigned* g_keys = nullptr;          // cell of each grid entry, sorted
-  unsigned* g_vals = nullptr;          // edge of each grid entry (edge order within a cell)
+  int* g_bstart = nullptr;             // first entry of each (cell, class) bucket (+ end)
+  unsigned* g_vals = nullptr;          // edge of each grid entry, grouped by bucket
   long long g_n = 0;
-  int* g_cstart = nullptr;             // first entry of each occupied cell (+ end)
-  int g_nCells = 0;
+  int g_nCells = 0;                    // gx * gy
   long long pair_cap_ = 0;             // candidate-pair buffer size that sufficed last time
   unsigned* d_flags = nullptr;         // device error flags (DevFlag bits)
   // intermediate arrays of the last overlay processed (device, diagnostics)

@@ -192,7 +192,7 @@ namespace {
 
 constexpr int kRadThreads = 256;
 constexpr int kRadWarps = kRadThreads / 32;
-constexpr int kRadRounds = 8;                               // 32-key rounds per warp
+constexpr int kRadRounds = 16;                              // 32-key rounds per warp
 constexpr int kRadTile = kRadThreads * kRadRounds;          // 2048 keys per block
 
 template <typename K>
@@ -297,20 +297,26 @@ void radix_sort_impl(K* keys, unsigned* vals, K* keys_tmp, unsigned* vals_tmp, l
   K* d_and = d_or + 1;
   unsigned* hist = (unsigned*)((char*)scratch + 64);
   void* sscr = (char*)scratch + 64 + (((size_t)256 * nblocks * sizeof(unsigned) + 255) / 256) * 256;
-  K h_or = 0, h_and = ~K(0);
-  cudaMemcpyAsync(d_or, &h_or, sizeof(K), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(d_and, &h_and, sizeof(K), cudaMemcpyHostToDevice, st);
-  unsigned g = (unsigned)((n + 1023) / 1024);
-  if (g > 2048) g = 2048;
-  {
-    ::sbc::KProbe kp_("k_bits_reduce", st);
-    k_bits_reduce<K><<<g, 1024, 0, st>>>(keys, n, d_or, d_and);
+  // 64-bit keys (doubles) often have constant high digits: one OR/AND
+  // reduction (and a host round trip) finds the digits worth sorting.  For
+  // 32-bit keys the caller's key_bits already bounds the passes.
+  K vary = ~K(0);
+  if (sizeof(K) == 8) {
+    K h_or = 0, h_and = ~K(0);
+    cudaMemcpyAsync(d_or, &h_or, sizeof(K), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_and, &h_and, sizeof(K), cudaMemcpyHostToDevice, st);
+    unsigned g = (unsigned)((n + 1023) / 1024);
+    if (g > 2048) g = 2048;
+    {
+      ::sbc::KProbe kp_("k_bits_reduce", st);
+      k_bits_reduce<K><<<g, 1024, 0, st>>>(keys, n, d_or, d_and);
+    }
+    K o, a;
+    cudaMemcpyAsync(&o, d_or, sizeof(K), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&a, d_and, sizeof(K), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    vary = o ^ a;
   }
-  K o, a;
-  cudaMemcpyAsync(&o, d_or, sizeof(K), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(&a, d_and, sizeof(K), cudaMemcpyDeviceToHost, st);
-  cudaStreamSynchronize(st);
-  K vary = o ^ a;
   K* src_k = keys;
   unsigned* src_v = vals;
   K* dst_k = keys_tmp;
