@@ -42,6 +42,7 @@ int Pipeline::run(const double* d_bxy, int nb_, const double* d_cxy, const int* 
   for (int t = 1; t <= k && !rc; ++t) rc = stage_overlay(t, outs_[t - 1]);
   mark(5);
   if (cudaGetLastError() != cudaSuccess && !rc) rc = fail(kECuda, "CUDA error in the pipeline");
+  if (scan_error_take() && !rc) rc = fail(kEInternal, "a scan's bounded wait gave up");
   if (timing) {
     cudaEventSynchronize(ev[5]);
     for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&times.ms[i], ev[i], ev[i + 1]);

@@ -128,6 +128,8 @@ size_t scan_scratch_bytes(long long n);
 // (optional) the total.
 void exclusive_scan_i32(int* d, long long n, void* scratch, cudaStream_t st);
 void exclusive_scan_i64(long long* d, long long n, void* scratch, cudaStream_t st);
+// true (and cleared) if a scan's bounded look-back wait gave up since the last call
+bool scan_error_take();
 
 // Stable LSD radix sort of (key, value) pairs, 8-bit digits, only the digit
 // positions that vary are sorted.  keys/vals are sorted in place; tmp buffers

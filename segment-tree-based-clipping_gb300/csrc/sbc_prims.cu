@@ -146,7 +146,101 @@ __global__ void k_scan_apply(T* __restrict__ d, long long n, const T* __restrict
 }
 
 template <typename T>
+void scan_multi(T* d, long long n, T* scratch, cudaStream_t st);
+
+// Single-pass scan with decoupled look-back.  Each block takes the next
+// tile index from a counter (so every earlier tile is already resident),
+// publishes its tile total, then warp 0 walks back over the predecessors 32
+// at a time, summing totals until it meets a tile that has published its
+// inclusive prefix, and publishes its own.  Status words: bits 63..62 =
+// 0 not ready / 1 total / 2 inclusive prefix, bits 61..0 = value (scanned
+// values are non-negative counts).  Every wait is bounded; a wait that gives
+// up sets g_scan_error (checked by the caller's pipeline) and carries on.
+constexpr unsigned long long kLbTotal = 1ull << 62, kLbPrefix = 2ull << 62;
+constexpr unsigned long long kLbMask = (1ull << 62) - 1;
+constexpr unsigned kLbSpin = 1u << 20;
+__device__ unsigned g_scan_error = 0;
+
+template <typename T>
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_lb(T* __restrict__ d, long long n, unsigned long long* __restrict__ state) {
+  __shared__ T sw[32];
+  __shared__ unsigned s_tile;
+  __shared__ T s_prefix;
+  if (threadIdx.x == 0) s_tile = atomicAdd((unsigned*)state, 1u);
+  __syncthreads();
+  const unsigned tile = s_tile;
+  unsigned long long* ts = state + 1;
+  const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
+  T v[kScanItems];
+  T s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    v[i] = (base + i < n) ? d[base + i] : T(0);
+    s += v[i];
+  }
+  T tot;
+  const T ex = block_exclusive_scan<T>(s, sw, &tot);
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    T prefix = 0;
+    if (tile == 0) {
+      if (lane == 0) atomicExch(&ts[0], kLbPrefix | ((unsigned long long)tot & kLbMask));
+    } else {
+      if (lane == 0) atomicExch(&ts[tile], kLbTotal | ((unsigned long long)tot & kLbMask));
+      long long top = (long long)tile - 1;
+      bool done = false;
+      while (!done) {
+        const long long j = top - lane;
+        unsigned long long w = kLbPrefix;  // before tile 0: nothing to add
+        if (j >= 0) {
+          unsigned spins = 0;
+          do {
+            w = *(volatile unsigned long long*)&ts[j];
+          } while ((w >> 62) == 0 && ++spins < kLbSpin);
+          if ((w >> 62) == 0) {
+            atomicOr(&g_scan_error, 1u);
+            w = kLbPrefix;
+          }
+        }
+        const unsigned pm = __ballot_sync(0xffffffffu, (w >> 62) == 2);
+        const int firstP = pm ? __ffs(pm) - 1 : 32;
+        T val = (lane <= firstP && j >= 0) ? (T)(w & kLbMask) : T(0);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+        prefix += val;
+        done = pm != 0;
+        top -= 32;
+      }
+      if (lane == 0) atomicExch(&ts[tile], kLbPrefix | ((unsigned long long)(prefix + tot) & kLbMask));
+    }
+    if (lane == 0) s_prefix = prefix;
+  }
+  __syncthreads();
+  T run = ex + s_prefix;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    if (base + i < n) d[base + i] = run;
+    run += v[i];
+  }
+}
+
+template <typename T>
 void scan_rec(T* d, long long n, T* scratch, cudaStream_t st) {
+  if (n <= 0) return;
+  const long long tiles = (n + kScanTile - 1) / kScanTile;
+  if (tiles > 1) {
+    auto* state = (unsigned long long*)scratch;
+    cudaMemsetAsync(state, 0, sizeof(unsigned long long) * (tiles + 1), st);
+    ::sbc::KProbe kp_("k_scan_lb", st);
+    k_scan_lb<T><<<(unsigned)tiles, kScanThreads, 0, st>>>(d, n, state);
+    return;
+  }
+  scan_multi(d, n, scratch, st);
+}
+
+template <typename T>
+void scan_multi(T* d, long long n, T* scratch, cudaStream_t st) {
   if (n <= 0) return;
   long long nb = (n + kScanTile - 1) / kScanTile;
   if (nb == 1) {
@@ -161,7 +255,7 @@ void scan_rec(T* d, long long n, T* scratch, cudaStream_t st) {
     ::sbc::KProbe kp_("k_scan_reduce", st);
     k_scan_reduce<T><<<(unsigned)nb, kScanThreads, 0, st>>>(d, n, sums);
   }
-  scan_rec<T>(sums, nb, scratch + ((nb + 63) / 64) * 64, st);
+  scan_multi<T>(sums, nb, scratch + ((nb + 63) / 64) * 64, st);
   {
     ::sbc::KProbe kp_("k_scan_apply", st);
     k_scan_apply<T><<<(unsigned)nb, kScanThreads, 0, st>>>(d, n, sums);
@@ -171,13 +265,24 @@ void scan_rec(T* d, long long n, T* scratch, cudaStream_t st) {
 }  // namespace
 
 size_t scan_scratch_bytes(long long n) {
+  const size_t lb = (size_t)((n + kScanTile - 1) / kScanTile + 1) * sizeof(unsigned long long);
   size_t tot = 0;
   while (n > kScanTile) {
     long long nb = (n + kScanTile - 1) / kScanTile;
     tot += (size_t)((nb + 63) / 64) * 64 * sizeof(long long);
     n = nb;
   }
-  return tot + 256;
+  return (tot > lb ? tot : lb) + 256;
+}
+
+bool scan_error_take() {
+  unsigned h = 0;
+  cudaMemcpyFromSymbol(&h, g_scan_error, sizeof(h));
+  if (h) {
+    const unsigned z = 0;
+    cudaMemcpyToSymbol(g_scan_error, &z, sizeof(z));
+  }
+  return h != 0;
 }
 
 void exclusive_scan_i32(int* d, long long n, void* scratch, cudaStream_t st) {
