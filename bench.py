@@ -133,25 +133,24 @@ class ClockSampler:
 
 
 # Algorithmic bytes per launch of the kernels that can dominate a step, from
-# the run's statistics.  The candidate kernels count 64 B per candidate pair
-# tested (the two edges' coordinates); the tree kernels count their inputs
-# and outputs once.
+# the run's statistics.  The exact candidate kernel counts 64 B per
+# box-overlapping edge pair (the two edges' coordinates); the tree kernels
+# count their inputs and outputs once.
 def algorithmic_bytes(kernel: str, st: dict, launches: int):
     E = st["edges"]
     P = 2 * E
     per = max(launches, 1)
-    if kernel in ("k_cand_test", "k_cand_exact"):
-        return 64.0 * st["candidates_tested"] / per
+    if kernel == "k_pair_exact":
+        # the two edges' coordinates of every box-overlapping pair (64 B)
+        return 64.0 * st["grid_pairs"] / per
     if kernel == "k_rad_scatter_u64":
         return 24.0 * P  # read (key 8 + value 4) and write them once per pass
     if kernel == "k_rad_hist_u64":
         return 8.0 * P
-    if kernel == "k_cover":
-        return (16.0 * E + 8.0 * st["cover_entries"]) / per
     if kernel == "k_find_leaves":
         return 16.0 * E + 8.0 * E
-    if kernel == "k_rad_scatter_u32":
-        return 16.0 * st["cover_entries"]
+    if kernel == "k_edge_range":
+        return 16.0 * E + 8.0 * E
     return None
 
 

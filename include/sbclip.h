@@ -79,14 +79,15 @@ int sbc_clip_pair_device(sbc_ctx* ctx, const double* d_b_xy, int nb, const doubl
 #define SBC_STAT_TREE_SIZE 2
 #define SBC_STAT_COVER_ENTRIES 3
 #define SBC_STAT_LEAF_END_ENTRIES 4
-#define SBC_STAT_CANDIDATES_TESTED 5    /* overlay 1: pairs reaching the FP64 test */
-#define SBC_STAT_RAW_HITS 6             /* overlay 1 */
+#define SBC_STAT_CANDIDATES_TESTED 5    /* overlay 1: emissions passing LSMF (the reference's tests) */
+#define SBC_STAT_RAW_HITS 6             /* overlay 1: the reference's raw candidate hits */
 #define SBC_STAT_UNIQUE 7               /* overlay 1: unique intersecting edge pairs */
 #define SBC_STAT_SLOTS_B 8
 #define SBC_STAT_SLOTS_C 9
 #define SBC_STAT_SERIAL_BACKEND 10      /* 1 if the exact serial back end ran */
-#define SBC_STAT_WORK_UNITS 11          /* overlay 1: candidate pairs enumerated (cover x cover + cover x end) */
-#define SBC_STAT_NUM 12
+#define SBC_STAT_WORK_UNITS 11          /* overlay 1: edge-box pairs tested by the grid join */
+#define SBC_STAT_GRID_PAIRS 12          /* overlay 1: box-overlapping edge pairs the grid found */
+#define SBC_STAT_NUM 13
 int sbc_stats(const sbc_ctx* ctx, long long* out, int n);
 
 /* Per-phase device milliseconds of the last call when SBC_FLAG_TIMING is set:

@@ -116,6 +116,7 @@ void fill_stats(sbc_ctx* c) {
     c->stats[SBC_STAT_SLOTS_B] = o.slots_b;
     c->stats[SBC_STAT_SLOTS_C] = o.slots_c;
     c->stats[SBC_STAT_WORK_UNITS] = o.work;
+    c->stats[SBC_STAT_GRID_PAIRS] = o.survivors;
     int slow = 0;
     for (const auto& x : pl.outputs()) slow |= x.slow_path;
     c->stats[SBC_STAT_SERIAL_BACKEND] = slow;

@@ -22,7 +22,7 @@ SBC_FLAG_SERIAL_BACKEND = 2
 
 STATS = ["edges", "elementary_points", "tree_size", "cover_entries", "leaf_end_entries",
          "candidates_tested", "raw_hits", "unique", "slots_b", "slots_c", "serial_backend",
-         "work_units"]
+         "work_units", "grid_pairs"]
 PHASES = ["setup", "elementary", "end_lists", "cover_lists", "candidates_merge", "back_end",
           "device_to_host", "total"]
 DEBUG_ARRAYS = {
