@@ -79,7 +79,7 @@ int sbc_clip_pair_device(sbc_ctx* ctx, const double* d_b_xy, int nb, const doubl
 #define SBC_STAT_TREE_SIZE 2
 #define SBC_STAT_COVER_ENTRIES 3
 #define SBC_STAT_LEAF_END_ENTRIES 4
-#define SBC_STAT_CANDIDATES_TESTED 5    /* overlay 1: emissions passing LSMF (the reference's tests) */
+#define SBC_STAT_CANDIDATES_TESTED 5    /* overlay 1: box-overlapping edge pairs passing LSMF */
 #define SBC_STAT_RAW_HITS 6             /* overlay 1: the reference's raw candidate hits */
 #define SBC_STAT_UNIQUE 7               /* overlay 1: unique intersecting edge pairs */
 #define SBC_STAT_SLOTS_B 8

@@ -497,11 +497,13 @@ __global__ void k_vertex_f4(long long nv, const double* __restrict__ xy, float4*
 }
 
 // Exact stage per candidate pair.  Phase 1 (one pair per thread): FP64 LSMF,
-// the emission count and first key, then the float pre-test; pairs it cannot
-// rule out are queued in shared memory.  Phase 2: the queue runs seg_isect
-// in full warps (divergent FP64 lanes would cost a full warp each).
-// counters: [0] unique hits, [1] emissions reaching the FP64 test,
-// [3] emissions with a non-zero type (the reference's raw hit count).
+// then the float pre-test; pairs it cannot rule out are queued in shared
+// memory.  Phase 2: the queue runs seg_isect in full warps (divergent FP64
+// lanes would cost a full warp each); pairs with a non-zero type get their
+// emission count and first key (a pair the reference never emits is
+// dropped there).
+// counters: [0] unique hits, [1] pairs passing LSMF, [3] emissions with a
+// non-zero type (the reference's raw hit count).
 constexpr int kExBlock = 256;
 constexpr int kExPer = 4;
 constexpr int kExChunk = kExBlock * kExPer;
@@ -515,7 +517,6 @@ k_pair_exact(long long n, const int2* __restrict__ pairs, const int* __restrict_
              int* __restrict__ rb, int* __restrict__ rc, int* __restrict__ rt,
              unsigned long long* __restrict__ rkey) {
   __shared__ int4 q[kExChunk];
-  __shared__ unsigned long long qk[kExChunk];
   __shared__ int qn;
   __shared__ unsigned long long ntested;
   const int tid = threadIdx.x, lane = tid & 31;
@@ -531,21 +532,17 @@ k_pair_exact(long long n, const int2* __restrict__ pairs, const int* __restrict_
     const long long i = base + (long long)r * kExBlock + tid;
     bool keep = false;
     int4 e = make_int4(0, 0, 0, 0);
-    unsigned long long key = 0;
     if (i < n) {
       const int2 pr = pairs[i];
       const int bId = e_id[pr.x], cId = e_id[pr.y];
       const double* pb = bP + bId;
       const double* pc = cP + cId;
       if (lsmf_exact(pb[0], pb[1], pb[2], pb[3], pc[0], pc[1], pc[2], pc[3])) {
-        const unsigned cnt = emission(pr.x, pr.y, cId, lr, aft, bef, logL, &key);
-        if (cnt > 0) {
-          my_tested += cnt;
-          if (!certainly_disjoint(vfB[bId >> 1], vfB[(bId >> 1) + 1], vfC[cId >> 1],
-                                  vfC[(cId >> 1) + 1])) {
-            keep = true;
-            e = make_int4(bId, cId, (int)cnt, 0);
-          }
+        ++my_tested;
+        if (!certainly_disjoint(vfB[bId >> 1], vfB[(bId >> 1) + 1], vfC[cId >> 1],
+                                vfC[(cId >> 1) + 1])) {
+          keep = true;
+          e = make_int4(bId, cId, pr.x, pr.y);
         }
       }
     }
@@ -554,10 +551,7 @@ k_pair_exact(long long n, const int2* __restrict__ pairs, const int* __restrict_
       int w0 = 0;
       if (lane == 0) w0 = atomicAdd(&qn, __popc(bal));
       w0 = __shfl_sync(0xffffffffu, w0, 0);
-      if (keep) {
-        q[w0 + __popc(bal & lt)] = e;
-        qk[w0 + __popc(bal & lt)] = key;
-      }
+      if (keep) q[w0 + __popc(bal & lt)] = e;
     }
   }
   for (int o = 16; o > 0; o >>= 1) my_tested += __shfl_xor_sync(0xffffffffu, my_tested, o);
@@ -571,14 +565,18 @@ k_pair_exact(long long n, const int2* __restrict__ pairs, const int* __restrict_
     bool hit = false;
     int ty = 0;
     int4 e = make_int4(0, 0, 0, 0);
+    unsigned long long key = 0;
     if (j < nq) {
       e = q[j];
       const double* pb = bP + e.x;
       const double* pc = cP + e.y;
       double al, be;
       ty = seg_isect(pb[0], pb[1], pb[2], pb[3], pc[0], pc[1], pc[2], pc[3], &al, &be);
-      hit = ty != 0;
-      if (hit) my_raw += (unsigned)e.z;
+      if (ty != 0) {
+        const unsigned cnt = emission(e.z, e.w, e.y, lr, aft, bef, logL, &key);
+        hit = cnt > 0;
+        my_raw += cnt;
+      }
     }
     const unsigned m = __ballot_sync(0xffffffffu, hit);
     if (m) {
@@ -592,7 +590,7 @@ k_pair_exact(long long n, const int2* __restrict__ pairs, const int* __restrict_
           rb[idx] = e.x;
           rc[idx] = e.y;
           rt[idx] = ty;
-          rkey[idx] = qk[j];
+          rkey[idx] = key;
         }
       }
     }

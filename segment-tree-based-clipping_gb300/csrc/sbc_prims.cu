@@ -297,8 +297,9 @@ namespace {
 
 constexpr int kRadThreads = 256;
 constexpr int kRadWarps = kRadThreads / 32;
-constexpr int kRadRounds = 16;                              // 32-key rounds per warp
-constexpr int kRadTile = kRadThreads * kRadRounds;          // 2048 keys per block
+// 32-key rounds per warp: 4, 8 or 16 (tiles of 1024, 2048 or 4096 keys),
+// chosen per sort so that the grid has about four CTAs per SM
+constexpr int kRadMinTile = kRadThreads * 4;
 
 template <typename K>
 __global__ void k_bits_reduce(const K* __restrict__ keys, long long n, K* __restrict__ out_or,
@@ -326,9 +327,10 @@ __device__ __forceinline__ unsigned digit_of(K k, int shift) {
 }
 
 // per-block digit histogram, digit-major layout hist[d * nblocks + b]
-template <typename K>
+template <typename K, int kRadRounds>
 __global__ void k_rad_hist(const K* __restrict__ keys, long long n, int shift,
                            unsigned* __restrict__ hist, unsigned nblocks) {
+  constexpr int kRadTile = kRadThreads * kRadRounds;
   __shared__ unsigned h[256];
   h[threadIdx.x] = 0;
   __syncthreads();
@@ -341,11 +343,12 @@ __global__ void k_rad_hist(const K* __restrict__ keys, long long n, int shift,
   hist[(size_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
 }
 
-// stable scatter: warp w owns keys [base + w*256, base + (w+1)*256) in order
-template <typename K>
+// stable scatter: warp w owns keys [base + w*32*R, base + (w+1)*32*R) in order
+template <typename K, int kRadRounds>
 __global__ void k_rad_scatter(const K* __restrict__ keys, const unsigned* __restrict__ vals,
                               K* __restrict__ okeys, unsigned* __restrict__ ovals, long long n,
                               int shift, const unsigned* __restrict__ offs, unsigned nblocks) {
+  constexpr int kRadTile = kRadThreads * kRadRounds;
   __shared__ unsigned wcnt[kRadWarps][256];
   __shared__ unsigned boff[256];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -392,11 +395,31 @@ __global__ void k_rad_scatter(const K* __restrict__ keys, const unsigned* __rest
   }
 }
 
+template <typename K, int kRadRounds>
+void radix_pass(const K* sk, const unsigned* sv, K* dk, unsigned* dv, long long n, int shift,
+                unsigned* hist, unsigned nblocks, void* sscr, cudaStream_t st) {
+  {
+    ::sbc::KProbe kp_(sizeof(K) == 8 ? "k_rad_hist_u64" : "k_rad_hist_u32", st);
+    k_rad_hist<K, kRadRounds><<<nblocks, kRadThreads, 0, st>>>(sk, n, shift, hist, nblocks);
+  }
+  // exclusive scan of the digit-major histogram gives each (digit, block) its base
+  scan_rec<int>((int*)hist, (long long)256 * nblocks, (int*)sscr, st);
+  {
+    ::sbc::KProbe kp_(sizeof(K) == 8 ? "k_rad_scatter_u64" : "k_rad_scatter_u32", st);
+    k_rad_scatter<K, kRadRounds><<<nblocks, kRadThreads, 0, st>>>(sk, sv, dk, dv, n, shift, hist,
+                                                                nblocks);
+  }
+}
+
 template <typename K>
 void radix_sort_impl(K* keys, unsigned* vals, K* keys_tmp, unsigned* vals_tmp, long long n,
                      int key_bits, void* scratch, cudaStream_t st) {
   if (n <= 1) return;
-  unsigned nblocks = (unsigned)((n + kRadTile - 1) / kRadTile);
+  // tile size: the largest of 4096 / 2048 / 1024 keys that still gives about
+  // four CTAs per SM (152 SMs)
+  const int rounds = n >= 4LL * 152 * kRadThreads * 16 ? 16 : (n >= 4LL * 152 * kRadThreads * 8 ? 8 : 4);
+  const int tile = kRadThreads * rounds;
+  unsigned nblocks = (unsigned)((n + tile - 1) / tile);
   // scratch: [or, and] then hist (256*nblocks u32) then scan scratch
   K* d_or = (K*)scratch;
   K* d_and = d_or + 1;
@@ -428,17 +451,12 @@ void radix_sort_impl(K* keys, unsigned* vals, K* keys_tmp, unsigned* vals_tmp, l
   unsigned* dst_v = vals_tmp;
   for (int shift = 0; shift < key_bits; shift += 8) {
     if (((vary >> shift) & K(0xff)) == 0) continue;
-    {
-      ::sbc::KProbe kp_(sizeof(K) == 8 ? "k_rad_hist_u64" : "k_rad_hist_u32", st);
-      k_rad_hist<K><<<nblocks, kRadThreads, 0, st>>>(src_k, n, shift, hist, nblocks);
-    }
-    // exclusive scan of the digit-major histogram gives each (digit, block) its base
-    scan_rec<int>((int*)hist, (long long)256 * nblocks, (int*)sscr, st);
-    {
-      ::sbc::KProbe kp_(sizeof(K) == 8 ? "k_rad_scatter_u64" : "k_rad_scatter_u32", st);
-      k_rad_scatter<K><<<nblocks, kRadThreads, 0, st>>>(src_k, src_v, dst_k, dst_v, n, shift, hist,
-                                                     nblocks);
-    }
+    if (rounds == 16)
+      radix_pass<K, 16>(src_k, src_v, dst_k, dst_v, n, shift, hist, nblocks, sscr, st);
+    else if (rounds == 8)
+      radix_pass<K, 8>(src_k, src_v, dst_k, dst_v, n, shift, hist, nblocks, sscr, st);
+    else
+      radix_pass<K, 4>(src_k, src_v, dst_k, dst_v, n, shift, hist, nblocks, sscr, st);
     K* tk = src_k; src_k = dst_k; dst_k = tk;
     unsigned* tv = src_v; src_v = dst_v; dst_v = tv;
   }
@@ -451,7 +469,7 @@ void radix_sort_impl(K* keys, unsigned* vals, K* keys_tmp, unsigned* vals_tmp, l
 }  // namespace
 
 size_t radix_scratch_bytes(long long n) {
-  long long nblocks = (n + kRadTile - 1) / kRadTile;
+  long long nblocks = (n + kRadMinTile - 1) / kRadMinTile;
   size_t h = (((size_t)256 * nblocks * sizeof(unsigned) + 255) / 256) * 256;
   return 64 + h + scan_scratch_bytes(256 * nblocks) * 2 + 256;
 }
