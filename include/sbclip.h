@@ -122,6 +122,63 @@ int sbc_debug_array(sbc_ctx* ctx, int which, void* host_dst, long long cap, long
 int sbc_classify_pairs(sbc_ctx* ctx, const double* pairs, int n, int* types, double* alpha,
                        double* beta, int* alpha_int, int* beta_int);
 
+/* ---- Batches of independent pairs --------------------------------------
+ * Many base/overlay pairs in one call: the result for every pair equals
+ * sbc_clip_pair on that pair (the reference's `seg base overlay`, run once
+ * per pair; the reference itself has no batched call).  Each pair is clipped
+ * by one device thread, all pairs in one launch.  Polygons are concatenated:
+ * pair p's base is vertices [b_off[p], b_off[p+1]) of b_xy, its overlay
+ * vertices [c_off[p], c_off[p+1]) of c_xy.  A polygon needs 3 to
+ * SBC_BATCH_MAX_VERTICES vertices; a pair outside that range gets status
+ * SBC_EINPUT and no rings.  Per-pair failures (SBC_EUNDEF where the
+ * reference's behaviour is undefined) are reported in the per-pair status;
+ * the call itself fails only on argument, allocation or CUDA errors. */
+#define SBC_BATCH_MAX_VERTICES 4096
+typedef struct sbc_batch {
+  int npairs;
+  const double* b_xy;
+  const long long* b_off;     /* npairs+1 */
+  const double* c_xy;
+  const long long* c_off;     /* npairs+1 */
+} sbc_batch;
+
+typedef struct sbc_batch_rings {
+  int npairs;
+  long long nrings, nverts;
+  const long long* pair_ring; /* npairs+1: pair p owns rings [pair_ring[p], pair_ring[p+1]) */
+  const long long* ring_off;  /* nrings+1 vertex offsets into xy */
+  const double* xy;           /* 2*nverts */
+  const int* status;          /* npairs */
+} sbc_batch_rings;
+
+/* Rings of every pair.  sbc_clip_batch: host arrays in, host arrays out
+ * (owned by the context until its next call).  _device: device arrays in,
+ * device arrays out (owned by the context). */
+int sbc_clip_batch(sbc_ctx* ctx, const sbc_batch* batch, sbc_batch_rings* out, void* stream);
+int sbc_clip_batch_device(sbc_ctx* ctx, const sbc_batch* batch, sbc_batch_rings* out,
+                          void* stream);
+
+/* Intersection area of every pair: the sum of the shoelace areas of its rings
+ * (0 for pairs whose status is not SBC_OK).  area[npairs], status[npairs]
+ * (status may be NULL).  Host arrays, or device arrays for _device. */
+int sbc_area_forward(sbc_ctx* ctx, const sbc_batch* batch, double* area, int* status,
+                     void* stream);
+int sbc_area_forward_device(sbc_ctx* ctx, const sbc_batch* batch, double* area, int* status,
+                            void* stream);
+
+/* Gradient of sum_p grad_area[p] * area[p] with respect to every vertex
+ * coordinate, with the combinatorial structure of each result held fixed:
+ * grad_b receives 2 * b_off[npairs] doubles, grad_c 2 * c_off[npairs].  A ring
+ * vertex that is a proper crossing passes its gradient to both edges through
+ * I = (1 - alpha) b1 + alpha b2, alpha = A(b1,c1,c2) / (A(b1,c1,c2) - A(b2,c1,c2)).
+ * _device reuses the records of the last sbc_area_forward_device call on this
+ * context when it was given the same batch (same arrays and count), and runs
+ * the forward pass first otherwise; the host variant always runs it. */
+int sbc_area_backward(sbc_ctx* ctx, const sbc_batch* batch, const double* grad_area,
+                      double* grad_b, double* grad_c, void* stream);
+int sbc_area_backward_device(sbc_ctx* ctx, const sbc_batch* batch, const double* grad_area,
+                             double* grad_b, double* grad_c, void* stream);
+
 /* Allocation-free ring tracing.  No counterpart in the reference: it exists
  * for callers that are not allowed to allocate device memory themselves or
  * through this library -- for example an engine that owns every byte of the

@@ -69,6 +69,11 @@ struct sbc_ctx {
   double* d_in = nullptr;
   size_t d_in_cap = 0;
   long long stats[SBC_STAT_NUM] = {0};
+  sbc::BatchRunner* br = nullptr;
+  // host copies of batched ring results
+  std::vector<long long> hb_pair_ring, hb_ring_off;
+  std::vector<double> hb_xy;
+  std::vector<int> hb_status;
   float phase_ms[8] = {0};
 };
 
@@ -155,6 +160,7 @@ int sbc_create(const sbc_options* opt, sbc_ctx** out) {
     return rc;
   }
   c->pl = new Pipeline(c->device, c->own);
+  c->br = new sbc::BatchRunner(*c->pl);
   *out = c;
   return SBC_OK;
 }
@@ -163,6 +169,7 @@ void sbc_destroy(sbc_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->own) cudaStreamSynchronize(c->own);
+  delete c->br;
   delete c->pl;
   for (auto p : c->h_off)
     if (p) cudaFreeHost(p);
@@ -396,4 +403,202 @@ extern "C" int sbc_classify_pairs(sbc_ctx* c, const double* pairs, int n, int* t
   if (alpha_int) cudaMemcpyAsync(alpha_int, dai, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
   if (beta_int) cudaMemcpyAsync(beta_int, dbi, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
   return cuda_check(c, cudaStreamSynchronize(st), "classifier");
+}
+
+// ------------------------------------------------------------------ batches
+namespace {
+
+int batch_check(sbc_ctx* c, const sbc_batch* b) {
+  if (!c || !b) return set_err(c, SBC_EINPUT, "null argument");
+  if (b->npairs < 0) return set_err(c, SBC_EINPUT, "negative pair count");
+  if (b->npairs > 0 && (!b->b_xy || !b->b_off || !b->c_xy || !b->c_off))
+    return set_err(c, SBC_EINPUT, "null batch array");
+  return SBC_OK;
+}
+
+// host batch -> device copies in the context's pool
+int batch_to_device(sbc_ctx* c, const sbc_batch* b, cudaStream_t st, sbc_batch* d) {
+  const int np = b->npairs;
+  *d = *b;
+  if (np == 0) return SBC_OK;
+  const long long nbv = b->b_off[np], ncv = b->c_off[np];
+  if (b->b_off[0] != 0 || b->c_off[0] != 0 || nbv < 0 || ncv < 0)
+    return set_err(c, SBC_EINPUT, "batch offsets must start at 0");
+  sbc::BufferPool& bp = c->pl->pool();
+  auto* dbx = (double*)bp.get("hbt_bxy", sizeof(double) * 2 * (nbv + 1));
+  auto* dcx = (double*)bp.get("hbt_cxy", sizeof(double) * 2 * (ncv + 1));
+  auto* dbo = (long long*)bp.get("hbt_boff", sizeof(long long) * (np + 1));
+  auto* dco = (long long*)bp.get("hbt_coff", sizeof(long long) * (np + 1));
+  if (bp.failed) return set_err(c, SBC_ENOMEM, "device allocation failed (batch inputs)");
+  cudaMemcpyAsync(dbx, b->b_xy, sizeof(double) * 2 * nbv, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dcx, b->c_xy, sizeof(double) * 2 * ncv, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dbo, b->b_off, sizeof(long long) * (np + 1), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dco, b->c_off, sizeof(long long) * (np + 1), cudaMemcpyHostToDevice, st);
+  d->b_xy = dbx;
+  d->c_xy = dcx;
+  d->b_off = dbo;
+  d->c_off = dco;
+  return SBC_OK;
+}
+
+int batch_run(sbc_ctx* c, const sbc_batch* d, cudaStream_t st) {
+  c->pl->clear_error();
+  int rc = c->br->forward(d->npairs, d->b_xy, d->b_off, d->c_xy, d->c_off, st);
+  if (rc) return set_err(c, rc, c->pl->error());
+  return SBC_OK;
+}
+
+}  // namespace
+
+extern "C" int sbc_area_forward_device(sbc_ctx* c, const sbc_batch* b, double* area, int* status,
+                                       void* stream) {
+  int rc = batch_check(c, b);
+  if (rc) return rc;
+  if (b->npairs > 0 && !area) return set_err(c, SBC_EINPUT, "null area output");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  rc = batch_run(c, b, st);
+  if (rc) return rc;
+  const int np = b->npairs;
+  if (np > 0) {
+    cudaMemcpyAsync(area, c->br->area, sizeof(double) * np, cudaMemcpyDeviceToDevice, st);
+    if (status)
+      cudaMemcpyAsync(status, c->br->status, sizeof(int) * np, cudaMemcpyDeviceToDevice, st);
+  }
+  return cuda_check(c, cudaStreamSynchronize(st), "area forward");
+}
+
+extern "C" int sbc_area_forward(sbc_ctx* c, const sbc_batch* b, double* area, int* status,
+                                void* stream) {
+  int rc = batch_check(c, b);
+  if (rc) return rc;
+  if (b->npairs > 0 && !area) return set_err(c, SBC_EINPUT, "null area output");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  sbc_batch d;
+  rc = batch_to_device(c, b, st, &d);
+  if (rc) return rc;
+  rc = batch_run(c, &d, st);
+  if (rc) return rc;
+  const int np = b->npairs;
+  if (np > 0) {
+    cudaMemcpyAsync(area, c->br->area, sizeof(double) * np, cudaMemcpyDeviceToHost, st);
+    if (status) cudaMemcpyAsync(status, c->br->status, sizeof(int) * np, cudaMemcpyDeviceToHost, st);
+  }
+  return cuda_check(c, cudaStreamSynchronize(st), "area forward");
+}
+
+extern "C" int sbc_area_backward_device(sbc_ctx* c, const sbc_batch* b, const double* grad_area,
+                                        double* grad_b, double* grad_c, void* stream) {
+  int rc = batch_check(c, b);
+  if (rc) return rc;
+  if (b->npairs > 0 && (!grad_area || !grad_b || !grad_c))
+    return set_err(c, SBC_EINPUT, "null gradient array");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  if (!(c->br->valid && c->br->np == b->npairs && c->br->key_b == b->b_xy &&
+        c->br->key_c == b->c_xy)) {
+    rc = batch_run(c, b, st);
+    if (rc) return rc;
+  }
+  c->pl->clear_error();
+  rc = c->br->backward(b->b_xy, b->b_off, b->c_xy, b->c_off, grad_area, grad_b, grad_c, st);
+  if (rc) return set_err(c, rc, c->pl->error());
+  return SBC_OK;
+}
+
+extern "C" int sbc_area_backward(sbc_ctx* c, const sbc_batch* b, const double* grad_area,
+                                 double* grad_b, double* grad_c, void* stream) {
+  int rc = batch_check(c, b);
+  if (rc) return rc;
+  const int np = b->npairs;
+  if (np > 0 && (!grad_area || !grad_b || !grad_c))
+    return set_err(c, SBC_EINPUT, "null gradient array");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  sbc_batch d;
+  rc = batch_to_device(c, b, st, &d);
+  if (rc) return rc;
+  rc = batch_run(c, &d, st);
+  if (rc) return rc;
+  if (np == 0) return SBC_OK;
+  const long long nbv = b->b_off[np], ncv = b->c_off[np];
+  sbc::BufferPool& bp = c->pl->pool();
+  auto* dga = (double*)bp.get("hbt_ga", sizeof(double) * (np + 1));
+  auto* dgb = (double*)bp.get("hbt_gb", sizeof(double) * 2 * (nbv + 1));
+  auto* dgc = (double*)bp.get("hbt_gc", sizeof(double) * 2 * (ncv + 1));
+  if (bp.failed) return set_err(c, SBC_ENOMEM, "device allocation failed (gradients)");
+  cudaMemcpyAsync(dga, grad_area, sizeof(double) * np, cudaMemcpyHostToDevice, st);
+  c->pl->clear_error();
+  rc = c->br->backward(d.b_xy, d.b_off, d.c_xy, d.c_off, dga, dgb, dgc, st);
+  if (rc) return set_err(c, rc, c->pl->error());
+  cudaMemcpyAsync(grad_b, dgb, sizeof(double) * 2 * nbv, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(grad_c, dgc, sizeof(double) * 2 * ncv, cudaMemcpyDeviceToHost, st);
+  return cuda_check(c, cudaStreamSynchronize(st), "area backward");
+}
+
+extern "C" int sbc_clip_batch_device(sbc_ctx* c, const sbc_batch* b, sbc_batch_rings* out,
+                                     void* stream) {
+  int rc = batch_check(c, b);
+  if (rc) return rc;
+  if (!out) return set_err(c, SBC_EINPUT, "null output");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  rc = batch_run(c, b, st);
+  if (rc) return rc;
+  long long *pr = nullptr, *ro = nullptr;
+  double* xy = nullptr;
+  long long nr = 0, nv = 0;
+  if (b->npairs > 0) {
+    c->pl->clear_error();
+    rc = c->br->rings(b->b_off, b->c_off, st, &pr, &ro, &xy, &nr, &nv);
+    if (rc) return set_err(c, rc, c->pl->error());
+  }
+  out->npairs = b->npairs;
+  out->nrings = nr;
+  out->nverts = nv;
+  out->pair_ring = pr;
+  out->ring_off = ro;
+  out->xy = xy;
+  out->status = c->br->status;
+  return SBC_OK;
+}
+
+extern "C" int sbc_clip_batch(sbc_ctx* c, const sbc_batch* b, sbc_batch_rings* out, void* stream) {
+  int rc = batch_check(c, b);
+  if (rc) return rc;
+  if (!out) return set_err(c, SBC_EINPUT, "null output");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  sbc_batch d;
+  rc = batch_to_device(c, b, st, &d);
+  if (rc) return rc;
+  sbc_batch_rings dr;
+  rc = sbc_clip_batch_device(c, &d, &dr, st);
+  if (rc) return rc;
+  const int np = b->npairs;
+  c->hb_pair_ring.assign((size_t)np + 1, 0);
+  c->hb_ring_off.assign((size_t)dr.nrings + 1, 0);
+  c->hb_xy.assign((size_t)2 * dr.nverts + 1, 0.0);
+  c->hb_status.assign((size_t)np + 1, 0);
+  if (np > 0) {
+    cudaMemcpyAsync(c->hb_pair_ring.data(), dr.pair_ring, sizeof(long long) * (np + 1),
+                    cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(c->hb_ring_off.data(), dr.ring_off, sizeof(long long) * (dr.nrings + 1),
+                    cudaMemcpyDeviceToHost, st);
+    if (dr.nverts > 0)
+      cudaMemcpyAsync(c->hb_xy.data(), dr.xy, sizeof(double) * 2 * dr.nverts,
+                      cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(c->hb_status.data(), dr.status, sizeof(int) * np, cudaMemcpyDeviceToHost, st);
+  }
+  rc = cuda_check(c, cudaStreamSynchronize(st), "batch rings");
+  if (rc) return rc;
+  out->npairs = np;
+  out->nrings = dr.nrings;
+  out->nverts = dr.nverts;
+  out->pair_ring = c->hb_pair_ring.data();
+  out->ring_off = c->hb_ring_off.data();
+  out->xy = c->hb_xy.data();
+  out->status = c->hb_status.data();
+  return SBC_OK;
 }

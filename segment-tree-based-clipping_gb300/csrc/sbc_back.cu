@@ -27,14 +27,11 @@
 
 #include "../../include/sbclip.h"
 #include "sbc_pipeline.cuh"
+#include "sbc_serial.cuh"
 
 namespace sbc {
 
 namespace {
-
-enum { L_NONE = 0, L_CROSSING, L_BOUNCING, L_LEFT_ON, L_RIGHT_ON, L_ON_ON, L_ON_LEFT, L_ON_RIGHT,
-       L_DCROSS, L_DBOUNCE };
-enum { EX_EXIT = 0, EX_ENTRY = 1, EX_NEITHER = 2 };
 
 // scalars the fast path computes (one struct, one read-back)
 struct BkScalars {
@@ -525,437 +522,6 @@ __global__ void k_copy_list(int n, const double* __restrict__ src, double* __res
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 2 * n) return;
   dst[i] = src[i];
-}
-
-// ================================================================ serial emulation
-// A literal restatement of copyToLinkedList + labelIntersections2 +
-// createResult2 + cleanUpResult2 over index-linked pools (one thread).
-struct Pool {
-  double *x, *y;
-  int *next, *prev, *nb, *label, *enex;
-  unsigned char *source, *isect;
-  int n, cap;
-};
-
-struct SerialArgs {
-  Pool P, Q, R;
-  int* rroot;
-  int rcap;
-  int* nrings;
-  unsigned char *splitP, *splitQ, *crossP, *crossQ;
-  int bSize, cSize, cStart, nB, nQ;
-  const double *bP, *cP, *ixB, *ixC;
-  const int *alB, *nbC, *labB, *labC;
-  int* status;   // 0 ok, 2 undefined, 3 capacity
-};
-
-__device__ int pnew(Pool& p, double x, double y) {
-  if (p.n >= p.cap) return -1;
-  int v = p.n++;
-  p.x[v] = x;
-  p.y[v] = y;
-  p.next[v] = p.prev[v] = v;
-  p.nb[v] = -1;
-  p.label[v] = L_NONE;
-  p.enex[v] = EX_NEITHER;
-  p.source[v] = 0;
-  p.isect[v] = 0;
-  return v;
-}
-
-__device__ void pinsert_after(Pool& p, int V, int curr) {
-  curr = p.next[curr];
-  p.next[p.prev[curr]] = V;
-  p.prev[V] = p.prev[curr];
-  p.next[V] = curr;
-  p.prev[curr] = V;
-}
-
-__device__ int ppip(const Pool& p, int root, double rx, double ry) {
-  int w = 0, one = root;
-  do {
-    int two = p.next[one];
-    double x0 = p.x[one], y0 = p.y[one], x1 = p.x[two], y1 = p.y[two];
-    if ((y0 < ry) != (y1 < ry)) {
-      if (x0 >= rx) {
-        if (x1 > rx) w = w + 2 * (y1 > y0) - 1;
-        else if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (y1 > y0)) w = w + 2 * (y1 > y0) - 1;
-      } else if (x1 > rx) {
-        if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (y1 > y0)) w = w + 2 * (y1 > y0) - 1;
-      }
-    }
-    one = two;
-  } while (one != root);
-  return (w % 2) != 0;
-}
-
-__device__ int rnew(SerialArgs& a) {
-  if (*a.nrings >= a.rcap) return -1;
-  int r = (*a.nrings)++;
-  a.rroot[r] = -1;
-  return r;
-}
-
-__device__ int radd(SerialArgs& a, int r, double x, double y) {
-  int v = pnew(a.R, x, y);
-  if (v < 0) return -1;
-  int root = a.rroot[r];
-  if (root < 0) {
-    a.rroot[r] = v;
-  } else {
-    a.R.prev[v] = a.R.prev[root];
-    a.R.next[v] = root;
-    a.R.next[a.R.prev[root]] = v;
-    a.R.prev[root] = v;
-  }
-  return 0;
-}
-
-__device__ int rcopy(SerialArgs& a, const Pool& p, int root) {
-  int r = rnew(a);
-  if (r < 0) return -1;
-  int v = root;
-  do {
-    if (radd(a, r, p.x[v], p.y[v])) return -1;
-    v = p.next[v];
-  } while (v != root);
-  return 0;
-}
-
-__device__ void tog(int* s) {
-  if (*s == EX_ENTRY) *s = EX_EXIT;
-  else if (*s == EX_EXIT) *s = EX_ENTRY;
-}
-
-__device__ int ser_build(SerialArgs& a) {
-  Pool& P = a.P;
-  Pool& Q = a.Q;
-  int nB = a.nB, nQ = a.nQ, i = 0;
-  for (int ii = 0; ii <= a.bSize; ++ii) {
-    int sv = ii < a.bSize ? ii : 0;
-    double vx = a.bP[2 * sv], vy = a.bP[2 * sv + 1];
-    while (a.ixB[(2 * i) % (2 * nB)] != vx || a.ixB[(2 * i + 1) % (2 * nB)] != vy) {
-      if (i >= nB) return 2;
-      int v = pnew(P, a.ixB[2 * i], a.ixB[2 * i + 1]);
-      if (v < 0) return 3;
-      P.label[v] = a.labB[i];
-      P.isect[v] = 1;
-      i++;
-    }
-    if (ii < a.bSize) {
-      int v = pnew(P, vx, vy);
-      if (v != i) return 2;
-      P.source[v] = 1;
-      P.label[v] = a.labB[i];
-      if (a.alB[i] != -100) P.isect[v] = 1;
-    }
-    i++;
-  }
-  if (P.n != nB) return 2;
-  for (int v = 0; v < nB; ++v) {
-    P.next[v] = (v + 1) % nB;
-    P.prev[v] = (v + nB - 1) % nB;
-  }
-  i = 0;
-  for (int ii = 0; ii <= a.cSize; ++ii) {
-    int sv = ii < a.cSize ? ii : 0;
-    double vx = a.cP[2 * (a.cStart + sv)], vy = a.cP[2 * (a.cStart + sv) + 1];
-    while (a.ixC[(2 * i) % (2 * nQ)] != vx || a.ixC[(2 * i + 1) % (2 * nQ)] != vy) {
-      if (i >= nQ) return 2;
-      int v = pnew(Q, a.ixC[2 * i], a.ixC[2 * i + 1]);
-      if (v < 0) return 3;
-      Q.label[v] = a.labC[i];
-      Q.isect[v] = 1;
-      int t = a.nbC[i] - 1;
-      if (t < 0 || t >= nB) return 2;
-      Q.nb[v] = t;
-      P.nb[t] = v;
-      i++;
-    }
-    if (ii < a.cSize) {
-      int v = pnew(Q, vx, vy);
-      if (v != i) return 2;
-      Q.source[v] = 1;
-      Q.label[v] = a.labC[i];
-      if (a.nbC[i] != -100) {
-        int t = a.nbC[i] - 1;
-        if (t < 0 || t >= nB) return 2;
-        Q.isect[v] = 1;
-        Q.nb[v] = t;
-        P.nb[t] = v;
-      }
-    }
-    i++;
-  }
-  if (Q.n != nQ) return 2;
-  for (int v = 0; v < nQ; ++v) {
-    Q.next[v] = (v + 1) % nQ;
-    Q.prev[v] = (v + nQ - 1) % nQ;
-  }
-  return 0;
-}
-
-__device__ Pool& side(SerialArgs& a, int s) { return s == 0 ? a.P : a.Q; }
-
-__device__ int ser_non_isect_vertex(SerialArgs& a, int s, int root) {
-  Pool& p = side(a, s);
-  Pool& o = side(a, 1 - s);
-  int V = root;
-  do {
-    if (!p.isect[V]) return V;
-    V = p.next[V];
-  } while (V != root);
-  V = root;
-  do {
-    int nbV = p.nb[V], nbN = p.nb[p.next[V]];
-    if (nbV < 0) return -2;
-    if (nbN != o.prev[nbV] && nbN != o.next[nbV]) {
-      double mx = 0.5 * (p.x[V] + p.x[p.next[V]]);
-      double my = 0.5 * (p.y[V] + p.y[p.next[V]]);
-      mx = dmul(0.5, dadd(p.x[V], p.x[p.next[V]]));
-      my = dmul(0.5, dadd(p.y[V], p.y[p.next[V]]));
-      int T = pnew(p, mx, my);
-      if (T < 0) return -3;
-      pinsert_after(p, T, V);
-      return T;
-    }
-    V = p.next[V];
-  } while (V != root);
-  return -2;
-}
-
-__device__ int ser_label_trace(SerialArgs& a) {
-  Pool& P = a.P;
-  Pool& Q = a.Q;
-  int roots[2] = {0, 0};
-  // (2) chains
-  {
-    int V = roots[0];
-    do {
-      if (P.isect[V] && (P.label[V] == L_LEFT_ON || P.label[V] == L_RIGHT_ON)) {
-        int x = P.label[V] == L_LEFT_ON ? 0 : 1;
-        int X = V, I = V;
-        int guard = P.n + 1;
-        do {
-          P.label[I] = L_NONE;
-          if (P.nb[I] < 0) return 2;
-          Q.label[P.nb[I]] = L_NONE;
-          I = P.next[I];
-          if (--guard < 0) return 2;
-        } while (P.label[I] == L_ON_ON);
-        int y = P.label[I] == L_ON_LEFT ? 0 : 1;
-        int chain = (x != y) ? L_DCROSS : L_DBOUNCE;
-        P.label[X] = chain;
-        P.label[I] = chain;
-        if (P.nb[X] < 0 || P.nb[I] < 0) return 2;
-        Q.label[P.nb[X]] = chain;
-        Q.label[P.nb[I]] = chain;
-      }
-      V = P.next[V];
-    } while (V != roots[0]);
-  }
-  // (3.5)
-  int noIsect[2] = {0, 0}, ident[2] = {0, 0};
-  for (int s = 0; s < 2; ++s) {
-    Pool& p = side(a, s);
-    int root = roots[s], nocross = 1, V = root;
-    do {
-      if (p.isect[V] && (p.label[V] == L_CROSSING || p.label[V] == L_DCROSS)) nocross = 0;
-      V = p.next[V];
-    } while (V != root);
-    if (!nocross) continue;
-    noIsect[s] = 1;
-    int allon = 1;
-    V = root;
-    do {
-      if (p.label[V] != L_ON_ON) allon = 0;
-      V = p.next[V];
-    } while (V != root);
-    if (allon) {
-      ident[s] = 1;
-      continue;
-    }
-    double px = 0, py = 0;
-    int found = 0;
-    V = root;
-    do {
-      if (!p.isect[V]) {
-        px = p.x[V];
-        py = p.y[V];
-        found = 1;
-        break;
-      }
-      V = p.next[V];
-    } while (V != root);
-    if (!found) {
-      Pool& o = side(a, 1 - s);
-      V = root;
-      do {
-        int nbV = p.nb[V], nbN = p.nb[p.next[V]];
-        if (nbV < 0) return 2;
-        if (nbN != o.prev[nbV] && nbN != o.next[nbV]) {
-          px = dmul(0.5, dadd(p.x[V], p.x[p.next[V]]));
-          py = dmul(0.5, dadd(p.y[V], p.y[p.next[V]]));
-          found = 1;
-          break;
-        }
-        V = p.next[V];
-      } while (V != root);
-      if (!found) return 2;
-    }
-    if (ppip(side(a, 1 - s), roots[1 - s], px, py))
-      if (rcopy(a, p, root)) return 3;
-  }
-  if (ident[0] && ident[1]) {
-    int target = P.nb[roots[0]], V = roots[1], found = 0;
-    do {
-      if (V == target) found = 1;
-      V = Q.next[V];
-    } while (V != roots[1]);
-    if (found && rcopy(a, P, roots[0])) return 3;
-  }
-  // (4)
-  for (int s = 0; s < 2; ++s) {
-    if (noIsect[s]) continue;
-    Pool& p = side(a, s);
-    unsigned char* split = s == 0 ? a.splitP : a.splitQ;
-    unsigned char* cross = s == 0 ? a.crossP : a.crossQ;
-    int V = ser_non_isect_vertex(a, s, roots[s]);
-    if (V == -3) return 3;
-    if (V < 0) return 2;
-    int status = EX_ENTRY;
-    if (ppip(side(a, 1 - s), roots[1 - s], p.x[V], p.y[V])) tog(&status);
-    int first = 1, I = V;
-    do {
-      if (p.isect[I]) {
-        if (p.label[I] == L_CROSSING) {
-          p.enex[I] = status;
-          tog(&status);
-        }
-        if (p.label[I] == L_BOUNCING && status == EX_EXIT) split[I] = 1;
-        if (p.label[I] == L_DCROSS) {
-          p.enex[I] = status;
-          if (first) {
-            if (status == EX_EXIT) p.label[I] = L_CROSSING;
-            first = 0;
-          } else {
-            if (status == EX_ENTRY) p.label[I] = L_CROSSING;
-            first = 1;
-            tog(&status);
-          }
-        }
-        if (p.label[I] == L_DBOUNCE) {
-          p.enex[I] = status;
-          if (first) {
-            if (status == EX_EXIT) cross[I] = 1;
-            first = 0;
-          } else {
-            if (status == EX_ENTRY) cross[I] = 1;
-            first = 1;
-          }
-          tog(&status);
-        }
-      }
-      I = p.next[I];
-    } while (I != V);
-  }
-  // (5) split pairs
-  {
-    int nP0 = P.n;
-    for (int IP = 0; IP < nP0; ++IP) {
-      if (!a.splitP[IP]) continue;
-      int IQ = P.nb[IP];
-      if (IQ < 0 || !a.splitQ[IQ]) continue;
-      int VP = pnew(P, P.x[IP], P.y[IP]);
-      int VQ = pnew(Q, Q.x[IQ], Q.y[IQ]);
-      if (VP < 0 || VQ < 0) return 3;
-      double sP = area3(P.x[P.prev[IP]], P.y[P.prev[IP]], P.x[IP], P.y[IP], P.x[P.next[IP]],
-                        P.y[P.next[IP]]);
-      double sQ = area3(Q.x[Q.prev[IQ]], Q.y[Q.prev[IQ]], Q.x[IQ], Q.y[IQ], Q.x[Q.next[IQ]],
-                        Q.y[Q.next[IQ]]);
-      if (dmul(sP, sQ) > 0) {
-        P.nb[IP] = VQ; Q.nb[VQ] = IP; P.isect[IP] = 1; Q.isect[VQ] = 1;
-        Q.nb[IQ] = VP; P.nb[VP] = IQ; Q.isect[IQ] = 1; P.isect[VP] = 1;
-      } else {
-        P.nb[VP] = VQ; Q.nb[VQ] = VP; P.isect[VP] = 1; Q.isect[VQ] = 1;
-      }
-      pinsert_after(P, VP, IP);
-      pinsert_after(Q, VQ, IQ);
-      P.enex[IP] = EX_EXIT; P.enex[VP] = EX_ENTRY;
-      Q.enex[IQ] = EX_EXIT; Q.enex[VQ] = EX_ENTRY;
-      P.label[IP] = P.label[VP] = L_CROSSING;
-      Q.label[IQ] = Q.label[VQ] = L_CROSSING;
-    }
-  }
-  // (6)
-  for (int IP = 0; IP < P.n; ++IP) {
-    if (!a.crossP[IP]) continue;
-    int IQ = P.nb[IP];
-    if (IQ >= 0 && a.crossQ[IQ]) {
-      P.label[IP] = L_CROSSING;
-      Q.label[IQ] = L_CROSSING;
-    }
-  }
-  // createResult2
-  {
-    int root = roots[0], It = root;
-    long long guard = 4LL * (P.n + Q.n) + 16;
-    do {
-      if (P.isect[It] && P.label[It] == L_CROSSING) {
-        int r = rnew(a);
-        if (r < 0) return 3;
-        int sI = 0, I = It, sV = 0, V = I;
-        P.isect[I] = 0;
-        do {
-          int status = side(a, sV).enex[V];
-          tog(&status);
-          Pool* pv;
-          do {
-            pv = &side(a, sV);
-            V = (status == EX_EXIT) ? pv->next[V] : pv->prev[V];
-            pv->isect[V] = 0;
-            if (radd(a, r, pv->x[V], pv->y[V])) return 2;
-            if (--guard < 0) return 2;
-          } while (!(pv->enex[V] == status) && !(sV == sI && V == I));
-          if (!(sV == sI && V == I)) {
-            int nbv = side(a, sV).nb[V];
-            if (nbv < 0) return 2;
-            sV = 1 - sV;
-            V = nbv;
-            side(a, sV).isect[V] = 0;
-          }
-        } while (!(sV == sI && V == I));
-      }
-      It = P.next[It];
-    } while (It != root);
-  }
-  return 0;
-}
-
-__device__ void ser_cleanup(SerialArgs& a) {
-  Pool& p = a.R;
-  for (int r = 0; r < *a.nrings; ++r) {
-    auto A = [&](int v) {
-      return fabs(area3(p.x[p.prev[v]], p.y[p.prev[v]], p.x[v], p.y[v], p.x[p.next[v]],
-                        p.y[p.next[v]]));
-    };
-    auto remove = [&](int V) {
-      if (a.rroot[r] == V) {
-        a.rroot[r] = p.next[V];
-        if (p.next[a.rroot[r]] == a.rroot[r]) a.rroot[r] = -1;
-      }
-      p.next[p.prev[V]] = p.next[V];
-      p.prev[p.next[V]] = p.prev[V];
-    };
-    while (a.rroot[r] >= 0 && A(a.rroot[r]) < kEps) remove(a.rroot[r]);
-    if (a.rroot[r] < 0) continue;
-    int start = a.rroot[r], V = start;
-    do {
-      int nx = p.next[V];
-      if (A(V) < kEps) remove(V);
-      V = nx;
-    } while (V != start);
-  }
 }
 
 __global__ void k_serial_backend(SerialArgs a) {

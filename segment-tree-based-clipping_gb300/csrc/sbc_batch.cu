@@ -1,0 +1,1098 @@
+// sbc_batch.cu -- many small independent base/overlay pairs in one launch,
+// and the area of their intersections with its gradient.
+//
+// One device thread clips one pair with the same rules as the pair pipeline
+// (rows A1-A18 of the reference, multicore_clipping src/clip.cpp:1415-2115),
+// in order, over a private scratch arena: the elementary intervals and their
+// quirks, the border search, each edge's leaf range and end leaves, the
+// candidate pairs with their first-emission keys (all base x overlay edge
+// pairs are tested: small pairs need no grid), the unique records, per-edge
+// counts, alpha order, merged arrays, initial labels, and the exact
+// linked-list back end (sbc_serial.cuh).  Results are those of
+// sbc_clip_pair for every pair.
+//
+// Area and gradient.  The area of a pair is the sum of the shoelace areas of
+// its rings.  Every ring vertex is a copy of a merged slot (base slots are
+// searched first), so it is a base vertex, an overlay vertex or a proper
+// crossing I = (1 - alpha) b1 + alpha b2, alpha = A(b1,c1,c2) / (A(b1,c1,c2)
+// - A(b2,c1,c2)).  The forward pass stores that provenance ("tape"); the
+// backward pass chains d(area)/d(vertex) through it with the combinatorial
+// structure held fixed.
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/sbclip.h"
+#include "sbc_pipeline.cuh"
+#include "sbc_serial.cuh"
+
+namespace sbc {
+
+namespace {
+
+constexpr int kBatchBlock = 128;
+
+// ------------------------------------------------------------------ arena
+struct Carver {
+  unsigned char* base;
+  size_t off;
+  template <class T>
+  __host__ __device__ T* take(long long n) {
+    off = (off + 15) & ~(size_t)15;
+    T* r = (T*)(base + off);
+    off += sizeof(T) * (size_t)(n > 0 ? n : 0);
+    return r;
+  }
+};
+
+__host__ __device__ __forceinline__ int npow2_dev(int n) {
+  int p = 1;
+  while (p < n) p <<= 1;
+  return p;
+}
+
+// capacities of one pair
+struct Caps {
+  int nb, nc, E, K;        // K = capacity for unique hits
+  int epcMax, nBmax, nQmax, capP, capQ, capR, rcap;
+};
+
+__host__ __device__ __forceinline__ Caps caps_of(int nb, int nc, int K) {
+  Caps c;
+  c.nb = nb;
+  c.nc = nc;
+  c.E = nb + nc;
+  c.K = K;
+  c.epcMax = npow2_dev(2 * c.E) + 2;
+  c.nBmax = nb + K;
+  c.nQmax = nc + K;
+  c.capP = c.nBmax + 2 * K + 8;
+  c.capQ = c.nQmax + 2 * K + 8;
+  c.capR = c.nBmax + c.nQmax + 2 * (2 * K + 8) + 16;
+  c.rcap = c.nBmax + 16;
+  return c;
+}
+
+// The arrays of one pair.  Carved in a fixed order from a base pointer, so a
+// null base gives the byte count.
+struct PairWork {
+  // edges
+  double *es, *ee;
+  float4* fbox;
+  // elementary intervals
+  int *sidx, *stmp, *vl, *vloc;
+  double* ea;
+  // end leaves, leaf ranges
+  int *aft, *bef;
+  int2* lr;
+  // hits
+  int *hb, *hc, *ht, *hord, *htmp;
+  unsigned long long* hkey;
+  // counts, order, records
+  int *bAll, *bND, *cAll, *cND, *cfill, *csorted;
+  double* isxy;
+  int *aB, *aC, *sB, *sC, *skey;
+  // merged arrays
+  double *ixB, *ixC;
+  int *alB, *alC, *nbB, *nbC, *bNI, *cNI, *labB, *labC, *cWin, *srcB, *srcC, *recB, *recC;
+  // back end
+  Pool P, Q, R;
+  int *rroot, *counts;
+  unsigned char *splitP, *splitQ, *crossP, *crossQ;
+  // output: ring offsets, ring xy, provenance
+  int* roff;
+  double* rxy;
+  int4* tape;
+};
+
+__host__ __device__ __forceinline__ void carve_pool(Carver& cv, int cap, Pool& p) {
+  p.x = cv.take<double>(cap);
+  p.y = cv.take<double>(cap);
+  p.next = cv.take<int>(cap);
+  p.prev = cv.take<int>(cap);
+  p.nb = cv.take<int>(cap);
+  p.label = cv.take<int>(cap);
+  p.enex = cv.take<int>(cap);
+  p.source = cv.take<unsigned char>(cap);
+  p.isect = cv.take<unsigned char>(cap);
+  p.n = 0;
+  p.cap = cap;
+}
+
+__host__ __device__ __forceinline__ PairWork carve(Carver& cv, const Caps& c) {
+  PairWork w;
+  const int E = c.E, n2 = 2 * E, K = c.K;
+  w.es = cv.take<double>(E);
+  w.ee = cv.take<double>(E);
+  w.fbox = cv.take<float4>(E);
+  w.sidx = cv.take<int>(n2);
+  w.stmp = cv.take<int>(n2);
+  w.vl = cv.take<int>(E + 1);
+  w.vloc = cv.take<int>(E + 1);
+  w.ea = cv.take<double>(c.epcMax);
+  w.aft = cv.take<int>(E);
+  w.bef = cv.take<int>(E);
+  w.lr = cv.take<int2>(E);
+  w.hb = cv.take<int>(K);
+  w.hc = cv.take<int>(K);
+  w.ht = cv.take<int>(K);
+  w.hord = cv.take<int>(K);
+  w.htmp = cv.take<int>(K);
+  w.hkey = cv.take<unsigned long long>(K);
+  w.bAll = cv.take<int>(c.nb + 1);
+  w.bND = cv.take<int>(c.nb + 1);
+  w.cAll = cv.take<int>(c.nc + 1);
+  w.cND = cv.take<int>(c.nc + 1);
+  w.cfill = cv.take<int>(c.nc + 1);
+  w.csorted = cv.take<int>(K);
+  w.isxy = cv.take<double>(2 * K);
+  w.aB = cv.take<int>(K);
+  w.aC = cv.take<int>(K);
+  w.sB = cv.take<int>(K);
+  w.sC = cv.take<int>(K);
+  w.skey = cv.take<int>(K);
+  w.ixB = cv.take<double>(2 * c.nBmax);
+  w.ixC = cv.take<double>(2 * c.nQmax);
+  w.alB = cv.take<int>(c.nBmax);
+  w.alC = cv.take<int>(c.nQmax);
+  w.nbB = cv.take<int>(c.nBmax);
+  w.nbC = cv.take<int>(c.nQmax);
+  w.bNI = cv.take<int>(K);
+  w.cNI = cv.take<int>(K);
+  w.labB = cv.take<int>(c.nBmax);
+  w.labC = cv.take<int>(c.nQmax);
+  w.cWin = cv.take<int>(c.nQmax);
+  w.srcB = cv.take<int>(c.nBmax);
+  w.srcC = cv.take<int>(c.nQmax);
+  w.recB = cv.take<int>(c.nBmax);
+  w.recC = cv.take<int>(c.nQmax);
+  carve_pool(cv, c.capP, w.P);
+  carve_pool(cv, c.capQ, w.Q);
+  carve_pool(cv, c.capR, w.R);
+  w.rroot = cv.take<int>(c.rcap);
+  w.counts = cv.take<int>(4);
+  w.splitP = cv.take<unsigned char>(c.capP);
+  w.crossP = cv.take<unsigned char>(c.capP);
+  w.splitQ = cv.take<unsigned char>(c.capQ);
+  w.crossQ = cv.take<unsigned char>(c.capQ);
+  w.roff = cv.take<int>(c.rcap + 1);
+  w.rxy = cv.take<double>(2 * (long long)c.capR);
+  w.tape = cv.take<int4>(c.capR);
+  return w;
+}
+
+__host__ __device__ __forceinline__ size_t arena_bytes(int nb, int nc, int K) {
+  Carver cv{nullptr, 0};
+  carve(cv, caps_of(nb, nc, K));
+  return (cv.off + 255) & ~(size_t)255;
+}
+
+// hit capacity of a pair: generous for star-like polygons; a pair that needs
+// more is run again with the full product
+__host__ __device__ __forceinline__ int hit_cap(int nb, int nc, int pass) {
+  const long long full = (long long)nb * nc;
+  const long long first = 4LL * (nb + nc) + 16;
+  const long long k = pass == 0 ? (first < full ? first : full) : full;
+  return (int)(k > 0 ? k : 1);
+}
+
+// ------------------------------------------------------------------ small helpers
+__device__ __forceinline__ double bvx(const double* p, int n, int i) { return p[2 * (i % n)]; }
+__device__ __forceinline__ double bvy(const double* p, int n, int i) { return p[2 * (i % n) + 1]; }
+
+__device__ __forceinline__ bool lsmf_d(double p1x, double p1y, double p2x, double p2y, double q1x,
+                                       double q1y, double q2x, double q2y) {
+  double minPX = p1x, minPY = p1y, maxPX = p2x, maxPY = p2y;
+  double minQX = q1x, minQY = q1y, maxQX = q2x, maxQY = q2y;
+  if (minPX > p2x) { minPX = p2x; maxPX = p1x; }
+  if (minPY > p2y) { minPY = p2y; maxPY = p1y; }
+  if (minQX > q2x) { minQX = q2x; maxQX = q1x; }
+  if (minQY > q2y) { minQY = q2y; maxQY = q1y; }
+  if (minPX > maxQX || maxPX < minQX) return false;
+  if (minPY > maxQY || maxPY < minQY) return false;
+  return true;
+}
+
+// stable bottom-up merge sort of idx[0..n) by less(a, b)
+template <class Less>
+__device__ void merge_sort(int* idx, int* tmp, int n, Less less) {
+  for (int w = 1; w < n; w <<= 1) {
+    for (int lo = 0; lo < n; lo += 2 * w) {
+      const int mid = min(lo + w, n), hi = min(lo + 2 * w, n);
+      int i = lo, j = mid, o = lo;
+      while (i < mid && j < hi) tmp[o++] = less(idx[j], idx[i]) ? idx[j++] : idx[i++];
+      while (i < mid) tmp[o++] = idx[i++];
+      while (j < hi) tmp[o++] = idx[j++];
+    }
+    for (int i = 0; i < n; ++i) idx[i] = tmp[i];
+  }
+}
+
+// findBoarder over S(m) (oacc_segment_tree.cpp:420-460) with the zero
+// border slot at z (the same emulation as the pair pipeline)
+struct BordersS {
+  const double* ea;
+  int epc, z;
+  __device__ double S(int m) const {
+    if (m < 0 || m >= epc) return __longlong_as_double(0x7ff8000000000000ll);
+    if (m < z) return ea[m + 1];
+    if (m == z) return 0.0;
+    return ea[m];
+  }
+  __device__ int J(int m) const { return m < z ? m : (m == z ? epc - 1 : m - 1); }
+};
+
+__device__ int find_border_s(const BordersS& B, double q) {
+  int l = 0, h = B.epc;
+  while (l < h) {
+    const int m = l + (h - l) / 2;
+    const double sm = B.S(m);
+    if (sm == q) {
+      if (B.S(m - 1) != q) {
+        h = m;
+        l = h;
+      } else {
+        h = m - 1;
+      }
+    } else if (sm < q) {
+      l = m + 1;
+    } else {
+      h = m - 1;
+    }
+  }
+  if (!(B.S(h) == q)) return -1;
+  return h;
+}
+
+__device__ __forceinline__ bool canonical_s(int v, int logL, int l, int r1) {
+  const int L = 1 << logL;
+  const int d = 31 - __clz(v), h = logL - d;
+  const int lo = (v << h) - L, hi = ((v + 1) << h) - L;
+  if (lo < l || hi > r1) return false;
+  if (v == 1) return true;
+  const int p = v >> 1;
+  const int plo = (p << (h + 1)) - L, phi = ((p + 1) << (h + 1)) - L;
+  return !(plo >= l && phi <= r1);
+}
+
+__device__ __forceinline__ bool below_s(int x, int v, int logL) {
+  if (x < 0) return false;
+  const int h = logL - (31 - __clz(v));
+  return (x >> h) == v;
+}
+
+// emission count and first key of base edge b with overlay edge c (edge
+// indices of the pair; cId = the overlay edge's id)
+__device__ unsigned emission_s(int b, int c, int cId, const PairWork& w, int logL,
+                               unsigned long long* key) {
+  const int L = 1 << logL;
+  const int2 rb = w.lr[b], rc = w.lr[c];
+  const int eb0 = w.aft[b], eb1 = w.bef[b], ec0 = w.aft[c], ec1 = w.bef[c];
+  unsigned n = 0;
+  unsigned long long best = ~0ull;
+  for (int a = rb.x + L, z = rb.y + L; a < z; a >>= 1, z >>= 1) {
+    for (int side = 0; side < 2; ++side) {
+      int v = -1;
+      if (side == 0 && (a & 1)) v = a++;
+      if (side == 1 && (z & 1)) v = --z;
+      if (v < 0) continue;
+      if (canonical_s(v, logL, rc.x, rc.y)) {
+        n += 2;
+        best = min(best, ((unsigned long long)v << 33) | (unsigned)cId);
+      }
+      if (below_s(ec0, v, logL) || below_s(ec1, v, logL)) {
+        n += 1;
+        best = min(best, ((unsigned long long)v << 33) | (1ull << 31) | (unsigned)cId);
+      }
+    }
+  }
+  for (int a = rc.x + L, z = rc.y + L; a < z; a >>= 1, z >>= 1) {
+    for (int side = 0; side < 2; ++side) {
+      int v = -1;
+      if (side == 0 && (a & 1)) v = a++;
+      if (side == 1 && (z & 1)) v = --z;
+      if (v < 0) continue;
+      if (below_s(eb0, v, logL) || below_s(eb1, v, logL)) {
+        n += 1;
+        best = min(best, ((unsigned long long)v << 33) | (1ull << 32) | (unsigned)c);
+      }
+    }
+  }
+  *key = best;
+  return n;
+}
+
+__device__ __forceinline__ bool nd_b(int t) { return t == 1 || t == 3 || t == 5 || t == 7; }
+__device__ __forceinline__ bool nd_c(int t) { return t == 1 || t == 2 || t == 6; }
+
+// status codes of one pair
+enum { PS_OK = 0, PS_UNDEF = 2, PS_CAP = 3 };
+
+struct PairResult {
+  int status;
+  int nrings;
+  int nverts;
+  double area;
+};
+
+// ------------------------------------------------------------------ one pair
+__device__ PairResult clip_pair_serial(const double* b, int nb, const double* c, int nc,
+                                       const Caps& cp, PairWork& w) {
+  PairResult res{PS_OK, 0, 0, 0.0};
+  const int E = nb + nc, n2 = 2 * E;
+  // ---- A1 edges (edge.h:190-202); ids are offsets into the interleaved arrays
+  double minI = bvx(b, nb, 0), maxI = minI;
+  for (int e = 0; e < E; ++e) {
+    double a0, a1, y0, y1;
+    if (e < nb) {
+      a0 = bvx(b, nb, e);
+      a1 = bvx(b, nb, e + 1);
+      y0 = bvy(b, nb, e);
+      y1 = bvy(b, nb, e + 1);
+    } else {
+      a0 = bvx(c, nc, e - nb);
+      a1 = bvx(c, nc, e - nb + 1);
+      y0 = bvy(c, nc, e - nb);
+      y1 = bvy(c, nc, e - nb + 1);
+    }
+    if (a0 < a1) {
+      w.es[e] = a0;
+      w.ee[e] = a1;
+    } else {
+      w.ee[e] = a0;
+      w.es[e] = a1;
+    }
+    minI = fmin(minI, a0);
+    maxI = fmax(maxI, a0);
+    w.fbox[e] = make_float4(__double2float_rd(fmin(a0, a1)), __double2float_rd(fmin(y0, y1)),
+                            __double2float_ru(fmax(a0, a1)), __double2float_ru(fmax(y0, y1)));
+  }
+  // ---- A4 elementary intervals (:4513-4692): stable sort of the endpoints
+  auto val = [&](int idx) { return (idx & 1) ? w.ee[idx >> 1] : w.es[idx >> 1]; };
+  for (int i = 0; i < n2; ++i) w.sidx[i] = i;
+  merge_sort(w.sidx, w.stmp, n2, [&](int x, int y) { return dkey(val(x)) < dkey(val(y)); });
+  for (int i = 0; i <= E; ++i) w.vl[i] = 0;
+  for (int j = 0; j < E; ++j) {
+    const int i = w.sidx[j] >> 1;
+    if (w.es[i] == w.ee[i]) w.vl[i] = 1;
+  }
+  {
+    int s = 0;
+    for (int i = 0; i <= E; ++i) {
+      const int x = w.vl[i];
+      w.vl[i] = s;
+      s += x;
+    }
+    for (int i = 0; i < E; ++i)
+      if (w.vl[i] != w.vl[i + 1]) w.vloc[w.vl[i]] = i;
+  }
+  int count = 0;
+  double* ea = w.ea;
+  for (int i = 0; i < n2 - 1; ++i) {
+    const double v0 = val(w.sidx[i]), v1 = val(w.sidx[i + 1]);
+    const int intvi = w.sidx[i] >> 1;
+    const int comid = w.vl[i / 2];
+    if (v0 != v1) {
+      ea[count++] = v0;
+    } else if (w.es[intvi] == w.ee[intvi]) {
+      bool keep = comid == 0;
+      if (!keep) {
+        const int lookup = w.vloc[comid - 1];
+        keep = w.es[lookup] != w.es[intvi] && w.ee[lookup] != w.es[intvi];
+      }
+      if (keep) ea[count++] = w.es[intvi];
+    }
+    if (i == n2 - 2 && v0 != v1) ea[count++] = v0;  // the last slot repeats v0
+  }
+  if (count < 1) {
+    res.status = PS_UNDEF;
+    return res;
+  }
+  const int epc = npow2_dev(count) + 1;
+  for (int i = count; i < epc; ++i) ea[i] = ea[count - 1];
+  const int L = epc - 1;
+  int logL = 0;
+  while ((1 << logL) < L) ++logL;
+  // ---- A6 borders (realToInt keys, :203-206 with 64-bit; digit sort :616-689)
+  const double absMin = fabs(minI);
+  const double dv = dadd(maxI, absMin);
+  if (!(dv < 2147483647.0)) {
+    res.status = PS_UNDEF;
+    return res;
+  }
+  int digits = 1;
+  for (int iv = (int)trunc(dv); iv / 10 > 0; iv /= 10) ++digits;
+  double scale = 1.0;
+  for (int t = 0; t < 11 - digits; ++t) scale = dmul(scale, 10.0);
+  const bool shift = minI < 0;
+  int z = 0;
+  {
+    auto key = [&](int t) -> long long {
+      const double v = shift ? dmul(scale, dadd(ea[t], absMin)) : dmul(scale, ea[t]);
+      return (long long)v;
+    };
+    for (int i = 1; i < epc; ++i) {
+      const long long ki = key(i);
+      if (ki < 0 || ki >= 100000000000LL || (i + 1 < epc && key(i + 1) < ki)) {
+        res.status = PS_UNDEF;
+        return res;
+      }
+      if (ki == 0) ++z;
+    }
+  }
+  const BordersS B{ea, epc, z};
+  for (int e = 0; e < E; ++e) {
+    int a = -1, bb = -1;
+    const int en = find_border_s(B, w.ee[e]);
+    const int st = find_border_s(B, w.es[e]);
+    if (en >= 0) {
+      const int j = B.J(en);
+      int node = 0;
+      if (j <= epc - 2) {
+        const int i = j + 1;
+        node = L + i;
+        if (i != 1 && i + 1 < epc && ea[i] == ea[i + 1]) node = L + i + 1;
+      }
+      if (node >= L && node < 2 * L && ea[node - L] != ea[node - L + 1]) a = node;
+    }
+    if (st >= 0) {
+      const int j = B.J(st);
+      int node = 0;
+      if (j <= epc - 2) node = L + j;
+      if (node >= L && node < 2 * L && ea[node - L] != ea[node - L + 1]) bb = node;
+    }
+    w.aft[e] = a;
+    w.bef[e] = bb;
+    // ---- A7 leaf range [l, r1) of the edge's interval
+    int lo = 0, hi = L;
+    while (lo < hi) {
+      const int m = (lo + hi) >> 1;
+      if (ea[m] < w.es[e]) lo = m + 1;
+      else hi = m;
+    }
+    const int l = lo;
+    lo = 0;
+    hi = L;
+    while (lo < hi) {
+      const int m = (lo + hi) >> 1;
+      if (ea[m + 1] <= w.ee[e]) lo = m + 1;
+      else hi = m;
+    }
+    w.lr[e] = make_int2(l, lo > l ? lo : l);
+  }
+  // ---- A8 candidate pairs: all base x overlay edge pairs, float boxes first
+  int K = 0;
+  for (int be = 0; be < nb; ++be) {
+    const float4 fb = w.fbox[be];
+    const double p1x = bvx(b, nb, be), p1y = bvy(b, nb, be);
+    const double p2x = bvx(b, nb, be + 1), p2y = bvy(b, nb, be + 1);
+    for (int j = 0; j < nc; ++j) {
+      const float4 fc = w.fbox[nb + j];
+      if (fb.x > fc.z || fb.z < fc.x || fb.y > fc.w || fb.w < fc.y) continue;
+      const double q1x = bvx(c, nc, j), q1y = bvy(c, nc, j);
+      const double q2x = bvx(c, nc, j + 1), q2y = bvy(c, nc, j + 1);
+      if (!lsmf_d(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y)) continue;
+      double al, bt;
+      const int ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
+      if (!ty) continue;
+      unsigned long long key;
+      if (emission_s(be, nb + j, 2 * j, w, logL, &key) == 0) continue;
+      if (K >= cp.K) {
+        res.status = PS_CAP;
+        return res;
+      }
+      w.hb[K] = 2 * be;
+      w.hc[K] = 2 * j;
+      w.ht[K] = ty;
+      w.hkey[K] = key;
+      ++K;
+    }
+  }
+  // ---- A9 unique records in the reference's order: base id, then first key
+  for (int i = 0; i < K; ++i) w.hord[i] = i;
+  merge_sort(w.hord, w.htmp, K, [&](int x, int y) {
+    return w.hb[x] != w.hb[y] ? w.hb[x] < w.hb[y] : w.hkey[x] < w.hkey[y];
+  });
+  // records in that order: ub/uc/ut = hb/hc/ht through hord
+  int* ub = w.htmp;  // reuse: ub[i] = hb[hord[i]]
+  for (int i = 0; i < K; ++i) ub[i] = w.hb[w.hord[i]];
+  int* uc = w.skey;  // uc[i] = hc[hord[i]]
+  for (int i = 0; i < K; ++i) uc[i] = w.hc[w.hord[i]];
+  int* ut = w.ht;  // permuted in place through csorted below: keep a copy order
+  {
+    // permute types into record order using aB as temporary
+    for (int i = 0; i < K; ++i) w.aB[i] = w.ht[w.hord[i]];
+    for (int i = 0; i < K; ++i) ut[i] = w.aB[i];
+  }
+  // ---- A10 counts (countEdgeIntersections, src/clip.cpp:522-601) + scans
+  for (int i = 0; i <= nb; ++i) w.bAll[i] = w.bND[i] = 0;
+  for (int i = 0; i <= nc; ++i) w.cAll[i] = w.cND[i] = w.cfill[i] = 0;
+  for (int i = 0; i < K; ++i) {
+    const int eb = ub[i] >> 1, ec = uc[i] >> 1;
+    w.bAll[eb]++;
+    if (nd_b(ut[i])) w.bND[eb]++;
+    w.cAll[ec]++;
+    if (nd_c(ut[i])) w.cND[ec]++;
+  }
+  auto excl = [](int* a, int n) {
+    int s = 0;
+    for (int i = 0; i < n; ++i) {
+      const int x = a[i];
+      a[i] = s;
+      s += x;
+    }
+  };
+  excl(w.bAll, nb + 1);
+  excl(w.bND, nb + 1);
+  excl(w.cAll, nc + 1);
+  excl(w.cND, nc + 1);
+  // records stable by overlay id (radixsort of cPolLineIds, :1805)
+  for (int i = 0; i < K; ++i) {
+    const int ec = uc[i] >> 1;
+    w.csorted[w.cAll[ec] + w.cfill[ec]++] = i;
+  }
+  const int nB = nb + w.bND[nb], nQ = nc + w.cND[nc];
+  // ---- A11 records (saveIntersectionsParallel, :7257-7341)
+  for (int i = 0; i < K; ++i) {
+    const int bi = ub[i] >> 1, ci = uc[i] >> 1;
+    const double p1x = bvx(b, nb, bi), p1y = bvy(b, nb, bi);
+    const double p2x = bvx(b, nb, bi + 1), p2y = bvy(b, nb, bi + 1);
+    const double q1x = bvx(c, nc, ci), q1y = bvy(c, nc, ci);
+    const double q2x = bvx(c, nc, ci + 1), q2y = bvy(c, nc, ci + 1);
+    double al = 0.0, bt = 0.0;
+    const int ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
+    double x = 0.0, y = 0.0;
+    if (ty == 1) {
+      const double oma = dsub(1.0, al);
+      x = dadd(dmul(oma, p1x), dmul(al, p2x));
+      y = dadd(dmul(oma, p1y), dmul(al, p2y));
+    } else if (ty == 3 || ty == 4 || ty == 5 || ty == 7 || ty == 8) {
+      x = q1x;
+      y = q1y;
+    } else if (ty == 2 || ty == 6) {
+      x = p1x;
+      y = p1y;
+    }
+    w.isxy[2 * i] = x;
+    w.isxy[2 * i + 1] = y;
+    w.aB[i] = ty ? alpha_to_int(al) : 0;
+    w.aC[i] = ty ? alpha_to_int(bt) : 0;
+  }
+  // ---- A12 per-edge alpha order (sortIntersectionsAtEdgesParallel, :7436-7473)
+  auto alpha_sort = [&](int n, const int* allPS, const int* ndPS, const int* alpha,
+                        const int* order, int* sorted) -> bool {
+    for (int i = 0; i < K; ++i) sorted[i] = i;
+    for (int e = 0; e < n; ++e) {
+      const int s = allPS[e], t = allPS[e + 1];
+      if (ndPS[e + 1] - ndPS[e] <= 1) continue;
+      for (int i = s; i < t; ++i)
+        if (alpha[order ? order[i] : i] < 0) return false;
+      for (int i = s + 1; i < t; ++i) {  // stable insertion by alpha mod 1e9
+        const int p = sorted[i];
+        const int kp = alpha[order ? order[p] : p] % 1000000000;
+        int j = i;
+        while (j > s) {
+          const int q = sorted[j - 1];
+          if (alpha[order ? order[q] : q] % 1000000000 <= kp) break;
+          sorted[j] = q;
+          --j;
+        }
+        sorted[j] = p;
+      }
+    }
+    return true;
+  };
+  if (!alpha_sort(nb, w.bAll, w.bND, w.aB, nullptr, w.sB) ||
+      !alpha_sort(nc, w.cAll, w.cND, w.aC, w.csorted, w.sC)) {
+    res.status = PS_UNDEF;
+    return res;
+  }
+  // ---- A13 merged arrays (copyIntersectionsParallel, :7508-7664); unwritten
+  // slots read 0 as on the reference's zero-filled heap
+  for (int i = 0; i < nB; ++i) {
+    w.ixB[2 * i] = w.ixB[2 * i + 1] = 0.0;
+    w.alB[i] = w.nbB[i] = 0;
+    w.srcB[i] = -1;
+    w.recB[i] = -1;
+  }
+  for (int i = 0; i < nQ; ++i) {
+    w.ixC[2 * i] = w.ixC[2 * i + 1] = 0.0;
+    w.alC[i] = w.nbC[i] = 0;
+    w.srcC[i] = -1;
+    w.recC[i] = -1;
+  }
+  for (int id = 0; id < nb; ++id) {
+    const int p = id + w.bND[id];
+    w.ixB[2 * p] = bvx(b, nb, id);
+    w.ixB[2 * p + 1] = bvy(b, nb, id);
+    w.alB[p] = -100;
+    w.nbB[p] = -100;
+    w.srcB[p] = id;
+  }
+  for (int id = 0; id < nc; ++id) {
+    const int p = id + w.cND[id];
+    w.ixC[2 * p] = bvx(c, nc, id);
+    w.ixC[2 * p + 1] = bvy(c, nc, id);
+    w.alC[p] = -100;
+    w.nbC[p] = -100;
+    w.srcC[p] = id;
+  }
+  for (int i = 0; i < K; ++i) w.bNI[i] = w.cNI[i] = 0;
+  auto copy_runs = [&](bool base, int n, const int* allPS, const int* ndPS, const int* sorted,
+                       const int* order, const int* ids, const int* avals, double* ix, int* al,
+                       int* NI, int* rec) {
+    for (int e = 0; e < n; ++e) {
+      const int s = allPS[e];
+      if (allPS[e + 1] == s) continue;
+      auto entry = [&](int pos) { return order ? order[sorted[pos]] : sorted[pos]; };
+      int bid = s;
+      int lid = entry(bid);
+      const int t = ut[lid];
+      const bool deg = base ? (t == 2 || t == 4 || t == 6 || t == 8)
+                            : (t == 3 || t == 4 || t == 5 || t == 7 || t == 8);
+      if (deg) {
+        const int slot = e + ndPS[e];
+        al[slot] = avals[lid];
+        NI[lid] = slot;
+        if (bid < K - 1) lid = entry(++bid);
+      }
+      const int edge = ids[lid] >> 1;
+      if (edge != e) continue;
+      const int ns = ndPS[e], ne = ndPS[e + 1];
+      for (int q = 0; q < ne - ns; ++q) {
+        const int slot = ns + e + 1 + q;
+        ix[2 * slot] = w.isxy[2 * lid];
+        ix[2 * slot + 1] = w.isxy[2 * lid + 1];
+        al[slot] = avals[lid];
+        NI[lid] = slot;
+        rec[slot] = lid;
+        if (bid < K - 1) lid = entry(++bid);
+      }
+    }
+  };
+  copy_runs(true, nb, w.bAll, w.bND, w.sB, nullptr, ub, w.aB, w.ixB, w.alB, w.bNI, w.recB);
+  copy_runs(false, nc, w.cAll, w.cND, w.sC, w.csorted, uc, w.aC, w.ixC, w.alC, w.cNI, w.recC);
+  // neighbours: the last record written to a slot wins
+  for (int i = 0; i < K; ++i) {
+    w.nbB[w.bNI[i]] = w.cNI[i] + 1;
+    w.nbC[w.cNI[i]] = w.bNI[i] + 1;
+  }
+  // ---- A14 initial labels (calculateInitLabelParallel, :7925-7988)
+  for (int q = 0; q < nQ; ++q) w.cWin[q] = -1;
+  for (int i = 0; i < nB; ++i) {
+    w.labB[i] = 0;
+    if (w.alB[i] == -100) continue;
+    const double cx = w.ixB[2 * i], cy = w.ixB[2 * i + 1];
+    const int tm = (i - 1 == -1) ? nB - 1 : i - 1;
+    const double pmx = w.ixB[2 * tm], pmy = w.ixB[2 * tm + 1];
+    const int pMN = w.alB[tm] != -100 ? w.nbB[tm] - 1 : -100;
+    const int tp = (i + 1 == nB) ? 0 : i + 1;
+    const double ppx = w.ixB[2 * tp], ppy = w.ixB[2 * tp + 1];
+    const int pPN = w.alB[tp] != -100 ? w.nbB[tp] - 1 : -100;
+    const int nId = w.nbB[i] - 1;
+    int qt[2];
+    for (int side = 0; side < 2; ++side) {
+      int q = side == 0 ? nId - 1 : nId + 1;
+      if (q == nQ) q = 0;
+      else if (q == -1) q = nQ - 1;
+      if (q < 0 || q >= nQ) {
+        res.status = PS_UNDEF;
+        return res;
+      }
+      const double qx = w.ixC[2 * q], qy = w.ixC[2 * q + 1];
+      int r;
+      if (pMN != -100 && pMN == q) r = 2;
+      else if (pPN != -100 && pPN == q) r = 3;
+      else {
+        const double s1 = area3(qx, qy, pmx, pmy, cx, cy);
+        const double s2 = area3(qx, qy, cx, cy, ppx, ppy);
+        const double s3 = area3(pmx, pmy, cx, cy, ppx, ppy);
+        if (s3 > 0) r = (s1 > 0 && s2 > 0) ? 0 : 1;
+        else r = (s1 < 0 && s2 < 0) ? 1 : 0;
+      }
+      qt[side] = r;
+    }
+    const int qm = qt[0], qp = qt[1];
+    int lab;
+    if ((qm == 0 && qp == 1) || (qm == 1 && qp == 0)) lab = 1;
+    else if ((qm == 0 && qp == 0) || (qm == 1 && qp == 1)) lab = 2;
+    else if ((qp == 3 && qm == 1) || (qm == 3 && qp == 1)) lab = 3;
+    else if ((qp == 3 && qm == 0) || (qm == 3 && qp == 0)) lab = 4;
+    else if ((qp == 3 && qm == 2) || (qm == 3 && qp == 2)) lab = 5;
+    else if ((qm == 2 && qp == 1) || (qp == 2 && qm == 1)) lab = 6;
+    else if ((qm == 2 && qp == 0) || (qp == 2 && qm == 0)) lab = 7;
+    else lab = -102;
+    w.labB[i] = lab;
+    if (nId < 0 || nId >= nQ) {
+      res.status = PS_UNDEF;
+      return res;
+    }
+    w.cWin[nId] = max(w.cWin[nId], i);
+  }
+  for (int q = 0; q < nQ; ++q) w.labC[q] = w.cWin[q] >= 0 ? w.labB[w.cWin[q]] : 0;
+  // ---- A15-A18 linked-list back end
+  SerialArgs a;
+  a.P = w.P;
+  a.Q = w.Q;
+  a.R = w.R;
+  a.P.n = a.Q.n = a.R.n = 0;
+  a.rroot = w.rroot;
+  a.rcap = cp.rcap;
+  a.nrings = &w.counts[0];
+  a.status = &w.counts[1];
+  a.splitP = w.splitP;
+  a.splitQ = w.splitQ;
+  a.crossP = w.crossP;
+  a.crossQ = w.crossQ;
+  for (int i = 0; i < cp.capP; ++i) w.splitP[i] = w.crossP[i] = 0;
+  for (int i = 0; i < cp.capQ; ++i) w.splitQ[i] = w.crossQ[i] = 0;
+  a.bSize = nb;
+  a.cSize = nc;
+  a.cStart = 0;
+  a.nB = nB;
+  a.nQ = nQ;
+  a.bP = b;
+  a.cP = c;
+  a.ixB = w.ixB;
+  a.ixC = w.ixC;
+  a.alB = w.alB;
+  a.nbC = w.nbC;
+  a.labB = w.labB;
+  a.labC = w.labC;
+  *a.nrings = 0;
+  int st = ser_build(a);
+  if (!st) st = ser_label_trace(a);
+  if (!st) ser_cleanup(a);
+  if (st) {
+    res.status = st == 2 ? PS_UNDEF : PS_CAP;
+    return res;
+  }
+  // ---- rings out: offsets, coordinates, provenance, area
+  int nr = 0, nv = 0;
+  double area = 0.0;
+  w.roff[0] = 0;
+  for (int r = 0; r < *a.nrings; ++r) {
+    const int root = a.rroot[r];
+    if (root < 0) continue;
+    int v = root;
+    const int first = nv;
+    do {
+      const double x = a.R.x[v], y = a.R.y[v];
+      w.rxy[2 * nv] = x;
+      w.rxy[2 * nv + 1] = y;
+      // provenance: the merged slot the vertex was copied from (base first)
+      int4 tp = make_int4(-1, 0, 0, 0);
+      for (int s = 0; s < nB && tp.x < 0; ++s) {
+        if (w.ixB[2 * s] != x || w.ixB[2 * s + 1] != y) continue;
+        if (w.srcB[s] >= 0) tp = make_int4(0, w.srcB[s], 0, 0);
+        else if (w.recB[s] >= 0) {
+          const int rr = w.recB[s];
+          tp = ut[rr] == 1 ? make_int4(2, ub[rr] >> 1, uc[rr] >> 1, 0)
+                           : ((ut[rr] == 2 || ut[rr] == 6) ? make_int4(0, ub[rr] >> 1, 0, 0)
+                                                           : make_int4(1, uc[rr] >> 1, 0, 0));
+        }
+      }
+      for (int s = 0; s < nQ && tp.x < 0; ++s) {
+        if (w.ixC[2 * s] != x || w.ixC[2 * s + 1] != y) continue;
+        if (w.srcC[s] >= 0) tp = make_int4(1, w.srcC[s], 0, 0);
+        else if (w.recC[s] >= 0) {
+          const int rr = w.recC[s];
+          tp = ut[rr] == 1 ? make_int4(2, ub[rr] >> 1, uc[rr] >> 1, 0)
+                           : ((ut[rr] == 2 || ut[rr] == 6) ? make_int4(0, ub[rr] >> 1, 0, 0)
+                                                           : make_int4(1, uc[rr] >> 1, 0, 0));
+        }
+      }
+      w.tape[nv] = tp;
+      ++nv;
+      v = a.R.next[v];
+    } while (v != root);
+    double s2 = 0.0;  // shoelace of the ring
+    for (int i = first; i < nv; ++i) {
+      const int j = (i + 1 == nv) ? first : i + 1;
+      s2 = dadd(s2, dsub(dmul(w.rxy[2 * i], w.rxy[2 * j + 1]), dmul(w.rxy[2 * j], w.rxy[2 * i + 1])));
+    }
+    area = dadd(area, dmul(0.5, s2));
+    w.roff[++nr] = nv;
+  }
+  res.nrings = nr;
+  res.nverts = nv;
+  res.area = area;
+  return res;
+}
+
+// ------------------------------------------------------------------ kernels
+__global__ void k_batch_size(int np, const long long* __restrict__ boff,
+                             const long long* __restrict__ coff, const int* __restrict__ pass_of,
+                             long long* __restrict__ bytes) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p > np) return;
+  if (p == np) {
+    bytes[p] = 0;
+    return;
+  }
+  const int nb = (int)(boff[p + 1] - boff[p]), nc = (int)(coff[p + 1] - coff[p]);
+  const int pass = pass_of ? pass_of[p] : 0;
+  const bool ok = nb >= 3 && nc >= 3 && nb <= SBC_BATCH_MAX_VERTICES && nc <= SBC_BATCH_MAX_VERTICES;
+  bytes[p] = (ok && pass >= 0) ? (long long)arena_bytes(nb, nc, hit_cap(nb, nc, pass)) : 0;
+}
+
+// per pair: status, rings, vertices, area (and the arena holds its rings/tape)
+__global__ void __launch_bounds__(kBatchBlock)
+k_batch_clip(int np, const double* __restrict__ bxy, const long long* __restrict__ boff,
+             const double* __restrict__ cxy, const long long* __restrict__ coff,
+             const int* __restrict__ pass_of, unsigned char* __restrict__ arena,
+             const long long* __restrict__ aoff, int* __restrict__ status, int* __restrict__ nrings,
+             int* __restrict__ nverts, double* __restrict__ area) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  const int pass = pass_of ? pass_of[p] : 0;
+  if (pass < 0) return;  // settled in an earlier pass
+  const int nb = (int)(boff[p + 1] - boff[p]), nc = (int)(coff[p + 1] - coff[p]);
+  if (nb < 3 || nc < 3 || nb > SBC_BATCH_MAX_VERTICES || nc > SBC_BATCH_MAX_VERTICES) {
+    status[p] = SBC_EINPUT;
+    nrings[p] = nverts[p] = 0;
+    area[p] = 0.0;
+    return;
+  }
+  const Caps cp = caps_of(nb, nc, hit_cap(nb, nc, pass));
+  Carver cv{arena + aoff[p], 0};
+  PairWork w = carve(cv, cp);
+  const PairResult r = clip_pair_serial(bxy + 2 * boff[p], nb, cxy + 2 * coff[p], nc, cp, w);
+  status[p] = r.status == PS_OK ? SBC_OK : (r.status == PS_UNDEF ? SBC_EUNDEF : SBC_ENOMEM);
+  nrings[p] = r.nrings;
+  nverts[p] = r.nverts;
+  area[p] = r.area;
+}
+
+__global__ void k_batch_counts(int np, const int* __restrict__ status, const int* __restrict__ nr,
+                               const int* __restrict__ nv, long long* __restrict__ rpre,
+                               long long* __restrict__ vpre) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p > np) return;
+  const bool ok = p < np && status[p] == SBC_OK;
+  rpre[p] = ok ? nr[p] : 0;
+  vpre[p] = ok ? nv[p] : 0;
+}
+
+// where a pair's data lives: pass 0 arena, or the retry arena (full capacity)
+struct Arenas {
+  const unsigned char* a0;
+  const long long* off0;
+  const unsigned char* a1;
+  const long long* off1;
+  const int* pass;  // per pair: 0 or 1
+  __device__ const unsigned char* at(int p) const {
+    return pass[p] == 1 ? a1 + off1[p] : a0 + off0[p];
+  }
+};
+
+// rings of every pair packed: pair_ring[p] .. pair_ring[p+1] ring offsets
+__global__ void k_batch_pack(int np, const long long* __restrict__ boff,
+                             const long long* __restrict__ coff, Arenas ar,
+                             const int* __restrict__ status,
+                             const long long* __restrict__ rpre, const long long* __restrict__ vpre,
+                             long long* __restrict__ ring_off, double* __restrict__ xy) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  const long long r0 = rpre[p], v0 = vpre[p];
+  const int nr = (int)(rpre[p + 1] - r0);
+  if (nr == 0 || status[p] != SBC_OK) return;
+  const int nb = (int)(boff[p + 1] - boff[p]), nc = (int)(coff[p + 1] - coff[p]);
+  const Caps cp = caps_of(nb, nc, hit_cap(nb, nc, ar.pass[p]));
+  Carver cv{const_cast<unsigned char*>(ar.at(p)), 0};
+  const PairWork w = carve(cv, cp);
+  for (int r = 0; r < nr; ++r) ring_off[r0 + r] = v0 + w.roff[r];
+  const int nv = w.roff[nr];
+  for (int i = 0; i < 2 * nv; ++i) xy[2 * v0 + i] = w.rxy[i];
+}
+
+// d(area)/d(vertices), one thread per pair, from the forward pass's tape
+__global__ void __launch_bounds__(kBatchBlock)
+k_batch_backward(int np, const double* __restrict__ bxy, const long long* __restrict__ boff,
+                 const double* __restrict__ cxy, const long long* __restrict__ coff, Arenas ar,
+                 const int* __restrict__ status, const int* __restrict__ nrings,
+                 const double* __restrict__ gA,
+                 double* __restrict__ gb, double* __restrict__ gc) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  const int nb = (int)(boff[p + 1] - boff[p]), nc = (int)(coff[p + 1] - coff[p]);
+  double* gbp = gb + 2 * boff[p];
+  double* gcp = gc + 2 * coff[p];
+  for (int i = 0; i < 2 * nb; ++i) gbp[i] = 0.0;
+  for (int i = 0; i < 2 * nc; ++i) gcp[i] = 0.0;
+  if (status[p] != SBC_OK || nrings[p] == 0) return;
+  const double* b = bxy + 2 * boff[p];
+  const double* c = cxy + 2 * coff[p];
+  const Caps cp = caps_of(nb, nc, hit_cap(nb, nc, ar.pass[p]));
+  Carver cv{const_cast<unsigned char*>(ar.at(p)), 0};
+  const PairWork w = carve(cv, cp);
+  const double g = gA[p];
+  const int nr = nrings[p];
+  for (int r = 0; r < nr; ++r) {
+    const int s = w.roff[r], e = w.roff[r + 1];
+    for (int i = s; i < e; ++i) {
+      const int ip = (i + 1 == e) ? s : i + 1, im = (i == s) ? e - 1 : i - 1;
+      // shoelace: dA/dx_i = (y_{i+1} - y_{i-1}) / 2, dA/dy_i = (x_{i-1} - x_{i+1}) / 2
+      const double gx = 0.5 * g * (w.rxy[2 * ip + 1] - w.rxy[2 * im + 1]);
+      const double gy = 0.5 * g * (w.rxy[2 * im] - w.rxy[2 * ip]);
+      const int4 t = w.tape[i];
+      if (t.x == 0) {
+        gbp[2 * t.y] += gx;
+        gbp[2 * t.y + 1] += gy;
+      } else if (t.x == 1) {
+        gcp[2 * t.y] += gx;
+        gcp[2 * t.y + 1] += gy;
+      } else if (t.x == 2) {
+        // I = (1 - alpha) b1 + alpha b2, alpha = A1 / (A1 - A2),
+        // A1 = A(b1, c1, c2), A2 = A(b2, c1, c2)
+        const int i1 = t.y, i2 = (t.y + 1) % nb, j1 = t.z, j2 = (t.z + 1) % nc;
+        const double b1x = b[2 * i1], b1y = b[2 * i1 + 1], b2x = b[2 * i2], b2y = b[2 * i2 + 1];
+        const double c1x = c[2 * j1], c1y = c[2 * j1 + 1], c2x = c[2 * j2], c2y = c[2 * j2 + 1];
+        const double A1 = (c1x - b1x) * (c2y - b1y) - (c1y - b1y) * (c2x - b1x);
+        const double A2 = (c1x - b2x) * (c2y - b2y) - (c1y - b2y) * (c2x - b2x);
+        const double d = A1 - A2;
+        const double al = A1 / d;
+        const double ga = gx * (b2x - b1x) + gy * (b2y - b1y);  // dA/dalpha
+        const double k1 = -A2 / (d * d) * ga, k2 = A1 / (d * d) * ga;  // dalpha/dA1, dalpha/dA2
+        // A(P, Q, R) partials: dP = (Qy - Ry, Rx - Qx), dQ = (Ry - Py, Px - Rx),
+        // dR = (Py - Qy, Qx - Px)
+        gbp[2 * i1] += (1.0 - al) * gx + k1 * (c1y - c2y);
+        gbp[2 * i1 + 1] += (1.0 - al) * gy + k1 * (c2x - c1x);
+        gbp[2 * i2] += al * gx + k2 * (c1y - c2y);
+        gbp[2 * i2 + 1] += al * gy + k2 * (c2x - c1x);
+        gcp[2 * j1] += k1 * (c2y - b1y) + k2 * (c2y - b2y);
+        gcp[2 * j1 + 1] += k1 * (b1x - c2x) + k2 * (b2x - c2x);
+        gcp[2 * j2] += k1 * (b1y - c1y) + k2 * (b2y - c1y);
+        gcp[2 * j2 + 1] += k1 * (c1x - b1x) + k2 * (c1x - b2x);
+      }
+    }
+  }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host
+int BatchRunner::forward(int np_, const double* d_bxy, const long long* d_boff,
+                         const double* d_cxy, const long long* d_coff, cudaStream_t st) {
+  BufferPool& pool = pl_.pool();
+  valid = false;
+  np = np_;
+  key_b = d_bxy;
+  key_c = d_cxy;
+  if (np <= 0) {
+    valid = true;
+    return kOk;
+  }
+  aoff[0] = (long long*)pool.get("bt_aoff0", sizeof(long long) * (np + 1));
+  aoff[1] = (long long*)pool.get("bt_aoff1", sizeof(long long) * (np + 1));
+  pass = (int*)pool.get("bt_pass", sizeof(int) * (np + 1));
+  status = (int*)pool.get("bt_status", sizeof(int) * (np + 1));
+  nrings = (int*)pool.get("bt_nrings", sizeof(int) * (np + 1));
+  nverts = (int*)pool.get("bt_nverts", sizeof(int) * (np + 1));
+  area = (double*)pool.get("bt_area", sizeof(double) * (np + 1));
+  void* sscr = pool.get("bt_scan", scan_scratch_bytes(np + 1));
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch)");
+  // pass 0: every pair with a generous hit capacity
+  {
+    ::sbc::KProbe kp_("k_batch_size", st);
+    k_batch_size<<<grid_for(np + 1, 256), 256, 0, st>>>(np, d_boff, d_coff, nullptr, aoff[0]);
+  }
+  exclusive_scan_i64(aoff[0], np + 1, sscr, st);
+  long long total = 0;
+  cudaMemcpyAsync(&total, aoff[0] + np, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch sizes");
+  arena[0] = (unsigned char*)pool.get("bt_arena0", (size_t)total + 256);
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch arena)");
+  {
+    ::sbc::KProbe kp_("k_batch_clip", st);
+    k_batch_clip<<<grid_for(np, kBatchBlock), kBatchBlock, 0, st>>>(
+        np, d_bxy, d_boff, d_cxy, d_coff, nullptr, arena[0], aoff[0], status, nrings, nverts, area);
+  }
+  std::vector<int> hs(np);
+  cudaMemcpyAsync(hs.data(), status, sizeof(int) * np, cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch clip");
+  // pass 1: pairs that ran out of hit capacity, with the full product
+  std::vector<int> hp(np, -1);
+  int retry = 0;
+  for (int p = 0; p < np; ++p)
+    if (hs[p] == SBC_ENOMEM) {
+      hp[p] = 1;
+      ++retry;
+    }
+  arena[1] = arena[0];
+  if (retry) {
+    cudaMemcpyAsync(pass, hp.data(), sizeof(int) * np, cudaMemcpyHostToDevice, st);
+    {
+      ::sbc::KProbe kp_("k_batch_size", st);
+      k_batch_size<<<grid_for(np + 1, 256), 256, 0, st>>>(np, d_boff, d_coff, pass, aoff[1]);
+    }
+    exclusive_scan_i64(aoff[1], np + 1, sscr, st);
+    cudaMemcpyAsync(&total, aoff[1] + np, sizeof(long long), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch sizes");
+    arena[1] = (unsigned char*)pool.get("bt_arena1", (size_t)total + 256);
+    if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch arena)");
+    {
+      ::sbc::KProbe kp_("k_batch_clip", st);
+      k_batch_clip<<<grid_for(np, kBatchBlock), kBatchBlock, 0, st>>>(
+          np, d_bxy, d_boff, d_cxy, d_coff, pass, arena[1], aoff[1], status, nrings, nverts, area);
+    }
+  }
+  for (int p = 0; p < np; ++p) hp[p] = hp[p] == 1 ? 1 : 0;
+  cudaMemcpyAsync(pass, hp.data(), sizeof(int) * np, cudaMemcpyHostToDevice, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch clip");
+  valid = true;
+  return kOk;
+}
+
+int BatchRunner::rings(const long long* d_boff, const long long* d_coff, cudaStream_t st,
+                       long long** pair_ring, long long** ring_off, double** xy,
+                       long long* total_rings, long long* total_verts) {
+  BufferPool& pool = pl_.pool();
+  long long* rpre = (long long*)pool.get("bt_rpre", sizeof(long long) * (np + 1));
+  long long* vpre = (long long*)pool.get("bt_vpre", sizeof(long long) * (np + 1));
+  void* sscr = pool.get("bt_scan", scan_scratch_bytes(np + 1));
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch rings)");
+  {
+    ::sbc::KProbe kp_("k_batch_counts", st);
+    k_batch_counts<<<grid_for(np + 1, 256), 256, 0, st>>>(np, status, nrings, nverts, rpre, vpre);
+  }
+  exclusive_scan_i64(rpre, np + 1, sscr, st);
+  exclusive_scan_i64(vpre, np + 1, sscr, st);
+  long long h[2];
+  cudaMemcpyAsync(&h[0], rpre + np, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(&h[1], vpre + np, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch rings");
+  long long* roff = (long long*)pool.get("bt_ring_off", sizeof(long long) * (h[0] + 1));
+  double* oxy = (double*)pool.get("bt_xy", sizeof(double) * 2 * (h[1] + 1));
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch rings)");
+  const Arenas ar{arena[0], aoff[0], arena[1], aoff[1], pass};
+  if (np > 0) {
+    ::sbc::KProbe kp_("k_batch_pack", st);
+    k_batch_pack<<<grid_for(np, 128), 128, 0, st>>>(np, d_boff, d_coff, ar, status, rpre, vpre,
+                                                    roff, oxy);
+  }
+  cudaMemcpyAsync(roff + h[0], &h[1], sizeof(long long), cudaMemcpyHostToDevice, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch pack");
+  *pair_ring = rpre;
+  *ring_off = roff;
+  *xy = oxy;
+  *total_rings = h[0];
+  *total_verts = h[1];
+  return kOk;
+}
+
+int BatchRunner::backward(const double* d_bxy, const long long* d_boff, const double* d_cxy,
+                          const long long* d_coff, const double* d_gA, double* d_gb,
+                          double* d_gc, cudaStream_t st) {
+  if (np <= 0) return kOk;
+  const Arenas ar{arena[0], aoff[0], arena[1], aoff[1], pass};
+  {
+    ::sbc::KProbe kp_("k_batch_backward", st);
+    k_batch_backward<<<grid_for(np, kBatchBlock), kBatchBlock, 0, st>>>(
+        np, d_bxy, d_boff, d_cxy, d_coff, ar, status, nrings, d_gA, d_gb, d_gc);
+  }
+  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch backward");
+  return kOk;
+}
+
+}  // namespace sbc

@@ -124,6 +124,7 @@ class Pipeline {
     if (err_.empty()) err_ = msg;
     return code;
   }
+  void clear_error() { err_.clear(); }
   unsigned read_flags();
   void clear_flags();
 
@@ -151,5 +152,34 @@ struct Merged {
   const double* cP;    // overlays with closing vertices
 };
 int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out);
+
+// Many small independent pairs, one device thread each (sbc_batch.cu).  The
+// forward pass keeps each pair's rings and vertex provenance in its arena
+// for rings() and backward().
+class BatchRunner {
+ public:
+  explicit BatchRunner(Pipeline& pl) : pl_(pl) {}
+  int forward(int np, const double* d_bxy, const long long* d_boff, const double* d_cxy,
+              const long long* d_coff, cudaStream_t st);
+  int rings(const long long* d_boff, const long long* d_coff, cudaStream_t st,
+            long long** pair_ring, long long** ring_off, double** xy, long long* total_rings,
+            long long* total_verts);
+  int backward(const double* d_bxy, const long long* d_boff, const double* d_cxy,
+               const long long* d_coff, const double* d_gA, double* d_gb, double* d_gc,
+               cudaStream_t st);
+  // per pair (device): status, rings, vertices, area
+  int np = 0;
+  int *status = nullptr, *nrings = nullptr, *nverts = nullptr;
+  double* area = nullptr;
+  const void* key_b = nullptr;  // the forward's inputs (for reuse by backward)
+  const void* key_c = nullptr;
+  bool valid = false;
+
+ private:
+  Pipeline& pl_;
+  unsigned char* arena[2] = {nullptr, nullptr};
+  long long* aoff[2] = {nullptr, nullptr};
+  int* pass = nullptr;
+};
 
 }  // namespace sbc

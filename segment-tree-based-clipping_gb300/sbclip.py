@@ -63,6 +63,30 @@ class _MergedLists(ctypes.Structure):
 NOALLOC_MAX_UNITS = 262144
 
 
+class _Batch(ctypes.Structure):
+    _fields_ = [("npairs", ctypes.c_int), ("b_xy", ctypes.c_void_p), ("b_off", ctypes.c_void_p),
+                ("c_xy", ctypes.c_void_p), ("c_off", ctypes.c_void_p)]
+
+
+class _BatchRings(ctypes.Structure):
+    _fields_ = [("npairs", ctypes.c_int), ("nrings", ctypes.c_longlong),
+                ("nverts", ctypes.c_longlong), ("pair_ring", ctypes.c_void_p),
+                ("ring_off", ctypes.c_void_p), ("xy", ctypes.c_void_p),
+                ("status", ctypes.c_void_p)]
+
+
+BATCH_MAX_VERTICES = 4096
+
+
+def pack_polygons(polys):
+    """Concatenate polygons: (xy (n,2) float64, offsets (len+1,) int64)."""
+    arrs = [np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 2) for p in polys]
+    off = np.zeros(len(arrs) + 1, dtype=np.int64)
+    off[1:] = np.cumsum([a.shape[0] for a in arrs])
+    xy = np.ascontiguousarray(np.concatenate(arrs, axis=0)) if arrs else np.zeros((0, 2))
+    return xy, off
+
+
 _lib = None
 
 
@@ -90,6 +114,12 @@ def load_library(path: str | os.PathLike | None = None):
     L.sbc_kernel_launches.restype = ctypes.c_ulonglong
     L.sbc_profile_end.argtypes = [vp, i, vp, vp, i, ctypes.POINTER(i)]
     L.sbc_version.restype = ctypes.c_char_p
+    for nm in ("sbc_clip_batch", "sbc_clip_batch_device"):
+        getattr(L, nm).argtypes = [vp, ctypes.POINTER(_Batch), ctypes.POINTER(_BatchRings), vp]
+    for nm in ("sbc_area_forward", "sbc_area_forward_device"):
+        getattr(L, nm).argtypes = [vp, ctypes.POINTER(_Batch), vp, vp, vp]
+    for nm in ("sbc_area_backward", "sbc_area_backward_device"):
+        getattr(L, nm).argtypes = [vp, ctypes.POINTER(_Batch), vp, vp, vp, vp]
     L.sbc_trace_rings_noalloc.argtypes = [ctypes.POINTER(_MergedLists), vp, i, vp, ll,
                                           ctypes.POINTER(i), ctypes.POINTER(ll), vp,
                                           ctypes.c_char_p, i]
@@ -199,6 +229,70 @@ class Clipper:
         self._check(self._L.sbc_clip_pair_device(self._h, d_base, nb, d_overlay, nc,
                                                  ctypes.byref(r), stream))
         return r.nrings, int(r.nverts), r.offsets, r.xy
+
+    # ---- batches of independent pairs (host arrays)
+    def _batch(self, bases, overlays):
+        if len(bases) != len(overlays):
+            raise ValueError("one overlay per base")
+        bxy, boff = pack_polygons(bases)
+        cxy, coff = pack_polygons(overlays)
+        keep = (bxy, boff, cxy, coff)
+        b = _Batch(len(bases), bxy.ctypes.data, boff.ctypes.data, cxy.ctypes.data, coff.ctypes.data)
+        return b, keep
+
+    def clip_batch(self, bases, overlays, stream: int | None = None):
+        """Rings of every pair: (list of ring lists, status array)."""
+        b, keep = self._batch(bases, overlays)
+        r = _BatchRings()
+        self._check(self._L.sbc_clip_batch(self._h, ctypes.byref(b), ctypes.byref(r), stream))
+        np_ = len(bases)
+        pr = np.ctypeslib.as_array(ctypes.cast(r.pair_ring, ctypes.POINTER(ctypes.c_longlong)),
+                                   (np_ + 1,)).copy()
+        ro = np.ctypeslib.as_array(ctypes.cast(r.ring_off, ctypes.POINTER(ctypes.c_longlong)),
+                                   (int(r.nrings) + 1,)).copy()
+        xy = (np.ctypeslib.as_array(ctypes.cast(r.xy, ctypes.POINTER(ctypes.c_double)),
+                                    (2 * int(r.nverts),)).copy().reshape(-1, 2)
+              if r.nverts > 0 else np.zeros((0, 2)))
+        st = np.ctypeslib.as_array(ctypes.cast(r.status, ctypes.POINTER(ctypes.c_int)),
+                                   (np_,)).copy() if np_ else np.zeros(0, np.int32)
+        out = []
+        for p in range(np_):
+            out.append([xy[ro[q]:ro[q + 1]] for q in range(pr[p], pr[p + 1])])
+        return out, st
+
+    def area_forward(self, bases, overlays, stream: int | None = None):
+        """Intersection area of every pair: (area, status)."""
+        b, keep = self._batch(bases, overlays)
+        area = np.zeros(len(bases), np.float64)
+        st = np.zeros(len(bases), np.int32)
+        self._check(self._L.sbc_area_forward(self._h, ctypes.byref(b), area.ctypes.data,
+                                             st.ctypes.data, stream))
+        return area, st
+
+    def area_backward(self, bases, overlays, grad_area, stream: int | None = None):
+        """d(sum grad_area * area)/d(vertices): (list of (nb,2), list of (nc,2))."""
+        b, keep = self._batch(bases, overlays)
+        ga = np.ascontiguousarray(grad_area, dtype=np.float64)
+        boff, coff = keep[1], keep[3]
+        gb = np.zeros((int(boff[-1]), 2))
+        gc = np.zeros((int(coff[-1]), 2))
+        self._check(self._L.sbc_area_backward(self._h, ctypes.byref(b), ga.ctypes.data,
+                                              gb.ctypes.data, gc.ctypes.data, stream))
+        return ([gb[boff[p]:boff[p + 1]] for p in range(len(bases))],
+                [gc[coff[p]:coff[p + 1]] for p in range(len(overlays))])
+
+    # ---- device-array variants (pointers from e.g. torch tensors)
+    def area_forward_device(self, npairs, d_bxy, d_boff, d_cxy, d_coff, d_area, d_status=None,
+                            stream: int | None = None):
+        b = _Batch(npairs, d_bxy, d_boff, d_cxy, d_coff)
+        self._check(self._L.sbc_area_forward_device(self._h, ctypes.byref(b), d_area, d_status,
+                                                    stream))
+
+    def area_backward_device(self, npairs, d_bxy, d_boff, d_cxy, d_coff, d_grad_area, d_grad_b,
+                             d_grad_c, stream: int | None = None):
+        b = _Batch(npairs, d_bxy, d_boff, d_cxy, d_coff)
+        self._check(self._L.sbc_area_backward_device(self._h, ctypes.byref(b), d_grad_area,
+                                                     d_grad_b, d_grad_c, stream))
 
     def stats(self) -> dict:
         arr = (ctypes.c_longlong * len(STATS))()
