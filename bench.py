@@ -2,7 +2,7 @@
 """Benchmark: milliseconds per 1M x 1M polygon clip on one GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload pair_1m_1m|pair_200k_200k|pair_10k_8k]
+                    [--workload pair_1m_1m|pair_200k_200k|pair_10k_8k|small_pairs_65536]
 
 A step is one full clip of the workload pair (segment tree build, candidate
 stab queries, FP64 intersection, merge, labelling and ring tracing) by the
@@ -18,6 +18,13 @@ that a C caller reads in place) inside every step.
 The single pair does not shard across GPUs (the tree and the tracing are
 global), so N > 1 runs N independent replicas, one per rank (torchrun), and
 reports the max over ranks.
+
+`--workload small_pairs_65536` measures the batched path instead: 65,536
+independent small pairs (4-64 vertices), one step = their intersection areas
+and area gradients on device-resident arrays, reported as pairs per second
+(whole job; under torchrun each rank clips its own 65,536 pairs), next to
+the plain per-pair GPU path (one sbc_clip_pair_device call per pair) and the
+reference run pairwise on the host cores.
 
 `--impl reference` times the reference's own CPU (OpenMP) build
 (oracle/_ref/seg, all host threads) on the same workload; when that build is
@@ -283,7 +290,180 @@ def cpu_baseline(b, c, args, steps: int = 1):
             "sample": f"{steps} full {args.workload} clip(s) by the C restatement (1 thread)"}
 
 
+# ---------------------------------------------------------------- small-pair batches
+SMALL_PAIRS = 65536
+
+
+def small_pairs_workload(n: int, seed: int):
+    pairs = gen.small_pairs(n, seed=seed)
+    desc = {"workload": f"small_pairs_{n}", "pairs": n, "vertices_per_polygon": "U[4,64]",
+            "generator": "plain stars r=0.5+0.5u, overlay centre offset U[-0.5,0.5]^2"}
+    return pairs, desc
+
+
+def reference_pairs_per_s(pairs, threads: int):
+    """The reference's CPU build run pairwise (one process per pair, `threads`
+    processes at a time) on a sample of pairs: clipped pairs per second."""
+    import oracle_py as O
+    from concurrent.futures import ThreadPoolExecutor
+    if not O.ref_available():
+        t0 = time.perf_counter()
+        for b, c in pairs:
+            O.clip(b, [c])
+        return len(pairs) / (time.perf_counter() - t0), 1, "port"
+    def one(bc):
+        try:  # the reference crashes on some inputs (reads past its arrays)
+            O.run_reference(bc[0], [bc[1]], threads=1, precision=6, timeout=60)
+            return 1
+        except RuntimeError:
+            return 0
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(one, pairs))
+    return len(pairs) / (time.perf_counter() - t0), threads, "reference"
+
+
+def run_small_pairs(args, rank: int, world: int):
+    """One step = intersection areas of every pair (sbc_area_forward_device)
+    and their gradient (sbc_area_backward_device, reusing the forward's
+    records), all pairs in one launch each; inputs resident on the device."""
+    import torch
+    import sbclip
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    n = SMALL_PAIRS
+    pairs, desc = small_pairs_workload(n, 4000 + rank)
+    bases, ovs = [b for b, _ in pairs], [c for _, c in pairs]
+    bxy, boff = sbclip.pack_polygons(bases)
+    cxy, coff = sbclip.pack_polygons(ovs)
+    cuda = f"cuda:{dev}"
+    t = {k: torch.from_numpy(v).to(cuda) for k, v in
+         (("bxy", bxy), ("boff", boff), ("cxy", cxy), ("coff", coff))}
+    area = torch.zeros(n, dtype=torch.float64, device=cuda)
+    st = torch.zeros(n, dtype=torch.int32, device=cuda)
+    ga = torch.ones(n, dtype=torch.float64, device=cuda)
+    gb = torch.zeros_like(t["bxy"])
+    gc = torch.zeros_like(t["cxy"])
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=cuda)
+    clip = sbclip.Clipper(dev)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    a = (n, t["bxy"].data_ptr(), t["boff"].data_ptr(), t["cxy"].data_ptr(), t["coff"].data_ptr())
+
+    def step():
+        clip.area_forward_device(*a, area.data_ptr(), st.data_ptr(), sp)
+        clip.area_backward_device(*a, ga.data_ptr(), gb.data_ptr(), gc.data_ptr(), sp)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    l0 = sbclip.kernel_launches()
+    times = []
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+    launches = sbclip.kernel_launches() - l0
+    ms = float(np.mean(times))
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([ms], device=cuda)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    n_ok = int((st == 0).sum().item())
+    # per-kernel times of one more step
+    torch.cuda.synchronize()
+    sbclip.profile_begin()
+    step()
+    torch.cuda.synchronize()
+    prof = sbclip.profile_end()
+    # end to end through the host-array C ABI: inputs copied in, areas and
+    # gradients copied out (the host backward call runs its own forward)
+    e2e_t = []
+    for _ in range(max(args.steps, 1)):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        clip.area_forward(bases, ovs)
+        clip.area_backward(bases, ovs, np.ones(n))
+        e2e_t.append((time.perf_counter() - t0) * 1e3)
+    in_bytes = 16 * (int(boff[-1]) + int(coff[-1])) + 16 * (n + 1)
+    e2e = {"value": n * world / (float(np.mean(e2e_t)) * 1e-3), "unit": "pairs/s",
+           "h2d_bytes_per_step": 2 * in_bytes + 8 * n,
+           "d2h_bytes_per_step": 12 * n + 16 * (int(boff[-1]) + int(coff[-1]))}
+    # the plain per-pair GPU path (one sbc_clip_pair_device call per pair, forward only)
+    sample = 256
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for p in range(sample):
+        clip.clip_pair_device(t["bxy"].data_ptr() + 16 * int(boff[p]), int(boff[p + 1] - boff[p]),
+                              t["cxy"].data_ptr() + 16 * int(coff[p]), int(coff[p + 1] - coff[p]), sp)
+    torch.cuda.synchronize()
+    per_pair = sample / (time.perf_counter() - t0)
+    pk, kind = peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][0]) if prof else None
+    roof = None
+    if dom:
+        name, (tot_ms, n_l) = dom
+        ab = 16.0 * (int(boff[-1]) + int(coff[-1])) + 12.0 * n  # coordinates in, area + status out
+        achieved = ab / (tot_ms / max(n_l, 1) * 1e-3) / 1e9
+        roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
+                "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "traffic": None,
+                "peak_source": kind, "ms_per_launch": tot_ms / max(n_l, 1)}
+    out = {
+        "metric": "clipped pairs/s, batched area forward+backward, 65,536 small pairs",
+        "value": n * world / (ms * 1e-3), "unit": "pairs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded star polygons)",
+        "config": dict(desc, parallelism="pairs sharded by rank" if world > 1 else "single",
+                       l2="flushed between steps (256 MiB write)"),
+        "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
+        "kernels_top": {k: {"ms_per_step": v[0], "launches_per_step": v[1]}
+                        for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])[:6]},
+        "clocks": clk.summary(),
+        "counts": {"pairs_ok": n_ok, "per_pair_gpu_path_pairs_per_s": per_pair,
+                   "per_pair_sample": sample,
+                   "batched_over_per_pair": (n * world / (ms * 1e-3)) / per_pair},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        v, cores, kind2 = reference_pairs_per_s(pairs[:256], os.cpu_count() or 1)
+        out["cpu_baseline"] = {"value": v, "unit": "pairs/s", "cores": cores, "kind": kind2,
+                               "sample": "256 pairs clipped pairwise (forward only; the "
+                                         "reference computes no gradients)"}
+    clip.close()
+    return out
+
+
 def run_reference_arm(args):
+    if args.workload.startswith("small_pairs"):
+        pairs, desc = small_pairs_workload(SMALL_PAIRS, 4000)
+        steps = max(1, min(args.steps, 3))
+        threads = os.cpu_count() or 1
+        vals = [reference_pairs_per_s(pairs[256 * i:256 * (i + 1)], threads) for i in range(steps)]
+        v = float(np.mean([x[0] for x in vals]))
+        base = {"value": v, "unit": "pairs/s", "cores": vals[0][1], "kind": vals[0][2],
+                "sample": f"{steps} x 256 pairs clipped pairwise (forward only)"}
+        return {"impl": "reference",
+                "metric": "clipped pairs/s, batched area forward+backward, 65,536 small pairs",
+                "value": v, "unit": "pairs/s", "n_gpus": args.gpus, "steps": steps, "warmup": 0,
+                "ms_per_step": 256 / v * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded star polygons)",
+                "config": dict(desc, parallelism="host cores"), "cpu_baseline": base,
+                "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
     b, c, desc = workload(args.workload)
     # each step is one full clip; the CPU arm is capped at 3 steps so the run
     # stays within a few minutes
@@ -309,7 +489,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="pair_1m_1m",
-                    choices=["pair_1m_1m", "pair_200k_200k", "pair_10k_8k"])
+                    choices=["pair_1m_1m", "pair_200k_200k", "pair_10k_8k", "small_pairs_65536"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -321,7 +501,10 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    out = run_gb300(args, rank, world)
+    if args.workload.startswith("small_pairs"):
+        out = run_small_pairs(args, rank, world)
+    else:
+        out = run_gb300(args, rank, world)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
