@@ -249,9 +249,13 @@ unsigned long long sbc_kernel_launches(void);
  * Between sbc_profile_begin and sbc_profile_end every launch of this library
  * is bracketed by CUDA events on its stream.  sbc_profile_end writes up to
  * `cap` kernels: NUL-separated names into `names` (names_len bytes), total
- * milliseconds into ms[i], launch counts into counts[i]; *n_out = kernels. */
+ * milliseconds into ms[i], launch counts into counts[i], and the launches'
+ * summed algorithmic bytes (inputs read and outputs written once, 0 where a
+ * launch states none) into bytes[i]; *n_out = kernels.  Any output pointer
+ * may be NULL. */
 int sbc_profile_begin(void);
-int sbc_profile_end(char* names, int names_len, float* ms, int* counts, int cap, int* n_out);
+int sbc_profile_end(char* names, int names_len, float* ms, int* counts, double* bytes, int cap,
+                    int* n_out);
 
 /* Library version string. */
 const char* sbc_version(void);

@@ -335,16 +335,19 @@ int sbc_profile_begin(void) {
   return SBC_OK;
 }
 
-int sbc_profile_end(char* names, int names_len, float* ms, int* counts, int cap, int* n_out) {
+int sbc_profile_end(char* names, int names_len, float* ms, int* counts, double* bytes, int cap,
+                    int* n_out) {
   std::vector<std::string> nm;
   std::vector<float> t;
   std::vector<int> c;
-  int n = sbc::profile_end(&nm, &t, &c);
+  std::vector<double> by;
+  int n = sbc::profile_end(&nm, &t, &c, &by);
   if (n_out) *n_out = n;
   int w = 0;
   for (int i = 0; i < n && i < cap; ++i) {
     if (ms) ms[i] = t[i];
     if (counts) counts[i] = c[i];
+    if (bytes) bytes[i] = by[i];
     if (names) {
       int need = (int)nm[i].size() + 1;
       if (w + need <= names_len) {

@@ -992,6 +992,13 @@ int BatchRunner::forward(int np_, const double* d_bxy, const long long* d_boff,
   area = (double*)pool.get("bt_area", sizeof(double) * (np + 1));
   void* sscr = pool.get("bt_scan", scan_scratch_bytes(np + 1));
   if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch)");
+  {
+    long long hb = 0, hc = 0;
+    cudaMemcpyAsync(&hb, d_boff + np, sizeof(long long), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&hc, d_coff + np, sizeof(long long), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch offsets");
+    in_verts = (double)(hb + hc);
+  }
   // pass 0: every pair with a generous hit capacity
   {
     ::sbc::KProbe kp_("k_batch_size", st);
@@ -1004,7 +1011,8 @@ int BatchRunner::forward(int np_, const double* d_bxy, const long long* d_boff,
   arena[0] = (unsigned char*)pool.get("bt_arena0", (size_t)total + 256);
   if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch arena)");
   {
-    ::sbc::KProbe kp_("k_batch_clip", st);
+    // coordinates in; area, status, ring and vertex counts out
+    ::sbc::KProbe kp_("k_batch_clip", st, 16.0 * in_verts + 20.0 * np);
     k_batch_clip<<<grid_for(np, kBatchBlock), kBatchBlock, 0, st>>>(
         np, d_bxy, d_boff, d_cxy, d_coff, nullptr, arena[0], aoff[0], status, nrings, nverts, area);
   }
@@ -1087,7 +1095,8 @@ int BatchRunner::backward(const double* d_bxy, const long long* d_boff, const do
   if (np <= 0) return kOk;
   const Arenas ar{arena[0], aoff[0], arena[1], aoff[1], pass};
   {
-    ::sbc::KProbe kp_("k_batch_backward", st);
+    // coordinates in, one gradient per coordinate out
+    ::sbc::KProbe kp_("k_batch_backward", st, 32.0 * in_verts + 8.0 * np);
     k_batch_backward<<<grid_for(np, kBatchBlock), kBatchBlock, 0, st>>>(
         np, d_bxy, d_boff, d_cxy, d_coff, ar, status, nrings, d_gA, d_gb, d_gc);
   }

@@ -761,7 +761,7 @@ int Pipeline::stage_candidates(int cType, int** rb_out, int** rc_out, int** rt_o
   auto* rkey = (unsigned long long*)pool_.get("raw_key", sizeof(unsigned long long) * hcap);
   if (pool_.failed) return fail(kENoMem, "device allocation failed (hits)");
   if (npairs > 0) {
-    ::sbc::KProbe kp_("k_pair_exact", st);
+    ::sbc::KProbe kp_("k_pair_exact", st, 72.0 * npairs);  // pair + both edges' coordinates
     k_pair_exact<<<grid_for(npairs, kExChunk), kExBlock, 0, st>>>(
         npairs, pairs, e_id, bP, cP, vfB, vfC, lr, aft, bef, logL, counters, hcap, rb, rc, rt, rkey);
   }

@@ -488,7 +488,7 @@ int Pipeline::stage_endlists() {
   // ea[0] < 0 decides the shift; ea[0] equals minI
   Borders B{ea, epc, z};
   {
-    ::sbc::KProbe kp_("k_find_leaves", st_);
+    ::sbc::KProbe kp_("k_find_leaves", st_, 24.0 * E);  // es, ee in; aft, bef out
     k_find_leaves<<<grid_for(E, 256), 256, 0, st_>>>(e_s, e_e, E, B, logL, aft, bef, d_treecnt);
   }
   return kOk;
@@ -546,7 +546,7 @@ int Pipeline::stage_cover() {
   lr = (int2*)pool_.get("edge_leaf_range", sizeof(int2) * (E + 1));
   if (pool_.failed) return fail(kENoMem, "device allocation failed (leaf ranges)");
   {
-    ::sbc::KProbe kp_("k_edge_range", st_);
+    ::sbc::KProbe kp_("k_edge_range", st_, 24.0 * E);  // es, ee in; leaf range out
     k_edge_range<<<grid_for(E, 256), 256, 0, st_>>>(e_s, e_e, E, ea, logL, lr, d_treecnt);
   }
   unsigned long long hc[2] = {0, 0};

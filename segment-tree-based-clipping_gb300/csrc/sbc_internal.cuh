@@ -145,8 +145,10 @@ extern unsigned long long g_launches;
 
 // Scoped launch probe: counts the launch and, while profiling is on, brackets
 // it with a pair of CUDA events on its stream (per-kernel device time).
+// `bytes` is the launch's algorithmic traffic (its inputs read and outputs
+// written once; 0 where none is stated), summed per kernel for rooflines.
 struct KProbe {
-  KProbe(const char* name, cudaStream_t st);
+  KProbe(const char* name, cudaStream_t st, double bytes = 0.0);
   ~KProbe();
   const char* name_;
   cudaStream_t st_;
@@ -154,7 +156,8 @@ struct KProbe {
 };
 void profile_begin();
 // aggregated per kernel name: returns the number of distinct kernels
-int profile_end(std::vector<std::string>* names, std::vector<float>* ms, std::vector<int>* counts);
+int profile_end(std::vector<std::string>* names, std::vector<float>* ms, std::vector<int>* counts,
+                std::vector<double>* bytes = nullptr);
 
 inline unsigned grid_for(long long n, int per_block) {
   long long g = (n + per_block - 1) / per_block;

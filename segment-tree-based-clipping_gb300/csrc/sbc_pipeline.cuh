@@ -171,6 +171,7 @@ class BatchRunner {
   int np = 0;
   int *status = nullptr, *nrings = nullptr, *nverts = nullptr;
   double* area = nullptr;
+  double in_verts = 0.0;         // input vertices of the batch (profiling)
   const void* key_b = nullptr;  // the forward's inputs (for reuse by backward)
   const void* key_c = nullptr;
   bool valid = false;

@@ -18,6 +18,7 @@ namespace {
 struct ProbeRec {
   const char* name;
   cudaEvent_t a, b;
+  double bytes;
 };
 bool g_prof_on = false;
 std::vector<ProbeRec> g_recs;
@@ -34,10 +35,10 @@ cudaEvent_t next_event() {
 }
 }  // namespace
 
-KProbe::KProbe(const char* name, cudaStream_t st) : name_(name), st_(st), slot_(-1) {
+KProbe::KProbe(const char* name, cudaStream_t st, double bytes) : name_(name), st_(st), slot_(-1) {
   ++g_launches;
   if (!g_prof_on) return;
-  ProbeRec r{name, next_event(), next_event()};
+  ProbeRec r{name, next_event(), next_event(), bytes};
   cudaEventRecord(r.a, st);
   slot_ = (int)g_recs.size();
   g_recs.push_back(r);
@@ -53,11 +54,13 @@ void profile_begin() {
   g_prof_on = true;
 }
 
-int profile_end(std::vector<std::string>* names, std::vector<float>* ms, std::vector<int>* counts) {
+int profile_end(std::vector<std::string>* names, std::vector<float>* ms, std::vector<int>* counts,
+                std::vector<double>* bytes) {
   g_prof_on = false;
   names->clear();
   ms->clear();
   counts->clear();
+  if (bytes) bytes->clear();
   for (auto& r : g_recs) {
     cudaEventSynchronize(r.b);
     float t = 0.f;
@@ -68,9 +71,11 @@ int profile_end(std::vector<std::string>* names, std::vector<float>* ms, std::ve
       names->push_back(r.name);
       ms->push_back(0.f);
       counts->push_back(0);
+      if (bytes) bytes->push_back(0.0);
     }
     (*ms)[i] += t;
     (*counts)[i] += 1;
+    if (bytes) (*bytes)[i] += r.bytes;
   }
   g_recs.clear();
   g_event_next = 0;
@@ -232,7 +237,7 @@ void scan_rec(T* d, long long n, T* scratch, cudaStream_t st) {
   if (tiles > 1) {
     auto* state = (unsigned long long*)scratch;
     cudaMemsetAsync(state, 0, sizeof(unsigned long long) * (tiles + 1), st);
-    ::sbc::KProbe kp_("k_scan_lb", st);
+    ::sbc::KProbe kp_("k_scan_lb", st, 2.0 * sizeof(T) * (double)n);
     k_scan_lb<T><<<(unsigned)tiles, kScanThreads, 0, st>>>(d, n, state);
     return;
   }
@@ -399,13 +404,15 @@ template <typename K, int kRadRounds>
 void radix_pass(const K* sk, const unsigned* sv, K* dk, unsigned* dv, long long n, int shift,
                 unsigned* hist, unsigned nblocks, void* sscr, cudaStream_t st) {
   {
-    ::sbc::KProbe kp_(sizeof(K) == 8 ? "k_rad_hist_u64" : "k_rad_hist_u32", st);
+    ::sbc::KProbe kp_(sizeof(K) == 8 ? "k_rad_hist_u64" : "k_rad_hist_u32", st,
+                      (double)sizeof(K) * n);
     k_rad_hist<K, kRadRounds><<<nblocks, kRadThreads, 0, st>>>(sk, n, shift, hist, nblocks);
   }
   // exclusive scan of the digit-major histogram gives each (digit, block) its base
   scan_rec<int>((int*)hist, (long long)256 * nblocks, (int*)sscr, st);
   {
-    ::sbc::KProbe kp_(sizeof(K) == 8 ? "k_rad_scatter_u64" : "k_rad_scatter_u32", st);
+    ::sbc::KProbe kp_(sizeof(K) == 8 ? "k_rad_scatter_u64" : "k_rad_scatter_u32", st,
+                      2.0 * (sizeof(K) + sizeof(unsigned)) * n);
     k_rad_scatter<K, kRadRounds><<<nblocks, kRadThreads, 0, st>>>(sk, sv, dk, dv, n, shift, hist,
                                                                 nblocks);
   }

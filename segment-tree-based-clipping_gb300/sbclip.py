@@ -112,7 +112,7 @@ def load_library(path: str | os.PathLike | None = None):
     L.sbc_debug_array.argtypes = [vp, i, vp, ll, ctypes.POINTER(ll)]
     L.sbc_classify_pairs.argtypes = [vp, vp, i, vp, vp, vp, vp, vp]
     L.sbc_kernel_launches.restype = ctypes.c_ulonglong
-    L.sbc_profile_end.argtypes = [vp, i, vp, vp, i, ctypes.POINTER(i)]
+    L.sbc_profile_end.argtypes = [vp, i, vp, vp, vp, i, ctypes.POINTER(i)]
     L.sbc_version.restype = ctypes.c_char_p
     for nm in ("sbc_clip_batch", "sbc_clip_batch_device"):
         getattr(L, nm).argtypes = [vp, ctypes.POINTER(_Batch), ctypes.POINTER(_BatchRings), vp]
@@ -136,16 +136,21 @@ def profile_begin() -> None:
     load_library().sbc_profile_begin()
 
 
-def profile_end() -> dict:
-    """Stop profiling; {kernel name: (total ms, launches)}."""
+def profile_end(with_bytes: bool = False) -> dict:
+    """Stop profiling; {kernel name: (total ms, launches)}, or (total ms,
+    launches, algorithmic bytes) with with_bytes."""
     L = load_library()
     cap = 256
     names = ctypes.create_string_buffer(cap * 64)
     ms = (ctypes.c_float * cap)()
     cnt = (ctypes.c_int * cap)()
+    by = (ctypes.c_double * cap)()
     n = ctypes.c_int()
-    L.sbc_profile_end(names, cap * 64, ms, cnt, cap, ctypes.byref(n))
+    L.sbc_profile_end(names, cap * 64, ms, cnt, by, cap, ctypes.byref(n))
     nm = names.raw.split(b"\0")
+    if with_bytes:
+        return {nm[i].decode(): (float(ms[i]), int(cnt[i]), float(by[i]))
+                for i in range(min(n.value, cap))}
     return {nm[i].decode(): (float(ms[i]), int(cnt[i])) for i in range(min(n.value, cap))}
 
 
