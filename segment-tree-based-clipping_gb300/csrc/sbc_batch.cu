@@ -115,6 +115,7 @@ __host__ __device__ __forceinline__ void carve_pool(Carver& cv, int cap, Pool& p
   p.enex = cv.take<int>(cap);
   p.source = cv.take<unsigned char>(cap);
   p.isect = cv.take<unsigned char>(cap);
+  p.src = cv.take<int>(cap);
   p.n = 0;
   p.cap = cap;
 }
@@ -191,7 +192,7 @@ __host__ __device__ __forceinline__ size_t arena_bytes(int nb, int nc, int K) {
 // more is run again with the full product
 __host__ __device__ __forceinline__ int hit_cap(int nb, int nc, int pass) {
   const long long full = (long long)nb * nc;
-  const long long first = 4LL * (nb + nc) + 16;
+  const long long first = (long long)nb + nc + 16;
   const long long k = pass == 0 ? (first < full ? first : full) : full;
   return (int)(k > 0 ? k : 1);
 }
@@ -761,7 +762,12 @@ __device__ PairResult clip_pair_serial(const double* b, int nb, const double* c,
   a.labC = w.labC;
   *a.nrings = 0;
   int st = ser_build(a);
-  if (!st) st = ser_label_trace(a);
+  if (!st) {
+    // list nodes built from the merged arrays sit at their slot index
+    for (int v = 0; v < a.P.n; ++v) a.P.src[v] = v;
+    for (int v = 0; v < a.Q.n; ++v) a.Q.src[v] = v;
+    st = ser_label_trace(a);
+  }
   if (!st) ser_cleanup(a);
   if (st) {
     res.status = st == 2 ? PS_UNDEF : PS_CAP;
@@ -780,8 +786,24 @@ __device__ PairResult clip_pair_serial(const double* b, int nb, const double* c,
       const double x = a.R.x[v], y = a.R.y[v];
       w.rxy[2 * nv] = x;
       w.rxy[2 * nv + 1] = y;
-      // provenance: the merged slot the vertex was copied from (base first)
+      // provenance: the merged slot the vertex was copied from, as the back
+      // end recorded it; a node it made itself (a midpoint) is looked up by
+      // its coordinates (base slots first)
       int4 tp = make_int4(-1, 0, 0, 0);
+      const int pv = a.R.src[v];
+      if (pv >= 0) {
+        const int sd = pv >> 30, s = pv & 0x3fffffff;
+        const int* srcS = sd ? w.srcC : w.srcB;
+        const int* recS = sd ? w.recC : w.recB;
+        if (srcS[s] >= 0) {
+          tp = make_int4(sd, srcS[s], 0, 0);
+        } else if (recS[s] >= 0) {
+          const int rr = recS[s];
+          tp = ut[rr] == 1 ? make_int4(2, ub[rr] >> 1, uc[rr] >> 1, 0)
+                           : ((ut[rr] == 2 || ut[rr] == 6) ? make_int4(0, ub[rr] >> 1, 0, 0)
+                                                           : make_int4(1, uc[rr] >> 1, 0, 0));
+        }
+      }
       for (int s = 0; s < nB && tp.x < 0; ++s) {
         if (w.ixB[2 * s] != x || w.ixB[2 * s + 1] != y) continue;
         if (w.srcB[s] >= 0) tp = make_int4(0, w.srcB[s], 0, 0);

@@ -24,6 +24,10 @@ struct Pool {
   int *next, *prev, *nb, *label, *enex;
   unsigned char *source, *isect;
   int n, cap;
+  // optional: where each node's coordinates come from (ring nodes: side << 30
+  // | merged slot, list nodes: their merged slot; -1 unknown).  Null when the
+  // caller does not track it.
+  int* src = nullptr;
 };
 
 struct SerialArgs {
@@ -41,6 +45,7 @@ struct SerialArgs {
 __device__ int pnew(Pool& p, double x, double y) {
   if (p.n >= p.cap) return -1;
   int v = p.n++;
+  if (p.src) p.src[v] = -1;
   p.x[v] = x;
   p.y[v] = y;
   p.next[v] = p.prev[v] = v;
@@ -85,9 +90,10 @@ __device__ int rnew(SerialArgs& a) {
   return r;
 }
 
-__device__ int radd(SerialArgs& a, int r, double x, double y) {
+__device__ int radd(SerialArgs& a, int r, double x, double y, int prov = -1) {
   int v = pnew(a.R, x, y);
   if (v < 0) return -1;
+  if (a.R.src) a.R.src[v] = prov;
   int root = a.rroot[r];
   if (root < 0) {
     a.rroot[r] = v;
@@ -105,7 +111,8 @@ __device__ int rcopy(SerialArgs& a, const Pool& p, int root) {
   if (r < 0) return -1;
   int v = root;
   do {
-    if (radd(a, r, p.x[v], p.y[v])) return -1;
+    const int prov = (p.src && p.src[v] >= 0) ? (((&p == &a.Q) ? 1 : 0) << 30) | p.src[v] : -1;
+    if (radd(a, r, p.x[v], p.y[v], prov)) return -1;
     v = p.next[v];
   } while (v != root);
   return 0;
@@ -358,6 +365,8 @@ __device__ int ser_label_trace(SerialArgs& a) {
       int VP = pnew(P, P.x[IP], P.y[IP]);
       int VQ = pnew(Q, Q.x[IQ], Q.y[IQ]);
       if (VP < 0 || VQ < 0) return 3;
+      if (P.src) P.src[VP] = P.src[IP];
+      if (Q.src) Q.src[VQ] = Q.src[IQ];
       double sP = area3(P.x[P.prev[IP]], P.y[P.prev[IP]], P.x[IP], P.y[IP], P.x[P.next[IP]],
                         P.y[P.next[IP]]);
       double sQ = area3(Q.x[Q.prev[IQ]], Q.y[Q.prev[IQ]], Q.x[IQ], Q.y[IQ], Q.x[Q.next[IQ]],
@@ -403,7 +412,8 @@ __device__ int ser_label_trace(SerialArgs& a) {
             pv = &side(a, sV);
             V = (status == EX_EXIT) ? pv->next[V] : pv->prev[V];
             pv->isect[V] = 0;
-            if (radd(a, r, pv->x[V], pv->y[V])) return 2;
+            const int prov = (pv->src && pv->src[V] >= 0) ? (sV << 30) | pv->src[V] : -1;
+            if (radd(a, r, pv->x[V], pv->y[V], prov)) return 2;
             if (--guard < 0) return 2;
           } while (!(pv->enex[V] == status) && !(sV == sI && V == I));
           if (!(sV == sI && V == I)) {
