@@ -179,6 +179,39 @@ int sbc_area_backward(sbc_ctx* ctx, const sbc_batch* batch, const double* grad_a
 int sbc_area_backward_device(sbc_ctx* ctx, const sbc_batch* batch, const double* grad_area,
                              double* grad_b, double* grad_c, void* stream);
 
+/* ---- One base against many overlays, pairwise ---------------------------
+ * The rings of `seg base overlay_i` for every overlay i (each equal to
+ * sbc_clip_pair(base, overlay_i)); the reference has no such call and is run
+ * once per overlay for it (multicore_clipping, src/clip.cpp:1415-2115, with
+ * one overlay).  Unlike sbc_clip_one_to_many, whose results follow the
+ * reference's single tree over all overlays (at most 9), every overlay here
+ * gets the result of its own pair, for any number of overlays.  The base is
+ * prepared once; overlay i is vertices [c_off[i], c_off[i+1]) of c_xy.  An
+ * overlay with fewer than 3 vertices gets status SBC_EINPUT and no rings;
+ * SBC_EUNDEF marks a pair on which the reference's behaviour is undefined.
+ * Output as for sbc_clip_batch (npairs = noverlays): host arrays owned by the
+ * context for sbc_clip_pairwise, device arrays for _device. */
+typedef struct sbc_pairwise_job {
+  const double* b_xy;         /* 2*nb */
+  int nb;
+  int noverlays;
+  const double* c_xy;
+  const long long* c_off;     /* noverlays+1 */
+} sbc_pairwise_job;
+int sbc_clip_pairwise(sbc_ctx* ctx, const sbc_pairwise_job* job, sbc_batch_rings* out,
+                      void* stream);
+int sbc_clip_pairwise_device(sbc_ctx* ctx, const sbc_pairwise_job* job, sbc_batch_rings* out,
+                             void* stream);
+/* Diagnostics of the last sbc_clip_pairwise call: out[0] overlays clipped by
+ * the single-pair pipeline (inputs outside the batched path's conditions),
+ * out[1] unique intersecting edge pairs, out[2] box-overlapping edge pairs
+ * tested, out[3] cells of the base grid. */
+int sbc_pairwise_info(const sbc_ctx* ctx, long long* out, int n);
+/* Base-grid cell width of sbc_clip_pairwise in units of
+ * sqrt(base bounding-box area / nb); default 1.  A tuning knob: results do not
+ * depend on it. */
+int sbc_pairwise_set_cell_factor(sbc_ctx* ctx, double factor);
+
 /* Allocation-free ring tracing.  No counterpart in the reference: it exists
  * for callers that are not allowed to allocate device memory themselves or
  * through this library -- for example an engine that owns every byte of the

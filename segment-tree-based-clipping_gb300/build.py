@@ -23,7 +23,7 @@ CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libsbclip.so"
 CLI = OUT / "seg"
-SOURCES = ["sbc_prims.cu", "sbc_front.cu", "sbc_cand.cu", "sbc_mid.cu", "sbc_back.cu", "sbc_batch.cu", "sbc_api.cu"]
+SOURCES = ["sbc_prims.cu", "sbc_front.cu", "sbc_cand.cu", "sbc_mid.cu", "sbc_back.cu", "sbc_batch.cu", "sbc_pairwise.cu", "sbc_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -70,6 +70,7 @@ struct sbc_ctx {
   size_t d_in_cap = 0;
   long long stats[SBC_STAT_NUM] = {0};
   sbc::BatchRunner* br = nullptr;
+  sbc::PairwiseRunner* pw = nullptr;
   // host copies of batched ring results
   std::vector<long long> hb_pair_ring, hb_ring_off;
   std::vector<double> hb_xy;
@@ -161,6 +162,7 @@ int sbc_create(const sbc_options* opt, sbc_ctx** out) {
   }
   c->pl = new Pipeline(c->device, c->own);
   c->br = new sbc::BatchRunner(*c->pl);
+  c->pw = new sbc::PairwiseRunner(*c->pl);
   *out = c;
   return SBC_OK;
 }
@@ -170,6 +172,7 @@ void sbc_destroy(sbc_ctx* c) {
   cudaSetDevice(c->device);
   if (c->own) cudaStreamSynchronize(c->own);
   delete c->br;
+  delete c->pw;
   delete c->pl;
   for (auto p : c->h_off)
     if (p) cudaFreeHost(p);
@@ -603,5 +606,106 @@ extern "C" int sbc_clip_batch(sbc_ctx* c, const sbc_batch* b, sbc_batch_rings* o
   out->ring_off = c->hb_ring_off.data();
   out->xy = c->hb_xy.data();
   out->status = c->hb_status.data();
+  return SBC_OK;
+}
+
+// ------------------------------------------------------------------ pairwise
+namespace {
+
+int pairwise_check(sbc_ctx* c, const sbc_pairwise_job* j) {
+  if (!c) return SBC_EINPUT;
+  if (!j) return set_err(c, SBC_EINPUT, "null job");
+  if (j->nb < 3) return set_err(c, SBC_EINPUT, "base needs at least 3 vertices");
+  if (j->noverlays < 0) return set_err(c, SBC_EINPUT, "negative overlay count");
+  if (!j->b_xy || (j->noverlays > 0 && (!j->c_xy || !j->c_off)))
+    return set_err(c, SBC_EINPUT, "null array");
+  return SBC_OK;
+}
+
+}  // namespace
+
+extern "C" int sbc_clip_pairwise_device(sbc_ctx* c, const sbc_pairwise_job* j,
+                                        sbc_batch_rings* out, void* stream) {
+  int rc = pairwise_check(c, j);
+  if (rc) return rc;
+  if (!out) return set_err(c, SBC_EINPUT, "null output");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  c->pl->set_stream(st);
+  c->pl->clear_error();
+  rc = c->pw->run(j->b_xy, j->nb, j->noverlays, j->c_xy, j->c_off, st);
+  if (rc) return set_err(c, rc, c->pl->error());
+  out->npairs = j->noverlays;
+  out->nrings = c->pw->total_rings;
+  out->nverts = c->pw->total_verts;
+  out->pair_ring = c->pw->pair_ring;
+  out->ring_off = c->pw->ring_off;
+  out->xy = c->pw->xy;
+  out->status = c->pw->status;
+  return SBC_OK;
+}
+
+extern "C" int sbc_clip_pairwise(sbc_ctx* c, const sbc_pairwise_job* j, sbc_batch_rings* out,
+                                 void* stream) {
+  int rc = pairwise_check(c, j);
+  if (rc) return rc;
+  if (!out) return set_err(c, SBC_EINPUT, "null output");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  const int nov = j->noverlays;
+  if (nov > 0 && j->c_off[0] != 0) return set_err(c, SBC_EINPUT, "c_off[0] must be 0");
+  for (int i = 0; i < nov; ++i)
+    if (j->c_off[i + 1] < j->c_off[i]) return set_err(c, SBC_EINPUT, "c_off must not decrease");
+  const long long ncv = nov > 0 ? j->c_off[nov] : 0;
+  sbc::BufferPool& bp = c->pl->pool();
+  auto* db = (double*)bp.get("hpw_b", sizeof(double) * 2 * j->nb);
+  auto* dc = (double*)bp.get("hpw_c", sizeof(double) * 2 * (ncv + 1));
+  auto* dco = (long long*)bp.get("hpw_coff", sizeof(long long) * (nov + 1));
+  if (bp.failed) return set_err(c, SBC_ENOMEM, "device allocation failed (pairwise input)");
+  // straight from the caller's buffers (pageable copies run at pinned speed on Grace)
+  cudaMemcpyAsync(db, j->b_xy, sizeof(double) * 2 * j->nb, cudaMemcpyHostToDevice, st);
+  if (ncv > 0) cudaMemcpyAsync(dc, j->c_xy, sizeof(double) * 2 * ncv, cudaMemcpyHostToDevice, st);
+  if (nov > 0)
+    cudaMemcpyAsync(dco, j->c_off, sizeof(long long) * (nov + 1), cudaMemcpyHostToDevice, st);
+  sbc_pairwise_job d{db, j->nb, nov, dc, dco};
+  sbc_batch_rings dr;
+  rc = sbc_clip_pairwise_device(c, &d, &dr, st);
+  if (rc) return rc;
+  c->hb_ring_off.assign((size_t)dr.nrings + 1, 0);
+  c->hb_xy.assign((size_t)2 * dr.nverts + 1, 0.0);
+  c->hb_pair_ring = c->pw->h_pair_ring;
+  c->hb_status = c->pw->h_status;
+  c->hb_pair_ring.resize((size_t)nov + 1, 0);
+  c->hb_status.resize((size_t)nov + 1, 0);
+  if (nov > 0) {
+    cudaMemcpyAsync(c->hb_ring_off.data(), dr.ring_off, sizeof(long long) * (dr.nrings + 1),
+                    cudaMemcpyDeviceToHost, st);
+    if (dr.nverts > 0)
+      cudaMemcpyAsync(c->hb_xy.data(), dr.xy, sizeof(double) * 2 * dr.nverts,
+                      cudaMemcpyDeviceToHost, st);
+  }
+  rc = cuda_check(c, cudaStreamSynchronize(st), "pairwise rings");
+  if (rc) return rc;
+  out->npairs = nov;
+  out->nrings = dr.nrings;
+  out->nverts = dr.nverts;
+  out->pair_ring = c->hb_pair_ring.data();
+  out->ring_off = c->hb_ring_off.data();
+  out->xy = c->hb_xy.data();
+  out->status = c->hb_status.data();
+  return SBC_OK;
+}
+
+extern "C" int sbc_pairwise_info(const sbc_ctx* c, long long* out, int n) {
+  if (!c || !out) return SBC_EINPUT;
+  const long long v[4] = {c->pw->fallback_pairs, c->pw->hits, c->pw->tested, c->pw->grid_cells};
+  for (int i = 0; i < n && i < 4; ++i) out[i] = v[i];
+  return SBC_OK;
+}
+
+extern "C" int sbc_pairwise_set_cell_factor(sbc_ctx* c, double f) {
+  if (!c) return SBC_EINPUT;
+  if (!(f > 0.0) || f > 1e6) return set_err(c, SBC_EINPUT, "cell factor must be positive");
+  c->pw->cell_factor = f;
   return SBC_OK;
 }

@@ -24,6 +24,7 @@
 
 #include "../../include/sbclip.h"
 #include "sbc_pipeline.cuh"
+#include "sbc_pairops.cuh"
 #include "sbc_serial.cuh"
 
 namespace sbc {
@@ -33,24 +34,6 @@ namespace {
 constexpr int kBatchBlock = 128;
 
 // ------------------------------------------------------------------ arena
-struct Carver {
-  unsigned char* base;
-  size_t off;
-  template <class T>
-  __host__ __device__ T* take(long long n) {
-    off = (off + 15) & ~(size_t)15;
-    T* r = (T*)(base + off);
-    off += sizeof(T) * (size_t)(n > 0 ? n : 0);
-    return r;
-  }
-};
-
-__host__ __device__ __forceinline__ int npow2_dev(int n) {
-  int p = 1;
-  while (p < n) p <<= 1;
-  return p;
-}
-
 // capacities of one pair
 struct Caps {
   int nb, nc, E, K;        // K = capacity for unique hits
@@ -197,38 +180,6 @@ __host__ __device__ __forceinline__ int hit_cap(int nb, int nc, int pass) {
   return (int)(k > 0 ? k : 1);
 }
 
-// ------------------------------------------------------------------ small helpers
-__device__ __forceinline__ double bvx(const double* p, int n, int i) { return p[2 * (i % n)]; }
-__device__ __forceinline__ double bvy(const double* p, int n, int i) { return p[2 * (i % n) + 1]; }
-
-__device__ __forceinline__ bool lsmf_d(double p1x, double p1y, double p2x, double p2y, double q1x,
-                                       double q1y, double q2x, double q2y) {
-  double minPX = p1x, minPY = p1y, maxPX = p2x, maxPY = p2y;
-  double minQX = q1x, minQY = q1y, maxQX = q2x, maxQY = q2y;
-  if (minPX > p2x) { minPX = p2x; maxPX = p1x; }
-  if (minPY > p2y) { minPY = p2y; maxPY = p1y; }
-  if (minQX > q2x) { minQX = q2x; maxQX = q1x; }
-  if (minQY > q2y) { minQY = q2y; maxQY = q1y; }
-  if (minPX > maxQX || maxPX < minQX) return false;
-  if (minPY > maxQY || maxPY < minQY) return false;
-  return true;
-}
-
-// stable bottom-up merge sort of idx[0..n) by less(a, b)
-template <class Less>
-__device__ void merge_sort(int* idx, int* tmp, int n, Less less) {
-  for (int w = 1; w < n; w <<= 1) {
-    for (int lo = 0; lo < n; lo += 2 * w) {
-      const int mid = min(lo + w, n), hi = min(lo + 2 * w, n);
-      int i = lo, j = mid, o = lo;
-      while (i < mid && j < hi) tmp[o++] = less(idx[j], idx[i]) ? idx[j++] : idx[i++];
-      while (i < mid) tmp[o++] = idx[i++];
-      while (j < hi) tmp[o++] = idx[j++];
-    }
-    for (int i = 0; i < n; ++i) idx[i] = tmp[i];
-  }
-}
-
 // findBoarder over S(m) (oacc_segment_tree.cpp:420-460) with the zero
 // border slot at z (the same emulation as the pair pipeline)
 struct BordersS {
@@ -265,69 +216,11 @@ __device__ int find_border_s(const BordersS& B, double q) {
   return h;
 }
 
-__device__ __forceinline__ bool canonical_s(int v, int logL, int l, int r1) {
-  const int L = 1 << logL;
-  const int d = 31 - __clz(v), h = logL - d;
-  const int lo = (v << h) - L, hi = ((v + 1) << h) - L;
-  if (lo < l || hi > r1) return false;
-  if (v == 1) return true;
-  const int p = v >> 1;
-  const int plo = (p << (h + 1)) - L, phi = ((p + 1) << (h + 1)) - L;
-  return !(plo >= l && phi <= r1);
-}
-
-__device__ __forceinline__ bool below_s(int x, int v, int logL) {
-  if (x < 0) return false;
-  const int h = logL - (31 - __clz(v));
-  return (x >> h) == v;
-}
-
-// emission count and first key of base edge b with overlay edge c (edge
-// indices of the pair; cId = the overlay edge's id)
+// emission of base edge b with overlay edge c of this pair (edge indices)
 __device__ unsigned emission_s(int b, int c, int cId, const PairWork& w, int logL,
                                unsigned long long* key) {
-  const int L = 1 << logL;
-  const int2 rb = w.lr[b], rc = w.lr[c];
-  const int eb0 = w.aft[b], eb1 = w.bef[b], ec0 = w.aft[c], ec1 = w.bef[c];
-  unsigned n = 0;
-  unsigned long long best = ~0ull;
-  for (int a = rb.x + L, z = rb.y + L; a < z; a >>= 1, z >>= 1) {
-    for (int side = 0; side < 2; ++side) {
-      int v = -1;
-      if (side == 0 && (a & 1)) v = a++;
-      if (side == 1 && (z & 1)) v = --z;
-      if (v < 0) continue;
-      if (canonical_s(v, logL, rc.x, rc.y)) {
-        n += 2;
-        best = min(best, ((unsigned long long)v << 33) | (unsigned)cId);
-      }
-      if (below_s(ec0, v, logL) || below_s(ec1, v, logL)) {
-        n += 1;
-        best = min(best, ((unsigned long long)v << 33) | (1ull << 31) | (unsigned)cId);
-      }
-    }
-  }
-  for (int a = rc.x + L, z = rc.y + L; a < z; a >>= 1, z >>= 1) {
-    for (int side = 0; side < 2; ++side) {
-      int v = -1;
-      if (side == 0 && (a & 1)) v = a++;
-      if (side == 1 && (z & 1)) v = --z;
-      if (v < 0) continue;
-      if (below_s(eb0, v, logL) || below_s(eb1, v, logL)) {
-        n += 1;
-        best = min(best, ((unsigned long long)v << 33) | (1ull << 32) | (unsigned)c);
-      }
-    }
-  }
-  *key = best;
-  return n;
+  return emission_q(w.lr[b], w.lr[c], w.aft[b], w.bef[b], w.aft[c], w.bef[c], c, cId, logL, key);
 }
-
-__device__ __forceinline__ bool nd_b(int t) { return t == 1 || t == 3 || t == 5 || t == 7; }
-__device__ __forceinline__ bool nd_c(int t) { return t == 1 || t == 2 || t == 6; }
-
-// status codes of one pair
-enum { PS_OK = 0, PS_UNDEF = 2, PS_CAP = 3 };
 
 struct PairResult {
   int status;

@@ -1,0 +1,1603 @@
+// sbc_pairwise.cu -- one base polygon against many overlays, pairwise.
+//
+// The result for overlay i is the reference's `seg base overlay_i` (the same
+// rings as sbc_clip_pair on that pair).  Every pair would build its own
+// segment tree over the base's edges and the overlay's; here no pair builds
+// one.  The base is prepared once: its sorted distinct x values, the rank of
+// each vertex among them, and a uniform grid over its edge boxes.  A pair's
+// tree quantities then follow from ranks alone:
+//
+//  * With no vertical edge (equal x at both ends) in either polygon and no x
+//    value shared between them, the elementary points of the pair
+//    (constructElementaryIntervalsArrayMulticore, oacc_segment_tree.cpp:
+//    4513-4692) are the distinct x values of both polygons in order, without
+//    the largest, padded with the second largest up to 2^k + 1 entries.
+//    Position t of a value is its rank among the base's values plus its rank
+//    among the overlay's.
+//  * findBoarder (:420-460) runs over those positions with the zero border
+//    slot at z (preparePointsToNodeMapMulticore, :1970-2008): its comparisons
+//    become integer comparisons of positions, so its search path, including
+//    the misses the zero slot causes, is followed exactly.
+//  * The end-list leaves and the covered leaf range of an edge
+//    (insertToLeafLevelEdgeListMulticore :2010-2113, insertEdgeParallel
+//    :2496-2564) and the emission rule of the candidate loops (:6010-6244)
+//    follow from those positions as in the pair pipeline.
+//
+// A pair that breaks one of these conditions, or whose arrays take a path
+// the sparse back end does not follow (see below), is clipped by the pair
+// pipeline instead, so every pair's result is the pair pipeline's.
+//
+// Candidates: one thread per overlay edge visits the base grid cells its box
+// covers; a base edge is tested in the cell holding the low corner of the two
+// boxes' overlap only, so every box-overlapping pair is tested once.
+//
+// Back end: one thread per pair runs rows A9-A18 (src/clip.cpp:368-695,
+// foster/polyclip.h:337-787) with the overlay's merged arrays in full and the
+// base's only where intersections are: the base's merged list holds ~n_b
+// plain vertices per pair, so its linked list is built with run nodes (a
+// stretch of plain vertices as one node, sbc_serial.cuh) and pointInPoly
+// against it adds the winding steps of the run-internal base edges from one
+// row of the grid.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/sbclip.h"
+#include "sbc_pipeline.cuh"
+#include "sbc_pairops.cuh"
+#include "sbc_serial.cuh"
+
+namespace sbc {
+
+namespace {
+
+constexpr int kPwMaxOverlay = 16384;  // larger overlays go to the pair pipeline
+constexpr int kPwMaxCells = 1 << 14;  // an overlay edge box over more cells: pair pipeline
+constexpr int kPwLongCells = 64;      // base edges over more cells per axis skip the grid
+constexpr int kPwPrepThreads = 256;
+constexpr int kPwPairBlock = 64;
+
+enum { PW_FAST = 0, PW_FALLBACK = 1, PW_INPUT = 2 };
+enum { PS_FALLBACK = 4 };
+
+// base statistics (device)
+struct PwBaseStats {
+  unsigned long long mnx, mxx, mny, mxy;  // dkey of min/max x and y
+  double ext;                             // sum of max(|dx|, |dy|) over edges
+  unsigned flags;                         // 1: non-finite, 2: vertical edge
+};
+
+struct PwGrid {
+  float x0, y0, inv;
+  int gx, gy;
+};
+
+__device__ __forceinline__ int pw_cellx(const PwGrid& g, float x) {
+  const float t = floorf(__fmul_rn(__fsub_rn(x, g.x0), g.inv));
+  return t < 0.f ? 0 : (t >= (float)g.gx ? g.gx - 1 : (int)t);
+}
+__device__ __forceinline__ int pw_celly(const PwGrid& g, float y) {
+  const float t = floorf(__fmul_rn(__fsub_rn(y, g.y0), g.inv));
+  return t < 0.f ? 0 : (t >= (float)g.gy ? g.gy - 1 : (int)t);
+}
+
+// per overlay: how it is clipped and its tree parameters
+struct PwPair {
+  int mode;   // PW_FAST / PW_FALLBACK / PW_INPUT
+  int nuc;    // distinct overlay x values
+  int count;  // elementary points before padding
+  int epc;    // 2^k + 1
+  int logL;
+  int z;      // zero border slot
+};
+
+struct PwHit {
+  int pair, b, j, type;
+  unsigned long long key;
+};
+
+__device__ __forceinline__ int lower_bound_d(const double* a, int n, double x) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int m = (lo + hi) >> 1;
+    if (a[m] < x) lo = m + 1;
+    else hi = m;
+  }
+  return lo;
+}
+
+// ------------------------------------------------------------------ tree by rank
+struct PwTree {
+  int count, epc, z, L, logL;
+};
+
+// positions [lo, hi) of the elementary entries equal to the value of
+// combined rank r (entries before lo are smaller)
+__device__ __forceinline__ void pw_lohi(const PwTree& T, int r, int* lo, int* hi) {
+  if (r < T.count - 1) {
+    *lo = r;
+    *hi = r + 1;
+  } else if (r == T.count - 1) {
+    *lo = r;
+    *hi = T.epc;
+  } else {
+    *lo = *hi = T.epc;
+  }
+}
+
+// S(m) against q: -1 smaller, 0 equal, 1 greater, 2 past the arrays (NaN)
+__device__ __forceinline__ int pw_scmp(const PwTree& T, int m, int lo, int hi, double q) {
+  if (m < 0 || m >= T.epc) return 2;
+  if (m == T.z) return (0.0 == q) ? 0 : (0.0 < q ? -1 : 1);
+  const int t = m < T.z ? m + 1 : m;
+  return t < lo ? -1 : (t < hi ? 0 : 1);
+}
+
+// findBoarder (oacc_segment_tree.cpp:420-460) on positions
+__device__ int pw_find_border(const PwTree& T, int lo, int hi, double q) {
+  int l = 0, h = T.epc;
+  while (l < h) {
+    const int m = l + (h - l) / 2;
+    const int c = pw_scmp(T, m, lo, hi, q);
+    if (c == 0) {
+      if (pw_scmp(T, m - 1, lo, hi, q) != 0) {
+        h = m;
+        l = h;
+      } else {
+        h = m - 1;
+      }
+    } else if (c == -1) {
+      l = m + 1;
+    } else {
+      h = m - 1;
+    }
+  }
+  return pw_scmp(T, h, lo, hi, q) == 0 ? h : -1;
+}
+
+// end-list leaves and covered leaf range of an edge whose start (smaller x)
+// s has combined rank rs and whose end e has rank re
+__device__ void pw_edge_tree(const PwTree& T, int rs, double s, int re, double e, int* aft,
+                             int* bef, int2* lr) {
+  const int L = T.L, epc = T.epc;
+  auto J = [&](int m) { return m < T.z ? m : (m == T.z ? epc - 1 : m - 1); };
+  auto eqnext = [&](int i) { return i >= T.count - 1; };  // ea[i] == ea[i+1]
+  int lo, hi;
+  pw_lohi(T, re, &lo, &hi);
+  const int hiE = hi;
+  int a = -1, b = -1;
+  const int en = pw_find_border(T, lo, hi, e);
+  if (en >= 0) {
+    const int j = J(en);
+    int node = 0;
+    if (j <= epc - 2) {
+      const int i = j + 1;
+      node = L + i;
+      if (i != 1 && i + 1 < epc && eqnext(i)) node = L + i + 1;
+    }
+    if (node >= L && node < 2 * L && !eqnext(node - L)) a = node;
+  }
+  pw_lohi(T, rs, &lo, &hi);
+  const int st = pw_find_border(T, lo, hi, s);
+  if (st >= 0) {
+    const int j = J(st);
+    int node = 0;
+    if (j <= epc - 2) node = L + j;
+    if (node >= L && node < 2 * L && !eqnext(node - L)) b = node;
+  }
+  *aft = a;
+  *bef = b;
+  const int l = lo < L ? lo : L;
+  int r1 = hiE - 1;
+  r1 = r1 < 0 ? 0 : (r1 > L ? L : r1);
+  *lr = make_int2(l, r1 > l ? r1 : l);
+}
+
+// ------------------------------------------------------------------ base preparation
+__global__ void k_pw_base_edges(int nb, const double* __restrict__ b,
+                                unsigned long long* __restrict__ keys, unsigned* __restrict__ vals,
+                                float4* __restrict__ fbox, PwBaseStats* st) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nb) return;
+  const int w = v + 1 == nb ? 0 : v + 1;
+  const double x0 = b[2 * v], y0 = b[2 * v + 1], x1 = b[2 * w], y1 = b[2 * w + 1];
+  keys[v] = dkey(x0);
+  vals[v] = v;
+  fbox[v] = make_float4(__double2float_rd(fmin(x0, x1)), __double2float_rd(fmin(y0, y1)),
+                        __double2float_ru(fmax(x0, x1)), __double2float_ru(fmax(y0, y1)));
+  unsigned f = 0;
+  if (!isfinite(x0) || !isfinite(y0)) f |= 1u;
+  if (x0 == x1) f |= 2u;
+  if (f) atomicOr(&st->flags, f);
+  atomicMin(&st->mnx, dkey(x0));
+  atomicMax(&st->mxx, dkey(x0));
+  atomicMin(&st->mny, dkey(y0));
+  atomicMax(&st->mxy, dkey(y0));
+  atomicAdd(&st->ext, fmax(fabs(x1 - x0), fabs(y1 - y0)));
+}
+
+__global__ void k_pw_uflag(int n, const unsigned long long* __restrict__ keys, int* __restrict__ flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  flag[i] = (i < n && (i == 0 || keys[i] != keys[i - 1])) ? 1 : 0;
+}
+
+// after the exclusive scan of the flags: distinct values and vertex ranks
+__global__ void k_pw_uscatter(int n, const unsigned long long* __restrict__ keys,
+                              const unsigned* __restrict__ vals, const int* __restrict__ pre,
+                              const double* __restrict__ b, double* __restrict__ ub,
+                              int* __restrict__ rank) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const bool first = i == 0 || keys[i] != keys[i - 1];
+  const int u = pre[i] + (first ? 0 : -1);
+  const int v = (int)vals[i];
+  if (first) ub[u] = b[2 * v];
+  rank[v] = u;
+}
+
+__global__ void k_pw_grid_count(int nb, const float4* __restrict__ fbox, PwGrid g,
+                                int* __restrict__ cnt, int* __restrict__ lng,
+                                unsigned* __restrict__ nlong) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nb) return;
+  const float4 f = fbox[e];
+  const int cx0 = pw_cellx(g, f.x), cx1 = pw_cellx(g, f.z);
+  const int cy0 = pw_celly(g, f.y), cy1 = pw_celly(g, f.w);
+  if (cx1 - cx0 >= kPwLongCells || cy1 - cy0 >= kPwLongCells) {
+    lng[atomicAdd(nlong, 1u)] = e;
+    return;
+  }
+  for (int cy = cy0; cy <= cy1; ++cy)
+    for (int cx = cx0; cx <= cx1; ++cx) atomicAdd(&cnt[cy * g.gx + cx], 1);
+}
+
+__global__ void k_pw_grid_fill(int nb, const float4* __restrict__ fbox, PwGrid g,
+                               const int* __restrict__ start, int* __restrict__ cur,
+                               int* __restrict__ ent) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nb) return;
+  const float4 f = fbox[e];
+  const int cx0 = pw_cellx(g, f.x), cx1 = pw_cellx(g, f.z);
+  const int cy0 = pw_celly(g, f.y), cy1 = pw_celly(g, f.w);
+  if (cx1 - cx0 >= kPwLongCells || cy1 - cy0 >= kPwLongCells) return;
+  for (int cy = cy0; cy <= cy1; ++cy)
+    for (int cx = cx0; cx <= cx1; ++cx) {
+      const int c = cy * g.gx + cx;
+      ent[start[c] + atomicAdd(&cur[c], 1)] = e;
+    }
+}
+
+// ------------------------------------------------------------------ overlay preparation
+// One CTA per overlay of the size class (lo, hi]: sort its x values in shared
+// memory, rank them, check the conditions of the rank shortcut and work out
+// the pair's tree parameters.
+__global__ void __launch_bounds__(kPwPrepThreads)
+k_pw_overlay_prep(int nov, const long long* __restrict__ coff, const double* __restrict__ cxy,
+                  int lo_n, int hi_n, const double* __restrict__ ub, int nub, int base_flags,
+                  PwPair* __restrict__ pp, int* __restrict__ rankC, int* __restrict__ rankCB,
+                  double* __restrict__ uval) {
+  extern __shared__ unsigned long long sk[];
+  const int i = blockIdx.x;
+  if (i >= nov) return;
+  const long long o = coff[i];
+  const int n = (int)(coff[i + 1] - o);
+  if (n <= lo_n || n > hi_n) return;
+  const int tid = threadIdx.x;
+  int P2 = 1;
+  while (P2 < n) P2 <<= 1;
+  int* sidx = (int*)(sk + P2);
+  __shared__ int s_bad, s_cnt[kPwPrepThreads];
+  if (tid == 0) s_bad = 0;
+  const double* c = cxy + 2 * o;
+  for (int t = tid; t < P2; t += blockDim.x) {
+    if (t < n) {
+      const double x = c[2 * t];
+      sk[t] = dkey(x);
+      sidx[t] = t;
+      const double xn = c[2 * (t + 1 == n ? 0 : t + 1)];
+      if (!isfinite(x) || !isfinite(c[2 * t + 1]) || x == xn) atomicOr(&s_bad, 1);
+    } else {
+      sk[t] = ~0ull;
+      sidx[t] = -1;
+    }
+  }
+  __syncthreads();
+  for (int k = 2; k <= P2; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int t = tid; t < P2; t += blockDim.x) {
+        const int u = t ^ j;
+        if (u > t) {
+          const bool up = (t & k) == 0;
+          const unsigned long long a = sk[t], bk = sk[u];
+          if ((a > bk) == up) {
+            sk[t] = bk;
+            sk[u] = a;
+            const int ti = sidx[t];
+            sidx[t] = sidx[u];
+            sidx[u] = ti;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // distinct ranks: each thread a contiguous chunk
+  const int chunk = (n + blockDim.x - 1) / blockDim.x;
+  const int t0 = tid * chunk, t1 = min(n, t0 + chunk);
+  int local = 0;
+  for (int t = t0; t < t1; ++t) local += (t == 0 || sk[t] != sk[t - 1]) ? 1 : 0;
+  s_cnt[tid] = local;
+  __syncthreads();
+  if (tid == 0) {
+    int run = 0;
+    for (int t = 0; t < (int)blockDim.x; ++t) {
+      const int x = s_cnt[t];
+      s_cnt[t] = run;
+      run += x;
+    }
+    pp[i].nuc = run;
+  }
+  __syncthreads();
+  {
+    int u = s_cnt[tid] - 1;
+    for (int t = t0; t < t1; ++t) {
+      const bool first = t == 0 || sk[t] != sk[t - 1];
+      if (first) {
+        ++u;
+        uval[o + u] = c[2 * sidx[t]];
+      }
+      rankC[o + sidx[t]] = u;
+    }
+  }
+  // rank among the base's values; a shared x value breaks the shortcut
+  for (int t = tid; t < n; t += blockDim.x) {
+    const double x = c[2 * t];
+    const int r = lower_bound_d(ub, nub, x);
+    rankCB[o + t] = r;
+    if (r < nub && ub[r] == x) atomicOr(&s_bad, 2);
+  }
+  __syncthreads();
+  if (tid != 0) return;
+  PwPair q = pp[i];
+  q.mode = PW_FAST;
+  if (n < 3) {
+    q.mode = PW_INPUT;
+    pp[i] = q;
+    return;
+  }
+  if (s_bad || (base_flags & 3)) {
+    q.mode = PW_FALLBACK;
+    pp[i] = q;
+    return;
+  }
+  const int nuc = q.nuc;
+  const double* uc = uval + o;
+  const int count = nub + nuc - 1;
+  const double minI = fmin(ub[0], uc[0]), maxI = fmax(ub[nub - 1], uc[nuc - 1]);
+  const double absMin = fabs(minI);
+  const double dv = dadd(maxI, absMin);
+  bool ok = count >= 1 && dv < 2147483647.0;
+  int epc = 0, logL = 0, z = 0;
+  if (ok) {
+    epc = npow2_dev(count) + 1;
+    while ((1 << logL) < epc - 1) ++logL;
+    int digits = 1;
+    for (int iv = (int)trunc(dv); iv / 10 > 0; iv /= 10) ++digits;
+    double scale = 1.0;
+    for (int t = 0; t < 11 - digits; ++t) scale = dmul(scale, 10.0);
+    const bool shift = minI < 0;
+    auto key = [&](double v) -> long long {
+      return (long long)(shift ? dmul(scale, dadd(v, absMin)) : dmul(scale, v));
+    };
+    // the smallest elementary points in order: merge the two sorted sets
+    int ib = 0, ic = 0;
+    auto next_val = [&]() -> double {
+      if (ic >= nuc || (ib < nub && ub[ib] < uc[ic])) return ub[ib++];
+      return uc[ic++];
+    };
+    (void)next_val();  // ea[0]
+    for (int t = 1; t < epc && ok; ++t) {
+      const double v = t < count ? next_val() : (count >= 2 ? 0.0 : 0.0);
+      if (t >= count) {
+        ok = false;  // all points key to zero: leave it to the pair pipeline
+        break;
+      }
+      if (key(v) != 0) break;
+      if (++z > 64) ok = false;
+    }
+    // the last border (padding: the second largest distinct value) must key below 1e11
+    if (ok) {
+      int jb = nub - 1, jc = nuc - 1;
+      // drop the largest, then take the next
+      if (jc < 0 || (jb >= 0 && ub[jb] > uc[jc])) --jb;
+      else --jc;
+      const double v2 = (jc < 0 || (jb >= 0 && ub[jb] > uc[jc])) ? ub[jb] : uc[jc];
+      const long long k2 = key(v2);
+      if (k2 < 0 || k2 >= 100000000000LL) ok = false;
+    }
+  }
+  if (!ok) {
+    q.mode = PW_FALLBACK;
+  } else {
+    q.count = count;
+    q.epc = epc;
+    q.logL = logL;
+    q.z = z;
+  }
+  pp[i] = q;
+}
+
+// ------------------------------------------------------------------ candidates
+struct PwCandArgs {
+  int nov;
+  const long long* coff;
+  long long totalC;
+  const double* cxy;
+  const double* b;
+  int nb;
+  PwGrid g;
+  const int* gstart;
+  const int* gent;
+  const int* lng;
+  const unsigned* nlong;
+  const float4* fbox;
+  PwPair* pp;
+  const int* rankB;
+  const int* rankC;
+  const int* rankCB;
+  const double* uval;
+  PwHit* hits;
+  unsigned long long cap;
+  unsigned long long* nhits;
+  int* pairK;
+  unsigned long long* tested;  // box-overlapping pairs passing LSMF
+};
+
+__global__ void k_pw_candidates(PwCandArgs A) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= A.totalC) return;
+  int lo = 0, hi = A.nov;  // pair: last i with coff[i] <= t
+  while (hi - lo > 1) {
+    const int m = (lo + hi) >> 1;
+    if (A.coff[m] <= t) lo = m;
+    else hi = m;
+  }
+  const int i = lo;
+  const PwPair q = A.pp[i];
+  if (q.mode != PW_FAST) return;
+  const long long o = A.coff[i];
+  const int n = (int)(A.coff[i + 1] - o);
+  const int j = (int)(t - o), j2 = j + 1 == n ? 0 : j + 1;
+  const double* c = A.cxy + 2 * o;
+  const double q1x = c[2 * j], q1y = c[2 * j + 1], q2x = c[2 * j2], q2y = c[2 * j2 + 1];
+  const float4 fc = make_float4(__double2float_rd(fmin(q1x, q2x)), __double2float_rd(fmin(q1y, q2y)),
+                                __double2float_ru(fmax(q1x, q2x)), __double2float_ru(fmax(q1y, q2y)));
+  const int cx0 = pw_cellx(A.g, fc.x), cx1 = pw_cellx(A.g, fc.z);
+  const int cy0 = pw_celly(A.g, fc.y), cy1 = pw_celly(A.g, fc.w);
+  if ((long long)(cx1 - cx0 + 1) * (cy1 - cy0 + 1) > kPwMaxCells) {
+    atomicExch(&A.pp[i].mode, PW_FALLBACK);
+    return;
+  }
+  const PwTree T{q.count, q.epc, q.z, q.epc - 1, q.logL};
+  const int nb = A.nb;
+  const double* uc = A.uval + o;
+  bool haveC = false;
+  int aftC = -1, befC = -1;
+  int2 lrC = make_int2(0, 0);
+  unsigned long long tested = 0;
+  auto test = [&](int be) {
+    const int be2 = be + 1 == nb ? 0 : be + 1;
+    const double p1x = A.b[2 * be], p1y = A.b[2 * be + 1];
+    const double p2x = A.b[2 * be2], p2y = A.b[2 * be2 + 1];
+    if (!lsmf_d(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y)) return;
+    ++tested;
+    double al, bt;
+    const int ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
+    if (!ty) return;
+    if (!haveC) {
+      const int r1 = A.rankC[o + j] + A.rankCB[o + j], r2 = A.rankC[o + j2] + A.rankCB[o + j2];
+      if (q1x < q2x) pw_edge_tree(T, r1, q1x, r2, q2x, &aftC, &befC, &lrC);
+      else pw_edge_tree(T, r2, q2x, r1, q1x, &aftC, &befC, &lrC);
+      haveC = true;
+    }
+    const int r1 = A.rankB[be] + lower_bound_d(uc, q.nuc, p1x);
+    const int r2 = A.rankB[be2] + lower_bound_d(uc, q.nuc, p2x);
+    int aftB, befB;
+    int2 lrB;
+    if (p1x < p2x) pw_edge_tree(T, r1, p1x, r2, p2x, &aftB, &befB, &lrB);
+    else pw_edge_tree(T, r2, p2x, r1, p1x, &aftB, &befB, &lrB);
+    unsigned long long key;
+    if (emission_q(lrB, lrC, aftB, befB, aftC, befC, nb + j, 2 * j, T.logL, &key) == 0) return;
+    const unsigned long long h = atomicAdd(A.nhits, 1ull);
+    atomicAdd(&A.pairK[i], 1);
+    if (h < A.cap) A.hits[h] = PwHit{i, be, j, ty, key};
+  };
+  for (int cy = cy0; cy <= cy1; ++cy) {
+    for (int cx = cx0; cx <= cx1; ++cx) {
+      const int cell = cy * A.g.gx + cx;
+      const int e0 = A.gstart[cell], e1 = A.gstart[cell + 1];
+      for (int k = e0; k < e1; ++k) {
+        const int be = A.gent[k];
+        const float4 fb = A.fbox[be];
+        if (fb.x > fc.z || fb.z < fc.x || fb.y > fc.w || fb.w < fc.y) continue;
+        if (pw_cellx(A.g, fmaxf(fb.x, fc.x)) != cx || pw_celly(A.g, fmaxf(fb.y, fc.y)) != cy)
+          continue;
+        test(be);
+      }
+    }
+  }
+  const int nl = (int)*A.nlong;
+  for (int k = 0; k < nl; ++k) {
+    const int be = A.lng[k];
+    const float4 fb = A.fbox[be];
+    if (fb.x > fc.z || fb.z < fc.x || fb.y > fc.w || fb.w < fc.y) continue;
+    test(be);
+  }
+  if (tested) atomicAdd(A.tested, tested);
+}
+
+__global__ void k_pw_group(unsigned long long nh, const PwHit* __restrict__ hits,
+                           const int* __restrict__ hstart, int* __restrict__ cur,
+                           PwHit* __restrict__ out) {
+  const unsigned long long h = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= nh) return;
+  const PwHit x = hits[h];
+  out[hstart[x.pair] + atomicAdd(&cur[x.pair], 1)] = x;
+}
+
+// ------------------------------------------------------------------ one pair
+struct PwCaps {
+  int nc, K, nQmax, sp, capP, capQ, capR, rcap;
+};
+
+__host__ __device__ __forceinline__ PwCaps pw_caps(int nb, int nc, int K, int pass) {
+  PwCaps c;
+  c.nc = nc;
+  c.K = K;
+  c.nQmax = nc + K;
+  c.sp = 2 * K + 1;
+  c.capP = 7 * K + 16;
+  c.capQ = c.nQmax + 2 * K + 8;
+  c.capR = pass == 0 ? 2 * c.nQmax + 8 * K + 64 : nb + K + c.nQmax + 2 * (2 * K + 8) + 16;
+  c.rcap = 2 * K + 16;
+  return c;
+}
+
+struct PwWork {
+  int *hord, *htmp, *ub, *uc, *ut;
+  int *re_e, *re_s, *re_nd, *re_pre, *re_si;
+  int *cAll, *cND, *cfill, *csorted;
+  double* isxy;
+  int *aB, *aC, *sB, *sC, *bNI, *cNI;
+  double *spx, *spy;
+  int *spal, *spnb, *splab, *spnode;
+  double* ixC;
+  int *alC, *nbC, *labC, *cWin;
+  Pool P, Q, R;
+  int* runIds;
+  int* rroot;
+  int* counts;
+  unsigned char *splitP, *splitQ, *crossP, *crossQ;
+  int* roff;
+  double* rxy;
+};
+
+__host__ __device__ __forceinline__ void pw_pool(Carver& cv, int cap, Pool& p, bool runs) {
+  p.x = cv.take<double>(cap);
+  p.y = cv.take<double>(cap);
+  p.next = cv.take<int>(cap);
+  p.prev = cv.take<int>(cap);
+  p.nb = cv.take<int>(cap);
+  p.label = cv.take<int>(cap);
+  p.enex = cv.take<int>(cap);
+  p.source = cv.take<unsigned char>(cap);
+  p.isect = cv.take<unsigned char>(cap);
+  p.src = nullptr;
+  p.run = runs ? cv.take<int>(cap) : nullptr;
+  p.rv0 = runs ? cv.take<int>(cap) : nullptr;
+  p.rxy = nullptr;
+  p.n = 0;
+  p.cap = cap;
+}
+
+__host__ __device__ __forceinline__ PwWork pw_carve(Carver& cv, const PwCaps& c) {
+  PwWork w;
+  const int K = c.K;
+  w.hord = cv.take<int>(K);
+  w.htmp = cv.take<int>(K);
+  w.ub = cv.take<int>(K);
+  w.uc = cv.take<int>(K);
+  w.ut = cv.take<int>(K);
+  w.re_e = cv.take<int>(K + 1);
+  w.re_s = cv.take<int>(K + 1);
+  w.re_nd = cv.take<int>(K + 1);
+  w.re_pre = cv.take<int>(K + 1);
+  w.re_si = cv.take<int>(K + 1);
+  w.cAll = cv.take<int>(c.nc + 1);
+  w.cND = cv.take<int>(c.nc + 1);
+  w.cfill = cv.take<int>(c.nc + 1);
+  w.csorted = cv.take<int>(K);
+  w.isxy = cv.take<double>(2 * K);
+  w.aB = cv.take<int>(K);
+  w.aC = cv.take<int>(K);
+  w.sB = cv.take<int>(K);
+  w.sC = cv.take<int>(K);
+  w.bNI = cv.take<int>(K);
+  w.cNI = cv.take<int>(K);
+  w.spx = cv.take<double>(c.sp);
+  w.spy = cv.take<double>(c.sp);
+  w.spal = cv.take<int>(c.sp);
+  w.spnb = cv.take<int>(c.sp);
+  w.splab = cv.take<int>(c.sp);
+  w.spnode = cv.take<int>(c.sp);
+  w.ixC = cv.take<double>(2 * c.nQmax);
+  w.alC = cv.take<int>(c.nQmax);
+  w.nbC = cv.take<int>(c.nQmax);
+  w.labC = cv.take<int>(c.nQmax);
+  w.cWin = cv.take<int>(c.nQmax);
+  pw_pool(cv, c.capP, w.P, true);
+  pw_pool(cv, c.capQ, w.Q, false);
+  pw_pool(cv, c.capR, w.R, false);
+  w.runIds = cv.take<int>(c.capP);
+  w.rroot = cv.take<int>(c.rcap);
+  w.counts = cv.take<int>(4);
+  w.splitP = cv.take<unsigned char>(c.capP);
+  w.crossP = cv.take<unsigned char>(c.capP);
+  w.splitQ = cv.take<unsigned char>(c.capQ);
+  w.crossQ = cv.take<unsigned char>(c.capQ);
+  w.roff = cv.take<int>(c.rcap + 1);
+  w.rxy = cv.take<double>(2 * (long long)c.capR);
+  return w;
+}
+
+__host__ __device__ __forceinline__ size_t pw_arena_bytes(int nb, int nc, int K, int pass) {
+  Carver cv{nullptr, 0};
+  pw_carve(cv, pw_caps(nb, nc, K, pass));
+  return (cv.off + 255) & ~(size_t)255;
+}
+
+// pointInPoly against the base side of a pair whose list has run nodes: the
+// steps of the edges between nodes, plus those of the base edges inside run
+// nodes, which come from the grid row holding ry (each edge counted in the
+// first cell of its box in that row)
+struct PwPip {
+  const double* b;
+  int nb;
+  PwGrid g;
+  const int* gstart;
+  const int* gent;
+  const int* lng;
+  int nlong;
+  const float4* fbox;
+  const int* runIds;
+  int nruns;
+  __device__ bool internal(const Pool& P, int u) const {
+    int lo = 0, hi = nruns;  // runs with rv0 <= u
+    while (lo < hi) {
+      const int m = (lo + hi) >> 1;
+      if (P.rv0[runIds[m]] <= u) lo = m + 1;
+      else hi = m;
+    }
+    if (lo == 0) return false;
+    const int v = runIds[lo - 1];
+    return u + 1 <= P.rv0[v] + P.run[v];
+  }
+  __device__ int operator()(SerialArgs& a, int root, double rx, double ry) const {
+    const Pool& P = a.P;
+    int w = 0, v = root;
+    do {
+      const int nx = P.next[v];
+      w += pip_step(last_x(P, v), last_y(P, v), P.x[nx], P.y[nx], rx, ry);
+      v = nx;
+    } while (v != root);
+    const int cy = pw_celly(g, __double2float_rd(ry));
+    auto step = [&](int u) {
+      if (!internal(P, u)) return;
+      w += pip_step(b[2 * u], b[2 * u + 1], b[2 * u + 2], b[2 * u + 3], rx, ry);
+    };
+    for (int cx = 0; cx < g.gx; ++cx) {
+      const int cell = cy * g.gx + cx;
+      for (int k = gstart[cell]; k < gstart[cell + 1]; ++k) {
+        const int u = gent[k];
+        if (pw_cellx(g, fbox[u].x) != cx) continue;
+        step(u);
+      }
+    }
+    for (int k = 0; k < nlong; ++k) step(lng[k]);
+    return (w % 2) != 0;
+  }
+};
+
+struct PwPairArgs {
+  int nov;
+  const long long* coff;
+  const double* cxy;
+  const double* b;
+  int nb;
+  const PwPair* pp;
+  const int* hstart;
+  const PwHit* hits;
+  const int* pass_of;  // null: every fast pair, pass 0
+  unsigned char* arena;
+  const long long* aoff;
+  int* status;  // per pair: PS_* code
+  int* nrings;
+  int* nverts;
+  PwPip pip;
+};
+
+// global slot s of the base's merged list: its sparse index, or -1 for a
+// plain vertex slot (then *vtx is the vertex)
+__device__ __forceinline__ int pw_slot(const PwWork& w, int nr, int s, int* vtx) {
+  int lo = 0, hi = nr;
+  while (lo < hi) {
+    const int m = (lo + hi) >> 1;
+    if (w.re_e[m] + w.re_pre[m] <= s) lo = m + 1;
+    else hi = m;
+  }
+  const int r = lo - 1;
+  if (r >= 0) {
+    const int st = w.re_e[r] + w.re_pre[r];
+    if (s <= st + w.re_nd[r]) return w.re_si[r] + (s - st);
+    *vtx = s - (w.re_pre[r] + w.re_nd[r]);
+  } else {
+    *vtx = s;
+  }
+  return -1;
+}
+
+__device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork& w, int* nrings_out,
+                            int* nverts_out) {
+  const double* b = A.b;
+  const int nb = A.nb;
+  const long long o = A.coff[p];
+  const int nc = (int)(A.coff[p + 1] - o);
+  const double* c = A.cxy + 2 * o;
+  const PwHit* H = A.hits + A.hstart[p];
+  const int K = cp.K;
+  // ---- A9: records in the reference's order (base id, then first emission)
+  for (int i = 0; i < K; ++i) w.hord[i] = i;
+  merge_sort(w.hord, w.htmp, K, [&](int x, int y) {
+    return H[x].b != H[y].b ? H[x].b < H[y].b : H[x].key < H[y].key;
+  });
+  for (int i = 0; i < K; ++i) {
+    const PwHit& h = H[w.hord[i]];
+    w.ub[i] = 2 * h.b;
+    w.uc[i] = 2 * h.j;
+    w.ut[i] = h.type;
+  }
+  const int* ub = w.ub;
+  const int* uc = w.uc;
+  const int* ut = w.ut;
+  // ---- A10: base edges with records (runs), overlay counts
+  int nr = 0, knd = 0;
+  for (int i = 0; i < K; ++i) {
+    const int e = ub[i] >> 1;
+    if (i == 0 || e != (ub[i - 1] >> 1)) {
+      w.re_e[nr] = e;
+      w.re_s[nr] = i;
+      w.re_nd[nr] = 0;
+      ++nr;
+    }
+    if (nd_b(ut[i])) {
+      w.re_nd[nr - 1]++;
+      ++knd;
+    }
+  }
+  w.re_s[nr] = K;
+  {
+    int s = 0;
+    for (int r = 0; r < nr; ++r) {
+      w.re_pre[r] = s;
+      w.re_si[r] = r + s;
+      s += w.re_nd[r];
+    }
+    w.re_pre[nr] = s;
+    w.re_si[nr] = nr + s;
+  }
+  for (int i = 0; i <= nc; ++i) w.cAll[i] = w.cND[i] = w.cfill[i] = 0;
+  for (int i = 0; i < K; ++i) {
+    const int ec = uc[i] >> 1;
+    w.cAll[ec]++;
+    if (nd_c(ut[i])) w.cND[ec]++;
+  }
+  auto excl = [](int* a, int n) {
+    int s = 0;
+    for (int i = 0; i < n; ++i) {
+      const int x = a[i];
+      a[i] = s;
+      s += x;
+    }
+  };
+  excl(w.cAll, nc + 1);
+  excl(w.cND, nc + 1);
+  for (int i = 0; i < K; ++i) {
+    const int ec = uc[i] >> 1;
+    w.csorted[w.cAll[ec] + w.cfill[ec]++] = i;
+  }
+  const int nB = nb + knd, nQ = nc + w.cND[nc];
+  // ---- A11 records
+  for (int i = 0; i < K; ++i) {
+    const int bi = ub[i] >> 1, ci = uc[i] >> 1;
+    const int bi2 = bi + 1 == nb ? 0 : bi + 1, ci2 = ci + 1 == nc ? 0 : ci + 1;
+    const double p1x = b[2 * bi], p1y = b[2 * bi + 1], p2x = b[2 * bi2], p2y = b[2 * bi2 + 1];
+    const double q1x = c[2 * ci], q1y = c[2 * ci + 1], q2x = c[2 * ci2], q2y = c[2 * ci2 + 1];
+    double al = 0.0, bt = 0.0;
+    const int ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
+    double x = 0.0, y = 0.0;
+    if (ty == 1) {
+      const double oma = dsub(1.0, al);
+      x = dadd(dmul(oma, p1x), dmul(al, p2x));
+      y = dadd(dmul(oma, p1y), dmul(al, p2y));
+    } else if (ty == 3 || ty == 4 || ty == 5 || ty == 7 || ty == 8) {
+      x = q1x;
+      y = q1y;
+    } else if (ty == 2 || ty == 6) {
+      x = p1x;
+      y = p1y;
+    }
+    w.isxy[2 * i] = x;
+    w.isxy[2 * i + 1] = y;
+    w.aB[i] = ty ? alpha_to_int(al) : 0;
+    w.aC[i] = ty ? alpha_to_int(bt) : 0;
+  }
+  // ---- A12 per-edge alpha order (stable by alpha mod 1e9)
+  auto isort = [&](int s, int t, const int* alpha, const int* order, int* sorted) -> bool {
+    for (int i = s; i < t; ++i)
+      if (alpha[order ? order[i] : i] < 0) return false;
+    for (int i = s + 1; i < t; ++i) {
+      const int pv = sorted[i];
+      const int kp = alpha[order ? order[pv] : pv] % 1000000000;
+      int j = i;
+      while (j > s) {
+        const int qv = sorted[j - 1];
+        if (alpha[order ? order[qv] : qv] % 1000000000 <= kp) break;
+        sorted[j] = qv;
+        --j;
+      }
+      sorted[j] = pv;
+    }
+    return true;
+  };
+  for (int i = 0; i < K; ++i) w.sB[i] = w.sC[i] = i;
+  for (int r = 0; r < nr; ++r)
+    if (w.re_nd[r] > 1 && !isort(w.re_s[r], w.re_s[r + 1], w.aB, nullptr, w.sB)) return PS_FALLBACK;
+  for (int e = 0; e < nc; ++e)
+    if (w.cND[e + 1] - w.cND[e] > 1 && !isort(w.cAll[e], w.cAll[e + 1], w.aC, w.csorted, w.sC))
+      return PS_FALLBACK;
+  // ---- A13 merged arrays: the base's where it has records, the overlay's in full
+  for (int r = 0; r < nr; ++r) {
+    const int si = w.re_si[r], e = w.re_e[r];
+    w.spx[si] = b[2 * e];
+    w.spy[si] = b[2 * e + 1];
+    w.spal[si] = -100;
+    w.spnb[si] = -100;
+    for (int q = 1; q <= w.re_nd[r]; ++q) {
+      w.spx[si + q] = w.spy[si + q] = 0.0;
+      w.spal[si + q] = w.spnb[si + q] = 0;
+    }
+  }
+  for (int s = 0; s < w.re_si[nr]; ++s) {
+    w.splab[s] = 0;
+    w.spnode[s] = -1;
+  }
+  for (int i = 0; i < nQ; ++i) {
+    w.ixC[2 * i] = w.ixC[2 * i + 1] = 0.0;
+    w.alC[i] = w.nbC[i] = 0;
+  }
+  for (int id = 0; id < nc; ++id) {
+    const int s = id + w.cND[id];
+    w.ixC[2 * s] = c[2 * id];
+    w.ixC[2 * s + 1] = c[2 * id + 1];
+    w.alC[s] = -100;
+    w.nbC[s] = -100;
+  }
+  for (int i = 0; i < K; ++i) w.bNI[i] = w.cNI[i] = 0;
+  // base runs (copyIntersectionsParallel per edge)
+  for (int r = 0; r < nr; ++r) {
+    const int e = w.re_e[r], s = w.re_s[r], pre = w.re_pre[r], si = w.re_si[r];
+    int bid = s;
+    int lid = w.sB[bid];
+    const int t = ut[lid];
+    if (t == 2 || t == 4 || t == 6 || t == 8) {
+      w.spal[si] = w.aB[lid];
+      w.bNI[lid] = e + pre;
+      if (bid < K - 1) lid = w.sB[++bid];
+    }
+    if ((ub[lid] >> 1) != e) continue;
+    for (int q = 0; q < w.re_nd[r]; ++q) {
+      w.spx[si + 1 + q] = w.isxy[2 * lid];
+      w.spy[si + 1 + q] = w.isxy[2 * lid + 1];
+      w.spal[si + 1 + q] = w.aB[lid];
+      w.bNI[lid] = pre + e + 1 + q;
+      if (bid < K - 1) lid = w.sB[++bid];
+    }
+  }
+  // overlay edges
+  for (int e = 0; e < nc; ++e) {
+    const int s = w.cAll[e];
+    if (w.cAll[e + 1] == s) continue;
+    auto entry = [&](int pos) { return w.csorted[w.sC[pos]]; };
+    int bid = s;
+    int lid = entry(bid);
+    const int t = ut[lid];
+    if (t == 3 || t == 4 || t == 5 || t == 7 || t == 8) {
+      const int slot = e + w.cND[e];
+      w.alC[slot] = w.aC[lid];
+      w.cNI[lid] = slot;
+      if (bid < K - 1) lid = entry(++bid);
+    }
+    if ((uc[lid] >> 1) != e) continue;
+    const int ns = w.cND[e], ne = w.cND[e + 1];
+    for (int q = 0; q < ne - ns; ++q) {
+      const int slot = ns + e + 1 + q;
+      w.ixC[2 * slot] = w.isxy[2 * lid];
+      w.ixC[2 * slot + 1] = w.isxy[2 * lid + 1];
+      w.alC[slot] = w.aC[lid];
+      w.cNI[lid] = slot;
+      if (bid < K - 1) lid = entry(++bid);
+    }
+  }
+  // neighbours: the last record written to a slot wins
+  for (int i = 0; i < K; ++i) {
+    int vtx;
+    const int si = pw_slot(w, nr, w.bNI[i], &vtx);
+    if (si < 0) return PS_FALLBACK;  // a plain slot would change
+    w.spnb[si] = w.cNI[i] + 1;
+    w.nbC[w.cNI[i]] = w.bNI[i] + 1;
+  }
+  // slot contents of the base's merged list
+  auto info = [&](int s, double* x, double* y, int* al, int* nbv) {
+    int vtx = 0;
+    const int si = pw_slot(w, nr, s, &vtx);
+    if (si >= 0) {
+      *x = w.spx[si];
+      *y = w.spy[si];
+      *al = w.spal[si];
+      *nbv = w.spnb[si];
+    } else {
+      *x = b[2 * vtx];
+      *y = b[2 * vtx + 1];
+      *al = -100;
+      *nbv = -100;
+    }
+  };
+  // ---- A14 initial labels
+  for (int q = 0; q < nQ; ++q) w.cWin[q] = -1;
+  for (int r = 0; r < nr; ++r) {
+    for (int q = 0; q <= w.re_nd[r]; ++q) {
+      const int si = w.re_si[r] + q;
+      if (w.spal[si] == -100) continue;
+      const int i = w.re_e[r] + w.re_pre[r] + q;
+      const double cx = w.spx[si], cy = w.spy[si];
+      const int tm = (i - 1 == -1) ? nB - 1 : i - 1;
+      const int tp = (i + 1 == nB) ? 0 : i + 1;
+      double pmx, pmy, ppx, ppy;
+      int alm, nbm, alp, nbp;
+      info(tm, &pmx, &pmy, &alm, &nbm);
+      info(tp, &ppx, &ppy, &alp, &nbp);
+      const int pMN = alm != -100 ? nbm - 1 : -100;
+      const int pPN = alp != -100 ? nbp - 1 : -100;
+      const int nId = w.spnb[si] - 1;
+      int qt[2];
+      for (int sd = 0; sd < 2; ++sd) {
+        int qq = sd == 0 ? nId - 1 : nId + 1;
+        if (qq == nQ) qq = 0;
+        else if (qq == -1) qq = nQ - 1;
+        if (qq < 0 || qq >= nQ) return PS_FALLBACK;
+        const double qx = w.ixC[2 * qq], qy = w.ixC[2 * qq + 1];
+        int rr;
+        if (pMN != -100 && pMN == qq) rr = 2;
+        else if (pPN != -100 && pPN == qq) rr = 3;
+        else {
+          const double s1 = area3(qx, qy, pmx, pmy, cx, cy);
+          const double s2 = area3(qx, qy, cx, cy, ppx, ppy);
+          const double s3 = area3(pmx, pmy, cx, cy, ppx, ppy);
+          if (s3 > 0) rr = (s1 > 0 && s2 > 0) ? 0 : 1;
+          else rr = (s1 < 0 && s2 < 0) ? 1 : 0;
+        }
+        qt[sd] = rr;
+      }
+      const int qm = qt[0], qp = qt[1];
+      int lab;
+      if ((qm == 0 && qp == 1) || (qm == 1 && qp == 0)) lab = 1;
+      else if ((qm == 0 && qp == 0) || (qm == 1 && qp == 1)) lab = 2;
+      else if ((qp == 3 && qm == 1) || (qm == 3 && qp == 1)) lab = 3;
+      else if ((qp == 3 && qm == 0) || (qm == 3 && qp == 0)) lab = 4;
+      else if ((qp == 3 && qm == 2) || (qm == 3 && qp == 2)) lab = 5;
+      else if ((qm == 2 && qp == 1) || (qp == 2 && qm == 1)) lab = 6;
+      else if ((qm == 2 && qp == 0) || (qp == 2 && qm == 0)) lab = 7;
+      else lab = -102;
+      w.splab[si] = lab;
+      if (nId < 0 || nId >= nQ) return PS_FALLBACK;
+      w.cWin[nId] = max(w.cWin[nId], i);
+    }
+  }
+  for (int q = 0; q < nQ; ++q) {
+    w.labC[q] = 0;
+    if (w.cWin[q] >= 0) {
+      int vtx;
+      const int si = pw_slot(w, nr, w.cWin[q], &vtx);
+      if (si < 0) return PS_FALLBACK;
+      w.labC[q] = w.splab[si];
+    }
+  }
+  // ---- A15 linked lists (copyToLinkedList, src/clip.cpp:606-695): the base's
+  // with run nodes for its stretches of plain vertices
+  Pool& P = w.P;
+  Pool& Q = w.Q;
+  P.n = Q.n = w.R.n = 0;
+  P.rxy = b;
+  int nruns = 0, lastPlain = -1;
+  auto plain = [&](int v0, int len) -> int {
+    if (lastPlain >= 0 && lastPlain == P.n - 1 && P.rv0[lastPlain] + P.run[lastPlain] == v0 - 1) {
+      P.run[lastPlain] += len;
+      return 0;
+    }
+    const int v = pnew(P, b[2 * v0], b[2 * v0 + 1]);
+    if (v < 0) return PS_CAP;
+    P.source[v] = 1;
+    P.rv0[v] = v0;
+    P.run[v] = len - 1;
+    w.runIds[nruns++] = v;
+    lastPlain = v;
+    return 0;
+  };
+  {
+    int vn = 0, i = 0, r = 0;
+    for (int ii = 0; ii <= nb;) {
+      while (r < nr && w.re_e[r] < ii) ++r;
+      if (ii < nb) {
+        const int slot = ii + w.re_pre[r];
+        const bool hasRec = r < nr && w.re_e[r] == ii;
+        if (!hasRec && i == slot) {
+          const int stop = r < nr ? w.re_e[r] : nb;
+          const int st = plain(ii, stop - ii);
+          if (st) return st;
+          vn += stop - ii;
+          i += stop - ii;
+          ii = stop;
+          continue;
+        }
+      }
+      const int sv = ii < nb ? ii : 0;
+      const double vx = b[2 * sv], vy = b[2 * sv + 1];
+      for (;;) {
+        const int s = i % nB;
+        double sx, sy;
+        int sal, snb;
+        info(s, &sx, &sy, &sal, &snb);
+        if (sx == vx && sy == vy) break;
+        if (i >= nB) return PS_UNDEF;
+        int vtx;
+        const int si = pw_slot(w, nr, s, &vtx);
+        if (si < 0) return PS_FALLBACK;
+        const int v = pnew(P, sx, sy);
+        if (v < 0) return PS_CAP;
+        P.label[v] = w.splab[si];
+        P.isect[v] = 1;
+        w.spnode[si] = v;
+        lastPlain = -1;
+        ++vn;
+        ++i;
+      }
+      if (ii < nb) {
+        if (vn != i) return PS_UNDEF;
+        if (i != ii + w.re_pre[r]) return PS_FALLBACK;  // stopped at another slot
+        int vtx;
+        const int si = pw_slot(w, nr, i, &vtx);
+        if (si >= 0) {
+          const int v = pnew(P, vx, vy);
+          if (v < 0) return PS_CAP;
+          P.source[v] = 1;
+          P.label[v] = w.splab[si];
+          if (w.spal[si] != -100) P.isect[v] = 1;
+          w.spnode[si] = v;
+          lastPlain = -1;
+        } else {
+          const int st = plain(ii, 1);
+          if (st) return st;
+        }
+        ++vn;
+      }
+      ++i;
+      ++ii;
+    }
+    if (vn != nB) return PS_UNDEF;
+  }
+  for (int v = 0; v < P.n; ++v) {
+    P.next[v] = (v + 1) % P.n;
+    P.prev[v] = (v + P.n - 1) % P.n;
+  }
+  {
+    int i = 0;
+    for (int ii = 0; ii <= nc; ++ii) {
+      const int sv = ii < nc ? ii : 0;
+      const double vx = c[2 * sv], vy = c[2 * sv + 1];
+      while (w.ixC[(2 * i) % (2 * nQ)] != vx || w.ixC[(2 * i + 1) % (2 * nQ)] != vy) {
+        if (i >= nQ) return PS_UNDEF;
+        const int v = pnew(Q, w.ixC[2 * i], w.ixC[2 * i + 1]);
+        if (v < 0) return PS_CAP;
+        Q.label[v] = w.labC[i];
+        Q.isect[v] = 1;
+        const int t = w.nbC[i] - 1;
+        if (t < 0 || t >= nB) return PS_UNDEF;
+        int vtx;
+        const int si = pw_slot(w, nr, t, &vtx);
+        if (si < 0 || w.spnode[si] < 0) return PS_FALLBACK;
+        Q.nb[v] = w.spnode[si];
+        P.nb[w.spnode[si]] = v;
+        i++;
+      }
+      if (ii < nc) {
+        const int v = pnew(Q, vx, vy);
+        if (v != i) return PS_UNDEF;
+        Q.source[v] = 1;
+        Q.label[v] = w.labC[i];
+        if (w.nbC[i] != -100) {
+          const int t = w.nbC[i] - 1;
+          if (t < 0 || t >= nB) return PS_UNDEF;
+          int vtx;
+          const int si = pw_slot(w, nr, t, &vtx);
+          if (si < 0 || w.spnode[si] < 0) return PS_FALLBACK;
+          Q.isect[v] = 1;
+          Q.nb[v] = w.spnode[si];
+          P.nb[w.spnode[si]] = v;
+        }
+      }
+      i++;
+    }
+    if (Q.n != nQ) return PS_UNDEF;
+    for (int v = 0; v < nQ; ++v) {
+      Q.next[v] = (v + 1) % nQ;
+      Q.prev[v] = (v + nQ - 1) % nQ;
+    }
+  }
+  // ---- A16-A18
+  SerialArgs a;
+  a.P = P;
+  a.Q = Q;
+  a.R = w.R;
+  a.rroot = w.rroot;
+  a.rcap = cp.rcap;
+  a.nrings = &w.counts[0];
+  a.status = &w.counts[1];
+  a.splitP = w.splitP;
+  a.splitQ = w.splitQ;
+  a.crossP = w.crossP;
+  a.crossQ = w.crossQ;
+  for (int i = 0; i < cp.capP; ++i) w.splitP[i] = w.crossP[i] = 0;
+  for (int i = 0; i < cp.capQ; ++i) w.splitQ[i] = w.crossQ[i] = 0;
+  a.bSize = nb;
+  a.cSize = nc;
+  a.cStart = 0;
+  a.nB = nB;
+  a.nQ = nQ;
+  a.bP = b;
+  a.cP = c;
+  a.ixB = nullptr;
+  a.ixC = w.ixC;
+  a.alB = nullptr;
+  a.nbC = w.nbC;
+  a.labB = nullptr;
+  a.labC = w.labC;
+  *a.nrings = 0;
+  PwPip pip = A.pip;
+  pip.runIds = w.runIds;
+  pip.nruns = nruns;
+  int st = ser_label_trace_t(a, pip);
+  if (a.rfull) return PS_CAP;
+  if (st) return st == 2 ? PS_UNDEF : PS_CAP;
+  ser_cleanup(a);
+  int nrg = 0, nv = 0;
+  w.roff[0] = 0;
+  for (int r = 0; r < *a.nrings; ++r) {
+    const int root = a.rroot[r];
+    if (root < 0) continue;
+    int v = root;
+    do {
+      w.rxy[2 * nv] = a.R.x[v];
+      w.rxy[2 * nv + 1] = a.R.y[v];
+      ++nv;
+      v = a.R.next[v];
+    } while (v != root);
+    w.roff[++nrg] = nv;
+  }
+  *nrings_out = nrg;
+  *nverts_out = nv;
+  return PS_OK;
+}
+
+__global__ void k_pw_sizes(int nov, const long long* __restrict__ coff, int nb,
+                           const PwPair* __restrict__ pp, const int* __restrict__ pairK,
+                           const int* __restrict__ pass_of, long long* __restrict__ bytes) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p > nov) return;
+  if (p == nov) {
+    bytes[p] = 0;
+    return;
+  }
+  const int pass = pass_of ? pass_of[p] : 0;
+  const bool run = pp[p].mode == PW_FAST && pass >= 0;
+  bytes[p] = run ? (long long)pw_arena_bytes(nb, (int)(coff[p + 1] - coff[p]), pairK[p], pass) : 0;
+}
+
+__global__ void __launch_bounds__(kPwPairBlock) k_pw_pairs(PwPairArgs A, const int* __restrict__ pairK) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= A.nov) return;
+  const int pass = A.pass_of ? A.pass_of[p] : 0;
+  if (pass < 0) return;
+  if (A.pp[p].mode != PW_FAST) {
+    A.status[p] = A.pp[p].mode == PW_INPUT ? PS_UNDEF + 100 : PS_FALLBACK;
+    A.nrings[p] = A.nverts[p] = 0;
+    return;
+  }
+  const int nc = (int)(A.coff[p + 1] - A.coff[p]);
+  const PwCaps cp = pw_caps(A.nb, nc, pairK[p], pass);
+  Carver cv{A.arena + A.aoff[p], 0};
+  PwWork w = pw_carve(cv, cp);
+  int nr = 0, nv = 0;
+  const int st = pw_clip_pair(A, p, cp, w, &nr, &nv);
+  A.status[p] = st;
+  A.nrings[p] = st == PS_OK ? nr : 0;
+  A.nverts[p] = st == PS_OK ? nv : 0;
+}
+
+// where a pair's rings live: pass 0 arena, or the retry arena
+struct PwArenas {
+  const unsigned char* a0;
+  const long long* off0;
+  const unsigned char* a1;
+  const long long* off1;
+  const int* pass;
+  __device__ const unsigned char* at(int p) const {
+    return pass[p] == 1 ? a1 + off1[p] : a0 + off0[p];
+  }
+};
+
+__global__ void k_pw_pack(int nov, const long long* __restrict__ coff, int nb,
+                          const int* __restrict__ pairK, PwArenas ar, const int* __restrict__ fast,
+                          const long long* __restrict__ rpre, const long long* __restrict__ vpre,
+                          long long* __restrict__ ring_off, double* __restrict__ xy) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nov || !fast[p]) return;
+  const long long r0 = rpre[p], v0 = vpre[p];
+  const int nr = (int)(rpre[p + 1] - r0);
+  if (nr == 0) return;
+  const PwCaps cp = pw_caps(nb, (int)(coff[p + 1] - coff[p]), pairK[p], ar.pass[p]);
+  Carver cv{const_cast<unsigned char*>(ar.at(p)), 0};
+  const PwWork w = pw_carve(cv, cp);
+  for (int r = 0; r < nr; ++r) ring_off[r0 + r] = v0 + w.roff[r];
+  const int nv = w.roff[nr];
+  for (int i = 0; i < 2 * nv; ++i) xy[2 * v0 + i] = w.rxy[i];
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host
+int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cxy,
+                        const long long* d_coff, cudaStream_t st) {
+  BufferPool& pool = pl_.pool();
+  np = nov;
+  fallback_pairs = 0;
+  hits = 0;
+  tested = 0;
+  if (nb < 3) return pl_.fail(kEInput, "base needs at least 3 vertices");
+  if (nov < 0) return pl_.fail(kEInput, "negative overlay count");
+  status = (int*)pool.get("pw_status", sizeof(int) * (nov + 1));
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise)");
+  h_status.assign(nov, SBC_OK);
+  h_pair_ring.assign(nov + 1, 0);
+  total_rings = total_verts = 0;
+  if (nov == 0) return kOk;
+  long long totalC = 0;
+  std::vector<long long> hoff(nov + 1);
+  cudaMemcpyAsync(hoff.data(), d_coff, sizeof(long long) * (nov + 1), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise offsets");
+  totalC = hoff[nov];
+  for (int i = 0; i < nov; ++i)
+    if (hoff[i + 1] < hoff[i]) return pl_.fail(kEInput, "overlay offsets must not decrease");
+  // ---- base
+  auto* keys = (unsigned long long*)pool.get("pw_bkeys", sizeof(unsigned long long) * nb);
+  auto* keys2 = (unsigned long long*)pool.get("pw_bkeys2", sizeof(unsigned long long) * nb);
+  auto* vals = (unsigned*)pool.get("pw_bvals", sizeof(unsigned) * nb);
+  auto* vals2 = (unsigned*)pool.get("pw_bvals2", sizeof(unsigned) * nb);
+  void* rscr = pool.get("pw_rscr", radix_scratch_bytes(nb));
+  auto* fbox = (float4*)pool.get("pw_fbox", sizeof(float4) * nb);
+  auto* stats = (PwBaseStats*)pool.get("pw_bstats", sizeof(PwBaseStats));
+  int* flag = (int*)pool.get("pw_uflag", sizeof(int) * (nb + 1));
+  void* sscr = pool.get("pw_scan", scan_scratch_bytes((long long)nb + nov + 2) * 2);
+  double* ub = (double*)pool.get("pw_ub", sizeof(double) * nb);
+  int* rankB = (int*)pool.get("pw_rankb", sizeof(int) * nb);
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise base)");
+  PwBaseStats hs0{~0ull, 0ull, ~0ull, 0ull, 0.0, 0u};
+  cudaMemcpyAsync(stats, &hs0, sizeof(hs0), cudaMemcpyHostToDevice, st);
+  {
+    ::sbc::KProbe kp_("k_pw_base_edges", st, 16.0 * nb + 28.0 * nb);
+    k_pw_base_edges<<<grid_for(nb, 256), 256, 0, st>>>(nb, d_bxy, keys, vals, fbox, stats);
+  }
+  radix_sort_u64(keys, vals, keys2, vals2, nb, rscr, st);
+  {
+    ::sbc::KProbe kp_("k_pw_uflag", st);
+    k_pw_uflag<<<grid_for(nb + 1, 256), 256, 0, st>>>(nb, keys, flag);
+  }
+  exclusive_scan_i32(flag, nb + 1, sscr, st);
+  {
+    ::sbc::KProbe kp_("k_pw_uscatter", st);
+    k_pw_uscatter<<<grid_for(nb, 256), 256, 0, st>>>(nb, keys, vals, flag, d_bxy, ub, rankB);
+  }
+  PwBaseStats hs;
+  int nub = 0;
+  cudaMemcpyAsync(&hs, stats, sizeof(hs), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(&nub, flag + nb, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise base");
+  auto unkey = [](unsigned long long k) {
+    unsigned long long u = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+    double d;
+    std::memcpy(&d, &u, sizeof d);
+    return d;
+  };
+  // grid: cells about sqrt(area / n_b) wide (times the tuned factor), at
+  // least 1.5 mean edge extents, at most 2^22 cells
+  const double bx0 = unkey(hs.mnx), bx1 = unkey(hs.mxx), by0 = unkey(hs.mny), by1 = unkey(hs.mxy);
+  const double W = std::max(bx1 - bx0, 1e-300), Hh = std::max(by1 - by0, 1e-300);
+  double h = std::max(cell_factor * std::sqrt(W * Hh / nb), 1.5 * hs.ext / nb);
+  if (!(h > 0) || !std::isfinite(h)) h = std::max(W, Hh);
+  while ((W / h + 1) * (Hh / h + 1) > (double)(1 << 22)) h *= 1.25;
+  PwGrid g;
+  g.x0 = (float)bx0;
+  g.y0 = (float)by0;
+  g.inv = (float)(1.0 / h);
+  g.gx = std::max(1, (int)std::ceil(W / h) + 1);
+  g.gy = std::max(1, (int)std::ceil(Hh / h) + 1);
+  grid_cells = (long long)g.gx * g.gy;
+  const int ncell = g.gx * g.gy;
+  int* gstart = (int*)pool.get("pw_gstart", sizeof(int) * (ncell + 1));
+  int* gcur = (int*)pool.get("pw_gcur", sizeof(int) * (ncell + 1));
+  int* lng = (int*)pool.get("pw_long", sizeof(int) * nb);
+  unsigned* nlong = (unsigned*)pool.get("pw_nlong", 256);
+  void* gscr = pool.get("pw_gscan", scan_scratch_bytes(ncell + 1));
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise grid)");
+  cudaMemsetAsync(gstart, 0, sizeof(int) * (ncell + 1), st);
+  cudaMemsetAsync(gcur, 0, sizeof(int) * (ncell + 1), st);
+  cudaMemsetAsync(nlong, 0, sizeof(unsigned), st);
+  {
+    ::sbc::KProbe kp_("k_pw_grid_count", st);
+    k_pw_grid_count<<<grid_for(nb, 256), 256, 0, st>>>(nb, fbox, g, gstart, lng, nlong);
+  }
+  exclusive_scan_i32(gstart, ncell + 1, gscr, st);
+  int gtotal = 0;
+  cudaMemcpyAsync(&gtotal, gstart + ncell, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise grid");
+  int* gent = (int*)pool.get("pw_gent", sizeof(int) * (gtotal + 1));
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise grid)");
+  {
+    ::sbc::KProbe kp_("k_pw_grid_fill", st);
+    k_pw_grid_fill<<<grid_for(nb, 256), 256, 0, st>>>(nb, fbox, g, gstart, gcur, gent);
+  }
+  // ---- overlays
+  PwPair* pp = (PwPair*)pool.get("pw_pairs", sizeof(PwPair) * nov);
+  int* rankC = (int*)pool.get("pw_rankc", sizeof(int) * (totalC + 1));
+  int* rankCB = (int*)pool.get("pw_rankcb", sizeof(int) * (totalC + 1));
+  double* uval = (double*)pool.get("pw_uval", sizeof(double) * (totalC + 1));
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise overlays)");
+  cudaMemsetAsync(pp, 0, sizeof(PwPair) * nov, st);
+  const int base_flags = (int)hs.flags;
+  int maxn = 0;
+  for (int i = 0; i < nov; ++i) maxn = std::max<long long>(maxn, hoff[i + 1] - hoff[i]);
+  const int classes[4] = {-1, 1024, 4096, kPwMaxOverlay};
+  for (int k = 0; k < 3; ++k) {
+    if (maxn <= classes[k]) break;
+    const int P2 = classes[k + 1];
+    const size_t smem = (size_t)P2 * (sizeof(unsigned long long) + sizeof(int));
+    cudaFuncSetAttribute(k_pw_overlay_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    ::sbc::KProbe kp_("k_pw_overlay_prep", st);
+    k_pw_overlay_prep<<<nov, kPwPrepThreads, smem, st>>>(nov, d_coff, d_cxy, classes[k], P2, ub, nub,
+                                                         base_flags, pp, rankC, rankCB, uval);
+  }
+  // overlays above the largest class
+  if (maxn > kPwMaxOverlay) {
+    std::vector<PwPair> hp(nov);
+    cudaMemcpyAsync(hp.data(), pp, sizeof(PwPair) * nov, cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise prep");
+    for (int i = 0; i < nov; ++i)
+      if (hoff[i + 1] - hoff[i] > kPwMaxOverlay) hp[i].mode = PW_FALLBACK;
+    cudaMemcpyAsync(pp, hp.data(), sizeof(PwPair) * nov, cudaMemcpyHostToDevice, st);
+  }
+  // ---- candidates
+  int* pairK = (int*)pool.get("pw_pairk", sizeof(int) * (nov + 1));
+  int* hstart = (int*)pool.get("pw_hstart", sizeof(int) * (nov + 1));
+  int* hcur = (int*)pool.get("pw_hcur", sizeof(int) * (nov + 1));
+  auto* cnt = (unsigned long long*)pool.get("pw_counters", 256);
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise)");
+  unsigned long long cap = std::max<unsigned long long>(hit_cap_, 1ull << 16);
+  PwHit* hbuf = nullptr;
+  unsigned long long nh = 0;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    hbuf = (PwHit*)pool.get("pw_hits", sizeof(PwHit) * cap);
+    if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise hits)");
+    cudaMemsetAsync(pairK, 0, sizeof(int) * (nov + 1), st);
+    cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), st);
+    PwCandArgs ca{nov, d_coff, totalC, d_cxy, d_bxy, nb, g, gstart, gent, lng, nlong, fbox, pp,
+                  rankB, rankC, rankCB, uval, hbuf, cap, &cnt[0], pairK, &cnt[1]};
+    if (totalC > 0) {
+      ::sbc::KProbe kp_("k_pw_candidates", st, 32.0 * totalC);
+      k_pw_candidates<<<grid_for(totalC, 128), 128, 0, st>>>(ca);
+    }
+    unsigned long long hc[2];
+    cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise candidates");
+    nh = hc[0];
+    tested = (long long)hc[1];
+    if (nh <= cap) break;
+    cap = nh + nh / 4 + 1024;
+  }
+  if (nh > cap) return pl_.fail(kEInternal, "pairwise hit count changed between passes");
+  hit_cap_ = std::max(hit_cap_, nh);
+  hits = (long long)nh;
+  cudaMemcpyAsync(hstart, pairK, sizeof(int) * (nov + 1), cudaMemcpyDeviceToDevice, st);
+  exclusive_scan_i32(hstart, nov + 1, sscr, st);
+  PwHit* grouped = (PwHit*)pool.get("pw_hits_grouped", sizeof(PwHit) * (nh + 1));
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise hits)");
+  cudaMemsetAsync(hcur, 0, sizeof(int) * (nov + 1), st);
+  if (nh) {
+    ::sbc::KProbe kp_("k_pw_group", st);
+    k_pw_group<<<grid_for((long long)nh, 256), 256, 0, st>>>(nh, hbuf, hstart, hcur, grouped);
+  }
+  // ---- one thread per pair: pass 0, then pairs that ran out of ring room
+  long long* aoff0 = (long long*)pool.get("pw_aoff0", sizeof(long long) * (nov + 1));
+  long long* aoff1 = (long long*)pool.get("pw_aoff1", sizeof(long long) * (nov + 1));
+  int* pass = (int*)pool.get("pw_pass", sizeof(int) * (nov + 1));
+  int* nrings = (int*)pool.get("pw_nrings", sizeof(int) * (nov + 1));
+  int* nverts = (int*)pool.get("pw_nverts", sizeof(int) * (nov + 1));
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise)");
+  PwPip pip{d_bxy, nb, g, gstart, gent, lng, 0, fbox, nullptr, 0};
+  unsigned hlong = 0;
+  cudaMemcpyAsync(&hlong, nlong, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  {
+    ::sbc::KProbe kp_("k_pw_sizes", st);
+    k_pw_sizes<<<grid_for(nov + 1, 256), 256, 0, st>>>(nov, d_coff, nb, pp, pairK, nullptr, aoff0);
+  }
+  exclusive_scan_i64(aoff0, nov + 1, sscr, st);
+  long long total = 0;
+  cudaMemcpyAsync(&total, aoff0 + nov, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise sizes");
+  pip.nlong = (int)hlong;
+  unsigned char* arena0 = (unsigned char*)pool.get("pw_arena0", (size_t)total + 256);
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise arena)");
+  PwPairArgs pa{nov, d_coff, d_cxy, d_bxy, nb, pp, hstart, grouped, nullptr, arena0, aoff0,
+                status, nrings, nverts, pip};
+  {
+    // coordinates and records in; rings out
+    ::sbc::KProbe kp_("k_pw_pairs", st, 16.0 * totalC + 24.0 * (double)nh);
+    k_pw_pairs<<<grid_for(nov, kPwPairBlock), kPwPairBlock, 0, st>>>(pa, pairK);
+  }
+  std::vector<int> hst(nov), hpass(nov, -1);
+  cudaMemcpyAsync(hst.data(), status, sizeof(int) * nov, cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise clip");
+  int retry = 0;
+  for (int p = 0; p < nov; ++p)
+    if (hst[p] == PS_CAP) {
+      hpass[p] = 1;
+      ++retry;
+    }
+  unsigned char* arena1 = arena0;
+  if (retry) {
+    cudaMemcpyAsync(pass, hpass.data(), sizeof(int) * nov, cudaMemcpyHostToDevice, st);
+    {
+      ::sbc::KProbe kp_("k_pw_sizes", st);
+      k_pw_sizes<<<grid_for(nov + 1, 256), 256, 0, st>>>(nov, d_coff, nb, pp, pairK, pass, aoff1);
+    }
+    exclusive_scan_i64(aoff1, nov + 1, sscr, st);
+    cudaMemcpyAsync(&total, aoff1 + nov, sizeof(long long), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise sizes");
+    arena1 = (unsigned char*)pool.get("pw_arena1", (size_t)total + 256);
+    if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise arena)");
+    pa.pass_of = pass;
+    pa.arena = arena1;
+    pa.aoff = aoff1;
+    {
+      ::sbc::KProbe kp_("k_pw_pairs", st);
+      k_pw_pairs<<<grid_for(nov, kPwPairBlock), kPwPairBlock, 0, st>>>(pa, pairK);
+    }
+    cudaMemcpyAsync(hst.data(), status, sizeof(int) * nov, cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise clip");
+  }
+  for (int p = 0; p < nov; ++p) hpass[p] = hpass[p] == 1 ? 1 : 0;
+  cudaMemcpyAsync(pass, hpass.data(), sizeof(int) * nov, cudaMemcpyHostToDevice, st);
+  // ---- per pair: fast result, input error, or the pair pipeline
+  std::vector<int> hnr(nov), hnv(nov), fast(nov, 0);
+  cudaMemcpyAsync(hnr.data(), nrings, sizeof(int) * nov, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(hnv.data(), nverts, sizeof(int) * nov, cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise clip");
+  struct Stash {
+    std::vector<int> off;
+    std::vector<double> xy;
+  };
+  std::vector<Stash> stash(nov);
+  std::vector<int> stash_of(nov, -1);
+  for (int p = 0; p < nov; ++p) {
+    if (hst[p] == PS_OK) {
+      fast[p] = 1;
+      continue;
+    }
+    hnr[p] = hnv[p] = 0;
+    const long long n = hoff[p + 1] - hoff[p];
+    if (hst[p] == PS_UNDEF + 100 || n < 3) {
+      h_status[p] = SBC_EINPUT;
+      continue;
+    }
+    // the pair pipeline, exactly as sbc_clip_pair would run it
+    ++fallback_pairs;
+    const int sizes[1] = {(int)n};
+    pl_.clear_error();
+    const int rc = pl_.run(d_bxy, nb, d_cxy + 2 * hoff[p], sizes, 1);
+    if (rc == kEInput || rc == kEUndef) {
+      h_status[p] = rc == kEInput ? SBC_EINPUT : SBC_EUNDEF;
+      continue;
+    }
+    if (rc) return rc;
+    const auto& out = pl_.outputs()[0];
+    Stash& s = stash[p];
+    s.off.resize(out.nrings + 1, 0);
+    s.xy.resize(2 * out.nverts);
+    if (out.nrings > 0)
+      cudaMemcpyAsync(s.off.data(), out.d_off, sizeof(int) * (out.nrings + 1),
+                      cudaMemcpyDeviceToHost, st);
+    if (out.nverts > 0)
+      cudaMemcpyAsync(s.xy.data(), out.d_xy, sizeof(double) * 2 * out.nverts,
+                      cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise fallback");
+    hnr[p] = out.nrings;
+    hnv[p] = (int)out.nverts;
+    stash_of[p] = p;
+  }
+  pl_.clear_error();
+  // ---- packed output
+  std::vector<long long> rpre(nov + 1, 0), vpre(nov + 1, 0);
+  for (int p = 0; p < nov; ++p) {
+    rpre[p + 1] = rpre[p] + hnr[p];
+    vpre[p + 1] = vpre[p] + hnv[p];
+  }
+  total_rings = rpre[nov];
+  total_verts = vpre[nov];
+  h_pair_ring = rpre;
+  long long* d_rpre = (long long*)pool.get("pw_rpre", sizeof(long long) * (nov + 1));
+  long long* d_vpre = (long long*)pool.get("pw_vpre", sizeof(long long) * (nov + 1));
+  int* d_fast = (int*)pool.get("pw_fast", sizeof(int) * (nov + 1));
+  ring_off = (long long*)pool.get("pw_ring_off", sizeof(long long) * (total_rings + 1));
+  xy = (double*)pool.get("pw_xy", sizeof(double) * 2 * (total_verts + 1));
+  pair_ring = d_rpre;
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise output)");
+  cudaMemcpyAsync(d_rpre, rpre.data(), sizeof(long long) * (nov + 1), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(d_vpre, vpre.data(), sizeof(long long) * (nov + 1), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(d_fast, fast.data(), sizeof(int) * nov, cudaMemcpyHostToDevice, st);
+  {
+    const PwArenas ar{arena0, aoff0, arena1, aoff1, pass};
+    ::sbc::KProbe kp_("k_pw_pack", st);
+    k_pw_pack<<<grid_for(nov, 128), 128, 0, st>>>(nov, d_coff, nb, pairK, ar, d_fast, d_rpre,
+                                                  d_vpre, ring_off, xy);
+  }
+  std::vector<long long> roff_h;
+  for (int p = 0; p < nov; ++p) {
+    if (stash_of[p] < 0 || hnr[p] == 0) continue;
+    const Stash& s = stash[p];
+    roff_h.resize(hnr[p]);
+    for (int r = 0; r < hnr[p]; ++r) roff_h[r] = vpre[p] + s.off[r];
+    cudaMemcpyAsync(ring_off + rpre[p], roff_h.data(), sizeof(long long) * hnr[p],
+                    cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(xy + 2 * vpre[p], s.xy.data(), sizeof(double) * 2 * hnv[p],
+                    cudaMemcpyHostToDevice, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise output");
+  }
+  cudaMemcpyAsync(ring_off + total_rings, &total_verts, sizeof(long long), cudaMemcpyHostToDevice,
+                  st);
+  cudaMemcpyAsync(status, h_status.data(), sizeof(int) * nov, cudaMemcpyHostToDevice, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise output");
+  return kOk;
+}
+
+}  // namespace sbc

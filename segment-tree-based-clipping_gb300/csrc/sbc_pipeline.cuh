@@ -183,4 +183,30 @@ class BatchRunner {
   int* pass = nullptr;
 };
 
+// One base polygon against many overlays with pairwise results: overlay i's
+// rings are those of `seg base overlay_i` (sbc_pairwise.cu).  Pairs outside
+// the rank shortcut's conditions run through the Pipeline.
+class PairwiseRunner {
+ public:
+  explicit PairwiseRunner(Pipeline& pl) : pl_(pl) {}
+  int run(const double* d_bxy, int nb, int nov, const double* d_cxy, const long long* d_coff,
+          cudaStream_t st);
+  int np = 0;
+  int* status = nullptr;            // device, per overlay: SBC_* code
+  long long* pair_ring = nullptr;   // device, np+1
+  long long* ring_off = nullptr;    // device, total_rings+1
+  double* xy = nullptr;             // device, 2*total_verts
+  long long total_rings = 0, total_verts = 0;
+  std::vector<int> h_status;
+  std::vector<long long> h_pair_ring;
+  // diagnostics of the last run
+  int fallback_pairs = 0;           // pairs clipped by the pair pipeline
+  long long hits = 0, tested = 0, grid_cells = 0;
+  double cell_factor = 1.0;         // grid cell width in units of sqrt(area / n_b)
+
+ private:
+  Pipeline& pl_;
+  unsigned long long hit_cap_ = 0;
+};
+
 }  // namespace sbc

@@ -28,7 +28,23 @@ struct Pool {
   // | merged slot, list nodes: their merged slot; -1 unknown).  Null when the
   // caller does not track it.
   int* src = nullptr;
+  // optional run nodes: a node v with run[v] > 0 stands for run[v] + 1
+  // consecutive plain vertices rv0[v] .. rv0[v] + run[v] of the interleaved
+  // coordinate array rxy (no labels, not intersections); x/y hold the first.
+  // Null when every node is one vertex.
+  int* run = nullptr;
+  int* rv0 = nullptr;
+  const double* rxy = nullptr;
 };
+
+__device__ __forceinline__ bool is_run(const Pool& p, int v) { return p.run && p.run[v] > 0; }
+// coordinates of the last vertex of node v (the one next to its successor)
+__device__ __forceinline__ double last_x(const Pool& p, int v) {
+  return is_run(p, v) ? p.rxy[2 * (p.rv0[v] + p.run[v])] : p.x[v];
+}
+__device__ __forceinline__ double last_y(const Pool& p, int v) {
+  return is_run(p, v) ? p.rxy[2 * (p.rv0[v] + p.run[v]) + 1] : p.y[v];
+}
 
 struct SerialArgs {
   Pool P, Q, R;
@@ -40,12 +56,14 @@ struct SerialArgs {
   const double *bP, *cP, *ixB, *ixC;
   const int *alB, *nbC, *labB, *labC;
   int* status;   // 0 ok, 2 undefined, 3 capacity
+  int rfull = 0;  // set when the ring pool ran out of nodes
 };
 
 __device__ int pnew(Pool& p, double x, double y) {
   if (p.n >= p.cap) return -1;
   int v = p.n++;
   if (p.src) p.src[v] = -1;
+  if (p.run) p.run[v] = 0;
   p.x[v] = x;
   p.y[v] = y;
   p.next[v] = p.prev[v] = v;
@@ -65,19 +83,26 @@ __device__ void pinsert_after(Pool& p, int V, int curr) {
   p.prev[curr] = V;
 }
 
+// winding-number step of pointInPoly (foster/polygon.h:427-448) for the edge
+// (x0,y0)-(x1,y1); the winding number is the (order-free) sum of the steps
+__device__ __forceinline__ int pip_step(double x0, double y0, double x1, double y1, double rx,
+                                        double ry) {
+  if ((y0 < ry) != (y1 < ry)) {
+    if (x0 >= rx) {
+      if (x1 > rx) return 2 * (y1 > y0) - 1;
+      if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (y1 > y0)) return 2 * (y1 > y0) - 1;
+    } else if (x1 > rx) {
+      if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (y1 > y0)) return 2 * (y1 > y0) - 1;
+    }
+  }
+  return 0;
+}
+
 __device__ int ppip(const Pool& p, int root, double rx, double ry) {
   int w = 0, one = root;
   do {
     int two = p.next[one];
-    double x0 = p.x[one], y0 = p.y[one], x1 = p.x[two], y1 = p.y[two];
-    if ((y0 < ry) != (y1 < ry)) {
-      if (x0 >= rx) {
-        if (x1 > rx) w = w + 2 * (y1 > y0) - 1;
-        else if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (y1 > y0)) w = w + 2 * (y1 > y0) - 1;
-      } else if (x1 > rx) {
-        if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (y1 > y0)) w = w + 2 * (y1 > y0) - 1;
-      }
-    }
+    w += pip_step(p.x[one], p.y[one], p.x[two], p.y[two], rx, ry);
     one = two;
   } while (one != root);
   return (w % 2) != 0;
@@ -92,7 +117,10 @@ __device__ int rnew(SerialArgs& a) {
 
 __device__ int radd(SerialArgs& a, int r, double x, double y, int prov = -1) {
   int v = pnew(a.R, x, y);
-  if (v < 0) return -1;
+  if (v < 0) {
+    a.rfull = 1;
+    return -1;
+  }
   if (a.R.src) a.R.src[v] = prov;
   int root = a.rroot[r];
   if (root < 0) {
@@ -106,13 +134,25 @@ __device__ int radd(SerialArgs& a, int r, double x, double y, int prov = -1) {
   return 0;
 }
 
+// every vertex of node v of p to ring r, in walking order (a run node's
+// vertices backwards when walking backwards)
+__device__ int radd_node(SerialArgs& a, int r, const Pool& p, int v, bool forward, int prov) {
+  if (!is_run(p, v)) return radd(a, r, p.x[v], p.y[v], prov);
+  const int n = p.run[v];
+  for (int t = 0; t <= n; ++t) {
+    const int u = p.rv0[v] + (forward ? t : n - t);
+    if (radd(a, r, p.rxy[2 * u], p.rxy[2 * u + 1])) return -1;
+  }
+  return 0;
+}
+
 __device__ int rcopy(SerialArgs& a, const Pool& p, int root) {
   int r = rnew(a);
   if (r < 0) return -1;
   int v = root;
   do {
     const int prov = (p.src && p.src[v] >= 0) ? (((&p == &a.Q) ? 1 : 0) << 30) | p.src[v] : -1;
-    if (radd(a, r, p.x[v], p.y[v], prov)) return -1;
+    if (radd_node(a, r, p, v, true, prov)) return -1;
     v = p.next[v];
   } while (v != root);
   return 0;
@@ -220,7 +260,23 @@ __device__ int ser_non_isect_vertex(SerialArgs& a, int s, int root) {
   return -2;
 }
 
-__device__ int ser_label_trace(SerialArgs& a) {
+// pointInPoly against side s: the pool's own edges, or, for a pool with run
+// nodes, the caller's run-aware test
+struct NoRunPip {
+  __device__ int operator()(SerialArgs& a, int root, double rx, double ry) const {
+    return ppip(a.P, root, rx, ry);
+  }
+};
+
+template <class PipP>
+__device__ int pip_side(SerialArgs& a, int s, int root, double rx, double ry, const PipP& pp) {
+  Pool& p = side(a, s);
+  if (p.run) return pp(a, root, rx, ry);
+  return ppip(p, root, rx, ry);
+}
+
+template <class PipP>
+__device__ int ser_label_trace_t(SerialArgs& a, const PipP& pipP) {
   Pool& P = a.P;
   Pool& Q = a.Q;
   int roots[2] = {0, 0};
@@ -299,7 +355,7 @@ __device__ int ser_label_trace(SerialArgs& a) {
       } while (V != root);
       if (!found) return 2;
     }
-    if (ppip(side(a, 1 - s), roots[1 - s], px, py))
+    if (pip_side(a, 1 - s, roots[1 - s], px, py, pipP))
       if (rcopy(a, p, root)) return 3;
   }
   if (ident[0] && ident[1]) {
@@ -320,7 +376,7 @@ __device__ int ser_label_trace(SerialArgs& a) {
     if (V == -3) return 3;
     if (V < 0) return 2;
     int status = EX_ENTRY;
-    if (ppip(side(a, 1 - s), roots[1 - s], p.x[V], p.y[V])) tog(&status);
+    if (pip_side(a, 1 - s, roots[1 - s], p.x[V], p.y[V], pipP)) tog(&status);
     int first = 1, I = V;
     do {
       if (p.isect[I]) {
@@ -367,8 +423,8 @@ __device__ int ser_label_trace(SerialArgs& a) {
       if (VP < 0 || VQ < 0) return 3;
       if (P.src) P.src[VP] = P.src[IP];
       if (Q.src) Q.src[VQ] = Q.src[IQ];
-      double sP = area3(P.x[P.prev[IP]], P.y[P.prev[IP]], P.x[IP], P.y[IP], P.x[P.next[IP]],
-                        P.y[P.next[IP]]);
+      double sP = area3(last_x(P, P.prev[IP]), last_y(P, P.prev[IP]), P.x[IP], P.y[IP],
+                        P.x[P.next[IP]], P.y[P.next[IP]]);
       double sQ = area3(Q.x[Q.prev[IQ]], Q.y[Q.prev[IQ]], Q.x[IQ], Q.y[IQ], Q.x[Q.next[IQ]],
                         Q.y[Q.next[IQ]]);
       if (dmul(sP, sQ) > 0) {
@@ -413,7 +469,7 @@ __device__ int ser_label_trace(SerialArgs& a) {
             V = (status == EX_EXIT) ? pv->next[V] : pv->prev[V];
             pv->isect[V] = 0;
             const int prov = (pv->src && pv->src[V] >= 0) ? (sV << 30) | pv->src[V] : -1;
-            if (radd(a, r, pv->x[V], pv->y[V], prov)) return 2;
+            if (radd_node(a, r, *pv, V, status == EX_EXIT, prov)) return 2;
             if (--guard < 0) return 2;
           } while (!(pv->enex[V] == status) && !(sV == sI && V == I));
           if (!(sV == sI && V == I)) {
@@ -430,6 +486,8 @@ __device__ int ser_label_trace(SerialArgs& a) {
   }
   return 0;
 }
+
+__device__ int ser_label_trace(SerialArgs& a) { return ser_label_trace_t(a, NoRunPip{}); }
 
 __device__ void ser_cleanup(SerialArgs& a) {
   Pool& p = a.R;

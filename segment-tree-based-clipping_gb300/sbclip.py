@@ -78,6 +78,11 @@ class _BatchRings(ctypes.Structure):
 BATCH_MAX_VERTICES = 4096
 
 
+class _PairwiseJob(ctypes.Structure):
+    _fields_ = [("b_xy", ctypes.c_void_p), ("nb", ctypes.c_int), ("noverlays", ctypes.c_int),
+                ("c_xy", ctypes.c_void_p), ("c_off", ctypes.c_void_p)]
+
+
 def pack_polygons(polys):
     """Concatenate polygons: (xy (n,2) float64, offsets (len+1,) int64)."""
     arrs = [np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 2) for p in polys]
@@ -120,6 +125,11 @@ def load_library(path: str | os.PathLike | None = None):
         getattr(L, nm).argtypes = [vp, ctypes.POINTER(_Batch), vp, vp, vp]
     for nm in ("sbc_area_backward", "sbc_area_backward_device"):
         getattr(L, nm).argtypes = [vp, ctypes.POINTER(_Batch), vp, vp, vp, vp]
+    for nm in ("sbc_clip_pairwise", "sbc_clip_pairwise_device"):
+        getattr(L, nm).argtypes = [vp, ctypes.POINTER(_PairwiseJob), ctypes.POINTER(_BatchRings),
+                                   vp]
+    L.sbc_pairwise_info.argtypes = [vp, ctypes.POINTER(ll), i]
+    L.sbc_pairwise_set_cell_factor.argtypes = [vp, ctypes.c_double]
     L.sbc_trace_rings_noalloc.argtypes = [ctypes.POINTER(_MergedLists), vp, i, vp, ll,
                                           ctypes.POINTER(i), ctypes.POINTER(ll), vp,
                                           ctypes.c_char_p, i]
@@ -264,6 +274,47 @@ class Clipper:
         for p in range(np_):
             out.append([xy[ro[q]:ro[q + 1]] for q in range(pr[p], pr[p + 1])])
         return out, st
+
+    @staticmethod
+    def _unpack_rings(r, np_):
+        pr = np.ctypeslib.as_array(ctypes.cast(r.pair_ring, ctypes.POINTER(ctypes.c_longlong)),
+                                   (np_ + 1,)).copy()
+        ro = np.ctypeslib.as_array(ctypes.cast(r.ring_off, ctypes.POINTER(ctypes.c_longlong)),
+                                   (int(r.nrings) + 1,)).copy()
+        xy = (np.ctypeslib.as_array(ctypes.cast(r.xy, ctypes.POINTER(ctypes.c_double)),
+                                    (2 * int(r.nverts),)).copy().reshape(-1, 2)
+              if r.nverts > 0 else np.zeros((0, 2)))
+        st = np.ctypeslib.as_array(ctypes.cast(r.status, ctypes.POINTER(ctypes.c_int)),
+                                   (np_,)).copy() if np_ else np.zeros(0, np.int32)
+        return [[xy[ro[q]:ro[q + 1]] for q in range(pr[p], pr[p + 1])] for p in range(np_)], st
+
+    def clip_pairwise(self, base, overlays, stream: int | None = None):
+        """`seg base overlay_i` for every overlay: (list of ring lists, status array)."""
+        bxy = np.ascontiguousarray(base, dtype=np.float64).reshape(-1, 2)
+        cxy, coff = pack_polygons(overlays)
+        j = _PairwiseJob(bxy.ctypes.data, bxy.shape[0], len(overlays), cxy.ctypes.data,
+                         coff.ctypes.data)
+        r = _BatchRings()
+        self._check(self._L.sbc_clip_pairwise(self._h, ctypes.byref(j), ctypes.byref(r), stream))
+        return self._unpack_rings(r, len(overlays))
+
+    def clip_pairwise_device(self, d_bxy, nb, noverlays, d_cxy, d_coff,
+                             stream: int | None = None):
+        """Device-array form; returns (nrings, nverts) and leaves the rings on the device."""
+        j = _PairwiseJob(d_bxy, nb, noverlays, d_cxy, d_coff)
+        r = _BatchRings()
+        self._check(self._L.sbc_clip_pairwise_device(self._h, ctypes.byref(j), ctypes.byref(r),
+                                                     stream))
+        return int(r.nrings), int(r.nverts)
+
+    def pairwise_info(self) -> dict:
+        """Diagnostics of the last pairwise call."""
+        v = (ctypes.c_longlong * 4)()
+        self._L.sbc_pairwise_info(self._h, v, 4)
+        return {"fallback_pairs": v[0], "unique": v[1], "tested": v[2], "grid_cells": v[3]}
+
+    def set_pairwise_cell_factor(self, f: float) -> None:
+        self._check(self._L.sbc_pairwise_set_cell_factor(self._h, float(f)))
 
     def area_forward(self, bases, overlays, stream: int | None = None):
         """Intersection area of every pair: (area, status)."""

@@ -12,6 +12,11 @@ shapes and sizes of the benchmark configurations:
 * ``pair_small``      10k x 8k plain stars (base at (0,0), overlay at (0.3,0.2)).
 * ``pair_large``      1M x 1M jagged stars, R = 1000; overlay offset
                       (0.25R, 0.1R) and rotated 0.3 rad about its centre.
+* ``one_to_many``     one jagged base (200k vertices, R = 1000) against many
+                      plain-star overlays: sizes log-uniform in [4, 5000], radii
+                      log-uniform in [0.001R, 0.05R], centres uniform in the
+                      base's bounding box (or, with ``near_boundary``, that
+                      fraction of them on base vertices).
 
 Files use the reference's text format (``src/clip.cpp:181-298``): the vertex
 count on the first line, then one ``x,y`` line per vertex, no closing duplicate.
@@ -140,6 +145,26 @@ def pair_large(n: int = 1_000_000, seed_base: int = 2000, base_freq: int = JAGGE
     c = jagged_star(n, seed_base + 1, centre=(0.25 * R, 0.1 * R), R=R, rotation=0.3,
                     base_freq=base_freq)
     return b, c
+
+
+def one_to_many(n_base: int = 200_000, n_overlays: int = 10_000, seed: int = 3000,
+                R: float = LARGE_R, lo: int = 4, hi: int = 5000, rmin: float = 0.001,
+                rmax: float = 0.05, near_boundary: float = 0.0):
+    """One jagged base and many plain-star overlays (log-uniform sizes and radii)."""
+    base = jagged_star(n_base, seed, R=R)
+    rng = np.random.default_rng(seed + 1)
+    lo_b, hi_b = base.min(axis=0), base.max(axis=0)
+    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi + 1), n_overlays)).astype(np.int64)
+    sizes = np.clip(sizes, lo, hi)
+    radii = R * np.exp(rng.uniform(np.log(rmin), np.log(rmax), n_overlays))
+    centres = rng.uniform(lo_b, hi_b, (n_overlays, 2))
+    on_edge = rng.uniform(0.0, 1.0, n_overlays) < near_boundary
+    picks = rng.integers(0, n_base, n_overlays)
+    centres[on_edge] = base[picks[on_edge]]
+    seeds = rng.integers(0, 2**62, n_overlays)
+    overlays = [star(int(n), int(s), centre=(float(c[0]), float(c[1])), R=float(r))
+                for n, s, c, r in zip(sizes, seeds, centres, radii)]
+    return base, overlays
 
 
 def small_pairs(npairs: int, seed: int = 4000, lo: int = 4, hi: int = 64):

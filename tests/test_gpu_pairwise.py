@@ -1,0 +1,99 @@
+"""GPU parity of the one-base-many-overlays call (sbc_clip_pairwise).
+
+Every overlay's rings must equal sbc_clip_pair(base, overlay) bit for bit:
+the pair pipeline is itself pinned to the reference's CPU build, and
+`seg base overlay` run once per overlay is what the reference offers for this
+workload.  The cases cover overlays inside, outside and across the base's
+boundary, inputs that leave the batched path's conditions (a shared x value, a
+vertical edge, a polygon the size of the base), an overlay that contains the
+whole base, and too-short overlays.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import sbclip_gen as gen
+from conftest import rings_equal
+
+pytestmark = pytest.mark.gpu
+
+
+def _check(clipper, base, overlays):
+    got, st = clipper.clip_pairwise(base, overlays)
+    assert len(got) == len(overlays)
+    bad = []
+    for i, c in enumerate(overlays):
+        if len(c) < 3:
+            assert st[i] == 1, i
+            assert got[i] == []
+            continue
+        want = clipper.clip_pair(base, c)
+        assert st[i] == 0, (i, st[i])
+        if not rings_equal(got[i], want):
+            bad.append(i)
+    assert not bad, f"{len(bad)} overlays differ, first {bad[:8]}"
+    return got
+
+
+def test_pairwise_random_overlays(clipper):
+    base, ovs = gen.one_to_many(n_base=20_000, n_overlays=300, seed=3100, hi=2000,
+                                near_boundary=0.5)
+    got = _check(clipper, base, ovs)
+    info = clipper.pairwise_info()
+    assert info["fallback_pairs"] <= len(ovs) // 20, info
+    assert info["unique"] > 100, info
+    assert sum(len(r) for r in got) > 50
+
+
+def test_pairwise_cell_factor_does_not_change_results(clipper):
+    base, ovs = gen.one_to_many(n_base=5_000, n_overlays=120, seed=3200, hi=800,
+                                near_boundary=0.6)
+    ref, _ = clipper.clip_pairwise(base, ovs)
+    for f in (0.25, 4.0):
+        clipper.set_pairwise_cell_factor(f)
+        try:
+            got, _ = clipper.clip_pairwise(base, ovs)
+        finally:
+            clipper.set_pairwise_cell_factor(1.0)
+        assert all(rings_equal(a, b) for a, b in zip(got, ref))
+
+
+def test_pairwise_special_overlays(clipper):
+    base = gen.jagged_star(3_000, 3300, R=1000.0)
+    b0 = base[0]
+    ovs = []
+    # a square across the boundary near vertex 0, and the same square sharing
+    # base vertex 0's x value (leaves the rank shortcut)
+    sq = np.array([[-30.0, -30.0], [30.0, -30.0], [30.0, 30.0], [-30.0, 30.0]])
+    ovs.append(sq * [1.0, 0.9] + b0 + [0.37, 0.11])
+    shared = sq + b0 + [0.0, 0.5]
+    shared[0, 0] = b0[0]
+    ovs.append(shared)
+    # an axis-aligned rectangle (vertical edges)
+    ovs.append(np.array([[0.0, 0.0], [200.0, 0.0], [200.0, 120.0], [0.0, 120.0]]) + b0 * 0.5)
+    # far outside, deep inside, and an overlay containing the whole base
+    ovs.append(gen.star(40, 1, centre=(5000.0, 5000.0), R=10.0))
+    ovs.append(gen.star(400, 2, centre=(1.0, 2.0), R=20.0))
+    ovs.append(gen.star(64, 3, centre=(0.5, -0.25), R=4000.0))
+    # larger than the base, crossing it
+    ovs.append(gen.star(4_000, 4, centre=(300.0, -200.0), R=900.0))
+    # too short
+    ovs.append(np.array([[0.0, 0.0], [1.0, 1.0]]))
+    # triangles straddling many base edges
+    for k in range(8):
+        v = base[(k * 373) % len(base)]
+        ovs.append(np.array([[v[0] - 40, v[1] - 35], [v[0] + 45, v[1] - 20], [v[0], v[1] + 50]]))
+    _check(clipper, base, ovs)
+    assert clipper.pairwise_info()["fallback_pairs"] >= 2
+
+
+def test_pairwise_small_base_and_repeat(clipper):
+    base = gen.star(12, 77, R=1.0)
+    ovs = [gen.star(int(n), 100 + n, centre=(0.1 * n % 1 - 0.5, 0.05 * n % 1 - 0.5), R=0.6)
+           for n in range(3, 40)]
+    a = _check(clipper, base, ovs)
+    b, _ = clipper.clip_pairwise(base, ovs)
+    assert all(rings_equal(x, y) for x, y in zip(a, b))
+    got, st = clipper.clip_pairwise(base, [])
+    assert got == [] and len(st) == 0
