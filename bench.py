@@ -2,7 +2,8 @@
 """Benchmark: milliseconds per 1M x 1M polygon clip on one GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload pair_1m_1m|pair_200k_200k|pair_10k_8k|small_pairs_65536]
+                    [--workload pair_1m_1m|pair_200k_200k|pair_10k_8k|small_pairs_65536|
+                                one_to_many_200k_10000]
 
 A step is one full clip of the workload pair (segment tree build, candidate
 stab queries, FP64 intersection, merge, labelling and ring tracing) by the
@@ -25,6 +26,13 @@ and area gradients on device-resident arrays, reported as pairs per second
 (whole job; under torchrun each rank clips its own 65,536 pairs), next to
 the plain per-pair GPU path (one sbc_clip_pair_device call per pair) and the
 reference run pairwise on the host cores.
+
+`--workload one_to_many_200k_10000` measures one 200,000-vertex jagged base
+against 10,000 overlays (sizes log-uniform in [4, 5000], radii log-uniform in
+[0.001R, 0.05R], centres uniform in the base's box), each overlay's result
+being `seg base overlay` (sbc_clip_pairwise): one step = all 10,000 pairs on
+device-resident inputs, reported as pairs per second, next to the plain
+per-pair GPU path and the reference run pairwise on the host cores.
 
 `--impl reference` times the reference's own CPU (OpenMP) build
 (oracle/_ref/seg, all host threads) on the same workload; when that build is
@@ -450,7 +458,162 @@ def run_small_pairs(args, rank: int, world: int):
     return out
 
 
+ONE_TO_MANY = (200_000, 10_000)
+ONE_TO_MANY_METRIC = "clipped pairs/s, one 200k-vertex base x 10,000 overlays, pairwise forward"
+
+
+def one_to_many_workload():
+    nb, nov = ONE_TO_MANY
+    base, ovs = gen.one_to_many(n_base=nb, n_overlays=nov, seed=3000)
+    desc = {"workload": f"one_to_many_{nb // 1000}k_{nov}", "base_vertices": nb,
+            "overlays": nov, "overlay_vertices": int(sum(len(o) for o in ovs)),
+            "generator": "jagged base R=1000; plain-star overlays, sizes log-U[4,5000], radii "
+                         "log-U[0.001R,0.05R], centres U(base box)"}
+    return base, ovs, desc
+
+
+def run_one_to_many(args, rank: int, world: int):
+    """One step = every overlay's pairwise result (sbc_clip_pairwise_device)
+    on device-resident inputs."""
+    import torch
+    import sbclip
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    base, ovs, desc = one_to_many_workload()
+    nov = len(ovs)
+    cxy, coff = sbclip.pack_polygons(ovs)
+    cuda = f"cuda:{dev}"
+    tb = torch.from_numpy(np.ascontiguousarray(base)).to(cuda)
+    tc = torch.from_numpy(cxy).to(cuda)
+    to = torch.from_numpy(coff).to(cuda)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=cuda)
+    clip = sbclip.Clipper(dev)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    def step():
+        return clip.clip_pairwise_device(tb.data_ptr(), len(base), nov, tc.data_ptr(),
+                                         to.data_ptr(), sp)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    l0 = sbclip.kernel_launches()
+    times = []
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            nr, nv = step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+    launches = sbclip.kernel_launches() - l0
+    info = clip.pairwise_info()
+    ms = float(np.mean(times))
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([ms], device=cuda)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    torch.cuda.synchronize()
+    sbclip.profile_begin()
+    step()
+    torch.cuda.synchronize()
+    prof_b = sbclip.profile_end(with_bytes=True)
+    prof = {k: (v[0], v[1]) for k, v in prof_b.items()}
+    # end to end through the host-array C ABI (sbc_clip_pairwise): inputs
+    # copied in and every ring copied out, inside each step
+    e2e_t = []
+    d2h = 0
+    for _ in range(max(args.steps, 1)):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pr, ro, xy, stt = clip.clip_pairwise_flat(base, cxy, coff, sp, copy=False)
+        e2e_t.append((time.perf_counter() - t0) * 1e3)
+        d2h = ro.nbytes + xy.nbytes
+        n_ok = int((stt == 0).sum())
+    e2e = {"value": nov * world / (float(np.mean(e2e_t)) * 1e-3), "unit": "pairs/s",
+           "h2d_bytes_per_step": int(base.nbytes + cxy.nbytes + coff.nbytes),
+           "d2h_bytes_per_step": int(d2h)}
+    # the plain per-pair GPU path: one sbc_clip_pair_device call per overlay
+    sample = 64
+    rng = np.random.default_rng(5)
+    pick = rng.choice(nov, sample, replace=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for p in pick:
+        clip.clip_pair_device(tb.data_ptr(), len(base), tc.data_ptr() + 16 * int(coff[p]),
+                              int(coff[p + 1] - coff[p]), sp)
+    torch.cuda.synchronize()
+    per_pair = sample / (time.perf_counter() - t0)
+    pk, kind = peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][0]) if prof else None
+    roof = None
+    if dom:
+        name, (tot_ms, n_l) = dom
+        ab = prof_b[name][2] / max(n_l, 1)
+        achieved = ab / (tot_ms / max(n_l, 1) * 1e-3) / 1e9
+        roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
+                "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "traffic": None,
+                "peak_source": kind, "ms_per_launch": tot_ms / max(n_l, 1)}
+    value = nov * world / (ms * 1e-3)
+    out = {
+        "metric": ONE_TO_MANY_METRIC,
+        "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded star polygons)",
+        "config": dict(desc, parallelism="replicas" if world > 1 else "single",
+                       l2="flushed between steps (256 MiB write)"),
+        "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
+        "kernels_top": {k: {"ms_per_step": v[0], "launches_per_step": v[1]}
+                        for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])[:8]},
+        "clocks": clk.summary(),
+        "counts": {"pairs_ok": n_ok, "rings": nr, "ring_vertices": nv,
+                   "pairs_by_pair_pipeline": info["fallback_pairs"],
+                   "unique_intersections": info["unique"],
+                   "box_overlapping_edge_pairs_tested": info["tested"],
+                   "edge_pairs_tested_per_s": info["tested"] / (ms * 1e-3),
+                   "per_pair_gpu_path_pairs_per_s": per_pair, "per_pair_sample": sample,
+                   "batched_over_per_pair": value / per_pair},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        sample_cpu = [(base, ovs[int(p)]) for p in pick[:32]]
+        v, cores, kind2 = reference_pairs_per_s(sample_cpu, os.cpu_count() or 1)
+        out["cpu_baseline"] = {"value": v, "unit": "pairs/s", "cores": cores, "kind": kind2,
+                               "sample": "32 of the overlays, each clipped against the base by "
+                                         "its own reference run"}
+    clip.close()
+    return out
+
+
 def run_reference_arm(args):
+    if args.workload.startswith("one_to_many"):
+        base, ovs, desc = one_to_many_workload()
+        steps = max(1, min(args.steps, 3))
+        threads = os.cpu_count() or 1
+        rng = np.random.default_rng(5)
+        pick = rng.choice(len(ovs), 32 * steps, replace=False)
+        vals = [reference_pairs_per_s([(base, ovs[int(p)]) for p in pick[32 * i:32 * (i + 1)]],
+                                      threads) for i in range(steps)]
+        v = float(np.mean([x[0] for x in vals]))
+        cb = {"value": v, "unit": "pairs/s", "cores": vals[0][1], "kind": vals[0][2],
+              "sample": f"{steps} x 32 overlays, each clipped against the base by its own run"}
+        return {"impl": "reference", "metric": ONE_TO_MANY_METRIC, "value": v, "unit": "pairs/s",
+                "n_gpus": args.gpus, "steps": steps, "warmup": 0, "ms_per_step": 32 / v * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded star polygons)",
+                "config": dict(desc, parallelism="host cores"), "cpu_baseline": cb,
+                "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
     if args.workload.startswith("small_pairs"):
         pairs, desc = small_pairs_workload(SMALL_PAIRS, 4000)
         steps = max(1, min(args.steps, 3))
@@ -492,7 +655,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="pair_1m_1m",
-                    choices=["pair_1m_1m", "pair_200k_200k", "pair_10k_8k", "small_pairs_65536"])
+                    choices=["pair_1m_1m", "pair_200k_200k", "pair_10k_8k", "small_pairs_65536",
+                             "one_to_many_200k_10000"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -506,6 +670,8 @@ def main():
         dist.init_process_group("nccl")
     if args.workload.startswith("small_pairs"):
         out = run_small_pairs(args, rank, world)
+    elif args.workload.startswith("one_to_many"):
+        out = run_one_to_many(args, rank, world)
     else:
         out = run_gb300(args, rank, world)
     if rank == 0:

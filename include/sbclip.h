@@ -205,12 +205,18 @@ int sbc_clip_pairwise_device(sbc_ctx* ctx, const sbc_pairwise_job* job, sbc_batc
 /* Diagnostics of the last sbc_clip_pairwise call: out[0] overlays clipped by
  * the single-pair pipeline (inputs outside the batched path's conditions),
  * out[1] unique intersecting edge pairs, out[2] box-overlapping edge pairs
- * tested, out[3] cells of the base grid. */
+ * tested, out[3] cells of the base grid, out[4] overlays whose records went
+ * through the single-pair pipeline's data-parallel rows A9-A18 (see
+ * sbc_pairwise_set_split). */
 int sbc_pairwise_info(const sbc_ctx* ctx, long long* out, int n);
 /* Base-grid cell width of sbc_clip_pairwise in units of
  * sqrt(base bounding-box area / nb); default 1.  A tuning knob: results do not
  * depend on it. */
 int sbc_pairwise_set_cell_factor(sbc_ctx* ctx, double factor);
+/* Overlays with at least `records` intersecting edge pairs leave the
+ * one-thread-per-pair back end for the data-parallel one; default 8192.  A
+ * tuning knob: results do not depend on it. */
+int sbc_pairwise_set_split(sbc_ctx* ctx, int records);
 
 /* Allocation-free ring tracing.  No counterpart in the reference: it exists
  * for callers that are not allowed to allocate device memory themselves or

@@ -52,6 +52,22 @@ int Pipeline::run(const double* d_bxy, int nb_, const double* d_cxy, const int* 
   return rc;
 }
 
+int Pipeline::run_from_hits(const double* d_bxy, int nb_, const double* d_cxy, int nc,
+                            const int* rb, const int* rc, const int* rt,
+                            const unsigned long long* rkey, long long nhits) {
+  err_.clear();
+  outs_.assign(1, OverlayOut());
+  nb = nb_;
+  k = 1;
+  if (nb < 3 || nc < 3) return fail(kEInput, "polygons need at least 3 vertices");
+  const int sizes[1] = {nc};
+  int rc0 = stage_setup(d_bxy, d_cxy, sizes);
+  if (!rc0) rc0 = stage_records(1, rb, rc, rt, rkey, nhits, outs_[0], true);
+  if (cudaGetLastError() != cudaSuccess && !rc0) rc0 = fail(kECuda, "CUDA error in the pipeline");
+  if (scan_error_take() && !rc0) rc0 = fail(kEInternal, "a scan's bounded wait gave up");
+  return rc0;
+}
+
 }  // namespace sbc
 
 using sbc::Pipeline;
@@ -698,8 +714,9 @@ extern "C" int sbc_clip_pairwise(sbc_ctx* c, const sbc_pairwise_job* j, sbc_batc
 
 extern "C" int sbc_pairwise_info(const sbc_ctx* c, long long* out, int n) {
   if (!c || !out) return SBC_EINPUT;
-  const long long v[4] = {c->pw->fallback_pairs, c->pw->hits, c->pw->tested, c->pw->grid_cells};
-  for (int i = 0; i < n && i < 4; ++i) out[i] = v[i];
+  const long long v[5] = {c->pw->fallback_pairs, c->pw->hits, c->pw->tested, c->pw->grid_cells,
+                          c->pw->big_pairs};
+  for (int i = 0; i < n && i < 5; ++i) out[i] = v[i];
   return SBC_OK;
 }
 
@@ -707,5 +724,12 @@ extern "C" int sbc_pairwise_set_cell_factor(sbc_ctx* c, double f) {
   if (!c) return SBC_EINPUT;
   if (!(f > 0.0) || f > 1e6) return set_err(c, SBC_EINPUT, "cell factor must be positive");
   c->pw->cell_factor = f;
+  return SBC_OK;
+}
+
+extern "C" int sbc_pairwise_set_split(sbc_ctx* c, int records) {
+  if (!c) return SBC_EINPUT;
+  if (records < 1) return set_err(c, SBC_EINPUT, "split must be at least 1 record");
+  c->pw->big_k = records;
   return SBC_OK;
 }

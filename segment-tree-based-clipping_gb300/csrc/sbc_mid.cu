@@ -422,11 +422,6 @@ __global__ void k_labels_c(int nQ, const int* __restrict__ cWin, const int* __re
 
 // ============================================================== stage_overlay
 int Pipeline::stage_overlay(int cType, OverlayOut& out) {
-  cudaStream_t st = st_;
-  const int cListId = cType - 1;
-  const int bSize = nb;
-  const int cStart = hcS[cListId];
-  const int cSize = hcS[cType] - hcS[cListId] - 1;
   // ---- A8 candidate pairs: unique hits with the key of their first emission
   int *rb = nullptr, *rc = nullptr, *rt = nullptr;
   unsigned long long* rkey = nullptr;
@@ -435,6 +430,21 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
     int rc0 = stage_candidates(cType, &rb, &rc, &rt, &rkey, &nraw, out);
     if (rc0) return rc0;
   }
+  return stage_records(cType, rb, rc, rt, rkey, nraw, out);
+}
+
+// A9-A18 from the candidate hits of overlay cType: base ids rb, overlay ids
+// rc (offsets into the interleaved arrays), types rt, first-emission keys.
+// With `unique_sorted` the hits are already A9's output (unique pairs in base
+// id, then key order) and A9 is skipped.
+int Pipeline::stage_records(int cType, const int* rb, const int* rc, const int* rt,
+                            const unsigned long long* rkey, long long nraw, OverlayOut& out,
+                            bool unique_sorted) {
+  cudaStream_t st = st_;
+  const int cListId = cType - 1;
+  const int bSize = nb;
+  const int cStart = hcS[cListId];
+  const int cSize = hcS[cType] - hcS[cListId] - 1;
 
   // ---- A9 dedup: hits grouped by base edge (counting sort), put in key order
   // per edge, first occurrence per overlay edge kept
@@ -448,7 +458,8 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
   if (pool_.failed) return fail(kENoMem, "device allocation failed (dedup)");
   int K = 0;
   const int nseg = bSize;
-  if (R > 0) {
+  if (unique_sorted) K = (int)R;
+  if (R > 0 && !unique_sorted) {
     cudaMemsetAsync(segstart, 0, sizeof(int) * ((long long)bSize + 1), st);
     cudaMemsetAsync(bfill, 0, sizeof(int) * ((long long)bSize + 1), st);
     {
@@ -485,7 +496,11 @@ int Pipeline::stage_overlay(int cType, OverlayOut& out) {
   int* uc = (int*)pool_.get("u_c", sizeof(int) * (K + 1));
   int* ut = (int*)pool_.get("u_t", sizeof(int) * (K + 1));
   if (pool_.failed) return fail(kENoMem, "device allocation failed (unique)");
-  if (K > 0) {
+  if (K > 0 && unique_sorted) {
+    cudaMemcpyAsync(ub, rb, sizeof(int) * K, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(uc, rc, sizeof(int) * K, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(ut, rt, sizeof(int) * K, cudaMemcpyDeviceToDevice, st);
+  } else if (K > 0) {
     {
       ::sbc::KProbe kp_("k_dedup_write", st);
       k_dedup_write<<<grid_for(R, 256), 256, 0, st>>>(ord, keep, R, rb, rc, rt, ub, uc, ut);

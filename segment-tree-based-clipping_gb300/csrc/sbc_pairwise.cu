@@ -95,7 +95,8 @@ struct PwPair {
 
 struct PwHit {
   int pair, b, j, type;
-  unsigned long long key;
+  unsigned long long key;  // first emission
+  double al, bt;           // lineSegmentIntersection's alpha and beta
 };
 
 __device__ __forceinline__ int lower_bound_d(const double* a, int n, double x) {
@@ -513,7 +514,7 @@ __global__ void k_pw_candidates(PwCandArgs A) {
     if (emission_q(lrB, lrC, aftB, befB, aftC, befC, nb + j, 2 * j, T.logL, &key) == 0) return;
     const unsigned long long h = atomicAdd(A.nhits, 1ull);
     atomicAdd(&A.pairK[i], 1);
-    if (h < A.cap) A.hits[h] = PwHit{i, be, j, ty, key};
+    if (h < A.cap) A.hits[h] = PwHit{i, be, j, ty, key, al, bt};
   };
   for (int cy = cy0; cy <= cy1; ++cy) {
     for (int cx = cx0; cx <= cx1; ++cx) {
@@ -539,13 +540,44 @@ __global__ void k_pw_candidates(PwCandArgs A) {
   if (tested) atomicAdd(A.tested, tested);
 }
 
-__global__ void k_pw_group(unsigned long long nh, const PwHit* __restrict__ hits,
-                           const int* __restrict__ hstart, int* __restrict__ cur,
-                           PwHit* __restrict__ out) {
-  const unsigned long long h = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+// The hits of every pair in the reference's record order (base id, then
+// first emission; removeDuplicatesAtEdge after radixsort, src/clip.cpp:368-
+// 493): a stable sort by the emission key, then a stable sort by (pair, base
+// edge), then a gather.
+__global__ void k_pw_hit_keys(long long nh, const PwHit* __restrict__ hits,
+                              unsigned long long* __restrict__ keys, unsigned* __restrict__ vals) {
+  const long long h = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (h >= nh) return;
-  const PwHit x = hits[h];
-  out[hstart[x.pair] + atomicAdd(&cur[x.pair], 1)] = x;
+  keys[h] = hits[h].key;
+  vals[h] = (unsigned)h;
+}
+
+__global__ void k_pw_hit_keys2(long long nh, const PwHit* __restrict__ hits,
+                               const unsigned* __restrict__ vals,
+                               unsigned long long* __restrict__ keys) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nh) return;
+  const PwHit& x = hits[vals[t]];
+  keys[t] = ((unsigned long long)(unsigned)x.pair << 32) | (unsigned)x.b;
+}
+
+__global__ void k_pw_gather(long long nh, const PwHit* __restrict__ hits,
+                            const unsigned* __restrict__ vals, PwHit* __restrict__ out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nh) return;
+  out[t] = hits[vals[t]];
+}
+
+// one pair's records as the pair pipeline's candidate hits
+__global__ void k_pw_split(int n, const PwHit* __restrict__ h, int* __restrict__ rb,
+                           int* __restrict__ rc, int* __restrict__ rt,
+                           unsigned long long* __restrict__ key) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  rb[i] = 2 * h[i].b;
+  rc[i] = 2 * h[i].j;
+  rt[i] = h[i].type;
+  key[i] = h[i].key;
 }
 
 // ------------------------------------------------------------------ one pair
@@ -571,11 +603,11 @@ struct PwWork {
   int *re_e, *re_s, *re_nd, *re_pre, *re_si;
   int *cAll, *cND, *cfill, *csorted;
   double* isxy;
-  int *aB, *aC, *sB, *sC, *bNI, *cNI;
+  int *aB, *aC, *sB, *sC, *bNI, *cNI, *bSI;
   double *spx, *spy;
   int *spal, *spnb, *splab, *spnode;
   double* ixC;
-  int *alC, *nbC, *labC, *cWin;
+  int *alC, *nbC, *labC, *cWin, *cWinSI, *nbCsi;
   Pool P, Q, R;
   int* runIds;
   int* rroot;
@@ -627,6 +659,7 @@ __host__ __device__ __forceinline__ PwWork pw_carve(Carver& cv, const PwCaps& c)
   w.sC = cv.take<int>(K);
   w.bNI = cv.take<int>(K);
   w.cNI = cv.take<int>(K);
+  w.bSI = cv.take<int>(K);
   w.spx = cv.take<double>(c.sp);
   w.spy = cv.take<double>(c.sp);
   w.spal = cv.take<int>(c.sp);
@@ -638,6 +671,8 @@ __host__ __device__ __forceinline__ PwWork pw_carve(Carver& cv, const PwCaps& c)
   w.nbC = cv.take<int>(c.nQmax);
   w.labC = cv.take<int>(c.nQmax);
   w.cWin = cv.take<int>(c.nQmax);
+  w.cWinSI = cv.take<int>(c.nQmax);
+  w.nbCsi = cv.take<int>(c.nQmax);
   pw_pool(cv, c.capP, w.P, true);
   pw_pool(cv, c.capQ, w.Q, false);
   pw_pool(cv, c.capR, w.R, false);
@@ -721,6 +756,7 @@ struct PwPairArgs {
   const int* hstart;
   const PwHit* hits;
   const int* pass_of;  // null: every fast pair, pass 0
+  const int* order;    // pairs by decreasing expected work (warp w takes order[w])
   unsigned char* arena;
   const long long* aoff;
   int* status;  // per pair: PS_* code
@@ -731,8 +767,18 @@ struct PwPairArgs {
 
 // global slot s of the base's merged list: its sparse index, or -1 for a
 // plain vertex slot (then *vtx is the vertex)
-__device__ __forceinline__ int pw_slot(const PwWork& w, int nr, int s, int* vtx) {
-  int lo = 0, hi = nr;
+// (hint: a run index near the answer; the search is narrowed to runs
+// hint-1 .. hint+1 when they bracket s, and covers every run otherwise)
+__device__ __forceinline__ int pw_slot(const PwWork& w, int nr, int s, int* vtx, int hint = -1) {
+  auto start = [&](int k) { return w.re_e[k] + w.re_pre[k]; };
+  int lo = 0, hi = nr;  // the count of runs starting at or before s lies in [lo, hi]
+  if (hint >= 0) {
+    const int a = max(0, min(nr, hint - 1)), bnd = min(nr, hint + 2);
+    if ((a == 0 || start(a - 1) <= s) && (bnd == nr || start(bnd) > s)) {
+      lo = a;
+      hi = bnd;
+    }
+  }
   while (lo < hi) {
     const int m = (lo + hi) >> 1;
     if (w.re_e[m] + w.re_pre[m] <= s) lo = m + 1;
@@ -758,13 +804,10 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
   const double* c = A.cxy + 2 * o;
   const PwHit* H = A.hits + A.hstart[p];
   const int K = cp.K;
-  // ---- A9: records in the reference's order (base id, then first emission)
-  for (int i = 0; i < K; ++i) w.hord[i] = i;
-  merge_sort(w.hord, w.htmp, K, [&](int x, int y) {
-    return H[x].b != H[y].b ? H[x].b < H[y].b : H[x].key < H[y].key;
-  });
+  // ---- A9: records arrive in the reference's order (base id, then first
+  // emission), sorted for all pairs at once
   for (int i = 0; i < K; ++i) {
-    const PwHit& h = H[w.hord[i]];
+    const PwHit& h = H[i];
     w.ub[i] = 2 * h.b;
     w.uc[i] = 2 * h.j;
     w.ut[i] = h.type;
@@ -825,8 +868,8 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
     const int bi2 = bi + 1 == nb ? 0 : bi + 1, ci2 = ci + 1 == nc ? 0 : ci + 1;
     const double p1x = b[2 * bi], p1y = b[2 * bi + 1], p2x = b[2 * bi2], p2y = b[2 * bi2 + 1];
     const double q1x = c[2 * ci], q1y = c[2 * ci + 1], q2x = c[2 * ci2], q2y = c[2 * ci2 + 1];
-    double al = 0.0, bt = 0.0;
-    const int ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
+    const double al = H[i].al, bt = H[i].bt;  // lineSegmentIntersection of the candidate test
+    const int ty = ut[i];
     double x = 0.0, y = 0.0;
     if (ty == 1) {
       const double oma = dsub(1.0, al);
@@ -845,9 +888,17 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
     w.aC[i] = ty ? alpha_to_int(bt) : 0;
   }
   // ---- A12 per-edge alpha order (stable by alpha mod 1e9)
+  // (stable insertion for short runs; a long run -- an overlay edge across a
+  // jagged base can hold hundreds of crossings -- takes the stable merge sort)
   auto isort = [&](int s, int t, const int* alpha, const int* order, int* sorted) -> bool {
     for (int i = s; i < t; ++i)
       if (alpha[order ? order[i] : i] < 0) return false;
+    if (t - s > 32) {
+      merge_sort(sorted + s, w.htmp + s, t - s, [&](int x, int y) {
+        return alpha[order ? order[x] : x] % 1000000000 < alpha[order ? order[y] : y] % 1000000000;
+      });
+      return true;
+    }
     for (int i = s + 1; i < t; ++i) {
       const int pv = sorted[i];
       const int kp = alpha[order ? order[pv] : pv] % 1000000000;
@@ -887,6 +938,7 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
   for (int i = 0; i < nQ; ++i) {
     w.ixC[2 * i] = w.ixC[2 * i + 1] = 0.0;
     w.alC[i] = w.nbC[i] = 0;
+    w.nbCsi[i] = -1;
   }
   for (int id = 0; id < nc; ++id) {
     const int s = id + w.cND[id];
@@ -895,7 +947,10 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
     w.alC[s] = -100;
     w.nbC[s] = -100;
   }
-  for (int i = 0; i < K; ++i) w.bNI[i] = w.cNI[i] = 0;
+  for (int i = 0; i < K; ++i) {
+    w.bNI[i] = w.cNI[i] = 0;
+    w.bSI[i] = -1;  // the sparse index of bNI[i] once a slot is written
+  }
   // base runs (copyIntersectionsParallel per edge)
   for (int r = 0; r < nr; ++r) {
     const int e = w.re_e[r], s = w.re_s[r], pre = w.re_pre[r], si = w.re_si[r];
@@ -905,6 +960,7 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
     if (t == 2 || t == 4 || t == 6 || t == 8) {
       w.spal[si] = w.aB[lid];
       w.bNI[lid] = e + pre;
+      w.bSI[lid] = si;
       if (bid < K - 1) lid = w.sB[++bid];
     }
     if ((ub[lid] >> 1) != e) continue;
@@ -913,6 +969,7 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
       w.spy[si + 1 + q] = w.isxy[2 * lid + 1];
       w.spal[si + 1 + q] = w.aB[lid];
       w.bNI[lid] = pre + e + 1 + q;
+      w.bSI[lid] = si + 1 + q;
       if (bid < K - 1) lid = w.sB[++bid];
     }
   }
@@ -942,17 +999,25 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
     }
   }
   // neighbours: the last record written to a slot wins
+  int si0 = -3;  // sparse index of slot 0, where records never written point
   for (int i = 0; i < K; ++i) {
-    int vtx;
-    const int si = pw_slot(w, nr, w.bNI[i], &vtx);
+    int si = w.bSI[i];
+    if (si < 0) {
+      if (si0 == -3) {
+        int vtx;
+        si0 = pw_slot(w, nr, 0, &vtx);
+      }
+      si = si0;
+    }
     if (si < 0) return PS_FALLBACK;  // a plain slot would change
     w.spnb[si] = w.cNI[i] + 1;
     w.nbC[w.cNI[i]] = w.bNI[i] + 1;
+    w.nbCsi[w.cNI[i]] = si;
   }
   // slot contents of the base's merged list
-  auto info = [&](int s, double* x, double* y, int* al, int* nbv) {
+  auto info = [&](int s, int hint, double* x, double* y, int* al, int* nbv) {
     int vtx = 0;
-    const int si = pw_slot(w, nr, s, &vtx);
+    const int si = pw_slot(w, nr, s, &vtx, hint);
     if (si >= 0) {
       *x = w.spx[si];
       *y = w.spy[si];
@@ -977,8 +1042,8 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
       const int tp = (i + 1 == nB) ? 0 : i + 1;
       double pmx, pmy, ppx, ppy;
       int alm, nbm, alp, nbp;
-      info(tm, &pmx, &pmy, &alm, &nbm);
-      info(tp, &ppx, &ppy, &alp, &nbp);
+      info(tm, r, &pmx, &pmy, &alm, &nbm);
+      info(tp, r, &ppx, &ppy, &alp, &nbp);
       const int pMN = alm != -100 ? nbm - 1 : -100;
       const int pPN = alp != -100 ? nbp - 1 : -100;
       const int nId = w.spnb[si] - 1;
@@ -1013,17 +1078,15 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
       else lab = -102;
       w.splab[si] = lab;
       if (nId < 0 || nId >= nQ) return PS_FALLBACK;
-      w.cWin[nId] = max(w.cWin[nId], i);
+      if (i >= w.cWin[nId]) {  // slots come in increasing order: the last one wins
+        w.cWin[nId] = i;
+        w.cWinSI[nId] = si;
+      }
     }
   }
   for (int q = 0; q < nQ; ++q) {
     w.labC[q] = 0;
-    if (w.cWin[q] >= 0) {
-      int vtx;
-      const int si = pw_slot(w, nr, w.cWin[q], &vtx);
-      if (si < 0) return PS_FALLBACK;
-      w.labC[q] = w.splab[si];
-    }
+    if (w.cWin[q] >= 0) w.labC[q] = w.splab[w.cWinSI[q]];
   }
   // ---- A15 linked lists (copyToLinkedList, src/clip.cpp:606-695): the base's
   // with run nodes for its stretches of plain vertices
@@ -1069,11 +1132,11 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
         const int s = i % nB;
         double sx, sy;
         int sal, snb;
-        info(s, &sx, &sy, &sal, &snb);
+        info(s, r, &sx, &sy, &sal, &snb);
         if (sx == vx && sy == vy) break;
         if (i >= nB) return PS_UNDEF;
         int vtx;
-        const int si = pw_slot(w, nr, s, &vtx);
+        const int si = pw_slot(w, nr, s, &vtx, r);
         if (si < 0) return PS_FALLBACK;
         const int v = pnew(P, sx, sy);
         if (v < 0) return PS_CAP;
@@ -1088,7 +1151,7 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
         if (vn != i) return PS_UNDEF;
         if (i != ii + w.re_pre[r]) return PS_FALLBACK;  // stopped at another slot
         int vtx;
-        const int si = pw_slot(w, nr, i, &vtx);
+        const int si = pw_slot(w, nr, i, &vtx, r);
         if (si >= 0) {
           const int v = pnew(P, vx, vy);
           if (v < 0) return PS_CAP;
@@ -1125,8 +1188,7 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
         Q.isect[v] = 1;
         const int t = w.nbC[i] - 1;
         if (t < 0 || t >= nB) return PS_UNDEF;
-        int vtx;
-        const int si = pw_slot(w, nr, t, &vtx);
+        const int si = w.nbCsi[i];
         if (si < 0 || w.spnode[si] < 0) return PS_FALLBACK;
         Q.nb[v] = w.spnode[si];
         P.nb[w.spnode[si]] = v;
@@ -1140,8 +1202,7 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
         if (w.nbC[i] != -100) {
           const int t = w.nbC[i] - 1;
           if (t < 0 || t >= nB) return PS_UNDEF;
-          int vtx;
-          const int si = pw_slot(w, nr, t, &vtx);
+          const int si = w.nbCsi[i];
           if (si < 0 || w.spnode[si] < 0) return PS_FALLBACK;
           Q.isect[v] = 1;
           Q.nb[v] = w.spnode[si];
@@ -1225,9 +1286,13 @@ __global__ void k_pw_sizes(int nov, const long long* __restrict__ coff, int nb,
   bytes[p] = run ? (long long)pw_arena_bytes(nb, (int)(coff[p + 1] - coff[p]), pairK[p], pass) : 0;
 }
 
+// One pair per warp, run by its first lane: the back end is serial, and the
+// 32 pairs of a warp would otherwise take turns through diverging paths.
 __global__ void __launch_bounds__(kPwPairBlock) k_pw_pairs(PwPairArgs A, const int* __restrict__ pairK) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= A.nov) return;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int wi = (int)(t >> 5);
+  if ((threadIdx.x & 31) != 0 || wi >= A.nov) return;
+  const int p = A.order[wi];
   const int pass = A.pass_of ? A.pass_of[p] : 0;
   if (pass < 0) return;
   if (A.pp[p].mode != PW_FAST) {
@@ -1278,11 +1343,21 @@ __global__ void k_pw_pack(int nov, const long long* __restrict__ coff, int nb,
 }  // namespace
 
 // ------------------------------------------------------------------ host
+PairwiseRunner::~PairwiseRunner() {
+  if (st2_) {
+    cudaStreamSynchronize(st2_);
+    cudaStreamDestroy(st2_);
+  }
+  for (auto e : ev_)
+    if (e) cudaEventDestroy(e);
+}
+
 int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cxy,
                         const long long* d_coff, cudaStream_t st) {
   BufferPool& pool = pl_.pool();
   np = nov;
   fallback_pairs = 0;
+  big_pairs = 0;
   hits = 0;
   tested = 0;
   if (nb < 3) return pl_.fail(kEInput, "base needs at least 3 vertices");
@@ -1410,7 +1485,6 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
   // ---- candidates
   int* pairK = (int*)pool.get("pw_pairk", sizeof(int) * (nov + 1));
   int* hstart = (int*)pool.get("pw_hstart", sizeof(int) * (nov + 1));
-  int* hcur = (int*)pool.get("pw_hcur", sizeof(int) * (nov + 1));
   auto* cnt = (unsigned long long*)pool.get("pw_counters", 256);
   if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise)");
   unsigned long long cap = std::max<unsigned long long>(hit_cap_, 1ull << 16);
@@ -1441,49 +1515,157 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
   cudaMemcpyAsync(hstart, pairK, sizeof(int) * (nov + 1), cudaMemcpyDeviceToDevice, st);
   exclusive_scan_i32(hstart, nov + 1, sscr, st);
   PwHit* grouped = (PwHit*)pool.get("pw_hits_grouped", sizeof(PwHit) * (nh + 1));
+  auto* hk = (unsigned long long*)pool.get("pw_hk", sizeof(unsigned long long) * (nh + 1));
+  auto* hk2 = (unsigned long long*)pool.get("pw_hk2", sizeof(unsigned long long) * (nh + 1));
+  auto* hv = (unsigned*)pool.get("pw_hv", sizeof(unsigned) * (nh + 1));
+  auto* hv2 = (unsigned*)pool.get("pw_hv2", sizeof(unsigned) * (nh + 1));
+  void* hscr = pool.get("pw_hscr", radix_scratch_bytes((long long)nh + 1));
   if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise hits)");
-  cudaMemsetAsync(hcur, 0, sizeof(int) * (nov + 1), st);
   if (nh) {
-    ::sbc::KProbe kp_("k_pw_group", st);
-    k_pw_group<<<grid_for((long long)nh, 256), 256, 0, st>>>(nh, hbuf, hstart, hcur, grouped);
+    {
+      ::sbc::KProbe kp_("k_pw_hit_keys", st, 52.0 * (double)nh);
+      k_pw_hit_keys<<<grid_for((long long)nh, 256), 256, 0, st>>>((long long)nh, hbuf, hk, hv);
+    }
+    radix_sort_u64(hk, hv, hk2, hv2, (long long)nh, hscr, st);
+    {
+      ::sbc::KProbe kp_("k_pw_hit_keys2", st, 20.0 * (double)nh);
+      k_pw_hit_keys2<<<grid_for((long long)nh, 256), 256, 0, st>>>((long long)nh, hbuf, hv, hk);
+    }
+    radix_sort_u64(hk, hv, hk2, hv2, (long long)nh, hscr, st);
+    {
+      ::sbc::KProbe kp_("k_pw_gather", st, 84.0 * (double)nh);
+      k_pw_gather<<<grid_for((long long)nh, 256), 256, 0, st>>>((long long)nh, hbuf, hv, grouped);
+    }
   }
-  // ---- one thread per pair: pass 0, then pairs that ran out of ring room
+  // ---- pairs with many intersections take the pair pipeline's data-parallel
+  // rows A9-A18 on these records (no tree); the rest run one thread per pair,
+  // on a second stream at the same time.  Then pairs that ran out of ring
+  // room run again with full room.
   long long* aoff0 = (long long*)pool.get("pw_aoff0", sizeof(long long) * (nov + 1));
   long long* aoff1 = (long long*)pool.get("pw_aoff1", sizeof(long long) * (nov + 1));
   int* pass = (int*)pool.get("pw_pass", sizeof(int) * (nov + 1));
   int* nrings = (int*)pool.get("pw_nrings", sizeof(int) * (nov + 1));
   int* nverts = (int*)pool.get("pw_nverts", sizeof(int) * (nov + 1));
   if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise)");
-  PwPip pip{d_bxy, nb, g, gstart, gent, lng, 0, fbox, nullptr, 0};
+  std::vector<int> hK(nov + 1);
+  std::vector<PwPair> hpp(nov);
   unsigned hlong = 0;
+  cudaMemcpyAsync(hK.data(), pairK, sizeof(int) * nov, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(hpp.data(), pp, sizeof(PwPair) * nov, cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(&hlong, nlong, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise counts");
+  std::vector<int> hpass(nov, 0), is_big(nov, 0);
+  std::vector<long long> hstart_h(nov + 1, 0);
+  int maxBig = 0;
+  big_pairs = 0;
+  for (int p = 0; p < nov; ++p) {
+    hstart_h[p + 1] = hstart_h[p] + hK[p];
+    if (hpp[p].mode == PW_FAST && hK[p] >= big_k) {
+      is_big[p] = 1;
+      hpass[p] = -1;
+      maxBig = std::max(maxBig, hK[p]);
+      ++big_pairs;
+    }
+  }
+  cudaMemcpyAsync(pass, hpass.data(), sizeof(int) * nov, cudaMemcpyHostToDevice, st);
+  // longest first: the warps that start first take the pairs with the most
+  // records and vertices
+  {
+    std::vector<long long> cost(nov);
+    order_h.resize(nov);
+    for (int p = 0; p < nov; ++p) {
+      order_h[p] = p;
+      cost[p] = 8LL * hK[p] + (hoff[p + 1] - hoff[p]);
+    }
+    std::stable_sort(order_h.begin(), order_h.end(),
+                     [&](int a, int b) { return cost[a] > cost[b]; });
+  }
+  int* order = (int*)pool.get("pw_order", sizeof(int) * (nov + 1));
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise)");
+  cudaMemcpyAsync(order, order_h.data(), sizeof(int) * nov, cudaMemcpyHostToDevice, st);
+  PwPip pip{d_bxy, nb, g, gstart, gent, lng, (int)hlong, fbox, nullptr, 0};
   {
     ::sbc::KProbe kp_("k_pw_sizes", st);
-    k_pw_sizes<<<grid_for(nov + 1, 256), 256, 0, st>>>(nov, d_coff, nb, pp, pairK, nullptr, aoff0);
+    k_pw_sizes<<<grid_for(nov + 1, 256), 256, 0, st>>>(nov, d_coff, nb, pp, pairK, pass, aoff0);
   }
   exclusive_scan_i64(aoff0, nov + 1, sscr, st);
   long long total = 0;
   cudaMemcpyAsync(&total, aoff0 + nov, sizeof(long long), cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise sizes");
-  pip.nlong = (int)hlong;
   unsigned char* arena0 = (unsigned char*)pool.get("pw_arena0", (size_t)total + 256);
+  int* brb = (int*)pool.get("pw_big_rb", sizeof(int) * (maxBig + 1));
+  int* brc = (int*)pool.get("pw_big_rc", sizeof(int) * (maxBig + 1));
+  int* brt = (int*)pool.get("pw_big_rt", sizeof(int) * (maxBig + 1));
+  auto* bkey = (unsigned long long*)pool.get("pw_big_key", sizeof(unsigned long long) * (maxBig + 1));
   if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise arena)");
-  PwPairArgs pa{nov, d_coff, d_cxy, d_bxy, nb, pp, hstart, grouped, nullptr, arena0, aoff0,
+  if (!st2_ && cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking) != cudaSuccess)
+    return pl_.fail(kECuda, "pairwise stream");
+  if (!ev_[0] && (cudaEventCreateWithFlags(&ev_[0], cudaEventDisableTiming) != cudaSuccess ||
+                  cudaEventCreateWithFlags(&ev_[1], cudaEventDisableTiming) != cudaSuccess))
+    return pl_.fail(kECuda, "pairwise events");
+  PwPairArgs pa{nov, d_coff, d_cxy, d_bxy, nb, pp, hstart, grouped, pass, order, arena0, aoff0,
                 status, nrings, nverts, pip};
+  cudaEventRecord(ev_[0], st);
+  cudaStreamWaitEvent(st2_, ev_[0], 0);
   {
     // coordinates and records in; rings out
-    ::sbc::KProbe kp_("k_pw_pairs", st, 16.0 * totalC + 24.0 * (double)nh);
-    k_pw_pairs<<<grid_for(nov, kPwPairBlock), kPwPairBlock, 0, st>>>(pa, pairK);
+    ::sbc::KProbe kp_("k_pw_pairs", st2_, 16.0 * totalC + 40.0 * (double)nh);
+    k_pw_pairs<<<grid_for(32LL * nov, kPwPairBlock), kPwPairBlock, 0, st2_>>>(pa, pairK);
   }
-  std::vector<int> hst(nov), hpass(nov, -1);
+  cudaEventRecord(ev_[1], st2_);
+  struct Stash {
+    std::vector<int> off;
+    std::vector<double> xy;
+  };
+  std::vector<Stash> stash(nov);
+  std::vector<int> stash_of(nov, -1), hnr(nov, 0), hnv(nov, 0), fast(nov, 0);
+  auto keep = [&](int p) -> int {
+    const auto& out = pl_.outputs()[0];
+    Stash& sh = stash[p];
+    sh.off.assign(out.nrings + 1, 0);
+    sh.xy.resize(2 * out.nverts);
+    if (out.nrings > 0)
+      cudaMemcpyAsync(sh.off.data(), out.d_off, sizeof(int) * (out.nrings + 1),
+                      cudaMemcpyDeviceToHost, st);
+    if (out.nverts > 0)
+      cudaMemcpyAsync(sh.xy.data(), out.d_xy, sizeof(double) * 2 * out.nverts,
+                      cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise pipeline");
+    hnr[p] = out.nrings;
+    hnv[p] = (int)out.nverts;
+    stash_of[p] = p;
+    return kOk;
+  };
+  for (int p = 0; p < nov; ++p) {
+    if (!is_big[p]) continue;
+    const int K = hK[p];
+    {
+      ::sbc::KProbe kp_("k_pw_split", st, 72.0 * K);
+      k_pw_split<<<grid_for(K, 256), 256, 0, st>>>(K, grouped + hstart_h[p], brb, brc, brt, bkey);
+    }
+    pl_.clear_error();
+    const int rc = pl_.run_from_hits(d_bxy, nb, d_cxy + 2 * hoff[p], (int)(hoff[p + 1] - hoff[p]),
+                                     brb, brc, brt, bkey, K);
+    if (rc == kEInput || rc == kEUndef) {
+      h_status[p] = rc == kEInput ? SBC_EINPUT : SBC_EUNDEF;
+      continue;
+    }
+    if (rc) return rc;
+    const int k2 = keep(p);
+    if (k2) return k2;
+  }
+  cudaStreamWaitEvent(st, ev_[1], 0);
+  std::vector<int> hst(nov);
   cudaMemcpyAsync(hst.data(), status, sizeof(int) * nov, cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise clip");
   int retry = 0;
-  for (int p = 0; p < nov; ++p)
-    if (hst[p] == PS_CAP) {
+  for (int p = 0; p < nov; ++p) {
+    hpass[p] = -1;
+    if (!is_big[p] && hst[p] == PS_CAP) {
       hpass[p] = 1;
       ++retry;
     }
+  }
   unsigned char* arena1 = arena0;
   if (retry) {
     cudaMemcpyAsync(pass, hpass.data(), sizeof(int) * nov, cudaMemcpyHostToDevice, st);
@@ -1496,35 +1678,30 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
     if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise sizes");
     arena1 = (unsigned char*)pool.get("pw_arena1", (size_t)total + 256);
     if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise arena)");
-    pa.pass_of = pass;
     pa.arena = arena1;
     pa.aoff = aoff1;
     {
       ::sbc::KProbe kp_("k_pw_pairs", st);
-      k_pw_pairs<<<grid_for(nov, kPwPairBlock), kPwPairBlock, 0, st>>>(pa, pairK);
+      k_pw_pairs<<<grid_for(32LL * nov, kPwPairBlock), kPwPairBlock, 0, st>>>(pa, pairK);
     }
     cudaMemcpyAsync(hst.data(), status, sizeof(int) * nov, cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise clip");
   }
   for (int p = 0; p < nov; ++p) hpass[p] = hpass[p] == 1 ? 1 : 0;
   cudaMemcpyAsync(pass, hpass.data(), sizeof(int) * nov, cudaMemcpyHostToDevice, st);
-  // ---- per pair: fast result, input error, or the pair pipeline
-  std::vector<int> hnr(nov), hnv(nov), fast(nov, 0);
-  cudaMemcpyAsync(hnr.data(), nrings, sizeof(int) * nov, cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(hnv.data(), nverts, sizeof(int) * nov, cudaMemcpyDeviceToHost, st);
+  // ---- per pair: fast result, input error, or the whole pair pipeline
+  std::vector<int> fnr(nov), fnv(nov);
+  cudaMemcpyAsync(fnr.data(), nrings, sizeof(int) * nov, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(fnv.data(), nverts, sizeof(int) * nov, cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise clip");
-  struct Stash {
-    std::vector<int> off;
-    std::vector<double> xy;
-  };
-  std::vector<Stash> stash(nov);
-  std::vector<int> stash_of(nov, -1);
   for (int p = 0; p < nov; ++p) {
+    if (is_big[p]) continue;
     if (hst[p] == PS_OK) {
       fast[p] = 1;
+      hnr[p] = fnr[p];
+      hnv[p] = fnv[p];
       continue;
     }
-    hnr[p] = hnv[p] = 0;
     const long long n = hoff[p + 1] - hoff[p];
     if (hst[p] == PS_UNDEF + 100 || n < 3) {
       h_status[p] = SBC_EINPUT;
@@ -1540,20 +1717,8 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
       continue;
     }
     if (rc) return rc;
-    const auto& out = pl_.outputs()[0];
-    Stash& s = stash[p];
-    s.off.resize(out.nrings + 1, 0);
-    s.xy.resize(2 * out.nverts);
-    if (out.nrings > 0)
-      cudaMemcpyAsync(s.off.data(), out.d_off, sizeof(int) * (out.nrings + 1),
-                      cudaMemcpyDeviceToHost, st);
-    if (out.nverts > 0)
-      cudaMemcpyAsync(s.xy.data(), out.d_xy, sizeof(double) * 2 * out.nverts,
-                      cudaMemcpyDeviceToHost, st);
-    if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise fallback");
-    hnr[p] = out.nrings;
-    hnv[p] = (int)out.nverts;
-    stash_of[p] = p;
+    const int k2 = keep(p);
+    if (k2) return k2;
   }
   pl_.clear_error();
   // ---- packed output

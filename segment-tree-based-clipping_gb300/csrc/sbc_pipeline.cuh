@@ -119,6 +119,14 @@ class Pipeline {
   int stage_candidates(int cType, int** rb, int** rc, int** rt, unsigned long long** rkey,
                        long long* nhits, OverlayOut& out);
   int stage_overlay(int cType, OverlayOut& out);
+  int stage_records(int cType, const int* rb, const int* rc, const int* rt,
+                    const unsigned long long* rkey, long long nraw, OverlayOut& out,
+                    bool unique_sorted = false);
+  // one pair's rows A10-A18 from its unique candidate hits in A9's order
+  // (base id, then first-emission key; no tree): the same rings as run() on
+  // that pair when the hits are the pair's own
+  int run_from_hits(const double* d_bxy, int nb, const double* d_cxy, int nc, const int* rb,
+                    const int* rc, const int* rt, const unsigned long long* rkey, long long nhits);
 
   int fail(int code, const std::string& msg) {
     if (err_.empty()) err_ = msg;
@@ -189,6 +197,7 @@ class BatchRunner {
 class PairwiseRunner {
  public:
   explicit PairwiseRunner(Pipeline& pl) : pl_(pl) {}
+  ~PairwiseRunner();
   int run(const double* d_bxy, int nb, int nov, const double* d_cxy, const long long* d_coff,
           cudaStream_t st);
   int np = 0;
@@ -200,13 +209,18 @@ class PairwiseRunner {
   std::vector<int> h_status;
   std::vector<long long> h_pair_ring;
   // diagnostics of the last run
-  int fallback_pairs = 0;           // pairs clipped by the pair pipeline
+  int fallback_pairs = 0;           // pairs clipped by the whole pair pipeline
+  int big_pairs = 0;                // pairs whose records went to its rows A9-A18
+  int big_k = 8192;                 // records from which a pair counts as big
   long long hits = 0, tested = 0, grid_cells = 0;
   double cell_factor = 1.0;         // grid cell width in units of sqrt(area / n_b)
 
  private:
   Pipeline& pl_;
   unsigned long long hit_cap_ = 0;
+  cudaStream_t st2_ = nullptr;      // the one-thread-per-pair kernel's stream
+  cudaEvent_t ev_[2] = {nullptr, nullptr};
+  std::vector<int> order_h;
 };
 
 }  // namespace sbc

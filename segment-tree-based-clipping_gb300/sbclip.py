@@ -130,6 +130,7 @@ def load_library(path: str | os.PathLike | None = None):
                                    vp]
     L.sbc_pairwise_info.argtypes = [vp, ctypes.POINTER(ll), i]
     L.sbc_pairwise_set_cell_factor.argtypes = [vp, ctypes.c_double]
+    L.sbc_pairwise_set_split.argtypes = [vp, i]
     L.sbc_trace_rings_noalloc.argtypes = [ctypes.POINTER(_MergedLists), vp, i, vp, ll,
                                           ctypes.POINTER(i), ctypes.POINTER(ll), vp,
                                           ctypes.c_char_p, i]
@@ -290,13 +291,38 @@ class Clipper:
 
     def clip_pairwise(self, base, overlays, stream: int | None = None):
         """`seg base overlay_i` for every overlay: (list of ring lists, status array)."""
-        bxy = np.ascontiguousarray(base, dtype=np.float64).reshape(-1, 2)
         cxy, coff = pack_polygons(overlays)
-        j = _PairwiseJob(bxy.ctypes.data, bxy.shape[0], len(overlays), cxy.ctypes.data,
+        r = self._pairwise(base, cxy, coff, stream)
+        return self._unpack_rings(r, len(overlays))
+
+    def _pairwise(self, base, cxy, coff, stream):
+        bxy = np.ascontiguousarray(base, dtype=np.float64).reshape(-1, 2)
+        cxy = np.ascontiguousarray(cxy, dtype=np.float64)
+        coff = np.ascontiguousarray(coff, dtype=np.int64)
+        j = _PairwiseJob(bxy.ctypes.data, bxy.shape[0], len(coff) - 1, cxy.ctypes.data,
                          coff.ctypes.data)
         r = _BatchRings()
         self._check(self._L.sbc_clip_pairwise(self._h, ctypes.byref(j), ctypes.byref(r), stream))
-        return self._unpack_rings(r, len(overlays))
+        return r
+
+    def clip_pairwise_flat(self, base, cxy, coff, stream: int | None = None, copy: bool = True):
+        """sbc_clip_pairwise on packed overlays (pack_polygons): (pair_ring,
+        ring_off, xy, status) arrays; with copy=False, views of the context's
+        result memory valid until the next call (what a C caller receives)."""
+        r = self._pairwise(base, cxy, coff, stream)
+        n = len(coff) - 1
+
+        def view(ptr, ct, count):
+            if count <= 0:
+                return np.zeros(0, np.int64 if ct is ctypes.c_longlong else
+                                (np.int32 if ct is ctypes.c_int else np.float64))
+            a = np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ct)), (count,))
+            return a.copy() if copy else a
+
+        return (view(r.pair_ring, ctypes.c_longlong, n + 1),
+                view(r.ring_off, ctypes.c_longlong, int(r.nrings) + 1),
+                view(r.xy, ctypes.c_double, 2 * int(r.nverts)).reshape(-1, 2),
+                view(r.status, ctypes.c_int, n))
 
     def clip_pairwise_device(self, d_bxy, nb, noverlays, d_cxy, d_coff,
                              stream: int | None = None):
@@ -309,12 +335,16 @@ class Clipper:
 
     def pairwise_info(self) -> dict:
         """Diagnostics of the last pairwise call."""
-        v = (ctypes.c_longlong * 4)()
-        self._L.sbc_pairwise_info(self._h, v, 4)
-        return {"fallback_pairs": v[0], "unique": v[1], "tested": v[2], "grid_cells": v[3]}
+        v = (ctypes.c_longlong * 5)()
+        self._L.sbc_pairwise_info(self._h, v, 5)
+        return {"fallback_pairs": v[0], "unique": v[1], "tested": v[2], "grid_cells": v[3],
+                "big_pairs": v[4]}
 
     def set_pairwise_cell_factor(self, f: float) -> None:
         self._check(self._L.sbc_pairwise_set_cell_factor(self._h, float(f)))
+
+    def set_pairwise_split(self, records: int) -> None:
+        self._check(self._L.sbc_pairwise_set_split(self._h, int(records)))
 
     def area_forward(self, bases, overlays, stream: int | None = None):
         """Intersection area of every pair: (area, status)."""

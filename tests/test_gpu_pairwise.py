@@ -59,6 +59,29 @@ def test_pairwise_cell_factor_does_not_change_results(clipper):
         assert all(rings_equal(a, b) for a, b in zip(got, ref))
 
 
+def test_pairwise_split_does_not_change_results(clipper):
+    """Every overlay with at least one record through the data-parallel rows
+    A9-A18, then none: the same rings as the default split."""
+    base, ovs = gen.one_to_many(n_base=8_000, n_overlays=150, seed=3250, hi=1500,
+                                near_boundary=0.7)
+    ref, _ = clipper.clip_pairwise(base, ovs)
+    try:
+        for split in (1, 1 << 30):
+            clipper.set_pairwise_split(split)
+            got, st = clipper.clip_pairwise(base, ovs)
+            assert (st == 0).all()
+            info = clipper.pairwise_info()
+            if split == 1:
+                assert info["big_pairs"] > 50, info
+            else:
+                assert info["big_pairs"] == 0, info
+            assert all(rings_equal(a, b) for a, b in zip(got, ref))
+    finally:
+        clipper.set_pairwise_split(8192)
+    for i in range(0, len(ovs), 10):
+        assert rings_equal(ref[i], clipper.clip_pair(base, ovs[i])), i
+
+
 def test_pairwise_special_overlays(clipper):
     base = gen.jagged_star(3_000, 3300, R=1000.0)
     b0 = base[0]
