@@ -496,6 +496,10 @@ def run_one_to_many(args, rank: int, world: int):
         return clip.clip_pairwise_device(tb.data_ptr(), len(base), nov, tc.data_ptr(),
                                          to.data_ptr(), sp)
 
+    # the autotuner picks the big-pair split and the grid cell width (outside
+    # the timed region; results do not depend on them)
+    tuned = clip.autotune_pairwise_device(tb.data_ptr(), len(base), nov, tc.data_ptr(),
+                                          to.data_ptr(), sp)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -572,13 +576,16 @@ def run_one_to_many(args, rank: int, world: int):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded star polygons)",
         "config": dict(desc, parallelism="replicas" if world > 1 else "single",
-                       l2="flushed between steps (256 MiB write)"),
+                       l2="flushed between steps (256 MiB write)",
+                       autotuned={"big_pair_split_records": tuned["split"],
+                                  "grid_cell_factor": tuned["cell_factor"]}),
         "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
         "kernels_top": {k: {"ms_per_step": v[0], "launches_per_step": v[1]}
                         for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])[:8]},
         "clocks": clk.summary(),
         "counts": {"pairs_ok": n_ok, "rings": nr, "ring_vertices": nv,
                    "pairs_by_pair_pipeline": info["fallback_pairs"],
+                   "pairs_by_pipeline_rows_a10_a18": info["big_pairs"],
                    "unique_intersections": info["unique"],
                    "box_overlapping_edge_pairs_tested": info["tested"],
                    "edge_pairs_tested_per_s": info["tested"] / (ms * 1e-3),

@@ -217,6 +217,12 @@ int sbc_pairwise_set_cell_factor(sbc_ctx* ctx, double factor);
  * one-thread-per-pair back end for the data-parallel one; default 8192.  A
  * tuning knob: results do not depend on it. */
 int sbc_pairwise_set_split(sbc_ctx* ctx, int records);
+/* Autotuner: runs the job (device arrays, as for sbc_clip_pairwise_device)
+ * under several splits and cell widths, keeps the fastest setting in the
+ * context and reports it (any output may be NULL).  The rings of the last run
+ * are left as sbc_clip_pairwise_device would leave them. */
+int sbc_pairwise_autotune(sbc_ctx* ctx, const sbc_pairwise_job* job, int* split,
+                          double* cell_factor, double* best_ms, void* stream);
 
 /* Allocation-free ring tracing.  No counterpart in the reference: it exists
  * for callers that are not allowed to allocate device memory themselves or

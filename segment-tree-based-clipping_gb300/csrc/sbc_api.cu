@@ -733,3 +733,18 @@ extern "C" int sbc_pairwise_set_split(sbc_ctx* c, int records) {
   c->pw->big_k = records;
   return SBC_OK;
 }
+
+extern "C" int sbc_pairwise_autotune(sbc_ctx* c, const sbc_pairwise_job* j, int* split,
+                                     double* cell_factor, double* best_ms, void* stream) {
+  int rc = pairwise_check(c, j);
+  if (rc) return rc;
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  c->pl->set_stream(st);
+  c->pl->clear_error();
+  rc = c->pw->autotune(j->b_xy, j->nb, j->noverlays, j->c_xy, j->c_off, st, best_ms);
+  if (rc) return set_err(c, rc, c->pl->error());
+  if (split) *split = c->pw->big_k;
+  if (cell_factor) *cell_factor = c->pw->cell_factor;
+  return SBC_OK;
+}

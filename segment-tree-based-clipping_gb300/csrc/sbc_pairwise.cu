@@ -39,6 +39,7 @@
 // against it adds the winding steps of the run-internal base edges from one
 // row of the grid.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1286,29 +1287,34 @@ __global__ void k_pw_sizes(int nov, const long long* __restrict__ coff, int nb,
   bytes[p] = run ? (long long)pw_arena_bytes(nb, (int)(coff[p + 1] - coff[p]), pairK[p], pass) : 0;
 }
 
-// One pair per warp, run by its first lane: the back end is serial, and the
-// 32 pairs of a warp would otherwise take turns through diverging paths.
-__global__ void __launch_bounds__(kPwPairBlock) k_pw_pairs(PwPairArgs A, const int* __restrict__ pairK) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int wi = (int)(t >> 5);
-  if ((threadIdx.x & 31) != 0 || wi >= A.nov) return;
-  const int p = A.order[wi];
-  const int pass = A.pass_of ? A.pass_of[p] : 0;
-  if (pass < 0) return;
-  if (A.pp[p].mode != PW_FAST) {
-    A.status[p] = A.pp[p].mode == PW_INPUT ? PS_UNDEF + 100 : PS_FALLBACK;
-    A.nrings[p] = A.nverts[p] = 0;
-    return;
+// Persistent work queue, one pair per warp at a time run by the warp's first
+// lane (the back end is serial; 32 pairs sharing a warp would take turns
+// through diverging paths).  The queue hands out pairs by decreasing expected
+// work; a warp takes the next one until the queue is empty.
+__global__ void __launch_bounds__(kPwPairBlock)
+k_pw_pairs(PwPairArgs A, const int* __restrict__ pairK, int* __restrict__ queue) {
+  if ((threadIdx.x & 31) != 0) return;
+  for (;;) {
+    const int wi = atomicAdd(queue, 1);
+    if (wi >= A.nov) return;
+    const int p = A.order[wi];
+    const int pass = A.pass_of ? A.pass_of[p] : 0;
+    if (pass < 0) continue;
+    if (A.pp[p].mode != PW_FAST) {
+      A.status[p] = A.pp[p].mode == PW_INPUT ? PS_UNDEF + 100 : PS_FALLBACK;
+      A.nrings[p] = A.nverts[p] = 0;
+      continue;
+    }
+    const int nc = (int)(A.coff[p + 1] - A.coff[p]);
+    const PwCaps cp = pw_caps(A.nb, nc, pairK[p], pass);
+    Carver cv{A.arena + A.aoff[p], 0};
+    PwWork w = pw_carve(cv, cp);
+    int nr = 0, nv = 0;
+    const int st = pw_clip_pair(A, p, cp, w, &nr, &nv);
+    A.status[p] = st;
+    A.nrings[p] = st == PS_OK ? nr : 0;
+    A.nverts[p] = st == PS_OK ? nv : 0;
   }
-  const int nc = (int)(A.coff[p + 1] - A.coff[p]);
-  const PwCaps cp = pw_caps(A.nb, nc, pairK[p], pass);
-  Carver cv{A.arena + A.aoff[p], 0};
-  PwWork w = pw_carve(cv, cp);
-  int nr = 0, nv = 0;
-  const int st = pw_clip_pair(A, p, cp, w, &nr, &nv);
-  A.status[p] = st;
-  A.nrings[p] = st == PS_OK ? nr : 0;
-  A.nverts[p] = st == PS_OK ? nv : 0;
 }
 
 // where a pair's rings live: pass 0 arena, or the retry arena
@@ -1343,6 +1349,59 @@ __global__ void k_pw_pack(int nov, const long long* __restrict__ coff, int nb,
 }  // namespace
 
 // ------------------------------------------------------------------ host
+// resident warps of the per-pair kernel (the whole GPU), at most one per pair
+unsigned PairwiseRunner::pair_grid(int nov) {
+  if (pair_blocks_ == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pw_pairs, kPwPairBlock, 0);
+    pair_blocks_ = (unsigned)std::max(1, sms * std::max(1, per_sm));
+  }
+  const unsigned need = grid_for(32LL * nov, kPwPairBlock);
+  return need < pair_blocks_ ? need : pair_blocks_;
+}
+
+// Time the job under a few settings of the big-pair split and the grid cell
+// width and keep the fastest (results do not depend on either): the split
+// first at the current cell width, then the cell width at the best split.
+int PairwiseRunner::autotune(const double* d_bxy, int nb, int nov, const double* d_cxy,
+                             const long long* d_coff, cudaStream_t st, double* best_ms) {
+  auto timed = [&](double* ms) -> int {
+    const auto t0 = std::chrono::steady_clock::now();
+    const int rc = run(d_bxy, nb, nov, d_cxy, d_coff, st);
+    *ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+  };
+  double ms = 0;
+  int rc = timed(&ms);  // warm-up: buffers grow to size
+  if (rc) return rc;
+  int best_split = big_k;
+  double best_cell = cell_factor, best = 1e300;
+  for (int split : {2048, 4096, 8192, 16384, 32768}) {
+    big_k = split;
+    rc = timed(&ms);
+    if (rc) return rc;
+    if (ms < best) {
+      best = ms;
+      best_split = split;
+    }
+  }
+  big_k = best_split;
+  for (double f : {0.5, 2.0}) {
+    cell_factor = f;
+    rc = timed(&ms);
+    if (rc) return rc;
+    if (ms < best) {
+      best = ms;
+      best_cell = f;
+    }
+  }
+  cell_factor = best_cell;
+  if (best_ms) *best_ms = best;
+  return kOk;
+}
+
 PairwiseRunner::~PairwiseRunner() {
   if (st2_) {
     cudaStreamSynchronize(st2_);
@@ -1581,8 +1640,10 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
                      [&](int a, int b) { return cost[a] > cost[b]; });
   }
   int* order = (int*)pool.get("pw_order", sizeof(int) * (nov + 1));
+  int* queue = (int*)pool.get("pw_queue", 256);
   if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise)");
   cudaMemcpyAsync(order, order_h.data(), sizeof(int) * nov, cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(queue, 0, 2 * sizeof(int), st);
   PwPip pip{d_bxy, nb, g, gstart, gent, lng, (int)hlong, fbox, nullptr, 0};
   {
     ::sbc::KProbe kp_("k_pw_sizes", st);
@@ -1610,7 +1671,7 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
   {
     // coordinates and records in; rings out
     ::sbc::KProbe kp_("k_pw_pairs", st2_, 16.0 * totalC + 40.0 * (double)nh);
-    k_pw_pairs<<<grid_for(32LL * nov, kPwPairBlock), kPwPairBlock, 0, st2_>>>(pa, pairK);
+    k_pw_pairs<<<pair_grid(nov), kPwPairBlock, 0, st2_>>>(pa, pairK, queue);
   }
   cudaEventRecord(ev_[1], st2_);
   struct Stash {
@@ -1682,7 +1743,7 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
     pa.aoff = aoff1;
     {
       ::sbc::KProbe kp_("k_pw_pairs", st);
-      k_pw_pairs<<<grid_for(32LL * nov, kPwPairBlock), kPwPairBlock, 0, st>>>(pa, pairK);
+      k_pw_pairs<<<pair_grid(nov), kPwPairBlock, 0, st>>>(pa, pairK, queue + 1);
     }
     cudaMemcpyAsync(hst.data(), status, sizeof(int) * nov, cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise clip");

@@ -200,6 +200,8 @@ class PairwiseRunner {
   ~PairwiseRunner();
   int run(const double* d_bxy, int nb, int nov, const double* d_cxy, const long long* d_coff,
           cudaStream_t st);
+  int autotune(const double* d_bxy, int nb, int nov, const double* d_cxy, const long long* d_coff,
+               cudaStream_t st, double* best_ms);
   int np = 0;
   int* status = nullptr;            // device, per overlay: SBC_* code
   long long* pair_ring = nullptr;   // device, np+1
@@ -221,6 +223,8 @@ class PairwiseRunner {
   cudaStream_t st2_ = nullptr;      // the one-thread-per-pair kernel's stream
   cudaEvent_t ev_[2] = {nullptr, nullptr};
   std::vector<int> order_h;
+  unsigned pair_blocks_ = 0;
+  unsigned pair_grid(int nov);
 };
 
 }  // namespace sbc

@@ -131,6 +131,9 @@ def load_library(path: str | os.PathLike | None = None):
     L.sbc_pairwise_info.argtypes = [vp, ctypes.POINTER(ll), i]
     L.sbc_pairwise_set_cell_factor.argtypes = [vp, ctypes.c_double]
     L.sbc_pairwise_set_split.argtypes = [vp, i]
+    L.sbc_pairwise_autotune.argtypes = [vp, ctypes.POINTER(_PairwiseJob), ctypes.POINTER(i),
+                                        ctypes.POINTER(ctypes.c_double),
+                                        ctypes.POINTER(ctypes.c_double), vp]
     L.sbc_trace_rings_noalloc.argtypes = [ctypes.POINTER(_MergedLists), vp, i, vp, ll,
                                           ctypes.POINTER(i), ctypes.POINTER(ll), vp,
                                           ctypes.c_char_p, i]
@@ -345,6 +348,15 @@ class Clipper:
 
     def set_pairwise_split(self, records: int) -> None:
         self._check(self._L.sbc_pairwise_set_split(self._h, int(records)))
+
+    def autotune_pairwise_device(self, d_bxy, nb, noverlays, d_cxy, d_coff,
+                                 stream: int | None = None) -> dict:
+        """Pick the big-pair split and grid cell width by timing the job."""
+        j = _PairwiseJob(d_bxy, nb, noverlays, d_cxy, d_coff)
+        sp, cf, ms = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+        self._check(self._L.sbc_pairwise_autotune(self._h, ctypes.byref(j), ctypes.byref(sp),
+                                                  ctypes.byref(cf), ctypes.byref(ms), stream))
+        return {"split": sp.value, "cell_factor": cf.value, "best_ms": ms.value}
 
     def area_forward(self, bases, overlays, stream: int | None = None):
         """Intersection area of every pair: (area, status)."""

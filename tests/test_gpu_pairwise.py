@@ -82,6 +82,29 @@ def test_pairwise_split_does_not_change_results(clipper):
         assert rings_equal(ref[i], clipper.clip_pair(base, ovs[i])), i
 
 
+def test_pairwise_autotune(clipper):
+    torch = pytest.importorskip("torch")
+    import sbclip
+    base, ovs = gen.one_to_many(n_base=6_000, n_overlays=100, seed=3260, hi=1200,
+                                near_boundary=0.6)
+    ref, _ = clipper.clip_pairwise(base, ovs)
+    cxy, coff = sbclip.pack_polygons(ovs)
+    tb = torch.from_numpy(np.ascontiguousarray(base)).to("cuda:0")
+    tc = torch.from_numpy(cxy).to("cuda:0")
+    to = torch.from_numpy(coff).to("cuda:0")
+    try:
+        t = clipper.autotune_pairwise_device(tb.data_ptr(), len(base), len(ovs), tc.data_ptr(),
+                                             to.data_ptr())
+        assert t["split"] in (2048, 4096, 8192, 16384, 32768)
+        assert t["cell_factor"] in (0.5, 1.0, 2.0) and t["best_ms"] > 0
+        got, st = clipper.clip_pairwise(base, ovs)
+        assert (st == 0).all()
+        assert all(rings_equal(a, b) for a, b in zip(got, ref))
+    finally:
+        clipper.set_pairwise_split(8192)
+        clipper.set_pairwise_cell_factor(1.0)
+
+
 def test_pairwise_special_overlays(clipper):
     base = gen.jagged_star(3_000, 3300, R=1000.0)
     b0 = base[0]
