@@ -462,9 +462,12 @@ ONE_TO_MANY = (200_000, 10_000)
 ONE_TO_MANY_METRIC = "clipped pairs/s, one 200k-vertex base x 10,000 overlays, pairwise forward"
 
 
-def one_to_many_workload():
+def one_to_many_workload(n_overlays: int | None = None):
     nb, nov = ONE_TO_MANY
     base, ovs = gen.one_to_many(n_base=nb, n_overlays=nov, seed=3000)
+    if n_overlays is not None:
+        ovs = ovs[:n_overlays]
+        nov = len(ovs)
     desc = {"workload": f"one_to_many_{nb // 1000}k_{nov}", "base_vertices": nb,
             "overlays": nov, "overlay_vertices": int(sum(len(o) for o in ovs)),
             "generator": "jagged base R=1000; plain-star overlays, sizes log-U[4,5000], radii "
@@ -480,7 +483,7 @@ def run_one_to_many(args, rank: int, world: int):
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    base, ovs, desc = one_to_many_workload()
+    base, ovs, desc = one_to_many_workload(args.overlays)
     nov = len(ovs)
     cxy, coff = sbclip.pack_polygons(ovs)
     cuda = f"cuda:{dev}"
@@ -495,6 +498,16 @@ def run_one_to_many(args, rank: int, world: int):
     def step():
         return clip.clip_pairwise_device(tb.data_ptr(), len(base), nov, tc.data_ptr(),
                                          to.data_ptr(), sp)
+
+    if args.job_only:
+        # profiling mode: the job alone, default settings, no JSON line
+        for _ in range(args.job_only):
+            nr, nv = step()
+        torch.cuda.synchronize()
+        print(f"job ok: {nov} overlays, {nr} rings, {nv} vertices, {clip.pairwise_info()}",
+              file=sys.stderr)
+        clip.close()
+        return None
 
     # the autotuner picks the big-pair split and the grid cell width (outside
     # the timed region; results do not depend on them)
@@ -665,6 +678,11 @@ def main():
                     choices=["pair_1m_1m", "pair_200k_200k", "pair_10k_8k", "small_pairs_65536",
                              "one_to_many_200k_10000"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--job-only", type=int, default=0,
+                    help="one_to_many only: run the job this many times and print no JSON "
+                         "line (for profilers)")
+    ap.add_argument("--overlays", type=int, default=None,
+                    help="one_to_many only: use the first N overlays of the workload")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -681,7 +699,7 @@ def main():
         out = run_one_to_many(args, rank, world)
     else:
         out = run_gb300(args, rank, world)
-    if rank == 0:
+    if rank == 0 and out is not None:
         print(json.dumps(out), flush=True)
     if world > 1:
         import torch.distributed as dist

@@ -210,8 +210,8 @@ int sbc_clip_pairwise_device(sbc_ctx* ctx, const sbc_pairwise_job* job, sbc_batc
  * sbc_pairwise_set_split). */
 int sbc_pairwise_info(const sbc_ctx* ctx, long long* out, int n);
 /* Base-grid cell width of sbc_clip_pairwise in units of
- * sqrt(base bounding-box area / nb); default 1.  A tuning knob: results do not
- * depend on it. */
+ * max(sqrt(base bounding-box area / nb), 1.5 mean base edge extents); default
+ * 1.  A tuning knob: results do not depend on it. */
 int sbc_pairwise_set_cell_factor(sbc_ctx* ctx, double factor);
 /* Overlays with at least `records` intersecting edge pairs leave the
  * one-thread-per-pair back end for the data-parallel one; default 8192.  A

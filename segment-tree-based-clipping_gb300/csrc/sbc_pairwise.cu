@@ -1474,11 +1474,11 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
     std::memcpy(&d, &u, sizeof d);
     return d;
   };
-  // grid: cells about sqrt(area / n_b) wide (times the tuned factor), at
-  // least 1.5 mean edge extents, at most 2^22 cells
+  // grid: cells the larger of sqrt(area / n_b) and 1.5 mean edge extents
+  // wide, times the tuned factor, at most 2^22 cells
   const double bx0 = unkey(hs.mnx), bx1 = unkey(hs.mxx), by0 = unkey(hs.mny), by1 = unkey(hs.mxy);
   const double W = std::max(bx1 - bx0, 1e-300), Hh = std::max(by1 - by0, 1e-300);
-  double h = std::max(cell_factor * std::sqrt(W * Hh / nb), 1.5 * hs.ext / nb);
+  double h = cell_factor * std::max(std::sqrt(W * Hh / nb), 1.5 * hs.ext / nb);
   if (!(h > 0) || !std::isfinite(h)) h = std::max(W, Hh);
   while ((W / h + 1) * (Hh / h + 1) > (double)(1 << 22)) h *= 1.25;
   PwGrid g;
