@@ -125,14 +125,17 @@ int sbc_classify_pairs(sbc_ctx* ctx, const double* pairs, int n, int* types, dou
 /* ---- Batches of independent pairs --------------------------------------
  * Many base/overlay pairs in one call: the result for every pair equals
  * sbc_clip_pair on that pair (the reference's `seg base overlay`, run once
- * per pair; the reference itself has no batched call).  Each pair is clipped
- * by one device thread, all pairs in one launch.  Polygons are concatenated:
- * pair p's base is vertices [b_off[p], b_off[p+1]) of b_xy, its overlay
- * vertices [c_off[p], c_off[p+1]) of c_xy.  A polygon needs 3 to
- * SBC_BATCH_MAX_VERTICES vertices; a pair outside that range gets status
- * SBC_EINPUT and no rings.  Per-pair failures (SBC_EUNDEF where the
- * reference's behaviour is undefined) are reported in the per-pair status;
- * the call itself fails only on argument, allocation or CUDA errors. */
+ * per pair; the reference itself has no batched call).  Polygons are
+ * concatenated: pair p's base is vertices [b_off[p], b_off[p+1]) of b_xy, its
+ * overlay vertices [c_off[p], c_off[p+1]) of c_xy.  A pair whose polygons
+ * have at most SBC_BATCH_MAX_VERTICES vertices is clipped by one device
+ * thread, all such pairs in one launch per chunk (consecutive pairs whose
+ * scratch arenas fit the budget, sbc_batch_set_arena_budget); a pair with a
+ * larger polygon is clipped by the single-pair pipeline.  A polygon needs at
+ * least 3 vertices; a pair with a smaller one gets status SBC_EINPUT and no
+ * rings.  Per-pair failures (SBC_EUNDEF where the reference's behaviour is
+ * undefined) are reported in the per-pair status; the call itself fails only
+ * on argument, allocation or CUDA errors. */
 #define SBC_BATCH_MAX_VERTICES 4096
 typedef struct sbc_batch {
   int npairs;
@@ -223,6 +226,15 @@ int sbc_pairwise_set_split(sbc_ctx* ctx, int records);
  * are left as sbc_clip_pairwise_device would leave them. */
 int sbc_pairwise_autotune(sbc_ctx* ctx, const sbc_pairwise_job* job, int* split,
                           double* cell_factor, double* best_ms, void* stream);
+
+/* Bytes of per-pair scratch arenas one chunk of a batch may hold (0: the
+ * smaller of 96 GiB and half of the device's free memory).  A batch larger
+ * than one chunk runs chunk by chunk; its backward pass then recomputes each
+ * chunk's forward pass instead of keeping every intersection record. */
+int sbc_batch_set_arena_budget(sbc_ctx* ctx, long long bytes);
+/* Shape of the last batch call: out[0] chunks, out[1] pairs clipped by the
+ * single-pair pipeline because a polygon exceeds SBC_BATCH_MAX_VERTICES. */
+int sbc_batch_info(const sbc_ctx* ctx, long long* out, int n);
 
 /* Allocation-free ring tracing.  No counterpart in the reference: it exists
  * for callers that are not allowed to allocate device memory themselves or

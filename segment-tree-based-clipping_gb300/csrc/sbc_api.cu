@@ -465,6 +465,7 @@ int batch_to_device(sbc_ctx* c, const sbc_batch* b, cudaStream_t st, sbc_batch* 
 
 int batch_run(sbc_ctx* c, const sbc_batch* d, cudaStream_t st) {
   c->pl->clear_error();
+  c->pl->set_stream(st);
   int rc = c->br->forward(d->npairs, d->b_xy, d->b_off, d->c_xy, d->c_off, st);
   if (rc) return set_err(c, rc, c->pl->error());
   return SBC_OK;
@@ -573,7 +574,7 @@ extern "C" int sbc_clip_batch_device(sbc_ctx* c, const sbc_batch* b, sbc_batch_r
   long long nr = 0, nv = 0;
   if (b->npairs > 0) {
     c->pl->clear_error();
-    rc = c->br->rings(b->b_off, b->c_off, st, &pr, &ro, &xy, &nr, &nv);
+    rc = c->br->rings(b->b_xy, b->b_off, b->c_xy, b->c_off, st, &pr, &ro, &xy, &nr, &nv);
     if (rc) return set_err(c, rc, c->pl->error());
   }
   out->npairs = b->npairs;
@@ -746,5 +747,19 @@ extern "C" int sbc_pairwise_autotune(sbc_ctx* c, const sbc_pairwise_job* j, int*
   if (rc) return set_err(c, rc, c->pl->error());
   if (split) *split = c->pw->big_k;
   if (cell_factor) *cell_factor = c->pw->cell_factor;
+  return SBC_OK;
+}
+
+extern "C" int sbc_batch_set_arena_budget(sbc_ctx* c, long long bytes) {
+  if (!c) return SBC_EINPUT;
+  if (bytes < 0) return set_err(c, SBC_EINPUT, "negative budget");
+  c->br->arena_budget = bytes;
+  return SBC_OK;
+}
+
+extern "C" int sbc_batch_info(const sbc_ctx* c, long long* out, int n) {
+  if (!c || !out) return SBC_EINPUT;
+  const long long v[2] = {c->br->chunks(), c->br->large_pairs()};
+  for (int i = 0; i < n && i < 2; ++i) out[i] = v[i];
   return SBC_OK;
 }

@@ -756,8 +756,8 @@ __global__ void __launch_bounds__(kBatchBlock)
 k_batch_clip(int np, const double* __restrict__ bxy, const long long* __restrict__ boff,
              const double* __restrict__ cxy, const long long* __restrict__ coff,
              const int* __restrict__ pass_of, unsigned char* __restrict__ arena,
-             const long long* __restrict__ aoff, int* __restrict__ status, int* __restrict__ nrings,
-             int* __restrict__ nverts, double* __restrict__ area) {
+             const long long* __restrict__ aoff, long long abase, int* __restrict__ status,
+             int* __restrict__ nrings, int* __restrict__ nverts, double* __restrict__ area) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= np) return;
   const int pass = pass_of ? pass_of[p] : 0;
@@ -770,7 +770,7 @@ k_batch_clip(int np, const double* __restrict__ bxy, const long long* __restrict
     return;
   }
   const Caps cp = caps_of(nb, nc, hit_cap(nb, nc, pass));
-  Carver cv{arena + aoff[p], 0};
+  Carver cv{arena + (aoff[p] - abase), 0};
   PairWork w = carve(cv, cp);
   const PairResult r = clip_pair_serial(bxy + 2 * boff[p], nb, cxy + 2 * coff[p], nc, cp, w);
   status[p] = r.status == PS_OK ? SBC_OK : (r.status == PS_UNDEF ? SBC_EUNDEF : SBC_ENOMEM);
@@ -789,15 +789,18 @@ __global__ void k_batch_counts(int np, const int* __restrict__ status, const int
   vpre[p] = ok ? nv[p] : 0;
 }
 
-// where a pair's data lives: pass 0 arena, or the retry arena (full capacity)
+// where a pair's data lives: pass 0 arena, or the retry arena (full
+// capacity); offsets are relative to each arena's first pair (abase)
 struct Arenas {
   const unsigned char* a0;
   const long long* off0;
+  long long abase0;
   const unsigned char* a1;
   const long long* off1;
-  const int* pass;  // per pair: 0 or 1
+  long long abase1;
+  const int* pass;  // per pair: 0, 1, or -1 (no arena: a large or invalid pair)
   __device__ const unsigned char* at(int p) const {
-    return pass[p] == 1 ? a1 + off1[p] : a0 + off0[p];
+    return pass[p] == 1 ? a1 + (off1[p] - abase1) : a0 + (off0[p] - abase0);
   }
 };
 
@@ -811,7 +814,7 @@ __global__ void k_batch_pack(int np, const long long* __restrict__ boff,
   if (p >= np) return;
   const long long r0 = rpre[p], v0 = vpre[p];
   const int nr = (int)(rpre[p + 1] - r0);
-  if (nr == 0 || status[p] != SBC_OK) return;
+  if (nr == 0 || status[p] != SBC_OK || ar.pass[p] < 0) return;
   const int nb = (int)(boff[p + 1] - boff[p]), nc = (int)(coff[p + 1] - coff[p]);
   const Caps cp = caps_of(nb, nc, hit_cap(nb, nc, ar.pass[p]));
   Carver cv{const_cast<unsigned char*>(ar.at(p)), 0};
@@ -835,7 +838,7 @@ k_batch_backward(int np, const double* __restrict__ bxy, const long long* __rest
   double* gcp = gc + 2 * coff[p];
   for (int i = 0; i < 2 * nb; ++i) gbp[i] = 0.0;
   for (int i = 0; i < 2 * nc; ++i) gcp[i] = 0.0;
-  if (status[p] != SBC_OK || nrings[p] == 0) return;
+  if (status[p] != SBC_OK || nrings[p] == 0 || ar.pass[p] < 0) return;
   const double* b = bxy + 2 * boff[p];
   const double* c = cxy + 2 * coff[p];
   const Caps cp = caps_of(nb, nc, hit_cap(nb, nc, ar.pass[p]));
@@ -884,20 +887,149 @@ k_batch_backward(int np, const double* __restrict__ bxy, const long long* __rest
   }
 }
 
+// ------------------------------------------------------------------ large pairs
+// A pair with a polygon above SBC_BATCH_MAX_VERTICES is clipped by the pair
+// pipeline.  Its ring vertices get the provenance the small-pair engine
+// records, by exact coordinates: a base vertex first, then an overlay vertex,
+// then a proper crossing (a type-1 record) -- candidates sorted by (x, y),
+// ties in that order, and each ring vertex looked up.
+__global__ void k_big_cand(int nb, int nc, int K, const double* __restrict__ b,
+                           const double* __restrict__ c, const int* __restrict__ ut,
+                           const double* __restrict__ isxy, unsigned long long* __restrict__ kx,
+                           unsigned long long* __restrict__ ky, unsigned* __restrict__ val) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = nb + nc + K;
+  if (i >= n) return;
+  double x, y;
+  bool use = true;
+  if (i < nb) {
+    x = b[2 * i];
+    y = b[2 * i + 1];
+  } else if (i < nb + nc) {
+    x = c[2 * (i - nb)];
+    y = c[2 * (i - nb) + 1];
+  } else {
+    const int r = i - nb - nc;
+    x = isxy[2 * r];
+    y = isxy[2 * r + 1];
+    use = ut[r] == 1;
+  }
+  kx[i] = use ? dkey(x) : ~0ull;
+  ky[i] = use ? dkey(y) : ~0ull;
+  val[i] = (unsigned)i;
+}
+
+__global__ void k_big_gather(int n, const unsigned long long* __restrict__ src,
+                             const unsigned* __restrict__ val, unsigned long long* __restrict__ dst) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) dst[t] = src[val[t]];
+}
+
+// tape of each ring vertex: (0, base vertex) / (1, overlay vertex) /
+// (2, base edge, overlay edge) for a proper crossing / (-1) none
+__global__ void k_big_tape(int nv, const double* __restrict__ xy, int n,
+                           const unsigned long long* __restrict__ kxs,
+                           const unsigned long long* __restrict__ kys,
+                           const unsigned* __restrict__ val, int nb, int nc,
+                           const int* __restrict__ ub, const int* __restrict__ uc,
+                           int4* __restrict__ tape) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const unsigned long long qx = dkey(xy[2 * v]), qy = dkey(xy[2 * v + 1]);
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int m = (lo + hi) >> 1;
+    if (kxs[m] < qx || (kxs[m] == qx && kys[m] < qy)) lo = m + 1;
+    else hi = m;
+  }
+  int4 t = make_int4(-1, 0, 0, 0);
+  if (lo < n && kxs[lo] == qx && kys[lo] == qy) {
+    const int i = (int)val[lo];
+    if (i < nb) t = make_int4(0, i, 0, 0);
+    else if (i < nb + nc) t = make_int4(1, i - nb, 0, 0);
+    else t = make_int4(2, ub[i - nb - nc] >> 1, uc[i - nb - nc] >> 1, 0);
+  }
+  tape[v] = t;
+}
+
+// signed shoelace sum over every ring of one pair (one block, fixed order)
+__global__ void __launch_bounds__(1024) k_big_area(int nr, const int* __restrict__ off,
+                                                   const double* __restrict__ xy,
+                                                   double* __restrict__ area) {
+  __shared__ double part[1024];
+  double s = 0.0;
+  for (int r = 0; r < nr; ++r) {
+    const int a = off[r], e = off[r + 1];
+    for (int i = a + threadIdx.x; i < e; i += blockDim.x) {
+      const int j = (i + 1 == e) ? a : i + 1;
+      s += xy[2 * i] * xy[2 * j + 1] - xy[2 * j] * xy[2 * i + 1];
+    }
+  }
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 512; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *area = 0.5 * part[0];
+}
+
+// d(area)/d(vertices) of one large pair, one thread per ring vertex
+// (contributions are added atomically: their order, and so the last bits of
+// the sums, may differ between runs)
+__global__ void k_big_backward(int nr, int nv, const int* __restrict__ off,
+                               const double* __restrict__ xy, const int4* __restrict__ tape,
+                               const double* __restrict__ b, int nb, const double* __restrict__ c,
+                               int nc, double g, double* __restrict__ gb, double* __restrict__ gc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  int lo = 0, hi = nr;  // the ring holding vertex i
+  while (hi - lo > 1) {
+    const int m = (lo + hi) >> 1;
+    if (off[m] <= i) lo = m;
+    else hi = m;
+  }
+  const int s = off[lo], e = off[lo + 1];
+  const int ip = (i + 1 == e) ? s : i + 1, im = (i == s) ? e - 1 : i - 1;
+  const double gx = 0.5 * g * (xy[2 * ip + 1] - xy[2 * im + 1]);
+  const double gy = 0.5 * g * (xy[2 * im] - xy[2 * ip]);
+  const int4 t = tape[i];
+  if (t.x == 0) {
+    atomicAdd(&gb[2 * t.y], gx);
+    atomicAdd(&gb[2 * t.y + 1], gy);
+  } else if (t.x == 1) {
+    atomicAdd(&gc[2 * t.y], gx);
+    atomicAdd(&gc[2 * t.y + 1], gy);
+  } else if (t.x == 2) {
+    const int i1 = t.y, i2 = (t.y + 1) % nb, j1 = t.z, j2 = (t.z + 1) % nc;
+    const double b1x = b[2 * i1], b1y = b[2 * i1 + 1], b2x = b[2 * i2], b2y = b[2 * i2 + 1];
+    const double c1x = c[2 * j1], c1y = c[2 * j1 + 1], c2x = c[2 * j2], c2y = c[2 * j2 + 1];
+    const double A1 = (c1x - b1x) * (c2y - b1y) - (c1y - b1y) * (c2x - b1x);
+    const double A2 = (c1x - b2x) * (c2y - b2y) - (c1y - b2y) * (c2x - b2x);
+    const double d = A1 - A2;
+    const double al = A1 / d;
+    const double ga = gx * (b2x - b1x) + gy * (b2y - b1y);
+    const double k1 = -A2 / (d * d) * ga, k2 = A1 / (d * d) * ga;
+    atomicAdd(&gb[2 * i1], (1.0 - al) * gx + k1 * (c1y - c2y));
+    atomicAdd(&gb[2 * i1 + 1], (1.0 - al) * gy + k1 * (c2x - c1x));
+    atomicAdd(&gb[2 * i2], al * gx + k2 * (c1y - c2y));
+    atomicAdd(&gb[2 * i2 + 1], al * gy + k2 * (c2x - c1x));
+    atomicAdd(&gc[2 * j1], k1 * (c2y - b1y) + k2 * (c2y - b2y));
+    atomicAdd(&gc[2 * j1 + 1], k1 * (b1x - c2x) + k2 * (b2x - c2x));
+    atomicAdd(&gc[2 * j2], k1 * (b1y - c1y) + k2 * (b2y - c1y));
+    atomicAdd(&gc[2 * j2 + 1], k1 * (c1x - b1x) + k2 * (c1x - b2x));
+  }
+}
+
 }  // namespace
 
+
 // ------------------------------------------------------------------ host
-int BatchRunner::forward(int np_, const double* d_bxy, const long long* d_boff,
-                         const double* d_cxy, const long long* d_coff, cudaStream_t st) {
+// Sizes, large pairs and chunks of a batch.  Consecutive pairs whose
+// first-pass arenas fit the budget form one chunk; a large pair has no arena.
+int BatchRunner::plan(int np_, const long long* d_boff, const long long* d_coff, cudaStream_t st) {
   BufferPool& pool = pl_.pool();
-  valid = false;
   np = np_;
-  key_b = d_bxy;
-  key_c = d_cxy;
-  if (np <= 0) {
-    valid = true;
-    return kOk;
-  }
   aoff[0] = (long long*)pool.get("bt_aoff0", sizeof(long long) * (np + 1));
   aoff[1] = (long long*)pool.get("bt_aoff1", sizeof(long long) * (np + 1));
   pass = (int*)pool.get("bt_pass", sizeof(int) * (np + 1));
@@ -905,102 +1037,282 @@ int BatchRunner::forward(int np_, const double* d_bxy, const long long* d_boff,
   nrings = (int*)pool.get("bt_nrings", sizeof(int) * (np + 1));
   nverts = (int*)pool.get("bt_nverts", sizeof(int) * (np + 1));
   area = (double*)pool.get("bt_area", sizeof(double) * (np + 1));
-  void* sscr = pool.get("bt_scan", scan_scratch_bytes(np + 1));
+  sscr_ = pool.get("bt_scan", scan_scratch_bytes(np + 1));
   if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch)");
-  {
-    long long hb = 0, hc = 0;
-    cudaMemcpyAsync(&hb, d_boff + np, sizeof(long long), cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(&hc, d_coff + np, sizeof(long long), cudaMemcpyDeviceToHost, st);
-    if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch offsets");
-    in_verts = (double)(hb + hc);
-  }
-  // pass 0: every pair with a generous hit capacity
+  h_boff_.resize(np + 1);
+  h_coff_.resize(np + 1);
+  h_aoff0_.resize(np + 1);
+  cudaMemcpyAsync(h_boff_.data(), d_boff, sizeof(long long) * (np + 1), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(h_coff_.data(), d_coff, sizeof(long long) * (np + 1), cudaMemcpyDeviceToHost, st);
   {
     ::sbc::KProbe kp_("k_batch_size", st);
     k_batch_size<<<grid_for(np + 1, 256), 256, 0, st>>>(np, d_boff, d_coff, nullptr, aoff[0]);
   }
-  exclusive_scan_i64(aoff[0], np + 1, sscr, st);
-  long long total = 0;
-  cudaMemcpyAsync(&total, aoff[0] + np, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  exclusive_scan_i64(aoff[0], np + 1, sscr_, st);
+  cudaMemcpyAsync(h_aoff0_.data(), aoff[0], sizeof(long long) * (np + 1), cudaMemcpyDeviceToHost,
+                  st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch sizes");
-  arena[0] = (unsigned char*)pool.get("bt_arena0", (size_t)total + 256);
+  in_verts = (double)(h_boff_[np] + h_coff_[np]);
+  big_.clear();
+  for (int p = 0; p < np; ++p) {
+    const long long nb = h_boff_[p + 1] - h_boff_[p], nc = h_coff_[p + 1] - h_coff_[p];
+    if (nb >= 3 && nc >= 3 && (nb > SBC_BATCH_MAX_VERTICES || nc > SBC_BATCH_MAX_VERTICES)) {
+      BigOut b;
+      b.p = p;
+      big_.push_back(b);
+    }
+  }
+  long long budget = arena_budget;
+  if (budget <= 0) {
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    budget = std::min<long long>(96LL << 30, (long long)(fr / 2));
+    budget = std::max<long long>(budget, 1LL << 28);
+  }
+  chunks_.clear();
+  for (int p0 = 0; p0 < np;) {
+    // the last p1 with aoff0[p1] - aoff0[p0] <= budget (at least one pair)
+    int lo = p0 + 1, hi = np;
+    while (lo < hi) {
+      const int m = (lo + hi + 1) / 2;
+      if (h_aoff0_[m] - h_aoff0_[p0] <= budget) lo = m;
+      else hi = m - 1;
+    }
+    chunks_.push_back({p0, lo});
+    p0 = lo;
+  }
+  resident_ = -1;
+  return kOk;
+}
+
+// The small pairs of chunk c: pass 0, then the pairs that ran out of hit
+// room again with the full product.  The chunk's arenas stay resident.
+int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
+                           const double* d_cxy, const long long* d_coff, cudaStream_t st) {
+  BufferPool& pool = pl_.pool();
+  const int p0 = chunks_[c].first, p1 = chunks_[c].second, n = p1 - p0;
+  abase_[0] = h_aoff0_[p0];
+  arena[0] = (unsigned char*)pool.get("bt_arena0", (size_t)(h_aoff0_[p1] - h_aoff0_[p0]) + 256);
   if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch arena)");
+  // large pairs (-1) keep what the pipeline gave them; every other pair runs
+  std::vector<char> is_small(n);
+  std::vector<int> hp(n);
+  for (int i = 0; i < n; ++i) {
+    const long long nb = h_boff_[p0 + i + 1] - h_boff_[p0 + i];
+    const long long nc = h_coff_[p0 + i + 1] - h_coff_[p0 + i];
+    is_small[i] = nb <= SBC_BATCH_MAX_VERTICES && nc <= SBC_BATCH_MAX_VERTICES;
+    hp[i] = (nb >= 3 && nc >= 3 && !is_small[i]) ? -1 : 0;
+  }
+  cudaMemcpyAsync(pass + p0, hp.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
   {
     // coordinates in; area, status, ring and vertex counts out
-    ::sbc::KProbe kp_("k_batch_clip", st, 16.0 * in_verts + 20.0 * np);
-    k_batch_clip<<<grid_for(np, kBatchBlock), kBatchBlock, 0, st>>>(
-        np, d_bxy, d_boff, d_cxy, d_coff, nullptr, arena[0], aoff[0], status, nrings, nverts, area);
+    ::sbc::KProbe kp_("k_batch_clip", st,
+                      16.0 * (double)(h_boff_[p1] - h_boff_[p0] + h_coff_[p1] - h_coff_[p0]) +
+                          20.0 * n);
+    k_batch_clip<<<grid_for(n, kBatchBlock), kBatchBlock, 0, st>>>(
+        n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[0], aoff[0] + p0, abase_[0],
+        status + p0, nrings + p0, nverts + p0, area + p0);
   }
-  std::vector<int> hs(np);
-  cudaMemcpyAsync(hs.data(), status, sizeof(int) * np, cudaMemcpyDeviceToHost, st);
+  std::vector<int> hs(n);
+  cudaMemcpyAsync(hs.data(), status + p0, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch clip");
-  // pass 1: pairs that ran out of hit capacity, with the full product
-  std::vector<int> hp(np, -1);
   int retry = 0;
-  for (int p = 0; p < np; ++p)
-    if (hs[p] == SBC_ENOMEM) {
-      hp[p] = 1;
+  for (int i = 0; i < n; ++i) {
+    hp[i] = -1;
+    if (is_small[i] && hs[i] == SBC_ENOMEM) {
+      hp[i] = 1;
       ++retry;
     }
+  }
   arena[1] = arena[0];
+  abase_[1] = 0;
   if (retry) {
-    cudaMemcpyAsync(pass, hp.data(), sizeof(int) * np, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(pass + p0, hp.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
     {
       ::sbc::KProbe kp_("k_batch_size", st);
-      k_batch_size<<<grid_for(np + 1, 256), 256, 0, st>>>(np, d_boff, d_coff, pass, aoff[1]);
+      k_batch_size<<<grid_for(n + 1, 256), 256, 0, st>>>(n, d_boff + p0, d_coff + p0, pass + p0,
+                                                         aoff[1] + p0);
     }
-    exclusive_scan_i64(aoff[1], np + 1, sscr, st);
-    cudaMemcpyAsync(&total, aoff[1] + np, sizeof(long long), cudaMemcpyDeviceToHost, st);
+    exclusive_scan_i64(aoff[1] + p0, n + 1, sscr_, st);
+    long long total = 0;
+    cudaMemcpyAsync(&total, aoff[1] + p1, sizeof(long long), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch sizes");
     arena[1] = (unsigned char*)pool.get("bt_arena1", (size_t)total + 256);
     if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch arena)");
     {
       ::sbc::KProbe kp_("k_batch_clip", st);
-      k_batch_clip<<<grid_for(np, kBatchBlock), kBatchBlock, 0, st>>>(
-          np, d_bxy, d_boff, d_cxy, d_coff, pass, arena[1], aoff[1], status, nrings, nverts, area);
+      k_batch_clip<<<grid_for(n, kBatchBlock), kBatchBlock, 0, st>>>(
+          n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[1], aoff[1] + p0, 0,
+          status + p0, nrings + p0, nverts + p0, area + p0);
     }
   }
-  for (int p = 0; p < np; ++p) hp[p] = hp[p] == 1 ? 1 : 0;
-  cudaMemcpyAsync(pass, hp.data(), sizeof(int) * np, cudaMemcpyHostToDevice, st);
+  // where each pair's data lives now: pass 0 arena, retry arena, or none
+  for (int i = 0; i < n; ++i) {
+    const long long nb = h_boff_[p0 + i + 1] - h_boff_[p0 + i];
+    const long long nc = h_coff_[p0 + i + 1] - h_coff_[p0 + i];
+    const bool ok = nb >= 3 && nc >= 3 && is_small[i];
+    hp[i] = !ok ? -1 : (hp[i] == 1 ? 1 : 0);
+  }
+  cudaMemcpyAsync(pass + p0, hp.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch clip");
+  resident_ = c;
+  return kOk;
+}
+
+// Large pairs through the pair pipeline: rings, provenance tape and area.
+int BatchRunner::run_big(const double* d_bxy, const double* d_cxy, cudaStream_t st) {
+  BufferPool& pool = pl_.pool();
+  for (size_t k = 0; k < big_.size(); ++k) {
+    BigOut& bo = big_[k];
+    const int p = bo.p;
+    const int nb = (int)(h_boff_[p + 1] - h_boff_[p]), nc = (int)(h_coff_[p + 1] - h_coff_[p]);
+    const double* b = d_bxy + 2 * h_boff_[p];
+    const double* c = d_cxy + 2 * h_coff_[p];
+    const int sizes[1] = {nc};
+    pl_.clear_error();
+    int rc = pl_.run(b, nb, c, sizes, 1);
+    int hstat = SBC_OK;
+    bo.nrings = bo.nverts = 0;
+    if (rc == kEInput || rc == kEUndef) {
+      hstat = rc == kEInput ? SBC_EINPUT : SBC_EUNDEF;
+    } else if (rc) {
+      return rc;
+    } else {
+      const auto& out = pl_.outputs()[0];
+      bo.nrings = out.nrings;
+      bo.nverts = (int)out.nverts;
+      const std::string tag = std::to_string(k);
+      bo.off = (int*)pool.get("bt_big_off_" + tag, sizeof(int) * (bo.nrings + 1));
+      bo.xy = (double*)pool.get("bt_big_xy_" + tag, sizeof(double) * 2 * (bo.nverts + 1));
+      bo.tape = (int4*)pool.get("bt_big_tape_" + tag, sizeof(int4) * (bo.nverts + 1));
+      const int K = pl_.dbg_K, n = nb + nc + K;
+      auto* kx = (unsigned long long*)pool.get("bt_big_kx", sizeof(unsigned long long) * (n + 1));
+      auto* ky = (unsigned long long*)pool.get("bt_big_ky", sizeof(unsigned long long) * (n + 1));
+      auto* k2 = (unsigned long long*)pool.get("bt_big_k2", sizeof(unsigned long long) * (n + 1));
+      auto* k3 = (unsigned long long*)pool.get("bt_big_k3", sizeof(unsigned long long) * (n + 1));
+      auto* val = (unsigned*)pool.get("bt_big_val", sizeof(unsigned) * (n + 1));
+      auto* val2 = (unsigned*)pool.get("bt_big_val2", sizeof(unsigned) * (n + 1));
+      void* rscr = pool.get("bt_big_rscr", radix_scratch_bytes(n + 1));
+      if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (large pair)");
+      if (bo.nrings > 0) {
+        cudaMemcpyAsync(bo.off, out.d_off, sizeof(int) * (bo.nrings + 1), cudaMemcpyDeviceToDevice,
+                        st);
+        cudaMemcpyAsync(bo.xy, out.d_xy, sizeof(double) * 2 * bo.nverts, cudaMemcpyDeviceToDevice,
+                        st);
+        {
+          ::sbc::KProbe kp_("k_big_cand", st, 40.0 * n);
+          k_big_cand<<<grid_for(n, 256), 256, 0, st>>>(nb, nc, K, b, c, pl_.dbg_ut, pl_.dbg_isxy,
+                                                       kx, ky, val);
+        }
+        // by y, then stably by x: sorted by (x, y), ties in candidate order
+        cudaMemcpyAsync(k2, ky, sizeof(unsigned long long) * n, cudaMemcpyDeviceToDevice, st);
+        radix_sort_u64(k2, val, k3, val2, n, rscr, st);
+        {
+          ::sbc::KProbe kp_("k_big_gather", st, 20.0 * n);
+          k_big_gather<<<grid_for(n, 256), 256, 0, st>>>(n, kx, val, k2);
+        }
+        radix_sort_u64(k2, val, k3, val2, n, rscr, st);
+        {
+          ::sbc::KProbe kp_("k_big_gather", st, 20.0 * n);
+          k_big_gather<<<grid_for(n, 256), 256, 0, st>>>(n, ky, val, k3);
+        }
+        {
+          ::sbc::KProbe kp_("k_big_tape", st, 32.0 * bo.nverts);
+          k_big_tape<<<grid_for(bo.nverts, 256), 256, 0, st>>>(
+              bo.nverts, bo.xy, n, k2, k3, val, nb, nc, pl_.dbg_ub, pl_.dbg_uc, bo.tape);
+        }
+        {
+          ::sbc::KProbe kp_("k_big_area", st, 16.0 * bo.nverts);
+          k_big_area<<<1, 1024, 0, st>>>(bo.nrings, bo.off, bo.xy, area + p);
+        }
+      } else {
+        cudaMemsetAsync(area + p, 0, sizeof(double), st);
+      }
+    }
+    const int hv[3] = {hstat, bo.nrings, bo.nverts};
+    cudaMemcpyAsync(status + p, &hv[0], sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(nrings + p, &hv[1], sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(nverts + p, &hv[2], sizeof(int), cudaMemcpyHostToDevice, st);
+    if (hstat != SBC_OK) cudaMemsetAsync(area + p, 0, sizeof(double), st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "large pair");
+    bo.ok = hstat == SBC_OK;
+  }
+  pl_.clear_error();
+  return kOk;
+}
+
+int BatchRunner::forward(int np_, const double* d_bxy, const long long* d_boff,
+                         const double* d_cxy, const long long* d_coff, cudaStream_t st) {
+  valid = false;
+  key_b = d_bxy;
+  key_c = d_cxy;
+  np = np_;
+  if (np <= 0) {
+    valid = true;
+    return kOk;
+  }
+  int rc = plan(np_, d_boff, d_coff, st);
+  for (size_t c = 0; c < chunks_.size() && !rc; ++c)
+    rc = run_chunk((int)c, d_bxy, d_boff, d_cxy, d_coff, st);
+  if (!rc) rc = run_big(d_bxy, d_cxy, st);
+  if (rc) return rc;
   valid = true;
   return kOk;
 }
 
-int BatchRunner::rings(const long long* d_boff, const long long* d_coff, cudaStream_t st,
-                       long long** pair_ring, long long** ring_off, double** xy,
-                       long long* total_rings, long long* total_verts) {
+__global__ void k_big_place(int nr, const int* __restrict__ off, long long v0,
+                            long long* __restrict__ ring_off) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < nr) ring_off[r] = v0 + off[r];
+}
+
+int BatchRunner::rings(const double* d_bxy, const long long* d_boff, const double* d_cxy,
+                       const long long* d_coff, cudaStream_t st, long long** pair_ring,
+                       long long** ring_off, double** xy, long long* total_rings,
+                       long long* total_verts) {
   BufferPool& pool = pl_.pool();
   long long* rpre = (long long*)pool.get("bt_rpre", sizeof(long long) * (np + 1));
   long long* vpre = (long long*)pool.get("bt_vpre", sizeof(long long) * (np + 1));
-  void* sscr = pool.get("bt_scan", scan_scratch_bytes(np + 1));
   if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch rings)");
   {
     ::sbc::KProbe kp_("k_batch_counts", st);
     k_batch_counts<<<grid_for(np + 1, 256), 256, 0, st>>>(np, status, nrings, nverts, rpre, vpre);
   }
-  exclusive_scan_i64(rpre, np + 1, sscr, st);
-  exclusive_scan_i64(vpre, np + 1, sscr, st);
-  long long h[2];
-  cudaMemcpyAsync(&h[0], rpre + np, sizeof(long long), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(&h[1], vpre + np, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  exclusive_scan_i64(rpre, np + 1, sscr_, st);
+  exclusive_scan_i64(vpre, np + 1, sscr_, st);
+  std::vector<long long> hr(np + 1), hv(np + 1);
+  cudaMemcpyAsync(hr.data(), rpre, sizeof(long long) * (np + 1), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(hv.data(), vpre, sizeof(long long) * (np + 1), cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch rings");
-  long long* roff = (long long*)pool.get("bt_ring_off", sizeof(long long) * (h[0] + 1));
-  double* oxy = (double*)pool.get("bt_xy", sizeof(double) * 2 * (h[1] + 1));
+  long long* roff = (long long*)pool.get("bt_ring_off", sizeof(long long) * (hr[np] + 1));
+  double* oxy = (double*)pool.get("bt_xy", sizeof(double) * 2 * (hv[np] + 1));
   if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch rings)");
-  const Arenas ar{arena[0], aoff[0], arena[1], aoff[1], pass};
-  if (np > 0) {
+  for (size_t c = 0; c < chunks_.size(); ++c) {
+    if (resident_ != (int)c) {  // recompute a chunk whose arenas were reused
+      const int rc = run_chunk((int)c, d_bxy, d_boff, d_cxy, d_coff, st);
+      if (rc) return rc;
+    }
+    const int p0 = chunks_[c].first, n = chunks_[c].second - p0;
+    const Arenas ar{arena[0], aoff[0] + p0, abase_[0], arena[1], aoff[1] + p0, abase_[1], pass + p0};
     ::sbc::KProbe kp_("k_batch_pack", st);
-    k_batch_pack<<<grid_for(np, 128), 128, 0, st>>>(np, d_boff, d_coff, ar, status, rpre, vpre,
-                                                    roff, oxy);
+    k_batch_pack<<<grid_for(n, 128), 128, 0, st>>>(n, d_boff + p0, d_coff + p0, ar, status + p0,
+                                                   rpre + p0, vpre + p0, roff, oxy);
   }
-  cudaMemcpyAsync(roff + h[0], &h[1], sizeof(long long), cudaMemcpyHostToDevice, st);
+  for (const BigOut& bo : big_) {
+    if (!bo.ok || bo.nrings == 0) continue;
+    ::sbc::KProbe kp_("k_big_place", st);
+    k_big_place<<<grid_for(bo.nrings, 256), 256, 0, st>>>(bo.nrings, bo.off, hv[bo.p],
+                                                          roff + hr[bo.p]);
+    cudaMemcpyAsync(oxy + 2 * hv[bo.p], bo.xy, sizeof(double) * 2 * bo.nverts,
+                    cudaMemcpyDeviceToDevice, st);
+  }
+  cudaMemcpyAsync(roff + hr[np], &hv[np], sizeof(long long), cudaMemcpyHostToDevice, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch pack");
   *pair_ring = rpre;
   *ring_off = roff;
   *xy = oxy;
-  *total_rings = h[0];
-  *total_verts = h[1];
+  *total_rings = hr[np];
+  *total_verts = hv[np];
   return kOk;
 }
 
@@ -1008,12 +1320,33 @@ int BatchRunner::backward(const double* d_bxy, const long long* d_boff, const do
                           const long long* d_coff, const double* d_gA, double* d_gb,
                           double* d_gc, cudaStream_t st) {
   if (np <= 0) return kOk;
-  const Arenas ar{arena[0], aoff[0], arena[1], aoff[1], pass};
-  {
+  for (size_t c = 0; c < chunks_.size(); ++c) {
+    // a batch larger than the arena budget recomputes each chunk's forward
+    if (resident_ != (int)c) {
+      const int rc = run_chunk((int)c, d_bxy, d_boff, d_cxy, d_coff, st);
+      if (rc) return rc;
+    }
+    const int p0 = chunks_[c].first, p1 = chunks_[c].second, n = p1 - p0;
+    const Arenas ar{arena[0], aoff[0] + p0, abase_[0], arena[1], aoff[1] + p0, abase_[1], pass + p0};
     // coordinates in, one gradient per coordinate out
-    ::sbc::KProbe kp_("k_batch_backward", st, 32.0 * in_verts + 8.0 * np);
-    k_batch_backward<<<grid_for(np, kBatchBlock), kBatchBlock, 0, st>>>(
-        np, d_bxy, d_boff, d_cxy, d_coff, ar, status, nrings, d_gA, d_gb, d_gc);
+    ::sbc::KProbe kp_("k_batch_backward", st,
+                      32.0 * (double)(h_boff_[p1] - h_boff_[p0] + h_coff_[p1] - h_coff_[p0]) +
+                          8.0 * n);
+    k_batch_backward<<<grid_for(n, kBatchBlock), kBatchBlock, 0, st>>>(
+        n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, ar, status + p0, nrings + p0, d_gA + p0, d_gb,
+        d_gc);
+  }
+  for (const BigOut& bo : big_) {
+    if (!bo.ok || bo.nverts == 0) continue;
+    const int p = bo.p;
+    const int nb = (int)(h_boff_[p + 1] - h_boff_[p]), nc = (int)(h_coff_[p + 1] - h_coff_[p]);
+    double g = 0.0;
+    cudaMemcpyAsync(&g, d_gA + p, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "large pair backward");
+    ::sbc::KProbe kp_("k_big_backward", st, 48.0 * bo.nverts);
+    k_big_backward<<<grid_for(bo.nverts, 256), 256, 0, st>>>(
+        bo.nrings, bo.nverts, bo.off, bo.xy, bo.tape, d_bxy + 2 * h_boff_[p], nb,
+        d_cxy + 2 * h_coff_[p], nc, g, d_gb + 2 * h_boff_[p], d_gc + 2 * h_coff_[p]);
   }
   if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch backward");
   return kOk;

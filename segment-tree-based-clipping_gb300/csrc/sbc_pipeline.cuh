@@ -161,17 +161,19 @@ struct Merged {
 };
 int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out);
 
-// Many small independent pairs, one device thread each (sbc_batch.cu).  The
-// forward pass keeps each pair's rings and vertex provenance in its arena
-// for rings() and backward().
+// Many independent pairs (sbc_batch.cu): pairs whose polygons have at most
+// SBC_BATCH_MAX_VERTICES vertices one device thread each, in chunks whose
+// arenas fit a memory budget; larger pairs through the Pipeline with a
+// provenance tape.  The forward pass keeps the last chunk's rings and tapes
+// resident for rings() and backward(); other chunks are recomputed there.
 class BatchRunner {
  public:
   explicit BatchRunner(Pipeline& pl) : pl_(pl) {}
   int forward(int np, const double* d_bxy, const long long* d_boff, const double* d_cxy,
               const long long* d_coff, cudaStream_t st);
-  int rings(const long long* d_boff, const long long* d_coff, cudaStream_t st,
-            long long** pair_ring, long long** ring_off, double** xy, long long* total_rings,
-            long long* total_verts);
+  int rings(const double* d_bxy, const long long* d_boff, const double* d_cxy,
+            const long long* d_coff, cudaStream_t st, long long** pair_ring, long long** ring_off,
+            double** xy, long long* total_rings, long long* total_verts);
   int backward(const double* d_bxy, const long long* d_boff, const double* d_cxy,
                const long long* d_coff, const double* d_gA, double* d_gb, double* d_gc,
                cudaStream_t st);
@@ -183,12 +185,32 @@ class BatchRunner {
   const void* key_b = nullptr;  // the forward's inputs (for reuse by backward)
   const void* key_c = nullptr;
   bool valid = false;
+  long long arena_budget = 0;   // bytes per chunk of arenas; 0: min(96 GiB, half of free)
+  int chunks() const { return (int)chunks_.size(); }
+  int large_pairs() const { return (int)big_.size(); }
 
  private:
+  struct BigOut {
+    int p = 0, nrings = 0, nverts = 0;
+    bool ok = false;
+    int* off = nullptr;
+    double* xy = nullptr;
+    int4* tape = nullptr;
+  };
+  int plan(int np, const long long* d_boff, const long long* d_coff, cudaStream_t st);
+  int run_chunk(int c, const double* d_bxy, const long long* d_boff, const double* d_cxy,
+                const long long* d_coff, cudaStream_t st);
+  int run_big(const double* d_bxy, const double* d_cxy, cudaStream_t st);
   Pipeline& pl_;
   unsigned char* arena[2] = {nullptr, nullptr};
   long long* aoff[2] = {nullptr, nullptr};
+  long long abase_[2] = {0, 0};
   int* pass = nullptr;
+  void* sscr_ = nullptr;
+  std::vector<long long> h_boff_, h_coff_, h_aoff0_;
+  std::vector<std::pair<int, int>> chunks_;
+  std::vector<BigOut> big_;
+  int resident_ = -1;
 };
 
 // One base polygon against many overlays with pairwise results: overlay i's

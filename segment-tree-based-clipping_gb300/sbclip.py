@@ -129,6 +129,8 @@ def load_library(path: str | os.PathLike | None = None):
         getattr(L, nm).argtypes = [vp, ctypes.POINTER(_PairwiseJob), ctypes.POINTER(_BatchRings),
                                    vp]
     L.sbc_pairwise_info.argtypes = [vp, ctypes.POINTER(ll), i]
+    L.sbc_batch_set_arena_budget.argtypes = [vp, ll]
+    L.sbc_batch_info.argtypes = [vp, ctypes.POINTER(ll), i]
     L.sbc_pairwise_set_cell_factor.argtypes = [vp, ctypes.c_double]
     L.sbc_pairwise_set_split.argtypes = [vp, i]
     L.sbc_pairwise_autotune.argtypes = [vp, ctypes.POINTER(_PairwiseJob), ctypes.POINTER(i),
@@ -335,6 +337,15 @@ class Clipper:
         self._check(self._L.sbc_clip_pairwise_device(self._h, ctypes.byref(j), ctypes.byref(r),
                                                      stream))
         return int(r.nrings), int(r.nverts)
+
+    def set_batch_arena_budget(self, nbytes: int) -> None:
+        self._check(self._L.sbc_batch_set_arena_budget(self._h, int(nbytes)))
+
+    def batch_info(self) -> dict:
+        """Shape of the last batch call."""
+        v = (ctypes.c_longlong * 2)()
+        self._L.sbc_batch_info(self._h, v, 2)
+        return {"chunks": v[0], "large_pairs": v[1]}
 
     def pairwise_info(self) -> dict:
         """Diagnostics of the last pairwise call."""

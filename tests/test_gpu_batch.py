@@ -96,11 +96,70 @@ def test_batch_statuses_and_empty_batch(cl):
     tiny = np.array([[0.0, 0.0], [1.0, 0.0]])
     huge = gen.star(sbclip.BATCH_MAX_VERTICES + 1, 7)
     rings, st = cl.clip_batch([b, tiny, b, huge], [c, c, tiny, c])
-    assert list(st) == [0, 1, 1, 1]
-    assert rings[1] == [] and rings[2] == [] and rings[3] == []
+    assert list(st) == [0, 1, 1, 0]
+    assert rings[1] == [] and rings[2] == []
     assert rings_equal(rings[0], cl.clip_pair(b, c))
+    assert rings_equal(rings[3], cl.clip_pair(huge, c))
+    assert cl.batch_info()["large_pairs"] == 1
     area, st = cl.area_forward([], [])
     assert len(area) == 0
+
+
+def _mixed(seed):
+    """Small pairs with large ones (a polygon above the per-thread limit) mixed in."""
+    import sbclip
+    pairs = gen.small_pairs(300, seed=seed)
+    big = sbclip.BATCH_MAX_VERTICES + 500
+    pairs.insert(7, (gen.star(big, seed + 1), gen.star(300, seed + 2, centre=(0.2, -0.1))))
+    pairs.insert(150, (gen.star(250, seed + 3), gen.star(big, seed + 4, centre=(-0.1, 0.15))))
+    pairs.append((gen.star(big + 100, seed + 5), gen.star(big, seed + 6, centre=(0.3, 0.1))))
+    return pairs
+
+
+def test_batch_large_pairs_rings_areas_gradients(cl):
+    pairs = _mixed(4500)
+    bases, ovs = [b for b, _ in pairs], [c for _, c in pairs]
+    rings, st = cl.clip_batch(bases, ovs)
+    assert (st == 0).all()
+    assert cl.batch_info()["large_pairs"] == 3
+    for i in (7, 150, len(pairs) - 1, 0, 99):
+        assert rings_equal(rings[i], cl.clip_pair(bases[i], ovs[i])), i
+    area, st = cl.area_forward(bases, ovs)
+    ga = np.random.default_rng(3).uniform(0.5, 2.0, len(pairs))
+    gb, gc = cl.area_backward(bases, ovs, ga)
+    for i in (7, 150, len(pairs) - 1):
+        want = AG.area(bases[i], ovs[i])
+        assert abs(area[i] - want) <= 1e-12 * max(1.0, abs(want)), i
+        _, hb, hc = AG.area_gradient(bases[i], ovs[i])
+        scale = max(np.abs(hb).max(), np.abs(hc).max(), 1e-300) * ga[i]
+        assert np.abs(gb[i] - ga[i] * hb).max() <= 1e-12 * scale, i
+        assert np.abs(gc[i] - ga[i] * hc).max() <= 1e-12 * scale, i
+
+
+def test_batch_chunks_match_one_chunk(cl):
+    """A tiny arena budget cuts the batch into many chunks; the backward pass
+    then recomputes each chunk's forward.  Results equal the one-chunk run."""
+    pairs = _mixed(4600)
+    bases, ovs = [b for b, _ in pairs], [c for _, c in pairs]
+    ga = np.random.default_rng(4).uniform(0.5, 2.0, len(pairs))
+    r1, s1 = cl.clip_batch(bases, ovs)
+    a1, _ = cl.area_forward(bases, ovs)
+    gb1, gc1 = cl.area_backward(bases, ovs, ga)
+    try:
+        cl.set_batch_arena_budget(2 << 20)
+        r2, s2 = cl.clip_batch(bases, ovs)
+        assert cl.batch_info()["chunks"] > 5
+        a2, _ = cl.area_forward(bases, ovs)
+        gb2, gc2 = cl.area_backward(bases, ovs, ga)
+    finally:
+        cl.set_batch_arena_budget(0)
+    assert np.array_equal(s1, s2) and np.array_equal(a1, a2)
+    assert all(rings_equal(x, y) for x, y in zip(r1, r2))
+    small = [i for i in range(len(pairs)) if i not in (7, 150, len(pairs) - 1)]
+    for i in small:
+        assert np.array_equal(gb1[i], gb2[i]) and np.array_equal(gc1[i], gc2[i]), i
+    for i in (7, 150, len(pairs) - 1):
+        assert np.allclose(gb1[i], gb2[i], rtol=1e-12, atol=1e-12 * np.abs(gb1[i]).max())
 
 
 def test_batch_device_arrays_match_host_arrays(cl):
