@@ -34,6 +34,13 @@ being `seg base overlay` (sbc_clip_pairwise): one step = all 10,000 pairs on
 device-resident inputs, reported as pairs per second, next to the plain
 per-pair GPU path and the reference run pairwise on the host cores.
 
+`--workload uneven_pairs_1m` measures 1,000,000 pairs with vertex counts
+log-uniform in [3, 2048] per polygon plus 16 pairs of 200,000 vertices mixed
+in: one step = every pair's intersection area and its gradient
+(sbc_area_forward_device + sbc_area_backward_device), with the arenas cut
+into chunks under the memory budget and each chunk's forward recomputed for
+the backward pass.
+
 `--impl reference` times the reference's own CPU (OpenMP) build
 (oracle/_ref/seg, all host threads) on the same workload; when that build is
 absent, the C restatement of the same algorithm (one thread).
@@ -615,6 +622,127 @@ def run_one_to_many(args, rank: int, world: int):
     return out
 
 
+UNEVEN = (1_000_000, 16)
+UNEVEN_METRIC = ("clipped pairs/s, area forward+backward, 1M uneven pairs (3-2048 vertices) "
+                 "+ 16 pairs of 200k")
+
+
+def uneven_workload():
+    n, nl = UNEVEN
+    bxy, boff, cxy, coff = gen.uneven_pairs(n, nl, seed=5000)
+    desc = {"workload": "uneven_pairs_1m", "pairs": n + nl, "large_pairs": nl,
+            "vertices": int(boff[-1] + coff[-1]),
+            "generator": "plain stars, sizes log-U[3,2048], stratified angles, overlay centre "
+                         "U[-0.5,0.5]^2; 16 jagged 200k-vertex pairs (R=1000) mixed in"}
+    return bxy, boff, cxy, coff, desc
+
+
+def run_uneven(args, rank: int, world: int):
+    """One step = areas and area gradients of every pair on device arrays."""
+    import torch
+    import sbclip
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    bxy, boff, cxy, coff, desc = uneven_workload()
+    n = len(boff) - 1
+    cuda = f"cuda:{dev}"
+    t = {k: torch.from_numpy(v).to(cuda) for k, v in
+         (("bxy", bxy), ("boff", boff), ("cxy", cxy), ("coff", coff))}
+    area = torch.zeros(n, dtype=torch.float64, device=cuda)
+    st = torch.zeros(n, dtype=torch.int32, device=cuda)
+    ga = torch.ones(n, dtype=torch.float64, device=cuda)
+    gb = torch.zeros_like(t["bxy"])
+    gc = torch.zeros_like(t["cxy"])
+    clip = sbclip.Clipper(dev)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    a = (n, t["bxy"].data_ptr(), t["boff"].data_ptr(), t["cxy"].data_ptr(), t["coff"].data_ptr())
+
+    def step():
+        clip.area_forward_device(*a, area.data_ptr(), st.data_ptr(), sp)
+        clip.area_backward_device(*a, ga.data_ptr(), gb.data_ptr(), gc.data_ptr(), sp)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    l0 = sbclip.kernel_launches()
+    times = []
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+    launches = sbclip.kernel_launches() - l0
+    binfo = clip.batch_info()
+    ms = float(np.mean(times))
+    n_ok = int((st == 0).sum().item())
+    torch.cuda.synchronize()
+    sbclip.profile_begin()
+    step()
+    torch.cuda.synchronize()
+    prof_b = sbclip.profile_end(with_bytes=True)
+    prof = {k: (v[0], v[1]) for k, v in prof_b.items()}
+    # end to end through the host-array C ABI (the host backward runs its own forward)
+    t0 = time.perf_counter()
+    clip.area_forward_packed(bxy, boff, cxy, coff)
+    clip.area_backward_packed(bxy, boff, cxy, coff, np.ones(n))
+    e2e_ms = (time.perf_counter() - t0) * 1e3
+    in_bytes = bxy.nbytes + cxy.nbytes + boff.nbytes + coff.nbytes
+    e2e = {"value": n / (e2e_ms * 1e-3), "unit": "pairs/s",
+           "h2d_bytes_per_step": 2 * in_bytes + 8 * n,
+           "d2h_bytes_per_step": 12 * n + bxy.nbytes + cxy.nbytes, "steps": 1}
+    # the plain per-pair GPU path on a sample of the pairs
+    rng = np.random.default_rng(7)
+    pick = rng.choice(n, 128, replace=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for p in pick:
+        clip.clip_pair_device(t["bxy"].data_ptr() + 16 * int(boff[p]), int(boff[p + 1] - boff[p]),
+                              t["cxy"].data_ptr() + 16 * int(coff[p]), int(coff[p + 1] - coff[p]),
+                              sp)
+    torch.cuda.synchronize()
+    per_pair = len(pick) / (time.perf_counter() - t0)
+    pk, kind = peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][0]) if prof else None
+    roof = None
+    if dom:
+        name, (tot_ms, n_l) = dom
+        ab = prof_b[name][2] / max(n_l, 1)
+        achieved = ab / (tot_ms / max(n_l, 1) * 1e-3) / 1e9
+        roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
+                "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "traffic": None,
+                "peak_source": kind, "ms_per_launch": tot_ms / max(n_l, 1)}
+    value = n / (ms * 1e-3)
+    out = {
+        "metric": UNEVEN_METRIC, "value": value, "unit": "pairs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded star polygons)",
+        "config": dict(desc, parallelism="single", l2="inputs (10 GB) larger than L2",
+                       arena_chunks=binfo["chunks"]),
+        "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
+        "kernels_top": {k: {"ms_per_step": v[0], "launches_per_step": v[1]}
+                        for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])[:8]},
+        "clocks": clk.summary(),
+        "counts": {"pairs_ok": n_ok, "large_pairs": binfo["large_pairs"],
+                   "per_pair_gpu_path_pairs_per_s": per_pair, "per_pair_sample": len(pick),
+                   "batched_over_per_pair": value / per_pair},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        sample = [(bxy[boff[p]:boff[p + 1]], cxy[coff[p]:coff[p + 1]]) for p in pick[:64]]
+        v, cores, kind2 = reference_pairs_per_s(sample, os.cpu_count() or 1)
+        out["cpu_baseline"] = {"value": v, "unit": "pairs/s", "cores": cores, "kind": kind2,
+                               "sample": "64 random pairs clipped pairwise (forward only)"}
+    clip.close()
+    return out
+
+
 def run_reference_arm(args):
     if args.workload.startswith("one_to_many"):
         base, ovs, desc = one_to_many_workload()
@@ -676,7 +804,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="pair_1m_1m",
                     choices=["pair_1m_1m", "pair_200k_200k", "pair_10k_8k", "small_pairs_65536",
-                             "one_to_many_200k_10000"])
+                             "one_to_many_200k_10000", "uneven_pairs_1m"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--job-only", type=int, default=0,
                     help="one_to_many only: run the job this many times and print no JSON "
@@ -697,6 +825,8 @@ def main():
         out = run_small_pairs(args, rank, world)
     elif args.workload.startswith("one_to_many"):
         out = run_one_to_many(args, rank, world)
+    elif args.workload.startswith("uneven"):
+        out = run_uneven(args, rank, world)
     else:
         out = run_gb300(args, rank, world)
     if rank == 0 and out is not None:

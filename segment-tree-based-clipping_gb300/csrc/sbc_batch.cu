@@ -18,6 +18,7 @@
 // - A(b2,c1,c2)).  The forward pass stores that provenance ("tape"); the
 // backward pass chains d(area)/d(vertex) through it with the combinatorial
 // structure held fixed.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -81,6 +82,8 @@ struct PairWork {
   // back end
   Pool P, Q, R;
   int *rroot, *counts;
+  // between the three kernels of a pair: [0] front status, [1] logL, [2] hits
+  int* state;
   unsigned char *splitP, *splitQ, *crossP, *crossQ;
   // output: ring offsets, ring xy, provenance
   int* roff;
@@ -155,6 +158,7 @@ __host__ __device__ __forceinline__ PairWork carve(Carver& cv, const Caps& c) {
   carve_pool(cv, c.capR, w.R);
   w.rroot = cv.take<int>(c.rcap);
   w.counts = cv.take<int>(4);
+  w.state = cv.take<int>(4);
   w.splitP = cv.take<unsigned char>(c.capP);
   w.crossP = cv.take<unsigned char>(c.capP);
   w.splitQ = cv.take<unsigned char>(c.capQ);
@@ -171,12 +175,14 @@ __host__ __device__ __forceinline__ size_t arena_bytes(int nb, int nc, int K) {
   return (cv.off + 255) & ~(size_t)255;
 }
 
-// hit capacity of a pair: generous for star-like polygons; a pair that needs
-// more is run again with the full product
-__host__ __device__ __forceinline__ int hit_cap(int nb, int nc, int pass) {
+// hit capacity of a pair: generous for star-like polygons in the first
+// pass; a pair that needs more runs again with the count its first pass
+// found (need)
+__host__ __device__ __forceinline__ int hit_cap(int nb, int nc, int pass, int need) {
   const long long full = (long long)nb * nc;
   const long long first = (long long)nb + nc + 16;
-  const long long k = pass == 0 ? (first < full ? first : full) : full;
+  long long k = pass == 0 ? (first < full ? first : full) : need;
+  if (k > full) k = full;
   return (int)(k > 0 ? k : 1);
 }
 
@@ -227,12 +233,16 @@ struct PairResult {
   int nrings;
   int nverts;
   double area;
+  int need;  // PS_CAP: the hit count the candidate stage found
 };
 
 // ------------------------------------------------------------------ one pair
-__device__ PairResult clip_pair_serial(const double* b, int nb, const double* c, int nc,
-                                       const Caps& cp, PairWork& w) {
-  PairResult res{PS_OK, 0, 0, 0.0};
+// Three kernels per pair: the front (rows A1-A7, one thread), the candidate
+// pairs (A8, one warp) and the rest (A9-A18, one thread); w.state carries
+// the front's status, logL and the hit count between them.
+__device__ int clip_pair_front(const double* b, int nb, const double* c, int nc, const Caps& cp,
+                               PairWork& w) {
+  PairResult res{PS_OK, 0, 0, 0.0, 0};
   const int E = nb + nc, n2 = 2 * E;
   // ---- A1 edges (edge.h:190-202); ids are offsets into the interleaved arrays
   double minI = bvx(b, nb, 0), maxI = minI;
@@ -300,7 +310,7 @@ __device__ PairResult clip_pair_serial(const double* b, int nb, const double* c,
   }
   if (count < 1) {
     res.status = PS_UNDEF;
-    return res;
+    return res.status;
   }
   const int epc = npow2_dev(count) + 1;
   for (int i = count; i < epc; ++i) ea[i] = ea[count - 1];
@@ -312,7 +322,7 @@ __device__ PairResult clip_pair_serial(const double* b, int nb, const double* c,
   const double dv = dadd(maxI, absMin);
   if (!(dv < 2147483647.0)) {
     res.status = PS_UNDEF;
-    return res;
+    return res.status;
   }
   int digits = 1;
   for (int iv = (int)trunc(dv); iv / 10 > 0; iv /= 10) ++digits;
@@ -329,7 +339,7 @@ __device__ PairResult clip_pair_serial(const double* b, int nb, const double* c,
       const long long ki = key(i);
       if (ki < 0 || ki >= 100000000000LL || (i + 1 < epc && key(i + 1) < ki)) {
         res.status = PS_UNDEF;
-        return res;
+        return res.status;
       }
       if (ki == 0) ++z;
     }
@@ -374,33 +384,61 @@ __device__ PairResult clip_pair_serial(const double* b, int nb, const double* c,
     }
     w.lr[e] = make_int2(l, lo > l ? lo : l);
   }
-  // ---- A8 candidate pairs: all base x overlay edge pairs, float boxes first
-  int K = 0;
-  for (int be = 0; be < nb; ++be) {
+  w.state[1] = logL;
+  w.state[2] = 0;
+  return PS_OK;
+}
+
+// A8 for one pair by one warp: every base x overlay edge pair, float boxes
+// first; lanes take the pairs in strides of 32 (coalesced overlay boxes)
+__device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc, const Caps& cp,
+                               PairWork& w, int lane) {
+  const int logL = w.state[1];
+  int be = 0, j = lane;
+  while (j >= nc && be < nb) {
+    j -= nc;
+    ++be;
+  }
+  while (be < nb) {
     const float4 fb = w.fbox[be];
-    const double p1x = bvx(b, nb, be), p1y = bvy(b, nb, be);
-    const double p2x = bvx(b, nb, be + 1), p2y = bvy(b, nb, be + 1);
-    for (int j = 0; j < nc; ++j) {
-      const float4 fc = w.fbox[nb + j];
-      if (fb.x > fc.z || fb.z < fc.x || fb.y > fc.w || fb.w < fc.y) continue;
+    const float4 fc = w.fbox[nb + j];
+    if (!(fb.x > fc.z || fb.z < fc.x || fb.y > fc.w || fb.w < fc.y)) {
+      const double p1x = bvx(b, nb, be), p1y = bvy(b, nb, be);
+      const double p2x = bvx(b, nb, be + 1), p2y = bvy(b, nb, be + 1);
       const double q1x = bvx(c, nc, j), q1y = bvy(c, nc, j);
       const double q2x = bvx(c, nc, j + 1), q2y = bvy(c, nc, j + 1);
-      if (!lsmf_d(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y)) continue;
-      double al, bt;
-      const int ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
-      if (!ty) continue;
-      unsigned long long key;
-      if (emission_s(be, nb + j, 2 * j, w, logL, &key) == 0) continue;
-      if (K >= cp.K) {
-        res.status = PS_CAP;
-        return res;
+      if (lsmf_d(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y)) {
+        double al, bt;
+        const int ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
+        unsigned long long key;
+        if (ty && emission_s(be, nb + j, 2 * j, w, logL, &key) > 0) {
+          // out of room: only counted, for the retry's capacity
+          const int k = atomicAdd(&w.state[2], 1);
+          if (k < cp.K) {
+            w.hb[k] = 2 * be;
+            w.hc[k] = 2 * j;
+            w.ht[k] = ty;
+            w.hkey[k] = key;
+          }
+        }
       }
-      w.hb[K] = 2 * be;
-      w.hc[K] = 2 * j;
-      w.ht[K] = ty;
-      w.hkey[K] = key;
-      ++K;
     }
+    j += 32;
+    while (j >= nc && be < nb) {
+      j -= nc;
+      ++be;
+    }
+  }
+}
+
+__device__ PairResult clip_pair_back(const double* b, int nb, const double* c, int nc,
+                                     const Caps& cp, PairWork& w) {
+  PairResult res{PS_OK, 0, 0, 0.0, 0};
+  const int K = w.state[2];
+  if (K > cp.K) {
+    res.status = PS_CAP;
+    res.need = K;
+    return res;
   }
   // ---- A9 unique records in the reference's order: base id, then first key
   for (int i = 0; i < K; ++i) w.hord[i] = i;
@@ -481,6 +519,12 @@ __device__ PairResult clip_pair_serial(const double* b, int nb, const double* c,
       if (ndPS[e + 1] - ndPS[e] <= 1) continue;
       for (int i = s; i < t; ++i)
         if (alpha[order ? order[i] : i] < 0) return false;
+      if (t - s > 32) {  // a long run (an edge crossed many times): stable merge sort
+        merge_sort(sorted + s, w.hord + s, t - s, [&](int x, int y) {
+          return alpha[order ? order[x] : x] % 1000000000 < alpha[order ? order[y] : y] % 1000000000;
+        });
+        continue;
+      }
       for (int i = s + 1; i < t; ++i) {  // stable insertion by alpha mod 1e9
         const int p = sorted[i];
         const int kp = alpha[order ? order[p] : p] % 1000000000;
@@ -738,7 +782,7 @@ __device__ PairResult clip_pair_serial(const double* b, int nb, const double* c,
 // ------------------------------------------------------------------ kernels
 __global__ void k_batch_size(int np, const long long* __restrict__ boff,
                              const long long* __restrict__ coff, const int* __restrict__ pass_of,
-                             long long* __restrict__ bytes) {
+                             const int* __restrict__ need, long long* __restrict__ bytes) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p > np) return;
   if (p == np) {
@@ -748,35 +792,107 @@ __global__ void k_batch_size(int np, const long long* __restrict__ boff,
   const int nb = (int)(boff[p + 1] - boff[p]), nc = (int)(coff[p + 1] - coff[p]);
   const int pass = pass_of ? pass_of[p] : 0;
   const bool ok = nb >= 3 && nc >= 3 && nb <= SBC_BATCH_MAX_VERTICES && nc <= SBC_BATCH_MAX_VERTICES;
-  bytes[p] = (ok && pass >= 0) ? (long long)arena_bytes(nb, nc, hit_cap(nb, nc, pass)) : 0;
+  bytes[p] = (ok && pass >= 0)
+                 ? (long long)arena_bytes(nb, nc, hit_cap(nb, nc, pass, need ? need[p] : 0))
+                 : 0;
 }
 
-// per pair: status, rings, vertices, area (and the arena holds its rings/tape)
-__global__ void __launch_bounds__(kBatchBlock)
-k_batch_clip(int np, const double* __restrict__ bxy, const long long* __restrict__ boff,
-             const double* __restrict__ cxy, const long long* __restrict__ coff,
-             const int* __restrict__ pass_of, unsigned char* __restrict__ arena,
-             const long long* __restrict__ aoff, long long abase, int* __restrict__ status,
-             int* __restrict__ nrings, int* __restrict__ nverts, double* __restrict__ area) {
+// The three kernels of a chunk: per pair status, rings, vertices, area (and
+// the arena holds its rings and tape).  Arguments common to the three:
+struct ClipArgs {
+  int np;
+  const double* bxy;
+  const long long* boff;
+  const double* cxy;
+  const long long* coff;
+  const int* pass_of;  // null: every pair, pass 0
+
+  unsigned char* arena;
+  const long long* aoff;
+  long long abase;
+  int* need;
+  int* status;
+  int* nrings;
+  int* nverts;
+  double* area;
+  __device__ bool small(int p, int* nb, int* nc) const {
+    *nb = (int)(boff[p + 1] - boff[p]);
+    *nc = (int)(coff[p + 1] - coff[p]);
+    return *nb >= 3 && *nc >= 3 && *nb <= SBC_BATCH_MAX_VERTICES && *nc <= SBC_BATCH_MAX_VERTICES;
+  }
+  __device__ PairWork work(int p, int nb, int nc, int pass, Caps* cp) const {
+    *cp = caps_of(nb, nc, hit_cap(nb, nc, pass, need[p]));
+    Carver cv{arena + (aoff[p] - abase), 0};
+    return carve(cv, *cp);
+  }
+};
+
+__global__ void __launch_bounds__(kBatchBlock) k_batch_front(ClipArgs A) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= np) return;
-  const int pass = pass_of ? pass_of[p] : 0;
-  if (pass < 0) return;  // settled in an earlier pass
-  const int nb = (int)(boff[p + 1] - boff[p]), nc = (int)(coff[p + 1] - coff[p]);
-  if (nb < 3 || nc < 3 || nb > SBC_BATCH_MAX_VERTICES || nc > SBC_BATCH_MAX_VERTICES) {
-    status[p] = SBC_EINPUT;
-    nrings[p] = nverts[p] = 0;
-    area[p] = 0.0;
+  if (p >= A.np) return;
+  const int pass = A.pass_of ? A.pass_of[p] : 0;
+  if (pass < 0) return;  // settled in an earlier pass, or a large pair
+  int nb, nc;
+  if (!A.small(p, &nb, &nc)) {
+    A.status[p] = SBC_EINPUT;
+    A.nrings[p] = A.nverts[p] = 0;
+    A.area[p] = 0.0;
     return;
   }
-  const Caps cp = caps_of(nb, nc, hit_cap(nb, nc, pass));
-  Carver cv{arena + (aoff[p] - abase), 0};
-  PairWork w = carve(cv, cp);
-  const PairResult r = clip_pair_serial(bxy + 2 * boff[p], nb, cxy + 2 * coff[p], nc, cp, w);
-  status[p] = r.status == PS_OK ? SBC_OK : (r.status == PS_UNDEF ? SBC_EUNDEF : SBC_ENOMEM);
-  nrings[p] = r.nrings;
-  nverts[p] = r.nverts;
-  area[p] = r.area;
+  Caps cp;
+  PairWork w = A.work(p, nb, nc, pass, &cp);
+  const int st = clip_pair_front(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w);
+  w.state[0] = st;
+  if (st != PS_OK) {
+    A.status[p] = st == PS_UNDEF ? SBC_EUNDEF : SBC_ENOMEM;
+    A.nrings[p] = A.nverts[p] = 0;
+    A.area[p] = 0.0;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_batch_cand(ClipArgs A) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = (int)(t >> 5), lane = threadIdx.x & 31;
+  if (p >= A.np) return;
+  const int pass = A.pass_of ? A.pass_of[p] : 0;
+  int nb, nc;
+  if (pass < 0 || !A.small(p, &nb, &nc)) return;
+  Caps cp;
+  PairWork w = A.work(p, nb, nc, pass, &cp);
+  if (w.state[0] != PS_OK) return;
+  clip_pair_cand(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w, lane);
+}
+
+__global__ void __launch_bounds__(kBatchBlock) k_batch_back(ClipArgs A) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= A.np) return;
+  const int pass = A.pass_of ? A.pass_of[p] : 0;
+  int nb, nc;
+  if (pass < 0 || !A.small(p, &nb, &nc)) return;
+  Caps cp;
+  PairWork w = A.work(p, nb, nc, pass, &cp);
+  if (w.state[0] != PS_OK) return;
+  const PairResult r = clip_pair_back(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w);
+  A.status[p] = r.status == PS_OK ? SBC_OK : (r.status == PS_UNDEF ? SBC_EUNDEF : SBC_ENOMEM);
+  if (r.status == PS_CAP) A.need[p] = r.need;
+  A.nrings[p] = r.nrings;
+  A.nverts[p] = r.nverts;
+  A.area[p] = r.area;
+}
+
+void launch_clip(const ClipArgs& A, double in_bytes, cudaStream_t st) {
+  {
+    ::sbc::KProbe kp_("k_batch_front", st, in_bytes);
+    k_batch_front<<<grid_for(A.np, kBatchBlock), kBatchBlock, 0, st>>>(A);
+  }
+  {
+    ::sbc::KProbe kp_("k_batch_cand", st, in_bytes);
+    k_batch_cand<<<grid_for(32LL * A.np, 128), 128, 0, st>>>(A);
+  }
+  {
+    ::sbc::KProbe kp_("k_batch_back", st, in_bytes + 20.0 * A.np);
+    k_batch_back<<<grid_for(A.np, kBatchBlock), kBatchBlock, 0, st>>>(A);
+  }
 }
 
 __global__ void k_batch_counts(int np, const int* __restrict__ status, const int* __restrict__ nr,
@@ -799,6 +915,7 @@ struct Arenas {
   const long long* off1;
   long long abase1;
   const int* pass;  // per pair: 0, 1, or -1 (no arena: a large or invalid pair)
+  const int* need;  // per pair: the retry pass's hit capacity
   __device__ const unsigned char* at(int p) const {
     return pass[p] == 1 ? a1 + (off1[p] - abase1) : a0 + (off0[p] - abase0);
   }
@@ -816,7 +933,7 @@ __global__ void k_batch_pack(int np, const long long* __restrict__ boff,
   const int nr = (int)(rpre[p + 1] - r0);
   if (nr == 0 || status[p] != SBC_OK || ar.pass[p] < 0) return;
   const int nb = (int)(boff[p + 1] - boff[p]), nc = (int)(coff[p + 1] - coff[p]);
-  const Caps cp = caps_of(nb, nc, hit_cap(nb, nc, ar.pass[p]));
+  const Caps cp = caps_of(nb, nc, hit_cap(nb, nc, ar.pass[p], ar.need[p]));
   Carver cv{const_cast<unsigned char*>(ar.at(p)), 0};
   const PairWork w = carve(cv, cp);
   for (int r = 0; r < nr; ++r) ring_off[r0 + r] = v0 + w.roff[r];
@@ -841,7 +958,7 @@ k_batch_backward(int np, const double* __restrict__ bxy, const long long* __rest
   if (status[p] != SBC_OK || nrings[p] == 0 || ar.pass[p] < 0) return;
   const double* b = bxy + 2 * boff[p];
   const double* c = cxy + 2 * coff[p];
-  const Caps cp = caps_of(nb, nc, hit_cap(nb, nc, ar.pass[p]));
+  const Caps cp = caps_of(nb, nc, hit_cap(nb, nc, ar.pass[p], ar.need[p]));
   Carver cv{const_cast<unsigned char*>(ar.at(p)), 0};
   const PairWork w = carve(cv, cp);
   const double g = gA[p];
@@ -952,26 +1069,45 @@ __global__ void k_big_tape(int nv, const double* __restrict__ xy, int n,
   tape[v] = t;
 }
 
-// signed shoelace sum over every ring of one pair (one block, fixed order)
-__global__ void __launch_bounds__(1024) k_big_area(int nr, const int* __restrict__ off,
-                                                   const double* __restrict__ xy,
-                                                   double* __restrict__ area) {
-  __shared__ double part[1024];
+// signed shoelace sum over every ring of one pair: per-block partial sums
+// of the vertices' cross terms, then one block adds the partials (a fixed
+// order, so the result does not vary between runs)
+constexpr int kAreaBlocks = 256;
+
+__global__ void __launch_bounds__(256) k_big_area_part(int nr, int nv, const int* __restrict__ off,
+                                                       const double* __restrict__ xy,
+                                                       double* __restrict__ part) {
+  __shared__ double sh[256];
   double s = 0.0;
-  for (int r = 0; r < nr; ++r) {
-    const int a = off[r], e = off[r + 1];
-    for (int i = a + threadIdx.x; i < e; i += blockDim.x) {
-      const int j = (i + 1 == e) ? a : i + 1;
-      s += xy[2 * i] * xy[2 * j + 1] - xy[2 * j] * xy[2 * i + 1];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x) {
+    int lo = 0, hi = nr;  // the ring holding vertex i
+    while (hi - lo > 1) {
+      const int m = (lo + hi) >> 1;
+      if (off[m] <= i) lo = m;
+      else hi = m;
     }
+    const int j = (i + 1 == off[lo + 1]) ? off[lo] : i + 1;
+    s += xy[2 * i] * xy[2 * j + 1] - xy[2 * j] * xy[2 * i + 1];
   }
-  part[threadIdx.x] = s;
+  sh[threadIdx.x] = s;
   __syncthreads();
-  for (int w = 512; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) *area = 0.5 * part[0];
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void __launch_bounds__(kAreaBlocks) k_big_area_sum(const double* __restrict__ part,
+                                                              double* __restrict__ area) {
+  __shared__ double sh[kAreaBlocks];
+  sh[threadIdx.x] = part[threadIdx.x];
+  __syncthreads();
+  for (int w = kAreaBlocks / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *area = 0.5 * sh[0];
 }
 
 // d(area)/d(vertices) of one large pair, one thread per ring vertex
@@ -1033,6 +1169,7 @@ int BatchRunner::plan(int np_, const long long* d_boff, const long long* d_coff,
   aoff[0] = (long long*)pool.get("bt_aoff0", sizeof(long long) * (np + 1));
   aoff[1] = (long long*)pool.get("bt_aoff1", sizeof(long long) * (np + 1));
   pass = (int*)pool.get("bt_pass", sizeof(int) * (np + 1));
+  need_ = (int*)pool.get("bt_need", sizeof(int) * (np + 1));
   status = (int*)pool.get("bt_status", sizeof(int) * (np + 1));
   nrings = (int*)pool.get("bt_nrings", sizeof(int) * (np + 1));
   nverts = (int*)pool.get("bt_nverts", sizeof(int) * (np + 1));
@@ -1046,7 +1183,8 @@ int BatchRunner::plan(int np_, const long long* d_boff, const long long* d_coff,
   cudaMemcpyAsync(h_coff_.data(), d_coff, sizeof(long long) * (np + 1), cudaMemcpyDeviceToHost, st);
   {
     ::sbc::KProbe kp_("k_batch_size", st);
-    k_batch_size<<<grid_for(np + 1, 256), 256, 0, st>>>(np, d_boff, d_coff, nullptr, aoff[0]);
+    k_batch_size<<<grid_for(np + 1, 256), 256, 0, st>>>(np, d_boff, d_coff, nullptr, nullptr,
+                                                       aoff[0]);
   }
   exclusive_scan_i64(aoff[0], np + 1, sscr_, st);
   cudaMemcpyAsync(h_aoff0_.data(), aoff[0], sizeof(long long) * (np + 1), cudaMemcpyDeviceToHost,
@@ -1104,15 +1242,12 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
     hp[i] = (nb >= 3 && nc >= 3 && !is_small[i]) ? -1 : 0;
   }
   cudaMemcpyAsync(pass + p0, hp.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
-  {
-    // coordinates in; area, status, ring and vertex counts out
-    ::sbc::KProbe kp_("k_batch_clip", st,
-                      16.0 * (double)(h_boff_[p1] - h_boff_[p0] + h_coff_[p1] - h_coff_[p0]) +
-                          20.0 * n);
-    k_batch_clip<<<grid_for(n, kBatchBlock), kBatchBlock, 0, st>>>(
-        n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[0], aoff[0] + p0, abase_[0],
-        status + p0, nrings + p0, nverts + p0, area + p0);
-  }
+  // coordinates in; area, status, ring and vertex counts out
+  const double in_bytes =
+      16.0 * (double)(h_boff_[p1] - h_boff_[p0] + h_coff_[p1] - h_coff_[p0]);
+  launch_clip(ClipArgs{n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[0], aoff[0] + p0,
+                       abase_[0], need_ + p0, status + p0, nrings + p0, nverts + p0, area + p0},
+              in_bytes, st);
   std::vector<int> hs(n);
   cudaMemcpyAsync(hs.data(), status + p0, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch clip");
@@ -1131,7 +1266,7 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
     {
       ::sbc::KProbe kp_("k_batch_size", st);
       k_batch_size<<<grid_for(n + 1, 256), 256, 0, st>>>(n, d_boff + p0, d_coff + p0, pass + p0,
-                                                         aoff[1] + p0);
+                                                         need_ + p0, aoff[1] + p0);
     }
     exclusive_scan_i64(aoff[1] + p0, n + 1, sscr_, st);
     long long total = 0;
@@ -1139,12 +1274,10 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
     if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch sizes");
     arena[1] = (unsigned char*)pool.get("bt_arena1", (size_t)total + 256);
     if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch arena)");
-    {
-      ::sbc::KProbe kp_("k_batch_clip", st);
-      k_batch_clip<<<grid_for(n, kBatchBlock), kBatchBlock, 0, st>>>(
-          n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[1], aoff[1] + p0, 0,
-          status + p0, nrings + p0, nverts + p0, area + p0);
-    }
+    launch_clip(ClipArgs{n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[1],
+                         aoff[1] + p0, 0, need_ + p0, status + p0, nrings + p0, nverts + p0,
+                         area + p0},
+                in_bytes, st);
   }
   // where each pair's data lives now: pass 0 arena, retry arena, or none
   for (int i = 0; i < n; ++i) {
@@ -1222,8 +1355,11 @@ int BatchRunner::run_big(const double* d_bxy, const double* d_cxy, cudaStream_t 
               bo.nverts, bo.xy, n, k2, k3, val, nb, nc, pl_.dbg_ub, pl_.dbg_uc, bo.tape);
         }
         {
+          double* part = (double*)pool.get("bt_big_part", sizeof(double) * kAreaBlocks);
+          if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (large pair)");
           ::sbc::KProbe kp_("k_big_area", st, 16.0 * bo.nverts);
-          k_big_area<<<1, 1024, 0, st>>>(bo.nrings, bo.off, bo.xy, area + p);
+          k_big_area_part<<<kAreaBlocks, 256, 0, st>>>(bo.nrings, bo.nverts, bo.off, bo.xy, part);
+          k_big_area_sum<<<1, kAreaBlocks, 0, st>>>(part, area + p);
         }
       } else {
         cudaMemsetAsync(area + p, 0, sizeof(double), st);
@@ -1293,7 +1429,8 @@ int BatchRunner::rings(const double* d_bxy, const long long* d_boff, const doubl
       if (rc) return rc;
     }
     const int p0 = chunks_[c].first, n = chunks_[c].second - p0;
-    const Arenas ar{arena[0], aoff[0] + p0, abase_[0], arena[1], aoff[1] + p0, abase_[1], pass + p0};
+    const Arenas ar{arena[0], aoff[0] + p0, abase_[0], arena[1], aoff[1] + p0, abase_[1], pass + p0,
+                    need_ + p0};
     ::sbc::KProbe kp_("k_batch_pack", st);
     k_batch_pack<<<grid_for(n, 128), 128, 0, st>>>(n, d_boff + p0, d_coff + p0, ar, status + p0,
                                                    rpre + p0, vpre + p0, roff, oxy);
@@ -1327,7 +1464,8 @@ int BatchRunner::backward(const double* d_bxy, const long long* d_boff, const do
       if (rc) return rc;
     }
     const int p0 = chunks_[c].first, p1 = chunks_[c].second, n = p1 - p0;
-    const Arenas ar{arena[0], aoff[0] + p0, abase_[0], arena[1], aoff[1] + p0, abase_[1], pass + p0};
+    const Arenas ar{arena[0], aoff[0] + p0, abase_[0], arena[1], aoff[1] + p0, abase_[1], pass + p0,
+                    need_ + p0};
     // coordinates in, one gradient per coordinate out
     ::sbc::KProbe kp_("k_batch_backward", st,
                       32.0 * (double)(h_boff_[p1] - h_boff_[p0] + h_coff_[p1] - h_coff_[p0]) +

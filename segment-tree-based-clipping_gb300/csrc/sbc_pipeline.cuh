@@ -206,6 +206,7 @@ class BatchRunner {
   long long* aoff[2] = {nullptr, nullptr};
   long long abase_[2] = {0, 0};
   int* pass = nullptr;
+  int* need_ = nullptr;          // per pair: hits found by a first pass that ran out of room
   void* sscr_ = nullptr;
   std::vector<long long> h_boff_, h_coff_, h_aoff0_;
   std::vector<std::pair<int, int>> chunks_;

@@ -378,6 +378,28 @@ class Clipper:
                                              st.ctypes.data, stream))
         return area, st
 
+    def area_forward_packed(self, bxy, boff, cxy, coff, stream: int | None = None):
+        """sbc_area_forward on packed host arrays (pack_polygons): (area, status)."""
+        b = _Batch(len(boff) - 1, bxy.ctypes.data, boff.ctypes.data, cxy.ctypes.data,
+                   coff.ctypes.data)
+        n = len(boff) - 1
+        area = np.zeros(n, np.float64)
+        st = np.zeros(n, np.int32)
+        self._check(self._L.sbc_area_forward(self._h, ctypes.byref(b), area.ctypes.data,
+                                             st.ctypes.data, stream))
+        return area, st
+
+    def area_backward_packed(self, bxy, boff, cxy, coff, grad_area, stream: int | None = None):
+        """sbc_area_backward on packed host arrays: (grad_b, grad_c) packed like bxy, cxy."""
+        b = _Batch(len(boff) - 1, bxy.ctypes.data, boff.ctypes.data, cxy.ctypes.data,
+                   coff.ctypes.data)
+        ga = np.ascontiguousarray(grad_area, dtype=np.float64)
+        gb = np.empty_like(bxy)
+        gc = np.empty_like(cxy)
+        self._check(self._L.sbc_area_backward(self._h, ctypes.byref(b), ga.ctypes.data,
+                                              gb.ctypes.data, gc.ctypes.data, stream))
+        return gb, gc
+
     def area_backward(self, bases, overlays, grad_area, stream: int | None = None):
         """d(sum grad_area * area)/d(vertices): (list of (nb,2), list of (nc,2))."""
         b, keep = self._batch(bases, overlays)

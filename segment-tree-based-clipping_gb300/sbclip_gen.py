@@ -12,6 +12,13 @@ shapes and sizes of the benchmark configurations:
 * ``pair_small``      10k x 8k plain stars (base at (0,0), overlay at (0.3,0.2)).
 * ``pair_large``      1M x 1M jagged stars, R = 1000; overlay offset
                       (0.25R, 0.1R) and rotated 0.3 rad about its centre.
+* ``uneven_pairs``    many independent pairs with vertex counts log-uniform in
+                      [3, 2048] per polygon (plain stars, overlay centre offset
+                      U[-0.5,0.5]^2; angles stratified: vertex k at
+                      2pi (k + u_k) / n, so each polygon is simple without a
+                      per-polygon sort), plus a few large jagged pairs (the
+                      ``pair_large`` generator at 200k vertices) mixed in;
+                      returned packed.
 * ``one_to_many``     one jagged base (200k vertices, R = 1000) against many
                       plain-star overlays: sizes log-uniform in [4, 5000], radii
                       log-uniform in [0.001R, 0.05R], centres uniform in the
@@ -165,6 +172,48 @@ def one_to_many(n_base: int = 200_000, n_overlays: int = 10_000, seed: int = 300
     overlays = [star(int(n), int(s), centre=(float(c[0]), float(c[1])), R=float(r))
                 for n, s, c, r in zip(sizes, seeds, centres, radii)]
     return base, overlays
+
+
+def uneven_pairs(n_pairs: int = 1_000_000, n_large: int = 16, seed: int = 5000, lo: int = 3,
+                 hi: int = 2048, large: int = 200_000, chunk: int = 65536):
+    """Packed (bxy, boff, cxy, coff) of n_pairs + n_large pairs; the large pairs
+    sit at evenly spaced positions."""
+    rng = np.random.default_rng(seed)
+    total = n_pairs + n_large
+    large_at = set(int(round((i + 0.5) * total / max(n_large, 1))) for i in range(n_large))
+    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi + 1), (total, 2))).astype(np.int64)
+    sizes = np.clip(sizes, lo, hi)
+    for q in large_at:
+        sizes[q] = (large, large)
+    boff = np.zeros(total + 1, np.int64)
+    coff = np.zeros(total + 1, np.int64)
+    boff[1:] = np.cumsum(sizes[:, 0])
+    coff[1:] = np.cumsum(sizes[:, 1])
+    bxy = np.empty((int(boff[-1]), 2))
+    cxy = np.empty((int(coff[-1]), 2))
+    centres = rng.uniform(-0.5, 0.5, (total, 2))
+
+    def fill(out, off, p0, p1, centre):
+        n = sizes[p0:p1, 0 if out is bxy else 1]
+        m = int(n.sum())
+        seg = np.repeat(np.arange(p1 - p0), n)
+        k = np.arange(m) - np.repeat(off[p0:p1] - off[p0], n)
+        th = TWO_PI * (k + rng.uniform(0.0, 1.0, m)) / np.repeat(n, n)
+        r = 0.5 + 0.5 * rng.uniform(0.0, 1.0, m)
+        sl = slice(int(off[p0]), int(off[p1]))
+        out[sl, 0] = centre[seg, 0] + r * np.cos(th)
+        out[sl, 1] = centre[seg, 1] + r * np.sin(th)
+
+    zero = np.zeros((total, 2))
+    for p0 in range(0, total, chunk):
+        p1 = min(total, p0 + chunk)
+        fill(bxy, boff, p0, p1, zero[p0:p1])
+        fill(cxy, coff, p0, p1, centres[p0:p1])
+    for i, q in enumerate(sorted(large_at)):
+        b, c = pair_large(large, seed_base=seed + 10 * i)
+        bxy[boff[q]:boff[q + 1]] = b
+        cxy[coff[q]:coff[q + 1]] = c
+    return bxy, boff, cxy, coff
 
 
 def small_pairs(npairs: int, seed: int = 4000, lo: int = 4, hi: int = 64):
