@@ -365,13 +365,17 @@ def run_small_pairs(args, rank: int, world: int):
     gc = torch.zeros_like(t["cxy"])
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=cuda)
     clip = sbclip.Clipper(dev)
-    stream = torch.cuda.current_stream()
+    # an explicit stream: the graph runs, and the events time it, on one stream
+    stream = torch.cuda.Stream(device=dev)
     sp = stream.cuda_stream
     a = (n, t["bxy"].data_ptr(), t["boff"].data_ptr(), t["cxy"].data_ptr(), t["coff"].data_ptr())
 
+    # the whole forward + backward step as one CUDA graph, recorded once
+    graph = clip.area_graph(*a, ga.data_ptr(), gb.data_ptr(), gc.data_ptr(), area.data_ptr(),
+                            st.data_ptr(), sp)
+
     def step():
-        clip.area_forward_device(*a, area.data_ptr(), st.data_ptr(), sp)
-        clip.area_backward_device(*a, ga.data_ptr(), gb.data_ptr(), gc.data_ptr(), sp)
+        graph.launch(sp)
 
     for _ in range(args.warmup):
         step()
@@ -400,12 +404,15 @@ def run_small_pairs(args, rank: int, world: int):
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         ms = float(tt.item())
     n_ok = int((st == 0).sum().item())
-    # per-kernel times of one more step
+    # per-kernel times of one more step, run as the separate calls the graph
+    # was recorded from (a graph replay has no per-launch events)
     torch.cuda.synchronize()
     sbclip.profile_begin()
-    step()
+    clip.area_forward_device(*a, area.data_ptr(), st.data_ptr(), sp)
+    clip.area_backward_device(*a, ga.data_ptr(), gb.data_ptr(), gc.data_ptr(), sp)
     torch.cuda.synchronize()
     prof_b = sbclip.profile_end(with_bytes=True)
+    graph.close()
     prof = {k: (v[0], v[1]) for k, v in prof_b.items()}
     # end to end through the host-array C ABI: inputs copied in, areas and
     # gradients copied out (the host backward call runs its own forward)
@@ -447,7 +454,8 @@ def run_small_pairs(args, rank: int, world: int):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded star polygons)",
         "config": dict(desc, parallelism="pairs sharded by rank" if world > 1 else "single",
-                       l2="flushed between steps (256 MiB write)"),
+                       l2="flushed between steps (256 MiB write)",
+                       launch="one CUDA graph per step (area forward + backward)"),
         "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
         "kernels_top": {k: {"ms_per_step": v[0], "launches_per_step": v[1]}
                         for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])[:6]},

@@ -227,6 +227,26 @@ int sbc_pairwise_set_split(sbc_ctx* ctx, int records);
 int sbc_pairwise_autotune(sbc_ctx* ctx, const sbc_pairwise_job* job, int* split,
                           double* cell_factor, double* best_ms, void* stream);
 
+/* The area forward + backward of one batch as a single CUDA graph launch.
+ * sbc_area_graph_create runs the batch once (device arrays, as for the
+ * _device calls) to fix its arena chunk, scratch buffers and the pairs that
+ * need a second pass with more hit room, then records pass one, the second
+ * pass, the backward pass and copies of area and status (either may be NULL)
+ * into a graph.  sbc_area_graph_launch replays it on `stream`: the batch's
+ * arrays are read anew, so new coordinates of the same polygons give new
+ * areas and gradients; a pair that now needs more hit room than recorded
+ * reports SBC_ENOMEM in its status (re-create the graph then).  The graph
+ * uses the context's batch buffers: a later batched call on the context makes
+ * it stale and sbc_area_graph_launch then fails with SBC_EINPUT.  Needs a
+ * batch that fits one arena chunk with no polygon above SBC_BATCH_MAX_VERTICES
+ * vertices. */
+typedef struct sbc_graph sbc_graph;
+int sbc_area_graph_create(sbc_ctx* ctx, const sbc_batch* batch, const double* grad_area,
+                          double* grad_b, double* grad_c, double* area, int* status,
+                          void* stream, sbc_graph** out);
+int sbc_area_graph_launch(sbc_graph* graph, void* stream);
+void sbc_area_graph_destroy(sbc_graph* graph);
+
 /* Bytes of per-pair scratch arenas one chunk of a batch may hold (0: the
  * smaller of 96 GiB and half of the device's free memory).  A batch larger
  * than one chunk runs chunk by chunk; its backward pass then recomputes each

@@ -763,3 +763,54 @@ extern "C" int sbc_batch_info(const sbc_ctx* c, long long* out, int n) {
   for (int i = 0; i < n && i < 2; ++i) out[i] = v[i];
   return SBC_OK;
 }
+
+struct sbc_graph {
+  sbc_ctx* ctx = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  unsigned long long kernels = 0;
+  unsigned long long generation = 0;
+};
+
+extern "C" int sbc_area_graph_create(sbc_ctx* c, const sbc_batch* b, const double* grad_area,
+                                     double* grad_b, double* grad_c, double* area, int* status,
+                                     void* stream, sbc_graph** out) {
+  if (!out) return set_err(c, SBC_EINPUT, "null output");
+  *out = nullptr;
+  int rc = batch_check(c, b);
+  if (rc) return rc;
+  if (!grad_area || !grad_b || !grad_c) return set_err(c, SBC_EINPUT, "null gradient array");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  c->pl->set_stream(st);
+  c->pl->clear_error();
+  auto* g = new (std::nothrow) sbc_graph();
+  if (!g) return set_err(c, SBC_ENOMEM, "graph");
+  rc = c->br->graph_record(b->npairs, b->b_xy, b->b_off, b->c_xy, b->c_off, grad_area, grad_b,
+                           grad_c, area, status, st, &g->exec, &g->kernels);
+  if (rc) {
+    delete g;
+    return set_err(c, rc, c->pl->error());
+  }
+  g->ctx = c;
+  g->generation = c->br->generation;
+  *out = g;
+  return SBC_OK;
+}
+
+extern "C" int sbc_area_graph_launch(sbc_graph* g, void* stream) {
+  if (!g || !g->exec) return SBC_EINPUT;
+  sbc_ctx* c = g->ctx;
+  if (c->br->generation != g->generation)
+    return set_err(c, SBC_EINPUT, "stale graph: a later batched call replaced its buffers");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  const int rc = cuda_check(c, cudaGraphLaunch(g->exec, st), "graph launch");
+  if (!rc) sbc::g_launches += g->kernels;
+  return rc;
+}
+
+extern "C" void sbc_area_graph_destroy(sbc_graph* g) {
+  if (!g) return;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  delete g;
+}

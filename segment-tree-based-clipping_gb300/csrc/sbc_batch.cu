@@ -810,7 +810,8 @@ struct ClipArgs {
   unsigned char* arena;
   const long long* aoff;
   long long abase;
-  int* need;
+  int* need;            // written: the hit count of a pair that ran out of room
+  const int* need_in;   // read: the retry pass's hit capacity
   int* status;
   int* nrings;
   int* nverts;
@@ -821,7 +822,7 @@ struct ClipArgs {
     return *nb >= 3 && *nc >= 3 && *nb <= SBC_BATCH_MAX_VERTICES && *nc <= SBC_BATCH_MAX_VERTICES;
   }
   __device__ PairWork work(int p, int nb, int nc, int pass, Caps* cp) const {
-    *cp = caps_of(nb, nc, hit_cap(nb, nc, pass, need[p]));
+    *cp = caps_of(nb, nc, hit_cap(nb, nc, pass, need_in[p]));
     Carver cv{arena + (aoff[p] - abase), 0};
     return carve(cv, *cp);
   }
@@ -878,6 +879,16 @@ __global__ void __launch_bounds__(kBatchBlock) k_batch_back(ClipArgs A) {
   A.nrings[p] = r.nrings;
   A.nverts[p] = r.nverts;
   A.area[p] = r.area;
+}
+
+// the pass arrays of a recorded batch: pass 0 for every pair the forward
+// pass ran (-1: a large pair or none), pass 1 for the pairs it retried
+__global__ void k_graph_passes(int n, const int* __restrict__ pass, const int* __restrict__ status,
+                               int* __restrict__ pass0, int* __restrict__ pass1) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  pass0[p] = (pass[p] >= 0 || status[p] == SBC_EINPUT) ? 0 : -1;
+  pass1[p] = pass[p] == 1 ? 1 : -1;
 }
 
 void launch_clip(const ClipArgs& A, double in_bytes, cudaStream_t st) {
@@ -1246,7 +1257,8 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
   const double in_bytes =
       16.0 * (double)(h_boff_[p1] - h_boff_[p0] + h_coff_[p1] - h_coff_[p0]);
   launch_clip(ClipArgs{n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[0], aoff[0] + p0,
-                       abase_[0], need_ + p0, status + p0, nrings + p0, nverts + p0, area + p0},
+                       abase_[0], need_ + p0, need_ + p0, status + p0, nrings + p0, nverts + p0,
+                       area + p0},
               in_bytes, st);
   std::vector<int> hs(n);
   cudaMemcpyAsync(hs.data(), status + p0, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
@@ -1275,8 +1287,8 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
     arena[1] = (unsigned char*)pool.get("bt_arena1", (size_t)total + 256);
     if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch arena)");
     launch_clip(ClipArgs{n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[1],
-                         aoff[1] + p0, 0, need_ + p0, status + p0, nrings + p0, nverts + p0,
-                         area + p0},
+                         aoff[1] + p0, 0, need_ + p0, need_ + p0, status + p0, nrings + p0,
+                         nverts + p0, area + p0},
                 in_bytes, st);
   }
   // where each pair's data lives now: pass 0 arena, retry arena, or none
@@ -1380,6 +1392,7 @@ int BatchRunner::run_big(const double* d_bxy, const double* d_cxy, cudaStream_t 
 int BatchRunner::forward(int np_, const double* d_bxy, const long long* d_boff,
                          const double* d_cxy, const long long* d_coff, cudaStream_t st) {
   valid = false;
+  ++generation;
   key_b = d_bxy;
   key_c = d_cxy;
   np = np_;
@@ -1487,6 +1500,74 @@ int BatchRunner::backward(const double* d_bxy, const long long* d_boff, const do
         d_cxy + 2 * h_coff_[p], nc, g, d_gb + 2 * h_boff_[p], d_gc + 2 * h_coff_[p]);
   }
   if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch backward");
+  return kOk;
+}
+
+}  // namespace sbc
+
+namespace sbc {
+
+// Records the batch's area forward + backward as one CUDA graph.  The normal
+// forward pass runs first: it fixes the chunk (one), the arenas and the set
+// of pairs that need the retry pass with their hit capacities.  The graph
+// replays pass 0, the retry pass and the backward pass on those buffers.
+int BatchRunner::graph_record(int np_, const double* d_bxy, const long long* d_boff,
+                              const double* d_cxy, const long long* d_coff, const double* d_gA,
+                              double* d_gb, double* d_gc, double* out_area, int* out_status,
+                              cudaStream_t st, cudaGraphExec_t* exec,
+                              unsigned long long* kernels) {
+  int rc = forward(np_, d_bxy, d_boff, d_cxy, d_coff, st);
+  if (rc) return rc;
+  if (np <= 0 || chunks_.size() != 1 || !big_.empty())
+    return pl_.fail(kEInput, "graph capture needs a non-empty batch in one arena chunk with no "
+                             "polygon above SBC_BATCH_MAX_VERTICES vertices");
+  BufferPool& pool = pl_.pool();
+  int* pass0 = (int*)pool.get("bt_g_pass0", sizeof(int) * (np + 1));
+  int* pass1 = (int*)pool.get("bt_g_pass1", sizeof(int) * (np + 1));
+  int* need_rec = (int*)pool.get("bt_g_need_rec", sizeof(int) * (np + 1));
+  int* need_scr = (int*)pool.get("bt_g_need_scr", sizeof(int) * (np + 1));
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (graph)");
+  {
+    ::sbc::KProbe kp_("k_graph_passes", st);
+    k_graph_passes<<<grid_for(np, 256), 256, 0, st>>>(np, pass, status, pass0, pass1);
+  }
+  cudaMemcpyAsync(need_rec, need_, sizeof(int) * np, cudaMemcpyDeviceToDevice, st);
+  std::vector<int> hp(np);
+  cudaMemcpyAsync(hp.data(), pass, sizeof(int) * np, cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "graph setup");
+  bool retry = false;
+  for (int p = 0; p < np; ++p) retry |= hp[p] == 1;
+  const double in_bytes = 16.0 * in_verts;
+  const bool prof = profiling_suspend();
+  const unsigned long long l0 = g_launches;
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    launch_clip(ClipArgs{np, d_bxy, d_boff, d_cxy, d_coff, pass0, arena[0], aoff[0], abase_[0],
+                         need_scr, need_rec, status, nrings, nverts, area},
+                in_bytes, st);
+    if (retry)
+      launch_clip(ClipArgs{np, d_bxy, d_boff, d_cxy, d_coff, pass1, arena[1], aoff[1], 0, need_scr,
+                           need_rec, status, nrings, nverts, area},
+                  in_bytes, st);
+    const Arenas ar{arena[0], aoff[0], abase_[0], arena[1], aoff[1], 0, pass, need_rec};
+    {
+      ::sbc::KProbe kp_("k_batch_backward", st);
+      k_batch_backward<<<grid_for(np, kBatchBlock), kBatchBlock, 0, st>>>(
+          np, d_bxy, d_boff, d_cxy, d_coff, ar, status, nrings, d_gA, d_gb, d_gc);
+    }
+    if (out_area) cudaMemcpyAsync(out_area, area, sizeof(double) * np, cudaMemcpyDeviceToDevice, st);
+    if (out_status)
+      cudaMemcpyAsync(out_status, status, sizeof(int) * np, cudaMemcpyDeviceToDevice, st);
+    e = cudaStreamEndCapture(st, &graph);
+  }
+  profiling_restore(prof);
+  *kernels = g_launches - l0;
+  g_launches = l0;
+  if (e != cudaSuccess || !graph) return pl_.fail(kECuda, "graph capture");
+  e = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return pl_.fail(kECuda, "graph instantiation");
   return kOk;
 }
 

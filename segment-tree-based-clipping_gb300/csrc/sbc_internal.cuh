@@ -155,6 +155,9 @@ struct KProbe {
   int slot_;
 };
 void profile_begin();
+// per-launch events stay out of a graph being captured
+bool profiling_suspend();
+void profiling_restore(bool on);
 // aggregated per kernel name: returns the number of distinct kernels
 int profile_end(std::vector<std::string>* names, std::vector<float>* ms, std::vector<int>* counts,
                 std::vector<double>* bytes = nullptr);

@@ -186,6 +186,13 @@ class BatchRunner {
   const void* key_c = nullptr;
   bool valid = false;
   long long arena_budget = 0;   // bytes per chunk of arenas; 0: min(96 GiB, half of free)
+  // the area forward + backward of this batch as one CUDA graph (needs one
+  // arena chunk and no large pair); kernels: launches per replay
+  int graph_record(int np, const double* d_bxy, const long long* d_boff, const double* d_cxy,
+                   const long long* d_coff, const double* d_gA, double* d_gb, double* d_gc,
+                   double* out_area, int* out_status, cudaStream_t st, cudaGraphExec_t* exec,
+                   unsigned long long* kernels);
+  unsigned long long generation = 0;  // bumped by every forward pass
   int chunks() const { return (int)chunks_.size(); }
   int large_pairs() const { return (int)big_.size(); }
 

@@ -48,6 +48,14 @@ KProbe::~KProbe() {
   if (slot_ >= 0) cudaEventRecord(g_recs[slot_].b, st_);
 }
 
+bool profiling_suspend() {
+  const bool on = g_prof_on;
+  g_prof_on = false;
+  return on;
+}
+
+void profiling_restore(bool on) { g_prof_on = on; }
+
 void profile_begin() {
   g_recs.clear();
   g_event_next = 0;

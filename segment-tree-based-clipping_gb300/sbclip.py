@@ -78,6 +78,21 @@ class _BatchRings(ctypes.Structure):
 BATCH_MAX_VERTICES = 4096
 
 
+class AreaGraph:
+    """A recorded batch area forward + backward (sbc_area_graph_*)."""
+
+    def __init__(self, clipper, handle):
+        self._c, self._h = clipper, handle
+
+    def launch(self, stream: int | None = None) -> None:
+        self._c._check(self._c._L.sbc_area_graph_launch(self._h, stream))
+
+    def close(self) -> None:
+        if self._h:
+            self._c._L.sbc_area_graph_destroy(self._h)
+            self._h = None
+
+
 class _PairwiseJob(ctypes.Structure):
     _fields_ = [("b_xy", ctypes.c_void_p), ("nb", ctypes.c_int), ("noverlays", ctypes.c_int),
                 ("c_xy", ctypes.c_void_p), ("c_off", ctypes.c_void_p)]
@@ -130,6 +145,10 @@ def load_library(path: str | os.PathLike | None = None):
                                    vp]
     L.sbc_pairwise_info.argtypes = [vp, ctypes.POINTER(ll), i]
     L.sbc_batch_set_arena_budget.argtypes = [vp, ll]
+    L.sbc_area_graph_create.argtypes = [vp, ctypes.POINTER(_Batch), vp, vp, vp, vp, vp, vp,
+                                        ctypes.POINTER(vp)]
+    L.sbc_area_graph_launch.argtypes = [vp, vp]
+    L.sbc_area_graph_destroy.argtypes = [vp]
     L.sbc_batch_info.argtypes = [vp, ctypes.POINTER(ll), i]
     L.sbc_pairwise_set_cell_factor.argtypes = [vp, ctypes.c_double]
     L.sbc_pairwise_set_split.argtypes = [vp, i]
@@ -337,6 +356,16 @@ class Clipper:
         self._check(self._L.sbc_clip_pairwise_device(self._h, ctypes.byref(j), ctypes.byref(r),
                                                      stream))
         return int(r.nrings), int(r.nverts)
+
+    def area_graph(self, npairs, d_bxy, d_boff, d_cxy, d_coff, d_grad_area, d_grad_b, d_grad_c,
+                   d_area=None, d_status=None, stream: int | None = None) -> "AreaGraph":
+        """Record the batch's area forward + backward as one CUDA graph."""
+        b = _Batch(npairs, d_bxy, d_boff, d_cxy, d_coff)
+        h = ctypes.c_void_p()
+        self._check(self._L.sbc_area_graph_create(self._h, ctypes.byref(b), d_grad_area, d_grad_b,
+                                                  d_grad_c, d_area, d_status, stream,
+                                                  ctypes.byref(h)))
+        return AreaGraph(self, h)
 
     def set_batch_arena_budget(self, nbytes: int) -> None:
         self._check(self._L.sbc_batch_set_arena_budget(self._h, int(nbytes)))

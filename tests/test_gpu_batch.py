@@ -187,3 +187,61 @@ def test_batch_device_arrays_match_host_arrays(cl):
     assert np.array_equal(st.cpu().numpy(), h_st)
     assert np.array_equal(gb.cpu().numpy(), np.concatenate(h_gb))
     assert np.array_equal(gc.cpu().numpy(), np.concatenate(h_gc))
+
+
+def test_batch_area_graph_replays_forward_and_backward(cl):
+    """One CUDA graph launch equals sbc_area_forward_device +
+    sbc_area_backward_device, bit for bit, also after the coordinates change
+    in place; a later batched call on the context makes the graph stale."""
+    torch = pytest.importorskip("torch")
+    import sbclip
+    pairs = gen.small_pairs(500, seed=4700)
+    bxy, boff = sbclip.pack_polygons([b for b, _ in pairs])
+    cxy, coff = sbclip.pack_polygons([c for _, c in pairs])
+    dev = "cuda:0"
+    t = {k: torch.from_numpy(v).to(dev) for k, v in
+         (("bxy", bxy), ("boff", boff), ("cxy", cxy), ("coff", coff))}
+    n = len(pairs)
+    args = (n, t["bxy"].data_ptr(), t["boff"].data_ptr(), t["cxy"].data_ptr(),
+            t["coff"].data_ptr())
+    ga = torch.linspace(0.5, 2.0, n, dtype=torch.float64, device=dev)
+    out = {k: torch.zeros_like(t[s2]) for k, s2 in (("gb", "bxy"), ("gc", "cxy"))}
+    area = torch.zeros(n, dtype=torch.float64, device=dev)
+    st = torch.zeros(n, dtype=torch.int32, device=dev)
+    g = cl.area_graph(*args, ga.data_ptr(), out["gb"].data_ptr(), out["gc"].data_ptr(),
+                      area.data_ptr(), st.data_ptr())
+    ref = sbclip.Clipper(0)
+    try:
+        def reference():
+            a = torch.zeros(n, dtype=torch.float64, device=dev)
+            s_ = torch.zeros(n, dtype=torch.int32, device=dev)
+            gb = torch.zeros_like(t["bxy"])
+            gc = torch.zeros_like(t["cxy"])
+            ref.area_forward_device(*args, a.data_ptr(), s_.data_ptr())
+            ref.area_backward_device(*args, ga.data_ptr(), gb.data_ptr(), gc.data_ptr())
+            return a, s_, gb, gc
+        for _ in range(2):
+            area.zero_()
+            out["gb"].zero_()
+            g.launch()
+            torch.cuda.synchronize()
+            a, s_, gb, gc = reference()
+            assert torch.equal(area, a) and torch.equal(st, s_)
+            assert torch.equal(out["gb"], gb) and torch.equal(out["gc"], gc)
+            assert (s_ == 0).all()
+        # new coordinates of the same polygons, in place: a uniform scaling
+        # keeps every pair's combinatorics, so its hit room still fits
+        t["bxy"].mul_(1.25)
+        t["cxy"].mul_(1.25)
+        g.launch()
+        torch.cuda.synchronize()
+        a, s_, gb, gc = reference()
+        assert torch.equal(area, a) and torch.equal(out["gb"], gb) and torch.equal(out["gc"], gc)
+        # a later batched call on the same context replaces the graph's buffers
+        cl.area_forward([pairs[0][0]], [pairs[0][1]])
+        with pytest.raises(sbclip.SbcError) as e:
+            g.launch()
+        assert e.value.code == 1
+    finally:
+        g.close()
+        ref.close()
