@@ -350,7 +350,7 @@ def run_small_pairs(args, rank: int, world: int):
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    n = SMALL_PAIRS
+    n = args.pairs or SMALL_PAIRS
     pairs, desc = small_pairs_workload(n, 4000 + rank)
     bases, ovs = [b for b, _ in pairs], [c for _, c in pairs]
     bxy, boff = sbclip.pack_polygons(bases)
@@ -817,6 +817,8 @@ def main():
     ap.add_argument("--job-only", type=int, default=0,
                     help="one_to_many only: run the job this many times and print no JSON "
                          "line (for profilers)")
+    ap.add_argument("--pairs", type=int, default=None,
+                    help="small_pairs only: number of pairs (default 65,536)")
     ap.add_argument("--overlays", type=int, default=None,
                     help="one_to_many only: use the first N overlays of the workload")
     args = ap.parse_args()
