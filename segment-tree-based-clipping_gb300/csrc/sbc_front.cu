@@ -325,8 +325,9 @@ int Pipeline::stage_elementary() {
     k_ele_flags<<<grid_for(n2, 256), 256, 0, st_>>>(sidx, e_s, e_e, vl, vloc, E, flag, val);
   }
   exclusive_scan_i32(flag, n2 + 1, sscr, st_);
-  int count = 0;
+  int count = 0, before_last = 0;
   cudaMemcpyAsync(&count, flag + n2, sizeof(int), cudaMemcpyDeviceToHost, st_);
+  cudaMemcpyAsync(&before_last, flag + n2 - 1, sizeof(int), cudaMemcpyDeviceToHost, st_);
   cudaStreamSynchronize(st_);
   if (count < 1) return fail(kEUndef, "no elementary interval (all endpoints equal)");
   int round = npow2_host(count) + 1;
@@ -347,6 +348,8 @@ int Pipeline::stage_elementary() {
       k_ele_pad<<<grid_for(round - count, 256), 256, 0, st_>>>(ea, count, round);
     }
   }
+  ele_count = count;
+  ele_tail = count != before_last;  // the last slot repeats the second-to-last value
   stat_edges = E;
   stat_epc = epc;
   stat_ts = ts;
@@ -452,6 +455,111 @@ __global__ void k_find_leaves(const double* __restrict__ es, const double* __res
   if ((threadIdx.x & 31) == 0 && n) atomicAdd(cnt, (unsigned long long)n);
 }
 
+// ---- end leaves and leaf ranges from the endpoint sort.  The endpoints of
+// one value form a run of the sorted order; with ea sorted, the entries of
+// ea equal to the value are [F[run start], F[run end + 1]) (F: the keep
+// flags' exclusive prefix), the padding added when the value is ea's last.
+// findBoarder then runs on positions (border_by_position) and the leaf range
+// needs no search.
+__global__ void k_ea_sorted(int epc, const double* __restrict__ ea, unsigned* __restrict__ flags) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i + 1 < epc && !(ea[i] <= ea[i + 1])) atomicOr(flags, (unsigned)kFlagUnsorted);
+}
+
+__global__ void k_run_start(long long n2, const unsigned long long* __restrict__ keys,
+                            int* __restrict__ chg) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n2) return;
+  chg[i] = (i < n2 && (i == 0 || keys[i] != keys[i - 1])) ? 1 : 0;
+}
+
+// after the exclusive scan of the run starts: first and last position of each run
+__global__ void k_run_bounds(long long n2, const unsigned long long* __restrict__ keys,
+                             const int* __restrict__ rpre, int* __restrict__ rs,
+                             int* __restrict__ re) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n2) return;
+  const bool first = i == 0 || keys[i] != keys[i - 1];
+  const bool last = i == n2 - 1 || keys[i + 1] != keys[i];
+  const int r = rpre[i] + (first ? 0 : -1);
+  if (first) rs[r] = (int)i;
+  if (last) re[r] = (int)i;
+}
+
+// per endpoint: the positions [lo, hi) of ea holding its value
+__global__ void k_endpoint_range(long long n2, const unsigned long long* __restrict__ keys,
+                                 const unsigned* __restrict__ sidx, const int* __restrict__ rpre,
+                                 const int* __restrict__ rs, const int* __restrict__ re,
+                                 const int* __restrict__ F, int count, int epc,
+                                 const double* __restrict__ ea, int2* __restrict__ erange) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n2) return;
+  const bool first = i == 0 || keys[i] != keys[i - 1];
+  const int r = rpre[i] + (first ? 0 : -1);
+  const unsigned long long kl = dkey(ea[count - 1]);
+  int lo = F[rs[r]], hi = F[re[r] + 1];
+  if (keys[i] == kl) hi = epc;             // and the padding
+  else if (keys[i] > kl) lo = hi = epc;    // above every entry, padding included
+  erange[sidx[i]] = make_int2(lo, hi);
+}
+
+__global__ void k_edge_tree(const double* __restrict__ es, const double* __restrict__ ee, int E,
+                            const int2* __restrict__ erange, const double* __restrict__ ea,
+                            int epc, int z, int logL, int* __restrict__ aft, int* __restrict__ bef,
+                            int2* __restrict__ lr, unsigned long long* __restrict__ cnt) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned n_leaf = 0, n_cover = 0;
+  if (e < E) {
+    const int L = 1 << logL;
+    const int2 rS = erange[2 * e], rE = erange[2 * e + 1];
+    auto J = [&](int m) { return m < z ? m : (m == z ? epc - 1 : m - 1); };
+    int a = -1, b = -1;
+    const int en = border_by_position(epc, z, rE.x, rE.y, ee[e]);
+    if (en >= 0) {
+      const int j = J(en);  // right[j]
+      int node = 0;
+      if (j <= epc - 2) {
+        const int i = j + 1;
+        node = L + i;
+        if (i != 1 && i + 1 < epc && ea[i] == ea[i + 1]) node = L + i + 1;
+      }
+      if (node >= L && node < 2 * L && ea[node - L] != ea[node - L + 1]) a = node;
+    }
+    const int st = border_by_position(epc, z, rS.x, rS.y, es[e]);
+    if (st >= 0) {
+      const int j = J(st);  // left[j]
+      int node = 0;
+      if (j <= epc - 2) node = L + j;
+      if (node >= L && node < 2 * L && ea[node - L] != ea[node - L + 1]) b = node;
+    }
+    aft[e] = a;
+    bef[e] = b;
+    n_leaf = (a >= 0) + (b >= 0);
+    // leaves inside [start, end]: from the first entry >= start to before
+    // the first entry > end
+    const int l = rS.x < L ? rS.x : L;
+    int r1 = rE.y - 1;
+    r1 = r1 < 0 ? 0 : (r1 > L ? L : r1);
+    lr[e] = make_int2(l, r1 > l ? r1 : l);
+    for (int x = l + L, y = (r1 > l ? r1 : l) + L; x < y; x >>= 1, y >>= 1) {
+      if (x & 1) {
+        ++n_cover;
+        ++x;
+      }
+      if (y & 1) {
+        ++n_cover;
+        --y;
+      }
+    }
+  }
+  n_leaf = __reduce_add_sync(0xffffffffu, n_leaf);
+  n_cover = __reduce_add_sync(0xffffffffu, n_cover);
+  if ((threadIdx.x & 31) == 0) {
+    if (n_leaf) atomicAdd(cnt, (unsigned long long)n_leaf);
+    if (n_cover) atomicAdd(cnt + 1, (unsigned long long)n_cover);
+  }
+}
+
 static int digit_count_host(double val) {
   int d = 1;
   int iv = (int)trunc(val);
@@ -481,10 +589,52 @@ int Pipeline::stage_endlists() {
     k_border_check<<<grid_for(epc, 256), 256, 0, st_>>>(ea, epc, scale, absMin, minI < 0 ? 1 : 0, zc,
                                                      d_flags);
   }
+  {
+    ::sbc::KProbe kp_("k_ea_sorted", st_, 8.0 * epc);
+    k_ea_sorted<<<grid_for(epc, 256), 256, 0, st_>>>(epc, ea, d_flags);
+  }
   int z = 0;
   cudaMemcpyAsync(&z, zc, sizeof(int), cudaMemcpyDeviceToHost, st_);
-  if (read_flags() & kFlagUndef) return fail(kEUndef, "border keys not monotone (realToInt)");
+  const unsigned fl = read_flags();
+  if (fl & kFlagUndef) return fail(kEUndef, "border keys not monotone (realToInt)");
   z_garbage = z;
+  lr_ready = false;
+  if (!(fl & kFlagUnsorted) && !ele_tail) {
+    // positions from the endpoint sort (see k_endpoint_range)
+    const long long n2 = 2LL * E;
+    auto* keys = (unsigned long long*)pool_.get("ele_keys", sizeof(unsigned long long) * n2);
+    auto* sidx = (unsigned*)pool_.get("ele_sidx", sizeof(unsigned) * n2);
+    int* F = (int*)pool_.get("ele_flag", sizeof(int) * (n2 + 1));
+    int* rpre = (int*)pool_.get("run_pre", sizeof(int) * (n2 + 1));
+    int* rs = (int*)pool_.get("run_s", sizeof(int) * n2);
+    int* re = (int*)pool_.get("run_e", sizeof(int) * n2);
+    int2* erange = (int2*)pool_.get("endpoint_range", sizeof(int2) * n2);
+    void* sscr = pool_.get("scan_scr", scan_scratch_bytes(n2 + 1));
+    lr = (int2*)pool_.get("edge_leaf_range", sizeof(int2) * (E + 1));
+    if (pool_.failed) return fail(kENoMem, "device allocation failed (end lists)");
+    {
+      ::sbc::KProbe kp_("k_run_start", st_, 12.0 * n2);
+      k_run_start<<<grid_for(n2 + 1, 256), 256, 0, st_>>>(n2, keys, rpre);
+    }
+    exclusive_scan_i32(rpre, n2 + 1, sscr, st_);
+    {
+      ::sbc::KProbe kp_("k_run_bounds", st_, 20.0 * n2);
+      k_run_bounds<<<grid_for(n2, 256), 256, 0, st_>>>(n2, keys, rpre, rs, re);
+    }
+    {
+      ::sbc::KProbe kp_("k_endpoint_range", st_, 36.0 * n2);
+      k_endpoint_range<<<grid_for(n2, 256), 256, 0, st_>>>(n2, keys, sidx, rpre, rs, re, F,
+                                                           ele_count, epc, ea, erange);
+    }
+    {
+      // es, ee and two endpoint ranges in; aft, bef, leaf range out
+      ::sbc::KProbe kp_("k_edge_tree", st_, 48.0 * E);
+      k_edge_tree<<<grid_for(E, 256), 256, 0, st_>>>(e_s, e_e, E, erange, ea, epc, z, logL, aft, bef,
+                                                     lr, d_treecnt);
+    }
+    lr_ready = true;
+    return kOk;
+  }
   // ea[0] < 0 decides the shift; ea[0] equals minI
   Borders B{ea, epc, z};
   {
@@ -545,7 +695,7 @@ __global__ void k_edge_range(const double* __restrict__ es, const double* __rest
 int Pipeline::stage_cover() {
   lr = (int2*)pool_.get("edge_leaf_range", sizeof(int2) * (E + 1));
   if (pool_.failed) return fail(kENoMem, "device allocation failed (leaf ranges)");
-  {
+  if (!lr_ready) {
     ::sbc::KProbe kp_("k_edge_range", st_, 24.0 * E);  // es, ee in; leaf range out
     k_edge_range<<<grid_for(E, 256), 256, 0, st_>>>(e_s, e_e, E, ea, logL, lr, d_treecnt);
   }

@@ -39,6 +39,7 @@ enum DevFlag : unsigned {
   kFlagOverflow = 2u,       // an output buffer was too small; host grows and retries
   kFlagSlowPath = 4u,       // back end needs the serial emulation path
   kFlagSpin = 8u,           // a bounded wait gave up
+  kFlagUnsorted = 16u,      // the elementary array is not in order
 };
 
 // ---------------------------------------------------------------- FP64 geometry
@@ -119,6 +120,44 @@ __device__ __forceinline__ int alpha_to_int(double a) {
 __device__ __forceinline__ unsigned long long dkey(double x) {
   unsigned long long u = (unsigned long long)__double_as_longlong(x == 0.0 ? 0.0 : x);
   return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+
+// ---------------------------------------------------------------- findBoarder on positions
+// The border sequence S(m) of preparePointsToNodeMapMulticore
+// (oacc_segment_tree.cpp:1970-2008) is the sorted elementary array ea with
+// the never-written slot read as 0.0 moved to position z: S(m) = ea[m+1] for
+// m < z, 0.0 at z, ea[m] above, past the arrays NaN.  When ea is sorted and
+// the entries equal to q sit at positions [lo, hi) of ea, comparing S(m)
+// with q needs no memory access.  Returns -1 smaller, 0 equal, 1 greater,
+// 2 past the arrays.
+__device__ __forceinline__ int border_cmp(int epc, int z, int m, int lo, int hi, double q) {
+  if (m < 0 || m >= epc) return 2;
+  if (m == z) return (0.0 == q) ? 0 : (0.0 < q ? -1 : 1);
+  const int t = m < z ? m + 1 : m;
+  return t < lo ? -1 : (t < hi ? 0 : 1);
+}
+
+// findBoarder (oacc_segment_tree.cpp:420-460), its search path followed on
+// positions (including the misses the zero slot causes)
+__device__ __forceinline__ int border_by_position(int epc, int z, int lo, int hi, double q) {
+  int l = 0, h = epc;
+  while (l < h) {
+    const int m = l + (h - l) / 2;
+    const int c = border_cmp(epc, z, m, lo, hi, q);
+    if (c == 0) {
+      if (border_cmp(epc, z, m - 1, lo, hi, q) != 0) {
+        h = m;
+        l = h;
+      } else {
+        h = m - 1;
+      }
+    } else if (c == -1) {
+      l = m + 1;
+    } else {
+      h = m - 1;
+    }
+  }
+  return border_cmp(epc, z, h, lo, hi, q) == 0 ? h : -1;
 }
 
 // ---------------------------------------------------------------- primitives

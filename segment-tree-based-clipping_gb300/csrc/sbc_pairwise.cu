@@ -129,36 +129,6 @@ __device__ __forceinline__ void pw_lohi(const PwTree& T, int r, int* lo, int* hi
   }
 }
 
-// S(m) against q: -1 smaller, 0 equal, 1 greater, 2 past the arrays (NaN)
-__device__ __forceinline__ int pw_scmp(const PwTree& T, int m, int lo, int hi, double q) {
-  if (m < 0 || m >= T.epc) return 2;
-  if (m == T.z) return (0.0 == q) ? 0 : (0.0 < q ? -1 : 1);
-  const int t = m < T.z ? m + 1 : m;
-  return t < lo ? -1 : (t < hi ? 0 : 1);
-}
-
-// findBoarder (oacc_segment_tree.cpp:420-460) on positions
-__device__ int pw_find_border(const PwTree& T, int lo, int hi, double q) {
-  int l = 0, h = T.epc;
-  while (l < h) {
-    const int m = l + (h - l) / 2;
-    const int c = pw_scmp(T, m, lo, hi, q);
-    if (c == 0) {
-      if (pw_scmp(T, m - 1, lo, hi, q) != 0) {
-        h = m;
-        l = h;
-      } else {
-        h = m - 1;
-      }
-    } else if (c == -1) {
-      l = m + 1;
-    } else {
-      h = m - 1;
-    }
-  }
-  return pw_scmp(T, h, lo, hi, q) == 0 ? h : -1;
-}
-
 // end-list leaves and covered leaf range of an edge whose start (smaller x)
 // s has combined rank rs and whose end e has rank re
 __device__ void pw_edge_tree(const PwTree& T, int rs, double s, int re, double e, int* aft,
@@ -170,7 +140,7 @@ __device__ void pw_edge_tree(const PwTree& T, int rs, double s, int re, double e
   pw_lohi(T, re, &lo, &hi);
   const int hiE = hi;
   int a = -1, b = -1;
-  const int en = pw_find_border(T, lo, hi, e);
+  const int en = border_by_position(T.epc, T.z, lo, hi, e);
   if (en >= 0) {
     const int j = J(en);
     int node = 0;
@@ -182,7 +152,7 @@ __device__ void pw_edge_tree(const PwTree& T, int rs, double s, int re, double e
     if (node >= L && node < 2 * L && !eqnext(node - L)) a = node;
   }
   pw_lohi(T, rs, &lo, &hi);
-  const int st = pw_find_border(T, lo, hi, s);
+  const int st = border_by_position(T.epc, T.z, lo, hi, s);
   if (st >= 0) {
     const int j = J(st);
     int node = 0;

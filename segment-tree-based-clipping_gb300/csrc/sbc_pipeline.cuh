@@ -78,6 +78,9 @@ class Pipeline {
   double* ea = nullptr;
   int epc = 0, numLeaves = 0, ts = 0, logL = 0;
   int z_garbage = 0;                   // position of the zero border entry
+  int ele_count = 0;                   // elementary points before padding
+  bool ele_tail = false;               // the last slot repeats the second-to-last value
+  bool lr_ready = false;               // end leaves and leaf ranges came from the sort
   int* aft = nullptr;                  // leaf node from the edge's end (or -1)
   int* bef = nullptr;                  // leaf node from the edge's start (or -1)
   int2* lr = nullptr;                  // per edge: leaves [l, r1) its interval contains
