@@ -103,21 +103,22 @@ __global__ void k_side_stats(int n, const unsigned char* __restrict__ isect,
                              BkScalars* sc) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int cross = 0, notonon = 0;
+  unsigned free_i = 0xffffffffu;  // first slot without an intersection, per warp first
   if (i < n) {
     int l = lab[i];
     if (isect[i] && l == L_CROSSING) cross = 1;
     if (l != L_ON_ON) notonon = 1;
-    if (!isect[i]) atomicMin(&sc->firstFree[side], i);
+    if (!isect[i]) free_i = (unsigned)i;
     if (checkChains && isect[i] && (l == L_LEFT_ON || l == L_RIGHT_ON)) atomicOr(&sc->anomaly, 4u);
     if (l == L_DCROSS || l == L_DBOUNCE) atomicOr(&sc->anomaly, 4u);
   }
-  for (int s = 16; s > 0; s >>= 1) {
-    cross += __shfl_xor_sync(0xffffffffu, cross, s);
-    notonon += __shfl_xor_sync(0xffffffffu, notonon, s);
-  }
-  if ((threadIdx.x & 31) == 0) {
+  cross = block_sum(cross);
+  notonon = block_sum(notonon);
+  free_i = block_min(free_i);
+  if (threadIdx.x == 0) {
     if (cross) atomicAdd(&sc->crossCount[side], cross);
     if (notonon) atomicAdd(&sc->notOnOn[side], notonon);
+    if (free_i != 0xffffffffu) atomicMin(&sc->firstFree[side], (int)free_i);
   }
 }
 
@@ -365,24 +366,46 @@ __global__ void k_lr_copy(Trace T, const int* __restrict__ nxt, const long long*
                           const int* __restrict__ ringI, const int* __restrict__ startPre,
                           const int* __restrict__ vOff, const double* __restrict__ ixB,
                           const double* __restrict__ ixC, double* __restrict__ out) {
-  int x = blockIdx.x * blockDim.x + threadIdx.x;
-  int n = T.cP + T.cQ;
-  if (x >= n || nxt[x] != -1) return;  // only segments of a start's orbit
-  int I = ringI[x];
-  long long base = vOff[startPre[I]] + S[I] - S[x];
-  int t = tr_target(T, x);
-  int len = tr_len(T, x, t);
-  bool onP = x < T.cP;
-  int m = onP ? T.nB : T.nQ;
-  int sx = tr_slot(T, x);
-  bool fwd = (onP ? T.enexP[sx] : T.enexQ[sx]) == EX_ENTRY;
-  const double* src = onP ? ixB : ixC;
-  for (int step = 1; step <= len; ++step) {
-    int slot = fwd ? sx + step : sx - step;
-    if (slot >= m) slot -= m;
-    if (slot < 0) slot += m;
-    out[2 * (base + step - 1)] = src[2 * slot];
-    out[2 * (base + step - 1) + 1] = src[2 * slot + 1];
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int n = T.cP + T.cQ;
+  const bool mine = x < n && nxt[x] == -1;  // only segments of a start's orbit
+  long long base = 0;
+  int len = 0, m = 1, sx = 0;
+  bool onP = false, fwd = false;
+  if (mine) {
+    const int I = ringI[x];
+    base = vOff[startPre[I]] + S[I] - S[x];
+    const int t = tr_target(T, x);
+    len = tr_len(T, x, t);
+    onP = x < T.cP;
+    m = onP ? T.nB : T.nQ;
+    sx = tr_slot(T, x);
+    fwd = (onP ? T.enexP[sx] : T.enexQ[sx]) == EX_ENTRY;
+  }
+  auto copy = [&](long long b0, int s0, int mm, bool f, bool p, int step) {
+    int slot = f ? s0 + step : s0 - step;
+    if (slot >= mm) slot -= mm;
+    if (slot < 0) slot += mm;
+    const double* src = p ? ixB : ixC;
+    out[2 * (b0 + step - 1)] = src[2 * slot];
+    out[2 * (b0 + step - 1) + 1] = src[2 * slot + 1];
+  };
+  // short segments: one thread each; long ones: the whole warp, in turn
+  const bool longseg = mine && len > 32;
+  if (mine && !longseg)
+    for (int step = 1; step <= len; ++step) copy(base, sx, m, fwd, onP, step);
+  unsigned lm = __ballot_sync(0xffffffffu, longseg);
+  while (lm) {
+    const int src = __ffs(lm) - 1;
+    lm &= lm - 1;
+    const long long b0 = __shfl_sync(0xffffffffu, base, src);
+    const int l0 = __shfl_sync(0xffffffffu, len, src);
+    const int s0 = __shfl_sync(0xffffffffu, sx, src);
+    const int m0 = __shfl_sync(0xffffffffu, m, src);
+    const bool f0 = __shfl_sync(0xffffffffu, (int)fwd, src) != 0;
+    const bool p0 = __shfl_sync(0xffffffffu, (int)onP, src) != 0;
+    for (int step = 1 + lane; step <= l0; step += 32) copy(b0, s0, m0, f0, p0, step);
   }
 }
 

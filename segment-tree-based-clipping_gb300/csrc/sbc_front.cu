@@ -552,11 +552,11 @@ __global__ void k_edge_tree(const double* __restrict__ es, const double* __restr
       }
     }
   }
-  n_leaf = __reduce_add_sync(0xffffffffu, n_leaf);
-  n_cover = __reduce_add_sync(0xffffffffu, n_cover);
-  if ((threadIdx.x & 31) == 0) {
-    if (n_leaf) atomicAdd(cnt, (unsigned long long)n_leaf);
-    if (n_cover) atomicAdd(cnt + 1, (unsigned long long)n_cover);
+  const unsigned long long t_leaf = block_sum((unsigned long long)n_leaf);
+  const unsigned long long t_cover = block_sum((unsigned long long)n_cover);
+  if (threadIdx.x == 0) {
+    if (t_leaf) atomicAdd(cnt, t_leaf);
+    if (t_cover) atomicAdd(cnt + 1, t_cover);
   }
 }
 

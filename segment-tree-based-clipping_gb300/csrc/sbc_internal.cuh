@@ -122,6 +122,37 @@ __device__ __forceinline__ unsigned long long dkey(double x) {
   return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
 }
 
+// ---------------------------------------------------------------- block reductions
+// Sum (or min) over the block, then one atomic per block: same-address
+// atomics from every warp of a large grid serialise at the L2.  Every
+// thread of the block must call these (blockDim a multiple of 32, <= 1024).
+template <typename T>
+__device__ __forceinline__ T block_sum(T v) {
+  __shared__ T part[32];
+  for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) part[w] = v;
+  __syncthreads();
+  T t = 0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < nw; ++i) t += part[i];
+  return t;  // valid in thread 0
+}
+
+__device__ __forceinline__ unsigned block_min(unsigned v) {
+  __shared__ unsigned part[32];
+  v = __reduce_min_sync(0xffffffffu, v);
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) part[w] = v;
+  __syncthreads();
+  unsigned t = 0xffffffffu;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < nw; ++i) t = part[i] < t ? part[i] : t;
+  return t;  // valid in thread 0
+}
+
 // ---------------------------------------------------------------- findBoarder on positions
 // The border sequence S(m) of preparePointsToNodeMapMulticore
 // (oacc_segment_tree.cpp:1970-2008) is the sorted elementary array ea with
