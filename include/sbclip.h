@@ -41,6 +41,11 @@ typedef struct sbc_options {
 
 #define SBC_FLAG_TIMING 1          /* record per-phase CUDA-event times (sbc_stats) */
 #define SBC_FLAG_SERIAL_BACKEND 2  /* run the back end's exact single-thread emulation */
+#define SBC_FLAG_UNION 4           /* union instead of intersection: the Foster back end's
+                                      UNION switch (foster/polyclip.h:39), which the
+                                      reference's seg driver leaves off; every clipping
+                                      call of the context (pair, one-to-many, batches,
+                                      pairwise) then returns union rings */
 
 typedef struct sbc_rings {
   int nrings;

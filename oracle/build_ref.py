@@ -19,6 +19,9 @@ Recipe (nothing is written outside oracle/_ref/):
      ``(LONG)(pow(10, positions) * val)``.
    * ``savePolygon`` (``foster/polyclip.h:861-865``) honours
      ``SBC_REF_PRECISION`` (17 gives bit-exact dumps; default stays 6).
+   * the Foster back end's ``UNION`` switch (``foster/polyclip.h:39``), which
+     the driver leaves off, is set when ``SBC_REF_UNION`` is in the
+     environment (union fixtures for the library's union mode).
    * ``multicore_clipping`` (``src/clip.cpp:1415-2115``) dumps its intermediate
      arrays (raw / unique candidates, intersection records, merged vertex
      arrays, initial labels) when ``SBC_REF_DUMP`` names a file prefix.
@@ -94,6 +97,11 @@ PATCHES = [
     ("p_seg_tree/oacc_segment_tree.cpp",
      "return (int)pow(10, positions) * val;",
      "return (LONG)(pow(10, positions) * val);", None),
+    # the back end's UNION switch, off in the reference's driver, settable
+    # for union fixtures
+    ("foster/polyclip.h",
+     "bool UNION = false;",
+     "bool UNION = (getenv(\"SBC_REF_UNION\") != nullptr);", None),
     ("foster/polyclip.h",
      "  ofstream to(s);\n",
      "  ofstream to(s);\n  if (getenv(\"SBC_REF_PRECISION\")) to.precision(atoi(getenv(\"SBC_REF_PRECISION\")));\n",

@@ -48,6 +48,7 @@ def lib():
         L.sbco_clip.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                 ctypes.c_int]
         L.sbco_status.argtypes = [ctypes.c_void_p]
+        L.sbco_set_union.argtypes = [ctypes.c_int]
         L.sbco_message.restype = ctypes.c_char_p
         L.sbco_message.argtypes = [ctypes.c_void_p]
         L.sbco_len.restype = ctypes.c_long
@@ -68,9 +69,11 @@ class OracleError(RuntimeError):
         self.status = status
 
 
-def clip(base: np.ndarray, overlays) -> dict:
-    """Run the restatement.  Returns {'stats': {...}, 'overlays': [ {name: array} ]}."""
+def clip(base: np.ndarray, overlays, union: bool = False) -> dict:
+    """Run the restatement (union instead of intersection with `union`).
+    Returns {'stats': {...}, 'overlays': [ {name: array} ]}."""
     L = lib()
+    L.sbco_set_union(1 if union else 0)
     b = np.ascontiguousarray(base, dtype=np.float64).reshape(-1, 2)
     ovs = [np.ascontiguousarray(o, dtype=np.float64).reshape(-1, 2) for o in overlays]
     cxy = np.ascontiguousarray(np.concatenate(ovs, axis=0))
@@ -140,7 +143,7 @@ def parse_rings(text: str):
 
 
 def run_reference(base: np.ndarray, overlays, threads: int = 1, precision: int = 17,
-                  dump: bool = False, timeout: float = 600.0) -> dict:
+                  dump: bool = False, timeout: float = 600.0, union: bool = False) -> dict:
     """Run oracle/_ref/seg on the polygons (written `x,y` at %.17g).
 
     Returns {'rings': [list per overlay], 'time_line': [...], 'dumps': {...}}.
@@ -162,6 +165,8 @@ def run_reference(base: np.ndarray, overlays, threads: int = 1, precision: int =
         env = dict(os.environ)
         env["OMP_NUM_THREADS"] = str(threads)
         env["SBC_REF_PRECISION"] = str(precision)
+        if union:
+            env["SBC_REF_UNION"] = "1"
         if dump:
             env["SBC_REF_DUMP"] = str(td / "dump")
         p = subprocess.run([str(REF_EXE), str(td / "b.txt"), *files], cwd=td / "work", env=env,

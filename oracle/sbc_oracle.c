@@ -1043,7 +1043,13 @@ static void toggle(int *st) {
   else if (*st == EX_EXIT) *st = EX_ENTRY;
 }
 
-/* labelIntersections2 + createResult2, foster/polyclip.h:337-759 (UNION off) */
+/* The back end's UNION switch (foster/polyclip.h:39): the reference's seg
+ * driver leaves it off; its Foster back end supports it (:451-470, :571-618,
+ * :669-680, :740). */
+static int g_union = 0;
+void sbco_set_union(int on) { g_union = on ? 1 : 0; }
+
+/* labelIntersections2 + createResult2, foster/polyclip.h:337-759 */
 static int label_and_trace(lists_t *Ls, rings_t *R) {
   pool_t *P = &Ls->P, *Q = &Ls->Q;
   int roots[2] = {Ls->rootP, Ls->rootQ};
@@ -1081,6 +1087,10 @@ static int label_and_trace(lists_t *Ls, rings_t *R) {
     int V = root;
     do {
       if (p->isect[V] && (p->label[V] == L_CROSSING || p->label[V] == L_DELAYED_CROSSING)) nocross = 0;
+      /* noCrossingVertex(UNION), foster/polygon.h:465-475 */
+      if (g_union && p->isect[V] &&
+          (p->label[V] == L_BOUNCING || p->label[V] == L_DELAYED_BOUNCING))
+        nocross = 0;
       V = p->next[V];
     } while (V != root);
     if (!nocross) continue;
@@ -1096,7 +1106,7 @@ static int label_and_trace(lists_t *Ls, rings_t *R) {
     } else {
       double px, py;
       if (non_isect_point(Ls, s, root, &px, &py)) return -2;
-      if (point_in_poly(side_pool(Ls, OTHER(s)), roots[OTHER(s)], px, py))
+      if (point_in_poly(side_pool(Ls, OTHER(s)), roots[OTHER(s)], px, py) ^ g_union)
         if (ring_copy_list(R, p, root)) return -1;
     }
   }
@@ -1131,14 +1141,14 @@ static int label_and_trace(lists_t *Ls, rings_t *R) {
     do {
       if (p->isect[I]) {
         if (p->label[I] == L_CROSSING) { p->enex[I] = status; toggle(&status); }
-        if (p->label[I] == L_BOUNCING && status == EX_EXIT) split[s][I] = 1;
+        if (p->label[I] == L_BOUNCING && ((status == EX_EXIT) ^ g_union)) split[s][I] = 1;
         if (p->label[I] == L_DELAYED_CROSSING) {
           p->enex[I] = status;
           if (first) {
-            if (status == EX_EXIT) p->label[I] = L_CROSSING;
+            if ((status == EX_EXIT) ^ g_union) p->label[I] = L_CROSSING;
             first = 0;
           } else {
-            if (status == EX_ENTRY) p->label[I] = L_CROSSING;
+            if ((status == EX_ENTRY) ^ g_union) p->label[I] = L_CROSSING;
             first = 1;
             toggle(&status);
           }
@@ -1146,10 +1156,10 @@ static int label_and_trace(lists_t *Ls, rings_t *R) {
         if (p->label[I] == L_DELAYED_BOUNCING) {
           p->enex[I] = status;
           if (first) {
-            if (status == EX_EXIT) cross[s][I] = 1;
+            if ((status == EX_EXIT) ^ g_union) cross[s][I] = 1;
             first = 0;
           } else {
-            if (status == EX_ENTRY) cross[s][I] = 1;
+            if ((status == EX_ENTRY) ^ g_union) cross[s][I] = 1;
             first = 1;
           }
           toggle(&status);
@@ -1180,8 +1190,13 @@ static int label_and_trace(lists_t *Ls, rings_t *R) {
       }
       insert_after(P, VP, IP);
       insert_after(Q, VQ, IQ);
-      P->enex[IP] = EX_EXIT; P->enex[VP] = EX_ENTRY;
-      Q->enex[IQ] = EX_EXIT; Q->enex[VQ] = EX_ENTRY;
+      if (!g_union) {
+        P->enex[IP] = EX_EXIT; P->enex[VP] = EX_ENTRY;
+        Q->enex[IQ] = EX_EXIT; Q->enex[VQ] = EX_ENTRY;
+      } else {
+        P->enex[IP] = EX_ENTRY; P->enex[VP] = EX_EXIT;
+        Q->enex[IQ] = EX_ENTRY; Q->enex[VQ] = EX_EXIT;
+      }
       P->label[IP] = P->label[VP] = L_CROSSING;
       Q->label[IQ] = Q->label[VQ] = L_CROSSING;
     }
@@ -1210,7 +1225,7 @@ static int label_and_trace(lists_t *Ls, rings_t *R) {
           toggle(&status);
           do {
             pv = side_pool(Ls, sV);
-            V = (status == EX_EXIT) ? pv->next[V] : pv->prev[V];
+            V = ((status == EX_EXIT) ^ g_union) ? pv->next[V] : pv->prev[V];
             pv->isect[V] = 0;
             /* the pool holds every vertex once plus slack: running out means
              * the trace never returns to its start (the reference loops) */

@@ -43,6 +43,9 @@ enum sbco_stat {
  * sbco_status().
  */
 sbco_run *sbco_clip(const double *b_xy, int nb, const double *c_xy, const int *c_sizes, int k);
+/* Union instead of intersection in the back end (the Foster code's UNION
+ * switch, foster/polyclip.h:39); applies to later sbco_clip calls. */
+void sbco_set_union(int on);
 int sbco_status(const sbco_run *r);              /* 0 = ok, else SBCO_E* */
 const char *sbco_message(const sbco_run *r);
 long sbco_len(const sbco_run *r, int ov, int which);  /* element count */

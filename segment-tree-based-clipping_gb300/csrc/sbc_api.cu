@@ -179,6 +179,8 @@ int sbc_create(const sbc_options* opt, sbc_ctx** out) {
   c->pl = new Pipeline(c->device, c->own);
   c->br = new sbc::BatchRunner(*c->pl);
   c->pw = new sbc::PairwiseRunner(*c->pl);
+  c->pl->unite = (c->flags & SBC_FLAG_UNION) != 0;
+  c->br->unite = c->pl->unite;
   *out = c;
   return SBC_OK;
 }

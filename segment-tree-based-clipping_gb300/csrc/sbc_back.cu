@@ -634,6 +634,7 @@ static int serial_backend(Pipeline& pl, const Merged& m, OverlayOut& out, int ta
   a.nbC = m.nbC;
   a.labB = m.labB;
   a.labC = m.labC;
+  a.unite = pl.unite ? 1 : 0;
   {
     ::sbc::KProbe kp_("k_serial_backend", st);
     k_serial_backend<<<1, 1, 0, st>>>(a);
@@ -668,7 +669,8 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
   cudaStream_t st = pl.stream();
   BufferPool& bp = pl.pool();
   const int ovTag = (int)(&out - &pl.outputs()[0]);
-  if (pl.force_serial_backend) return serial_backend(pl, m, out, ovTag);
+  // union mode has only the exact serial back end
+  if (pl.force_serial_backend || pl.unite) return serial_backend(pl, m, out, ovTag);
   const int nB = m.nB, nQ = m.nQ;
   auto* sc = (BkScalars*)bp.get("bk_scalars", sizeof(BkScalars));
   auto* srcP = (unsigned char*)bp.get("bk_srcP", nB);

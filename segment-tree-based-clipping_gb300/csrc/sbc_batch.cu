@@ -432,7 +432,7 @@ __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc,
 }
 
 __device__ PairResult clip_pair_back(const double* b, int nb, const double* c, int nc,
-                                     const Caps& cp, PairWork& w) {
+                                     const Caps& cp, PairWork& w, int unite) {
   PairResult res{PS_OK, 0, 0, 0.0, 0};
   const int K = w.state[2];
   if (K > cp.K) {
@@ -697,6 +697,7 @@ __device__ PairResult clip_pair_back(const double* b, int nb, const double* c, i
   a.nbC = w.nbC;
   a.labB = w.labB;
   a.labC = w.labC;
+  a.unite = unite;
   *a.nrings = 0;
   int st = ser_build(a);
   if (!st) {
@@ -816,6 +817,7 @@ struct ClipArgs {
   int* nrings;
   int* nverts;
   double* area;
+  int unite;            // union instead of intersection
   __device__ bool small(int p, int* nb, int* nc) const {
     *nb = (int)(boff[p + 1] - boff[p]);
     *nc = (int)(coff[p + 1] - coff[p]);
@@ -873,7 +875,8 @@ __global__ void __launch_bounds__(kBatchBlock) k_batch_back(ClipArgs A) {
   Caps cp;
   PairWork w = A.work(p, nb, nc, pass, &cp);
   if (w.state[0] != PS_OK) return;
-  const PairResult r = clip_pair_back(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w);
+  const PairResult r =
+      clip_pair_back(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w, A.unite);
   A.status[p] = r.status == PS_OK ? SBC_OK : (r.status == PS_UNDEF ? SBC_EUNDEF : SBC_ENOMEM);
   if (r.status == PS_CAP) A.need[p] = r.need;
   A.nrings[p] = r.nrings;
@@ -1258,7 +1261,7 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
       16.0 * (double)(h_boff_[p1] - h_boff_[p0] + h_coff_[p1] - h_coff_[p0]);
   launch_clip(ClipArgs{n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[0], aoff[0] + p0,
                        abase_[0], need_ + p0, need_ + p0, status + p0, nrings + p0, nverts + p0,
-                       area + p0},
+                       area + p0, unite ? 1 : 0},
               in_bytes, st);
   std::vector<int> hs(n);
   cudaMemcpyAsync(hs.data(), status + p0, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
@@ -1288,7 +1291,7 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
     if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch arena)");
     launch_clip(ClipArgs{n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[1],
                          aoff[1] + p0, 0, need_ + p0, need_ + p0, status + p0, nrings + p0,
-                         nverts + p0, area + p0},
+                         nverts + p0, area + p0, unite ? 1 : 0},
                 in_bytes, st);
   }
   // where each pair's data lives now: pass 0 arena, retry arena, or none
@@ -1544,11 +1547,11 @@ int BatchRunner::graph_record(int np_, const double* d_bxy, const long long* d_b
   cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     launch_clip(ClipArgs{np, d_bxy, d_boff, d_cxy, d_coff, pass0, arena[0], aoff[0], abase_[0],
-                         need_scr, need_rec, status, nrings, nverts, area},
+                         need_scr, need_rec, status, nrings, nverts, area, unite ? 1 : 0},
                 in_bytes, st);
     if (retry)
       launch_clip(ClipArgs{np, d_bxy, d_boff, d_cxy, d_coff, pass1, arena[1], aoff[1], 0, need_scr,
-                           need_rec, status, nrings, nverts, area},
+                           need_rec, status, nrings, nverts, area, unite ? 1 : 0},
                   in_bytes, st);
     const Arenas ar{arena[0], aoff[0], abase_[0], arena[1], aoff[1], 0, pass, need_rec};
     {

@@ -731,6 +731,7 @@ struct PwPairArgs {
   unsigned char* arena;
   const long long* aoff;
   int* status;  // per pair: PS_* code
+  int unite;    // union instead of intersection
   int* nrings;
   int* nverts;
   PwPip pip;
@@ -1216,6 +1217,7 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
   a.nbC = w.nbC;
   a.labB = nullptr;
   a.labC = w.labC;
+  a.unite = A.unite;
   *a.nrings = 0;
   PwPip pip = A.pip;
   pip.runIds = w.runIds;
@@ -1635,7 +1637,7 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
                   cudaEventCreateWithFlags(&ev_[1], cudaEventDisableTiming) != cudaSuccess))
     return pl_.fail(kECuda, "pairwise events");
   PwPairArgs pa{nov, d_coff, d_cxy, d_bxy, nb, pp, hstart, grouped, pass, order, arena0, aoff0,
-                status, nrings, nverts, pip};
+                status, pl_.unite ? 1 : 0, nrings, nverts, pip};
   cudaEventRecord(ev_[0], st);
   cudaStreamWaitEvent(st2_, ev_[0], 0);
   {

@@ -62,6 +62,8 @@ class Pipeline {
   long long stat_edges = 0, stat_epc = 0, stat_ts = 0, stat_cover = 0, stat_leaf = 0;
   // force the serial emulation of the back end (test hook)
   int force_serial_backend = 0;
+  // union instead of intersection (the Foster back end's UNION switch)
+  bool unite = false;
 
   // ---- shared state (public for the stage kernels' launchers) ----
   int nb = 0, k = 0, clSize = 0, E = 0;
@@ -189,6 +191,7 @@ class BatchRunner {
   const void* key_c = nullptr;
   bool valid = false;
   long long arena_budget = 0;   // bytes per chunk of arenas; 0: min(96 GiB, half of free)
+  bool unite = false;           // union instead of intersection
   // the area forward + backward of this batch as one CUDA graph (needs one
   // arena chunk and no large pair); kernels: launches per replay
   int graph_record(int np, const double* d_bxy, const long long* d_boff, const double* d_cxy,

@@ -57,6 +57,7 @@ struct SerialArgs {
   const int *alB, *nbC, *labB, *labC;
   int* status;   // 0 ok, 2 undefined, 3 capacity
   int rfull = 0;  // set when the ring pool ran out of nodes
+  int unite = 0;  // union instead of intersection (foster/polyclip.h:39 UNION)
 };
 
 __device__ int pnew(Pool& p, double x, double y) {
@@ -313,6 +314,9 @@ __device__ int ser_label_trace_t(SerialArgs& a, const PipP& pipP) {
     int root = roots[s], nocross = 1, V = root;
     do {
       if (p.isect[V] && (p.label[V] == L_CROSSING || p.label[V] == L_DCROSS)) nocross = 0;
+      // noCrossingVertex(UNION), foster/polygon.h:465-475
+      if (a.unite && p.isect[V] && (p.label[V] == L_BOUNCING || p.label[V] == L_DBOUNCE))
+        nocross = 0;
       V = p.next[V];
     } while (V != root);
     if (!nocross) continue;
@@ -355,7 +359,7 @@ __device__ int ser_label_trace_t(SerialArgs& a, const PipP& pipP) {
       } while (V != root);
       if (!found) return 2;
     }
-    if (pip_side(a, 1 - s, roots[1 - s], px, py, pipP))
+    if (pip_side(a, 1 - s, roots[1 - s], px, py, pipP) ^ a.unite)
       if (rcopy(a, p, root)) return 3;
   }
   if (ident[0] && ident[1]) {
@@ -384,14 +388,14 @@ __device__ int ser_label_trace_t(SerialArgs& a, const PipP& pipP) {
           p.enex[I] = status;
           tog(&status);
         }
-        if (p.label[I] == L_BOUNCING && status == EX_EXIT) split[I] = 1;
+        if (p.label[I] == L_BOUNCING && ((status == EX_EXIT) ^ a.unite)) split[I] = 1;
         if (p.label[I] == L_DCROSS) {
           p.enex[I] = status;
           if (first) {
-            if (status == EX_EXIT) p.label[I] = L_CROSSING;
+            if ((status == EX_EXIT) ^ a.unite) p.label[I] = L_CROSSING;
             first = 0;
           } else {
-            if (status == EX_ENTRY) p.label[I] = L_CROSSING;
+            if ((status == EX_ENTRY) ^ a.unite) p.label[I] = L_CROSSING;
             first = 1;
             tog(&status);
           }
@@ -399,10 +403,10 @@ __device__ int ser_label_trace_t(SerialArgs& a, const PipP& pipP) {
         if (p.label[I] == L_DBOUNCE) {
           p.enex[I] = status;
           if (first) {
-            if (status == EX_EXIT) cross[I] = 1;
+            if ((status == EX_EXIT) ^ a.unite) cross[I] = 1;
             first = 0;
           } else {
-            if (status == EX_ENTRY) cross[I] = 1;
+            if ((status == EX_ENTRY) ^ a.unite) cross[I] = 1;
             first = 1;
           }
           tog(&status);
@@ -435,8 +439,13 @@ __device__ int ser_label_trace_t(SerialArgs& a, const PipP& pipP) {
       }
       pinsert_after(P, VP, IP);
       pinsert_after(Q, VQ, IQ);
-      P.enex[IP] = EX_EXIT; P.enex[VP] = EX_ENTRY;
-      Q.enex[IQ] = EX_EXIT; Q.enex[VQ] = EX_ENTRY;
+      if (!a.unite) {
+        P.enex[IP] = EX_EXIT; P.enex[VP] = EX_ENTRY;
+        Q.enex[IQ] = EX_EXIT; Q.enex[VQ] = EX_ENTRY;
+      } else {
+        P.enex[IP] = EX_ENTRY; P.enex[VP] = EX_EXIT;
+        Q.enex[IQ] = EX_ENTRY; Q.enex[VQ] = EX_EXIT;
+      }
       P.label[IP] = P.label[VP] = L_CROSSING;
       Q.label[IQ] = Q.label[VQ] = L_CROSSING;
     }
@@ -466,10 +475,10 @@ __device__ int ser_label_trace_t(SerialArgs& a, const PipP& pipP) {
           Pool* pv;
           do {
             pv = &side(a, sV);
-            V = (status == EX_EXIT) ? pv->next[V] : pv->prev[V];
+            V = ((status == EX_EXIT) ^ a.unite) ? pv->next[V] : pv->prev[V];
             pv->isect[V] = 0;
             const int prov = (pv->src && pv->src[V] >= 0) ? (sV << 30) | pv->src[V] : -1;
-            if (radd_node(a, r, *pv, V, status == EX_EXIT, prov)) return 2;
+            if (radd_node(a, r, *pv, V, (status == EX_EXIT) ^ a.unite, prov)) return 2;
             if (--guard < 0) return 2;
           } while (!(pv->enex[V] == status) && !(sV == sI && V == I));
           if (!(sV == sI && V == I)) {

@@ -19,6 +19,7 @@ LIB_PATH = PKG / "_build" / "libsbclip.so"
 
 SBC_FLAG_TIMING = 1
 SBC_FLAG_SERIAL_BACKEND = 2
+SBC_FLAG_UNION = 4
 
 STATS = ["edges", "elementary_points", "tree_size", "cover_entries", "leaf_end_entries",
          "candidates_tested", "raw_hits", "unique", "slots_b", "slots_c", "serial_backend",
@@ -203,10 +204,13 @@ def _rings_from(r: _Rings):
 class Clipper:
     """One library context (one CUDA stream, grow-only device buffers)."""
 
-    def __init__(self, device: int = 0, timing: bool = False, serial_backend: bool = False):
+    def __init__(self, device: int = 0, timing: bool = False, serial_backend: bool = False,
+                 union: bool = False):
+        """union: every clipping call returns base ∪ overlay instead of base ∩ overlay."""
         self._L = load_library()
         opt = _Options(device, (SBC_FLAG_TIMING if timing else 0) |
-                       (SBC_FLAG_SERIAL_BACKEND if serial_backend else 0))
+                       (SBC_FLAG_SERIAL_BACKEND if serial_backend else 0) |
+                       (SBC_FLAG_UNION if union else 0))
         h = ctypes.c_void_p()
         rc = self._L.sbc_create(ctypes.byref(opt), ctypes.byref(h))
         if rc != 0:

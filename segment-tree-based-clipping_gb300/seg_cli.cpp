@@ -3,7 +3,7 @@
 // clipping on the GPU through libsbclip.so.
 //
 //   seg <base> <overlay_1> [<overlay_2> ... <overlay_k>] [--out DIR] [--precision P]
-//       [--device D]
+//       [--device D] [--union]
 //
 // Input files: the vertex count, then one `x,y` (or `x y`) line per vertex,
 // no closing duplicate (src/clip.cpp:181-298).  For overlay i the rings of
@@ -15,7 +15,9 @@
 // file.  With one overlay, the larger polygon is the base (the reference's
 // pairwise reader, src/clip.cpp:63-77; its copy loop requires it).  stdout:
 // a banner, `R ` per overlay, then the reference's TIME line fields in
-// microseconds: skeleton endlist cover cand+merge label total.
+// microseconds: skeleton endlist cover cand+merge label total.  --union
+// writes base ∪ overlay_i instead (the Foster back end's UNION switch,
+// foster/polyclip.h:39, which the reference's driver leaves off).
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -87,11 +89,12 @@ bool write_rings(const std::string& path, const sbc_rings& r, int precision) {
 int main(int argc, char** argv) {
   std::vector<const char*> pos;
   std::string outdir = "../results", outfile;
-  int precision = 6, device = 0;
+  int precision = 6, device = 0, flags = SBC_FLAG_TIMING;
   for (int i = 1; i < argc; ++i) {
     if (!strcmp(argv[i], "--out") && i + 1 < argc) outdir = argv[++i];
     else if (!strcmp(argv[i], "--precision") && i + 1 < argc) precision = atoi(argv[++i]);
     else if (!strcmp(argv[i], "--device") && i + 1 < argc) device = atoi(argv[++i]);
+    else if (!strcmp(argv[i], "--union")) flags |= SBC_FLAG_UNION;
     else pos.push_back(argv[i]);
   }
   if (pos.size() < 2) {
@@ -123,7 +126,7 @@ int main(int argc, char** argv) {
     sizes[0] = (int)(c.size() / 2);
   }
   printf("GB300 algorithm\n");
-  sbc_options opt{device, SBC_FLAG_TIMING};
+  sbc_options opt{device, flags};
   sbc_ctx* ctx = nullptr;
   int rc = sbc_create(&opt, &ctx);
   if (rc) {

@@ -105,3 +105,19 @@ KAT_PAIRS = [
     ((0, 0), (2, 0), (0, 0), (3, 0), 8),        # V overlap
     ((0, 0), (1, 0), (0, 1), (1, 1), 0),        # parallel, not collinear
 ]
+
+
+def load_union_cases():
+    """Union fixtures: (kind, base, overlay, rings) from the reference's back end
+    with its UNION switch set (tests/golden/make_golden.py)."""
+    z = np.load(GOLDEN / "golden_union.npz")
+    out, ro, ri = [], 0, 0
+    for i, kind in enumerate(z["kind"]):
+        b = z["b_xy"][z["b_off"][i]:z["b_off"][i + 1]]
+        c = z["c_xy"][z["c_off"][i]:z["c_off"][i + 1]]
+        rings = []
+        for _ in range(int(z["r_ring_cnt"][i])):
+            rings.append(z["r_xy"][z["r_off"][ro]:z["r_off"][ro + 1]])
+            ro += 1
+        out.append((str(kind), b, c, rings))
+    return out

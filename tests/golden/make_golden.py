@@ -178,5 +178,50 @@ def main():
     (OUT / "golden_digests.json").write_text(json.dumps(dig, indent=1) + "\n")
 
 
+def main_union():
+    """Union fixtures: the reference's Foster back end with its UNION switch
+    set (the harness's SBC_REF_UNION), one overlay per case: the small cases
+    with a single overlay, plus two star pairs of a few thousand vertices."""
+    if not O.ref_available():
+        raise SystemExit("build the reference first: python oracle/build_ref.py")
+    cases = [(k, b, ovs[0]) for k, b, ovs in small_cases() if len(ovs) == 1]
+    cases.append(("stars-3000-2500", gen.star(3000, 71), gen.star(2500, 72, centre=(0.2, -0.1))))
+    cases.append(("stars-1200-900", gen.star(1200, 73), gen.star(900, 74, centre=(-0.3, 0.25))))
+    store = {"kind": [], "b_off": [0], "b_xy": [], "c_off": [0], "c_xy": [], "r_ring_cnt": [],
+             "r_off": [0], "r_xy": []}
+    n_ok = n_skip = 0
+    for kind, b, c in cases:
+        try:
+            res = O.run_reference(b, [c], timeout=30, union=True)
+        except Exception:
+            n_skip += 1
+            continue
+        n_ok += 1
+        store["kind"].append(kind)
+        store["b_xy"].append(b)
+        store["b_off"].append(store["b_off"][-1] + len(b))
+        store["c_xy"].append(c)
+        store["c_off"].append(store["c_off"][-1] + len(c))
+        rings = res["rings"][0]
+        store["r_ring_cnt"].append(len(rings))
+        for r in rings:
+            store["r_xy"].append(r)
+            store["r_off"].append(store["r_off"][-1] + len(r))
+    np.savez_compressed(
+        OUT / "golden_union.npz",
+        kind=np.array(store["kind"]),
+        b_off=np.array(store["b_off"], np.int64), b_xy=np.concatenate(store["b_xy"]).astype(np.float64),
+        c_off=np.array(store["c_off"], np.int64), c_xy=np.concatenate(store["c_xy"]).astype(np.float64),
+        r_ring_cnt=np.array(store["r_ring_cnt"], np.int64), r_off=np.array(store["r_off"], np.int64),
+        r_xy=(np.concatenate(store["r_xy"]).astype(np.float64) if store["r_xy"] else np.zeros((0, 2))),
+    )
+    print(f"union cases: {n_ok} stored, {n_skip} skipped (reference crashed)")
+
+
 if __name__ == "__main__":
-    main()
+    import sys as _sys
+    if "--union-only" in _sys.argv:
+        main_union()
+    else:
+        main()
+        main_union()
