@@ -210,6 +210,23 @@ int sbc_clip_pairwise(sbc_ctx* ctx, const sbc_pairwise_job* job, sbc_batch_rings
                       void* stream);
 int sbc_clip_pairwise_device(sbc_ctx* ctx, const sbc_pairwise_job* job, sbc_batch_rings* out,
                              void* stream);
+/* Area of every overlay's result (the signed shoelace sum of its rings, 0
+ * where the status is not SBC_OK) and its gradient, for device arrays:
+ * sbc_pairwise_area_device clips the job (as sbc_clip_pairwise_device) and
+ * writes area[noverlays] and, if status is not NULL, status[noverlays].
+ * sbc_pairwise_area_backward_device writes d(sum_i grad_area[i] area[i]) /
+ * d(vertex) with the combinatorial structure held fixed: grad_b (2*nb
+ * doubles, summed over every overlay) and grad_c (2*c_off[noverlays]); it
+ * reuses the last pairwise call's rings when given the same job arrays and
+ * clips first otherwise.  A ring vertex's provenance is found by exact
+ * coordinates: a base vertex first, then an overlay vertex, then a proper
+ * crossing I = (1 - a) b1 + a b2.  Contributions are added atomically, so the
+ * last bits of the sums may differ between runs. */
+int sbc_pairwise_area_device(sbc_ctx* ctx, const sbc_pairwise_job* job, double* area, int* status,
+                             void* stream);
+int sbc_pairwise_area_backward_device(sbc_ctx* ctx, const sbc_pairwise_job* job,
+                                      const double* grad_area, double* grad_b, double* grad_c,
+                                      void* stream);
 /* Diagnostics of the last sbc_clip_pairwise call: out[0] overlays clipped by
  * the single-pair pipeline (inputs outside the batched path's conditions),
  * out[1] unique intersecting edge pairs, out[2] box-overlapping edge pairs

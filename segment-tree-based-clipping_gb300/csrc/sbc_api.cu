@@ -816,3 +816,38 @@ extern "C" void sbc_area_graph_destroy(sbc_graph* g) {
   if (g->exec) cudaGraphExecDestroy(g->exec);
   delete g;
 }
+
+extern "C" int sbc_pairwise_area_device(sbc_ctx* c, const sbc_pairwise_job* j, double* area,
+                                        int* status, void* stream) {
+  if (c && j && j->noverlays > 0 && !area) return set_err(c, SBC_EINPUT, "null area output");
+  sbc_batch_rings dr;
+  int rc = sbc_clip_pairwise_device(c, j, &dr, stream);
+  if (rc) return rc;
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  rc = c->pw->area(area, st);
+  if (rc) return set_err(c, rc, c->pl->error());
+  if (status && j->noverlays > 0)
+    cudaMemcpyAsync(status, c->pw->status, sizeof(int) * j->noverlays, cudaMemcpyDeviceToDevice, st);
+  return cuda_check(c, cudaStreamSynchronize(st), "pairwise area");
+}
+
+extern "C" int sbc_pairwise_area_backward_device(sbc_ctx* c, const sbc_pairwise_job* j,
+                                                 const double* grad_area, double* grad_b,
+                                                 double* grad_c, void* stream) {
+  int rc = pairwise_check(c, j);
+  if (rc) return rc;
+  if (!grad_b || (j->noverlays > 0 && (!grad_area || !grad_c)))
+    return set_err(c, SBC_EINPUT, "null gradient array");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  if (!(c->pw->valid && c->pw->np == j->noverlays && c->pw->key_b == j->b_xy &&
+        c->pw->key_c == j->c_xy)) {
+    sbc_batch_rings dr;
+    rc = sbc_clip_pairwise_device(c, j, &dr, stream);
+    if (rc) return rc;
+  }
+  c->pl->clear_error();
+  rc = c->pw->backward(j->b_xy, j->c_xy, j->c_off, grad_area, grad_b, grad_c, st);
+  if (rc) return set_err(c, rc, c->pl->error());
+  return SBC_OK;
+}

@@ -1389,6 +1389,9 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
   np = nov;
   fallback_pairs = 0;
   big_pairs = 0;
+  fb_rec_.clear();
+  fb_xy_.clear();
+  valid = false;
   hits = 0;
   tested = 0;
   if (nb < 3) return pl_.fail(kEInput, "base needs at least 3 vertices");
@@ -1750,6 +1753,23 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
       continue;
     }
     if (rc) return rc;
+    // its records too (the gradient's provenance of crossings)
+    const int K = pl_.dbg_K;
+    if (K > 0) {
+      std::vector<int> rb(K), rc2(K), rt(K);
+      std::vector<double> rxy(2 * (size_t)K);
+      cudaMemcpyAsync(rb.data(), pl_.dbg_ub, sizeof(int) * K, cudaMemcpyDeviceToHost, st);
+      cudaMemcpyAsync(rc2.data(), pl_.dbg_uc, sizeof(int) * K, cudaMemcpyDeviceToHost, st);
+      cudaMemcpyAsync(rt.data(), pl_.dbg_ut, sizeof(int) * K, cudaMemcpyDeviceToHost, st);
+      cudaMemcpyAsync(rxy.data(), pl_.dbg_isxy, sizeof(double) * 2 * K, cudaMemcpyDeviceToHost, st);
+      if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise records");
+      for (int r = 0; r < K; ++r) {
+        if (rt[r] != 1) continue;
+        fb_rec_.push_back({{p, rb[r] >> 1, rc2[r] >> 1, 1}});
+        fb_xy_.push_back(rxy[2 * r]);
+        fb_xy_.push_back(rxy[2 * r + 1]);
+      }
+    }
     const int k2 = keep(p);
     if (k2) return k2;
   }
@@ -1795,6 +1815,344 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
                   st);
   cudaMemcpyAsync(status, h_status.data(), sizeof(int) * nov, cudaMemcpyHostToDevice, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise output");
+  // kept for the area gradient
+  last_nb_ = nb;
+  last_totalC_ = totalC;
+  last_nh_ = (long long)nh;
+  h_coff_ = hoff;
+  key_b = d_bxy;
+  key_c = d_cxy;
+  valid = true;
+  return kOk;
+}
+
+}  // namespace sbc
+
+// ------------------------------------------------------------------ area and gradient
+// Area of overlay i's result: the signed shoelace sum of its rings.  Its
+// gradient with the combinatorial structure held fixed chains through where
+// each ring vertex comes from, found by exact coordinates in the order a base
+// vertex, an overlay vertex, a proper crossing I = (1 - a) b1 + a b2 (a
+// type-1 record) -- candidates sorted by (pair, x, y), ties in that order.
+namespace sbc {
+namespace {
+
+__global__ void k_pwa_area(int nov, const long long* __restrict__ pair_ring,
+                           const long long* __restrict__ ring_off, const double* __restrict__ xy,
+                           const int* __restrict__ status, double* __restrict__ area) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nov) return;
+  double a = 0.0;
+  if (status[p] == SBC_OK) {
+    for (long long r = pair_ring[p]; r < pair_ring[p + 1]; ++r) {
+      const long long s = ring_off[r], e = ring_off[r + 1];
+      double s2 = 0.0;
+      for (long long i = s; i < e; ++i) {
+        const long long j = (i + 1 == e) ? s : i + 1;
+        s2 = dadd(s2, dsub(dmul(xy[2 * i], xy[2 * j + 1]), dmul(xy[2 * j], xy[2 * i + 1])));
+      }
+      a = dadd(a, dmul(0.5, s2));
+    }
+  }
+  area[p] = a;
+}
+
+__global__ void k_pwa_base_keys(int nb, const double* __restrict__ b,
+                                unsigned long long* __restrict__ kx,
+                                unsigned long long* __restrict__ ky, unsigned* __restrict__ val) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  kx[i] = dkey(b[2 * i]);
+  ky[i] = dkey(b[2 * i + 1]);
+  val[i] = (unsigned)i;
+}
+
+// per-pair candidates: overlay vertices, then the type-1 records of the
+// batched pairs (hits), then those of pairs the pair pipeline clipped
+struct PwaCand {
+  int nov;
+  const long long* coff;
+  long long totalC;
+  const double* cxy;
+  long long nh;
+  const PwHit* hits;
+  int nb;
+  const double* b;
+  long long nfb;
+  const int4* fb_rec;   // pair, base edge, overlay edge, type
+  const double* fb_xy;  // crossing coordinates
+};
+
+__device__ __forceinline__ void pwa_decode(const PwaCand& C, long long i, int* pair, int4* t) {
+  if (i < C.totalC) {
+    int lo = 0, hi = C.nov;
+    while (hi - lo > 1) {
+      const int m = (lo + hi) >> 1;
+      if (C.coff[m] <= i) lo = m;
+      else hi = m;
+    }
+    *pair = lo;
+    *t = make_int4(1, (int)(i - C.coff[lo]), 0, 0);
+  } else if (i < C.totalC + C.nh) {
+    const PwHit& h = C.hits[i - C.totalC];
+    *pair = h.pair;
+    *t = make_int4(2, h.b, h.j, h.type);
+  } else {
+    const int4 r = C.fb_rec[i - C.totalC - C.nh];
+    *pair = r.x;
+    *t = make_int4(2, r.y, r.z, r.w);
+  }
+}
+
+__global__ void k_pwa_cand(PwaCand C, long long n, unsigned long long* __restrict__ kx,
+                           unsigned long long* __restrict__ ky, unsigned long long* __restrict__ kp,
+                           unsigned* __restrict__ val) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int pair;
+  int4 t;
+  pwa_decode(C, i, &pair, &t);
+  double x = 0.0, y = 0.0;
+  bool use = true;
+  if (t.x == 1) {
+    x = C.cxy[2 * (C.coff[pair] + t.y)];
+    y = C.cxy[2 * (C.coff[pair] + t.y) + 1];
+  } else if (i < C.totalC + C.nh) {
+    use = t.w == 1;
+    if (use) {  // I = (1 - a) b1 + a b2, as the record stage computed it
+      const double al = C.hits[i - C.totalC].al;
+      const int i2 = t.y + 1 == C.nb ? 0 : t.y + 1;
+      const double oma = dsub(1.0, al);
+      x = dadd(dmul(oma, C.b[2 * t.y]), dmul(al, C.b[2 * i2]));
+      y = dadd(dmul(oma, C.b[2 * t.y + 1]), dmul(al, C.b[2 * i2 + 1]));
+    }
+  } else {
+    const long long r = i - C.totalC - C.nh;
+    x = C.fb_xy[2 * r];
+    y = C.fb_xy[2 * r + 1];
+  }
+  kx[i] = use ? dkey(x) : ~0ull;
+  ky[i] = use ? dkey(y) : ~0ull;
+  kp[i] = use ? (unsigned long long)pair : ~0ull;
+  val[i] = (unsigned)i;
+}
+
+__global__ void k_pwa_gather(long long n, const unsigned long long* __restrict__ src,
+                             const unsigned* __restrict__ val, unsigned long long* __restrict__ dst) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) dst[t] = src[val[t]];
+}
+
+struct PwaLook {
+  int nov;
+  const long long* pair_ring;
+  long long nrings;
+  const long long* ring_off;
+  const double* xy;
+  int nb;
+  const unsigned long long* bkx;  // base vertices sorted by (x, y)
+  const unsigned long long* bky;
+  const unsigned* bval;
+  long long nc;                   // candidates sorted by (pair, x, y)
+  const unsigned long long* ckp;
+  const unsigned long long* ckx;
+  const unsigned long long* cky;
+  const unsigned* cval;
+  PwaCand C;
+};
+
+// the ring and pair that own output vertex v
+__device__ __forceinline__ void pwa_owner(const PwaLook& L, long long v, long long* ring, int* pair) {
+  long long lo = 0, hi = L.nrings;
+  while (hi - lo > 1) {
+    const long long m = (lo + hi) >> 1;
+    if (L.ring_off[m] <= v) lo = m;
+    else hi = m;
+  }
+  *ring = lo;
+  int a = 0, b = L.nov;  // last pair with pair_ring <= ring (and rings to own)
+  while (b - a > 1) {
+    const int m = (a + b) >> 1;
+    if (L.pair_ring[m] <= lo) a = m;
+    else b = m;
+  }
+  while (a + 1 < L.nov && L.pair_ring[a + 1] <= lo) ++a;
+  *pair = a;
+}
+
+__global__ void k_pwa_tape(PwaLook L, long long nv, int4* __restrict__ tape) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  long long ring;
+  int pair;
+  pwa_owner(L, v, &ring, &pair);
+  const unsigned long long qx = dkey(L.xy[2 * v]), qy = dkey(L.xy[2 * v + 1]);
+  int4 t = make_int4(-1, 0, 0, 0);
+  {
+    int lo = 0, hi = L.nb;
+    while (lo < hi) {
+      const int m = (lo + hi) >> 1;
+      if (L.bkx[m] < qx || (L.bkx[m] == qx && L.bky[m] < qy)) lo = m + 1;
+      else hi = m;
+    }
+    if (lo < L.nb && L.bkx[lo] == qx && L.bky[lo] == qy) t = make_int4(0, (int)L.bval[lo], 0, 0);
+  }
+  if (t.x < 0) {
+    const unsigned long long qp = (unsigned long long)pair;
+    long long lo = 0, hi = L.nc;
+    while (lo < hi) {
+      const long long m = (lo + hi) >> 1;
+      const bool less = L.ckp[m] < qp || (L.ckp[m] == qp && (L.ckx[m] < qx ||
+                                                            (L.ckx[m] == qx && L.cky[m] < qy)));
+      if (less) lo = m + 1;
+      else hi = m;
+    }
+    if (lo < L.nc && L.ckp[lo] == qp && L.ckx[lo] == qx && L.cky[lo] == qy) {
+      int pr;
+      int4 d;
+      pwa_decode(L.C, (long long)L.cval[lo], &pr, &d);
+      t = d.x == 1 ? make_int4(1, d.y, 0, 0) : make_int4(2, d.y, d.z, 0);
+    }
+  }
+  tape[v] = t;
+}
+
+__global__ void k_pwa_backward(PwaLook L, long long nv, const int4* __restrict__ tape,
+                               const double* __restrict__ gA, const double* __restrict__ b,
+                               const double* __restrict__ cxy, const long long* __restrict__ coff,
+                               double* __restrict__ gb, double* __restrict__ gc) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  long long ring;
+  int pair;
+  pwa_owner(L, v, &ring, &pair);
+  const long long s = L.ring_off[ring], e = L.ring_off[ring + 1];
+  const long long ip = (v + 1 == e) ? s : v + 1, im = (v == s) ? e - 1 : v - 1;
+  const double g = gA[pair];
+  const double gx = 0.5 * g * (L.xy[2 * ip + 1] - L.xy[2 * im + 1]);
+  const double gy = 0.5 * g * (L.xy[2 * im] - L.xy[2 * ip]);
+  const int4 t = tape[v];
+  const int nb = L.nb;
+  const long long c0 = coff[pair];
+  const int nc = (int)(coff[pair + 1] - c0);
+  const double* c = cxy + 2 * c0;
+  double* gcp = gc + 2 * c0;
+  if (t.x == 0) {
+    atomicAdd(&gb[2 * t.y], gx);
+    atomicAdd(&gb[2 * t.y + 1], gy);
+  } else if (t.x == 1) {
+    atomicAdd(&gcp[2 * t.y], gx);
+    atomicAdd(&gcp[2 * t.y + 1], gy);
+  } else if (t.x == 2) {
+    const int i1 = t.y, i2 = (t.y + 1) % nb, j1 = t.z, j2 = (t.z + 1) % nc;
+    const double b1x = b[2 * i1], b1y = b[2 * i1 + 1], b2x = b[2 * i2], b2y = b[2 * i2 + 1];
+    const double c1x = c[2 * j1], c1y = c[2 * j1 + 1], c2x = c[2 * j2], c2y = c[2 * j2 + 1];
+    const double A1 = (c1x - b1x) * (c2y - b1y) - (c1y - b1y) * (c2x - b1x);
+    const double A2 = (c1x - b2x) * (c2y - b2y) - (c1y - b2y) * (c2x - b2x);
+    const double d = A1 - A2;
+    const double al = A1 / d;
+    const double ga = gx * (b2x - b1x) + gy * (b2y - b1y);
+    const double k1 = -A2 / (d * d) * ga, k2 = A1 / (d * d) * ga;
+    atomicAdd(&gb[2 * i1], (1.0 - al) * gx + k1 * (c1y - c2y));
+    atomicAdd(&gb[2 * i1 + 1], (1.0 - al) * gy + k1 * (c2x - c1x));
+    atomicAdd(&gb[2 * i2], al * gx + k2 * (c1y - c2y));
+    atomicAdd(&gb[2 * i2 + 1], al * gy + k2 * (c2x - c1x));
+    atomicAdd(&gcp[2 * j1], k1 * (c2y - b1y) + k2 * (c2y - b2y));
+    atomicAdd(&gcp[2 * j1 + 1], k1 * (b1x - c2x) + k2 * (b2x - c2x));
+    atomicAdd(&gcp[2 * j2], k1 * (b1y - c1y) + k2 * (b2y - c1y));
+    atomicAdd(&gcp[2 * j2 + 1], k1 * (c1x - b1x) + k2 * (c1x - b2x));
+  }
+}
+
+}  // namespace
+
+int PairwiseRunner::area(double* d_area, cudaStream_t st) {
+  if (!valid) return pl_.fail(kEInput, "no pairwise result to take the area of");
+  if (np <= 0) return kOk;
+  ::sbc::KProbe kp_("k_pwa_area", st, 16.0 * (double)total_verts);
+  k_pwa_area<<<grid_for(np, 128), 128, 0, st>>>(np, pair_ring, ring_off, xy, status, d_area);
+  return kOk;
+}
+
+int PairwiseRunner::backward(const double* d_bxy, const double* d_cxy, const long long* d_coff,
+                             const double* d_gA, double* d_gb, double* d_gc, cudaStream_t st) {
+  if (!valid) return pl_.fail(kEInput, "no pairwise result to differentiate");
+  BufferPool& pool = pl_.pool();
+  const int nb = last_nb_;
+  const long long totalC = last_totalC_, nh = last_nh_, nfb = (long long)fb_rec_.size();
+  cudaMemsetAsync(d_gb, 0, sizeof(double) * 2 * nb, st);
+  if (totalC > 0) cudaMemsetAsync(d_gc, 0, sizeof(double) * 2 * totalC, st);
+  if (np <= 0 || total_verts == 0) {
+    if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise backward");
+    return kOk;
+  }
+  // base vertices sorted by (x, y): by y, then stably by x
+  auto* bkx = (unsigned long long*)pool.get("pwa_bkx", sizeof(unsigned long long) * (nb + 1));
+  auto* bky = (unsigned long long*)pool.get("pwa_bky", sizeof(unsigned long long) * (nb + 1));
+  auto* bk2 = (unsigned long long*)pool.get("pwa_bk2", sizeof(unsigned long long) * (nb + 1));
+  auto* bk3 = (unsigned long long*)pool.get("pwa_bk3", sizeof(unsigned long long) * (nb + 1));
+  auto* bval = (unsigned*)pool.get("pwa_bval", sizeof(unsigned) * (nb + 1));
+  auto* bval2 = (unsigned*)pool.get("pwa_bval2", sizeof(unsigned) * (nb + 1));
+  const long long nc = totalC + nh + nfb;
+  auto* ckx = (unsigned long long*)pool.get("pwa_ckx", sizeof(unsigned long long) * (nc + 1));
+  auto* cky = (unsigned long long*)pool.get("pwa_cky", sizeof(unsigned long long) * (nc + 1));
+  auto* ckp = (unsigned long long*)pool.get("pwa_ckp", sizeof(unsigned long long) * (nc + 1));
+  auto* ck2 = (unsigned long long*)pool.get("pwa_ck2", sizeof(unsigned long long) * (nc + 1));
+  auto* ck3 = (unsigned long long*)pool.get("pwa_ck3", sizeof(unsigned long long) * (nc + 1));
+  auto* cval = (unsigned*)pool.get("pwa_cval", sizeof(unsigned) * (nc + 1));
+  auto* cval2 = (unsigned*)pool.get("pwa_cval2", sizeof(unsigned) * (nc + 1));
+  void* rscr = pool.get("pwa_rscr", radix_scratch_bytes((nc > nb ? nc : nb) + 1));
+  int4* fbr = (int4*)pool.get("pwa_fbrec", sizeof(int4) * (nfb + 1));
+  double* fbxy = (double*)pool.get("pwa_fbxy", sizeof(double) * 2 * (nfb + 1));
+  int4* tape = (int4*)pool.get("pwa_tape", sizeof(int4) * (total_verts + 1));
+  const PwHit* hits = (const PwHit*)pool.get("pw_hits_grouped", sizeof(PwHit) * (nh + 1));
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise backward)");
+  if (nfb) {
+    std::vector<int4> h(nfb);
+    for (long long r = 0; r < nfb; ++r)
+      h[r] = make_int4(fb_rec_[r][0], fb_rec_[r][1], fb_rec_[r][2], fb_rec_[r][3]);
+    cudaMemcpyAsync(fbr, h.data(), sizeof(int4) * nfb, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(fbxy, fb_xy_.data(), sizeof(double) * 2 * nfb, cudaMemcpyHostToDevice, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise backward");
+  }
+  {
+    ::sbc::KProbe kp_("k_pwa_base_keys", st, 36.0 * nb);
+    k_pwa_base_keys<<<grid_for(nb, 256), 256, 0, st>>>(nb, d_bxy, bkx, bky, bval);
+  }
+  cudaMemcpyAsync(bk2, bky, sizeof(unsigned long long) * nb, cudaMemcpyDeviceToDevice, st);
+  radix_sort_u64(bk2, bval, bk3, bval2, nb, rscr, st);
+  k_pwa_gather<<<grid_for(nb, 256), 256, 0, st>>>(nb, bkx, bval, bk2);
+  radix_sort_u64(bk2, bval, bk3, bval2, nb, rscr, st);
+  // bk2: x keys in (x, y) order; bk3: the y keys in that order
+  k_pwa_gather<<<grid_for(nb, 256), 256, 0, st>>>(nb, bky, bval, bk3);
+  PwaCand C{np, d_coff, totalC, d_cxy, nh, hits, nb, d_bxy, nfb, fbr, fbxy};
+  {
+    ::sbc::KProbe kp_("k_pwa_cand", st, 40.0 * (double)nc);
+    k_pwa_cand<<<grid_for(nc, 256), 256, 0, st>>>(C, nc, ckx, cky, ckp, cval);
+  }
+  // by y, by x, by pair (stable): sorted by (pair, x, y), ties in candidate order
+  cudaMemcpyAsync(ck2, cky, sizeof(unsigned long long) * nc, cudaMemcpyDeviceToDevice, st);
+  radix_sort_u64(ck2, cval, ck3, cval2, nc, rscr, st);
+  k_pwa_gather<<<grid_for(nc, 256), 256, 0, st>>>(nc, ckx, cval, ck2);
+  radix_sort_u64(ck2, cval, ck3, cval2, nc, rscr, st);
+  k_pwa_gather<<<grid_for(nc, 256), 256, 0, st>>>(nc, ckp, cval, ck2);
+  radix_sort_u64(ck2, cval, ck3, cval2, nc, rscr, st);
+  // ck2 now holds pair keys in order; gather x and y keys in the same order
+  k_pwa_gather<<<grid_for(nc, 256), 256, 0, st>>>(nc, ckx, cval, ck3);
+  k_pwa_gather<<<grid_for(nc, 256), 256, 0, st>>>(nc, cky, cval, ckx);
+  // (ckx reused for sorted y keys: the unsorted x keys are no longer needed)
+  const PwaLook L{np, pair_ring, total_rings, ring_off, xy, nb, bk2, bk3, bval, nc, ck2, ck3, ckx,
+                  cval, C};
+  {
+    ::sbc::KProbe kp_("k_pwa_tape", st, 48.0 * (double)total_verts);
+    k_pwa_tape<<<grid_for(total_verts, 256), 256, 0, st>>>(L, total_verts, tape);
+  }
+  {
+    ::sbc::KProbe kp_("k_pwa_backward", st, 64.0 * (double)total_verts);
+    k_pwa_backward<<<grid_for(total_verts, 256), 256, 0, st>>>(L, total_verts, tape, d_gA, d_bxy,
+                                                               d_cxy, d_coff, d_gb, d_gc);
+  }
+  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise backward");
   return kOk;
 }
 

@@ -4,6 +4,7 @@
 // repeated calls of the same size allocate nothing.
 #pragma once
 
+#include <array>
 #include <map>
 #include <string>
 #include <vector>
@@ -238,6 +239,14 @@ class PairwiseRunner {
           cudaStream_t st);
   int autotune(const double* d_bxy, int nb, int nov, const double* d_cxy, const long long* d_coff,
                cudaStream_t st, double* best_ms);
+  // area of every overlay's result (device, np doubles) from the last run
+  int area(double* d_area, cudaStream_t st);
+  // d(sum grad_area * area)/d(base, overlays) from the last run's rings
+  int backward(const double* d_bxy, const double* d_cxy, const long long* d_coff,
+               const double* d_gA, double* d_gb, double* d_gc, cudaStream_t st);
+  const void* key_b = nullptr;   // the last run's inputs (for reuse by backward)
+  const void* key_c = nullptr;
+  bool valid = false;
   int np = 0;
   int* status = nullptr;            // device, per overlay: SBC_* code
   long long* pair_ring = nullptr;   // device, np+1
@@ -261,6 +270,12 @@ class PairwiseRunner {
   std::vector<int> order_h;
   unsigned pair_blocks_ = 0;
   unsigned pair_grid(int nov);
+  // the last run, for area and backward
+  int last_nb_ = 0;
+  long long last_totalC_ = 0, last_nh_ = 0;
+  std::vector<long long> h_coff_;
+  std::vector<std::array<int, 4>> fb_rec_;  // records of pipeline-clipped pairs: pair, b, c, type
+  std::vector<double> fb_xy_;
 };
 
 }  // namespace sbc

@@ -145,6 +145,9 @@ def load_library(path: str | os.PathLike | None = None):
         getattr(L, nm).argtypes = [vp, ctypes.POINTER(_PairwiseJob), ctypes.POINTER(_BatchRings),
                                    vp]
     L.sbc_pairwise_info.argtypes = [vp, ctypes.POINTER(ll), i]
+    L.sbc_pairwise_area_device.argtypes = [vp, ctypes.POINTER(_PairwiseJob), vp, vp, vp]
+    L.sbc_pairwise_area_backward_device.argtypes = [vp, ctypes.POINTER(_PairwiseJob), vp, vp, vp,
+                                                    vp]
     L.sbc_batch_set_arena_budget.argtypes = [vp, ll]
     L.sbc_area_graph_create.argtypes = [vp, ctypes.POINTER(_Batch), vp, vp, vp, vp, vp, vp,
                                         ctypes.POINTER(vp)]
@@ -379,6 +382,19 @@ class Clipper:
         v = (ctypes.c_longlong * 2)()
         self._L.sbc_batch_info(self._h, v, 2)
         return {"chunks": v[0], "large_pairs": v[1]}
+
+    def pairwise_area_device(self, d_bxy, nb, noverlays, d_cxy, d_coff, d_area, d_status=None,
+                             stream: int | None = None) -> None:
+        j = _PairwiseJob(d_bxy, nb, noverlays, d_cxy, d_coff)
+        self._check(self._L.sbc_pairwise_area_device(self._h, ctypes.byref(j), d_area, d_status,
+                                                     stream))
+
+    def pairwise_area_backward_device(self, d_bxy, nb, noverlays, d_cxy, d_coff, d_grad_area,
+                                      d_grad_b, d_grad_c, stream: int | None = None) -> None:
+        j = _PairwiseJob(d_bxy, nb, noverlays, d_cxy, d_coff)
+        self._check(self._L.sbc_pairwise_area_backward_device(self._h, ctypes.byref(j),
+                                                              d_grad_area, d_grad_b, d_grad_c,
+                                                              stream))
 
     def pairwise_info(self) -> dict:
         """Diagnostics of the last pairwise call."""

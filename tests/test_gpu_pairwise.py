@@ -143,3 +143,44 @@ def test_pairwise_small_base_and_repeat(clipper):
     assert all(rings_equal(x, y) for x, y in zip(a, b))
     got, st = clipper.clip_pairwise(base, [])
     assert got == [] and len(st) == 0
+
+
+def test_pairwise_area_and_gradient(clipper):
+    """Areas against the FP64 shoelace of the oracle's rings, gradients against
+    the host FP64 gradient of the same rings (base gradient summed over the
+    overlays), 1e-12 relative; a fallback pair (shared x value) included."""
+    torch = pytest.importorskip("torch")
+    import area_grad as AG
+    import sbclip
+    base, ovs = gen.one_to_many(n_base=1_500, n_overlays=40, seed=3500, hi=300,
+                                near_boundary=0.7)
+    sq = np.array([[-30.0, -30.0], [30.0, -30.0], [30.0, 30.0], [-30.0, 30.0]]) + base[5]
+    sq[1, 0] += 0.37
+    sq[0, 0] = base[5, 0]  # shares an x value with the base: the pair pipeline clips it
+    ovs.append(sq)
+    cxy, coff = sbclip.pack_polygons(ovs)
+    dev = "cuda:0"
+    tb = torch.from_numpy(np.ascontiguousarray(base)).to(dev)
+    tc = torch.from_numpy(cxy).to(dev)
+    to = torch.from_numpy(coff).to(dev)
+    n = len(ovs)
+    area = torch.zeros(n, dtype=torch.float64, device=dev)
+    st = torch.zeros(n, dtype=torch.int32, device=dev)
+    args = (tb.data_ptr(), len(base), n, tc.data_ptr(), to.data_ptr())
+    clipper.pairwise_area_device(*args, area.data_ptr(), st.data_ptr())
+    assert (st == 0).all()
+    assert clipper.pairwise_info()["fallback_pairs"] >= 1
+    w = torch.linspace(0.5, 2.0, n, dtype=torch.float64, device=dev)
+    gb = torch.zeros_like(tb)
+    gc = torch.zeros_like(tc)
+    clipper.pairwise_area_backward_device(*args, w.data_ptr(), gb.data_ptr(), gc.data_ptr())
+    a = area.cpu().numpy()
+    gb, gc = gb.cpu().numpy(), gc.cpu().numpy()
+    wb = np.zeros_like(base)
+    for i, c in enumerate(ovs):
+        want, hb, hc = AG.area_gradient(base, c)
+        assert abs(a[i] - want) <= 1e-12 * max(1.0, abs(want)), i
+        wb += w[i].item() * hb
+        scale = max(np.abs(hc).max(), 1e-300) * w[i].item()
+        assert np.abs(gc[coff[i]:coff[i + 1]] - w[i].item() * hc).max() <= 1e-11 * scale, i
+    assert np.abs(gb - wb).max() <= 1e-11 * max(np.abs(wb).max(), 1e-300)
