@@ -576,6 +576,25 @@ def run_one_to_many(args, rank: int, world: int):
     e2e = {"value": nov * world / (float(np.mean(e2e_t)) * 1e-3), "unit": "pairs/s",
            "h2d_bytes_per_step": int(base.nbytes + cxy.nbytes + coff.nbytes),
            "d2h_bytes_per_step": int(d2h)}
+    # area forward + backward of every pair (the gradient of the shared base
+    # summed over the overlays): a separate figure next to the forward metric
+    fb_area = torch.zeros(nov, dtype=torch.float64, device=cuda)
+    fb_g = torch.ones(nov, dtype=torch.float64, device=cuda)
+    fb_gb = torch.zeros_like(tb)
+    fb_gc = torch.zeros_like(tc)
+    fb_t = []
+    for k in range(3):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        clip.pairwise_area_device(tb.data_ptr(), len(base), nov, tc.data_ptr(), to.data_ptr(),
+                                  fb_area.data_ptr(), None, sp)
+        clip.pairwise_area_backward_device(tb.data_ptr(), len(base), nov, tc.data_ptr(),
+                                           to.data_ptr(), fb_g.data_ptr(), fb_gb.data_ptr(),
+                                           fb_gc.data_ptr(), sp)
+        torch.cuda.synchronize()
+        if k:
+            fb_t.append((time.perf_counter() - t0) * 1e3)
     # the plain per-pair GPU path: one sbc_clip_pair_device call per overlay
     sample = 64
     rng = np.random.default_rng(5)
@@ -618,7 +637,9 @@ def run_one_to_many(args, rank: int, world: int):
                    "box_overlapping_edge_pairs_tested": info["tested"],
                    "edge_pairs_tested_per_s": info["tested"] / (ms * 1e-3),
                    "per_pair_gpu_path_pairs_per_s": per_pair, "per_pair_sample": sample,
-                   "batched_over_per_pair": value / per_pair},
+                   "batched_over_per_pair": value / per_pair,
+                   "area_forward_backward_ms": float(np.mean(fb_t)),
+                   "area_forward_backward_pairs_per_s": nov / (float(np.mean(fb_t)) * 1e-3)},
     }
     if rank == 0 and not args.no_cpu_baseline:
         sample_cpu = [(base, ovs[int(p)]) for p in pick[:32]]
