@@ -31,8 +31,9 @@
 // covers; a base edge is tested in the cell holding the low corner of the two
 // boxes' overlap only, so every box-overlapping pair is tested once.
 //
-// Back end: one thread per pair runs rows A9-A18 (src/clip.cpp:368-695,
-// foster/polyclip.h:337-787) with the overlay's merged arrays in full and the
+// Back end: one warp per pair runs rows A9-A18 (src/clip.cpp:368-695,
+// foster/polyclip.h:337-787), its lanes sharing the per-record, per-run and
+// per-slot steps, with the overlay's merged arrays in full and the
 // base's only where intersections are: the base's merged list holds ~n_b
 // plain vertices per pair, so its linked list is built with run nodes (a
 // stretch of plain vertices as one node, sbc_serial.cuh) and pointInPoly
@@ -40,6 +41,7 @@
 // row of the grid.
 #include <algorithm>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -54,6 +56,7 @@ namespace sbc {
 
 namespace {
 
+constexpr unsigned kFullMask = 0xffffffffu;
 constexpr int kPwMaxOverlay = 16384;  // larger overlays go to the pair pipeline
 constexpr int kPwMaxCells = 1 << 14;  // an overlay edge box over more cells: pair pipeline
 constexpr int kPwLongCells = 64;      // base edges over more cells per axis skip the grid
@@ -668,7 +671,9 @@ __host__ __device__ __forceinline__ size_t pw_arena_bytes(int nb, int nc, int K,
 // pointInPoly against the base side of a pair whose list has run nodes: the
 // steps of the edges between nodes, plus those of the base edges inside run
 // nodes, which come from the grid row holding ry (each edge counted in the
-// first cell of its box in that row)
+// first cell of its box in that row).  Called by all 32 lanes of a warp with
+// the same arguments: the row's cells and the long edges are split over the
+// lanes and the steps summed (the winding number is order-free).
 struct PwPip {
   const double* b;
   int nb;
@@ -699,12 +704,14 @@ struct PwPip {
       w += pip_step(last_x(P, v), last_y(P, v), P.x[nx], P.y[nx], rx, ry);
       v = nx;
     } while (v != root);
+    const int lane = threadIdx.x & 31;
     const int cy = pw_celly(g, __double2float_rd(ry));
+    int part = 0;
     auto step = [&](int u) {
       if (!internal(P, u)) return;
-      w += pip_step(b[2 * u], b[2 * u + 1], b[2 * u + 2], b[2 * u + 3], rx, ry);
+      part += pip_step(b[2 * u], b[2 * u + 1], b[2 * u + 2], b[2 * u + 3], rx, ry);
     };
-    for (int cx = 0; cx < g.gx; ++cx) {
+    for (int cx = lane; cx < g.gx; cx += 32) {
       const int cell = cy * g.gx + cx;
       for (int k = gstart[cell]; k < gstart[cell + 1]; ++k) {
         const int u = gent[k];
@@ -712,7 +719,8 @@ struct PwPip {
         step(u);
       }
     }
-    for (int k = 0; k < nlong; ++k) step(lng[k]);
+    for (int k = lane; k < nlong; k += 32) step(lng[k]);
+    w += __reduce_add_sync(kFullMask, part);
     return (w % 2) != 0;
   }
 };
@@ -767,8 +775,44 @@ __device__ __forceinline__ int pw_slot(const PwWork& w, int nr, int s, int* vtx,
   return -1;
 }
 
+// exclusive prefix sums of a[0..n) in place by the calling warp (all 32 lanes);
+// returns the total.  Element i is read and written by lane i % 32.
+__device__ int warp_excl_scan(int* a, int n) {
+  const int lane = threadIdx.x & 31;
+  int carry = 0;
+  for (int i0 = 0; i0 < n; i0 += 32) {
+    const int i = i0 + lane;
+    const int x = i < n ? a[i] : 0;
+    int s = x;
+    for (int d = 1; d < 32; d <<= 1) {
+      const int t = __shfl_up_sync(kFullMask, s, d);
+      if (lane >= d) s += t;
+    }
+    if (i < n) a[i] = carry + s - x;
+    carry += __shfl_sync(kFullMask, s, 31);
+  }
+  return carry;
+}
+
+// closes a lane-parallel step: orders its stores before the next step's
+// loads and tells every lane whether any lane failed
+__device__ __forceinline__ bool warp_fail(bool bad) {
+  __syncwarp();
+  return __any_sync(kFullMask, bad);
+}
+
+// Rows A9-A18 of one pair, run by all 32 lanes of a warp.  The serial steps
+// (the linked-list build of the base, labelling, tracing, clean-up) run on
+// every lane alike: the lanes read the same values, take the same branches
+// and store the same values, so the warp never diverges there.  The steps
+// that are independent per record, per run, per overlay edge or per slot
+// split their loops over the lanes and end with __syncwarp; where the serial
+// loop lets the last of several writes to one slot win, the lanes keep the
+// largest writer index with atomicMax and that writer stores.  Every return
+// is taken by all lanes together.
 __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork& w, int* nrings_out,
                             int* nverts_out) {
+  const int lane = threadIdx.x & 31;
   const double* b = A.b;
   const int nb = A.nb;
   const long long o = A.coff[p];
@@ -778,68 +822,80 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
   const int K = cp.K;
   // ---- A9: records arrive in the reference's order (base id, then first
   // emission), sorted for all pairs at once
-  for (int i = 0; i < K; ++i) {
+  for (int i = lane; i < K; i += 32) {
     const PwHit& h = H[i];
     w.ub[i] = 2 * h.b;
     w.uc[i] = 2 * h.j;
     w.ut[i] = h.type;
   }
+  for (int r = lane; r <= K; r += 32) w.re_nd[r] = 0;
+  for (int i = lane; i <= nc; i += 32) w.cAll[i] = w.cND[i] = w.cfill[i] = 0;
+  __syncwarp();
   const int* ub = w.ub;
   const int* uc = w.uc;
   const int* ut = w.ut;
   // ---- A10: base edges with records (runs), overlay counts
   int nr = 0, knd = 0;
-  for (int i = 0; i < K; ++i) {
-    const int e = ub[i] >> 1;
-    if (i == 0 || e != (ub[i - 1] >> 1)) {
-      w.re_e[nr] = e;
-      w.re_s[nr] = i;
-      w.re_nd[nr] = 0;
-      ++nr;
+  for (int i0 = 0; i0 < K; i0 += 32) {
+    const int i = i0 + lane;
+    const bool ok = i < K;
+    const int e = ok ? ub[i] >> 1 : 0;
+    const bool start = ok && (i == 0 || e != (ub[i - 1] >> 1));
+    const bool nd = ok && nd_b(ut[i]);
+    const unsigned sm = __ballot_sync(kFullMask, start);
+    const int ri = nr + __popc(sm & ((2u << lane) - 1u)) - 1;  // the run holding record i
+    if (start) {
+      w.re_e[ri] = e;
+      w.re_s[ri] = i;
     }
-    if (nd_b(ut[i])) {
-      w.re_nd[nr - 1]++;
-      ++knd;
+    if (nd) atomicAdd(&w.re_nd[ri], 1);
+    if (ok) {
+      const int ec = uc[i] >> 1;
+      atomicAdd(&w.cAll[ec], 1);
+      if (nd_c(ut[i])) atomicAdd(&w.cND[ec], 1);
     }
+    nr += __popc(sm);
+    knd += __popc(__ballot_sync(kFullMask, nd));
   }
   w.re_s[nr] = K;
-  {
-    int s = 0;
-    for (int r = 0; r < nr; ++r) {
-      w.re_pre[r] = s;
-      w.re_si[r] = r + s;
-      s += w.re_nd[r];
-    }
-    w.re_pre[nr] = s;
-    w.re_si[nr] = nr + s;
-  }
-  for (int i = 0; i <= nc; ++i) w.cAll[i] = w.cND[i] = w.cfill[i] = 0;
-  for (int i = 0; i < K; ++i) {
+  __syncwarp();
+  for (int r = lane; r <= nr; r += 32) w.re_pre[r] = w.re_nd[r];  // re_nd[nr] is 0
+  warp_excl_scan(w.re_pre, nr + 1);
+  for (int r = lane; r <= nr; r += 32) w.re_si[r] = r + w.re_pre[r];
+  warp_excl_scan(w.cAll, nc + 1);
+  warp_excl_scan(w.cND, nc + 1);
+  __syncwarp();
+  // records of each overlay edge, in record order
+  for (int i = lane; i < K; i += 32) {
     const int ec = uc[i] >> 1;
-    w.cAll[ec]++;
-    if (nd_c(ut[i])) w.cND[ec]++;
+    w.csorted[w.cAll[ec] + atomicAdd(&w.cfill[ec], 1)] = i;
   }
-  auto excl = [](int* a, int n) {
-    int s = 0;
-    for (int i = 0; i < n; ++i) {
-      const int x = a[i];
-      a[i] = s;
-      s += x;
+  __syncwarp();
+  for (int e = lane; e < nc; e += 32) {
+    const int s = w.cAll[e], t = w.cAll[e + 1];
+    if (t - s < 2) continue;
+    int* v = w.csorted + s;
+    if (t - s > 32) {
+      merge_sort(v, w.htmp + s, t - s, [](int x, int y) { return x < y; });
+      continue;
     }
-  };
-  excl(w.cAll, nc + 1);
-  excl(w.cND, nc + 1);
-  for (int i = 0; i < K; ++i) {
-    const int ec = uc[i] >> 1;
-    w.csorted[w.cAll[ec] + w.cfill[ec]++] = i;
+    for (int i = 1; i < t - s; ++i) {
+      const int x = v[i];
+      int j = i;
+      while (j > 0 && v[j - 1] > x) {
+        v[j] = v[j - 1];
+        --j;
+      }
+      v[j] = x;
+    }
   }
   const int nB = nb + knd, nQ = nc + w.cND[nc];
   // ---- A11 records
-  for (int i = 0; i < K; ++i) {
+  for (int i = lane; i < K; i += 32) {
     const int bi = ub[i] >> 1, ci = uc[i] >> 1;
     const int bi2 = bi + 1 == nb ? 0 : bi + 1, ci2 = ci + 1 == nc ? 0 : ci + 1;
     const double p1x = b[2 * bi], p1y = b[2 * bi + 1], p2x = b[2 * bi2], p2y = b[2 * bi2 + 1];
-    const double q1x = c[2 * ci], q1y = c[2 * ci + 1], q2x = c[2 * ci2], q2y = c[2 * ci2 + 1];
+    const double q1x = c[2 * ci], q1y = c[2 * ci + 1];
     const double al = H[i].al, bt = H[i].bt;  // lineSegmentIntersection of the candidate test
     const int ty = ut[i];
     double x = 0.0, y = 0.0;
@@ -858,8 +914,11 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
     w.isxy[2 * i + 1] = y;
     w.aB[i] = ty ? alpha_to_int(al) : 0;
     w.aC[i] = ty ? alpha_to_int(bt) : 0;
+    w.sB[i] = w.sC[i] = i;
   }
-  // ---- A12 per-edge alpha order (stable by alpha mod 1e9)
+  __syncwarp();
+  // ---- A12 per-edge alpha order (stable by alpha mod 1e9), one run or one
+  // overlay edge per lane
   // (stable insertion for short runs; a long run -- an overlay edge across a
   // jagged base can hold hundreds of crossings -- takes the stable merge sort)
   auto isort = [&](int s, int t, const int* alpha, const int* order, int* sorted) -> bool {
@@ -885,47 +944,43 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
     }
     return true;
   };
-  for (int i = 0; i < K; ++i) w.sB[i] = w.sC[i] = i;
-  for (int r = 0; r < nr; ++r)
-    if (w.re_nd[r] > 1 && !isort(w.re_s[r], w.re_s[r + 1], w.aB, nullptr, w.sB)) return PS_FALLBACK;
-  for (int e = 0; e < nc; ++e)
+  bool bad = false;
+  for (int r = lane; r < nr; r += 32)
+    if (w.re_nd[r] > 1 && !isort(w.re_s[r], w.re_s[r + 1], w.aB, nullptr, w.sB)) bad = true;
+  __syncwarp();  // both sorts use htmp
+  for (int e = lane; e < nc; e += 32)
     if (w.cND[e + 1] - w.cND[e] > 1 && !isort(w.cAll[e], w.cAll[e + 1], w.aC, w.csorted, w.sC))
-      return PS_FALLBACK;
-  // ---- A13 merged arrays: the base's where it has records, the overlay's in full
-  for (int r = 0; r < nr; ++r) {
-    const int si = w.re_si[r], e = w.re_e[r];
+      bad = true;
+  if (warp_fail(bad)) return PS_FALLBACK;
+  // ---- A13 merged arrays: the base's where it has records, the overlay's in
+  // full.  A run (overlay edge) writes only its own slots and the neighbour
+  // indices of its own records, so runs (edges) go one per lane.
+  for (int i = lane; i < nQ; i += 32) {
+    w.ixC[2 * i] = w.ixC[2 * i + 1] = 0.0;
+    w.alC[i] = w.nbC[i] = 0;
+    w.nbCsi[i] = -1;
+    w.cWin[i] = -1;
+  }
+  for (int i = lane; i < K; i += 32) {
+    w.bNI[i] = w.cNI[i] = 0;
+    w.bSI[i] = -1;  // the sparse index of bNI[i] once a slot is written
+  }
+  __syncwarp();
+  // base runs (copyIntersectionsParallel per edge)
+  for (int r = lane; r < nr; r += 32) {
+    const int e = w.re_e[r], s = w.re_s[r], pre = w.re_pre[r], si = w.re_si[r];
     w.spx[si] = b[2 * e];
     w.spy[si] = b[2 * e + 1];
     w.spal[si] = -100;
     w.spnb[si] = -100;
+    w.splab[si] = 0;
+    w.spnode[si] = -1;
     for (int q = 1; q <= w.re_nd[r]; ++q) {
       w.spx[si + q] = w.spy[si + q] = 0.0;
       w.spal[si + q] = w.spnb[si + q] = 0;
+      w.splab[si + q] = 0;
+      w.spnode[si + q] = -1;
     }
-  }
-  for (int s = 0; s < w.re_si[nr]; ++s) {
-    w.splab[s] = 0;
-    w.spnode[s] = -1;
-  }
-  for (int i = 0; i < nQ; ++i) {
-    w.ixC[2 * i] = w.ixC[2 * i + 1] = 0.0;
-    w.alC[i] = w.nbC[i] = 0;
-    w.nbCsi[i] = -1;
-  }
-  for (int id = 0; id < nc; ++id) {
-    const int s = id + w.cND[id];
-    w.ixC[2 * s] = c[2 * id];
-    w.ixC[2 * s + 1] = c[2 * id + 1];
-    w.alC[s] = -100;
-    w.nbC[s] = -100;
-  }
-  for (int i = 0; i < K; ++i) {
-    w.bNI[i] = w.cNI[i] = 0;
-    w.bSI[i] = -1;  // the sparse index of bNI[i] once a slot is written
-  }
-  // base runs (copyIntersectionsParallel per edge)
-  for (int r = 0; r < nr; ++r) {
-    const int e = w.re_e[r], s = w.re_s[r], pre = w.re_pre[r], si = w.re_si[r];
     int bid = s;
     int lid = w.sB[bid];
     const int t = ut[lid];
@@ -945,8 +1000,13 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
       if (bid < K - 1) lid = w.sB[++bid];
     }
   }
-  // overlay edges
-  for (int e = 0; e < nc; ++e) {
+  // overlay edges: the vertex slot, then the edge's intersection slots
+  for (int e = lane; e < nc; e += 32) {
+    const int vs = e + w.cND[e];
+    w.ixC[2 * vs] = c[2 * e];
+    w.ixC[2 * vs + 1] = c[2 * e + 1];
+    w.alC[vs] = -100;
+    w.nbC[vs] = -100;
     const int s = w.cAll[e];
     if (w.cAll[e + 1] == s) continue;
     auto entry = [&](int pos) { return w.csorted[w.sC[pos]]; };
@@ -954,9 +1014,8 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
     int lid = entry(bid);
     const int t = ut[lid];
     if (t == 3 || t == 4 || t == 5 || t == 7 || t == 8) {
-      const int slot = e + w.cND[e];
-      w.alC[slot] = w.aC[lid];
-      w.cNI[lid] = slot;
+      w.alC[vs] = w.aC[lid];
+      w.cNI[lid] = vs;
       if (bid < K - 1) lid = entry(++bid);
     }
     if ((uc[lid] >> 1) != e) continue;
@@ -970,22 +1029,38 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
       if (bid < K - 1) lid = entry(++bid);
     }
   }
-  // neighbours: the last record written to a slot wins
-  int si0 = -3;  // sparse index of slot 0, where records never written point
-  for (int i = 0; i < K; ++i) {
-    int si = w.bSI[i];
-    if (si < 0) {
-      if (si0 == -3) {
-        int vtx;
-        si0 = pw_slot(w, nr, 0, &vtx);
-      }
-      si = si0;
-    }
-    if (si < 0) return PS_FALLBACK;  // a plain slot would change
-    w.spnb[si] = w.cNI[i] + 1;
-    w.nbC[w.cNI[i]] = w.bNI[i] + 1;
-    w.nbCsi[w.cNI[i]] = si;
+  __syncwarp();
+  // neighbours: the last record written to a slot wins (spnode and cWin hold
+  // the winning record until the winners have stored)
+  int si0;  // sparse index of slot 0, where records never written point
+  {
+    int vtx;
+    si0 = pw_slot(w, nr, 0, &vtx);
   }
+  for (int i = lane; i < K; i += 32) {
+    const int si = w.bSI[i] < 0 ? si0 : w.bSI[i];
+    if (si < 0) {
+      bad = true;  // a plain slot would change
+      continue;
+    }
+    atomicMax(&w.spnode[si], i);
+    atomicMax(&w.cWin[w.cNI[i]], i);
+  }
+  if (warp_fail(bad)) return PS_FALLBACK;
+  for (int i = lane; i < K; i += 32) {
+    const int si = w.bSI[i] < 0 ? si0 : w.bSI[i];
+    const int cq = w.cNI[i];
+    if (w.spnode[si] == i) w.spnb[si] = cq + 1;
+    if (w.cWin[cq] == i) {
+      w.nbC[cq] = w.bNI[i] + 1;
+      w.nbCsi[cq] = si;
+    }
+  }
+  __syncwarp();
+  const int nsp = w.re_si[nr];
+  for (int s = lane; s < nsp; s += 32) w.spnode[s] = -1;
+  for (int q = lane; q < nQ; q += 32) w.cWin[q] = -1;
+  __syncwarp();
   // slot contents of the base's merged list
   auto info = [&](int s, int hint, double* x, double* y, int* al, int* nbv) {
     int vtx = 0;
@@ -1002,9 +1077,9 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
       *nbv = -100;
     }
   };
-  // ---- A14 initial labels
-  for (int q = 0; q < nQ; ++q) w.cWin[q] = -1;
-  for (int r = 0; r < nr; ++r) {
+  // ---- A14 initial labels, one run per lane; the overlay slot takes the
+  // label of the last base slot naming it
+  for (int r = lane; r < nr && !bad; r += 32) {
     for (int q = 0; q <= w.re_nd[r]; ++q) {
       const int si = w.re_si[r] + q;
       if (w.spal[si] == -100) continue;
@@ -1020,11 +1095,14 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
       const int pPN = alp != -100 ? nbp - 1 : -100;
       const int nId = w.spnb[si] - 1;
       int qt[2];
-      for (int sd = 0; sd < 2; ++sd) {
+      for (int sd = 0; sd < 2 && !bad; ++sd) {
         int qq = sd == 0 ? nId - 1 : nId + 1;
         if (qq == nQ) qq = 0;
         else if (qq == -1) qq = nQ - 1;
-        if (qq < 0 || qq >= nQ) return PS_FALLBACK;
+        if (qq < 0 || qq >= nQ) {
+          bad = true;
+          break;
+        }
         const double qx = w.ixC[2 * qq], qy = w.ixC[2 * qq + 1];
         int rr;
         if (pMN != -100 && pMN == qq) rr = 2;
@@ -1038,6 +1116,7 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
         }
         qt[sd] = rr;
       }
+      if (bad) break;
       const int qm = qt[0], qp = qt[1];
       int lab;
       if ((qm == 0 && qp == 1) || (qm == 1 && qp == 0)) lab = 1;
@@ -1049,19 +1128,27 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
       else if ((qm == 2 && qp == 0) || (qp == 2 && qm == 0)) lab = 7;
       else lab = -102;
       w.splab[si] = lab;
-      if (nId < 0 || nId >= nQ) return PS_FALLBACK;
-      if (i >= w.cWin[nId]) {  // slots come in increasing order: the last one wins
-        w.cWin[nId] = i;
-        w.cWinSI[nId] = si;
+      if (nId < 0 || nId >= nQ) {
+        bad = true;
+        break;
       }
+      atomicMax(&w.cWin[nId], i);  // slots come in increasing order: the last one wins
     }
   }
-  for (int q = 0; q < nQ; ++q) {
-    w.labC[q] = 0;
-    if (w.cWin[q] >= 0) w.labC[q] = w.splab[w.cWinSI[q]];
+  if (warp_fail(bad)) return PS_FALLBACK;
+  for (int r = lane; r < nr; r += 32) {
+    for (int q = 0; q <= w.re_nd[r]; ++q) {
+      const int si = w.re_si[r] + q;
+      if (w.spal[si] == -100) continue;
+      const int nId = w.spnb[si] - 1;
+      if (w.cWin[nId] == w.re_e[r] + w.re_pre[r] + q) w.cWinSI[nId] = si;
+    }
   }
+  __syncwarp();
+  for (int q = lane; q < nQ; q += 32) w.labC[q] = w.cWin[q] >= 0 ? w.splab[w.cWinSI[q]] : 0;
+  __syncwarp();
   // ---- A15 linked lists (copyToLinkedList, src/clip.cpp:606-695): the base's
-  // with run nodes for its stretches of plain vertices
+  // with run nodes for its stretches of plain vertices (serial, on every lane)
   Pool& P = w.P;
   Pool& Q = w.Q;
   P.n = Q.n = w.R.n = 0;
@@ -1143,11 +1230,62 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
     }
     if (vn != nB) return PS_UNDEF;
   }
-  for (int v = 0; v < P.n; ++v) {
-    P.next[v] = (v + 1) % P.n;
-    P.prev[v] = (v + P.n - 1) % P.n;
+  __syncwarp();
+  for (int v = lane; v < P.n; v += 32) {
+    P.next[v] = v + 1 == P.n ? 0 : v + 1;
+    P.prev[v] = v == 0 ? P.n - 1 : v - 1;
   }
-  {
+  // The overlay's list is its merged array in order (node i is slot i) unless
+  // a slot's coordinates stop the reference's walk early: an overlay vertex
+  // whose slot does not hold its own coordinates (NaN), or an intersection
+  // slot of edge e that repeats vertex e + 1.  The walk then takes the serial
+  // path below, which follows the reference in every case.
+  bool odd = false;
+  for (int e = lane; e < nc && !odd; e += 32) {
+    const int vs = e + w.cND[e], ne = w.cND[e + 1] - w.cND[e];
+    const int nx = e + 1 == nc ? 0 : e + 1;
+    const double vx = c[2 * nx], vy = c[2 * nx + 1];
+    if (!(w.ixC[2 * vs] == c[2 * e] && w.ixC[2 * vs + 1] == c[2 * e + 1])) odd = true;
+    for (int q = 1; q <= ne; ++q)
+      if (w.ixC[2 * (vs + q)] == vx && w.ixC[2 * (vs + q) + 1] == vy) odd = true;
+  }
+  if (!__any_sync(kFullMask, odd)) {
+    // node v = slot v; the first failing slot decides the status
+    int first = INT_MAX;  // 4 * slot + 1 (undefined) or + 2 (pair pipeline)
+    for (int e = lane; e < nc; e += 32) {
+      const int vs = e + w.cND[e], ne = w.cND[e + 1] - w.cND[e];
+      for (int q = 0; q <= ne; ++q) {
+        const int v = vs + q;
+        Q.x[v] = w.ixC[2 * v];
+        Q.y[v] = w.ixC[2 * v + 1];
+        Q.nb[v] = -1;
+        Q.label[v] = w.labC[v];
+        Q.enex[v] = EX_NEITHER;
+        Q.source[v] = q == 0;
+        Q.isect[v] = 0;
+        Q.next[v] = v + 1 == nQ ? 0 : v + 1;
+        Q.prev[v] = v == 0 ? nQ - 1 : v - 1;
+        if (q == 0 && w.nbC[v] == -100) continue;  // a plain overlay vertex
+        const int t = w.nbC[v] - 1;
+        if (t < 0 || t >= nB) {
+          first = min(first, 4 * v + 1);
+          continue;
+        }
+        const int si = w.nbCsi[v];
+        if (si < 0 || w.spnode[si] < 0) {
+          first = min(first, 4 * v + 2);
+          continue;
+        }
+        Q.isect[v] = 1;
+        Q.nb[v] = w.spnode[si];
+        atomicMax(&P.nb[w.spnode[si]], v);  // the last overlay node naming it wins
+      }
+    }
+    first = __reduce_min_sync(kFullMask, first);
+    __syncwarp();
+    if (first != INT_MAX) return (first & 3) == 1 ? PS_UNDEF : PS_FALLBACK;
+    Q.n = nQ;
+  } else {
     int i = 0;
     for (int ii = 0; ii <= nc; ++ii) {
       const int sv = ii < nc ? ii : 0;
@@ -1189,7 +1327,11 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
       Q.prev[v] = (v + nQ - 1) % nQ;
     }
   }
-  // ---- A16-A18
+  for (int i = lane; i < cp.capP; i += 32) w.splitP[i] = w.crossP[i] = 0;
+  for (int i = lane; i < cp.capQ; i += 32) w.splitQ[i] = w.crossQ[i] = 0;
+  __syncwarp();
+  // ---- A16-A18 (serial, on every lane; pointInPoly against the base splits
+  // its grid row over the lanes)
   SerialArgs a;
   a.P = P;
   a.Q = Q;
@@ -1202,8 +1344,6 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
   a.splitQ = w.splitQ;
   a.crossP = w.crossP;
   a.crossQ = w.crossQ;
-  for (int i = 0; i < cp.capP; ++i) w.splitP[i] = w.crossP[i] = 0;
-  for (int i = 0; i < cp.capQ; ++i) w.splitQ[i] = w.crossQ[i] = 0;
   a.bSize = nb;
   a.cSize = nc;
   a.cStart = 0;
@@ -1259,15 +1399,17 @@ __global__ void k_pw_sizes(int nov, const long long* __restrict__ coff, int nb,
   bytes[p] = run ? (long long)pw_arena_bytes(nb, (int)(coff[p + 1] - coff[p]), pairK[p], pass) : 0;
 }
 
-// Persistent work queue, one pair per warp at a time run by the warp's first
-// lane (the back end is serial; 32 pairs sharing a warp would take turns
-// through diverging paths).  The queue hands out pairs by decreasing expected
-// work; a warp takes the next one until the queue is empty.
+// Persistent work queue, one pair per warp at a time (32 pairs sharing a warp
+// would take turns through diverging paths; one warp shares a pair's
+// data-parallel steps among its lanes instead).  The queue hands out pairs by
+// decreasing expected work; a warp takes the next one until the queue is
+// empty.
 __global__ void __launch_bounds__(kPwPairBlock)
 k_pw_pairs(PwPairArgs A, const int* __restrict__ pairK, int* __restrict__ queue) {
-  if ((threadIdx.x & 31) != 0) return;
   for (;;) {
-    const int wi = atomicAdd(queue, 1);
+    int wi = 0;
+    if ((threadIdx.x & 31) == 0) wi = atomicAdd(queue, 1);
+    wi = __shfl_sync(kFullMask, wi, 0);
     if (wi >= A.nov) return;
     const int p = A.order[wi];
     const int pass = A.pass_of ? A.pass_of[p] : 0;
