@@ -13,6 +13,7 @@
 //   merged       ring slot arrays ixB / ixC (x,y), alpha, neighbour, label
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -210,8 +211,8 @@ void radix_sort_u32(unsigned* keys, unsigned* vals, unsigned* keys_tmp, unsigned
 void radix_sort_u64(unsigned long long* keys, unsigned* vals, unsigned long long* keys_tmp,
                     unsigned* vals_tmp, long long n, void* scratch, cudaStream_t st);
 
-// number of this library's kernels launched by the process
-extern unsigned long long g_launches;
+// number of this library's kernels launched by the process (any host thread)
+extern std::atomic<unsigned long long> g_launches;
 
 // Scoped launch probe: counts the launch and, while profiling is on, brackets
 // it with a pair of CUDA events on its stream (per-kernel device time).

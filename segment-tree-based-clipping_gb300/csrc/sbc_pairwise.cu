@@ -45,6 +45,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "../../include/sbclip.h"
@@ -574,6 +575,7 @@ __host__ __device__ __forceinline__ PwCaps pw_caps(int nb, int nc, int K, int pa
 
 struct PwWork {
   int *hord, *htmp, *ub, *uc, *ut;
+  unsigned long long* sscr;  // warp sorts of long runs: 2K (key, position) pairs
   int *re_e, *re_s, *re_nd, *re_pre, *re_si;
   int *cAll, *cND, *cfill, *csorted;
   double* isxy;
@@ -614,6 +616,7 @@ __host__ __device__ __forceinline__ PwWork pw_carve(Carver& cv, const PwCaps& c)
   const int K = c.K;
   w.hord = cv.take<int>(K);
   w.htmp = cv.take<int>(K);
+  w.sscr = cv.take<unsigned long long>(2 * K + 2);
   w.ub = cv.take<int>(K);
   w.uc = cv.take<int>(K);
   w.ut = cv.take<int>(K);
@@ -801,6 +804,52 @@ __device__ __forceinline__ bool warp_fail(bool bad) {
   return __any_sync(kFullMask, bad);
 }
 
+constexpr int kWarpSortMin = 32;  // runs longer than this are sorted by the whole warp
+
+// sorts scr[0..n) -- distinct 64-bit values, key(m) for m < n -- ascending,
+// by the whole warp: a bitonic network over the next power of two (padding
+// sorts last)
+template <class Key>
+__device__ void warp_bitonic(int n, unsigned long long* scr, Key key) {
+  const int lane = threadIdx.x & 31;
+  const int np = npow2_dev(n);
+  for (int m = lane; m < np; m += 32) scr[m] = m < n ? key(m) : ~0ull;
+  __syncwarp();
+  for (int k = 2; k <= np; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int m = lane; m < np; m += 32) {
+        const int l = m ^ j;
+        if (l > m) {
+          const unsigned long long x = scr[m], y = scr[l];
+          if ((x > y) == ((m & k) == 0)) {
+            scr[m] = y;
+            scr[l] = x;
+          }
+        }
+      }
+      __syncwarp();
+    }
+}
+
+// stable order of sorted[s..t) (holding s..t) by alpha mod 1e9, by the whole
+// warp: ties keep position order because the position is the key's low half.
+// False (on every lane) when an alpha is negative.
+__device__ bool warp_alpha_sort(int s, int t, const int* alpha, const int* order, int* sorted,
+                                unsigned long long* scr) {
+  const int lane = threadIdx.x & 31;
+  bool neg = false;
+  for (int x = s + lane; x < t; x += 32)
+    if (alpha[order ? order[x] : x] < 0) neg = true;
+  if (warp_fail(neg)) return false;
+  warp_bitonic(t - s, scr, [&](int m) {
+    const int x = s + m;
+    return ((unsigned long long)(alpha[order ? order[x] : x] % 1000000000) << 32) | (unsigned)x;
+  });
+  for (int m = lane; m < t - s; m += 32) sorted[s + m] = (int)(unsigned)scr[m];
+  __syncwarp();
+  return true;
+}
+
 // Rows A9-A18 of one pair, run by all 32 lanes of a warp.  The serial steps
 // (the linked-list build of the base, labelling, tracing, clean-up) run on
 // every lane alike: the lanes read the same values, take the same branches
@@ -871,22 +920,27 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
     w.csorted[w.cAll[ec] + atomicAdd(&w.cfill[ec], 1)] = i;
   }
   __syncwarp();
-  for (int e = lane; e < nc; e += 32) {
-    const int s = w.cAll[e], t = w.cAll[e + 1];
-    if (t - s < 2) continue;
-    int* v = w.csorted + s;
-    if (t - s > 32) {
-      merge_sort(v, w.htmp + s, t - s, [](int x, int y) { return x < y; });
-      continue;
-    }
-    for (int i = 1; i < t - s; ++i) {
-      const int x = v[i];
-      int j = i;
-      while (j > 0 && v[j - 1] > x) {
-        v[j] = v[j - 1];
-        --j;
+  for (int e0 = 0; e0 < nc; e0 += 32) {
+    const int e = e0 + lane;
+    const int s = e < nc ? w.cAll[e] : 0, t = e < nc ? w.cAll[e + 1] : 0;
+    if (t - s > 1 && t - s <= kWarpSortMin) {
+      int* v = w.csorted + s;
+      for (int i = 1; i < t - s; ++i) {
+        const int x = v[i];
+        int j = i;
+        while (j > 0 && v[j - 1] > x) {
+          v[j] = v[j - 1];
+          --j;
+        }
+        v[j] = x;
       }
-      v[j] = x;
+    }
+    for (unsigned m = __ballot_sync(kFullMask, t - s > kWarpSortMin); m; m &= m - 1) {
+      const int ee = e0 + __ffs(m) - 1;
+      const int s2 = w.cAll[ee], t2 = w.cAll[ee + 1];
+      warp_bitonic(t2 - s2, w.sscr, [&](int k) { return (unsigned long long)w.csorted[s2 + k]; });
+      for (int k = lane; k < t2 - s2; k += 32) w.csorted[s2 + k] = (int)w.sscr[k];
+      __syncwarp();
     }
   }
   const int nB = nb + knd, nQ = nc + w.cND[nc];
@@ -919,17 +973,12 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
   __syncwarp();
   // ---- A12 per-edge alpha order (stable by alpha mod 1e9), one run or one
   // overlay edge per lane
-  // (stable insertion for short runs; a long run -- an overlay edge across a
-  // jagged base can hold hundreds of crossings -- takes the stable merge sort)
+  // (stable insertion for short runs on one lane; a long run -- an overlay
+  // edge across a jagged base can hold hundreds of crossings -- is sorted by
+  // the whole warp)
   auto isort = [&](int s, int t, const int* alpha, const int* order, int* sorted) -> bool {
     for (int i = s; i < t; ++i)
       if (alpha[order ? order[i] : i] < 0) return false;
-    if (t - s > 32) {
-      merge_sort(sorted + s, w.htmp + s, t - s, [&](int x, int y) {
-        return alpha[order ? order[x] : x] % 1000000000 < alpha[order ? order[y] : y] % 1000000000;
-      });
-      return true;
-    }
     for (int i = s + 1; i < t; ++i) {
       const int pv = sorted[i];
       const int kp = alpha[order ? order[pv] : pv] % 1000000000;
@@ -945,12 +994,30 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
     return true;
   };
   bool bad = false;
-  for (int r = lane; r < nr; r += 32)
-    if (w.re_nd[r] > 1 && !isort(w.re_s[r], w.re_s[r + 1], w.aB, nullptr, w.sB)) bad = true;
-  __syncwarp();  // both sorts use htmp
-  for (int e = lane; e < nc; e += 32)
-    if (w.cND[e + 1] - w.cND[e] > 1 && !isort(w.cAll[e], w.cAll[e + 1], w.aC, w.csorted, w.sC))
-      bad = true;
+  for (int r0 = 0; r0 < nr; r0 += 32) {
+    const int r = r0 + lane;
+    bool lng = false;
+    if (r < nr && w.re_nd[r] > 1) {
+      if (w.re_s[r + 1] - w.re_s[r] > kWarpSortMin) lng = true;
+      else if (!isort(w.re_s[r], w.re_s[r + 1], w.aB, nullptr, w.sB)) bad = true;
+    }
+    for (unsigned m = __ballot_sync(kFullMask, lng); m; m &= m - 1) {
+      const int rr = r0 + __ffs(m) - 1;
+      if (!warp_alpha_sort(w.re_s[rr], w.re_s[rr + 1], w.aB, nullptr, w.sB, w.sscr)) bad = true;
+    }
+  }
+  for (int e0 = 0; e0 < nc; e0 += 32) {
+    const int e = e0 + lane;
+    bool lng = false;
+    if (e < nc && w.cND[e + 1] - w.cND[e] > 1) {
+      if (w.cAll[e + 1] - w.cAll[e] > kWarpSortMin) lng = true;
+      else if (!isort(w.cAll[e], w.cAll[e + 1], w.aC, w.csorted, w.sC)) bad = true;
+    }
+    for (unsigned m = __ballot_sync(kFullMask, lng); m; m &= m - 1) {
+      const int ee = e0 + __ffs(m) - 1;
+      if (!warp_alpha_sort(w.cAll[ee], w.cAll[ee + 1], w.aC, w.csorted, w.sC, w.sscr)) bad = true;
+    }
+  }
   if (warp_fail(bad)) return PS_FALLBACK;
   // ---- A13 merged arrays: the base's where it has records, the overlay's in
   // full.  A run (overlay edge) writes only its own slots and the neighbour
@@ -1464,14 +1531,31 @@ __global__ void k_pw_pack(int nov, const long long* __restrict__ coff, int nb,
 
 // ------------------------------------------------------------------ host
 // resident warps of the per-pair kernel (the whole GPU), at most one per pair
-unsigned PairwiseRunner::pair_grid(int nov) {
-  if (pair_blocks_ == 0) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pw_pairs, kPwPairBlock, 0);
-    pair_blocks_ = (unsigned)std::max(1, sms * std::max(1, per_sm));
+// one pipeline, stream and host thread taking big pairs
+struct PairwiseRunner::BigWorker {
+  cudaStream_t st = nullptr;
+  std::unique_ptr<Pipeline> pl;
+  int rc = 0;
+  std::string msg;
+  ~BigWorker() {
+    if (!st) return;
+    cudaStreamSynchronize(st);
+    pl.reset();
+    cudaStreamDestroy(st);
   }
+};
+
+// persistent grid of the per-pair kernel: every block slot of every SM, less
+// `pair_reserve` slots per SM while big pairs run beside it (their pipeline
+// kernels need room on the SMs)
+unsigned PairwiseRunner::pair_grid(int nov, bool reserve) {
+  static_assert(kPwPairBlock % 32 == 0, "whole warps");
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pw_pairs, kPwPairBlock, 0);
+  const int slots = std::max(1, reserve ? per_sm - pair_reserve : per_sm);
+  pair_blocks_ = (unsigned)std::max(1, sms * slots);
   const unsigned need = grid_for(32LL * nov, kPwPairBlock);
   return need < pair_blocks_ ? need : pair_blocks_;
 }
@@ -1502,6 +1586,18 @@ int PairwiseRunner::autotune(const double* d_bxy, int nb, int nov, const double*
     }
   }
   big_k = best_split;
+  int best_reserve = pair_reserve;
+  for (int r : {0, 1, 2}) {
+    if (r == best_reserve) continue;
+    pair_reserve = r;
+    rc = timed(&ms);
+    if (rc) return rc;
+    if (ms < best) {
+      best = ms;
+      best_reserve = r;
+    }
+  }
+  pair_reserve = best_reserve;
   for (double f : {0.5, 2.0}) {
     cell_factor = f;
     rc = timed(&ms);
@@ -1515,6 +1611,8 @@ int PairwiseRunner::autotune(const double* d_bxy, int nb, int nov, const double*
   if (best_ms) *best_ms = best;
   return kOk;
 }
+
+PairwiseRunner::PairwiseRunner(Pipeline& pl) : pl_(pl) {}
 
 PairwiseRunner::~PairwiseRunner() {
   if (st2_) {
@@ -1771,10 +1869,6 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
   cudaMemcpyAsync(&total, aoff0 + nov, sizeof(long long), cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise sizes");
   unsigned char* arena0 = (unsigned char*)pool.get("pw_arena0", (size_t)total + 256);
-  int* brb = (int*)pool.get("pw_big_rb", sizeof(int) * (maxBig + 1));
-  int* brc = (int*)pool.get("pw_big_rc", sizeof(int) * (maxBig + 1));
-  int* brt = (int*)pool.get("pw_big_rt", sizeof(int) * (maxBig + 1));
-  auto* bkey = (unsigned long long*)pool.get("pw_big_key", sizeof(unsigned long long) * (maxBig + 1));
   if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise arena)");
   if (!st2_ && cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking) != cudaSuccess)
     return pl_.fail(kECuda, "pairwise stream");
@@ -1788,7 +1882,7 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
   {
     // coordinates and records in; rings out
     ::sbc::KProbe kp_("k_pw_pairs", st2_, 16.0 * totalC + 40.0 * (double)nh);
-    k_pw_pairs<<<pair_grid(nov), kPwPairBlock, 0, st2_>>>(pa, pairK, queue);
+    k_pw_pairs<<<pair_grid(nov, big_pairs > 0), kPwPairBlock, 0, st2_>>>(pa, pairK, queue);
   }
   cudaEventRecord(ev_[1], st2_);
   struct Stash {
@@ -1814,23 +1908,96 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
     stash_of[p] = p;
     return kOk;
   };
-  for (int p = 0; p < nov; ++p) {
-    if (!is_big[p]) continue;
-    const int K = hK[p];
-    {
-      ::sbc::KProbe kp_("k_pw_split", st, 72.0 * K);
-      k_pw_split<<<grid_for(K, 256), 256, 0, st>>>(K, grouped + hstart_h[p], brb, brc, brt, bkey);
+  // big pairs: worker host threads, each with its own pipeline and stream,
+  // take them one at a time (a pair's pipeline waits on the host between its
+  // stages; several pairs in flight keep the GPU busy meanwhile)
+  std::vector<int> bigs;
+  for (int p = 0; p < nov; ++p)
+    if (is_big[p]) bigs.push_back(p);
+  if (!bigs.empty()) {
+    const int nw = std::max(1, std::min<int>(big_workers, (int)bigs.size()));
+    int dev = 0;
+    cudaGetDevice(&dev);
+    while ((int)workers_.size() < nw) {
+      auto wk = std::make_unique<BigWorker>();
+      if (cudaStreamCreateWithFlags(&wk->st, cudaStreamNonBlocking) != cudaSuccess)
+        return pl_.fail(kECuda, "pairwise worker stream");
+      wk->pl = std::make_unique<Pipeline>(dev, wk->st);
+      workers_.push_back(std::move(wk));
     }
-    pl_.clear_error();
-    const int rc = pl_.run_from_hits(d_bxy, nb, d_cxy + 2 * hoff[p], (int)(hoff[p + 1] - hoff[p]),
-                                     brb, brc, brt, bkey, K);
-    if (rc == kEInput || rc == kEUndef) {
-      h_status[p] = rc == kEInput ? SBC_EINPUT : SBC_EUNDEF;
-      continue;
-    }
-    if (rc) return rc;
-    const int k2 = keep(p);
-    if (k2) return k2;
+    std::atomic<int> next{0};
+    std::atomic<bool> stop{false};
+    auto work = [&](BigWorker& W) {
+      cudaSetDevice(dev);
+      Pipeline& wp = *W.pl;
+      wp.unite = pl_.unite;
+      wp.force_serial_backend = pl_.force_serial_backend;
+      W.rc = 0;
+      W.msg.clear();
+      BufferPool& wpool = wp.pool();
+      int* brb = (int*)wpool.get("pw_big_rb", sizeof(int) * (maxBig + 1));
+      int* brc = (int*)wpool.get("pw_big_rc", sizeof(int) * (maxBig + 1));
+      int* brt = (int*)wpool.get("pw_big_rt", sizeof(int) * (maxBig + 1));
+      auto* bkey =
+          (unsigned long long*)wpool.get("pw_big_key", sizeof(unsigned long long) * (maxBig + 1));
+      if (wpool.failed) {
+        W.rc = kENoMem;
+        W.msg = "device allocation failed (pairwise big pairs)";
+        stop = true;
+        return;
+      }
+      cudaStreamWaitEvent(W.st, ev_[0], 0);  // the grouped records
+      for (;;) {
+        const int i = stop ? (int)bigs.size() : next++;
+        if (i >= (int)bigs.size()) break;
+        const int p = bigs[i];
+        const int K = hK[p];
+        {
+          ::sbc::KProbe kp_("k_pw_split", W.st, 72.0 * K);
+          k_pw_split<<<grid_for(K, 256), 256, 0, W.st>>>(K, grouped + hstart_h[p], brb, brc, brt,
+                                                         bkey);
+        }
+        wp.clear_error();
+        const int rc = wp.run_from_hits(d_bxy, nb, d_cxy + 2 * hoff[p],
+                                        (int)(hoff[p + 1] - hoff[p]), brb, brc, brt, bkey, K);
+        if (rc == kEInput || rc == kEUndef) {
+          h_status[p] = rc == kEInput ? SBC_EINPUT : SBC_EUNDEF;
+          continue;
+        }
+        if (rc) {
+          W.rc = rc;
+          W.msg = wp.error();
+          stop = true;
+          break;
+        }
+        const auto& out = wp.outputs()[0];
+        Stash& sh = stash[p];
+        sh.off.assign(out.nrings + 1, 0);
+        sh.xy.resize(2 * out.nverts);
+        if (out.nrings > 0)
+          cudaMemcpyAsync(sh.off.data(), out.d_off, sizeof(int) * (out.nrings + 1),
+                          cudaMemcpyDeviceToHost, W.st);
+        if (out.nverts > 0)
+          cudaMemcpyAsync(sh.xy.data(), out.d_xy, sizeof(double) * 2 * out.nverts,
+                          cudaMemcpyDeviceToHost, W.st);
+        if (cudaStreamSynchronize(W.st) != cudaSuccess) {
+          W.rc = kECuda;
+          W.msg = "pairwise pipeline";
+          stop = true;
+          break;
+        }
+        hnr[p] = out.nrings;
+        hnv[p] = (int)out.nverts;
+        stash_of[p] = p;
+      }
+      cudaStreamSynchronize(W.st);
+    };
+    std::vector<std::thread> th;
+    for (int w = 1; w < nw; ++w) th.emplace_back(work, std::ref(*workers_[w]));
+    work(*workers_[0]);
+    for (auto& t : th) t.join();
+    for (int w = 0; w < nw; ++w)
+      if (workers_[w]->rc) return pl_.fail(workers_[w]->rc, workers_[w]->msg);
   }
   cudaStreamWaitEvent(st, ev_[1], 0);
   std::vector<int> hst(nov);
@@ -1860,7 +2027,7 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
     pa.aoff = aoff1;
     {
       ::sbc::KProbe kp_("k_pw_pairs", st);
-      k_pw_pairs<<<pair_grid(nov), kPwPairBlock, 0, st>>>(pa, pairK, queue + 1);
+      k_pw_pairs<<<pair_grid(nov, false), kPwPairBlock, 0, st>>>(pa, pairK, queue + 1);
     }
     cudaMemcpyAsync(hst.data(), status, sizeof(int) * nov, cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise clip");

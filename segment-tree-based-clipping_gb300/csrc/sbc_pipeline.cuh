@@ -7,6 +7,7 @@
 #include <array>
 #include <map>
 #include <string>
+#include <memory>
 #include <vector>
 
 #include "sbc_internal.cuh"
@@ -233,7 +234,7 @@ class BatchRunner {
 // the rank shortcut's conditions run through the Pipeline.
 class PairwiseRunner {
  public:
-  explicit PairwiseRunner(Pipeline& pl) : pl_(pl) {}
+  explicit PairwiseRunner(Pipeline& pl);
   ~PairwiseRunner();
   int run(const double* d_bxy, int nb, int nov, const double* d_cxy, const long long* d_coff,
           cudaStream_t st);
@@ -259,17 +260,21 @@ class PairwiseRunner {
   int fallback_pairs = 0;           // pairs clipped by the whole pair pipeline
   int big_pairs = 0;                // pairs whose records went to its rows A9-A18
   int big_k = 8192;                 // records from which a pair counts as big
+  int big_workers = 8;              // host threads, each with a pipeline and a stream, for big pairs
+  int pair_reserve = 1;             // block slots per SM the per-pair kernel leaves to big pairs
   long long hits = 0, tested = 0, grid_cells = 0;
   double cell_factor = 1.0;         // grid cell width in units of sqrt(area / n_b)
 
  private:
+  struct BigWorker;
+  std::vector<std::unique_ptr<BigWorker>> workers_;
   Pipeline& pl_;
   unsigned long long hit_cap_ = 0;
   cudaStream_t st2_ = nullptr;      // the one-thread-per-pair kernel's stream
   cudaEvent_t ev_[2] = {nullptr, nullptr};
   std::vector<int> order_h;
   unsigned pair_blocks_ = 0;
-  unsigned pair_grid(int nov);
+  unsigned pair_grid(int nov, bool reserve);
   // the last run, for area and backward
   int last_nb_ = 0;
   long long last_totalC_ = 0, last_nh_ = 0;

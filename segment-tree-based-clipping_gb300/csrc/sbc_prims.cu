@@ -8,10 +8,11 @@
 #include "sbc_internal.cuh"
 
 #include <cstdio>
+#include <mutex>
 
 namespace sbc {
 
-unsigned long long g_launches = 0;
+std::atomic<unsigned long long> g_launches{0};
 
 // ============================================================== launch probes
 namespace {
@@ -20,7 +21,10 @@ struct ProbeRec {
   cudaEvent_t a, b;
   double bytes;
 };
-bool g_prof_on = false;
+// probes may come from several host threads (the pairwise engine's big-pair
+// workers): the record list is guarded
+std::atomic<bool> g_prof_on{false};
+std::mutex g_prof_mu;
 std::vector<ProbeRec> g_recs;
 std::vector<cudaEvent_t> g_event_pool;
 size_t g_event_next = 0;
@@ -38,6 +42,7 @@ cudaEvent_t next_event() {
 KProbe::KProbe(const char* name, cudaStream_t st, double bytes) : name_(name), st_(st), slot_(-1) {
   ++g_launches;
   if (!g_prof_on) return;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
   ProbeRec r{name, next_event(), next_event(), bytes};
   cudaEventRecord(r.a, st);
   slot_ = (int)g_recs.size();
@@ -45,7 +50,9 @@ KProbe::KProbe(const char* name, cudaStream_t st, double bytes) : name_(name), s
 }
 
 KProbe::~KProbe() {
-  if (slot_ >= 0) cudaEventRecord(g_recs[slot_].b, st_);
+  if (slot_ < 0) return;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  cudaEventRecord(g_recs[slot_].b, st_);
 }
 
 bool profiling_suspend() {
@@ -57,6 +64,7 @@ bool profiling_suspend() {
 void profiling_restore(bool on) { g_prof_on = on; }
 
 void profile_begin() {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
   g_recs.clear();
   g_event_next = 0;
   g_prof_on = true;
@@ -65,6 +73,7 @@ void profile_begin() {
 int profile_end(std::vector<std::string>* names, std::vector<float>* ms, std::vector<int>* counts,
                 std::vector<double>* bytes) {
   g_prof_on = false;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
   names->clear();
   ms->clear();
   counts->clear();
