@@ -239,11 +239,13 @@ int sbc_pairwise_info(const sbc_ctx* ctx, long long* out, int n);
  * 1.  A tuning knob: results do not depend on it. */
 int sbc_pairwise_set_cell_factor(sbc_ctx* ctx, double factor);
 /* Overlays with at least `records` intersecting edge pairs leave the
- * one-thread-per-pair back end for the data-parallel one; default 8192.  A
- * tuning knob: results do not depend on it. */
+ * one-warp-per-pair back end for the data-parallel one (several such overlays
+ * at a time, each on its own stream); default 8192.  A tuning knob: results
+ * do not depend on it. */
 int sbc_pairwise_set_split(sbc_ctx* ctx, int records);
 /* Autotuner: runs the job (device arrays, as for sbc_clip_pairwise_device)
- * under several splits and cell widths, keeps the fastest setting in the
+ * under several splits, block-slot reserves and worker counts for the big
+ * overlays, and cell widths, keeps the fastest setting in the
  * context and reports it (any output may be NULL).  The rings of the last run
  * are left as sbc_clip_pairwise_device would leave them. */
 int sbc_pairwise_autotune(sbc_ctx* ctx, const sbc_pairwise_job* job, int* split,

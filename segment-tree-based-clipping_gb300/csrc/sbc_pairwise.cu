@@ -575,7 +575,7 @@ __host__ __device__ __forceinline__ PwCaps pw_caps(int nb, int nc, int K, int pa
 
 struct PwWork {
   int *hord, *htmp, *ub, *uc, *ut;
-  unsigned long long* sscr;  // warp sorts of long runs: 2K (key, position) pairs
+  unsigned long long* sscr;  // warp sorts of long runs; ring lengths at output
   int *re_e, *re_s, *re_nd, *re_pre, *re_si;
   int *cAll, *cND, *cfill, *csorted;
   double* isxy;
@@ -616,7 +616,7 @@ __host__ __device__ __forceinline__ PwWork pw_carve(Carver& cv, const PwCaps& c)
   const int K = c.K;
   w.hord = cv.take<int>(K);
   w.htmp = cv.take<int>(K);
-  w.sscr = cv.take<unsigned long long>(2 * K + 2);
+  w.sscr = cv.take<unsigned long long>(2 * K + 16);  // also one per ring (rcap)
   w.ub = cv.take<int>(K);
   w.uc = cv.take<int>(K);
   w.ut = cv.take<int>(K);
@@ -701,32 +701,338 @@ struct PwPip {
   }
   __device__ int operator()(SerialArgs& a, int root, double rx, double ry) const {
     const Pool& P = a.P;
-    int w = 0, v = root;
-    do {
-      const int nx = P.next[v];
-      w += pip_step(last_x(P, v), last_y(P, v), P.x[nx], P.y[nx], rx, ry);
-      v = nx;
-    } while (v != root);
     const int lane = threadIdx.x & 31;
-    const int cy = pw_celly(g, __double2float_rd(ry));
+    // the edges between list nodes: every pool node is on the list
     int part = 0;
-    auto step = [&](int u) {
-      if (!internal(P, u)) return;
-      part += pip_step(b[2 * u], b[2 * u + 1], b[2 * u + 2], b[2 * u + 3], rx, ry);
-    };
+    for (int v = lane; v < P.n; v += 32) {
+      const int nx = P.next[v];
+      part += pip_step(last_x(P, v), last_y(P, v), P.x[nx], P.y[nx], rx, ry);
+    }
+    const int cy = pw_celly(g, __double2float_rd(ry));
+    // the step first: most edges of the row do not cross the ray, and only
+    // those that do need the cell and run-membership tests
     for (int cx = lane; cx < g.gx; cx += 32) {
       const int cell = cy * g.gx + cx;
       for (int k = gstart[cell]; k < gstart[cell + 1]; ++k) {
         const int u = gent[k];
-        if (pw_cellx(g, fbox[u].x) != cx) continue;
-        step(u);
+        const int st = pip_step(b[2 * u], b[2 * u + 1], b[2 * u + 2], b[2 * u + 3], rx, ry);
+        if (st && pw_cellx(g, fbox[u].x) == cx && internal(P, u)) part += st;
       }
     }
-    for (int k = lane; k < nlong; k += 32) step(lng[k]);
-    w += __reduce_add_sync(kFullMask, part);
-    return (w % 2) != 0;
+    for (int k = lane; k < nlong; k += 32) {
+      const int u = lng[k];
+      const int st = pip_step(b[2 * u], b[2 * u + 1], b[2 * u + 2], b[2 * u + 3], rx, ry);
+      if (st && internal(P, u)) part += st;
+    }
+    return (__reduce_add_sync(kFullMask, part) % 2) != 0;
   }
 };
+
+// ---------------------------------------------------------------- warp helpers
+// first i in [0, n) with pred(i), or -1; called by all 32 lanes
+template <class Pred>
+__device__ int warp_first(int n, Pred pred) {
+  const int lane = threadIdx.x & 31;
+  for (int i0 = 0; i0 < n; i0 += 32) {
+    const int i = i0 + lane;
+    const unsigned m = __ballot_sync(kFullMask, i < n && pred(i));
+    if (m) return i0 + __ffs(m) - 1;
+  }
+  return -1;
+}
+
+// pointInPoly against a pool every node of which is on its one list (the
+// pairwise back end never unlinks a list node): the winding steps of the
+// edges v -> next[v], summed over the lanes
+__device__ int warp_ppip(const Pool& p, double rx, double ry) {
+  const int lane = threadIdx.x & 31;
+  int part = 0;
+  for (int v = lane; v < p.n; v += 32) {
+    const int nx = p.next[v];
+    part += pip_step(last_x(p, v), last_y(p, v), p.x[nx], p.y[nx], rx, ry);
+  }
+  return __reduce_add_sync(kFullMask, part);
+}
+
+// rcopy of a plain pool whose list is its nodes in index order: ring node
+// base + i is list node i
+__device__ int warp_rcopy_plain(SerialArgs& a, const Pool& p) {
+  const int lane = threadIdx.x & 31;
+  const int r = rnew(a);
+  if (r < 0) return -1;
+  Pool& R = a.R;
+  const int n = p.n, base = R.n;
+  if (n == 0) return 0;
+  if (base + n > R.cap) {
+    a.rfull = 1;
+    return -1;
+  }
+  for (int i = lane; i < n; i += 32) {
+    const int v = base + i;
+    R.x[v] = p.x[i];
+    R.y[v] = p.y[i];
+    R.next[v] = i + 1 == n ? base : v + 1;
+    R.prev[v] = i == 0 ? base + n - 1 : v - 1;
+    R.nb[v] = -1;
+    R.label[v] = L_NONE;
+    R.enex[v] = EX_NEITHER;
+    R.source[v] = 0;
+    R.isect[v] = 0;
+  }
+  R.n = base + n;
+  a.rroot[r] = base;
+  __syncwarp();
+  return 0;
+}
+
+// transition of the entry/exit walk (polyclip.h:337-709 step 4) at a node
+// with label `lab`, on state x = (status is entry) | (first << 1)
+__device__ __forceinline__ int walk_step(int lab, int x) {
+  const int sb = x & 1, f = x >> 1;
+  if (lab == L_CROSSING) return (sb ^ 1) | (f << 1);
+  if (lab == L_DCROSS) return f ? sb : ((sb ^ 1) | 2);
+  if (lab == L_DBOUNCE) return (sb ^ 1) | ((f ^ 1) << 1);
+  return x;
+}
+// the transition as a table: 2 bits per state
+__device__ __forceinline__ unsigned walk_table(int lab) {
+  unsigned t = 0;
+  for (int x = 0; x < 4; ++x) t |= (unsigned)walk_step(lab, x) << (2 * x);
+  return t;
+}
+// g after f
+__device__ __forceinline__ unsigned walk_compose(unsigned g, unsigned f) {
+  unsigned h = 0;
+  for (int x = 0; x < 4; ++x) h |= ((g >> (2 * ((f >> (2 * x)) & 3))) & 3) << (2 * x);
+  return h;
+}
+
+// labelIntersections2 + createResult2 (polyclip.h:337-759) of one pair, run
+// by all 32 lanes: the serial restatement (sbc_serial.cuh) with the searches,
+// point-in-polygon sums, list copies and the entry/exit walk spread over the
+// lanes.  On entry both lists are their pools in index order; a list node is
+// never unlinked, so every pool node is on its list throughout.
+__device__ int pw_label_trace(SerialArgs& a, const PwPip& pipP) {
+  const int lane = threadIdx.x & 31;
+  Pool& P = a.P;
+  Pool& Q = a.Q;
+  // (2) chains: rare (overlapping edges), so the serial pass runs only when
+  // a chain start exists
+  if (warp_first(P.n, [&](int v) {
+        return P.isect[v] && (P.label[v] == L_LEFT_ON || P.label[v] == L_RIGHT_ON);
+      }) >= 0) {
+    int V = 0;
+    do {
+      if (P.isect[V] && (P.label[V] == L_LEFT_ON || P.label[V] == L_RIGHT_ON)) {
+        int x = P.label[V] == L_LEFT_ON ? 0 : 1;
+        int X = V, I = V;
+        int guard = P.n + 1;
+        do {
+          P.label[I] = L_NONE;
+          if (P.nb[I] < 0) return 2;
+          Q.label[P.nb[I]] = L_NONE;
+          I = P.next[I];
+          if (--guard < 0) return 2;
+        } while (P.label[I] == L_ON_ON);
+        int y = P.label[I] == L_ON_LEFT ? 0 : 1;
+        int chain = (x != y) ? L_DCROSS : L_DBOUNCE;
+        P.label[X] = chain;
+        P.label[I] = chain;
+        if (P.nb[X] < 0 || P.nb[I] < 0) return 2;
+        Q.label[P.nb[X]] = chain;
+        Q.label[P.nb[I]] = chain;
+      }
+      V = P.next[V];
+    } while (V != 0);
+    __syncwarp();
+  }
+  auto pip_of = [&](int s, double rx, double ry) -> int {
+    if (s == 0) return pipP(a, 0, rx, ry);
+    return (warp_ppip(Q, rx, ry) % 2) != 0;
+  };
+  // (3.5) sides without crossings
+  int noIsect[2] = {0, 0}, ident[2] = {0, 0};
+  for (int s = 0; s < 2; ++s) {
+    Pool& p = side(a, s);
+    Pool& o = side(a, 1 - s);
+    const int n = p.n;
+    const bool cross = warp_first(n, [&](int v) {
+                         if (!p.isect[v]) return false;
+                         const int l = p.label[v];
+                         // noCrossingVertex(UNION), foster/polygon.h:465-475
+                         return l == L_CROSSING || l == L_DCROSS ||
+                                (a.unite && (l == L_BOUNCING || l == L_DBOUNCE));
+                       }) >= 0;
+    if (cross) continue;
+    noIsect[s] = 1;
+    if (warp_first(n, [&](int v) { return p.label[v] != L_ON_ON; }) < 0) {
+      ident[s] = 1;
+      continue;
+    }
+    double px, py;
+    const int f = warp_first(n, [&](int v) { return !p.isect[v]; });
+    if (f >= 0) {
+      px = p.x[f];
+      py = p.y[f];
+    } else {
+      const int V = warp_first(n, [&](int v) {
+        const int nbV = p.nb[v], nbN = p.nb[p.next[v]];
+        return nbV < 0 || (nbN != o.prev[nbV] && nbN != o.next[nbV]);
+      });
+      if (V < 0 || p.nb[V] < 0) return 2;
+      px = dmul(0.5, dadd(p.x[V], p.x[p.next[V]]));
+      py = dmul(0.5, dadd(p.y[V], p.y[p.next[V]]));
+    }
+    if (pip_of(1 - s, px, py) ^ a.unite) {
+      const int rc = s == 1 ? warp_rcopy_plain(a, p) : rcopy(a, p, 0);
+      if (rc) return 3;
+    }
+  }
+  if (ident[0] && ident[1]) {
+    const int target = P.nb[0];
+    if (warp_first(Q.n, [&](int v) { return v == target; }) >= 0 && rcopy(a, P, 0)) return 3;
+  }
+  __syncwarp();
+  // (4) entry/exit walk from a non-intersection vertex of each side
+  for (int s = 0; s < 2; ++s) {
+    if (noIsect[s]) continue;
+    Pool& p = side(a, s);
+    Pool& o = side(a, 1 - s);
+    unsigned char* split = s == 0 ? a.splitP : a.splitQ;
+    unsigned char* cross = s == 0 ? a.crossP : a.crossQ;
+    const int n0 = p.n;  // this side's list is still its pool in index order
+    int V = warp_first(n0, [&](int v) { return !p.isect[v]; });
+    int start = V;
+    if (V < 0) {
+      const int U = warp_first(n0, [&](int v) {
+        const int nbV = p.nb[v], nbN = p.nb[p.next[v]];
+        return nbV < 0 || (nbN != o.prev[nbV] && nbN != o.next[nbV]);
+      });
+      if (U < 0 || p.nb[U] < 0) return 2;
+      const double mx = dmul(0.5, dadd(p.x[U], p.x[p.next[U]]));
+      const double my = dmul(0.5, dadd(p.y[U], p.y[p.next[U]]));
+      V = pnew(p, mx, my);
+      if (V < 0) return 3;
+      pinsert_after(p, V, U);
+      start = U + 1 == n0 ? 0 : U + 1;  // the midpoint itself is no intersection
+      __syncwarp();
+    }
+    int x0 = 1 | 2;  // entry, first
+    if (pip_of(1 - s, p.x[V], p.y[V])) x0 ^= 1;
+    // the walk over the list from V: its original nodes in cyclic index
+    // order from `start`; transitions composed by a warp scan per chunk
+    for (int j0 = 0; j0 < n0; j0 += 32) {
+      const int j = j0 + lane;
+      int I = start + j;
+      if (I >= n0) I -= n0;
+      const bool ok = j < n0;
+      const int lab = ok && p.isect[I] ? p.label[I] : L_NONE;
+      unsigned t = walk_table(lab);
+      for (int d = 1; d < 32; d <<= 1) {
+        const unsigned u = __shfl_up_sync(kFullMask, t, d);
+        if (lane >= d) t = walk_compose(t, u);
+      }
+      const int after = (t >> (2 * x0)) & 3;
+      int before = __shfl_up_sync(kFullMask, after, 1);
+      if (lane == 0) before = x0;
+      x0 = __shfl_sync(kFullMask, after, 31);
+      if (!ok || !p.isect[I]) continue;
+      const int status = (before & 1) ? EX_ENTRY : EX_EXIT;
+      const int first = before >> 1;
+      if (lab == L_CROSSING) p.enex[I] = status;
+      if (lab == L_BOUNCING && ((status == EX_EXIT) ^ a.unite)) split[I] = 1;
+      if (lab == L_DCROSS) {
+        p.enex[I] = status;
+        if (first ? ((status == EX_EXIT) ^ a.unite) : ((status == EX_ENTRY) ^ a.unite))
+          p.label[I] = L_CROSSING;
+      }
+      if (lab == L_DBOUNCE) {
+        p.enex[I] = status;
+        if (first ? ((status == EX_EXIT) ^ a.unite) : ((status == EX_ENTRY) ^ a.unite))
+          cross[I] = 1;
+      }
+    }
+    __syncwarp();
+  }
+  // (5) split pairs: rare (bouncing vertices), serial when present
+  const int nP0 = P.n;
+  if (warp_first(nP0, [&](int v) { return a.splitP[v] != 0; }) >= 0) {
+    for (int IP = 0; IP < nP0; ++IP) {
+      if (!a.splitP[IP]) continue;
+      int IQ = P.nb[IP];
+      if (IQ < 0 || !a.splitQ[IQ]) continue;
+      int VP = pnew(P, P.x[IP], P.y[IP]);
+      int VQ = pnew(Q, Q.x[IQ], Q.y[IQ]);
+      if (VP < 0 || VQ < 0) return 3;
+      double sP = area3(last_x(P, P.prev[IP]), last_y(P, P.prev[IP]), P.x[IP], P.y[IP],
+                        P.x[P.next[IP]], P.y[P.next[IP]]);
+      double sQ = area3(Q.x[Q.prev[IQ]], Q.y[Q.prev[IQ]], Q.x[IQ], Q.y[IQ], Q.x[Q.next[IQ]],
+                        Q.y[Q.next[IQ]]);
+      if (dmul(sP, sQ) > 0) {
+        P.nb[IP] = VQ; Q.nb[VQ] = IP; P.isect[IP] = 1; Q.isect[VQ] = 1;
+        Q.nb[IQ] = VP; P.nb[VP] = IQ; Q.isect[IQ] = 1; P.isect[VP] = 1;
+      } else {
+        P.nb[VP] = VQ; Q.nb[VQ] = VP; P.isect[VP] = 1; Q.isect[VQ] = 1;
+      }
+      pinsert_after(P, VP, IP);
+      pinsert_after(Q, VQ, IQ);
+      if (!a.unite) {
+        P.enex[IP] = EX_EXIT; P.enex[VP] = EX_ENTRY;
+        Q.enex[IQ] = EX_EXIT; Q.enex[VQ] = EX_ENTRY;
+      } else {
+        P.enex[IP] = EX_ENTRY; P.enex[VP] = EX_EXIT;
+        Q.enex[IQ] = EX_ENTRY; Q.enex[VQ] = EX_EXIT;
+      }
+      P.label[IP] = P.label[VP] = L_CROSSING;
+      Q.label[IQ] = Q.label[VQ] = L_CROSSING;
+    }
+    __syncwarp();
+  }
+  // (6) each P node and its neighbour, independently
+  for (int IP = lane; IP < P.n; IP += 32) {
+    if (!a.crossP[IP]) continue;
+    const int IQ = P.nb[IP];
+    if (IQ >= 0 && a.crossQ[IQ]) {
+      P.label[IP] = L_CROSSING;
+      Q.label[IQ] = L_CROSSING;
+    }
+  }
+  __syncwarp();
+  // createResult2 (serial, on every lane)
+  {
+    int It = 0;
+    long long guard = 4LL * (P.n + Q.n) + 16;
+    do {
+      if (P.isect[It] && P.label[It] == L_CROSSING) {
+        int r = rnew(a);
+        if (r < 0) return 3;
+        int sI = 0, I = It, sV = 0, V = I;
+        P.isect[I] = 0;
+        do {
+          int status = side(a, sV).enex[V];
+          tog(&status);
+          Pool* pv;
+          do {
+            pv = &side(a, sV);
+            V = ((status == EX_EXIT) ^ a.unite) ? pv->next[V] : pv->prev[V];
+            pv->isect[V] = 0;
+            if (radd_node(a, r, *pv, V, (status == EX_EXIT) ^ a.unite, -1)) return 2;
+            if (--guard < 0) return 2;
+          } while (!(pv->enex[V] == status) && !(sV == sI && V == I));
+          if (!(sV == sI && V == I)) {
+            int nbv = side(a, sV).nb[V];
+            if (nbv < 0) return 2;
+            sV = 1 - sV;
+            V = nbv;
+            side(a, sV).isect[V] = 0;
+          }
+        } while (!(sV == sI && V == I));
+      }
+      It = P.next[It];
+    } while (It != 0);
+  }
+  return 0;
+}
 
 struct PwPairArgs {
   int nov;
@@ -1215,12 +1521,77 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
   for (int q = lane; q < nQ; q += 32) w.labC[q] = w.cWin[q] >= 0 ? w.splab[w.cWinSI[q]] : 0;
   __syncwarp();
   // ---- A15 linked lists (copyToLinkedList, src/clip.cpp:606-695): the base's
-  // with run nodes for its stretches of plain vertices (serial, on every lane)
+  // with run nodes for its stretches of plain vertices.  Its walk visits, per
+  // run r, the stretch of plain vertices since the previous run (one run
+  // node), the vertex of edge e_r and its intersections, and a last stretch
+  // to the end -- unless a coordinate stops the walk early: a slot of edge
+  // e_r repeating vertex e_r + 1, or a NaN.  Those lists take the serial walk.
   Pool& P = w.P;
   Pool& Q = w.Q;
   P.n = Q.n = w.R.n = 0;
   P.rxy = b;
   int nruns = 0, lastPlain = -1;
+  bool oddP = false;
+  for (int r = lane; r < nr && !oddP; r += 32) {
+    const int e = w.re_e[r], si = w.re_si[r], nd = w.re_nd[r];
+    if (!(w.spx[si] == b[2 * e] && w.spy[si] == b[2 * e + 1])) oddP = true;
+    if (nd == 0) continue;
+    const int nx = e + 1 == nb ? 0 : e + 1;
+    const double vx = b[2 * nx], vy = b[2 * nx + 1];
+    if (!(vx == vx && vy == vy)) oddP = true;
+    for (int q = 1; q <= nd; ++q)
+      if (w.spx[si + q] == vx && w.spy[si + q] == vy) oddP = true;
+  }
+  if (!__any_sync(kFullMask, oddP)) {
+    // nodes per run (stretch, vertex, intersections), offsets by a scan in re_s
+    for (int r = lane; r < nr; r += 32) {
+      const int e = w.re_e[r], pe = r == 0 ? 0 : w.re_e[r - 1] + 1;
+      w.re_s[r] = (e > pe ? 1 : 0) + 1 + w.re_nd[r];
+    }
+    if (lane == (nr & 31)) w.re_s[nr] = 0;
+    __syncwarp();
+    const int tot0 = warp_excl_scan(w.re_s, nr + 1);
+    const int pe_last = nr == 0 ? 0 : w.re_e[nr - 1] + 1;
+    const int tail = pe_last < nb ? 1 : 0;
+    if (tot0 + tail > P.cap) return PS_CAP;
+    auto put = [&](int v, double x, double y, int src1, int lab, int isect) {
+      P.x[v] = x;
+      P.y[v] = y;
+      P.nb[v] = -1;
+      P.label[v] = lab;
+      P.enex[v] = EX_NEITHER;
+      P.source[v] = (unsigned char)src1;
+      P.isect[v] = (unsigned char)isect;
+      P.run[v] = 0;
+      P.rv0[v] = 0;
+    };
+    __syncwarp();
+    for (int r = lane; r < nr; r += 32) {
+      const int e = w.re_e[r], pe = r == 0 ? 0 : w.re_e[r - 1] + 1, si = w.re_si[r];
+      int v = w.re_s[r];
+      if (e > pe) {  // the stretch pe .. e-1; it is stretch number v - r - re_pre[r]
+        put(v, b[2 * pe], b[2 * pe + 1], 1, L_NONE, 0);
+        P.run[v] = e - pe - 1;
+        P.rv0[v] = pe;
+        w.runIds[v - r - w.re_pre[r]] = v;
+        ++v;
+      }
+      put(v, b[2 * e], b[2 * e + 1], 1, w.splab[si], w.spal[si] != -100);
+      w.spnode[si] = v++;
+      for (int q = 1; q <= w.re_nd[r]; ++q) {
+        put(v, w.spx[si + q], w.spy[si + q], 0, w.splab[si + q], 1);
+        w.spnode[si + q] = v++;
+      }
+    }
+    if (tail && lane == 0) {
+      put(tot0, b[2 * pe_last], b[2 * pe_last + 1], 1, L_NONE, 0);
+      P.run[tot0] = nb - pe_last - 1;
+      P.rv0[tot0] = pe_last;
+      w.runIds[tot0 - nr - knd] = tot0;
+    }
+    nruns = tot0 - nr - knd + tail;
+    P.n = tot0 + tail;
+  } else {
   auto plain = [&](int v0, int len) -> int {
     if (lastPlain >= 0 && lastPlain == P.n - 1 && P.rv0[lastPlain] + P.run[lastPlain] == v0 - 1) {
       P.run[lastPlain] += len;
@@ -1296,6 +1667,7 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
       ++ii;
     }
     if (vn != nB) return PS_UNDEF;
+  }
   }
   __syncwarp();
   for (int v = lane; v < P.n; v += 32) {
@@ -1429,26 +1801,88 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
   PwPip pip = A.pip;
   pip.runIds = w.runIds;
   pip.nruns = nruns;
-  int st = ser_label_trace_t(a, pip);
+  int st = pw_label_trace(a, pip);
   if (a.rfull) return PS_CAP;
   if (st) return st == 2 ? PS_UNDEF : PS_CAP;
-  ser_cleanup(a);
-  int nrg = 0, nv = 0;
-  w.roff[0] = 0;
-  for (int r = 0; r < *a.nrings; ++r) {
-    const int root = a.rroot[r];
-    if (root < 0) continue;
-    int v = root;
-    do {
-      w.rxy[2 * nv] = a.R.x[v];
-      w.rxy[2 * nv + 1] = a.R.y[v];
-      ++nv;
-      v = a.R.next[v];
-    } while (v != root);
-    w.roff[++nrg] = nv;
+  // cleanUpResult2 (ser_cleanup) ring by ring, one ring per lane (rings
+  // share no nodes), then each ring's length: ring r's vertex count in the
+  // low half of sscr[r], 1 << 32 in the high half when it is not empty
+  const int nring = *a.nrings;
+  {
+    Pool& R = a.R;
+    for (int r = lane; r < nring; r += 32) {
+      auto A3 = [&](int v) {
+        return fabs(area3(R.x[R.prev[v]], R.y[R.prev[v]], R.x[v], R.y[v], R.x[R.next[v]],
+                          R.y[R.next[v]]));
+      };
+      int root = a.rroot[r];
+      auto remove = [&](int V) {
+        if (root == V) {
+          root = R.next[V];
+          if (R.next[root] == root) root = -1;
+        }
+        R.next[R.prev[V]] = R.next[V];
+        R.prev[R.next[V]] = R.prev[V];
+      };
+      while (root >= 0 && A3(root) < kEps) remove(root);
+      unsigned long long len = 0;
+      if (root >= 0) {
+        const int start = root;
+        int V = start;
+        do {
+          const int nx = R.next[V];
+          if (A3(V) < kEps) remove(V);
+          V = nx;
+        } while (V != start);
+      }
+      if (root >= 0) {
+        int V = root;
+        do {
+          ++len;
+          V = R.next[V];
+        } while (V != root);
+        len |= 1ull << 32;
+      }
+      a.rroot[r] = root;
+      w.sscr[r] = len;
+    }
   }
-  *nrings_out = nrg;
-  *nverts_out = nv;
+  __syncwarp();
+  // output offsets (one scan of both halves), then the rings' coordinates
+  {
+    unsigned long long carry = 0;
+    for (int r0 = 0; r0 < nring; r0 += 32) {
+      const int r = r0 + lane;
+      const unsigned long long x = r < nring ? w.sscr[r] : 0;
+      unsigned long long sc = x;
+      for (int d = 1; d < 32; d <<= 1) {
+        const unsigned long long t = __shfl_up_sync(kFullMask, sc, d);
+        if (lane >= d) sc += t;
+      }
+      if (r < nring) w.sscr[r] = carry + sc - x;
+      carry += __shfl_sync(kFullMask, sc, 31);
+    }
+    __syncwarp();
+    w.roff[0] = 0;
+    for (int r = lane; r < nring; r += 32) {
+      const int root = a.rroot[r];
+      if (root < 0) continue;
+      const unsigned long long off = w.sscr[r];
+      int nv = (int)(unsigned)off;
+      const int k = (int)(off >> 32);
+      int v = root;
+      do {
+        w.rxy[2 * nv] = a.R.x[v];
+        w.rxy[2 * nv + 1] = a.R.y[v];
+        ++nv;
+        v = a.R.next[v];
+      } while (v != root);
+      w.roff[k + 1] = nv;
+    }
+    __syncwarp();
+    *nrings_out = (int)(carry >> 32);
+    *nverts_out = (int)(unsigned)carry;
+  }
   return PS_OK;
 }
 
@@ -1560,9 +1994,10 @@ unsigned PairwiseRunner::pair_grid(int nov, bool reserve) {
   return need < pair_blocks_ ? need : pair_blocks_;
 }
 
-// Time the job under a few settings of the big-pair split and the grid cell
-// width and keep the fastest (results do not depend on either): the split
-// first at the current cell width, then the cell width at the best split.
+// Time the job under a few settings and keep the fastest (results depend on
+// none of them), one setting at a time at the best so far: the big-pair
+// split, the block slots left to big pairs, the big-pair worker count, the
+// grid cell width.
 int PairwiseRunner::autotune(const double* d_bxy, int nb, int nov, const double* d_cxy,
                              const long long* d_coff, cudaStream_t st, double* best_ms) {
   auto timed = [&](double* ms) -> int {
@@ -1576,7 +2011,7 @@ int PairwiseRunner::autotune(const double* d_bxy, int nb, int nov, const double*
   if (rc) return rc;
   int best_split = big_k;
   double best_cell = cell_factor, best = 1e300;
-  for (int split : {2048, 4096, 8192, 16384, 32768}) {
+  for (int split : {2048, 4096, 6144, 8192, 12288, 16384, 32768}) {
     big_k = split;
     rc = timed(&ms);
     if (rc) return rc;
@@ -1598,6 +2033,17 @@ int PairwiseRunner::autotune(const double* d_bxy, int nb, int nov, const double*
     }
   }
   pair_reserve = best_reserve;
+  int best_workers = big_workers;
+  for (int nw : {4, 16}) {
+    big_workers = nw;
+    rc = timed(&ms);
+    if (rc) return rc;
+    if (ms < best) {
+      best = ms;
+      best_workers = nw;
+    }
+  }
+  big_workers = best_workers;
   for (double f : {0.5, 2.0}) {
     cell_factor = f;
     rc = timed(&ms);
