@@ -425,6 +425,13 @@ struct PwCandArgs {
   const int* rankC;
   const int* rankCB;
   const double* uval;
+  int* tpair;                  // per overlay edge: its pair, or -1 (not on the fast path)
+  long long* coffs;            // per overlay edge: its candidates' offset (count before the scan)
+  int2* cand;                  // (overlay edge, base edge) of every candidate
+  long long ncand;
+  PwHit* raw;                  // intersecting candidates (key not yet known)
+  unsigned long long rawcap;
+  unsigned long long* nraw;
   PwHit* hits;
   unsigned long long cap;
   unsigned long long* nhits;
@@ -432,67 +439,55 @@ struct PwCandArgs {
   unsigned long long* tested;  // box-overlapping pairs passing LSMF
 };
 
-__global__ void k_pw_candidates(PwCandArgs A) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= A.totalC) return;
+// Candidates in three converged steps (one thread per overlay edge walking
+// a varying number of grid entries, with the FP64 test inside the walk,
+// leaves most lanes of a warp idle on the FP64 pipe):
+//   1. per overlay edge, the base edges whose float boxes overlap its own,
+//      each in the cell of the overlap's low corner (counted, then written);
+//   2. one thread per candidate: LSMF and lineSegmentIntersection in FP64;
+//   3. one thread per intersection: tree quantities and emission key.
+// The overlay edge's cells; false when it is not on the fast path.
+struct PwEdge {
+  int i, n, j, j2;
+  double q1x, q1y, q2x, q2y;
+  float4 fc;
+  int cx0, cx1, cy0, cy1;
+};
+
+__device__ bool pw_edge_of(const PwCandArgs& A, long long t, PwEdge& E, bool fast_only = true) {
   int lo = 0, hi = A.nov;  // pair: last i with coff[i] <= t
   while (hi - lo > 1) {
     const int m = (lo + hi) >> 1;
     if (A.coff[m] <= t) lo = m;
     else hi = m;
   }
-  const int i = lo;
-  const PwPair q = A.pp[i];
-  if (q.mode != PW_FAST) return;
-  const long long o = A.coff[i];
-  const int n = (int)(A.coff[i + 1] - o);
-  const int j = (int)(t - o), j2 = j + 1 == n ? 0 : j + 1;
+  E.i = lo;
+  if (fast_only && A.pp[E.i].mode != PW_FAST) return false;
+  const long long o = A.coff[E.i];
+  E.n = (int)(A.coff[E.i + 1] - o);
+  E.j = (int)(t - o);
+  E.j2 = E.j + 1 == E.n ? 0 : E.j + 1;
   const double* c = A.cxy + 2 * o;
-  const double q1x = c[2 * j], q1y = c[2 * j + 1], q2x = c[2 * j2], q2y = c[2 * j2 + 1];
-  const float4 fc = make_float4(__double2float_rd(fmin(q1x, q2x)), __double2float_rd(fmin(q1y, q2y)),
-                                __double2float_ru(fmax(q1x, q2x)), __double2float_ru(fmax(q1y, q2y)));
-  const int cx0 = pw_cellx(A.g, fc.x), cx1 = pw_cellx(A.g, fc.z);
-  const int cy0 = pw_celly(A.g, fc.y), cy1 = pw_celly(A.g, fc.w);
-  if ((long long)(cx1 - cx0 + 1) * (cy1 - cy0 + 1) > kPwMaxCells) {
-    atomicExch(&A.pp[i].mode, PW_FALLBACK);
-    return;
-  }
-  const PwTree T{q.count, q.epc, q.z, q.epc - 1, q.logL};
-  const int nb = A.nb;
-  const double* uc = A.uval + o;
-  bool haveC = false;
-  int aftC = -1, befC = -1;
-  int2 lrC = make_int2(0, 0);
-  unsigned long long tested = 0;
-  auto test = [&](int be) {
-    const int be2 = be + 1 == nb ? 0 : be + 1;
-    const double p1x = A.b[2 * be], p1y = A.b[2 * be + 1];
-    const double p2x = A.b[2 * be2], p2y = A.b[2 * be2 + 1];
-    if (!lsmf_d(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y)) return;
-    ++tested;
-    double al, bt;
-    const int ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
-    if (!ty) return;
-    if (!haveC) {
-      const int r1 = A.rankC[o + j] + A.rankCB[o + j], r2 = A.rankC[o + j2] + A.rankCB[o + j2];
-      if (q1x < q2x) pw_edge_tree(T, r1, q1x, r2, q2x, &aftC, &befC, &lrC);
-      else pw_edge_tree(T, r2, q2x, r1, q1x, &aftC, &befC, &lrC);
-      haveC = true;
-    }
-    const int r1 = A.rankB[be] + lower_bound_d(uc, q.nuc, p1x);
-    const int r2 = A.rankB[be2] + lower_bound_d(uc, q.nuc, p2x);
-    int aftB, befB;
-    int2 lrB;
-    if (p1x < p2x) pw_edge_tree(T, r1, p1x, r2, p2x, &aftB, &befB, &lrB);
-    else pw_edge_tree(T, r2, p2x, r1, p1x, &aftB, &befB, &lrB);
-    unsigned long long key;
-    if (emission_q(lrB, lrC, aftB, befB, aftC, befC, nb + j, 2 * j, T.logL, &key) == 0) return;
-    const unsigned long long h = atomicAdd(A.nhits, 1ull);
-    atomicAdd(&A.pairK[i], 1);
-    if (h < A.cap) A.hits[h] = PwHit{i, be, j, ty, key, al, bt};
-  };
-  for (int cy = cy0; cy <= cy1; ++cy) {
-    for (int cx = cx0; cx <= cx1; ++cx) {
+  E.q1x = c[2 * E.j];
+  E.q1y = c[2 * E.j + 1];
+  E.q2x = c[2 * E.j2];
+  E.q2y = c[2 * E.j2 + 1];
+  E.fc = make_float4(__double2float_rd(fmin(E.q1x, E.q2x)), __double2float_rd(fmin(E.q1y, E.q2y)),
+                     __double2float_ru(fmax(E.q1x, E.q2x)), __double2float_ru(fmax(E.q1y, E.q2y)));
+  E.cx0 = pw_cellx(A.g, E.fc.x);
+  E.cx1 = pw_cellx(A.g, E.fc.z);
+  E.cy0 = pw_celly(A.g, E.fc.y);
+  E.cy1 = pw_celly(A.g, E.fc.w);
+  return true;
+}
+
+// every base edge whose box overlaps the overlay edge's, once: in the cell of
+// the overlap's low corner, or from the list of long base edges
+template <class F>
+__device__ void pw_edge_walk(const PwCandArgs& A, const PwEdge& E, F f) {
+  const float4 fc = E.fc;
+  for (int cy = E.cy0; cy <= E.cy1; ++cy) {
+    for (int cx = E.cx0; cx <= E.cx1; ++cx) {
       const int cell = cy * A.g.gx + cx;
       const int e0 = A.gstart[cell], e1 = A.gstart[cell + 1];
       for (int k = e0; k < e1; ++k) {
@@ -501,7 +496,7 @@ __global__ void k_pw_candidates(PwCandArgs A) {
         if (fb.x > fc.z || fb.z < fc.x || fb.y > fc.w || fb.w < fc.y) continue;
         if (pw_cellx(A.g, fmaxf(fb.x, fc.x)) != cx || pw_celly(A.g, fmaxf(fb.y, fc.y)) != cy)
           continue;
-        test(be);
+        f(be);
       }
     }
   }
@@ -510,9 +505,114 @@ __global__ void k_pw_candidates(PwCandArgs A) {
     const int be = A.lng[k];
     const float4 fb = A.fbox[be];
     if (fb.x > fc.z || fb.z < fc.x || fb.y > fc.w || fb.w < fc.y) continue;
-    test(be);
+    f(be);
   }
-  if (tested) atomicAdd(A.tested, tested);
+}
+
+__global__ void k_pw_cand_count(PwCandArgs A) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t > A.totalC) return;
+  long long cnt = 0;
+  int pair = -1;
+  PwEdge E;
+  if (t < A.totalC && pw_edge_of(A, t, E)) {
+    if ((long long)(E.cx1 - E.cx0 + 1) * (E.cy1 - E.cy0 + 1) > kPwMaxCells) {
+      atomicExch(&A.pp[E.i].mode, PW_FALLBACK);
+    } else {
+      pair = E.i;
+      pw_edge_walk(A, E, [&](int) { ++cnt; });
+    }
+  }
+  A.coffs[t] = cnt;
+  if (t < A.totalC) A.tpair[t] = pair;
+}
+
+__global__ void k_pw_cand_fill(PwCandArgs A) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= A.totalC || A.tpair[t] < 0) return;
+  PwEdge E;
+  pw_edge_of(A, t, E, false);  // counted: fill every slot even if the pair left the fast path
+  long long k = A.coffs[t];
+  pw_edge_walk(A, E, [&](int be) { A.cand[k++] = make_int2((int)t, be); });
+}
+
+// appends to a counter-indexed buffer, one atomic per warp: all 32 lanes
+// call it; lanes with `take` get consecutive slots
+__device__ __forceinline__ unsigned long long warp_append(bool take, unsigned long long* counter) {
+  const int lane = threadIdx.x & 31;
+  const unsigned m = __ballot_sync(kFullMask, take);
+  if (!m) return 0;
+  const int leader = __ffs(m) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(m));
+  base = __shfl_sync(kFullMask, base, leader);
+  return base + __popc(m & ((1u << lane) - 1u));
+}
+
+__global__ void k_pw_cand_test(PwCandArgs A) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool ok = c < A.ncand;
+  int ty = 0, t = 0, be = 0, i = 0, j = 0;
+  double al = 0.0, bt = 0.0;
+  bool lsmf = false;
+  if (ok) {
+    const int2 cb = A.cand[c];
+    t = cb.x;
+    be = cb.y;
+    i = A.tpair[t];
+    const long long o = A.coff[i];
+    const int n = (int)(A.coff[i + 1] - o);
+    j = (int)(t - o);
+    const int j2 = j + 1 == n ? 0 : j + 1;
+    const double* cc = A.cxy + 2 * o;
+    const double q1x = cc[2 * j], q1y = cc[2 * j + 1], q2x = cc[2 * j2], q2y = cc[2 * j2 + 1];
+    const int be2 = be + 1 == A.nb ? 0 : be + 1;
+    const double p1x = A.b[2 * be], p1y = A.b[2 * be + 1];
+    const double p2x = A.b[2 * be2], p2y = A.b[2 * be2 + 1];
+    lsmf = lsmf_d(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y);
+    if (lsmf) ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
+  }
+  const unsigned tm = __ballot_sync(kFullMask, lsmf);
+  if ((threadIdx.x & 31) == 0 && tm) atomicAdd(A.tested, (unsigned long long)__popc(tm));
+  const unsigned long long h = warp_append(ty != 0, A.nraw);
+  if (ty != 0 && h < A.rawcap) A.raw[h] = PwHit{i, be, j, ty, 0ull, al, bt};
+}
+
+__global__ void k_pw_hit_tree(PwCandArgs A, long long nraw) {
+  const long long h = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool emit = false;
+  PwHit x{};
+  if (h < nraw) {
+    x = A.raw[h];
+    const PwPair q = A.pp[x.pair];
+    const long long o = A.coff[x.pair];
+    const int n = (int)(A.coff[x.pair + 1] - o);
+    const int j = x.j, j2 = j + 1 == n ? 0 : j + 1;
+    const double* c = A.cxy + 2 * o;
+    const double q1x = c[2 * j], q2x = c[2 * j2];
+    const PwTree T{q.count, q.epc, q.z, q.epc - 1, q.logL};
+    int aftC, befC, aftB, befB;
+    int2 lrC, lrB;
+    const int c1 = A.rankC[o + j] + A.rankCB[o + j], c2 = A.rankC[o + j2] + A.rankCB[o + j2];
+    if (q1x < q2x) pw_edge_tree(T, c1, q1x, c2, q2x, &aftC, &befC, &lrC);
+    else pw_edge_tree(T, c2, q2x, c1, q1x, &aftC, &befC, &lrC);
+    const int be = x.b, be2 = be + 1 == A.nb ? 0 : be + 1;
+    const double p1x = A.b[2 * be], p2x = A.b[2 * be2];
+    const double* uc = A.uval + o;
+    const int r1 = A.rankB[be] + lower_bound_d(uc, q.nuc, p1x);
+    const int r2 = A.rankB[be2] + lower_bound_d(uc, q.nuc, p2x);
+    if (p1x < p2x) pw_edge_tree(T, r1, p1x, r2, p2x, &aftB, &befB, &lrB);
+    else pw_edge_tree(T, r2, p2x, r1, p1x, &aftB, &befB, &lrB);
+    emit = emission_q(lrB, lrC, aftB, befB, aftC, befC, A.nb + j, 2 * j, T.logL, &x.key) != 0;
+  }
+  const unsigned long long slot = warp_append(emit, A.nhits);
+  if (emit && slot < A.cap) A.hits[slot] = x;
+  // per pair counts: one atomic per group of lanes with the same pair
+  const unsigned em = __ballot_sync(kFullMask, emit);
+  if (emit) {
+    const unsigned same = __match_any_sync(em, x.pair);
+    if ((threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(&A.pairK[x.pair], __popc(same));
+  }
 }
 
 // The hits of every pair in the reference's record order (base id, then
@@ -1804,10 +1904,48 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
   int st = pw_label_trace(a, pip);
   if (a.rfull) return PS_CAP;
   if (st) return st == 2 ? PS_UNDEF : PS_CAP;
-  // cleanUpResult2 (ser_cleanup) ring by ring, one ring per lane (rings
-  // share no nodes), then each ring's length: ring r's vertex count in the
-  // low half of sscr[r], 1 << 32 in the high half when it is not empty
+  // cleanUpResult2 (ser_cleanup).  Rings are built one after another and
+  // grow at their end, so ring r is the pool nodes rroot[r] .. rroot[r+1]-1
+  // in order.  A vertex with |area3| < eps marks its ring; with no ring
+  // marked nothing is removed and the output is the pool itself.
   const int nring = *a.nrings;
+  for (int r = lane; r < nring; r += 32) w.sscr[r] = 0;
+  __syncwarp();
+  {
+    const Pool& R = a.R;
+    for (int v = lane; v < R.n; v += 32) {
+      const double ar = fabs(area3(R.x[R.prev[v]], R.y[R.prev[v]], R.x[v], R.y[v],
+                                   R.x[R.next[v]], R.y[R.next[v]]));
+      if (!(ar < kEps)) continue;
+      int lo = 0, hi = nring;  // rings with rroot <= v
+      while (lo < hi) {
+        const int m = (lo + hi) >> 1;
+        if (a.rroot[m] <= v) lo = m + 1;
+        else hi = m;
+      }
+      if (lo > 0) w.sscr[lo - 1] = 1;
+    }
+  }
+  __syncwarp();
+  if (warp_first(nring, [&](int r) {
+        return w.sscr[r] != 0 || (r > 0 && a.rroot[r] <= a.rroot[r - 1]);
+      }) < 0 &&
+      (nring == 0 || a.rroot[0] == 0)) {
+    const Pool& R = a.R;
+    for (int v = lane; v < R.n; v += 32) {
+      w.rxy[2 * v] = R.x[v];
+      w.rxy[2 * v + 1] = R.y[v];
+    }
+    for (int r = lane; r < nring; r += 32) w.roff[r] = a.rroot[r];
+    if (lane == 0) w.roff[nring] = R.n;
+    __syncwarp();
+    *nrings_out = nring;
+    *nverts_out = R.n;
+    return PS_OK;
+  }
+  // some ring loses vertices: ring by ring, one ring per lane (rings share no
+  // nodes), then each ring's length: ring r's vertex count in the low half of
+  // sscr[r], 1 << 32 in the high half when it is not empty
   {
     Pool& R = a.R;
     for (int r = lane; r < nring; r += 32) {
@@ -2207,30 +2345,91 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
   int* hstart = (int*)pool.get("pw_hstart", sizeof(int) * (nov + 1));
   auto* cnt = (unsigned long long*)pool.get("pw_counters", 256);
   if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise)");
-  unsigned long long cap = std::max<unsigned long long>(hit_cap_, 1ull << 16);
-  PwHit* hbuf = nullptr;
-  unsigned long long nh = 0;
+  int* tpair = (int*)pool.get("pw_tpair", sizeof(int) * (totalC + 1));
+  long long* coffs = (long long*)pool.get("pw_coffs", sizeof(long long) * (totalC + 1));
+  void* cscr = pool.get("pw_cscan", scan_scratch_bytes(totalC + 1));
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise candidates)");
+  cudaMemsetAsync(pairK, 0, sizeof(int) * (nov + 1), st);
+  cudaMemsetAsync(cnt, 0, 3 * sizeof(unsigned long long), st);
+  PwCandArgs ca{};
+  ca.nov = nov;
+  ca.coff = d_coff;
+  ca.totalC = totalC;
+  ca.cxy = d_cxy;
+  ca.b = d_bxy;
+  ca.nb = nb;
+  ca.g = g;
+  ca.gstart = gstart;
+  ca.gent = gent;
+  ca.lng = lng;
+  ca.nlong = nlong;
+  ca.fbox = fbox;
+  ca.pp = pp;
+  ca.rankB = rankB;
+  ca.rankC = rankC;
+  ca.rankCB = rankCB;
+  ca.uval = uval;
+  ca.tpair = tpair;
+  ca.coffs = coffs;
+  ca.nhits = &cnt[0];
+  ca.tested = &cnt[1];
+  ca.nraw = &cnt[2];
+  ca.pairK = pairK;
+  // 1. box-overlapping (overlay edge, base edge) pairs
+  long long ncand = 0;
+  if (totalC > 0) {
+    {
+      ::sbc::KProbe kp_("k_pw_cand_count", st, 40.0 * totalC);
+      k_pw_cand_count<<<grid_for(totalC + 1, 128), 128, 0, st>>>(ca);
+    }
+    exclusive_scan_i64(coffs, totalC + 1, cscr, st);
+    cudaMemcpyAsync(&ncand, coffs + totalC, sizeof(long long), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise candidates");
+  }
+  int2* cand = (int2*)pool.get("pw_cand", sizeof(int2) * (ncand + 1));
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise candidates)");
+  ca.cand = cand;
+  ca.ncand = ncand;
+  if (ncand > 0) {
+    ::sbc::KProbe kp_("k_pw_cand_fill", st, 40.0 * totalC + 8.0 * ncand);
+    k_pw_cand_fill<<<grid_for(totalC, 128), 128, 0, st>>>(ca);
+  }
+  // 2. the FP64 test of each
+  unsigned long long rawcap = std::max<unsigned long long>(hit_cap_, 1ull << 16);
+  unsigned long long nraw = 0;
   for (int attempt = 0; attempt < 2; ++attempt) {
-    hbuf = (PwHit*)pool.get("pw_hits", sizeof(PwHit) * cap);
+    ca.raw = (PwHit*)pool.get("pw_raw", sizeof(PwHit) * rawcap);
+    ca.rawcap = rawcap;
     if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise hits)");
-    cudaMemsetAsync(pairK, 0, sizeof(int) * (nov + 1), st);
-    cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), st);
-    PwCandArgs ca{nov, d_coff, totalC, d_cxy, d_bxy, nb, g, gstart, gent, lng, nlong, fbox, pp,
-                  rankB, rankC, rankCB, uval, hbuf, cap, &cnt[0], pairK, &cnt[1]};
-    if (totalC > 0) {
-      ::sbc::KProbe kp_("k_pw_candidates", st, 32.0 * totalC);
-      k_pw_candidates<<<grid_for(totalC, 128), 128, 0, st>>>(ca);
+    cudaMemsetAsync(&cnt[1], 0, 2 * sizeof(unsigned long long), st);
+    if (ncand > 0) {
+      ::sbc::KProbe kp_("k_pw_cand_test", st, 72.0 * ncand);
+      k_pw_cand_test<<<grid_for(ncand, 256), 256, 0, st>>>(ca);
     }
     unsigned long long hc[2];
-    cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(hc, &cnt[1], sizeof(hc), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise candidates");
-    nh = hc[0];
-    tested = (long long)hc[1];
-    if (nh <= cap) break;
-    cap = nh + nh / 4 + 1024;
+    tested = (long long)hc[0];
+    nraw = hc[1];
+    if (nraw <= rawcap) break;
+    rawcap = nraw + nraw / 4 + 1024;
   }
-  if (nh > cap) return pl_.fail(kEInternal, "pairwise hit count changed between passes");
-  hit_cap_ = std::max(hit_cap_, nh);
+  if (nraw > rawcap) return pl_.fail(kEInternal, "pairwise hit count changed between passes");
+  hit_cap_ = std::max(hit_cap_, nraw);
+  // 3. tree quantities and emission keys of the intersections
+  PwHit* hbuf = (PwHit*)pool.get("pw_hits", sizeof(PwHit) * (nraw + 1));
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (pairwise hits)");
+  ca.hits = hbuf;
+  ca.cap = nraw + 1;
+  unsigned long long nh = 0;
+  if (nraw > 0) {
+    {
+      ::sbc::KProbe kp_("k_pw_hit_tree", st, 120.0 * (double)nraw);
+      k_pw_hit_tree<<<grid_for((long long)nraw, 256), 256, 0, st>>>(ca, (long long)nraw);
+    }
+    cudaMemcpyAsync(&nh, &cnt[0], sizeof(nh), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise candidates");
+  }
   hits = (long long)nh;
   cudaMemcpyAsync(hstart, pairK, sizeof(int) * (nov + 1), cudaMemcpyDeviceToDevice, st);
   exclusive_scan_i32(hstart, nov + 1, sscr, st);
