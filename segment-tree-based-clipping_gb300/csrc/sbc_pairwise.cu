@@ -1098,25 +1098,55 @@ __device__ int pw_label_trace(SerialArgs& a, const PwPip& pipP) {
     }
   }
   __syncwarp();
-  // createResult2 (serial, on every lane)
+  // createResult2 (serial, on every lane).  Rings grow at their end only, so
+  // a traced vertex is appended to the ring pool (coordinates alone: nothing
+  // reads the other fields of ring nodes) and the ring is linked in pool
+  // order once it is closed.  A run node's vertices are copied by all lanes.
   {
+    Pool& R = a.R;
+    auto emit = [&](const Pool& p, int v, bool forward) -> bool {
+      if (!is_run(p, v)) {
+        if (R.n >= R.cap) {
+          a.rfull = 1;
+          return false;
+        }
+        R.x[R.n] = p.x[v];
+        R.y[R.n] = p.y[v];
+        ++R.n;
+        return true;
+      }
+      const int n = p.run[v] + 1, room = R.cap - R.n, m = n < room ? n : room;
+      for (int t = lane; t < m; t += 32) {
+        const int u = p.rv0[v] + (forward ? t : n - 1 - t);
+        R.x[R.n + t] = p.rxy[2 * u];
+        R.y[R.n + t] = p.rxy[2 * u + 1];
+      }
+      R.n += m;
+      if (m < n) {
+        a.rfull = 1;
+        return false;
+      }
+      return true;
+    };
     int It = 0;
     long long guard = 4LL * (P.n + Q.n) + 16;
     do {
       if (P.isect[It] && P.label[It] == L_CROSSING) {
-        int r = rnew(a);
+        const int r = rnew(a);
         if (r < 0) return 3;
+        const int rs = R.n;
         int sI = 0, I = It, sV = 0, V = I;
         P.isect[I] = 0;
         do {
           int status = side(a, sV).enex[V];
           tog(&status);
+          const bool fwd = (status == EX_EXIT) ^ a.unite;
           Pool* pv;
           do {
             pv = &side(a, sV);
-            V = ((status == EX_EXIT) ^ a.unite) ? pv->next[V] : pv->prev[V];
+            V = fwd ? pv->next[V] : pv->prev[V];
             pv->isect[V] = 0;
-            if (radd_node(a, r, *pv, V, (status == EX_EXIT) ^ a.unite, -1)) return 2;
+            if (!emit(*pv, V, fwd)) return 2;
             if (--guard < 0) return 2;
           } while (!(pv->enex[V] == status) && !(sV == sI && V == I));
           if (!(sV == sI && V == I)) {
@@ -1127,9 +1157,15 @@ __device__ int pw_label_trace(SerialArgs& a, const PwPip& pipP) {
             side(a, sV).isect[V] = 0;
           }
         } while (!(sV == sI && V == I));
+        for (int v = rs + lane; v < R.n; v += 32) {
+          R.next[v] = v + 1 == R.n ? rs : v + 1;
+          R.prev[v] = v == rs ? R.n - 1 : v - 1;
+        }
+        a.rroot[r] = rs;
       }
       It = P.next[It];
     } while (It != 0);
+    __syncwarp();
   }
   return 0;
 }
@@ -1556,14 +1592,34 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
     for (int q = 0; q <= w.re_nd[r]; ++q) {
       const int si = w.re_si[r] + q;
       if (w.spal[si] == -100) continue;
-      const int i = w.re_e[r] + w.re_pre[r] + q;
+      const int e = w.re_e[r], nd = w.re_nd[r];
+      const int i = e + w.re_pre[r] + q;
       const double cx = w.spx[si], cy = w.spy[si];
-      const int tm = (i - 1 == -1) ? nB - 1 : i - 1;
-      const int tp = (i + 1 == nB) ? 0 : i + 1;
+      // the slots before and after: the next sparse ones inside a run or
+      // across adjacent runs, else plain base vertices (wrapping at the ends)
       double pmx, pmy, ppx, ppy;
       int alm, nbm, alp, nbp;
-      info(tm, r, &pmx, &pmy, &alm, &nbm);
-      info(tp, r, &ppx, &ppy, &alp, &nbp);
+      auto sparse = [&](int s2, double* x, double* y, int* al, int* nbv) {
+        *x = w.spx[s2];
+        *y = w.spy[s2];
+        *al = w.spal[s2];
+        *nbv = w.spnb[s2];
+      };
+      auto plainv = [&](int vtx, double* x, double* y, int* al, int* nbv) {
+        *x = b[2 * vtx];
+        *y = b[2 * vtx + 1];
+        *al = -100;
+        *nbv = -100;
+      };
+      if (q > 0 || (e > 0 && r > 0 && w.re_e[r - 1] == e - 1)) sparse(si - 1, &pmx, &pmy, &alm, &nbm);
+      else if (e > 0) plainv(e - 1, &pmx, &pmy, &alm, &nbm);
+      else if (w.re_e[nr - 1] == nb - 1) sparse(w.re_si[nr] - 1, &pmx, &pmy, &alm, &nbm);
+      else plainv(nb - 1, &pmx, &pmy, &alm, &nbm);
+      if (q < nd || (e + 1 < nb && r + 1 < nr && w.re_e[r + 1] == e + 1))
+        sparse(si + 1, &ppx, &ppy, &alp, &nbp);
+      else if (e + 1 < nb) plainv(e + 1, &ppx, &ppy, &alp, &nbp);
+      else if (w.re_e[0] == 0) sparse(0, &ppx, &ppy, &alp, &nbp);
+      else plainv(0, &ppx, &ppy, &alp, &nbp);
       const int pMN = alm != -100 ? nbm - 1 : -100;
       const int pPN = alp != -100 ? nbp - 1 : -100;
       const int nId = w.spnb[si] - 1;
