@@ -199,9 +199,13 @@ int Pipeline::stage_setup(const double* d_bxy, const double* d_cxy, const int* c
                                                    d_flags);
   }
   unsigned long long hm[2];
+  unsigned hf = 0;
   cudaMemcpyAsync(hm, mm, 16, cudaMemcpyDeviceToHost, st_);
+  cudaMemcpyAsync(&hf, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st_);
   cudaStreamSynchronize(st_);
-  if (read_flags() & kFlagUndef) return fail(kEInput, "non-finite vertex coordinate");
+  if (hf & kFlagUndef) return fail(kEInput, "non-finite vertex coordinate");
+  key_lo = hm[0];
+  key_hi = hm[1];
   minI = key_to_double(hm[0]);
   maxI = key_to_double(hm[1]);
   return kOk;
@@ -308,7 +312,8 @@ int Pipeline::stage_elementary() {
     ::sbc::KProbe kp_("k_ele_keys", st_);
     k_ele_keys<<<grid_for(E, 256), 256, 0, st_>>>(e_s, e_e, E, keys, sidx);
   }
-  radix_sort_u64(keys, sidx, keys2, sidx2, n2, rscr, st_);
+  // every endpoint is a vertex x value: its key lies in the setup's [min, max]
+  radix_sort_u64_within(keys, sidx, keys2, sidx2, n2, key_lo, key_hi, rscr, st_);
   cudaMemsetAsync(vl, 0, sizeof(int) * (E + 1), st_);
   {
     ::sbc::KProbe kp_("k_vl_mark", st_);

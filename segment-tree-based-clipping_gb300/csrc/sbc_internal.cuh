@@ -210,6 +210,12 @@ void radix_sort_u32(unsigned* keys, unsigned* vals, unsigned* keys_tmp, unsigned
                     long long n, int key_bits, void* scratch, cudaStream_t st);
 void radix_sort_u64(unsigned long long* keys, unsigned* vals, unsigned long long* keys_tmp,
                     unsigned* vals_tmp, long long n, void* scratch, cudaStream_t st);
+// the same for keys known to lie in [lo, hi]: the digits above the highest bit
+// where lo and hi differ are constant, so no reduction (and no host round
+// trip) is needed to skip them
+void radix_sort_u64_within(unsigned long long* keys, unsigned* vals, unsigned long long* keys_tmp,
+                           unsigned* vals_tmp, long long n, unsigned long long lo,
+                           unsigned long long hi, void* scratch, cudaStream_t st);
 
 // number of this library's kernels launched by the process (any host thread)
 extern std::atomic<unsigned long long> g_launches;

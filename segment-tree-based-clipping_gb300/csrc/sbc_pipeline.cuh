@@ -78,6 +78,7 @@ class Pipeline {
   double* e_s = nullptr;
   double* e_e = nullptr;
   double minI = 0, maxI = 0;
+  unsigned long long key_lo = 0, key_hi = 0;  // order keys of minI and maxI
   // tree
   double* ea = nullptr;
   int epc = 0, numLeaves = 0, ts = 0, logL = 0;

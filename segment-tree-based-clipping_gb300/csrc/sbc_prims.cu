@@ -437,7 +437,7 @@ void radix_pass(const K* sk, const unsigned* sv, K* dk, unsigned* dv, long long 
 
 template <typename K>
 void radix_sort_impl(K* keys, unsigned* vals, K* keys_tmp, unsigned* vals_tmp, long long n,
-                     int key_bits, void* scratch, cudaStream_t st) {
+                     int key_bits, void* scratch, cudaStream_t st, const K* known_vary = nullptr) {
   if (n <= 1) return;
   // tile size: the largest of 4096 / 2048 / 1024 keys that still gives about
   // four CTAs per SM (152 SMs)
@@ -453,7 +453,9 @@ void radix_sort_impl(K* keys, unsigned* vals, K* keys_tmp, unsigned* vals_tmp, l
   // reduction (and a host round trip) finds the digits worth sorting.  For
   // 32-bit keys the caller's key_bits already bounds the passes.
   K vary = ~K(0);
-  if (sizeof(K) == 8) {
+  if (known_vary) {
+    vary = *known_vary;
+  } else if (sizeof(K) == 8) {
     K h_or = 0, h_and = ~K(0);
     cudaMemcpyAsync(d_or, &h_or, sizeof(K), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(d_and, &h_and, sizeof(K), cudaMemcpyHostToDevice, st);
@@ -506,6 +508,15 @@ void radix_sort_u32(unsigned* keys, unsigned* vals, unsigned* keys_tmp, unsigned
 void radix_sort_u64(unsigned long long* keys, unsigned* vals, unsigned long long* keys_tmp,
                     unsigned* vals_tmp, long long n, void* scratch, cudaStream_t st) {
   radix_sort_impl<unsigned long long>(keys, vals, keys_tmp, vals_tmp, n, 64, scratch, st);
+}
+
+void radix_sort_u64_within(unsigned long long* keys, unsigned* vals, unsigned long long* keys_tmp,
+                           unsigned* vals_tmp, long long n, unsigned long long lo,
+                           unsigned long long hi, void* scratch, cudaStream_t st) {
+  // keys in [lo, hi] share every bit above the highest bit where lo and hi differ
+  const unsigned long long d = lo ^ hi;
+  const unsigned long long vary = d ? (~0ull >> __builtin_clzll(d)) : 0ull;
+  radix_sort_impl<unsigned long long>(keys, vals, keys_tmp, vals_tmp, n, 64, scratch, st, &vary);
 }
 
 }  // namespace sbc
