@@ -7,6 +7,7 @@
 // keys are skipped (one OR/AND reduction decides).
 #include "sbc_internal.cuh"
 
+#include <cstdint>
 #include <cstdio>
 #include <mutex>
 
@@ -106,6 +107,49 @@ constexpr int kScanThreads = 512;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;  // 4096
 
+// a thread's kScanItems consecutive elements as 16-byte loads and stores
+// (the array 16-byte aligned, all items in range); else one by one
+template <typename T>
+__device__ __forceinline__ void scan_load(const T* d, long long base, long long n, bool vec,
+                                          T (&v)[kScanItems]) {
+  constexpr int nv = (int)(sizeof(T) * kScanItems / 16);
+  if (vec && base + kScanItems <= n) {
+    union {
+      uint4 u[nv];
+      T t[kScanItems];
+    } x;
+    const uint4* q = reinterpret_cast<const uint4*>(d + base);
+#pragma unroll
+    for (int k = 0; k < nv; ++k) x.u[k] = q[k];
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) v[i] = x.t[i];
+    return;
+  }
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) v[i] = (base + i < n) ? d[base + i] : T(0);
+}
+
+template <typename T>
+__device__ __forceinline__ void scan_store(T* d, long long base, long long n, bool vec,
+                                           const T (&v)[kScanItems]) {
+  constexpr int nv = (int)(sizeof(T) * kScanItems / 16);
+  if (vec && base + kScanItems <= n) {
+    union {
+      uint4 u[nv];
+      T t[kScanItems];
+    } x;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) x.t[i] = v[i];
+    uint4* q = reinterpret_cast<uint4*>(d + base);
+#pragma unroll
+    for (int k = 0; k < nv; ++k) q[k] = x.u[k];
+    return;
+  }
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i)
+    if (base + i < n) d[base + i] = v[i];
+}
+
 template <typename T>
 __device__ T block_exclusive_scan(T v, T* smem_warp, T* total) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -148,23 +192,23 @@ __global__ void k_scan_reduce(const T* __restrict__ d, long long n, T* __restric
 }
 
 template <typename T>
-__global__ void k_scan_apply(T* __restrict__ d, long long n, const T* __restrict__ offs) {
+__global__ void k_scan_apply(T* __restrict__ d, long long n, const T* __restrict__ offs, bool vec) {
   __shared__ T sw[32];
   long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
   T v[kScanItems];
+  scan_load(d, base, n, vec, v);
   T s = 0;
 #pragma unroll
-  for (int i = 0; i < kScanItems; ++i) {
-    v[i] = (base + i < n) ? d[base + i] : T(0);
-    s += v[i];
-  }
+  for (int i = 0; i < kScanItems; ++i) s += v[i];
   T ex = block_exclusive_scan<T>(s, sw, nullptr);
   T run = ex + (offs ? offs[blockIdx.x] : T(0));
+  T o[kScanItems];
 #pragma unroll
   for (int i = 0; i < kScanItems; ++i) {
-    if (base + i < n) d[base + i] = run;
+    o[i] = run;
     run += v[i];
   }
+  scan_store(d, base, n, vec, o);
 }
 
 template <typename T>
@@ -185,7 +229,7 @@ __device__ unsigned g_scan_error = 0;
 
 template <typename T>
 __global__ void __launch_bounds__(kScanThreads)
-k_scan_lb(T* __restrict__ d, long long n, unsigned long long* __restrict__ state) {
+k_scan_lb(T* __restrict__ d, long long n, unsigned long long* __restrict__ state, bool vec) {
   __shared__ T sw[32];
   __shared__ unsigned s_tile;
   __shared__ T s_prefix;
@@ -195,12 +239,10 @@ k_scan_lb(T* __restrict__ d, long long n, unsigned long long* __restrict__ state
   unsigned long long* ts = state + 1;
   const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
   T v[kScanItems];
+  scan_load(d, base, n, vec, v);
   T s = 0;
 #pragma unroll
-  for (int i = 0; i < kScanItems; ++i) {
-    v[i] = (base + i < n) ? d[base + i] : T(0);
-    s += v[i];
-  }
+  for (int i = 0; i < kScanItems; ++i) s += v[i];
   T tot;
   const T ex = block_exclusive_scan<T>(s, sw, &tot);
   if (threadIdx.x < 32) {
@@ -240,11 +282,13 @@ k_scan_lb(T* __restrict__ d, long long n, unsigned long long* __restrict__ state
   }
   __syncthreads();
   T run = ex + s_prefix;
+  T o[kScanItems];
 #pragma unroll
   for (int i = 0; i < kScanItems; ++i) {
-    if (base + i < n) d[base + i] = run;
+    o[i] = run;
     run += v[i];
   }
+  scan_store(d, base, n, vec, o);
 }
 
 template <typename T>
@@ -255,7 +299,8 @@ void scan_rec(T* d, long long n, T* scratch, cudaStream_t st) {
     auto* state = (unsigned long long*)scratch;
     cudaMemsetAsync(state, 0, sizeof(unsigned long long) * (tiles + 1), st);
     ::sbc::KProbe kp_("k_scan_lb", st, 2.0 * sizeof(T) * (double)n);
-    k_scan_lb<T><<<(unsigned)tiles, kScanThreads, 0, st>>>(d, n, state);
+    k_scan_lb<T><<<(unsigned)tiles, kScanThreads, 0, st>>>(d, n, state,
+                                                       ((uintptr_t)d & 15) == 0);
     return;
   }
   scan_multi(d, n, scratch, st);
@@ -268,7 +313,7 @@ void scan_multi(T* d, long long n, T* scratch, cudaStream_t st) {
   if (nb == 1) {
     {
       ::sbc::KProbe kp_("k_scan_apply", st);
-      k_scan_apply<T><<<1, kScanThreads, 0, st>>>(d, n, nullptr);
+      k_scan_apply<T><<<1, kScanThreads, 0, st>>>(d, n, nullptr, ((uintptr_t)d & 15) == 0);
     }
     return;
   }
@@ -280,7 +325,7 @@ void scan_multi(T* d, long long n, T* scratch, cudaStream_t st) {
   scan_multi<T>(sums, nb, scratch + ((nb + 63) / 64) * 64, st);
   {
     ::sbc::KProbe kp_("k_scan_apply", st);
-    k_scan_apply<T><<<(unsigned)nb, kScanThreads, 0, st>>>(d, n, sums);
+    k_scan_apply<T><<<(unsigned)nb, kScanThreads, 0, st>>>(d, n, sums, ((uintptr_t)d & 15) == 0);
   }
 }
 
