@@ -184,3 +184,40 @@ def test_pairwise_area_and_gradient(clipper):
         scale = max(np.abs(hc).max(), 1e-300) * w[i].item()
         assert np.abs(gc[coff[i]:coff[i + 1]] - w[i].item() * hc).max() <= 1e-11 * scale, i
     assert np.abs(gb - wb).max() <= 1e-11 * max(np.abs(wb).max(), 1e-300)
+
+
+def test_pairwise_touching_overlays(clipper):
+    """Overlays that touch the base exactly (vertices on its edges, an edge lying
+    along one of its edges, bounces from either side) without sharing an x value
+    with it, so they stay on the batched path: their labels take the rare
+    branches (chains of overlapping edges, bouncing vertices, split pairs).
+    Results and statuses must equal sbc_clip_pair's."""
+    import sbclip
+    base = np.array([[0.0, -8.0], [6.0, -6.0], [8.0, 0.0], [6.0, 6.0], [0.0, 8.0],
+                     [-6.0, 6.0], [-8.0, 0.0], [-6.0, -6.0]])
+    # edge (0,-8)-(6,-6): y = -8 + x/3; edge (6,-6)-(8,0): y = -6 + 3 (x - 6)
+    on1 = lambda x: [x, -8.0 + x / 3.0]
+    on2 = lambda x: [x, -6.0 + 3.0 * (x - 6.0)]
+    ovs = [
+        np.array([[2.0, -9.0], on1(3.0), [4.0, -9.5]]),             # bounce from outside
+        np.array([[2.0, -5.0], [4.0, -5.5], on1(3.0)]),             # bounce from inside
+        np.array([on1(1.5), on1(4.5), [4.5, -4.0], [1.5, -5.0]]),   # edge along the base's, inside
+        np.array([on1(1.5), on1(4.5), [4.5, -9.0], [1.5, -9.5]]),   # the same, outside
+        np.array([on1(1.5), on1(4.5), [4.5, -4.0], [2.5, -9.5]]),   # shared edge, then across
+        np.array([on1(3.0), [7.5, -7.5], on2(7.0)]),                # a corner outside the base
+        np.array([on1(3.0), on2(7.0), [4.5, -3.0]]),                # a corner cut inside
+        np.array([on1(1.5), on1(3.0), [2.25, -10.0]]),              # two vertices on one edge
+        np.array([[-1.0, -9.0], on1(3.0), [5.0, -9.0], [5.0, -4.0], [-1.0, -4.0]]),
+    ]
+    ovs += [o + [0.0, 0.0] for o in ovs[:4]]  # repeats in one call
+    got, st = clipper.clip_pairwise(base, ovs)
+    assert len(got) == len(ovs)
+    for i, c in enumerate(ovs):
+        try:
+            want = clipper.clip_pair(base, c)
+        except sbclip.SbcError as e:
+            assert st[i] == e.code, (i, st[i], e.code)
+            continue
+        assert st[i] == 0, (i, st[i])
+        assert rings_equal(got[i], want), i
+    assert clipper.pairwise_info()["fallback_pairs"] < len(ovs)

@@ -47,3 +47,31 @@ def test_union_pairwise_matches_pair_path(uc):
     finally:
         uc.set_pairwise_split(8192)
     assert all(rings_equal(a, b) for a, b in zip(got, got2))
+
+
+def test_union_pairwise_touching_overlays(uc):
+    """Overlays touching the base exactly (see the intersection version in
+    test_gpu_pairwise.py) in union mode: the pairwise engine against the pair
+    path, rings and statuses."""
+    import sbclip
+    base = np.array([[0.0, -8.0], [6.0, -6.0], [8.0, 0.0], [6.0, 6.0], [0.0, 8.0],
+                     [-6.0, 6.0], [-8.0, 0.0], [-6.0, -6.0]])
+    on1 = lambda x: [x, -8.0 + x / 3.0]
+    on2 = lambda x: [x, -6.0 + 3.0 * (x - 6.0)]
+    ovs = [
+        np.array([[2.0, -9.0], on1(3.0), [4.0, -9.5]]),
+        np.array([[2.0, -5.0], [4.0, -5.5], on1(3.0)]),
+        np.array([on1(1.5), on1(4.5), [4.5, -4.0], [1.5, -5.0]]),
+        np.array([on1(1.5), on1(4.5), [4.5, -9.0], [1.5, -9.5]]),
+        np.array([on1(3.0), [7.5, -7.5], on2(7.0)]),
+        np.array([on1(3.0), on2(7.0), [4.5, -3.0]]),
+    ]
+    got, st = uc.clip_pairwise(base, ovs)
+    for i, c in enumerate(ovs):
+        try:
+            want = uc.clip_pair(base, c)
+        except sbclip.SbcError as e:
+            assert st[i] == e.code, (i, st[i], e.code)
+            continue
+        assert st[i] == 0, (i, st[i])
+        assert rings_equal(got[i], want), i
