@@ -1292,6 +1292,75 @@ __device__ bool warp_alpha_sort(int s, int t, const int* alpha, const int* order
   return true;
 }
 
+// A13 for base run r (copyIntersectionsParallel for one edge): its slots,
+// then its records' positions in the merged list, walking the run's records
+// in α order (they never run past the run's own records)
+__device__ __forceinline__ void pw_fill_run(PwWork& w, const double* b, const int* ub,
+                                            const int* ut, int K, int r) {
+  const int e = w.re_e[r], s = w.re_s[r], pre = w.re_pre[r], si = w.re_si[r], nd = w.re_nd[r];
+  w.spx[si] = b[2 * e];
+  w.spy[si] = b[2 * e + 1];
+  w.spal[si] = -100;
+  w.spnb[si] = -100;
+  w.splab[si] = 0;
+  w.spnode[si] = -1;
+  for (int q = 1; q <= nd; ++q) {
+    w.spx[si + q] = w.spy[si + q] = 0.0;
+    w.spal[si + q] = w.spnb[si + q] = 0;
+    w.splab[si + q] = 0;
+    w.spnode[si + q] = -1;
+  }
+  int bid = s;
+  int lid = w.sB[bid];
+  const int t = ut[lid];
+  if (t == 2 || t == 4 || t == 6 || t == 8) {
+    w.spal[si] = w.aB[lid];
+    w.bNI[lid] = e + pre;
+    w.bSI[lid] = si;
+    if (bid < K - 1) lid = w.sB[++bid];
+  }
+  if ((ub[lid] >> 1) != e) return;
+  for (int q = 0; q < nd; ++q) {
+    w.spx[si + 1 + q] = w.isxy[2 * lid];
+    w.spy[si + 1 + q] = w.isxy[2 * lid + 1];
+    w.spal[si + 1 + q] = w.aB[lid];
+    w.bNI[lid] = pre + e + 1 + q;
+    w.bSI[lid] = si + 1 + q;
+    if (bid < K - 1) lid = w.sB[++bid];
+  }
+}
+
+// A13 for overlay edge e: its vertex slot, then its intersection slots
+__device__ __forceinline__ void pw_fill_edge(PwWork& w, const double* c, const int* uc,
+                                             const int* ut, int K, int e) {
+  const int vs = e + w.cND[e];
+  w.ixC[2 * vs] = c[2 * e];
+  w.ixC[2 * vs + 1] = c[2 * e + 1];
+  w.alC[vs] = -100;
+  w.nbC[vs] = -100;
+  const int s = w.cAll[e];
+  if (w.cAll[e + 1] == s) return;
+  auto entry = [&](int pos) { return w.csorted[w.sC[pos]]; };
+  int bid = s;
+  int lid = entry(bid);
+  const int t = ut[lid];
+  if (t == 3 || t == 4 || t == 5 || t == 7 || t == 8) {
+    w.alC[vs] = w.aC[lid];
+    w.cNI[lid] = vs;
+    if (bid < K - 1) lid = entry(++bid);
+  }
+  if ((uc[lid] >> 1) != e) return;
+  const int ns = w.cND[e], ne = w.cND[e + 1];
+  for (int q = 0; q < ne - ns; ++q) {
+    const int slot = ns + e + 1 + q;
+    w.ixC[2 * slot] = w.isxy[2 * lid];
+    w.ixC[2 * slot + 1] = w.isxy[2 * lid + 1];
+    w.alC[slot] = w.aC[lid];
+    w.cNI[lid] = slot;
+    if (bid < K - 1) lid = entry(++bid);
+  }
+}
+
 // Rows A9-A18 of one pair, run by all 32 lanes of a warp.  The serial steps
 // (the linked-list build of the base, labelling, tracing, clean-up) run on
 // every lane alike: the lanes read the same values, take the same branches
@@ -1475,70 +1544,18 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
     w.bSI[i] = -1;  // the sparse index of bNI[i] once a slot is written
   }
   __syncwarp();
-  // base runs (copyIntersectionsParallel per edge)
-  for (int r = lane; r < nr; r += 32) {
-    const int e = w.re_e[r], s = w.re_s[r], pre = w.re_pre[r], si = w.re_si[r];
-    w.spx[si] = b[2 * e];
-    w.spy[si] = b[2 * e + 1];
-    w.spal[si] = -100;
-    w.spnb[si] = -100;
-    w.splab[si] = 0;
-    w.spnode[si] = -1;
-    for (int q = 1; q <= w.re_nd[r]; ++q) {
-      w.spx[si + q] = w.spy[si + q] = 0.0;
-      w.spal[si + q] = w.spnb[si + q] = 0;
-      w.splab[si + q] = 0;
-      w.spnode[si + q] = -1;
-    }
-    int bid = s;
-    int lid = w.sB[bid];
-    const int t = ut[lid];
-    if (t == 2 || t == 4 || t == 6 || t == 8) {
-      w.spal[si] = w.aB[lid];
-      w.bNI[lid] = e + pre;
-      w.bSI[lid] = si;
-      if (bid < K - 1) lid = w.sB[++bid];
-    }
-    if ((ub[lid] >> 1) != e) continue;
-    for (int q = 0; q < w.re_nd[r]; ++q) {
-      w.spx[si + 1 + q] = w.isxy[2 * lid];
-      w.spy[si + 1 + q] = w.isxy[2 * lid + 1];
-      w.spal[si + 1 + q] = w.aB[lid];
-      w.bNI[lid] = pre + e + 1 + q;
-      w.bSI[lid] = si + 1 + q;
-      if (bid < K - 1) lid = w.sB[++bid];
-    }
+  // base runs (copyIntersectionsParallel per edge), in chunks of 32 runs
+  for (int r0 = 0; r0 < nr; r0 += 32) {
+    const int r = r0 + lane;
+    if (r < nr) pw_fill_run(w, b, ub, ut, K, r);
+    __syncwarp();
   }
   // overlay edges: the vertex slot, then the edge's intersection slots
-  for (int e = lane; e < nc; e += 32) {
-    const int vs = e + w.cND[e];
-    w.ixC[2 * vs] = c[2 * e];
-    w.ixC[2 * vs + 1] = c[2 * e + 1];
-    w.alC[vs] = -100;
-    w.nbC[vs] = -100;
-    const int s = w.cAll[e];
-    if (w.cAll[e + 1] == s) continue;
-    auto entry = [&](int pos) { return w.csorted[w.sC[pos]]; };
-    int bid = s;
-    int lid = entry(bid);
-    const int t = ut[lid];
-    if (t == 3 || t == 4 || t == 5 || t == 7 || t == 8) {
-      w.alC[vs] = w.aC[lid];
-      w.cNI[lid] = vs;
-      if (bid < K - 1) lid = entry(++bid);
-    }
-    if ((uc[lid] >> 1) != e) continue;
-    const int ns = w.cND[e], ne = w.cND[e + 1];
-    for (int q = 0; q < ne - ns; ++q) {
-      const int slot = ns + e + 1 + q;
-      w.ixC[2 * slot] = w.isxy[2 * lid];
-      w.ixC[2 * slot + 1] = w.isxy[2 * lid + 1];
-      w.alC[slot] = w.aC[lid];
-      w.cNI[lid] = slot;
-      if (bid < K - 1) lid = entry(++bid);
-    }
+  for (int e0 = 0; e0 < nc; e0 += 32) {
+    const int e = e0 + lane;
+    if (e < nc) pw_fill_edge(w, c, uc, ut, K, e);
+    __syncwarp();
   }
-  __syncwarp();
   // neighbours: the last record written to a slot wins (spnode and cWin hold
   // the winning record until the winners have stored)
   int si0;  // sparse index of slot 0, where records never written point
@@ -1586,13 +1603,23 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
       *nbv = -100;
     }
   };
-  // ---- A14 initial labels, one run per lane; the overlay slot takes the
-  // label of the last base slot naming it
-  for (int r = lane; r < nr && !bad; r += 32) {
-    for (int q = 0; q <= w.re_nd[r]; ++q) {
-      const int si = w.re_si[r] + q;
-      if (w.spal[si] == -100) continue;
-      const int e = w.re_e[r], nd = w.re_nd[r];
+  // ---- A14 initial labels, one sparse slot per lane (spnode holds each
+  // slot's run meanwhile); the overlay slot takes the label of the last base
+  // slot naming it.  Loops over lanes run in chunks closed by __syncwarp, so
+  // that lanes that branch apart join again every chunk.
+  for (int r0 = 0; r0 < nr; r0 += 32) {
+    const int r = r0 + lane;
+    if (r < nr) {
+      const int si0 = w.re_si[r], nd = w.re_nd[r];
+      for (int q = 0; q <= nd; ++q) w.spnode[si0 + q] = r;
+    }
+    __syncwarp();
+  }
+  for (int s0 = 0; s0 < nsp; s0 += 32) {
+    const int si = s0 + lane;
+    if (si < nsp && !bad && w.spal[si] != -100) {
+      const int r = w.spnode[si];
+      const int e = w.re_e[r], nd = w.re_nd[r], q = si - w.re_si[r];
       const int i = e + w.re_pre[r] + q;
       const double cx = w.spx[si], cy = w.spy[si];
       // the slots before and after: the next sparse ones inside a run or
@@ -1613,7 +1640,7 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
       };
       if (q > 0 || (e > 0 && r > 0 && w.re_e[r - 1] == e - 1)) sparse(si - 1, &pmx, &pmy, &alm, &nbm);
       else if (e > 0) plainv(e - 1, &pmx, &pmy, &alm, &nbm);
-      else if (w.re_e[nr - 1] == nb - 1) sparse(w.re_si[nr] - 1, &pmx, &pmy, &alm, &nbm);
+      else if (w.re_e[nr - 1] == nb - 1) sparse(nsp - 1, &pmx, &pmy, &alm, &nbm);
       else plainv(nb - 1, &pmx, &pmy, &alm, &nbm);
       if (q < nd || (e + 1 < nb && r + 1 < nr && w.re_e[r + 1] == e + 1))
         sparse(si + 1, &ppx, &ppy, &alp, &nbp);
@@ -1623,57 +1650,54 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
       const int pMN = alm != -100 ? nbm - 1 : -100;
       const int pPN = alp != -100 ? nbp - 1 : -100;
       const int nId = w.spnb[si] - 1;
-      int qt[2];
-      for (int sd = 0; sd < 2 && !bad; ++sd) {
-        int qq = sd == 0 ? nId - 1 : nId + 1;
-        if (qq == nQ) qq = 0;
-        else if (qq == -1) qq = nQ - 1;
-        if (qq < 0 || qq >= nQ) {
-          bad = true;
-          break;
-        }
+      // the overlay slots before and after nId: left (0), right (1), or the
+      // base neighbours' own slots (2, 3)
+      auto side_of = [&](int qq) -> int {
+        if (pMN != -100 && pMN == qq) return 2;
+        if (pPN != -100 && pPN == qq) return 3;
         const double qx = w.ixC[2 * qq], qy = w.ixC[2 * qq + 1];
-        int rr;
-        if (pMN != -100 && pMN == qq) rr = 2;
-        else if (pPN != -100 && pPN == qq) rr = 3;
-        else {
-          const double s1 = area3(qx, qy, pmx, pmy, cx, cy);
-          const double s2 = area3(qx, qy, cx, cy, ppx, ppy);
-          const double s3 = area3(pmx, pmy, cx, cy, ppx, ppy);
-          if (s3 > 0) rr = (s1 > 0 && s2 > 0) ? 0 : 1;
-          else rr = (s1 < 0 && s2 < 0) ? 1 : 0;
-        }
-        qt[sd] = rr;
-      }
-      if (bad) break;
-      const int qm = qt[0], qp = qt[1];
-      int lab;
-      if ((qm == 0 && qp == 1) || (qm == 1 && qp == 0)) lab = 1;
-      else if ((qm == 0 && qp == 0) || (qm == 1 && qp == 1)) lab = 2;
-      else if ((qp == 3 && qm == 1) || (qm == 3 && qp == 1)) lab = 3;
-      else if ((qp == 3 && qm == 0) || (qm == 3 && qp == 0)) lab = 4;
-      else if ((qp == 3 && qm == 2) || (qm == 3 && qp == 2)) lab = 5;
-      else if ((qm == 2 && qp == 1) || (qp == 2 && qm == 1)) lab = 6;
-      else if ((qm == 2 && qp == 0) || (qp == 2 && qm == 0)) lab = 7;
-      else lab = -102;
-      w.splab[si] = lab;
-      if (nId < 0 || nId >= nQ) {
+        const double s1 = area3(qx, qy, pmx, pmy, cx, cy);
+        const double s2 = area3(qx, qy, cx, cy, ppx, ppy);
+        const double s3 = area3(pmx, pmy, cx, cy, ppx, ppy);
+        if (s3 > 0) return (s1 > 0 && s2 > 0) ? 0 : 1;
+        return (s1 < 0 && s2 < 0) ? 1 : 0;
+      };
+      int qq0 = nId - 1, qq1 = nId + 1;
+      if (qq0 == nQ) qq0 = 0;
+      else if (qq0 == -1) qq0 = nQ - 1;
+      if (qq1 == nQ) qq1 = 0;
+      else if (qq1 == -1) qq1 = nQ - 1;
+      if (qq0 < 0 || qq0 >= nQ || qq1 < 0 || qq1 >= nQ) {
         bad = true;
-        break;
+      } else {
+        const int qm = side_of(qq0), qp = side_of(qq1);
+        int lab;
+        if ((qm == 0 && qp == 1) || (qm == 1 && qp == 0)) lab = 1;
+        else if ((qm == 0 && qp == 0) || (qm == 1 && qp == 1)) lab = 2;
+        else if ((qp == 3 && qm == 1) || (qm == 3 && qp == 1)) lab = 3;
+        else if ((qp == 3 && qm == 0) || (qm == 3 && qp == 0)) lab = 4;
+        else if ((qp == 3 && qm == 2) || (qm == 3 && qp == 2)) lab = 5;
+        else if ((qm == 2 && qp == 1) || (qp == 2 && qm == 1)) lab = 6;
+        else if ((qm == 2 && qp == 0) || (qp == 2 && qm == 0)) lab = 7;
+        else lab = -102;
+        w.splab[si] = lab;
+        if (nId < 0 || nId >= nQ) bad = true;
+        else atomicMax(&w.cWin[nId], i);  // slots come in increasing order: the last one wins
       }
-      atomicMax(&w.cWin[nId], i);  // slots come in increasing order: the last one wins
     }
+    __syncwarp();
   }
   if (warp_fail(bad)) return PS_FALLBACK;
-  for (int r = lane; r < nr; r += 32) {
-    for (int q = 0; q <= w.re_nd[r]; ++q) {
-      const int si = w.re_si[r] + q;
-      if (w.spal[si] == -100) continue;
+  for (int s0 = 0; s0 < nsp; s0 += 32) {
+    const int si = s0 + lane;
+    if (si < nsp && w.spal[si] != -100) {
+      const int r = w.spnode[si];
       const int nId = w.spnb[si] - 1;
-      if (w.cWin[nId] == w.re_e[r] + w.re_pre[r] + q) w.cWinSI[nId] = si;
+      if (w.cWin[nId] == w.re_e[r] + w.re_pre[r] + (si - w.re_si[r])) w.cWinSI[nId] = si;
     }
+    __syncwarp();
   }
-  __syncwarp();
+  for (int s = lane; s < nsp; s += 32) w.spnode[s] = -1;
   for (int q = lane; q < nQ; q += 32) w.labC[q] = w.cWin[q] >= 0 ? w.splab[w.cWinSI[q]] : 0;
   __syncwarp();
   // ---- A15 linked lists (copyToLinkedList, src/clip.cpp:606-695): the base's
@@ -1722,22 +1746,26 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
       P.rv0[v] = 0;
     };
     __syncwarp();
-    for (int r = lane; r < nr; r += 32) {
-      const int e = w.re_e[r], pe = r == 0 ? 0 : w.re_e[r - 1] + 1, si = w.re_si[r];
-      int v = w.re_s[r];
-      if (e > pe) {  // the stretch pe .. e-1; it is stretch number v - r - re_pre[r]
-        put(v, b[2 * pe], b[2 * pe + 1], 1, L_NONE, 0);
-        P.run[v] = e - pe - 1;
-        P.rv0[v] = pe;
-        w.runIds[v - r - w.re_pre[r]] = v;
-        ++v;
+    for (int r0 = 0; r0 < nr; r0 += 32) {
+      const int r = r0 + lane;
+      if (r < nr) {
+        const int e = w.re_e[r], pe = r == 0 ? 0 : w.re_e[r - 1] + 1, si = w.re_si[r];
+        int v = w.re_s[r];
+        if (e > pe) {  // the stretch pe .. e-1; it is stretch number v - r - re_pre[r]
+          put(v, b[2 * pe], b[2 * pe + 1], 1, L_NONE, 0);
+          P.run[v] = e - pe - 1;
+          P.rv0[v] = pe;
+          w.runIds[v - r - w.re_pre[r]] = v;
+          ++v;
+        }
+        put(v, b[2 * e], b[2 * e + 1], 1, w.splab[si], w.spal[si] != -100);
+        w.spnode[si] = v++;
+        for (int q = 1; q <= w.re_nd[r]; ++q) {
+          put(v, w.spx[si + q], w.spy[si + q], 0, w.splab[si + q], 1);
+          w.spnode[si + q] = v++;
+        }
       }
-      put(v, b[2 * e], b[2 * e + 1], 1, w.splab[si], w.spal[si] != -100);
-      w.spnode[si] = v++;
-      for (int q = 1; q <= w.re_nd[r]; ++q) {
-        put(v, w.spx[si + q], w.spy[si + q], 0, w.splab[si + q], 1);
-        w.spnode[si + q] = v++;
-      }
+      __syncwarp();
     }
     if (tail && lane == 0) {
       put(tot0, b[2 * pe_last], b[2 * pe_last + 1], 1, L_NONE, 0);
@@ -1847,8 +1875,9 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
   if (!__any_sync(kFullMask, odd)) {
     // node v = slot v; the first failing slot decides the status
     int first = INT_MAX;  // 4 * slot + 1 (undefined) or + 2 (pair pipeline)
-    for (int e = lane; e < nc; e += 32) {
-      const int vs = e + w.cND[e], ne = w.cND[e + 1] - w.cND[e];
+    for (int e0 = 0; e0 < nc; e0 += 32) {
+      const int e = e0 + lane;
+      const int vs = e < nc ? e + w.cND[e] : 0, ne = e < nc ? w.cND[e + 1] - w.cND[e] : -1;
       for (int q = 0; q <= ne; ++q) {
         const int v = vs + q;
         Q.x[v] = w.ixC[2 * v];
@@ -1875,6 +1904,7 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
         Q.nb[v] = w.spnode[si];
         atomicMax(&P.nb[w.spnode[si]], v);  // the last overlay node naming it wins
       }
+      __syncwarp();
     }
     first = __reduce_min_sync(kFullMask, first);
     __syncwarp();
