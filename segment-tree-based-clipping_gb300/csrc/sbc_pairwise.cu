@@ -1137,24 +1137,44 @@ __device__ int pw_label_trace(SerialArgs& a, const PwPip& pipP) {
         const int rs = R.n;
         int sI = 0, I = It, sV = 0, V = I;
         P.isect[I] = 0;
+        int enV = P.enex[V];
         do {
-          int status = side(a, sV).enex[V];
+          int status = enV;
           tog(&status);
           const bool fwd = (status == EX_EXIT) ^ a.unite;
-          Pool* pv;
+          Pool* pv = &side(a, sV);
+          // a node's fields, its successor among them, are all read before
+          // anything is stored (a byte store may alias them), so the next
+          // node's reads need not wait for this node's stores
+          int nx = fwd ? pv->next[V] : pv->prev[V];
+          int en, nbV;
           do {
-            pv = &side(a, sV);
-            V = fwd ? pv->next[V] : pv->prev[V];
+            V = nx;
+            en = pv->enex[V];
+            nbV = pv->nb[V];
+            nx = fwd ? pv->next[V] : pv->prev[V];
+            const bool run = is_run(*pv, V);
+            const double x = pv->x[V], y = pv->y[V];
             pv->isect[V] = 0;
-            if (!emit(*pv, V, fwd)) return 2;
+            if (!run) {
+              if (R.n >= R.cap) {
+                a.rfull = 1;
+                return 2;
+              }
+              R.x[R.n] = x;
+              R.y[R.n] = y;
+              ++R.n;
+            } else if (!emit(*pv, V, fwd)) {
+              return 2;
+            }
             if (--guard < 0) return 2;
-          } while (!(pv->enex[V] == status) && !(sV == sI && V == I));
+          } while (!(en == status) && !(sV == sI && V == I));
           if (!(sV == sI && V == I)) {
-            int nbv = side(a, sV).nb[V];
-            if (nbv < 0) return 2;
+            if (nbV < 0) return 2;
             sV = 1 - sV;
-            V = nbv;
+            V = nbV;
             side(a, sV).isect[V] = 0;
+            enV = side(a, sV).enex[V];
           }
         } while (!(sV == sI && V == I));
         for (int v = rs + lane; v < R.n; v += 32) {
@@ -2172,7 +2192,9 @@ __global__ void k_pw_pack(int nov, const long long* __restrict__ coff, int nb,
                           const int* __restrict__ pairK, PwArenas ar, const int* __restrict__ fast,
                           const long long* __restrict__ rpre, const long long* __restrict__ vpre,
                           long long* __restrict__ ring_off, double* __restrict__ xy) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  // one warp per pair, its lanes over the ring offsets and coordinates
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = (int)(t >> 5), lane = threadIdx.x & 31;
   if (p >= nov || !fast[p]) return;
   const long long r0 = rpre[p], v0 = vpre[p];
   const int nr = (int)(rpre[p + 1] - r0);
@@ -2180,15 +2202,14 @@ __global__ void k_pw_pack(int nov, const long long* __restrict__ coff, int nb,
   const PwCaps cp = pw_caps(nb, (int)(coff[p + 1] - coff[p]), pairK[p], ar.pass[p]);
   Carver cv{const_cast<unsigned char*>(ar.at(p)), 0};
   const PwWork w = pw_carve(cv, cp);
-  for (int r = 0; r < nr; ++r) ring_off[r0 + r] = v0 + w.roff[r];
+  for (int r = lane; r < nr; r += 32) ring_off[r0 + r] = v0 + w.roff[r];
   const int nv = w.roff[nr];
-  for (int i = 0; i < 2 * nv; ++i) xy[2 * v0 + i] = w.rxy[i];
+  for (int i = lane; i < 2 * nv; i += 32) xy[2 * v0 + i] = w.rxy[i];
 }
 
 }  // namespace
 
 // ------------------------------------------------------------------ host
-// resident warps of the per-pair kernel (the whole GPU), at most one per pair
 // one pipeline, stream and host thread taking big pairs
 struct PairwiseRunner::BigWorker {
   cudaStream_t st = nullptr;
@@ -2836,7 +2857,7 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
   {
     const PwArenas ar{arena0, aoff0, arena1, aoff1, pass};
     ::sbc::KProbe kp_("k_pw_pack", st);
-    k_pw_pack<<<grid_for(nov, 128), 128, 0, st>>>(nov, d_coff, nb, pairK, ar, d_fast, d_rpre,
+    k_pw_pack<<<grid_for(32LL * nov, 128), 128, 0, st>>>(nov, d_coff, nb, pairK, ar, d_fast, d_rpre,
                                                   d_vpre, ring_off, xy);
   }
   std::vector<long long> roff_h;
