@@ -570,7 +570,7 @@ __global__ void k_pw_cand_test(PwCandArgs A) {
     const double p1x = A.b[2 * be], p1y = A.b[2 * be + 1];
     const double p2x = A.b[2 * be2], p2y = A.b[2 * be2 + 1];
     lsmf = lsmf_d(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y);
-    if (lsmf) ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
+    if (lsmf) ty = seg_isect<true>(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
   }
   const unsigned tm = __ballot_sync(kFullMask, lsmf);
   if ((threadIdx.x & 31) == 0 && tm) atomicAdd(A.tested, (unsigned long long)__popc(tm));
@@ -2245,18 +2245,26 @@ unsigned PairwiseRunner::pair_grid(int nov, bool reserve) {
 // grid cell width.
 int PairwiseRunner::autotune(const double* d_bxy, int nb, int nov, const double* d_cxy,
                              const long long* d_coff, cudaStream_t st, double* best_ms) {
+  // the better of two runs: one run's time varies by several percent
   auto timed = [&](double* ms) -> int {
-    const auto t0 = std::chrono::steady_clock::now();
-    const int rc = run(d_bxy, nb, nov, d_cxy, d_coff, st);
-    *ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    return rc;
+    *ms = 1e300;
+    for (int k = 0; k < 2; ++k) {
+      const auto t0 = std::chrono::steady_clock::now();
+      const int rc = run(d_bxy, nb, nov, d_cxy, d_coff, st);
+      if (rc) return rc;
+      if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "pairwise autotune");
+      const double t =
+          std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      *ms = std::min(*ms, t);
+    }
+    return kOk;
   };
   double ms = 0;
   int rc = timed(&ms);  // warm-up: buffers grow to size
   if (rc) return rc;
   int best_split = big_k;
   double best_cell = cell_factor, best = 1e300;
-  for (int split : {2048, 4096, 6144, 8192, 12288, 16384, 32768}) {
+  for (int split : {2048, 4096, 6144, 8192, 10240, 12288, 14336, 16384, 32768}) {
     big_k = split;
     rc = timed(&ms);
     if (rc) return rc;

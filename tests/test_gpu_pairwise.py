@@ -95,7 +95,7 @@ def test_pairwise_autotune(clipper):
     try:
         t = clipper.autotune_pairwise_device(tb.data_ptr(), len(base), len(ovs), tc.data_ptr(),
                                              to.data_ptr())
-        assert t["split"] in (2048, 4096, 6144, 8192, 12288, 16384, 32768)
+        assert t["split"] in (2048, 4096, 6144, 8192, 10240, 12288, 14336, 16384, 32768)
         assert t["cell_factor"] in (0.5, 1.0, 2.0) and t["best_ms"] > 0
         got, st = clipper.clip_pairwise(base, ovs)
         assert (st == 0).all()
