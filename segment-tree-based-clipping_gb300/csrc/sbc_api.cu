@@ -87,9 +87,13 @@ struct sbc_ctx {
   long long stats[SBC_STAT_NUM] = {0};
   sbc::BatchRunner* br = nullptr;
   sbc::PairwiseRunner* pw = nullptr;
-  // host copies of batched ring results
-  std::vector<long long> hb_pair_ring, hb_ring_off;
-  std::vector<double> hb_xy;
+  // host copies of batched ring results (offsets and coordinates pinned and
+  // only grown: nothing is filled before the copies land)
+  std::vector<long long> hb_pair_ring;
+  long long* hb_ring_off = nullptr;
+  size_t hb_ring_off_cap = 0;
+  double* hb_xy = nullptr;
+  size_t hb_xy_cap = 0;
   std::vector<int> hb_status;
   float phase_ms[8] = {0};
 };
@@ -196,6 +200,8 @@ void sbc_destroy(sbc_ctx* c) {
     if (p) cudaFreeHost(p);
   for (auto p : c->h_xy)
     if (p) cudaFreeHost(p);
+  if (c->hb_ring_off) cudaFreeHost(c->hb_ring_off);
+  if (c->hb_xy) cudaFreeHost(c->hb_xy);
   if (c->d_in) cudaFree(c->d_in);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
@@ -603,17 +609,19 @@ extern "C" int sbc_clip_batch(sbc_ctx* c, const sbc_batch* b, sbc_batch_rings* o
   if (rc) return rc;
   const int np = b->npairs;
   c->hb_pair_ring.assign((size_t)np + 1, 0);
-  c->hb_ring_off.assign((size_t)dr.nrings + 1, 0);
-  c->hb_xy.assign((size_t)2 * dr.nverts + 1, 0.0);
   c->hb_status.assign((size_t)np + 1, 0);
+  if (!ensure_pinned(c->hb_ring_off, c->hb_ring_off_cap, (size_t)dr.nrings + 1) ||
+      !ensure_pinned(c->hb_xy, c->hb_xy_cap, (size_t)2 * dr.nverts + 1))
+    return set_err(c, SBC_ENOMEM, "pinned host allocation failed (batch rings)");
+  c->hb_ring_off[0] = 0;
   if (np > 0) {
     cudaMemcpyAsync(c->hb_pair_ring.data(), dr.pair_ring, sizeof(long long) * (np + 1),
                     cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(c->hb_ring_off.data(), dr.ring_off, sizeof(long long) * (dr.nrings + 1),
+    cudaMemcpyAsync(c->hb_ring_off, dr.ring_off, sizeof(long long) * (dr.nrings + 1),
                     cudaMemcpyDeviceToHost, st);
     if (dr.nverts > 0)
-      cudaMemcpyAsync(c->hb_xy.data(), dr.xy, sizeof(double) * 2 * dr.nverts,
-                      cudaMemcpyDeviceToHost, st);
+      cudaMemcpyAsync(c->hb_xy, dr.xy, sizeof(double) * 2 * dr.nverts, cudaMemcpyDeviceToHost,
+                      st);
     cudaMemcpyAsync(c->hb_status.data(), dr.status, sizeof(int) * np, cudaMemcpyDeviceToHost, st);
   }
   rc = cuda_check(c, cudaStreamSynchronize(st), "batch rings");
@@ -622,8 +630,8 @@ extern "C" int sbc_clip_batch(sbc_ctx* c, const sbc_batch* b, sbc_batch_rings* o
   out->nrings = dr.nrings;
   out->nverts = dr.nverts;
   out->pair_ring = c->hb_pair_ring.data();
-  out->ring_off = c->hb_ring_off.data();
-  out->xy = c->hb_xy.data();
+  out->ring_off = c->hb_ring_off;
+  out->xy = c->hb_xy;
   out->status = c->hb_status.data();
   return SBC_OK;
 }
@@ -690,18 +698,20 @@ extern "C" int sbc_clip_pairwise(sbc_ctx* c, const sbc_pairwise_job* j, sbc_batc
   sbc_batch_rings dr;
   rc = sbc_clip_pairwise_device(c, &d, &dr, st);
   if (rc) return rc;
-  c->hb_ring_off.assign((size_t)dr.nrings + 1, 0);
-  c->hb_xy.assign((size_t)2 * dr.nverts + 1, 0.0);
+  if (!ensure_pinned(c->hb_ring_off, c->hb_ring_off_cap, (size_t)dr.nrings + 1) ||
+      !ensure_pinned(c->hb_xy, c->hb_xy_cap, (size_t)2 * dr.nverts + 1))
+    return set_err(c, SBC_ENOMEM, "pinned host allocation failed (pairwise rings)");
+  c->hb_ring_off[0] = 0;
   c->hb_pair_ring = c->pw->h_pair_ring;
   c->hb_status = c->pw->h_status;
   c->hb_pair_ring.resize((size_t)nov + 1, 0);
   c->hb_status.resize((size_t)nov + 1, 0);
   if (nov > 0) {
-    cudaMemcpyAsync(c->hb_ring_off.data(), dr.ring_off, sizeof(long long) * (dr.nrings + 1),
+    cudaMemcpyAsync(c->hb_ring_off, dr.ring_off, sizeof(long long) * (dr.nrings + 1),
                     cudaMemcpyDeviceToHost, st);
     if (dr.nverts > 0)
-      cudaMemcpyAsync(c->hb_xy.data(), dr.xy, sizeof(double) * 2 * dr.nverts,
-                      cudaMemcpyDeviceToHost, st);
+      cudaMemcpyAsync(c->hb_xy, dr.xy, sizeof(double) * 2 * dr.nverts, cudaMemcpyDeviceToHost,
+                      st);
   }
   rc = cuda_check(c, cudaStreamSynchronize(st), "pairwise rings");
   if (rc) return rc;
@@ -709,8 +719,8 @@ extern "C" int sbc_clip_pairwise(sbc_ctx* c, const sbc_pairwise_job* j, sbc_batc
   out->nrings = dr.nrings;
   out->nverts = dr.nverts;
   out->pair_ring = c->hb_pair_ring.data();
-  out->ring_off = c->hb_ring_off.data();
-  out->xy = c->hb_xy.data();
+  out->ring_off = c->hb_ring_off;
+  out->xy = c->hb_xy;
   out->status = c->hb_status.data();
   return SBC_OK;
 }
