@@ -414,15 +414,17 @@ def run_small_pairs(args, rank: int, world: int):
     prof_b = sbclip.profile_end(with_bytes=True)
     graph.close()
     prof = {k: (v[0], v[1]) for k, v in prof_b.items()}
-    # end to end through the host-array C ABI: inputs copied in, areas and
-    # gradients copied out (the host backward call runs its own forward)
+    # end to end through the host-array C ABI (sbc_area_forward and
+    # sbc_area_backward on the packed host arrays): inputs copied in, areas
+    # and gradients copied out (the host backward call runs its own forward)
     e2e_t = []
+    ones = np.ones(n)
     for _ in range(max(args.steps, 1)):
         flush.fill_(1.0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        clip.area_forward(bases, ovs)
-        clip.area_backward(bases, ovs, np.ones(n))
+        clip.area_forward_packed(bxy, boff, cxy, coff)
+        clip.area_backward_packed(bxy, boff, cxy, coff, ones)
         e2e_t.append((time.perf_counter() - t0) * 1e3)
     in_bytes = 16 * (int(boff[-1]) + int(coff[-1])) + 16 * (n + 1)
     e2e = {"value": n * world / (float(np.mean(e2e_t)) * 1e-3), "unit": "pairs/s",
