@@ -1507,21 +1507,29 @@ __device__ int pw_clip_pair(const PwPairArgs& A, int p, const PwCaps& cp, PwWork
   // (stable insertion for short runs on one lane; a long run -- an overlay
   // edge across a jagged base can hold hundreds of crossings -- is sorted by
   // the whole warp)
+  // (the run, at most kWarpSortMin long, holds positions s..t-1; its keys
+  // are copied to the lane's own array first)
   auto isort = [&](int s, int t, const int* alpha, const int* order, int* sorted) -> bool {
-    for (int i = s; i < t; ++i)
-      if (alpha[order ? order[i] : i] < 0) return false;
-    for (int i = s + 1; i < t; ++i) {
-      const int pv = sorted[i];
-      const int kp = alpha[order ? order[pv] : pv] % 1000000000;
+    int key[kWarpSortMin], val[kWarpSortMin];
+    const int m = t - s;
+    for (int i = 0; i < m; ++i) {
+      const int a = alpha[order ? order[s + i] : s + i];
+      if (a < 0) return false;
+      key[i] = a % 1000000000;
+      val[i] = s + i;
+    }
+    for (int i = 1; i < m; ++i) {
+      const int kp = key[i], pv = val[i];
       int j = i;
-      while (j > s) {
-        const int qv = sorted[j - 1];
-        if (alpha[order ? order[qv] : qv] % 1000000000 <= kp) break;
-        sorted[j] = qv;
+      while (j > 0 && key[j - 1] > kp) {
+        key[j] = key[j - 1];
+        val[j] = val[j - 1];
         --j;
       }
-      sorted[j] = pv;
+      key[j] = kp;
+      val[j] = pv;
     }
+    for (int i = 0; i < m; ++i) sorted[s + i] = val[i];
     return true;
   };
   bool bad = false;
