@@ -2580,9 +2580,9 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
     }
   }
   // ---- pairs with many intersections take the pair pipeline's data-parallel
-  // rows A9-A18 on these records (no tree); the rest run one thread per pair,
-  // on a second stream at the same time.  Then pairs that ran out of ring
-  // room run again with full room.
+  // rows A9-A18 on these records (no tree), on worker streams; the rest run
+  // one warp per pair on a second stream at the same time.  Then pairs that
+  // ran out of ring room run again with full room.
   long long* aoff0 = (long long*)pool.get("pw_aoff0", sizeof(long long) * (nov + 1));
   long long* aoff1 = (long long*)pool.get("pw_aoff1", sizeof(long long) * (nov + 1));
   int* pass = (int*)pool.get("pw_pass", sizeof(int) * (nov + 1));

@@ -271,7 +271,7 @@ class PairwiseRunner {
   std::vector<std::unique_ptr<BigWorker>> workers_;
   Pipeline& pl_;
   unsigned long long hit_cap_ = 0;
-  cudaStream_t st2_ = nullptr;      // the one-thread-per-pair kernel's stream
+  cudaStream_t st2_ = nullptr;      // the per-pair kernel's stream
   cudaEvent_t ev_[2] = {nullptr, nullptr};
   std::vector<int> order_h;
   unsigned pair_blocks_ = 0;
