@@ -409,7 +409,7 @@ __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc,
       const double q2x = bvx(c, nc, j + 1), q2y = bvy(c, nc, j + 1);
       if (lsmf_d(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y)) {
         double al, bt;
-        const int ty = seg_isect<true>(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
+        const int ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
         unsigned long long key;
         if (ty && emission_s(be, nb + j, 2 * j, w, logL, &key) > 0) {
           // out of room: only counted, for the retry's capacity
@@ -492,7 +492,7 @@ __device__ PairResult clip_pair_back(const double* b, int nb, const double* c, i
     const double q1x = bvx(c, nc, ci), q1y = bvy(c, nc, ci);
     const double q2x = bvx(c, nc, ci + 1), q2y = bvy(c, nc, ci + 1);
     double al = 0.0, bt = 0.0;
-    const int ty = seg_isect<true>(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
+    const int ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
     double x = 0.0, y = 0.0;
     if (ty == 1) {
       const double oma = dsub(1.0, al);

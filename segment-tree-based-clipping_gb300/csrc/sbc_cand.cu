@@ -571,7 +571,7 @@ k_pair_exact(long long n, const int2* __restrict__ pairs, const int* __restrict_
       const double* pb = bP + e.x;
       const double* pc = cP + e.y;
       double al, be;
-      ty = seg_isect<true>(pb[0], pb[1], pb[2], pb[3], pc[0], pc[1], pc[2], pc[3], &al, &be);
+      ty = seg_isect(pb[0], pb[1], pb[2], pb[3], pc[0], pc[1], pc[2], pc[3], &al, &be);
       if (ty != 0) {
         const unsigned cnt = emission(e.z, e.w, e.y, lr, aft, bef, logL, &key);
         hit = cnt > 0;

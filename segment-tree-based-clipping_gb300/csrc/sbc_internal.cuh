@@ -61,20 +61,6 @@ __device__ __forceinline__ double area3(double px, double py, double qx, double 
 // Edge-pair classification, lineSegmentIntersection(2)
 // (p_seg_tree/oacc_segment_tree.cpp:5426-5611).  Returns the type 0..8 and
 // the parameters alpha (on P) and beta (on Q).
-// The quotient n / d (d != 0) provably rounds outside [-eps, 1 - eps): its
-// exact value is above 2, or below -4 eps (up to the rounding of 4 eps d), so
-// the rounded division is too.  Used to skip the divisions of pairs that
-// cannot be classified as intersecting.
-__device__ __forceinline__ bool quot_outside(double n, double d) {
-  const double m = dmul(-4.0 * kEps, d);
-  return d > 0.0 ? (n > dmul(2.0, d) || n < m) : (d < 0.0 && (n < dmul(2.0, d) || n > m));
-}
-
-// lineSegmentIntersection.  With kEarly, a pair whose alpha or beta provably
-// falls outside [-eps, 1 - eps) returns 0 before the divisions, without
-// writing alpha and beta (the type is the same; callers that read alpha and
-// beta only for nonzero types use it).
-template <bool kEarly = false>
 __device__ __forceinline__ int seg_isect(double p1x, double p1y, double p2x, double p2y,
                                          double q1x, double q1y, double q2x, double q2y,
                                          double* alpha, double* beta) {
@@ -82,13 +68,10 @@ __device__ __forceinline__ int seg_isect(double p1x, double p1y, double p2x, dou
   double AP2 = area3(p2x, p2y, q1x, q1y, q2x, q2y);
   double d = dsub(AP1, AP2);
   if (fabs(d) > kEps) {
-    if (kEarly && quot_outside(AP1, d)) return 0;
     double AQ1 = area3(q1x, q1y, p1x, p1y, p2x, p2y);
     double AQ2 = area3(q2x, q2y, p1x, p1y, p2x, p2y);
-    const double e = dsub(AQ1, AQ2);
-    if (kEarly && quot_outside(AQ1, e)) return 0;
     double a = ddiv(AP1, d);
-    double b = ddiv(AQ1, e);
+    double b = ddiv(AQ1, dsub(AQ1, AQ2));
     *alpha = a;
     *beta = b;
     bool a01 = false, a0 = false, b01 = false, b0 = false;

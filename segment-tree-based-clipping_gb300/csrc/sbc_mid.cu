@@ -180,7 +180,7 @@ __global__ void k_records(const int* __restrict__ ub, const int* __restrict__ uc
   const double* b = bP + ub[j];
   const double* c = cP + uc[j];
   double al = 0.0, be = 0.0;
-  int ty = seg_isect<true>(b[0], b[1], b[2], b[3], c[0], c[1], c[2], c[3], &al, &be);
+  int ty = seg_isect(b[0], b[1], b[2], b[3], c[0], c[1], c[2], c[3], &al, &be);
   double x = 0.0, y = 0.0;
   if (ty == 1) {
     // (1-alpha)*b1 + alpha*b2, mulScalar/add (:5349-5363)

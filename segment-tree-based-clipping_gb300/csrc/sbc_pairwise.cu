@@ -570,7 +570,7 @@ __global__ void k_pw_cand_test(PwCandArgs A) {
     const double p1x = A.b[2 * be], p1y = A.b[2 * be + 1];
     const double p2x = A.b[2 * be2], p2y = A.b[2 * be2 + 1];
     lsmf = lsmf_d(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y);
-    if (lsmf) ty = seg_isect<true>(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
+    if (lsmf) ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
   }
   const unsigned tm = __ballot_sync(kFullMask, lsmf);
   if ((threadIdx.x & 31) == 0 && tm) atomicAdd(A.tested, (unsigned long long)__popc(tm));
