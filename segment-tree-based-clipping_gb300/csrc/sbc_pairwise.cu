@@ -2760,8 +2760,20 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
       }
       cudaStreamSynchronize(W.st);
     };
+    for (int w = 0; w < nw; ++w) {
+      workers_[w]->rc = 0;
+      workers_[w]->msg.clear();
+    }
     std::vector<std::thread> th;
-    for (int w = 1; w < nw; ++w) th.emplace_back(work, std::ref(*workers_[w]));
+    for (int w = 1; w < nw; ++w) {
+      // a thread that cannot be started leaves its share to the others (the
+      // queue is shared)
+      try {
+        th.emplace_back(work, std::ref(*workers_[w]));
+      } catch (...) {
+        break;
+      }
+    }
     work(*workers_[0]);
     for (auto& t : th) t.join();
     for (int w = 0; w < nw; ++w)
