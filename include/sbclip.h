@@ -117,6 +117,11 @@ int sbc_phase_times(const sbc_ctx* ctx, float* out_ms, int n);
 #define SBC_ARR_MERGED_CNB 11
 #define SBC_ARR_LABEL_B 12
 #define SBC_ARR_LABEL_C 13
+/* tree arrays of the last call (overlay-independent) */
+#define SBC_ARR_ELEMENTARY 14  /* double: the padded elementary points (2^k+1) */
+#define SBC_ARR_LEAF_AFTER 15  /* int per edge: leaf node of its end-list entry from its end, or -1 */
+#define SBC_ARR_LEAF_BEFORE 16 /* int per edge: leaf node of its entry from its start, or -1 */
+#define SBC_ARR_LEAF_RANGE 17  /* int pairs per edge: leaves [l, r1) its cover lists span */
 int sbc_debug_array(sbc_ctx* ctx, int which, void* host_dst, long long cap, long long* count);
 
 /* Edge-pair classification of n pairs (p1,p2,q1,q2 as 8 doubles per pair,

@@ -30,7 +30,11 @@ Recipe (nothing is written outside oracle/_ref/):
    ``segment_tree.h:150-156``); zero-filling makes those reads defined and the
    run deterministic.
 4. ``g++ -O2 -fopenmp -ffp-contract=off`` with the CCCL Thrust host headers of
-   the CUDA toolkit.  ``-ffp-contract=off`` keeps every FP64 expression
+   the CUDA toolkit.
+5. Foster's sequential Greiner-Hormann code, the reference's own baseline
+   (``lib/optimizedFostersAlgorithm/polyclip.cpp`` with its headers), staged
+   unpatched and compiled as shipped (``g++ -O2 -std=c++11``) into
+   ``oracle/_ref/foster``: ``foster [-union] P.poly Q.poly R.poly``.  ``-ffp-contract=off`` keeps every FP64 expression
    unfused on hosts whose compilers contract by default (aarch64), matching an
    x86-64 ``-O2`` build.
 
@@ -64,6 +68,13 @@ FILES = [
     "foster/polyclip.h",
     "foster/polygon.h",
     "foster/point2D.h",
+]
+
+FOSTER_FILES = [
+    "lib/optimizedFostersAlgorithm/polyclip.cpp",
+    "lib/optimizedFostersAlgorithm/point2D.h",
+    "lib/optimizedFostersAlgorithm/polygon.h",
+    "lib/optimizedFostersAlgorithm/readSCPolygon.h",
 ]
 
 DUMP_HELPERS = r'''
@@ -152,7 +163,7 @@ PATCHES = [
 def stage(ref: Path) -> None:
     if STAGE.exists():
         shutil.rmtree(STAGE)
-    for rel in FILES:
+    for rel in FILES + FOSTER_FILES:
         dst = STAGE / rel
         dst.parent.mkdir(parents=True, exist_ok=True)
         shutil.copyfile(ref / rel, dst)
@@ -188,6 +199,15 @@ def compile_ref() -> Path:
     return exe
 
 
+def compile_foster() -> Path | None:
+    src = STAGE / "lib/optimizedFostersAlgorithm/polyclip.cpp"
+    if not src.exists():
+        return None
+    exe = OUT / "foster"
+    subprocess.run(["g++", "-O2", "-w", "-std=c++11", str(src), "-o", str(exe)], check=True)
+    return exe
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--ref", default=os.environ.get("SBC_REFERENCE_DIR", "/root/reference"))
@@ -201,6 +221,9 @@ def main(argv=None) -> int:
         return 2
     exe = compile_ref()
     print(exe)
+    fexe = compile_foster()
+    if fexe:
+        print(fexe)
     return 0
 
 

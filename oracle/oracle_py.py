@@ -8,6 +8,7 @@ import ctypes
 import os
 import subprocess
 import tempfile
+import time
 from pathlib import Path
 
 import numpy as np
@@ -15,6 +16,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_build" / "libsbc_oracle.so"
 REF_EXE = HERE / "_ref" / "seg"
+FOSTER_EXE = HERE / "_ref" / "foster"
 
 ARRAYS = [
     "raw_b", "raw_c", "raw_t", "uniq_b", "uniq_c", "uniq_t",
@@ -24,6 +26,7 @@ ARRAYS = [
 ]
 REAL_ARRAYS = {"isect_xy", "merged_bxy", "merged_cxy", "ring_xy"}
 STATS = ["edges", "elem_count", "tree_size", "cover_total", "leaf_end_total"]
+TREE_ARRAYS = ["ea", "leaf_off", "leaf_edge", "cov_off", "cov_edge"]
 
 
 def build_oracle_lib() -> Path:
@@ -58,6 +61,10 @@ def lib():
         L.sbco_stat.restype = ctypes.c_long
         L.sbco_stat.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.sbco_free.argtypes = [ctypes.c_void_p]
+        L.sbco_tree_len.restype = ctypes.c_long
+        L.sbco_tree_len.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.sbco_tree_data.restype = ctypes.c_void_p
+        L.sbco_tree_data.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.sbco_segment_intersection.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_void_p] * 2
         _lib = L
     return _lib
@@ -83,7 +90,14 @@ def clip(base: np.ndarray, overlays, union: bool = False) -> dict:
         st = L.sbco_status(run)
         if st != 0:
             raise OracleError(st, L.sbco_message(run).decode())
-        out = {"stats": {n: L.sbco_stat(run, i) for i, n in enumerate(STATS)}, "overlays": []}
+        out = {"stats": {n: L.sbco_stat(run, i) for i, n in enumerate(STATS)}, "overlays": [],
+               "tree": {}}
+        for w, name in enumerate(TREE_ARRAYS):
+            n = L.sbco_tree_len(run, w)
+            ptr = L.sbco_tree_data(run, w)
+            ct = ctypes.c_double if name == "ea" else ctypes.c_int
+            a = np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ct)), (max(n, 1),))[:n]
+            out["tree"][name] = a.copy()
         for ov in range(1, len(ovs) + 1):
             d = {}
             for w, name in enumerate(ARRAYS):
@@ -191,3 +205,63 @@ def run_reference(base: np.ndarray, overlays, threads: int = 1, precision: int =
                         d[name] = np.array(txt, dtype=dt) if txt else np.zeros(0, dt)
                 dumps[i + 1] = d
         return {"rings": rings, "time_line": time_line, "dumps": dumps, "stdout": p.stdout}
+
+
+def _clip_one(args):
+    base, overlay, union = args
+    try:
+        return 0, rings_of(clip(base, [overlay], union=union)["overlays"][0])
+    except OracleError as e:
+        return e.status, []
+
+
+def clip_pairs_parallel(pairs, threads: int | None = None, union: bool = False):
+    """[(status, rings)] of the restatement on every (base, overlay) pair, on
+    `threads` host threads (default: all host cores).  ctypes releases the
+    GIL for the C calls, and the restatement keeps no state between calls
+    but the union switch, which is the same for every pair here."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    lib()
+    args = [(np.ascontiguousarray(b, np.float64), np.ascontiguousarray(c, np.float64), union)
+            for b, c in pairs]
+    n = max(1, min(threads or os.cpu_count() or 1, len(args)))
+    if n == 1:
+        return [_clip_one(a) for a in args]
+    with ThreadPoolExecutor(n) as ex:
+        return list(ex.map(_clip_one, args))
+
+
+# ---------------------------------------------------------------------------
+# Foster's sequential code (the reference's own baseline)
+# ---------------------------------------------------------------------------
+
+def foster_available() -> bool:
+    return FOSTER_EXE.exists()
+
+
+def write_poly_components(path, comps) -> None:
+    """Foster's .poly format: `x y,` per vertex, `;` after each component."""
+    with open(path, "w") as f:
+        for xy in comps:
+            xy = np.asarray(xy, np.float64).reshape(-1, 2)
+            lines = [f"{x:.17g} {y:.17g}" for x, y in xy]
+            f.write(",\n".join(lines) + ";\n")
+
+
+def run_foster(base: np.ndarray, overlay: np.ndarray, timeout: float = 1800.0) -> dict:
+    """Run oracle/_ref/foster on one pair (stdout discarded): the result rings
+    (precision 6, the program's output format) and the wall time in ms."""
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        write_poly_components(td / "p.poly", [base])
+        write_poly_components(td / "q.poly", [overlay])
+        t0 = time.perf_counter()
+        p = subprocess.run([str(FOSTER_EXE), str(td / "p.poly"), str(td / "q.poly"),
+                            str(td / "r.poly")], stdout=subprocess.DEVNULL,
+                           stderr=subprocess.PIPE, text=True, timeout=timeout)
+        wall = (time.perf_counter() - t0) * 1e3
+        if p.returncode != 0:
+            raise RuntimeError(f"foster exited {p.returncode}: {p.stderr[-400:]}")
+        text = (td / "r.poly").read_text() if (td / "r.poly").exists() else ""
+    return {"rings": parse_rings(text), "ms": wall}

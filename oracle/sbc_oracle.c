@@ -210,6 +210,8 @@ struct sbco_run {
   int k;
   struct ov_out *ov;
   long stats[SBCO_STAT_NUM];
+  void *tree[SBCO_TREE_NUM];
+  long tree_len[SBCO_TREE_NUM];
 };
 
 static void set_err(sbco_run *r, int st, const char *m) {
@@ -1609,6 +1611,20 @@ sbco_run *sbco_clip(const double *b_xy, int nb, const double *c_xy, const int *c
   run->stats[SBCO_STAT_TREE_SIZE] = t.ts;
   run->stats[SBCO_STAT_COVER_TOTAL] = t.cov_off[t.ts];
   run->stats[SBCO_STAT_LEAF_END_TOTAL] = t.leaf_off[t.numLeaves];
+  /* the run keeps the tree's arrays for sbco_tree_data (the tree itself is
+   * freed at the end of the run) */
+  {
+    const void *src[SBCO_TREE_NUM] = {t.ea, t.leaf_off, t.leaf_edge, t.cov_off, t.cov_edge};
+    const long n[SBCO_TREE_NUM] = {t.epc, (long)t.numLeaves + 1, t.leaf_off[t.numLeaves],
+                                   (long)t.ts + 1, t.cov_off[t.ts]};
+    for (int w = 0; w < SBCO_TREE_NUM; ++w) {
+      const size_t es = w == SBCO_TREE_EA ? sizeof(double) : sizeof(int);
+      run->tree[w] = malloc(es * (size_t)(n[w] > 0 ? n[w] : 1));
+      if (!run->tree[w]) { set_err(run, SBCO_ENOMEM, "out of memory"); goto done; }
+      if (n[w]) memcpy(run->tree[w], src[w], es * (size_t)n[w]);
+      run->tree_len[w] = n[w];
+    }
+  }
   for (int c = 1; c <= k; ++c)
     if (clip_overlay(run, &t, c)) break;
 done:
@@ -1634,8 +1650,19 @@ long sbco_stat(const sbco_run *r, int which) {
   return r->stats[which];
 }
 
+long sbco_tree_len(const sbco_run *r, int which) {
+  if (!r || which < 0 || which >= SBCO_TREE_NUM || !r->tree[which]) return -1;
+  return r->tree_len[which];
+}
+
+const void *sbco_tree_data(const sbco_run *r, int which) {
+  if (!r || which < 0 || which >= SBCO_TREE_NUM) return NULL;
+  return r->tree[which];
+}
+
 void sbco_free(sbco_run *r) {
   if (!r) return;
+  for (int w = 0; w < SBCO_TREE_NUM; ++w) free(r->tree[w]);
   if (r->ov)
     for (int i = 0; i < r->k; ++i)
       for (int w = 0; w < SBCO_NUM_ARRAYS; ++w) free(r->ov[i].arr[w]);

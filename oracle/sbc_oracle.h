@@ -36,6 +36,23 @@ enum sbco_stat {
   SBCO_STAT_COVER_TOTAL, SBCO_STAT_LEAF_END_TOTAL, SBCO_STAT_NUM
 };
 
+/* Tree-level arrays (overlay-independent), for direct checks of the tree
+ * build: the padded elementary points (A4), the leaf end lists as CSR by leaf
+ * (A6: leaf q's entries leaf_edge[leaf_off[q] .. leaf_off[q+1]), edge
+ * indices, an edge's end entry before its start entry) and the cover lists
+ * as CSR by node (A7: node v's edges cov_edge[cov_off[v] .. cov_off[v+1]),
+ * ascending edge index). */
+enum sbco_tree_array {
+  SBCO_TREE_EA = 0,         /* doubles, epc */
+  SBCO_TREE_LEAF_OFF,       /* ints, numLeaves+1 */
+  SBCO_TREE_LEAF_EDGE,      /* ints */
+  SBCO_TREE_COV_OFF,        /* ints, ts+1 */
+  SBCO_TREE_COV_EDGE,       /* ints */
+  SBCO_TREE_NUM
+};
+long sbco_tree_len(const sbco_run *r, int which);
+const void *sbco_tree_data(const sbco_run *r, int which);
+
 /*
  * Run the whole path for one base polygon (nb vertices, interleaved xy) and k
  * overlays (concatenated interleaved xy, sizes in c_sizes).  No closing

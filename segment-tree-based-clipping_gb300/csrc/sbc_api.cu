@@ -342,8 +342,13 @@ int sbc_debug_array(sbc_ctx* c, int which, void* dst, long long cap, long long* 
     case SBC_ARR_MERGED_CNB: src = p.dbg_nbC; n = p.dbg_nQ; break;
     case SBC_ARR_LABEL_B: src = p.dbg_labB; n = p.dbg_nB; break;
     case SBC_ARR_LABEL_C: src = p.dbg_labC; n = p.dbg_nQ; break;
+    case SBC_ARR_ELEMENTARY: src = p.ea; n = p.epc; es = sizeof(double); break;
+    case SBC_ARR_LEAF_AFTER: src = p.aft; n = p.E; break;
+    case SBC_ARR_LEAF_BEFORE: src = p.bef; n = p.E; break;
+    case SBC_ARR_LEAF_RANGE: src = p.lr; n = 2LL * p.E; break;
     default: return set_err(c, SBC_EINPUT, "unknown array");
   }
+  if (!src) n = 0;  // not produced by the last call
   *count = n;
   long long m = n < cap ? n : cap;
   if (dst && src && m > 0) {

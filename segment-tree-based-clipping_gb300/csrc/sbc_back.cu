@@ -1152,15 +1152,25 @@ extern "C" int sbc_trace_rings_noalloc(const sbc_merged_lists* in, int* ring_off
 
   // the flags and counters must start at zero; the pools are written before
   // they are read
+  // Every runtime call's own return code is checked, and the kernels go
+  // through cudaLaunchKernel, whose return is that launch's status alone: an
+  // error the caller left pending on this thread is neither reported as this
+  // call's nor cleared.
   cudaStream_t st = (cudaStream_t)stream;
-  cudaMemsetAsync(block, 0, 256, st);
-  cudaMemsetAsync(flags, 0, flag_bytes, st);
+  ce = cudaMemsetAsync(block, 0, 256, st);
+  if (ce == cudaSuccess) ce = cudaMemsetAsync(flags, 0, flag_bytes, st);
+  if (ce != cudaSuccess)
+    return na_fail(err, err_len, SBC_ECUDA, "cudaMemsetAsync failed (%lld)", (long long)ce);
   ++g_launches;
-  k_serial_backend<<<1, 1, 0, st>>>(a);
+  {
+    void* args[] = {&a};
+    ce = cudaLaunchKernel((const void*)k_serial_backend, dim3(1), dim3(1), args, 0, st);
+  }
+  if (ce != cudaSuccess)
+    return na_fail(err, err_len, SBC_ECUDA, "back-end launch failed (%lld)", (long long)ce);
   int hst = 0;
-  cudaMemcpyAsync(&hst, a.status, sizeof(int), cudaMemcpyDeviceToHost, st);
-  ce = cudaStreamSynchronize(st);
-  if (ce == cudaSuccess) ce = cudaGetLastError();
+  ce = cudaMemcpyAsync(&hst, a.status, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
   if (ce != cudaSuccess)
     return na_fail(err, err_len, SBC_ECUDA, "CUDA error %lld in the allocation-free back end", (long long)ce);
   if (hst == 2)
@@ -1168,11 +1178,15 @@ extern "C" int sbc_trace_rings_noalloc(const sbc_merged_lists* in, int* ring_off
   if (hst != 0)
     return na_fail(err, err_len, SBC_EINTERNAL, "linked-list back end capacity exceeded (status %lld)", hst);
   ++g_launches;
-  k_serial_emit<<<1, 1, 0, st>>>(a, ring_offsets, ring_xy, xy_cap_verts, block);
+  {
+    void* args[] = {&a, &ring_offsets, &ring_xy, &xy_cap_verts, &block};
+    ce = cudaLaunchKernel((const void*)k_serial_emit, dim3(1), dim3(1), args, 0, st);
+  }
+  if (ce != cudaSuccess)
+    return na_fail(err, err_len, SBC_ECUDA, "ring-output launch failed (%lld)", (long long)ce);
   int hc[2] = {0, 0};
-  cudaMemcpyAsync(hc, block, sizeof(hc), cudaMemcpyDeviceToHost, st);
-  ce = cudaStreamSynchronize(st);
-  if (ce == cudaSuccess) ce = cudaGetLastError();
+  ce = cudaMemcpyAsync(hc, block, sizeof(hc), cudaMemcpyDeviceToHost, st);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
   if (ce != cudaSuccess)
     return na_fail(err, err_len, SBC_ECUDA, "CUDA error %lld in the allocation-free ring output", (long long)ce);
   *nrings_out = hc[0];

@@ -162,6 +162,10 @@ static double key_to_double(unsigned long long k) {
 }
 
 int Pipeline::stage_setup(const double* d_bxy, const double* d_cxy, const int* c_sizes) {
+  // tree arrays of an earlier run are not this run's (diagnostics read them)
+  ea = nullptr;
+  aft = bef = nullptr;
+  lr = nullptr;
   hcS.assign(k + 1, 0);
   hcc.assign(k + 1, 0);
   for (int i = 0; i < k; ++i) {

@@ -33,6 +33,8 @@ DEBUG_ARRAYS = {
     "merged_balpha": (8, np.int32), "merged_calpha": (9, np.int32),
     "merged_bnb": (10, np.int32), "merged_cnb": (11, np.int32),
     "label_b": (12, np.int32), "label_c": (13, np.int32),
+    "elementary": (14, np.float64), "leaf_after": (15, np.int32),
+    "leaf_before": (16, np.int32), "leaf_range": (17, np.int32),
 }
 
 

@@ -59,6 +59,14 @@ def test_small_cases_serial_back_end_matches(small_cases):
         c.close()
 
 
+def test_small_cases_tree_stages_match_oracle(clipper, small_cases):
+    """Rows A4-A7 (elementary points, end lists, cover lists) on every small
+    case, degenerate grids and vertical edges included."""
+    for case in small_cases:
+        clipper.clip(case.base, case.overlays)
+        _check_tree(clipper, O.clip(case.base, case.overlays))
+
+
 def test_unique_pairs_match_reference(clipper, small_cases):
     for case in small_cases:
         if len(case.overlays) != 1:
@@ -70,9 +78,70 @@ def test_unique_pairs_match_reference(clipper, small_cases):
         assert np.array_equal(clipper.debug_array("uniq_t"), ut)
 
 
+def _cover_pairs(lr, L):
+    """(node, edge) pairs of every edge's canonical decomposition of its leaf
+    range [l, r1): the nodes the reference's insertEdgeParallel
+    (p_seg_tree/oacc_segment_tree.cpp:2496-2564) puts the edge in."""
+    e = np.arange(len(lr), dtype=np.int64)
+    x = lr[:, 0].astype(np.int64) + L
+    y = lr[:, 1].astype(np.int64) + L
+    nodes, edges = [], []
+    while True:
+        live = x < y
+        if not live.any():
+            break
+        a = live & (x & 1 == 1)
+        nodes.append(x[a]); edges.append(e[a])
+        x = np.where(a, x + 1, x)
+        b = live & (y & 1 == 1)
+        y = np.where(b, y - 1, y)
+        nodes.append(y[b]); edges.append(e[b])
+        x >>= 1
+        y >>= 1
+    nodes = np.concatenate(nodes) if nodes else np.zeros(0, np.int64)
+    edges = np.concatenate(edges) if edges else np.zeros(0, np.int64)
+    o = np.lexsort((edges, nodes))
+    return nodes[o], edges[o]
+
+
+def _check_tree(clipper, ora):
+    """Rows A4-A7 directly: the elementary points bit for bit, every leaf's
+    end list and every node's cover list entry for entry, and the counts."""
+    st, t, s = clipper.stats(), ora["tree"], ora["stats"]
+    assert st["elementary_points"] == s["elem_count"]
+    assert st["tree_size"] == s["tree_size"]
+    assert st["cover_entries"] == s["cover_total"]
+    assert st["leaf_end_entries"] == s["leaf_end_total"]
+    ea = clipper.debug_array("elementary")
+    assert np.array_equal(ea.view(np.int64), t["ea"].view(np.int64))
+    L = s["tree_size"] // 2
+    aft = clipper.debug_array("leaf_after").astype(np.int64)
+    bef = clipper.debug_array("leaf_before").astype(np.int64)
+    E = len(aft)
+    assert E == s["edges"] == len(bef)
+    # A6: leaf q lists, in edge order, each edge's end entry, then its start entry
+    e = np.arange(E, dtype=np.int64)
+    leaf = np.concatenate([aft, bef])
+    ent = np.concatenate([e, e])
+    kind = np.concatenate([np.zeros(E, np.int64), np.ones(E, np.int64)])
+    ok = leaf >= 0
+    leaf, ent, kind = leaf[ok] - L, ent[ok], kind[ok]
+    o = np.lexsort((kind, ent, leaf))
+    assert np.array_equal(ent[o], t["leaf_edge"])
+    assert np.array_equal(np.searchsorted(leaf[o], np.arange(L + 1)), t["leaf_off"])
+    # A7: node v's cover list, ascending edge index
+    lr = clipper.debug_array("leaf_range").reshape(-1, 2)
+    nodes, edges = _cover_pairs(lr, L)
+    assert np.array_equal(edges, t["cov_edge"])
+    assert np.array_equal(np.searchsorted(nodes, np.arange(2 * L + 1)), t["cov_off"])
+
+
 def _compare_all(clipper, b, c, entry=None):
     rings = clipper.clip(b, [c])[0]
-    ora = O.clip(b, [c])["overlays"][0]
+    run = O.clip(b, [c])
+    ora = run["overlays"][0]
+    _check_tree(clipper, run)
+    assert clipper.stats()["raw_hits"] == len(ora["raw_b"])
     for name in ("uniq_b", "uniq_c", "uniq_t", "isect_ab", "isect_ac", "isect_xy",
                  "merged_bxy", "merged_cxy", "merged_balpha", "merged_calpha",
                  "merged_bnb", "merged_cnb", "label_b", "label_c"):

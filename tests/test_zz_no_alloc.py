@@ -6,7 +6,9 @@ not allocate device memory.  Every case here first runs the ordinary entry
 point (sbc_clip_pair, which grows context buffers), takes the merged lists it
 exports, and hands device copies of them to the allocation-free entry point
 twice in a row; both calls must return exactly the rings sbc_clip_pair
-returned (bit for bit, the tolerance of every ring test in this suite).
+returned (bit for bit, the tolerance of every ring test in this suite), and
+every call after the process's first must leave the device's free memory
+unchanged (cudaMemGetInfo before and after the call).
 
 The module is named so that pytest collects it last: it must pass both on
 its own in a fresh process (the first call does the per-device set-up) and
@@ -36,14 +38,27 @@ def _merged_lists(clipper, torch):
     return dev, len(arr["merged_balpha"]), len(arr["merged_cnb"]), len(arr["uniq_b"])
 
 
+_FIRST_CALL_DONE = [False]
+
+
 def _call(torch, sbclip, b_d, nb, c_d, nc, dev, n_b, n_c, k, offsets, xy, xy_cap):
     offsets.fill_(-7)
     xy.fill_(float("nan"))
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info(0)[0]
     nr, nv = sbclip.trace_rings_noalloc(
         b_d.data_ptr(), nb, c_d.data_ptr(), nc,
         dev["merged_bxy"].data_ptr(), dev["merged_balpha"].data_ptr(), dev["label_b"].data_ptr(), n_b,
         dev["merged_cxy"].data_ptr(), dev["merged_cnb"].data_ptr(), dev["label_c"].data_ptr(), n_c,
         k, offsets.data_ptr(), offsets.numel(), xy.data_ptr(), xy_cap)
+    free_after = torch.cuda.mem_get_info(0)[0]
+    # The first call of the process may load the library's device module
+    # (and with it the static scratch array) and looks up the array's
+    # address; from then on a call must leave the device's free memory as
+    # it found it: no allocation, no pool growth.
+    if _FIRST_CALL_DONE[0]:
+        assert free_after == free_before, (free_before, free_after)
+    _FIRST_CALL_DONE[0] = True
     off = offsets[: nr + 1].cpu().numpy()
     pts = xy[: 2 * nv].cpu().numpy().reshape(-1, 2)
     assert off[0] == 0 and off[-1] == nv
