@@ -16,6 +16,16 @@ with every launch bracketed by CUDA events.  `e2e` times the public host API
 the result rings (offsets + vertices, into the context's host result memory
 that a C caller reads in place) inside every step.
 
+The default line also carries `batched`, the second half of the headline
+metric measured in the same run: the 65,536 small pairs (area forward +
+backward as one CUDA graph launch per step) and one 200k-vertex base against
+10,000 overlays (forward, and area forward + backward), each next to the plain
+per-pair GPU path on the same inputs (`--no-batched` leaves it out).  Its
+`cpu_baseline.others` adds the reference's CPU build at one thread and at all
+host threads on the 10k x 8k pair and Foster's sequential code (the
+reference's own baseline) on 64 small pairs (`--foster`: also on the
+10k x 8k pair, about 5 minutes).
+
 The single pair does not shard across GPUs (the tree and the tracing are
 global), so N > 1 runs N independent replicas, one per rank (torchrun), and
 reports the max over ranks.
@@ -76,15 +86,20 @@ def metric_of(workload: str) -> str:
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 
 
+JAGGED_DESC = ("jagged stars, R=%g, r=R(1+0.3g) clamped >= 0.2R, g = 8 octaves of value noise, "
+               "base_freq=%d; overlay offset (0.25R, 0.1R), rotated 0.3 rad"
+               % (gen.LARGE_R, gen.JAGGED_BASE_FREQ))
+
+
 def workload(name: str):
     if name == "pair_1m_1m":
         b, c = gen.pair_large()
         desc = {"workload": "pair_1m_1m", "base_vertices": len(b), "overlay_vertices": len(c),
-                "generator": "jagged stars, 8 octaves value noise, base_freq=%d" % gen.JAGGED_BASE_FREQ}
+                "generator": JAGGED_DESC}
     elif name == "pair_200k_200k":
         b, c = gen.pair_large(n=200_000)
         desc = {"workload": "pair_200k_200k", "base_vertices": len(b), "overlay_vertices": len(c),
-                "generator": "jagged stars, 8 octaves value noise, base_freq=%d" % gen.JAGGED_BASE_FREQ}
+                "generator": JAGGED_DESC}
     elif name == "pair_10k_8k":
         b, c = gen.pair_small()
         desc = {"workload": "pair_10k_8k", "base_vertices": len(b), "overlay_vertices": len(c),
@@ -152,6 +167,50 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": float(max(smax)) if smax else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# What bounds each kernel that can dominate a step (ncu summaries in
+# profiles/): "hbm" for byte-moving passes, "fp64" for the edge-pair
+# classifier kernels (the FP64 pipe; GB300's FP64 rate is low), "latency" for
+# dependent pointer chases and serial per-pair code, where neither HBM nor a
+# pipe is busy.  The roofline entry reports the kernel against HBM bytes in
+# every case and says which bound applies.
+KERNEL_BOUND = {
+    "k_rad_scatter_u64": "hbm", "k_rad_hist_u64": "hbm", "k_rad_scatter_u32": "hbm",
+    "k_rad_hist_u32": "hbm", "k_scan_lb": "hbm", "k_setup_edges": "hbm", "k_edge_tree": "hbm",
+    "k_grid_scatter": "hbm", "k_edge_fbox": "hbm", "k_copy_runs": "hbm",
+    "k_pair_exact": "fp64", "k_pw_cand_test": "fp64", "k_batch_cand": "fp64", "k_labels": "fp64",
+    "k_grid_warp": "latency", "k_grid_small": "latency", "k_lr_jump": "latency",
+    "k_tr_jump": "latency", "k_alpha_sort": "latency", "k_batch_back": "latency",
+    "k_batch_front": "latency", "k_pw_pairs": "latency", "k_dedup": "latency",
+}
+
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
+# kernels captured with ncu on the named workload, keyed (kernel, workload).
+# A capture on a smaller case of the same kernel is scaled by the units it
+# processed where the traffic grows in proportion (said in the source note).
+TRAFFIC = {}
+
+
+def roofline_of(prof_b: dict, workload_name: str, fallback_bytes=None):
+    """Roofline entry of the kernel with the largest device time in a
+    per-launch profile {name: (ms, launches, stated bytes)}."""
+    if not prof_b:
+        return None
+    pk, kind = peaks()
+    name, (tot_ms, n_l, by) = max(prof_b.items(), key=lambda kv: kv[1][0])
+    per_ms = tot_ms / max(n_l, 1)
+    ab = by / max(n_l, 1) if by else (fallback_bytes(name, n_l) if fallback_bytes else None)
+    achieved = ab / (per_ms * 1e-3) / 1e9 if ab else None
+    tr = TRAFFIC.get((name, workload_name))
+    return {"kernel": name, "bound": KERNEL_BOUND.get(name, "hbm"), "achieved": achieved,
+            "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / pk["hbm_gbs"] if achieved else None,
+            "traffic": tr["bytes"] if tr else None,
+            "traffic_source": tr["source"] if tr else None,
+            "algorithmic_bytes_per_launch": ab, "ms_per_launch": per_ms,
+            "share_of_step": tot_ms / max(sum(v[0] for v in prof_b.values()), 1e-9),
+            "peak_source": kind}
 
 
 # Algorithmic bytes per launch of the kernels that can dominate a step, from
@@ -235,6 +294,10 @@ def run_gb300(args, rank: int, world: int):
     # host->device and device->host copies inside every step
     e2e_times = []
     off = xy = None
+    # untimed warm-up of the host path (its first call sizes the context's
+    # input staging and pinned result memory)
+    for _ in range(args.warmup):
+        clip.clip_pair_flat(b, c, copy=False)
     for i in range(max(args.steps, 1)):
         flush.fill_(1.0)
         torch.cuda.synchronize()
@@ -247,21 +310,9 @@ def run_gb300(args, rank: int, world: int):
            "h2d_bytes_per_step": int(16 * (nb + nc)),
            "d2h_bytes_per_step": int(4 * (nrings + 1) + 16 * nverts)}
 
-    # ---- roofline of the dominant kernel
-    pk, kind = peaks()
-    dom = max(prof.items(), key=lambda kv: kv[1][0]) if prof else None
-    roof = None
-    if dom:
-        name, (tot_ms, n_l) = dom
-        per_launch_ms = tot_ms / max(n_l, 1)
-        # the bytes the launch sites state, else the table above
-        ab = prof_b[name][2] / max(n_l, 1) or algorithmic_bytes(name, stats, n_l)
-        achieved = (ab / (per_launch_ms * 1e-3) / 1e9) if ab else None
-        roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
-                "unit": "GB/s", "frac": (achieved / pk["hbm_gbs"]) if achieved else None,
-                "traffic": None, "peak_source": kind,
-                "share_of_step": tot_ms / max(sum(v[0] for v in prof.values()), 1e-9),
-                "ms_per_launch": per_launch_ms}
+    # ---- roofline of the dominant kernel (the bytes the launch sites state,
+    # else the table above)
+    roof = roofline_of(prof_b, args.workload, lambda k, n: algorithmic_bytes(k, stats, n))
     top = sorted(prof.items(), key=lambda kv: -kv[1][0])[:10]
 
     out = {
@@ -277,9 +328,12 @@ def run_gb300(args, rank: int, world: int):
         "counts": {"rings": nrings, "vertices": nverts, "unique_intersections": stats["unique"],
                    "candidates_tested_per_s": stats["candidates_tested"] / (ms * 1e-3)},
     }
+    clip.close()
+    if args.workload == "pair_1m_1m" and not args.no_batched:
+        out["batched"] = batched_summary(args, rank, world)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(b, c, args)
-    clip.close()
+        out["cpu_baseline"]["others"] = extra_cpu_baselines(args.foster)
     return out
 
 
@@ -341,6 +395,33 @@ def reference_pairs_per_s(pairs, threads: int):
     return len(pairs) / (time.perf_counter() - t0), threads, "reference"
 
 
+def max_over_ranks(x: float, world: int, device: str) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def shard_job(nb, nc, rank: int, world: int, hits=None):
+    """This rank's pairs of one job partitioned over the ranks by estimated
+    cost (longest processing time first), and a summary of the partition."""
+    import shard
+    costs = shard.pair_costs(nb, nc, hits)
+    parts = shard.lpt_partition(costs, world)
+    return parts[rank], shard.shard_summary(costs, parts)
+
+
+def gather_check(local: dict, n_total: int, args):
+    """Host-side gather of per-pair outputs on rank 0 (outside the timed
+    region); returns the number of pairs gathered (rank 0) or None."""
+    import shard
+    got = shard.gather_outputs(local, n_total, group=getattr(args, "gloo", None))
+    return None if got is None else len(got)
+
+
 def run_small_pairs(args, rank: int, world: int):
     """One step = intersection areas of every pair (sbc_area_forward_device)
     and their gradient (sbc_area_backward_device, reusing the forward's
@@ -351,7 +432,15 @@ def run_small_pairs(args, rank: int, world: int):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     n = args.pairs or SMALL_PAIRS
-    pairs, desc = small_pairs_workload(n, 4000 + rank)
+    n_total = n * world  # weak scaling: n pairs per GPU in one job
+    pairs, desc = small_pairs_workload(n_total, 4000)
+    shard_info = None
+    mine = np.arange(n_total)
+    if world > 1:
+        mine, shard_info = shard_job([len(b) for b, _ in pairs], [len(c) for _, c in pairs],
+                                     rank, world)
+        pairs = [pairs[i] for i in mine]
+        n = len(pairs)
     bases, ovs = [b for b, _ in pairs], [c for _, c in pairs]
     bxy, boff = sbclip.pack_polygons(bases)
     cxy, coff = sbclip.pack_polygons(ovs)
@@ -419,6 +508,9 @@ def run_small_pairs(args, rank: int, world: int):
     # and gradients copied out (the host backward call runs its own forward)
     e2e_t = []
     ones = np.ones(n)
+    for _ in range(args.warmup):
+        clip.area_forward_packed(bxy, boff, cxy, coff)
+        clip.area_backward_packed(bxy, boff, cxy, coff, ones)
     for _ in range(max(args.steps, 1)):
         flush.fill_(1.0)
         torch.cuda.synchronize()
@@ -427,7 +519,10 @@ def run_small_pairs(args, rank: int, world: int):
         clip.area_backward_packed(bxy, boff, cxy, coff, ones)
         e2e_t.append((time.perf_counter() - t0) * 1e3)
     in_bytes = 16 * (int(boff[-1]) + int(coff[-1])) + 16 * (n + 1)
-    e2e = {"value": n * world / (float(np.mean(e2e_t)) * 1e-3), "unit": "pairs/s",
+    gathered = gather_check({int(i): float(a) for i, a in zip(mine, area.cpu().numpy())},
+                            n_total, args) if world > 1 else n_total
+    e2e_ms = max_over_ranks(float(np.mean(e2e_t)), world, cuda)
+    e2e = {"value": n_total / (e2e_ms * 1e-3), "unit": "pairs/s",
            "h2d_bytes_per_step": 2 * in_bytes + 8 * n,
            "d2h_bytes_per_step": 12 * n + 16 * (int(boff[-1]) + int(coff[-1]))}
     # the plain per-pair GPU path (one sbc_clip_pair_device call per pair, forward only)
@@ -439,23 +534,16 @@ def run_small_pairs(args, rank: int, world: int):
                               t["cxy"].data_ptr() + 16 * int(coff[p]), int(coff[p + 1] - coff[p]), sp)
     torch.cuda.synchronize()
     per_pair = sample / (time.perf_counter() - t0)
-    pk, kind = peaks()
-    dom = max(prof.items(), key=lambda kv: kv[1][0]) if prof else None
-    roof = None
-    if dom:
-        name, (tot_ms, n_l) = dom
-        ab = prof_b[name][2] / max(n_l, 1)
-        achieved = ab / (tot_ms / max(n_l, 1) * 1e-3) / 1e9
-        roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
-                "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "traffic": None,
-                "peak_source": kind, "ms_per_launch": tot_ms / max(n_l, 1)}
+    roof = roofline_of(prof_b, desc["workload"])
     out = {
         "metric": "clipped pairs/s, batched area forward+backward, 65,536 small pairs",
-        "value": n * world / (ms * 1e-3), "unit": "pairs/s", "n_gpus": world,
+        "value": n_total / (ms * 1e-3), "unit": "pairs/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded star polygons)",
-        "config": dict(desc, parallelism="pairs sharded by rank" if world > 1 else "single",
+        "config": dict(desc, parallelism=("one job sharded by cost (LPT), gathered on rank 0"
+                                          if world > 1 else "single"),
+                       shard=shard_info, gathered_pairs=gathered,
                        l2="flushed between steps (256 MiB write)",
                        launch="one CUDA graph per step (area forward + backward)"),
         "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
@@ -464,7 +552,7 @@ def run_small_pairs(args, rank: int, world: int):
         "clocks": clk.summary(),
         "counts": {"pairs_ok": n_ok, "per_pair_gpu_path_pairs_per_s": per_pair,
                    "per_pair_sample": sample,
-                   "batched_over_per_pair": (n * world / (ms * 1e-3)) / per_pair},
+                   "batched_over_per_pair": (n_total / (ms * 1e-3)) / per_pair},
     }
     if rank == 0 and not args.no_cpu_baseline:
         v, cores, kind2 = reference_pairs_per_s(pairs[:256], os.cpu_count() or 1)
@@ -479,8 +567,9 @@ ONE_TO_MANY = (200_000, 10_000)
 ONE_TO_MANY_METRIC = "clipped pairs/s, one 200k-vertex base x 10,000 overlays, pairwise forward"
 
 
-def one_to_many_workload(n_overlays: int | None = None):
+def one_to_many_workload(n_overlays: int | None = None, per_gpu: int = 1):
     nb, nov = ONE_TO_MANY
+    nov *= per_gpu
     base, ovs = gen.one_to_many(n_base=nb, n_overlays=nov, seed=3000)
     if n_overlays is not None:
         ovs = ovs[:n_overlays]
@@ -500,10 +589,28 @@ def run_one_to_many(args, rank: int, world: int):
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    base, ovs, desc = one_to_many_workload(args.overlays)
+    # weak scaling: 10,000 overlays per GPU in one job against the replicated base
+    base, ovs, desc = one_to_many_workload(args.overlays, per_gpu=world)
+    nov_total = len(ovs)
+    cuda = f"cuda:{dev}"
+    shard_info = None
+    mine = np.arange(nov_total)
+    if world > 1:
+        # cost: n log n plus K estimated per size class from a sampled run
+        # (every 25th overlay; the same sample and result on every rank)
+        sample = np.arange(0, nov_total, 25)
+        sxy, soff = sbclip.pack_polygons([ovs[i] for i in sample])
+        pre = sbclip.Clipper(dev)
+        pr, ro, _xy, _st = pre.clip_pairwise_flat(base, sxy, soff, copy=True)
+        pre.close()
+        k_sample = np.array([ro[pr[i + 1]] - ro[pr[i]] for i in range(len(sample))], np.float64)
+        import shard
+        nc_all = np.array([len(o) for o in ovs])
+        hits = shard.estimate_hits(len(base) + nc_all, sample, k_sample)
+        mine, shard_info = shard_job(np.full(nov_total, len(base)), nc_all, rank, world, hits)
+        ovs = [ovs[i] for i in mine]
     nov = len(ovs)
     cxy, coff = sbclip.pack_polygons(ovs)
-    cuda = f"cuda:{dev}"
     tb = torch.from_numpy(np.ascontiguousarray(base)).to(cuda)
     tc = torch.from_numpy(cxy).to(cuda)
     to = torch.from_numpy(coff).to(cuda)
@@ -557,16 +664,24 @@ def run_one_to_many(args, rank: int, world: int):
         tt = torch.tensor([ms], device=cuda)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         ms = float(tt.item())
+    # per-kernel times of one more step with the big overlays on one worker:
+    # kernels on concurrent worker streams would each be timed with the
+    # others' work inside their event pairs
     torch.cuda.synchronize()
+    workers = clip.pairwise_workers()
+    clip.set_pairwise_workers(1)
     sbclip.profile_begin()
     step()
     torch.cuda.synchronize()
     prof_b = sbclip.profile_end(with_bytes=True)
+    clip.set_pairwise_workers(workers)
     prof = {k: (v[0], v[1]) for k, v in prof_b.items()}
     # end to end through the host-array C ABI (sbc_clip_pairwise): inputs
     # copied in and every ring copied out, inside each step
     e2e_t = []
     d2h = 0
+    for _ in range(args.warmup):
+        clip.clip_pairwise_flat(base, cxy, coff, sp, copy=False)
     for _ in range(max(args.steps, 1)):
         flush.fill_(1.0)
         torch.cuda.synchronize()
@@ -575,9 +690,15 @@ def run_one_to_many(args, rank: int, world: int):
         e2e_t.append((time.perf_counter() - t0) * 1e3)
         d2h = ro.nbytes + xy.nbytes
         n_ok = int((stt == 0).sum())
-    e2e = {"value": nov * world / (float(np.mean(e2e_t)) * 1e-3), "unit": "pairs/s",
+    e2e_ms = max_over_ranks(float(np.mean(e2e_t)), world, cuda)
+    e2e = {"value": nov_total / (e2e_ms * 1e-3), "unit": "pairs/s",
            "h2d_bytes_per_step": int(base.nbytes + cxy.nbytes + coff.nbytes),
            "d2h_bytes_per_step": int(d2h)}
+    gathered = nov_total
+    if world > 1:
+        counts = np.diff(pr)
+        gathered = gather_check({int(i): int(counts[j]) for j, i in enumerate(mine)},
+                                nov_total, args)
     # area forward + backward of every pair (the gradient of the shared base
     # summed over the overlays): a separate figure next to the forward metric
     fb_area = torch.zeros(nov, dtype=torch.float64, device=cuda)
@@ -585,18 +706,21 @@ def run_one_to_many(args, rank: int, world: int):
     fb_gb = torch.zeros_like(tb)
     fb_gc = torch.zeros_like(tc)
     fb_t = []
-    for k in range(3):
+    for k in range(args.warmup + max(args.steps, 1)):
         flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
+        e0.record(stream)
         clip.pairwise_area_device(tb.data_ptr(), len(base), nov, tc.data_ptr(), to.data_ptr(),
                                   fb_area.data_ptr(), None, sp)
         clip.pairwise_area_backward_device(tb.data_ptr(), len(base), nov, tc.data_ptr(),
                                            to.data_ptr(), fb_g.data_ptr(), fb_gb.data_ptr(),
                                            fb_gc.data_ptr(), sp)
+        e1.record(stream)
         torch.cuda.synchronize()
-        if k:
-            fb_t.append((time.perf_counter() - t0) * 1e3)
+        if k >= args.warmup:
+            fb_t.append(e0.elapsed_time(e1))
     # the plain per-pair GPU path: one sbc_clip_pair_device call per overlay
     sample = 64
     rng = np.random.default_rng(5)
@@ -608,23 +732,17 @@ def run_one_to_many(args, rank: int, world: int):
                               int(coff[p + 1] - coff[p]), sp)
     torch.cuda.synchronize()
     per_pair = sample / (time.perf_counter() - t0)
-    pk, kind = peaks()
-    dom = max(prof.items(), key=lambda kv: kv[1][0]) if prof else None
-    roof = None
-    if dom:
-        name, (tot_ms, n_l) = dom
-        ab = prof_b[name][2] / max(n_l, 1)
-        achieved = ab / (tot_ms / max(n_l, 1) * 1e-3) / 1e9
-        roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
-                "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "traffic": None,
-                "peak_source": kind, "ms_per_launch": tot_ms / max(n_l, 1)}
-    value = nov * world / (ms * 1e-3)
+    roof = roofline_of(prof_b, desc["workload"])
+    value = nov_total / (ms * 1e-3)
+    fb_ms = max_over_ranks(float(np.mean(fb_t)), world, cuda)
     out = {
         "metric": ONE_TO_MANY_METRIC,
         "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded star polygons)",
-        "config": dict(desc, parallelism="replicas" if world > 1 else "single",
+        "config": dict(desc, parallelism=("one job sharded by cost (LPT), base replicated, "
+                                          "gathered on rank 0" if world > 1 else "single"),
+                       shard=shard_info, gathered_pairs=gathered,
                        l2="flushed between steps (256 MiB write)",
                        autotuned={"big_pair_split_records": tuned["split"],
                                   "grid_cell_factor": tuned["cell_factor"]}),
@@ -640,8 +758,8 @@ def run_one_to_many(args, rank: int, world: int):
                    "edge_pairs_tested_per_s": info["tested"] / (ms * 1e-3),
                    "per_pair_gpu_path_pairs_per_s": per_pair, "per_pair_sample": sample,
                    "batched_over_per_pair": value / per_pair,
-                   "area_forward_backward_ms": float(np.mean(fb_t)),
-                   "area_forward_backward_pairs_per_s": nov / (float(np.mean(fb_t)) * 1e-3)},
+                   "area_forward_backward_ms": fb_ms,
+                   "area_forward_backward_pairs_per_s": nov_total / (fb_ms * 1e-3)},
     }
     if rank == 0 and not args.no_cpu_baseline:
         sample_cpu = [(base, ovs[int(p)]) for p in pick[:32]]
@@ -739,16 +857,7 @@ def run_uneven(args, rank: int, world: int):
                               sp)
     torch.cuda.synchronize()
     per_pair = len(pick) / (time.perf_counter() - t0)
-    pk, kind = peaks()
-    dom = max(prof.items(), key=lambda kv: kv[1][0]) if prof else None
-    roof = None
-    if dom:
-        name, (tot_ms, n_l) = dom
-        ab = prof_b[name][2] / max(n_l, 1)
-        achieved = ab / (tot_ms / max(n_l, 1) * 1e-3) / 1e9
-        roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
-                "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "traffic": None,
-                "peak_source": kind, "ms_per_launch": tot_ms / max(n_l, 1)}
+    roof = roofline_of(prof_b, desc["workload"])
     value = n / (ms * 1e-3)
     out = {
         "metric": UNEVEN_METRIC, "value": value, "unit": "pairs/s", "n_gpus": world,
@@ -771,6 +880,76 @@ def run_uneven(args, rank: int, world: int):
         out["cpu_baseline"] = {"value": v, "unit": "pairs/s", "cores": cores, "kind": kind2,
                                "sample": "64 random pairs clipped pairwise (forward only)"}
     clip.close()
+    return out
+
+
+def batched_summary(args, rank: int, world: int):
+    """The batched half of the headline metric, measured in the same run: the
+    small-pair batch (area forward + backward, one CUDA graph launch per step)
+    and one base against many overlays (forward, and area forward + backward),
+    each next to the plain per-pair GPU path (one sbc_clip_pair_device call
+    per pair) on the same inputs."""
+    sub = argparse.Namespace(**vars(args))
+    sub.pairs = None
+    sub.overlays = None
+    sub.job_only = 0
+    sp = run_small_pairs(sub, rank, world)
+    om = run_one_to_many(sub, rank, world)
+    c3 = om["counts"]
+    out = {
+        "target": "batched forward+backward pairs/s >= 5x the plain per-pair GPU path",
+        "small_pairs_65536": {
+            "metric": sp["metric"], "pairs_per_s": sp["value"], "ms_per_step": sp["ms_per_step"],
+            "launch": "one CUDA graph per step (area forward + backward)",
+            "e2e_pairs_per_s": sp["e2e"]["value"],
+            "per_pair_gpu_path_pairs_per_s": sp["counts"]["per_pair_gpu_path_pairs_per_s"],
+            "forward_backward_over_per_pair": sp["counts"]["batched_over_per_pair"],
+            "gpu_launches": sp["gpu_launches"], "roofline": sp["roofline"],
+            "kernels_top": dict(list(sp["kernels_top"].items())[:4]), "clocks": sp["clocks"],
+            "cpu_baseline": sp.get("cpu_baseline")},
+        "one_to_many_200k_10000": {
+            "metric": "clipped pairs/s, one 200k-vertex base x 10,000 overlays",
+            "forward_pairs_per_s": om["value"], "forward_ms_per_step": om["ms_per_step"],
+            "forward_backward_pairs_per_s": c3["area_forward_backward_pairs_per_s"],
+            "forward_backward_ms_per_step": c3["area_forward_backward_ms"],
+            "e2e_forward_pairs_per_s": om["e2e"]["value"],
+            "per_pair_gpu_path_pairs_per_s": c3["per_pair_gpu_path_pairs_per_s"],
+            "forward_over_per_pair": c3["batched_over_per_pair"],
+            "forward_backward_over_per_pair":
+                c3["area_forward_backward_pairs_per_s"] / c3["per_pair_gpu_path_pairs_per_s"],
+            "autotuned": om["config"]["autotuned"], "gpu_launches": om["gpu_launches"],
+            "roofline": om["roofline"], "kernels_top": dict(list(om["kernels_top"].items())[:4]),
+            "clocks": om["clocks"], "cpu_baseline": om.get("cpu_baseline")},
+    }
+    return out
+
+
+def extra_cpu_baselines(foster_full: bool):
+    """The reference's CPU build at one thread and at every host thread on the
+    10k x 8k pair, and Foster's sequential code on 64 small pairs (and, with
+    foster_full, on the 10k x 8k pair: about 5 minutes)."""
+    import oracle_py as O
+    out = []
+    b, c = gen.pair_small()
+    threads = os.cpu_count() or 1
+    if O.ref_available():
+        for t in (1, threads):
+            t0 = time.perf_counter()
+            res = O.run_reference(b, [c], threads=t, precision=6, timeout=600)
+            wall = (time.perf_counter() - t0) * 1e3
+            tl = res["time_line"]
+            out.append({"impl": "reference", "cores": t, "workload": "pair_10k_8k",
+                        "value": tl[-1] / 1e3 if tl else wall, "unit": "ms"})
+    if O.foster_available():
+        pairs = gen.small_pairs(64, seed=4000)
+        t0 = time.perf_counter()
+        for pb, pc in pairs:
+            O.run_foster(pb, pc)
+        out.append({"impl": "foster", "cores": 1, "workload": "small_pairs sample (64 pairs)",
+                    "value": len(pairs) / (time.perf_counter() - t0), "unit": "pairs/s"})
+        if foster_full:
+            out.append({"impl": "foster", "cores": 1, "workload": "pair_10k_8k",
+                        "value": O.run_foster(b, c)["ms"], "unit": "ms"})
     return out
 
 
@@ -837,6 +1016,10 @@ def main():
                     choices=["pair_1m_1m", "pair_200k_200k", "pair_10k_8k", "small_pairs_65536",
                              "one_to_many_200k_10000", "uneven_pairs_1m"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="pair_1m_1m only: leave out the batched measurements")
+    ap.add_argument("--foster", action="store_true",
+                    help="also time Foster's sequential code on the 10k x 8k pair (~5 min)")
     ap.add_argument("--job-only", type=int, default=0,
                     help="one_to_many only: run the job this many times and print no JSON "
                          "line (for profilers)")
@@ -854,6 +1037,8 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
+        # host-side gathers of per-pair outputs (no device collective on the data path)
+        args.gloo = dist.new_group(backend="gloo")
     if args.workload.startswith("small_pairs"):
         out = run_small_pairs(args, rank, world)
     elif args.workload.startswith("one_to_many"):

@@ -46,6 +46,9 @@ typedef struct sbc_options {
                                       reference's seg driver leaves off; every clipping
                                       call of the context (pair, one-to-many, batches,
                                       pairwise) then returns union rings */
+#define SBC_FLAG_ENDPOINT_SORT 8   /* build the elementary intervals from a sort of all 2E edge
+                                      endpoints instead of the E vertices (a test hook: the
+                                      arrays and rings are the same either way) */
 
 typedef struct sbc_rings {
   int nrings;
@@ -92,7 +95,11 @@ int sbc_clip_pair_device(sbc_ctx* ctx, const double* d_b_xy, int nb, const doubl
 #define SBC_STAT_SERIAL_BACKEND 10      /* 1 if the exact serial back end ran */
 #define SBC_STAT_WORK_UNITS 11          /* overlay 1: edge-box pairs tested by the grid join */
 #define SBC_STAT_GRID_PAIRS 12          /* overlay 1: box-overlapping edge pairs the grid found */
-#define SBC_STAT_NUM 13
+#define SBC_STAT_VERTEX_SORT 13         /* 1 if the endpoint order came from the vertex sort */
+#define SBC_STAT_OUTSIDE_CMBR 14        /* edges whose box misses the common MBR of the base and
+                                           the overlays (left out of the candidate search; the
+                                           reference's getCMBR, src/clip.cpp:743-777) */
+#define SBC_STAT_NUM 15
 int sbc_stats(const sbc_ctx* ctx, long long* out, int n);
 
 /* Per-phase device milliseconds of the last call when SBC_FLAG_TIMING is set:
@@ -248,6 +255,12 @@ int sbc_pairwise_set_cell_factor(sbc_ctx* ctx, double factor);
  * at a time, each on its own stream); default 8192.  A tuning knob: results
  * do not depend on it. */
 int sbc_pairwise_set_split(sbc_ctx* ctx, int records);
+/* Host worker threads (each with its own stream) that clip the big overlays
+ * concurrently with the one-warp-per-pair kernel; default 8, 1 to 64.  A
+ * tuning knob: results do not depend on it (1 serialises the big overlays,
+ * which per-kernel profiling needs).  sbc_pairwise_get_workers reads it. */
+int sbc_pairwise_set_workers(sbc_ctx* ctx, int workers);
+int sbc_pairwise_get_workers(const sbc_ctx* ctx);
 /* Autotuner: runs the job (device arrays, as for sbc_clip_pairwise_device)
  * under several splits, block-slot reserves and worker counts for the big
  * overlays, and cell widths, keeps the fastest setting in the

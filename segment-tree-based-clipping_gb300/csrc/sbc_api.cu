@@ -134,6 +134,8 @@ void fill_stats(sbc_ctx* c) {
   c->stats[SBC_STAT_TREE_SIZE] = pl.stat_ts;
   c->stats[SBC_STAT_COVER_ENTRIES] = pl.stat_cover;
   c->stats[SBC_STAT_LEAF_END_ENTRIES] = pl.stat_leaf;
+  c->stats[SBC_STAT_VERTEX_SORT] = pl.stat_vertex_sort;
+  c->stats[SBC_STAT_OUTSIDE_CMBR] = pl.stat_outside_cmbr;
   if (!pl.outputs().empty()) {
     const auto& o = pl.outputs()[0];
     c->stats[SBC_STAT_CANDIDATES_TESTED] = o.tests;
@@ -155,6 +157,7 @@ int run_device(sbc_ctx* c, const double* d_b, int nb, const double* d_c, const i
   pl.set_stream(st);
   pl.timing = (c->flags & SBC_FLAG_TIMING) != 0;
   pl.force_serial_backend = (c->flags & SBC_FLAG_SERIAL_BACKEND) ? 1 : 0;
+  pl.force_endpoint_sort = (c->flags & SBC_FLAG_ENDPOINT_SORT) ? 1 : 0;
   int rc = pl.run(d_b, nb, d_c, sizes, k);
   if (rc) return set_err(c, rc, pl.error());
   fill_stats(c);
@@ -751,6 +754,15 @@ extern "C" int sbc_pairwise_set_split(sbc_ctx* c, int records) {
   c->pw->big_k = records;
   return SBC_OK;
 }
+
+extern "C" int sbc_pairwise_set_workers(sbc_ctx* c, int workers) {
+  if (!c) return SBC_EINPUT;
+  if (workers < 1 || workers > 64) return set_err(c, SBC_EINPUT, "workers must be 1 to 64");
+  c->pw->big_workers = workers;
+  return SBC_OK;
+}
+
+extern "C" int sbc_pairwise_get_workers(const sbc_ctx* c) { return c ? c->pw->big_workers : -1; }
 
 extern "C" int sbc_pairwise_autotune(sbc_ctx* c, const sbc_pairwise_job* j, int* split,
                                      double* cell_factor, double* best_ms, void* stream) {

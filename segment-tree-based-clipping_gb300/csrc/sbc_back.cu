@@ -22,6 +22,7 @@
 // entry/exit structure, coordinate collisions in the list bridge) are
 // detected on the device and run through `k_serial_backend`, a single-thread
 // kernel that follows the reference's linked-list algorithm step by step.
+#include <cooperative_groups.h>
 #include <cstdio>
 #include <mutex>
 
@@ -266,6 +267,90 @@ __global__ void k_tr_jump(int n, const int* __restrict__ jin, const int* __restr
   int a = min_[x], b = min_[j];
   mout[x] = a < b ? a : b;
   jout[x] = jin[j];
+}
+
+// The two pointer-jumping passes below as one cooperative launch each,
+// rounds separated by grid-wide barriers and ended on the device as soon as
+// a round changes nothing that is read afterwards:
+//  * orbit minimum (k_tr_jump): after round r every element holds the
+//    minimum over the next 2^(r+1) elements of its orbit; a round that
+//    changes no minimum means every orbit is covered (the orbit's minimum is
+//    unique, and it would reach a new element in every round until then);
+//  * weighted list ranking (k_lr_jump): after round r an element's pointer
+//    is -1 iff it is fewer than 2^(r+1) hops from its path's end; a path
+//    holding an element 2^r hops from its end ends one in round r, so a
+//    round that ends none leaves no path unfinished (orbits that never meet
+//    the break stay cycles and are not read).
+// The flag of round r is flags[r % 3]; thread 0 clears flags[(r + 1) % 3] at
+// the start of round r, which every thread last read before the barrier that
+// ended round r - 1.  Every thread reads the same flag after the same
+// barrier, so all leave the loop in the same round.  The result is left in
+// the A arrays.
+__global__ void k_tr_jump_coop(int n, int* __restrict__ jA, int* __restrict__ mA,
+                               int* __restrict__ jB, int* __restrict__ mB,
+                               unsigned* __restrict__ flags, int max_rounds) {
+  cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nth = (long long)gridDim.x * blockDim.x;
+  int *jin = jA, *min_ = mA, *jout = jB, *mout = mB;
+  for (int r = 0; r < max_rounds; ++r) {
+    if (tid == 0) flags[(r + 1) % 3] = 0u;
+    bool ch = false;
+    for (long long x = tid; x < n; x += nth) {
+      const int j = jin[x];
+      const int a = min_[x], b = min_[j];
+      const int m = a < b ? a : b;
+      mout[x] = m;
+      jout[x] = jin[j];
+      ch |= m != a;
+    }
+    if (__any_sync(0xffffffffu, ch) && (threadIdx.x & 31) == 0) atomicOr(&flags[r % 3], 1u);
+    grid.sync();
+    int* t0 = jin; jin = jout; jout = t0;
+    int* t1 = min_; min_ = mout; mout = t1;
+    if (*(volatile unsigned*)&flags[r % 3] == 0u) break;
+  }
+  if (min_ != mA)
+    for (long long x = tid; x < n; x += nth) {
+      mA[x] = min_[x];
+      jA[x] = jin[x];
+    }
+}
+
+__global__ void k_lr_jump_coop(int n, int* __restrict__ nA, long long* __restrict__ SA,
+                               int* __restrict__ nB, long long* __restrict__ SB,
+                               unsigned* __restrict__ flags, int max_rounds) {
+  cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nth = (long long)gridDim.x * blockDim.x;
+  int *nin = nA, *nout = nB;
+  long long *Sin = SA, *Sout = SB;
+  for (int r = 0; r < max_rounds; ++r) {
+    if (tid == 0) flags[(r + 1) % 3] = 0u;
+    bool ch = false;
+    for (long long x = tid; x < n; x += nth) {
+      const int j = nin[x];
+      if (j < 0) {
+        nout[x] = -1;
+        Sout[x] = Sin[x];
+      } else {
+        const int jj = nin[j];
+        nout[x] = jj;
+        Sout[x] = Sin[x] + Sin[j];
+        ch |= jj < 0;
+      }
+    }
+    if (__any_sync(0xffffffffu, ch) && (threadIdx.x & 31) == 0) atomicOr(&flags[r % 3], 1u);
+    grid.sync();
+    int* t0 = nin; nin = nout; nout = t0;
+    long long* t1 = Sin; Sin = Sout; Sout = t1;
+    if (*(volatile unsigned*)&flags[r % 3] == 0u) break;
+  }
+  if (nin != nA)
+    for (long long x = tid; x < n; x += nth) {
+      nA[x] = nin[x];
+      SA[x] = Sin[x];
+    }
 }
 
 // every enex vertex must agree with its successor and its target on the
@@ -585,6 +670,44 @@ __global__ void k_serial_emit(SerialArgs a, int* __restrict__ ooff, double* __re
 }  // namespace
 
 // ============================================================== host driver
+// One cooperative launch of a jump kernel above over n elements, with as
+// many blocks as can be resident at once (grid-wide barriers need them all
+// running); false if the launch is refused, and the caller then runs the
+// plain launch loop.
+template <typename A>
+static bool jump_coop(void (*kern)(int, int*, A*, int*, A*, unsigned*, int), int n, int* pA,
+                      A* vA, int* pB, A* vB, unsigned* flags, int rounds, cudaStream_t st) {
+  if (n <= 0) return true;
+  static std::mutex mu;
+  static int cap[64][2] = {};  // per device and value type: co-resident blocks of 256 threads
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+  const int kind = sizeof(A) == 8 ? 1 : 0;
+  int maxb = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!cap[dev][kind]) {
+      int per = 0, sms = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)kern, 256, 0) !=
+              cudaSuccess ||
+          cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+          per < 1)
+        return false;
+      cap[dev][kind] = per * sms;
+    }
+    maxb = cap[dev][kind];
+  }
+  const int blocks = (int)std::min<long long>(((long long)n + 255) / 256, (long long)maxb);
+  if (cudaMemsetAsync(flags, 0, 3 * sizeof(unsigned), st) != cudaSuccess) return false;
+  void* args[] = {&n, &pA, &vA, &pB, &vB, &flags, &rounds};
+  ::sbc::KProbe kp_(kind ? "k_lr_jump_coop" : "k_tr_jump_coop", st);
+  if (cudaLaunchCooperativeKernel((const void*)kern, dim3(blocks), dim3(256), args, 0, st) ==
+      cudaSuccess)
+    return true;
+  cudaGetLastError();  // this refused launch's own error: the loop below replaces it
+  return false;
+}
+
 static int serial_backend(Pipeline& pl, const Merged& m, OverlayOut& out, int tag) {
   cudaStream_t st = pl.stream();
   BufferPool& bp = pl.pool();
@@ -839,13 +962,19 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
       ::sbc::KProbe kp_("k_tr_init", st);
       k_tr_init<<<grid_for(nE, 256), 256, 0, st>>>(T, jmpA, mA, sc);
     }
-    for (int span = 1; span < nE; span <<= 1) {
-      {
-        ::sbc::KProbe kp_("k_tr_jump", st);
-        k_tr_jump<<<grid_for(nE, 256), 256, 0, st>>>(nE, jmpA, mA, jmpB, mB);
+    int rounds = 0;
+    for (int span = 1; span < nE; span <<= 1) ++rounds;
+    unsigned* jflags = (unsigned*)bp.get("bk_jump_flags", 256);
+    if (bp.failed) return pl.fail(kENoMem, "device allocation failed (rings)");
+    if (!jump_coop(k_tr_jump_coop, nE, jmpA, mA, jmpB, mB, jflags, rounds, st)) {
+      for (int r = 0; r < rounds; ++r) {
+        {
+          ::sbc::KProbe kp_("k_tr_jump", st);
+          k_tr_jump<<<grid_for(nE, 256), 256, 0, st>>>(nE, jmpA, mA, jmpB, mB);
+        }
+        std::swap(jmpA, jmpB);
+        std::swap(mA, mB);
       }
-      std::swap(jmpA, jmpB);
-      std::swap(mA, mB);
     }
     {
       ::sbc::KProbe kp_("k_tr_consistent", st);
@@ -882,11 +1011,13 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
       ::sbc::KProbe kp_("k_lr_init", st);
       k_lr_init<<<grid_for(nE, 256), 256, 0, st>>>(T, mA, nxA, SA, ringI, indeg, sc);
     }
-    for (int span = 1; span < nE; span <<= 1) {
-      ::sbc::KProbe kp_("k_lr_jump", st);
-      k_lr_jump<<<grid_for(nE, 256), 256, 0, st>>>(nE, nxA, SA, nxB, SB);
-      std::swap(nxA, nxB);
-      std::swap(SA, SB);
+    if (!jump_coop(k_lr_jump_coop, nE, nxA, SA, nxB, SB, jflags, rounds, st)) {
+      for (int r = 0; r < rounds; ++r) {
+        ::sbc::KProbe kp_("k_lr_jump", st);
+        k_lr_jump<<<grid_for(nE, 256), 256, 0, st>>>(nE, nxA, SA, nxB, SB);
+        std::swap(nxA, nxB);
+        std::swap(SA, SB);
+      }
     }
     {
       ::sbc::KProbe kp_("k_lr_check", st);

@@ -72,58 +72,59 @@ struct Grid {
   }
 };
 
-// float edge boxes (bounds rounded outwards), their union and summed extent
+// Float edge boxes (bounds rounded outwards), the bounding box of the base's
+// edges and of the overlays' edges, and the summed extent.  bnd holds order
+// keys: [0..3] base box, [4..7] overlay box (min x, min y, max x, max y).
 __global__ void k_edge_fbox(int E, const int* __restrict__ e_id, const int* __restrict__ tstart,
                             int k, const double* __restrict__ bP, const double* __restrict__ cP,
                             float4* __restrict__ fbox, unsigned* __restrict__ bnd,
                             double* __restrict__ sum_ext) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned k0 = 0xffffffffu, k1 = 0xffffffffu, k2 = 0u, k3 = 0u;
+  // per class (0 base, 1 overlays): min x, min y, max x, max y as order keys
+  unsigned kb[2][4] = {{0xffffffffu, 0xffffffffu, 0u, 0u}, {0xffffffffu, 0xffffffffu, 0u, 0u}};
   float ext = 0.f;
   if (e < E) {
-    const double* p = (class_of_edge(tstart, k, e) == 0 ? bP : cP) + e_id[e];
+    const int cl = class_of_edge(tstart, k, e) == 0 ? 0 : 1;
+    const double* p = (cl == 0 ? bP : cP) + e_id[e];
     const float4 f = make_float4(__double2float_rd(fmin(p[0], p[2])), __double2float_rd(fmin(p[1], p[3])),
                                  __double2float_ru(fmax(p[0], p[2])), __double2float_ru(fmax(p[1], p[3])));
     fbox[e] = f;
-    k0 = fkey(f.x);
-    k1 = fkey(f.y);
-    k2 = fkey(f.z);
-    k3 = fkey(f.w);
+    kb[cl][0] = fkey(f.x);
+    kb[cl][1] = fkey(f.y);
+    kb[cl][2] = fkey(f.z);
+    kb[cl][3] = fkey(f.w);
     ext = fmaxf(f.z - f.x, f.w - f.y);
   }
   for (int o = 16; o > 0; o >>= 1) {
-    k0 = min(k0, __shfl_xor_sync(0xffffffffu, k0, o));
-    k1 = min(k1, __shfl_xor_sync(0xffffffffu, k1, o));
-    k2 = max(k2, __shfl_xor_sync(0xffffffffu, k2, o));
-    k3 = max(k3, __shfl_xor_sync(0xffffffffu, k3, o));
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      kb[c][0] = min(kb[c][0], __shfl_xor_sync(0xffffffffu, kb[c][0], o));
+      kb[c][1] = min(kb[c][1], __shfl_xor_sync(0xffffffffu, kb[c][1], o));
+      kb[c][2] = max(kb[c][2], __shfl_xor_sync(0xffffffffu, kb[c][2], o));
+      kb[c][3] = max(kb[c][3], __shfl_xor_sync(0xffffffffu, kb[c][3], o));
+    }
     ext += __shfl_xor_sync(0xffffffffu, ext, o);
   }
   // one set of atomics per block (same-address atomics serialise)
-  __shared__ unsigned sk[4][8];
+  __shared__ unsigned sk[8][8];
   __shared__ float se[8];
   const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
-    sk[0][w] = k0;
-    sk[1][w] = k1;
-    sk[2][w] = k2;
-    sk[3][w] = k3;
+    for (int j = 0; j < 8; ++j) sk[j][w] = kb[j >> 2][j & 3];
     se[w] = ext;
   }
   __syncthreads();
+  if (threadIdx.x < 8) {
+    const int j = threadIdx.x, nw = blockDim.x >> 5;
+    unsigned v = sk[j][0];
+    for (int i = 1; i < nw; ++i) v = (j & 3) < 2 ? min(v, sk[j][i]) : max(v, sk[j][i]);
+    if ((j & 3) < 2) atomicMin(&bnd[j], v);
+    else atomicMax(&bnd[j], v);
+  }
   if (threadIdx.x == 0) {
     const int nw = blockDim.x >> 5;
     double es = 0.0;
-    for (int i = 1; i < nw; ++i) {
-      k0 = min(k0, sk[0][i]);
-      k1 = min(k1, sk[1][i]);
-      k2 = max(k2, sk[2][i]);
-      k3 = max(k3, sk[3][i]);
-    }
     for (int i = 0; i < nw; ++i) es += se[i];
-    atomicMin(&bnd[0], k0);
-    atomicMin(&bnd[1], k1);
-    atomicMax(&bnd[2], k2);
-    atomicMax(&bnd[3], k3);
     atomicAdd(sum_ext, es);
   }
 }
@@ -132,13 +133,24 @@ __global__ void k_edge_fbox(int E, const int* __restrict__ e_id, const int* __re
 // counting sort: the order inside a bucket does not matter, each pair is a
 // set element and its emission key fixes its final order).  Edges spanning
 // more than kLongCells cells go to long_list instead.
+// Common-MBR filter (the reference's getCMBR, src/clip.cpp:743-777): an edge
+// whose box misses the intersection of the base's and the overlays' boxes
+// overlaps no edge of the other polygon, so it never forms a candidate pair.
+// Such an edge gets islong = 2 and enters neither the grid nor the long list
+// (the tree build keeps every edge: the elementary points do not change).
 __global__ void k_grid_count(int E, const float4* __restrict__ fbox, Grid g,
                              const int* __restrict__ tstart, int k, int* __restrict__ bcnt,
                              unsigned char* __restrict__ islong, int* __restrict__ long_list,
-                             unsigned* __restrict__ long_count) {
+                             unsigned* __restrict__ long_count, float4 cmbr,
+                             unsigned* __restrict__ outside) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
   const float4 f = fbox[e];
+  if (f.x > cmbr.z || f.z < cmbr.x || f.y > cmbr.w || f.w < cmbr.y) {
+    islong[e] = 2;
+    atomicAdd(outside, 1u);
+    return;
+  }
   const int x0 = g.cx(f.x), x1 = g.cx(f.z), y0 = g.cy(f.y), y1 = g.cy(f.w);
   const long long n = (long long)(x1 - x0 + 1) * (y1 - y0 + 1);
   const bool lg = n > kLongCells;
@@ -618,7 +630,7 @@ int Pipeline::stage_grid() {
   g_long_count = (unsigned*)pool_.get("grid_long_count", 256);
   if (pool_.failed) return fail(kENoMem, "device allocation failed (grid)");
   cudaMemcpyAsync(g_tstart, hstart.data(), sizeof(int) * (k + 2), cudaMemcpyHostToDevice, st);
-  unsigned init[4] = {0xffffffffu, 0xffffffffu, 0u, 0u};
+  unsigned init[8] = {0xffffffffu, 0xffffffffu, 0u, 0u, 0xffffffffu, 0xffffffffu, 0u, 0u};
   cudaMemcpyAsync(bnd, init, sizeof(init), cudaMemcpyHostToDevice, st);
   cudaMemsetAsync(sum_ext, 0, sizeof(double), st);
   cudaMemsetAsync(g_long_count, 0, sizeof(unsigned), st);
@@ -634,7 +646,7 @@ int Pipeline::stage_grid() {
     ::sbc::KProbe kp_("k_vertex_f4", st);
     k_vertex_f4<<<grid_for((long long)clSize + k, 256), 256, 0, st>>>((long long)clSize + k, cP, vfC);
   }
-  unsigned hb[4];
+  unsigned hb[8];
   double hsum = 0.0;
   cudaMemcpyAsync(hb, bnd, sizeof(hb), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(&hsum, sum_ext, sizeof(double), cudaMemcpyDeviceToHost, st);
@@ -645,7 +657,13 @@ int Pipeline::stage_grid() {
     memcpy(&f, &u, sizeof f);
     return f;
   };
-  const float x0 = unkey(hb[0]), y0 = unkey(hb[1]), x1 = unkey(hb[2]), y1 = unkey(hb[3]);
+  // the grid covers the common MBR: the base's box cut with the overlays'
+  // box (an empty cut leaves a one-cell grid that every edge misses)
+  float x0 = std::max(unkey(hb[0]), unkey(hb[4])), y0 = std::max(unkey(hb[1]), unkey(hb[5]));
+  float x1 = std::min(unkey(hb[2]), unkey(hb[6])), y1 = std::min(unkey(hb[3]), unkey(hb[7]));
+  const float4 cmbr = make_float4(x0, y0, x1, y1);
+  if (!(x1 >= x0)) x1 = x0;
+  if (!(y1 >= y0)) y1 = y0;
   const double spanx = (double)x1 - x0, spany = (double)y1 - y0;
   // cell size: 1.5 x the mean edge extent, with at most max(2^21, 4E)
   // (cell, class) buckets in all
@@ -668,15 +686,20 @@ int Pipeline::stage_grid() {
   if (pool_.failed) return fail(kENoMem, "device allocation failed (grid buckets)");
   cudaMemsetAsync(g_bstart, 0, sizeof(int) * (nBk + 1), st);
   cudaMemsetAsync(fill, 0, sizeof(int) * (nBk + 1), st);
+  unsigned* outside = (unsigned*)((char*)bnd + 128);
+  cudaMemsetAsync(outside, 0, sizeof(unsigned), st);
   {
     ::sbc::KProbe kp_("k_grid_count", st);
     k_grid_count<<<grid_for(E, 256), 256, 0, st>>>(E, fbox, g, g_tstart, k, g_bstart, g_islong,
-                                                 g_long, g_long_count);
+                                                 g_long, g_long_count, cmbr, outside);
   }
   exclusive_scan_i32(g_bstart, nBk + 1, sscr2, st);
   int total = 0;
+  unsigned n_out = 0;
   cudaMemcpyAsync(&total, g_bstart + nBk, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(&n_out, outside, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "grid count");
+  stat_outside_cmbr = n_out;
   if (total < 0) return fail(kEInput, "grid too large");
   g_n = total;
   g_vals = (unsigned*)pool_.get("grid_vals", sizeof(unsigned) * ((long long)total + 1));

@@ -112,7 +112,8 @@ __global__ void k_setup_edges(const double* __restrict__ bP, const double* __res
                               const int* __restrict__ cS, const int* __restrict__ cc, int nb, int k,
                               int E, int* __restrict__ eid, double* __restrict__ es,
                               double* __restrict__ ee, unsigned long long* __restrict__ minmax,
-                              unsigned* __restrict__ flags) {
+                              unsigned* __restrict__ flags, unsigned long long* __restrict__ vkey,
+                              unsigned* __restrict__ vid, unsigned char* __restrict__ eflip) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long kmin = ~0ull, kmax = 0ull;
   if (e < E) {
@@ -137,6 +138,11 @@ __global__ void k_setup_edges(const double* __restrict__ bP, const double* __res
       ee[e] = a;
       es[e] = b;
     }
+    // the edge's first vertex (vertex e) as a sort key, and whether it is the
+    // edge's end point (endpoint 2e+1) rather than its start (2e)
+    vkey[e] = dkey(a);
+    vid[e] = (unsigned)e;
+    eflip[e] = (a < b) ? 0 : 1;
     // every vertex is the first endpoint of exactly one edge: min/max over
     // vertices equals the reference's min/max over non-closing edges
     if (!isfinite(a)) atomicOr(flags, (unsigned)kFlagUndef);
@@ -183,6 +189,9 @@ int Pipeline::stage_setup(const double* d_bxy, const double* d_cxy, const int* c
   e_e = (double*)pool_.get("e_e", sizeof(double) * E);
   unsigned long long* mm = (unsigned long long*)pool_.get("minmax", 16);
   d_flags = (unsigned*)pool_.get("flags", 256);
+  v_key = (unsigned long long*)pool_.get("v_key", sizeof(unsigned long long) * E);
+  v_id = (unsigned*)pool_.get("v_id", sizeof(unsigned) * E);
+  e_flip = (unsigned char*)pool_.get("e_flip", E);
   if (pool_.failed) return fail(kENoMem, "device allocation failed (setup)");
   cudaMemcpyAsync(cS, hcS.data(), sizeof(int) * (k + 1), cudaMemcpyHostToDevice, st_);
   cudaMemcpyAsync(cc, hcc.data(), sizeof(int) * (k + 1), cudaMemcpyHostToDevice, st_);
@@ -200,7 +209,7 @@ int Pipeline::stage_setup(const double* d_bxy, const double* d_cxy, const int* c
   {
     ::sbc::KProbe kp_("k_setup_edges", st_);
     k_setup_edges<<<grid_for(E, 256), 256, 0, st_>>>(bP, cP, cS, cc, nb, k, E, e_id, e_s, e_e, mm,
-                                                   d_flags);
+                                                   d_flags, v_key, v_id, e_flip);
   }
   unsigned long long hm[2];
   unsigned hf = 0;
@@ -224,6 +233,41 @@ __global__ void k_ele_keys(const double* __restrict__ es, const double* __restri
   keys[2 * j + 1] = dkey(ee[j]);
   vals[2 * j] = 2 * j;
   vals[2 * j + 1] = 2 * j + 1;
+}
+
+// The endpoint order from the vertex order.  Every endpoint is a vertex's
+// x value, and vertex v is an endpoint of exactly two edges: of edge v (index
+// 2v, or 2v+1 when the edge runs right to left and v is its end) and of the
+// polygon's previous edge p (v is that edge's second vertex: index 2p+1, or
+// 2p when p runs right to left).  When no other vertex shares v's x value,
+// its two endpoints are a run of their own in the stable endpoint sort, in
+// index order; a shared x value sets kFlagSharedX and the caller sorts the
+// endpoints themselves instead.
+__global__ void k_ele_expand(const unsigned long long* __restrict__ skey,
+                             const unsigned* __restrict__ svid,
+                             const unsigned char* __restrict__ flip, const int* __restrict__ cc,
+                             int nb, int k, int E, unsigned long long* __restrict__ keys,
+                             unsigned* __restrict__ sidx, unsigned* __restrict__ flags) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= E) return;
+  const unsigned long long key = skey[i];
+  if ((i > 0 && skey[i - 1] == key) || (i + 1 < E && skey[i + 1] == key))
+    atomicOr(flags, (unsigned)kFlagSharedX);
+  const int v = (int)svid[i];
+  int p;
+  if (v < nb) {
+    p = v ? v - 1 : nb - 1;
+  } else {
+    const int g = v - nb;
+    const int o = overlay_of(cc, k, g);
+    p = g == cc[o] ? nb + cc[o + 1] - 1 : v - 1;
+  }
+  const unsigned a = 2u * (unsigned)v + flip[v];
+  const unsigned b = 2u * (unsigned)p + 1u - flip[p];
+  keys[2LL * i] = key;
+  keys[2LL * i + 1] = key;
+  sidx[2LL * i] = a < b ? a : b;
+  sidx[2LL * i + 1] = a < b ? b : a;
 }
 
 __device__ __forceinline__ double ele_val(const double* es, const double* ee, unsigned idx) {
@@ -311,13 +355,26 @@ int Pipeline::stage_elementary() {
   int* flag = (int*)pool_.get("ele_flag", sizeof(int) * (n2 + 1));
   double* val = (double*)pool_.get("ele_val", sizeof(double) * n2);
   void* sscr = pool_.get("scan_scr", scan_scratch_bytes(n2 + 1));
+  auto* vkey2 = (unsigned long long*)pool_.get("v_key2", sizeof(unsigned long long) * E);
+  auto* vid2 = (unsigned*)pool_.get("v_id2", sizeof(unsigned) * E);
   if (pool_.failed) return fail(kENoMem, "device allocation failed (elementary)");
-  {
-    ::sbc::KProbe kp_("k_ele_keys", st_);
-    k_ele_keys<<<grid_for(E, 256), 256, 0, st_>>>(e_s, e_e, E, keys, sidx);
-  }
   // every endpoint is a vertex x value: its key lies in the setup's [min, max]
-  radix_sort_u64_within(keys, sidx, keys2, sidx2, n2, key_lo, key_hi, rscr, st_);
+  bool by_vertex = !force_endpoint_sort;
+  int count = 0, before_last = 0;
+  for (;;) {
+  if (by_vertex) {
+    // sort the E vertex keys, then expand to the 2E endpoints
+    radix_sort_u64_within(v_key, v_id, vkey2, vid2, E, key_lo, key_hi, rscr, st_);
+    ::sbc::KProbe kp_("k_ele_expand", st_, 12.0 * E + 9.0 * E + 24.0 * E);
+    k_ele_expand<<<grid_for(E, 256), 256, 0, st_>>>(v_key, v_id, e_flip, cc, nb, k, E, keys, sidx,
+                                                    d_flags);
+  } else {
+    {
+      ::sbc::KProbe kp_("k_ele_keys", st_);
+      k_ele_keys<<<grid_for(E, 256), 256, 0, st_>>>(e_s, e_e, E, keys, sidx);
+    }
+    radix_sort_u64_within(keys, sidx, keys2, sidx2, n2, key_lo, key_hi, rscr, st_);
+  }
   cudaMemsetAsync(vl, 0, sizeof(int) * (E + 1), st_);
   {
     ::sbc::KProbe kp_("k_vl_mark", st_);
@@ -334,10 +391,20 @@ int Pipeline::stage_elementary() {
     k_ele_flags<<<grid_for(n2, 256), 256, 0, st_>>>(sidx, e_s, e_e, vl, vloc, E, flag, val);
   }
   exclusive_scan_i32(flag, n2 + 1, sscr, st_);
-  int count = 0, before_last = 0;
+  unsigned fl = 0;
   cudaMemcpyAsync(&count, flag + n2, sizeof(int), cudaMemcpyDeviceToHost, st_);
   cudaMemcpyAsync(&before_last, flag + n2 - 1, sizeof(int), cudaMemcpyDeviceToHost, st_);
+  cudaMemcpyAsync(&fl, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st_);
   cudaStreamSynchronize(st_);
+  if (by_vertex && (fl & kFlagSharedX)) {
+    // a shared x value: the endpoints' own stable sort decides their order
+    by_vertex = false;
+    clear_flags();
+    continue;
+  }
+  break;
+  }
+  stat_vertex_sort = by_vertex ? 1 : 0;
   if (count < 1) return fail(kEUndef, "no elementary interval (all endpoints equal)");
   int round = npow2_host(count) + 1;
   epc = round;

@@ -41,6 +41,7 @@ enum DevFlag : unsigned {
   kFlagSlowPath = 4u,       // back end needs the serial emulation path
   kFlagSpin = 8u,           // a bounded wait gave up
   kFlagUnsorted = 16u,      // the elementary array is not in order
+  kFlagSharedX = 32u,       // two vertices share an x value (endpoint order needs the full sort)
 };
 
 // ---------------------------------------------------------------- FP64 geometry
@@ -204,7 +205,8 @@ bool scan_error_take();
 
 // Stable LSD radix sort of (key, value) pairs, 8-bit digits, only the digit
 // positions that vary are sorted.  keys/vals are sorted in place; tmp buffers
-// of the same sizes plus `radix_scratch_bytes(n)` bytes are needed.
+// of the same sizes plus `radix_scratch_bytes(n)` bytes are needed; n < 2^32.
+// No host synchronisation.
 size_t radix_scratch_bytes(long long n);
 void radix_sort_u32(unsigned* keys, unsigned* vals, unsigned* keys_tmp, unsigned* vals_tmp,
                     long long n, int key_bits, void* scratch, cudaStream_t st);

@@ -62,6 +62,7 @@ class Pipeline {
   Timing times;
   // tree statistics of the last run
   long long stat_edges = 0, stat_epc = 0, stat_ts = 0, stat_cover = 0, stat_leaf = 0;
+  long long stat_outside_cmbr = 0;     // edges left out of the candidate grid (common MBR)
   // force the serial emulation of the back end (test hook)
   int force_serial_backend = 0;
   // union instead of intersection (the Foster back end's UNION switch)
@@ -77,6 +78,11 @@ class Pipeline {
   int* e_id = nullptr;
   double* e_s = nullptr;
   double* e_e = nullptr;
+  unsigned long long* v_key = nullptr;  // per vertex (= its edge): order key of its x value
+  unsigned* v_id = nullptr;            // vertex index (the sort's payload)
+  unsigned char* e_flip = nullptr;     // edge runs right to left (its first vertex is its end)
+  int force_endpoint_sort = 0;         // test hook: sort the 2E endpoints, not the E vertices
+  int stat_vertex_sort = 0;            // the last run's endpoint order came from the vertex sort
   double minI = 0, maxI = 0;
   unsigned long long key_lo = 0, key_hi = 0;  // order keys of minI and maxI
   // tree

@@ -2,9 +2,9 @@
 //
 // These replace the reference's Thrust calls (p_seg_tree/thrust_func.cu:19-42:
 // stable_sort_by_key on double / int / long keys, exclusive_scan on int /
-// long).  HBM-bound: each radix pass reads and writes every (key, value) once
-// plus a per-tile digit histogram; passes whose digit is constant over all
-// keys are skipped (one OR/AND reduction decides).
+// long).  HBM-bound: each radix pass reads and writes every (key, value)
+// once; one histogram kernel counts all digit positions up front, and passes
+// whose digit is constant over all keys are skipped on the device.
 #include "sbc_internal.cuh"
 
 #include <cstdint>
@@ -360,208 +360,358 @@ void exclusive_scan_i64(long long* d, long long n, void* scratch, cudaStream_t s
 }
 
 // ============================================================== radix sort
+// Stable LSD radix sort with 8-bit digits in the onesweep arrangement
+// (Adinets and Merrill, "Onesweep: a faster least significant digit radix
+// sort for GPUs", 2022).  One histogram kernel counts every digit position in
+// a single read of the keys.  Each pass is then one scatter kernel: a tile
+// ranks its keys per digit with warp match/popc, publishes its per-digit
+// counts, and takes its bucket offsets from a decoupled look-back over the
+// tiles before it (a tile takes its index from a counter, so every earlier
+// tile is already running; waits are bounded).  Keys are staged in shared
+// memory in tile order so each digit's run is written out contiguously.
+// A pass whose digit is the same for every key (one bucket holds all n) is
+// skipped on the device, and which buffer a pass reads is worked out on the
+// device from the passes before it, so the sort never waits on the host.
 namespace {
 
-constexpr int kRadThreads = 256;
-constexpr int kRadWarps = kRadThreads / 32;
-// 32-key rounds per warp: 4, 8 or 16 (tiles of 1024, 2048 or 4096 keys),
-// chosen per sort so that the grid has about four CTAs per SM
-constexpr int kRadMinTile = kRadThreads * 4;
+constexpr int kOsThreads = 256;
+constexpr int kOsWarps = kOsThreads / 32;
+constexpr int kOsItems = 16;                    // keys per thread
+constexpr int kOsTile = kOsThreads * kOsItems;  // 4096 keys per tile
+constexpr int kOsMaxPasses = 8;
+constexpr int kOsHistItems = 4;                 // keys per thread per round of the histogram
+constexpr unsigned long long kOsAgg = 1ull << 62, kOsInc = 2ull << 62;
+constexpr unsigned long long kOsMask = (1ull << 62) - 1;
+constexpr size_t kOsHistBytes = sizeof(unsigned long long) * kOsMaxPasses * 256;
+constexpr size_t kOsCtrBytes = 256;
+
+// the digit positions (bytes) the host launches passes for, in order
+struct OsPlan {
+  int npass;
+  int pos[kOsMaxPasses];
+};
 
 template <typename K>
-__global__ void k_bits_reduce(const K* __restrict__ keys, long long n, K* __restrict__ out_or,
-                              K* __restrict__ out_and) {
-  K o = 0, a = ~K(0);
+__device__ __forceinline__ unsigned os_digit(K k, int pos) {
+  return (unsigned)((k >> (8 * pos)) & 0xffu);
+}
+
+// Counts of every planned digit position in one read of the keys (warp
+// aggregated with match_any: skewed digits do not serialise on one shared
+// counter).  Also zeroes the look-back words of the first pass.
+template <typename K>
+__global__ void __launch_bounds__(kOsThreads)
+k_os_hist(const K* __restrict__ keys, long long n, OsPlan plan,
+          unsigned long long* __restrict__ hist, unsigned long long* __restrict__ look0,
+          long long look_words) {
+  __shared__ unsigned h[kOsMaxPasses][256];
+  for (int i = threadIdx.x; i < kOsMaxPasses * 256; i += kOsThreads) (&h[0][0])[i] = 0u;
+  const long long gstride = (long long)gridDim.x * kOsThreads;
+  for (long long i = (long long)blockIdx.x * kOsThreads + threadIdx.x; i < look_words; i += gstride)
+    look0[i] = 0ull;
+  __syncthreads();
+  const unsigned lt = (1u << (threadIdx.x & 31)) - 1u;
+  const long long step = gstride * kOsHistItems;
+  // the loop bound is the same for every thread of the block, so whole warps
+  // reach the match instructions
+  for (long long base = (long long)blockIdx.x * kOsThreads * kOsHistItems; base < n; base += step) {
+    K k[kOsHistItems];
+    bool ok[kOsHistItems];
+#pragma unroll
+    for (int r = 0; r < kOsHistItems; ++r) {
+      const long long j = base + (long long)r * kOsThreads + threadIdx.x;
+      ok[r] = j < n;
+      k[r] = ok[r] ? keys[j] : K(0);
+    }
+#pragma unroll
+    for (int r = 0; r < kOsHistItems; ++r) {
+      for (int q = 0; q < plan.npass; ++q) {
+        const unsigned d = ok[r] ? os_digit(k[r], plan.pos[q]) : 256u;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        if (ok[r] && (peers & lt) == 0u) atomicAdd(&h[q][d], (unsigned)__popc(peers));
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < plan.npass * 256; i += kOsThreads) {
+    const unsigned v = (&h[0][0])[i];
+    if (v) atomicAdd(&hist[i], (unsigned long long)v);
+  }
+}
+
+// whether planned pass q sorts nothing: its histogram has one bucket of n
+// (warp-wide: every lane of the calling warp must take part)
+__device__ __forceinline__ bool os_constant(const unsigned long long* __restrict__ hist, int q,
+                                            long long n) {
+  bool full = false;
+  for (int d = threadIdx.x & 31; d < 256; d += 32) full |= hist[q * 256 + d] == (unsigned long long)n;
+  return __any_sync(0xffffffffu, full);
+}
+
+// exclusive scan of one value per thread over a 256-thread block
+template <typename T>
+__device__ __forceinline__ T os_block_scan(T v, T* s_warp) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  T x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[w] = x;
+  __syncthreads();
+  T off = 0;
+  for (int i = 0; i < w; ++i) off += s_warp[i];
+  __syncthreads();
+  return off + x - v;
+}
+
+// One pass: planned pass `q` (digit position plan.pos[q]).  (ka, va) hold the
+// input of the first pass; each pass that runs moves the keys to the other
+// buffer pair.  Dynamic shared memory: kOsTile keys then kOsTile values.
+constexpr int kOsLook = 16;  // earlier tiles read per look-back round trip
+template <typename K>
+constexpr size_t os_dyn_smem() { return (sizeof(K) + sizeof(unsigned)) * kOsTile; }
+
+template <typename K>
+__global__ void __launch_bounds__(kOsThreads, 2)
+k_os_scatter(K* __restrict__ ka, unsigned* __restrict__ va, K* __restrict__ kb,
+             unsigned* __restrict__ vb, long long n, int q, OsPlan plan,
+             const unsigned long long* __restrict__ hist, unsigned* __restrict__ ctr,
+             unsigned long long* __restrict__ look, long long tiles) {
+  extern __shared__ __align__(16) unsigned char os_smem[];
+  K* s_k = reinterpret_cast<K*>(os_smem);                                   // tile order
+  unsigned* s_v = reinterpret_cast<unsigned*>(os_smem + sizeof(K) * kOsTile);
+  __shared__ unsigned s_wcnt[kOsWarps][256];         // per-warp digit counts, then offsets
+  __shared__ unsigned s_dstart[256];                 // tile-local start of each digit
+  __shared__ unsigned long long s_gbase[256];        // output position of each digit's first key
+  __shared__ unsigned long long s_wscan[kOsWarps];
+  __shared__ unsigned s_tile;
+  __shared__ int s_skip, s_odd;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int pos = plan.pos[q];
+  unsigned long long* cur = look + (size_t)(q & 1) * tiles * 256;
+  unsigned long long* nxt = look + (size_t)((q + 1) & 1) * tiles * 256;
+  // the next pass's look-back words (not read by this pass)
+  if (q + 1 < plan.npass) nxt[(size_t)blockIdx.x * 256 + t] = 0ull;
+  if (w == 0) {
+    int ran = 0;
+    for (int p = 0; p < q; ++p) ran += os_constant(hist, p, n) ? 0 : 1;
+    const bool skip = os_constant(hist, q, n);
+    if (lane == 0) {
+      s_skip = skip;
+      s_odd = ran & 1;
+      if (!skip) s_tile = atomicAdd(&ctr[q], 1u);
+    }
+  }
+  for (int i = t; i < kOsWarps * 256; i += kOsThreads) (&s_wcnt[0][0])[i] = 0u;
+  __syncthreads();
+  if (s_skip) return;
+  const K* __restrict__ sk = s_odd ? kb : ka;
+  const unsigned* __restrict__ sv = s_odd ? vb : va;
+  K* __restrict__ dk = s_odd ? ka : kb;
+  unsigned* __restrict__ dv = s_odd ? va : vb;
+  const long long tile = s_tile;
+  const long long base = tile * kOsTile;
+  const long long wbase = base + (long long)w * 32 * kOsItems;
+  const unsigned lt = (1u << lane) - 1u;
+
+  // load (warp w owns keys [wbase, wbase + 32*kOsItems), lane order within a round)
+  K k[kOsItems];
+  unsigned v[kOsItems], rank[kOsItems];
+#pragma unroll
+  for (int r = 0; r < kOsItems; ++r) {
+    const long long j = wbase + r * 32 + lane;
+    k[r] = j < n ? sk[j] : K(0);
+    v[r] = j < n ? sv[j] : 0u;
+  }
+  // stable ranks within the warp, per digit
+#pragma unroll
+  for (int r = 0; r < kOsItems; ++r) {
+    const bool ok = wbase + r * 32 + lane < n;
+    const unsigned d = ok ? os_digit(k[r], pos) : 256u;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    rank[r] = ok ? s_wcnt[w][d] + __popc(peers & lt) : 0u;
+    __syncwarp();
+    if (ok && (peers & lt) == 0u) s_wcnt[w][d] += __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  // per digit t: warp offsets and the tile's count; publish it at once so
+  // later tiles can move on
+  unsigned cnt = 0;
+  for (int i = 0; i < kOsWarps; ++i) {
+    const unsigned c = s_wcnt[i][t];
+    s_wcnt[i][t] = cnt;
+    cnt += c;
+  }
+  unsigned long long* row = cur + (size_t)tile * 256;
+  atomicExch(&row[t], (tile == 0 ? kOsInc : kOsAgg) | (unsigned long long)cnt);
+  // the digit's global start, and its start inside the tile
+  const unsigned long long gstart = os_block_scan<unsigned long long>(hist[q * 256 + t], s_wscan);
+  const unsigned long long lstart = os_block_scan<unsigned long long>(cnt, s_wscan);
+  s_dstart[t] = (unsigned)lstart;
+  __syncthreads();
+  // keys and values into tile order (the registers are free before the wait)
+#pragma unroll
+  for (int r = 0; r < kOsItems; ++r) {
+    if (wbase + r * 32 + lane < n) {
+      const unsigned d = os_digit(k[r], pos);
+      const unsigned lp = rank[r] + s_dstart[d] + s_wcnt[w][d];
+      s_k[lp] = k[r];
+      s_v[lp] = v[r];
+    }
+  }
+  // decoupled look-back over the earlier tiles for digit t: a window of
+  // kOsLook words per round trip, nearest first, until a tile's inclusive
+  // prefix (bounded waits on words not yet published)
+  unsigned long long excl = 0;
+  if (tile > 0) {
+    long long j = tile - 1;
+    bool done = false;
+    while (!done) {
+      unsigned long long wv[kOsLook];
+#pragma unroll
+      for (int u = 0; u < kOsLook; ++u)
+        wv[u] = (j - u >= 0) ? __ldcg(&cur[(size_t)(j - u) * 256 + t]) : kOsInc;
+#pragma unroll
+      for (int u = 0; u < kOsLook; ++u) {
+        if (!done) {
+          unsigned long long x = wv[u];
+          if ((x >> 62) == 0) {
+            unsigned spins = 0;
+            do {
+              x = *(volatile unsigned long long*)&cur[(size_t)(j - u) * 256 + t];
+            } while ((x >> 62) == 0 && ++spins < kLbSpin);
+            if ((x >> 62) == 0) {
+              atomicOr(&g_scan_error, 2u);
+              x = kOsInc;
+            }
+          }
+          excl += x & kOsMask;
+          if ((x >> 62) == 2) done = true;
+        }
+      }
+      j -= kOsLook;
+    }
+    atomicExch(&row[t], kOsInc | ((excl + cnt) & kOsMask));
+  }
+  s_gbase[t] = gstart + excl;
+  __syncthreads();
+  // out: each digit's keys to consecutive positions
+  const int tn = (int)((n - base) < kOsTile ? (n - base) : kOsTile);
+  for (int i = t; i < tn; i += kOsThreads) {
+    const K kk = s_k[i];
+    const unsigned d = os_digit(kk, pos);
+    const unsigned long long o = s_gbase[d] + (unsigned long long)(i - (int)s_dstart[d]);
+    dk[o] = kk;
+    dv[o] = s_v[i];
+  }
+}
+
+// after the passes: if an odd number of them ran, the result is in (kb, vb)
+template <typename K>
+__global__ void k_os_final(K* __restrict__ ka, unsigned* __restrict__ va, const K* __restrict__ kb,
+                           const unsigned* __restrict__ vb, long long n, OsPlan plan,
+                           const unsigned long long* __restrict__ hist) {
+  __shared__ int s_odd;
+  if (threadIdx.x < 32) {
+    int ran = 0;
+    for (int p = 0; p < plan.npass; ++p) ran += os_constant(hist, p, n) ? 0 : 1;
+    if (threadIdx.x == 0) s_odd = ran & 1;
+  }
+  __syncthreads();
+  if (!s_odd) return;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    K k = keys[i];
-    o |= k;
-    a &= k;
+    ka[i] = kb[i];
+    va[i] = vb[i];
   }
-  for (int s = 16; s > 0; s >>= 1) {
-    o |= __shfl_xor_sync(0xffffffffu, o, s);
-    a &= __shfl_xor_sync(0xffffffffu, a, s);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicOr(out_or, o);
-    atomicAnd(out_and, a);
-  }
+}
+
+long long os_tiles(long long n) { return (n + kOsTile - 1) / kOsTile; }
+
+// the scatter's dynamic shared memory (with its static part above 48 KB)
+// needs an opt-in, once per device
+template <typename K>
+void os_smem_optin() {
+  static std::mutex mu;
+  static bool done[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return;
+  std::lock_guard<std::mutex> lk(mu);
+  if (done[dev]) return;
+  cudaFuncSetAttribute((const void*)k_os_scatter<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)os_dyn_smem<K>());
+  done[dev] = true;
 }
 
 template <typename K>
-__device__ __forceinline__ unsigned digit_of(K k, int shift) {
-  return (unsigned)((k >> shift) & 0xffu);
-}
-
-// per-block digit histogram, digit-major layout hist[d * nblocks + b]
-template <typename K, int kRadRounds>
-__global__ void k_rad_hist(const K* __restrict__ keys, long long n, int shift,
-                           unsigned* __restrict__ hist, unsigned nblocks) {
-  constexpr int kRadTile = kRadThreads * kRadRounds;
-  __shared__ unsigned h[256];
-  h[threadIdx.x] = 0;
-  __syncthreads();
-  long long base = (long long)blockIdx.x * kRadTile;
-  for (int i = threadIdx.x; i < kRadTile; i += kRadThreads) {
-    long long j = base + i;
-    if (j < n) atomicAdd(&h[digit_of(keys[j], shift)], 1u);
-  }
-  __syncthreads();
-  hist[(size_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
-}
-
-// stable scatter: warp w owns keys [base + w*32*R, base + (w+1)*32*R) in order
-template <typename K, int kRadRounds>
-__global__ void k_rad_scatter(const K* __restrict__ keys, const unsigned* __restrict__ vals,
-                              K* __restrict__ okeys, unsigned* __restrict__ ovals, long long n,
-                              int shift, const unsigned* __restrict__ offs, unsigned nblocks) {
-  constexpr int kRadTile = kRadThreads * kRadRounds;
-  __shared__ unsigned wcnt[kRadWarps][256];
-  __shared__ unsigned boff[256];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int i = threadIdx.x; i < kRadWarps * 256; i += kRadThreads) (&wcnt[0][0])[i] = 0;
-  boff[threadIdx.x] = offs[(size_t)threadIdx.x * nblocks + blockIdx.x];
-  __syncthreads();
-  const long long wbase = (long long)blockIdx.x * kRadTile + (long long)warp * (32 * kRadRounds);
-  const unsigned lt = (1u << lane) - 1u;
-  // pass A: per-warp digit counts
-  for (int r = 0; r < kRadRounds; ++r) {
-    long long j = wbase + r * 32 + lane;
-    unsigned d = j < n ? digit_of(keys[j], shift) : 256u;
-    unsigned peers = __match_any_sync(0xffffffffu, d);
-    if (d < 256u && (peers & lt) == 0) wcnt[warp][d] += __popc(peers);
-    __syncwarp();
-  }
-  __syncthreads();
-  // exclusive scan over warps per digit
-  {
-    unsigned d = threadIdx.x, run = 0;
-    for (int w = 0; w < kRadWarps; ++w) {
-      unsigned c = wcnt[w][d];
-      wcnt[w][d] = run;
-      run += c;
-    }
-  }
-  __syncthreads();
-  // pass B: ranks and scatter
-  for (int r = 0; r < kRadRounds; ++r) {
-    long long j = wbase + r * 32 + lane;
-    bool ok = j < n;
-    K k = ok ? keys[j] : K(0);
-    unsigned d = ok ? digit_of(k, shift) : 256u;
-    unsigned peers = __match_any_sync(0xffffffffu, d);
-    unsigned pos = 0;
-    if (ok) pos = boff[d] + wcnt[warp][d] + __popc(peers & lt);
-    __syncwarp();
-    if (ok && (peers & lt) == 0) wcnt[warp][d] += __popc(peers);
-    __syncwarp();
-    if (ok) {
-      okeys[pos] = k;
-      ovals[pos] = vals[j];
-    }
-  }
-}
-
-template <typename K, int kRadRounds>
-void radix_pass(const K* sk, const unsigned* sv, K* dk, unsigned* dv, long long n, int shift,
-                unsigned* hist, unsigned nblocks, void* sscr, cudaStream_t st) {
-  {
-    ::sbc::KProbe kp_(sizeof(K) == 8 ? "k_rad_hist_u64" : "k_rad_hist_u32", st,
-                      (double)sizeof(K) * n);
-    k_rad_hist<K, kRadRounds><<<nblocks, kRadThreads, 0, st>>>(sk, n, shift, hist, nblocks);
-  }
-  // exclusive scan of the digit-major histogram gives each (digit, block) its base
-  scan_rec<int>((int*)hist, (long long)256 * nblocks, (int*)sscr, st);
-  {
-    ::sbc::KProbe kp_(sizeof(K) == 8 ? "k_rad_scatter_u64" : "k_rad_scatter_u32", st,
-                      2.0 * (sizeof(K) + sizeof(unsigned)) * n);
-    k_rad_scatter<K, kRadRounds><<<nblocks, kRadThreads, 0, st>>>(sk, sv, dk, dv, n, shift, hist,
-                                                                nblocks);
-  }
-}
-
-template <typename K>
-void radix_sort_impl(K* keys, unsigned* vals, K* keys_tmp, unsigned* vals_tmp, long long n,
-                     int key_bits, void* scratch, cudaStream_t st, const K* known_vary = nullptr) {
+void onesweep(K* keys, unsigned* vals, K* keys_tmp, unsigned* vals_tmp, long long n,
+              unsigned pos_mask, void* scratch, cudaStream_t st) {
   if (n <= 1) return;
-  // tile size: the largest of 4096 / 2048 / 1024 keys that still gives about
-  // four CTAs per SM (152 SMs)
-  const int rounds = n >= 4LL * 152 * kRadThreads * 16 ? 16 : (n >= 4LL * 152 * kRadThreads * 8 ? 8 : 4);
-  const int tile = kRadThreads * rounds;
-  unsigned nblocks = (unsigned)((n + tile - 1) / tile);
-  // scratch: [or, and] then hist (256*nblocks u32) then scan scratch
-  K* d_or = (K*)scratch;
-  K* d_and = d_or + 1;
-  unsigned* hist = (unsigned*)((char*)scratch + 64);
-  void* sscr = (char*)scratch + 64 + (((size_t)256 * nblocks * sizeof(unsigned) + 255) / 256) * 256;
-  // 64-bit keys (doubles) often have constant high digits: one OR/AND
-  // reduction (and a host round trip) finds the digits worth sorting.  For
-  // 32-bit keys the caller's key_bits already bounds the passes.
-  K vary = ~K(0);
-  if (known_vary) {
-    vary = *known_vary;
-  } else if (sizeof(K) == 8) {
-    K h_or = 0, h_and = ~K(0);
-    cudaMemcpyAsync(d_or, &h_or, sizeof(K), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(d_and, &h_and, sizeof(K), cudaMemcpyHostToDevice, st);
-    unsigned g = (unsigned)((n + 1023) / 1024);
-    if (g > 2048) g = 2048;
-    {
-      ::sbc::KProbe kp_("k_bits_reduce", st);
-      k_bits_reduce<K><<<g, 1024, 0, st>>>(keys, n, d_or, d_and);
-    }
-    K o, a;
-    cudaMemcpyAsync(&o, d_or, sizeof(K), cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(&a, d_and, sizeof(K), cudaMemcpyDeviceToHost, st);
-    cudaStreamSynchronize(st);
-    vary = o ^ a;
+  OsPlan plan{};
+  for (int p = 0; p < (int)sizeof(K) && p < kOsMaxPasses; ++p)
+    if ((pos_mask >> p) & 1u) plan.pos[plan.npass++] = p;
+  if (plan.npass == 0) return;
+  const long long tiles = os_tiles(n);
+  auto* hist = (unsigned long long*)scratch;
+  auto* ctr = (unsigned*)((char*)scratch + kOsHistBytes);
+  auto* look = (unsigned long long*)((char*)scratch + kOsHistBytes + kOsCtrBytes);
+  cudaMemsetAsync(scratch, 0, kOsHistBytes + kOsCtrBytes, st);
+  {
+    long long g = (n + (long long)kOsThreads * kOsHistItems - 1) / ((long long)kOsThreads * kOsHistItems);
+    if (g > 152 * 8) g = 152 * 8;
+    ::sbc::KProbe kp_(sizeof(K) == 8 ? "k_os_hist_u64" : "k_os_hist_u32", st, (double)sizeof(K) * n);
+    k_os_hist<K><<<(unsigned)g, kOsThreads, 0, st>>>(keys, n, plan, hist, look, tiles * 256);
   }
-  K* src_k = keys;
-  unsigned* src_v = vals;
-  K* dst_k = keys_tmp;
-  unsigned* dst_v = vals_tmp;
-  for (int shift = 0; shift < key_bits; shift += 8) {
-    if (((vary >> shift) & K(0xff)) == 0) continue;
-    if (rounds == 16)
-      radix_pass<K, 16>(src_k, src_v, dst_k, dst_v, n, shift, hist, nblocks, sscr, st);
-    else if (rounds == 8)
-      radix_pass<K, 8>(src_k, src_v, dst_k, dst_v, n, shift, hist, nblocks, sscr, st);
-    else
-      radix_pass<K, 4>(src_k, src_v, dst_k, dst_v, n, shift, hist, nblocks, sscr, st);
-    K* tk = src_k; src_k = dst_k; dst_k = tk;
-    unsigned* tv = src_v; src_v = dst_v; dst_v = tv;
+  os_smem_optin<K>();
+  for (int q = 0; q < plan.npass; ++q) {
+    ::sbc::KProbe kp_(sizeof(K) == 8 ? "k_os_scatter_u64" : "k_os_scatter_u32", st,
+                      2.0 * (sizeof(K) + sizeof(unsigned)) * n);
+    k_os_scatter<K><<<(unsigned)tiles, kOsThreads, os_dyn_smem<K>(), st>>>(
+        keys, vals, keys_tmp, vals_tmp, n, q, plan, hist, ctr, look, tiles);
   }
-  if (src_k != keys) {
-    cudaMemcpyAsync(keys, src_k, sizeof(K) * n, cudaMemcpyDeviceToDevice, st);
-    cudaMemcpyAsync(vals, src_v, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, st);
+  {
+    long long g = (n + 1023) / 1024;
+    if (g > 152 * 4) g = 152 * 4;
+    ::sbc::KProbe kp_("k_os_final", st);
+    k_os_final<K><<<(unsigned)g, 256, 0, st>>>(keys, vals, keys_tmp, vals_tmp, n, plan, hist);
   }
 }
 
 }  // namespace
 
 size_t radix_scratch_bytes(long long n) {
-  long long nblocks = (n + kRadMinTile - 1) / kRadMinTile;
-  size_t h = (((size_t)256 * nblocks * sizeof(unsigned) + 255) / 256) * 256;
-  return 64 + h + scan_scratch_bytes(256 * nblocks) * 2 + 256;
+  const long long tiles = os_tiles(n > 1 ? n : 1);
+  return kOsHistBytes + kOsCtrBytes + (size_t)2 * tiles * 256 * sizeof(unsigned long long) + 256;
 }
 
 void radix_sort_u32(unsigned* keys, unsigned* vals, unsigned* keys_tmp, unsigned* vals_tmp,
                     long long n, int key_bits, void* scratch, cudaStream_t st) {
-  radix_sort_impl<unsigned>(keys, vals, keys_tmp, vals_tmp, n, key_bits, scratch, st);
+  unsigned mask = 0;
+  for (int p = 0; p < 4 && 8 * p < key_bits; ++p) mask |= 1u << p;
+  onesweep<unsigned>(keys, vals, keys_tmp, vals_tmp, n, mask, scratch, st);
 }
 
 void radix_sort_u64(unsigned long long* keys, unsigned* vals, unsigned long long* keys_tmp,
                     unsigned* vals_tmp, long long n, void* scratch, cudaStream_t st) {
-  radix_sort_impl<unsigned long long>(keys, vals, keys_tmp, vals_tmp, n, 64, scratch, st);
+  onesweep<unsigned long long>(keys, vals, keys_tmp, vals_tmp, n, 0xffu, scratch, st);
 }
 
 void radix_sort_u64_within(unsigned long long* keys, unsigned* vals, unsigned long long* keys_tmp,
                            unsigned* vals_tmp, long long n, unsigned long long lo,
                            unsigned long long hi, void* scratch, cudaStream_t st) {
-  // keys in [lo, hi] share every bit above the highest bit where lo and hi differ
+  // keys in [lo, hi] share every bit above the highest bit where lo and hi
+  // differ: only the bytes at or below it can vary
   const unsigned long long d = lo ^ hi;
-  const unsigned long long vary = d ? (~0ull >> __builtin_clzll(d)) : 0ull;
-  radix_sort_impl<unsigned long long>(keys, vals, keys_tmp, vals_tmp, n, 64, scratch, st, &vary);
+  unsigned mask = 0;
+  if (d) {
+    const int top = 63 - __builtin_clzll(d);
+    for (int p = 0; p <= top / 8; ++p) mask |= 1u << p;
+  }
+  onesweep<unsigned long long>(keys, vals, keys_tmp, vals_tmp, n, mask, scratch, st);
 }
 
 }  // namespace sbc

@@ -20,10 +20,11 @@ LIB_PATH = PKG / "_build" / "libsbclip.so"
 SBC_FLAG_TIMING = 1
 SBC_FLAG_SERIAL_BACKEND = 2
 SBC_FLAG_UNION = 4
+SBC_FLAG_ENDPOINT_SORT = 8
 
 STATS = ["edges", "elementary_points", "tree_size", "cover_entries", "leaf_end_entries",
          "candidates_tested", "raw_hits", "unique", "slots_b", "slots_c", "serial_backend",
-         "work_units", "grid_pairs"]
+         "work_units", "grid_pairs", "vertex_sort", "outside_cmbr"]
 PHASES = ["setup", "elementary", "end_lists", "cover_lists", "candidates_merge", "back_end",
           "device_to_host", "total"]
 DEBUG_ARRAYS = {
@@ -158,6 +159,8 @@ def load_library(path: str | os.PathLike | None = None):
     L.sbc_batch_info.argtypes = [vp, ctypes.POINTER(ll), i]
     L.sbc_pairwise_set_cell_factor.argtypes = [vp, ctypes.c_double]
     L.sbc_pairwise_set_split.argtypes = [vp, i]
+    L.sbc_pairwise_set_workers.argtypes = [vp, i]
+    L.sbc_pairwise_get_workers.argtypes = [vp]
     L.sbc_pairwise_autotune.argtypes = [vp, ctypes.POINTER(_PairwiseJob), ctypes.POINTER(i),
                                         ctypes.POINTER(ctypes.c_double),
                                         ctypes.POINTER(ctypes.c_double), vp]
@@ -210,12 +213,15 @@ class Clipper:
     """One library context (one CUDA stream, grow-only device buffers)."""
 
     def __init__(self, device: int = 0, timing: bool = False, serial_backend: bool = False,
-                 union: bool = False):
-        """union: every clipping call returns base ∪ overlay instead of base ∩ overlay."""
+                 union: bool = False, endpoint_sort: bool = False):
+        """union: every clipping call returns base ∪ overlay instead of base ∩ overlay.
+        endpoint_sort: the elementary intervals from the sort of all edge
+        endpoints rather than of the vertices (a test hook; same results)."""
         self._L = load_library()
         opt = _Options(device, (SBC_FLAG_TIMING if timing else 0) |
                        (SBC_FLAG_SERIAL_BACKEND if serial_backend else 0) |
-                       (SBC_FLAG_UNION if union else 0))
+                       (SBC_FLAG_UNION if union else 0) |
+                       (SBC_FLAG_ENDPOINT_SORT if endpoint_sort else 0))
         h = ctypes.c_void_p()
         rc = self._L.sbc_create(ctypes.byref(opt), ctypes.byref(h))
         if rc != 0:
@@ -410,6 +416,12 @@ class Clipper:
 
     def set_pairwise_split(self, records: int) -> None:
         self._check(self._L.sbc_pairwise_set_split(self._h, int(records)))
+
+    def set_pairwise_workers(self, workers: int) -> None:
+        self._check(self._L.sbc_pairwise_set_workers(self._h, int(workers)))
+
+    def pairwise_workers(self) -> int:
+        return int(self._L.sbc_pairwise_get_workers(self._h))
 
     def autotune_pairwise_device(self, d_bxy, nb, noverlays, d_cxy, d_coff,
                                  stream: int | None = None) -> dict:

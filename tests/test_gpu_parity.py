@@ -217,3 +217,51 @@ def test_kernels_were_launched(clipper):
     before = sbclip.kernel_launches()
     clipper.clip(gen.star(100, 1), [gen.star(80, 2, centre=(0.1, 0.1))])
     assert sbclip.kernel_launches() > before + 20
+
+
+def test_vertex_sort_and_endpoint_sort_agree(clipper, small_cases):
+    """The elementary intervals come from a sort of the E vertex keys,
+    expanded to the 2E endpoints; inputs with a shared x value fall back to
+    sorting the endpoints themselves.  Both routes give the same tree arrays
+    and rings as the oracle."""
+    import sbclip
+    ref = sbclip.Clipper(0, endpoint_sort=True)
+    try:
+        kinds = set()
+        cases = [(c.kind, c.base, c.overlays) for c in small_cases]
+        pb, pc = gen.pair_small()
+        cases.append(("pair_10k_8k", pb, [pc]))
+        for kind, b, ovs in cases:
+            got = clipper.clip(b, ovs)
+            vs = clipper.stats()["vertex_sort"]
+            kinds.add(vs)
+            want = ref.clip(b, ovs)
+            assert ref.stats()["vertex_sort"] == 0
+            for name in ("elementary", "leaf_after", "leaf_before", "leaf_range"):
+                a, w = clipper.debug_array(name), ref.debug_array(name)
+                assert np.array_equal(a.view(np.int64) if a.dtype == np.float64 else a,
+                                      w.view(np.int64) if w.dtype == np.float64 else w), (kind, name)
+            for x, y in zip(got, want):
+                assert rings_equal(x, y), kind
+        assert kinds == {0, 1}  # both routes ran
+    finally:
+        ref.close()
+
+
+def test_common_mbr_filter_keeps_every_candidate(clipper):
+    """A small overlay against a large base: most base edges miss the common
+    MBR of the two polygons and are left out of the candidate search; every
+    stage and the rings still equal the oracle's (also with several overlays,
+    and with an overlay whose box misses the base's entirely)."""
+    b = gen.star(20_000, 61)
+    c = gen.star(300, 62, centre=(0.55, 0.05), R=0.12)
+    _compare_all(clipper, b, c)
+    st = clipper.stats()
+    assert st["outside_cmbr"] > 15_000, st
+    far = gen.star(50, 63, centre=(5.0, 5.0), R=0.1)
+    ovs = [c, gen.star(200, 64, centre=(-0.4, 0.3), R=0.2), far]
+    got = clipper.clip(b, ovs)
+    ora = O.clip(b, ovs)["overlays"]
+    for i in range(len(ovs)):
+        assert rings_equal(got[i], O.rings_of(ora[i])), i
+    assert got[2] == []
