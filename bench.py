@@ -324,6 +324,11 @@ def run_gb300(args, rank: int, world: int):
                        l2="flushed between steps (256 MiB write)"),
         "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
         "kernels_top": {k: {"ms_per_step": v[0], "launches_per_step": v[1]} for k, v in top},
+        # the profiled step's launches, each bracketed by CUDA events: their
+        # summed time next to the device time per step shows the gaps between
+        # kernels (host round trips, launch latency)
+        "kernel_ms_per_step": float(sum(v[0] for v in prof.values())),
+        "launches_per_step": int(sum(v[1] for v in prof.values())),
         "stats": stats, "clocks": clk.summary(),
         "counts": {"rings": nrings, "vertices": nverts, "unique_intersections": stats["unique"],
                    "candidates_tested_per_s": stats["candidates_tested"] / (ms * 1e-3)},

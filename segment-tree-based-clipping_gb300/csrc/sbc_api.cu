@@ -17,6 +17,7 @@ namespace sbc {
 int Pipeline::run(const double* d_bxy, int nb_, const double* d_cxy, const int* c_sizes, int k_) {
   err_.clear();
   outs_.assign(k_, OverlayOut());
+  join_ready_ = 0;
   nb = nb_;
   k = k_;
   if (nb < 3) return fail(kEInput, "base polygon needs at least 3 vertices");
@@ -30,17 +31,28 @@ int Pipeline::run(const double* d_bxy, int nb_, const double* d_cxy, const int* 
     if (timing) cudaEventRecord(ev[i], st_);
   };
   mark(0);
+  // the tree stages on the main stream; the grid stage's three steps on the
+  // side stream in between (each step's host read mostly finds its work done)
   int rc = stage_setup(d_bxy, d_cxy, c_sizes);
+  if (!rc) rc = stage_grid_boxes();
   mark(1);
   if (!rc) rc = stage_elementary();
+  if (!rc) rc = stage_grid_count();
   mark(2);
   if (!rc) rc = stage_endlists();
+  if (!rc) rc = stage_grid_fill();
   mark(3);
   if (!rc) rc = stage_cover();
-  if (!rc) rc = stage_grid();
+  // the first overlay's box join reads only the grid: on the side stream too
+  if (!rc) rc = stage_join(1, side_stream());
   mark(4);
+  // the candidate stage (main stream) reads the grid and the join; on an
+  // error, later work on the main stream still waits for the side stream's
+  // kernels (they read this context's buffers)
+  join_side();
   for (int t = 1; t <= k && !rc; ++t) rc = stage_overlay(t, outs_[t - 1]);
   mark(5);
+  take_tree_stats();
   if (cudaGetLastError() != cudaSuccess && !rc) rc = fail(kECuda, "CUDA error in the pipeline");
   if (scan_error_take() && !rc) rc = fail(kEInternal, "a scan's bounded wait gave up");
   if (timing) {
@@ -62,6 +74,8 @@ int Pipeline::run_from_hits(const double* d_bxy, int nb_, const double* d_cxy, i
   if (nb < 3 || nc < 3) return fail(kEInput, "polygons need at least 3 vertices");
   const int sizes[1] = {nc};
   int rc0 = stage_setup(d_bxy, d_cxy, sizes);
+  // the setup's non-finite check (run() reads it with the elementary counts)
+  if (!rc0 && (read_flags() & kFlagUndef)) rc0 = fail(kEInput, "non-finite vertex coordinate");
   if (!rc0) rc0 = stage_records(1, rb, rc, rt, rkey, nhits, outs_[0], true);
   if (cudaGetLastError() != cudaSuccess && !rc0) rc0 = fail(kECuda, "CUDA error in the pipeline");
   if (scan_error_take() && !rc0) rc0 = fail(kEInternal, "a scan's bounded wait gave up");

@@ -614,29 +614,39 @@ k_pair_exact(long long n, const int2* __restrict__ pairs, const int* __restrict_
 }  // namespace
 
 // ------------------------------------------------------------------ host
-int Pipeline::stage_grid() {
-  cudaStream_t st = st_;
-  std::vector<int> hstart(k + 2);
-  hstart[0] = 0;
-  for (int t = 0; t <= k; ++t) hstart[t + 1] = nb + hcc[t];
+// The grid stage does not depend on the tree: it runs on the pipeline's
+// second stream (side_stream()), issued in three steps that run() interleaves
+// with the tree stages, so its kernels overlap the tree build and its two
+// host reads mostly find the work already done.  The last step makes the
+// main stream wait for the grid before the candidate stage.
+int Pipeline::stage_grid_boxes() {
+  cudaStream_t st = side_stream();
+  if (!st) return fail(kECuda, "side stream");
+  h_tstart_.assign(k + 2, 0);
+  for (int t = 0; t <= k; ++t) h_tstart_[t + 1] = nb + hcc[t];
   g_tstart = (int*)pool_.get("grid_tstart", sizeof(int) * (k + 2));
   fbox = (float4*)pool_.get("grid_fbox", sizeof(float4) * (E + 1));
-  auto* bnd = (unsigned*)pool_.get("grid_bnd", 256);
-  auto* sum_ext = (double*)((char*)bnd + 64);
+  g_bnd = (unsigned*)pool_.get("grid_bnd", 256);
   vfB = (float4*)pool_.get("grid_vfB", sizeof(float4) * (nb + 1));
   vfC = (float4*)pool_.get("grid_vfC", sizeof(float4) * ((long long)clSize + k));
   g_islong = (unsigned char*)pool_.get("grid_islong", (size_t)E + 1);
   g_long = (int*)pool_.get("grid_long", sizeof(int) * (E + 1));
   g_long_count = (unsigned*)pool_.get("grid_long_count", 256);
   if (pool_.failed) return fail(kENoMem, "device allocation failed (grid)");
-  cudaMemcpyAsync(g_tstart, hstart.data(), sizeof(int) * (k + 2), cudaMemcpyHostToDevice, st);
-  unsigned init[8] = {0xffffffffu, 0xffffffffu, 0u, 0u, 0xffffffffu, 0xffffffffu, 0u, 0u};
-  cudaMemcpyAsync(bnd, init, sizeof(init), cudaMemcpyHostToDevice, st);
+  auto* sum_ext = (double*)((char*)g_bnd + 64);
+  // the setup's arrays are written on the main stream
+  cudaEventRecord(ev_setup_, st_);
+  cudaStreamWaitEvent(st, ev_setup_, 0);
+  cudaMemcpyAsync(g_tstart, h_tstart_.data(), sizeof(int) * (k + 2), cudaMemcpyHostToDevice, st);
+  static const unsigned init[8] = {0xffffffffu, 0xffffffffu, 0u, 0u,
+                                   0xffffffffu, 0xffffffffu, 0u, 0u};
+  cudaMemcpyAsync(g_bnd, init, sizeof(init), cudaMemcpyHostToDevice, st);
   cudaMemsetAsync(sum_ext, 0, sizeof(double), st);
   cudaMemsetAsync(g_long_count, 0, sizeof(unsigned), st);
   {
     ::sbc::KProbe kp_("k_edge_fbox", st);
-    k_edge_fbox<<<grid_for(E, 256), 256, 0, st>>>(E, e_id, g_tstart, k, bP, cP, fbox, bnd, sum_ext);
+    k_edge_fbox<<<grid_for(E, 256), 256, 0, st>>>(E, e_id, g_tstart, k, bP, cP, fbox, g_bnd,
+                                                  sum_ext);
   }
   {
     ::sbc::KProbe kp_("k_vertex_f4", st);
@@ -646,11 +656,18 @@ int Pipeline::stage_grid() {
     ::sbc::KProbe kp_("k_vertex_f4", st);
     k_vertex_f4<<<grid_for((long long)clSize + k, 256), 256, 0, st>>>((long long)clSize + k, cP, vfC);
   }
+  cudaMemcpyAsync(h_side_rd_, g_bnd, 8 * sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(h_side_rd_ + 8, sum_ext, sizeof(double), cudaMemcpyDeviceToHost, st);
+  return kOk;
+}
+
+int Pipeline::stage_grid_count() {
+  cudaStream_t st = side_stream();
+  if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "grid bounds");
   unsigned hb[8];
   double hsum = 0.0;
-  cudaMemcpyAsync(hb, bnd, sizeof(hb), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(&hsum, sum_ext, sizeof(double), cudaMemcpyDeviceToHost, st);
-  if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "grid bounds");
+  memcpy(hb, h_side_rd_, sizeof(hb));
+  memcpy(&hsum, h_side_rd_ + 8, sizeof(double));
   auto unkey = [](unsigned kk) {
     unsigned u = (kk & 0x80000000u) ? (kk & 0x7fffffffu) : ~kk;
     float f;
@@ -681,12 +698,12 @@ int Pipeline::stage_grid() {
   g_nCells = grid_.gx * grid_.gy;
   const long long nBk = (long long)g_nCells * (k + 1);
   g_bstart = (int*)pool_.get("grid_bstart", sizeof(int) * (nBk + 1));
-  int* fill = (int*)pool_.get("grid_fill", sizeof(int) * (nBk + 1));
+  g_fill = (int*)pool_.get("grid_fill", sizeof(int) * (nBk + 1));
   void* sscr2 = pool_.get("scan_scr_grid2", scan_scratch_bytes(nBk + 1));
   if (pool_.failed) return fail(kENoMem, "device allocation failed (grid buckets)");
   cudaMemsetAsync(g_bstart, 0, sizeof(int) * (nBk + 1), st);
-  cudaMemsetAsync(fill, 0, sizeof(int) * (nBk + 1), st);
-  unsigned* outside = (unsigned*)((char*)bnd + 128);
+  cudaMemsetAsync(g_fill, 0, sizeof(int) * (nBk + 1), st);
+  unsigned* outside = (unsigned*)((char*)g_bnd + 128);
   cudaMemsetAsync(outside, 0, sizeof(unsigned), st);
   {
     ::sbc::KProbe kp_("k_grid_count", st);
@@ -694,27 +711,38 @@ int Pipeline::stage_grid() {
                                                  g_long, g_long_count, cmbr, outside);
   }
   exclusive_scan_i32(g_bstart, nBk + 1, sscr2, st);
+  cudaMemcpyAsync(h_side_rd_, g_bstart + nBk, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(h_side_rd_ + 1, outside, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  return kOk;
+}
+
+int Pipeline::stage_grid_fill() {
+  cudaStream_t st = side_stream();
+  if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "grid count");
   int total = 0;
   unsigned n_out = 0;
-  cudaMemcpyAsync(&total, g_bstart + nBk, sizeof(int), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(&n_out, outside, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
-  if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "grid count");
+  memcpy(&total, h_side_rd_, sizeof(int));
+  memcpy(&n_out, h_side_rd_ + 1, sizeof(unsigned));
   stat_outside_cmbr = n_out;
   if (total < 0) return fail(kEInput, "grid too large");
   g_n = total;
   g_vals = (unsigned*)pool_.get("grid_vals", sizeof(unsigned) * ((long long)total + 1));
   if (pool_.failed) return fail(kENoMem, "device allocation failed (grid entries)");
+  const Grid g{grid_.x0, grid_.y0, grid_.inv, grid_.gx, grid_.gy};
   if (total > 0) {
     ::sbc::KProbe kp_("k_grid_scatter", st);
-    k_grid_scatter<<<grid_for(E, 256), 256, 0, st>>>(E, fbox, g, g_tstart, k, g_bstart, fill,
+    k_grid_scatter<<<grid_for(E, 256), 256, 0, st>>>(E, fbox, g, g_tstart, k, g_bstart, g_fill,
                                                    g_islong, g_vals);
   }
   return kOk;
 }
 
-int Pipeline::stage_candidates(int cType, int** rb_out, int** rc_out, int** rt_out,
-                               unsigned long long** rkey_out, long long* nhits, OverlayOut& out) {
-  cudaStream_t st = st_;
+// The box join of overlay cType on stream `st`: every box-overlapping
+// (base edge, overlay edge) pair, reported once (in the cell of the low
+// corner of the boxes' overlap).  It reads only the grid, so run() issues the
+// first overlay's join on the side stream, next to the tree build.
+int Pipeline::stage_join(int cType, cudaStream_t st) {
+  join_ready_ = 0;
   const Grid g{grid_.x0, grid_.y0, grid_.inv, grid_.gx, grid_.gy};
   const int nCells = g_nCells;
   auto* cdesc = (int4*)pool_.get("cg_desc", sizeof(int4) * ((long long)nCells + 1));
@@ -776,6 +804,25 @@ int Pipeline::stage_candidates(int cType, int** rb_out, int** rc_out, int** rt_o
     cap = npairs + (1 << 20);
   }
   pair_cap_ = cap;
+  join_pairs_ = pairs;
+  join_npairs_ = npairs;
+  join_work_ = W;
+  join_ready_ = cType;
+  return kOk;
+}
+
+int Pipeline::stage_candidates(int cType, int** rb_out, int** rc_out, int** rt_out,
+                               unsigned long long** rkey_out, long long* nhits, OverlayOut& out) {
+  cudaStream_t st = st_;
+  if (join_ready_ != cType) {
+    const int rj = stage_join(cType, st);
+    if (rj) return rj;
+  }
+  join_ready_ = 0;
+  const long long npairs = join_npairs_;
+  const int2* pairs = join_pairs_;
+  auto* counters = (unsigned long long*)pool_.get("cg_counters", 64);
+  if (pool_.failed) return fail(kENoMem, "device allocation failed (candidate pairs)");
   // exact stage: one record per unique hit
   long long hcap = npairs + 1;
   int* rb = (int*)pool_.get("raw_b", sizeof(int) * hcap);
@@ -801,7 +848,7 @@ int Pipeline::stage_candidates(int cType, int** rb_out, int** rc_out, int** rt_o
   out.survivors = npairs;
   out.tests = (long long)hc[1];
   out.raw_hits = (long long)hc[3];
-  out.work = W;
+  out.work = join_work_;
   return kOk;
 }
 

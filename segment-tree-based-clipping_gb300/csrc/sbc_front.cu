@@ -50,6 +50,48 @@ void BufferPool::release_all() {
   bufs_.clear();
 }
 
+Pipeline::~Pipeline() {
+  if (st2_) {
+    cudaStreamSynchronize(st2_);
+    cudaStreamDestroy(st2_);
+  }
+  if (ev_setup_) cudaEventDestroy(ev_setup_);
+  if (ev_side_) cudaEventDestroy(ev_side_);
+  if (h_side_rd_) cudaFreeHost(h_side_rd_);
+}
+
+// the second stream of this pipeline, created on first use with its two
+// events and 256 bytes of pinned host memory for reads back
+cudaStream_t Pipeline::side_stream() {
+  if (st2_) return st2_;
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+  if (cudaEventCreateWithFlags(&ev_setup_, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ev_side_, cudaEventDisableTiming) != cudaSuccess ||
+      cudaMallocHost((void**)&h_side_rd_, 256) != cudaSuccess) {
+    cudaStreamDestroy(s);
+    return nullptr;
+  }
+  st2_ = s;
+  return st2_;
+}
+
+void Pipeline::join_side() {
+  if (!st2_) return;
+  cudaEventRecord(ev_side_, st2_);
+  cudaStreamWaitEvent(st_, ev_side_, 0);
+}
+
+void Pipeline::take_tree_stats() {
+  if (!tree_stats_pending_) return;
+  cudaStreamSynchronize(st_);
+  unsigned long long hc[2];
+  memcpy(hc, h_side_rd_ + 32, sizeof(hc));
+  stat_leaf = (long long)hc[0];
+  stat_cover = (long long)hc[1];
+  tree_stats_pending_ = false;
+}
+
 unsigned Pipeline::read_flags() {
   unsigned f = 0;
   cudaMemcpyAsync(&f, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st_);
@@ -211,16 +253,11 @@ int Pipeline::stage_setup(const double* d_bxy, const double* d_cxy, const int* c
     k_setup_edges<<<grid_for(E, 256), 256, 0, st_>>>(bP, cP, cS, cc, nb, k, E, e_id, e_s, e_e, mm,
                                                    d_flags, v_key, v_id, e_flip);
   }
-  unsigned long long hm[2];
-  unsigned hf = 0;
-  cudaMemcpyAsync(hm, mm, 16, cudaMemcpyDeviceToHost, st_);
-  cudaMemcpyAsync(&hf, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st_);
-  cudaStreamSynchronize(st_);
-  if (hf & kFlagUndef) return fail(kEInput, "non-finite vertex coordinate");
-  key_lo = hm[0];
-  key_hi = hm[1];
-  minI = key_to_double(hm[0]);
-  maxI = key_to_double(hm[1]);
+  // the x range and the non-finite flag are read with the elementary
+  // stage's counts (one host round trip for both): nothing before that read
+  // needs them on the host, and the kernels in between are index-safe on any
+  // coordinate values
+  d_minmax = mm;
   return kOk;
 }
 
@@ -364,7 +401,7 @@ int Pipeline::stage_elementary() {
   for (;;) {
   if (by_vertex) {
     // sort the E vertex keys, then expand to the 2E endpoints
-    radix_sort_u64_within(v_key, v_id, vkey2, vid2, E, key_lo, key_hi, rscr, st_);
+    radix_sort_u64(v_key, v_id, vkey2, vid2, E, rscr, st_);
     ::sbc::KProbe kp_("k_ele_expand", st_, 12.0 * E + 9.0 * E + 24.0 * E);
     k_ele_expand<<<grid_for(E, 256), 256, 0, st_>>>(v_key, v_id, e_flip, cc, nb, k, E, keys, sidx,
                                                     d_flags);
@@ -373,7 +410,7 @@ int Pipeline::stage_elementary() {
       ::sbc::KProbe kp_("k_ele_keys", st_);
       k_ele_keys<<<grid_for(E, 256), 256, 0, st_>>>(e_s, e_e, E, keys, sidx);
     }
-    radix_sort_u64_within(keys, sidx, keys2, sidx2, n2, key_lo, key_hi, rscr, st_);
+    radix_sort_u64(keys, sidx, keys2, sidx2, n2, rscr, st_);
   }
   cudaMemsetAsync(vl, 0, sizeof(int) * (E + 1), st_);
   {
@@ -392,10 +429,17 @@ int Pipeline::stage_elementary() {
   }
   exclusive_scan_i32(flag, n2 + 1, sscr, st_);
   unsigned fl = 0;
+  unsigned long long hm[2] = {0, 0};
   cudaMemcpyAsync(&count, flag + n2, sizeof(int), cudaMemcpyDeviceToHost, st_);
   cudaMemcpyAsync(&before_last, flag + n2 - 1, sizeof(int), cudaMemcpyDeviceToHost, st_);
   cudaMemcpyAsync(&fl, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st_);
+  cudaMemcpyAsync(hm, d_minmax, sizeof(hm), cudaMemcpyDeviceToHost, st_);
   cudaStreamSynchronize(st_);
+  if (fl & kFlagUndef) return fail(kEInput, "non-finite vertex coordinate");
+  key_lo = hm[0];
+  key_hi = hm[1];
+  minI = key_to_double(hm[0]);
+  maxI = key_to_double(hm[1]);
   if (by_vertex && (fl & kFlagSharedX)) {
     // a shared x value: the endpoints' own stable sort decides their order
     by_vertex = false;
@@ -775,11 +819,11 @@ int Pipeline::stage_cover() {
     ::sbc::KProbe kp_("k_edge_range", st_, 24.0 * E);  // es, ee in; leaf range out
     k_edge_range<<<grid_for(E, 256), 256, 0, st_>>>(e_s, e_e, E, ea, logL, lr, d_treecnt);
   }
-  unsigned long long hc[2] = {0, 0};
-  cudaMemcpyAsync(hc, d_treecnt, sizeof(hc), cudaMemcpyDeviceToHost, st_);
-  if (cudaStreamSynchronize(st_) != cudaSuccess) return fail(kECuda, "leaf ranges");
-  stat_leaf = (long long)hc[0];
-  stat_cover = (long long)hc[1];
+  // the two counts are statistics only: copied now, read at the end of run()
+  if (!side_stream()) return fail(kECuda, "side stream");
+  cudaMemcpyAsync(h_side_rd_ + 32, d_treecnt, 2 * sizeof(unsigned long long),
+                  cudaMemcpyDeviceToHost, st_);
+  tree_stats_pending_ = true;
   return kOk;
 }
 

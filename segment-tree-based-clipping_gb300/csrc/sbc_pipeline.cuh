@@ -51,6 +51,7 @@ struct Timing {
 class Pipeline {
  public:
   Pipeline(int device, cudaStream_t st) : dev_(device), st_(st) {}
+  ~Pipeline();
   // polygons already on the device (no closing vertex), sizes on the host
   int run(const double* d_bxy, int nb, const double* d_cxy, const int* c_sizes, int k);
   const std::vector<OverlayOut>& outputs() const { return outs_; }
@@ -85,6 +86,7 @@ class Pipeline {
   int stat_vertex_sort = 0;            // the last run's endpoint order came from the vertex sort
   double minI = 0, maxI = 0;
   unsigned long long key_lo = 0, key_hi = 0;  // order keys of minI and maxI
+  unsigned long long* d_minmax = nullptr;     // device copy of (key_lo, key_hi) from the setup
   // tree
   double* ea = nullptr;
   int epc = 0, numLeaves = 0, ts = 0, logL = 0;
@@ -114,6 +116,11 @@ class Pipeline {
   int g_nCells = 0;                    // gx * gy
   long long pair_cap_ = 0;             // candidate-pair buffer size that sufficed last time
   unsigned* d_flags = nullptr;         // device error flags (DevFlag bits)
+  unsigned* g_bnd = nullptr;           // grid bounds (order keys), extent sum, outside count
+  int* g_fill = nullptr;               // per-bucket fill counters of the grid scatter
+  int join_ready_ = 0;                 // overlay whose box join below is ready (0: none)
+  const int2* join_pairs_ = nullptr;
+  long long join_npairs_ = 0, join_work_ = 0;
   // intermediate arrays of the last overlay processed (device, diagnostics)
   int *dbg_ub = nullptr, *dbg_uc = nullptr, *dbg_ut = nullptr;
   int dbg_K = 0;
@@ -129,7 +136,18 @@ class Pipeline {
   int stage_elementary();
   int stage_endlists();
   int stage_cover();
-  int stage_grid();
+  // the grid in three steps on the side stream: boxes and bounds; cell
+  // counts (reads the bounds); entries (reads the count, then the main
+  // stream waits for the side stream)
+  int stage_grid_boxes();
+  int stage_grid_count();
+  int stage_grid_fill();
+  // the box join of overlay cType on stream st (results kept for the
+  // candidate stage of that overlay)
+  int stage_join(int cType, cudaStream_t st);
+  cudaStream_t side_stream();     // created on first use; nullptr if that fails
+  void join_side();               // later work on the main stream waits for the side stream
+  void take_tree_stats();         // the cover stage's statistics, once their copy landed
   int stage_candidates(int cType, int** rb, int** rc, int** rt, unsigned long long** rkey,
                        long long* nhits, OverlayOut& out);
   int stage_overlay(int cType, OverlayOut& out);
@@ -153,6 +171,12 @@ class Pipeline {
  private:
   int dev_;
   cudaStream_t st_;
+  cudaStream_t st2_ = nullptr;         // side stream (grid stage)
+  cudaEvent_t ev_setup_ = nullptr, ev_side_ = nullptr;
+  unsigned* h_side_rd_ = nullptr;      // 256 B pinned: the grid stage's reads ([0..9]),
+                                       // the cover stage's two counts ([32..35])
+  bool tree_stats_pending_ = false;
+  std::vector<int> h_tstart_;
   BufferPool pool_;
   std::vector<OverlayOut> outs_;
   std::string err_;

@@ -318,17 +318,21 @@ def test_pairwise_big_pairs_on_several_workers_match_oracle(cl):
     oracle directly."""
     base, ovs = gen.one_to_many(n_base=20_000, n_overlays=48, seed=3700, hi=2000,
                                 near_boundary=0.8)
+    workers = cl.pairwise_workers()
     try:
         cl.set_pairwise_split(64)
         got, st = cl.clip_pairwise(base, ovs)
         info = cl.pairwise_info()
+        cl.set_pairwise_workers(3)
+        got3, st3 = cl.clip_pairwise(base, ovs)
     finally:
         cl.set_pairwise_split(8192)
+        cl.set_pairwise_workers(workers)
     assert info["big_pairs"] >= 16, info
     runs = _oracle_runs([(base, c) for c in ovs])
     for i, (s, want, *_rest) in enumerate(runs):
-        assert st[i] == s, (i, st[i], s)
-        assert rings_equal(got[i], want), i
+        assert st[i] == s and st3[i] == s, (i, st[i], st3[i], s)
+        assert rings_equal(got[i], want) and rings_equal(got3[i], want), i
 
 
 def test_jagged_pair_at_unit_radius_fails_cleanly():
