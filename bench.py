@@ -176,8 +176,10 @@ class ClockSampler:
 # pipe is busy.  The roofline entry reports the kernel against HBM bytes in
 # every case and says which bound applies.
 KERNEL_BOUND = {
-    "k_rad_scatter_u64": "hbm", "k_rad_hist_u64": "hbm", "k_rad_scatter_u32": "hbm",
-    "k_rad_hist_u32": "hbm", "k_scan_lb": "hbm", "k_setup_edges": "hbm", "k_edge_tree": "hbm",
+    "k_os_scatter_u64": "hbm", "k_os_hist_u64": "hbm", "k_os_scatter_u32": "hbm",
+    "k_os_hist_u32": "hbm", "k_scan_lb": "hbm", "k_setup_edges": "hbm", "k_edge_tree": "hbm",
+    "k_alpha_classify": "hbm", "k_cover_count": "latency", "k_alpha_sort_long": "latency",
+    "k_lr_jump_coop": "latency", "k_tr_jump_coop": "latency",
     "k_grid_scatter": "hbm", "k_edge_fbox": "hbm", "k_copy_runs": "hbm",
     "k_pair_exact": "fp64", "k_pw_cand_test": "fp64", "k_batch_cand": "fp64", "k_labels": "fp64",
     "k_grid_warp": "latency", "k_grid_small": "latency", "k_lr_jump": "latency",
@@ -189,7 +191,16 @@ KERNEL_BOUND = {
 # kernels captured with ncu on the named workload, keyed (kernel, workload).
 # A capture on a smaller case of the same kernel is scaled by the units it
 # processed where the traffic grows in proportion (said in the source note).
-TRAFFIC = {}
+TRAFFIC = {
+    ("k_os_scatter_u64", "pair_1m_1m"): {
+        "bytes": 25078016 + 121088,
+        "source": "profiles/k_os_scatter_u64_pair_1m_1m.md (one pass of 2M keys: the 25 MB "
+                  "input from DRAM; the output stays in L2 for the next pass)"},
+    ("k_os_hist_u64", "pair_1m_1m"): {
+        "bytes": 16046336, "source": "profiles/k_os_hist_u64_pair_1m_1m.md"},
+    ("k_pair_exact", "pair_1m_1m"): {
+        "bytes": 140120320 + 7214336, "source": "profiles/k_pair_exact_pair_1m_1m.md"},
+}
 
 
 def roofline_of(prof_b: dict, workload_name: str, fallback_bytes=None):
@@ -224,9 +235,9 @@ def algorithmic_bytes(kernel: str, st: dict, launches: int):
     if kernel == "k_pair_exact":
         # the two edges' coordinates of every box-overlapping pair (64 B)
         return 64.0 * st["grid_pairs"] / per
-    if kernel == "k_rad_scatter_u64":
+    if kernel == "k_os_scatter_u64":
         return 24.0 * P  # read (key 8 + value 4) and write them once per pass
-    if kernel == "k_rad_hist_u64":
+    if kernel == "k_os_hist_u64":
         return 8.0 * P
     if kernel == "k_find_leaves":
         return 16.0 * E + 8.0 * E
@@ -464,6 +475,10 @@ def run_small_pairs(args, rank: int, world: int):
     sp = stream.cuda_stream
     a = (n, t["bxy"].data_ptr(), t["boff"].data_ptr(), t["cxy"].data_ptr(), t["coff"].data_ptr())
 
+    # the autotuner picks the batch engine's block sizes (and the small/large
+    # split where it applies) by timing forward + backward on this batch,
+    # outside the timed region; results do not depend on them
+    tuned = clip.autotune_batch_device(*a, ga.data_ptr(), gb.data_ptr(), gc.data_ptr(), sp)
     # the whole forward + backward step as one CUDA graph, recorded once
     graph = clip.area_graph(*a, ga.data_ptr(), gb.data_ptr(), gc.data_ptr(), area.data_ptr(),
                             st.data_ptr(), sp)
@@ -550,7 +565,8 @@ def run_small_pairs(args, rank: int, world: int):
                                           if world > 1 else "single"),
                        shard=shard_info, gathered_pairs=gathered,
                        l2="flushed between steps (256 MiB write)",
-                       launch="one CUDA graph per step (area forward + backward)"),
+                       launch="one CUDA graph per step (area forward + backward)",
+                       autotuned={k: v for k, v in tuned.items() if k != "best_ms"}),
         "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
         "kernels_top": {k: {"ms_per_step": v[0], "launches_per_step": v[1]}
                         for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])[:6]},
@@ -906,6 +922,7 @@ def batched_summary(args, rank: int, world: int):
         "small_pairs_65536": {
             "metric": sp["metric"], "pairs_per_s": sp["value"], "ms_per_step": sp["ms_per_step"],
             "launch": "one CUDA graph per step (area forward + backward)",
+            "autotuned": sp["config"]["autotuned"],
             "e2e_pairs_per_s": sp["e2e"]["value"],
             "per_pair_gpu_path_pairs_per_s": sp["counts"]["per_pair_gpu_path_pairs_per_s"],
             "forward_backward_over_per_pair": sp["counts"]["batched_over_per_pair"],

@@ -295,8 +295,27 @@ void sbc_area_graph_destroy(sbc_graph* graph);
  * chunk's forward pass instead of keeping every intersection record. */
 int sbc_batch_set_arena_budget(sbc_ctx* ctx, long long bytes);
 /* Shape of the last batch call: out[0] chunks, out[1] pairs clipped by the
- * single-pair pipeline because a polygon exceeds SBC_BATCH_MAX_VERTICES. */
+ * single-pair pipeline because a polygon exceeds the small/large split. */
 int sbc_batch_info(const sbc_ctx* ctx, long long* out, int n);
+/* Tuning knobs of the batch engine, shape[5]: block sizes (threads: 32, 64,
+ * 96 or 128) of the per-pair front kernel, the warp-per-pair candidate
+ * kernel, the per-pair back end and the backward kernel, then the small/large
+ * split (a pair with a polygon above it is clipped by the single-pair
+ * pipeline; 3 to SBC_BATCH_MAX_VERTICES, default SBC_BATCH_MAX_VERTICES).
+ * Results do not depend on them.  A graph (sbc_area_graph_create) needs a
+ * batch with no polygon above the split. */
+int sbc_batch_set_shape(sbc_ctx* ctx, const int* shape);
+int sbc_batch_get_shape(const sbc_ctx* ctx, int* shape);
+/* Autotuner: times the batch's area forward + backward (device arrays, as for
+ * the _device calls; grad_b and grad_c are overwritten) under each knob's
+ * settings in turn, keeps the fastest in the context and reports it in
+ * shape[5] and best_ms (either may be NULL).  A split below the batch's
+ * largest polygons is tried only when it moves at most 64 pairs to the
+ * single-pair pipeline.  The reference has no counterpart: it clips pairs one
+ * at a time. */
+int sbc_batch_autotune(sbc_ctx* ctx, const sbc_batch* batch, const double* grad_area,
+                       double* grad_b, double* grad_c, int* shape, double* best_ms,
+                       void* stream);
 
 /* Allocation-free ring tracing.  No counterpart in the reference: it exists
  * for callers that are not allowed to allocate device memory themselves or

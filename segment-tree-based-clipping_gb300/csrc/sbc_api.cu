@@ -18,6 +18,7 @@ int Pipeline::run(const double* d_bxy, int nb_, const double* d_cxy, const int* 
   err_.clear();
   outs_.assign(k_, OverlayOut());
   join_ready_ = 0;
+  cover_count_pending_ = false;
   nb = nb_;
   k = k_;
   if (nb < 3) return fail(kEInput, "base polygon needs at least 3 vertices");
@@ -50,6 +51,8 @@ int Pipeline::run(const double* d_bxy, int nb_, const double* d_cxy, const int* 
   // error, later work on the main stream still waits for the side stream's
   // kernels (they read this context's buffers)
   join_side();
+  // a statistic, off the critical path (its kernel reads the leaf ranges)
+  if (!rc) launch_cover_count();
   for (int t = 1; t <= k && !rc; ++t) rc = stage_overlay(t, outs_[t - 1]);
   mark(5);
   take_tree_stats();
@@ -797,6 +800,45 @@ extern "C" int sbc_batch_set_arena_budget(sbc_ctx* c, long long bytes) {
   if (!c) return SBC_EINPUT;
   if (bytes < 0) return set_err(c, SBC_EINPUT, "negative budget");
   c->br->arena_budget = bytes;
+  return SBC_OK;
+}
+
+extern "C" int sbc_batch_set_shape(sbc_ctx* c, const int* shape) {
+  if (!c || !shape) return SBC_EINPUT;
+  for (int i = 0; i < 4; ++i)
+    if (shape[i] < 32 || shape[i] > 128 || shape[i] % 32)
+      return set_err(c, SBC_EINPUT, "block sizes must be 32, 64, 96 or 128");
+  if (shape[4] < 3 || shape[4] > SBC_BATCH_MAX_VERTICES)
+    return set_err(c, SBC_EINPUT, "split must be 3 to SBC_BATCH_MAX_VERTICES");
+  c->br->shape = sbc::BatchShape{shape[0], shape[1], shape[2], shape[3]};
+  c->br->split = shape[4];
+  c->br->valid = false;  // later calls re-run the forward pass with these settings
+  return SBC_OK;
+}
+
+extern "C" int sbc_batch_get_shape(const sbc_ctx* c, int* shape) {
+  if (!c || !shape) return SBC_EINPUT;
+  const sbc::BatchShape& s = c->br->shape;
+  const int v[5] = {s.front, s.cand, s.back, s.bwd, c->br->split};
+  for (int i = 0; i < 5; ++i) shape[i] = v[i];
+  return SBC_OK;
+}
+
+extern "C" int sbc_batch_autotune(sbc_ctx* c, const sbc_batch* b, const double* grad_area,
+                                  double* grad_b, double* grad_c, int* shape, double* best_ms,
+                                  void* stream) {
+  int rc = batch_check(c, b);
+  if (rc) return rc;
+  if (b->npairs > 0 && (!grad_area || !grad_b || !grad_c))
+    return set_err(c, SBC_EINPUT, "null gradient array");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  c->pl->clear_error();
+  c->pl->set_stream(st);
+  rc = c->br->autotune(b->npairs, b->b_xy, b->b_off, b->c_xy, b->c_off, grad_area, grad_b, grad_c,
+                       st, best_ms);
+  if (rc) return set_err(c, rc, c->pl->error());
+  if (shape) sbc_batch_get_shape(c, shape);
   return SBC_OK;
 }
 

@@ -783,7 +783,7 @@ __device__ PairResult clip_pair_back(const double* b, int nb, const double* c, i
 // ------------------------------------------------------------------ kernels
 __global__ void k_batch_size(int np, const long long* __restrict__ boff,
                              const long long* __restrict__ coff, const int* __restrict__ pass_of,
-                             const int* __restrict__ need, long long* __restrict__ bytes) {
+                             const int* __restrict__ need, long long* __restrict__ bytes, int maxv) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p > np) return;
   if (p == np) {
@@ -792,7 +792,7 @@ __global__ void k_batch_size(int np, const long long* __restrict__ boff,
   }
   const int nb = (int)(boff[p + 1] - boff[p]), nc = (int)(coff[p + 1] - coff[p]);
   const int pass = pass_of ? pass_of[p] : 0;
-  const bool ok = nb >= 3 && nc >= 3 && nb <= SBC_BATCH_MAX_VERTICES && nc <= SBC_BATCH_MAX_VERTICES;
+  const bool ok = nb >= 3 && nc >= 3 && nb <= maxv && nc <= maxv;
   bytes[p] = (ok && pass >= 0)
                  ? (long long)arena_bytes(nb, nc, hit_cap(nb, nc, pass, need ? need[p] : 0))
                  : 0;
@@ -818,10 +818,11 @@ struct ClipArgs {
   int* nverts;
   double* area;
   int unite;            // union instead of intersection
+  int maxv;             // the small/large split: larger polygons go to the pair pipeline
   __device__ bool small(int p, int* nb, int* nc) const {
     *nb = (int)(boff[p + 1] - boff[p]);
     *nc = (int)(coff[p + 1] - coff[p]);
-    return *nb >= 3 && *nc >= 3 && *nb <= SBC_BATCH_MAX_VERTICES && *nc <= SBC_BATCH_MAX_VERTICES;
+    return *nb >= 3 && *nc >= 3 && *nb <= maxv && *nc <= maxv;
   }
   __device__ PairWork work(int p, int nb, int nc, int pass, Caps* cp) const {
     *cp = caps_of(nb, nc, hit_cap(nb, nc, pass, need_in[p]));
@@ -894,18 +895,20 @@ __global__ void k_graph_passes(int n, const int* __restrict__ pass, const int* _
   pass1[p] = pass[p] == 1 ? 1 : -1;
 }
 
-void launch_clip(const ClipArgs& A, double in_bytes, cudaStream_t st) {
+// block sizes (threads) of the three kernels: tuning knobs, each at most
+// kBatchBlock (128) and a multiple of 32
+void launch_clip(const ClipArgs& A, const BatchShape& sh, double in_bytes, cudaStream_t st) {
   {
     ::sbc::KProbe kp_("k_batch_front", st, in_bytes);
-    k_batch_front<<<grid_for(A.np, kBatchBlock), kBatchBlock, 0, st>>>(A);
+    k_batch_front<<<grid_for(A.np, sh.front), sh.front, 0, st>>>(A);
   }
   {
     ::sbc::KProbe kp_("k_batch_cand", st, in_bytes);
-    k_batch_cand<<<grid_for(32LL * A.np, 128), 128, 0, st>>>(A);
+    k_batch_cand<<<grid_for(32LL * A.np, sh.cand), sh.cand, 0, st>>>(A);
   }
   {
     ::sbc::KProbe kp_("k_batch_back", st, in_bytes + 20.0 * A.np);
-    k_batch_back<<<grid_for(A.np, kBatchBlock), kBatchBlock, 0, st>>>(A);
+    k_batch_back<<<grid_for(A.np, sh.back), sh.back, 0, st>>>(A);
   }
 }
 
@@ -1019,7 +1022,8 @@ k_batch_backward(int np, const double* __restrict__ bxy, const long long* __rest
 }
 
 // ------------------------------------------------------------------ large pairs
-// A pair with a polygon above SBC_BATCH_MAX_VERTICES is clipped by the pair
+// A pair with a polygon above the small/large split (SBC_BATCH_MAX_VERTICES by
+// default) is clipped by the pair
 // pipeline.  Its ring vertices get the provenance the small-pair engine
 // records, by exact coordinates: a base vertex first, then an overlay vertex,
 // then a proper crossing (a type-1 record) -- candidates sorted by (x, y),
@@ -1198,7 +1202,7 @@ int BatchRunner::plan(int np_, const long long* d_boff, const long long* d_coff,
   {
     ::sbc::KProbe kp_("k_batch_size", st);
     k_batch_size<<<grid_for(np + 1, 256), 256, 0, st>>>(np, d_boff, d_coff, nullptr, nullptr,
-                                                       aoff[0]);
+                                                       aoff[0], split);
   }
   exclusive_scan_i64(aoff[0], np + 1, sscr_, st);
   cudaMemcpyAsync(h_aoff0_.data(), aoff[0], sizeof(long long) * (np + 1), cudaMemcpyDeviceToHost,
@@ -1208,7 +1212,7 @@ int BatchRunner::plan(int np_, const long long* d_boff, const long long* d_coff,
   big_.clear();
   for (int p = 0; p < np; ++p) {
     const long long nb = h_boff_[p + 1] - h_boff_[p], nc = h_coff_[p + 1] - h_coff_[p];
-    if (nb >= 3 && nc >= 3 && (nb > SBC_BATCH_MAX_VERTICES || nc > SBC_BATCH_MAX_VERTICES)) {
+    if (nb >= 3 && nc >= 3 && (nb > split || nc > split)) {
       BigOut b;
       b.p = p;
       big_.push_back(b);
@@ -1252,7 +1256,7 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
   for (int i = 0; i < n; ++i) {
     const long long nb = h_boff_[p0 + i + 1] - h_boff_[p0 + i];
     const long long nc = h_coff_[p0 + i + 1] - h_coff_[p0 + i];
-    is_small[i] = nb <= SBC_BATCH_MAX_VERTICES && nc <= SBC_BATCH_MAX_VERTICES;
+    is_small[i] = nb <= split && nc <= split;
     hp[i] = (nb >= 3 && nc >= 3 && !is_small[i]) ? -1 : 0;
   }
   cudaMemcpyAsync(pass + p0, hp.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
@@ -1261,8 +1265,8 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
       16.0 * (double)(h_boff_[p1] - h_boff_[p0] + h_coff_[p1] - h_coff_[p0]);
   launch_clip(ClipArgs{n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[0], aoff[0] + p0,
                        abase_[0], need_ + p0, need_ + p0, status + p0, nrings + p0, nverts + p0,
-                       area + p0, unite ? 1 : 0},
-              in_bytes, st);
+                       area + p0, unite ? 1 : 0, split},
+              shape, in_bytes, st);
   std::vector<int> hs(n);
   cudaMemcpyAsync(hs.data(), status + p0, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch clip");
@@ -1281,7 +1285,7 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
     {
       ::sbc::KProbe kp_("k_batch_size", st);
       k_batch_size<<<grid_for(n + 1, 256), 256, 0, st>>>(n, d_boff + p0, d_coff + p0, pass + p0,
-                                                         need_ + p0, aoff[1] + p0);
+                                                         need_ + p0, aoff[1] + p0, split);
     }
     exclusive_scan_i64(aoff[1] + p0, n + 1, sscr_, st);
     long long total = 0;
@@ -1291,8 +1295,8 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
     if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch arena)");
     launch_clip(ClipArgs{n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[1],
                          aoff[1] + p0, 0, need_ + p0, need_ + p0, status + p0, nrings + p0,
-                         nverts + p0, area + p0, unite ? 1 : 0},
-                in_bytes, st);
+                         nverts + p0, area + p0, unite ? 1 : 0, split},
+                shape, in_bytes, st);
   }
   // where each pair's data lives now: pass 0 arena, retry arena, or none
   for (int i = 0; i < n; ++i) {
@@ -1486,7 +1490,7 @@ int BatchRunner::backward(const double* d_bxy, const long long* d_boff, const do
     ::sbc::KProbe kp_("k_batch_backward", st,
                       32.0 * (double)(h_boff_[p1] - h_boff_[p0] + h_coff_[p1] - h_coff_[p0]) +
                           8.0 * n);
-    k_batch_backward<<<grid_for(n, kBatchBlock), kBatchBlock, 0, st>>>(
+    k_batch_backward<<<grid_for(n, shape.bwd), shape.bwd, 0, st>>>(
         n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, ar, status + p0, nrings + p0, d_gA + p0, d_gb,
         d_gc);
   }
@@ -1510,6 +1514,77 @@ int BatchRunner::backward(const double* d_bxy, const long long* d_boff, const do
 
 namespace sbc {
 
+// The batch autotuner: the block size of each of the four kernels, then the
+// small/large split, one knob at a time, each setting timed as forward +
+// backward (CUDA events on st, the better of two runs); a change is kept only
+// if it is faster.  A split below the batch's largest polygons is tried only
+// when it moves at most 64 pairs to the pair pipeline (each costs about a
+// millisecond there).  Results do not depend on any knob.
+int BatchRunner::autotune(int np_, const double* d_bxy, const long long* d_boff,
+                          const double* d_cxy, const long long* d_coff, const double* d_gA,
+                          double* d_gb, double* d_gc, cudaStream_t st, double* best_ms) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    return pl_.fail(kECuda, "autotune events");
+  }
+  const bool prof = profiling_suspend();
+  auto timed = [&](double* ms) -> int {
+    double best = 1e300;
+    for (int r = 0; r < 2; ++r) {
+      cudaEventRecord(e0, st);
+      int rc = forward(np_, d_bxy, d_boff, d_cxy, d_coff, st);
+      if (!rc) rc = backward(d_bxy, d_boff, d_cxy, d_coff, d_gA, d_gb, d_gc, st);
+      cudaEventRecord(e1, st);
+      if (rc) return rc;
+      if (cudaEventSynchronize(e1) != cudaSuccess) return pl_.fail(kECuda, "autotune timing");
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e0, e1);
+      best = std::min(best, (double)t);
+    }
+    *ms = best;
+    return kOk;
+  };
+  double cur = 0.0;
+  int rc = timed(&cur);
+  int* knobs[4] = {&shape.front, &shape.cand, &shape.back, &shape.bwd};
+  for (int i = 0; i < 4 && !rc; ++i) {
+    for (int b : {32, 64, 128}) {
+      if (b == *knobs[i]) continue;
+      const int keep = *knobs[i];
+      *knobs[i] = b;
+      double t = 0.0;
+      rc = timed(&t);
+      if (rc || !(t < cur)) *knobs[i] = keep;
+      else cur = t;
+      if (rc) break;
+    }
+  }
+  for (int sp : {2048, 1024}) {
+    if (rc || sp >= split) continue;
+    int moved = 0;
+    for (int p = 0; p < np && moved <= 64; ++p) {
+      const long long nb = h_boff_[p + 1] - h_boff_[p], nc = h_coff_[p + 1] - h_coff_[p];
+      const long long m = nb > nc ? nb : nc;
+      if (nb >= 3 && nc >= 3 && m > sp && m <= split) ++moved;
+    }
+    if (moved == 0 || moved > 64) continue;
+    const int keep = split;
+    split = sp;
+    double t = 0.0;
+    rc = timed(&t);
+    if (rc || !(t < cur)) split = keep;
+    else cur = t;
+  }
+  // leave the forward state of the chosen settings
+  if (!rc) rc = forward(np_, d_bxy, d_boff, d_cxy, d_coff, st);
+  profiling_restore(prof);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (best_ms) *best_ms = cur;
+  return rc;
+}
+
 // Records the batch's area forward + backward as one CUDA graph.  The normal
 // forward pass runs first: it fixes the chunk (one), the arenas and the set
 // of pairs that need the retry pass with their hit capacities.  The graph
@@ -1523,7 +1598,8 @@ int BatchRunner::graph_record(int np_, const double* d_bxy, const long long* d_b
   if (rc) return rc;
   if (np <= 0 || chunks_.size() != 1 || !big_.empty())
     return pl_.fail(kEInput, "graph capture needs a non-empty batch in one arena chunk with no "
-                             "polygon above SBC_BATCH_MAX_VERTICES vertices");
+                             "polygon above the small/large split (SBC_BATCH_MAX_VERTICES by "
+                             "default)");
   BufferPool& pool = pl_.pool();
   int* pass0 = (int*)pool.get("bt_g_pass0", sizeof(int) * (np + 1));
   int* pass1 = (int*)pool.get("bt_g_pass1", sizeof(int) * (np + 1));
@@ -1547,16 +1623,16 @@ int BatchRunner::graph_record(int np_, const double* d_bxy, const long long* d_b
   cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     launch_clip(ClipArgs{np, d_bxy, d_boff, d_cxy, d_coff, pass0, arena[0], aoff[0], abase_[0],
-                         need_scr, need_rec, status, nrings, nverts, area, unite ? 1 : 0},
-                in_bytes, st);
+                         need_scr, need_rec, status, nrings, nverts, area, unite ? 1 : 0, split},
+                shape, in_bytes, st);
     if (retry)
       launch_clip(ClipArgs{np, d_bxy, d_boff, d_cxy, d_coff, pass1, arena[1], aoff[1], 0, need_scr,
-                           need_rec, status, nrings, nverts, area, unite ? 1 : 0},
-                  in_bytes, st);
+                           need_rec, status, nrings, nverts, area, unite ? 1 : 0, split},
+                  shape, in_bytes, st);
     const Arenas ar{arena[0], aoff[0], abase_[0], arena[1], aoff[1], 0, pass, need_rec};
     {
       ::sbc::KProbe kp_("k_batch_backward", st);
-      k_batch_backward<<<grid_for(np, kBatchBlock), kBatchBlock, 0, st>>>(
+      k_batch_backward<<<grid_for(np, shape.bwd), shape.bwd, 0, st>>>(
           np, d_bxy, d_boff, d_cxy, d_coff, ar, status, nrings, d_gA, d_gb, d_gc);
     }
     if (out_area) cudaMemcpyAsync(out_area, area, sizeof(double) * np, cudaMemcpyDeviceToDevice, st);

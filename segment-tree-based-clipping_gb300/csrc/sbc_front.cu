@@ -57,6 +57,7 @@ Pipeline::~Pipeline() {
   }
   if (ev_setup_) cudaEventDestroy(ev_setup_);
   if (ev_side_) cudaEventDestroy(ev_side_);
+  if (ev_lr_) cudaEventDestroy(ev_lr_);
   if (h_side_rd_) cudaFreeHost(h_side_rd_);
 }
 
@@ -68,6 +69,7 @@ cudaStream_t Pipeline::side_stream() {
   if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
   if (cudaEventCreateWithFlags(&ev_setup_, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&ev_side_, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ev_lr_, cudaEventDisableTiming) != cudaSuccess ||
       cudaMallocHost((void**)&h_side_rd_, 256) != cudaSuccess) {
     cudaStreamDestroy(s);
     return nullptr;
@@ -83,6 +85,8 @@ void Pipeline::join_side() {
 }
 
 void Pipeline::take_tree_stats() {
+  // no side-stream work outlives the call
+  if (st2_) cudaStreamSynchronize(st2_);
   if (!tree_stats_pending_) return;
   cudaStreamSynchronize(st_);
   unsigned long long hc[2];
@@ -196,7 +200,20 @@ __global__ void k_setup_edges(const double* __restrict__ bP, const double* __res
     kmin = o1 < kmin ? o1 : kmin;
     kmax = o2 > kmax ? o2 : kmax;
   }
+  // one pair of atomics per block: same-address atomics from every warp of
+  // the grid serialise at the L2
+  __shared__ unsigned long long s_min[32], s_max[32];
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   if ((threadIdx.x & 31) == 0) {
+    s_min[w] = kmin;
+    s_max[w] = kmax;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < nw; ++i) {
+      kmin = s_min[i] < kmin ? s_min[i] : kmin;
+      kmax = s_max[i] > kmax ? s_max[i] : kmax;
+    }
     atomicMin(&minmax[0], kmin);
     atomicMax(&minmax[1], kmax);
   }
@@ -628,7 +645,7 @@ __global__ void k_edge_tree(const double* __restrict__ es, const double* __restr
                             int epc, int z, int logL, int* __restrict__ aft, int* __restrict__ bef,
                             int2* __restrict__ lr, unsigned long long* __restrict__ cnt) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned n_leaf = 0, n_cover = 0;
+  unsigned n_leaf = 0;
   if (e < E) {
     const int L = 1 << logL;
     const int2 rS = erange[2 * e], rE = erange[2 * e + 1];
@@ -661,7 +678,22 @@ __global__ void k_edge_tree(const double* __restrict__ es, const double* __restr
     int r1 = rE.y - 1;
     r1 = r1 < 0 ? 0 : (r1 > L ? L : r1);
     lr[e] = make_int2(l, r1 > l ? r1 : l);
-    for (int x = l + L, y = (r1 > l ? r1 : l) + L; x < y; x >>= 1, y >>= 1) {
+  }
+  const unsigned long long t_leaf = block_sum((unsigned long long)n_leaf);
+  if (threadIdx.x == 0 && t_leaf) atomicAdd(cnt, t_leaf);
+}
+
+// The number of cover-list entries (a statistic: the nodes of every edge's
+// canonical decomposition of its leaf range), counted off the critical path
+// on the side stream.  cnt[1] accumulates it.
+__global__ void k_cover_count(int E, const int2* __restrict__ lr, int logL,
+                              unsigned long long* __restrict__ cnt) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned n_cover = 0;
+  if (e < E) {
+    const int L = 1 << logL;
+    const int2 r = lr[e];
+    for (int x = r.x + L, y = r.y + L; x < y; x >>= 1, y >>= 1) {
       if (x & 1) {
         ++n_cover;
         ++x;
@@ -672,12 +704,8 @@ __global__ void k_edge_tree(const double* __restrict__ es, const double* __restr
       }
     }
   }
-  const unsigned long long t_leaf = block_sum((unsigned long long)n_leaf);
-  const unsigned long long t_cover = block_sum((unsigned long long)n_cover);
-  if (threadIdx.x == 0) {
-    if (t_leaf) atomicAdd(cnt, t_leaf);
-    if (t_cover) atomicAdd(cnt + 1, t_cover);
-  }
+  const unsigned long long t = block_sum((unsigned long long)n_cover);
+  if (threadIdx.x == 0 && t) atomicAdd(cnt + 1, t);
 }
 
 static int digit_count_host(double val) {
@@ -819,12 +847,31 @@ int Pipeline::stage_cover() {
     ::sbc::KProbe kp_("k_edge_range", st_, 24.0 * E);  // es, ee in; leaf range out
     k_edge_range<<<grid_for(E, 256), 256, 0, st_>>>(e_s, e_e, E, ea, logL, lr, d_treecnt);
   }
-  // the two counts are statistics only: copied now, read at the end of run()
+  // the two counts are statistics only, read at the end of run().  With the
+  // leaf ranges from the sort, the cover entries are counted by
+  // k_cover_count on the side stream (launch_cover_count)
   if (!side_stream()) return fail(kECuda, "side stream");
-  cudaMemcpyAsync(h_side_rd_ + 32, d_treecnt, 2 * sizeof(unsigned long long),
-                  cudaMemcpyDeviceToHost, st_);
+  if (lr_ready) {
+    cudaEventRecord(ev_lr_, st_);
+    cover_count_pending_ = true;
+  } else {
+    cudaMemcpyAsync(h_side_rd_ + 32, d_treecnt, 2 * sizeof(unsigned long long),
+                    cudaMemcpyDeviceToHost, st_);
+  }
   tree_stats_pending_ = true;
   return kOk;
+}
+
+void Pipeline::launch_cover_count() {
+  if (!cover_count_pending_) return;
+  cover_count_pending_ = false;
+  cudaStreamWaitEvent(st2_, ev_lr_, 0);
+  {
+    ::sbc::KProbe kp_("k_cover_count", st2_);
+    k_cover_count<<<grid_for(E, 256), 256, 0, st2_>>>(E, lr, logL, d_treecnt);
+  }
+  cudaMemcpyAsync(h_side_rd_ + 32, d_treecnt, 2 * sizeof(unsigned long long),
+                  cudaMemcpyDeviceToHost, st2_);
 }
 
 }  // namespace sbc

@@ -209,39 +209,74 @@ __global__ void k_records(const int* __restrict__ ub, const int* __restrict__ uc
 // ---------------------------------------------------------------- A12 alpha sort
 // stable sort of positions [s,e) of one edge by alpha mod 1e9 (9 decimal
 // LSD passes), only for edges with more than one non-degenerate intersection
-__global__ void k_alpha_sort(int n, const int* __restrict__ allPS, const int* __restrict__ ndPS,
-                             const int* __restrict__ alpha, const int* __restrict__ order,
-                             int* __restrict__ sorted, unsigned* __restrict__ flags,
-                             int* __restrict__ long_list, unsigned* __restrict__ long_count) {
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= n) return;
-  int s = allPS[e], t = allPS[e + 1];
-  if (ndPS[e + 1] - ndPS[e] > 1 && t - s > kSegShort) {
-    long_list[atomicAdd(long_count, 1u)] = e;
-    return;
+// The identity order over all K records (coalesced), and the edges whose
+// records need sorting (more than one non-degenerate intersection) appended
+// to the short list (up to kSegShort records) or the long list, one atomic
+// per warp and list.  Edges with at most one such record keep the identity
+// (the reference sorts only those with more, :7436-7473).
+__global__ void k_alpha_classify(int n, int K, const int* __restrict__ allPS,
+                                 const int* __restrict__ ndPS, int* __restrict__ sorted,
+                                 int* __restrict__ short_list, unsigned* __restrict__ counts,
+                                 int* __restrict__ long_list) {
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nth = (long long)gridDim.x * blockDim.x;
+  for (long long i = tid; i < K; i += nth) sorted[i] = (int)i;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  // whole warps walk the edges (the loop bound is the same for a warp)
+  for (long long base = tid - lane; base < n; base += nth) {
+    const long long e = base + lane;
+    bool sh = false, lg = false;
+    if (e < n && ndPS[e + 1] - ndPS[e] > 1) {
+      lg = allPS[e + 1] - allPS[e] > kSegShort;
+      sh = !lg;
+    }
+    const unsigned ms = __ballot_sync(0xffffffffu, sh), ml = __ballot_sync(0xffffffffu, lg);
+    unsigned bs = 0, bl = 0;
+    if (lane == 0) {
+      if (ms) bs = atomicAdd(&counts[0], (unsigned)__popc(ms));
+      if (ml) bl = atomicAdd(&counts[1], (unsigned)__popc(ml));
+    }
+    bs = __shfl_sync(0xffffffffu, bs, 0);
+    bl = __shfl_sync(0xffffffffu, bl, 0);
+    if (sh) short_list[bs + __popc(ms & lt)] = (int)e;
+    if (lg) long_list[bl + __popc(ml & lt)] = (int)e;
   }
-  for (int i = s; i < t; ++i) sorted[i] = i;
-  if (ndPS[e + 1] - ndPS[e] <= 1) return;
-  for (int i = s; i < t; ++i) {
-    int a = alpha[order ? order[i] : i];
+}
+
+// Short edges of the list, one thread each: stable insertion by alpha mod 1e9.
+__global__ void k_alpha_sort(const int* __restrict__ list, const unsigned* __restrict__ count,
+                             const int* __restrict__ allPS, const int* __restrict__ alpha,
+                             const int* __restrict__ order, int* __restrict__ sorted,
+                             unsigned* __restrict__ flags) {
+  const unsigned x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= *count) return;
+  const int e = list[x];
+  const int s = allPS[e], m = allPS[e + 1] - s;  // 2 <= m <= kSegShort
+  // the run's keys read once into a thread-local copy, then a stable
+  // insertion sort of (key, record) on the copy
+  int kk[kSegShort], ii[kSegShort];
+  for (int i = 0; i < m; ++i) {
+    const int a = alpha[order ? order[s + i] : s + i];
     if (a < 0) {
       atomicOr(flags, (unsigned)kFlagUndef);
       return;
     }
+    kk[i] = a % 1000000000;
+    ii[i] = s + i;
   }
-  for (int i = s + 1; i < t; ++i) {
-    int p = sorted[i];
-    int kp = alpha[order ? order[p] : p] % 1000000000;
+  for (int i = 1; i < m; ++i) {
+    const int kp = kk[i], p = ii[i];
     int j = i;
-    while (j > s) {
-      int q = sorted[j - 1];
-      int kq = alpha[order ? order[q] : q] % 1000000000;
-      if (kq <= kp) break;
-      sorted[j] = q;
+    while (j > 0 && kk[j - 1] > kp) {
+      kk[j] = kk[j - 1];
+      ii[j] = ii[j - 1];
       --j;
     }
-    sorted[j] = p;
+    kk[j] = kp;
+    ii[j] = p;
   }
+  for (int i = 0; i < m; ++i) sorted[s + i] = ii[i];
 }
 
 // Long edges, one warp each: the stable position of record i is the number
@@ -574,26 +609,39 @@ int Pipeline::stage_records(int cType, const int* rb, const int* rc, const int* 
     }
     // ---- A12 per-edge alpha sorts
     int* along = (int*)pool_.get("alpha_long_list", sizeof(int) * ((long long)(bSize > cSize ? bSize : cSize) + 1));
-    auto* acount = (unsigned*)pool_.get("alpha_long_count", 256);
+    int* ashort = (int*)pool_.get("alpha_short_list", sizeof(int) * ((long long)(bSize > cSize ? bSize : cSize) + 1));
+    auto* acounts = (unsigned*)pool_.get("alpha_counts", 256);  // [0] short, [1] long
+    unsigned* acount = acounts + 1;
     if (pool_.failed) return fail(kENoMem, "device allocation failed (alpha lists)");
+    // edges with two or more records to sort: at most K / 2 of them
+    const unsigned sg = grid_for(K / 2 + 1, 128);
+    const unsigned cg = grid_for((long long)(bSize > cSize ? bSize : cSize), 256) < 2048
+                            ? grid_for((long long)(bSize > cSize ? bSize : cSize), 256)
+                            : 2048;
     const unsigned ag = grid_for((long long)(bSize > cSize ? bSize : cSize) * 32, 256) < 1024
                             ? grid_for((long long)(bSize > cSize ? bSize : cSize) * 32, 256)
                             : 1024;
-    cudaMemsetAsync(acount, 0, sizeof(unsigned), st);
+    cudaMemsetAsync(acounts, 0, 2 * sizeof(unsigned), st);
+    {
+      ::sbc::KProbe kp_("k_alpha_classify", st, 8.0 * bSize + 4.0 * K);
+      k_alpha_classify<<<cg, 256, 0, st>>>(bSize, K, bAll, bND, sB, ashort, acounts, along);
+    }
     {
       ::sbc::KProbe kp_("k_alpha_sort", st);
-      k_alpha_sort<<<grid_for(bSize, 128), 128, 0, st>>>(bSize, bAll, bND, aB, nullptr, sB, d_flags,
-                                                         along, acount);
+      k_alpha_sort<<<sg, 128, 0, st>>>(ashort, acounts, bAll, aB, nullptr, sB, d_flags);
     }
     {
       ::sbc::KProbe kp_("k_alpha_sort_long", st);
       k_alpha_sort_long<<<ag, 256, 0, st>>>(bAll, along, acount, aB, nullptr, sB, d_flags);
     }
-    cudaMemsetAsync(acount, 0, sizeof(unsigned), st);
+    cudaMemsetAsync(acounts, 0, 2 * sizeof(unsigned), st);
+    {
+      ::sbc::KProbe kp_("k_alpha_classify", st, 8.0 * cSize + 4.0 * K);
+      k_alpha_classify<<<cg, 256, 0, st>>>(cSize, K, cAll, cND, sC, ashort, acounts, along);
+    }
     {
       ::sbc::KProbe kp_("k_alpha_sort", st);
-      k_alpha_sort<<<grid_for(cSize, 128), 128, 0, st>>>(cSize, cAll, cND, aC, csorted, sC, d_flags,
-                                                         along, acount);
+      k_alpha_sort<<<sg, 128, 0, st>>>(ashort, acounts, cAll, aC, csorted, sC, d_flags);
     }
     {
       ::sbc::KProbe kp_("k_alpha_sort_long", st);

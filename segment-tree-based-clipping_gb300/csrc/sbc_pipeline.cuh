@@ -10,6 +10,7 @@
 #include <memory>
 #include <vector>
 
+#include "../../include/sbclip.h"
 #include "sbc_internal.cuh"
 
 namespace sbc {
@@ -148,6 +149,7 @@ class Pipeline {
   cudaStream_t side_stream();     // created on first use; nullptr if that fails
   void join_side();               // later work on the main stream waits for the side stream
   void take_tree_stats();         // the cover stage's statistics, once their copy landed
+  void launch_cover_count();      // the cover-entry statistic on the side stream
   int stage_candidates(int cType, int** rb, int** rc, int** rt, unsigned long long** rkey,
                        long long* nhits, OverlayOut& out);
   int stage_overlay(int cType, OverlayOut& out);
@@ -172,7 +174,8 @@ class Pipeline {
   int dev_;
   cudaStream_t st_;
   cudaStream_t st2_ = nullptr;         // side stream (grid stage)
-  cudaEvent_t ev_setup_ = nullptr, ev_side_ = nullptr;
+  cudaEvent_t ev_setup_ = nullptr, ev_side_ = nullptr, ev_lr_ = nullptr;
+  bool cover_count_pending_ = false;
   unsigned* h_side_rd_ = nullptr;      // 256 B pinned: the grid stage's reads ([0..9]),
                                        // the cover stage's two counts ([32..35])
   bool tree_stats_pending_ = false;
@@ -204,9 +207,23 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out);
 // arenas fit a memory budget; larger pairs through the Pipeline with a
 // provenance tape.  The forward pass keeps the last chunk's rings and tapes
 // resident for rings() and backward(); other chunks are recomputed there.
+// block sizes of the batch engine's kernels (tuning knobs: results do not
+// depend on them); each a multiple of 32, at most 128
+struct BatchShape {
+  int front = 128, cand = 128, back = 128, bwd = 128;
+};
+
 class BatchRunner {
  public:
   explicit BatchRunner(Pipeline& pl) : pl_(pl) {}
+  BatchShape shape;
+  int split = SBC_BATCH_MAX_VERTICES;  // polygons above it go to the pair pipeline (<= the max)
+  // times forward + backward of the batch under each knob's candidates in
+  // turn (the better of two runs), keeps the fastest; the forward results of
+  // the last run are left as forward() leaves them
+  int autotune(int np, const double* d_bxy, const long long* d_boff, const double* d_cxy,
+               const long long* d_coff, const double* d_gA, double* d_gb, double* d_gc,
+               cudaStream_t st, double* best_ms);
   int forward(int np, const double* d_bxy, const long long* d_boff, const double* d_cxy,
               const long long* d_coff, cudaStream_t st);
   int rings(const double* d_bxy, const long long* d_boff, const double* d_cxy,

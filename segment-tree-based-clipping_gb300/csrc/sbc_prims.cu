@@ -396,9 +396,24 @@ __device__ __forceinline__ unsigned os_digit(K k, int pos) {
   return (unsigned)((k >> (8 * pos)) & 0xffu);
 }
 
-// Counts of every planned digit position in one read of the keys (warp
-// aggregated with match_any: skewed digits do not serialise on one shared
-// counter).  Also zeroes the look-back words of the first pass.
+// The lanes of the warp holding the same 9-bit value d (a digit, or 256 for
+// "no key"): the AND over its bits of the bit's ballot or its complement.
+// Nine votes; every lane of the warp must take part.
+__device__ __forceinline__ unsigned os_peers(unsigned d) {
+  unsigned m = 0xffffffffu;
+#pragma unroll
+  for (int b = 0; b < 9; ++b) {
+    const bool bit = (d >> b) & 1u;
+    const unsigned v = __ballot_sync(0xffffffffu, bit);
+    m &= bit ? v : ~v;
+  }
+  return m;
+}
+
+// Counts of every planned digit position in one read of the keys: a warp
+// whose keys share the digit adds 32 with one atomic (the high, nearly
+// constant digits), otherwise every lane adds its own.  Also zeroes the
+// look-back words of the first pass.
 template <typename K>
 __global__ void __launch_bounds__(kOsThreads)
 k_os_hist(const K* __restrict__ keys, long long n, OsPlan plan,
@@ -427,8 +442,12 @@ k_os_hist(const K* __restrict__ keys, long long n, OsPlan plan,
     for (int r = 0; r < kOsHistItems; ++r) {
       for (int q = 0; q < plan.npass; ++q) {
         const unsigned d = ok[r] ? os_digit(k[r], plan.pos[q]) : 256u;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
-        if (ok[r] && (peers & lt) == 0u) atomicAdd(&h[q][d], (unsigned)__popc(peers));
+        const unsigned d0 = __shfl_sync(0xffffffffu, d, 0);
+        if (__all_sync(0xffffffffu, d == d0 && d0 < 256u)) {
+          if (lt == 0u) atomicAdd(&h[q][d0], 32u);
+        } else if (ok[r]) {
+          atomicAdd(&h[q][d], 1u);
+        }
       }
     }
   }
@@ -530,7 +549,7 @@ k_os_scatter(K* __restrict__ ka, unsigned* __restrict__ va, K* __restrict__ kb,
   for (int r = 0; r < kOsItems; ++r) {
     const bool ok = wbase + r * 32 + lane < n;
     const unsigned d = ok ? os_digit(k[r], pos) : 256u;
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const unsigned peers = os_peers(d);
     rank[r] = ok ? s_wcnt[w][d] + __popc(peers & lt) : 0u;
     __syncwarp();
     if (ok && (peers & lt) == 0u) s_wcnt[w][d] += __popc(peers);

@@ -21,6 +21,7 @@ SBC_FLAG_TIMING = 1
 SBC_FLAG_SERIAL_BACKEND = 2
 SBC_FLAG_UNION = 4
 SBC_FLAG_ENDPOINT_SORT = 8
+BATCH_SHAPE_KEYS = ("front", "cand", "back", "backward", "split")
 
 STATS = ["edges", "elementary_points", "tree_size", "cover_entries", "leaf_end_entries",
          "candidates_tested", "raw_hits", "unique", "slots_b", "slots_c", "serial_backend",
@@ -160,6 +161,9 @@ def load_library(path: str | os.PathLike | None = None):
     L.sbc_pairwise_set_cell_factor.argtypes = [vp, ctypes.c_double]
     L.sbc_pairwise_set_split.argtypes = [vp, i]
     L.sbc_pairwise_set_workers.argtypes = [vp, i]
+    L.sbc_batch_set_shape.argtypes = [vp, vp]
+    L.sbc_batch_get_shape.argtypes = [vp, vp]
+    L.sbc_batch_autotune.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
     L.sbc_pairwise_get_workers.argtypes = [vp]
     L.sbc_pairwise_autotune.argtypes = [vp, ctypes.POINTER(_PairwiseJob), ctypes.POINTER(i),
                                         ctypes.POINTER(ctypes.c_double),
@@ -384,6 +388,31 @@ class Clipper:
 
     def set_batch_arena_budget(self, nbytes: int) -> None:
         self._check(self._L.sbc_batch_set_arena_budget(self._h, int(nbytes)))
+
+    def batch_shape(self) -> dict:
+        """The batch engine's knobs: block sizes and the small/large split."""
+        v = (ctypes.c_int * 5)()
+        self._check(self._L.sbc_batch_get_shape(self._h, v))
+        return dict(zip(BATCH_SHAPE_KEYS, list(v)))
+
+    def set_batch_shape(self, **kw) -> None:
+        cur = self.batch_shape()
+        cur.update(kw)
+        v = (ctypes.c_int * 5)(*[int(cur[k]) for k in BATCH_SHAPE_KEYS])
+        self._check(self._L.sbc_batch_set_shape(self._h, v))
+
+    def autotune_batch_device(self, npairs, d_bxy, d_boff, d_cxy, d_coff, d_grad_area, d_grad_b,
+                              d_grad_c, stream: int | None = None) -> dict:
+        """Pick the batch engine's block sizes and split by timing forward +
+        backward on this batch (the gradient outputs are overwritten)."""
+        b = _Batch(npairs, d_bxy, d_boff, d_cxy, d_coff)
+        v = (ctypes.c_int * 5)()
+        ms = ctypes.c_double()
+        self._check(self._L.sbc_batch_autotune(self._h, ctypes.byref(b), d_grad_area, d_grad_b,
+                                               d_grad_c, v, ctypes.byref(ms), stream))
+        out = dict(zip(BATCH_SHAPE_KEYS, list(v)))
+        out["best_ms"] = ms.value
+        return out
 
     def batch_info(self) -> dict:
         """Shape of the last batch call."""

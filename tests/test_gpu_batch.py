@@ -245,3 +245,53 @@ def test_batch_area_graph_replays_forward_and_backward(cl):
     finally:
         g.close()
         ref.close()
+
+
+def test_batch_shape_and_autotune_do_not_change_results(cl):
+    """Block sizes and the small/large split are tuning knobs: rings, areas and
+    gradients are the same under any setting (a split of 40 sends the pairs
+    with a polygon above 40 vertices through the single-pair pipeline), and
+    the autotuner keeps a valid setting."""
+    torch = pytest.importorskip("torch")
+    import sbclip
+    pairs = gen.small_pairs(400, seed=4900)
+    bases, ovs = [b for b, _ in pairs], [c for _, c in pairs]
+    ga = np.random.default_rng(5).uniform(0.5, 2.0, len(pairs))
+    r0, s0 = cl.clip_batch(bases, ovs)
+    a0, _ = cl.area_forward(bases, ovs)
+    gb0, gc0 = cl.area_backward(bases, ovs, ga)
+    default = cl.batch_shape()
+    try:
+        cl.set_batch_shape(front=32, cand=64, back=32, backward=64, split=40)
+        r1, s1 = cl.clip_batch(bases, ovs)
+        assert cl.batch_info()["large_pairs"] > 50
+        a1, _ = cl.area_forward(bases, ovs)
+        gb1, gc1 = cl.area_backward(bases, ovs, ga)
+        assert np.array_equal(s0, s1)
+        assert all(rings_equal(x, y) for x, y in zip(r0, r1))
+        # the single-pair path sums areas in two stages and gradients with atomics
+        assert np.all(np.abs(a0 - a1) <= 1e-12 * np.maximum(1.0, np.abs(a0)))
+        for p in range(len(pairs)):
+            sc = max(np.abs(gb0[p]).max(), np.abs(gc0[p]).max(), 1e-300)
+            assert np.abs(gb0[p] - gb1[p]).max() <= 1e-11 * sc, p
+            assert np.abs(gc0[p] - gc1[p]).max() <= 1e-11 * sc, p
+        cl.set_batch_shape(**default)
+        bxy, boff = sbclip.pack_polygons(bases)
+        cxy, coff = sbclip.pack_polygons(ovs)
+        t = {k: torch.from_numpy(v).to("cuda:0") for k, v in
+             (("bxy", bxy), ("boff", boff), ("cxy", cxy), ("coff", coff))}
+        tga = torch.from_numpy(ga).to("cuda:0")
+        gb = torch.zeros_like(t["bxy"])
+        gc = torch.zeros_like(t["cxy"])
+        tuned = cl.autotune_batch_device(len(pairs), t["bxy"].data_ptr(), t["boff"].data_ptr(),
+                                         t["cxy"].data_ptr(), t["coff"].data_ptr(),
+                                         tga.data_ptr(), gb.data_ptr(), gc.data_ptr())
+        assert tuned["best_ms"] > 0
+        assert all(tuned[k] in (32, 64, 128) for k in ("front", "cand", "back", "backward"))
+        assert tuned["split"] == sbclip.BATCH_MAX_VERTICES  # no pair above 64 vertices
+        r2, s2 = cl.clip_batch(bases, ovs)
+        a2, _ = cl.area_forward(bases, ovs)
+        assert np.array_equal(s0, s2) and np.array_equal(a0, a2)
+        assert all(rings_equal(x, y) for x, y in zip(r0, r2))
+    finally:
+        cl.set_batch_shape(**default)
