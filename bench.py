@@ -300,6 +300,8 @@ def run_gb300(args, rank: int, world: int):
     torch.cuda.synchronize()
     prof_b = sbclip.profile_end(with_bytes=True)
     prof = {k: (v[0], v[1]) for k, v in prof_b.items()}
+    if args.timeline and rank == 0:
+        write_timeline(args.timeline, sbclip.profile_timeline())
 
     # ---- end to end through the host C ABI (sbc_clip_pair): host buffers in,
     # host->device and device->host copies inside every step
@@ -1028,6 +1030,24 @@ def run_reference_arm(args):
     return out
 
 
+def write_timeline(path: str, tl) -> None:
+    """One line per launch of the profiled step: start and duration (us), the
+    stream, and the idle time on that stream since its previous launch ended
+    (host round trips and launch latency)."""
+    last_end: dict[int, float] = {}
+    idle = {}
+    with open(path, "w") as f:
+        f.write("start_us  dur_us  stream  idle_us  kernel\n")
+        for name, t0, dur, sid in tl:
+            gap = (t0 - last_end[sid]) * 1e3 if sid in last_end else 0.0
+            idle[sid] = idle.get(sid, 0.0) + max(gap, 0.0)
+            last_end[sid] = t0 + dur
+            f.write(f"{t0 * 1e3:9.1f} {dur * 1e3:7.1f} {sid:6d} {gap:8.1f}  {name}\n")
+        end = max(last_end.values()) if last_end else 0.0
+        f.write(f"# span {end * 1e3:.1f} us; idle per stream (us): "
+                + ", ".join(f"{k}: {v:.1f}" for k, v in sorted(idle.items())) + "\n")
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -1045,6 +1065,9 @@ def main():
     ap.add_argument("--job-only", type=int, default=0,
                     help="one_to_many only: run the job this many times and print no JSON "
                          "line (for profilers)")
+    ap.add_argument("--timeline", default=None,
+                    help="pair workloads: write the profiled step's launches (start, duration, "
+                         "stream, idle gap before each) to this file")
     ap.add_argument("--pairs", type=int, default=None,
                     help="small_pairs only: number of pairs (default 65,536)")
     ap.add_argument("--overlays", type=int, default=None,

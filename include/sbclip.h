@@ -394,6 +394,15 @@ unsigned long long sbc_kernel_launches(void);
 int sbc_profile_begin(void);
 int sbc_profile_end(char* names, int names_len, float* ms, int* counts, double* bytes, int cap,
                     int* n_out);
+/* The launches of the window the last sbc_profile_end closed, in launch
+ * order (a device timeline; diagnostics): up to `cap` NUL-separated names,
+ * start_ms[i] from the first launch's start to launch i's start, dur_ms[i],
+ * and stream[i], the streams numbered in order of first use.  Gaps between
+ * one launch's end and the next one's start on a stream are idle time: host
+ * round trips and launch latency.  *n_out = launches; any output pointer may
+ * be NULL. */
+int sbc_profile_timeline(char* names, int names_len, float* start_ms, float* dur_ms, int* stream,
+                         int cap, int* n_out);
 
 /* Library version string. */
 const char* sbc_version(void);

@@ -411,6 +411,27 @@ int sbc_profile_end(char* names, int names_len, float* ms, int* counts, double* 
   return SBC_OK;
 }
 
+int sbc_profile_timeline(char* names, int names_len, float* start_ms, float* dur_ms, int* stream,
+                         int cap, int* n_out) {
+  const auto& tl = sbc::profile_timeline();
+  const int n = (int)tl.size();
+  if (n_out) *n_out = n;
+  int w = 0;
+  for (int i = 0; i < n && i < cap; ++i) {
+    if (start_ms) start_ms[i] = tl[i].start_ms;
+    if (dur_ms) dur_ms[i] = tl[i].dur_ms;
+    if (stream) stream[i] = tl[i].stream;
+    if (names) {
+      const int need = (int)strlen(tl[i].name) + 1;
+      if (w + need <= names_len) {
+        memcpy(names + w, tl[i].name, need);
+        w += need;
+      }
+    }
+  }
+  return SBC_OK;
+}
+
 const char* sbc_version(void) { return "sbclip-gb300 0.1 (sm_103a)"; }
 
 }  // extern "C"

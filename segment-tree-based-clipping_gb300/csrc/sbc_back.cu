@@ -916,7 +916,7 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
     int* listQ = (int*)bp.get("bk_listQ", sizeof(int) * (h.crossCount[1] + 1));
     int* rankP = (int*)bp.get("bk_rankP", sizeof(int) * nB);
     int* rankQ = (int*)bp.get("bk_rankQ", sizeof(int) * nQ);
-    void* sscr = bp.get("bk_scan", scan_scratch_bytes((long long)nB + nQ + 4));
+    void* sscr = bp.get_zeroed("bk_scan", scan_scratch_bytes((long long)nB + nQ + 4), st);
     if (bp.failed) return pl.fail(kENoMem, "device allocation failed (entry/exit)");
     {
       ::sbc::KProbe kp_("k_cross_flags", st);
@@ -926,8 +926,8 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
       ::sbc::KProbe kp_("k_cross_flags", st);
       k_cross_flags<<<grid_for(nQ + 1, 256), 256, 0, st>>>(nQ, isQ, labQ, preQ);
     }
-    exclusive_scan_i32(preP, nB + 1, sscr, st);
-    exclusive_scan_i32(preQ, nQ + 1, sscr, st);
+    exclusive_scan_i32(preP, nB + 1, sscr, st, true);
+    exclusive_scan_i32(preQ, nQ + 1, sscr, st, true);
     {
       ::sbc::KProbe kp_("k_enex", st);
       k_enex<<<grid_for(nB, 256), 256, 0, st>>>(nB, isP, labP, preP, 0, sc, enexP, splitP, listP);
@@ -989,7 +989,7 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
       ::sbc::KProbe kp_("k_tr_starts", st);
       k_tr_starts<<<grid_for(cPn + 1, 256), 256, 0, st>>>(T, mA, isStart);
     }
-    exclusive_scan_i32(isStart, cPn + 1, sscr, st);
+    exclusive_scan_i32(isStart, cPn + 1, sscr, st, true);
     int nRings = 0;
     cudaMemcpyAsync(&nRings, isStart + cPn, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
@@ -1027,7 +1027,7 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
       ::sbc::KProbe kp_("k_lr_ringlen", st);
       k_lr_ringlen<<<grid_for(nRings + 1, 256), 256, 0, st>>>(nRings, starts, SA, rlen);
     }
-    exclusive_scan_i32(rlen, nRings + 1, sscr, st);
+    exclusive_scan_i32(rlen, nRings + 1, sscr, st, true);
     int hv = 0;
     cudaMemcpyAsync(&hv, rlen + nRings, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(&h, sc, sizeof h, cudaMemcpyDeviceToHost, st);
@@ -1061,7 +1061,7 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
     int* rpre = (int*)bp.get("cl_rpre", sizeof(int) * (nR + 2));
     int* ooff = (int*)bp.get("ring_off_" + tg, sizeof(int) * (nR + 2));
     double* oxy = (double*)bp.get("ring_xy_" + tg, sizeof(double) * 2 * (nv + 1));
-    void* sscr = bp.get("cl_scan", scan_scratch_bytes(nv + nR + 4));
+    void* sscr = bp.get_zeroed("cl_scan", scan_scratch_bytes(nv + nR + 4), st);
     if (bp.failed) return pl.fail(kENoMem, "device allocation failed (clean-up)");
     cudaMemsetAsync(ringFlag, 0, sizeof(int) * (nR + 1), st);
     if (nv > 0) {
@@ -1073,7 +1073,7 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
       k_collinear<<<grid_for(nv + 1, 256), 256, 0, st>>>(nv, out.d_off, ringOf, out.d_xy, ringFlag,
                                                         keep, flagV, nxt, prv);
     }
-    exclusive_scan_i32(flagV, nv + 1, sscr, st);
+    exclusive_scan_i32(flagV, nv + 1, sscr, st, true);
     int nflag = 0;
     cudaMemcpyAsync(&nflag, flagV + nv, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
@@ -1087,12 +1087,12 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
                                                       out.d_xy, nxt, prv, keep);
     }
     int* kpv = keep;  // exclusive prefix of the keep flags (nv+1 entries)
-    exclusive_scan_i32(kpv, nv + 1, sscr, st);
+    exclusive_scan_i32(kpv, nv + 1, sscr, st, true);
     {
       ::sbc::KProbe kp_("k_ring_nonempty", st);
       k_ring_nonempty<<<grid_for(nR + 1, 128), 128, 0, st>>>(nR, out.d_off, kpv, rpre);
     }
-    exclusive_scan_i32(rpre, nR + 1, sscr, st);
+    exclusive_scan_i32(rpre, nR + 1, sscr, st, true);
     if (nv > 0) {
       ::sbc::KProbe kp_("k_compact_xy", st);
       k_compact_xy<<<grid_for(nv, 256), 256, 0, st>>>(nv, kpv, out.d_xy, oxy);

@@ -699,7 +699,7 @@ int Pipeline::stage_grid_count() {
   const long long nBk = (long long)g_nCells * (k + 1);
   g_bstart = (int*)pool_.get("grid_bstart", sizeof(int) * (nBk + 1));
   g_fill = (int*)pool_.get("grid_fill", sizeof(int) * (nBk + 1));
-  void* sscr2 = pool_.get("scan_scr_grid2", scan_scratch_bytes(nBk + 1));
+  void* sscr2 = pool_.get_zeroed("scan_scr_grid2", scan_scratch_bytes(nBk + 1), st);
   if (pool_.failed) return fail(kENoMem, "device allocation failed (grid buckets)");
   cudaMemsetAsync(g_bstart, 0, sizeof(int) * (nBk + 1), st);
   cudaMemsetAsync(g_fill, 0, sizeof(int) * (nBk + 1), st);
@@ -710,7 +710,7 @@ int Pipeline::stage_grid_count() {
     k_grid_count<<<grid_for(E, 256), 256, 0, st>>>(E, fbox, g, g_tstart, k, g_bstart, g_islong,
                                                  g_long, g_long_count, cmbr, outside);
   }
-  exclusive_scan_i32(g_bstart, nBk + 1, sscr2, st);
+  exclusive_scan_i32(g_bstart, nBk + 1, sscr2, st, true);
   cudaMemcpyAsync(h_side_rd_, g_bstart + nBk, sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(h_side_rd_ + 1, outside, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
   return kOk;
@@ -750,16 +750,16 @@ int Pipeline::stage_join(int cType, cudaStream_t st) {
   int* tiles = (int*)pool_.get("cg_tiles", sizeof(int) * ((long long)nCells + 1));
   long long* work = (long long*)pool_.get("cg_work", sizeof(long long) * ((long long)nCells + 1));
   auto* counters = (unsigned long long*)pool_.get("cg_counters", 64);
-  void* sscr = pool_.get("scan_scr_cg", scan_scratch_bytes((long long)nCells + 1));
+  void* sscr = pool_.get_zeroed("scan_scr_cg", scan_scratch_bytes((long long)nCells + 1), st);
   if (pool_.failed) return fail(kENoMem, "device allocation failed (grid items)");
   {
     ::sbc::KProbe kp_("k_cell_items", st);
     k_cell_items<<<grid_for((long long)nCells + 1, 256), 256, 0, st>>>(nCells, g_bstart, k, cType,
                                                                        cdesc, smalls, tiles, work);
   }
-  exclusive_scan_i32(smalls, (long long)nCells + 1, sscr, st);
-  exclusive_scan_i32(tiles, (long long)nCells + 1, sscr, st);
-  exclusive_scan_i64(work, (long long)nCells + 1, sscr, st);
+  exclusive_scan_i32(smalls, (long long)nCells + 1, sscr, st, true);
+  exclusive_scan_i32(tiles, (long long)nCells + 1, sscr, st, true);
+  exclusive_scan_i64(work, (long long)nCells + 1, sscr, st, true);
   int nS = 0, nW = 0;
   long long W = 0;
   cudaMemcpyAsync(&nS, smalls + nCells, sizeof(int), cudaMemcpyDeviceToHost, st);

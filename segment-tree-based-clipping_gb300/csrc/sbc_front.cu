@@ -38,6 +38,13 @@ void* BufferPool::get(const std::string& name, size_t bytes) {
   return b.p;
 }
 
+void* BufferPool::get_zeroed(const std::string& name, size_t bytes, cudaStream_t st) {
+  void* before = bufs_[name].p;
+  void* p = get(name, bytes);
+  if (p && p != before) cudaMemsetAsync(p, 0, bufs_[name].n, st);
+  return p;
+}
+
 size_t BufferPool::bytes_held() const {
   size_t t = 0;
   for (auto& kv : bufs_) t += kv.second.n;
@@ -408,7 +415,7 @@ int Pipeline::stage_elementary() {
   int* vloc = (int*)pool_.get("ele_vloc", sizeof(int) * (E + 1));
   int* flag = (int*)pool_.get("ele_flag", sizeof(int) * (n2 + 1));
   double* val = (double*)pool_.get("ele_val", sizeof(double) * n2);
-  void* sscr = pool_.get("scan_scr", scan_scratch_bytes(n2 + 1));
+  void* sscr = pool_.get_zeroed("scan_scr", scan_scratch_bytes(n2 + 1), st_);
   auto* vkey2 = (unsigned long long*)pool_.get("v_key2", sizeof(unsigned long long) * E);
   auto* vid2 = (unsigned*)pool_.get("v_id2", sizeof(unsigned) * E);
   if (pool_.failed) return fail(kENoMem, "device allocation failed (elementary)");
@@ -434,7 +441,7 @@ int Pipeline::stage_elementary() {
     ::sbc::KProbe kp_("k_vl_mark", st_);
     k_vl_mark<<<grid_for(E, 256), 256, 0, st_>>>(sidx, e_s, e_e, E, vl);
   }
-  exclusive_scan_i32(vl, E + 1, sscr, st_);
+  exclusive_scan_i32(vl, E + 1, sscr, st_, true);
   {
     ::sbc::KProbe kp_("k_vl_loc", st_);
     k_vl_loc<<<grid_for(E, 256), 256, 0, st_>>>(vl, E, vloc);
@@ -444,7 +451,7 @@ int Pipeline::stage_elementary() {
     ::sbc::KProbe kp_("k_ele_flags", st_);
     k_ele_flags<<<grid_for(n2, 256), 256, 0, st_>>>(sidx, e_s, e_e, vl, vloc, E, flag, val);
   }
-  exclusive_scan_i32(flag, n2 + 1, sscr, st_);
+  exclusive_scan_i32(flag, n2 + 1, sscr, st_, true);
   unsigned fl = 0;
   unsigned long long hm[2] = {0, 0};
   cudaMemcpyAsync(&count, flag + n2, sizeof(int), cudaMemcpyDeviceToHost, st_);
@@ -623,12 +630,17 @@ __global__ void k_run_bounds(long long n2, const unsigned long long* __restrict_
   if (last) re[r] = (int)i;
 }
 
-// per endpoint: the positions [lo, hi) of ea holding its value
+// per endpoint: the positions [lo, hi) of ea holding its value and its run.
+// Every endpoint of a run has the same value, range and search path, so the
+// run's first endpoint runs findBoarder's search (border_by_position) once
+// and stores it per run; k_edge_tree reads it through the run index.
 __global__ void k_endpoint_range(long long n2, const unsigned long long* __restrict__ keys,
                                  const unsigned* __restrict__ sidx, const int* __restrict__ rpre,
                                  const int* __restrict__ rs, const int* __restrict__ re,
-                                 const int* __restrict__ F, int count, int epc,
-                                 const double* __restrict__ ea, int2* __restrict__ erange) {
+                                 const int* __restrict__ F, int count, int epc, int z,
+                                 const double* __restrict__ ea, const double* __restrict__ es,
+                                 const double* __restrict__ ee, int2* __restrict__ erange,
+                                 int* __restrict__ erun, int* __restrict__ rbord) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n2) return;
   const bool first = i == 0 || keys[i] != keys[i - 1];
@@ -637,13 +649,20 @@ __global__ void k_endpoint_range(long long n2, const unsigned long long* __restr
   int lo = F[rs[r]], hi = F[re[r] + 1];
   if (keys[i] == kl) hi = epc;             // and the padding
   else if (keys[i] > kl) lo = hi = epc;    // above every entry, padding included
-  erange[sidx[i]] = make_int2(lo, hi);
+  const unsigned x = sidx[i];
+  erange[x] = make_int2(lo, hi);
+  erun[x] = r;
+  if (first) {
+    const double q = (x & 1u) ? ee[x >> 1] : es[x >> 1];
+    rbord[r] = border_by_position(epc, z, lo, hi, q);
+  }
 }
 
-__global__ void k_edge_tree(const double* __restrict__ es, const double* __restrict__ ee, int E,
-                            const int2* __restrict__ erange, const double* __restrict__ ea,
-                            int epc, int z, int logL, int* __restrict__ aft, int* __restrict__ bef,
-                            int2* __restrict__ lr, unsigned long long* __restrict__ cnt) {
+__global__ void k_edge_tree(int E, const int2* __restrict__ erange, const int* __restrict__ erun,
+                            const int* __restrict__ rbord,
+                            const double* __restrict__ ea, int epc, int z, int logL,
+                            int* __restrict__ aft, int* __restrict__ bef, int2* __restrict__ lr,
+                            unsigned long long* __restrict__ cnt) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned n_leaf = 0;
   if (e < E) {
@@ -651,7 +670,7 @@ __global__ void k_edge_tree(const double* __restrict__ es, const double* __restr
     const int2 rS = erange[2 * e], rE = erange[2 * e + 1];
     auto J = [&](int m) { return m < z ? m : (m == z ? epc - 1 : m - 1); };
     int a = -1, b = -1;
-    const int en = border_by_position(epc, z, rE.x, rE.y, ee[e]);
+    const int en = rbord[erun[2 * e + 1]];
     if (en >= 0) {
       const int j = J(en);  // right[j]
       int node = 0;
@@ -662,7 +681,7 @@ __global__ void k_edge_tree(const double* __restrict__ es, const double* __restr
       }
       if (node >= L && node < 2 * L && ea[node - L] != ea[node - L + 1]) a = node;
     }
-    const int st = border_by_position(epc, z, rS.x, rS.y, es[e]);
+    const int st = rbord[erun[2 * e]];
     if (st >= 0) {
       const int j = J(st);  // left[j]
       int node = 0;
@@ -757,14 +776,16 @@ int Pipeline::stage_endlists() {
     int* rs = (int*)pool_.get("run_s", sizeof(int) * n2);
     int* re = (int*)pool_.get("run_e", sizeof(int) * n2);
     int2* erange = (int2*)pool_.get("endpoint_range", sizeof(int2) * n2);
-    void* sscr = pool_.get("scan_scr", scan_scratch_bytes(n2 + 1));
+    int* erun = (int*)pool_.get("endpoint_run", sizeof(int) * n2);
+    int* rbord = (int*)pool_.get("run_border", sizeof(int) * n2);
+    void* sscr = pool_.get_zeroed("scan_scr", scan_scratch_bytes(n2 + 1), st_);
     lr = (int2*)pool_.get("edge_leaf_range", sizeof(int2) * (E + 1));
     if (pool_.failed) return fail(kENoMem, "device allocation failed (end lists)");
     {
       ::sbc::KProbe kp_("k_run_start", st_, 12.0 * n2);
       k_run_start<<<grid_for(n2 + 1, 256), 256, 0, st_>>>(n2, keys, rpre);
     }
-    exclusive_scan_i32(rpre, n2 + 1, sscr, st_);
+    exclusive_scan_i32(rpre, n2 + 1, sscr, st_, true);
     {
       ::sbc::KProbe kp_("k_run_bounds", st_, 20.0 * n2);
       k_run_bounds<<<grid_for(n2, 256), 256, 0, st_>>>(n2, keys, rpre, rs, re);
@@ -772,13 +793,14 @@ int Pipeline::stage_endlists() {
     {
       ::sbc::KProbe kp_("k_endpoint_range", st_, 36.0 * n2);
       k_endpoint_range<<<grid_for(n2, 256), 256, 0, st_>>>(n2, keys, sidx, rpre, rs, re, F,
-                                                           ele_count, epc, ea, erange);
+                                                           ele_count, epc, z, ea, e_s, e_e, erange,
+                                                           erun, rbord);
     }
     {
       // es, ee and two endpoint ranges in; aft, bef, leaf range out
       ::sbc::KProbe kp_("k_edge_tree", st_, 48.0 * E);
-      k_edge_tree<<<grid_for(E, 256), 256, 0, st_>>>(e_s, e_e, E, erange, ea, epc, z, logL, aft, bef,
-                                                     lr, d_treecnt);
+      k_edge_tree<<<grid_for(E, 256), 256, 0, st_>>>(E, erange, erun, rbord, ea, epc, z, logL,
+                                                     aft, bef, lr, d_treecnt);
     }
     lr_ready = true;
     return kOk;

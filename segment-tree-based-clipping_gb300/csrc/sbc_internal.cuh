@@ -163,9 +163,11 @@ __device__ __forceinline__ unsigned block_min(unsigned v) {
 // the entries equal to q sit at positions [lo, hi) of ea, comparing S(m)
 // with q needs no memory access.  Returns -1 smaller, 0 equal, 1 greater,
 // 2 past the arrays.
-__device__ __forceinline__ int border_cmp(int epc, int z, int m, int lo, int hi, double q) {
+// cz: the comparison at the zero slot, (0.0 == q) ? 0 : (0.0 < q ? -1 : 1),
+// taken once per search
+__device__ __forceinline__ int border_cmp(int epc, int z, int m, int lo, int hi, int cz) {
   if (m < 0 || m >= epc) return 2;
-  if (m == z) return (0.0 == q) ? 0 : (0.0 < q ? -1 : 1);
+  if (m == z) return cz;
   const int t = m < z ? m + 1 : m;
   return t < lo ? -1 : (t < hi ? 0 : 1);
 }
@@ -173,12 +175,13 @@ __device__ __forceinline__ int border_cmp(int epc, int z, int m, int lo, int hi,
 // findBoarder (oacc_segment_tree.cpp:420-460), its search path followed on
 // positions (including the misses the zero slot causes)
 __device__ __forceinline__ int border_by_position(int epc, int z, int lo, int hi, double q) {
+  const int cz = (0.0 == q) ? 0 : (0.0 < q ? -1 : 1);
   int l = 0, h = epc;
   while (l < h) {
     const int m = l + (h - l) / 2;
-    const int c = border_cmp(epc, z, m, lo, hi, q);
+    const int c = border_cmp(epc, z, m, lo, hi, cz);
     if (c == 0) {
-      if (border_cmp(epc, z, m - 1, lo, hi, q) != 0) {
+      if (border_cmp(epc, z, m - 1, lo, hi, cz) != 0) {
         h = m;
         l = h;
       } else {
@@ -190,16 +193,20 @@ __device__ __forceinline__ int border_by_position(int epc, int z, int lo, int hi
       h = m - 1;
     }
   }
-  return border_cmp(epc, z, h, lo, hi, q) == 0 ? h : -1;
+  return border_cmp(epc, z, h, lo, hi, cz) == 0 ? h : -1;
 }
 
 // ---------------------------------------------------------------- primitives
 // (sbc_prims.cu)  All run on `st`; scratch comes from the caller.
 size_t scan_scratch_bytes(long long n);
-// exclusive scan in place over n int32 (or int64) values; returns via d_total
-// (optional) the total.
-void exclusive_scan_i32(int* d, long long n, void* scratch, cudaStream_t st);
-void exclusive_scan_i64(long long* d, long long n, void* scratch, cudaStream_t st);
+// exclusive scan in place over n int32 (or int64) values.  The scan leaves
+// the look-back words of its scratch zero; state_zero says the scratch is
+// known to start zero (allocated zeroed and only used by scans), which saves
+// a memset per scan.
+void exclusive_scan_i32(int* d, long long n, void* scratch, cudaStream_t st,
+                        bool state_zero = false);
+void exclusive_scan_i64(long long* d, long long n, void* scratch, cudaStream_t st,
+                        bool state_zero = false);
 // true (and cleared) if a scan's bounded look-back wait gave up since the last call
 bool scan_error_take();
 
@@ -238,8 +245,15 @@ void profile_begin();
 bool profiling_suspend();
 void profiling_restore(bool on);
 // aggregated per kernel name: returns the number of distinct kernels
+struct TimelineRec {
+  const char* name;
+  float start_ms, dur_ms;
+  int stream;
+};
 int profile_end(std::vector<std::string>* names, std::vector<float>* ms, std::vector<int>* counts,
                 std::vector<double>* bytes = nullptr);
+// the launches of the window profile_end closed, in launch order
+const std::vector<TimelineRec>& profile_timeline();
 
 inline unsigned grid_for(long long n, int per_block) {
   long long g = (n + per_block - 1) / per_block;

@@ -489,7 +489,7 @@ int Pipeline::stage_records(int cType, const int* rb, const int* rc, const int* 
   int* bfill = (int*)pool_.get("dd_bfill", sizeof(int) * ((long long)bSize + 2));
   auto* ord = (unsigned*)pool_.get("dd_ord", sizeof(unsigned) * (R + 1));
   int* keep = (int*)pool_.get("dd_keep", sizeof(int) * (R + 2));
-  void* sscr2 = pool_.get("scan_scr5", scan_scratch_bytes(R + 2 > bSize + 2 ? R + 2 : bSize + 2));
+  void* sscr2 = pool_.get_zeroed("scan_scr5", scan_scratch_bytes(R + 2 > bSize + 2 ? R + 2 : bSize + 2), st);
   if (pool_.failed) return fail(kENoMem, "device allocation failed (dedup)");
   int K = 0;
   const int nseg = bSize;
@@ -501,7 +501,7 @@ int Pipeline::stage_records(int cType, const int* rb, const int* rc, const int* 
       ::sbc::KProbe kp_("k_bucket_count", st);
       k_bucket_count<<<grid_for(R, 256), 256, 0, st>>>(rb, R, segstart);
     }
-    exclusive_scan_i32(segstart, (long long)bSize + 1, sscr2, st);
+    exclusive_scan_i32(segstart, (long long)bSize + 1, sscr2, st, true);
     {
       ::sbc::KProbe kp_("k_bucket_scatter", st);
       k_bucket_scatter<<<grid_for(R, 256), 256, 0, st>>>(rb, R, segstart, bfill, sv);
@@ -522,7 +522,7 @@ int Pipeline::stage_records(int cType, const int* rb, const int* rc, const int* 
                      256, 0, st>>>(segstart, long_list, long_count, sv, rkey, rc, ord, keep);
     }
     cudaMemsetAsync(keep + R, 0, sizeof(int), st);
-    exclusive_scan_i32(keep, R + 1, sscr2, st);
+    exclusive_scan_i32(keep, R + 1, sscr2, st, true);
     cudaMemcpyAsync(&K, keep + R, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
   }
@@ -562,7 +562,7 @@ int Pipeline::stage_records(int cType, const int* rb, const int* rc, const int* 
   auto* csk2 = (unsigned*)pool_.get("cs_keys2", sizeof(unsigned) * (K + 1));
   auto* csv2 = (unsigned*)pool_.get("cs_vals2", sizeof(unsigned) * (K + 1));
   void* rscr2 = pool_.get("radix_scr_cs", radix_scratch_bytes(K + 1));
-  void* sscr3 = pool_.get("scan_scr6", scan_scratch_bytes(bSize + cSize + 4));
+  void* sscr3 = pool_.get_zeroed("scan_scr6", scan_scratch_bytes(bSize + cSize + 4), st);
   if (pool_.failed) return fail(kENoMem, "device allocation failed (counts)");
   cudaMemsetAsync(bAll, 0, sizeof(int) * (bSize + 1), st);
   cudaMemsetAsync(bND, 0, sizeof(int) * (bSize + 1), st);
@@ -581,10 +581,10 @@ int Pipeline::stage_records(int cType, const int* rb, const int* rc, const int* 
     while ((1LL << bits) < 2LL * (clSize + k)) ++bits;
     radix_sort_u32(csk, csv, csk2, csv2, K, bits, rscr2, st);
   }
-  exclusive_scan_i32(bAll, bSize + 1, sscr3, st);
-  exclusive_scan_i32(bND, bSize + 1, sscr3, st);
-  exclusive_scan_i32(cAll, cSize + 1, sscr3, st);
-  exclusive_scan_i32(cND, cSize + 1, sscr3, st);
+  exclusive_scan_i32(bAll, bSize + 1, sscr3, st, true);
+  exclusive_scan_i32(bND, bSize + 1, sscr3, st, true);
+  exclusive_scan_i32(cAll, cSize + 1, sscr3, st, true);
+  exclusive_scan_i32(cND, cSize + 1, sscr3, st, true);
   int hb = 0, hc = 0;
   cudaMemcpyAsync(&hb, bND + bSize, sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(&hc, cND + cSize, sizeof(int), cudaMemcpyDeviceToHost, st);

@@ -21,6 +21,9 @@ class BufferPool {
   ~BufferPool();
   // returns a device pointer of at least `bytes` (256-byte aligned)
   void* get(const std::string& name, size_t bytes);
+  // the same, with newly allocated memory cleared on stream st (for scan
+  // scratch, which every scan leaves zero)
+  void* get_zeroed(const std::string& name, size_t bytes, cudaStream_t st);
   size_t bytes_held() const;
   void release_all();
   int failed = 0;

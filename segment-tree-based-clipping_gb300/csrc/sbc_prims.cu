@@ -21,7 +21,11 @@ struct ProbeRec {
   const char* name;
   cudaEvent_t a, b;
   double bytes;
+  cudaStream_t st;
 };
+// the last profiled window, launch by launch: start relative to the first
+// launch's start, duration, stream (numbered in order of first use)
+std::vector<TimelineRec> g_timeline;
 // probes may come from several host threads (the pairwise engine's big-pair
 // workers): the record list is guarded
 std::atomic<bool> g_prof_on{false};
@@ -44,7 +48,7 @@ KProbe::KProbe(const char* name, cudaStream_t st, double bytes) : name_(name), s
   ++g_launches;
   if (!g_prof_on) return;
   std::lock_guard<std::mutex> lk(g_prof_mu);
-  ProbeRec r{name, next_event(), next_event(), bytes};
+  ProbeRec r{name, next_event(), next_event(), bytes, st};
   cudaEventRecord(r.a, st);
   slot_ = (int)g_recs.size();
   g_recs.push_back(r);
@@ -64,6 +68,8 @@ bool profiling_suspend() {
 
 void profiling_restore(bool on) { g_prof_on = on; }
 
+const std::vector<TimelineRec>& profile_timeline() { return g_timeline; }
+
 void profile_begin() {
   std::lock_guard<std::mutex> lk(g_prof_mu);
   g_recs.clear();
@@ -79,10 +85,17 @@ int profile_end(std::vector<std::string>* names, std::vector<float>* ms, std::ve
   ms->clear();
   counts->clear();
   if (bytes) bytes->clear();
+  g_timeline.clear();
+  std::vector<cudaStream_t> streams;
   for (auto& r : g_recs) {
     cudaEventSynchronize(r.b);
-    float t = 0.f;
+    float t = 0.f, t0 = 0.f;
     cudaEventElapsedTime(&t, r.a, r.b);
+    cudaEventElapsedTime(&t0, g_recs[0].a, r.a);
+    int sid = 0;
+    while (sid < (int)streams.size() && streams[sid] != r.st) ++sid;
+    if (sid == (int)streams.size()) streams.push_back(r.st);
+    g_timeline.push_back(TimelineRec{r.name, t0, t, sid});
     size_t i = 0;
     while (i < names->size() && (*names)[i] != r.name) ++i;
     if (i == names->size()) {
@@ -289,15 +302,28 @@ k_scan_lb(T* __restrict__ d, long long n, unsigned long long* __restrict__ state
     run += v[i];
   }
   scan_store(d, base, n, vec, o);
+  // The last block to finish clears the look-back words (ticket, tile words,
+  // this counter) so the next scan on the same scratch needs no memset: a
+  // block counts itself done only after its own look-back reads, so when the
+  // count reaches the number of tiles nobody reads the words any more.
+  __shared__ bool s_last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(&state[gridDim.x + 1], 1ull) == (unsigned long long)gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last)
+    for (unsigned i = threadIdx.x; i <= gridDim.x + 1; i += blockDim.x) state[i] = 0ull;
 }
 
 template <typename T>
-void scan_rec(T* d, long long n, T* scratch, cudaStream_t st) {
+void scan_rec(T* d, long long n, T* scratch, cudaStream_t st, bool state_zero = false) {
   if (n <= 0) return;
   const long long tiles = (n + kScanTile - 1) / kScanTile;
   if (tiles > 1) {
     auto* state = (unsigned long long*)scratch;
-    cudaMemsetAsync(state, 0, sizeof(unsigned long long) * (tiles + 1), st);
+    // the scan leaves its words zero; a scratch not known to start zero is cleared first
+    if (!state_zero) cudaMemsetAsync(state, 0, sizeof(unsigned long long) * (tiles + 2), st);
     ::sbc::KProbe kp_("k_scan_lb", st, 2.0 * sizeof(T) * (double)n);
     k_scan_lb<T><<<(unsigned)tiles, kScanThreads, 0, st>>>(d, n, state,
                                                        ((uintptr_t)d & 15) == 0);
@@ -332,7 +358,7 @@ void scan_multi(T* d, long long n, T* scratch, cudaStream_t st) {
 }  // namespace
 
 size_t scan_scratch_bytes(long long n) {
-  const size_t lb = (size_t)((n + kScanTile - 1) / kScanTile + 1) * sizeof(unsigned long long);
+  const size_t lb = (size_t)((n + kScanTile - 1) / kScanTile + 2) * sizeof(unsigned long long);
   size_t tot = 0;
   while (n > kScanTile) {
     long long nb = (n + kScanTile - 1) / kScanTile;
@@ -352,11 +378,12 @@ bool scan_error_take() {
   return h != 0;
 }
 
-void exclusive_scan_i32(int* d, long long n, void* scratch, cudaStream_t st) {
-  scan_rec<int>(d, n, (int*)scratch, st);
+void exclusive_scan_i32(int* d, long long n, void* scratch, cudaStream_t st, bool state_zero) {
+  scan_rec<int>(d, n, (int*)scratch, st, state_zero);
 }
-void exclusive_scan_i64(long long* d, long long n, void* scratch, cudaStream_t st) {
-  scan_rec<long long>(d, n, (long long*)scratch, st);
+void exclusive_scan_i64(long long* d, long long n, void* scratch, cudaStream_t st,
+                        bool state_zero) {
+  scan_rec<long long>(d, n, (long long*)scratch, st, state_zero);
 }
 
 // ============================================================== radix sort

@@ -138,6 +138,7 @@ def load_library(path: str | os.PathLike | None = None):
     L.sbc_classify_pairs.argtypes = [vp, vp, i, vp, vp, vp, vp, vp]
     L.sbc_kernel_launches.restype = ctypes.c_ulonglong
     L.sbc_profile_end.argtypes = [vp, i, vp, vp, vp, i, ctypes.POINTER(i)]
+    L.sbc_profile_timeline.argtypes = [vp, i, vp, vp, vp, i, ctypes.POINTER(i)]
     L.sbc_version.restype = ctypes.c_char_p
     for nm in ("sbc_clip_batch", "sbc_clip_batch_device"):
         getattr(L, nm).argtypes = [vp, ctypes.POINTER(_Batch), ctypes.POINTER(_BatchRings), vp]
@@ -200,6 +201,25 @@ def profile_end(with_bytes: bool = False) -> dict:
         return {nm[i].decode(): (float(ms[i]), int(cnt[i]), float(by[i]))
                 for i in range(min(n.value, cap))}
     return {nm[i].decode(): (float(ms[i]), int(cnt[i])) for i in range(min(n.value, cap))}
+
+
+def profile_timeline() -> list[tuple[str, float, float, int]]:
+    """The launches of the window the last profile_end closed, in launch
+    order: (kernel name, start ms from the first launch's start, duration ms,
+    stream number)."""
+    L = load_library()
+    n = ctypes.c_int()
+    L.sbc_profile_timeline(None, 0, None, None, None, 0, ctypes.byref(n))
+    cap = n.value
+    if cap <= 0:
+        return []
+    names = ctypes.create_string_buffer(cap * 64)
+    t0 = (ctypes.c_float * cap)()
+    dur = (ctypes.c_float * cap)()
+    sid = (ctypes.c_int * cap)()
+    L.sbc_profile_timeline(names, cap * 64, t0, dur, sid, cap, ctypes.byref(n))
+    nm = names.raw.split(b"\0")
+    return [(nm[i].decode(), float(t0[i]), float(dur[i]), int(sid[i])) for i in range(cap)]
 
 
 def _rings_from(r: _Rings):
