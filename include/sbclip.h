@@ -49,6 +49,9 @@ typedef struct sbc_options {
 #define SBC_FLAG_ENDPOINT_SORT 8   /* build the elementary intervals from a sort of all 2E edge
                                       endpoints instead of the E vertices (a test hook: the
                                       arrays and rings are the same either way) */
+#define SBC_FLAG_WIDE_VERTEX_SORT 16 /* sort the vertices on their 64-bit order keys instead of
+                                      32-bit keys plus the fix-up of equal-key runs (a test
+                                      hook: same arrays and rings) */
 
 typedef struct sbc_rings {
   int nrings;
@@ -95,7 +98,9 @@ int sbc_clip_pair_device(sbc_ctx* ctx, const double* d_b_xy, int nb, const doubl
 #define SBC_STAT_SERIAL_BACKEND 10      /* 1 if the exact serial back end ran */
 #define SBC_STAT_WORK_UNITS 11          /* overlay 1: edge-box pairs tested by the grid join */
 #define SBC_STAT_GRID_PAIRS 12          /* overlay 1: box-overlapping edge pairs the grid found */
-#define SBC_STAT_VERTEX_SORT 13         /* 1 if the endpoint order came from the vertex sort */
+#define SBC_STAT_VERTEX_SORT 13         /* the endpoint order came from: 0 the endpoint sort,
+                                           1 the vertex sort on 64-bit keys, 2 the vertex sort
+                                           on 32-bit keys with equal-key runs fixed up */
 #define SBC_STAT_OUTSIDE_CMBR 14        /* edges whose box misses the common MBR of the base and
                                            the overlays (left out of the candidate search; the
                                            reference's getCMBR, src/clip.cpp:743-777) */

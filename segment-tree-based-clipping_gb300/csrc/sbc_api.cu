@@ -32,21 +32,46 @@ int Pipeline::run(const double* d_bxy, int nb_, const double* d_cxy, const int* 
     if (timing) cudaEventRecord(ev[i], st_);
   };
   mark(0);
-  // the tree stages on the main stream; the grid stage's three steps on the
-  // side stream in between (each step's host read mostly finds its work done)
   int rc = stage_setup(d_bxy, d_cxy, c_sizes);
-  if (!rc) rc = stage_grid_boxes();
+  // The grid stage and the first overlay's box join read only the setup's
+  // arrays: they run on the side stream, issued by the side worker thread,
+  // while this thread issues the tree stages on the main stream.  Each
+  // thread's host reads wait for its own stream only.
+  bool side_posted = false;
+  int side_rc = 0;
+  if (!rc) {
+    if (!side_stream()) {
+      rc = fail(kECuda, "side stream");
+    } else {
+      cudaEventRecord(ev_setup_, st_);
+      side_err_.clear();
+      auto side_task = [this]() {
+        int r = stage_grid_boxes();
+        if (!r) r = stage_grid_count();
+        if (!r) r = stage_grid_fill();
+        if (!r) r = stage_join(1, st2_);
+        if (cudaGetLastError() != cudaSuccess && !r) r = fail(kECuda, "CUDA error in the grid stage");
+        return r;
+      };
+      side_posted = side_.post(dev_, side_task);
+      if (!side_posted) {
+        // no worker thread: the same steps on this thread, before the tree
+        side_rc = side_task();
+        if (side_rc) rc = fail(side_rc, side_err_.empty() ? err_ : side_err_);
+      }
+    }
+  }
   mark(1);
   if (!rc) rc = stage_elementary();
-  if (!rc) rc = stage_grid_count();
   mark(2);
   if (!rc) rc = stage_endlists();
-  if (!rc) rc = stage_grid_fill();
   mark(3);
   if (!rc) rc = stage_cover();
-  // the first overlay's box join reads only the grid: on the side stream too
-  if (!rc) rc = stage_join(1, side_stream());
   mark(4);
+  if (side_posted) {
+    side_rc = side_.wait();
+    if (side_rc && !rc) rc = fail(side_rc, side_err_);
+  }
   // the candidate stage (main stream) reads the grid and the join; on an
   // error, later work on the main stream still waits for the side stream's
   // kernels (they read this context's buffers)
@@ -55,9 +80,14 @@ int Pipeline::run(const double* d_bxy, int nb_, const double* d_cxy, const int* 
   if (!rc) launch_cover_count();
   for (int t = 1; t <= k && !rc; ++t) rc = stage_overlay(t, outs_[t - 1]);
   mark(5);
+  // the scans' error word lands with the final wait (take_tree_stats)
+  unsigned* d_scan_err = scan_error_word();
+  const unsigned* r_scan = d_scan_err ? rd_.get(d_scan_err, HostReads::kFlags + 1, st_) : nullptr;
   take_tree_stats();
+  finish_counts();
   if (cudaGetLastError() != cudaSuccess && !rc) rc = fail(kECuda, "CUDA error in the pipeline");
-  if (scan_error_take() && !rc) rc = fail(kEInternal, "a scan's bounded wait gave up");
+  const bool scan_gave_up = r_scan ? (*r_scan != 0u && scan_error_take()) : scan_error_take();
+  if (scan_gave_up && !rc) rc = fail(kEInternal, "a scan's bounded wait gave up");
   if (timing) {
     cudaEventSynchronize(ev[5]);
     for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&times.ms[i], ev[i], ev[i + 1]);
@@ -80,6 +110,7 @@ int Pipeline::run_from_hits(const double* d_bxy, int nb_, const double* d_cxy, i
   // the setup's non-finite check (run() reads it with the elementary counts)
   if (!rc0 && (read_flags() & kFlagUndef)) rc0 = fail(kEInput, "non-finite vertex coordinate");
   if (!rc0) rc0 = stage_records(1, rb, rc, rt, rkey, nhits, outs_[0], true);
+  finish_counts();
   if (cudaGetLastError() != cudaSuccess && !rc0) rc0 = fail(kECuda, "CUDA error in the pipeline");
   if (scan_error_take() && !rc0) rc0 = fail(kEInternal, "a scan's bounded wait gave up");
   return rc0;
@@ -175,6 +206,7 @@ int run_device(sbc_ctx* c, const double* d_b, int nb, const double* d_c, const i
   pl.timing = (c->flags & SBC_FLAG_TIMING) != 0;
   pl.force_serial_backend = (c->flags & SBC_FLAG_SERIAL_BACKEND) ? 1 : 0;
   pl.force_endpoint_sort = (c->flags & SBC_FLAG_ENDPOINT_SORT) ? 1 : 0;
+  pl.force_wide_vertex_sort = (c->flags & SBC_FLAG_WIDE_VERTEX_SORT) ? 1 : 0;
   int rc = pl.run(d_b, nb, d_c, sizes, k);
   if (rc) return set_err(c, rc, pl.error());
   fill_stats(c);

@@ -440,10 +440,13 @@ __global__ void k_lr_check(Trace T, const int* __restrict__ nxt, const int* __re
   if (nxt[x] == -1 && tr_target(T, x) == ringI[x]) atomicOr(&sc->anomaly, 256u);
 }
 
-__global__ void k_lr_ringlen(int nRings, const int* __restrict__ starts,
-                             const long long* __restrict__ S, int* __restrict__ rlen) {
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r > nRings) return;
+// rlen[r] for r <= cap: ring r's length, 0 from the ring count on
+__global__ void k_lr_ringlen(int cap, const int* __restrict__ nRings_p,
+                             const int* __restrict__ starts, const long long* __restrict__ S,
+                             int* __restrict__ rlen) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r > cap) return;
+  const int nRings = *nRings_p;
   rlen[r] = r < nRings ? (int)S[starts[r]] : 0;
 }
 
@@ -550,12 +553,14 @@ __global__ void k_flag_list(long long nv, const int* __restrict__ fpre, int* __r
 // iterating from a deleted vertex through its old next pointer; so does this.
 __global__ void k_cleanup_ring(int nRings, const int* __restrict__ off,
                                const int* __restrict__ ringFlag, const int* __restrict__ flist,
-                               int nflag, const double* __restrict__ xy, int* __restrict__ nxt,
-                               int* __restrict__ prv, int* __restrict__ keep) {
+                               const int* __restrict__ nflag_p, const double* __restrict__ xy,
+                               int* __restrict__ nxt, int* __restrict__ prv,
+                               int* __restrict__ keep) {
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nRings) return;
   int a = off[r], b = off[r + 1];
   if (!ringFlag[r] || b == a) return;
+  const int nflag = *nflag_p;
   auto A = [&](int v) {
     int p = prv[v], q = nxt[v];
     return fabs(area3(xy[2 * p], xy[2 * p + 1], xy[2 * v], xy[2 * v + 1], xy[2 * q], xy[2 * q + 1]));
@@ -847,9 +852,12 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
     ::sbc::KProbe kp_("k_side_stats", st);
     k_side_stats<<<grid_for(nQ, 256), 256, 0, st>>>(nQ, isQ, labQ, 1, 0, sc);
   }
+  static_assert(sizeof(BkScalars) <= 8 * 8, "BkScalars fits the back end's host words");
+  HostReads& rd = pl.reads();
   BkScalars h;
-  cudaMemcpyAsync(&h, sc, sizeof h, cudaMemcpyDeviceToHost, st);
+  const BkScalars* r_sc = rd.get(sc, HostReads::kBack, st);
   cudaStreamSynchronize(st);
+  h = *r_sc;
   if (h.anomaly) return serial_backend(pl, m, out, ovTag);
   const bool noP = h.crossCount[0] == 0, noQ = h.crossCount[1] == 0;
   if (noP != noQ) return serial_backend(pl, m, out, ovTag);
@@ -872,8 +880,9 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
   std::string tg = std::to_string(ovTag);
   if (noP) {
     // both polygons without crossings: each one inside the other is a ring
-    cudaMemcpyAsync(&h, sc, sizeof h, cudaMemcpyDeviceToHost, st);
+    r_sc = rd.get(sc, HostReads::kBack, st);
     cudaStreamSynchronize(st);
+    h = *r_sc;
     bool inP = (h.winding[0] % 2) != 0, inQ = (h.winding[1] % 2) != 0;
     int nr = (inP ? 1 : 0) + (inQ ? 1 : 0);
     long long nv = (inP ? nB : 0) + (inQ ? nQ : 0);
@@ -980,21 +989,20 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
       ::sbc::KProbe kp_("k_tr_consistent", st);
       k_tr_consistent<<<grid_for(nE, 256), 256, 0, st>>>(T, mA, sc);
     }
-    cudaMemcpyAsync(&h, sc, sizeof h, cudaMemcpyDeviceToHost, st);
-    cudaStreamSynchronize(st);
-    if (h.anomaly) return serial_backend(pl, m, out, ovTag);
+    // An anomaly found so far is read with the ring count below: the
+    // kernels in between stay in bounds whatever the orbit minima hold
+    // (k_lr_init checks them, and ring starts are ranks of P crossings).
 
-    // ---- ring starts and segment walks
+    // ---- ring starts and segment walks.  There are at most cPn rings (a
+    // ring starts at a P crossing): the ring arrays are sized for that, and
+    // the ring count stays on the device until the one read below.
     {
       ::sbc::KProbe kp_("k_tr_starts", st);
       k_tr_starts<<<grid_for(cPn + 1, 256), 256, 0, st>>>(T, mA, isStart);
     }
     exclusive_scan_i32(isStart, cPn + 1, sscr, st, true);
-    int nRings = 0;
-    cudaMemcpyAsync(&nRings, isStart + cPn, sizeof(int), cudaMemcpyDeviceToHost, st);
-    cudaStreamSynchronize(st);
-    int* starts = (int*)bp.get("bk_starts", sizeof(int) * (nRings + 1));
-    int* rlen = (int*)bp.get("bk_rlen", sizeof(int) * (nRings + 2));
+    int* starts = (int*)bp.get("bk_starts", sizeof(int) * (cPn + 1));
+    int* rlen = (int*)bp.get("bk_rlen", sizeof(int) * (cPn + 2));
     int* nxA = (int*)bp.get("bk_lrnA", sizeof(int) * (nE + 1));
     int* nxB = (int*)bp.get("bk_lrnB", sizeof(int) * (nE + 1));
     long long* SA = (long long*)bp.get("bk_lrSA", sizeof(long long) * (nE + 1));
@@ -1025,15 +1033,18 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
     }
     {
       ::sbc::KProbe kp_("k_lr_ringlen", st);
-      k_lr_ringlen<<<grid_for(nRings + 1, 256), 256, 0, st>>>(nRings, starts, SA, rlen);
+      k_lr_ringlen<<<grid_for(cPn + 1, 256), 256, 0, st>>>(cPn, isStart + cPn, starts, SA, rlen);
     }
-    exclusive_scan_i32(rlen, nRings + 1, sscr, st, true);
-    int hv = 0;
-    cudaMemcpyAsync(&hv, rlen + nRings, sizeof(int), cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(&h, sc, sizeof h, cudaMemcpyDeviceToHost, st);
+    // zero lengths past the last ring: rlen[cPn] is the vertex total
+    exclusive_scan_i32(rlen, cPn + 1, sscr, st, true);
+    const int* r_nr = rd.get(isStart + cPn, HostReads::kBack + 8, st);
+    const int* r_nv = rd.get(rlen + cPn, HostReads::kBack + 9, st);
+    r_sc = rd.get(sc, HostReads::kBack, st);
     cudaStreamSynchronize(st);
+    h = *r_sc;
     if (h.anomaly) return serial_backend(pl, m, out, ovTag);
-    const long long nv = hv;
+    const int nRings = *r_nr;
+    const long long nv = *r_nv;
     double* rxy = (double*)bp.get("bk_rxy", sizeof(double) * 2 * (nv + 1));
     if (bp.failed) return pl.fail(kENoMem, "device allocation failed (ring vertices)");
     {
@@ -1074,17 +1085,16 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
                                                         keep, flagV, nxt, prv);
     }
     exclusive_scan_i32(flagV, nv + 1, sscr, st, true);
-    int nflag = 0;
-    cudaMemcpyAsync(&nflag, flagV + nv, sizeof(int), cudaMemcpyDeviceToHost, st);
-    cudaStreamSynchronize(st);
-    if (nflag > 0) {
+    // the flagged-vertex count stays on the device (flagV[nv]); rings
+    // without a flagged vertex leave k_cleanup_ring at once
+    if (nv > 0) {
       {
         ::sbc::KProbe kp_("k_flag_list", st);
         k_flag_list<<<grid_for(nv, 256), 256, 0, st>>>(nv, flagV, flist);
       }
       ::sbc::KProbe kp_("k_cleanup_ring", st);
-      k_cleanup_ring<<<grid_for(nR, 128), 128, 0, st>>>(nR, out.d_off, ringFlag, flist, nflag,
-                                                      out.d_xy, nxt, prv, keep);
+      k_cleanup_ring<<<grid_for(nR, 128), 128, 0, st>>>(nR, out.d_off, ringFlag, flist,
+                                                      flagV + nv, out.d_xy, nxt, prv, keep);
     }
     int* kpv = keep;  // exclusive prefix of the keep flags (nv+1 entries)
     exclusive_scan_i32(kpv, nv + 1, sscr, st, true);
@@ -1101,12 +1111,12 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
       ::sbc::KProbe kp_("k_compact_off", st);
       k_compact_off<<<grid_for(nR + 1, 128), 128, 0, st>>>(nR, nv, out.d_off, kpv, rpre, ooff);
     }
-    int hh[2];
-    cudaMemcpyAsync(&hh[0], rpre + nR, sizeof(int), cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(&hh[1], kpv + nv, sizeof(int), cudaMemcpyDeviceToHost, st);
-    cudaStreamSynchronize(st);
-    out.nrings = hh[0];
-    out.nverts = hh[1];
+    // the two counts land with the caller's next wait on the stream
+    // (Pipeline::finish_counts); both sit in one host word of this overlay
+    int* hh = (int*)rd.word(HostReads::kCounts + ovTag);
+    cudaMemcpyAsync(hh, rpre + nR, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(hh + 1, kpv + nv, sizeof(int), cudaMemcpyDeviceToHost, st);
+    out.counts = hh;
     out.d_off = ooff;
     out.d_xy = oxy;
   }

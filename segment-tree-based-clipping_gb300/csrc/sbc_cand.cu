@@ -624,18 +624,18 @@ int Pipeline::stage_grid_boxes() {
   if (!st) return fail(kECuda, "side stream");
   h_tstart_.assign(k + 2, 0);
   for (int t = 0; t <= k; ++t) h_tstart_[t + 1] = nb + hcc[t];
-  g_tstart = (int*)pool_.get("grid_tstart", sizeof(int) * (k + 2));
-  fbox = (float4*)pool_.get("grid_fbox", sizeof(float4) * (E + 1));
-  g_bnd = (unsigned*)pool_.get("grid_bnd", 256);
-  vfB = (float4*)pool_.get("grid_vfB", sizeof(float4) * (nb + 1));
-  vfC = (float4*)pool_.get("grid_vfC", sizeof(float4) * ((long long)clSize + k));
-  g_islong = (unsigned char*)pool_.get("grid_islong", (size_t)E + 1);
-  g_long = (int*)pool_.get("grid_long", sizeof(int) * (E + 1));
-  g_long_count = (unsigned*)pool_.get("grid_long_count", 256);
-  if (pool_.failed) return fail(kENoMem, "device allocation failed (grid)");
+  g_tstart = (int*)side_pool_.get("grid_tstart", sizeof(int) * (k + 2));
+  fbox = (float4*)side_pool_.get("grid_fbox", sizeof(float4) * (E + 1));
+  g_bnd = (unsigned*)side_pool_.get("grid_bnd", 256);
+  vfB = (float4*)side_pool_.get("grid_vfB", sizeof(float4) * (nb + 1));
+  vfC = (float4*)side_pool_.get("grid_vfC", sizeof(float4) * ((long long)clSize + k));
+  g_islong = (unsigned char*)side_pool_.get("grid_islong", (size_t)E + 1);
+  g_long = (int*)side_pool_.get("grid_long", sizeof(int) * (E + 1));
+  g_long_count = (unsigned*)side_pool_.get("grid_long_count", 256);
+  if (side_pool_.failed) return fail(kENoMem, "device allocation failed (grid)");
   auto* sum_ext = (double*)((char*)g_bnd + 64);
-  // the setup's arrays are written on the main stream
-  cudaEventRecord(ev_setup_, st_);
+  // the setup's arrays are written on the main stream (run() records
+  // ev_setup_ after the setup)
   cudaStreamWaitEvent(st, ev_setup_, 0);
   cudaMemcpyAsync(g_tstart, h_tstart_.data(), sizeof(int) * (k + 2), cudaMemcpyHostToDevice, st);
   static const unsigned init[8] = {0xffffffffu, 0xffffffffu, 0u, 0u,
@@ -656,8 +656,8 @@ int Pipeline::stage_grid_boxes() {
     ::sbc::KProbe kp_("k_vertex_f4", st);
     k_vertex_f4<<<grid_for((long long)clSize + k, 256), 256, 0, st>>>((long long)clSize + k, cP, vfC);
   }
-  cudaMemcpyAsync(h_side_rd_, g_bnd, 8 * sizeof(unsigned), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(h_side_rd_ + 8, sum_ext, sizeof(double), cudaMemcpyDeviceToHost, st);
+  side_rd_.get(g_bnd, 0, st, 8);
+  side_rd_.get(sum_ext, 4, st);
   return kOk;
 }
 
@@ -666,8 +666,8 @@ int Pipeline::stage_grid_count() {
   if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "grid bounds");
   unsigned hb[8];
   double hsum = 0.0;
-  memcpy(hb, h_side_rd_, sizeof(hb));
-  memcpy(&hsum, h_side_rd_ + 8, sizeof(double));
+  memcpy(hb, side_rd_.word(0), sizeof(hb));
+  memcpy(&hsum, side_rd_.word(4), sizeof(double));
   auto unkey = [](unsigned kk) {
     unsigned u = (kk & 0x80000000u) ? (kk & 0x7fffffffu) : ~kk;
     float f;
@@ -697,10 +697,10 @@ int Pipeline::stage_grid_count() {
   const Grid g{grid_.x0, grid_.y0, grid_.inv, grid_.gx, grid_.gy};
   g_nCells = grid_.gx * grid_.gy;
   const long long nBk = (long long)g_nCells * (k + 1);
-  g_bstart = (int*)pool_.get("grid_bstart", sizeof(int) * (nBk + 1));
-  g_fill = (int*)pool_.get("grid_fill", sizeof(int) * (nBk + 1));
-  void* sscr2 = pool_.get_zeroed("scan_scr_grid2", scan_scratch_bytes(nBk + 1), st);
-  if (pool_.failed) return fail(kENoMem, "device allocation failed (grid buckets)");
+  g_bstart = (int*)side_pool_.get("grid_bstart", sizeof(int) * (nBk + 1));
+  g_fill = (int*)side_pool_.get("grid_fill", sizeof(int) * (nBk + 1));
+  void* sscr2 = side_pool_.get_zeroed("scan_scr_grid2", scan_scratch_bytes(nBk + 1), st);
+  if (side_pool_.failed) return fail(kENoMem, "device allocation failed (grid buckets)");
   cudaMemsetAsync(g_bstart, 0, sizeof(int) * (nBk + 1), st);
   cudaMemsetAsync(g_fill, 0, sizeof(int) * (nBk + 1), st);
   unsigned* outside = (unsigned*)((char*)g_bnd + 128);
@@ -711,8 +711,8 @@ int Pipeline::stage_grid_count() {
                                                  g_long, g_long_count, cmbr, outside);
   }
   exclusive_scan_i32(g_bstart, nBk + 1, sscr2, st, true);
-  cudaMemcpyAsync(h_side_rd_, g_bstart + nBk, sizeof(int), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(h_side_rd_ + 1, outside, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  side_rd_.get(g_bstart + nBk, 0, st);
+  side_rd_.get(outside, 1, st);
   return kOk;
 }
 
@@ -721,13 +721,13 @@ int Pipeline::stage_grid_fill() {
   if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "grid count");
   int total = 0;
   unsigned n_out = 0;
-  memcpy(&total, h_side_rd_, sizeof(int));
-  memcpy(&n_out, h_side_rd_ + 1, sizeof(unsigned));
+  memcpy(&total, side_rd_.word(0), sizeof(int));
+  memcpy(&n_out, side_rd_.word(1), sizeof(unsigned));
   stat_outside_cmbr = n_out;
   if (total < 0) return fail(kEInput, "grid too large");
   g_n = total;
-  g_vals = (unsigned*)pool_.get("grid_vals", sizeof(unsigned) * ((long long)total + 1));
-  if (pool_.failed) return fail(kENoMem, "device allocation failed (grid entries)");
+  g_vals = (unsigned*)side_pool_.get("grid_vals", sizeof(unsigned) * ((long long)total + 1));
+  if (side_pool_.failed) return fail(kENoMem, "device allocation failed (grid entries)");
   const Grid g{grid_.x0, grid_.y0, grid_.inv, grid_.gx, grid_.gy};
   if (total > 0) {
     ::sbc::KProbe kp_("k_grid_scatter", st);
@@ -742,16 +742,19 @@ int Pipeline::stage_grid_fill() {
 // corner of the boxes' overlap).  It reads only the grid, so run() issues the
 // first overlay's join on the side stream, next to the tree build.
 int Pipeline::stage_join(int cType, cudaStream_t st) {
+  // on the side stream it runs on the side worker: its buffers and reads
+  BufferPool& pool = st == st2_ ? side_pool_ : pool_;
+  HostReads& rd = st == st2_ ? side_rd_ : rd_;
   join_ready_ = 0;
   const Grid g{grid_.x0, grid_.y0, grid_.inv, grid_.gx, grid_.gy};
   const int nCells = g_nCells;
-  auto* cdesc = (int4*)pool_.get("cg_desc", sizeof(int4) * ((long long)nCells + 1));
-  int* smalls = (int*)pool_.get("cg_small", sizeof(int) * ((long long)nCells + 1));
-  int* tiles = (int*)pool_.get("cg_tiles", sizeof(int) * ((long long)nCells + 1));
-  long long* work = (long long*)pool_.get("cg_work", sizeof(long long) * ((long long)nCells + 1));
-  auto* counters = (unsigned long long*)pool_.get("cg_counters", 64);
-  void* sscr = pool_.get_zeroed("scan_scr_cg", scan_scratch_bytes((long long)nCells + 1), st);
-  if (pool_.failed) return fail(kENoMem, "device allocation failed (grid items)");
+  auto* cdesc = (int4*)pool.get("cg_desc", sizeof(int4) * ((long long)nCells + 1));
+  int* smalls = (int*)pool.get("cg_small", sizeof(int) * ((long long)nCells + 1));
+  int* tiles = (int*)pool.get("cg_tiles", sizeof(int) * ((long long)nCells + 1));
+  long long* work = (long long*)pool.get("cg_work", sizeof(long long) * ((long long)nCells + 1));
+  auto* counters = (unsigned long long*)pool.get("cg_counters", 64);
+  void* sscr = pool.get_zeroed("scan_scr_cg", scan_scratch_bytes((long long)nCells + 1), st);
+  if (pool.failed) return fail(kENoMem, "device allocation failed (grid items)");
   {
     ::sbc::KProbe kp_("k_cell_items", st);
     k_cell_items<<<grid_for((long long)nCells + 1, 256), 256, 0, st>>>(nCells, g_bstart, k, cType,
@@ -760,15 +763,15 @@ int Pipeline::stage_join(int cType, cudaStream_t st) {
   exclusive_scan_i32(smalls, (long long)nCells + 1, sscr, st, true);
   exclusive_scan_i32(tiles, (long long)nCells + 1, sscr, st, true);
   exclusive_scan_i64(work, (long long)nCells + 1, sscr, st, true);
-  int nS = 0, nW = 0;
-  long long W = 0;
-  cudaMemcpyAsync(&nS, smalls + nCells, sizeof(int), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(&nW, tiles + nCells, sizeof(int), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(&W, work + nCells, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  const int* r_nS = rd.get(smalls + nCells, HostReads::kCand, st);
+  const int* r_nW = rd.get(tiles + nCells, HostReads::kCand + 1, st);
+  const long long* r_W = rd.get(work + nCells, HostReads::kCand + 2, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "grid items");
-  int* srec = (int*)pool_.get("cg_srec", sizeof(int) * ((long long)nS + 1));
-  auto* wrec = (int2*)pool_.get("cg_wrec", sizeof(int2) * ((long long)nW + 1));
-  if (pool_.failed) return fail(kENoMem, "device allocation failed (grid items)");
+  const int nS = *r_nS, nW = *r_nW;
+  const long long W = *r_W;
+  int* srec = (int*)pool.get("cg_srec", sizeof(int) * ((long long)nS + 1));
+  auto* wrec = (int2*)pool.get("cg_wrec", sizeof(int2) * ((long long)nW + 1));
+  if (pool.failed) return fail(kENoMem, "device allocation failed (grid items)");
   if (nCells > 0) {
     ::sbc::KProbe kp_("k_cell_expand", st);
     k_cell_expand<<<grid_for(nCells, 256), 256, 0, st>>>(nCells, smalls, tiles, srec, wrec);
@@ -778,8 +781,8 @@ int Pipeline::stage_join(int cType, cudaStream_t st) {
   long long npairs = 0;
   int2* pairs = nullptr;
   for (int attempt = 0; attempt < 2; ++attempt) {
-    pairs = (int2*)pool_.get("cg_pairs", sizeof(int2) * (cap + 1));
-    if (pool_.failed) return fail(kENoMem, "device allocation failed (candidate pairs)");
+    pairs = (int2*)pool.get("cg_pairs", sizeof(int2) * (cap + 1));
+    if (pool.failed) return fail(kENoMem, "device allocation failed (candidate pairs)");
     cudaMemsetAsync(counters, 0, 64, st);
     if (nS > 0) {
       ::sbc::KProbe kp_("k_grid_small", st);
@@ -796,14 +799,14 @@ int Pipeline::stage_join(int cType, cudaStream_t st) {
       k_grid_long<<<64, kGBlock, 0, st>>>(g_long, g_long_count, g_tstart, cType, g_islong, fbox,
                                           &counters[2], cap, pairs);
     }
-    unsigned long long hp = 0;
-    cudaMemcpyAsync(&hp, counters + 2, sizeof(hp), cudaMemcpyDeviceToHost, st);
+    const unsigned long long* r_hp = rd.get(counters + 2, HostReads::kCand + 3, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "candidate pairs");
-    npairs = (long long)hp;
+    npairs = (long long)*r_hp;
     if (npairs <= cap) break;
     cap = npairs + (1 << 20);
   }
   pair_cap_ = cap;
+  join_counters_ = counters;
   join_pairs_ = pairs;
   join_npairs_ = npairs;
   join_work_ = W;
@@ -821,8 +824,8 @@ int Pipeline::stage_candidates(int cType, int** rb_out, int** rc_out, int** rt_o
   join_ready_ = 0;
   const long long npairs = join_npairs_;
   const int2* pairs = join_pairs_;
-  auto* counters = (unsigned long long*)pool_.get("cg_counters", 64);
-  if (pool_.failed) return fail(kENoMem, "device allocation failed (candidate pairs)");
+  // the join's counters: [2] holds its pair count, the others start at zero
+  auto* counters = join_counters_;
   // exact stage: one record per unique hit
   long long hcap = npairs + 1;
   int* rb = (int*)pool_.get("raw_b", sizeof(int) * hcap);
@@ -835,8 +838,7 @@ int Pipeline::stage_candidates(int cType, int** rb_out, int** rc_out, int** rt_o
     k_pair_exact<<<grid_for(npairs, kExChunk), kExBlock, 0, st>>>(
         npairs, pairs, e_id, bP, cP, vfB, vfC, lr, aft, bef, logL, counters, hcap, rb, rc, rt, rkey);
   }
-  unsigned long long hc[4];
-  cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, st);
+  const unsigned long long* hc = rd_.get(counters, HostReads::kCand + 8, st, 4);
   if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "exact stage");
   if ((long long)hc[0] > hcap) return fail(kEInternal, "hit buffer overflow");
   if (hc[0] >= (1ULL << 31)) return fail(kEInput, "too many intersections");

@@ -57,6 +57,71 @@ void BufferPool::release_all() {
   bufs_.clear();
 }
 
+namespace {
+// set on the side worker's thread: Pipeline::fail records its message apart
+thread_local bool t_side_worker = false;
+}  // namespace
+
+SideWorker::~SideWorker() {
+  if (!started_) return;
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    stop_ = true;
+  }
+  cv_.notify_all();
+  th_.join();
+}
+
+bool SideWorker::post(int dev, std::function<int()> f) {
+  if (!started_) {
+    dev_ = dev;
+    try {
+      th_ = std::thread(&SideWorker::loop, this);
+    } catch (...) {
+      return false;
+    }
+    started_ = true;
+  }
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    task_ = std::move(f);
+    has_task_ = true;
+    busy_ = true;
+  }
+  cv_.notify_all();
+  return true;
+}
+
+int SideWorker::wait() {
+  std::unique_lock<std::mutex> lk(mu_);
+  cv_.wait(lk, [&] { return !busy_; });
+  return result_;
+}
+
+void SideWorker::loop() {
+  t_side_worker = true;
+  cudaSetDevice(dev_);
+  std::unique_lock<std::mutex> lk(mu_);
+  while (true) {
+    cv_.wait(lk, [&] { return has_task_ || stop_; });
+    if (stop_) return;
+    std::function<int()> f = std::move(task_);
+    has_task_ = false;
+    lk.unlock();
+    const int r = f();
+    lk.lock();
+    result_ = r;
+    busy_ = false;
+    cv_.notify_all();
+  }
+}
+
+int Pipeline::fail(int code, const std::string& msg) {
+  std::string& e = t_side_worker ? side_err_ : err_;
+  if (e.empty()) e = msg;
+  return code;
+}
+
 Pipeline::~Pipeline() {
   if (st2_) {
     cudaStreamSynchronize(st2_);
@@ -92,10 +157,10 @@ void Pipeline::join_side() {
 }
 
 void Pipeline::take_tree_stats() {
-  // no side-stream work outlives the call
+  // no work of the run outlives the call
   if (st2_) cudaStreamSynchronize(st2_);
-  if (!tree_stats_pending_) return;
   cudaStreamSynchronize(st_);
+  if (!tree_stats_pending_) return;
   unsigned long long hc[2];
   memcpy(hc, h_side_rd_ + 32, sizeof(hc));
   stat_leaf = (long long)hc[0];
@@ -104,10 +169,22 @@ void Pipeline::take_tree_stats() {
 }
 
 unsigned Pipeline::read_flags() {
-  unsigned f = 0;
-  cudaMemcpyAsync(&f, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st_);
+  const unsigned* f = rd_.get(d_flags, HostReads::kFlags, st_);
   cudaStreamSynchronize(st_);
-  return f;
+  return *f;
+}
+
+void Pipeline::finish_counts() {
+  bool pending = false;
+  for (auto& o : outs_) pending |= o.counts != nullptr;
+  if (!pending) return;
+  cudaStreamSynchronize(st_);
+  for (auto& o : outs_)
+    if (o.counts) {
+      o.nrings = o.counts[0];
+      o.nverts = o.counts[1];
+      o.counts = nullptr;
+    }
 }
 
 void Pipeline::clear_flags() { cudaMemsetAsync(d_flags, 0, sizeof(unsigned), st_); }
@@ -404,6 +481,77 @@ static int npow2_host(int n) {
   return p;
 }
 
+// ---- the vertex order from 32-bit keys.  The key of x is its offset from
+// the smallest x scaled to [0, 2^32 - 1] and rounded down: each step
+// (subtraction, multiplication by a positive constant, floor, clamp) is
+// monotone, so x < x' gives key <= key'.  Sorting (key, vertex) takes 4 radix
+// passes instead of 8; only vertices with equal keys (x values closer than
+// the x range / 2^32) can be out of full order, and those runs are put in
+// (full key, vertex) order, the order of the stable sort on full keys.
+constexpr int kFixRun = 32;  // longer runs fall back to the 64-bit sort
+
+__global__ void k_vertex_narrow(int E, const unsigned long long* __restrict__ vkey,
+                                const unsigned long long* __restrict__ mm,
+                                unsigned* __restrict__ g, unsigned* __restrict__ gid) {
+  __shared__ double s_lo, s_scale;
+  if (threadIdx.x == 0) {
+    const double lo = dkey_value(mm[0]), hi = dkey_value(mm[1]);
+    s_lo = lo;
+    s_scale = hi > lo ? 4294967295.0 / (hi - lo) : 0.0;
+  }
+  __syncthreads();
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= E) return;
+  const double t = floor((dkey_value(vkey[v]) - s_lo) * s_scale);
+  g[v] = t >= 4294967295.0 ? 0xffffffffu : (t > 0.0 ? (unsigned)t : 0u);
+  gid[v] = (unsigned)v;
+}
+
+// full keys in the narrow order, equal-key runs sorted; the run's first
+// thread handles the whole run
+__global__ void k_vertex_full(int E, const unsigned* __restrict__ g, unsigned* __restrict__ gid,
+                              const unsigned long long* __restrict__ vkey,
+                              unsigned long long* __restrict__ skey, unsigned* __restrict__ flags) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= E) return;
+  const unsigned gi = g[i];
+  const bool prev_eq = i > 0 && g[i - 1] == gi;
+  const bool next_eq = i + 1 < E && g[i + 1] == gi;
+  if (!prev_eq && !next_eq) {
+    skey[i] = vkey[gid[i]];
+    return;
+  }
+  if (prev_eq) return;
+  int m = 1;
+  while (i + m < E && g[i + m] == gi && m < kFixRun) ++m;
+  if (i + m < E && g[i + m] == gi) {
+    atomicOr(flags, (unsigned)kFlagLongRun);
+    return;
+  }
+  unsigned long long kk[kFixRun];
+  unsigned ii[kFixRun];
+  for (int t = 0; t < m; ++t) {
+    ii[t] = gid[i + t];
+    kk[t] = vkey[ii[t]];
+  }
+  for (int t = 1; t < m; ++t) {
+    const unsigned long long k0 = kk[t];
+    const unsigned i0 = ii[t];
+    int u = t - 1;
+    while (u >= 0 && (kk[u] > k0 || (kk[u] == k0 && ii[u] > i0))) {
+      kk[u + 1] = kk[u];
+      ii[u + 1] = ii[u];
+      --u;
+    }
+    kk[u + 1] = k0;
+    ii[u + 1] = i0;
+  }
+  for (int t = 0; t < m; ++t) {
+    skey[i + t] = kk[t];
+    gid[i + t] = ii[t];
+  }
+}
+
 int Pipeline::stage_elementary() {
   long long n2 = 2LL * E;
   auto* keys = (unsigned long long*)pool_.get("ele_keys", sizeof(unsigned long long) * n2);
@@ -418,12 +566,31 @@ int Pipeline::stage_elementary() {
   void* sscr = pool_.get_zeroed("scan_scr", scan_scratch_bytes(n2 + 1), st_);
   auto* vkey2 = (unsigned long long*)pool_.get("v_key2", sizeof(unsigned long long) * E);
   auto* vid2 = (unsigned*)pool_.get("v_id2", sizeof(unsigned) * E);
+  auto* vg = (unsigned*)pool_.get("v_g", sizeof(unsigned) * E);
+  auto* vg2 = (unsigned*)pool_.get("v_g2", sizeof(unsigned) * E);
+  auto* vgid = (unsigned*)pool_.get("v_gid", sizeof(unsigned) * E);
   if (pool_.failed) return fail(kENoMem, "device allocation failed (elementary)");
   // every endpoint is a vertex x value: its key lies in the setup's [min, max]
   bool by_vertex = !force_endpoint_sort;
+  bool narrow = by_vertex && !force_wide_vertex_sort;
   int count = 0, before_last = 0;
   for (;;) {
-  if (by_vertex) {
+  if (by_vertex && narrow) {
+    // 32-bit keys (4 passes), then the full keys and the equal-key runs;
+    // vkey2 holds the sorted full keys, vgid the vertices
+    {
+      ::sbc::KProbe kp_("k_vertex_narrow", st_, 16.0 * E);
+      k_vertex_narrow<<<grid_for(E, 256), 256, 0, st_>>>(E, v_key, d_minmax, vg, vgid);
+    }
+    radix_sort_u32(vg, vgid, vg2, vid2, E, 32, rscr, st_);
+    {
+      ::sbc::KProbe kp_("k_vertex_full", st_, 24.0 * E);
+      k_vertex_full<<<grid_for(E, 256), 256, 0, st_>>>(E, vg, vgid, v_key, vkey2, d_flags);
+    }
+    ::sbc::KProbe kp_("k_ele_expand", st_, 12.0 * E + 9.0 * E + 24.0 * E);
+    k_ele_expand<<<grid_for(E, 256), 256, 0, st_>>>(vkey2, vgid, e_flip, cc, nb, k, E, keys, sidx,
+                                                    d_flags);
+  } else if (by_vertex) {
     // sort the E vertex keys, then expand to the 2E endpoints
     radix_sort_u64(v_key, v_id, vkey2, vid2, E, rscr, st_);
     ::sbc::KProbe kp_("k_ele_expand", st_, 12.0 * E + 9.0 * E + 24.0 * E);
@@ -452,18 +619,25 @@ int Pipeline::stage_elementary() {
     k_ele_flags<<<grid_for(n2, 256), 256, 0, st_>>>(sidx, e_s, e_e, vl, vloc, E, flag, val);
   }
   exclusive_scan_i32(flag, n2 + 1, sscr, st_, true);
-  unsigned fl = 0;
-  unsigned long long hm[2] = {0, 0};
-  cudaMemcpyAsync(&count, flag + n2, sizeof(int), cudaMemcpyDeviceToHost, st_);
-  cudaMemcpyAsync(&before_last, flag + n2 - 1, sizeof(int), cudaMemcpyDeviceToHost, st_);
-  cudaMemcpyAsync(&fl, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st_);
-  cudaMemcpyAsync(hm, d_minmax, sizeof(hm), cudaMemcpyDeviceToHost, st_);
+  const int* r_cnt = rd_.get(flag + n2 - 1, HostReads::kFront, st_, 2);  // before_last, count
+  const unsigned* r_fl = rd_.get(d_flags, HostReads::kFront + 1, st_);
+  const unsigned long long* r_mm = rd_.get(d_minmax, HostReads::kFront + 2, st_, 2);
   cudaStreamSynchronize(st_);
+  before_last = r_cnt[0];
+  count = r_cnt[1];
+  const unsigned fl = *r_fl;
+  const unsigned long long hm[2] = {r_mm[0], r_mm[1]};
   if (fl & kFlagUndef) return fail(kEInput, "non-finite vertex coordinate");
   key_lo = hm[0];
   key_hi = hm[1];
   minI = key_to_double(hm[0]);
   maxI = key_to_double(hm[1]);
+  if (narrow && (fl & kFlagLongRun)) {
+    // nearly equal x values in a long run: the 64-bit vertex sort
+    narrow = false;
+    clear_flags();
+    continue;
+  }
   if (by_vertex && (fl & kFlagSharedX)) {
     // a shared x value: the endpoints' own stable sort decides their order
     by_vertex = false;
@@ -472,7 +646,7 @@ int Pipeline::stage_elementary() {
   }
   break;
   }
-  stat_vertex_sort = by_vertex ? 1 : 0;
+  stat_vertex_sort = by_vertex ? (narrow ? 2 : 1) : 0;
   if (count < 1) return fail(kEUndef, "no elementary interval (all endpoints equal)");
   int round = npow2_host(count) + 1;
   epc = round;
@@ -630,32 +804,50 @@ __global__ void k_run_bounds(long long n2, const unsigned long long* __restrict_
   if (last) re[r] = (int)i;
 }
 
-// per endpoint: the positions [lo, hi) of ea holding its value and its run.
-// Every endpoint of a run has the same value, range and search path, so the
-// run's first endpoint runs findBoarder's search (border_by_position) once
-// and stores it per run; k_edge_tree reads it through the run index.
+// the positions [lo, hi) of ea holding the value of run r (sorted endpoint
+// keys; run r spans [rs[r], re[r]])
+__device__ __forceinline__ int2 run_range(int r, unsigned long long key,
+                                          const int* __restrict__ rs, const int* __restrict__ re,
+                                          const int* __restrict__ F, unsigned long long kl,
+                                          int epc) {
+  int lo = F[rs[r]], hi = F[re[r] + 1];
+  if (key == kl) hi = epc;             // and the padding
+  else if (key > kl) lo = hi = epc;    // above every entry, padding included
+  return make_int2(lo, hi);
+}
+
+// per endpoint: its value's positions [lo, hi) in ea and its run
 __global__ void k_endpoint_range(long long n2, const unsigned long long* __restrict__ keys,
                                  const unsigned* __restrict__ sidx, const int* __restrict__ rpre,
                                  const int* __restrict__ rs, const int* __restrict__ re,
-                                 const int* __restrict__ F, int count, int epc, int z,
-                                 const double* __restrict__ ea, const double* __restrict__ es,
-                                 const double* __restrict__ ee, int2* __restrict__ erange,
-                                 int* __restrict__ erun, int* __restrict__ rbord) {
+                                 const int* __restrict__ F, int count, int epc,
+                                 const double* __restrict__ ea, int2* __restrict__ erange,
+                                 int* __restrict__ erun) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n2) return;
   const bool first = i == 0 || keys[i] != keys[i - 1];
   const int r = rpre[i] + (first ? 0 : -1);
-  const unsigned long long kl = dkey(ea[count - 1]);
-  int lo = F[rs[r]], hi = F[re[r] + 1];
-  if (keys[i] == kl) hi = epc;             // and the padding
-  else if (keys[i] > kl) lo = hi = epc;    // above every entry, padding included
   const unsigned x = sidx[i];
-  erange[x] = make_int2(lo, hi);
+  erange[x] = run_range(r, keys[i], rs, re, F, dkey(ea[count - 1]), epc);
   erun[x] = r;
-  if (first) {
-    const double q = (x & 1u) ? ee[x >> 1] : es[x >> 1];
-    rbord[r] = border_by_position(epc, z, lo, hi, q);
-  }
+}
+
+// per run of equal endpoint values: findBoarder's search (followed on
+// positions, border_by_position), the same for every endpoint of the run;
+// one thread per run (runs = rpre[n2])
+__global__ void k_run_border(long long n2, const unsigned long long* __restrict__ keys,
+                             const unsigned* __restrict__ sidx, const int* __restrict__ rpre,
+                             const int* __restrict__ rs, const int* __restrict__ re,
+                             const int* __restrict__ F, int count, int epc, int z,
+                             const double* __restrict__ ea, const double* __restrict__ es,
+                             const double* __restrict__ ee, int* __restrict__ rbord) {
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rpre[n2]) return;
+  const int i = rs[r];
+  const unsigned x = sidx[i];
+  const double q = (x & 1u) ? ee[x >> 1] : es[x >> 1];
+  const int2 lh = run_range((int)r, keys[i], rs, re, F, dkey(ea[count - 1]), epc);
+  rbord[r] = border_by_position(epc, z, lh.x, lh.y, q);
 }
 
 __global__ void k_edge_tree(int E, const int2* __restrict__ erange, const int* __restrict__ erun,
@@ -760,9 +952,11 @@ int Pipeline::stage_endlists() {
     ::sbc::KProbe kp_("k_ea_sorted", st_, 8.0 * epc);
     k_ea_sorted<<<grid_for(epc, 256), 256, 0, st_>>>(epc, ea, d_flags);
   }
-  int z = 0;
-  cudaMemcpyAsync(&z, zc, sizeof(int), cudaMemcpyDeviceToHost, st_);
-  const unsigned fl = read_flags();
+  const int* r_z = rd_.get(zc, HostReads::kFront, st_);
+  const unsigned* r_fl = rd_.get(d_flags, HostReads::kFront + 1, st_);
+  cudaStreamSynchronize(st_);
+  const int z = *r_z;
+  const unsigned fl = *r_fl;
   if (fl & kFlagUndef) return fail(kEUndef, "border keys not monotone (realToInt)");
   z_garbage = z;
   lr_ready = false;
@@ -793,8 +987,12 @@ int Pipeline::stage_endlists() {
     {
       ::sbc::KProbe kp_("k_endpoint_range", st_, 36.0 * n2);
       k_endpoint_range<<<grid_for(n2, 256), 256, 0, st_>>>(n2, keys, sidx, rpre, rs, re, F,
-                                                           ele_count, epc, z, ea, e_s, e_e, erange,
-                                                           erun, rbord);
+                                                           ele_count, epc, ea, erange, erun);
+    }
+    {
+      ::sbc::KProbe kp_("k_run_border", st_);
+      k_run_border<<<grid_for(n2, 256), 256, 0, st_>>>(n2, keys, sidx, rpre, rs, re, F, ele_count,
+                                                       epc, z, ea, e_s, e_e, rbord);
     }
     {
       // es, ee and two endpoint ranges in; aft, bef, leaf range out

@@ -42,6 +42,7 @@ enum DevFlag : unsigned {
   kFlagSpin = 8u,           // a bounded wait gave up
   kFlagUnsorted = 16u,      // the elementary array is not in order
   kFlagSharedX = 32u,       // two vertices share an x value (endpoint order needs the full sort)
+  kFlagLongRun = 64u,       // a run of equal 32-bit vertex keys too long to fix up in place
 };
 
 // ---------------------------------------------------------------- FP64 geometry
@@ -122,6 +123,11 @@ __device__ __forceinline__ int alpha_to_int(double a) {
 __device__ __forceinline__ unsigned long long dkey(double x) {
   unsigned long long u = (unsigned long long)__double_as_longlong(x == 0.0 ? 0.0 : x);
   return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+// the value of an order key
+__device__ __forceinline__ double dkey_value(unsigned long long k) {
+  const unsigned long long u = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)u);
 }
 
 // ---------------------------------------------------------------- block reductions
@@ -209,6 +215,9 @@ void exclusive_scan_i64(long long* d, long long n, void* scratch, cudaStream_t s
                         bool state_zero = false);
 // true (and cleared) if a scan's bounded look-back wait gave up since the last call
 bool scan_error_take();
+// the device address of the scans' error word (for a read queued on a
+// stream); nullptr if it cannot be had
+unsigned* scan_error_word();
 
 // Stable LSD radix sort of (key, value) pairs, 8-bit digits, only the digit
 // positions that vary are sorted.  keys/vals are sorted in place; tmp buffers

@@ -390,14 +390,15 @@ __global__ void k_nbr_apply(const int* __restrict__ win, int n, const int* __res
 }
 
 // ---------------------------------------------------------------- A14 labels
-__global__ void k_labels(int nB, int nQ, const double* __restrict__ ixB,
-                         const double* __restrict__ ixC, const int* __restrict__ alB,
-                         const int* __restrict__ nbB, int* __restrict__ labB,
-                         int* __restrict__ cWin, unsigned* __restrict__ flags) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nB) return;
+// initial label of intersection slot i (alpha != -100) of the merged base
+// list.  The orientation of (prev, current, next) does not depend on the
+// overlay neighbour: it is computed once, when first needed.
+__device__ __forceinline__ void label_slot(int i, int nB, int nQ, const double* __restrict__ ixB,
+                                           const double* __restrict__ ixC,
+                                           const int* __restrict__ alB,
+                                           const int* __restrict__ nbB, int* __restrict__ labB,
+                                           int* __restrict__ cWin, unsigned* __restrict__ flags) {
   labB[i] = 0;
-  if (alB[i] == -100) return;
   double cx = ixB[2 * i], cy = ixB[2 * i + 1];
   int tm = (i - 1 == -1) ? nB - 1 : i - 1;  // getCircularId
   double pmx = ixB[2 * tm], pmy = ixB[2 * tm + 1];
@@ -407,6 +408,8 @@ __global__ void k_labels(int nB, int nQ, const double* __restrict__ ixB,
   int pPN = alB[tp] != -100 ? nbB[tp] - 1 : -100;
   int nId = nbB[i] - 1;
   int qt[2];
+  double s3 = 0.0;
+  bool have_s3 = false;
   for (int side = 0; side < 2; ++side) {
     int q = side == 0 ? nId - 1 : nId + 1;
     if (q == nQ) q = 0;
@@ -422,7 +425,10 @@ __global__ void k_labels(int nB, int nQ, const double* __restrict__ ixB,
     else {
       double s1 = area3(qx, qy, pmx, pmy, cx, cy);
       double s2 = area3(qx, qy, cx, cy, ppx, ppy);
-      double s3 = area3(pmx, pmy, cx, cy, ppx, ppy);
+      if (!have_s3) {
+        s3 = area3(pmx, pmy, cx, cy, ppx, ppy);
+        have_s3 = true;
+      }
       if (s3 > 0) r = (s1 > 0 && s2 > 0) ? 0 : 1;
       else r = (s1 < 0 && s2 < 0) ? 1 : 0;
     }
@@ -443,6 +449,56 @@ __global__ void k_labels(int nB, int nQ, const double* __restrict__ ixB,
     return;
   }
   atomicMax(&cWin[nId], i);
+}
+
+// Only intersection slots (alpha != -100) have work, about a third of the
+// slots and spread over every warp.  The orientation tests are FP64, and an
+// FP64 instruction costs its issue slots whatever its active lanes: each
+// block gathers its tile's intersection slots into shared memory and works
+// through them with full warps.
+constexpr int kLabThreads = 256, kLabItems = 8;
+__global__ void __launch_bounds__(kLabThreads)
+    k_labels(int nB, int nQ, const double* __restrict__ ixB, const double* __restrict__ ixC,
+             const int* __restrict__ alB, const int* __restrict__ nbB, int* __restrict__ labB,
+             int* __restrict__ cWin, unsigned* __restrict__ flags) {
+  __shared__ int list[kLabThreads * kLabItems];
+  __shared__ int wsum[kLabThreads / 32];
+  __shared__ int total;
+  const long long base = (long long)blockIdx.x * (kLabThreads * kLabItems);
+  unsigned act = 0;
+  for (int j = 0; j < kLabItems; ++j) {
+    const long long i = base + (long long)j * kLabThreads + threadIdx.x;
+    if (i < nB) {
+      if (alB[i] != -100) act |= 1u << j;
+      else labB[i] = 0;
+    }
+  }
+  const int cnt = __popc(act);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int inc = cnt;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) wsum[w] = inc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int k2 = 0; k2 < kLabThreads / 32; ++k2) {
+      const int t = wsum[k2];
+      wsum[k2] = acc;
+      acc += t;
+    }
+    total = acc;
+  }
+  __syncthreads();
+  int pos = wsum[w] + inc - cnt;
+  for (int j = 0; j < kLabItems; ++j)
+    if ((act >> j) & 1u) list[pos++] = (int)(base + (long long)j * kLabThreads + threadIdx.x);
+  __syncthreads();
+  const int n = total;
+  for (int t = threadIdx.x; t < n; t += kLabThreads)
+    label_slot(list[t], nB, nQ, ixB, ixC, alB, nbB, labB, cWin, flags);
 }
 
 __global__ void k_labels_c(int nQ, const int* __restrict__ cWin, const int* __restrict__ labB,
@@ -523,8 +579,9 @@ int Pipeline::stage_records(int cType, const int* rb, const int* rc, const int* 
     }
     cudaMemsetAsync(keep + R, 0, sizeof(int), st);
     exclusive_scan_i32(keep, R + 1, sscr2, st, true);
-    cudaMemcpyAsync(&K, keep + R, sizeof(int), cudaMemcpyDeviceToHost, st);
+    const int* r_K = rd_.get(keep + R, HostReads::kMid, st);
     cudaStreamSynchronize(st);
+    K = *r_K;
   }
   out.unique = K;
   int* ub = (int*)pool_.get("u_b", sizeof(int) * (K + 1));
@@ -585,10 +642,10 @@ int Pipeline::stage_records(int cType, const int* rb, const int* rc, const int* 
   exclusive_scan_i32(bND, bSize + 1, sscr3, st, true);
   exclusive_scan_i32(cAll, cSize + 1, sscr3, st, true);
   exclusive_scan_i32(cND, cSize + 1, sscr3, st, true);
-  int hb = 0, hc = 0;
-  cudaMemcpyAsync(&hb, bND + bSize, sizeof(int), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(&hc, cND + cSize, sizeof(int), cudaMemcpyDeviceToHost, st);
+  const int* r_hb = rd_.get(bND + bSize, HostReads::kMid + 1, st);
+  const int* r_hc = rd_.get(cND + cSize, HostReads::kMid + 2, st);
   cudaStreamSynchronize(st);
+  const int hb = *r_hb, hc = *r_hc;
   const int nB = bSize + hb, nQ = cSize + hc;
   out.slots_b = nB;
   out.slots_c = nQ;
@@ -715,7 +772,8 @@ int Pipeline::stage_records(int cType, const int* rb, const int* rc, const int* 
   cudaMemsetAsync(winC, 0xff, sizeof(int) * nQ, st);
   {
     ::sbc::KProbe kp_("k_labels", st);
-    k_labels<<<grid_for(nB, 256), 256, 0, st>>>(nB, nQ, ixB, ixC, alB, nbB, labB, winC, d_flags);
+    k_labels<<<grid_for(nB, kLabThreads * kLabItems), kLabThreads, 0, st>>>(
+        nB, nQ, ixB, ixC, alB, nbB, labB, winC, d_flags);
   }
   {
     ::sbc::KProbe kp_("k_labels_c", st);

@@ -5,7 +5,11 @@
 #pragma once
 
 #include <array>
+#include <condition_variable>
+#include <functional>
 #include <map>
+#include <mutex>
+#include <thread>
 #include <string>
 #include <memory>
 #include <vector>
@@ -45,6 +49,82 @@ struct OverlayOut {
   // diagnostics
   long long raw_hits = 0, tests = 0, unique = 0, slots_b = 0, slots_c = 0, work = 0, survivors = 0;
   int slow_path = 0;
+  // nrings and nverts still on their way to this host word pair (set by
+  // the back end, filled by Pipeline::finish_counts)
+  const int* counts = nullptr;
+};
+
+// Small host reads of device values.  A copy into pageable memory waits for
+// the stream by itself, so every pageable read is a round trip; these copies
+// go to pinned memory instead and all land at the stream's next
+// synchronisation: a stage pays one round trip for all its reads.  The area
+// is kWords 8-byte words; each stage reads through its own words
+// (HostReads::k*), valid after the synchronisation that follows the copy.
+class HostReads {
+ public:
+  static constexpr int kWords = 256;
+  static constexpr int kFlags = 0;       // read_flags
+  static constexpr int kFront = 8;       // elementary and end-list stages
+  static constexpr int kCand = 24;       // candidate and exact stages
+  static constexpr int kMid = 40;        // record and merge stages
+  static constexpr int kBack = 64;       // back end
+  static constexpr int kCounts = 128;    // per overlay (1..9): ring and vertex counts
+  HostReads() = default;
+  HostReads(const HostReads&) = delete;
+  HostReads& operator=(const HostReads&) = delete;
+  ~HostReads() {
+    if (pinned_) cudaFreeHost(p_);
+  }
+  // queue a copy of n values at word w; returns where they will be
+  template <typename T>
+  T* get(const T* d, int w, cudaStream_t st, int n = 1) {
+    T* h = (T*)word(w);
+    cudaMemcpyAsync(h, d, sizeof(T) * n, cudaMemcpyDeviceToHost, st);
+    return h;
+  }
+  void* word(int w) {
+    if (!p_) {
+      if (cudaMallocHost((void**)&p_, 8 * kWords) == cudaSuccess) {
+        pinned_ = true;
+      } else {
+        cudaGetLastError();
+        fallback_.assign(8 * kWords, 0);  // pageable: correct, one round trip per read
+        p_ = fallback_.data();
+      }
+    }
+    return p_ + 8 * w;
+  }
+
+ private:
+  unsigned char* p_ = nullptr;
+  bool pinned_ = false;
+  std::vector<unsigned char> fallback_;
+};
+
+// One host thread that issues a pipeline's side-stream work (the grid stage
+// and the first overlay's box join), so the host reads of that work wait for
+// the side stream only, and the main thread's reads for the main stream only:
+// neither stream idles behind the other's round trips.
+class SideWorker {
+ public:
+  SideWorker() = default;
+  SideWorker(const SideWorker&) = delete;
+  SideWorker& operator=(const SideWorker&) = delete;
+  ~SideWorker();
+  // run f on the worker thread (started on first use, current device dev);
+  // false if no thread could be started (the caller runs f itself)
+  bool post(int dev, std::function<int()> f);
+  // the posted task's result
+  int wait();
+
+ private:
+  void loop();
+  std::thread th_;
+  std::mutex mu_;
+  std::condition_variable cv_;
+  std::function<int()> task_;
+  bool has_task_ = false, busy_ = false, stop_ = false, started_ = false;
+  int result_ = 0, dev_ = 0;
 };
 
 struct Timing {
@@ -87,7 +167,9 @@ class Pipeline {
   unsigned* v_id = nullptr;            // vertex index (the sort's payload)
   unsigned char* e_flip = nullptr;     // edge runs right to left (its first vertex is its end)
   int force_endpoint_sort = 0;         // test hook: sort the 2E endpoints, not the E vertices
-  int stat_vertex_sort = 0;            // the last run's endpoint order came from the vertex sort
+  int force_wide_vertex_sort = 0;      // test hook: the vertex sort on 64-bit keys only
+  int stat_vertex_sort = 0;            // the last run's endpoint order: 0 endpoint sort, 1 vertex
+                                       // sort on 64-bit keys, 2 on 32-bit keys
   double minI = 0, maxI = 0;
   unsigned long long key_lo = 0, key_hi = 0;  // order keys of minI and maxI
   unsigned long long* d_minmax = nullptr;     // device copy of (key_lo, key_hi) from the setup
@@ -124,6 +206,7 @@ class Pipeline {
   int* g_fill = nullptr;               // per-bucket fill counters of the grid scatter
   int join_ready_ = 0;                 // overlay whose box join below is ready (0: none)
   const int2* join_pairs_ = nullptr;
+  unsigned long long* join_counters_ = nullptr;
   long long join_npairs_ = 0, join_work_ = 0;
   // intermediate arrays of the last overlay processed (device, diagnostics)
   int *dbg_ub = nullptr, *dbg_uc = nullptr, *dbg_ut = nullptr;
@@ -165,13 +248,15 @@ class Pipeline {
   int run_from_hits(const double* d_bxy, int nb, const double* d_cxy, int nc, const int* rb,
                     const int* rc, const int* rt, const unsigned long long* rkey, long long nhits);
 
-  int fail(int code, const std::string& msg) {
-    if (err_.empty()) err_ = msg;
-    return code;
-  }
+  // records the first error message (the side worker's own, on its thread)
+  int fail(int code, const std::string& msg);
   void clear_error() { err_.clear(); }
   unsigned read_flags();
   void clear_flags();
+  HostReads& reads() { return rd_; }
+  // ring and vertex counts of the overlays whose back end queued them
+  // (OverlayOut::counts): waits for the main stream once if any is pending
+  void finish_counts();
 
  private:
   int dev_;
@@ -184,6 +269,13 @@ class Pipeline {
   bool tree_stats_pending_ = false;
   std::vector<int> h_tstart_;
   BufferPool pool_;
+  HostReads rd_;
+  // the side worker's buffers, host reads and first error (its stages run
+  // concurrently with the main thread's)
+  BufferPool side_pool_;
+  HostReads side_rd_;
+  std::string side_err_;
+  SideWorker side_;
   std::vector<OverlayOut> outs_;
   std::string err_;
 };

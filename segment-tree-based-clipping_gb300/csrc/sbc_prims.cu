@@ -368,6 +368,24 @@ size_t scan_scratch_bytes(long long n) {
   return (tot > lb ? tot : lb) + 256;
 }
 
+unsigned* scan_error_word() {
+  static std::mutex mu;
+  static unsigned* addr[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_scan_error) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    addr[dev] = (unsigned*)p;
+  }
+  return addr[dev];
+}
+
 bool scan_error_take() {
   unsigned h = 0;
   cudaMemcpyFromSymbol(&h, g_scan_error, sizeof(h));

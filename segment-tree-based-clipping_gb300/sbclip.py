@@ -21,6 +21,7 @@ SBC_FLAG_TIMING = 1
 SBC_FLAG_SERIAL_BACKEND = 2
 SBC_FLAG_UNION = 4
 SBC_FLAG_ENDPOINT_SORT = 8
+SBC_FLAG_WIDE_VERTEX_SORT = 16
 BATCH_SHAPE_KEYS = ("front", "cand", "back", "backward", "split")
 
 STATS = ["edges", "elementary_points", "tree_size", "cover_entries", "leaf_end_entries",
@@ -237,15 +238,19 @@ class Clipper:
     """One library context (one CUDA stream, grow-only device buffers)."""
 
     def __init__(self, device: int = 0, timing: bool = False, serial_backend: bool = False,
-                 union: bool = False, endpoint_sort: bool = False):
+                 union: bool = False, endpoint_sort: bool = False,
+                 wide_vertex_sort: bool = False):
         """union: every clipping call returns base ∪ overlay instead of base ∩ overlay.
         endpoint_sort: the elementary intervals from the sort of all edge
-        endpoints rather than of the vertices (a test hook; same results)."""
+        endpoints rather than of the vertices (a test hook; same results).
+        wide_vertex_sort: the vertex sort on 64-bit keys rather than 32-bit
+        keys with the equal-key runs fixed up (a test hook; same results)."""
         self._L = load_library()
         opt = _Options(device, (SBC_FLAG_TIMING if timing else 0) |
                        (SBC_FLAG_SERIAL_BACKEND if serial_backend else 0) |
                        (SBC_FLAG_UNION if union else 0) |
-                       (SBC_FLAG_ENDPOINT_SORT if endpoint_sort else 0))
+                       (SBC_FLAG_ENDPOINT_SORT if endpoint_sort else 0) |
+                       (SBC_FLAG_WIDE_VERTEX_SORT if wide_vertex_sort else 0))
         h = ctypes.c_void_p()
         rc = self._L.sbc_create(ctypes.byref(opt), ctypes.byref(h))
         if rc != 0:

@@ -219,13 +219,23 @@ def test_kernels_were_launched(clipper):
     assert sbclip.kernel_launches() > before + 20
 
 
+def _same_tree_arrays(a_clip, b_clip, tag):
+    for name in ("elementary", "leaf_after", "leaf_before", "leaf_range"):
+        a, w = a_clip.debug_array(name), b_clip.debug_array(name)
+        assert np.array_equal(a.view(np.int64) if a.dtype == np.float64 else a,
+                              w.view(np.int64) if w.dtype == np.float64 else w), (tag, name)
+
+
 def test_vertex_sort_and_endpoint_sort_agree(clipper, small_cases):
     """The elementary intervals come from a sort of the E vertex keys,
     expanded to the 2E endpoints; inputs with a shared x value fall back to
-    sorting the endpoints themselves.  Both routes give the same tree arrays
-    and rings as the oracle."""
+    sorting the endpoints themselves.  The vertex sort runs on 32-bit keys
+    with equal-key runs fixed up (stat 2), or on the 64-bit keys (stat 1, the
+    wide_vertex_sort hook).  Every route gives the same tree arrays and
+    rings."""
     import sbclip
     ref = sbclip.Clipper(0, endpoint_sort=True)
+    wide = sbclip.Clipper(0, wide_vertex_sort=True)
     try:
         kinds = set()
         cases = [(c.kind, c.base, c.overlays) for c in small_cases]
@@ -237,13 +247,45 @@ def test_vertex_sort_and_endpoint_sort_agree(clipper, small_cases):
             kinds.add(vs)
             want = ref.clip(b, ovs)
             assert ref.stats()["vertex_sort"] == 0
-            for name in ("elementary", "leaf_after", "leaf_before", "leaf_range"):
-                a, w = clipper.debug_array(name), ref.debug_array(name)
-                assert np.array_equal(a.view(np.int64) if a.dtype == np.float64 else a,
-                                      w.view(np.int64) if w.dtype == np.float64 else w), (kind, name)
-            for x, y in zip(got, want):
-                assert rings_equal(x, y), kind
-        assert kinds == {0, 1}  # both routes ran
+            _same_tree_arrays(clipper, ref, kind)
+            got_w = wide.clip(b, ovs)
+            assert wide.stats()["vertex_sort"] in (0, 1) and (vs == 0) == (
+                wide.stats()["vertex_sort"] == 0), kind
+            _same_tree_arrays(wide, ref, kind)
+            for x, y, z in zip(got, want, got_w):
+                assert rings_equal(x, y) and rings_equal(z, y), kind
+        assert kinds == {0, 2}  # both routes ran
+    finally:
+        ref.close()
+        wide.close()
+
+
+def _near_vertical_chain(n: int):
+    """A simple polygon whose right side is a chain of n vertices going up
+    with x = 1 - i * 2^-50: distinct x values far closer together than the
+    x range / 2^32, and falling with the vertex index, so one 32-bit key run
+    holds them in reverse order."""
+    d = 2.0 ** -50
+    chain = [(1.0 - i * d, -0.9 + 1.8 * i / (n - 1)) for i in range(n)]
+    pts = [(-1.0, -1.0), (0.97, -1.03)] + chain + [(0.96, 1.04), (-1.02, 0.99)]
+    return np.array(pts, dtype=np.float64)
+
+
+@pytest.mark.parametrize("n,stat", [(6, 2), (33, 2), (48, 1)])
+def test_vertex_key_runs_are_fixed_up(clipper, n, stat):
+    """Equal 32-bit vertex keys: runs of up to 32 vertices are put in full-key
+    order in place (stat 2); a longer run sends the stage back to the 64-bit
+    vertex sort (stat 1).  Every stage and the rings equal the oracle's and
+    the endpoint sort's."""
+    import sbclip
+    b = _near_vertical_chain(n)
+    c = gen.star(64, 71, centre=(0.95, 0.0), R=0.3)
+    _compare_all(clipper, b, c)
+    assert clipper.stats()["vertex_sort"] == stat
+    ref = sbclip.Clipper(0, endpoint_sort=True)
+    try:
+        ref.clip(b, [c])
+        _same_tree_arrays(clipper, ref, n)
     finally:
         ref.close()
 
