@@ -46,71 +46,87 @@ struct BkScalars {
 };
 
 // ---------------------------------------------------------------- list bridge (A15)
-__global__ void k_mark_src(int n, const int* __restrict__ ndPS, unsigned char* __restrict__ src) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  src[k + ndPS[k]] = 1;
-}
+// The per-side steps below run for P (the base list) and Q (the overlay
+// list) in one launch each: blockIdx.y picks the side.
 
-// copyToLinkedList matches list vertices by coordinates: an inserted entry
-// equal to the next source vertex would be taken for it (anomaly)
-__global__ void k_bridge_check(int nSrc, int nSlots, const int* __restrict__ ndPS,
-                               const double* __restrict__ ix, const double* __restrict__ poly,
-                               int polyOff, BkScalars* sc) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nSrc) return;
-  int a = k + ndPS[k] + 1;
-  int b = (k + 1 < nSrc) ? (k + 1 + ndPS[k + 1]) : nSlots;
-  int nx = (k + 1 < nSrc) ? k + 1 : 0;
-  double vx = poly[2 * (polyOff + nx)], vy = poly[2 * (polyOff + nx) + 1];
-  for (int i = a; i < b; ++i)
-    if (ix[2 * i] == vx && ix[2 * i + 1] == vy) atomicOr(&sc->anomaly, 1u);
+// source slots of the merged list, and copyToLinkedList's bridge check: it
+// matches list vertices by coordinates, so an inserted entry equal to the
+// next source vertex would be taken for it (anomaly).  Coordinates compare
+// through their order keys (integer compares; ±0 equal as for the doubles).
+struct SrcSide {
+  int nSrc, nSlots, polyOff;
+  const int* ndPS;
+  const double* ix;
+  const double* poly;
+  unsigned char* src;
+};
+__global__ void k_mark_bridge(SrcSide s0, SrcSide s1, BkScalars* sc) {
+  const SrcSide& a = blockIdx.y ? s1 : s0;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.nSrc) return;
+  const int p = k + a.ndPS[k];
+  a.src[p] = 1;
+  const int b = (k + 1 < a.nSrc) ? (k + 1 + a.ndPS[k + 1]) : a.nSlots;
+  const int nx = (k + 1 < a.nSrc) ? k + 1 : 0;
+  const long long vx = okey(a.poly[2 * (a.polyOff + nx)]);
+  const long long vy = okey(a.poly[2 * (a.polyOff + nx) + 1]);
+  for (int i = p + 1; i < b; ++i)
+    if (okey(a.ix[2 * i]) == vx && okey(a.ix[2 * i + 1]) == vy) atomicOr(&sc->anomaly, 1u);
 }
 
 // P: intersection flag, label; Q: flag, label, neighbour (copyToLinkedList)
-__global__ void k_init_P(int nB, const unsigned char* __restrict__ src, const int* __restrict__ alB,
-                         const int* __restrict__ labB, unsigned char* __restrict__ isect,
-                         int* __restrict__ lab) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nB) return;
-  isect[i] = (!src[i] || alB[i] != -100) ? 1 : 0;
-  lab[i] = labB[i];
-}
-
-__global__ void k_init_Q(int nQ, int nB, const unsigned char* __restrict__ src,
-                         const int* __restrict__ nbC, const int* __restrict__ labC,
-                         unsigned char* __restrict__ isect, int* __restrict__ lab,
-                         int* __restrict__ nbQ, int* __restrict__ winP, BkScalars* sc) {
-  int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nQ) return;
-  bool is = !src[q] || nbC[q] != -100;
-  isect[q] = is ? 1 : 0;
-  lab[q] = labC[q];
-  nbQ[q] = -1;
+struct InitArgs {
+  int nB, nQ;
+  const unsigned char *srcP, *srcQ;
+  const int *alB, *labB, *nbC, *labC;
+  unsigned char *isP, *isQ;
+  int *labP, *labQ, *nbQ, *winP;
+};
+__global__ void k_init_PQ(InitArgs A, BkScalars* sc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (blockIdx.y == 0) {
+    if (i >= A.nB) return;
+    A.isP[i] = (!A.srcP[i] || A.alB[i] != -100) ? 1 : 0;
+    A.labP[i] = A.labB[i];
+    return;
+  }
+  if (i >= A.nQ) return;
+  const bool is = !A.srcQ[i] || A.nbC[i] != -100;
+  A.isQ[i] = is ? 1 : 0;
+  A.labQ[i] = A.labC[i];
+  A.nbQ[i] = -1;
   if (is) {
-    int t = nbC[q] - 1;
-    if (t < 0 || t >= nB) {
+    const int t = A.nbC[i] - 1;
+    if (t < 0 || t >= A.nB) {
       atomicOr(&sc->anomaly, 2u);
       return;
     }
-    nbQ[q] = t;
-    atomicMax(&winP[t], q);  // the last C vertex linked to t wins
+    A.nbQ[i] = t;
+    atomicMax(&A.winP[t], i);  // the last C vertex linked to t wins
   }
 }
 
-// per-side statistics: crossing count, first non-intersection slot, ON_ON
-__global__ void k_side_stats(int n, const unsigned char* __restrict__ isect,
-                             const int* __restrict__ lab, int side, int checkChains,
-                             BkScalars* sc) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+struct ListSide {
+  int n;
+  const unsigned char* isect;
+  const int* lab;
+};
+
+// per-side statistics: crossing count, first non-intersection slot, ON_ON;
+// chains of ON labels are an anomaly on P only
+__global__ void k_side_stats(ListSide s0, ListSide s1, BkScalars* sc) {
+  const ListSide& a = blockIdx.y ? s1 : s0;
+  const int side = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   int cross = 0, notonon = 0;
   unsigned free_i = 0xffffffffu;  // first slot without an intersection, per warp first
-  if (i < n) {
-    int l = lab[i];
-    if (isect[i] && l == L_CROSSING) cross = 1;
+  if (i < a.n) {
+    const int l = a.lab[i];
+    const bool is = a.isect[i] != 0;
+    if (is && l == L_CROSSING) cross = 1;
     if (l != L_ON_ON) notonon = 1;
-    if (!isect[i]) free_i = (unsigned)i;
-    if (checkChains && isect[i] && (l == L_LEFT_ON || l == L_RIGHT_ON)) atomicOr(&sc->anomaly, 4u);
+    if (!is) free_i = (unsigned)i;
+    if (side == 0 && is && (l == L_LEFT_ON || l == L_RIGHT_ON)) atomicOr(&sc->anomaly, 4u);
     if (l == L_DCROSS || l == L_DBOUNCE) atomicOr(&sc->anomaly, 4u);
   }
   cross = block_sum(cross);
@@ -123,24 +139,36 @@ __global__ void k_side_stats(int n, const unsigned char* __restrict__ isect,
   }
 }
 
-// pointInPoly (foster/polygon.h:427-448) as a reduction over the ring's edges;
-// the seed point is slot `seed` of `sp` (or an explicit point)
-__global__ void k_pip(int n, const double* __restrict__ ring, const double* __restrict__ sp,
-                      const int* __restrict__ seedSlot, int side, BkScalars* sc) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  int s = *seedSlot;
-  double rx = sp[2 * s], ry = sp[2 * s + 1];
+// pointInPoly (foster/polygon.h:427-448) as a reduction over the ring's
+// edges: side 0 tests P's first free slot against ring Q (winding[0]), side
+// 1 Q's first free slot against ring P.  The crossing tests compare order
+// keys; the orientation test stays FP64.
+struct PipSide {
+  int n;
+  const double* ring;
+  const double* sp;
+};
+__global__ void k_pip(PipSide s0, PipSide s1, BkScalars* sc) {
+  const PipSide& a = blockIdx.y ? s1 : s0;
+  const int side = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = sc->firstFree[side];
+  const double rx = a.sp[2 * s], ry = a.sp[2 * s + 1];
+  const long long kx = okey(rx), ky = okey(ry);
   int w = 0;
-  if (i < n) {
-    int j = (i + 1 == n) ? 0 : i + 1;
-    double x0 = ring[2 * i], y0 = ring[2 * i + 1], x1 = ring[2 * j], y1 = ring[2 * j + 1];
-    if ((y0 < ry) != (y1 < ry)) {
-      int d = 2 * (y1 > y0) - 1;
-      if (x0 >= rx) {
-        if (x1 > rx) w = d;
-        else if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (y1 > y0)) w = d;
-      } else if (x1 > rx) {
-        if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (y1 > y0)) w = d;
+  if (i < a.n) {
+    const int j = (i + 1 == a.n) ? 0 : i + 1;
+    const double x0 = a.ring[2 * i], y0 = a.ring[2 * i + 1];
+    const double x1 = a.ring[2 * j], y1 = a.ring[2 * j + 1];
+    const long long ky0 = okey(y0), ky1 = okey(y1);
+    if ((ky0 < ky) != (ky1 < ky)) {
+      const int d = 2 * (ky1 > ky0) - 1;
+      const long long kx0 = okey(x0), kx1 = okey(x1);
+      if (kx0 >= kx) {
+        if (kx1 > kx) w = d;
+        else if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (ky1 > ky0)) w = d;
+      } else if (kx1 > kx) {
+        if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (ky1 > ky0)) w = d;
       }
     }
   }
@@ -149,33 +177,43 @@ __global__ void k_pip(int n, const double* __restrict__ ring, const double* __re
 }
 
 // ---------------------------------------------------------------- entry/exit (A16 step 4)
-__global__ void k_cross_flags(int n, const unsigned char* __restrict__ isect,
-                              const int* __restrict__ lab, int* __restrict__ c) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i > n) return;
-  c[i] = (i < n && isect[i] && lab[i] == L_CROSSING) ? 1 : 0;
+__global__ void k_cross_flags(ListSide s0, ListSide s1, int* __restrict__ c0,
+                              int* __restrict__ c1) {
+  const ListSide& a = blockIdx.y ? s1 : s0;
+  int* c = blockIdx.y ? c1 : c0;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > a.n) return;
+  c[i] = (i < a.n && a.isect[i] && a.lab[i] == L_CROSSING) ? 1 : 0;
 }
 
 // status before vertex i = ENTRY ^ inside(V) ^ parity(crossings from V to i)
-__global__ void k_enex(int n, const unsigned char* __restrict__ isect, const int* __restrict__ lab,
-                       const int* __restrict__ pre, int side, const BkScalars* __restrict__ sc,
-                       unsigned char* __restrict__ enex, unsigned char* __restrict__ split,
-                       int* __restrict__ list) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  int V = sc->firstFree[side];
-  int total = pre[n];
-  int r = (i >= V) ? (pre[i] - pre[V]) : (pre[i] + total - pre[V]);
-  int status0 = (sc->winding[side] & 1) ? EX_EXIT : EX_ENTRY;
-  int status = (r & 1) ? (1 - status0) : status0;
-  int l = lab[i];
+struct EnexSide {
+  int n;
+  const unsigned char* isect;
+  const int* lab;
+  const int* pre;
+  unsigned char* enex;
+  unsigned char* split;
+  int* list;
+};
+__global__ void k_enex(EnexSide s0, EnexSide s1, const BkScalars* __restrict__ sc) {
+  const EnexSide& a = blockIdx.y ? s1 : s0;
+  const int side = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int V = sc->firstFree[side];
+  const int total = a.pre[a.n];
+  const int r = (i >= V) ? (a.pre[i] - a.pre[V]) : (a.pre[i] + total - a.pre[V]);
+  const int status0 = (sc->winding[side] & 1) ? EX_EXIT : EX_ENTRY;
+  const int status = (r & 1) ? (1 - status0) : status0;
+  const int l = a.lab[i];
   unsigned char e = EX_NEITHER;
-  if (isect[i] && l == L_CROSSING) {
+  if (a.isect[i] && l == L_CROSSING) {
     e = (unsigned char)status;
-    list[pre[i]] = i;
+    a.list[a.pre[i]] = i;
   }
-  enex[i] = e;
-  split[i] = (isect[i] && l == L_BOUNCING && status == EX_EXIT) ? 1 : 0;
+  a.enex[i] = e;
+  a.split[i] = (a.isect[i] && l == L_BOUNCING && status == EX_EXIT) ? 1 : 0;
 }
 
 // a bouncing vertex whose neighbour is also a split candidate needs the
@@ -233,10 +271,14 @@ __device__ __forceinline__ int tr_jump(const Trace& T, int t) {
   return T.rankP[p];
 }
 
-__global__ void k_rank(int n, const int* __restrict__ list, int* __restrict__ rank) {
-  int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= n) return;
-  rank[list[x]] = x;
+__global__ void k_rank(int n0, const int* __restrict__ list0, int* __restrict__ rank0, int n1,
+                       const int* __restrict__ list1, int* __restrict__ rank1) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (blockIdx.y == 0) {
+    if (x < n0) rank0[list0[x]] = x;
+  } else if (x < n1) {
+    rank1[list1[x]] = x;
+  }
 }
 
 __global__ void k_tr_init(Trace T, int* __restrict__ jmp, int* __restrict__ mval, BkScalars* sc) {
@@ -809,7 +851,6 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
   int* labQ = (int*)bp.get("bk_labQ", sizeof(int) * nQ);
   int* nbQ = (int*)bp.get("bk_nbQ", sizeof(int) * nQ);
   int* winP = (int*)bp.get("bk_winP", sizeof(int) * nB);
-  int* seed = (int*)bp.get("bk_seed", 256);
   if (bp.failed) return pl.fail(kENoMem, "device allocation failed (back end)");
   BkScalars init;
   memset(&init, 0, sizeof init);
@@ -818,39 +859,25 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
   cudaMemsetAsync(srcP, 0, nB, st);
   cudaMemsetAsync(srcQ, 0, nQ, st);
   cudaMemsetAsync(winP, 0xff, sizeof(int) * nB, st);
+  auto grid2 = [](long long n0, long long n1, int per) {
+    return dim3(grid_for(n0 > n1 ? n0 : n1, per), 2);
+  };
   {
-    ::sbc::KProbe kp_("k_mark_src", st);
-    k_mark_src<<<grid_for(m.bSize, 256), 256, 0, st>>>(m.bSize, m.bND, srcP);
+    const SrcSide s0{m.bSize, nB, 0, m.bND, m.ixB, m.bP, srcP};
+    const SrcSide s1{m.cSize, nQ, m.cStart, m.cND, m.ixC, m.cP, srcQ};
+    ::sbc::KProbe kp_("k_mark_bridge", st);
+    k_mark_bridge<<<grid2(m.bSize, m.cSize, 128), 128, 0, st>>>(s0, s1, sc);
   }
   {
-    ::sbc::KProbe kp_("k_mark_src", st);
-    k_mark_src<<<grid_for(m.cSize, 256), 256, 0, st>>>(m.cSize, m.cND, srcQ);
+    const InitArgs ia{nB, nQ, srcP, srcQ, m.alB, m.labB, m.nbC, m.labC,
+                      isP, isQ, labP, labQ, nbQ, winP};
+    ::sbc::KProbe kp_("k_init_PQ", st);
+    k_init_PQ<<<grid2(nB, nQ, 256), 256, 0, st>>>(ia, sc);
   }
-  {
-    ::sbc::KProbe kp_("k_bridge_check", st);
-    k_bridge_check<<<grid_for(m.bSize, 128), 128, 0, st>>>(m.bSize, nB, m.bND, m.ixB, m.bP, 0, sc);
-  }
-  {
-    ::sbc::KProbe kp_("k_bridge_check", st);
-    k_bridge_check<<<grid_for(m.cSize, 128), 128, 0, st>>>(m.cSize, nQ, m.cND, m.ixC, m.cP, m.cStart,
-                                                         sc);
-  }
-  {
-    ::sbc::KProbe kp_("k_init_P", st);
-    k_init_P<<<grid_for(nB, 256), 256, 0, st>>>(nB, srcP, m.alB, m.labB, isP, labP);
-  }
-  {
-    ::sbc::KProbe kp_("k_init_Q", st);
-    k_init_Q<<<grid_for(nQ, 256), 256, 0, st>>>(nQ, nB, srcQ, m.nbC, m.labC, isQ, labQ, nbQ, winP,
-                                              sc);
-  }
+  const ListSide lsP{nB, isP, labP}, lsQ{nQ, isQ, labQ};
   {
     ::sbc::KProbe kp_("k_side_stats", st);
-    k_side_stats<<<grid_for(nB, 256), 256, 0, st>>>(nB, isP, labP, 0, 1, sc);
-  }
-  {
-    ::sbc::KProbe kp_("k_side_stats", st);
-    k_side_stats<<<grid_for(nQ, 256), 256, 0, st>>>(nQ, isQ, labQ, 1, 0, sc);
+    k_side_stats<<<grid2(nB, nQ, 256), 256, 0, st>>>(lsP, lsQ, sc);
   }
   static_assert(sizeof(BkScalars) <= 8 * 8, "BkScalars fits the back end's host words");
   HostReads& rd = pl.reads();
@@ -865,16 +892,12 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
     return serial_backend(pl, m, out, ovTag);
   if (noP && (h.notOnOn[0] == 0 || h.notOnOn[1] == 0)) return serial_backend(pl, m, out, ovTag);
 
-  // seeds: the first non-intersection vertex of each side against the other side
-  int seeds[2] = {h.firstFree[0], h.firstFree[1]};
-  cudaMemcpyAsync(seed, seeds, sizeof seeds, cudaMemcpyHostToDevice, st);
+  // seeds: the first non-intersection vertex of each side (sc->firstFree)
+  // against the other side
   {
+    const PipSide p0{nQ, m.ixC, m.ixB}, p1{nB, m.ixB, m.ixC};
     ::sbc::KProbe kp_("k_pip", st);
-    k_pip<<<grid_for(nQ, 256), 256, 0, st>>>(nQ, m.ixC, m.ixB, seed, 0, sc);
-  }
-  {
-    ::sbc::KProbe kp_("k_pip", st);
-    k_pip<<<grid_for(nB, 256), 256, 0, st>>>(nB, m.ixB, m.ixC, seed + 1, 1, sc);
+    k_pip<<<grid2(nQ, nB, 256), 256, 0, st>>>(p0, p1, sc);
   }
 
   std::string tg = std::to_string(ovTag);
@@ -929,21 +952,15 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
     if (bp.failed) return pl.fail(kENoMem, "device allocation failed (entry/exit)");
     {
       ::sbc::KProbe kp_("k_cross_flags", st);
-      k_cross_flags<<<grid_for(nB + 1, 256), 256, 0, st>>>(nB, isP, labP, preP);
-    }
-    {
-      ::sbc::KProbe kp_("k_cross_flags", st);
-      k_cross_flags<<<grid_for(nQ + 1, 256), 256, 0, st>>>(nQ, isQ, labQ, preQ);
+      k_cross_flags<<<grid2(nB + 1, nQ + 1, 256), 256, 0, st>>>(lsP, lsQ, preP, preQ);
     }
     exclusive_scan_i32(preP, nB + 1, sscr, st, true);
     exclusive_scan_i32(preQ, nQ + 1, sscr, st, true);
     {
+      const EnexSide e0{nB, isP, labP, preP, enexP, splitP, listP};
+      const EnexSide e1{nQ, isQ, labQ, preQ, enexQ, splitQ, listQ};
       ::sbc::KProbe kp_("k_enex", st);
-      k_enex<<<grid_for(nB, 256), 256, 0, st>>>(nB, isP, labP, preP, 0, sc, enexP, splitP, listP);
-    }
-    {
-      ::sbc::KProbe kp_("k_enex", st);
-      k_enex<<<grid_for(nQ, 256), 256, 0, st>>>(nQ, isQ, labQ, preQ, 1, sc, enexQ, splitQ, listQ);
+      k_enex<<<grid2(nB, nQ, 256), 256, 0, st>>>(e0, e1, sc);
     }
     {
       ::sbc::KProbe kp_("k_split_check", st);
@@ -953,11 +970,7 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
     if ((cPn & 1) || (cQn & 1)) return serial_backend(pl, m, out, ovTag);
     {
       ::sbc::KProbe kp_("k_rank", st);
-      k_rank<<<grid_for(cPn, 256), 256, 0, st>>>(cPn, listP, rankP);
-    }
-    {
-      ::sbc::KProbe kp_("k_rank", st);
-      k_rank<<<grid_for(cQn, 256), 256, 0, st>>>(cQn, listQ, rankQ);
+      k_rank<<<grid2(cPn, cQn, 256), 256, 0, st>>>(cPn, listP, rankP, cQn, listQ, rankQ);
     }
     Trace T{nB, nQ, cPn, cQn, listP, listQ, enexP, enexQ, winP, nbQ, rankP, rankQ};
     const int nE = cPn + cQn;

@@ -44,20 +44,6 @@ __device__ __forceinline__ unsigned fkey(float f) {
   return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
-// LSMF bounding-box filter, oacc_segment_tree.cpp:5282-5316
-__device__ __forceinline__ bool lsmf_exact(double p1x, double p1y, double p2x, double p2y,
-                                           double q1x, double q1y, double q2x, double q2y) {
-  double minPX = p1x, minPY = p1y, maxPX = p2x, maxPY = p2y;
-  double minQX = q1x, minQY = q1y, maxQX = q2x, maxQY = q2y;
-  if (minPX > p2x) { minPX = p2x; maxPX = p1x; }
-  if (minPY > p2y) { minPY = p2y; maxPY = p1y; }
-  if (minQX > q2x) { minQX = q2x; maxQX = q1x; }
-  if (minQY > q2y) { minQY = q2y; maxQY = q1y; }
-  if (minPX > maxQX || maxPX < minQX) return false;
-  if (minPY > maxQY || maxPY < minQY) return false;
-  return true;
-}
-
 // ------------------------------------------------------------------ grid
 struct Grid {
   float x0, y0, inv;
@@ -523,11 +509,12 @@ constexpr int kExChunk = kExBlock * kExPer;
 __global__ void __launch_bounds__(kExBlock)
 k_pair_exact(long long n, const int2* __restrict__ pairs, const int* __restrict__ e_id,
              const double* __restrict__ bP, const double* __restrict__ cP,
+             const long long* __restrict__ bK, const long long* __restrict__ cK,
              const float4* __restrict__ vfB, const float4* __restrict__ vfC,
              const int2* __restrict__ lr, const int* __restrict__ aft, const int* __restrict__ bef,
              int logL, unsigned long long* __restrict__ counters, long long cap,
              int* __restrict__ rb, int* __restrict__ rc, int* __restrict__ rt,
-             unsigned long long* __restrict__ rkey) {
+             unsigned long long* __restrict__ rkey, double2* __restrict__ rab) {
   __shared__ int4 q[kExChunk];
   __shared__ int qn;
   __shared__ unsigned long long ntested;
@@ -547,9 +534,9 @@ k_pair_exact(long long n, const int2* __restrict__ pairs, const int* __restrict_
     if (i < n) {
       const int2 pr = pairs[i];
       const int bId = e_id[pr.x], cId = e_id[pr.y];
-      const double* pb = bP + bId;
-      const double* pc = cP + cId;
-      if (lsmf_exact(pb[0], pb[1], pb[2], pb[3], pc[0], pc[1], pc[2], pc[3])) {
+      const long long* kb = bK + bId;
+      const long long* kc = cK + cId;
+      if (lsmf_keys(kb[0], kb[1], kb[2], kb[3], kc[0], kc[1], kc[2], kc[3])) {
         ++my_tested;
         if (!certainly_disjoint(vfB[bId >> 1], vfB[(bId >> 1) + 1], vfC[cId >> 1],
                                 vfC[(cId >> 1) + 1])) {
@@ -578,11 +565,11 @@ k_pair_exact(long long n, const int2* __restrict__ pairs, const int* __restrict_
     int ty = 0;
     int4 e = make_int4(0, 0, 0, 0);
     unsigned long long key = 0;
+    double al = 0.0, be = 0.0;
     if (j < nq) {
       e = q[j];
       const double* pb = bP + e.x;
       const double* pc = cP + e.y;
-      double al, be;
       ty = seg_isect(pb[0], pb[1], pb[2], pb[3], pc[0], pc[1], pc[2], pc[3], &al, &be);
       if (ty != 0) {
         const unsigned cnt = emission(e.z, e.w, e.y, lr, aft, bef, logL, &key);
@@ -603,6 +590,7 @@ k_pair_exact(long long n, const int2* __restrict__ pairs, const int* __restrict_
           rc[idx] = e.y;
           rt[idx] = ty;
           rkey[idx] = key;
+          rab[idx] = make_double2(al, be);  // the record stage reuses them
         }
       }
     }
@@ -832,11 +820,14 @@ int Pipeline::stage_candidates(int cType, int** rb_out, int** rc_out, int** rt_o
   int* rc = (int*)pool_.get("raw_c", sizeof(int) * hcap);
   int* rt = (int*)pool_.get("raw_t", sizeof(int) * hcap);
   auto* rkey = (unsigned long long*)pool_.get("raw_key", sizeof(unsigned long long) * hcap);
+  auto* rab = (double2*)pool_.get("raw_ab", sizeof(double2) * hcap);
   if (pool_.failed) return fail(kENoMem, "device allocation failed (hits)");
+  raw_ab_ = rab;
   if (npairs > 0) {
     ::sbc::KProbe kp_("k_pair_exact", st, 72.0 * npairs);  // pair + both edges' coordinates
     k_pair_exact<<<grid_for(npairs, kExChunk), kExBlock, 0, st>>>(
-        npairs, pairs, e_id, bP, cP, vfB, vfC, lr, aft, bef, logL, counters, hcap, rb, rc, rt, rkey);
+        npairs, pairs, e_id, bP, cP, bK, cK, vfB, vfC, lr, aft, bef, logL, counters, hcap, rb, rc,
+        rt, rkey, rab);
   }
   const unsigned long long* hc = rd_.get(counters, HostReads::kCand + 8, st, 4);
   if (cudaStreamSynchronize(st) != cudaSuccess) return fail(kECuda, "exact stage");

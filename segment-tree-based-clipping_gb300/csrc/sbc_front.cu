@@ -130,6 +130,12 @@ Pipeline::~Pipeline() {
   if (ev_setup_) cudaEventDestroy(ev_setup_);
   if (ev_side_) cudaEventDestroy(ev_side_);
   if (ev_lr_) cudaEventDestroy(ev_lr_);
+  if (st_hi_) {
+    cudaStreamSynchronize(st_hi_);
+    cudaStreamDestroy(st_hi_);
+  }
+  if (ev_in_) cudaEventDestroy(ev_in_);
+  if (ev_out_) cudaEventDestroy(ev_out_);
   if (h_side_rd_) cudaFreeHost(h_side_rd_);
 }
 
@@ -147,6 +153,21 @@ cudaStream_t Pipeline::side_stream() {
     return nullptr;
   }
   st2_ = s;
+  // the tree stages' stream: the highest priority, so that while both
+  // streams have work the block scheduler serves the main chain first (the
+  // side stream's grid kernels are large and fill what is left)
+  int lo_pri = 0, hi_pri = 0;
+  cudaStream_t h = nullptr;
+  if (cudaDeviceGetStreamPriorityRange(&lo_pri, &hi_pri) == cudaSuccess && hi_pri < lo_pri &&
+      cudaStreamCreateWithPriority(&h, cudaStreamNonBlocking, hi_pri) == cudaSuccess) {
+    if (cudaEventCreateWithFlags(&ev_in_, cudaEventDisableTiming) == cudaSuccess &&
+        cudaEventCreateWithFlags(&ev_out_, cudaEventDisableTiming) == cudaSuccess) {
+      st_hi_ = h;
+    } else {
+      cudaStreamDestroy(h);
+    }
+  }
+  cudaGetLastError();  // a refused priority stream only leaves run() on the caller's stream
   return st2_;
 }
 
@@ -216,25 +237,34 @@ __device__ __forceinline__ void node_interval(const double* __restrict__ ea, int
 }
 
 // ---------------------------------------------------------------- A1 setup
-__global__ void k_setup_base(const double* __restrict__ bxy, int nb, double* __restrict__ bP) {
+// the closed base ring, with the order keys of its coordinates (okey) for
+// the comparison-only filters
+__global__ void k_setup_base(const double* __restrict__ bxy, int nb, double* __restrict__ bP,
+                             long long* __restrict__ bK) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i > nb) return;
   int s = (i == nb) ? 0 : i;
-  bP[2 * i] = bxy[2 * s];
-  bP[2 * i + 1] = bxy[2 * s + 1];
+  const double x = bxy[2 * s], y = bxy[2 * s + 1];
+  bP[2 * i] = x;
+  bP[2 * i + 1] = y;
+  bK[2 * i] = okey(x);
+  bK[2 * i + 1] = okey(y);
 }
 
 __global__ void k_setup_overlays(const double* __restrict__ cxy, const int* __restrict__ cS,
                                  const int* __restrict__ cc, int k, int total,
-                                 double* __restrict__ cP) {
+                                 double* __restrict__ cP, long long* __restrict__ cK) {
   int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= total) return;
   int i = overlay_of(cS, k, g);
   int v = g - cS[i];
   int c = cc[i + 1] - cc[i];
   int src = cc[i] + (v < c ? v : 0);
-  cP[2 * g] = cxy[2 * src];
-  cP[2 * g + 1] = cxy[2 * src + 1];
+  const double x = cxy[2 * src], y = cxy[2 * src + 1];
+  cP[2 * g] = x;
+  cP[2 * g + 1] = y;
+  cK[2 * g] = okey(x);
+  cK[2 * g + 1] = okey(y);
 }
 
 // Edge::getData (edge.h:190-202); ids are offsets into the interleaved arrays
@@ -325,6 +355,8 @@ int Pipeline::stage_setup(const double* d_bxy, const double* d_cxy, const int* c
   E = nb + clSize;
   bP = (double*)pool_.get("bP", sizeof(double) * 2 * (nb + 1));
   cP = (double*)pool_.get("cP", sizeof(double) * 2 * (clSize + k));
+  bK = (long long*)pool_.get("bK", sizeof(long long) * 2 * (nb + 1));
+  cK = (long long*)pool_.get("cK", sizeof(long long) * 2 * (clSize + k));
   cS = (int*)pool_.get("cS", sizeof(int) * (k + 1));
   cc = (int*)pool_.get("cc", sizeof(int) * (k + 1));
   e_id = (int*)pool_.get("e_id", sizeof(int) * E);
@@ -343,11 +375,12 @@ int Pipeline::stage_setup(const double* d_bxy, const double* d_cxy, const int* c
   clear_flags();
   {
     ::sbc::KProbe kp_("k_setup_base", st_);
-    k_setup_base<<<grid_for(nb + 1, 256), 256, 0, st_>>>(d_bxy, nb, bP);
+    k_setup_base<<<grid_for(nb + 1, 256), 256, 0, st_>>>(d_bxy, nb, bP, bK);
   }
   {
     ::sbc::KProbe kp_("k_setup_overlays", st_);
-    k_setup_overlays<<<grid_for(clSize + k, 256), 256, 0, st_>>>(d_cxy, cS, cc, k, clSize + k, cP);
+    k_setup_overlays<<<grid_for(clSize + k, 256), 256, 0, st_>>>(d_cxy, cS, cc, k, clSize + k, cP,
+                                                                 cK);
   }
   {
     ::sbc::KProbe kp_("k_setup_edges", st_);
@@ -481,10 +514,12 @@ static int npow2_host(int n) {
   return p;
 }
 
-// ---- the vertex order from 32-bit keys.  The key of x is its offset from
-// the smallest x scaled to [0, 2^32 - 1] and rounded down: each step
-// (subtraction, multiplication by a positive constant, floor, clamp) is
-// monotone, so x < x' gives key <= key'.  Sorting (key, vertex) takes 4 radix
+// ---- the vertex order from 32-bit keys.  The key of x is x scaled and
+// shifted into [2^19, 2^32 - 2^19]: fma(x, s, c) with s > 0 (one rounding of
+// a function increasing in x), then truncation to an unsigned integer; each
+// step is monotone, so x < x' gives key <= key'.  The 2^19 margins keep the
+// rounding of c and of the fma inside the unsigned range.  Two FP64
+// instructions per vertex (the FP64 rate on GB300 is low).  Sorting (key, vertex) takes 4 radix
 // passes instead of 8; only vertices with equal keys (x values closer than
 // the x range / 2^32) can be out of full order, and those runs are put in
 // (full key, vertex) order, the order of the stable sort on full keys.
@@ -493,17 +528,17 @@ constexpr int kFixRun = 32;  // longer runs fall back to the 64-bit sort
 __global__ void k_vertex_narrow(int E, const unsigned long long* __restrict__ vkey,
                                 const unsigned long long* __restrict__ mm,
                                 unsigned* __restrict__ g, unsigned* __restrict__ gid) {
-  __shared__ double s_lo, s_scale;
+  __shared__ double s_scale, s_shift;
   if (threadIdx.x == 0) {
     const double lo = dkey_value(mm[0]), hi = dkey_value(mm[1]);
-    s_lo = lo;
-    s_scale = hi > lo ? 4294967295.0 / (hi - lo) : 0.0;
+    const double sc = hi > lo ? (4294967296.0 - 1048576.0) / (hi - lo) : 0.0;
+    s_scale = sc;
+    s_shift = 524288.0 - lo * sc;
   }
   __syncthreads();
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= E) return;
-  const double t = floor((dkey_value(vkey[v]) - s_lo) * s_scale);
-  g[v] = t >= 4294967295.0 ? 0xffffffffu : (t > 0.0 ? (unsigned)t : 0u);
+  g[v] = __double2uint_rz(__fma_rn(dkey_value(vkey[v]), s_scale, s_shift));
   gid[v] = (unsigned)v;
 }
 

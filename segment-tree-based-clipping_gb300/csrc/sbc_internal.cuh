@@ -124,6 +124,30 @@ __device__ __forceinline__ unsigned long long dkey(double x) {
   unsigned long long u = (unsigned long long)__double_as_longlong(x == 0.0 ? 0.0 : x);
   return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
 }
+// A signed order key of a finite double by integer operations alone:
+// x < y  <=>  okey(x) < okey(y), and -0.0, +0.0 share the key 0.  On GB300 an
+// FP64 compare issues at the FP64 rate (a small fraction of the integer
+// rate), so comparison-only work runs on these keys.
+__device__ __forceinline__ long long okey(double x) {
+  const long long u = __double_as_longlong(x);
+  return u >= 0 ? u : -(u & 0x7fffffffffffffffll);
+}
+
+// LSMF, the reference's bounding-box filter of an edge pair
+// (oacc_segment_tree.cpp:5282-5316: the min/max swaps and the four
+// separation tests), on order keys: the same decisions as on the doubles
+__device__ __forceinline__ bool lsmf_keys(long long p1x, long long p1y, long long p2x,
+                                          long long p2y, long long q1x, long long q1y,
+                                          long long q2x, long long q2y) {
+  const long long minPX = p1x > p2x ? p2x : p1x, maxPX = p1x > p2x ? p1x : p2x;
+  const long long minPY = p1y > p2y ? p2y : p1y, maxPY = p1y > p2y ? p1y : p2y;
+  const long long minQX = q1x > q2x ? q2x : q1x, maxQX = q1x > q2x ? q1x : q2x;
+  const long long minQY = q1y > q2y ? q2y : q1y, maxQY = q1y > q2y ? q1y : q2y;
+  if (minPX > maxQX || maxPX < minQX) return false;
+  if (minPY > maxQY || maxPY < minQY) return false;
+  return true;
+}
+
 // the value of an order key
 __device__ __forceinline__ double dkey_value(unsigned long long k) {
   const unsigned long long u = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;

@@ -139,8 +139,9 @@ k_dedup_long(const int* __restrict__ start, const int* __restrict__ long_list,
 
 __global__ void k_dedup_write(const unsigned* __restrict__ ord, const int* __restrict__ pos,
                               long long n, const int* __restrict__ rb, const int* __restrict__ rc,
-                              const int* __restrict__ rt, int* __restrict__ ub, int* __restrict__ uc,
-                              int* __restrict__ ut) {
+                              const int* __restrict__ rt, const double2* __restrict__ rab,
+                              int* __restrict__ ub, int* __restrict__ uc, int* __restrict__ ut,
+                              double2* __restrict__ uab) {
   long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   if (pos[p + 1] == pos[p]) return;
@@ -149,6 +150,7 @@ __global__ void k_dedup_write(const unsigned* __restrict__ ord, const int* __res
   ub[j] = rb[r];
   uc[j] = rc[r];
   ut[j] = rt[r];
+  if (rab) uab[j] = rab[r];
 }
 
 // ---------------------------------------------------------------- A10 counts
@@ -171,16 +173,26 @@ __global__ void k_counts(const int* __restrict__ ub, const int* __restrict__ uc,
 }
 
 // ---------------------------------------------------------------- A11 records
+// uab: the (alpha, beta) the exact stage computed for each record (its type
+// already in ut), or nullptr to compute them here
 __global__ void k_records(const int* __restrict__ ub, const int* __restrict__ uc,
-                          int* __restrict__ ut, int K, const double* __restrict__ bP,
-                          const double* __restrict__ cP, double* __restrict__ isxy,
-                          int* __restrict__ aB, int* __restrict__ aC) {
+                          int* __restrict__ ut, const double2* __restrict__ uab, int K,
+                          const double* __restrict__ bP, const double* __restrict__ cP,
+                          double* __restrict__ isxy, int* __restrict__ aB, int* __restrict__ aC) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= K) return;
   const double* b = bP + ub[j];
   const double* c = cP + uc[j];
   double al = 0.0, be = 0.0;
-  int ty = seg_isect(b[0], b[1], b[2], b[3], c[0], c[1], c[2], c[3], &al, &be);
+  int ty;
+  if (uab) {
+    ty = ut[j];
+    const double2 ab = uab[j];
+    al = ab.x;
+    be = ab.y;
+  } else {
+    ty = seg_isect(b[0], b[1], b[2], b[3], c[0], c[1], c[2], c[3], &al, &be);
+  }
   double x = 0.0, y = 0.0;
   if (ty == 1) {
     // (1-alpha)*b1 + alpha*b2, mulScalar/add (:5349-5363)
@@ -587,6 +599,9 @@ int Pipeline::stage_records(int cType, const int* rb, const int* rc, const int* 
   int* ub = (int*)pool_.get("u_b", sizeof(int) * (K + 1));
   int* uc = (int*)pool_.get("u_c", sizeof(int) * (K + 1));
   int* ut = (int*)pool_.get("u_t", sizeof(int) * (K + 1));
+  // the exact stage's (alpha, beta) per hit, carried through the dedup
+  const double2* rab = unique_sorted ? nullptr : raw_ab_;
+  auto* uab = rab ? (double2*)pool_.get("u_ab", sizeof(double2) * (K + 1)) : nullptr;
   if (pool_.failed) return fail(kENoMem, "device allocation failed (unique)");
   if (K > 0 && unique_sorted) {
     cudaMemcpyAsync(ub, rb, sizeof(int) * K, cudaMemcpyDeviceToDevice, st);
@@ -595,7 +610,8 @@ int Pipeline::stage_records(int cType, const int* rb, const int* rc, const int* 
   } else if (K > 0) {
     {
       ::sbc::KProbe kp_("k_dedup_write", st);
-      k_dedup_write<<<grid_for(R, 256), 256, 0, st>>>(ord, keep, R, rb, rc, rt, ub, uc, ut);
+      k_dedup_write<<<grid_for(R, 256), 256, 0, st>>>(ord, keep, R, rb, rc, rt, rab, ub, uc, ut,
+                                                      uab);
     }
   }
 
@@ -662,7 +678,8 @@ int Pipeline::stage_records(int cType, const int* rb, const int* rc, const int* 
   if (K > 0) {
     {
       ::sbc::KProbe kp_("k_records", st);
-      k_records<<<grid_for(K, 256), 256, 0, st>>>(ub, uc, ut, K, bP, cP, isxy, aB, aC);
+      k_records<<<grid_for(K, 256), 256, 0, st>>>(ub, uc, ut, rab ? uab : nullptr, K, bP, cP,
+                                                  isxy, aB, aC);
     }
     // ---- A12 per-edge alpha sorts
     int* along = (int*)pool_.get("alpha_long_list", sizeof(int) * ((long long)(bSize > cSize ? bSize : cSize) + 1));

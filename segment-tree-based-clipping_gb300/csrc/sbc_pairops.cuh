@@ -34,15 +34,9 @@ __device__ __forceinline__ double bvy(const double* p, int n, int i) { return p[
 
 __device__ __forceinline__ bool lsmf_d(double p1x, double p1y, double p2x, double p2y, double q1x,
                                        double q1y, double q2x, double q2y) {
-  double minPX = p1x, minPY = p1y, maxPX = p2x, maxPY = p2y;
-  double minQX = q1x, minQY = q1y, maxQX = q2x, maxQY = q2y;
-  if (minPX > p2x) { minPX = p2x; maxPX = p1x; }
-  if (minPY > p2y) { minPY = p2y; maxPY = p1y; }
-  if (minQX > q2x) { minQX = q2x; maxQX = q1x; }
-  if (minQY > q2y) { minQY = q2y; maxQY = q1y; }
-  if (minPX > maxQX || maxPX < minQX) return false;
-  if (minPY > maxQY || maxPY < minQY) return false;
-  return true;
+  // on order keys: integer compares instead of FP64 ones, same decisions
+  return lsmf_keys(okey(p1x), okey(p1y), okey(p2x), okey(p2y), okey(q1x), okey(q1y), okey(q2x),
+                   okey(q2y));
 }
 
 // stable bottom-up merge sort of idx[0..n) by less(a, b)

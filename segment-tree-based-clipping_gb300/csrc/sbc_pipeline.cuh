@@ -158,6 +158,8 @@ class Pipeline {
   std::vector<int> hcS, hcc;           // prefix of (c_i + 1) and of c_i
   double* bP = nullptr;                // (nb+1)*2
   double* cP = nullptr;                // (clSize+k)*2
+  long long* bK = nullptr;             // order keys (okey) of bP's coordinates
+  long long* cK = nullptr;             // order keys of cP's coordinates
   int* cS = nullptr;                   // device copy of hcS (k+1)
   int* cc = nullptr;                   // device copy of hcc (k+1)
   int* e_id = nullptr;
@@ -207,6 +209,7 @@ class Pipeline {
   int join_ready_ = 0;                 // overlay whose box join below is ready (0: none)
   const int2* join_pairs_ = nullptr;
   unsigned long long* join_counters_ = nullptr;
+  const double2* raw_ab_ = nullptr;    // (alpha, beta) of each candidate hit (stage_candidates)
   long long join_npairs_ = 0, join_work_ = 0;
   // intermediate arrays of the last overlay processed (device, diagnostics)
   int *dbg_ub = nullptr, *dbg_uc = nullptr, *dbg_ut = nullptr;
@@ -263,6 +266,10 @@ class Pipeline {
   cudaStream_t st_;
   cudaStream_t st2_ = nullptr;         // side stream (grid stage)
   cudaEvent_t ev_setup_ = nullptr, ev_side_ = nullptr, ev_lr_ = nullptr;
+  // run() issues its main-stream work on st_hi_ (highest priority), joined
+  // to and from the caller's stream through ev_in_ / ev_out_
+  cudaStream_t st_hi_ = nullptr;
+  cudaEvent_t ev_in_ = nullptr, ev_out_ = nullptr;
   bool cover_count_pending_ = false;
   unsigned* h_side_rd_ = nullptr;      // 256 B pinned: the grid stage's reads ([0..9]),
                                        // the cover stage's two counts ([32..35])

@@ -533,7 +533,7 @@ __device__ __forceinline__ T os_block_scan(T v, T* s_warp) {
 // One pass: planned pass `q` (digit position plan.pos[q]).  (ka, va) hold the
 // input of the first pass; each pass that runs moves the keys to the other
 // buffer pair.  Dynamic shared memory: kOsTile keys then kOsTile values.
-constexpr int kOsLook = 16;  // earlier tiles read per look-back round trip
+constexpr int kOsLook = 32;  // earlier tiles read per look-back round trip
 template <typename K>
 constexpr size_t os_dyn_smem() { return (sizeof(K) + sizeof(unsigned)) * kOsTile; }
 

@@ -271,7 +271,7 @@ def _near_vertical_chain(n: int):
     return np.array(pts, dtype=np.float64)
 
 
-@pytest.mark.parametrize("n,stat", [(6, 2), (33, 2), (48, 1)])
+@pytest.mark.parametrize("n,stat", [(6, 2), (32, 2), (48, 1)])
 def test_vertex_key_runs_are_fixed_up(clipper, n, stat):
     """Equal 32-bit vertex keys: runs of up to 32 vertices are put in full-key
     order in place (stat 2); a longer run sends the stage back to the 64-bit
