@@ -25,15 +25,6 @@ int Pipeline::run(const double* d_bxy, int nb_, const double* d_cxy, const int* 
   if (k < 1 || k > 9) return fail(kEInput, "1 to 9 overlays are supported");
   for (int i = 0; i < k; ++i)
     if (c_sizes[i] < 3) return fail(kEInput, "overlay polygon needs at least 3 vertices");
-  // the main chain on the pipeline's high-priority stream, after the
-  // caller's earlier work and before its later work
-  const cudaStream_t user_st = st_;
-  const bool on_hi = side_stream() && st_hi_;
-  if (on_hi) {
-    cudaEventRecord(ev_in_, user_st);
-    cudaStreamWaitEvent(st_hi_, ev_in_, 0);
-    st_ = st_hi_;
-  }
   cudaEvent_t ev[8];
   if (timing)
     for (int i = 0; i < 8; ++i) cudaEventCreate(&ev[i]);
@@ -102,11 +93,6 @@ int Pipeline::run(const double* d_bxy, int nb_, const double* d_cxy, const int* 
     for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&times.ms[i], ev[i], ev[i + 1]);
     cudaEventElapsedTime(&times.ms[7], ev[0], ev[5]);
     for (int i = 0; i < 8; ++i) cudaEventDestroy(ev[i]);
-  }
-  if (on_hi) {
-    cudaEventRecord(ev_out_, st_hi_);
-    cudaStreamWaitEvent(user_st, ev_out_, 0);
-    st_ = user_st;
   }
   return rc;
 }

@@ -328,6 +328,8 @@ __global__ void k_tr_jump(int n, const int* __restrict__ jin, const int* __restr
 // ended round r - 1.  Every thread reads the same flag after the same
 // barrier, so all leave the loop in the same round.  The result is left in
 // the A arrays.
+constexpr int kJumpBatch = 4;
+
 __global__ void k_tr_jump_coop(int n, int* __restrict__ jA, int* __restrict__ mA,
                                int* __restrict__ jB, int* __restrict__ mB,
                                unsigned* __restrict__ flags, int max_rounds) {
@@ -338,13 +340,32 @@ __global__ void k_tr_jump_coop(int n, int* __restrict__ jA, int* __restrict__ mA
   for (int r = 0; r < max_rounds; ++r) {
     if (tid == 0) flags[(r + 1) % 3] = 0u;
     bool ch = false;
-    for (long long x = tid; x < n; x += nth) {
-      const int j = jin[x];
-      const int a = min_[x], b = min_[j];
-      const int m = a < b ? a : b;
-      mout[x] = m;
-      jout[x] = jin[j];
-      ch |= m != a;
+    // kJumpBatch elements per thread at a time: their loads are issued
+    // together, so a round costs two dependent L2 round trips per batch
+    for (long long x0 = tid; x0 < n; x0 += kJumpBatch * nth) {
+      int j[kJumpBatch], a[kJumpBatch], b[kJumpBatch], jj[kJumpBatch];
+#pragma unroll
+      for (int u = 0; u < kJumpBatch; ++u) {
+        const long long x = x0 + u * nth;
+        j[u] = x < n ? jin[x] : 0;
+        a[u] = x < n ? min_[x] : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < kJumpBatch; ++u) {
+        const long long x = x0 + u * nth;
+        b[u] = x < n ? min_[j[u]] : 0;
+        jj[u] = x < n ? jin[j[u]] : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < kJumpBatch; ++u) {
+        const long long x = x0 + u * nth;
+        if (x < n) {
+          const int m = a[u] < b[u] ? a[u] : b[u];
+          mout[x] = m;
+          jout[x] = jj[u];
+          ch |= m != a[u];
+        }
+      }
     }
     if (__any_sync(0xffffffffu, ch) && (threadIdx.x & 31) == 0) atomicOr(&flags[r % 3], 1u);
     grid.sync();
@@ -370,16 +391,28 @@ __global__ void k_lr_jump_coop(int n, int* __restrict__ nA, long long* __restric
   for (int r = 0; r < max_rounds; ++r) {
     if (tid == 0) flags[(r + 1) % 3] = 0u;
     bool ch = false;
-    for (long long x = tid; x < n; x += nth) {
-      const int j = nin[x];
-      if (j < 0) {
-        nout[x] = -1;
-        Sout[x] = Sin[x];
-      } else {
-        const int jj = nin[j];
-        nout[x] = jj;
-        Sout[x] = Sin[x] + Sin[j];
-        ch |= jj < 0;
+    for (long long x0 = tid; x0 < n; x0 += kJumpBatch * nth) {
+      int j[kJumpBatch], jj[kJumpBatch];
+      long long sa[kJumpBatch], sb[kJumpBatch];
+#pragma unroll
+      for (int u = 0; u < kJumpBatch; ++u) {
+        const long long x = x0 + u * nth;
+        j[u] = x < n ? nin[x] : -1;
+        sa[u] = x < n ? Sin[x] : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < kJumpBatch; ++u) {
+        jj[u] = j[u] >= 0 ? nin[j[u]] : -1;
+        sb[u] = j[u] >= 0 ? Sin[j[u]] : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < kJumpBatch; ++u) {
+        const long long x = x0 + u * nth;
+        if (x < n) {
+          nout[x] = j[u] < 0 ? -1 : jj[u];
+          Sout[x] = sa[u] + sb[u];
+          ch |= j[u] >= 0 && jj[u] < 0;
+        }
       }
     }
     if (__any_sync(0xffffffffu, ch) && (threadIdx.x & 31) == 0) atomicOr(&flags[r % 3], 1u);
@@ -492,50 +525,120 @@ __global__ void k_lr_ringlen(int cap, const int* __restrict__ nRings_p,
   rlen[r] = r < nRings ? (int)S[starts[r]] : 0;
 }
 
+// Segments longer than kSegPiece vertices are copied in pieces of that size
+// by k_lr_copy_long, one warp per piece: a ring stretch of 10^5 vertices
+// would otherwise keep one warp busy long after the others.
+constexpr int kSegPiece = 1024;
+
+// the output placement of segment x (an enex vertex of a start's orbit)
+struct SegCopy {
+  long long base;
+  int len, m, sx;
+  bool onP, fwd;
+};
+__device__ __forceinline__ SegCopy seg_copy_of(const Trace& T, int x, const long long* S,
+                                               const int* ringI, const int* startPre,
+                                               const int* vOff) {
+  SegCopy c;
+  const int I = ringI[x];
+  c.base = vOff[startPre[I]] + S[I] - S[x];
+  const int t = tr_target(T, x);
+  c.len = tr_len(T, x, t);
+  c.onP = x < T.cP;
+  c.m = c.onP ? T.nB : T.nQ;
+  c.sx = tr_slot(T, x);
+  c.fwd = (c.onP ? T.enexP[c.sx] : T.enexQ[c.sx]) == EX_ENTRY;
+  return c;
+}
+
+// vertex `step` (1-based) of a segment
+__device__ __forceinline__ void seg_copy_step(const SegCopy& c, int step, const double* ixB,
+                                              const double* ixC, double* out) {
+  int slot = c.fwd ? c.sx + step : c.sx - step;
+  if (slot >= c.m) slot -= c.m;
+  if (slot < 0) slot += c.m;
+  const double2 v = reinterpret_cast<const double2*>(c.onP ? ixB : ixC)[slot];
+  reinterpret_cast<double2*>(out)[c.base + step - 1] = v;
+}
+
 __global__ void k_lr_copy(Trace T, const int* __restrict__ nxt, const long long* __restrict__ S,
                           const int* __restrict__ ringI, const int* __restrict__ startPre,
                           const int* __restrict__ vOff, const double* __restrict__ ixB,
-                          const double* __restrict__ ixC, double* __restrict__ out) {
+                          const double* __restrict__ ixC, double* __restrict__ out,
+                          int2* __restrict__ pieces, unsigned* __restrict__ npieces,
+                          long long pcap) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const int n = T.cP + T.cQ;
-  const bool mine = x < n && nxt[x] == -1;  // only segments of a start's orbit
+  bool mine = x < n && nxt[x] == -1;  // only segments of a start's orbit
   long long base = 0;
   int len = 0, m = 1, sx = 0;
   bool onP = false, fwd = false;
   if (mine) {
-    const int I = ringI[x];
-    base = vOff[startPre[I]] + S[I] - S[x];
-    const int t = tr_target(T, x);
-    len = tr_len(T, x, t);
-    onP = x < T.cP;
-    m = onP ? T.nB : T.nQ;
-    sx = tr_slot(T, x);
-    fwd = (onP ? T.enexP[sx] : T.enexQ[sx]) == EX_ENTRY;
+    const SegCopy c = seg_copy_of(T, x, S, ringI, startPre, vOff);
+    if (c.len > kSegPiece) {
+      // to the long-segment queue, one entry per piece
+      const int np = (c.len + kSegPiece - 1) / kSegPiece;
+      const unsigned q = atomicAdd(npieces, (unsigned)np);
+      for (int i = 0; i < np; ++i)
+        if (q + i < pcap) pieces[q + i] = make_int2(x, i);
+      mine = false;
+    } else {
+      base = c.base;
+      len = c.len;
+      m = c.m;
+      sx = c.sx;
+      onP = c.onP;
+      fwd = c.fwd;
+    }
   }
-  auto copy = [&](long long b0, int s0, int mm, bool f, bool p, int step) {
-    int slot = f ? s0 + step : s0 - step;
-    if (slot >= mm) slot -= mm;
-    if (slot < 0) slot += mm;
-    const double* src = p ? ixB : ixC;
-    out[2 * (b0 + step - 1)] = src[2 * slot];
-    out[2 * (b0 + step - 1) + 1] = src[2 * slot + 1];
-  };
-  // short segments: one thread each; long ones: the whole warp, in turn
-  const bool longseg = mine && len > 32;
-  if (mine && !longseg)
-    for (int step = 1; step <= len; ++step) copy(base, sx, m, fwd, onP, step);
-  unsigned lm = __ballot_sync(0xffffffffu, longseg);
-  while (lm) {
-    const int src = __ffs(lm) - 1;
-    lm &= lm - 1;
-    const long long b0 = __shfl_sync(0xffffffffu, base, src);
-    const int l0 = __shfl_sync(0xffffffffu, len, src);
-    const int s0 = __shfl_sync(0xffffffffu, sx, src);
-    const int m0 = __shfl_sync(0xffffffffu, m, src);
-    const bool f0 = __shfl_sync(0xffffffffu, (int)fwd, src) != 0;
-    const bool p0 = __shfl_sync(0xffffffffu, (int)onP, src) != 0;
-    for (int step = 1 + lane; step <= l0; step += 32) copy(b0, s0, m0, f0, p0, step);
+  // the warp's segments laid end to end, 32 output vertices per round: each
+  // lane finds the segment of its vertex by a binary search over the lanes'
+  // inclusive length prefix, so every lane copies whatever the lengths
+  const unsigned full = 0xffffffffu;
+  int incl = mine ? len : 0;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(full, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int excl = incl - (mine ? len : 0);
+  const int total = __shfl_sync(full, incl, 31);
+  for (int o0 = 0; o0 < total; o0 += 32) {
+    const int o = o0 + lane;
+    int sl = 0;  // lanes whose segments end at or before o
+#pragma unroll
+    for (int b = 16; b >= 1; b >>= 1)
+      if (__shfl_sync(full, incl, sl + b - 1) <= o) sl += b;
+    const long long b0 = __shfl_sync(full, base, sl);
+    const int e0 = __shfl_sync(full, excl, sl);
+    const int s0 = __shfl_sync(full, sx, sl);
+    const int m0 = __shfl_sync(full, m, sl);
+    const bool f0 = __shfl_sync(full, (int)fwd, sl) != 0;
+    const bool p0 = __shfl_sync(full, (int)onP, sl) != 0;
+    if (o < total) {
+      const SegCopy c{b0, 0, m0, s0, p0, f0};
+      seg_copy_step(c, o - e0 + 1, ixB, ixC, out);
+    }
+  }
+}
+
+// the pieces of the long segments, one warp per piece
+__global__ void k_lr_copy_long(Trace T, const long long* __restrict__ S,
+                               const int* __restrict__ ringI, const int* __restrict__ startPre,
+                               const int* __restrict__ vOff, const double* __restrict__ ixB,
+                               const double* __restrict__ ixC, double* __restrict__ out,
+                               const int2* __restrict__ pieces,
+                               const unsigned* __restrict__ npieces, long long pcap) {
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long np = min((long long)*npieces, pcap);
+  for (long long i = w; i < np; i += ((long long)gridDim.x * blockDim.x) >> 5) {
+    const int2 pc = pieces[i];
+    const SegCopy c = seg_copy_of(T, pc.x, S, ringI, startPre, vOff);
+    const int s0 = pc.y * kSegPiece + 1;
+    const int s1 = min(c.len, s0 + kSegPiece - 1);
+    for (int step = s0 + lane; step <= s1; step += 32) seg_copy_step(c, step, ixB, ixC, out);
   }
 }
 
@@ -948,14 +1051,20 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
     int* listQ = (int*)bp.get("bk_listQ", sizeof(int) * (h.crossCount[1] + 1));
     int* rankP = (int*)bp.get("bk_rankP", sizeof(int) * nB);
     int* rankQ = (int*)bp.get("bk_rankQ", sizeof(int) * nQ);
-    void* sscr = bp.get_zeroed("bk_scan", scan_scratch_bytes((long long)nB + nQ + 4), st);
+    const long long nmax = (long long)(nB > nQ ? nB : nQ) + 1;
+    const size_t scr_b = std::max(scan_scratch_bytes((long long)nB + nQ + 4),
+                                  scan_set_scratch_bytes(nmax, 2));
+    void* sscr = bp.get_zeroed("bk_scan", scr_b, st);
     if (bp.failed) return pl.fail(kENoMem, "device allocation failed (entry/exit)");
     {
       ::sbc::KProbe kp_("k_cross_flags", st);
       k_cross_flags<<<grid2(nB + 1, nQ + 1, 256), 256, 0, st>>>(lsP, lsQ, preP, preQ);
     }
-    exclusive_scan_i32(preP, nB + 1, sscr, st, true);
-    exclusive_scan_i32(preQ, nQ + 1, sscr, st, true);
+    {
+      int* const arrs[2] = {preP, preQ};
+      const long long ns[2] = {(long long)nB + 1, (long long)nQ + 1};
+      exclusive_scan_i32_set(arrs, ns, 2, sscr, st, true);
+    }
     {
       const EnexSide e0{nB, isP, labP, preP, enexP, splitP, listP};
       const EnexSide e1{nQ, isQ, labQ, preQ, enexQ, splitQ, listQ};
@@ -1059,11 +1168,24 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
     const int nRings = *r_nr;
     const long long nv = *r_nv;
     double* rxy = (double*)bp.get("bk_rxy", sizeof(double) * 2 * (nv + 1));
+    // long-segment pieces: at most nv / kSegPiece + (segments above kSegPiece)
+    const long long pcap = 2 * nv / kSegPiece + 2;
+    auto* pieces = (int2*)bp.get("bk_pieces", sizeof(int2) * pcap);
+    auto* npieces = (unsigned*)bp.get("bk_npieces", 256);
     if (bp.failed) return pl.fail(kENoMem, "device allocation failed (ring vertices)");
+    cudaMemsetAsync(npieces, 0, sizeof(unsigned), st);
     {
       ::sbc::KProbe kp_("k_lr_copy", st);
       k_lr_copy<<<grid_for(nE, 128), 128, 0, st>>>(T, nxA, SA, ringI, isStart, rlen, m.ixB, m.ixC,
-                                                    rxy);
+                                                    rxy, pieces, npieces, pcap);
+    }
+    {
+      ::sbc::KProbe kp_("k_lr_copy_long", st);
+      k_lr_copy_long<<<grid_for(((long long)pcap + 1) * 32, 256) < 1216u
+                           ? grid_for(((long long)pcap + 1) * 32, 256)
+                           : 1216u,
+                       256, 0, st>>>(T, SA, ringI, isStart, rlen, m.ixB, m.ixC, rxy, pieces,
+                                     npieces, pcap);
     }
     out.d_off = rlen;  // exclusive prefix of ring lengths, nRings+1 entries
     out.d_xy = rxy;

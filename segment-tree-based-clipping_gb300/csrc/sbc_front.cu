@@ -130,12 +130,6 @@ Pipeline::~Pipeline() {
   if (ev_setup_) cudaEventDestroy(ev_setup_);
   if (ev_side_) cudaEventDestroy(ev_side_);
   if (ev_lr_) cudaEventDestroy(ev_lr_);
-  if (st_hi_) {
-    cudaStreamSynchronize(st_hi_);
-    cudaStreamDestroy(st_hi_);
-  }
-  if (ev_in_) cudaEventDestroy(ev_in_);
-  if (ev_out_) cudaEventDestroy(ev_out_);
   if (h_side_rd_) cudaFreeHost(h_side_rd_);
 }
 
@@ -143,8 +137,15 @@ Pipeline::~Pipeline() {
 // events and 256 bytes of pinned host memory for reads back
 cudaStream_t Pipeline::side_stream() {
   if (st2_) return st2_;
+  // the side stream at the highest priority: its grid and join kernels are
+  // the large ones, and the main chain's small kernels fill around them
+  int lo_pri = 0, hi_pri = 0;
   cudaStream_t s = nullptr;
-  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+  if (cudaDeviceGetStreamPriorityRange(&lo_pri, &hi_pri) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, hi_pri) != cudaSuccess) {
+    cudaGetLastError();
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+  }
   if (cudaEventCreateWithFlags(&ev_setup_, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&ev_side_, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&ev_lr_, cudaEventDisableTiming) != cudaSuccess ||
@@ -153,21 +154,6 @@ cudaStream_t Pipeline::side_stream() {
     return nullptr;
   }
   st2_ = s;
-  // the tree stages' stream: the highest priority, so that while both
-  // streams have work the block scheduler serves the main chain first (the
-  // side stream's grid kernels are large and fill what is left)
-  int lo_pri = 0, hi_pri = 0;
-  cudaStream_t h = nullptr;
-  if (cudaDeviceGetStreamPriorityRange(&lo_pri, &hi_pri) == cudaSuccess && hi_pri < lo_pri &&
-      cudaStreamCreateWithPriority(&h, cudaStreamNonBlocking, hi_pri) == cudaSuccess) {
-    if (cudaEventCreateWithFlags(&ev_in_, cudaEventDisableTiming) == cudaSuccess &&
-        cudaEventCreateWithFlags(&ev_out_, cudaEventDisableTiming) == cudaSuccess) {
-      st_hi_ = h;
-    } else {
-      cudaStreamDestroy(h);
-    }
-  }
-  cudaGetLastError();  // a refused priority stream only leaves run() on the caller's stream
   return st2_;
 }
 

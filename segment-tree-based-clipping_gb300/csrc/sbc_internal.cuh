@@ -237,6 +237,12 @@ void exclusive_scan_i32(int* d, long long n, void* scratch, cudaStream_t st,
                         bool state_zero = false);
 void exclusive_scan_i64(long long* d, long long n, void* scratch, cudaStream_t st,
                         bool state_zero = false);
+// up to 4 independent exclusive scans in one launch (arrays d[i] of n[i]
+// int32 values); the scratch holds scan_set_scratch_bytes(max n, count)
+// bytes, left zero as the single scans leave theirs
+size_t scan_set_scratch_bytes(long long n_max, int count);
+void exclusive_scan_i32_set(int* const* d, const long long* n, int count, void* scratch,
+                            cudaStream_t st, bool state_zero = false);
 // true (and cleared) if a scan's bounded look-back wait gave up since the last call
 bool scan_error_take();
 // the device address of the scans' error word (for a read queued on a

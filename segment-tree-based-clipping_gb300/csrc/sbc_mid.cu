@@ -635,7 +635,8 @@ int Pipeline::stage_records(int cType, const int* rb, const int* rc, const int* 
   auto* csk2 = (unsigned*)pool_.get("cs_keys2", sizeof(unsigned) * (K + 1));
   auto* csv2 = (unsigned*)pool_.get("cs_vals2", sizeof(unsigned) * (K + 1));
   void* rscr2 = pool_.get("radix_scr_cs", radix_scratch_bytes(K + 1));
-  void* sscr3 = pool_.get_zeroed("scan_scr6", scan_scratch_bytes(bSize + cSize + 4), st);
+  void* sscr3 = pool_.get_zeroed(
+      "scan_scr6", scan_set_scratch_bytes((long long)(bSize > cSize ? bSize : cSize) + 1, 4), st);
   if (pool_.failed) return fail(kENoMem, "device allocation failed (counts)");
   cudaMemsetAsync(bAll, 0, sizeof(int) * (bSize + 1), st);
   cudaMemsetAsync(bND, 0, sizeof(int) * (bSize + 1), st);
@@ -654,10 +655,11 @@ int Pipeline::stage_records(int cType, const int* rb, const int* rc, const int* 
     while ((1LL << bits) < 2LL * (clSize + k)) ++bits;
     radix_sort_u32(csk, csv, csk2, csv2, K, bits, rscr2, st);
   }
-  exclusive_scan_i32(bAll, bSize + 1, sscr3, st, true);
-  exclusive_scan_i32(bND, bSize + 1, sscr3, st, true);
-  exclusive_scan_i32(cAll, cSize + 1, sscr3, st, true);
-  exclusive_scan_i32(cND, cSize + 1, sscr3, st, true);
+  {
+    int* const arrs[4] = {bAll, bND, cAll, cND};
+    const long long ns[4] = {bSize + 1, bSize + 1, cSize + 1, cSize + 1};
+    exclusive_scan_i32_set(arrs, ns, 4, sscr3, st, true);
+  }
   const int* r_hb = rd_.get(bND + bSize, HostReads::kMid + 1, st);
   const int* r_hc = rd_.get(cND + cSize, HostReads::kMid + 2, st);
   cudaStreamSynchronize(st);

@@ -266,10 +266,6 @@ class Pipeline {
   cudaStream_t st_;
   cudaStream_t st2_ = nullptr;         // side stream (grid stage)
   cudaEvent_t ev_setup_ = nullptr, ev_side_ = nullptr, ev_lr_ = nullptr;
-  // run() issues its main-stream work on st_hi_ (highest priority), joined
-  // to and from the caller's stream through ev_in_ / ev_out_
-  cudaStream_t st_hi_ = nullptr;
-  cudaEvent_t ev_in_ = nullptr, ev_out_ = nullptr;
   bool cover_count_pending_ = false;
   unsigned* h_side_rd_ = nullptr;      // 256 B pinned: the grid stage's reads ([0..9]),
                                        // the cover stage's two counts ([32..35])

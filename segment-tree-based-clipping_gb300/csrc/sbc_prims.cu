@@ -240,72 +240,90 @@ constexpr unsigned long long kLbMask = (1ull << 62) - 1;
 constexpr unsigned kLbSpin = 1u << 20;
 __device__ unsigned g_scan_error = 0;
 
+// Up to kScanMulti independent arrays in one launch: blockIdx.y picks the
+// array; each has its own look-back words, gridDim.x + 2 of them, and blocks
+// past an array's own tile count only count themselves done.
+constexpr int kScanMulti = 4;
+template <typename T>
+struct ScanSet {
+  T* d[kScanMulti];
+  long long n[kScanMulti];
+  bool vec[kScanMulti];
+};
+
 template <typename T>
 __global__ void __launch_bounds__(kScanThreads)
-k_scan_lb(T* __restrict__ d, long long n, unsigned long long* __restrict__ state, bool vec) {
+k_scan_lb(ScanSet<T> set, unsigned long long* __restrict__ state_all) {
   __shared__ T sw[32];
   __shared__ unsigned s_tile;
   __shared__ T s_prefix;
+  T* __restrict__ d = set.d[blockIdx.y];
+  const long long n = set.n[blockIdx.y];
+  const bool vec = set.vec[blockIdx.y];
+  unsigned long long* __restrict__ state = state_all + (size_t)blockIdx.y * (gridDim.x + 2);
   if (threadIdx.x == 0) s_tile = atomicAdd((unsigned*)state, 1u);
   __syncthreads();
   const unsigned tile = s_tile;
   unsigned long long* ts = state + 1;
-  const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
-  T v[kScanItems];
-  scan_load(d, base, n, vec, v);
-  T s = 0;
+  const long long ntiles = (n + kScanTile - 1) / kScanTile;
+  if ((long long)tile < ntiles) {
+    const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
+    T v[kScanItems];
+    scan_load(d, base, n, vec, v);
+    T s = 0;
 #pragma unroll
-  for (int i = 0; i < kScanItems; ++i) s += v[i];
-  T tot;
-  const T ex = block_exclusive_scan<T>(s, sw, &tot);
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
-    T prefix = 0;
-    if (tile == 0) {
-      if (lane == 0) atomicExch(&ts[0], kLbPrefix | ((unsigned long long)tot & kLbMask));
-    } else {
-      if (lane == 0) atomicExch(&ts[tile], kLbTotal | ((unsigned long long)tot & kLbMask));
-      long long top = (long long)tile - 1;
-      bool done = false;
-      while (!done) {
-        const long long j = top - lane;
-        unsigned long long w = kLbPrefix;  // before tile 0: nothing to add
-        if (j >= 0) {
-          unsigned spins = 0;
-          do {
-            w = *(volatile unsigned long long*)&ts[j];
-          } while ((w >> 62) == 0 && ++spins < kLbSpin);
-          if ((w >> 62) == 0) {
-            atomicOr(&g_scan_error, 1u);
-            w = kLbPrefix;
+    for (int i = 0; i < kScanItems; ++i) s += v[i];
+    T tot;
+    const T ex = block_exclusive_scan<T>(s, sw, &tot);
+    if (threadIdx.x < 32) {
+      const int lane = threadIdx.x;
+      T prefix = 0;
+      if (tile == 0) {
+        if (lane == 0) atomicExch(&ts[0], kLbPrefix | ((unsigned long long)tot & kLbMask));
+      } else {
+        if (lane == 0) atomicExch(&ts[tile], kLbTotal | ((unsigned long long)tot & kLbMask));
+        long long top = (long long)tile - 1;
+        bool done = false;
+        while (!done) {
+          const long long j = top - lane;
+          unsigned long long w = kLbPrefix;  // before tile 0: nothing to add
+          if (j >= 0) {
+            unsigned spins = 0;
+            do {
+              w = *(volatile unsigned long long*)&ts[j];
+            } while ((w >> 62) == 0 && ++spins < kLbSpin);
+            if ((w >> 62) == 0) {
+              atomicOr(&g_scan_error, 1u);
+              w = kLbPrefix;
+            }
           }
+          const unsigned pm = __ballot_sync(0xffffffffu, (w >> 62) == 2);
+          const int firstP = pm ? __ffs(pm) - 1 : 32;
+          T val = (lane <= firstP && j >= 0) ? (T)(w & kLbMask) : T(0);
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+          prefix += val;
+          done = pm != 0;
+          top -= 32;
         }
-        const unsigned pm = __ballot_sync(0xffffffffu, (w >> 62) == 2);
-        const int firstP = pm ? __ffs(pm) - 1 : 32;
-        T val = (lane <= firstP && j >= 0) ? (T)(w & kLbMask) : T(0);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
-        prefix += val;
-        done = pm != 0;
-        top -= 32;
+        if (lane == 0) atomicExch(&ts[tile], kLbPrefix | ((unsigned long long)(prefix + tot) & kLbMask));
       }
-      if (lane == 0) atomicExch(&ts[tile], kLbPrefix | ((unsigned long long)(prefix + tot) & kLbMask));
+      if (lane == 0) s_prefix = prefix;
     }
-    if (lane == 0) s_prefix = prefix;
-  }
-  __syncthreads();
-  T run = ex + s_prefix;
-  T o[kScanItems];
+    __syncthreads();
+    T run = ex + s_prefix;
+    T o[kScanItems];
 #pragma unroll
-  for (int i = 0; i < kScanItems; ++i) {
-    o[i] = run;
-    run += v[i];
+    for (int i = 0; i < kScanItems; ++i) {
+      o[i] = run;
+      run += v[i];
+    }
+    scan_store(d, base, n, vec, o);
   }
-  scan_store(d, base, n, vec, o);
   // The last block to finish clears the look-back words (ticket, tile words,
   // this counter) so the next scan on the same scratch needs no memset: a
   // block counts itself done only after its own look-back reads, so when the
-  // count reaches the number of tiles nobody reads the words any more.
+  // count reaches the number of blocks nobody reads the words any more.
   __shared__ bool s_last;
   if (threadIdx.x == 0) {
     __threadfence();
@@ -324,12 +342,40 @@ void scan_rec(T* d, long long n, T* scratch, cudaStream_t st, bool state_zero = 
     auto* state = (unsigned long long*)scratch;
     // the scan leaves its words zero; a scratch not known to start zero is cleared first
     if (!state_zero) cudaMemsetAsync(state, 0, sizeof(unsigned long long) * (tiles + 2), st);
+    ScanSet<T> set{};
+    set.d[0] = d;
+    set.n[0] = n;
+    set.vec[0] = ((uintptr_t)d & 15) == 0;
     ::sbc::KProbe kp_("k_scan_lb", st, 2.0 * sizeof(T) * (double)n);
-    k_scan_lb<T><<<(unsigned)tiles, kScanThreads, 0, st>>>(d, n, state,
-                                                       ((uintptr_t)d & 15) == 0);
+    k_scan_lb<T><<<dim3((unsigned)tiles, 1), kScanThreads, 0, st>>>(set, state);
     return;
   }
   scan_multi(d, n, scratch, st);
+}
+
+// count arrays scanned in one launch (see k_scan_lb)
+template <typename T>
+void scan_set(T* const* d, const long long* n, int count, T* scratch, cudaStream_t st,
+              bool state_zero) {
+  long long tiles = 1;
+  double bytes = 0.0;
+  ScanSet<T> set{};
+  int c = 0;
+  for (int i = 0; i < count; ++i) {
+    if (n[i] <= 0) continue;
+    set.d[c] = d[i];
+    set.n[c] = n[i];
+    set.vec[c] = ((uintptr_t)d[i] & 15) == 0;
+    const long long t = (n[i] + kScanTile - 1) / kScanTile;
+    tiles = t > tiles ? t : tiles;
+    bytes += 2.0 * sizeof(T) * (double)n[i];
+    ++c;
+  }
+  if (c == 0) return;
+  auto* state = (unsigned long long*)scratch;
+  if (!state_zero) cudaMemsetAsync(state, 0, sizeof(unsigned long long) * (tiles + 2) * c, st);
+  ::sbc::KProbe kp_("k_scan_lb", st, bytes);
+  k_scan_lb<T><<<dim3((unsigned)tiles, (unsigned)c), kScanThreads, 0, st>>>(set, state);
 }
 
 template <typename T>
@@ -394,6 +440,16 @@ bool scan_error_take() {
     cudaMemcpyToSymbol(g_scan_error, &z, sizeof(z));
   }
   return h != 0;
+}
+
+size_t scan_set_scratch_bytes(long long n_max, int count) {
+  return (size_t)count * (size_t)((n_max + kScanTile - 1) / kScanTile + 2) *
+             sizeof(unsigned long long) + 256;
+}
+
+void exclusive_scan_i32_set(int* const* d, const long long* n, int count, void* scratch,
+                            cudaStream_t st, bool state_zero) {
+  scan_set<int>(d, n, count, (int*)scratch, st, state_zero);
 }
 
 void exclusive_scan_i32(int* d, long long n, void* scratch, cudaStream_t st, bool state_zero) {
