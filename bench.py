@@ -192,14 +192,12 @@ KERNEL_BOUND = {
 # A capture on a smaller case of the same kernel is scaled by the units it
 # processed where the traffic grows in proportion (said in the source note).
 TRAFFIC = {
-    ("k_os_scatter_u64", "pair_1m_1m"): {
-        "bytes": 25078016 + 121088,
-        "source": "profiles/k_os_scatter_u64_pair_1m_1m.md (one pass of 2M keys: the 25 MB "
-                  "input from DRAM; the output stays in L2 for the next pass)"},
-    ("k_os_hist_u64", "pair_1m_1m"): {
-        "bytes": 16046336, "source": "profiles/k_os_hist_u64_pair_1m_1m.md"},
+    ("k_os_scatter_u32", "pair_1m_1m"): {
+        "bytes": 17076480 + 5888,
+        "source": "profiles/k_os_scatter_u32_pair_1m_1m.md (one pass of 2M 32-bit vertex keys: "
+                  "the 16 MB input from DRAM; the output stays in L2 for the next pass)"},
     ("k_pair_exact", "pair_1m_1m"): {
-        "bytes": 140120320 + 7214336, "source": "profiles/k_pair_exact_pair_1m_1m.md"},
+        "bytes": 163223808 + 11570432, "source": "profiles/k_pair_exact_pair_1m_1m.md"},
 }
 
 
@@ -230,15 +228,10 @@ def roofline_of(prof_b: dict, workload_name: str, fallback_bytes=None):
 # count their inputs and outputs once.
 def algorithmic_bytes(kernel: str, st: dict, launches: int):
     E = st["edges"]
-    P = 2 * E
     per = max(launches, 1)
     if kernel == "k_pair_exact":
         # the two edges' coordinates of every box-overlapping pair (64 B)
         return 64.0 * st["grid_pairs"] / per
-    if kernel == "k_os_scatter_u64":
-        return 24.0 * P  # read (key 8 + value 4) and write them once per pass
-    if kernel == "k_os_hist_u64":
-        return 8.0 * P
     if kernel == "k_find_leaves":
         return 16.0 * E + 8.0 * E
     if kernel == "k_edge_range":

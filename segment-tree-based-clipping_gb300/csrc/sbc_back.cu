@@ -525,10 +525,13 @@ __global__ void k_lr_ringlen(int cap, const int* __restrict__ nRings_p,
   rlen[r] = r < nRings ? (int)S[starts[r]] : 0;
 }
 
-// Segments longer than kSegPiece vertices are copied in pieces of that size
-// by k_lr_copy_long, one warp per piece: a ring stretch of 10^5 vertices
-// would otherwise keep one warp busy long after the others.
-constexpr int kSegPiece = 1024;
+// Segments of up to kSegInline vertices are copied by their own warp (so a
+// warp copies at most 32 x kSegInline vertices); longer ones are cut into
+// pieces of kSegPiece vertices that k_lr_copy_long copies one warp per piece.
+// Otherwise one warp holding long ring stretches would run long after the
+// others.
+constexpr int kSegInline = 32;
+constexpr int kSegPiece = 256;
 
 // the output placement of segment x (an enex vertex of a start's orbit)
 struct SegCopy {
@@ -551,6 +554,12 @@ __device__ __forceinline__ SegCopy seg_copy_of(const Trace& T, int x, const long
   return c;
 }
 
+// a piece of a long segment: its placement and steps [step0, step0 + count)
+struct SegPiece {
+  long long base;
+  int sx, m, step0, count, onP, fwd;
+};
+
 // vertex `step` (1-based) of a segment
 __device__ __forceinline__ void seg_copy_step(const SegCopy& c, int step, const double* ixB,
                                               const double* ixC, double* out) {
@@ -565,7 +574,7 @@ __global__ void k_lr_copy(Trace T, const int* __restrict__ nxt, const long long*
                           const int* __restrict__ ringI, const int* __restrict__ startPre,
                           const int* __restrict__ vOff, const double* __restrict__ ixB,
                           const double* __restrict__ ixC, double* __restrict__ out,
-                          int2* __restrict__ pieces, unsigned* __restrict__ npieces,
+                          SegPiece* __restrict__ pieces, unsigned* __restrict__ npieces,
                           long long pcap) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
@@ -576,12 +585,16 @@ __global__ void k_lr_copy(Trace T, const int* __restrict__ nxt, const long long*
   bool onP = false, fwd = false;
   if (mine) {
     const SegCopy c = seg_copy_of(T, x, S, ringI, startPre, vOff);
-    if (c.len > kSegPiece) {
+    if (c.len > kSegInline) {
       // to the long-segment queue, one entry per piece
       const int np = (c.len + kSegPiece - 1) / kSegPiece;
       const unsigned q = atomicAdd(npieces, (unsigned)np);
       for (int i = 0; i < np; ++i)
-        if (q + i < pcap) pieces[q + i] = make_int2(x, i);
+        if (q + i < pcap) {
+          const int s0 = i * kSegPiece + 1;
+          pieces[q + i] = SegPiece{c.base, c.sx, c.m, s0, min(kSegPiece, c.len - s0 + 1),
+                                   (int)c.onP, (int)c.fwd};
+        }
       mine = false;
     } else {
       base = c.base;
@@ -624,21 +637,16 @@ __global__ void k_lr_copy(Trace T, const int* __restrict__ nxt, const long long*
 }
 
 // the pieces of the long segments, one warp per piece
-__global__ void k_lr_copy_long(Trace T, const long long* __restrict__ S,
-                               const int* __restrict__ ringI, const int* __restrict__ startPre,
-                               const int* __restrict__ vOff, const double* __restrict__ ixB,
-                               const double* __restrict__ ixC, double* __restrict__ out,
-                               const int2* __restrict__ pieces,
+__global__ void k_lr_copy_long(const double* __restrict__ ixB, const double* __restrict__ ixC,
+                               double* __restrict__ out, const SegPiece* __restrict__ pieces,
                                const unsigned* __restrict__ npieces, long long pcap) {
   const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const long long np = min((long long)*npieces, pcap);
   for (long long i = w; i < np; i += ((long long)gridDim.x * blockDim.x) >> 5) {
-    const int2 pc = pieces[i];
-    const SegCopy c = seg_copy_of(T, pc.x, S, ringI, startPre, vOff);
-    const int s0 = pc.y * kSegPiece + 1;
-    const int s1 = min(c.len, s0 + kSegPiece - 1);
-    for (int step = s0 + lane; step <= s1; step += 32) seg_copy_step(c, step, ixB, ixC, out);
+    const SegPiece pc = pieces[i];
+    const SegCopy c{pc.base, 0, pc.m, pc.sx, pc.onP != 0, pc.fwd != 0};
+    for (int k = lane; k < pc.count; k += 32) seg_copy_step(c, pc.step0 + k, ixB, ixC, out);
   }
 }
 
@@ -1168,9 +1176,9 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
     const int nRings = *r_nr;
     const long long nv = *r_nv;
     double* rxy = (double*)bp.get("bk_rxy", sizeof(double) * 2 * (nv + 1));
-    // long-segment pieces: at most nv / kSegPiece + (segments above kSegPiece)
-    const long long pcap = 2 * nv / kSegPiece + 2;
-    auto* pieces = (int2*)bp.get("bk_pieces", sizeof(int2) * pcap);
+    // long-segment pieces: at most nv / kSegPiece + (segments above kSegInline)
+    const long long pcap = nv / kSegPiece + nv / kSegInline + 2;
+    auto* pieces = (SegPiece*)bp.get("bk_pieces", sizeof(SegPiece) * pcap);
     auto* npieces = (unsigned*)bp.get("bk_npieces", 256);
     if (bp.failed) return pl.fail(kENoMem, "device allocation failed (ring vertices)");
     cudaMemsetAsync(npieces, 0, sizeof(unsigned), st);
@@ -1184,8 +1192,7 @@ int run_backend(Pipeline& pl, const Merged& m, OverlayOut& out) {
       k_lr_copy_long<<<grid_for(((long long)pcap + 1) * 32, 256) < 1216u
                            ? grid_for(((long long)pcap + 1) * 32, 256)
                            : 1216u,
-                       256, 0, st>>>(T, SA, ringI, isStart, rlen, m.ixB, m.ixC, rxy, pieces,
-                                     npieces, pcap);
+                       256, 0, st>>>(m.ixB, m.ixC, rxy, pieces, npieces, pcap);
     }
     out.d_off = rlen;  // exclusive prefix of ring lengths, nRings+1 entries
     out.d_xy = rxy;

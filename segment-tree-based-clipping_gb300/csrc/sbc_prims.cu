@@ -238,6 +238,22 @@ void scan_multi(T* d, long long n, T* scratch, cudaStream_t st);
 constexpr unsigned long long kLbTotal = 1ull << 62, kLbPrefix = 2ull << 62;
 constexpr unsigned long long kLbMask = (1ull << 62) - 1;
 constexpr unsigned kLbSpin = 1u << 20;
+// Two-level look-back: tiles also add their totals into a word per group of
+// kScanGroup tiles (count in bits 56-61, sum below), and a group's last tile
+// marks the word with the group's inclusive prefix (bit 63).  A tile reads its
+// own group's tile words, then whole groups, 32 per round trip: when every
+// tile starts at once, the walk to tile 0 takes tiles / 1024 round trips
+// instead of tiles / 32.
+constexpr int kScanGroup = 32;
+constexpr unsigned long long kGrpInc = 1ull << 63, kGrpOne = 1ull << 56;
+constexpr unsigned long long kGrpMask = (1ull << 56) - 1;
+__host__ __device__ constexpr unsigned scan_groups(unsigned tiles) {
+  return (tiles + kScanGroup - 1) / kScanGroup;
+}
+// look-back words of one scan over `tiles` tiles: ticket, tiles, groups, done counter
+__host__ __device__ constexpr size_t scan_words(unsigned tiles) {
+  return (size_t)tiles + scan_groups(tiles) + 2;
+}
 __device__ unsigned g_scan_error = 0;
 
 // Up to kScanMulti independent arrays in one launch: blockIdx.y picks the
@@ -251,25 +267,27 @@ struct ScanSet {
   bool vec[kScanMulti];
 };
 
-template <typename T>
-__global__ void __launch_bounds__(kScanThreads)
-k_scan_lb(ScanSet<T> set, unsigned long long* __restrict__ state_all) {
+// One tile of a decoupled look-back scan over n values: load(base, v)
+// fetches the kScanItems values from position base (zero past n), store(base,
+// o) writes their exclusive prefix.  `state` holds scan_words(gridDim.x)
+// look-back words; T_ = gridDim.x tiles are launched.
+template <typename T, typename Load, typename Store>
+__device__ __forceinline__ void scan_tile_lb(Load load, Store store, long long n,
+                                             unsigned long long* __restrict__ state) {
   __shared__ T sw[32];
   __shared__ unsigned s_tile;
   __shared__ T s_prefix;
-  T* __restrict__ d = set.d[blockIdx.y];
-  const long long n = set.n[blockIdx.y];
-  const bool vec = set.vec[blockIdx.y];
-  unsigned long long* __restrict__ state = state_all + (size_t)blockIdx.y * (gridDim.x + 2);
+  const unsigned T_ = gridDim.x, G_ = scan_groups(gridDim.x);
   if (threadIdx.x == 0) s_tile = atomicAdd((unsigned*)state, 1u);
   __syncthreads();
   const unsigned tile = s_tile;
-  unsigned long long* ts = state + 1;
+  unsigned long long* ts = state + 1;         // tile words
+  unsigned long long* gs = state + 1 + T_;    // group words
   const long long ntiles = (n + kScanTile - 1) / kScanTile;
   if ((long long)tile < ntiles) {
     const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanItems;
     T v[kScanItems];
-    scan_load(d, base, n, vec, v);
+    load(base, v);
     T s = 0;
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) s += v[i];
@@ -277,37 +295,67 @@ k_scan_lb(ScanSet<T> set, unsigned long long* __restrict__ state_all) {
     const T ex = block_exclusive_scan<T>(s, sw, &tot);
     if (threadIdx.x < 32) {
       const int lane = threadIdx.x;
+      const long long g = tile / kScanGroup, g0 = g * kScanGroup;
+      // the group's aggregate first, then the tile's own word: whoever sees
+      // the tile word also sees its share of the group word
+      if (lane == 0) {
+        atomicAdd(&gs[g], kGrpOne | ((unsigned long long)tot & kGrpMask));
+        __threadfence();
+        atomicExch(&ts[tile], (tile == 0 ? kLbPrefix : kLbTotal) |
+                                  ((unsigned long long)tot & kLbMask));
+      }
       T prefix = 0;
-      if (tile == 0) {
-        if (lane == 0) atomicExch(&ts[0], kLbPrefix | ((unsigned long long)tot & kLbMask));
-      } else {
-        if (lane == 0) atomicExch(&ts[tile], kLbTotal | ((unsigned long long)tot & kLbMask));
-        long long top = (long long)tile - 1;
-        bool done = false;
-        while (!done) {
-          const long long j = top - lane;
-          unsigned long long w = kLbPrefix;  // before tile 0: nothing to add
-          if (j >= 0) {
+      if (tile > 0) {
+        // 1. the tiles of the own group before this one (one round trip)
+        const long long j = (long long)tile - 1 - lane;
+        unsigned long long w = 0;
+        if (j >= g0) {
+          unsigned spins = 0;
+          do {
+            w = *(volatile unsigned long long*)&ts[j];
+          } while ((w >> 62) == 0 && ++spins < kLbSpin);
+          if ((w >> 62) == 0) {
+            atomicOr(&g_scan_error, 1u);
+            w = kLbPrefix;
+          }
+        }
+        unsigned pm = __ballot_sync(0xffffffffu, j >= g0 && (w >> 62) == 2);
+        int firstP = pm ? __ffs(pm) - 1 : 32;
+        T val = (j >= g0 && lane <= firstP) ? (T)(w & kLbMask) : T(0);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+        prefix += val;
+        // 2. earlier groups, 32 per round trip, nearest first, until a
+        // group's inclusive prefix (or group 0)
+        bool done = pm != 0;
+        for (long long gt = g - 1; !done && gt >= 0; gt -= 32) {
+          const long long q = gt - lane;
+          unsigned long long x = 0;
+          if (q >= 0) {
             unsigned spins = 0;
             do {
-              w = *(volatile unsigned long long*)&ts[j];
-            } while ((w >> 62) == 0 && ++spins < kLbSpin);
-            if ((w >> 62) == 0) {
+              x = *(volatile unsigned long long*)&gs[q];
+            } while (!(x & kGrpInc) && (x >> 56) != (unsigned long long)kScanGroup &&
+                     ++spins < kLbSpin);
+            if (!(x & kGrpInc) && (x >> 56) != (unsigned long long)kScanGroup) {
               atomicOr(&g_scan_error, 1u);
-              w = kLbPrefix;
+              x = kGrpInc;
             }
           }
-          const unsigned pm = __ballot_sync(0xffffffffu, (w >> 62) == 2);
-          const int firstP = pm ? __ffs(pm) - 1 : 32;
-          T val = (lane <= firstP && j >= 0) ? (T)(w & kLbMask) : T(0);
+          pm = __ballot_sync(0xffffffffu, q >= 0 && (x & kGrpInc));
+          firstP = pm ? __ffs(pm) - 1 : 32;
+          val = (q >= 0 && lane <= firstP) ? (T)(x & kGrpMask) : T(0);
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
           prefix += val;
           done = pm != 0;
-          top -= 32;
         }
         if (lane == 0) atomicExch(&ts[tile], kLbPrefix | ((unsigned long long)(prefix + tot) & kLbMask));
       }
+      // the group's last tile publishes the group's inclusive prefix (every
+      // tile of the group has added to the group word: step 1 saw their words)
+      if (lane == 0 && ((long long)tile == g0 + kScanGroup - 1 || (long long)tile == ntiles - 1))
+        atomicExch(&gs[g], kGrpInc | ((unsigned long long)(prefix + tot) & kGrpMask));
       if (lane == 0) s_prefix = prefix;
     }
     __syncthreads();
@@ -318,20 +366,51 @@ k_scan_lb(ScanSet<T> set, unsigned long long* __restrict__ state_all) {
       o[i] = run;
       run += v[i];
     }
-    scan_store(d, base, n, vec, o);
+    store(base, o);
   }
-  // The last block to finish clears the look-back words (ticket, tile words,
-  // this counter) so the next scan on the same scratch needs no memset: a
-  // block counts itself done only after its own look-back reads, so when the
-  // count reaches the number of blocks nobody reads the words any more.
+  // The last block to finish clears the look-back words (ticket, tile and
+  // group words, this counter) so the next scan on the same scratch needs no
+  // memset: a block counts itself done only after its own look-back reads, so
+  // when the count reaches the number of blocks nobody reads the words any more.
   __shared__ bool s_last;
+  const unsigned last_word = T_ + G_ + 1;
   if (threadIdx.x == 0) {
     __threadfence();
-    s_last = atomicAdd(&state[gridDim.x + 1], 1ull) == (unsigned long long)gridDim.x - 1;
+    s_last = atomicAdd(&state[last_word], 1ull) == (unsigned long long)gridDim.x - 1;
   }
   __syncthreads();
   if (s_last)
-    for (unsigned i = threadIdx.x; i <= gridDim.x + 1; i += blockDim.x) state[i] = 0ull;
+    for (unsigned i = threadIdx.x; i <= last_word; i += blockDim.x) state[i] = 0ull;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_lb(ScanSet<T> set, unsigned long long* __restrict__ state_all) {
+  // the array of this blockIdx.y (selects, not an indexed parameter: that
+  // would copy the set to local memory)
+  const unsigned y = blockIdx.y;
+  T* __restrict__ d = y == 0 ? set.d[0] : y == 1 ? set.d[1] : y == 2 ? set.d[2] : set.d[3];
+  const long long n = y == 0 ? set.n[0] : y == 1 ? set.n[1] : y == 2 ? set.n[2] : set.n[3];
+  const bool vec = y == 0 ? set.vec[0] : y == 1 ? set.vec[1] : y == 2 ? set.vec[2] : set.vec[3];
+  scan_tile_lb<T>([&](long long base, T(&v)[kScanItems]) { scan_load(d, base, n, vec, v); },
+                  [&](long long base, const T(&o)[kScanItems]) { scan_store(d, base, n, vec, o); },
+                  n, state_all + (size_t)y * scan_words(gridDim.x));
+}
+
+// The exclusive scan of f(0..n-1) into out: a map kernel and the scan in one
+// launch (f reads its inputs at index i; out may be one of them only if f(i)
+// reads nothing but position i)
+template <typename T, typename F>
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_map(F f, T* __restrict__ out, long long n, unsigned long long* __restrict__ state) {
+  const bool vec = ((uintptr_t)out & 15) == 0;
+  scan_tile_lb<T>(
+      [&](long long base, T(&v)[kScanItems]) {
+#pragma unroll
+        for (int i = 0; i < kScanItems; ++i) v[i] = (base + i < n) ? f(base + i) : T(0);
+      },
+      [&](long long base, const T(&o)[kScanItems]) { scan_store(out, base, n, vec, o); }, n,
+      state);
 }
 
 template <typename T>
@@ -341,7 +420,8 @@ void scan_rec(T* d, long long n, T* scratch, cudaStream_t st, bool state_zero = 
   if (tiles > 1) {
     auto* state = (unsigned long long*)scratch;
     // the scan leaves its words zero; a scratch not known to start zero is cleared first
-    if (!state_zero) cudaMemsetAsync(state, 0, sizeof(unsigned long long) * (tiles + 2), st);
+    if (!state_zero)
+      cudaMemsetAsync(state, 0, sizeof(unsigned long long) * scan_words((unsigned)tiles), st);
     ScanSet<T> set{};
     set.d[0] = d;
     set.n[0] = n;
@@ -373,7 +453,8 @@ void scan_set(T* const* d, const long long* n, int count, T* scratch, cudaStream
   }
   if (c == 0) return;
   auto* state = (unsigned long long*)scratch;
-  if (!state_zero) cudaMemsetAsync(state, 0, sizeof(unsigned long long) * (tiles + 2) * c, st);
+  if (!state_zero)
+    cudaMemsetAsync(state, 0, sizeof(unsigned long long) * scan_words((unsigned)tiles) * c, st);
   ::sbc::KProbe kp_("k_scan_lb", st, bytes);
   k_scan_lb<T><<<dim3((unsigned)tiles, (unsigned)c), kScanThreads, 0, st>>>(set, state);
 }
@@ -404,7 +485,8 @@ void scan_multi(T* d, long long n, T* scratch, cudaStream_t st) {
 }  // namespace
 
 size_t scan_scratch_bytes(long long n) {
-  const size_t lb = (size_t)((n + kScanTile - 1) / kScanTile + 2) * sizeof(unsigned long long);
+  const unsigned tiles = (unsigned)((n + kScanTile - 1) / kScanTile);
+  const size_t lb = scan_words(tiles > 0 ? tiles : 1) * sizeof(unsigned long long);
   size_t tot = 0;
   while (n > kScanTile) {
     long long nb = (n + kScanTile - 1) / kScanTile;
@@ -443,8 +525,8 @@ bool scan_error_take() {
 }
 
 size_t scan_set_scratch_bytes(long long n_max, int count) {
-  return (size_t)count * (size_t)((n_max + kScanTile - 1) / kScanTile + 2) *
-             sizeof(unsigned long long) + 256;
+  const unsigned tiles = (unsigned)((n_max + kScanTile - 1) / kScanTile);
+  return (size_t)count * scan_words(tiles > 0 ? tiles : 1) * sizeof(unsigned long long) + 256;
 }
 
 void exclusive_scan_i32_set(int* const* d, const long long* n, int count, void* scratch,
@@ -610,10 +692,16 @@ k_os_scatter(K* __restrict__ ka, unsigned* __restrict__ va, K* __restrict__ kb,
   __shared__ int s_skip, s_odd;
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const int pos = plan.pos[q];
-  unsigned long long* cur = look + (size_t)(q & 1) * tiles * 256;
-  unsigned long long* nxt = look + (size_t)((q + 1) & 1) * tiles * 256;
+  // per pass parity: tile words (tiles x 256), then group words (groups x 256)
+  const long long groups = (tiles + kScanGroup - 1) / kScanGroup;
+  unsigned long long* cur = look + (size_t)(q & 1) * (tiles + groups) * 256;
+  unsigned long long* nxt = look + (size_t)((q + 1) & 1) * (tiles + groups) * 256;
+  unsigned long long* gcur = cur + (size_t)tiles * 256;
   // the next pass's look-back words (not read by this pass)
-  if (q + 1 < plan.npass) nxt[(size_t)blockIdx.x * 256 + t] = 0ull;
+  if (q + 1 < plan.npass) {
+    nxt[(size_t)blockIdx.x * 256 + t] = 0ull;
+    if (blockIdx.x < groups) nxt[(size_t)(tiles + blockIdx.x) * 256 + t] = 0ull;
+  }
   if (w == 0) {
     int ran = 0;
     for (int p = 0; p < q; ++p) ran += os_constant(hist, p, n) ? 0 : 1;
@@ -666,6 +754,10 @@ k_os_scatter(K* __restrict__ ka, unsigned* __restrict__ va, K* __restrict__ kb,
     cnt += c;
   }
   unsigned long long* row = cur + (size_t)tile * 256;
+  const long long grp = tile / kScanGroup, g0 = grp * kScanGroup;
+  // the group's count first, then the tile's own word (see k_scan_lb)
+  atomicAdd(&gcur[(size_t)grp * 256 + t], kGrpOne | (unsigned long long)cnt);
+  __threadfence();
   atomicExch(&row[t], (tile == 0 ? kOsInc : kOsAgg) | (unsigned long long)cnt);
   // the digit's global start, and its start inside the tile
   const unsigned long long gstart = os_block_scan<unsigned long long>(hist[q * 256 + t], s_wscan);
@@ -682,26 +774,26 @@ k_os_scatter(K* __restrict__ ka, unsigned* __restrict__ va, K* __restrict__ kb,
       s_v[lp] = v[r];
     }
   }
-  // decoupled look-back over the earlier tiles for digit t: a window of
-  // kOsLook words per round trip, nearest first, until a tile's inclusive
-  // prefix (bounded waits on words not yet published)
+  // decoupled look-back for digit t in two levels (see k_scan_lb): the
+  // tiles of the own group before this one, nearest first, until a tile's
+  // inclusive prefix; then whole groups, kOsLook per round trip, until a
+  // group's inclusive prefix or group 0.  Every wait is bounded.
   unsigned long long excl = 0;
   if (tile > 0) {
-    long long j = tile - 1;
     bool done = false;
-    while (!done) {
-      unsigned long long wv[kOsLook];
+    {
+      unsigned long long wv[kScanGroup];
 #pragma unroll
-      for (int u = 0; u < kOsLook; ++u)
-        wv[u] = (j - u >= 0) ? __ldcg(&cur[(size_t)(j - u) * 256 + t]) : kOsInc;
+      for (int u = 0; u < kScanGroup; ++u)
+        wv[u] = (tile - 1 - u >= g0) ? __ldcg(&cur[(size_t)(tile - 1 - u) * 256 + t]) : 0ull;
 #pragma unroll
-      for (int u = 0; u < kOsLook; ++u) {
-        if (!done) {
+      for (int u = 0; u < kScanGroup; ++u) {
+        if (!done && tile - 1 - u >= g0) {
           unsigned long long x = wv[u];
           if ((x >> 62) == 0) {
             unsigned spins = 0;
             do {
-              x = *(volatile unsigned long long*)&cur[(size_t)(j - u) * 256 + t];
+              x = *(volatile unsigned long long*)&cur[(size_t)(tile - 1 - u) * 256 + t];
             } while ((x >> 62) == 0 && ++spins < kLbSpin);
             if ((x >> 62) == 0) {
               atomicOr(&g_scan_error, 2u);
@@ -712,10 +804,39 @@ k_os_scatter(K* __restrict__ ka, unsigned* __restrict__ va, K* __restrict__ kb,
           if ((x >> 62) == 2) done = true;
         }
       }
-      j -= kOsLook;
+    }
+    for (long long gt = grp - 1; !done && gt >= 0; gt -= kOsLook) {
+      unsigned long long wv[kOsLook];
+#pragma unroll
+      for (int u = 0; u < kOsLook; ++u)
+        wv[u] = (gt - u >= 0) ? __ldcg(&gcur[(size_t)(gt - u) * 256 + t]) : kGrpInc;
+#pragma unroll
+      for (int u = 0; u < kOsLook; ++u) {
+        if (!done) {
+          unsigned long long x = wv[u];
+          auto ready = [](unsigned long long y) {
+            return (y & kGrpInc) || (y >> 56) == (unsigned long long)kScanGroup;
+          };
+          if (!ready(x)) {
+            unsigned spins = 0;
+            do {
+              x = *(volatile unsigned long long*)&gcur[(size_t)(gt - u) * 256 + t];
+            } while (!ready(x) && ++spins < kLbSpin);
+            if (!ready(x)) {
+              atomicOr(&g_scan_error, 2u);
+              x = kGrpInc;
+            }
+          }
+          excl += x & kGrpMask;
+          if (x & kGrpInc) done = true;
+        }
+      }
     }
     atomicExch(&row[t], kOsInc | ((excl + cnt) & kOsMask));
   }
+  // the group's last tile: the group's inclusive prefix for digit t
+  if (tile == g0 + kScanGroup - 1 || tile == tiles - 1)
+    atomicExch(&gcur[(size_t)grp * 256 + t], kGrpInc | ((excl + cnt) & kGrpMask));
   s_gbase[t] = gstart + excl;
   __syncthreads();
   // out: each digit's keys to consecutive positions
@@ -750,6 +871,7 @@ __global__ void k_os_final(K* __restrict__ ka, unsigned* __restrict__ va, const 
 }
 
 long long os_tiles(long long n) { return (n + kOsTile - 1) / kOsTile; }
+long long os_groups(long long tiles) { return (tiles + kScanGroup - 1) / kScanGroup; }
 
 // the scatter's dynamic shared memory (with its static part above 48 KB)
 // needs an opt-in, once per device
@@ -784,7 +906,8 @@ void onesweep(K* keys, unsigned* vals, K* keys_tmp, unsigned* vals_tmp, long lon
     long long g = (n + (long long)kOsThreads * kOsHistItems - 1) / ((long long)kOsThreads * kOsHistItems);
     if (g > 152 * 8) g = 152 * 8;
     ::sbc::KProbe kp_(sizeof(K) == 8 ? "k_os_hist_u64" : "k_os_hist_u32", st, (double)sizeof(K) * n);
-    k_os_hist<K><<<(unsigned)g, kOsThreads, 0, st>>>(keys, n, plan, hist, look, tiles * 256);
+    k_os_hist<K><<<(unsigned)g, kOsThreads, 0, st>>>(keys, n, plan, hist, look,
+                                                     (tiles + os_groups(tiles)) * 256);
   }
   os_smem_optin<K>();
   for (int q = 0; q < plan.npass; ++q) {
@@ -805,7 +928,8 @@ void onesweep(K* keys, unsigned* vals, K* keys_tmp, unsigned* vals_tmp, long lon
 
 size_t radix_scratch_bytes(long long n) {
   const long long tiles = os_tiles(n > 1 ? n : 1);
-  return kOsHistBytes + kOsCtrBytes + (size_t)2 * tiles * 256 * sizeof(unsigned long long) + 256;
+  return kOsHistBytes + kOsCtrBytes +
+         (size_t)2 * (tiles + os_groups(tiles)) * 256 * sizeof(unsigned long long) + 256;
 }
 
 void radix_sort_u32(unsigned* keys, unsigned* vals, unsigned* keys_tmp, unsigned* vals_tmp,
