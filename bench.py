@@ -192,10 +192,13 @@ KERNEL_BOUND = {
 # A capture on a smaller case of the same kernel is scaled by the units it
 # processed where the traffic grows in proportion (said in the source note).
 TRAFFIC = {
+    # a radix pass moves 16 algorithmic bytes per key; the capture is a pass
+    # of the 2M vertex keys (32 MB algorithmic), scaled to the average launch
     ("k_os_scatter_u32", "pair_1m_1m"): {
-        "bytes": 17076480 + 5888,
+        "per_algorithmic_byte": (17076480 + 5888) / 32.0e6,
         "source": "profiles/k_os_scatter_u32_pair_1m_1m.md (one pass of 2M 32-bit vertex keys: "
-                  "the 16 MB input from DRAM; the output stays in L2 for the next pass)"},
+                  "the 16 MB input from DRAM, the output left in L2 for the next pass; scaled "
+                  "to the launch's keys)"},
     ("k_pair_exact", "pair_1m_1m"): {
         "bytes": 163223808 + 11570432, "source": "profiles/k_pair_exact_pair_1m_1m.md"},
 }
@@ -212,10 +215,15 @@ def roofline_of(prof_b: dict, workload_name: str, fallback_bytes=None):
     ab = by / max(n_l, 1) if by else (fallback_bytes(name, n_l) if fallback_bytes else None)
     achieved = ab / (per_ms * 1e-3) / 1e9 if ab else None
     tr = TRAFFIC.get((name, workload_name))
+    traffic = None
+    if tr and "bytes" in tr:
+        traffic = tr["bytes"]
+    elif tr and ab:
+        traffic = tr["per_algorithmic_byte"] * ab
     return {"kernel": name, "bound": KERNEL_BOUND.get(name, "hbm"), "achieved": achieved,
             "peak": pk["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / pk["hbm_gbs"] if achieved else None,
-            "traffic": tr["bytes"] if tr else None,
+            "traffic": traffic,
             "traffic_source": tr["source"] if tr else None,
             "algorithmic_bytes_per_launch": ab, "ms_per_launch": per_ms,
             "share_of_step": tot_ms / max(sum(v[0] for v in prof_b.values()), 1e-9),

@@ -58,7 +58,15 @@ int Pipeline::run(const double* d_bxy, int nb_, const double* d_cxy, const int* 
         // no worker thread: the same steps on this thread, before the tree
         side_rc = side_task();
         if (side_rc) rc = fail(side_rc, side_err_.empty() ? err_ : side_err_);
+      } else if (profiling_on()) {
+        side_rc = side_.wait();
+        side_posted = false;
+        if (side_rc) rc = fail(side_rc, side_err_);
       }
+      // per-kernel times: while profiling, the side stream's work finishes
+      // before the tree stages start, so no two launches share the GPU and
+      // each launch's events time it alone
+      if (profiling_on()) cudaStreamSynchronize(st2_);
     }
   }
   mark(1);

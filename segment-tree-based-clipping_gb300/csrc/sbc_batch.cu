@@ -819,6 +819,11 @@ struct ClipArgs {
   double* area;
   int unite;            // union instead of intersection
   int maxv;             // the small/large split: larger polygons go to the pair pipeline
+  // pairs by decreasing vertex count: thread (or warp) t clips pair order[t],
+  // so the pairs a warp runs side by side are of like size and their loops
+  // diverge less (null: pair t)
+  const int* order;
+  __device__ int pair_of(int t) const { return order ? order[t] : t; }
   __device__ bool small(int p, int* nb, int* nc) const {
     *nb = (int)(boff[p + 1] - boff[p]);
     *nc = (int)(coff[p + 1] - coff[p]);
@@ -832,8 +837,9 @@ struct ClipArgs {
 };
 
 __global__ void __launch_bounds__(kBatchBlock) k_batch_front(ClipArgs A) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= A.np) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= A.np) return;
+  const int p = A.pair_of(t);
   const int pass = A.pass_of ? A.pass_of[p] : 0;
   if (pass < 0) return;  // settled in an earlier pass, or a large pair
   int nb, nc;
@@ -856,8 +862,9 @@ __global__ void __launch_bounds__(kBatchBlock) k_batch_front(ClipArgs A) {
 
 __global__ void __launch_bounds__(128) k_batch_cand(ClipArgs A) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int p = (int)(t >> 5), lane = threadIdx.x & 31;
-  if (p >= A.np) return;
+  const int lane = threadIdx.x & 31;
+  if ((t >> 5) >= A.np) return;
+  const int p = A.pair_of((int)(t >> 5));
   const int pass = A.pass_of ? A.pass_of[p] : 0;
   int nb, nc;
   if (pass < 0 || !A.small(p, &nb, &nc)) return;
@@ -868,8 +875,9 @@ __global__ void __launch_bounds__(128) k_batch_cand(ClipArgs A) {
 }
 
 __global__ void __launch_bounds__(kBatchBlock) k_batch_back(ClipArgs A) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= A.np) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= A.np) return;
+  const int p = A.pair_of(t);
   const int pass = A.pass_of ? A.pass_of[p] : 0;
   int nb, nc;
   if (pass < 0 || !A.small(p, &nb, &nc)) return;
@@ -1237,6 +1245,24 @@ int BatchRunner::plan(int np_, const long long* d_boff, const long long* d_coff,
     chunks_.push_back({p0, lo});
     p0 = lo;
   }
+  // within each chunk, its pairs by decreasing vertex count (stable): the
+  // order the clip kernels hand pairs to threads and warps
+  order_ = (int*)pool.get("bt_order", sizeof(int) * (np + 1));
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch)");
+  h_order_.resize(np);
+  for (const auto& ch : chunks_) {
+    int* o = h_order_.data() + ch.first;
+    const int n = ch.second - ch.first;
+    for (int i = 0; i < n; ++i) o[i] = i;
+    std::stable_sort(o, o + n, [&](int a, int b) {
+      const long long pa = ch.first + a, pb = ch.first + b;
+      const long long sa = h_boff_[pa + 1] - h_boff_[pa] + h_coff_[pa + 1] - h_coff_[pa];
+      const long long sb = h_boff_[pb + 1] - h_boff_[pb] + h_coff_[pb + 1] - h_coff_[pb];
+      return sa > sb;
+    });
+  }
+  cudaMemcpyAsync(order_, h_order_.data(), sizeof(int) * np, cudaMemcpyHostToDevice, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch order");
   resident_ = -1;
   return kOk;
 }
@@ -1265,7 +1291,7 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
       16.0 * (double)(h_boff_[p1] - h_boff_[p0] + h_coff_[p1] - h_coff_[p0]);
   launch_clip(ClipArgs{n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[0], aoff[0] + p0,
                        abase_[0], need_ + p0, need_ + p0, status + p0, nrings + p0, nverts + p0,
-                       area + p0, unite ? 1 : 0, split},
+                       area + p0, unite ? 1 : 0, split, order_ + p0},
               shape, in_bytes, st);
   std::vector<int> hs(n);
   cudaMemcpyAsync(hs.data(), status + p0, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
@@ -1295,7 +1321,7 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
     if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch arena)");
     launch_clip(ClipArgs{n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[1],
                          aoff[1] + p0, 0, need_ + p0, need_ + p0, status + p0, nrings + p0,
-                         nverts + p0, area + p0, unite ? 1 : 0, split},
+                         nverts + p0, area + p0, unite ? 1 : 0, split, order_ + p0},
                 shape, in_bytes, st);
   }
   // where each pair's data lives now: pass 0 arena, retry arena, or none
@@ -1623,11 +1649,13 @@ int BatchRunner::graph_record(int np_, const double* d_bxy, const long long* d_b
   cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     launch_clip(ClipArgs{np, d_bxy, d_boff, d_cxy, d_coff, pass0, arena[0], aoff[0], abase_[0],
-                         need_scr, need_rec, status, nrings, nverts, area, unite ? 1 : 0, split},
+                         need_scr, need_rec, status, nrings, nverts, area, unite ? 1 : 0, split,
+                         order_},
                 shape, in_bytes, st);
     if (retry)
       launch_clip(ClipArgs{np, d_bxy, d_boff, d_cxy, d_coff, pass1, arena[1], aoff[1], 0, need_scr,
-                           need_rec, status, nrings, nverts, area, unite ? 1 : 0, split},
+                           need_rec, status, nrings, nverts, area, unite ? 1 : 0, split,
+                           order_},
                   shape, in_bytes, st);
     const Arenas ar{arena[0], aoff[0], abase_[0], arena[1], aoff[1], 0, pass, need_rec};
     {

@@ -281,6 +281,7 @@ struct KProbe {
 };
 void profile_begin();
 // per-launch events stay out of a graph being captured
+bool profiling_on();
 bool profiling_suspend();
 void profiling_restore(bool on);
 // aggregated per kernel name: returns the number of distinct kernels

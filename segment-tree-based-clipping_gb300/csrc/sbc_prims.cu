@@ -60,6 +60,8 @@ KProbe::~KProbe() {
   cudaEventRecord(g_recs[slot_].b, st_);
 }
 
+bool profiling_on() { return g_prof_on; }
+
 bool profiling_suspend() {
   const bool on = g_prof_on;
   g_prof_on = false;
