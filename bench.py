@@ -185,6 +185,7 @@ KERNEL_BOUND = {
     "k_grid_warp": "latency", "k_grid_small": "latency", "k_lr_jump": "latency",
     "k_tr_jump": "latency", "k_alpha_sort": "latency", "k_batch_back": "latency",
     "k_batch_front": "latency", "k_pw_pairs": "latency", "k_dedup": "latency",
+    "k_batch_labels": "fp64", "k_batch_back2": "latency",
 }
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of

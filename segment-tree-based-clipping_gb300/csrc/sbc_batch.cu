@@ -72,6 +72,7 @@ struct PairWork {
   // hits
   int *hb, *hc, *ht, *hord, *htmp;
   unsigned long long* hkey;
+  double *hal, *hbt;  // lineSegmentIntersection's alpha and beta of each hit
   // counts, order, records
   int *bAll, *bND, *cAll, *cND, *cfill, *csorted;
   double* isxy;
@@ -126,6 +127,8 @@ __host__ __device__ __forceinline__ PairWork carve(Carver& cv, const Caps& c) {
   w.hord = cv.take<int>(K);
   w.htmp = cv.take<int>(K);
   w.hkey = cv.take<unsigned long long>(K);
+  w.hal = cv.take<double>(K);
+  w.hbt = cv.take<double>(K);
   w.bAll = cv.take<int>(c.nb + 1);
   w.bND = cv.take<int>(c.nb + 1);
   w.cAll = cv.take<int>(c.nc + 1);
@@ -419,6 +422,8 @@ __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc,
             w.hc[k] = 2 * j;
             w.ht[k] = ty;
             w.hkey[k] = key;
+            w.hal[k] = al;
+            w.hbt[k] = bt;
           }
         }
       }
@@ -431,8 +436,9 @@ __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc,
   }
 }
 
-__device__ PairResult clip_pair_back(const double* b, int nb, const double* c, int nc,
-                                     const Caps& cp, PairWork& w, int unite) {
+// A9-A13: records, counts, alpha order, merged arrays (one thread per pair)
+__device__ PairResult clip_pair_back1(const double* b, int nb, const double* c, int nc,
+                                      const Caps& cp, PairWork& w) {
   PairResult res{PS_OK, 0, 0, 0.0, 0};
   const int K = w.state[2];
   if (K > cp.K) {
@@ -484,15 +490,17 @@ __device__ PairResult clip_pair_back(const double* b, int nb, const double* c, i
     w.csorted[w.cAll[ec] + w.cfill[ec]++] = i;
   }
   const int nB = nb + w.bND[nb], nQ = nc + w.cND[nc];
-  // ---- A11 records (saveIntersectionsParallel, :7257-7341)
+  // ---- A11 records (saveIntersectionsParallel, :7257-7341): the type,
+  // alpha and beta the candidate stage's lineSegmentIntersection found (FP64
+  // work on one thread per pair costs its issue slots for a whole warp)
   for (int i = 0; i < K; ++i) {
-    const int bi = ub[i] >> 1, ci = uc[i] >> 1;
+    const int bi = ub[i] >> 1;
     const double p1x = bvx(b, nb, bi), p1y = bvy(b, nb, bi);
     const double p2x = bvx(b, nb, bi + 1), p2y = bvy(b, nb, bi + 1);
-    const double q1x = bvx(c, nc, ci), q1y = bvy(c, nc, ci);
-    const double q2x = bvx(c, nc, ci + 1), q2y = bvy(c, nc, ci + 1);
-    double al = 0.0, bt = 0.0;
-    const int ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
+    const double q1x = bvx(c, nc, uc[i] >> 1), q1y = bvy(c, nc, uc[i] >> 1);
+    const int h = w.hord[i];
+    const double al = w.hal[h], bt = w.hbt[h];
+    const int ty = ut[i];
     double x = 0.0, y = 0.0;
     if (ty == 1) {
       const double oma = dsub(1.0, al);
@@ -615,9 +623,20 @@ __device__ PairResult clip_pair_back(const double* b, int nb, const double* c, i
     w.nbB[w.bNI[i]] = w.cNI[i] + 1;
     w.nbC[w.cNI[i]] = w.bNI[i] + 1;
   }
-  // ---- A14 initial labels (calculateInitLabelParallel, :7925-7988)
-  for (int q = 0; q < nQ; ++q) w.cWin[q] = -1;
-  for (int i = 0; i < nB; ++i) {
+  return res;
+}
+
+// ---- A14 initial labels (calculateInitLabelParallel, :7925-7988), one warp
+// per pair, a slot per lane: the orientation tests are FP64, and FP64 run
+// by one thread of a warp costs the issue slots of all 32.  Reads the merged
+// arrays clip_pair_back1 left in the arena; PS_UNDEF where the reference's
+// behaviour is undefined.
+__device__ int clip_pair_labels(int nb, int nc, PairWork& w, int lane) {
+  const int nB = nb + w.bND[nb], nQ = nc + w.cND[nc];
+  for (int q = lane; q < nQ; q += 32) w.cWin[q] = -1;
+  __syncwarp();
+  bool bad = false;
+  for (int i = lane; i < nB; i += 32) {
     w.labB[i] = 0;
     if (w.alB[i] == -100) continue;
     const double cx = w.ixB[2 * i], cy = w.ixB[2 * i + 1];
@@ -629,13 +648,17 @@ __device__ PairResult clip_pair_back(const double* b, int nb, const double* c, i
     const int pPN = w.alB[tp] != -100 ? w.nbB[tp] - 1 : -100;
     const int nId = w.nbB[i] - 1;
     int qt[2];
-    for (int side = 0; side < 2; ++side) {
+    double s3 = 0.0;
+    bool have_s3 = false;
+    bool skip = false;
+    for (int side = 0; side < 2 && !skip; ++side) {
       int q = side == 0 ? nId - 1 : nId + 1;
       if (q == nQ) q = 0;
       else if (q == -1) q = nQ - 1;
       if (q < 0 || q >= nQ) {
-        res.status = PS_UNDEF;
-        return res;
+        bad = true;
+        skip = true;
+        break;
       }
       const double qx = w.ixC[2 * q], qy = w.ixC[2 * q + 1];
       int r;
@@ -644,12 +667,16 @@ __device__ PairResult clip_pair_back(const double* b, int nb, const double* c, i
       else {
         const double s1 = area3(qx, qy, pmx, pmy, cx, cy);
         const double s2 = area3(qx, qy, cx, cy, ppx, ppy);
-        const double s3 = area3(pmx, pmy, cx, cy, ppx, ppy);
+        if (!have_s3) {
+          s3 = area3(pmx, pmy, cx, cy, ppx, ppy);
+          have_s3 = true;
+        }
         if (s3 > 0) r = (s1 > 0 && s2 > 0) ? 0 : 1;
         else r = (s1 < 0 && s2 < 0) ? 1 : 0;
       }
       qt[side] = r;
     }
+    if (skip) continue;
     const int qm = qt[0], qp = qt[1];
     int lab;
     if ((qm == 0 && qp == 1) || (qm == 1 && qp == 0)) lab = 1;
@@ -662,12 +689,27 @@ __device__ PairResult clip_pair_back(const double* b, int nb, const double* c, i
     else lab = -102;
     w.labB[i] = lab;
     if (nId < 0 || nId >= nQ) {
-      res.status = PS_UNDEF;
-      return res;
+      bad = true;
+      continue;
     }
-    w.cWin[nId] = max(w.cWin[nId], i);
+    atomicMax(&w.cWin[nId], i);
   }
-  for (int q = 0; q < nQ; ++q) w.labC[q] = w.cWin[q] >= 0 ? w.labB[w.cWin[q]] : 0;
+  if (__any_sync(0xffffffffu, bad)) return PS_UNDEF;
+  __syncwarp();
+  for (int q = lane; q < nQ; q += 32) w.labC[q] = w.cWin[q] >= 0 ? w.labB[w.cWin[q]] : 0;
+  __syncwarp();
+  return PS_OK;
+}
+
+// A15-A18 and the rings out, from the labelled merged arrays
+__device__ PairResult clip_pair_back2(const double* b, int nb, const double* c, int nc,
+                                      const Caps& cp, PairWork& w, int unite) {
+  PairResult res{PS_OK, 0, 0, 0.0, 0};
+  const int nB = nb + w.bND[nb], nQ = nc + w.cND[nc];
+  // the record arrays clip_pair_back1 left: ub/uc in record order, ut
+  const int* ub = w.htmp;
+  const int* uc = w.skey;
+  const int* ut = w.ht;
   // ---- A15-A18 linked-list back end
   SerialArgs a;
   a.P = w.P;
@@ -819,11 +861,6 @@ struct ClipArgs {
   double* area;
   int unite;            // union instead of intersection
   int maxv;             // the small/large split: larger polygons go to the pair pipeline
-  // pairs by decreasing vertex count: thread (or warp) t clips pair order[t],
-  // so the pairs a warp runs side by side are of like size and their loops
-  // diverge less (null: pair t)
-  const int* order;
-  __device__ int pair_of(int t) const { return order ? order[t] : t; }
   __device__ bool small(int p, int* nb, int* nc) const {
     *nb = (int)(boff[p + 1] - boff[p]);
     *nc = (int)(coff[p + 1] - coff[p]);
@@ -839,7 +876,7 @@ struct ClipArgs {
 __global__ void __launch_bounds__(kBatchBlock) k_batch_front(ClipArgs A) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= A.np) return;
-  const int p = A.pair_of(t);
+  const int p = t;
   const int pass = A.pass_of ? A.pass_of[p] : 0;
   if (pass < 0) return;  // settled in an earlier pass, or a large pair
   int nb, nc;
@@ -864,7 +901,7 @@ __global__ void __launch_bounds__(128) k_batch_cand(ClipArgs A) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   if ((t >> 5) >= A.np) return;
-  const int p = A.pair_of((int)(t >> 5));
+  const int p = (int)(t >> 5);
   const int pass = A.pass_of ? A.pass_of[p] : 0;
   int nb, nc;
   if (pass < 0 || !A.small(p, &nb, &nc)) return;
@@ -874,10 +911,50 @@ __global__ void __launch_bounds__(128) k_batch_cand(ClipArgs A) {
   clip_pair_cand(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w, lane);
 }
 
+// The back end in three kernels: A9-A13 on one thread per pair, the labels
+// on one warp per pair, A15-A18 on one thread per pair.  w.state[0] carries
+// a pair's failure from one to the next.
+__device__ void batch_fail(const ClipArgs& A, int p, PairWork& w, int st, int need) {
+  A.status[p] = st == PS_UNDEF ? SBC_EUNDEF : SBC_ENOMEM;
+  if (st == PS_CAP) A.need[p] = need;
+  A.nrings[p] = A.nverts[p] = 0;
+  A.area[p] = 0.0;
+  w.state[0] = st;
+}
+
 __global__ void __launch_bounds__(kBatchBlock) k_batch_back(ClipArgs A) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= A.np) return;
-  const int p = A.pair_of(t);
+  const int p = t;
+  const int pass = A.pass_of ? A.pass_of[p] : 0;
+  int nb, nc;
+  if (pass < 0 || !A.small(p, &nb, &nc)) return;
+  Caps cp;
+  PairWork w = A.work(p, nb, nc, pass, &cp);
+  if (w.state[0] != PS_OK) return;
+  const PairResult r = clip_pair_back1(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w);
+  if (r.status != PS_OK) batch_fail(A, p, w, r.status, r.need);
+}
+
+__global__ void __launch_bounds__(128) k_batch_labels(ClipArgs A) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  if ((t >> 5) >= A.np) return;
+  const int p = (int)(t >> 5);
+  const int pass = A.pass_of ? A.pass_of[p] : 0;
+  int nb, nc;
+  if (pass < 0 || !A.small(p, &nb, &nc)) return;
+  Caps cp;
+  PairWork w = A.work(p, nb, nc, pass, &cp);
+  if (w.state[0] != PS_OK) return;
+  const int st = clip_pair_labels(nb, nc, w, lane);
+  if (st != PS_OK && lane == 0) batch_fail(A, p, w, st, 0);
+}
+
+__global__ void __launch_bounds__(kBatchBlock) k_batch_back2(ClipArgs A) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= A.np) return;
+  const int p = t;
   const int pass = A.pass_of ? A.pass_of[p] : 0;
   int nb, nc;
   if (pass < 0 || !A.small(p, &nb, &nc)) return;
@@ -885,7 +962,7 @@ __global__ void __launch_bounds__(kBatchBlock) k_batch_back(ClipArgs A) {
   PairWork w = A.work(p, nb, nc, pass, &cp);
   if (w.state[0] != PS_OK) return;
   const PairResult r =
-      clip_pair_back(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w, A.unite);
+      clip_pair_back2(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w, A.unite);
   A.status[p] = r.status == PS_OK ? SBC_OK : (r.status == PS_UNDEF ? SBC_EUNDEF : SBC_ENOMEM);
   if (r.status == PS_CAP) A.need[p] = r.need;
   A.nrings[p] = r.nrings;
@@ -915,8 +992,16 @@ void launch_clip(const ClipArgs& A, const BatchShape& sh, double in_bytes, cudaS
     k_batch_cand<<<grid_for(32LL * A.np, sh.cand), sh.cand, 0, st>>>(A);
   }
   {
-    ::sbc::KProbe kp_("k_batch_back", st, in_bytes + 20.0 * A.np);
+    ::sbc::KProbe kp_("k_batch_back", st, in_bytes);
     k_batch_back<<<grid_for(A.np, sh.back), sh.back, 0, st>>>(A);
+  }
+  {
+    ::sbc::KProbe kp_("k_batch_labels", st, in_bytes);
+    k_batch_labels<<<grid_for(32LL * A.np, 128), 128, 0, st>>>(A);
+  }
+  {
+    ::sbc::KProbe kp_("k_batch_back2", st, in_bytes + 20.0 * A.np);
+    k_batch_back2<<<grid_for(A.np, sh.back), sh.back, 0, st>>>(A);
   }
 }
 
@@ -1245,24 +1330,6 @@ int BatchRunner::plan(int np_, const long long* d_boff, const long long* d_coff,
     chunks_.push_back({p0, lo});
     p0 = lo;
   }
-  // within each chunk, its pairs by decreasing vertex count (stable): the
-  // order the clip kernels hand pairs to threads and warps
-  order_ = (int*)pool.get("bt_order", sizeof(int) * (np + 1));
-  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch)");
-  h_order_.resize(np);
-  for (const auto& ch : chunks_) {
-    int* o = h_order_.data() + ch.first;
-    const int n = ch.second - ch.first;
-    for (int i = 0; i < n; ++i) o[i] = i;
-    std::stable_sort(o, o + n, [&](int a, int b) {
-      const long long pa = ch.first + a, pb = ch.first + b;
-      const long long sa = h_boff_[pa + 1] - h_boff_[pa] + h_coff_[pa + 1] - h_coff_[pa];
-      const long long sb = h_boff_[pb + 1] - h_boff_[pb] + h_coff_[pb + 1] - h_coff_[pb];
-      return sa > sb;
-    });
-  }
-  cudaMemcpyAsync(order_, h_order_.data(), sizeof(int) * np, cudaMemcpyHostToDevice, st);
-  if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch order");
   resident_ = -1;
   return kOk;
 }
@@ -1291,7 +1358,7 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
       16.0 * (double)(h_boff_[p1] - h_boff_[p0] + h_coff_[p1] - h_coff_[p0]);
   launch_clip(ClipArgs{n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[0], aoff[0] + p0,
                        abase_[0], need_ + p0, need_ + p0, status + p0, nrings + p0, nverts + p0,
-                       area + p0, unite ? 1 : 0, split, order_ + p0},
+                       area + p0, unite ? 1 : 0, split},
               shape, in_bytes, st);
   std::vector<int> hs(n);
   cudaMemcpyAsync(hs.data(), status + p0, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
@@ -1321,7 +1388,7 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
     if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch arena)");
     launch_clip(ClipArgs{n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[1],
                          aoff[1] + p0, 0, need_ + p0, need_ + p0, status + p0, nrings + p0,
-                         nverts + p0, area + p0, unite ? 1 : 0, split, order_ + p0},
+                         nverts + p0, area + p0, unite ? 1 : 0, split},
                 shape, in_bytes, st);
   }
   // where each pair's data lives now: pass 0 arena, retry arena, or none
@@ -1649,13 +1716,11 @@ int BatchRunner::graph_record(int np_, const double* d_bxy, const long long* d_b
   cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     launch_clip(ClipArgs{np, d_bxy, d_boff, d_cxy, d_coff, pass0, arena[0], aoff[0], abase_[0],
-                         need_scr, need_rec, status, nrings, nverts, area, unite ? 1 : 0, split,
-                         order_},
+                         need_scr, need_rec, status, nrings, nverts, area, unite ? 1 : 0, split},
                 shape, in_bytes, st);
     if (retry)
       launch_clip(ClipArgs{np, d_bxy, d_boff, d_cxy, d_coff, pass1, arena[1], aoff[1], 0, need_scr,
-                           need_rec, status, nrings, nverts, area, unite ? 1 : 0, split,
-                           order_},
+                           need_rec, status, nrings, nverts, area, unite ? 1 : 0, split},
                   shape, in_bytes, st);
     const Arenas ar{arena[0], aoff[0], abase_[0], arena[1], aoff[1], 0, pass, need_rec};
     {

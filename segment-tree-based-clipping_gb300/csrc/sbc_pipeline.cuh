@@ -368,8 +368,6 @@ class BatchRunner {
   long long abase_[2] = {0, 0};
   int* pass = nullptr;
   int* need_ = nullptr;          // per pair: hits found by a first pass that ran out of room
-  int* order_ = nullptr;         // per chunk: its pairs by decreasing vertex count
-  std::vector<int> h_order_;
   void* sscr_ = nullptr;
   std::vector<long long> h_boff_, h_coff_, h_aoff0_;
   std::vector<std::pair<int, int>> chunks_;
