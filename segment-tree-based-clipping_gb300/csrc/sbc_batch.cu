@@ -60,12 +60,14 @@ __host__ __device__ __forceinline__ Caps caps_of(int nb, int nc, int K) {
 // The arrays of one pair.  Carved in a fixed order from a base pointer, so a
 // null base gives the byte count.
 struct PairWork {
-  // edges
+  // edges, and the order keys (okey) of their ends for comparison-only work
   double *es, *ee;
+  long long *kes, *kee;
   float4* fbox;
   // elementary intervals
   int *sidx, *stmp, *vl, *vloc;
   double* ea;
+  long long* kea;  // order keys of ea
   // end leaves, leaf ranges
   int *aft, *bef;
   int2* lr;
@@ -112,12 +114,15 @@ __host__ __device__ __forceinline__ PairWork carve(Carver& cv, const Caps& c) {
   const int E = c.E, n2 = 2 * E, K = c.K;
   w.es = cv.take<double>(E);
   w.ee = cv.take<double>(E);
+  w.kes = cv.take<long long>(E);
+  w.kee = cv.take<long long>(E);
   w.fbox = cv.take<float4>(E);
   w.sidx = cv.take<int>(n2);
   w.stmp = cv.take<int>(n2);
   w.vl = cv.take<int>(E + 1);
   w.vloc = cv.take<int>(E + 1);
   w.ea = cv.take<double>(c.epcMax);
+  w.kea = cv.take<long long>(c.epcMax);
   w.aft = cv.take<int>(E);
   w.bef = cv.take<int>(E);
   w.lr = cv.take<int2>(E);
@@ -190,24 +195,27 @@ __host__ __device__ __forceinline__ int hit_cap(int nb, int nc, int pass, int ne
 }
 
 // findBoarder over S(m) (oacc_segment_tree.cpp:420-460) with the zero
-// border slot at z (the same emulation as the pair pipeline)
+// border slot at z (the same emulation as the pair pipeline), compared on
+// order keys: S(m) past the arrays is NaN in the reference, which is neither
+// equal to nor below any value; kPastKey (above every finite key) does the same.
+constexpr long long kPastKey = 0x7fffffffffffffffll;
 struct BordersS {
-  const double* ea;
+  const long long* kea;
   int epc, z;
-  __device__ double S(int m) const {
-    if (m < 0 || m >= epc) return __longlong_as_double(0x7ff8000000000000ll);
-    if (m < z) return ea[m + 1];
-    if (m == z) return 0.0;
-    return ea[m];
+  __device__ long long S(int m) const {
+    if (m < 0 || m >= epc) return kPastKey;
+    if (m < z) return kea[m + 1];
+    if (m == z) return 0;  // okey(0.0)
+    return kea[m];
   }
   __device__ int J(int m) const { return m < z ? m : (m == z ? epc - 1 : m - 1); }
 };
 
-__device__ int find_border_s(const BordersS& B, double q) {
+__device__ int find_border_s(const BordersS& B, long long q) {
   int l = 0, h = B.epc;
   while (l < h) {
     const int m = l + (h - l) / 2;
-    const double sm = B.S(m);
+    const long long sm = B.S(m);
     if (sm == q) {
       if (B.S(m - 1) != q) {
         h = m;
@@ -247,8 +255,11 @@ __device__ int clip_pair_front(const double* b, int nb, const double* c, int nc,
                                PairWork& w) {
   PairResult res{PS_OK, 0, 0, 0.0, 0};
   const int E = nb + nc, n2 = 2 * E;
-  // ---- A1 edges (edge.h:190-202); ids are offsets into the interleaved arrays
+  // ---- A1 edges (edge.h:190-202); ids are offsets into the interleaved arrays.
+  // Compares, minima and maxima run on order keys (okey): an FP64 compare
+  // issues at the FP64 rate, and here one thread works per pair.
   double minI = bvx(b, nb, 0), maxI = minI;
+  long long kmin = okey(minI), kmax = kmin;
   for (int e = 0; e < E; ++e) {
     double a0, a1, y0, y1;
     if (e < nb) {
@@ -262,26 +273,39 @@ __device__ int clip_pair_front(const double* b, int nb, const double* c, int nc,
       y0 = bvy(c, nc, e - nb);
       y1 = bvy(c, nc, e - nb + 1);
     }
-    if (a0 < a1) {
+    const long long k0 = okey(a0), k1 = okey(a1), ky0 = okey(y0), ky1 = okey(y1);
+    if (k0 < k1) {
       w.es[e] = a0;
       w.ee[e] = a1;
+      w.kes[e] = k0;
+      w.kee[e] = k1;
     } else {
       w.ee[e] = a0;
       w.es[e] = a1;
+      w.kee[e] = k0;
+      w.kes[e] = k1;
     }
-    minI = fmin(minI, a0);
-    maxI = fmax(maxI, a0);
-    w.fbox[e] = make_float4(__double2float_rd(fmin(a0, a1)), __double2float_rd(fmin(y0, y1)),
-                            __double2float_ru(fmax(a0, a1)), __double2float_ru(fmax(y0, y1)));
+    if (k0 < kmin) {
+      kmin = k0;
+      minI = a0;
+    }
+    if (k0 > kmax) {
+      kmax = k0;
+      maxI = a0;
+    }
+    const bool xs = k0 < k1, ys = ky0 < ky1;
+    w.fbox[e] = make_float4(__double2float_rd(xs ? a0 : a1), __double2float_rd(ys ? y0 : y1),
+                            __double2float_ru(xs ? a1 : a0), __double2float_ru(ys ? y1 : y0));
   }
   // ---- A4 elementary intervals (:4513-4692): stable sort of the endpoints
   auto val = [&](int idx) { return (idx & 1) ? w.ee[idx >> 1] : w.es[idx >> 1]; };
+  auto kval = [&](int idx) { return (idx & 1) ? w.kee[idx >> 1] : w.kes[idx >> 1]; };
   for (int i = 0; i < n2; ++i) w.sidx[i] = i;
-  merge_sort(w.sidx, w.stmp, n2, [&](int x, int y) { return dkey(val(x)) < dkey(val(y)); });
+  merge_sort(w.sidx, w.stmp, n2, [&](int x, int y) { return kval(x) < kval(y); });
   for (int i = 0; i <= E; ++i) w.vl[i] = 0;
   for (int j = 0; j < E; ++j) {
     const int i = w.sidx[j] >> 1;
-    if (w.es[i] == w.ee[i]) w.vl[i] = 1;
+    if (w.kes[i] == w.kee[i]) w.vl[i] = 1;
   }
   {
     int s = 0;
@@ -295,28 +319,39 @@ __device__ int clip_pair_front(const double* b, int nb, const double* c, int nc,
   }
   int count = 0;
   double* ea = w.ea;
+  long long* kea = w.kea;
   for (int i = 0; i < n2 - 1; ++i) {
-    const double v0 = val(w.sidx[i]), v1 = val(w.sidx[i + 1]);
+    const long long k0 = kval(w.sidx[i]), k1 = kval(w.sidx[i + 1]);
     const int intvi = w.sidx[i] >> 1;
     const int comid = w.vl[i / 2];
-    if (v0 != v1) {
-      ea[count++] = v0;
-    } else if (w.es[intvi] == w.ee[intvi]) {
+    if (k0 != k1) {
+      kea[count] = k0;
+      ea[count++] = val(w.sidx[i]);
+    } else if (w.kes[intvi] == w.kee[intvi]) {
       bool keep = comid == 0;
       if (!keep) {
         const int lookup = w.vloc[comid - 1];
-        keep = w.es[lookup] != w.es[intvi] && w.ee[lookup] != w.es[intvi];
+        keep = w.kes[lookup] != w.kes[intvi] && w.kee[lookup] != w.kes[intvi];
       }
-      if (keep) ea[count++] = w.es[intvi];
+      if (keep) {
+        kea[count] = w.kes[intvi];
+        ea[count++] = w.es[intvi];
+      }
     }
-    if (i == n2 - 2 && v0 != v1) ea[count++] = v0;  // the last slot repeats v0
+    if (i == n2 - 2 && k0 != k1) {  // the last slot repeats v0
+      kea[count] = k0;
+      ea[count++] = val(w.sidx[i]);
+    }
   }
   if (count < 1) {
     res.status = PS_UNDEF;
     return res.status;
   }
   const int epc = npow2_dev(count) + 1;
-  for (int i = count; i < epc; ++i) ea[i] = ea[count - 1];
+  for (int i = count; i < epc; ++i) {
+    ea[i] = ea[count - 1];
+    kea[i] = kea[count - 1];
+  }
   const int L = epc - 1;
   int logL = 0;
   while ((1 << logL) < L) ++logL;
@@ -347,26 +382,27 @@ __device__ int clip_pair_front(const double* b, int nb, const double* c, int nc,
       if (ki == 0) ++z;
     }
   }
-  const BordersS B{ea, epc, z};
+  const BordersS B{kea, epc, z};
   for (int e = 0; e < E; ++e) {
     int a = -1, bb = -1;
-    const int en = find_border_s(B, w.ee[e]);
-    const int st = find_border_s(B, w.es[e]);
+    const long long kee = w.kee[e], kes = w.kes[e];
+    const int en = find_border_s(B, kee);
+    const int st = find_border_s(B, kes);
     if (en >= 0) {
       const int j = B.J(en);
       int node = 0;
       if (j <= epc - 2) {
         const int i = j + 1;
         node = L + i;
-        if (i != 1 && i + 1 < epc && ea[i] == ea[i + 1]) node = L + i + 1;
+        if (i != 1 && i + 1 < epc && kea[i] == kea[i + 1]) node = L + i + 1;
       }
-      if (node >= L && node < 2 * L && ea[node - L] != ea[node - L + 1]) a = node;
+      if (node >= L && node < 2 * L && kea[node - L] != kea[node - L + 1]) a = node;
     }
     if (st >= 0) {
       const int j = B.J(st);
       int node = 0;
       if (j <= epc - 2) node = L + j;
-      if (node >= L && node < 2 * L && ea[node - L] != ea[node - L + 1]) bb = node;
+      if (node >= L && node < 2 * L && kea[node - L] != kea[node - L + 1]) bb = node;
     }
     w.aft[e] = a;
     w.bef[e] = bb;
@@ -374,7 +410,7 @@ __device__ int clip_pair_front(const double* b, int nb, const double* c, int nc,
     int lo = 0, hi = L;
     while (lo < hi) {
       const int m = (lo + hi) >> 1;
-      if (ea[m] < w.es[e]) lo = m + 1;
+      if (kea[m] < kes) lo = m + 1;
       else hi = m;
     }
     const int l = lo;
@@ -382,7 +418,7 @@ __device__ int clip_pair_front(const double* b, int nb, const double* c, int nc,
     hi = L;
     while (lo < hi) {
       const int m = (lo + hi) >> 1;
-      if (ea[m + 1] <= w.ee[e]) lo = m + 1;
+      if (kea[m + 1] <= kee) lo = m + 1;
       else hi = m;
     }
     w.lr[e] = make_int2(l, lo > l ? lo : l);
@@ -753,15 +789,13 @@ __device__ PairResult clip_pair_back2(const double* b, int nb, const double* c, 
     res.status = st == 2 ? PS_UNDEF : PS_CAP;
     return res;
   }
-  // ---- rings out: offsets, coordinates, provenance, area
+  // ---- rings out: offsets, coordinates, provenance (the area: k_batch_area)
   int nr = 0, nv = 0;
-  double area = 0.0;
   w.roff[0] = 0;
   for (int r = 0; r < *a.nrings; ++r) {
     const int root = a.rroot[r];
     if (root < 0) continue;
     int v = root;
-    const int first = nv;
     do {
       const double x = a.R.x[v], y = a.R.y[v];
       w.rxy[2 * nv] = x;
@@ -808,18 +842,31 @@ __device__ PairResult clip_pair_back2(const double* b, int nb, const double* c, 
       ++nv;
       v = a.R.next[v];
     } while (v != root);
-    double s2 = 0.0;  // shoelace of the ring
-    for (int i = first; i < nv; ++i) {
-      const int j = (i + 1 == nv) ? first : i + 1;
-      s2 = dadd(s2, dsub(dmul(w.rxy[2 * i], w.rxy[2 * j + 1]), dmul(w.rxy[2 * j], w.rxy[2 * i + 1])));
-    }
-    area = dadd(area, dmul(0.5, s2));
     w.roff[++nr] = nv;
   }
   res.nrings = nr;
   res.nverts = nv;
-  res.area = area;
+  res.area = 0.0;  // k_batch_area
   return res;
+}
+
+// The pair's area: the sum over its rings of the shoelace, one warp per pair
+// (FP64 products at the full warp rather than on one thread of each warp);
+// the lanes' partial sums combine in a fixed order, so the area does not
+// depend on how the batch was cut into chunks.
+__device__ double pair_area_warp(const int* roff, const double* rxy, int nr, int lane) {
+  double area = 0.0;
+  for (int r = 0; r < nr; ++r) {
+    const int first = roff[r], last = roff[r + 1];
+    double s2 = 0.0;
+    for (int i = first + lane; i < last; i += 32) {
+      const int j = (i + 1 == last) ? first : i + 1;
+      s2 = dadd(s2, dsub(dmul(rxy[2 * i], rxy[2 * j + 1]), dmul(rxy[2 * j], rxy[2 * i + 1])));
+    }
+    for (int o = 16; o > 0; o >>= 1) s2 = dadd(s2, __shfl_xor_sync(0xffffffffu, s2, o));
+    area = dadd(area, dmul(0.5, s2));
+  }
+  return area;
 }
 
 // ------------------------------------------------------------------ kernels
@@ -970,6 +1017,20 @@ __global__ void __launch_bounds__(kBatchBlock) k_batch_back2(ClipArgs A) {
   A.area[p] = r.area;
 }
 
+__global__ void __launch_bounds__(128) k_batch_area(ClipArgs A) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  if ((t >> 5) >= A.np) return;
+  const int p = (int)(t >> 5);
+  const int pass = A.pass_of ? A.pass_of[p] : 0;
+  int nb, nc;
+  if (pass < 0 || !A.small(p, &nb, &nc) || A.status[p] != SBC_OK) return;
+  Caps cp;
+  PairWork w = A.work(p, nb, nc, pass, &cp);
+  const double a = pair_area_warp(w.roff, w.rxy, A.nrings[p], lane);
+  if (lane == 0) A.area[p] = a;
+}
+
 // the pass arrays of a recorded batch: pass 0 for every pair the forward
 // pass ran (-1: a large pair or none), pass 1 for the pairs it retried
 __global__ void k_graph_passes(int n, const int* __restrict__ pass, const int* __restrict__ status,
@@ -1002,6 +1063,10 @@ void launch_clip(const ClipArgs& A, const BatchShape& sh, double in_bytes, cudaS
   {
     ::sbc::KProbe kp_("k_batch_back2", st, in_bytes + 20.0 * A.np);
     k_batch_back2<<<grid_for(A.np, sh.back), sh.back, 0, st>>>(A);
+  }
+  {
+    ::sbc::KProbe kp_("k_batch_area", st);
+    k_batch_area<<<grid_for(32LL * A.np, 128), 128, 0, st>>>(A);
   }
 }
 

@@ -86,14 +86,20 @@ __device__ void pinsert_after(Pool& p, int V, int curr) {
 
 // winding-number step of pointInPoly (foster/polygon.h:427-448) for the edge
 // (x0,y0)-(x1,y1); the winding number is the (order-free) sum of the steps
+// one edge's step of pointInPoly (foster/polygon.h:427-448); the compares
+// run on integer order keys (okey: the same decisions as on the doubles, at
+// the integer rate), the orientation test in FP64
 __device__ __forceinline__ int pip_step(double x0, double y0, double x1, double y1, double rx,
                                         double ry) {
-  if ((y0 < ry) != (y1 < ry)) {
-    if (x0 >= rx) {
-      if (x1 > rx) return 2 * (y1 > y0) - 1;
-      if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (y1 > y0)) return 2 * (y1 > y0) - 1;
-    } else if (x1 > rx) {
-      if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (y1 > y0)) return 2 * (y1 > y0) - 1;
+  const long long ky0 = okey(y0), ky1 = okey(y1), kry = okey(ry);
+  if ((ky0 < kry) != (ky1 < kry)) {
+    const long long kx0 = okey(x0), kx1 = okey(x1), krx = okey(rx);
+    const int d = 2 * (ky1 > ky0) - 1;
+    if (kx0 >= krx) {
+      if (kx1 > krx) return d;
+      if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (ky1 > ky0)) return d;
+    } else if (kx1 > krx) {
+      if ((area3(x0, y0, x1, y1, rx, ry) > 0) == (ky1 > ky0)) return d;
     }
   }
   return 0;
@@ -171,7 +177,8 @@ __device__ int ser_build(SerialArgs& a) {
   for (int ii = 0; ii <= a.bSize; ++ii) {
     int sv = ii < a.bSize ? ii : 0;
     double vx = a.bP[2 * sv], vy = a.bP[2 * sv + 1];
-    while (a.ixB[(2 * i) % (2 * nB)] != vx || a.ixB[(2 * i + 1) % (2 * nB)] != vy) {
+    const long long kvx = okey(vx), kvy = okey(vy);  // compares on order keys
+    while (okey(a.ixB[(2 * i) % (2 * nB)]) != kvx || okey(a.ixB[(2 * i + 1) % (2 * nB)]) != kvy) {
       if (i >= nB) return 2;
       int v = pnew(P, a.ixB[2 * i], a.ixB[2 * i + 1]);
       if (v < 0) return 3;
@@ -197,7 +204,8 @@ __device__ int ser_build(SerialArgs& a) {
   for (int ii = 0; ii <= a.cSize; ++ii) {
     int sv = ii < a.cSize ? ii : 0;
     double vx = a.cP[2 * (a.cStart + sv)], vy = a.cP[2 * (a.cStart + sv) + 1];
-    while (a.ixC[(2 * i) % (2 * nQ)] != vx || a.ixC[(2 * i + 1) % (2 * nQ)] != vy) {
+    const long long kvx = okey(vx), kvy = okey(vy);
+    while (okey(a.ixC[(2 * i) % (2 * nQ)]) != kvx || okey(a.ixC[(2 * i + 1) % (2 * nQ)]) != kvy) {
       if (i >= nQ) return 2;
       int v = pnew(Q, a.ixC[2 * i], a.ixC[2 * i + 1]);
       if (v < 0) return 3;
