@@ -430,39 +430,69 @@ __device__ int clip_pair_front(const double* b, int nb, const double* c, int nc,
 
 // A8 for one pair by one warp: every base x overlay edge pair, float boxes
 // first; lanes take the pairs in strides of 32 (coalesced overlay boxes)
+// The edge pairs past the float box test and LSMF are queued per warp
+// (kCandQ entries of shared memory) and classified 32 at a time, so that
+// lineSegmentIntersection's FP64 work runs in full warps: only a few pairs in
+// a hundred pass the filters, and FP64 run by a few lanes costs the issue
+// slots of all 32.
+constexpr int kCandQ = 64;
 __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc, const Caps& cp,
-                               PairWork& w, int lane) {
+                               PairWork& w, int lane, int2* q) {
+  const unsigned full = 0xffffffffu;
   const int logL = w.state[1];
+  int nq = 0;  // queued pairs (the same in every lane)
+  auto classify = [&](int count) {
+    if (lane < count) {
+      const int2 e = q[lane];
+      const int be = e.x, j = e.y;
+      const double p1x = bvx(b, nb, be), p1y = bvy(b, nb, be);
+      const double p2x = bvx(b, nb, be + 1), p2y = bvy(b, nb, be + 1);
+      const double q1x = bvx(c, nc, j), q1y = bvy(c, nc, j);
+      const double q2x = bvx(c, nc, j + 1), q2y = bvy(c, nc, j + 1);
+      double al, bt;
+      const int ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
+      unsigned long long key;
+      if (ty && emission_s(be, nb + j, 2 * j, w, logL, &key) > 0) {
+        // out of room: only counted, for the retry's capacity
+        const int k = atomicAdd(&w.state[2], 1);
+        if (k < cp.K) {
+          w.hb[k] = 2 * be;
+          w.hc[k] = 2 * j;
+          w.ht[k] = ty;
+          w.hkey[k] = key;
+          w.hal[k] = al;
+          w.hbt[k] = bt;
+        }
+      }
+    }
+    __syncwarp();
+  };
   int be = 0, j = lane;
   while (j >= nc && be < nb) {
     j -= nc;
     ++be;
   }
-  while (be < nb) {
-    const float4 fb = w.fbox[be];
-    const float4 fc = w.fbox[nb + j];
-    if (!(fb.x > fc.z || fb.z < fc.x || fb.y > fc.w || fb.w < fc.y)) {
-      const double p1x = bvx(b, nb, be), p1y = bvy(b, nb, be);
-      const double p2x = bvx(b, nb, be + 1), p2y = bvy(b, nb, be + 1);
-      const double q1x = bvx(c, nc, j), q1y = bvy(c, nc, j);
-      const double q2x = bvx(c, nc, j + 1), q2y = bvy(c, nc, j + 1);
-      if (lsmf_d(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y)) {
-        double al, bt;
-        const int ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
-        unsigned long long key;
-        if (ty && emission_s(be, nb + j, 2 * j, w, logL, &key) > 0) {
-          // out of room: only counted, for the retry's capacity
-          const int k = atomicAdd(&w.state[2], 1);
-          if (k < cp.K) {
-            w.hb[k] = 2 * be;
-            w.hc[k] = 2 * j;
-            w.ht[k] = ty;
-            w.hkey[k] = key;
-            w.hal[k] = al;
-            w.hbt[k] = bt;
-          }
-        }
-      }
+  while (__any_sync(full, be < nb)) {
+    bool pass = false;
+    if (be < nb) {
+      const float4 fb = w.fbox[be];
+      const float4 fc = w.fbox[nb + j];
+      if (!(fb.x > fc.z || fb.z < fc.x || fb.y > fc.w || fb.w < fc.y))
+        pass = lsmf_d(bvx(b, nb, be), bvy(b, nb, be), bvx(b, nb, be + 1), bvy(b, nb, be + 1),
+                      bvx(c, nc, j), bvy(c, nc, j), bvx(c, nc, j + 1), bvy(c, nc, j + 1));
+    }
+    const unsigned m = __ballot_sync(full, pass);
+    if (pass) q[nq + __popc(m & ((1u << lane) - 1u))] = make_int2(be, j);
+    nq += __popc(m);
+    __syncwarp();
+    if (nq >= 32) {
+      classify(32);
+      const int rest = nq - 32;
+      const int2 t = lane < rest ? q[32 + lane] : make_int2(0, 0);
+      __syncwarp();
+      if (lane < rest) q[lane] = t;
+      nq = rest;
+      __syncwarp();
     }
     j += 32;
     while (j >= nc && be < nb) {
@@ -470,6 +500,7 @@ __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc,
       ++be;
     }
   }
+  if (nq > 0) classify(nq);
 }
 
 // A9-A13: records, counts, alpha order, merged arrays (one thread per pair)
@@ -945,6 +976,7 @@ __global__ void __launch_bounds__(kBatchBlock) k_batch_front(ClipArgs A) {
 }
 
 __global__ void __launch_bounds__(128) k_batch_cand(ClipArgs A) {
+  __shared__ int2 s_q[4][kCandQ];
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   if ((t >> 5) >= A.np) return;
@@ -955,7 +987,8 @@ __global__ void __launch_bounds__(128) k_batch_cand(ClipArgs A) {
   Caps cp;
   PairWork w = A.work(p, nb, nc, pass, &cp);
   if (w.state[0] != PS_OK) return;
-  clip_pair_cand(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w, lane);
+  clip_pair_cand(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w, lane,
+                 s_q[threadIdx.x >> 5]);
 }
 
 // The back end in three kernels: A9-A13 on one thread per pair, the labels
