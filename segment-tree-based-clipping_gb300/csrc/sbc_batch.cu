@@ -26,6 +26,7 @@
 #include "../../include/sbclip.h"
 #include "sbc_pipeline.cuh"
 #include "sbc_pairops.cuh"
+#include "sbc_pwpair.cuh"
 #include "sbc_serial.cuh"
 
 namespace sbc {
@@ -53,7 +54,8 @@ __host__ __device__ __forceinline__ Caps caps_of(int nb, int nc, int K) {
   c.capP = c.nBmax + 2 * K + 8;
   c.capQ = c.nQmax + 2 * K + 8;
   c.capR = c.nBmax + c.nQmax + 2 * (2 * K + 8) + 16;
-  c.rcap = c.nBmax + 16;
+  // ring count: the serial back end's bound, or the warp back end's
+  c.rcap = (c.nBmax > 2 * K ? c.nBmax : 2 * K) + 16;
   return c;
 }
 
@@ -92,6 +94,13 @@ struct PairWork {
   int* roff;
   double* rxy;
   int4* tape;
+  // the warp back end (sbc_pwpair.cuh): its hits in record order, its
+  // arrays, and the coordinate table of the provenance lookup (ptab
+  // entries: a candidate's index, and the best provenance of its point)
+  PwHit* phit;
+  PwWork pw;
+  int *ptab, *pbest;
+  int ptabn;
 };
 
 __host__ __device__ __forceinline__ void carve_pool(Carver& cv, int cap, Pool& p) {
@@ -174,6 +183,11 @@ __host__ __device__ __forceinline__ PairWork carve(Carver& cv, const Caps& c) {
   w.roff = cv.take<int>(c.rcap + 1);
   w.rxy = cv.take<double>(2 * (long long)c.capR);
   w.tape = cv.take<int4>(c.capR);
+  w.phit = cv.take<PwHit>(K);
+  w.pw = pw_carve(cv, pw_caps(c.nb, c.nc, K, 1));
+  w.ptabn = npow2_dev(2 * (c.nb + c.nc + K) + 2);
+  w.ptab = cv.take<int>(w.ptabn);
+  w.pbest = cv.take<int>(w.ptabn);
   return w;
 }
 
@@ -1002,6 +1016,166 @@ __device__ void batch_fail(const ClipArgs& A, int p, PairWork& w, int st, int ne
   w.state[0] = st;
 }
 
+// ---- the warp back end: rows A9-A18 of a pair by one warp (sbc_pwpair.cuh)
+
+// pointInPoly against the base side: the pairwise engine's functor without
+// its grid (the base is small, so every base edge is tested for membership
+// in a run node)
+struct PipSmall {
+  const double* b;
+  int nb;
+  const int* runIds;
+  int nruns;
+  __device__ bool internal(const Pool& P, int u) const {
+    int lo = 0, hi = nruns;  // runs with rv0 <= u
+    while (lo < hi) {
+      const int m = (lo + hi) >> 1;
+      if (P.rv0[runIds[m]] <= u) lo = m + 1;
+      else hi = m;
+    }
+    if (lo == 0) return false;
+    const int v = runIds[lo - 1];
+    return u + 1 <= P.rv0[v] + P.run[v];
+  }
+  __device__ int operator()(SerialArgs& a, int root, double rx, double ry) const {
+    const Pool& P = a.P;
+    const int lane = threadIdx.x & 31;
+    int part = 0;
+    for (int v = lane; v < P.n; v += 32) {
+      const int nx = P.next[v];
+      part += pip_step(last_x(P, v), last_y(P, v), P.x[nx], P.y[nx], rx, ry);
+    }
+    for (int u = lane; u < nb; u += 32) {
+      const int u2 = u + 1 == nb ? 0 : u + 1;
+      const int st = pip_step(b[2 * u], b[2 * u + 1], b[2 * u2], b[2 * u2 + 1], rx, ry);
+      if (st && internal(P, u)) part += st;
+    }
+    return (__reduce_add_sync(kFullMask, part) % 2) != 0;
+  }
+};
+
+// Provenance of ring vertices by exact coordinates, as the area oracle
+// defines it: a base vertex (lowest index) first, then an overlay vertex,
+// then a proper crossing (a type-1 record, first in record order).  The
+// candidates are numbered in that order (base vertices, overlay vertices,
+// records), so the best one for a point is the least number; an open-address
+// table keyed by the point's order keys holds, per point, one candidate (to
+// compare coordinates) and the least number.
+__device__ __forceinline__ unsigned ptab_slot(long long kx, long long ky, int mask) {
+  const unsigned long long h = (unsigned long long)kx * 0x9e3779b97f4a7c15ull ^
+                               ((unsigned long long)ky + 0x632be59bd9b4e019ull) *
+                                   0xc2b2ae3d27d4eb4full;
+  return (unsigned)(h >> 32) & (unsigned)mask;
+}
+
+__device__ void pair_tape_warp(const double* b, int nb, const double* c, int nc, const PwWork& pw,
+                               int K, PairWork& w, int nv, int lane) {
+  const int T = w.ptabn, mask = T - 1;
+  for (int i = lane; i < T; i += 32) {
+    w.ptab[i] = -1;
+    w.pbest[i] = INT_MAX;
+  }
+  __syncwarp();
+  auto cx = [&](int t) { return t < nb ? b[2 * t] : (t < nb + nc ? c[2 * (t - nb)] : pw.isxy[2 * (t - nb - nc)]); };
+  auto cy = [&](int t) {
+    return t < nb ? b[2 * t + 1] : (t < nb + nc ? c[2 * (t - nb) + 1] : pw.isxy[2 * (t - nb - nc) + 1]);
+  };
+  const int ncand = nb + nc + K;
+  for (int t = lane; t < ncand; t += 32) {
+    if (t >= nb + nc && pw.ut[t - nb - nc] != 1) continue;  // crossings only
+    const long long kx = okey(cx(t)), ky = okey(cy(t));
+    unsigned h = ptab_slot(kx, ky, mask);
+    for (int probe = 0; probe < T; ++probe) {
+      const int old = atomicCAS(&w.ptab[h], -1, t);
+      if (old == -1 || (okey(cx(old)) == kx && okey(cy(old)) == ky)) {
+        atomicMin(&w.pbest[h], t);
+        break;
+      }
+      h = (h + 1) & (unsigned)mask;
+    }
+  }
+  __syncwarp();
+  for (int v = lane; v < nv; v += 32) {
+    const long long kx = okey(w.rxy[2 * v]), ky = okey(w.rxy[2 * v + 1]);
+    unsigned h = ptab_slot(kx, ky, mask);
+    int best = -1;
+    for (int probe = 0; probe < T; ++probe) {
+      const int t = w.ptab[h];
+      if (t == -1) break;
+      if (okey(cx(t)) == kx && okey(cy(t)) == ky) {
+        best = w.pbest[h];
+        break;
+      }
+      h = (h + 1) & (unsigned)mask;
+    }
+    int4 tp = make_int4(-1, 0, 0, 0);
+    if (best >= 0 && best < nb) tp = make_int4(0, best, 0, 0);
+    else if (best >= nb && best < nb + nc) tp = make_int4(1, best - nb, 0, 0);
+    else if (best >= nb + nc) tp = make_int4(2, pw.ub[best - nb - nc] >> 1, pw.uc[best - nb - nc] >> 1, 0);
+    w.tape[v] = tp;
+  }
+  __syncwarp();
+}
+
+// One warp per pair: the records in the reference's order, then rows
+// A9-A18 by the warp; a pair whose arrays take a path the warp back end does
+// not follow (w.state[3] = 1) is clipped by the thread back end below.
+__global__ void __launch_bounds__(128) k_batch_pw(ClipArgs A) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  if ((t >> 5) >= A.np) return;
+  const int p = (int)(t >> 5);
+  const int pass = A.pass_of ? A.pass_of[p] : 0;
+  int nb, nc;
+  if (pass < 0 || !A.small(p, &nb, &nc)) return;
+  Caps cp;
+  PairWork w = A.work(p, nb, nc, pass, &cp);
+  if (w.state[0] != PS_OK) return;
+  const int K = w.state[2];
+  if (K > cp.K) {
+    if (lane == 0) batch_fail(A, p, w, PS_CAP, K);
+    return;
+  }
+  // A9 order (base id, then first emission)
+  if (lane == 0) {
+    for (int i = 0; i < K; ++i) w.hord[i] = i;
+    merge_sort(w.hord, w.htmp, K, [&](int x, int y) {
+      return w.hb[x] != w.hb[y] ? w.hb[x] < w.hb[y] : w.hkey[x] < w.hkey[y];
+    });
+  }
+  __syncwarp();
+  for (int i = lane; i < K; i += 32) {
+    const int h = w.hord[i];
+    w.phit[i] = PwHit{0, w.hb[h] >> 1, w.hc[h] >> 1, w.ht[h], w.hkey[h], w.hal[h], w.hbt[h]};
+  }
+  __syncwarp();
+  const double* b = A.bxy + 2 * A.boff[p];
+  const double* c = A.cxy + 2 * A.coff[p];
+  PwWork pw = w.pw;
+  int nr = 0, nv = 0;
+  const int st = pw_clip_core(b, nb, c, nc, w.phit, pw_caps(nb, nc, K, 1), pw,
+                              PipSmall{b, nb, nullptr, 0}, A.unite, &nr, &nv);
+  if (st != PS_OK && st != PS_UNDEF) {
+    if (lane == 0) w.state[3] = 1;  // the thread back end takes the pair
+    return;
+  }
+  if (st == PS_UNDEF) {
+    if (lane == 0) batch_fail(A, p, w, PS_UNDEF, 0);
+    return;
+  }
+  for (int r = lane; r <= nr; r += 32) w.roff[r] = pw.roff[r];
+  for (int i = lane; i < 2 * nv; i += 32) w.rxy[i] = pw.rxy[i];
+  __syncwarp();
+  pair_tape_warp(b, nb, c, nc, pw, K, w, nv, lane);
+  if (lane == 0) {
+    w.state[3] = 0;
+    A.status[p] = SBC_OK;
+    A.nrings[p] = nr;
+    A.nverts[p] = nv;
+    A.area[p] = 0.0;  // k_batch_area
+  }
+}
+
 __global__ void __launch_bounds__(kBatchBlock) k_batch_back(ClipArgs A) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= A.np) return;
@@ -1011,7 +1185,7 @@ __global__ void __launch_bounds__(kBatchBlock) k_batch_back(ClipArgs A) {
   if (pass < 0 || !A.small(p, &nb, &nc)) return;
   Caps cp;
   PairWork w = A.work(p, nb, nc, pass, &cp);
-  if (w.state[0] != PS_OK) return;
+  if (w.state[0] != PS_OK || w.state[3] != 1) return;
   const PairResult r = clip_pair_back1(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w);
   if (r.status != PS_OK) batch_fail(A, p, w, r.status, r.need);
 }
@@ -1026,7 +1200,7 @@ __global__ void __launch_bounds__(128) k_batch_labels(ClipArgs A) {
   if (pass < 0 || !A.small(p, &nb, &nc)) return;
   Caps cp;
   PairWork w = A.work(p, nb, nc, pass, &cp);
-  if (w.state[0] != PS_OK) return;
+  if (w.state[0] != PS_OK || w.state[3] != 1) return;
   const int st = clip_pair_labels(nb, nc, w, lane);
   if (st != PS_OK && lane == 0) batch_fail(A, p, w, st, 0);
 }
@@ -1040,7 +1214,7 @@ __global__ void __launch_bounds__(kBatchBlock) k_batch_back2(ClipArgs A) {
   if (pass < 0 || !A.small(p, &nb, &nc)) return;
   Caps cp;
   PairWork w = A.work(p, nb, nc, pass, &cp);
-  if (w.state[0] != PS_OK) return;
+  if (w.state[0] != PS_OK || w.state[3] != 1) return;
   const PairResult r =
       clip_pair_back2(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w, A.unite);
   A.status[p] = r.status == PS_OK ? SBC_OK : (r.status == PS_UNDEF ? SBC_EUNDEF : SBC_ENOMEM);
@@ -1084,6 +1258,10 @@ void launch_clip(const ClipArgs& A, const BatchShape& sh, double in_bytes, cudaS
   {
     ::sbc::KProbe kp_("k_batch_cand", st, in_bytes);
     k_batch_cand<<<grid_for(32LL * A.np, sh.cand), sh.cand, 0, st>>>(A);
+  }
+  {
+    ::sbc::KProbe kp_("k_batch_pw", st, in_bytes + 20.0 * A.np);
+    k_batch_pw<<<grid_for(32LL * A.np, 128), 128, 0, st>>>(A);
   }
   {
     ::sbc::KProbe kp_("k_batch_back", st, in_bytes);
