@@ -101,6 +101,10 @@ struct PairWork {
   PwWork pw;
   int *ptab, *pbest;
   int ptabn;
+  // the warp front's endpoint sort: (key, endpoint) pairs padded to a power of two
+  long long* fkey;
+  int* fval;
+  int* eflag;  // per sorted endpoint: entries it adds to the elementary array
 };
 
 __host__ __device__ __forceinline__ void carve_pool(Carver& cv, int cap, Pool& p) {
@@ -188,6 +192,9 @@ __host__ __device__ __forceinline__ PairWork carve(Carver& cv, const Caps& c) {
   w.ptabn = npow2_dev(2 * (c.nb + c.nc + K) + 2);
   w.ptab = cv.take<int>(w.ptabn);
   w.pbest = cv.take<int>(w.ptabn);
+  w.fkey = cv.take<long long>(npow2_dev(n2));
+  w.fval = cv.take<int>(npow2_dev(n2));
+  w.eflag = cv.take<int>(n2 + 1);
   return w;
 }
 
@@ -262,19 +269,24 @@ struct PairResult {
 };
 
 // ------------------------------------------------------------------ one pair
-// Three kernels per pair: the front (rows A1-A7, one thread), the candidate
-// pairs (A8, one warp) and the rest (A9-A18, one thread); w.state carries
-// the front's status, logL and the hit count between them.
-__device__ int clip_pair_front(const double* b, int nb, const double* c, int nc, const Caps& cp,
-                               PairWork& w) {
-  PairResult res{PS_OK, 0, 0, 0.0, 0};
+// Kernels per pair: the front (rows A1-A7, one warp), the candidate pairs
+// (A8, one warp), the warp back end (A9-A18) with the thread back end for the
+// pairs it hands over, and the area; w.state carries the front's status,
+// logL, the hit count and the back end's route between them.
+// Rows A1-A7 of one pair by one warp, in the reference's order
+// (edge.h:190-202 edges; oacc_segment_tree.cpp:4513-4692 elementary
+// intervals; :203-206 and :616-689 realToInt borders; findBoarder; leaf
+// ranges), every loop shared among the lanes: the endpoint sort is a bitonic
+// network over (key, endpoint) pairs (the stable order), the elementary
+// array comes from a scan of per-endpoint entry counts.  Compares run on
+// order keys (okey).
+__device__ int clip_pair_front_warp(const double* b, int nb, const double* c, int nc,
+                                    const Caps& cp, PairWork& w, int lane) {
   const int E = nb + nc, n2 = 2 * E;
-  // ---- A1 edges (edge.h:190-202); ids are offsets into the interleaved arrays.
-  // Compares, minima and maxima run on order keys (okey): an FP64 compare
-  // issues at the FP64 rate, and here one thread works per pair.
-  double minI = bvx(b, nb, 0), maxI = minI;
-  long long kmin = okey(minI), kmax = kmin;
-  for (int e = 0; e < E; ++e) {
+  // ---- A1 edges; the x range on order keys (ties: the earlier vertex)
+  long long kmin = LLONG_MAX, kmax = LLONG_MIN;
+  int imin = INT_MAX, imax = INT_MAX;
+  for (int e = lane; e < E; e += 32) {
     double a0, a1, y0, y1;
     if (e < nb) {
       a0 = bvx(b, nb, e);
@@ -301,68 +313,117 @@ __device__ int clip_pair_front(const double* b, int nb, const double* c, int nc,
     }
     if (k0 < kmin) {
       kmin = k0;
-      minI = a0;
+      imin = e;
     }
     if (k0 > kmax) {
       kmax = k0;
-      maxI = a0;
+      imax = e;
     }
     const bool xs = k0 < k1, ys = ky0 < ky1;
     w.fbox[e] = make_float4(__double2float_rd(xs ? a0 : a1), __double2float_rd(ys ? y0 : y1),
                             __double2float_ru(xs ? a1 : a0), __double2float_ru(ys ? y1 : y0));
   }
-  // ---- A4 elementary intervals (:4513-4692): stable sort of the endpoints
-  auto val = [&](int idx) { return (idx & 1) ? w.ee[idx >> 1] : w.es[idx >> 1]; };
+  for (int o = 16; o > 0; o >>= 1) {
+    const long long km = __shfl_xor_sync(kFullMask, kmin, o), kx = __shfl_xor_sync(kFullMask, kmax, o);
+    const int im = __shfl_xor_sync(kFullMask, imin, o), ix = __shfl_xor_sync(kFullMask, imax, o);
+    if (km < kmin || (km == kmin && im < imin)) {
+      kmin = km;
+      imin = im;
+    }
+    if (kx > kmax || (kx == kmax && ix < imax)) {
+      kmax = kx;
+      imax = ix;
+    }
+  }
+  // the vertex values behind the extreme keys (edge e's first vertex)
+  auto vx0 = [&](int e) { return e < nb ? bvx(b, nb, e) : bvx(c, nc, e - nb); };
+  const double minI = vx0(imin), maxI = vx0(imax);
+  __syncwarp();
+  // ---- A4 elementary intervals: stable sort of the endpoints by key, the
+  // endpoint index breaking ties
   auto kval = [&](int idx) { return (idx & 1) ? w.kee[idx >> 1] : w.kes[idx >> 1]; };
-  for (int i = 0; i < n2; ++i) w.sidx[i] = i;
-  merge_sort(w.sidx, w.stmp, n2, [&](int x, int y) { return kval(x) < kval(y); });
-  for (int i = 0; i <= E; ++i) w.vl[i] = 0;
-  for (int j = 0; j < E; ++j) {
+  auto val = [&](int idx) { return (idx & 1) ? w.ee[idx >> 1] : w.es[idx >> 1]; };
+  const int np2 = npow2_dev(n2);
+  for (int m = lane; m < np2; m += 32) {
+    w.fkey[m] = m < n2 ? kval(m) : LLONG_MAX;
+    w.fval[m] = m < n2 ? m : INT_MAX;
+  }
+  __syncwarp();
+  for (int k = 2; k <= np2; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int m = lane; m < np2; m += 32) {
+        const int l = m ^ j;
+        if (l > m) {
+          const long long xk = w.fkey[m], yk = w.fkey[l];
+          const int xv = w.fval[m], yv = w.fval[l];
+          const bool gt = xk > yk || (xk == yk && xv > yv);
+          if (gt == ((m & k) == 0)) {
+            w.fkey[m] = yk;
+            w.fkey[l] = xk;
+            w.fval[m] = yv;
+            w.fval[l] = xv;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  for (int i = lane; i < n2; i += 32) w.sidx[i] = w.fval[i];
+  for (int i = lane; i <= E; i += 32) w.vl[i] = 0;
+  __syncwarp();
+  for (int j = lane; j < E; j += 32) {
     const int i = w.sidx[j] >> 1;
     if (w.kes[i] == w.kee[i]) w.vl[i] = 1;
   }
-  {
-    int s = 0;
-    for (int i = 0; i <= E; ++i) {
-      const int x = w.vl[i];
-      w.vl[i] = s;
-      s += x;
-    }
-    for (int i = 0; i < E; ++i)
-      if (w.vl[i] != w.vl[i + 1]) w.vloc[w.vl[i]] = i;
-  }
-  int count = 0;
-  double* ea = w.ea;
-  long long* kea = w.kea;
-  for (int i = 0; i < n2 - 1; ++i) {
+  __syncwarp();
+  warp_excl_scan(w.vl, E + 1);
+  __syncwarp();
+  for (int i = lane; i < E; i += 32)
+    if (w.vl[i] != w.vl[i + 1]) w.vloc[w.vl[i]] = i;
+  __syncwarp();
+  // entries per sorted endpoint i (0, 1, or 2 for the last pair), then their places
+  for (int i = lane; i < n2 - 1; i += 32) {
     const long long k0 = kval(w.sidx[i]), k1 = kval(w.sidx[i + 1]);
     const int intvi = w.sidx[i] >> 1;
     const int comid = w.vl[i / 2];
+    int n = 0;
     if (k0 != k1) {
-      kea[count] = k0;
-      ea[count++] = val(w.sidx[i]);
+      n = 1;
     } else if (w.kes[intvi] == w.kee[intvi]) {
       bool keep = comid == 0;
       if (!keep) {
         const int lookup = w.vloc[comid - 1];
         keep = w.kes[lookup] != w.kes[intvi] && w.kee[lookup] != w.kes[intvi];
       }
-      if (keep) {
-        kea[count] = w.kes[intvi];
-        ea[count++] = w.es[intvi];
+      n = keep ? 1 : 0;
+    }
+    if (i == n2 - 2 && k0 != k1) ++n;  // the last slot repeats v0
+    w.eflag[i] = n;
+  }
+  if (lane == 0) w.eflag[n2 - 1] = 0;
+  __syncwarp();
+  const int count = warp_excl_scan(w.eflag, n2);
+  __syncwarp();
+  if (count < 1) return PS_UNDEF;
+  double* ea = w.ea;
+  long long* kea = w.kea;
+  for (int i = lane; i < n2 - 1; i += 32) {
+    const int at = w.eflag[i], n = (i + 1 < n2 ? w.eflag[i + 1] : count) - at;
+    if (n == 0) continue;
+    const int si = w.sidx[i];
+    const long long k0 = kval(si), k1 = kval(w.sidx[i + 1]);
+    if (k0 != k1) {
+      for (int t = 0; t < n; ++t) {
+        kea[at + t] = k0;
+        ea[at + t] = val(si);
       }
-    }
-    if (i == n2 - 2 && k0 != k1) {  // the last slot repeats v0
-      kea[count] = k0;
-      ea[count++] = val(w.sidx[i]);
+    } else {
+      kea[at] = w.kes[si >> 1];
+      ea[at] = w.es[si >> 1];
     }
   }
-  if (count < 1) {
-    res.status = PS_UNDEF;
-    return res.status;
-  }
+  __syncwarp();
   const int epc = npow2_dev(count) + 1;
-  for (int i = count; i < epc; ++i) {
+  for (int i = count + lane; i < epc; i += 32) {
     ea[i] = ea[count - 1];
     kea[i] = kea[count - 1];
   }
@@ -372,32 +433,30 @@ __device__ int clip_pair_front(const double* b, int nb, const double* c, int nc,
   // ---- A6 borders (realToInt keys, :203-206 with 64-bit; digit sort :616-689)
   const double absMin = fabs(minI);
   const double dv = dadd(maxI, absMin);
-  if (!(dv < 2147483647.0)) {
-    res.status = PS_UNDEF;
-    return res.status;
-  }
+  if (!(dv < 2147483647.0)) return PS_UNDEF;
   int digits = 1;
   for (int iv = (int)trunc(dv); iv / 10 > 0; iv /= 10) ++digits;
   double scale = 1.0;
   for (int t = 0; t < 11 - digits; ++t) scale = dmul(scale, 10.0);
   const bool shift = minI < 0;
-  int z = 0;
+  __syncwarp();
+  int zl = 0;
+  bool bad = false;
   {
     auto key = [&](int t) -> long long {
       const double v = shift ? dmul(scale, dadd(ea[t], absMin)) : dmul(scale, ea[t]);
       return (long long)v;
     };
-    for (int i = 1; i < epc; ++i) {
+    for (int i = 1 + lane; i < epc; i += 32) {
       const long long ki = key(i);
-      if (ki < 0 || ki >= 100000000000LL || (i + 1 < epc && key(i + 1) < ki)) {
-        res.status = PS_UNDEF;
-        return res.status;
-      }
-      if (ki == 0) ++z;
+      if (ki < 0 || ki >= 100000000000LL || (i + 1 < epc && key(i + 1) < ki)) bad = true;
+      if (ki == 0) ++zl;
     }
   }
+  if (__any_sync(kFullMask, bad)) return PS_UNDEF;
+  const int z = __reduce_add_sync(kFullMask, zl);
   const BordersS B{kea, epc, z};
-  for (int e = 0; e < E; ++e) {
+  for (int e = lane; e < E; e += 32) {
     int a = -1, bb = -1;
     const long long kee = w.kee[e], kes = w.kes[e];
     const int en = find_border_s(B, kee);
@@ -437,8 +496,12 @@ __device__ int clip_pair_front(const double* b, int nb, const double* c, int nc,
     }
     w.lr[e] = make_int2(l, lo > l ? lo : l);
   }
-  w.state[1] = logL;
-  w.state[2] = 0;
+  __syncwarp();
+  if (lane == 0) {
+    w.state[1] = logL;
+    w.state[2] = 0;
+  }
+  __syncwarp();
   return PS_OK;
 }
 
@@ -965,27 +1028,33 @@ struct ClipArgs {
   }
 };
 
-__global__ void __launch_bounds__(kBatchBlock) k_batch_front(ClipArgs A) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= A.np) return;
-  const int p = t;
+__global__ void __launch_bounds__(128) k_batch_front(ClipArgs A) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  if ((t >> 5) >= A.np) return;
+  const int p = (int)(t >> 5);
   const int pass = A.pass_of ? A.pass_of[p] : 0;
   if (pass < 0) return;  // settled in an earlier pass, or a large pair
   int nb, nc;
   if (!A.small(p, &nb, &nc)) {
-    A.status[p] = SBC_EINPUT;
-    A.nrings[p] = A.nverts[p] = 0;
-    A.area[p] = 0.0;
+    if (lane == 0) {
+      A.status[p] = SBC_EINPUT;
+      A.nrings[p] = A.nverts[p] = 0;
+      A.area[p] = 0.0;
+    }
     return;
   }
   Caps cp;
   PairWork w = A.work(p, nb, nc, pass, &cp);
-  const int st = clip_pair_front(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w);
-  w.state[0] = st;
-  if (st != PS_OK) {
-    A.status[p] = st == PS_UNDEF ? SBC_EUNDEF : SBC_ENOMEM;
-    A.nrings[p] = A.nverts[p] = 0;
-    A.area[p] = 0.0;
+  const int st =
+      clip_pair_front_warp(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w, lane);
+  if (lane == 0) {
+    w.state[0] = st;
+    if (st != PS_OK) {
+      A.status[p] = st == PS_UNDEF ? SBC_EUNDEF : SBC_ENOMEM;
+      A.nrings[p] = A.nverts[p] = 0;
+      A.area[p] = 0.0;
+    }
   }
 }
 
@@ -1253,7 +1322,7 @@ __global__ void k_graph_passes(int n, const int* __restrict__ pass, const int* _
 void launch_clip(const ClipArgs& A, const BatchShape& sh, double in_bytes, cudaStream_t st) {
   {
     ::sbc::KProbe kp_("k_batch_front", st, in_bytes);
-    k_batch_front<<<grid_for(A.np, sh.front), sh.front, 0, st>>>(A);
+    k_batch_front<<<grid_for(32LL * A.np, sh.front), sh.front, 0, st>>>(A);
   }
   {
     ::sbc::KProbe kp_("k_batch_cand", st, in_bytes);
