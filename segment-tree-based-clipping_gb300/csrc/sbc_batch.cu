@@ -105,6 +105,7 @@ struct PairWork {
   long long* fkey;
   int* fval;
   int* eflag;  // per sorted endpoint: entries it adds to the elementary array
+  unsigned long long* csort;  // the candidate sweep's overlay edges by box min x
 };
 
 __host__ __device__ __forceinline__ void carve_pool(Carver& cv, int cap, Pool& p) {
@@ -195,6 +196,7 @@ __host__ __device__ __forceinline__ PairWork carve(Carver& cv, const Caps& c) {
   w.fkey = cv.take<long long>(npow2_dev(n2));
   w.fval = cv.take<int>(npow2_dev(n2));
   w.eflag = cv.take<int>(n2 + 1);
+  w.csort = cv.take<unsigned long long>(npow2_dev(c.nc));
   return w;
 }
 
@@ -513,6 +515,7 @@ __device__ int clip_pair_front_warp(const double* b, int nb, const double* c, in
 // a hundred pass the filters, and FP64 run by a few lanes costs the issue
 // slots of all 32.
 constexpr int kCandQ = 64;
+constexpr long long kSweepMin = 4096;  // pairs with more edge pairs sweep in x
 __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc, const Caps& cp,
                                PairWork& w, int lane, int2* q) {
   const unsigned full = 0xffffffffu;
@@ -544,20 +547,7 @@ __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc,
     }
     __syncwarp();
   };
-  int be = 0, j = lane;
-  while (j >= nc && be < nb) {
-    j -= nc;
-    ++be;
-  }
-  while (__any_sync(full, be < nb)) {
-    bool pass = false;
-    if (be < nb) {
-      const float4 fb = w.fbox[be];
-      const float4 fc = w.fbox[nb + j];
-      if (!(fb.x > fc.z || fb.z < fc.x || fb.y > fc.w || fb.w < fc.y))
-        pass = lsmf_d(bvx(b, nb, be), bvy(b, nb, be), bvx(b, nb, be + 1), bvy(b, nb, be + 1),
-                      bvx(c, nc, j), bvy(c, nc, j), bvx(c, nc, j + 1), bvy(c, nc, j + 1));
-    }
+  auto enqueue = [&](bool pass, int be, int j) {
     const unsigned m = __ballot_sync(full, pass);
     if (pass) q[nq + __popc(m & ((1u << lane) - 1u))] = make_int2(be, j);
     nq += __popc(m);
@@ -571,6 +561,72 @@ __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc,
       nq = rest;
       __syncwarp();
     }
+  };
+  auto boxes_meet = [](const float4& fb, const float4& fc) {
+    return !(fb.x > fc.z || fb.z < fc.x || fb.y > fc.w || fb.w < fc.y);
+  };
+  if ((long long)nb * nc > kSweepMin) {
+    // Sweep in x: the overlay edges sorted by box min x (float order key,
+    // -0 as +0, then the edge); a base edge's candidates are the overlay
+    // edges with min x in [its min x - the largest overlay x extent, its max
+    // x], every box-overlapping pair among them
+    auto fk = [](float f) {
+      const unsigned u = __float_as_uint(f == 0.f ? 0.f : f);
+      return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    };
+    warp_bitonic(nc, w.csort, [&](int k) {
+      return ((unsigned long long)fk(w.fbox[nb + k].x) << 32) | (unsigned)k;
+    });
+    float ext = 0.f;
+    for (int k = lane; k < nc; k += 32) ext = fmaxf(ext, __fsub_ru(w.fbox[nb + k].z, w.fbox[nb + k].x));
+    for (int o = 16; o > 0; o >>= 1) ext = fmaxf(ext, __shfl_xor_sync(full, ext, o));
+    // first sorted position whose min-x key exceeds kx (or reaches it: ge)
+    auto bound = [&](unsigned kx, bool ge) {
+      int lo = 0, hi = nc;
+      while (lo < hi) {
+        const int m = (lo + hi) >> 1;
+        const unsigned km = (unsigned)(w.csort[m] >> 32);
+        if (ge ? km < kx : km <= kx) lo = m + 1;
+        else hi = m;
+      }
+      return lo;
+    };
+    for (int be0 = 0; be0 < nb; be0 += 32) {
+      const int be = be0 + lane;
+      int k = 0, kend = 0;
+      float4 fb = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (be < nb) {
+        fb = w.fbox[be];
+        k = bound(fk(__fsub_rd(fb.x, ext)), true);
+        kend = bound(fk(fb.z), false);
+      }
+      while (__any_sync(full, k < kend)) {
+        bool pass = false;
+        int j = 0;
+        if (k < kend) {
+          j = (int)(unsigned)w.csort[k];
+          ++k;
+          if (boxes_meet(fb, w.fbox[nb + j]))
+            pass = lsmf_d(bvx(b, nb, be), bvy(b, nb, be), bvx(b, nb, be + 1), bvy(b, nb, be + 1),
+                          bvx(c, nc, j), bvy(c, nc, j), bvx(c, nc, j + 1), bvy(c, nc, j + 1));
+        }
+        enqueue(pass, be, j);
+      }
+    }
+    if (nq > 0) classify(nq);
+    return;
+  }
+  int be = 0, j = lane;
+  while (j >= nc && be < nb) {
+    j -= nc;
+    ++be;
+  }
+  while (__any_sync(full, be < nb)) {
+    bool pass = false;
+    if (be < nb && boxes_meet(w.fbox[be], w.fbox[nb + j]))
+      pass = lsmf_d(bvx(b, nb, be), bvy(b, nb, be), bvx(b, nb, be + 1), bvy(b, nb, be + 1),
+                    bvx(c, nc, j), bvy(c, nc, j), bvx(c, nc, j + 1), bvy(c, nc, j + 1));
+    enqueue(pass, be, j);
     j += 32;
     while (j >= nc && be < nb) {
       j -= nc;
