@@ -515,7 +515,7 @@ __device__ int clip_pair_front_warp(const double* b, int nb, const double* c, in
 // a hundred pass the filters, and FP64 run by a few lanes costs the issue
 // slots of all 32.
 constexpr int kCandQ = 64;
-constexpr long long kSweepMin = 4096;  // pairs with more edge pairs sweep in x
+constexpr long long kSweepMin = 16384;  // pairs with more edge pairs sweep in x
 __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc, const Caps& cp,
                                PairWork& w, int lane, int2* q) {
   const unsigned full = 0xffffffffu;

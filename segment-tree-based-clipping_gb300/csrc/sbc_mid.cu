@@ -265,30 +265,43 @@ __global__ void k_alpha_sort(const int* __restrict__ list, const unsigned* __res
   if (x >= *count) return;
   const int e = list[x];
   const int s = allPS[e], m = allPS[e + 1] - s;  // 2 <= m <= kSegShort
-  // the run's keys read once into a thread-local copy, then a stable
-  // insertion sort of (key, record) on the copy
+  // The run's (key, record) pairs in registers, padded past m, sorted by an
+  // odd-even transposition network on (key, record): fixed indices keep the
+  // arrays in registers, and the record breaking ties gives the stable order.
   int kk[kSegShort], ii[kSegShort];
-  for (int i = 0; i < m; ++i) {
-    const int a = alpha[order ? order[s + i] : s + i];
-    if (a < 0) {
-      atomicOr(flags, (unsigned)kFlagUndef);
-      return;
+  bool neg = false;
+#pragma unroll
+  for (int i = 0; i < kSegShort; ++i) {
+    if (i < m) {
+      const int a = alpha[order ? order[s + i] : s + i];
+      neg |= a < 0;
+      kk[i] = a % 1000000000;
+      ii[i] = s + i;
+    } else {
+      kk[i] = INT_MAX;
+      ii[i] = INT_MAX;
     }
-    kk[i] = a % 1000000000;
-    ii[i] = s + i;
   }
-  for (int i = 1; i < m; ++i) {
-    const int kp = kk[i], p = ii[i];
-    int j = i;
-    while (j > 0 && kk[j - 1] > kp) {
-      kk[j] = kk[j - 1];
-      ii[j] = ii[j - 1];
-      --j;
+  if (neg) {
+    atomicOr(flags, (unsigned)kFlagUndef);
+    return;
+  }
+#pragma unroll
+  for (int r = 0; r < kSegShort; ++r) {
+#pragma unroll
+    for (int i = r & 1; i + 1 < kSegShort; i += 2) {
+      const bool sw = kk[i] > kk[i + 1] || (kk[i] == kk[i + 1] && ii[i] > ii[i + 1]);
+      const int k0 = sw ? kk[i + 1] : kk[i], k1 = sw ? kk[i] : kk[i + 1];
+      const int i0 = sw ? ii[i + 1] : ii[i], i1 = sw ? ii[i] : ii[i + 1];
+      kk[i] = k0;
+      kk[i + 1] = k1;
+      ii[i] = i0;
+      ii[i + 1] = i1;
     }
-    kk[j] = kp;
-    ii[j] = p;
   }
-  for (int i = 0; i < m; ++i) sorted[s + i] = ii[i];
+#pragma unroll
+  for (int i = 0; i < kSegShort; ++i)
+    if (i < m) sorted[s + i] = ii[i];
 }
 
 // Long edges, one warp each: the stable position of record i is the number
