@@ -66,6 +66,10 @@ def lib():
         L.sbco_tree_data.restype = ctypes.c_void_p
         L.sbco_tree_data.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.sbco_segment_intersection.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_void_p] * 2
+        L.sbco_clip_components.restype = ctypes.c_void_p
+        L.sbco_clip_components.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                           ctypes.c_void_p, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -86,6 +90,30 @@ def clip(base: np.ndarray, overlays, union: bool = False) -> dict:
     cxy = np.ascontiguousarray(np.concatenate(ovs, axis=0))
     sizes = np.array([o.shape[0] for o in ovs], dtype=np.int32)
     run = L.sbco_clip(b.ctypes.data, b.shape[0], cxy.ctypes.data, sizes.ctypes.data, len(ovs))
+    return _collect(L, run, len(ovs))
+
+
+def comps_of(comps):
+    """(xy, offsets) of a list of (n_i, 2) component arrays."""
+    comps = [np.ascontiguousarray(c, dtype=np.float64).reshape(-1, 2) for c in comps]
+    off = np.zeros(len(comps) + 1, dtype=np.int32)
+    off[1:] = np.cumsum([c.shape[0] for c in comps])
+    return np.ascontiguousarray(np.concatenate(comps, axis=0)), off
+
+
+def clip_components(base_comps, overlay_comps, union: bool = False) -> dict:
+    """The restatement on one base and one overlay given as lists of
+    components (holes and islands, Foster's .poly format)."""
+    L = lib()
+    L.sbco_set_union(1 if union else 0)
+    b, bo = comps_of(base_comps)
+    c, co = comps_of(overlay_comps)
+    run = L.sbco_clip_components(b.ctypes.data, b.shape[0], bo.ctypes.data, len(bo) - 1,
+                                 c.ctypes.data, c.shape[0], co.ctypes.data, len(co) - 1)
+    return _collect(L, run, 1)
+
+
+def _collect(L, run, k: int) -> dict:
     try:
         st = L.sbco_status(run)
         if st != 0:
@@ -98,7 +126,7 @@ def clip(base: np.ndarray, overlays, union: bool = False) -> dict:
             ct = ctypes.c_double if name == "ea" else ctypes.c_int
             a = np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ct)), (max(n, 1),))[:n]
             out["tree"][name] = a.copy()
-        for ov in range(1, len(ovs) + 1):
+        for ov in range(1, k + 1):
             d = {}
             for w, name in enumerate(ARRAYS):
                 n = L.sbco_len(run, ov, w)
@@ -249,17 +277,22 @@ def write_poly_components(path, comps) -> None:
             f.write(",\n".join(lines) + ";\n")
 
 
-def run_foster(base: np.ndarray, overlay: np.ndarray, timeout: float = 1800.0) -> dict:
+def run_foster(base, overlay, timeout: float = 1800.0, union: bool = False) -> dict:
     """Run oracle/_ref/foster on one pair (stdout discarded): the result rings
-    (precision 6, the program's output format) and the wall time in ms."""
+    (precision 6, the program's output format) and the wall time in ms.  A
+    polygon is one (n, 2) array or a list of component arrays."""
+    def comps(p):
+        return list(p) if isinstance(p, (list, tuple)) else [p]
+
     with tempfile.TemporaryDirectory() as td:
         td = Path(td)
-        write_poly_components(td / "p.poly", [base])
-        write_poly_components(td / "q.poly", [overlay])
+        write_poly_components(td / "p.poly", comps(base))
+        write_poly_components(td / "q.poly", comps(overlay))
+        args = [str(FOSTER_EXE)] + (["-union"] if union else [])
         t0 = time.perf_counter()
-        p = subprocess.run([str(FOSTER_EXE), str(td / "p.poly"), str(td / "q.poly"),
-                            str(td / "r.poly")], stdout=subprocess.DEVNULL,
-                           stderr=subprocess.PIPE, text=True, timeout=timeout)
+        p = subprocess.run(args + [str(td / "p.poly"), str(td / "q.poly"), str(td / "r.poly")],
+                           stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True,
+                           timeout=timeout)
         wall = (time.perf_counter() - t0) * 1e3
         if p.returncode != 0:
             raise RuntimeError(f"foster exited {p.returncode}: {p.stderr[-400:]}")

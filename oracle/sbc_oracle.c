@@ -249,6 +249,11 @@ typedef struct {
   double *cP;  /* (clSize+k)*2 */
   int nb, k, clSize;
   int *cS;     /* k+1 prefix of (c_i+1) */
+  /* end vertex of the edge that starts at each vertex: bnx[v] indexes bP
+   * (v+1 for a single ring, whose last edge ends at the closing copy), cnx
+   * indexes cP's slots; with several components an edge from a component's
+   * last vertex ends at that component's first vertex */
+  int *bnx, *cnx;
   /* edges (intervals), src/clip.cpp:207-298 */
   int E;
   int *eid, *etype;
@@ -265,7 +270,7 @@ typedef struct {
 } tree_t;
 
 static void tree_free(tree_t *t) {
-  free(t->bP); free(t->cP); free(t->cS);
+  free(t->bP); free(t->cP); free(t->cS); free(t->bnx); free(t->cnx);
   free(t->eid); free(t->etype); free(t->es); free(t->ee);
   free(t->ea); free(t->nia);
   free(t->cov_off); free(t->cov_edge);
@@ -280,9 +285,15 @@ static void put_edge(tree_t *t, int e, int id, int type, double a, double b) {
   else { t->ee[e] = a; t->es[e] = b; }
 }
 
-/* gpc_read_multi_polygon, src/clip.cpp:172-311 (from arrays, not files). */
+/* gpc_read_multi_polygon, src/clip.cpp:172-311 (from arrays, not files).
+ * bcomp/ccomp (NULL: one ring each) split the base and the single overlay
+ * into components (Foster's .poly format, lib/optimizedFostersAlgorithm/
+ * README.md:43-62): component i is vertices [comp[i], comp[i+1]).  Edges keep
+ * the reference's order, one per vertex in vertex order; every component
+ * closes on its own first vertex, and closing edges leave the interval
+ * bounds alone as the reference's closing edges do (:233-237). */
 static int read_input(tree_t *t, const double *bxy, int nb, const double *cxy, const int *csz,
-                      int k) {
+                      int k, const int *bcomp, int nbc, const int *ccomp, int ncc) {
   t->nb = nb;
   t->k = k;
   t->clSize = 0;
@@ -295,38 +306,47 @@ static int read_input(tree_t *t, const double *bxy, int nb, const double *cxy, c
   t->etype = (int *)malloc(sizeof(int) * (size_t)t->E);
   t->es = (double *)malloc(sizeof(double) * (size_t)t->E);
   t->ee = (double *)malloc(sizeof(double) * (size_t)t->E);
-  if (!t->cS || !t->bP || !t->cP || !t->eid || !t->etype || !t->es || !t->ee) return -1;
+  t->bnx = (int *)malloc(sizeof(int) * (size_t)nb);
+  t->cnx = (int *)malloc(sizeof(int) * ((size_t)t->clSize + k));
+  if (!t->cS || !t->bP || !t->cP || !t->eid || !t->etype || !t->es || !t->ee || !t->bnx ||
+      !t->cnx)
+    return -1;
   for (int i = 0; i < k; ++i) t->cS[i + 1] = t->cS[i] + csz[i] + 1;
   memcpy(t->bP, bxy, sizeof(double) * 2 * (size_t)nb);
   t->bP[2 * nb] = t->bP[0];
   t->bP[2 * nb + 1] = t->bP[1];
-  int id = 0;
-  for (int v = 1; v < nb; ++v) {
-    put_edge(t, id, 2 * v - 2, 0, t->bP[2 * v - 2], t->bP[2 * v]);
-    if (v == 1) { t->minI = t->es[id]; t->maxI = t->ee[id]; }
-    if (t->minI > t->es[id]) t->minI = t->es[id];
-    if (t->maxI < t->ee[id]) t->maxI = t->ee[id];
+  for (int v = 0; v < nb; ++v) t->bnx[v] = v + 1;
+  for (int i = 0; bcomp && i < nbc; ++i) t->bnx[bcomp[i + 1] - 1] = bcomp[i];
+  int id = 0, first = 1;
+  for (int v = 0; v < nb; ++v) {
+    const int w = t->bnx[v];
+    put_edge(t, id, 2 * v, 0, t->bP[2 * v], t->bP[2 * w]);
+    if (w == v + 1 && v + 1 < nb) {
+      if (first) { t->minI = t->es[id]; t->maxI = t->ee[id]; first = 0; }
+      if (t->minI > t->es[id]) t->minI = t->es[id];
+      if (t->maxI < t->ee[id]) t->maxI = t->ee[id];
+    }
     id++;
   }
-  /* closing base edge: no min/max update (src/clip.cpp:233-237) */
-  put_edge(t, id++, 2 * nb - 2, 0, t->bP[2 * nb - 2], t->bP[2 * nb]);
   long off = 0;
   for (int i = 0; i < k; ++i) {
     int c = csz[i];
-    int v2 = 2 * t->cS[i];
-    memcpy(t->cP + v2, cxy + off, sizeof(double) * 2 * (size_t)c);
+    int v0 = t->cS[i];
+    memcpy(t->cP + 2 * v0, cxy + off, sizeof(double) * 2 * (size_t)c);
     off += 2L * c;
-    for (int v = 1; v < c; ++v) {
-      int w = v2 + 2 * v;
-      put_edge(t, id, w - 2, i + 1, t->cP[w - 2], t->cP[w]);
-      if (t->minI > t->es[id]) t->minI = t->es[id];
-      if (t->maxI < t->ee[id]) t->maxI = t->ee[id];
+    t->cP[2 * (v0 + c)] = t->cP[2 * v0];
+    t->cP[2 * (v0 + c) + 1] = t->cP[2 * v0 + 1];
+    for (int v = 0; v <= c; ++v) t->cnx[v0 + v] = v0 + v + 1;
+    for (int j = 0; ccomp && j < ncc; ++j) t->cnx[v0 + ccomp[j + 1] - 1] = v0 + ccomp[j];
+    for (int v = 0; v < c; ++v) {
+      const int w = t->cnx[v0 + v];
+      put_edge(t, id, 2 * (v0 + v), i + 1, t->cP[2 * (v0 + v)], t->cP[2 * w]);
+      if (w == v0 + v + 1 && v + 1 < c) {
+        if (t->minI > t->es[id]) t->minI = t->es[id];
+        if (t->maxI < t->ee[id]) t->maxI = t->ee[id];
+      }
       id++;
     }
-    int l = v2 + 2 * c;
-    t->cP[l] = t->cP[v2];
-    t->cP[l + 1] = t->cP[v2 + 1];
-    put_edge(t, id++, l - 2, i + 1, t->cP[l - 2], t->cP[l]);
   }
   return 0;
 }
@@ -626,11 +646,11 @@ static int candidates(const tree_t *t, int cType, ivec *rb, ivec *rc, ivec *rt) 
         if (t->etype[it] == 0 && t->etype[in] == cType) { bId = t->eid[it]; cId = t->eid[in]; go = 1; }
         else if (t->etype[it] == cType && t->etype[in] == 0) { bId = t->eid[in]; cId = t->eid[it]; go = 1; }
         if (!go) continue;
-        if (lsmf(bP[bId], bP[bId + 1], bP[bId + 2], bP[bId + 3], cP[cId], cP[cId + 1], cP[cId + 2],
-                 cP[cId + 3])) {
+        const double *bq = bP + 2 * t->bnx[bId / 2], *cq = cP + 2 * t->cnx[cId / 2];
+        if (lsmf(bP[bId], bP[bId + 1], bq[0], bq[1], cP[cId], cP[cId + 1], cq[0], cq[1])) {
           double al, be;
-          int ty = seg_isect(bP[bId], bP[bId + 1], bP[bId + 2], bP[bId + 3], cP[cId], cP[cId + 1],
-                             cP[cId + 2], cP[cId + 3], &al, &be);
+          int ty = seg_isect(bP[bId], bP[bId + 1], bq[0], bq[1], cP[cId], cP[cId + 1], cq[0],
+                             cq[1], &al, &be);
           if (ty && (iv_push(rb, bId) || iv_push(rc, cId) || iv_push(rt, ty))) goto fail;
         }
       }
@@ -640,11 +660,11 @@ static int candidates(const tree_t *t, int cType, ivec *rb, ivec *rc, ivec *rt) 
         if (t->etype[it] == 0 && t->etype[en] == cType) { bId = t->eid[it]; cId = t->eid[en]; go = 1; }
         else if (t->etype[it] == cType && t->etype[en] == 0) { cId = t->eid[it]; bId = t->eid[en]; go = 1; }
         if (!go) continue;
-        if (lsmf(bP[bId], bP[bId + 1], bP[bId + 2], bP[bId + 3], cP[cId], cP[cId + 1], cP[cId + 2],
-                 cP[cId + 3])) {
+        const double *bq = bP + 2 * t->bnx[bId / 2], *cq = cP + 2 * t->cnx[cId / 2];
+        if (lsmf(bP[bId], bP[bId + 1], bq[0], bq[1], cP[cId], cP[cId + 1], cq[0], cq[1])) {
           double al, be;
-          int ty = seg_isect(bP[bId], bP[bId + 1], bP[bId + 2], bP[bId + 3], cP[cId], cP[cId + 1],
-                             cP[cId + 2], cP[cId + 3], &al, &be);
+          int ty = seg_isect(bP[bId], bP[bId + 1], bq[0], bq[1], cP[cId], cP[cId + 1], cq[0],
+                             cq[1], &al, &be);
           if (ty && (iv_push(rb, bId) || iv_push(rc, cId) || iv_push(rt, ty))) goto fail;
         }
       }
@@ -908,81 +928,85 @@ static void cleanup(rings_t *R) {
   }
 }
 
+/* roots[s][k]: the list node of side s's component k's first vertex (its
+ * merged slot); roots[s][nr[s]] = the side's slot count.  One component per
+ * side reproduces the reference (root 0). */
 typedef struct {
   pool_t P, Q;
-  int rootP, rootQ;
+  int *roots[2];
+  int nr[2];
 } lists_t;
 
-/* copyToLinkedList, src/clip.cpp:606-695, restated over slot arrays.  The
- * list order equals the slot order; a source vertex matched early by an
- * intersection vertex with identical coordinates makes the reference's
- * bookkeeping undefined (rejected here). */
-static int build_lists(lists_t *Ls, const double *bPoly, int bSize, const double *cPoly,
-                       int cStart, int cSize, const double *ixB, const double *ixC,
+/* copyToLinkedList, src/clip.cpp:606-695, restated over slot arrays, one
+ * component after another (each walked from its first vertex and closed on
+ * it, as the reference's single ring is).  The list order equals the slot
+ * order; a source vertex matched early by an intersection vertex with
+ * identical coordinates makes the reference's bookkeeping undefined
+ * (rejected here).  vs[k] .. vs[k+1] are component k's source vertices. */
+static int build_side(pool_t *P, pool_t *O, int is_q, const double *poly, int start,
+                      const int *vs, int nr, const int *roots, const double *ix, int n,
+                      const int *alpha, const int *nb, const int *lab) {
+  for (int k = 0; k < nr; ++k) {
+    const int lo = roots[k], hi = roots[k + 1];
+    int i = lo;
+    for (int ii = vs[k]; ii <= vs[k + 1]; ++ii) {
+      const int last = ii == vs[k + 1];
+      const int srcv = last ? vs[k] : ii;
+      const double vx = poly[2 * (start + srcv)], vy = poly[2 * (start + srcv) + 1];
+      for (;;) {
+        const int sl = i == hi ? lo : i;
+        if (i > hi || (ix[2 * sl] == vx && ix[2 * sl + 1] == vy)) break;
+        if (i >= hi) return -2;
+        int v = pool_new(P, ix[2 * i], ix[2 * i + 1]);
+        P->label[v] = lab[i];
+        P->isect[v] = 1;
+        if (is_q) {
+          int t = nb[i] - 1;
+          if (t < 0 || t >= O->n) return -2;
+          P->nb[v] = t;
+          O->nb[t] = v;
+        }
+        i++;
+      }
+      if (i > hi) return -2;
+      if (!last) {
+        int v = pool_new(P, vx, vy);
+        if (v != i) return -2;
+        P->source[v] = 1;
+        P->label[v] = lab[i];
+        if (!is_q) {
+          if (alpha[i] != -100) P->isect[v] = 1;
+        } else if (nb[i] != -100) {
+          int t = nb[i] - 1;
+          if (t < 0 || t >= O->n) return -2;
+          P->isect[v] = 1;
+          P->nb[v] = t;
+          O->nb[t] = v;
+        }
+      }
+      i++;
+    }
+    for (int v = lo; v < hi; ++v) {
+      P->next[v] = v + 1 == hi ? lo : v + 1;
+      P->prev[v] = v == lo ? hi - 1 : v - 1;
+    }
+  }
+  return P->n == n ? 0 : -2;
+}
+
+static int build_lists(lists_t *Ls, const double *bPoly, const double *cPoly, int cStart,
+                       const int *vsB, const int *vsC, const double *ixB, const double *ixC,
                        const int *alphaB, const int *nbC, int nB, int nQ, const int *labB,
                        const int *labC, int extra) {
   pool_t *P = &Ls->P, *Q = &Ls->Q;
   if (pool_init(P, nB + extra) || pool_init(Q, nQ + extra)) return -1;
-  /* P: walk source vertices and slots */
-  int i = 0;
-  for (int ii = 0; ii <= bSize; ++ii) {
-    int srcv = ii < bSize ? ii : 0;
-    double vx = bPoly[2 * srcv], vy = bPoly[2 * srcv + 1];
-    while (ixB[(2 * i) % (2 * nB)] != vx || ixB[(2 * i + 1) % (2 * nB)] != vy) {
-      if (ii < bSize && i >= nB) return -2;
-      if (i >= nB) return -2;
-      int v = pool_new(P, ixB[2 * i], ixB[2 * i + 1]);
-      P->label[v] = labB[i];
-      P->isect[v] = 1;
-      i++;
-    }
-    if (ii < bSize) {
-      int v = pool_new(P, vx, vy);
-      if (v != i) return -2;
-      P->source[v] = 1;
-      P->label[v] = labB[i];
-      if (alphaB[i] != -100) P->isect[v] = 1;
-    }
-    i++;
-  }
-  if (P->n != nB) return -2;
-  for (int v = 0; v < nB; ++v) { P->next[v] = (v + 1) % nB; P->prev[v] = (v + nB - 1) % nB; }
-  /* Q */
-  i = 0;
-  for (int ii = 0; ii <= cSize; ++ii) {
-    int srcv = ii < cSize ? ii : 0;
-    double vx = cPoly[2 * (cStart + srcv)], vy = cPoly[2 * (cStart + srcv) + 1];
-    while (ixC[(2 * i) % (2 * nQ)] != vx || ixC[(2 * i + 1) % (2 * nQ)] != vy) {
-      if (i >= nQ) return -2;
-      int v = pool_new(Q, ixC[2 * i], ixC[2 * i + 1]);
-      Q->label[v] = labC[i];
-      Q->isect[v] = 1;
-      int t = nbC[i] - 1;
-      if (t < 0 || t >= nB) return -2;
-      Q->nb[v] = t;
-      P->nb[t] = v;
-      i++;
-    }
-    if (ii < cSize) {
-      int v = pool_new(Q, vx, vy);
-      if (v != i) return -2;
-      Q->source[v] = 1;
-      Q->label[v] = labC[i];
-      if (nbC[i] != -100) {
-        int t = nbC[i] - 1;
-        if (t < 0 || t >= nB) return -2;
-        Q->isect[v] = 1;
-        Q->nb[v] = t;
-        P->nb[t] = v;
-      }
-    }
-    i++;
-  }
-  if (Q->n != nQ) return -2;
-  for (int v = 0; v < nQ; ++v) { Q->next[v] = (v + 1) % nQ; Q->prev[v] = (v + nQ - 1) % nQ; }
-  Ls->rootP = 0;
-  Ls->rootQ = 0;
-  return 0;
+  int r = build_side(P, Q, 0, bPoly, 0, vsB, Ls->nr[0], Ls->roots[0], ixB, nB, alphaB, NULL,
+                     labB);
+  if (r) return r;
+  /* the base's node count is its slot count: a neighbour id past it is
+   * undefined, as the reference's (t >= nB) check */
+  return build_side(Q, P, 1, cPoly, cStart, vsC, Ls->nr[1], Ls->roots[1], ixC, nQ, NULL, nbC,
+                    labC);
 }
 
 /* neighbour of vertex v of polygon `side` lives in the other polygon */
@@ -1051,13 +1075,26 @@ static void toggle(int *st) {
 static int g_union = 0;
 void sbco_set_union(int on) { g_union = on ? 1 : 0; }
 
-/* labelIntersections2 + createResult2, foster/polyclip.h:337-759 */
+/* pointInPoly against every component of side s: a component toggles the
+ * answer when it contains the point (lib/optimizedFostersAlgorithm/
+ * polyclip.cpp:503-507, :593-595); one component is the reference's test */
+static int point_in_side(lists_t *Ls, int s, double x, double y) {
+  int in = 0;
+  for (int k = 0; k < Ls->nr[s]; ++k) in ^= point_in_poly(side_pool(Ls, s), Ls->roots[s][k], x, y);
+  return in;
+}
+
+/* labelIntersections2 + createResult2, foster/polyclip.h:337-759, over every
+ * component of both sides in the order of Foster's multi-component code
+ * (lib/optimizedFostersAlgorithm/polyclip.cpp:335-780): chains, interior and
+ * identical components, entry/exit flags per component, and the result
+ * traced from P's components in order. */
 static int label_and_trace(lists_t *Ls, rings_t *R) {
   pool_t *P = &Ls->P, *Q = &Ls->Q;
-  int roots[2] = {Ls->rootP, Ls->rootQ};
   /* (2) intersection chains on P */
-  {
-    int V = roots[0];
+  for (int k = 0; k < Ls->nr[0]; ++k) {
+    const int root = Ls->roots[0][k];
+    int V = root;
     do {
       if (P->isect[V] && (P->label[V] == L_LEFT_ON || P->label[V] == L_RIGHT_ON)) {
         int x = P->label[V] == L_LEFT_ON ? 0 : 1; /* LEFT=0 RIGHT=1 */
@@ -1079,13 +1116,21 @@ static int label_and_trace(lists_t *Ls, rings_t *R) {
         Q->label[P->nb[I]] = chain;
       }
       V = P->next[V];
-    } while (V != roots[0]);
+    } while (V != root);
   }
-  /* (3.5) special cases */
-  int noIsect[2] = {0, 0}, ident[2] = {0, 0};
-  for (int s = 0; s < 2; ++s) {
+  /* (3.5) special cases, per component */
+  unsigned char *noIsect[2], *ident[2];
+  noIsect[0] = (unsigned char *)calloc((size_t)Ls->nr[0] + 1, 1);
+  noIsect[1] = (unsigned char *)calloc((size_t)Ls->nr[1] + 1, 1);
+  ident[0] = (unsigned char *)calloc((size_t)Ls->nr[0] + 1, 1);
+  ident[1] = (unsigned char *)calloc((size_t)Ls->nr[1] + 1, 1);
+  unsigned char *split[2] = {NULL, NULL}, *cross[2] = {NULL, NULL};
+  int rc = -1;
+  if (!noIsect[0] || !noIsect[1] || !ident[0] || !ident[1]) goto done;
+  for (int s = 0; s < 2; ++s)
+  for (int k = 0; k < Ls->nr[s]; ++k) {
     pool_t *p = side_pool(Ls, s);
-    int nocross = 1, root = roots[s];
+    int nocross = 1, root = Ls->roots[s][k];
     int V = root;
     do {
       if (p->isect[V] && (p->label[V] == L_CROSSING || p->label[V] == L_DELAYED_CROSSING)) nocross = 0;
@@ -1096,7 +1141,7 @@ static int label_and_trace(lists_t *Ls, rings_t *R) {
       V = p->next[V];
     } while (V != root);
     if (!nocross) continue;
-    noIsect[s] = 1;
+    noIsect[s][k] = 1;
     int allon = 1;
     V = root;
     do {
@@ -1104,40 +1149,55 @@ static int label_and_trace(lists_t *Ls, rings_t *R) {
       V = p->next[V];
     } while (V != root);
     if (allon) {
-      ident[s] = 1;
+      ident[s][k] = 1;
     } else {
       double px, py;
-      if (non_isect_point(Ls, s, root, &px, &py)) return -2;
-      if (point_in_poly(side_pool(Ls, OTHER(s)), roots[OTHER(s)], px, py) ^ g_union)
-        if (ring_copy_list(R, p, root)) return -1;
+      if (non_isect_point(Ls, s, root, &px, &py)) { rc = -2; goto done; }
+      if (point_in_side(Ls, OTHER(s), px, py) ^ g_union)
+        if (ring_copy_list(R, p, root)) goto done;
     }
   }
-  /* identical components: P added when Q is identical and linked to P's root */
-  if (ident[0] && ident[1]) {
-    int target = P->nb[roots[0]];
-    int V = roots[1], found = 0;
-    do {
-      if (V == target) found = 1;
-      V = Q->next[V];
-    } while (V != roots[1]);
-    if (found && ring_copy_list(R, P, roots[0])) return -1;
+  /* identical components (polyclip.cpp:516-538): P's component k is added
+   * when the identical component of Q holding its root's neighbour is a hole
+   * exactly when k is (inside an odd number of its side's other components) */
+  for (int k = 0; k < Ls->nr[0]; ++k) {
+    if (!ident[0][k]) continue;
+    const int rk = Ls->roots[0][k];
+    int holeP = 0;
+    for (int j = 0; j < Ls->nr[0]; ++j)
+      if (j != k) holeP ^= point_in_poly(P, Ls->roots[0][j], P->x[rk], P->y[rk]);
+    const int target = P->nb[rk];
+    for (int m = 0; m < Ls->nr[1]; ++m) {
+      if (!ident[1][m]) continue;
+      const int rm = Ls->roots[1][m];
+      int V = rm, found = 0;
+      do {
+        if (V == target) found = 1;
+        V = Q->next[V];
+      } while (V != rm);
+      if (!found) continue;
+      int holeQ = 0;
+      for (int j = 0; j < Ls->nr[1]; ++j)
+        if (j != m) holeQ ^= point_in_poly(Q, Ls->roots[1][j], Q->x[rm], Q->y[rm]);
+      if (holeP == holeQ && ring_copy_list(R, P, rk)) goto done;
+      break;
+    }
   }
   /* (4) entry/exit flags, split and crossing candidates */
-  unsigned char *split[2], *cross[2];
   split[0] = (unsigned char *)calloc((size_t)P->cap, 1);
   split[1] = (unsigned char *)calloc((size_t)Q->cap, 1);
   cross[0] = (unsigned char *)calloc((size_t)P->cap, 1);
   cross[1] = (unsigned char *)calloc((size_t)Q->cap, 1);
-  int rc = -1;
   if (!split[0] || !split[1] || !cross[0] || !cross[1]) goto done;
-  for (int s = 0; s < 2; ++s) {
-    if (noIsect[s]) continue;
+  for (int s = 0; s < 2; ++s)
+  for (int k = 0; k < Ls->nr[s]; ++k) {
+    if (noIsect[s][k]) continue;
     pool_t *p = side_pool(Ls, s);
     int err = 0;
-    int V = non_isect_vertex(Ls, s, roots[s], &err);
+    int V = non_isect_vertex(Ls, s, Ls->roots[s][k], &err);
     if (err) { rc = -2; goto done; }
     int status = EX_ENTRY;
-    if (point_in_poly(side_pool(Ls, OTHER(s)), roots[OTHER(s)], p->x[V], p->y[V])) toggle(&status);
+    if (point_in_side(Ls, OTHER(s), p->x[V], p->y[V])) toggle(&status);
     int first = 1;
     int I = V;
     do {
@@ -1210,10 +1270,10 @@ static int label_and_trace(lists_t *Ls, rings_t *R) {
     if (IQ >= 0 && cross[1][IQ]) { P->label[IP] = L_CROSSING; Q->label[IQ] = L_CROSSING; }
   }
   /* createResult2, polyclip.h:717-759 */
-  {
-    int root = roots[0];
+  long guard_total = 0, guard_max = 4L * (P->n + Q->n) + 16;
+  for (int k = 0; k < Ls->nr[0]; ++k) {
+    int root = Ls->roots[0][k];
     int It = root;
-    long guard_total = 0, guard_max = 4L * (P->n + Q->n) + 16;
     do {
       if (P->isect[It] && P->label[It] == L_CROSSING) {
         int r = ring_new(R);
@@ -1249,6 +1309,7 @@ static int label_and_trace(lists_t *Ls, rings_t *R) {
   rc = 0;
 done:
   free(split[0]); free(split[1]); free(cross[0]); free(cross[1]);
+  free(noIsect[0]); free(noIsect[1]); free(ident[0]); free(ident[1]);
   return rc;
 }
 
@@ -1265,6 +1326,7 @@ static int clip_overlay(sbco_run *run, const tree_t *t, int cType) {
   double *isxy = NULL, *ixB = NULL, *ixC = NULL;
   int *aB = NULL, *aC = NULL, *sB = NULL, *sC = NULL, *alB = NULL, *alC = NULL, *nbB = NULL,
       *nbC = NULL, *bNI = NULL, *cNI = NULL, *labB = NULL, *labC = NULL;
+  int *vsB = NULL, *vsC = NULL, *qlo = NULL, *qhi = NULL;
   lists_t Ls;
   memset(&Ls, 0, sizeof Ls);
   rings_t R;
@@ -1352,13 +1414,14 @@ static int clip_overlay(sbco_run *run, const tree_t *t, int cType) {
   if (!isxy || !aB || !aC) { free(bsorted); goto out; }
   for (int id = 0; id < K; ++id) {
     const double *bp = t->bP + ub[id], *cp = t->cP + uc[id];
+    const double *bq = t->bP + 2 * t->bnx[ub[id] / 2], *cq = t->cP + 2 * t->cnx[uc[id] / 2];
     double al = 0, be = 0;
-    int ty = seg_isect(bp[0], bp[1], bp[2], bp[3], cp[0], cp[1], cp[2], cp[3], &al, &be);
+    int ty = seg_isect(bp[0], bp[1], bq[0], bq[1], cp[0], cp[1], cq[0], cq[1], &al, &be);
     if (ty) {
       switch (ty) {
         case 1:
-          isxy[2 * id] = (1.0 - al) * bp[0] + al * bp[2];
-          isxy[2 * id + 1] = (1.0 - al) * bp[1] + al * bp[3];
+          isxy[2 * id] = (1.0 - al) * bp[0] + al * bq[0];
+          isxy[2 * id + 1] = (1.0 - al) * bp[1] + al * bq[1];
           break;
         case 3: case 4: case 5: case 7: case 8:
           isxy[2 * id] = cp[0];
@@ -1471,29 +1534,58 @@ static int clip_overlay(sbco_run *run, const tree_t *t, int cType) {
   put_ints(o, SBCO_MERGED_BNB, nbB, nB);
   put_ints(o, SBCO_MERGED_CNB, nbC, nQ);
 
-  /* calculateInitLabelParallel, oacc_segment_tree.cpp:7925-7988 */
+  /* components: their first source vertices (vs, ending with the vertex
+   * count) and first merged slots (roots, ending with the slot count) */
+  vsB = (int *)malloc(sizeof(int) * ((size_t)bSize + 1));
+  vsC = (int *)malloc(sizeof(int) * ((size_t)cSize + 1));
+  Ls.roots[0] = (int *)malloc(sizeof(int) * ((size_t)bSize + 1));
+  Ls.roots[1] = (int *)malloc(sizeof(int) * ((size_t)cSize + 1));
+  qlo = (int *)malloc(sizeof(int) * (size_t)(nQ > 0 ? nQ : 1));
+  qhi = (int *)malloc(sizeof(int) * (size_t)(nQ > 0 ? nQ : 1));
+  if (!vsB || !vsC || !Ls.roots[0] || !Ls.roots[1] || !qlo || !qhi) goto out;
+  for (int v = 0; v < bSize; ++v)
+    if (v == 0 || t->bnx[v - 1] != v) vsB[Ls.nr[0]++] = v;
+  vsB[Ls.nr[0]] = bSize;
+  for (int v = 0; v < cSize; ++v)
+    if (v == 0 || t->cnx[cStart + v - 1] != cStart + v) vsC[Ls.nr[1]++] = v;
+  vsC[Ls.nr[1]] = cSize;
+  for (int k = 0; k <= Ls.nr[0]; ++k) Ls.roots[0][k] = vsB[k] + bND[vsB[k]];
+  for (int k = 0; k <= Ls.nr[1]; ++k) Ls.roots[1][k] = vsC[k] + cND[vsC[k]];
+  for (int k = 0; k < Ls.nr[1]; ++k)
+    for (int q = Ls.roots[1][k]; q < Ls.roots[1][k + 1]; ++q) {
+      qlo[q] = Ls.roots[1][k];
+      qhi[q] = Ls.roots[1][k + 1];
+    }
+
+  /* calculateInitLabelParallel, oacc_segment_tree.cpp:7925-7988; the
+   * circular neighbours (getCircularId :7826-7834) wrap within the slot's
+   * component */
   labB = (int *)calloc((size_t)nB, sizeof(int));
   labC = (int *)calloc((size_t)nQ, sizeof(int));
   if (!labB || !labC) goto out;
-  for (int bid = 0; bid < bSize; ++bid) {
+  for (int bid = 0, kb = 0; bid < bSize; ++bid) {
+    if (bid == vsB[kb + 1]) ++kb;
+    const int lo = Ls.roots[0][kb], hi = Ls.roots[0][kb + 1];
     int s = bid + bND[bid], e = bid + bND[bid + 1] + 1;
     for (int i = s; i < e; ++i) {
       labB[i] = 0;
       if (alB[i] == -100) continue;
       double cx = ixB[2 * i], cy = ixB[2 * i + 1];
-      int tm = (i - 1 == -1) ? nB - 1 : i - 1; /* getCircularId :7826-7834 */
+      int tm = (i - 1 < lo) ? hi - 1 : i - 1;
       double pmx = ixB[2 * tm], pmy = ixB[2 * tm + 1];
       int pMN = alB[tm] != -100 ? nbB[tm] - 1 : -100;
-      int tp = (i + 1 == nB) ? 0 : i + 1;
+      int tp = (i + 1 == hi) ? lo : i + 1;
       double ppx = ixB[2 * tp], ppy = ixB[2 * tp + 1];
       int pPN = alB[tp] != -100 ? nbB[tp] - 1 : -100;
       int nId = nbB[i] - 1;
       int qt[2];
+      /* a neighbour outside the overlay's slots: undefined (the reference
+       * indexes past its arrays) */
+      if (nId < 0 || nId >= nQ) { st = -2; goto out; }
       for (int side = 0; side < 2; ++side) {
         int q = side == 0 ? nId - 1 : nId + 1;
-        if (q == nQ) q = 0;
-        else if (q == -1) q = nQ - 1;
-        if (q < 0 || q >= nQ) { st = -2; goto out; }
+        if (q == qhi[nId]) q = qlo[nId];
+        else if (q == qlo[nId] - 1) q = qhi[nId] - 1;
         double qx = ixC[2 * q], qy = ixC[2 * q + 1];
         int r;
         /* oracle(), :7847-7875 */
@@ -1519,7 +1611,6 @@ static int clip_overlay(sbco_run *run, const tree_t *t, int cType) {
       else if ((qm == 2 && qp == 0) || (qp == 2 && qm == 0)) lab = 7;
       else lab = -102;
       labB[i] = lab;
-      if (nId < 0 || nId >= nQ) { st = -2; goto out; }
       labC[nId] = lab;
     }
   }
@@ -1529,7 +1620,7 @@ static int clip_overlay(sbco_run *run, const tree_t *t, int cType) {
   /* copyToLinkedList + labelIntersections2 + createResult2 + cleanUpResult2 */
   {
     int extra = 2 * K + 8;
-    int r = build_lists(&Ls, t->bP, bSize, t->cP, cStart, cSize, ixB, ixC, alB, nbC, nB, nQ, labB,
+    int r = build_lists(&Ls, t->bP, t->cP, cStart, vsB, vsC, ixB, ixC, alB, nbC, nB, nQ, labB,
                         labC, extra);
     if (r) { st = r; goto out; }
     if (pool_init(&R.rp, nB + nQ + 2 * extra + 16)) goto out;
@@ -1576,18 +1667,35 @@ out:
   free(isxy); free(ixB); free(ixC); free(aB); free(aC); free(sB); free(sC);
   free(alB); free(alC); free(nbB); free(nbC); free(bNI); free(cNI); free(labB); free(labC);
   pool_free(&Ls.P); pool_free(&Ls.Q); pool_free(&R.rp); free(R.root);
+  free(Ls.roots[0]); free(Ls.roots[1]); free(vsB); free(vsC); free(qlo); free(qhi);
   if (st == -2) set_err(run, SBCO_EUNDEF, "reference behaviour undefined for this input");
   else if (st) set_err(run, SBCO_ENOMEM, "out of memory");
   return st;
 }
 
-sbco_run *sbco_clip(const double *b_xy, int nb, const double *c_xy, const int *c_sizes, int k) {
+/* component offsets: 0 = comp[0] < comp[1] < ... < comp[nc] = n, every
+ * component with at least 3 vertices (NULL: one ring) */
+static int comps_ok(const int *comp, int nc, int n) {
+  if (!comp) return 1;
+  if (nc < 1 || comp[0] != 0 || comp[nc] != n) return 0;
+  for (int i = 0; i < nc; ++i)
+    if (comp[i + 1] - comp[i] < 3) return 0;
+  return 1;
+}
+
+static sbco_run *clip_run(const double *b_xy, int nb, const int *bcomp, int nbc,
+                          const double *c_xy, const int *c_sizes, int k, const int *ccomp,
+                          int ncc) {
   sbco_run *run = (sbco_run *)calloc(1, sizeof(sbco_run));
   if (!run) return NULL;
   tree_t t;
   memset(&t, 0, sizeof t);
   if (k < 1 || k > 9 || nb < 3) {
     set_err(run, SBCO_EINPUT, "need nb >= 3 and 1..9 overlays");
+    return run;
+  }
+  if (!comps_ok(bcomp, nbc, nb) || (ccomp && (k != 1 || !comps_ok(ccomp, ncc, c_sizes[0])))) {
+    set_err(run, SBCO_EINPUT, "bad component offsets");
     return run;
   }
   for (int i = 0; i < k; ++i)
@@ -1599,7 +1707,10 @@ sbco_run *sbco_clip(const double *b_xy, int nb, const double *c_xy, const int *c
   run->ov = (struct ov_out *)calloc((size_t)k, sizeof(struct ov_out));
   if (!run->ov) { set_err(run, SBCO_ENOMEM, "out of memory"); return run; }
   int r;
-  if (read_input(&t, b_xy, nb, c_xy, c_sizes, k)) { set_err(run, SBCO_ENOMEM, "out of memory"); goto done; }
+  if (read_input(&t, b_xy, nb, c_xy, c_sizes, k, bcomp, nbc, ccomp, ncc)) {
+    set_err(run, SBCO_ENOMEM, "out of memory");
+    goto done;
+  }
   r = elementary(&t);
   if (r) { set_err(run, r == -2 ? SBCO_EUNDEF : SBCO_ENOMEM, "elementary intervals"); goto done; }
   if (tree_intervals(&t)) { set_err(run, SBCO_ENOMEM, "out of memory"); goto done; }
@@ -1630,6 +1741,15 @@ sbco_run *sbco_clip(const double *b_xy, int nb, const double *c_xy, const int *c
 done:
   tree_free(&t);
   return run;
+}
+
+sbco_run *sbco_clip(const double *b_xy, int nb, const double *c_xy, const int *c_sizes, int k) {
+  return clip_run(b_xy, nb, NULL, 0, c_xy, c_sizes, k, NULL, 0);
+}
+
+sbco_run *sbco_clip_components(const double *b_xy, int nb, const int *bcomp, int nbc,
+                               const double *c_xy, int nc, const int *ccomp, int ncc) {
+  return clip_run(b_xy, nb, bcomp, nbc, c_xy, &nc, 1, ccomp, ncc);
 }
 
 int sbco_status(const sbco_run *r) { return r ? r->status : SBCO_ENOMEM; }

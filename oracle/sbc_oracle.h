@@ -60,6 +60,15 @@ const void *sbco_tree_data(const sbco_run *r, int which);
  * sbco_status().
  */
 sbco_run *sbco_clip(const double *b_xy, int nb, const double *c_xy, const int *c_sizes, int k);
+/* One base against one overlay, each made of components (Foster's .poly
+ * format, lib/optimizedFostersAlgorithm/README.md:43-62): component i of the
+ * base is vertices [bcomp[i], bcomp[i+1]) (nbc components, bcomp[nbc] = nb),
+ * likewise for the overlay.  Every component closes on its own first
+ * vertex; labelling and tracing run over all components in the order of
+ * Foster's multi-component code (lib/optimizedFostersAlgorithm/
+ * polyclip.cpp:335-780).  One component each gives sbco_clip's result. */
+sbco_run *sbco_clip_components(const double *b_xy, int nb, const int *bcomp, int nbc,
+                               const double *c_xy, int nc, const int *ccomp, int ncc);
 /* Union instead of intersection in the back end (the Foster code's UNION
  * switch, foster/polyclip.h:39); applies to later sbco_clip calls. */
 void sbco_set_union(int on);

@@ -19,6 +19,12 @@ shapes and sizes of the benchmark configurations:
                       per-polygon sort), plus a few large jagged pairs (the
                       ``pair_large`` generator at 200k vertices) mixed in;
                       returned packed.
+* ``holed``           one polygon as components (Foster's .poly layout): an
+                      outer ring (stratified angles, radius R*U[0.7, 1]), holes
+                      (radius R*U[0.12, 0.2], clockwise) on a circle of radius
+                      0.35R, and islands (radius R*U[0.04, 0.08]) inside the
+                      first holes; the bounds keep every component simple and
+                      disjoint from the others.
 * ``one_to_many``     one jagged base (200k vertices, R = 1000) against many
                       plain-star overlays: sizes log-uniform in [4, 5000], radii
                       log-uniform in [0.001R, 0.05R], centres uniform in the
@@ -226,6 +232,42 @@ def small_pairs(npairs: int, seed: int = 4000, lo: int = 4, hi: int = 64):
         s = int(rng.integers(0, 2**62))
         out.append((star(int(nb), s), star(int(nc), s + 1, centre=(off[0], off[1]))))
     return out
+
+
+def ring(n: int, rng: np.random.Generator, centre, r_lo: float, r_hi: float,
+         clockwise: bool = False) -> np.ndarray:
+    """n vertices at stratified angles 2pi (k + u_k) / n, radius U[r_lo, r_hi]:
+    adjacent angles at most 4pi / n apart, so for n >= 16 every edge stays
+    farther than 0.94 r_lo from the centre."""
+    th = TWO_PI * (np.arange(n) + rng.uniform(0.05, 0.95, n)) / n
+    r = rng.uniform(r_lo, r_hi, n)
+    sn, cs = sincos(th)
+    xy = np.empty((n, 2), dtype=np.float64)
+    xy[:, 0] = centre[0] + r * cs
+    xy[:, 1] = centre[1] + r * sn
+    return xy[::-1].copy() if clockwise else xy
+
+
+def holed(n: int, seed: int, centre=(0.0, 0.0), R: float = 1.0, holes: int = 1,
+          islands: int = 0, n_hole: int | None = None):
+    """Components of one polygon: an outer ring of n vertices, `holes` holes
+    (at most 5) and `islands` islands inside the first holes.  Returns a list
+    of (m, 2) arrays, the outer ring first."""
+    if not 0 <= holes <= 5 or not 0 <= islands <= holes:
+        raise ValueError("0 <= islands <= holes <= 5")
+    rng = np.random.default_rng(seed)
+    n = max(int(n), 16)
+    m = max(int(n_hole if n_hole else n // 4), 16)
+    comps = [ring(n, rng, centre, 0.7 * R, R)]
+    phase = rng.uniform(0.0, TWO_PI)
+    for h in range(holes):
+        a = phase + TWO_PI * h / max(holes, 1)
+        hc = centre if holes == 1 else (centre[0] + 0.35 * R * np.cos(a),
+                                        centre[1] + 0.35 * R * np.sin(a))
+        comps.append(ring(m, rng, hc, 0.12 * R, 0.2 * R, clockwise=True))
+        if h < islands:
+            comps.append(ring(m, rng, hc, 0.04 * R, 0.08 * R))
+    return comps
 
 
 def write_poly(path, xy: np.ndarray, sep: str = ",") -> None:

@@ -121,3 +121,34 @@ def load_union_cases():
             ro += 1
         out.append((str(kind), b, c, rings))
     return out
+
+
+def load_component_cases():
+    """[(kind, union, base components, overlay components, Foster's rings)]
+    from golden_components.npz."""
+    z = np.load(GOLDEN / "golden_components.npz")
+    cases = []
+    bv = cv = bi = ci = ro = 0
+    for i, kind in enumerate(z["kind"]):
+        comps = []
+        for xy, cnt, n, pos in ((z["b_xy"], z["b_comp"], int(z["b_ncomp"][i]), "b"),
+                                (z["c_xy"], z["c_comp"], int(z["c_ncomp"][i]), "c")):
+            side = []
+            for _ in range(n):
+                if pos == "b":
+                    m = int(cnt[bi]); side.append(xy[bv:bv + m]); bv += m; bi += 1
+                else:
+                    m = int(cnt[ci]); side.append(xy[cv:cv + m]); cv += m; ci += 1
+            comps.append(side)
+        rings = []
+        for _ in range(int(z["r_ring_cnt"][i])):
+            rings.append(z["r_xy"][z["r_off"][ro]:z["r_off"][ro + 1]])
+            ro += 1
+        cases.append((str(kind), bool(z["union"][i]), comps[0], comps[1], rings))
+    return cases
+
+
+def text6(rings):
+    """Rings as Foster's program prints them (6 significant digits)."""
+    return [[f"{x:.6g} {y:.6g}" for x, y in np.asarray(r, np.float64).reshape(-1, 2)]
+            for r in rings]

@@ -2,12 +2,23 @@
 """Regenerate the golden fixtures from the reference's own CPU build.
 
     python oracle/build_ref.py && python tests/golden/make_golden.py
+    (--union-only / --components-only: just that fixture)
 
 Outputs (committed):
   golden_small.npz   ~100 small cases (random stars, integer-grid polygons
                      with T/V/overlap degeneracies, axis-aligned rectangles,
                      one-to-many runs): inputs and the reference's rings at
                      full precision, plus its unique candidate pairs.
+  golden_components.npz  multi-component polygons (holes and islands, the
+                     .poly format of lib/optimizedFostersAlgorithm): inputs and
+                     the rings of the reference's Foster program (precision 6,
+                     its output format), intersection and union.  The seg
+                     driver takes one ring per file; Foster's program is the
+                     reference's own code for several components.  Generic
+                     positions, plus components identical to the other side's
+                     (the identical-component rule): on partly shared edges
+                     the seg path and Foster's program differ already for
+                     single rings, so those are not fixtures.
   golden_digests.json  SHA-256 digests of the reference's rings and
                      intermediate arrays for the 10k x 8k star pair and the
                      1M x 1M jagged pair (inputs regenerated from their seeds).
@@ -218,10 +229,62 @@ def main_union():
     print(f"union cases: {n_ok} stored, {n_skip} skipped (reference crashed)")
 
 
+def component_cases():
+    cases = []
+    for t in range(24):
+        n1 = [16, 40, 200, 600][t % 4]
+        n2 = [16, 30, 300, 500][(t // 4) % 4]
+        hb, hc = t % 3 + 1, (t // 3) % 4
+        b = gen.holed(n1, 600 + t, R=1.0, holes=hb, islands=min(t % 2, hb))
+        c = gen.holed(n2, 700 + t, centre=(0.3 * np.cos(t), 0.3 * np.sin(t)), R=0.9, holes=hc,
+                      islands=min((t // 5) % 2, hc))
+        cases.append(("generic", b, c))
+    for t in range(4):
+        b = gen.holed(60 + 20 * t, 800 + t, R=1.0, holes=2, islands=1)
+        cases.append(("identical", b, [x.copy() for x in b]))
+        cases.append(("identical outer", b, [b[0]]))
+        cases.append(("hole as outer", b, [b[1][::-1].copy()]))
+    return cases
+
+
+def main_components():
+    if not O.foster_available():
+        raise SystemExit("build the reference first: python oracle/build_ref.py")
+    store = {"kind": [], "union": [], "b_xy": [], "b_comp": [], "b_ncomp": [], "c_xy": [],
+             "c_comp": [], "c_ncomp": [], "r_ring_cnt": [], "r_off": [0], "r_xy": []}
+    for kind, b, c in component_cases():
+        for union in (False, True):
+            rings = O.run_foster(b, c, timeout=60, union=union)["rings"]
+            store["kind"].append(kind)
+            store["union"].append(union)
+            for side, comps in (("b", b), ("c", c)):
+                store[side + "_xy"].extend(comps)
+                store[side + "_comp"].extend(len(x) for x in comps)
+                store[side + "_ncomp"].append(len(comps))
+            store["r_ring_cnt"].append(len(rings))
+            for r in rings:
+                store["r_xy"].append(r)
+                store["r_off"].append(store["r_off"][-1] + len(r))
+    np.savez_compressed(
+        OUT / "golden_components.npz",
+        kind=np.array(store["kind"]), union=np.array(store["union"], bool),
+        b_xy=np.concatenate(store["b_xy"]).astype(np.float64),
+        b_comp=np.array(store["b_comp"], np.int64), b_ncomp=np.array(store["b_ncomp"], np.int64),
+        c_xy=np.concatenate(store["c_xy"]).astype(np.float64),
+        c_comp=np.array(store["c_comp"], np.int64), c_ncomp=np.array(store["c_ncomp"], np.int64),
+        r_ring_cnt=np.array(store["r_ring_cnt"], np.int64), r_off=np.array(store["r_off"], np.int64),
+        r_xy=(np.concatenate(store["r_xy"]).astype(np.float64) if store["r_xy"] else np.zeros((0, 2))),
+    )
+    print(f"component cases: {len(store['kind'])} stored")
+
+
 if __name__ == "__main__":
     import sys as _sys
     if "--union-only" in _sys.argv:
         main_union()
+    elif "--components-only" in _sys.argv:
+        main_components()
     else:
         main()
         main_union()
+        main_components()
