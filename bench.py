@@ -181,7 +181,7 @@ KERNEL_BOUND = {
     "k_alpha_classify": "hbm", "k_cover_count": "latency", "k_alpha_sort_long": "latency",
     "k_lr_jump_coop": "latency", "k_tr_jump_coop": "latency",
     "k_grid_scatter": "hbm", "k_edge_fbox": "hbm", "k_copy_runs": "hbm",
-    "k_pair_exact": "fp64", "k_pw_cand_test": "fp64", "k_batch_cand": "fp64", "k_labels": "fp64",
+    "k_pair_exact": "fp64", "k_pw_cand_test": "fp64", "k_batch_cand": "fp64", "k_batch_cand_sweep": "fp64", "k_labels": "fp64",
     "k_grid_warp": "latency", "k_grid_small": "latency", "k_lr_jump": "latency",
     "k_tr_jump": "latency", "k_alpha_sort": "latency", "k_batch_back": "latency",
     "k_batch_front": "latency", "k_pw_pairs": "latency", "k_dedup": "latency",

@@ -516,6 +516,7 @@ __device__ int clip_pair_front_warp(const double* b, int nb, const double* c, in
 // slots of all 32.
 constexpr int kCandQ = 64;
 constexpr long long kSweepMin = 16384;  // pairs with more edge pairs sweep in x
+template <bool kSweep>
 __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc, const Caps& cp,
                                PairWork& w, int lane, int2* q) {
   const unsigned full = 0xffffffffu;
@@ -565,7 +566,7 @@ __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc,
   auto boxes_meet = [](const float4& fb, const float4& fc) {
     return !(fb.x > fc.z || fb.z < fc.x || fb.y > fc.w || fb.w < fc.y);
   };
-  if ((long long)nb * nc > kSweepMin) {
+  if constexpr (kSweep) {
     // Sweep in x: the overlay edges sorted by box min x (float order key,
     // -0 as +0, then the edge); a base edge's candidates are the overlay
     // edges with min x in [its min x - the largest overlay x extent, its max
@@ -615,8 +616,8 @@ __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc,
     }
     if (nq > 0) classify(nq);
     return;
-  }
-  int be = 0, j = lane;
+  } else {
+    int be = 0, j = lane;
   while (j >= nc && be < nb) {
     j -= nc;
     ++be;
@@ -633,7 +634,8 @@ __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc,
       ++be;
     }
   }
-  if (nq > 0) classify(nq);
+    if (nq > 0) classify(nq);
+  }
 }
 
 // A9-A13: records, counts, alpha order, merged arrays (one thread per pair)
@@ -1114,6 +1116,9 @@ __global__ void __launch_bounds__(128) k_batch_front(ClipArgs A) {
   }
 }
 
+// two instantiations with their own register budgets: the all-pairs test
+// for pairs up to kSweepMin edge pairs, the x sweep above
+template <bool kSweep>
 __global__ void __launch_bounds__(128) k_batch_cand(ClipArgs A) {
   __shared__ int2 s_q[4][kCandQ];
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1125,9 +1130,9 @@ __global__ void __launch_bounds__(128) k_batch_cand(ClipArgs A) {
   if (pass < 0 || !A.small(p, &nb, &nc)) return;
   Caps cp;
   PairWork w = A.work(p, nb, nc, pass, &cp);
-  if (w.state[0] != PS_OK) return;
-  clip_pair_cand(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w, lane,
-                 s_q[threadIdx.x >> 5]);
+  if (w.state[0] != PS_OK || ((long long)nb * nc > kSweepMin) != kSweep) return;
+  clip_pair_cand<kSweep>(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w, lane,
+                         s_q[threadIdx.x >> 5]);
 }
 
 // The back end in three kernels: A9-A13 on one thread per pair, the labels
@@ -1382,7 +1387,11 @@ void launch_clip(const ClipArgs& A, const BatchShape& sh, double in_bytes, cudaS
   }
   {
     ::sbc::KProbe kp_("k_batch_cand", st, in_bytes);
-    k_batch_cand<<<grid_for(32LL * A.np, sh.cand), sh.cand, 0, st>>>(A);
+    k_batch_cand<false><<<grid_for(32LL * A.np, sh.cand), sh.cand, 0, st>>>(A);
+  }
+  {
+    ::sbc::KProbe kp_("k_batch_cand_sweep", st);
+    k_batch_cand<true><<<grid_for(32LL * A.np, sh.cand), sh.cand, 0, st>>>(A);
   }
   {
     ::sbc::KProbe kp_("k_batch_pw", st, in_bytes + 20.0 * A.np);
