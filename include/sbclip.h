@@ -204,6 +204,55 @@ int sbc_area_backward(sbc_ctx* ctx, const sbc_batch* batch, const double* grad_a
 int sbc_area_backward_device(sbc_ctx* ctx, const sbc_batch* batch, const double* grad_area,
                              double* grad_b, double* grad_c, void* stream);
 
+/* ---- Polygons with several components (holes, islands) ------------------
+ * A polygon may be made of components, as in the .poly files of the
+ * reference's Foster program (lib/optimizedFostersAlgorithm/README.md:43-62:
+ * `x y,` per vertex, `;` closing a component); the seg driver itself reads
+ * one ring per file (gpc_read_multi_polygon, src/clip.cpp:172-311).  Every
+ * component closes on its own first vertex.  Labelling and tracing follow
+ * Foster's multi-component code (lib/optimizedFostersAlgorithm/
+ * polyclip.cpp:335-780): a point is inside a polygon when an odd number of
+ * its components contain it, a component without crossings is kept whole
+ * when it lies inside the other polygon, an identical component is kept when
+ * both are holes or neither is.  With one component per polygon the result
+ * is the batch engine's (and the reference's) ring for ring.
+ *
+ * b_comp lists the first vertex of every base component of the batch in
+ * ascending order and ends with b_off[npairs] (nb_comp + 1 entries,
+ * b_comp[0] = 0); every non-empty polygon starts a component, so none spans
+ * two pairs, and every component has at least 3 vertices.  Likewise c_comp.
+ * A null array: one ring per polygon on that side.  Pairs with components
+ * are clipped by the batch engine whatever their size. */
+typedef struct sbc_components {
+  const long long* b_comp;
+  long long nb_comp;
+  const long long* c_comp;
+  long long nc_comp;
+} sbc_components;
+
+/* sbc_clip_batch with components (host arrays; _device: device arrays, the
+ * offsets read back once to be checked). */
+int sbc_clip_batch_components(sbc_ctx* ctx, const sbc_batch* batch, const sbc_components* comps,
+                              sbc_batch_rings* out, void* stream);
+int sbc_clip_batch_components_device(sbc_ctx* ctx, const sbc_batch* batch,
+                                     const sbc_components* comps, sbc_batch_rings* out,
+                                     void* stream);
+/* One pair, host arrays: base components [b_comp[i], b_comp[i+1]) of b_xy
+ * (nb_comp components, b_comp[0] = 0), likewise the overlay.  The call fails
+ * with the pair's status (SBC_EUNDEF, ...) when the pair fails. */
+int sbc_clip_components(sbc_ctx* ctx, const double* b_xy, const int* b_comp, int nb_comp,
+                        const double* c_xy, const int* c_comp, int nc_comp, sbc_rings* out,
+                        void* stream);
+/* Area forward / backward (sbc_area_forward_device, sbc_area_backward_device)
+ * with components; the backward reuses the forward's records when given the
+ * same batch and component arrays. */
+int sbc_area_forward_components_device(sbc_ctx* ctx, const sbc_batch* batch,
+                                       const sbc_components* comps, double* area, int* status,
+                                       void* stream);
+int sbc_area_backward_components_device(sbc_ctx* ctx, const sbc_batch* batch,
+                                        const sbc_components* comps, const double* grad_area,
+                                        double* grad_b, double* grad_c, void* stream);
+
 /* ---- One base against many overlays, pairwise ---------------------------
  * The rings of `seg base overlay_i` for every overlay i (each equal to
  * sbc_clip_pair(base, overlay_i)); the reference has no such call and is run

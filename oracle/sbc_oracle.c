@@ -968,7 +968,7 @@ static int build_side(pool_t *P, pool_t *O, int is_q, const double *poly, int st
         }
         i++;
       }
-      if (i > hi) return -2;
+      if (i > hi || (!last && i >= hi)) return -2; /* more vertices than the component's slots */
       if (!last) {
         int v = pool_new(P, vx, vy);
         if (v != i) return -2;

@@ -151,6 +151,7 @@ struct sbc_ctx {
   double* hb_xy = nullptr;
   size_t hb_xy_cap = 0;
   std::vector<int> hb_status;
+  std::vector<int> hc_off;  // sbc_clip_components: ring offsets as int
   float phase_ms[8] = {0};
 };
 
@@ -557,11 +558,87 @@ int batch_to_device(sbc_ctx* c, const sbc_batch* b, cudaStream_t st, sbc_batch* 
   return SBC_OK;
 }
 
-int batch_run(sbc_ctx* c, const sbc_batch* d, cudaStream_t st) {
+// dk: the batch's component offsets on the device (null: one ring per
+// polygon), nbv / ncv their vertex totals
+int batch_run(sbc_ctx* c, const sbc_batch* d, cudaStream_t st,
+              const sbc_components* dk = nullptr, long long nbv = 0, long long ncv = 0) {
   c->pl->clear_error();
   c->pl->set_stream(st);
-  int rc = c->br->forward(d->npairs, d->b_xy, d->b_off, d->c_xy, d->c_off, st);
+  int rc = c->br->set_components(d->npairs, d->b_off, d->c_off, dk ? dk->b_comp : nullptr,
+                                 dk ? dk->nb_comp : 0, dk ? dk->c_comp : nullptr,
+                                 dk ? dk->nc_comp : 0, nbv, ncv, st);
+  if (!rc) rc = c->br->forward(d->npairs, d->b_xy, d->b_off, d->c_xy, d->c_off, st);
   if (rc) return set_err(c, rc, c->pl->error());
+  return SBC_OK;
+}
+
+// One side's component offsets (host): 0 = comp[0] < ... < comp[n] = off[np],
+// at least 3 vertices per component, every non-empty polygon starting one
+// (so no component spans two pairs).
+int comps_check(sbc_ctx* c, const long long* comp, long long n, const long long* off, int np) {
+  if (!comp) return SBC_OK;
+  if (n < 1 || comp[0] != 0 || comp[n] != off[np])
+    return set_err(c, SBC_EINPUT, "component offsets must run from 0 to the vertex count");
+  for (long long i = 0; i < n; ++i)
+    if (comp[i + 1] - comp[i] < 3)
+      return set_err(c, SBC_EINPUT, "a component needs at least 3 vertices");
+  long long i = 0;
+  for (int p = 0; p < np; ++p) {
+    if (off[p + 1] <= off[p]) continue;
+    while (i < n && comp[i] < off[p]) ++i;
+    if (i >= n || comp[i] != off[p])
+      return set_err(c, SBC_EINPUT, "every polygon must start a component");
+  }
+  return SBC_OK;
+}
+
+// The components of a batch checked on the host; hb / hk: host copies of the
+// batch offsets and the component offsets (read back for _device calls).
+// d receives device component offsets.
+int comps_prepare(sbc_ctx* c, const sbc_batch* b, const sbc_components* k, bool device,
+                  cudaStream_t st, sbc_components* d, long long* nbv, long long* ncv) {
+  if (!k) return set_err(c, SBC_EINPUT, "null components");
+  const int np = b->npairs;
+  *d = *k;
+  std::vector<long long> boff(np + 1), coff(np + 1), bc, cc;
+  const long long *hbo = b->b_off, *hco = b->c_off, *hbc = k->b_comp, *hcc = k->c_comp;
+  if (device) {
+    cudaMemcpyAsync(boff.data(), b->b_off, sizeof(long long) * (np + 1), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(coff.data(), b->c_off, sizeof(long long) * (np + 1), cudaMemcpyDeviceToHost, st);
+    if (k->b_comp && k->nb_comp >= 0) {
+      bc.resize(k->nb_comp + 1);
+      cudaMemcpyAsync(bc.data(), k->b_comp, sizeof(long long) * bc.size(), cudaMemcpyDeviceToHost, st);
+    }
+    if (k->c_comp && k->nc_comp >= 0) {
+      cc.resize(k->nc_comp + 1);
+      cudaMemcpyAsync(cc.data(), k->c_comp, sizeof(long long) * cc.size(), cudaMemcpyDeviceToHost, st);
+    }
+    int rc = cuda_check(c, cudaStreamSynchronize(st), "component offsets");
+    if (rc) return rc;
+    hbo = boff.data();
+    hco = coff.data();
+    hbc = k->b_comp ? bc.data() : nullptr;
+    hcc = k->c_comp ? cc.data() : nullptr;
+  }
+  int rc = comps_check(c, hbc, k->nb_comp, hbo, np);
+  if (!rc) rc = comps_check(c, hcc, k->nc_comp, hco, np);
+  if (rc) return rc;
+  *nbv = hbo[np];
+  *ncv = hco[np];
+  if (!device) {
+    sbc::BufferPool& bp = c->pl->pool();
+    auto* db = k->b_comp ? (long long*)bp.get("hbt_bcomp", sizeof(long long) * (k->nb_comp + 1))
+                         : nullptr;
+    auto* dc = k->c_comp ? (long long*)bp.get("hbt_ccomp", sizeof(long long) * (k->nc_comp + 1))
+                         : nullptr;
+    if (bp.failed) return set_err(c, SBC_ENOMEM, "device allocation failed (components)");
+    if (db)
+      cudaMemcpyAsync(db, k->b_comp, sizeof(long long) * (k->nb_comp + 1), cudaMemcpyHostToDevice, st);
+    if (dc)
+      cudaMemcpyAsync(dc, k->c_comp, sizeof(long long) * (k->nc_comp + 1), cudaMemcpyHostToDevice, st);
+    d->b_comp = db;
+    d->c_comp = dc;
+  }
   return SBC_OK;
 }
 
@@ -614,7 +691,7 @@ extern "C" int sbc_area_backward_device(sbc_ctx* c, const sbc_batch* b, const do
   cudaSetDevice(c->device);
   cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
   if (!(c->br->valid && c->br->np == b->npairs && c->br->key_b == b->b_xy &&
-        c->br->key_c == b->c_xy)) {
+        c->br->key_c == b->c_xy && !c->br->key_bcomp && !c->br->key_ccomp)) {
     rc = batch_run(c, b, st);
     if (rc) return rc;
   }
@@ -719,6 +796,168 @@ extern "C" int sbc_clip_batch(sbc_ctx* c, const sbc_batch* b, sbc_batch_rings* o
   out->ring_off = c->hb_ring_off;
   out->xy = c->hb_xy;
   out->status = c->hb_status.data();
+  return SBC_OK;
+}
+
+// ------------------------------------------------------------------ components
+extern "C" int sbc_clip_batch_components_device(sbc_ctx* c, const sbc_batch* b,
+                                                const sbc_components* k, sbc_batch_rings* out,
+                                                void* stream) {
+  int rc = batch_check(c, b);
+  if (rc) return rc;
+  if (!out) return set_err(c, SBC_EINPUT, "null output");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  sbc_components dk;
+  long long nbv = 0, ncv = 0;
+  rc = comps_prepare(c, b, k, true, st, &dk, &nbv, &ncv);
+  if (rc) return rc;
+  rc = batch_run(c, b, st, &dk, nbv, ncv);
+  if (rc) return rc;
+  long long *pr = nullptr, *ro = nullptr;
+  double* xy = nullptr;
+  long long nr = 0, nv = 0;
+  if (b->npairs > 0) {
+    c->pl->clear_error();
+    rc = c->br->rings(b->b_xy, b->b_off, b->c_xy, b->c_off, st, &pr, &ro, &xy, &nr, &nv);
+    if (rc) return set_err(c, rc, c->pl->error());
+  }
+  out->npairs = b->npairs;
+  out->nrings = nr;
+  out->nverts = nv;
+  out->pair_ring = pr;
+  out->ring_off = ro;
+  out->xy = xy;
+  out->status = c->br->status;
+  return SBC_OK;
+}
+
+extern "C" int sbc_clip_batch_components(sbc_ctx* c, const sbc_batch* b, const sbc_components* k,
+                                         sbc_batch_rings* out, void* stream) {
+  int rc = batch_check(c, b);
+  if (rc) return rc;
+  if (!out) return set_err(c, SBC_EINPUT, "null output");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  sbc_components dk;
+  long long nbv = 0, ncv = 0;
+  if (b->npairs > 0 && (b->b_off[0] != 0 || b->c_off[0] != 0))
+    return set_err(c, SBC_EINPUT, "batch offsets must start at 0");
+  rc = comps_prepare(c, b, k, false, st, &dk, &nbv, &ncv);
+  if (rc) return rc;
+  sbc_batch d;
+  rc = batch_to_device(c, b, st, &d);
+  if (rc) return rc;
+  rc = batch_run(c, &d, st, &dk, nbv, ncv);
+  if (rc) return rc;
+  const int np = b->npairs;
+  long long *pr = nullptr, *ro = nullptr;
+  double* xy = nullptr;
+  long long nr = 0, nv = 0;
+  if (np > 0) {
+    c->pl->clear_error();
+    rc = c->br->rings(d.b_xy, d.b_off, d.c_xy, d.c_off, st, &pr, &ro, &xy, &nr, &nv);
+    if (rc) return set_err(c, rc, c->pl->error());
+  }
+  c->hb_pair_ring.assign((size_t)np + 1, 0);
+  c->hb_status.assign((size_t)np + 1, 0);
+  if (!ensure_pinned(c->hb_ring_off, c->hb_ring_off_cap, (size_t)nr + 1) ||
+      !ensure_pinned(c->hb_xy, c->hb_xy_cap, (size_t)2 * nv + 1))
+    return set_err(c, SBC_ENOMEM, "pinned host allocation failed (batch rings)");
+  c->hb_ring_off[0] = 0;
+  if (np > 0) {
+    cudaMemcpyAsync(c->hb_pair_ring.data(), pr, sizeof(long long) * (np + 1),
+                    cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(c->hb_ring_off, ro, sizeof(long long) * (nr + 1), cudaMemcpyDeviceToHost, st);
+    if (nv > 0) cudaMemcpyAsync(c->hb_xy, xy, sizeof(double) * 2 * nv, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(c->hb_status.data(), c->br->status, sizeof(int) * np, cudaMemcpyDeviceToHost,
+                    st);
+  }
+  rc = cuda_check(c, cudaStreamSynchronize(st), "batch rings");
+  if (rc) return rc;
+  out->npairs = np;
+  out->nrings = nr;
+  out->nverts = nv;
+  out->pair_ring = c->hb_pair_ring.data();
+  out->ring_off = c->hb_ring_off;
+  out->xy = c->hb_xy;
+  out->status = c->hb_status.data();
+  return SBC_OK;
+}
+
+extern "C" int sbc_clip_components(sbc_ctx* c, const double* b_xy, const int* b_comp, int nb_comp,
+                                   const double* c_xy, const int* c_comp, int nc_comp,
+                                   sbc_rings* out, void* stream) {
+  if (!c) return SBC_EINPUT;
+  if (!b_xy || !b_comp || !c_xy || !c_comp || !out || nb_comp < 1 || nc_comp < 1)
+    return set_err(c, SBC_EINPUT, "null argument or no component");
+  std::vector<long long> bk(b_comp, b_comp + nb_comp + 1), ck(c_comp, c_comp + nc_comp + 1);
+  const long long boff[2] = {0, bk.back()}, coff[2] = {0, ck.back()};
+  const sbc_batch b{1, b_xy, boff, c_xy, coff};
+  const sbc_components k{bk.data(), nb_comp, ck.data(), nc_comp};
+  sbc_batch_rings r;
+  int rc = sbc_clip_batch_components(c, &b, &k, &r, stream);
+  if (rc) return rc;
+  if (r.status[0] != SBC_OK)
+    return set_err(c, r.status[0], r.status[0] == SBC_EUNDEF
+                                       ? "reference behaviour undefined for this input"
+                                       : "pair failed");
+  c->hc_off.resize((size_t)r.nrings + 1);
+  for (long long i = 0; i <= r.nrings; ++i) c->hc_off[i] = (int)r.ring_off[i];
+  out->nrings = (int)r.nrings;
+  out->nverts = r.nverts;
+  out->offsets = c->hc_off.data();
+  out->xy = r.xy;
+  return SBC_OK;
+}
+
+extern "C" int sbc_area_forward_components_device(sbc_ctx* c, const sbc_batch* b,
+                                                  const sbc_components* k, double* area,
+                                                  int* status, void* stream) {
+  int rc = batch_check(c, b);
+  if (rc) return rc;
+  if (b->npairs > 0 && !area) return set_err(c, SBC_EINPUT, "null area output");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  sbc_components dk;
+  long long nbv = 0, ncv = 0;
+  rc = comps_prepare(c, b, k, true, st, &dk, &nbv, &ncv);
+  if (rc) return rc;
+  rc = batch_run(c, b, st, &dk, nbv, ncv);
+  if (rc) return rc;
+  const int np = b->npairs;
+  if (np > 0) {
+    cudaMemcpyAsync(area, c->br->area, sizeof(double) * np, cudaMemcpyDeviceToDevice, st);
+    if (status)
+      cudaMemcpyAsync(status, c->br->status, sizeof(int) * np, cudaMemcpyDeviceToDevice, st);
+  }
+  return cuda_check(c, cudaStreamSynchronize(st), "area forward");
+}
+
+extern "C" int sbc_area_backward_components_device(sbc_ctx* c, const sbc_batch* b,
+                                                   const sbc_components* k,
+                                                   const double* grad_area, double* grad_b,
+                                                   double* grad_c, void* stream) {
+  int rc = batch_check(c, b);
+  if (rc) return rc;
+  if (!k) return set_err(c, SBC_EINPUT, "null components");
+  if (b->npairs > 0 && (!grad_area || !grad_b || !grad_c))
+    return set_err(c, SBC_EINPUT, "null gradient array");
+  cudaSetDevice(c->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
+  if (!(c->br->valid && c->br->np == b->npairs && c->br->key_b == b->b_xy &&
+        c->br->key_c == b->c_xy && c->br->key_bcomp == k->b_comp &&
+        c->br->key_ccomp == k->c_comp)) {
+    sbc_components dk;
+    long long nbv = 0, ncv = 0;
+    rc = comps_prepare(c, b, k, true, st, &dk, &nbv, &ncv);
+    if (rc) return rc;
+    rc = batch_run(c, b, st, &dk, nbv, ncv);
+    if (rc) return rc;
+  }
+  c->pl->clear_error();
+  rc = c->br->backward(b->b_xy, b->b_off, b->c_xy, b->c_off, grad_area, grad_b, grad_c, st);
+  if (rc) return set_err(c, rc, c->pl->error());
   return SBC_OK;
 }
 
@@ -896,6 +1135,7 @@ extern "C" int sbc_batch_autotune(sbc_ctx* c, const sbc_batch* b, const double* 
   cudaStream_t st = stream ? (cudaStream_t)stream : c->own;
   c->pl->clear_error();
   c->pl->set_stream(st);
+  c->br->set_components(b->npairs, b->b_off, b->c_off, nullptr, 0, nullptr, 0, 0, 0, st);
   rc = c->br->autotune(b->npairs, b->b_xy, b->b_off, b->c_xy, b->c_off, grad_area, grad_b, grad_c,
                        st, best_ms);
   if (rc) return set_err(c, rc, c->pl->error());
@@ -931,6 +1171,7 @@ extern "C" int sbc_area_graph_create(sbc_ctx* c, const sbc_batch* b, const doubl
   c->pl->clear_error();
   auto* g = new (std::nothrow) sbc_graph();
   if (!g) return set_err(c, SBC_ENOMEM, "graph");
+  c->br->set_components(b->npairs, b->b_off, b->c_off, nullptr, 0, nullptr, 0, 0, 0, st);
   rc = c->br->graph_record(b->npairs, b->b_xy, b->b_off, b->c_xy, b->c_off, grad_area, grad_b,
                            grad_c, area, status, st, &g->exec, &g->kernels);
   if (rc) {

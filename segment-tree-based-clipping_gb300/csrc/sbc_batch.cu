@@ -106,7 +106,20 @@ struct PairWork {
   int* fval;
   int* eflag;  // per sorted endpoint: entries it adds to the elementary array
   unsigned long long* csort;  // the candidate sweep's overlay edges by box min x
+  // components: the merged slot of each component's first vertex, ending
+  // with the slot count (filled by the thread back end)
+  int *rootB, *rootC;
+  // pair-relative successor of each vertex within its component (null: one
+  // ring); not carved, set per pair
+  const int* bnx = nullptr;
+  const int* cnx = nullptr;
 };
+
+// successor of vertex i of an n-vertex polygon: the next vertex of its
+// component (nx: pair-relative successors, null for one ring)
+__device__ __forceinline__ int vsucc(const int* nx, int n, int i) {
+  return nx ? nx[i] : (i + 1 == n ? 0 : i + 1);
+}
 
 __host__ __device__ __forceinline__ void carve_pool(Carver& cv, int cap, Pool& p) {
   p.x = cv.take<double>(cap);
@@ -197,6 +210,8 @@ __host__ __device__ __forceinline__ PairWork carve(Carver& cv, const Caps& c) {
   w.fval = cv.take<int>(npow2_dev(n2));
   w.eflag = cv.take<int>(n2 + 1);
   w.csort = cv.take<unsigned long long>(npow2_dev(c.nc));
+  w.rootB = cv.take<int>(c.nb + 1);
+  w.rootC = cv.take<int>(c.nc + 1);
   return w;
 }
 
@@ -291,15 +306,17 @@ __device__ int clip_pair_front_warp(const double* b, int nb, const double* c, in
   for (int e = lane; e < E; e += 32) {
     double a0, a1, y0, y1;
     if (e < nb) {
+      const int t = vsucc(w.bnx, nb, e);
       a0 = bvx(b, nb, e);
-      a1 = bvx(b, nb, e + 1);
+      a1 = bvx(b, nb, t);
       y0 = bvy(b, nb, e);
-      y1 = bvy(b, nb, e + 1);
+      y1 = bvy(b, nb, t);
     } else {
+      const int t = vsucc(w.cnx, nc, e - nb);
       a0 = bvx(c, nc, e - nb);
-      a1 = bvx(c, nc, e - nb + 1);
+      a1 = bvx(c, nc, t);
       y0 = bvy(c, nc, e - nb);
-      y1 = bvy(c, nc, e - nb + 1);
+      y1 = bvy(c, nc, t);
     }
     const long long k0 = okey(a0), k1 = okey(a1), ky0 = okey(y0), ky1 = okey(y1);
     if (k0 < k1) {
@@ -516,20 +533,24 @@ __device__ int clip_pair_front_warp(const double* b, int nb, const double* c, in
 // slots of all 32.
 constexpr int kCandQ = 64;
 constexpr long long kSweepMin = 16384;  // pairs with more edge pairs sweep in x
-template <bool kSweep>
+template <bool kSweep, bool kComp>
 __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc, const Caps& cp,
                                PairWork& w, int lane, int2* q) {
   const unsigned full = 0xffffffffu;
+  // component successors only in the instantiation for batches with them
+  const int* bn = kComp ? w.bnx : nullptr;
+  const int* cn = kComp ? w.cnx : nullptr;
   const int logL = w.state[1];
   int nq = 0;  // queued pairs (the same in every lane)
   auto classify = [&](int count) {
     if (lane < count) {
       const int2 e = q[lane];
       const int be = e.x, j = e.y;
+      const int bt2 = vsucc(bn, nb, be), ct2 = vsucc(cn, nc, j);
       const double p1x = bvx(b, nb, be), p1y = bvy(b, nb, be);
-      const double p2x = bvx(b, nb, be + 1), p2y = bvy(b, nb, be + 1);
+      const double p2x = bvx(b, nb, bt2), p2y = bvy(b, nb, bt2);
       const double q1x = bvx(c, nc, j), q1y = bvy(c, nc, j);
-      const double q2x = bvx(c, nc, j + 1), q2y = bvy(c, nc, j + 1);
+      const double q2x = bvx(c, nc, ct2), q2y = bvy(c, nc, ct2);
       double al, bt;
       const int ty = seg_isect(p1x, p1y, p2x, p2y, q1x, q1y, q2x, q2y, &al, &bt);
       unsigned long long key;
@@ -607,9 +628,11 @@ __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc,
         if (k < kend) {
           j = (int)(unsigned)w.csort[k];
           ++k;
-          if (boxes_meet(fb, w.fbox[nb + j]))
-            pass = lsmf_d(bvx(b, nb, be), bvy(b, nb, be), bvx(b, nb, be + 1), bvy(b, nb, be + 1),
-                          bvx(c, nc, j), bvy(c, nc, j), bvx(c, nc, j + 1), bvy(c, nc, j + 1));
+          if (boxes_meet(fb, w.fbox[nb + j])) {
+            const int bt2 = vsucc(bn, nb, be), ct2 = vsucc(cn, nc, j);
+            pass = lsmf_d(bvx(b, nb, be), bvy(b, nb, be), bvx(b, nb, bt2), bvy(b, nb, bt2),
+                          bvx(c, nc, j), bvy(c, nc, j), bvx(c, nc, ct2), bvy(c, nc, ct2));
+          }
         }
         enqueue(pass, be, j);
       }
@@ -618,22 +641,24 @@ __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc,
     return;
   } else {
     int be = 0, j = lane;
-  while (j >= nc && be < nb) {
-    j -= nc;
-    ++be;
-  }
-  while (__any_sync(full, be < nb)) {
-    bool pass = false;
-    if (be < nb && boxes_meet(w.fbox[be], w.fbox[nb + j]))
-      pass = lsmf_d(bvx(b, nb, be), bvy(b, nb, be), bvx(b, nb, be + 1), bvy(b, nb, be + 1),
-                    bvx(c, nc, j), bvy(c, nc, j), bvx(c, nc, j + 1), bvy(c, nc, j + 1));
-    enqueue(pass, be, j);
-    j += 32;
     while (j >= nc && be < nb) {
       j -= nc;
       ++be;
     }
-  }
+    while (__any_sync(full, be < nb)) {
+      bool pass = false;
+      if (be < nb && boxes_meet(w.fbox[be], w.fbox[nb + j])) {
+        const int bt2 = vsucc(bn, nb, be), ct2 = vsucc(cn, nc, j);
+        pass = lsmf_d(bvx(b, nb, be), bvy(b, nb, be), bvx(b, nb, bt2), bvy(b, nb, bt2),
+                      bvx(c, nc, j), bvy(c, nc, j), bvx(c, nc, ct2), bvy(c, nc, ct2));
+      }
+      enqueue(pass, be, j);
+      j += 32;
+      while (j >= nc && be < nb) {
+        j -= nc;
+        ++be;
+      }
+    }
     if (nq > 0) classify(nq);
   }
 }
@@ -692,13 +717,27 @@ __device__ PairResult clip_pair_back1(const double* b, int nb, const double* c, 
     w.csorted[w.cAll[ec] + w.cfill[ec]++] = i;
   }
   const int nB = nb + w.bND[nb], nQ = nc + w.cND[nc];
+  // components: the merged slot of each one's first vertex (a vertex starts
+  // a component when the vertex before it closes its own)
+  {
+    int nr = 0;
+    for (int v = 0; v < nb; ++v)
+      if (v == 0 || vsucc(w.bnx, nb, v - 1) != v) w.rootB[nr++] = v + w.bND[v];
+    w.rootB[nr] = nB;
+    w.counts[2] = nr;
+    nr = 0;
+    for (int v = 0; v < nc; ++v)
+      if (v == 0 || vsucc(w.cnx, nc, v - 1) != v) w.rootC[nr++] = v + w.cND[v];
+    w.rootC[nr] = nQ;
+    w.counts[3] = nr;
+  }
   // ---- A11 records (saveIntersectionsParallel, :7257-7341): the type,
   // alpha and beta the candidate stage's lineSegmentIntersection found (FP64
   // work on one thread per pair costs its issue slots for a whole warp)
   for (int i = 0; i < K; ++i) {
-    const int bi = ub[i] >> 1;
+    const int bi = ub[i] >> 1, bi2 = vsucc(w.bnx, nb, bi);
     const double p1x = bvx(b, nb, bi), p1y = bvy(b, nb, bi);
-    const double p2x = bvx(b, nb, bi + 1), p2y = bvy(b, nb, bi + 1);
+    const double p2x = bvx(b, nb, bi2), p2y = bvy(b, nb, bi2);
     const double q1x = bvx(c, nc, uc[i] >> 1), q1y = bvy(c, nc, uc[i] >> 1);
     const int h = w.hord[i];
     const double al = w.hal[h], bt = w.hbt[h];
@@ -833,8 +872,20 @@ __device__ PairResult clip_pair_back1(const double* b, int nb, const double* c, 
 // by one thread of a warp costs the issue slots of all 32.  Reads the merged
 // arrays clip_pair_back1 left in the arena; PS_UNDEF where the reference's
 // behaviour is undefined.
+// the component [lo, hi) of merged slot i: roots ascending, nr components
+__device__ __forceinline__ int2 comp_of_slot(const int* roots, int nr, int i) {
+  int lo = 0, hi = nr - 1;
+  while (lo < hi) {
+    const int m = (lo + hi + 1) >> 1;
+    if (roots[m] <= i) lo = m;
+    else hi = m - 1;
+  }
+  return make_int2(roots[lo], roots[lo + 1]);
+}
+
 __device__ int clip_pair_labels(int nb, int nc, PairWork& w, int lane) {
   const int nB = nb + w.bND[nb], nQ = nc + w.cND[nc];
+  const int nrB = w.counts[2], nrC = w.counts[3];
   for (int q = lane; q < nQ; q += 32) w.cWin[q] = -1;
   __syncwarp();
   bool bad = false;
@@ -842,26 +893,28 @@ __device__ int clip_pair_labels(int nb, int nc, PairWork& w, int lane) {
     w.labB[i] = 0;
     if (w.alB[i] == -100) continue;
     const double cx = w.ixB[2 * i], cy = w.ixB[2 * i + 1];
-    const int tm = (i - 1 == -1) ? nB - 1 : i - 1;
+    // getCircularId (:7826-7834) within the slot's component
+    const int2 cb = comp_of_slot(w.rootB, nrB, i);
+    const int tm = (i - 1 < cb.x) ? cb.y - 1 : i - 1;
     const double pmx = w.ixB[2 * tm], pmy = w.ixB[2 * tm + 1];
     const int pMN = w.alB[tm] != -100 ? w.nbB[tm] - 1 : -100;
-    const int tp = (i + 1 == nB) ? 0 : i + 1;
+    const int tp = (i + 1 == cb.y) ? cb.x : i + 1;
     const double ppx = w.ixB[2 * tp], ppy = w.ixB[2 * tp + 1];
     const int pPN = w.alB[tp] != -100 ? w.nbB[tp] - 1 : -100;
     const int nId = w.nbB[i] - 1;
+    // a neighbour outside the overlay's slots: undefined
+    if (nId < 0 || nId >= nQ) {
+      bad = true;
+      continue;
+    }
+    const int2 cq = comp_of_slot(w.rootC, nrC, nId);
     int qt[2];
     double s3 = 0.0;
     bool have_s3 = false;
-    bool skip = false;
-    for (int side = 0; side < 2 && !skip; ++side) {
+    for (int side = 0; side < 2; ++side) {
       int q = side == 0 ? nId - 1 : nId + 1;
-      if (q == nQ) q = 0;
-      else if (q == -1) q = nQ - 1;
-      if (q < 0 || q >= nQ) {
-        bad = true;
-        skip = true;
-        break;
-      }
+      if (q == cq.y) q = cq.x;
+      else if (q == cq.x - 1) q = cq.y - 1;
       const double qx = w.ixC[2 * q], qy = w.ixC[2 * q + 1];
       int r;
       if (pMN != -100 && pMN == q) r = 2;
@@ -878,7 +931,6 @@ __device__ int clip_pair_labels(int nb, int nc, PairWork& w, int lane) {
       }
       qt[side] = r;
     }
-    if (skip) continue;
     const int qm = qt[0], qp = qt[1];
     int lab;
     if ((qm == 0 && qp == 1) || (qm == 1 && qp == 0)) lab = 1;
@@ -890,10 +942,6 @@ __device__ int clip_pair_labels(int nb, int nc, PairWork& w, int lane) {
     else if ((qm == 2 && qp == 0) || (qp == 2 && qm == 0)) lab = 7;
     else lab = -102;
     w.labB[i] = lab;
-    if (nId < 0 || nId >= nQ) {
-      bad = true;
-      continue;
-    }
     atomicMax(&w.cWin[nId], i);
   }
   if (__any_sync(0xffffffffu, bad)) return PS_UNDEF;
@@ -942,6 +990,12 @@ __device__ PairResult clip_pair_back2(const double* b, int nb, const double* c, 
   a.labB = w.labB;
   a.labC = w.labC;
   a.unite = unite;
+  a.bnx = w.bnx;
+  a.cnx = w.cnx;
+  a.rootsP = w.rootB;
+  a.rootsQ = w.rootC;
+  a.nrP = w.counts[2];
+  a.nrQ = w.counts[3];
   *a.nrings = 0;
   int st = ser_build(a);
   if (!st) {
@@ -1074,15 +1128,27 @@ struct ClipArgs {
   double* area;
   int unite;            // union instead of intersection
   int maxv;             // the small/large split: larger polygons go to the pair pipeline
+  // components: pair-relative successor of every vertex within its
+  // component, indexed like bxy / cxy (null: every polygon one ring)
+  const int* bnx = nullptr;
+  const int* cnx = nullptr;
   __device__ bool small(int p, int* nb, int* nc) const {
     *nb = (int)(boff[p + 1] - boff[p]);
     *nc = (int)(coff[p + 1] - coff[p]);
     return *nb >= 3 && *nc >= 3 && *nb <= maxv && *nc <= maxv;
   }
+  // more than one component on either side: the last vertex's successor is
+  // the first vertex of a later component
+  __device__ bool multi(int p, int nb, int nc) const {
+    return (bnx && bnx[boff[p] + nb - 1] != 0) || (cnx && cnx[coff[p] + nc - 1] != 0);
+  }
   __device__ PairWork work(int p, int nb, int nc, int pass, Caps* cp) const {
     *cp = caps_of(nb, nc, hit_cap(nb, nc, pass, need_in[p]));
     Carver cv{arena + (aoff[p] - abase), 0};
-    return carve(cv, *cp);
+    PairWork w = carve(cv, *cp);
+    w.bnx = bnx ? bnx + boff[p] : nullptr;
+    w.cnx = cnx ? cnx + coff[p] : nullptr;
+    return w;
   }
 };
 
@@ -1116,9 +1182,10 @@ __global__ void __launch_bounds__(128) k_batch_front(ClipArgs A) {
   }
 }
 
-// two instantiations with their own register budgets: the all-pairs test
-// for pairs up to kSweepMin edge pairs, the x sweep above
-template <bool kSweep>
+// instantiations with their own register budgets: the all-pairs test for
+// pairs up to kSweepMin edge pairs, the x sweep above; each with or without
+// component successors
+template <bool kSweep, bool kComp>
 __global__ void __launch_bounds__(128) k_batch_cand(ClipArgs A) {
   __shared__ int2 s_q[4][kCandQ];
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1131,8 +1198,8 @@ __global__ void __launch_bounds__(128) k_batch_cand(ClipArgs A) {
   Caps cp;
   PairWork w = A.work(p, nb, nc, pass, &cp);
   if (w.state[0] != PS_OK || ((long long)nb * nc > kSweepMin) != kSweep) return;
-  clip_pair_cand<kSweep>(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w, lane,
-                         s_q[threadIdx.x >> 5]);
+  clip_pair_cand<kSweep, kComp>(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, cp, w,
+                                lane, s_q[threadIdx.x >> 5]);
 }
 
 // The back end in three kernels: A9-A13 on one thread per pair, the labels
@@ -1266,6 +1333,11 @@ __global__ void __launch_bounds__(128) k_batch_pw(ClipArgs A) {
     if (lane == 0) batch_fail(A, p, w, PS_CAP, K);
     return;
   }
+  // several components: the thread back end follows them
+  if (A.multi(p, nb, nc)) {
+    if (lane == 0) w.state[3] = 1;
+    return;
+  }
   // A9 order (base id, then first emission)
   if (lane == 0) {
     for (int i = 0; i < K; ++i) w.hord[i] = i;
@@ -1380,6 +1452,13 @@ __global__ void k_graph_passes(int n, const int* __restrict__ pass, const int* _
 
 // block sizes (threads) of the three kernels: tuning knobs, each at most
 // kBatchBlock (128) and a multiple of 32
+// the batch's component successors (null: one ring per polygon)
+ClipArgs with_components(ClipArgs a, const int* bnx, const int* cnx) {
+  a.bnx = bnx;
+  a.cnx = cnx;
+  return a;
+}
+
 void launch_clip(const ClipArgs& A, const BatchShape& sh, double in_bytes, cudaStream_t st) {
   {
     ::sbc::KProbe kp_("k_batch_front", st, in_bytes);
@@ -1387,11 +1466,17 @@ void launch_clip(const ClipArgs& A, const BatchShape& sh, double in_bytes, cudaS
   }
   {
     ::sbc::KProbe kp_("k_batch_cand", st, in_bytes);
-    k_batch_cand<false><<<grid_for(32LL * A.np, sh.cand), sh.cand, 0, st>>>(A);
+    if (A.bnx || A.cnx)
+      k_batch_cand<false, true><<<grid_for(32LL * A.np, sh.cand), sh.cand, 0, st>>>(A);
+    else
+      k_batch_cand<false, false><<<grid_for(32LL * A.np, sh.cand), sh.cand, 0, st>>>(A);
   }
   {
     ::sbc::KProbe kp_("k_batch_cand_sweep", st);
-    k_batch_cand<true><<<grid_for(32LL * A.np, sh.cand), sh.cand, 0, st>>>(A);
+    if (A.bnx || A.cnx)
+      k_batch_cand<true, true><<<grid_for(32LL * A.np, sh.cand), sh.cand, 0, st>>>(A);
+    else
+      k_batch_cand<true, false><<<grid_for(32LL * A.np, sh.cand), sh.cand, 0, st>>>(A);
   }
   {
     ::sbc::KProbe kp_("k_batch_pw", st, in_bytes + 20.0 * A.np);
@@ -1466,8 +1551,8 @@ __global__ void __launch_bounds__(kBatchBlock)
 k_batch_backward(int np, const double* __restrict__ bxy, const long long* __restrict__ boff,
                  const double* __restrict__ cxy, const long long* __restrict__ coff, Arenas ar,
                  const int* __restrict__ status, const int* __restrict__ nrings,
-                 const double* __restrict__ gA,
-                 double* __restrict__ gb, double* __restrict__ gc) {
+                 const double* __restrict__ gA, const int* __restrict__ bnx,
+                 const int* __restrict__ cnx, double* __restrict__ gb, double* __restrict__ gc) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= np) return;
   const int nb = (int)(boff[p + 1] - boff[p]), nc = (int)(coff[p + 1] - coff[p]);
@@ -1500,7 +1585,8 @@ k_batch_backward(int np, const double* __restrict__ bxy, const long long* __rest
       } else if (t.x == 2) {
         // I = (1 - alpha) b1 + alpha b2, alpha = A1 / (A1 - A2),
         // A1 = A(b1, c1, c2), A2 = A(b2, c1, c2)
-        const int i1 = t.y, i2 = (t.y + 1) % nb, j1 = t.z, j2 = (t.z + 1) % nc;
+        const int i1 = t.y, i2 = vsucc(bnx ? bnx + boff[p] : nullptr, nb, t.y), j1 = t.z,
+                  j2 = vsucc(cnx ? cnx + coff[p] : nullptr, nc, t.z);
         const double b1x = b[2 * i1], b1y = b[2 * i1 + 1], b2x = b[2 * i2], b2y = b[2 * i2 + 1];
         const double c1x = c[2 * j1], c1y = c[2 * j1 + 1], c2x = c[2 * j2], c2y = c[2 * j2 + 1];
         const double A1 = (c1x - b1x) * (c2y - b1y) - (c1y - b1y) * (c2x - b1x);
@@ -1705,7 +1791,7 @@ int BatchRunner::plan(int np_, const long long* d_boff, const long long* d_coff,
   {
     ::sbc::KProbe kp_("k_batch_size", st);
     k_batch_size<<<grid_for(np + 1, 256), 256, 0, st>>>(np, d_boff, d_coff, nullptr, nullptr,
-                                                       aoff[0], split);
+                                                       aoff[0], split_now());
   }
   exclusive_scan_i64(aoff[0], np + 1, sscr_, st);
   cudaMemcpyAsync(h_aoff0_.data(), aoff[0], sizeof(long long) * (np + 1), cudaMemcpyDeviceToHost,
@@ -1715,7 +1801,7 @@ int BatchRunner::plan(int np_, const long long* d_boff, const long long* d_coff,
   big_.clear();
   for (int p = 0; p < np; ++p) {
     const long long nb = h_boff_[p + 1] - h_boff_[p], nc = h_coff_[p + 1] - h_coff_[p];
-    if (nb >= 3 && nc >= 3 && (nb > split || nc > split)) {
+    if (nb >= 3 && nc >= 3 && (nb > split_now() || nc > split_now())) {
       BigOut b;
       b.p = p;
       big_.push_back(b);
@@ -1759,16 +1845,18 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
   for (int i = 0; i < n; ++i) {
     const long long nb = h_boff_[p0 + i + 1] - h_boff_[p0 + i];
     const long long nc = h_coff_[p0 + i + 1] - h_coff_[p0 + i];
-    is_small[i] = nb <= split && nc <= split;
+    is_small[i] = nb <= split_now() && nc <= split_now();
     hp[i] = (nb >= 3 && nc >= 3 && !is_small[i]) ? -1 : 0;
   }
   cudaMemcpyAsync(pass + p0, hp.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
   // coordinates in; area, status, ring and vertex counts out
   const double in_bytes =
       16.0 * (double)(h_boff_[p1] - h_boff_[p0] + h_coff_[p1] - h_coff_[p0]);
-  launch_clip(ClipArgs{n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[0], aoff[0] + p0,
-                       abase_[0], need_ + p0, need_ + p0, status + p0, nrings + p0, nverts + p0,
-                       area + p0, unite ? 1 : 0, split},
+  launch_clip(with_components(ClipArgs{n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0,
+                                       arena[0], aoff[0] + p0, abase_[0], need_ + p0, need_ + p0,
+                                       status + p0, nrings + p0, nverts + p0, area + p0,
+                                       unite ? 1 : 0, split_now()},
+                              bnx, cnx),
               shape, in_bytes, st);
   std::vector<int> hs(n);
   cudaMemcpyAsync(hs.data(), status + p0, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
@@ -1788,7 +1876,7 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
     {
       ::sbc::KProbe kp_("k_batch_size", st);
       k_batch_size<<<grid_for(n + 1, 256), 256, 0, st>>>(n, d_boff + p0, d_coff + p0, pass + p0,
-                                                         need_ + p0, aoff[1] + p0, split);
+                                                         need_ + p0, aoff[1] + p0, split_now());
     }
     exclusive_scan_i64(aoff[1] + p0, n + 1, sscr_, st);
     long long total = 0;
@@ -1796,9 +1884,11 @@ int BatchRunner::run_chunk(int c, const double* d_bxy, const long long* d_boff,
     if (cudaStreamSynchronize(st) != cudaSuccess) return pl_.fail(kECuda, "batch sizes");
     arena[1] = (unsigned char*)pool.get("bt_arena1", (size_t)total + 256);
     if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (batch arena)");
-    launch_clip(ClipArgs{n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0, arena[1],
-                         aoff[1] + p0, 0, need_ + p0, need_ + p0, status + p0, nrings + p0,
-                         nverts + p0, area + p0, unite ? 1 : 0, split},
+    launch_clip(with_components(ClipArgs{n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, pass + p0,
+                                         arena[1], aoff[1] + p0, 0, need_ + p0, need_ + p0,
+                                         status + p0, nrings + p0, nverts + p0, area + p0,
+                                         unite ? 1 : 0, split_now()},
+                                bnx, cnx),
                 shape, in_bytes, st);
   }
   // where each pair's data lives now: pass 0 arena, retry arena, or none
@@ -1899,6 +1989,53 @@ int BatchRunner::run_big(const double* d_bxy, const double* d_cxy, cudaStream_t 
   return kOk;
 }
 
+// successor of vertex g within its component, relative to its pair's first
+// vertex: comp[] holds the component starts of the batch (ending with the
+// vertex count), off[] the pairs' (no component spans two pairs)
+__global__ void k_comp_succ(long long nv, const long long* __restrict__ comp, long long ncomp,
+                            const long long* __restrict__ off, int np, int* __restrict__ nx) {
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nv) return;
+  auto last_le = [&](const long long* a, long long n, long long v) {
+    long long lo = 0, hi = n - 1;  // a[0] <= v < a[n]
+    while (lo < hi) {
+      const long long m = (lo + hi + 1) >> 1;
+      if (a[m] <= v) lo = m;
+      else hi = m - 1;
+    }
+    return lo;
+  };
+  const long long k = last_le(comp, ncomp, g);
+  const long long p = last_le(off, np, g);
+  const long long t = g + 1 < comp[k + 1] ? g + 1 : comp[k];
+  nx[g] = (int)(t - off[p]);
+}
+
+int BatchRunner::set_components(int np_, const long long* d_boff, const long long* d_coff,
+                                const long long* d_bcomp, long long nbc,
+                                const long long* d_ccomp, long long ncc, long long nbv,
+                                long long ncv, cudaStream_t st) {
+  key_bcomp = d_bcomp;
+  key_ccomp = d_ccomp;
+  bnx = cnx = nullptr;
+  valid = false;
+  BufferPool& pool = pl_.pool();
+  int* b = d_bcomp ? (int*)pool.get("bt_bnx", sizeof(int) * (nbv + 1)) : nullptr;
+  int* c = d_ccomp ? (int*)pool.get("bt_cnx", sizeof(int) * (ncv + 1)) : nullptr;
+  if (pool.failed) return pl_.fail(kENoMem, "device allocation failed (components)");
+  if (b && nbv > 0) {
+    ::sbc::KProbe kp_("k_comp_succ", st);
+    k_comp_succ<<<grid_for(nbv, 256), 256, 0, st>>>(nbv, d_bcomp, nbc, d_boff, np_, b);
+  }
+  if (c && ncv > 0) {
+    ::sbc::KProbe kp_("k_comp_succ", st);
+    k_comp_succ<<<grid_for(ncv, 256), 256, 0, st>>>(ncv, d_ccomp, ncc, d_coff, np_, c);
+  }
+  bnx = b;
+  cnx = c;
+  return kOk;
+}
+
 int BatchRunner::forward(int np_, const double* d_bxy, const long long* d_boff,
                          const double* d_cxy, const long long* d_coff, cudaStream_t st) {
   valid = false;
@@ -1994,8 +2131,8 @@ int BatchRunner::backward(const double* d_bxy, const long long* d_boff, const do
                       32.0 * (double)(h_boff_[p1] - h_boff_[p0] + h_coff_[p1] - h_coff_[p0]) +
                           8.0 * n);
     k_batch_backward<<<grid_for(n, shape.bwd), shape.bwd, 0, st>>>(
-        n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, ar, status + p0, nrings + p0, d_gA + p0, d_gb,
-        d_gc);
+        n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, ar, status + p0, nrings + p0, d_gA + p0, bnx,
+        cnx, d_gb, d_gc);
   }
   for (const BigOut& bo : big_) {
     if (!bo.ok || bo.nverts == 0) continue;
@@ -2125,18 +2262,22 @@ int BatchRunner::graph_record(int np_, const double* d_bxy, const long long* d_b
   cudaGraph_t graph = nullptr;
   cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    launch_clip(ClipArgs{np, d_bxy, d_boff, d_cxy, d_coff, pass0, arena[0], aoff[0], abase_[0],
-                         need_scr, need_rec, status, nrings, nverts, area, unite ? 1 : 0, split},
+    launch_clip(with_components(ClipArgs{np, d_bxy, d_boff, d_cxy, d_coff, pass0, arena[0],
+                                         aoff[0], abase_[0], need_scr, need_rec, status, nrings,
+                                         nverts, area, unite ? 1 : 0, split_now()},
+                                bnx, cnx),
                 shape, in_bytes, st);
     if (retry)
-      launch_clip(ClipArgs{np, d_bxy, d_boff, d_cxy, d_coff, pass1, arena[1], aoff[1], 0, need_scr,
-                           need_rec, status, nrings, nverts, area, unite ? 1 : 0, split},
+      launch_clip(with_components(ClipArgs{np, d_bxy, d_boff, d_cxy, d_coff, pass1, arena[1],
+                                           aoff[1], 0, need_scr, need_rec, status, nrings, nverts,
+                                           area, unite ? 1 : 0, split_now()},
+                                  bnx, cnx),
                   shape, in_bytes, st);
     const Arenas ar{arena[0], aoff[0], abase_[0], arena[1], aoff[1], 0, pass, need_rec};
     {
       ::sbc::KProbe kp_("k_batch_backward", st);
       k_batch_backward<<<grid_for(np, shape.bwd), shape.bwd, 0, st>>>(
-          np, d_bxy, d_boff, d_cxy, d_coff, ar, status, nrings, d_gA, d_gb, d_gc);
+          np, d_bxy, d_boff, d_cxy, d_coff, ar, status, nrings, d_gA, bnx, cnx, d_gb, d_gc);
     }
     if (out_area) cudaMemcpyAsync(out_area, area, sizeof(double) * np, cudaMemcpyDeviceToDevice, st);
     if (out_status)

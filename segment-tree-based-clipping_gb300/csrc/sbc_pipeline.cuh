@@ -316,6 +316,20 @@ class BatchRunner {
   explicit BatchRunner(Pipeline& pl) : pl_(pl) {}
   BatchShape shape;
   int split = SBC_BATCH_MAX_VERTICES;  // polygons above it go to the pair pipeline (<= the max)
+  // components of the current call (device, pair-relative successor of each
+  // vertex within its component; null: one ring per polygon).  A batch with
+  // components clips every pair here: the pair pipeline takes one ring.
+  const int* bnx = nullptr;
+  const int* cnx = nullptr;
+  const void* key_bcomp = nullptr;  // the component offsets they came from
+  const void* key_ccomp = nullptr;
+  int split_now() const { return (bnx || cnx) ? 0x7fffffff : split; }
+  // components for the calls that follow (device offsets, each side's
+  // component starts ending with its vertex count; null: one ring per
+  // polygon): builds bnx / cnx
+  int set_components(int np, const long long* d_boff, const long long* d_coff,
+                     const long long* d_bcomp, long long nbc, const long long* d_ccomp,
+                     long long ncc, long long nbv, long long ncv, cudaStream_t st);
   // times forward + backward of the batch under each knob's candidates in
   // turn (the better of two runs), keeps the fastest; the forward results of
   // the last run are left as forward() leaves them

@@ -58,7 +58,21 @@ struct SerialArgs {
   int* status;   // 0 ok, 2 undefined, 3 capacity
   int rfull = 0;  // set when the ring pool ran out of nodes
   int unite = 0;  // union instead of intersection (foster/polyclip.h:39 UNION)
+  // components (Foster's multi-component polygons): the successor of each
+  // source vertex within its component (null: one ring), and the list node of
+  // each component's first vertex, ending with the node count (the caller's;
+  // null with one ring: root 0)
+  const int* bnx = nullptr;
+  const int* cnx = nullptr;
+  int* rootsP = nullptr;
+  int* rootsQ = nullptr;
+  int nrP = 1, nrQ = 1;
 };
+
+__device__ __forceinline__ int sroot(const SerialArgs& a, int s, int k) {
+  const int* r = s == 0 ? a.rootsP : a.rootsQ;
+  return r ? r[k] : 0;
+}
 
 __device__ int pnew(Pool& p, double x, double y) {
   if (p.n >= p.cap) return -1;
@@ -170,74 +184,73 @@ __device__ void tog(int* s) {
   else if (*s == EX_EXIT) *s = EX_ENTRY;
 }
 
-__device__ int ser_build(SerialArgs& a) {
-  Pool& P = a.P;
-  Pool& Q = a.Q;
-  int nB = a.nB, nQ = a.nQ, i = 0;
-  for (int ii = 0; ii <= a.bSize; ++ii) {
-    int sv = ii < a.bSize ? ii : 0;
-    double vx = a.bP[2 * sv], vy = a.bP[2 * sv + 1];
-    const long long kvx = okey(vx), kvy = okey(vy);  // compares on order keys
-    while (okey(a.ixB[(2 * i) % (2 * nB)]) != kvx || okey(a.ixB[(2 * i + 1) % (2 * nB)]) != kvy) {
-      if (i >= nB) return 2;
-      int v = pnew(P, a.ixB[2 * i], a.ixB[2 * i + 1]);
-      if (v < 0) return 3;
-      P.label[v] = a.labB[i];
-      P.isect[v] = 1;
-      i++;
-    }
-    if (ii < a.bSize) {
-      int v = pnew(P, vx, vy);
-      if (v != i) return 2;
-      P.source[v] = 1;
-      P.label[v] = a.labB[i];
-      if (a.alB[i] != -100) P.isect[v] = 1;
-    }
-    i++;
-  }
-  if (P.n != nB) return 2;
-  for (int v = 0; v < nB; ++v) {
-    P.next[v] = (v + 1) % nB;
-    P.prev[v] = (v + nB - 1) % nB;
-  }
-  i = 0;
-  for (int ii = 0; ii <= a.cSize; ++ii) {
-    int sv = ii < a.cSize ? ii : 0;
-    double vx = a.cP[2 * (a.cStart + sv)], vy = a.cP[2 * (a.cStart + sv) + 1];
-    const long long kvx = okey(vx), kvy = okey(vy);
-    while (okey(a.ixC[(2 * i) % (2 * nQ)]) != kvx || okey(a.ixC[(2 * i + 1) % (2 * nQ)]) != kvy) {
-      if (i >= nQ) return 2;
-      int v = pnew(Q, a.ixC[2 * i], a.ixC[2 * i + 1]);
-      if (v < 0) return 3;
-      Q.label[v] = a.labC[i];
-      Q.isect[v] = 1;
-      int t = a.nbC[i] - 1;
-      if (t < 0 || t >= nB) return 2;
-      Q.nb[v] = t;
-      P.nb[t] = v;
-      i++;
-    }
-    if (ii < a.cSize) {
-      int v = pnew(Q, vx, vy);
-      if (v != i) return 2;
-      Q.source[v] = 1;
-      Q.label[v] = a.labC[i];
-      if (a.nbC[i] != -100) {
-        int t = a.nbC[i] - 1;
-        if (t < 0 || t >= nB) return 2;
-        Q.isect[v] = 1;
-        Q.nb[v] = t;
-        P.nb[t] = v;
+// copyToLinkedList (src/clip.cpp:606-695) for one side, one component after
+// another: each walked from its first vertex and closed on it as the
+// reference's single ring is; the lists wrap within their component.  O:
+// the base's pool when building the overlay's (neighbour links), else null.
+__device__ int ser_build_side(Pool& P, Pool* O, const double* poly, int n, const int* nx,
+                              int* roots, int nr, const double* ix, int nS, const int* alpha,
+                              const int* nbr, const int* lab) {
+  int vs = 0;
+  for (int k = 0; k < nr; ++k) {
+    int ve = vs + 1;
+    while (ve < n && (nx ? nx[ve - 1] : ve) == ve) ++ve;
+    const int lo = roots ? roots[k] : 0, hi = roots ? roots[k + 1] : nS;
+    int i = lo;
+    for (int ii = vs; ii <= ve; ++ii) {
+      const bool last = ii == ve;
+      const int sv = last ? vs : ii;
+      const double vx = poly[2 * sv], vy = poly[2 * sv + 1];
+      const long long kvx = okey(vx), kvy = okey(vy);  // compares on order keys
+      for (;;) {
+        const int sl = i == hi ? lo : i;
+        if (i > hi || (okey(ix[2 * sl]) == kvx && okey(ix[2 * sl + 1]) == kvy)) break;
+        if (i >= hi) return 2;
+        const int v = pnew(P, ix[2 * i], ix[2 * i + 1]);
+        if (v < 0) return 3;
+        P.label[v] = lab[i];
+        P.isect[v] = 1;
+        if (O) {
+          const int t = nbr[i] - 1;
+          if (t < 0 || t >= O->n) return 2;
+          P.nb[v] = t;
+          O->nb[t] = v;
+        }
+        i++;
       }
+      if (i > hi || (!last && i >= hi)) return 2;  // more vertices than the component's slots
+      if (!last) {
+        const int v = pnew(P, vx, vy);
+        if (v != i) return 2;
+        P.source[v] = 1;
+        P.label[v] = lab[i];
+        if (!O) {
+          if (alpha[i] != -100) P.isect[v] = 1;
+        } else if (nbr[i] != -100) {
+          const int t = nbr[i] - 1;
+          if (t < 0 || t >= O->n) return 2;
+          P.isect[v] = 1;
+          P.nb[v] = t;
+          O->nb[t] = v;
+        }
+      }
+      i++;
     }
-    i++;
+    for (int v = lo; v < hi; ++v) {
+      P.next[v] = v + 1 == hi ? lo : v + 1;
+      P.prev[v] = v == lo ? hi - 1 : v - 1;
+    }
+    vs = ve;
   }
-  if (Q.n != nQ) return 2;
-  for (int v = 0; v < nQ; ++v) {
-    Q.next[v] = (v + 1) % nQ;
-    Q.prev[v] = (v + nQ - 1) % nQ;
-  }
-  return 0;
+  return P.n == nS ? 0 : 2;
+}
+
+__device__ int ser_build(SerialArgs& a) {
+  const int r = ser_build_side(a.P, nullptr, a.bP, a.bSize, a.bnx, a.rootsP, a.nrP, a.ixB, a.nB,
+                               a.alB, nullptr, a.labB);
+  if (r) return r;
+  return ser_build_side(a.Q, &a.P, a.cP + 2 * a.cStart, a.cSize, a.cnx, a.rootsQ, a.nrQ, a.ixC,
+                        a.nQ, nullptr, a.nbC, a.labC);
 }
 
 __device__ Pool& side(SerialArgs& a, int s) { return s == 0 ? a.P : a.Q; }
@@ -284,14 +297,53 @@ __device__ int pip_side(SerialArgs& a, int s, int root, double rx, double ry, co
   return ppip(p, root, rx, ry);
 }
 
+// pointInPoly against every component of side s: each one containing the
+// point toggles the answer (lib/optimizedFostersAlgorithm/polyclip.cpp:
+// 503-507, :593-595); one component is the reference's test
+template <class PipP>
+__device__ int pip_all(SerialArgs& a, int s, double rx, double ry, const PipP& pp) {
+  const int nr = s == 0 ? a.nrP : a.nrQ;
+  int in = 0;
+  for (int k = 0; k < nr; ++k) in ^= pip_side(a, s, sroot(a, s, k), rx, ry, pp);
+  return in;
+}
+
+// noCrossingVertex(UNION) (foster/polygon.h:465-475) of the component at root
+__device__ bool no_cross(SerialArgs& a, const Pool& p, int root) {
+  int V = root;
+  do {
+    if (p.isect[V] && (p.label[V] == L_CROSSING || p.label[V] == L_DCROSS)) return false;
+    if (a.unite && p.isect[V] && (p.label[V] == L_BOUNCING || p.label[V] == L_DBOUNCE))
+      return false;
+    V = p.next[V];
+  } while (V != root);
+  return true;
+}
+
+__device__ bool all_on_on(const Pool& p, int root) {
+  int V = root;
+  do {
+    if (p.label[V] != L_ON_ON) return false;
+    V = p.next[V];
+  } while (V != root);
+  return true;
+}
+
+// labelIntersections2 (foster/polyclip.h:337-709) over every component of
+// both sides, in the order of Foster's multi-component code (lib/
+// optimizedFostersAlgorithm/polyclip.cpp:335-780): chains, interior and
+// identical components, entry/exit flags per component; then createResult2
+// (:717-759) from P's components in order.  A component's "no crossing"
+// and "all ON_ON" tests are repeated where needed: no label they read
+// changes between the steps.
 template <class PipP>
 __device__ int ser_label_trace_t(SerialArgs& a, const PipP& pipP) {
   Pool& P = a.P;
   Pool& Q = a.Q;
-  int roots[2] = {0, 0};
   // (2) chains
-  {
-    int V = roots[0];
+  for (int k = 0; k < a.nrP; ++k) {
+    const int root = sroot(a, 0, k);
+    int V = root;
     do {
       if (P.isect[V] && (P.label[V] == L_LEFT_ON || P.label[V] == L_RIGHT_ON)) {
         int x = P.label[V] == L_LEFT_ON ? 0 : 1;
@@ -313,116 +365,117 @@ __device__ int ser_label_trace_t(SerialArgs& a, const PipP& pipP) {
         Q.label[P.nb[I]] = chain;
       }
       V = P.next[V];
-    } while (V != roots[0]);
+    } while (V != root);
   }
-  // (3.5)
-  int noIsect[2] = {0, 0}, ident[2] = {0, 0};
-  for (int s = 0; s < 2; ++s) {
-    Pool& p = side(a, s);
-    int root = roots[s], nocross = 1, V = root;
-    do {
-      if (p.isect[V] && (p.label[V] == L_CROSSING || p.label[V] == L_DCROSS)) nocross = 0;
-      // noCrossingVertex(UNION), foster/polygon.h:465-475
-      if (a.unite && p.isect[V] && (p.label[V] == L_BOUNCING || p.label[V] == L_DBOUNCE))
-        nocross = 0;
-      V = p.next[V];
-    } while (V != root);
-    if (!nocross) continue;
-    noIsect[s] = 1;
-    int allon = 1;
-    V = root;
-    do {
-      if (p.label[V] != L_ON_ON) allon = 0;
-      V = p.next[V];
-    } while (V != root);
-    if (allon) {
-      ident[s] = 1;
-      continue;
-    }
-    double px = 0, py = 0;
-    int found = 0;
-    V = root;
-    do {
-      if (!p.isect[V]) {
-        px = p.x[V];
-        py = p.y[V];
-        found = 1;
-        break;
-      }
-      V = p.next[V];
-    } while (V != root);
-    if (!found) {
-      Pool& o = side(a, 1 - s);
-      V = root;
+  // (3.5) components without crossings: inside the other side (or outside,
+  // for the union), copied whole
+  for (int s = 0; s < 2; ++s)
+    for (int k = 0; k < (s == 0 ? a.nrP : a.nrQ); ++k) {
+      Pool& p = side(a, s);
+      const int root = sroot(a, s, k);
+      if (!no_cross(a, p, root) || all_on_on(p, root)) continue;
+      double px = 0, py = 0;
+      int found = 0, V = root;
       do {
-        int nbV = p.nb[V], nbN = p.nb[p.next[V]];
-        if (nbV < 0) return 2;
-        if (nbN != o.prev[nbV] && nbN != o.next[nbV]) {
-          px = dmul(0.5, dadd(p.x[V], p.x[p.next[V]]));
-          py = dmul(0.5, dadd(p.y[V], p.y[p.next[V]]));
+        if (!p.isect[V]) {
+          px = p.x[V];
+          py = p.y[V];
           found = 1;
           break;
         }
         V = p.next[V];
       } while (V != root);
-      if (!found) return 2;
+      if (!found) {
+        Pool& o = side(a, 1 - s);
+        V = root;
+        do {
+          int nbV = p.nb[V], nbN = p.nb[p.next[V]];
+          if (nbV < 0) return 2;
+          if (nbN != o.prev[nbV] && nbN != o.next[nbV]) {
+            px = dmul(0.5, dadd(p.x[V], p.x[p.next[V]]));
+            py = dmul(0.5, dadd(p.y[V], p.y[p.next[V]]));
+            found = 1;
+            break;
+          }
+          V = p.next[V];
+        } while (V != root);
+        if (!found) return 2;
+      }
+      if (pip_all(a, 1 - s, px, py, pipP) ^ a.unite)
+        if (rcopy(a, p, root)) return 3;
     }
-    if (pip_side(a, 1 - s, roots[1 - s], px, py, pipP) ^ a.unite)
-      if (rcopy(a, p, root)) return 3;
-  }
-  if (ident[0] && ident[1]) {
-    int target = P.nb[roots[0]], V = roots[1], found = 0;
-    do {
-      if (V == target) found = 1;
-      V = Q.next[V];
-    } while (V != roots[1]);
-    if (found && rcopy(a, P, roots[0])) return 3;
+  // identical components (polyclip.cpp:516-538): P's component k is added
+  // when the identical component of Q holding its root's neighbour is a hole
+  // exactly when k is (inside an odd number of its side's other components)
+  for (int k = 0; k < a.nrP; ++k) {
+    const int rk = sroot(a, 0, k);
+    if (!no_cross(a, P, rk) || !all_on_on(P, rk)) continue;
+    int holeP = 0;
+    for (int j = 0; j < a.nrP; ++j)
+      if (j != k) holeP ^= pip_side(a, 0, sroot(a, 0, j), P.x[rk], P.y[rk], pipP);
+    const int target = P.nb[rk];
+    for (int m = 0; m < a.nrQ; ++m) {
+      const int rm = sroot(a, 1, m);
+      if (!no_cross(a, Q, rm) || !all_on_on(Q, rm)) continue;
+      int V = rm, found = 0;
+      do {
+        if (V == target) found = 1;
+        V = Q.next[V];
+      } while (V != rm);
+      if (!found) continue;
+      int holeQ = 0;
+      for (int j = 0; j < a.nrQ; ++j)
+        if (j != m) holeQ ^= pip_side(a, 1, sroot(a, 1, j), Q.x[rm], Q.y[rm], pipP);
+      if (holeP == holeQ && rcopy(a, P, rk)) return 3;
+      break;
+    }
   }
   // (4)
-  for (int s = 0; s < 2; ++s) {
-    if (noIsect[s]) continue;
-    Pool& p = side(a, s);
-    unsigned char* split = s == 0 ? a.splitP : a.splitQ;
-    unsigned char* cross = s == 0 ? a.crossP : a.crossQ;
-    int V = ser_non_isect_vertex(a, s, roots[s]);
-    if (V == -3) return 3;
-    if (V < 0) return 2;
-    int status = EX_ENTRY;
-    if (pip_side(a, 1 - s, roots[1 - s], p.x[V], p.y[V], pipP)) tog(&status);
-    int first = 1, I = V;
-    do {
-      if (p.isect[I]) {
-        if (p.label[I] == L_CROSSING) {
-          p.enex[I] = status;
-          tog(&status);
-        }
-        if (p.label[I] == L_BOUNCING && ((status == EX_EXIT) ^ a.unite)) split[I] = 1;
-        if (p.label[I] == L_DCROSS) {
-          p.enex[I] = status;
-          if (first) {
-            if ((status == EX_EXIT) ^ a.unite) p.label[I] = L_CROSSING;
-            first = 0;
-          } else {
-            if ((status == EX_ENTRY) ^ a.unite) p.label[I] = L_CROSSING;
-            first = 1;
+  for (int s = 0; s < 2; ++s)
+    for (int k = 0; k < (s == 0 ? a.nrP : a.nrQ); ++k) {
+      Pool& p = side(a, s);
+      if (no_cross(a, p, sroot(a, s, k))) continue;
+      unsigned char* split = s == 0 ? a.splitP : a.splitQ;
+      unsigned char* cross = s == 0 ? a.crossP : a.crossQ;
+      int V = ser_non_isect_vertex(a, s, sroot(a, s, k));
+      if (V == -3) return 3;
+      if (V < 0) return 2;
+      int status = EX_ENTRY;
+      if (pip_all(a, 1 - s, p.x[V], p.y[V], pipP)) tog(&status);
+      int first = 1, I = V;
+      do {
+        if (p.isect[I]) {
+          if (p.label[I] == L_CROSSING) {
+            p.enex[I] = status;
+            tog(&status);
+          }
+          if (p.label[I] == L_BOUNCING && ((status == EX_EXIT) ^ a.unite)) split[I] = 1;
+          if (p.label[I] == L_DCROSS) {
+            p.enex[I] = status;
+            if (first) {
+              if ((status == EX_EXIT) ^ a.unite) p.label[I] = L_CROSSING;
+              first = 0;
+            } else {
+              if ((status == EX_ENTRY) ^ a.unite) p.label[I] = L_CROSSING;
+              first = 1;
+              tog(&status);
+            }
+          }
+          if (p.label[I] == L_DBOUNCE) {
+            p.enex[I] = status;
+            if (first) {
+              if ((status == EX_EXIT) ^ a.unite) cross[I] = 1;
+              first = 0;
+            } else {
+              if ((status == EX_ENTRY) ^ a.unite) cross[I] = 1;
+              first = 1;
+            }
             tog(&status);
           }
         }
-        if (p.label[I] == L_DBOUNCE) {
-          p.enex[I] = status;
-          if (first) {
-            if ((status == EX_EXIT) ^ a.unite) cross[I] = 1;
-            first = 0;
-          } else {
-            if ((status == EX_ENTRY) ^ a.unite) cross[I] = 1;
-            first = 1;
-          }
-          tog(&status);
-        }
-      }
-      I = p.next[I];
-    } while (I != V);
-  }
+        I = p.next[I];
+      } while (I != V);
+    }
   // (5) split pairs
   {
     int nP0 = P.n;
@@ -468,9 +521,9 @@ __device__ int ser_label_trace_t(SerialArgs& a, const PipP& pipP) {
     }
   }
   // createResult2
-  {
-    int root = roots[0], It = root;
-    long long guard = 4LL * (P.n + Q.n) + 16;
+  long long guard = 4LL * (P.n + Q.n) + 16;
+  for (int k = 0; k < a.nrP; ++k) {
+    int root = sroot(a, 0, k), It = root;
     do {
       if (P.isect[It] && P.label[It] == L_CROSSING) {
         int r = rnew(a);

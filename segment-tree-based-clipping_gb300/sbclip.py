@@ -99,6 +99,26 @@ class AreaGraph:
             self._h = None
 
 
+class _Components(ctypes.Structure):
+    _fields_ = [("b_comp", ctypes.c_void_p), ("nb_comp", ctypes.c_longlong),
+                ("c_comp", ctypes.c_void_p), ("nc_comp", ctypes.c_longlong)]
+
+
+def pack_components(polys):
+    """(xy, polygon offsets, component offsets) of polygons given as lists of
+    (n_i, 2) component arrays (a bare array is one component)."""
+    comps, off, comp = [], [0], [0]
+    for p in polys:
+        parts = list(p) if isinstance(p, (list, tuple)) else [p]
+        for c in parts:
+            c = np.ascontiguousarray(c, np.float64).reshape(-1, 2)
+            comps.append(c)
+            comp.append(comp[-1] + len(c))
+        off.append(comp[-1])
+    xy = np.ascontiguousarray(np.concatenate(comps)) if comps else np.zeros((0, 2))
+    return xy, np.array(off, np.int64), np.array(comp, np.int64)
+
+
 class _PairwiseJob(ctypes.Structure):
     _fields_ = [("b_xy", ctypes.c_void_p), ("nb", ctypes.c_int), ("noverlays", ctypes.c_int),
                 ("c_xy", ctypes.c_void_p), ("c_off", ctypes.c_void_p)]
@@ -147,6 +167,15 @@ def load_library(path: str | os.PathLike | None = None):
         getattr(L, nm).argtypes = [vp, ctypes.POINTER(_Batch), vp, vp, vp]
     for nm in ("sbc_area_backward", "sbc_area_backward_device"):
         getattr(L, nm).argtypes = [vp, ctypes.POINTER(_Batch), vp, vp, vp, vp]
+    for nm in ("sbc_clip_batch_components", "sbc_clip_batch_components_device"):
+        getattr(L, nm).argtypes = [vp, ctypes.POINTER(_Batch), ctypes.POINTER(_Components),
+                                   ctypes.POINTER(_BatchRings), vp]
+    L.sbc_clip_components.argtypes = [vp, vp, vp, i, vp, vp, i, ctypes.POINTER(_Rings), vp]
+    L.sbc_area_forward_components_device.argtypes = [vp, ctypes.POINTER(_Batch),
+                                                     ctypes.POINTER(_Components), vp, vp, vp]
+    L.sbc_area_backward_components_device.argtypes = [vp, ctypes.POINTER(_Batch),
+                                                      ctypes.POINTER(_Components), vp, vp, vp,
+                                                      vp]
     for nm in ("sbc_clip_pairwise", "sbc_clip_pairwise_device"):
         getattr(L, nm).argtypes = [vp, ctypes.POINTER(_PairwiseJob), ctypes.POINTER(_BatchRings),
                                    vp]
@@ -343,6 +372,49 @@ class Clipper:
         for p in range(np_):
             out.append([xy[ro[q]:ro[q + 1]] for q in range(pr[p], pr[p + 1])])
         return out, st
+
+    def clip_components(self, base, overlay, stream: int | None = None):
+        """Rings of one pair of multi-component polygons (lists of component
+        arrays) through sbc_clip_components."""
+        bxy, _, bk = pack_components([base])
+        cxy, _, ck = pack_components([overlay])
+        bk32, ck32 = bk.astype(np.int32), ck.astype(np.int32)
+        r = _Rings()
+        self._check(self._L.sbc_clip_components(self._h, bxy.ctypes.data, bk32.ctypes.data,
+                                                len(bk32) - 1, cxy.ctypes.data, ck32.ctypes.data,
+                                                len(ck32) - 1, ctypes.byref(r), stream))
+        return _rings_from(r)
+
+    def clip_batch_components(self, bases, overlays, stream: int | None = None):
+        """Rings of every pair of multi-component polygons (each a list of
+        component arrays, or one array): (list of ring lists, status array)."""
+        if len(bases) != len(overlays):
+            raise ValueError("one overlay per base")
+        bxy, boff, bk = pack_components(bases)
+        cxy, coff, ck = pack_components(overlays)
+        b = _Batch(len(bases), bxy.ctypes.data, boff.ctypes.data, cxy.ctypes.data,
+                   coff.ctypes.data)
+        k = _Components(bk.ctypes.data, len(bk) - 1, ck.ctypes.data, len(ck) - 1)
+        r = _BatchRings()
+        self._check(self._L.sbc_clip_batch_components(self._h, ctypes.byref(b), ctypes.byref(k),
+                                                      ctypes.byref(r), stream))
+        return self._unpack_rings(r, len(bases))
+
+    def area_forward_components_device(self, npairs, d_bxy, d_boff, d_cxy, d_coff, d_bcomp,
+                                       nb_comp, d_ccomp, nc_comp, d_area, d_status=None,
+                                       stream: int | None = None):
+        b = _Batch(npairs, d_bxy, d_boff, d_cxy, d_coff)
+        k = _Components(d_bcomp, nb_comp, d_ccomp, nc_comp)
+        self._check(self._L.sbc_area_forward_components_device(
+            self._h, ctypes.byref(b), ctypes.byref(k), d_area, d_status, stream))
+
+    def area_backward_components_device(self, npairs, d_bxy, d_boff, d_cxy, d_coff, d_bcomp,
+                                        nb_comp, d_ccomp, nc_comp, d_grad_area, d_grad_b,
+                                        d_grad_c, stream: int | None = None):
+        b = _Batch(npairs, d_bxy, d_boff, d_cxy, d_coff)
+        k = _Components(d_bcomp, nb_comp, d_ccomp, nc_comp)
+        self._check(self._L.sbc_area_backward_components_device(
+            self._h, ctypes.byref(b), ctypes.byref(k), d_grad_area, d_grad_b, d_grad_c, stream))
 
     @staticmethod
     def _unpack_rings(r, np_):

@@ -18,6 +18,14 @@
 // microseconds: skeleton endlist cover cand+merge label total.  --union
 // writes base ∪ overlay_i instead (the Foster back end's UNION switch,
 // foster/polyclip.h:39, which the reference's driver leaves off).
+//
+//   seg <P.poly> <Q.poly> <R.poly> [--union]
+//
+// Polygons with several components (holes, islands) in the .poly format of
+// the reference's Foster program (lib/optimizedFostersAlgorithm/README.md:
+// 43-62: `x y,` per vertex, `;` closing each component, no count line) are
+// clipped as such (sbc_clip_components), P as the base, and R written in the
+// same format.
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -60,6 +68,46 @@ bool read_poly(const char* path, std::vector<double>& xy) {
   return true;
 }
 
+// Foster's .poly format: the first line holds a vertex (two numbers), not a
+// vertex count
+bool is_foster_file(const char* path) {
+  FILE* f = fopen(path, "r");
+  if (!f) return false;
+  double x, y;
+  bool ok = fscanf(f, " %lf %lf", &x, &y) == 2;
+  if (ok) {
+    int c = fgetc(f);
+    while (c == ' ' || c == '\t') c = fgetc(f);
+    ok = c == ',' || c == ';';
+  }
+  fclose(f);
+  return ok;
+}
+
+// polygon.h operator>> (foster/polygon.h:550-571) per component: `x y`
+// then `,` (more vertices) or `;` (component ends); comp receives the
+// component starts and the vertex count
+bool read_foster(const char* path, std::vector<double>& xy, std::vector<int>& comp) {
+  FILE* f = fopen(path, "r");
+  if (!f) return false;
+  xy.clear();
+  comp.assign(1, 0);
+  double x, y;
+  int n = 0;
+  while (fscanf(f, " %lf %lf", &x, &y) == 2) {
+    xy.push_back(x);
+    xy.push_back(y);
+    ++n;
+    int c = fgetc(f);
+    while (c == ' ' || c == '\t') c = fgetc(f);
+    if (c != ',') comp.push_back(n);  // `;`, a line end or the end of the file
+    if (c == EOF) break;
+  }
+  if (comp.back() != n) comp.push_back(n);
+  fclose(f);
+  return n > 0;
+}
+
 bool is_poly_file(const char* path) {
   FILE* f = fopen(path, "r");
   if (!f) return false;
@@ -100,6 +148,32 @@ int main(int argc, char** argv) {
   if (pos.size() < 2) {
     printf("3 parameters required\n./seg <base polygon path> <subject polygon path>\n");
     return 1;
+  }
+  if (pos.size() == 3 && is_foster_file(pos[0]) && is_foster_file(pos[1])) {
+    std::vector<double> pxy, qxy;
+    std::vector<int> pk, qk;
+    if (!read_foster(pos[0], pxy, pk) || !read_foster(pos[1], qxy, qk)) {
+      fprintf(stderr, "cannot read the .poly inputs\n");
+      return 1;
+    }
+    sbc_options opt{device, flags};
+    sbc_ctx* ctx = nullptr;
+    if (sbc_create(&opt, &ctx)) {
+      fprintf(stderr, "sbc_create failed\n");
+      return 2;
+    }
+    sbc_rings r;
+    int rc = sbc_clip_components(ctx, pxy.data(), pk.data(), (int)pk.size() - 1, qxy.data(),
+                                 qk.data(), (int)qk.size() - 1, &r, nullptr);
+    if (rc) {
+      fprintf(stderr, "clipping failed (%d): %s\n", rc, sbc_last_error(ctx));
+      sbc_destroy(ctx);
+      return 3;
+    }
+    if (!write_rings(pos[2], r, precision)) fprintf(stderr, "cannot write %s\n", pos[2]);
+    printf("R %d rings\n", r.nrings);
+    sbc_destroy(ctx);
+    return 0;
   }
   if (pos.size() == 3 && !is_poly_file(pos[2])) {
     outfile = pos[2];
