@@ -109,6 +109,7 @@ struct PairWork {
   // components: the merged slot of each component's first vertex, ending
   // with the slot count (filled by the thread back end)
   int *rootB, *rootC;
+  int* pmid;  // the warp back end's PwMid between its two kernels
   // pair-relative successor of each vertex within its component (null: one
   // ring); not carved, set per pair
   const int* bnx = nullptr;
@@ -212,6 +213,7 @@ __host__ __device__ __forceinline__ PairWork carve(Carver& cv, const Caps& c) {
   w.csort = cv.take<unsigned long long>(npow2_dev(c.nc));
   w.rootB = cv.take<int>(c.nb + 1);
   w.rootC = cv.take<int>(c.nc + 1);
+  w.pmid = cv.take<int>(4);
   return w;
 }
 
@@ -1314,9 +1316,12 @@ __device__ void pair_tape_warp(const double* b, int nb, const double* c, int nc,
   __syncwarp();
 }
 
-// One warp per pair: the records in the reference's order, then rows
-// A9-A18 by the warp; a pair whose arrays take a path the warp back end does
-// not follow (w.state[3] = 1) is clipped by the thread back end below.
+// One warp per pair, in two kernels: the records in the reference's order
+// and rows A9-A14 (k_batch_pw, w.state[3] = 2 when done), then rows A15-A18
+// (k_batch_pw2).  Two kernels keep each one's code small enough for the
+// instruction cache when the warps of an SM are at different steps.  A pair
+// whose arrays take a path the warp back end does not follow (w.state[3] = 1)
+// is clipped by the thread back end below.
 __global__ void __launch_bounds__(128) k_batch_pw(ClipArgs A) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
@@ -1351,11 +1356,43 @@ __global__ void __launch_bounds__(128) k_batch_pw(ClipArgs A) {
     w.phit[i] = PwHit{0, w.hb[h] >> 1, w.hc[h] >> 1, w.ht[h], w.hkey[h], w.hal[h], w.hbt[h]};
   }
   __syncwarp();
+  PwWork pw = w.pw;
+  PwMid mid;
+  const int st = pw_clip_head(A.bxy + 2 * A.boff[p], nb, A.cxy + 2 * A.coff[p], nc, w.phit,
+                              pw_caps(nb, nc, K, 1), pw, &mid);
+  if (st == PS_UNDEF) {
+    if (lane == 0) batch_fail(A, p, w, PS_UNDEF, 0);
+    return;
+  }
+  if (lane == 0) {
+    if (st == PS_OK) {
+      w.pmid[0] = mid.nr;
+      w.pmid[1] = mid.knd;
+      w.pmid[2] = mid.nB;
+      w.pmid[3] = mid.nQ;
+    }
+    w.state[3] = st == PS_OK ? 2 : 1;  // PS_FALLBACK / PS_CAP: the thread back end
+  }
+}
+
+__global__ void __launch_bounds__(128, 4) k_batch_pw2(ClipArgs A) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  if ((t >> 5) >= A.np) return;
+  const int p = (int)(t >> 5);
+  const int pass = A.pass_of ? A.pass_of[p] : 0;
+  int nb, nc;
+  if (pass < 0 || !A.small(p, &nb, &nc)) return;
+  Caps cp;
+  PairWork w = A.work(p, nb, nc, pass, &cp);
+  if (w.state[0] != PS_OK || w.state[3] != 2) return;
+  const int K = w.state[2];
   const double* b = A.bxy + 2 * A.boff[p];
   const double* c = A.cxy + 2 * A.coff[p];
   PwWork pw = w.pw;
+  const PwMid mid{w.pmid[0], w.pmid[1], w.pmid[2], w.pmid[3]};
   int nr = 0, nv = 0;
-  const int st = pw_clip_core(b, nb, c, nc, w.phit, pw_caps(nb, nc, K, 1), pw,
+  const int st = pw_clip_tail(b, nb, c, nc, pw_caps(nb, nc, K, 1), pw, mid,
                               PipSmall{b, nb, nullptr, 0}, A.unite, &nr, &nv);
   if (st != PS_OK && st != PS_UNDEF) {
     if (lane == 0) w.state[3] = 1;  // the thread back end takes the pair
@@ -1483,6 +1520,10 @@ void launch_clip(const ClipArgs& A, const BatchShape& sh, double in_bytes, cudaS
     k_batch_pw<<<grid_for(32LL * A.np, 128), 128, 0, st>>>(A);
   }
   {
+    ::sbc::KProbe kp_("k_batch_pw2", st, in_bytes);
+    k_batch_pw2<<<grid_for(32LL * A.np, 128), 128, 0, st>>>(A);
+  }
+  {
     ::sbc::KProbe kp_("k_batch_back", st, in_bytes);
     k_batch_back<<<grid_for(A.np, sh.back), sh.back, 0, st>>>(A);
   }
@@ -1546,23 +1587,34 @@ __global__ void k_batch_pack(int np, const long long* __restrict__ boff,
   for (int i = 0; i < 2 * nv; ++i) xy[2 * v0 + i] = w.rxy[i];
 }
 
-// d(area)/d(vertices), one thread per pair, from the forward pass's tape
-__global__ void __launch_bounds__(kBatchBlock)
+// d(area)/d(vertices), one warp per pair, from the forward pass's tape.  The
+// lanes take 32 ring vertices at a time and compute their contributions
+// (the crossings' FP64 chain rule in parallel, up to four target vertices
+// each, in four rounds).  In each round the lanes naming the same vertex
+// form a group (match_any) whose lowest lane sums their values in lane order
+// and adds the sum: every gradient entry is summed in an order fixed by the
+// rings alone, whatever the launch shape.
+__global__ void __launch_bounds__(128)
 k_batch_backward(int np, const double* __restrict__ bxy, const long long* __restrict__ boff,
                  const double* __restrict__ cxy, const long long* __restrict__ coff, Arenas ar,
                  const int* __restrict__ status, const int* __restrict__ nrings,
                  const double* __restrict__ gA, const int* __restrict__ bnx,
                  const int* __restrict__ cnx, double* __restrict__ gb, double* __restrict__ gc) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= np) return;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  if ((t >> 5) >= np) return;
+  const int p = (int)(t >> 5);
   const int nb = (int)(boff[p + 1] - boff[p]), nc = (int)(coff[p + 1] - coff[p]);
   double* gbp = gb + 2 * boff[p];
   double* gcp = gc + 2 * coff[p];
-  for (int i = 0; i < 2 * nb; ++i) gbp[i] = 0.0;
-  for (int i = 0; i < 2 * nc; ++i) gcp[i] = 0.0;
+  for (int i = lane; i < 2 * nb; i += 32) gbp[i] = 0.0;
+  for (int i = lane; i < 2 * nc; i += 32) gcp[i] = 0.0;
   if (status[p] != SBC_OK || nrings[p] == 0 || ar.pass[p] < 0) return;
+  __syncwarp();
   const double* b = bxy + 2 * boff[p];
   const double* c = cxy + 2 * coff[p];
+  const int* bn = bnx ? bnx + boff[p] : nullptr;
+  const int* cn = cnx ? cnx + coff[p] : nullptr;
   const Caps cp = caps_of(nb, nc, hit_cap(nb, nc, ar.pass[p], ar.need[p]));
   Carver cv{const_cast<unsigned char*>(ar.at(p)), 0};
   const PairWork w = carve(cv, cp);
@@ -1570,41 +1622,65 @@ k_batch_backward(int np, const double* __restrict__ bxy, const long long* __rest
   const int nr = nrings[p];
   for (int r = 0; r < nr; ++r) {
     const int s = w.roff[r], e = w.roff[r + 1];
-    for (int i = s; i < e; ++i) {
-      const int ip = (i + 1 == e) ? s : i + 1, im = (i == s) ? e - 1 : i - 1;
-      // shoelace: dA/dx_i = (y_{i+1} - y_{i-1}) / 2, dA/dy_i = (x_{i-1} - x_{i+1}) / 2
-      const double gx = 0.5 * g * (w.rxy[2 * ip + 1] - w.rxy[2 * im + 1]);
-      const double gy = 0.5 * g * (w.rxy[2 * im] - w.rxy[2 * ip]);
-      const int4 t = w.tape[i];
-      if (t.x == 0) {
-        gbp[2 * t.y] += gx;
-        gbp[2 * t.y + 1] += gy;
-      } else if (t.x == 1) {
-        gcp[2 * t.y] += gx;
-        gcp[2 * t.y + 1] += gy;
-      } else if (t.x == 2) {
-        // I = (1 - alpha) b1 + alpha b2, alpha = A1 / (A1 - A2),
-        // A1 = A(b1, c1, c2), A2 = A(b2, c1, c2)
-        const int i1 = t.y, i2 = vsucc(bnx ? bnx + boff[p] : nullptr, nb, t.y), j1 = t.z,
-                  j2 = vsucc(cnx ? cnx + coff[p] : nullptr, nc, t.z);
-        const double b1x = b[2 * i1], b1y = b[2 * i1 + 1], b2x = b[2 * i2], b2y = b[2 * i2 + 1];
-        const double c1x = c[2 * j1], c1y = c[2 * j1 + 1], c2x = c[2 * j2], c2y = c[2 * j2 + 1];
-        const double A1 = (c1x - b1x) * (c2y - b1y) - (c1y - b1y) * (c2x - b1x);
-        const double A2 = (c1x - b2x) * (c2y - b2y) - (c1y - b2y) * (c2x - b2x);
-        const double d = A1 - A2;
-        const double al = A1 / d;
-        const double ga = gx * (b2x - b1x) + gy * (b2y - b1y);  // dA/dalpha
-        const double k1 = -A2 / (d * d) * ga, k2 = A1 / (d * d) * ga;  // dalpha/dA1, dalpha/dA2
-        // A(P, Q, R) partials: dP = (Qy - Ry, Rx - Qx), dQ = (Ry - Py, Px - Rx),
-        // dR = (Py - Qy, Qx - Px)
-        gbp[2 * i1] += (1.0 - al) * gx + k1 * (c1y - c2y);
-        gbp[2 * i1 + 1] += (1.0 - al) * gy + k1 * (c2x - c1x);
-        gbp[2 * i2] += al * gx + k2 * (c1y - c2y);
-        gbp[2 * i2 + 1] += al * gy + k2 * (c2x - c1x);
-        gcp[2 * j1] += k1 * (c2y - b1y) + k2 * (c2y - b2y);
-        gcp[2 * j1 + 1] += k1 * (b1x - c2x) + k2 * (b2x - c2x);
-        gcp[2 * j2] += k1 * (b1y - c1y) + k2 * (b2y - c1y);
-        gcp[2 * j2 + 1] += k1 * (c1x - b1x) + k2 * (c1x - b2x);
+    for (int i0 = s; i0 < e; i0 += 32) {
+      const int i = i0 + lane;
+      int tg[4] = {-1, -1, -1, -1};
+      double2 vv[4];
+      if (i < e) {
+        const int ip = (i + 1 == e) ? s : i + 1, im = (i == s) ? e - 1 : i - 1;
+        // shoelace: dA/dx_i = (y_{i+1} - y_{i-1}) / 2, dA/dy_i = (x_{i-1} - x_{i+1}) / 2
+        const double gx = 0.5 * g * (w.rxy[2 * ip + 1] - w.rxy[2 * im + 1]);
+        const double gy = 0.5 * g * (w.rxy[2 * im] - w.rxy[2 * ip]);
+        const int4 tp = w.tape[i];
+        if (tp.x == 0 || tp.x == 1) {
+          tg[0] = (tp.x << 30) | tp.y;
+          vv[0] = make_double2(gx, gy);
+        } else if (tp.x == 2) {
+          // I = (1 - alpha) b1 + alpha b2, alpha = A1 / (A1 - A2),
+          // A1 = A(b1, c1, c2), A2 = A(b2, c1, c2)
+          const int i1 = tp.y, i2 = vsucc(bn, nb, tp.y), j1 = tp.z, j2 = vsucc(cn, nc, tp.z);
+          const double b1x = b[2 * i1], b1y = b[2 * i1 + 1], b2x = b[2 * i2], b2y = b[2 * i2 + 1];
+          const double c1x = c[2 * j1], c1y = c[2 * j1 + 1], c2x = c[2 * j2], c2y = c[2 * j2 + 1];
+          const double A1 = (c1x - b1x) * (c2y - b1y) - (c1y - b1y) * (c2x - b1x);
+          const double A2 = (c1x - b2x) * (c2y - b2y) - (c1y - b2y) * (c2x - b2x);
+          const double d = A1 - A2;
+          const double al = A1 / d;
+          const double ga = gx * (b2x - b1x) + gy * (b2y - b1y);  // dA/dalpha
+          const double k1 = -A2 / (d * d) * ga, k2 = A1 / (d * d) * ga;  // dalpha/dA1, dalpha/dA2
+          // A(P, Q, R) partials: dP = (Qy - Ry, Rx - Qx), dQ = (Ry - Py, Px - Rx),
+          // dR = (Py - Qy, Qx - Px)
+          tg[0] = i1;
+          vv[0] = make_double2((1.0 - al) * gx + k1 * (c1y - c2y),
+                               (1.0 - al) * gy + k1 * (c2x - c1x));
+          tg[1] = i2;
+          vv[1] = make_double2(al * gx + k2 * (c1y - c2y), al * gy + k2 * (c2x - c1x));
+          tg[2] = (1 << 30) | j1;
+          vv[2] = make_double2(k1 * (c2y - b1y) + k2 * (c2y - b2y),
+                               k1 * (b1x - c2x) + k2 * (b2x - c2x));
+          tg[3] = (1 << 30) | j2;
+          vv[3] = make_double2(k1 * (b1y - c1y) + k2 * (b2y - c1y),
+                               k1 * (c1x - b1x) + k2 * (c1x - b2x));
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const unsigned act = __ballot_sync(0xffffffffu, tg[j] >= 0);
+        if (tg[j] >= 0) {
+          const unsigned grp = __match_any_sync(act, tg[j]);
+          double sx = 0.0, sy = 0.0;
+          for (unsigned m = grp; m; m &= m - 1) {
+            const int l = __ffs(m) - 1;
+            sx += __shfl_sync(grp, vv[j].x, l);
+            sy += __shfl_sync(grp, vv[j].y, l);
+          }
+          if (lane == __ffs(grp) - 1) {
+            double* gp = (tg[j] >> 30) ? gcp : gbp;
+            const int v = tg[j] & 0x3fffffff;
+            gp[2 * v] += sx;
+            gp[2 * v + 1] += sy;
+          }
+        }
+        __syncwarp();
       }
     }
   }
@@ -2130,7 +2206,7 @@ int BatchRunner::backward(const double* d_bxy, const long long* d_boff, const do
     ::sbc::KProbe kp_("k_batch_backward", st,
                       32.0 * (double)(h_boff_[p1] - h_boff_[p0] + h_coff_[p1] - h_coff_[p0]) +
                           8.0 * n);
-    k_batch_backward<<<grid_for(n, shape.bwd), shape.bwd, 0, st>>>(
+    k_batch_backward<<<grid_for(32LL * n, shape.bwd), shape.bwd, 0, st>>>(
         n, d_bxy, d_boff + p0, d_cxy, d_coff + p0, ar, status + p0, nrings + p0, d_gA + p0, bnx,
         cnx, d_gb, d_gc);
   }
@@ -2276,7 +2352,7 @@ int BatchRunner::graph_record(int np_, const double* d_bxy, const long long* d_b
     const Arenas ar{arena[0], aoff[0], abase_[0], arena[1], aoff[1], 0, pass, need_rec};
     {
       ::sbc::KProbe kp_("k_batch_backward", st);
-      k_batch_backward<<<grid_for(np, shape.bwd), shape.bwd, 0, st>>>(
+      k_batch_backward<<<grid_for(32LL * np, shape.bwd), shape.bwd, 0, st>>>(
           np, d_bxy, d_boff, d_cxy, d_coff, ar, status, nrings, d_gA, bnx, cnx, d_gb, d_gc);
     }
     if (out_area) cudaMemcpyAsync(out_area, area, sizeof(double) * np, cudaMemcpyDeviceToDevice, st);

@@ -685,17 +685,14 @@ __device__ __forceinline__ void pw_fill_edge(PwWork& w, const double* c, const i
 // loop lets the last of several writes to one slot win, the lanes keep the
 // largest writer index with atomicMax and that writer stores.  Every return
 // is taken by all lanes together.
-// One pair, rows A9-A18, by the calling warp (all 32 lanes): base b (nb
-// vertices), overlay c (nc), its K unique hits H in the reference's order
-// (base id, then first emission), a pointInPoly functor for the base side
-// (pip: its runIds / nruns are set here), union or intersection.  Returns
-// PS_OK with the rings in w.roff / w.rxy, PS_FALLBACK where the sparse back
-// end does not follow the arrays (the caller clips the pair another way),
-// PS_UNDEF or PS_CAP.
-template <class Pip>
-__device__ int pw_clip_core(const double* b, int nb, const double* c, int nc, const PwHit* H,
-                            const PwCaps& cp, PwWork& w, Pip pip, int unite, int* nrings_out,
-                            int* nverts_out) {
+// The scalars the two halves of the warp back end share.
+struct PwMid {
+  int nr, knd, nB, nQ;  // base runs, non-degenerate base records, slot counts
+};
+
+// Rows A9-A14: records, counts, alpha order, merged arrays, initial labels.
+__device__ int pw_clip_head(const double* b, int nb, const double* c, int nc, const PwHit* H,
+                            const PwCaps& cp, PwWork& w, PwMid* mid) {
   const int lane = threadIdx.x & 31;
   const int K = cp.K;
   // ---- A9: records arrive in the reference's order (base id, then first
@@ -913,22 +910,6 @@ __device__ int pw_clip_core(const double* b, int nb, const double* c, int nc, co
   for (int s = lane; s < nsp; s += 32) w.spnode[s] = -1;
   for (int q = lane; q < nQ; q += 32) w.cWin[q] = -1;
   __syncwarp();
-  // slot contents of the base's merged list
-  auto info = [&](int s, int hint, double* x, double* y, int* al, int* nbv) {
-    int vtx = 0;
-    const int si = pw_slot(w, nr, s, &vtx, hint);
-    if (si >= 0) {
-      *x = w.spx[si];
-      *y = w.spy[si];
-      *al = w.spal[si];
-      *nbv = w.spnb[si];
-    } else {
-      *x = b[2 * vtx];
-      *y = b[2 * vtx + 1];
-      *al = -100;
-      *nbv = -100;
-    }
-  };
   // ---- A14 initial labels, one sparse slot per lane (spnode holds each
   // slot's run meanwhile); the overlay slot takes the label of the last base
   // slot naming it.  Loops over lanes run in chunks closed by __syncwarp, so
@@ -1026,6 +1007,34 @@ __device__ int pw_clip_core(const double* b, int nb, const double* c, int nc, co
   for (int s = lane; s < nsp; s += 32) w.spnode[s] = -1;
   for (int q = lane; q < nQ; q += 32) w.labC[q] = w.cWin[q] >= 0 ? w.splab[w.cWinSI[q]] : 0;
   __syncwarp();
+  *mid = PwMid{nr, knd, nB, nQ};
+  return PS_OK;
+}
+
+// Rows A15-A18 from the head's arrays: linked lists, labelling, tracing,
+// clean-up and the rings out.
+template <class Pip>
+__device__ int pw_clip_tail(const double* b, int nb, const double* c, int nc, const PwCaps& cp,
+                            PwWork& w, const PwMid& mid, Pip pip, int unite, int* nrings_out,
+                            int* nverts_out) {
+  const int lane = threadIdx.x & 31;
+  const int nr = mid.nr, knd = mid.knd, nB = mid.nB, nQ = mid.nQ;
+  // slot contents of the base's merged list
+  auto info = [&](int s, int hint, double* x, double* y, int* al, int* nbv) {
+    int vtx = 0;
+    const int si = pw_slot(w, nr, s, &vtx, hint);
+    if (si >= 0) {
+      *x = w.spx[si];
+      *y = w.spy[si];
+      *al = w.spal[si];
+      *nbv = w.spnb[si];
+    } else {
+      *x = b[2 * vtx];
+      *y = b[2 * vtx + 1];
+      *al = -100;
+      *nbv = -100;
+    }
+  };
   // ---- A15 linked lists (copyToLinkedList, src/clip.cpp:606-695): the base's
   // with run nodes for its stretches of plain vertices.  Its walk visits, per
   // run r, the stretch of plain vertices since the previous run (one run
@@ -1433,6 +1442,24 @@ __device__ int pw_clip_core(const double* b, int nb, const double* c, int nc, co
     *nverts_out = (int)(unsigned)carry;
   }
   return PS_OK;
+}
+
+// One pair, rows A9-A18, by the calling warp (all 32 lanes): base b (nb
+// vertices), overlay c (nc), its K unique hits H in the reference's order
+// (base id, then first emission), a pointInPoly functor for the base side
+// (pip: its runIds / nruns are set by the tail), union or intersection.
+// Returns PS_OK with the rings in w.roff / w.rxy, PS_FALLBACK where the
+// sparse back end does not follow the arrays (the caller clips the pair
+// another way), PS_UNDEF or PS_CAP.  The head and the tail may also run as
+// separate kernels, PwMid carried between them.
+template <class Pip>
+__device__ int pw_clip_core(const double* b, int nb, const double* c, int nc, const PwHit* H,
+                            const PwCaps& cp, PwWork& w, Pip pip, int unite, int* nrings_out,
+                            int* nverts_out) {
+  PwMid mid;
+  const int st = pw_clip_head(b, nb, c, nc, H, cp, w, &mid);
+  if (st != PS_OK) return st;
+  return pw_clip_tail(b, nb, c, nc, cp, w, mid, pip, unite, nrings_out, nverts_out);
 }
 
 }  // namespace
