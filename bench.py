@@ -181,12 +181,20 @@ KERNEL_BOUND = {
     "k_alpha_classify": "hbm", "k_cover_count": "latency", "k_alpha_sort_long": "latency",
     "k_lr_jump_coop": "latency", "k_tr_jump_coop": "latency",
     "k_grid_scatter": "hbm", "k_edge_fbox": "hbm", "k_copy_runs": "hbm",
-    "k_pair_exact": "fp64", "k_pw_cand_test": "fp64", "k_batch_cand": "fp64", "k_batch_cand_sweep": "fp64", "k_labels": "fp64",
+    "k_pair_exact": "fp64", "k_pw_cand_test": "fp64", "k_batch_cand": "fp64",
+    "k_batch_cand_sweep": "fp64", "k_labels": "fp64", "k_batch_backward": "fp64",
     "k_grid_warp": "latency", "k_grid_small": "latency", "k_lr_jump": "latency",
     "k_tr_jump": "latency", "k_alpha_sort": "latency", "k_batch_back": "latency",
-    "k_batch_front": "latency", "k_pw_pairs": "latency", "k_dedup": "latency",
-    "k_batch_labels": "fp64", "k_batch_back2": "latency",
+    "k_batch_front": "latency", "k_pw_pairs": "latency", "k_pw_pairs_lists": "latency",
+    "k_pw_pairs_trace": "latency", "k_dedup": "latency", "k_batch_pw": "latency",
+    "k_batch_pw2": "latency", "k_batch_labels": "fp64", "k_batch_back2": "latency",
+    "k_comp_succ": "hbm",
 }
+
+# Pipe and issue utilisation of kernels that HBM does not bound, from one ncu
+# capture each (percentages, so a capture of a smaller case of the same
+# kernel applies), keyed (kernel, workload).
+PIPES = {}
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
 # kernels captured with ncu on the named workload, keyed (kernel, workload).
@@ -221,7 +229,10 @@ def roofline_of(prof_b: dict, workload_name: str, fallback_bytes=None):
         traffic = tr["bytes"]
     elif tr and ab:
         traffic = tr["per_algorithmic_byte"] * ab
-    return {"kernel": name, "bound": KERNEL_BOUND.get(name, "hbm"), "achieved": achieved,
+    bound = KERNEL_BOUND.get(name, "hbm")
+    pipes = PIPES.get((name, workload_name))
+    return {"kernel": name, "bound": bound, "achieved": achieved,
+            "pipes": pipes if bound != "hbm" else None,
             "peak": pk["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / pk["hbm_gbs"] if achieved else None,
             "traffic": traffic,

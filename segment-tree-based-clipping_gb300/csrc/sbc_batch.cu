@@ -109,7 +109,6 @@ struct PairWork {
   // components: the merged slot of each component's first vertex, ending
   // with the slot count (filled by the thread back end)
   int *rootB, *rootC;
-  int* pmid;  // the warp back end's PwMid between its two kernels
   // pair-relative successor of each vertex within its component (null: one
   // ring); not carved, set per pair
   const int* bnx = nullptr;
@@ -213,7 +212,6 @@ __host__ __device__ __forceinline__ PairWork carve(Carver& cv, const Caps& c) {
   w.csort = cv.take<unsigned long long>(npow2_dev(c.nc));
   w.rootB = cv.take<int>(c.nb + 1);
   w.rootC = cv.take<int>(c.nc + 1);
-  w.pmid = cv.take<int>(4);
   return w;
 }
 
@@ -1319,7 +1317,8 @@ __device__ void pair_tape_warp(const double* b, int nb, const double* c, int nc,
 // One warp per pair, in two kernels: the records in the reference's order
 // and rows A9-A14 (k_batch_pw, w.state[3] = 2 when done), then rows A15-A18
 // (k_batch_pw2).  Two kernels keep each one's code small enough for the
-// instruction cache when the warps of an SM are at different steps.  A pair
+// instruction cache when the warps of an SM are at different steps (a third
+// kernel between the lists and the labelling gains nothing).  A pair
 // whose arrays take a path the warp back end does not follow (w.state[3] = 1)
 // is clipped by the thread back end below.
 __global__ void __launch_bounds__(128) k_batch_pw(ClipArgs A) {
@@ -1365,12 +1364,7 @@ __global__ void __launch_bounds__(128) k_batch_pw(ClipArgs A) {
     return;
   }
   if (lane == 0) {
-    if (st == PS_OK) {
-      w.pmid[0] = mid.nr;
-      w.pmid[1] = mid.knd;
-      w.pmid[2] = mid.nB;
-      w.pmid[3] = mid.nQ;
-    }
+    if (st == PS_OK) pw_mid_store(mid, pw.mid);
     w.state[3] = st == PS_OK ? 2 : 1;  // PS_FALLBACK / PS_CAP: the thread back end
   }
 }
@@ -1389,11 +1383,13 @@ __global__ void __launch_bounds__(128, 4) k_batch_pw2(ClipArgs A) {
   const int K = w.state[2];
   const double* b = A.bxy + 2 * A.boff[p];
   const double* c = A.cxy + 2 * A.coff[p];
+  const PwCaps pc = pw_caps(nb, nc, K, 1);
   PwWork pw = w.pw;
-  const PwMid mid{w.pmid[0], w.pmid[1], w.pmid[2], w.pmid[3]};
+  PwMid mid = pw_mid_load(pw.mid);
   int nr = 0, nv = 0;
-  const int st = pw_clip_tail(b, nb, c, nc, pw_caps(nb, nc, K, 1), pw, mid,
-                              PipSmall{b, nb, nullptr, 0}, A.unite, &nr, &nv);
+  int st = pw_clip_lists(b, nb, c, nc, pc, pw, &mid);
+  if (st == PS_OK)
+    st = pw_clip_trace(b, nb, c, nc, pc, pw, mid, PipSmall{b, nb, nullptr, 0}, A.unite, &nr, &nv);
   if (st != PS_OK && st != PS_UNDEF) {
     if (lane == 0) w.state[3] = 1;  // the thread back end takes the pair
     return;
@@ -1523,6 +1519,7 @@ void launch_clip(const ClipArgs& A, const BatchShape& sh, double in_bytes, cudaS
     ::sbc::KProbe kp_("k_batch_pw2", st, in_bytes);
     k_batch_pw2<<<grid_for(32LL * A.np, 128), 128, 0, st>>>(A);
   }
+
   {
     ::sbc::KProbe kp_("k_batch_back", st, in_bytes);
     k_batch_back<<<grid_for(A.np, sh.back), sh.back, 0, st>>>(A);

@@ -62,6 +62,7 @@ struct PwWork {
   unsigned char *splitP, *splitQ, *crossP, *crossQ;
   int* roff;
   double* rxy;
+  int* mid;  // PwMid between the steps when they run as separate kernels
 };
 
 __host__ __device__ __forceinline__ void pw_pool(Carver& cv, int cap, Pool& p, bool runs) {
@@ -133,6 +134,7 @@ __host__ __device__ __forceinline__ PwWork pw_carve(Carver& cv, const PwCaps& c)
   w.crossQ = cv.take<unsigned char>(c.capQ);
   w.roff = cv.take<int>(c.rcap + 1);
   w.rxy = cv.take<double>(2 * (long long)c.capR);
+  w.mid = cv.take<int>(8);
   return w;
 }
 
@@ -688,7 +690,22 @@ __device__ __forceinline__ void pw_fill_edge(PwWork& w, const double* c, const i
 // The scalars the two halves of the warp back end share.
 struct PwMid {
   int nr, knd, nB, nQ;  // base runs, non-degenerate base records, slot counts
+  int pn, qn, nruns;    // after the lists: node counts of P and Q, P's run nodes
 };
+
+__device__ __forceinline__ void pw_mid_store(const PwMid& m, int* d) {
+  d[0] = m.nr;
+  d[1] = m.knd;
+  d[2] = m.nB;
+  d[3] = m.nQ;
+  d[4] = m.pn;
+  d[5] = m.qn;
+  d[6] = m.nruns;
+}
+
+__device__ __forceinline__ PwMid pw_mid_load(const int* d) {
+  return PwMid{d[0], d[1], d[2], d[3], d[4], d[5], d[6]};
+}
 
 // Rows A9-A14: records, counts, alpha order, merged arrays, initial labels.
 __device__ int pw_clip_head(const double* b, int nb, const double* c, int nc, const PwHit* H,
@@ -1007,18 +1024,16 @@ __device__ int pw_clip_head(const double* b, int nb, const double* c, int nc, co
   for (int s = lane; s < nsp; s += 32) w.spnode[s] = -1;
   for (int q = lane; q < nQ; q += 32) w.labC[q] = w.cWin[q] >= 0 ? w.splab[w.cWinSI[q]] : 0;
   __syncwarp();
-  *mid = PwMid{nr, knd, nB, nQ};
+  *mid = PwMid{nr, knd, nB, nQ, 0, 0, 0};
   return PS_OK;
 }
 
-// Rows A15-A18 from the head's arrays: linked lists, labelling, tracing,
-// clean-up and the rings out.
-template <class Pip>
-__device__ int pw_clip_tail(const double* b, int nb, const double* c, int nc, const PwCaps& cp,
-                            PwWork& w, const PwMid& mid, Pip pip, int unite, int* nrings_out,
-                            int* nverts_out) {
+// Row A15 from the head's arrays: the linked lists (mid receives their node
+// counts and P's run nodes).
+__device__ int pw_clip_lists(const double* b, int nb, const double* c, int nc, const PwCaps& cp,
+                             PwWork& w, PwMid* mid) {
   const int lane = threadIdx.x & 31;
-  const int nr = mid.nr, knd = mid.knd, nB = mid.nB, nQ = mid.nQ;
+  const int nr = mid->nr, knd = mid->knd, nB = mid->nB, nQ = mid->nQ;
   // slot contents of the base's merged list
   auto info = [&](int s, int hint, double* x, double* y, int* al, int* nbv) {
     int vtx = 0;
@@ -1290,6 +1305,26 @@ __device__ int pw_clip_tail(const double* b, int nb, const double* c, int nc, co
   for (int i = lane; i < cp.capP; i += 32) w.splitP[i] = w.crossP[i] = 0;
   for (int i = lane; i < cp.capQ; i += 32) w.splitQ[i] = w.crossQ[i] = 0;
   __syncwarp();
+  mid->pn = P.n;
+  mid->qn = Q.n;
+  mid->nruns = nruns;
+  return PS_OK;
+}
+
+// Rows A16-A18 from the lists: labelling, tracing, clean-up and the rings out.
+template <class Pip>
+__device__ int pw_clip_trace(const double* b, int nb, const double* c, int nc, const PwCaps& cp,
+                             PwWork& w, const PwMid& mid, Pip pip, int unite, int* nrings_out,
+                             int* nverts_out) {
+  const int lane = threadIdx.x & 31;
+  const int nB = mid.nB, nQ = mid.nQ;
+  Pool& P = w.P;
+  Pool& Q = w.Q;
+  P.n = mid.pn;
+  Q.n = mid.qn;
+  P.rxy = b;
+  w.R.n = 0;
+  const int nruns = mid.nruns;
   // ---- A16-A18 (serial, on every lane; pointInPoly against the base splits
   // its grid row over the lanes)
   SerialArgs a;
@@ -1450,16 +1485,17 @@ __device__ int pw_clip_tail(const double* b, int nb, const double* c, int nc, co
 // (pip: its runIds / nruns are set by the tail), union or intersection.
 // Returns PS_OK with the rings in w.roff / w.rxy, PS_FALLBACK where the
 // sparse back end does not follow the arrays (the caller clips the pair
-// another way), PS_UNDEF or PS_CAP.  The head and the tail may also run as
-// separate kernels, PwMid carried between them.
+// another way), PS_UNDEF or PS_CAP.  The head, the lists and the trace may
+// also run as separate kernels, PwMid carried between them.
 template <class Pip>
 __device__ int pw_clip_core(const double* b, int nb, const double* c, int nc, const PwHit* H,
                             const PwCaps& cp, PwWork& w, Pip pip, int unite, int* nrings_out,
                             int* nverts_out) {
   PwMid mid;
-  const int st = pw_clip_head(b, nb, c, nc, H, cp, w, &mid);
+  int st = pw_clip_head(b, nb, c, nc, H, cp, w, &mid);
+  if (st == PS_OK) st = pw_clip_lists(b, nb, c, nc, cp, w, &mid);
   if (st != PS_OK) return st;
-  return pw_clip_tail(b, nb, c, nc, cp, w, mid, pip, unite, nrings_out, nverts_out);
+  return pw_clip_trace(b, nb, c, nc, cp, w, mid, pip, unite, nrings_out, nverts_out);
 }
 
 }  // namespace
