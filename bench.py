@@ -194,7 +194,20 @@ KERNEL_BOUND = {
 # Pipe and issue utilisation of kernels that HBM does not bound, from one ncu
 # capture each (percentages, so a capture of a smaller case of the same
 # kernel applies), keyed (kernel, workload).
-PIPES = {}
+_BATCH_NCU = "profiles/k_batch_small_pairs_8192.md (8,192 pairs, the same kernel)"
+PIPES = {
+    ("k_batch_pw2", "small_pairs_65536"): {
+        "fp64_pipe_pct_active": 9.8, "warps_active_pct": 18.5, "issue_active_pct": 24.0,
+        "stall_cycles_per_issue": {"long_scoreboard": 5.2, "wait": 2.8, "no_instruction": 2.4},
+        "source": _BATCH_NCU},
+    ("k_batch_pw", "small_pairs_65536"): {
+        "fp64_pipe_pct_active": 19.3, "warps_active_pct": 18.9, "issue_active_pct": 21.9,
+        "stall_cycles_per_issue": {"no_instruction": 4.5, "long_scoreboard": 4.2, "wait": 3.4},
+        "source": _BATCH_NCU},
+    ("k_batch_backward", "small_pairs_65536"): {
+        "fp64_pipe_pct_active": 75.2, "warps_active_pct": 22.7, "issue_active_pct": 14.6,
+        "source": _BATCH_NCU},
+}
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
 # kernels captured with ncu on the named workload, keyed (kernel, workload).
