@@ -1318,10 +1318,12 @@ __device__ void pair_tape_warp(const double* b, int nb, const double* c, int nc,
 // and rows A9-A14 (k_batch_pw, w.state[3] = 2 when done), then rows A15-A18
 // (k_batch_pw2).  Two kernels keep each one's code small enough for the
 // instruction cache when the warps of an SM are at different steps (a third
-// kernel between the lists and the labelling gains nothing).  A pair
+// kernel between the lists and the labelling gains nothing).  Both run six
+// blocks per SM (80 registers, some spilled): latency-bound, they gain more
+// from the extra warps than the spills cost.  A pair
 // whose arrays take a path the warp back end does not follow (w.state[3] = 1)
 // is clipped by the thread back end below.
-__global__ void __launch_bounds__(128) k_batch_pw(ClipArgs A) {
+__global__ void __launch_bounds__(128, 6) k_batch_pw(ClipArgs A) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   if ((t >> 5) >= A.np) return;
@@ -1369,7 +1371,7 @@ __global__ void __launch_bounds__(128) k_batch_pw(ClipArgs A) {
   }
 }
 
-__global__ void __launch_bounds__(128, 4) k_batch_pw2(ClipArgs A) {
+__global__ void __launch_bounds__(128, 6) k_batch_pw2(ClipArgs A) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   if ((t >> 5) >= A.np) return;

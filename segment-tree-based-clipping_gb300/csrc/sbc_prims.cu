@@ -399,22 +399,6 @@ k_scan_lb(ScanSet<T> set, unsigned long long* __restrict__ state_all) {
                   n, state_all + (size_t)y * scan_words(gridDim.x));
 }
 
-// The exclusive scan of f(0..n-1) into out: a map kernel and the scan in one
-// launch (f reads its inputs at index i; out may be one of them only if f(i)
-// reads nothing but position i)
-template <typename T, typename F>
-__global__ void __launch_bounds__(kScanThreads)
-k_scan_map(F f, T* __restrict__ out, long long n, unsigned long long* __restrict__ state) {
-  const bool vec = ((uintptr_t)out & 15) == 0;
-  scan_tile_lb<T>(
-      [&](long long base, T(&v)[kScanItems]) {
-#pragma unroll
-        for (int i = 0; i < kScanItems; ++i) v[i] = (base + i < n) ? f(base + i) : T(0);
-      },
-      [&](long long base, const T(&o)[kScanItems]) { scan_store(out, base, n, vec, o); }, n,
-      state);
-}
-
 template <typename T>
 void scan_rec(T* d, long long n, T* scratch, cudaStream_t st, bool state_zero = false) {
   if (n <= 0) return;
