@@ -106,6 +106,7 @@ struct PairWork {
   int* fval;
   int* eflag;  // per sorted endpoint: entries it adds to the elementary array
   unsigned long long* csort;  // the candidate sweep's overlay edges by box min x
+  float4* sbox;               // their boxes in that order
   // components: the merged slot of each component's first vertex, ending
   // with the slot count (filled by the thread back end)
   int *rootB, *rootC;
@@ -210,6 +211,7 @@ __host__ __device__ __forceinline__ PairWork carve(Carver& cv, const Caps& c) {
   w.fval = cv.take<int>(npow2_dev(n2));
   w.eflag = cv.take<int>(n2 + 1);
   w.csort = cv.take<unsigned long long>(npow2_dev(c.nc));
+  w.sbox = cv.take<float4>(c.nc);
   w.rootB = cv.take<int>(c.nb + 1);
   w.rootC = cv.take<int>(c.nc + 1);
   return w;
@@ -368,20 +370,20 @@ __device__ int clip_pair_front_warp(const double* b, int nb, const double* c, in
     w.fval[m] = m < n2 ? m : INT_MAX;
   }
   __syncwarp();
+  // each lane takes compare-exchange pairs (m, m + j), not elements: every
+  // lane works in every round
   for (int k = 2; k <= np2; k <<= 1)
     for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int m = lane; m < np2; m += 32) {
-        const int l = m ^ j;
-        if (l > m) {
-          const long long xk = w.fkey[m], yk = w.fkey[l];
-          const int xv = w.fval[m], yv = w.fval[l];
-          const bool gt = xk > yk || (xk == yk && xv > yv);
-          if (gt == ((m & k) == 0)) {
-            w.fkey[m] = yk;
-            w.fkey[l] = xk;
-            w.fval[m] = yv;
-            w.fval[l] = xv;
-          }
+      for (int q = lane; q < (np2 >> 1); q += 32) {
+        const int m = ((q & ~(j - 1)) << 1) | (q & (j - 1)), l = m | j;
+        const long long xk = w.fkey[m], yk = w.fkey[l];
+        const int xv = w.fval[m], yv = w.fval[l];
+        const bool gt = xk > yk || (xk == yk && xv > yv);
+        if (gt == ((m & k) == 0)) {
+          w.fkey[m] = yk;
+          w.fkey[l] = xk;
+          w.fval[m] = yv;
+          w.fval[l] = xv;
         }
       }
       __syncwarp();
@@ -588,17 +590,34 @@ __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc,
     return !(fb.x > fc.z || fb.z < fc.x || fb.y > fc.w || fb.w < fc.y);
   };
   if constexpr (kSweep) {
-    // Sweep in x: the overlay edges sorted by box min x (float order key,
-    // -0 as +0, then the edge); a base edge's candidates are the overlay
-    // edges with min x in [its min x - the largest overlay x extent, its max
-    // x], every box-overlapping pair among them
+    // Sweep in x: the overlay edges ordered by box min x (float order key,
+    // -0 as +0); a base edge's candidates are the overlay edges with min x
+    // in [its min x - the largest overlay x extent, its max x], every
+    // box-overlapping pair among them.  The order comes from the front's
+    // stable endpoint sort (w.sidx, by the exact x keys, so by the rounded-
+    // down float keys as well): the overlay edges' min-x endpoints, compacted
     auto fk = [](float f) {
       const unsigned u = __float_as_uint(f == 0.f ? 0.f : f);
       return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
     };
-    warp_bitonic(nc, w.csort, [&](int k) {
-      return ((unsigned long long)fk(w.fbox[nb + k].x) << 32) | (unsigned)k;
-    });
+    {
+      const int n2 = 2 * (nb + nc);
+      int cnt = 0;
+      for (int i0 = 0; i0 < n2; i0 += 32) {
+        const int i = i0 + lane;
+        const int id = i < n2 ? w.sidx[i] : 1;
+        const bool take = !(id & 1) && (id >> 1) >= nb;
+        const unsigned m = __ballot_sync(full, take);
+        if (take) {
+          const int k = (id >> 1) - nb, at = cnt + __popc(m & ((1u << lane) - 1u));
+          const float4 bx = w.fbox[nb + k];
+          w.csort[at] = ((unsigned long long)fk(bx.x) << 32) | (unsigned)k;
+          w.sbox[at] = bx;
+        }
+        cnt += __popc(m);
+      }
+      __syncwarp();
+    }
     float ext = 0.f;
     for (int k = lane; k < nc; k += 32) ext = fmaxf(ext, __fsub_ru(w.fbox[nb + k].z, w.fbox[nb + k].x));
     for (int o = 16; o > 0; o >>= 1) ext = fmaxf(ext, __shfl_xor_sync(full, ext, o));
@@ -626,9 +645,10 @@ __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc,
         bool pass = false;
         int j = 0;
         if (k < kend) {
-          j = (int)(unsigned)w.csort[k];
+          const bool meet = boxes_meet(fb, w.sbox[k]);  // the boxes in sweep order
+          if (meet) j = (int)(unsigned)w.csort[k];
           ++k;
-          if (boxes_meet(fb, w.fbox[nb + j])) {
+          if (meet) {
             const int bt2 = vsucc(bn, nb, be), ct2 = vsucc(cn, nc, j);
             pass = lsmf_d(bvx(b, nb, be), bvy(b, nb, be), bvx(b, nb, bt2), bvy(b, nb, bt2),
                           bvx(c, nc, j), bvy(c, nc, j), bvx(c, nc, ct2), bvy(c, nc, ct2));

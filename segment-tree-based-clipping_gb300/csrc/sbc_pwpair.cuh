@@ -574,16 +574,16 @@ __device__ void warp_bitonic(int n, unsigned long long* scr, Key key) {
   const int np = npow2_dev(n);
   for (int m = lane; m < np; m += 32) scr[m] = m < n ? key(m) : ~0ull;
   __syncwarp();
+  // each lane takes compare-exchange pairs (m, m + j): every lane works in
+  // every round
   for (int k = 2; k <= np; k <<= 1)
     for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int m = lane; m < np; m += 32) {
-        const int l = m ^ j;
-        if (l > m) {
-          const unsigned long long x = scr[m], y = scr[l];
-          if ((x > y) == ((m & k) == 0)) {
-            scr[m] = y;
-            scr[l] = x;
-          }
+      for (int q = lane; q < (np >> 1); q += 32) {
+        const int m = ((q & ~(j - 1)) << 1) | (q & (j - 1)), l = m | j;
+        const unsigned long long x = scr[m], y = scr[l];
+        if ((x > y) == ((m & k) == 0)) {
+          scr[m] = y;
+          scr[l] = x;
         }
       }
       __syncwarp();
