@@ -107,6 +107,7 @@ struct PairWork {
   int* eflag;  // per sorted endpoint: entries it adds to the elementary array
   unsigned long long* csort;  // the candidate sweep's overlay edges by box min x
   float4* sbox;               // their boxes in that order
+  int* hsort;                 // the warp back end's hit order (a power-of-two network)
   // components: the merged slot of each component's first vertex, ending
   // with the slot count (filled by the thread back end)
   int *rootB, *rootC;
@@ -212,6 +213,7 @@ __host__ __device__ __forceinline__ PairWork carve(Carver& cv, const Caps& c) {
   w.eflag = cv.take<int>(n2 + 1);
   w.csort = cv.take<unsigned long long>(npow2_dev(c.nc));
   w.sbox = cv.take<float4>(c.nc);
+  w.hsort = cv.take<int>(npow2_dev(K));
   w.rootB = cv.take<int>(c.nb + 1);
   w.rootC = cv.take<int>(c.nc + 1);
   return w;
@@ -1364,16 +1366,35 @@ __global__ void __launch_bounds__(128, 6) k_batch_pw(ClipArgs A) {
     if (lane == 0) w.state[3] = 1;
     return;
   }
-  // A9 order (base id, then first emission)
-  if (lane == 0) {
-    for (int i = 0; i < K; ++i) w.hord[i] = i;
-    merge_sort(w.hord, w.htmp, K, [&](int x, int y) {
-      return w.hb[x] != w.hb[y] ? w.hb[x] < w.hb[y] : w.hkey[x] < w.hkey[y];
-    });
+  // A9 order (base id, then first emission; the hit index breaks ties, as a
+  // stable sort of the hits in index order would): a bitonic network over
+  // the hit indices, the lanes on compare-exchange pairs
+  {
+    const int np = npow2_dev(K);
+    for (int m = lane; m < np; m += 32) w.hsort[m] = m < K ? m : INT_MAX;
+    __syncwarp();
+    auto less = [&](int x, int y) {
+      if (y == INT_MAX) return x != INT_MAX;
+      if (x == INT_MAX) return false;
+      if (w.hb[x] != w.hb[y]) return w.hb[x] < w.hb[y];
+      if (w.hkey[x] != w.hkey[y]) return w.hkey[x] < w.hkey[y];
+      return x < y;
+    };
+    for (int k = 2; k <= np; k <<= 1)
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int q = lane; q < (np >> 1); q += 32) {
+          const int m = ((q & ~(j - 1)) << 1) | (q & (j - 1)), l = m | j;
+          const int x = w.hsort[m], y = w.hsort[l];
+          if (less(y, x) == ((m & k) == 0)) {
+            w.hsort[m] = y;
+            w.hsort[l] = x;
+          }
+        }
+        __syncwarp();
+      }
   }
-  __syncwarp();
   for (int i = lane; i < K; i += 32) {
-    const int h = w.hord[i];
+    const int h = w.hsort[i];
     w.phit[i] = PwHit{0, w.hb[h] >> 1, w.hc[h] >> 1, w.ht[h], w.hkey[h], w.hal[h], w.hbt[h]};
   }
   __syncwarp();
