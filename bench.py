@@ -197,12 +197,15 @@ KERNEL_BOUND = {
 _BATCH_NCU = "profiles/k_batch_small_pairs_8192.md (8,192 pairs, the same kernel)"
 PIPES = {
     ("k_batch_pw2", "small_pairs_65536"): {
-        "fp64_pipe_pct_active": 9.8, "warps_active_pct": 18.5, "issue_active_pct": 24.0,
-        "stall_cycles_per_issue": {"long_scoreboard": 5.2, "wait": 2.8, "no_instruction": 2.4},
+        "fp64_pipe_pct_active": 11.0, "warps_active_pct": 27.1, "issue_active_pct": 28.3,
+        "stall_cycles_per_issue": {"long_scoreboard": 7.0, "no_instruction": 3.3, "wait": 2.9},
         "source": _BATCH_NCU},
     ("k_batch_pw", "small_pairs_65536"): {
-        "fp64_pipe_pct_active": 19.3, "warps_active_pct": 18.9, "issue_active_pct": 21.9,
-        "stall_cycles_per_issue": {"no_instruction": 4.5, "long_scoreboard": 4.2, "wait": 3.4},
+        "fp64_pipe_pct_active": 27.4, "warps_active_pct": 29.0, "issue_active_pct": 29.2,
+        "stall_cycles_per_issue": {"long_scoreboard": 5.8, "no_instruction": 3.9, "wait": 3.5},
+        "source": _BATCH_NCU},
+    ("k_batch_front", "small_pairs_65536"): {
+        "fp64_pipe_pct_active": 18.4, "warps_active_pct": 32.4, "issue_active_pct": 44.4,
         "source": _BATCH_NCU},
     ("k_batch_backward", "small_pairs_65536"): {
         "fp64_pipe_pct_active": 75.2, "warps_active_pct": 22.7, "issue_active_pct": 14.6,
