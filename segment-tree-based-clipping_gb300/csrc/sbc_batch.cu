@@ -575,6 +575,7 @@ __device__ void clip_pair_cand(const double* b, int nb, const double* c, int nc,
   };
   auto enqueue = [&](bool pass, int be, int j) {
     const unsigned m = __ballot_sync(full, pass);
+    if (m == 0u) return;  // nothing to queue (the same on every lane)
     if (pass) q[nq + __popc(m & ((1u << lane) - 1u))] = make_int2(be, j);
     nq += __popc(m);
     __syncwarp();
