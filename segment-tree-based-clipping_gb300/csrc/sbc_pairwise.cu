@@ -1521,24 +1521,30 @@ int PairwiseRunner::run(const double* d_bxy, int nb, int nov, const double* d_cx
 namespace sbc {
 namespace {
 
+// one warp per pair: each ring's shoelace terms summed lane by lane, the
+// lanes' sums combined in a fixed order (the area does not depend on the
+// launch shape)
 __global__ void k_pwa_area(int nov, const long long* __restrict__ pair_ring,
                            const long long* __restrict__ ring_off, const double* __restrict__ xy,
                            const int* __restrict__ status, double* __restrict__ area) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= nov) return;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  if ((t >> 5) >= nov) return;
+  const int p = (int)(t >> 5);
   double a = 0.0;
   if (status[p] == SBC_OK) {
     for (long long r = pair_ring[p]; r < pair_ring[p + 1]; ++r) {
       const long long s = ring_off[r], e = ring_off[r + 1];
       double s2 = 0.0;
-      for (long long i = s; i < e; ++i) {
+      for (long long i = s + lane; i < e; i += 32) {
         const long long j = (i + 1 == e) ? s : i + 1;
         s2 = dadd(s2, dsub(dmul(xy[2 * i], xy[2 * j + 1]), dmul(xy[2 * j], xy[2 * i + 1])));
       }
+      for (int o = 16; o > 0; o >>= 1) s2 = dadd(s2, __shfl_xor_sync(0xffffffffu, s2, o));
       a = dadd(a, dmul(0.5, s2));
     }
   }
-  area[p] = a;
+  if (lane == 0) area[p] = a;
 }
 
 __global__ void k_pwa_base_keys(int nb, const double* __restrict__ b,
@@ -1754,7 +1760,7 @@ int PairwiseRunner::area(double* d_area, cudaStream_t st) {
   if (!valid) return pl_.fail(kEInput, "no pairwise result to take the area of");
   if (np <= 0) return kOk;
   ::sbc::KProbe kp_("k_pwa_area", st, 16.0 * (double)total_verts);
-  k_pwa_area<<<grid_for(np, 128), 128, 0, st>>>(np, pair_ring, ring_off, xy, status, d_area);
+  k_pwa_area<<<grid_for(32LL * np, 128), 128, 0, st>>>(np, pair_ring, ring_off, xy, status, d_area);
   return kOk;
 }
 
