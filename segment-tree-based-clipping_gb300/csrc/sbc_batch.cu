@@ -1608,14 +1608,17 @@ struct Arenas {
   }
 };
 
-// rings of every pair packed: pair_ring[p] .. pair_ring[p+1] ring offsets
+// rings of every pair packed: pair_ring[p] .. pair_ring[p+1] ring offsets;
+// one warp per pair, its lanes over the ring offsets and the coordinates
 __global__ void k_batch_pack(int np, const long long* __restrict__ boff,
                              const long long* __restrict__ coff, Arenas ar,
                              const int* __restrict__ status,
                              const long long* __restrict__ rpre, const long long* __restrict__ vpre,
                              long long* __restrict__ ring_off, double* __restrict__ xy) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= np) return;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  if ((t >> 5) >= np) return;
+  const int p = (int)(t >> 5);
   const long long r0 = rpre[p], v0 = vpre[p];
   const int nr = (int)(rpre[p + 1] - r0);
   if (nr == 0 || status[p] != SBC_OK || ar.pass[p] < 0) return;
@@ -1623,9 +1626,9 @@ __global__ void k_batch_pack(int np, const long long* __restrict__ boff,
   const Caps cp = caps_of(nb, nc, hit_cap(nb, nc, ar.pass[p], ar.need[p]));
   Carver cv{const_cast<unsigned char*>(ar.at(p)), 0};
   const PairWork w = carve(cv, cp);
-  for (int r = 0; r < nr; ++r) ring_off[r0 + r] = v0 + w.roff[r];
+  for (int r = lane; r < nr; r += 32) ring_off[r0 + r] = v0 + w.roff[r];
   const int nv = w.roff[nr];
-  for (int i = 0; i < 2 * nv; ++i) xy[2 * v0 + i] = w.rxy[i];
+  for (int i = lane; i < 2 * nv; i += 32) xy[2 * v0 + i] = w.rxy[i];
 }
 
 // d(area)/d(vertices), one warp per pair, from the forward pass's tape.  The
@@ -2209,8 +2212,9 @@ int BatchRunner::rings(const double* d_bxy, const long long* d_boff, const doubl
     const Arenas ar{arena[0], aoff[0] + p0, abase_[0], arena[1], aoff[1] + p0, abase_[1], pass + p0,
                     need_ + p0};
     ::sbc::KProbe kp_("k_batch_pack", st);
-    k_batch_pack<<<grid_for(n, 128), 128, 0, st>>>(n, d_boff + p0, d_coff + p0, ar, status + p0,
-                                                   rpre + p0, vpre + p0, roff, oxy);
+    k_batch_pack<<<grid_for(32LL * n, 128), 128, 0, st>>>(n, d_boff + p0, d_coff + p0, ar,
+                                                          status + p0, rpre + p0, vpre + p0, roff,
+                                                          oxy);
   }
   for (const BigOut& bo : big_) {
     if (!bo.ok || bo.nrings == 0) continue;
